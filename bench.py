@@ -1,0 +1,331 @@
+"""Benchmark: converged eigenpairs/s of the Krylov-Schur path on one GB300 (replicas on N GPUs).
+
+Default workload (one "step" = one complete EPSSolve): 3-D 7-point Laplacian 128^3 (n = 2,097,152,
+nnz = 14,581,760, FP64 CSR), EPS_HEP, nev = 50 largest algebraic, ncv = 128, tol = 1e-10, start vector
+uniform[-1,1] (splitmix64, seed 2).  The basis alone is 2.2 GB, far larger than the 129 MB L2, so no flush is needed
+between steps.
+
+  value      nev converged eigenpairs per solve / device time of EPSSolve (CUDA events on the solver's stream),
+             matrix resident in HBM since EPSSetUp (the start vector's 16.8 MB upload is inside EPSSolve)
+  e2e        the same metric through the public C-ABI from host buffers: MatCreateSeqAIJWithArrays + EPSSetUp (CSR
+             host->device) + EPSSolve + EPSGetEigenpair for all nev (eigenvectors device->host), host wall clock
+  roofline   the dominant kernel class of one profiled solve: algorithmic bytes / summed CUDA-event time
+  cpu_baseline  the oracle (CPU restatement of SLEPc's Krylov-Schur) on the host cores for a bounded time, scaled
+             by Krylov steps to the full solve
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference] [--workload lap3d128|lap2d100|convdiff1000]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "lap3d128": dict(desc="3-D 7-point Laplacian 128^3 (n=2097152, nnz=14581760, FP64 CSR), EPS_HEP, nev=50 "
+                          "largest algebraic, ncv=128, tol=1e-10, start vector uniform[-1,1] seed 2",
+                     gen=lambda mg: mg.laplacian_3d(128), hermitian=True, which="LR", nev=50, ncv=128, tol=1e-10,
+                     seed=2),
+    "lap2d100": dict(desc="2-D 5-point Laplacian 100x100 (n=10000, nnz=49600), EPS_HEP, nev=10 largest magnitude, "
+                          "ncv=32, tol=1e-8, start vector seed 1",
+                     gen=lambda mg: mg.laplacian_2d(100), hermitian=True, which="LM", nev=10, ncv=32, tol=1e-8, seed=1),
+    "convdiff1000": dict(desc="2-D upwind convection-diffusion 1000x1000 (n=1e6), Peclet 10, EPS_NHEP, nev=20 "
+                              "largest real, ncv=64, tol=1e-10, start vector seed 3",
+                         gen=lambda mg: mg.convection_diffusion_2d(1000, 10.0), hermitian=False, which="LR", nev=20,
+                         ncv=64, tol=1e-10, seed=3),
+}
+METRIC = "converged eigenpairs/s at tol 1e-10 (plain Krylov-Schur, one solve per step)"
+UNIT = "eigenpairs/s"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clock and throttle reasons during the timed region."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.index), "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=5)
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        mhz = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(mhz) if mhz else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def committed_traffic(workload):
+    """Per-launch DRAM traffic of the dominant kernel from the committed ncu summary, if one exists."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get(workload)
+    return None
+
+
+def cpu_baseline(csr, wl, steps_full, budget_s=20.0):
+    """Oracle (CPU restatement of the reference) on all host cores for a bounded time; eigenpairs/s extrapolated
+    by the number of Krylov steps of the full solve."""
+    import oracle
+    from slepc_gb300 import matgen
+
+    oracle.build()
+    cores = os.cpu_count() or 1
+    n = len(csr[0]) - 1
+    t = time.time()
+    r = oracle.solve(*csr, hermitian=wl["hermitian"], which=wl["which"], nev=wl["nev"], ncv=wl["ncv"], tol=wl["tol"],
+                     v0=matgen.start_vector(n, wl["seed"]), nthreads=cores, vectors=False, time_budget=budget_s)
+    el = time.time() - t
+    finished = r.reason in (1, -1, -2)
+    if finished:
+        value = wl["nev"] / el
+        sample = f"complete solve ({r.nsteps} Krylov steps, {r.its} restarts) in {el:.1f} s"
+    else:
+        per_step = el / max(r.nsteps, 1)
+        est = per_step * steps_full
+        value = wl["nev"] / est
+        sample = (f"first {r.nsteps} Krylov steps ({r.its} restarts, {el:.1f} s) of the same solve, scaled to the "
+                  f"full solve's {steps_full} steps")
+    return {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
+            "host": os.uname().machine}
+
+
+def run_reference(args, wl):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from slepc_gb300 import matgen
+
+    csr = wl["gen"](matgen)
+    steps_full = int(json.load(open(os.path.join(ROOT, "profiles", "reference_steps.json"))).get(args.workload, 0)) \
+        if os.path.exists(os.path.join(ROOT, "profiles", "reference_steps.json")) else 0
+    budget = 20.0 if args.workload == "lap3d128" else 10.0
+    vals = []
+    for i in range(args.warmup + args.steps):
+        b = cpu_baseline(csr, wl, steps_full or 5000, budget_s=budget if i >= args.warmup else 3.0)
+        if i >= args.warmup:
+            vals.append(b)
+    v = statistics.median([b["value"] for b in vals])
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * wl["nev"] / v,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": wl["desc"], "impl": "oracle port of SLEPc 3.22 Krylov-Schur (CGS+IFNEEDED, "
+                                                      "host DS), OpenMP over rows"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": vals[-1]["cores"], "kind": "port",
+                             "sample": vals[-1]["sample"]},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="lap3d128", choices=list(WORKLOADS))
+    ap.add_argument("--arith", default="pair", choices=["pair", "f64"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        run_reference(args, wl)
+        return
+
+    rank, world, local = dist_env()
+    import slepc_gb300 as sg
+    from slepc_gb300 import matgen
+
+    sg.build()
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as td
+
+        torch.cuda.set_device(local)
+        td.init_process_group("nccl")
+        dist = (torch, td)
+    else:
+        import ctypes
+        ctypes.CDLL("libcudart.so").cudaSetDevice(local)
+
+    csr = wl["gen"](matgen)
+    n = len(csr[0]) - 1
+    nnz = len(csr[1])
+    v0 = matgen.start_vector(n, wl["seed"])
+
+    def make_eps(A):
+        eps = sg.EPS().create()
+        eps.setOperators(A)
+        eps.setProblemType(sg.EPS.ProblemType.HEP if wl["hermitian"] else sg.EPS.ProblemType.NHEP)
+        eps.setDimensions(wl["nev"], wl["ncv"])
+        eps.setTolerances(wl["tol"])
+        eps.setWhichEigenpairs(wl["which"])
+        eps.setArithmetic(args.arith)
+        eps.setInitialSpace(v0)
+        return eps
+
+    def barrier():
+        if dist:
+            dist[1].barrier()
+            dist[0].cuda.synchronize()
+
+    def max_over_ranks(x):
+        if not dist:
+            return x
+        t = dist[0].tensor([x], dtype=dist[0].float64, device="cuda")
+        dist[1].all_reduce(t, op=dist[1].ReduceOp.MAX)
+        return float(t.item())
+
+    A = sg.Mat(*csr)
+    eps = make_eps(A)
+    eps.setUp()
+    for _ in range(args.warmup):
+        eps.solve()
+    clocks = ClockSampler(local)
+    barrier()
+    clocks.start()
+    dev_ms, lat, launches, nconvs, steps_k, restarts = [], [], 0, [], [], []
+    for _ in range(args.steps):
+        eps.solve()
+        st = eps.getStats()
+        dev_ms.append(st["solve_device_ms"])
+        lat.append(st["solve_seconds"] * 1000.0)
+        launches += st["kernel_launches"]
+        nconvs.append(eps.getConverged())
+        steps_k.append(st["krylov_steps"])
+        restarts.append(st["restarts"])
+    barrier()
+    clk = clocks.stop()
+    total_ms = max_over_ranks(sum(dev_ms))
+    assert min(nconvs) >= wl["nev"], f"solve did not converge ({nconvs})"
+    value = world * args.steps * wl["nev"] / (total_ms / 1000.0)
+
+    # e2e: public API from host buffers, per step: CSR + start vector host->device, solve, eigenpairs device->host
+    e2e = None
+    if not args.no_e2e:
+        e2e_times = []
+        h2d = csr[0].nbytes + csr[1].nbytes + csr[2].nbytes + v0.nbytes
+        d2h = wl["nev"] * (n * 8 + 16)
+        for _ in range(args.steps):
+            barrier()
+            t = time.perf_counter()
+            Ae = sg.Mat(*csr)
+            e = make_eps(Ae)
+            e.solve()
+            x = np.empty(n)
+            for i in range(wl["nev"]):
+                e.getEigenpair(i, x)
+            e.destroy()
+            Ae.destroy()
+            barrier()
+            e2e_times.append(time.perf_counter() - t)
+        e2e_t = max_over_ranks(sum(e2e_times))
+        e2e = {"value": world * args.steps * wl["nev"] / e2e_t, "unit": UNIT, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h}
+
+    # roofline: one profiled solve
+    eps.setProfiling(True)
+    eps.solve()
+    prof = eps.getProfile()
+    eps.setProfiling(False)
+    peak, peak_kind = measured_peaks()
+    top = max(("gs_dot", "gs_update", "spmv", "restart"), key=lambda k: prof[k][0])
+    ms_k, by_k, nl_k = prof[top]
+    achieved = by_k / (ms_k / 1000.0) / 1e9 if ms_k > 0 else None
+    tr = committed_traffic(args.workload)
+    roofline = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak if achieved else None, "peak_source": peak_kind,
+                "traffic": (tr or {}).get(top), "launches": nl_k,
+                "per_class_ms": {k: round(v[0], 3) for k, v in prof.items()},
+                "per_class_GBps": {k: (round(v[1] / (v[0] / 1000.0) / 1e9, 1) if v[0] > 0 else None)
+                                   for k, v in prof.items()}}
+    step_bytes = sum(v[1] for k, v in prof.items())
+    krylov_ms = sum(prof[k][0] for k in ("spmv", "gs_dot", "gs_update"))
+    krylov_bytes = sum(prof[k][1] for k in ("spmv", "gs_dot", "gs_update"))
+    roofline["krylov_step_GBps"] = round(krylov_bytes / (krylov_ms / 1000.0) / 1e9, 1) if krylov_ms > 0 else None
+    roofline["krylov_step_frac"] = round(roofline["krylov_step_GBps"] / peak, 4) if krylov_ms > 0 else None
+    roofline["solve_bytes"] = step_bytes
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(csr, wl, steps_k[-1])
+
+    if rank == 0:
+        lat_sorted = sorted(lat)
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": wl["desc"], "n": n, "nnz": nnz, "arith": args.arith,
+                           "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (basis 2.2 GB)"
+                           if args.workload == "lap3d128" else "small inputs",
+                           "krylov_steps_per_solve": steps_k[-1], "restarts_per_solve": restarts[-1],
+                           "nconv": nconvs[-1]},
+                "latency_ms": {"p50": float(np.percentile(lat_sorted, 50)), "p99": float(np.percentile(lat_sorted, 99))},
+                "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches}
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist[1].destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

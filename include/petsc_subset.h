@@ -1,0 +1,107 @@
+/*
+ * petsc_subset.h -- the part of PETSc's C API that SLEPc's Krylov-Schur path is typed on.
+ *
+ * PETSc is not part of this library.  These are the names, argument meanings and error conventions of the PETSc
+ * calls that the reference's EPS/BV/DS interfaces take and return (Mat, Vec, PetscErrorCode, PetscScalar = double,
+ * PetscReal = double, PetscInt = 32-bit, PetscBool), so that C code written against SLEPc's API compiles against
+ * this library unchanged.  Everything is backed by libslepc_gb300.so.
+ *
+ * Matrices: CSR ("AIJ") created from caller-owned host arrays with MatCreateSeqAIJWithArrays (the arrays must
+ * outlive the Mat, as in PETSc), and small dense matrices (MatCreateSeqDense) for BVMultInPlace.  Vectors:
+ * host arrays (VecCreateSeq / VecCreateSeqWithArray).  The eigensolver copies what it needs to device memory.
+ */
+#ifndef SLEPC_GB300_PETSC_SUBSET_H
+#define SLEPC_GB300_PETSC_SUBSET_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int PetscErrorCode;
+typedef int PetscInt;
+typedef int PetscMPIInt;
+typedef int PetscBLASInt;
+typedef double PetscScalar;
+typedef double PetscReal;
+typedef enum { PETSC_FALSE = 0, PETSC_TRUE = 1 } PetscBool;
+typedef int MPI_Comm; /* one process per GPU: communicators carry no information here */
+
+#define MPI_COMM_WORLD ((MPI_Comm)0)
+#define MPI_COMM_SELF ((MPI_Comm)1)
+#define PETSC_COMM_WORLD MPI_COMM_WORLD
+#define PETSC_COMM_SELF MPI_COMM_SELF
+
+/* "let the library decide" and "keep the current value" markers (PETSc 3.22 conventions) */
+#define PETSC_DECIDE (-1)
+#define PETSC_DETERMINE PETSC_DECIDE
+#define PETSC_DEFAULT (-2)
+#define PETSC_CURRENT (-2)
+#define PETSC_UNLIMITED (-3)
+#define PETSC_NULL_INTEGER ((PetscInt *)0)
+
+/* error codes (numbering of petscerror.h) */
+#define PETSC_SUCCESS 0
+#define PETSC_ERR_MEM 55
+#define PETSC_ERR_SUP 56
+#define PETSC_ERR_ORDER 58
+#define PETSC_ERR_ARG_SIZ 60
+#define PETSC_ERR_ARG_WRONG 62
+#define PETSC_ERR_ARG_OUTOFRANGE 63
+#define PETSC_ERR_ARG_WRONGSTATE 73
+#define PETSC_ERR_LIB 76
+#define PETSC_ERR_PLIB 77
+#define PETSC_ERR_CONV_FAILED 82
+#define PETSC_ERR_ARG_NULL 85
+#define PETSC_ERR_USER_INPUT 91
+#define PETSC_ERR_GPU_RESOURCE 96
+#define PETSC_ERR_GPU 97
+
+typedef enum { NORM_1 = 0, NORM_2 = 1, NORM_FROBENIUS = 2, NORM_INFINITY = 3, NORM_1_AND_2 = 4 } NormType;
+
+typedef struct _p_Mat *Mat;
+typedef struct _p_Vec *Vec;
+
+/* SlepcInitialize/PetscInitialize: a no-op shim (selects the current CUDA device lazily). */
+PetscErrorCode PetscInitialize(int *argc, char ***argv, const char file[], const char help[]);
+PetscErrorCode PetscFinalize(void);
+
+/* Error text of the last failing call on this thread (library extension; PETSc prints a traceback instead). */
+const char *PetscGB300LastError(void);
+
+/* --- Mat (petscmat.h) --- */
+/* CSR matrix over caller-owned arrays i[m+1], j[nnz], a[nnz]; column indices of a row in ascending order. */
+PetscErrorCode MatCreateSeqAIJWithArrays(MPI_Comm comm, PetscInt m, PetscInt n, PetscInt i[], PetscInt j[],
+                                         PetscScalar a[], Mat *A);
+/* Dense column-major matrix; data may be NULL (the library allocates and zeroes it). */
+PetscErrorCode MatCreateSeqDense(MPI_Comm comm, PetscInt m, PetscInt n, PetscScalar data[], Mat *A);
+PetscErrorCode MatDenseGetArray(Mat A, PetscScalar **array);
+PetscErrorCode MatDenseRestoreArray(Mat A, PetscScalar **array);
+PetscErrorCode MatDenseGetLDA(Mat A, PetscInt *lda);
+PetscErrorCode MatGetSize(Mat A, PetscInt *m, PetscInt *n);
+PetscErrorCode MatGetValue(Mat A, PetscInt row, PetscInt col, PetscScalar *v);
+PetscErrorCode MatMult(Mat A, Vec x, Vec y);
+PetscErrorCode MatNorm(Mat A, NormType type, PetscReal *nrm);
+PetscErrorCode MatCreateVecs(Mat A, Vec *right, Vec *left);
+PetscErrorCode MatDestroy(Mat *A);
+
+/* --- Vec (petscvec.h) --- */
+PetscErrorCode VecCreateSeq(MPI_Comm comm, PetscInt n, Vec *v);
+PetscErrorCode VecCreateSeqWithArray(MPI_Comm comm, PetscInt bs, PetscInt n, const PetscScalar array[], Vec *v);
+PetscErrorCode VecDuplicate(Vec v, Vec *newv);
+PetscErrorCode VecGetSize(Vec v, PetscInt *n);
+PetscErrorCode VecGetArray(Vec v, PetscScalar **a);
+PetscErrorCode VecRestoreArray(Vec v, PetscScalar **a);
+PetscErrorCode VecGetArrayRead(Vec v, const PetscScalar **a);
+PetscErrorCode VecRestoreArrayRead(Vec v, const PetscScalar **a);
+PetscErrorCode VecSet(Vec v, PetscScalar alpha);
+PetscErrorCode VecCopy(Vec x, Vec y);
+PetscErrorCode VecScale(Vec v, PetscScalar alpha);
+PetscErrorCode VecAXPY(Vec y, PetscScalar alpha, Vec x);
+PetscErrorCode VecDot(Vec x, Vec y, PetscScalar *val);
+PetscErrorCode VecNorm(Vec v, NormType type, PetscReal *nrm);
+PetscErrorCode VecDestroy(Vec *v);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,58 @@
+/*
+ * slepc_gb300.h -- GB300-specific entry points that have no counterpart in the reference.
+ *
+ * They select the arithmetic of the bandwidth-bound kernels, expose device-resident results and report
+ * per-solve statistics (Krylov steps, restarts, kernel time), for programs that want more than the SLEPc API.
+ */
+#ifndef SLEPC_GB300_H
+#define SLEPC_GB300_H
+
+#include "slepceps.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Arithmetic of the Gram-Schmidt, restart and residual kernels.
+ *   EPS_GB300_ARITH_PAIR (default): FP64 storage; products and sums on FP32 pairs with error-free
+ *       transformations (relative error per product below 2^-46), the only form that reaches the HBM roofline on
+ *       GB300, whose FP64 pipe runs at about 1.2 TFLOP/s.
+ *   EPS_GB300_ARITH_F64: plain IEEE FP64 fused multiply-add everywhere (slower on GB300). */
+typedef enum { EPS_GB300_ARITH_PAIR = 0, EPS_GB300_ARITH_F64 = 1 } EPSGB300Arith;
+PetscErrorCode EPSGB300SetArithmetic(EPS eps, EPSGB300Arith arith);
+PetscErrorCode EPSGB300GetArithmetic(EPS eps, EPSGB300Arith *arith);
+
+/* CUDA device ordinal used by this EPS (default: the current device at EPSCreate). */
+PetscErrorCode EPSGB300SetDevice(EPS eps, int device);
+
+/* Statistics of the last EPSSolve. */
+typedef struct {
+  long long krylov_steps;    /* operator applications inside factorisations */
+  long long restarts;        /* outer iterations */
+  double solve_seconds;      /* wall time of EPSSolve (device synchronised) */
+  double bytes_moved;        /* algorithmic HBM bytes of the factorisations and restarts */
+  double setup_seconds;      /* EPSSetUp: allocation and matrix upload */
+  long long kernel_launches; /* CUDA kernels launched by the last EPSSolve */
+  double solve_device_ms;    /* EPSSolve measured with CUDA events on the EPS stream */
+} EPSGB300Stats;
+PetscErrorCode EPSGB300GetStats(EPS eps, EPSGB300Stats *stats);
+
+/* Per-kernel-class timing of the next EPSSolve calls: CUDA events recorded around every launch on the EPS stream.
+ * Classes: 0 SpMV, 1 Gram-Schmidt dot half, 2 Gram-Schmidt update half, 3 thick restart, 4 projected problem.
+ * EPSGB300GetProfile returns the summed device time (ms), the algorithmic HBM bytes and the launch count. */
+typedef enum { EPS_GB300_K_SPMV = 0, EPS_GB300_K_GS_DOT, EPS_GB300_K_GS_UPDATE, EPS_GB300_K_RESTART, EPS_GB300_K_DS,
+               EPS_GB300_K_COUNT } EPSGB300KernelClass;
+PetscErrorCode EPSGB300SetProfiling(EPS eps, PetscBool on);
+PetscErrorCode EPSGB300GetProfile(EPS eps, EPSGB300KernelClass cls, double *ms, double *bytes, long long *launches);
+
+/* Device pointer to the basis (column-major, leading dimension *ld) after EPSSolve: columns 0..nconv-1 hold the
+ * eigenvectors (Hermitian) or the Schur/eigen vectors (non-Hermitian) in solver order (see EPSGetEigenpair). */
+PetscErrorCode EPSGB300GetDeviceBasis(EPS eps, const double **V, PetscInt *ld);
+
+/* Orthogonality ||V^T V - I||_max of the first nconv columns, computed on the device in FP64. */
+PetscErrorCode EPSGB300OrthogonalityError(EPS eps, PetscReal *err);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,83 @@
+/*
+ * slepceps.h -- EPS (eigenvalue problem solver) subset: the Krylov-Schur path on one GB300.
+ *
+ * Same prototypes, enum values and argument meanings as SLEPc 3.22's include/slepceps.h (:186-274) for the calls a
+ * program needs to run EPSKRYLOVSCHUR on a standard Hermitian (EPS_HEP) or non-Hermitian (EPS_NHEP) problem with
+ * Ritz extraction: create, set operators/type/dimensions/tolerances/which/initial space, solve, read eigenpairs,
+ * errors and convergence data, destroy.  Errors are PETSc error codes (0 = success); failure to converge is not an
+ * error but a negative EPSConvergedReason.  One CUDA stream per EPS; distinct EPS objects may be driven from
+ * distinct host threads.
+ */
+#ifndef SLEPC_GB300_SLEPCEPS_H
+#define SLEPC_GB300_SLEPCEPS_H
+
+#include "petsc_subset.h"
+#include "slepcbv.h"
+#include "slepcds.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct _p_EPS *EPS;
+typedef const char *EPSType;
+#define EPSKRYLOVSCHUR "krylovschur"
+
+typedef enum { EPS_HEP = 1, EPS_GHEP, EPS_NHEP, EPS_GNHEP, EPS_PGNHEP, EPS_GHIEP, EPS_BSE } EPSProblemType;
+typedef enum { EPS_RITZ, EPS_HARMONIC, EPS_HARMONIC_RELATIVE, EPS_HARMONIC_RIGHT, EPS_HARMONIC_LARGEST,
+               EPS_REFINED, EPS_REFINED_HARMONIC } EPSExtraction;
+typedef enum { EPS_LARGEST_MAGNITUDE = 1, EPS_SMALLEST_MAGNITUDE, EPS_LARGEST_REAL, EPS_SMALLEST_REAL,
+               EPS_LARGEST_IMAGINARY, EPS_SMALLEST_IMAGINARY, EPS_TARGET_MAGNITUDE, EPS_TARGET_REAL,
+               EPS_TARGET_IMAGINARY, EPS_ALL, EPS_WHICH_USER } EPSWhich;
+typedef enum { EPS_CONVERGED_TOL = 1, EPS_CONVERGED_USER = 2, EPS_DIVERGED_ITS = -1, EPS_DIVERGED_BREAKDOWN = -2,
+               EPS_DIVERGED_SYMMETRY_LOST = -3, EPS_CONVERGED_ITERATING = 0 } EPSConvergedReason;
+typedef enum { EPS_ERROR_ABSOLUTE, EPS_ERROR_RELATIVE, EPS_ERROR_BACKWARD } EPSErrorType;
+
+/* SlepcInitialize / SlepcFinalize (src/sys/slepcinit.c): no-op shims */
+PetscErrorCode SlepcInitialize(int *argc, char ***argv, const char file[], const char help[]);
+PetscErrorCode SlepcFinalize(void);
+
+/* life cycle: src/eps/interface/epsbasic.c:48-158 */
+PetscErrorCode EPSCreate(MPI_Comm comm, EPS *eps);
+PetscErrorCode EPSDestroy(EPS *eps);
+PetscErrorCode EPSReset(EPS eps);
+PetscErrorCode EPSSetType(EPS eps, EPSType type);
+PetscErrorCode EPSGetType(EPS eps, EPSType *type);
+/* problem definition: epssetup.c:470-520 (EPSSetOperators), epsopts.c */
+PetscErrorCode EPSSetOperators(EPS eps, Mat A, Mat B);
+PetscErrorCode EPSGetOperators(EPS eps, Mat *A, Mat *B);
+PetscErrorCode EPSSetProblemType(EPS eps, EPSProblemType type);
+PetscErrorCode EPSGetProblemType(EPS eps, EPSProblemType *type);
+PetscErrorCode EPSSetExtraction(EPS eps, EPSExtraction extr);
+PetscErrorCode EPSSetDimensions(EPS eps, PetscInt nev, PetscInt ncv, PetscInt mpd);     /* epsopts.c:392-417 */
+PetscErrorCode EPSGetDimensions(EPS eps, PetscInt *nev, PetscInt *ncv, PetscInt *mpd);
+PetscErrorCode EPSSetTolerances(EPS eps, PetscReal tol, PetscInt maxits);               /* epsopts.c:300-323 */
+PetscErrorCode EPSGetTolerances(EPS eps, PetscReal *tol, PetscInt *maxits);
+PetscErrorCode EPSSetWhichEigenpairs(EPS eps, EPSWhich which);
+PetscErrorCode EPSGetWhichEigenpairs(EPS eps, EPSWhich *which);
+PetscErrorCode EPSSetInitialSpace(EPS eps, PetscInt n, Vec is[]);                          /* epssetup.c:592 */
+PetscErrorCode EPSSetFromOptions(EPS eps);
+/* Krylov-Schur knobs: krylovschur.c:339-489 */
+PetscErrorCode EPSKrylovSchurSetRestart(EPS eps, PetscReal keep);
+PetscErrorCode EPSKrylovSchurGetRestart(EPS eps, PetscReal *keep);
+PetscErrorCode EPSKrylovSchurSetLocking(EPS eps, PetscBool lock);
+PetscErrorCode EPSKrylovSchurGetLocking(EPS eps, PetscBool *lock);
+/* setup and solve: epssetup.c:286-418, epssolve.c:119-208 */
+PetscErrorCode EPSSetUp(EPS eps);
+PetscErrorCode EPSSolve(EPS eps);
+/* results: epssolve.c:240-420, 742-815 */
+PetscErrorCode EPSGetConverged(EPS eps, PetscInt *nconv);
+PetscErrorCode EPSGetConvergedReason(EPS eps, EPSConvergedReason *reason);
+PetscErrorCode EPSGetIterationNumber(EPS eps, PetscInt *its);
+PetscErrorCode EPSGetEigenpair(EPS eps, PetscInt i, PetscScalar *eigr, PetscScalar *eigi, Vec Vr, Vec Vi);
+PetscErrorCode EPSGetEigenvalue(EPS eps, PetscInt i, PetscScalar *eigr, PetscScalar *eigi);
+PetscErrorCode EPSGetEigenvector(EPS eps, PetscInt i, Vec Vr, Vec Vi);
+PetscErrorCode EPSGetErrorEstimate(EPS eps, PetscInt i, PetscReal *errest);
+PetscErrorCode EPSComputeError(EPS eps, PetscInt i, EPSErrorType type, PetscReal *error);
+PetscErrorCode EPSGetBV(EPS eps, BV *V);
+PetscErrorCode EPSGetDS(EPS eps, DS *ds);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

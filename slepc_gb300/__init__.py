@@ -1,0 +1,367 @@
+"""slepc_gb300 -- GB300-native Krylov-Schur eigensolver behind SLEPc's API.
+
+The product is the C-ABI library ``_build/libslepc_gb300.so`` (hand-written sm_103a CUDA kernels plus the C++ host
+driver; headers in ``include/``).  This module is the Python host mirror of slepc4py's EPS/Mat/Vec interface for
+that path (``src/binding/slepc4py/SLEPc/EPS.pyx``: ``setOperators`` :1087, ``solve`` :1290, ``getEigenpair``
+:1426), implemented over ctypes.  There is no CPU fallback: loading fails loudly when the library is missing.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libslepc_gb300.so")
+
+_lib = None
+
+
+class SlepcError(RuntimeError):
+    def __init__(self, code, where, msg):
+        super().__init__(f"{where} failed with PETSc error {code}: {msg}")
+        self.code = code
+
+
+def build(force=False, verbose=False):
+    from . import buildlib as _b
+    return _b.build(force=force, verbose=verbose)
+
+
+def load():
+    """Load libslepc_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"slepc_gb300 CUDA library not built ({LIB_PATH}); run slepc_gb300.build()")
+    lib = ctypes.CDLL(LIB_PATH)
+    P, I, D = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+    PP = ctypes.POINTER(ctypes.c_void_p)
+    sig = {
+        "PetscGB300LastError": ([], ctypes.c_char_p),
+        "MatCreateSeqAIJWithArrays": ([I, I, I, P, P, P, PP], I),
+        "MatCreateSeqDense": ([I, I, I, P, PP], I),
+        "MatDestroy": ([PP], I),
+        "MatMult": ([P, P, P], I),
+        "VecCreateSeqWithArray": ([I, I, I, P, PP], I),
+        "VecDestroy": ([PP], I),
+        "EPSCreate": ([I, PP], I),
+        "EPSDestroy": ([PP], I),
+        "EPSSetOperators": ([P, P, P], I),
+        "EPSSetProblemType": ([P, I], I),
+        "EPSSetType": ([P, ctypes.c_char_p], I),
+        "EPSSetDimensions": ([P, I, I, I], I),
+        "EPSGetDimensions": ([P, P, P, P], I),
+        "EPSSetTolerances": ([P, D, I], I),
+        "EPSGetTolerances": ([P, P, P], I),
+        "EPSSetWhichEigenpairs": ([P, I], I),
+        "EPSSetInitialSpace": ([P, I, PP], I),
+        "EPSKrylovSchurSetRestart": ([P, D], I),
+        "EPSKrylovSchurSetLocking": ([P, I], I),
+        "EPSSetUp": ([P], I),
+        "EPSSolve": ([P], I),
+        "EPSGetConverged": ([P, P], I),
+        "EPSGetConvergedReason": ([P, P], I),
+        "EPSGetIterationNumber": ([P, P], I),
+        "EPSGetEigenpair": ([P, I, P, P, P, P], I),
+        "EPSGetEigenvalue": ([P, I, P, P], I),
+        "EPSGetErrorEstimate": ([P, I, P], I),
+        "EPSComputeError": ([P, I, I, P], I),
+        "EPSGB300SetArithmetic": ([P, I], I),
+        "EPSGB300GetStats": ([P, P], I),
+        "EPSGB300OrthogonalityError": ([P, P], I),
+        "EPSGB300SetProfiling": ([P, I], I),
+        "EPSGB300GetProfile": ([P, I, P, P, P], I),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = lib
+    return lib
+
+
+def _check(code, where):
+    if code:
+        msg = load().PetscGB300LastError().decode(errors="replace")
+        raise SlepcError(code, where, msg)
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Vec:
+    """A host vector wrapping a numpy float64 array (VecCreateSeqWithArray)."""
+
+    def __init__(self, array):
+        self.array = np.ascontiguousarray(array, dtype=np.float64)
+        self.handle = ctypes.c_void_p()
+        _check(load().VecCreateSeqWithArray(0, 1, self.array.size, _ptr(self.array), ctypes.byref(self.handle)),
+               "VecCreateSeqWithArray")
+
+    def destroy(self):
+        if self.handle:
+            load().VecDestroy(ctypes.byref(self.handle))
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
+class Mat:
+    """CSR matrix over caller-owned arrays (MatCreateSeqAIJWithArrays); the arrays are kept alive here."""
+
+    def __init__(self, rowptr, colidx, vals, ncols=None):
+        self.rowptr = np.ascontiguousarray(rowptr, dtype=np.int32)
+        self.colidx = np.ascontiguousarray(colidx, dtype=np.int32)
+        self.vals = np.ascontiguousarray(vals, dtype=np.float64)
+        self.m = self.rowptr.size - 1
+        self.n = self.m if ncols is None else int(ncols)
+        self.handle = ctypes.c_void_p()
+        _check(load().MatCreateSeqAIJWithArrays(0, self.m, self.n, _ptr(self.rowptr), _ptr(self.colidx),
+                                                _ptr(self.vals), ctypes.byref(self.handle)),
+               "MatCreateSeqAIJWithArrays")
+
+    @classmethod
+    def createAIJ(cls, csr):
+        return cls(*csr)
+
+    def mult(self, x):
+        y = np.zeros(self.m)
+        vx, vy = Vec(x), Vec(y)
+        _check(load().MatMult(self.handle, vx.handle, vy.handle), "MatMult")
+        return vy.array.copy()
+
+    def destroy(self):
+        if self.handle:
+            load().MatDestroy(ctypes.byref(self.handle))
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
+class EPS:
+    """Eigenvalue problem solver (EPSKRYLOVSCHUR), mirroring slepc4py.SLEPc.EPS."""
+
+    class ProblemType:
+        HEP = 1
+        NHEP = 3
+
+    class Which:
+        LARGEST_MAGNITUDE = 1
+        SMALLEST_MAGNITUDE = 2
+        LARGEST_REAL = 3
+        SMALLEST_REAL = 4
+        LARGEST_IMAGINARY = 5
+        SMALLEST_IMAGINARY = 6
+
+    class ErrorType:
+        ABSOLUTE = 0
+        RELATIVE = 1
+        BACKWARD = 2
+
+    class ConvergedReason:
+        CONVERGED_TOL = 1
+        DIVERGED_ITS = -1
+        DIVERGED_BREAKDOWN = -2
+        CONVERGED_ITERATING = 0
+
+    WHICH_NAMES = {"LM": 1, "SM": 2, "LR": 3, "SR": 4, "LI": 5, "SI": 6}
+
+    def __init__(self):
+        self.handle = ctypes.c_void_p()
+        self._A = None
+        self._v0 = None
+
+    def create(self, comm=None):
+        _check(load().EPSCreate(0, ctypes.byref(self.handle)), "EPSCreate")
+        return self
+
+    def destroy(self):
+        if self.handle:
+            load().EPSDestroy(ctypes.byref(self.handle))
+        return self
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+    def setType(self, t="krylovschur"):
+        _check(load().EPSSetType(self.handle, t.encode()), "EPSSetType")
+
+    def setOperators(self, A, B=None):
+        if B is not None:
+            raise SlepcError(56, "EPSSetOperators", "generalised problems are not provided")
+        self._A = A
+        _check(load().EPSSetOperators(self.handle, A.handle, None), "EPSSetOperators")
+
+    def setProblemType(self, ptype):
+        _check(load().EPSSetProblemType(self.handle, int(ptype)), "EPSSetProblemType")
+
+    def setDimensions(self, nev=None, ncv=None, mpd=None):
+        cur = -2
+        _check(load().EPSSetDimensions(self.handle, cur if nev is None else int(nev), cur if ncv is None else int(ncv),
+                                       cur if mpd is None else int(mpd)), "EPSSetDimensions")
+
+    def getDimensions(self):
+        a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _check(load().EPSGetDimensions(self.handle, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)), "EPSGetDimensions")
+        return a.value, b.value, c.value
+
+    def setTolerances(self, tol=None, max_it=None):
+        _check(load().EPSSetTolerances(self.handle, -2.0 if tol is None else float(tol),
+                                       -2 if max_it is None else int(max_it)), "EPSSetTolerances")
+
+    def getTolerances(self):
+        t, m = ctypes.c_double(), ctypes.c_int()
+        _check(load().EPSGetTolerances(self.handle, ctypes.byref(t), ctypes.byref(m)), "EPSGetTolerances")
+        return t.value, m.value
+
+    def setWhichEigenpairs(self, which):
+        if isinstance(which, str):
+            which = self.WHICH_NAMES[which]
+        _check(load().EPSSetWhichEigenpairs(self.handle, int(which)), "EPSSetWhichEigenpairs")
+
+    def setInitialSpace(self, space):
+        if space is None or (isinstance(space, (list, tuple)) and len(space) == 0):
+            _check(load().EPSSetInitialSpace(self.handle, 0, None), "EPSSetInitialSpace")
+            return
+        if isinstance(space, (list, tuple)):
+            space = space[0]
+        v = space if isinstance(space, Vec) else Vec(space)
+        self._v0 = v
+        arr = (ctypes.c_void_p * 1)(v.handle.value)
+        _check(load().EPSSetInitialSpace(self.handle, 1, arr), "EPSSetInitialSpace")
+
+    def setKrylovSchurRestart(self, keep):
+        _check(load().EPSKrylovSchurSetRestart(self.handle, float(keep)), "EPSKrylovSchurSetRestart")
+
+    def setKrylovSchurLocking(self, lock):
+        _check(load().EPSKrylovSchurSetLocking(self.handle, int(bool(lock))), "EPSKrylovSchurSetLocking")
+
+    def setArithmetic(self, arith):
+        """'pair' (FP64 storage, error-free FP32-pair arithmetic) or 'f64' (IEEE FP64 FMA)."""
+        _check(load().EPSGB300SetArithmetic(self.handle, 1 if arith == "f64" else 0), "EPSGB300SetArithmetic")
+
+    def setUp(self):
+        _check(load().EPSSetUp(self.handle), "EPSSetUp")
+
+    def solve(self):
+        _check(load().EPSSolve(self.handle), "EPSSolve")
+
+    def getConverged(self):
+        v = ctypes.c_int()
+        _check(load().EPSGetConverged(self.handle, ctypes.byref(v)), "EPSGetConverged")
+        return v.value
+
+    def getConvergedReason(self):
+        v = ctypes.c_int()
+        _check(load().EPSGetConvergedReason(self.handle, ctypes.byref(v)), "EPSGetConvergedReason")
+        return v.value
+
+    def getIterationNumber(self):
+        v = ctypes.c_int()
+        _check(load().EPSGetIterationNumber(self.handle, ctypes.byref(v)), "EPSGetIterationNumber")
+        return v.value
+
+    def getEigenvalue(self, i):
+        re, im = ctypes.c_double(), ctypes.c_double()
+        _check(load().EPSGetEigenvalue(self.handle, int(i), ctypes.byref(re), ctypes.byref(im)), "EPSGetEigenvalue")
+        return complex(re.value, im.value) if im.value != 0.0 else re.value
+
+    def getEigenpair(self, i, Vr=None, Vi=None):
+        """Returns the eigenvalue; fills the numpy arrays / Vec objects Vr, Vi (length n) when given."""
+        re, im = ctypes.c_double(), ctypes.c_double()
+        vr = Vr if (Vr is None or isinstance(Vr, Vec)) else Vec(Vr)
+        vi = Vi if (Vi is None or isinstance(Vi, Vec)) else Vec(Vi)
+        _check(load().EPSGetEigenpair(self.handle, int(i), ctypes.byref(re), ctypes.byref(im),
+                                      vr.handle if vr is not None else None, vi.handle if vi is not None else None),
+               "EPSGetEigenpair")
+        if Vr is not None and not isinstance(Vr, Vec):
+            Vr[...] = vr.array
+        if Vi is not None and not isinstance(Vi, Vec):
+            Vi[...] = vi.array
+        return complex(re.value, im.value) if im.value != 0.0 else re.value
+
+    def getErrorEstimate(self, i):
+        v = ctypes.c_double()
+        _check(load().EPSGetErrorEstimate(self.handle, int(i), ctypes.byref(v)), "EPSGetErrorEstimate")
+        return v.value
+
+    def computeError(self, i, etype=ErrorType.RELATIVE):
+        v = ctypes.c_double()
+        _check(load().EPSComputeError(self.handle, int(i), int(etype), ctypes.byref(v)), "EPSComputeError")
+        return v.value
+
+    def getStats(self):
+        buf = (ctypes.c_char * 64)()
+        _check(load().EPSGB300GetStats(self.handle, buf), "EPSGB300GetStats")
+        steps, restarts = np.frombuffer(bytes(buf[:16]), dtype=np.int64)
+        solve_s, bytes_moved, setup_s = np.frombuffer(bytes(buf[16:40]), dtype=np.float64)
+        launches = np.frombuffer(bytes(buf[40:48]), dtype=np.int64)[0]
+        dev_ms = np.frombuffer(bytes(buf[48:56]), dtype=np.float64)[0]
+        return {"krylov_steps": int(steps), "restarts": int(restarts), "solve_seconds": float(solve_s),
+                "bytes_moved": float(bytes_moved), "setup_seconds": float(setup_s), "kernel_launches": int(launches),
+                "solve_device_ms": float(dev_ms)}
+
+    KERNEL_CLASSES = ("spmv", "gs_dot", "gs_update", "restart", "ds")
+
+    def setProfiling(self, on=True):
+        _check(load().EPSGB300SetProfiling(self.handle, int(bool(on))), "EPSGB300SetProfiling")
+
+    def getProfile(self):
+        """{class: (device ms, algorithmic bytes, launches)} accumulated since setProfiling(True)."""
+        out = {}
+        for c, name in enumerate(self.KERNEL_CLASSES):
+            ms, by, nl = ctypes.c_double(), ctypes.c_double(), ctypes.c_longlong()
+            _check(load().EPSGB300GetProfile(self.handle, c, ctypes.byref(ms), ctypes.byref(by), ctypes.byref(nl)),
+                   "EPSGB300GetProfile")
+            out[name] = (ms.value, by.value, nl.value)
+        return out
+
+    def orthogonalityError(self):
+        v = ctypes.c_double()
+        _check(load().EPSGB300OrthogonalityError(self.handle, ctypes.byref(v)), "EPSGB300OrthogonalityError")
+        return v.value
+
+
+def solve(csr, *, hermitian=True, which="LM", nev=1, ncv=None, mpd=None, tol=None, max_it=None, v0=None,
+          arith="pair", vectors=True):
+    """One-call convenience: returns dict(eigr, eigi, X, nconv, its, reason, errors, stats)."""
+    A = Mat(*csr)
+    eps = EPS().create()
+    eps.setOperators(A)
+    eps.setProblemType(EPS.ProblemType.HEP if hermitian else EPS.ProblemType.NHEP)
+    eps.setDimensions(nev, ncv if ncv else -1, mpd if mpd else -1)
+    eps.setTolerances(tol if tol else -1.0, max_it if max_it else -1)
+    eps.setWhichEigenpairs(which)
+    eps.setArithmetic(arith)
+    if v0 is not None:
+        eps.setInitialSpace(v0)
+    eps.solve()
+    nconv = eps.getConverged()
+    n = A.m
+    eigr = np.zeros(nconv)
+    eigi = np.zeros(nconv)
+    X = np.zeros((n, nconv)) if vectors else None
+    for i in range(nconv):
+        xr = np.zeros(n)
+        lam = eps.getEigenpair(i, xr if vectors else None)
+        eigr[i] = lam.real if isinstance(lam, complex) else lam
+        eigi[i] = lam.imag if isinstance(lam, complex) else 0.0
+        if vectors:
+            X[:, i] = xr
+    out = {"eigr": eigr, "eigi": eigi, "X": X, "nconv": nconv, "its": eps.getIterationNumber(),
+           "reason": eps.getConvergedReason(), "stats": eps.getStats(),
+           "errors": np.array([eps.computeError(i) for i in range(nconv)]), "eps": eps, "A": A}
+    return out

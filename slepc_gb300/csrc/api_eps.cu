@@ -1,0 +1,1249 @@
+// api_eps.cu -- C API: errors, Mat, Vec and the EPS object with its device-resident Krylov-Schur driver.
+//
+// The restart loop is EPSSolve_KrylovSchur_Default (src/eps/impls/krylov/krylovschur/krylovschur.c:227-337):
+//   factorise (SpMV + fused Gram-Schmidt pair per step, all launches asynchronous on the EPS stream)
+//   -> projected problem, convergence, stopping test and restart sizes in one device kernel
+//   -> one 64-byte control record read back per restart
+//   -> thick restart V(:, nconv:k+l) = V(:, nconv:nv) Q, copy of the residual vector to column k+l.
+// No scalar of a Krylov step crosses to the host.
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <chrono>
+
+#include "internal.h"
+
+using namespace ksg;
+
+// ---------------------------------------------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------------------------------------------
+static thread_local char g_last_error[512] = "";
+
+PetscErrorCode ksg_set_error(PetscErrorCode code, const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_last_error, sizeof(g_last_error), fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+extern "C" const char *PetscGB300LastError(void) { return g_last_error; }
+
+extern "C" PetscErrorCode PetscInitialize(int *, char ***, const char[], const char[]) { return 0; }
+extern "C" PetscErrorCode PetscFinalize(void) { return 0; }
+
+static int g_argc = 0;
+static char **g_argv = nullptr;
+extern "C" PetscErrorCode SlepcInitialize(int *argc, char ***argv, const char[], const char[]) {
+  if (argc && argv) {
+    g_argc = *argc;
+    g_argv = *argv;
+  }
+  return 0;
+}
+extern "C" PetscErrorCode SlepcFinalize(void) { return 0; }
+
+// ---------------------------------------------------------------------------------------------------------------
+// random vectors: splitmix64 uniform in [-1, 1), counter-based so that any column can be regenerated
+// ---------------------------------------------------------------------------------------------------------------
+PetscErrorCode ksg_random_fill(double *host, int n, unsigned long long seed, unsigned long long stream_index) {
+  unsigned long long base = seed ^ (0xD1B54A32D192ED03ULL * (stream_index + 1));
+  for (int i = 0; i < n; ++i) {
+    unsigned long long z = base + (unsigned long long)(i + 1) * 0x9E3779B97F4A7C15ULL;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    z ^= z >> 31;
+    host[i] = (double)(z >> 11) * (2.0 / 9007199254740992.0) - 1.0;
+  }
+  return 0;
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// Mat
+// ---------------------------------------------------------------------------------------------------------------
+extern "C" PetscErrorCode MatCreateSeqAIJWithArrays(MPI_Comm, PetscInt m, PetscInt n, PetscInt i[], PetscInt j[],
+                                                    PetscScalar a[], Mat *A) {
+  KSG_CHECK(A, PETSC_ERR_ARG_NULL, "Null Mat pointer");
+  KSG_CHECK(m >= 0 && n >= 0, PETSC_ERR_ARG_OUTOFRANGE, "Negative dimension");
+  KSG_CHECK(i && (i[m] == 0 || (j && a)), PETSC_ERR_ARG_NULL, "Null CSR array");
+  KSG_CHECK(i[0] == 0, PETSC_ERR_ARG_WRONG, "i (row pointers) must start with 0");
+  for (int r = 0; r < m; ++r) {
+    KSG_CHECK(i[r + 1] >= i[r], PETSC_ERR_ARG_WRONG, "Row pointers must be nondecreasing (row %d)", r);
+    for (int p = i[r]; p < i[r + 1]; ++p) {
+      KSG_CHECK(j[p] >= 0 && j[p] < n, PETSC_ERR_ARG_OUTOFRANGE, "Column index %d out of range in row %d", j[p], r);
+      KSG_CHECK(isfinite(a[p]), PETSC_ERR_ARG_WRONG, "Matrix entry (%d,%d) is not finite", r, j[p]);
+    }
+  }
+  Mat M = new _p_Mat();
+  M->m = m;
+  M->n = n;
+  M->ai = i;
+  M->aj = j;
+  M->aa = a;
+  M->nnz = i[m];
+  *A = M;
+  return 0;
+}
+
+extern "C" PetscErrorCode MatCreateSeqDense(MPI_Comm, PetscInt m, PetscInt n, PetscScalar data[], Mat *A) {
+  KSG_CHECK(A, PETSC_ERR_ARG_NULL, "Null Mat pointer");
+  KSG_CHECK(m >= 0 && n >= 0, PETSC_ERR_ARG_OUTOFRANGE, "Negative dimension");
+  Mat M = new _p_Mat();
+  M->m = m;
+  M->n = n;
+  M->dense = 1;
+  M->lda = m > 0 ? m : 1;
+  if (data) M->data = data;
+  else {
+    M->dbuf.assign((size_t)M->lda * (n > 0 ? n : 1), 0.0);
+    M->data = M->dbuf.data();
+  }
+  *A = M;
+  return 0;
+}
+
+extern "C" PetscErrorCode MatDenseGetArray(Mat A, PetscScalar **array) {
+  KSG_CHECK(A && A->dense, PETSC_ERR_ARG_WRONG, "Not a dense Mat");
+  *array = A->data;
+  return 0;
+}
+extern "C" PetscErrorCode MatDenseRestoreArray(Mat A, PetscScalar **array) {
+  if (array) *array = nullptr;
+  return 0;
+}
+extern "C" PetscErrorCode MatDenseGetLDA(Mat A, PetscInt *lda) {
+  KSG_CHECK(A && A->dense, PETSC_ERR_ARG_WRONG, "Not a dense Mat");
+  *lda = A->lda;
+  return 0;
+}
+extern "C" PetscErrorCode MatGetSize(Mat A, PetscInt *m, PetscInt *n) {
+  KSG_CHECK(A, PETSC_ERR_ARG_NULL, "Null Mat");
+  if (m) *m = A->m;
+  if (n) *n = A->n;
+  return 0;
+}
+extern "C" PetscErrorCode MatGetValue(Mat A, PetscInt row, PetscInt col, PetscScalar *v) {
+  KSG_CHECK(A && v, PETSC_ERR_ARG_NULL, "Null argument");
+  KSG_CHECK(row >= 0 && row < A->m && col >= 0 && col < A->n, PETSC_ERR_ARG_OUTOFRANGE, "Index out of range");
+  if (A->dense) {
+    *v = A->data[row + (size_t)col * A->lda];
+    return 0;
+  }
+  *v = 0.0;
+  for (int p = A->ai[row]; p < A->ai[row + 1]; ++p)
+    if (A->aj[p] == col) *v += A->aa[p];
+  return 0;
+}
+
+PetscErrorCode ksg_mat_upload(Mat A) {
+  if (A->device_ready) return 0;
+  KSG_CHECK(!A->dense, PETSC_ERR_SUP, "Operator must be an AIJ (CSR) matrix");
+  KSG_CUDA(A->d_rp.alloc(A->m + 1));
+  KSG_CUDA(A->d_ci.alloc(A->nnz > 0 ? A->nnz : 1));
+  KSG_CUDA(A->d_va.alloc(A->nnz > 0 ? A->nnz : 1));
+  KSG_CUDA(cudaMemcpy(A->d_rp.p, A->ai, sizeof(int) * (A->m + 1), cudaMemcpyHostToDevice));
+  if (A->nnz > 0) {
+    KSG_CUDA(cudaMemcpy(A->d_ci.p, A->aj, sizeof(int) * A->nnz, cudaMemcpyHostToDevice));
+    KSG_CUDA(cudaMemcpy(A->d_va.p, A->aa, sizeof(double) * A->nnz, cudaMemcpyHostToDevice));
+  }
+  A->device_ready = 1;
+  return 0;
+}
+
+double ksg_mat_norm_inf(Mat A) {
+  if (A->norm_inf >= 0.0) return A->norm_inf;
+  double mx = 0.0;
+  if (A->dense) {
+    for (int r = 0; r < A->m; ++r) {
+      double s = 0.0;
+      for (int c = 0; c < A->n; ++c) s += fabs(A->data[r + (size_t)c * A->lda]);
+      mx = std::max(mx, s);
+    }
+  } else {
+    for (int r = 0; r < A->m; ++r) {
+      double s = 0.0;
+      for (int p = A->ai[r]; p < A->ai[r + 1]; ++p) s += fabs(A->aa[p]);
+      mx = std::max(mx, s);
+    }
+  }
+  A->norm_inf = mx;
+  return mx;
+}
+
+extern "C" PetscErrorCode MatNorm(Mat A, NormType type, PetscReal *nrm) {
+  KSG_CHECK(A && nrm, PETSC_ERR_ARG_NULL, "Null argument");
+  if (type == NORM_INFINITY) {
+    *nrm = ksg_mat_norm_inf(A);
+    return 0;
+  }
+  if (type == NORM_FROBENIUS) {
+    double s = 0.0;
+    if (A->dense) {
+      for (int c = 0; c < A->n; ++c)
+        for (int r = 0; r < A->m; ++r) s += A->data[r + (size_t)c * A->lda] * A->data[r + (size_t)c * A->lda];
+    } else {
+      for (long long p = 0; p < A->nnz; ++p) s += A->aa[p] * A->aa[p];
+    }
+    *nrm = sqrt(s);
+    return 0;
+  }
+  if (type == NORM_1) {
+    std::vector<double> col(A->n, 0.0);
+    if (A->dense) {
+      for (int c = 0; c < A->n; ++c)
+        for (int r = 0; r < A->m; ++r) col[c] += fabs(A->data[r + (size_t)c * A->lda]);
+    } else {
+      for (long long p = 0; p < A->nnz; ++p) col[A->aj[p]] += fabs(A->aa[p]);
+    }
+    *nrm = col.empty() ? 0.0 : *std::max_element(col.begin(), col.end());
+    return 0;
+  }
+  return ksg_set_error(PETSC_ERR_SUP, "MatNorm: unsupported norm type");
+}
+
+extern "C" PetscErrorCode MatMult(Mat A, Vec x, Vec y) {
+  KSG_CHECK(A && x && y, PETSC_ERR_ARG_NULL, "Null argument");
+  KSG_CHECK(x->n == A->n && y->n == A->m, PETSC_ERR_ARG_SIZ, "Nonconforming sizes");
+  if (A->dense) return ksg_set_error(PETSC_ERR_SUP, "MatMult on a dense Mat is not provided");
+  KSG_TRY(ksg_mat_upload(A));
+  DBuf<double> dx, dy;
+  KSG_CUDA(dx.alloc(A->n > 0 ? A->n : 1));
+  KSG_CUDA(dy.alloc(A->m > 0 ? A->m : 1));
+  KSG_CUDA(cudaMemcpy(dx.p, x->a, sizeof(double) * A->n, cudaMemcpyHostToDevice));
+  const int lanes = spmv_lanes_for(A->m > 0 ? (double)A->nnz / A->m : 1.0);
+  KSG_CUDA(launch_spmv(A->d_rp.p, A->d_ci.p, A->d_va.p, dx.p, dy.p, A->m, lanes, nullptr, 1.0, 0));
+  KSG_CUDA(cudaMemcpy(y->a, dy.p, sizeof(double) * A->m, cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+extern "C" PetscErrorCode MatCreateVecs(Mat A, Vec *right, Vec *left) {
+  KSG_CHECK(A, PETSC_ERR_ARG_NULL, "Null Mat");
+  if (right) KSG_TRY(VecCreateSeq(0, A->n, right));
+  if (left) KSG_TRY(VecCreateSeq(0, A->m, left));
+  return 0;
+}
+
+extern "C" PetscErrorCode MatDestroy(Mat *A) {
+  if (!A || !*A) return 0;
+  if (--(*A)->refs <= 0) delete *A;
+  *A = nullptr;
+  return 0;
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// Vec
+// ---------------------------------------------------------------------------------------------------------------
+extern "C" PetscErrorCode VecCreateSeq(MPI_Comm, PetscInt n, Vec *v) {
+  KSG_CHECK(v, PETSC_ERR_ARG_NULL, "Null Vec pointer");
+  KSG_CHECK(n >= 0, PETSC_ERR_ARG_OUTOFRANGE, "Negative size");
+  Vec V = new _p_Vec();
+  V->n = n;
+  V->own.assign(n > 0 ? n : 1, 0.0);
+  V->a = V->own.data();
+  *v = V;
+  return 0;
+}
+extern "C" PetscErrorCode VecCreateSeqWithArray(MPI_Comm, PetscInt, PetscInt n, const PetscScalar array[], Vec *v) {
+  KSG_CHECK(v, PETSC_ERR_ARG_NULL, "Null Vec pointer");
+  KSG_CHECK(n >= 0, PETSC_ERR_ARG_OUTOFRANGE, "Negative size");
+  Vec V = new _p_Vec();
+  V->n = n;
+  if (array) V->a = const_cast<double *>(array);
+  else {
+    V->own.assign(n > 0 ? n : 1, 0.0);
+    V->a = V->own.data();
+  }
+  *v = V;
+  return 0;
+}
+extern "C" PetscErrorCode VecDuplicate(Vec v, Vec *newv) { return VecCreateSeq(0, v->n, newv); }
+extern "C" PetscErrorCode VecGetSize(Vec v, PetscInt *n) {
+  KSG_CHECK(v && n, PETSC_ERR_ARG_NULL, "Null argument");
+  *n = v->n;
+  return 0;
+}
+extern "C" PetscErrorCode VecGetArray(Vec v, PetscScalar **a) {
+  KSG_CHECK(v && a, PETSC_ERR_ARG_NULL, "Null argument");
+  *a = v->a;
+  return 0;
+}
+extern "C" PetscErrorCode VecRestoreArray(Vec, PetscScalar **a) {
+  if (a) *a = nullptr;
+  return 0;
+}
+extern "C" PetscErrorCode VecGetArrayRead(Vec v, const PetscScalar **a) {
+  KSG_CHECK(v && a, PETSC_ERR_ARG_NULL, "Null argument");
+  *a = v->a;
+  return 0;
+}
+extern "C" PetscErrorCode VecRestoreArrayRead(Vec, const PetscScalar **a) {
+  if (a) *a = nullptr;
+  return 0;
+}
+extern "C" PetscErrorCode VecSet(Vec v, PetscScalar alpha) {
+  KSG_CHECK(v, PETSC_ERR_ARG_NULL, "Null Vec");
+  for (int i = 0; i < v->n; ++i) v->a[i] = alpha;
+  return 0;
+}
+extern "C" PetscErrorCode VecCopy(Vec x, Vec y) {
+  KSG_CHECK(x && y && x->n == y->n, PETSC_ERR_ARG_SIZ, "Nonconforming vectors");
+  memmove(y->a, x->a, sizeof(double) * x->n);
+  return 0;
+}
+extern "C" PetscErrorCode VecScale(Vec v, PetscScalar alpha) {
+  KSG_CHECK(v, PETSC_ERR_ARG_NULL, "Null Vec");
+  for (int i = 0; i < v->n; ++i) v->a[i] *= alpha;
+  return 0;
+}
+extern "C" PetscErrorCode VecAXPY(Vec y, PetscScalar alpha, Vec x) {
+  KSG_CHECK(x && y && x->n == y->n, PETSC_ERR_ARG_SIZ, "Nonconforming vectors");
+  for (int i = 0; i < x->n; ++i) y->a[i] += alpha * x->a[i];
+  return 0;
+}
+extern "C" PetscErrorCode VecDot(Vec x, Vec y, PetscScalar *val) {
+  KSG_CHECK(x && y && val && x->n == y->n, PETSC_ERR_ARG_SIZ, "Nonconforming vectors");
+  double s = 0.0;
+  for (int i = 0; i < x->n; ++i) s += x->a[i] * y->a[i];
+  *val = s;
+  return 0;
+}
+extern "C" PetscErrorCode VecNorm(Vec v, NormType type, PetscReal *nrm) {
+  KSG_CHECK(v && nrm, PETSC_ERR_ARG_NULL, "Null argument");
+  double r = 0.0;
+  if (type == NORM_2 || type == NORM_FROBENIUS) {
+    for (int i = 0; i < v->n; ++i) r += v->a[i] * v->a[i];
+    r = sqrt(r);
+  } else if (type == NORM_1) {
+    for (int i = 0; i < v->n; ++i) r += fabs(v->a[i]);
+  } else if (type == NORM_INFINITY) {
+    for (int i = 0; i < v->n; ++i) r = std::max(r, fabs(v->a[i]));
+  } else return ksg_set_error(PETSC_ERR_SUP, "VecNorm: unsupported norm type");
+  *nrm = r;
+  return 0;
+}
+extern "C" PetscErrorCode VecDestroy(Vec *v) {
+  if (!v || !*v) return 0;
+  delete *v;
+  *v = nullptr;
+  return 0;
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// shared Gram-Schmidt helper: orthonormalise V[:, j] against V[:, 0:j] with CGS passes (REFINE_IFNEEDED when
+// refine == 0, two passes when refine == 2, one pass plus explicit norm when refine == 1)
+// ---------------------------------------------------------------------------------------------------------------
+size_t ksg_part_stride(int ld) { return (size_t)2 * ld + 8; }
+size_t ksg_part_blocks(int n) { return (size_t)std::max(gs_dot_blocks(n), gs_update_blocks(n)); }
+
+PetscErrorCode ksg_orthonormalize_column(double *V, long long ldv, int n, int j, double *coef, float2 *part,
+                                         int pstride, KrylovState *st, int arith, cudaStream_t s, double *nrm,
+                                         int *lindep, int refine) {
+  StepArgs a = {};
+  a.V = V;
+  a.ldv = ldv;
+  a.n = n;
+  a.J = j;
+  a.j = j;
+  a.hermitian = 1;
+  a.U = V + (size_t)j * ldv;
+  a.W = nullptr;
+  a.eta = 0.7071;
+  a.coef = coef;
+  a.part = part;
+  a.pstride = pstride;
+  a.st = st;
+  // refine: 0 IFNEEDED (up to 3 passes, bvorthog.c:176-187), 1 NEVER (one pass), 2 ALWAYS (two passes)
+  const int passes_max = (refine == 2) ? 2 : (refine == 1 ? 1 : 3);
+  double total = 1.0;
+  int ld = 0;
+  for (int pass = 0; pass < passes_max; ++pass) {
+    KSG_CUDA(launch_segment_begin(st, j, j, s));
+    KSG_CUDA(launch_gs_dot(a, 1, GS_ORTHO, arith, s));
+    KSG_CUDA(launch_gs_update(a, 1, GS_ORTHO, arith, s));
+    KrylovState h;
+    KSG_CUDA(cudaMemcpyAsync(&h, st, sizeof(h), cudaMemcpyDeviceToHost, s));
+    KSG_CUDA(cudaStreamSynchronize(s));
+    if (h.breakdown) {
+      total = 0.0;
+      ld = 1;
+      break;
+    }
+    const double nu = 1.0 / h.invnu;  // norm kept by this pass (the pass leaves the vector normalised)
+    total *= nu;
+    const int kept = nu >= 0.7071 * h.onorm;
+    if (refine == 1) break;
+    if (refine == 0) {
+      if (kept) break;
+      if (pass == passes_max - 1) ld = 1;
+    }
+    if (refine == 2 && pass == 1) ld = !kept;
+  }
+  if (nrm) *nrm = total;
+  if (lindep) *lindep = ld;
+  return 0;
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// EPS
+// ---------------------------------------------------------------------------------------------------------------
+static PetscErrorCode eps_free_device(EPS eps) {
+  eps->V.release();
+  eps->d.release();
+  eps->e.release();
+  eps->H.release();
+  eps->Q.release();
+  eps->X.release();
+  eps->eigr.release();
+  eps->eigi.release();
+  eps->errest.release();
+  eps->coef.release();
+  eps->work.release();
+  eps->part.release();
+  eps->st.release();
+  eps->ctl.release();
+  if (eps->h_ctl) {
+    cudaFreeHost(eps->h_ctl);
+    eps->h_ctl = nullptr;
+  }
+  eps->setup = 0;
+  return 0;
+}
+
+extern "C" PetscErrorCode EPSCreate(MPI_Comm, EPS *outeps) {
+  KSG_CHECK(outeps, PETSC_ERR_ARG_NULL, "Null EPS pointer");
+  EPS eps = new _p_EPS();
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) dev = 0;
+  eps->device = dev;
+  *outeps = eps;
+  return 0;
+}
+
+extern "C" PetscErrorCode EPSReset(EPS eps) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  eps_free_device(eps);
+  eps->solved = 0;
+  eps->nconv = 0;
+  return 0;
+}
+
+extern "C" PetscErrorCode EPSDestroy(EPS *eps) {
+  if (!eps || !*eps) return 0;
+  EPS e = *eps;
+  if (e->device >= 0) cudaSetDevice(e->device);
+  eps_free_device(e);
+  for (cudaEvent_t ev : e->ev_pool) cudaEventDestroy(ev);
+  for (cudaEvent_t ev : e->ev_solve)
+    if (ev) cudaEventDestroy(ev);
+  if (e->bv) BVDestroy(&e->bv);
+  if (e->ds) DSDestroy(&e->ds);
+  if (e->stream) cudaStreamDestroy(e->stream);
+  if (e->A) MatDestroy(&e->A);
+  delete e;
+  *eps = nullptr;
+  return 0;
+}
+
+extern "C" PetscErrorCode EPSSetType(EPS eps, EPSType type) {
+  KSG_CHECK(eps && type, PETSC_ERR_ARG_NULL, "Null argument");
+  KSG_CHECK(strcmp(type, EPSKRYLOVSCHUR) == 0, PETSC_ERR_SUP, "Only EPSKRYLOVSCHUR is provided (requested %s)", type);
+  eps->type = type;
+  return 0;
+}
+extern "C" PetscErrorCode EPSGetType(EPS eps, EPSType *type) {
+  KSG_CHECK(eps && type, PETSC_ERR_ARG_NULL, "Null argument");
+  *type = EPSKRYLOVSCHUR;
+  return 0;
+}
+extern "C" PetscErrorCode EPSSetOperators(EPS eps, Mat A, Mat B) {
+  KSG_CHECK(eps && A, PETSC_ERR_ARG_NULL, "Null argument");
+  KSG_CHECK(!B, PETSC_ERR_SUP, "Generalised problems (B != NULL) are not provided");
+  KSG_CHECK(A->m == A->n, PETSC_ERR_ARG_WRONG, "A must be square");
+  A->refs++;
+  if (eps->A) MatDestroy(&eps->A);
+  eps->A = A;
+  eps->setup = 0;
+  eps->solved = 0;
+  return 0;
+}
+extern "C" PetscErrorCode EPSGetOperators(EPS eps, Mat *A, Mat *B) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  if (A) *A = eps->A;
+  if (B) *B = nullptr;
+  return 0;
+}
+extern "C" PetscErrorCode EPSSetProblemType(EPS eps, EPSProblemType type) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  KSG_CHECK(type == EPS_HEP || type == EPS_NHEP, PETSC_ERR_SUP, "Only EPS_HEP and EPS_NHEP are provided");
+  eps->problem = type;
+  eps->setup = 0;
+  eps->solved = 0;
+  return 0;
+}
+extern "C" PetscErrorCode EPSGetProblemType(EPS eps, EPSProblemType *type) {
+  KSG_CHECK(eps && type, PETSC_ERR_ARG_NULL, "Null argument");
+  *type = (EPSProblemType)eps->problem;
+  return 0;
+}
+extern "C" PetscErrorCode EPSSetExtraction(EPS eps, EPSExtraction extr) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  KSG_CHECK(extr == EPS_RITZ, PETSC_ERR_SUP, "Only Ritz extraction is provided");
+  eps->extraction = extr;
+  return 0;
+}
+extern "C" PetscErrorCode EPSSetDimensions(EPS eps, PetscInt nev, PetscInt ncv, PetscInt mpd) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  if (nev != PETSC_CURRENT) {
+    KSG_CHECK(nev > 0, PETSC_ERR_ARG_OUTOFRANGE, "Illegal value of nev. Must be > 0");
+    eps->nev = nev;
+  }
+  if (ncv == PETSC_DETERMINE) eps->ncv = PETSC_DETERMINE;
+  else if (ncv != PETSC_CURRENT) {
+    KSG_CHECK(ncv > 0, PETSC_ERR_ARG_OUTOFRANGE, "Illegal value of ncv. Must be > 0");
+    eps->ncv = ncv;
+  }
+  if (mpd == PETSC_DETERMINE) eps->mpd = PETSC_DETERMINE;
+  else if (mpd != PETSC_CURRENT) {
+    KSG_CHECK(mpd > 0, PETSC_ERR_ARG_OUTOFRANGE, "Illegal value of mpd. Must be > 0");
+    eps->mpd = mpd;
+  }
+  eps->setup = 0;
+  eps->solved = 0;
+  return 0;
+}
+extern "C" PetscErrorCode EPSGetDimensions(EPS eps, PetscInt *nev, PetscInt *ncv, PetscInt *mpd) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  if (nev) *nev = eps->setup ? eps->nev_e : eps->nev;
+  if (ncv) *ncv = eps->setup ? eps->ncv_e : eps->ncv;
+  if (mpd) *mpd = eps->setup ? eps->mpd_e : eps->mpd;
+  return 0;
+}
+extern "C" PetscErrorCode EPSSetTolerances(EPS eps, PetscReal tol, PetscInt maxits) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  if (tol == (PetscReal)PETSC_DETERMINE) eps->tol = PETSC_DETERMINE;
+  else if (tol != (PetscReal)PETSC_CURRENT) {
+    KSG_CHECK(tol > 0.0, PETSC_ERR_ARG_OUTOFRANGE, "Illegal value of tol. Must be > 0");
+    eps->tol = tol;
+  }
+  if (maxits == PETSC_DETERMINE) eps->max_it = PETSC_DETERMINE;
+  else if (maxits == PETSC_UNLIMITED) eps->max_it = 0x7fffffff;
+  else if (maxits != PETSC_CURRENT) {
+    KSG_CHECK(maxits > 0, PETSC_ERR_ARG_OUTOFRANGE, "Illegal value of maxits. Must be > 0");
+    eps->max_it = maxits;
+  }
+  eps->setup = 0;
+  eps->solved = 0;
+  return 0;
+}
+extern "C" PetscErrorCode EPSGetTolerances(EPS eps, PetscReal *tol, PetscInt *maxits) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  if (tol) *tol = eps->setup ? eps->tol_e : eps->tol;
+  if (maxits) *maxits = eps->setup ? eps->maxit_e : eps->max_it;
+  return 0;
+}
+extern "C" PetscErrorCode EPSSetWhichEigenpairs(EPS eps, EPSWhich which) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  KSG_CHECK(which >= EPS_LARGEST_MAGNITUDE && which <= EPS_SMALLEST_IMAGINARY, PETSC_ERR_SUP,
+            "Only EPS_LARGEST/SMALLEST_MAGNITUDE/REAL/IMAGINARY are provided");
+  eps->which = which;
+  eps->solved = 0;
+  return 0;
+}
+extern "C" PetscErrorCode EPSGetWhichEigenpairs(EPS eps, EPSWhich *which) {
+  KSG_CHECK(eps && which, PETSC_ERR_ARG_NULL, "Null argument");
+  *which = (EPSWhich)(eps->which ? eps->which : EPS_LARGEST_MAGNITUDE);
+  return 0;
+}
+extern "C" PetscErrorCode EPSSetInitialSpace(EPS eps, PetscInt n, Vec is[]) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  KSG_CHECK(n >= 0 && n <= 1, PETSC_ERR_SUP, "An initial space of at most one vector is provided");
+  if (n == 0) eps->v0.clear();
+  else {
+    KSG_CHECK(is && is[0], PETSC_ERR_ARG_NULL, "Null initial vector");
+    eps->v0.assign(is[0]->a, is[0]->a + is[0]->n);
+  }
+  eps->solved = 0;
+  return 0;
+}
+extern "C" PetscErrorCode EPSKrylovSchurSetRestart(EPS eps, PetscReal keep) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  if (keep == (PetscReal)PETSC_DETERMINE || keep == (PetscReal)PETSC_DEFAULT) eps->keep = 0.5;
+  else {
+    KSG_CHECK(keep >= 0.1 && keep <= 0.9, PETSC_ERR_ARG_OUTOFRANGE, "The keep argument %g must be in the range [0.1,0.9]", keep);
+    eps->keep = keep;
+  }
+  return 0;
+}
+extern "C" PetscErrorCode EPSKrylovSchurGetRestart(EPS eps, PetscReal *keep) {
+  KSG_CHECK(eps && keep, PETSC_ERR_ARG_NULL, "Null argument");
+  *keep = eps->keep;
+  return 0;
+}
+extern "C" PetscErrorCode EPSKrylovSchurSetLocking(EPS eps, PetscBool lock) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  eps->lock = lock ? 1 : 0;
+  return 0;
+}
+extern "C" PetscErrorCode EPSKrylovSchurGetLocking(EPS eps, PetscBool *lock) {
+  KSG_CHECK(eps && lock, PETSC_ERR_ARG_NULL, "Null argument");
+  *lock = eps->lock ? PETSC_TRUE : PETSC_FALSE;
+  return 0;
+}
+extern "C" PetscErrorCode EPSGB300SetArithmetic(EPS eps, EPSGB300Arith arith) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  KSG_CHECK(arith == EPS_GB300_ARITH_PAIR || arith == EPS_GB300_ARITH_F64, PETSC_ERR_ARG_OUTOFRANGE, "Unknown arithmetic");
+  eps->arith = arith;
+  return 0;
+}
+extern "C" PetscErrorCode EPSGB300GetArithmetic(EPS eps, EPSGB300Arith *arith) {
+  KSG_CHECK(eps && arith, PETSC_ERR_ARG_NULL, "Null argument");
+  *arith = (EPSGB300Arith)eps->arith;
+  return 0;
+}
+extern "C" PetscErrorCode EPSGB300SetDevice(EPS eps, int device) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  int count = 0;
+  KSG_CUDA(cudaGetDeviceCount(&count));
+  KSG_CHECK(device >= 0 && device < count, PETSC_ERR_ARG_OUTOFRANGE, "No CUDA device %d", device);
+  KSG_CHECK(!eps->setup, PETSC_ERR_ORDER, "Set the device before EPSSetUp");
+  eps->device = device;
+  return 0;
+}
+
+// -eps_* options from the argv given to SlepcInitialize (epsopts.c:84-260, krylovschur.c:1440-1475)
+extern "C" PetscErrorCode EPSSetFromOptions(EPS eps) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  for (int i = 1; i < g_argc; ++i) {
+    const char *o = g_argv[i];
+    const char *v = (i + 1 < g_argc) ? g_argv[i + 1] : nullptr;
+    if (!strcmp(o, "-eps_nev") && v) KSG_TRY(EPSSetDimensions(eps, atoi(v), PETSC_CURRENT, PETSC_CURRENT));
+    else if (!strcmp(o, "-eps_ncv") && v) KSG_TRY(EPSSetDimensions(eps, PETSC_CURRENT, atoi(v), PETSC_CURRENT));
+    else if (!strcmp(o, "-eps_mpd") && v) KSG_TRY(EPSSetDimensions(eps, PETSC_CURRENT, PETSC_CURRENT, atoi(v)));
+    else if (!strcmp(o, "-eps_tol") && v) KSG_TRY(EPSSetTolerances(eps, atof(v), PETSC_CURRENT));
+    else if (!strcmp(o, "-eps_max_it") && v) KSG_TRY(EPSSetTolerances(eps, PETSC_CURRENT, atoi(v)));
+    else if (!strcmp(o, "-eps_largest_magnitude")) KSG_TRY(EPSSetWhichEigenpairs(eps, EPS_LARGEST_MAGNITUDE));
+    else if (!strcmp(o, "-eps_smallest_magnitude")) KSG_TRY(EPSSetWhichEigenpairs(eps, EPS_SMALLEST_MAGNITUDE));
+    else if (!strcmp(o, "-eps_largest_real")) KSG_TRY(EPSSetWhichEigenpairs(eps, EPS_LARGEST_REAL));
+    else if (!strcmp(o, "-eps_smallest_real")) KSG_TRY(EPSSetWhichEigenpairs(eps, EPS_SMALLEST_REAL));
+    else if (!strcmp(o, "-eps_largest_imaginary")) KSG_TRY(EPSSetWhichEigenpairs(eps, EPS_LARGEST_IMAGINARY));
+    else if (!strcmp(o, "-eps_smallest_imaginary")) KSG_TRY(EPSSetWhichEigenpairs(eps, EPS_SMALLEST_IMAGINARY));
+    else if (!strcmp(o, "-eps_hermitian")) KSG_TRY(EPSSetProblemType(eps, EPS_HEP));
+    else if (!strcmp(o, "-eps_non_hermitian")) KSG_TRY(EPSSetProblemType(eps, EPS_NHEP));
+    else if (!strcmp(o, "-eps_krylovschur_restart") && v) KSG_TRY(EPSKrylovSchurSetRestart(eps, atof(v)));
+    else if (!strcmp(o, "-eps_krylovschur_locking") && v) KSG_TRY(EPSKrylovSchurSetLocking(eps, atoi(v) ? PETSC_TRUE : PETSC_FALSE));
+    else if (!strcmp(o, "-eps_type") && v) KSG_TRY(EPSSetType(eps, v));
+    else if (!strcmp(o, "-eps_gb300_arith") && v)
+      KSG_TRY(EPSGB300SetArithmetic(eps, !strcmp(v, "f64") ? EPS_GB300_ARITH_F64 : EPS_GB300_ARITH_PAIR));
+  }
+  return 0;
+}
+
+// EPSSetUp (epssetup.c:286-418 with EPSSetUp_KrylovSchur, krylovschur.c:93-194)
+extern "C" PetscErrorCode EPSSetUp(EPS eps) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  if (eps->setup) return 0;
+  auto t0 = std::chrono::steady_clock::now();
+  KSG_CHECK(eps->A, PETSC_ERR_ORDER, "EPSSetOperators must be called first");
+  if (!eps->problem) eps->problem = EPS_NHEP;  // the reference default for a single matrix
+  KSG_CHECK(eps->problem == EPS_HEP || eps->problem == EPS_NHEP, PETSC_ERR_SUP, "Unsupported problem type");
+  const int n = eps->A->m;
+  KSG_CHECK(n > 0, PETSC_ERR_ARG_WRONG, "Empty operator");
+  int nev = eps->nev, ncv = eps->ncv, mpd = eps->mpd;
+  // EPSSetDimensions_Default (epssetup.c:648-671)
+  if (ncv != PETSC_DETERMINE) {
+    KSG_CHECK(ncv >= nev + 1 || (ncv == nev && ncv == n), PETSC_ERR_USER_INPUT, "The value of ncv must be at least nev+1");
+  } else if (mpd != PETSC_DETERMINE) {
+    ncv = std::min(n, nev + mpd);
+  } else {
+    if (nev < 500) ncv = std::min(n, std::max(2 * nev, nev + 15));
+    else {
+      mpd = 500;
+      ncv = std::min(n, nev + mpd);
+    }
+  }
+  if (mpd == PETSC_DETERMINE) mpd = ncv;
+  KSG_CHECK(ncv <= nev + mpd, PETSC_ERR_USER_INPUT, "The value of ncv must not be larger than nev+mpd");
+  KSG_CHECK(ncv < n, PETSC_ERR_SUP, "ncv (%d) must be smaller than the problem size (%d) on this path", ncv, n);
+  KSG_CHECK(ncv + 1 <= 144, PETSC_ERR_SUP, "ncv (%d) above 143 is not provided by the device projected solver", ncv);
+  KSG_CHECK(eps->lock || mpd >= ncv, PETSC_ERR_SUP, "Should not use mpd parameter in non-locking variant");
+  KSG_CHECK(eps->v0.empty() || (int)eps->v0.size() == n, PETSC_ERR_ARG_SIZ, "Initial vector has the wrong length");
+  eps->nev_e = nev;
+  eps->ncv_e = ncv;
+  eps->mpd_e = mpd;
+  eps->maxit_e = (eps->max_it == PETSC_DETERMINE) ? std::max(100, 2 * n / ncv) : eps->max_it;
+  eps->tol_e = (eps->tol == (double)PETSC_DETERMINE) ? 1e-8 : eps->tol;
+  if (!eps->which) eps->which = EPS_LARGEST_MAGNITUDE;
+  eps->n = n;
+  eps->ld = ncv + 1;
+  // the device basis: columns 512-byte aligned
+  eps->ldv = ((long long)n + 63) / 64 * 64;
+  KSG_CUDA(cudaSetDevice(eps->device));
+  if (!eps->stream) KSG_CUDA(cudaStreamCreateWithFlags(&eps->stream, cudaStreamNonBlocking));
+  const int ld = eps->ld;
+  KSG_CUDA(eps->V.alloc((size_t)eps->ldv * (ld + 1)));
+  KSG_CUDA(cudaMemsetAsync(eps->V.p, 0, sizeof(double) * eps->V.count, eps->stream));
+  KSG_CUDA(eps->d.alloc(ld + 1));
+  KSG_CUDA(eps->e.alloc(ld + 1));
+  KSG_CUDA(eps->H.alloc((size_t)(ld + 1) * (ld + 1)));
+  KSG_CUDA(eps->Q.alloc((size_t)ld * ld));
+  KSG_CUDA(eps->X.alloc((size_t)ld * ld));
+  KSG_CUDA(eps->eigr.alloc(ld));
+  KSG_CUDA(eps->eigi.alloc(ld));
+  KSG_CUDA(eps->errest.alloc(ld));
+  KSG_CUDA(eps->coef.alloc(2 * ld + 8));
+  KSG_CUDA(eps->work.alloc(4 * ld + 8));
+  eps->pstride = (int)ksg_part_stride(ld);
+  KSG_CUDA(eps->part.alloc(ksg_part_blocks(n) * eps->pstride));
+  KSG_CUDA(eps->st.alloc(1));
+  KSG_CUDA(eps->ctl.alloc(1));
+  KSG_CUDA(cudaMemsetAsync(eps->st.p, 0, sizeof(KrylovState), eps->stream));
+  KSG_CUDA(cudaMemsetAsync(eps->H.p, 0, sizeof(double) * eps->H.count, eps->stream));
+  KSG_CUDA(cudaMemsetAsync(eps->d.p, 0, sizeof(double) * eps->d.count, eps->stream));
+  KSG_CUDA(cudaMemsetAsync(eps->e.p, 0, sizeof(double) * eps->e.count, eps->stream));
+  if (!eps->h_ctl) KSG_CUDA(cudaMallocHost((void **)&eps->h_ctl, sizeof(KSControl)));
+  KSG_TRY(ksg_mat_upload(eps->A));
+  // power-of-two operator scaling keeps every vector inside the range of the FP32-pair arithmetic; it is exact
+  const double nrm = ksg_mat_norm_inf(eps->A);
+  eps->opscale = 1.0;
+  if (nrm > 0.0 && (nrm > 1048576.0 || nrm < 1.0 / 1048576.0)) eps->opscale = ldexp(1.0, -ilogb(nrm));
+  eps->lanes = spmv_lanes_for((double)eps->A->nnz / n);
+  KSG_CUDA(cudaStreamSynchronize(eps->stream));
+  eps->setup = 1;
+  eps->stats.setup_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  return 0;
+}
+
+// launch bracketing: counts every launch; with profiling on, records an event pair on the EPS stream
+struct LaunchScope {
+  EPS eps;
+  int cls;
+  double bytes;
+  cudaEvent_t e1 = nullptr;
+  LaunchScope(EPS e, int c, double b) : eps(e), cls(c), bytes(b) {
+    eps->stats.kernel_launches++;
+    if (eps->prof) {
+      if (eps->ev_used + 2 > eps->ev_pool.size()) {
+        for (int i = 0; i < 256; ++i) {
+          cudaEvent_t ev;
+          cudaEventCreate(&ev);
+          eps->ev_pool.push_back(ev);
+        }
+      }
+      cudaEvent_t e0 = eps->ev_pool[eps->ev_used];
+      e1 = eps->ev_pool[eps->ev_used + 1];
+      eps->ev_used += 2;
+      cudaEventRecord(e0, eps->stream);
+    }
+  }
+  ~LaunchScope() {
+    if (eps->prof) {
+      cudaEventRecord(e1, eps->stream);
+      eps->ev_cls.push_back({cls, bytes});
+    }
+  }
+};
+
+static void prof_collect(EPS eps) {
+  if (!eps->prof) return;
+  for (size_t i = 0; i < eps->ev_cls.size(); ++i) {
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, eps->ev_pool[2 * i], eps->ev_pool[2 * i + 1]) == cudaSuccess) {
+      eps->prof_ms[eps->ev_cls[i].first] += ms;
+      eps->prof_bytes[eps->ev_cls[i].first] += eps->ev_cls[i].second;
+      eps->prof_launches[eps->ev_cls[i].first] += 1;
+    }
+  }
+  eps->ev_cls.clear();
+  eps->ev_used = 0;
+}
+
+extern "C" PetscErrorCode EPSGB300SetProfiling(EPS eps, PetscBool on) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  eps->prof = on ? 1 : 0;
+  for (int c = 0; c < EPS_GB300_K_COUNT; ++c) {
+    eps->prof_ms[c] = 0.0;
+    eps->prof_bytes[c] = 0.0;
+    eps->prof_launches[c] = 0;
+  }
+  return 0;
+}
+
+extern "C" PetscErrorCode EPSGB300GetProfile(EPS eps, EPSGB300KernelClass cls, double *ms, double *bytes, long long *launches) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  KSG_CHECK(cls >= 0 && cls < EPS_GB300_K_COUNT, PETSC_ERR_ARG_OUTOFRANGE, "Unknown kernel class");
+  if (ms) *ms = eps->prof_ms[cls];
+  if (bytes) *bytes = eps->prof_bytes[cls];
+  if (launches) *launches = eps->prof_launches[cls];
+  return 0;
+}
+
+static double spmv_bytes(EPS eps) {
+  const double n = eps->n, nnz = (double)eps->A->nnz;
+  return nnz * 12.0 + 4.0 * (n + 1) + 16.0 * n;
+}
+
+// one Krylov factorisation segment: steps k0..nv-1 plus the final reorthogonalisation of the residual vector
+static PetscErrorCode eps_factorize(EPS eps, int k0, int nv, double *bytes) {
+  cudaStream_t s = eps->stream;
+  const int n = eps->n;
+  const int herm = eps->problem == EPS_HEP;
+  KSG_CUDA(launch_segment_begin(eps->st.p, k0, nv, s));
+  StepArgs a = {};
+  a.V = eps->V.p;
+  a.ldv = eps->ldv;
+  a.n = n;
+  a.hermitian = herm;
+  a.d = eps->d.p;
+  a.e = eps->e.p;
+  a.H = eps->H.p;
+  a.ldh = eps->ld;
+  a.eta = 0.7071;
+  a.coef = eps->coef.p;
+  a.part = eps->part.p;
+  a.pstride = eps->pstride;
+  a.st = eps->st.p;
+  const double colb = 8.0 * n;
+  for (int j = k0; j < nv; ++j) {
+    double *u = eps->V.p + (size_t)j * eps->ldv;
+    double *w = u + eps->ldv;
+    {
+      LaunchScope ls(eps, EPS_GB300_K_SPMV, spmv_bytes(eps));
+      KSG_CUDA(launch_spmv(eps->A->d_rp.p, eps->A->d_ci.p, eps->A->d_va.p, u, w, n, eps->lanes, eps->st.p,
+                           eps->opscale, s));
+    }
+    a.J = j;
+    a.j = j;
+    a.U = u;
+    a.W = w;
+    {
+      LaunchScope ls(eps, EPS_GB300_K_GS_DOT, colb * (j + 2));
+      KSG_CUDA(launch_gs_dot(a, 2, GS_STEP, eps->arith, s));
+    }
+    {
+      LaunchScope ls(eps, EPS_GB300_K_GS_UPDATE, colb * (j + 4));
+      KSG_CUDA(launch_gs_update(a, 2, GS_STEP, eps->arith, s));
+    }
+    *bytes += spmv_bytes(eps) + colb * (j + 2) + colb * (j + 4);
+  }
+  a.J = nv;
+  a.j = nv;
+  a.U = eps->V.p + (size_t)nv * eps->ldv;
+  a.W = nullptr;
+  {
+    LaunchScope ls(eps, EPS_GB300_K_GS_DOT, colb * (nv + 1));
+    KSG_CUDA(launch_gs_dot(a, 1, GS_FINAL, eps->arith, s));
+  }
+  {
+    LaunchScope ls(eps, EPS_GB300_K_GS_UPDATE, colb * (nv + 2));
+    KSG_CUDA(launch_gs_update(a, 1, GS_FINAL, eps->arith, s));
+  }
+  *bytes += colb * (nv + 1) + colb * (nv + 2);
+  eps->stats.kernel_launches += 1;  // segment begin
+  eps->stats.krylov_steps += nv - k0;
+  return 0;
+}
+
+static PetscErrorCode eps_new_start_vector(EPS eps, int col, int *breakdown) {
+  std::vector<double> h(eps->n);
+  ksg_random_fill(h.data(), eps->n, eps->seed, ++eps->rng_counter);
+  double *dst = eps->V.p + (size_t)col * eps->ldv;
+  KSG_CUDA(cudaMemcpyAsync(dst, h.data(), sizeof(double) * eps->n, cudaMemcpyHostToDevice, eps->stream));
+  double nrm = 0.0;
+  int ld = 0;
+  KSG_TRY(ksg_orthonormalize_column(eps->V.p, eps->ldv, eps->n, col, eps->coef.p, eps->part.p, eps->pstride,
+                                    eps->st.p, eps->arith, eps->stream, &nrm, &ld, 2));
+  *breakdown = ld || nrm == 0.0;
+  return 0;
+}
+
+static int compare_which(int which, double ar, double ai, double br, double bi) {
+  double a, b;
+  switch (which) {
+    case EPS_LARGEST_MAGNITUDE: a = hypot(ar, ai); b = hypot(br, bi); return a < b ? 1 : (a > b ? -1 : 0);
+    case EPS_SMALLEST_MAGNITUDE: a = hypot(ar, ai); b = hypot(br, bi); return a > b ? 1 : (a < b ? -1 : 0);
+    case EPS_LARGEST_REAL: return ar < br ? 1 : (ar > br ? -1 : 0);
+    case EPS_SMALLEST_REAL: return ar > br ? 1 : (ar < br ? -1 : 0);
+    case EPS_LARGEST_IMAGINARY: a = fabs(ai); b = fabs(bi); return a < b ? 1 : (a > b ? -1 : 0);
+    case EPS_SMALLEST_IMAGINARY: a = fabs(ai); b = fabs(bi); return a > b ? 1 : (a < b ? -1 : 0);
+  }
+  return 0;
+}
+
+// SlepcSortEigenvalues (slepcsc.c:89-140): insertion sort keeping conjugate pairs together
+static void sort_eigenvalues(int which, int n, const double *eigr, const double *eigi, int *perm) {
+  for (int i = n - 1; i >= 0; i--) {
+    double re = eigr[perm[i]], im = eigi[perm[i]];
+    int j = i + 1;
+    if (im != 0.0) {
+      i--;
+      im = eigi[perm[i]];
+    }
+    while (j < n) {
+      if (compare_which(which, re, im, eigr[perm[j]], eigi[perm[j]]) <= 0) break;
+      int tmp;
+      if (im == 0.0) {
+        if (eigi[perm[j]] == 0.0) {
+          tmp = perm[j - 1]; perm[j - 1] = perm[j]; perm[j] = tmp; j++;
+        } else {
+          tmp = perm[j - 1]; perm[j - 1] = perm[j]; perm[j] = perm[j + 1]; perm[j + 1] = tmp; j += 2;
+        }
+      } else {
+        if (eigi[perm[j]] == 0.0) {
+          tmp = perm[j - 2]; perm[j - 2] = perm[j]; perm[j] = perm[j - 1]; perm[j - 1] = tmp; j++;
+        } else {
+          tmp = perm[j - 2]; perm[j - 2] = perm[j]; perm[j] = tmp;
+          tmp = perm[j - 1]; perm[j - 1] = perm[j + 1]; perm[j + 1] = tmp; j += 2;
+        }
+      }
+    }
+  }
+}
+
+// EPSSolve (epssolve.c:119-208) with EPSSolve_KrylovSchur_Default (krylovschur.c:227-337) on the device
+extern "C" PetscErrorCode EPSSolve(EPS eps) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  KSG_TRY(EPSSetUp(eps));
+  KSG_CUDA(cudaSetDevice(eps->device));
+  cudaStream_t s = eps->stream;
+  auto t0 = std::chrono::steady_clock::now();
+  if (!eps->ev_solve[0]) {
+    KSG_CUDA(cudaEventCreate(&eps->ev_solve[0]));
+    KSG_CUDA(cudaEventCreate(&eps->ev_solve[1]));
+  }
+  KSG_CUDA(cudaEventRecord(eps->ev_solve[0], s));
+  const int n = eps->n, ld = eps->ld, ncv = eps->ncv_e, mpd = eps->mpd_e, nev = eps->nev_e;
+  const int herm = eps->problem == EPS_HEP;
+  eps->stats.krylov_steps = 0;
+  eps->stats.restarts = 0;
+  eps->stats.bytes_moved = 0.0;
+  eps->stats.kernel_launches = 0;
+  eps->ev_cls.clear();
+  eps->ev_used = 0;
+  eps->solved = 0;
+  // start vector: the initial space, or a random vector (EPSGetStartVector, epssolve.c:841-873)
+  {
+    std::vector<double> h;
+    const double *src;
+    if (!eps->v0.empty()) src = eps->v0.data();
+    else {
+      h.resize(n);
+      ksg_random_fill(h.data(), n, eps->seed, 0);
+      src = h.data();
+    }
+    KSG_CUDA(cudaMemcpyAsync(eps->V.p, src, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    double nrm = 0.0;
+    int lindep = 0;
+    KSG_TRY(ksg_orthonormalize_column(eps->V.p, eps->ldv, n, 0, eps->coef.p, eps->part.p, eps->pstride, eps->st.p,
+                                      eps->arith, s, &nrm, &lindep, 1));
+    KSG_CHECK(!lindep && nrm != 0.0, PETSC_ERR_PLIB, "Initial vector is zero or belongs to the deflation space");
+  }
+  KSG_CUDA(cudaMemsetAsync(eps->d.p, 0, sizeof(double) * eps->d.count, s));
+  KSG_CUDA(cudaMemsetAsync(eps->e.p, 0, sizeof(double) * eps->e.count, s));
+  KSG_CUDA(cudaMemsetAsync(eps->H.p, 0, sizeof(double) * eps->H.count, s));
+  int nconv = 0, l = 0, its = 0, reason = 0;
+  double bytes = 0.0;
+  while (reason == 0) {
+    its++;
+    int nv = std::min(nconv + mpd, ncv);
+    const int k0 = nconv + l;
+    KSG_CHECK(nv > k0, PETSC_ERR_PLIB, "Internal error: empty Krylov segment (nv=%d, k=%d)", nv, k0);
+    KSG_TRY(eps_factorize(eps, k0, nv, &bytes));
+    DSArgs da = {};
+    da.ld = ld;
+    da.n = nv;
+    da.flags = DS_DO_ALL;
+    da.l = nconv;
+    da.k = k0;
+    da.raw = l > 0;
+    da.d = eps->d.p;
+    da.e = eps->e.p;
+    da.H = eps->H.p;
+    da.Q = eps->Q.p;
+    da.eigr = eps->eigr.p;
+    da.eigi = eps->eigi.p;
+    da.errest = eps->errest.p;
+    da.work = eps->work.p;
+    da.which = eps->which;
+    da.tol = eps->tol_e;
+    da.nev = nev;
+    da.its = its;
+    da.max_it = eps->maxit_e;
+    da.keep = eps->keep;
+    da.lock = eps->lock;
+    da.st = eps->st.p;
+    da.ctl = eps->ctl.p;
+    {
+      LaunchScope ls(eps, EPS_GB300_K_DS, 0.0);
+      if (herm) KSG_CUDA(launch_ds_hep(da, ld, s));
+      else KSG_CUDA(launch_ds_nhep(da, ld, s));
+    }
+    KSG_CUDA(cudaMemcpyAsync(eps->h_ctl, eps->ctl.p, sizeof(KSControl), cudaMemcpyDeviceToHost, s));
+    KSG_CUDA(cudaStreamSynchronize(s));
+    prof_collect(eps);
+    const KSControl c = *eps->h_ctl;
+    KSG_CHECK(!c.ds_error, PETSC_ERR_LIB, "The projected eigenproblem solver did not converge (restart %d)", its);
+    const int k = c.nconv;
+    l = c.l;
+    reason = c.reason;
+    nv = c.nv;
+    // thick restart: V(:, nconv:k+l) = V(:, nconv:nv) Q(nconv:nv, nconv:k+l)
+    {
+      LaunchScope ls(eps, EPS_GB300_K_RESTART, 8.0 * n * ((nv - nconv) + (k + l - nconv)));
+      KSG_CUDA(launch_restart(eps->V.p, eps->ldv, n, nconv, nv - nconv, nconv, k + l - nconv, eps->Q.p, ld, eps->arith, s));
+    }
+    bytes += 8.0 * n * ((nv - nconv) + (k + l - nconv));
+    if (reason == 0) {
+      if (c.breakdown || k == nv) {
+        // start a new Krylov factorisation at column k (after the rotation of the converged vectors)
+        if (k < nev) {
+          int bd = 0;
+          KSG_TRY(eps_new_start_vector(eps, k, &bd));
+          if (bd) reason = EPS_DIVERGED_BREAKDOWN;
+        }
+      } else {
+        KSG_CUDA(cudaMemcpyAsync(eps->V.p + (size_t)(k + l) * eps->ldv, eps->V.p + (size_t)nv * eps->ldv,
+                                 sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+      }
+    }
+    nconv = k;
+    eps->stats.restarts++;
+  }
+  // non-Hermitian: eigenvectors of the leading Schur block, V = V X (EPSComputeVectors_Schur, epsdefault.c:105-169)
+  if (!herm && nconv > 0) {
+    KSG_CUDA(launch_nhep_vectors(eps->H.p, ld, nconv, eps->X.p, s));
+    KSG_CUDA(launch_restart(eps->V.p, eps->ldv, n, 0, nconv, 0, nconv, eps->X.p, ld, eps->arith, s));
+    bytes += 16.0 * n * nconv;
+  }
+  std::vector<double> er(ld), ei(ld), es(ld);
+  KSG_CUDA(cudaMemcpyAsync(er.data(), eps->eigr.p, sizeof(double) * ld, cudaMemcpyDeviceToHost, s));
+  KSG_CUDA(cudaMemcpyAsync(ei.data(), eps->eigi.p, sizeof(double) * ld, cudaMemcpyDeviceToHost, s));
+  KSG_CUDA(cudaMemcpyAsync(es.data(), eps->errest.p, sizeof(double) * ld, cudaMemcpyDeviceToHost, s));
+  KSG_CUDA(cudaStreamSynchronize(s));
+  // undo the operator scaling and order the results (epssolve.c:159-178)
+  eps->r_eigr.assign(er.begin(), er.begin() + nconv);
+  eps->r_eigi.assign(ei.begin(), ei.begin() + nconv);
+  eps->r_errest.assign(es.begin(), es.begin() + nconv);
+  if (herm) std::fill(eps->r_eigi.begin(), eps->r_eigi.end(), 0.0);
+  for (int i = 0; i < nconv; ++i) {
+    eps->r_eigr[i] /= eps->opscale;
+    eps->r_eigi[i] /= eps->opscale;
+  }
+  for (int i = 0; i < nconv - 1; ++i) {
+    if (eps->r_eigi[i] != 0.0) {
+      if (eps->r_eigi[i] < 0.0) {
+        eps->r_eigi[i] = -eps->r_eigi[i];
+        eps->r_eigi[i + 1] = -eps->r_eigi[i + 1];
+        KSG_CUDA(launch_scale(eps->V.p + (size_t)(i + 1) * eps->ldv, n, -1.0, s));
+      }
+      i++;
+    }
+  }
+  eps->perm.resize(std::max(nconv, 1));
+  for (int i = 0; i < nconv; ++i) eps->perm[i] = i;
+  sort_eigenvalues(eps->which, nconv, eps->r_eigr.data(), eps->r_eigi.data(), eps->perm.data());
+  KSG_CUDA(cudaEventRecord(eps->ev_solve[1], s));
+  KSG_CUDA(cudaStreamSynchronize(s));
+  {
+    float ms = 0.0f;
+    KSG_CUDA(cudaEventElapsedTime(&ms, eps->ev_solve[0], eps->ev_solve[1]));
+    eps->stats.solve_device_ms = ms;
+  }
+  prof_collect(eps);
+  eps->nconv = nconv;
+  eps->its = its;
+  eps->reason = reason;
+  eps->solved = 1;
+  eps->stats.bytes_moved = bytes;
+  eps->stats.solve_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  return 0;
+}
+
+extern "C" PetscErrorCode EPSGetConverged(EPS eps, PetscInt *nconv) {
+  KSG_CHECK(eps && nconv, PETSC_ERR_ARG_NULL, "Null argument");
+  KSG_CHECK(eps->solved, PETSC_ERR_ORDER, "Must call EPSSolve() first");
+  *nconv = eps->nconv;
+  return 0;
+}
+extern "C" PetscErrorCode EPSGetConvergedReason(EPS eps, EPSConvergedReason *reason) {
+  KSG_CHECK(eps && reason, PETSC_ERR_ARG_NULL, "Null argument");
+  KSG_CHECK(eps->solved, PETSC_ERR_ORDER, "Must call EPSSolve() first");
+  *reason = (EPSConvergedReason)eps->reason;
+  return 0;
+}
+extern "C" PetscErrorCode EPSGetIterationNumber(EPS eps, PetscInt *its) {
+  KSG_CHECK(eps && its, PETSC_ERR_ARG_NULL, "Null argument");
+  *its = eps->its;
+  return 0;
+}
+extern "C" PetscErrorCode EPSGetEigenvalue(EPS eps, PetscInt i, PetscScalar *eigr, PetscScalar *eigi) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  KSG_CHECK(eps->solved, PETSC_ERR_ORDER, "Must call EPSSolve() first");
+  KSG_CHECK(i >= 0, PETSC_ERR_ARG_OUTOFRANGE, "The index cannot be negative");
+  KSG_CHECK(i < eps->nconv, PETSC_ERR_ARG_OUTOFRANGE, "The index can be nconv-1 at most, see EPSGetConverged()");
+  const int k = eps->perm[i];
+  if (eigr) *eigr = eps->r_eigr[k];
+  if (eigi) *eigi = eps->r_eigi[k];
+  return 0;
+}
+// BV_GetEigenvector (bvimpl.h:421-444)
+extern "C" PetscErrorCode EPSGetEigenvector(EPS eps, PetscInt i, Vec Vr, Vec Vi) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  KSG_CHECK(eps->solved, PETSC_ERR_ORDER, "Must call EPSSolve() first");
+  KSG_CHECK(i >= 0 && i < eps->nconv, PETSC_ERR_ARG_OUTOFRANGE, "Index out of range");
+  const int n = eps->n;
+  KSG_CHECK((!Vr || Vr->n == n) && (!Vi || Vi->n == n), PETSC_ERR_ARG_SIZ, "Vector of the wrong size");
+  const int k = eps->perm[i];
+  const double ei = eps->r_eigi[k];
+  const double *col = eps->V.p + (size_t)k * eps->ldv;
+  const size_t bytes = sizeof(double) * n;
+  if (ei > 0.0) {
+    if (Vr) KSG_CUDA(cudaMemcpy(Vr->a, col, bytes, cudaMemcpyDeviceToHost));
+    if (Vi) KSG_CUDA(cudaMemcpy(Vi->a, col + eps->ldv, bytes, cudaMemcpyDeviceToHost));
+  } else if (ei < 0.0) {
+    if (Vr) KSG_CUDA(cudaMemcpy(Vr->a, col - eps->ldv, bytes, cudaMemcpyDeviceToHost));
+    if (Vi) {
+      KSG_CUDA(cudaMemcpy(Vi->a, col, bytes, cudaMemcpyDeviceToHost));
+      for (int r = 0; r < n; ++r) Vi->a[r] = -Vi->a[r];
+    }
+  } else {
+    if (Vr) KSG_CUDA(cudaMemcpy(Vr->a, col, bytes, cudaMemcpyDeviceToHost));
+    if (Vi) memset(Vi->a, 0, bytes);
+  }
+  return 0;
+}
+extern "C" PetscErrorCode EPSGetEigenpair(EPS eps, PetscInt i, PetscScalar *eigr, PetscScalar *eigi, Vec Vr, Vec Vi) {
+  KSG_TRY(EPSGetEigenvalue(eps, i, eigr, eigi));
+  if (Vr || Vi) KSG_TRY(EPSGetEigenvector(eps, i, Vr, Vi));
+  return 0;
+}
+extern "C" PetscErrorCode EPSGetErrorEstimate(EPS eps, PetscInt i, PetscReal *errest) {
+  KSG_CHECK(eps && errest, PETSC_ERR_ARG_NULL, "Null argument");
+  KSG_CHECK(eps->solved, PETSC_ERR_ORDER, "Must call EPSSolve() first");
+  KSG_CHECK(i >= 0 && i < eps->nconv, PETSC_ERR_ARG_OUTOFRANGE, "Index out of range");
+  *errest = eps->r_errest[eps->perm[i]];
+  return 0;
+}
+
+// residual norms on the device: sums of (y - kr x + ki xi)^2 and (yi - kr xi - ki x)^2, FP64
+__global__ void k_residual(const double *y, const double *yi, const double *x, const double *xi, double kr, double ki,
+                           int n, double *part) {
+  __shared__ double s0[256], s1[256];
+  double a0 = 0.0, a1 = 0.0;
+  for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long long)gridDim.x * blockDim.x) {
+    double u = y[r] - kr * x[r] + (xi ? ki * xi[r] : 0.0);
+    a0 = fma(u, u, a0);
+    if (yi) {
+      double v = yi[r] - kr * xi[r] - ki * x[r];
+      a1 = fma(v, v, a1);
+    }
+  }
+  s0[threadIdx.x] = a0;
+  s1[threadIdx.x] = a1;
+  __syncthreads();
+  for (int off = 128; off > 0; off >>= 1) {
+    if (threadIdx.x < off) {
+      s0[threadIdx.x] += s0[threadIdx.x + off];
+      s1[threadIdx.x] += s1[threadIdx.x + off];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = s0[0];
+    part[2 * blockIdx.x + 1] = s1[0];
+  }
+}
+
+// EPSComputeError / EPSComputeResidualNorm_Private (epssolve.c:666-815)
+extern "C" PetscErrorCode EPSComputeError(EPS eps, PetscInt i, EPSErrorType type, PetscReal *error) {
+  KSG_CHECK(eps && error, PETSC_ERR_ARG_NULL, "Null argument");
+  KSG_CHECK(eps->solved, PETSC_ERR_ORDER, "Must call EPSSolve() first");
+  KSG_CHECK(i >= 0 && i < eps->nconv, PETSC_ERR_ARG_OUTOFRANGE, "Index out of range");
+  const int n = eps->n;
+  const int k = eps->perm[i];
+  double kr = eps->r_eigr[k], ki = eps->r_eigi[k];
+  const double *x = eps->V.p + (size_t)k * eps->ldv;
+  const double *xi = nullptr;
+  if (ki > 0.0) xi = x + eps->ldv;
+  else if (ki < 0.0) {
+    xi = x;
+    x = x - eps->ldv;
+    ki = -ki;  // the stored pair is (x, xi) for the eigenvalue with positive imaginary part
+  }
+  DBuf<double> y, yi, part;
+  const int blocks = std::min(1024, (n + 255) / 256);
+  KSG_CUDA(y.alloc(n));
+  if (xi) KSG_CUDA(yi.alloc(n));
+  KSG_CUDA(part.alloc(2 * blocks));
+  cudaStream_t s = eps->stream;
+  KSG_CUDA(launch_spmv(eps->A->d_rp.p, eps->A->d_ci.p, eps->A->d_va.p, x, y.p, n, eps->lanes, nullptr, 1.0, s));
+  if (xi) KSG_CUDA(launch_spmv(eps->A->d_rp.p, eps->A->d_ci.p, eps->A->d_va.p, xi, yi.p, n, eps->lanes, nullptr, 1.0, s));
+  k_residual<<<blocks, 256, 0, s>>>(y.p, xi ? yi.p : nullptr, x, xi, kr, ki, n, part.p);
+  KSG_CUDA(cudaGetLastError());
+  std::vector<double> h(2 * blocks);
+  KSG_CUDA(cudaMemcpyAsync(h.data(), part.p, sizeof(double) * 2 * blocks, cudaMemcpyDeviceToHost, s));
+  KSG_CUDA(cudaStreamSynchronize(s));
+  double s0 = 0.0, s1 = 0.0;
+  for (int b = 0; b < blocks; ++b) {
+    s0 += h[2 * b];
+    s1 += h[2 * b + 1];
+  }
+  double nrm = xi ? hypot(sqrt(s0), sqrt(s1)) : sqrt(s0);
+  const double lam = hypot(kr, ki);
+  switch (type) {
+    case EPS_ERROR_ABSOLUTE: break;
+    case EPS_ERROR_RELATIVE: nrm /= lam; break;
+    case EPS_ERROR_BACKWARD: nrm /= (ksg_mat_norm_inf(eps->A) + lam); break;
+    default: return ksg_set_error(PETSC_ERR_ARG_OUTOFRANGE, "Invalid error type");
+  }
+  *error = nrm;
+  return 0;
+}
+
+extern "C" PetscErrorCode EPSGB300GetStats(EPS eps, EPSGB300Stats *stats) {
+  KSG_CHECK(eps && stats, PETSC_ERR_ARG_NULL, "Null argument");
+  *stats = eps->stats;
+  return 0;
+}
+
+extern "C" PetscErrorCode EPSGB300GetDeviceBasis(EPS eps, const double **V, PetscInt *ld) {
+  KSG_CHECK(eps && V && ld, PETSC_ERR_ARG_NULL, "Null argument");
+  KSG_CHECK(eps->setup, PETSC_ERR_ORDER, "Must call EPSSetUp() first");
+  *V = eps->V.p;
+  *ld = (PetscInt)eps->ldv;
+  return 0;
+}
+
+// ||V^T V - I||_max over the first nconv columns (solver order), with the GS_DOTS kernel in the EPS arithmetic
+extern "C" PetscErrorCode EPSGB300OrthogonalityError(EPS eps, PetscReal *err) {
+  KSG_CHECK(eps && err, PETSC_ERR_ARG_NULL, "Null argument");
+  KSG_CHECK(eps->solved, PETSC_ERR_ORDER, "Must call EPSSolve() first");
+  const int m = eps->nconv;
+  double worst = 0.0;
+  StepArgs a = {};
+  a.V = eps->V.p;
+  a.ldv = eps->ldv;
+  a.n = eps->n;
+  a.coef = eps->coef.p;
+  a.part = eps->part.p;
+  a.pstride = eps->pstride;
+  a.st = eps->st.p;
+  a.eta = 0.7071;
+  std::vector<double> h(eps->ld + 1);
+  for (int j = 0; j < m; ++j) {
+    KSG_CUDA(launch_segment_begin(eps->st.p, 0, 0, eps->stream));
+    a.J = j;
+    a.j = j;
+    a.U = eps->V.p + (size_t)j * eps->ldv;
+    KSG_CUDA(launch_gs_dot(a, 1, GS_DOTS, ARITH_F64, eps->stream));
+    KSG_CUDA(cudaMemcpyAsync(h.data(), eps->coef.p, sizeof(double) * (j + 1), cudaMemcpyDeviceToHost, eps->stream));
+    KSG_CUDA(cudaStreamSynchronize(eps->stream));
+    for (int i = 0; i < j; ++i) worst = std::max(worst, fabs(h[i]));
+    worst = std::max(worst, fabs(h[j] - 1.0));
+  }
+  *err = worst;
+  return 0;
+}

@@ -1,0 +1,147 @@
+// internal.h -- object layouts and helpers shared by the C-API translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "kernels.h"
+#include "ks_types.h"
+#include "../../include/slepc_gb300.h"
+
+// ---------------------------------------------------------------------------------------------------------------
+// error handling: every entry point returns a PETSc error code and records a message for PetscGB300LastError()
+// ---------------------------------------------------------------------------------------------------------------
+PetscErrorCode ksg_set_error(PetscErrorCode code, const char *fmt, ...);
+
+#define KSG_CHECK(cond, code, ...)                                     \
+  do {                                                                 \
+    if (!(cond)) return ksg_set_error((code), __VA_ARGS__);            \
+  } while (0)
+
+#define KSG_CUDA(call)                                                                                     \
+  do {                                                                                                     \
+    cudaError_t e_ = (call);                                                                               \
+    if (e_ != cudaSuccess)                                                                                 \
+      return ksg_set_error(e_ == cudaErrorMemoryAllocation ? PETSC_ERR_GPU_RESOURCE : PETSC_ERR_GPU,       \
+                           "CUDA error %s at %s:%d: %s", cudaGetErrorName(e_), __FILE__, __LINE__,         \
+                           cudaGetErrorString(e_));                                                         \
+  } while (0)
+
+#define KSG_TRY(call)                          \
+  do {                                         \
+    PetscErrorCode ierr_ = (call);             \
+    if (ierr_) return ierr_;                   \
+  } while (0)
+
+// device buffer with RAII release
+template <class T>
+struct DBuf {
+  T *p = nullptr;
+  size_t count = 0;
+  cudaError_t alloc(size_t n) {
+    release();
+    if (n == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc((void **)&p, n * sizeof(T));
+    if (e == cudaSuccess) count = n;
+    else p = nullptr;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    count = 0;
+  }
+  ~DBuf() { release(); }
+};
+
+struct _p_Mat {
+  int m = 0, n = 0;
+  int dense = 0;
+  // AIJ (caller-owned arrays)
+  const PetscInt *ai = nullptr, *aj = nullptr;
+  const PetscScalar *aa = nullptr;
+  long long nnz = 0;
+  // dense
+  std::vector<double> dbuf;
+  double *data = nullptr;
+  int lda = 0;
+  int refs = 1;
+  // device copy of the CSR arrays (uploaded on first use by a solver)
+  DBuf<int> d_rp, d_ci;
+  DBuf<double> d_va;
+  int device_ready = 0;
+  double norm_inf = -1.0;
+};
+
+struct _p_Vec {
+  int n = 0;
+  std::vector<double> own;
+  double *a = nullptr;
+};
+
+// device helpers used by more than one object
+PetscErrorCode ksg_mat_upload(Mat A);
+double ksg_mat_norm_inf(Mat A);
+PetscErrorCode ksg_random_fill(double *host, int n, unsigned long long seed, unsigned long long stream_index);
+
+struct _p_DS;
+struct _p_BV;
+
+struct _p_EPS {
+  // configuration
+  Mat A = nullptr;
+  int problem = 0;  // EPSProblemType
+  std::string type = "krylovschur";
+  int which = 0;
+  int nev = 1, ncv = PETSC_DETERMINE, mpd = PETSC_DETERMINE;
+  double tol = PETSC_DETERMINE;
+  int max_it = PETSC_DETERMINE;
+  double keep = 0.5;
+  int lock = 1;
+  int extraction = 0;
+  int arith = ksg::ARITH_PAIR;
+  int device = -1;
+  std::vector<double> v0;
+  unsigned long long seed = 0x5EEDULL;
+  unsigned long long rng_counter = 0;
+  // state
+  int setup = 0, solved = 0;
+  int n = 0, ncv_e = 0, mpd_e = 0, maxit_e = 0, nev_e = 0, ld = 0;
+  double tol_e = 1e-8;
+  double opscale = 1.0;
+  int lanes = 8;
+  long long ldv = 0;
+  cudaStream_t stream = nullptr;
+  DBuf<double> V, d, e, H, Q, X, eigr, eigi, errest, coef, work;
+  DBuf<float2> part;
+  int pstride = 0;
+  DBuf<ksg::KrylovState> st;
+  DBuf<ksg::KSControl> ctl;
+  ksg::KSControl *h_ctl = nullptr;  // pinned
+  cudaEvent_t ev_solve[2] = {nullptr, nullptr};
+  // results
+  int nconv = 0, its = 0, reason = 0;
+  std::vector<double> r_eigr, r_eigi, r_errest;
+  std::vector<int> perm;
+  EPSGB300Stats stats = {};
+  // profiling: event pairs per launch, per kernel class
+  int prof = 0;
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_used = 0;
+  std::vector<std::pair<int, double>> ev_cls;  // class and bytes of each recorded pair
+  double prof_ms[EPS_GB300_K_COUNT] = {0};
+  double prof_bytes[EPS_GB300_K_COUNT] = {0};
+  long long prof_launches[EPS_GB300_K_COUNT] = {0};
+  BV bv = nullptr;
+  DS ds = nullptr;
+};
+
+// run the Gram-Schmidt pair kernels on one column (orthonormalise u = V[:, j] against V[:, 0:j]); returns the
+// norm of the orthogonalised vector in *nrm and the linear-dependence flag (two CGS passes)
+PetscErrorCode ksg_orthonormalize_column(double *V, long long ldv, int n, int j, double *coef, float2 *part,
+                                         int pstride, ksg::KrylovState *st, int arith, cudaStream_t s, double *nrm,
+                                         int *lindep, int refine);
+size_t ksg_part_stride(int ld);
+size_t ksg_part_blocks(int n);

@@ -1,0 +1,311 @@
+// k_ds_hep.cu -- projected problem of the symmetric Krylov-Schur iteration, solved on the device in FP64.
+//
+// One thread block per projected problem.  Follows DSSolve_HEP_QR (src/sys/classes/ds/impls/hep/dshep.c:383-426):
+// the arrowhead block left by the previous restart is reduced to tridiagonal form by Givens rotations chased to
+// the top-left corner (DSArrowTridiag, dshep.c:221-262), then the tridiagonal problem is solved by implicit QL
+// with Wilkinson shifts (the algorithm LAPACK's steqr implements), the eigenvalues are sorted ascending and then
+// by the requested criterion (DSSort_HEP, dshep.c:323-347 with dspriv.c:226-245), the extra row
+// b = beta * Q(n-1, :) is formed (DSUpdateExtraRow_HEP, dshep.c:349-381), and the convergence test, stopping
+// test and restart sizes of EPSSolve_KrylovSchur_Default (krylovschur.c:270-322, epskrylov.c:207-295,
+// epsdefault.c:224-232,290-302) are evaluated so the host reads only a small control record.
+//
+// The rotation sequences are computed by one thread and applied to the rows of Q by all threads; Q lives in
+// shared memory (n <= 144).
+#include <float.h>
+
+#include "common.cuh"
+#include "kernels.h"
+#include "ks_types.h"
+
+namespace ksg {
+
+constexpr int DS_THREADS = 256;
+constexpr int DS_MAXN = 144;
+
+KS_DEVICE void ds_givens(double f, double g, double &c, double &s, double &r) {
+  if (g == 0.0) {
+    c = 1.0; s = 0.0; r = f;
+  } else if (f == 0.0) {
+    c = 0.0; s = copysign(1.0, g); r = fabs(g);
+  } else {
+    const double d = hypot(f, g);
+    c = fabs(f) / d;
+    r = copysign(d, f);
+    s = g / r;
+  }
+}
+
+// criterion comparison (slepcsc.c): -1 if a goes first, 1 if b goes first, 0 if tied
+KS_DEVICE int ds_compare(int which, double ar, double ai, double br, double bi) {
+  double a, b;
+  switch (which) {
+    case 1: a = hypot(ar, ai); b = hypot(br, bi); return a < b ? 1 : (a > b ? -1 : 0);
+    case 2: a = hypot(ar, ai); b = hypot(br, bi); return a > b ? 1 : (a < b ? -1 : 0);
+    case 3: return ar < br ? 1 : (ar > br ? -1 : 0);
+    case 4: return ar > br ? 1 : (ar < br ? -1 : 0);
+    case 5: a = fabs(ai); b = fabs(bi); return a < b ? 1 : (a > b ? -1 : 0);
+    case 6: a = fabs(ai); b = fabs(bi); return a > b ? 1 : (a < b ? -1 : 0);
+    default: return 0;
+  }
+}
+
+__global__ void __launch_bounds__(DS_THREADS, 1) k_ds_hep(DSArgs a) {
+  extern __shared__ double Qs[];  // n x n, column-major with leading dimension n
+  __shared__ double sd[DS_MAXN], se[DS_MAXN], rc[DS_MAXN], rs[DS_MAXN], serr[DS_MAXN];
+  __shared__ int sperm[DS_MAXN], sw_a[DS_MAXN], sw_b[DS_MAXN];
+  __shared__ int s_cmd, s_lo, s_hi, s_nsw, s_fail;
+  __shared__ double s_beta_e;
+  const int tid = threadIdx.x;
+  const KrylovState *st = a.st;
+  const int n = st ? st->m : a.n;  // actual size of the factorisation
+  const int flags = a.flags;
+  const int l = a.l, k = a.k;
+  const int nq = n;
+  for (int i = tid; i < n; i += DS_THREADS) {
+    sd[i] = a.d[i];
+    se[i] = a.e[i];
+  }
+  if (flags & DS_DO_SOLVE) {
+    for (int i = tid; i < n * n; i += DS_THREADS) Qs[i] = ((i % n) == (i / n)) ? 1.0 : 0.0;
+  } else {
+    for (int i = tid; i < n * n; i += DS_THREADS) Qs[i] = a.Q[(i % n) + (size_t)(i / n) * a.ld];
+  }
+  if (tid == 0) s_fail = 0;
+  __syncthreads();
+  if (tid == 0) s_beta_e = se[n - 1];
+  // ---- arrowhead -> tridiagonal on the block [l, k] ----
+  const int n1 = ((flags & DS_DO_SOLVE) && a.raw && k - l + 1 > 0) ? k - l + 1 : 0;
+  for (int j = 0; j < n1 - 2; ++j) {
+    if (tid == 0) {
+      double *d = sd + l, *e = se + l;
+      double c, s, r;
+      ds_givens(e[j + 1], e[j], c, s, r);
+      e[j + 1] = r;
+      s = -s;
+      const double dj = d[j], dj1 = d[j + 1];
+      e[j] = c * s * (dj1 - dj);
+      d[j + 1] = s * s * dj + c * c * dj1;
+      d[j] = c * c * dj + s * s * dj1;
+      rc[0] = c;
+      rs[0] = s;
+      int t = 1;
+      for (int i = j - 1; i >= 0; --i, ++t) {
+        const double off = -s * e[i];
+        e[i] = c * e[i];
+        ds_givens(e[i + 1], off, c, s, r);
+        e[i + 1] = r;
+        s = -s;
+        const double tt = (d[i] - d[i + 1]) * s - 2.0 * c * e[i];
+        const double p = s * tt;
+        d[i + 1] += p;
+        d[i] -= p;
+        e[i] = -e[i] - c * tt;
+        rc[t] = c;
+        rs[t] = s;
+      }
+    }
+    __syncthreads();
+    // rows 0..j+1 of the block; rotation t acts on block columns (j - t + 1 ... ) : t = 0 -> (j, j+1), t >= 1 -> (j-t, j-t+1)
+    for (int r = tid; r < j + 2; r += DS_THREADS) {
+      double *row = Qs + (l + r);
+      for (int t = 0; t <= j; ++t) {
+        const int p = (t == 0) ? j : j - t;
+        const double c = rc[t], s = rs[t];
+        double *x = row + (size_t)(l + p) * n, *y = row + (size_t)(l + p + 1) * n;
+        const double xv = *x, yv = *y;
+        *x = c * xv + s * yv;
+        *y = c * yv - s * xv;
+      }
+    }
+    __syncthreads();
+  }
+  // ---- implicit QL on [l, n) ----
+  {
+    // thread 0 drives; other threads apply the recorded sweeps
+    int ll = 0, total = 0;       // thread 0 state (block-relative indices)
+    const int m_blk = (flags & DS_DO_SOLVE) ? n - l : 0;
+    double *d = sd + l, *e = se + l;
+    if (tid == 0 && m_blk > 0) e[m_blk - 1] = 0.0;
+    for (;;) {
+      if (tid == 0) {
+        s_cmd = 0;
+        while (ll < m_blk) {
+          int m;
+          for (m = ll; m < m_blk - 1; ++m) {
+            const double dd = fabs(d[m]) + fabs(d[m + 1]);
+            if (fabs(e[m]) <= DBL_EPSILON * dd) break;
+          }
+          if (m == ll) { ++ll; continue; }
+          if (++total > 30 * m_blk) { s_fail = 1; break; }
+          double g = (d[ll + 1] - d[ll]) / (2.0 * e[ll]);
+          double r = hypot(g, 1.0);
+          g = d[m] - d[ll] + e[ll] / (g + copysign(r, g));
+          double s = 1.0, c = 1.0, p = 0.0;
+          int i;
+          int under = 0;
+          for (i = m - 1; i >= ll; --i) {
+            const double f = s * e[i], b = c * e[i];
+            r = hypot(f, g);
+            e[i + 1] = r;
+            if (r == 0.0) { d[i + 1] -= p; e[m] = 0.0; under = 1; break; }
+            s = f / r;
+            c = g / r;
+            g = d[i + 1] - p;
+            r = (d[i] - g) * s + 2.0 * c * b;
+            p = s * r;
+            d[i + 1] = g + p;
+            g = c * r - b;
+            rc[i] = c;
+            rs[i] = s;
+          }
+          if (!under) {
+            d[ll] -= p;
+            e[ll] = g;
+            e[m] = 0.0;
+          }
+          s_lo = under ? i + 1 : ll;
+          s_hi = m;  // rotations i = s_hi-1 down to s_lo
+          s_cmd = 1;
+          break;
+        }
+      }
+      __syncthreads();
+      if (s_cmd == 0) break;
+      const int lo = s_lo, hi = s_hi;
+      for (int r = tid; r < nq; r += DS_THREADS) {
+        double *row = Qs + r;
+        for (int i = hi - 1; i >= lo; --i) {
+          const double c = rc[i], s = rs[i];
+          double *qi = row + (size_t)(l + i) * n, *qi1 = row + (size_t)(l + i + 1) * n;
+          const double t = *qi1;
+          *qi1 = s * (*qi) + c * t;
+          *qi = c * (*qi) - s * t;
+        }
+      }
+      __syncthreads();
+    }
+    // the last off-diagonal slot holds the extra-row scalar beta, which steqr never touches
+    if (tid == 0 && m_blk > 0) e[m_blk - 1] = s_beta_e;
+  }
+  // ---- ascending order (steqr) then sort by criterion (DSSort_HEP): one permutation, applied as swaps ----
+  if (tid == 0) {
+    const int m_blk = (flags & DS_DO_SOLVE) ? n - l : 0;
+    for (int i = 0; i < n; ++i) sperm[i] = i;
+    // ascending selection sort on the block
+    for (int i = 0; i < m_blk - 1; ++i) {
+      int kk = i;
+      double p = sd[l + i];
+      for (int j = i + 1; j < m_blk; ++j)
+        if (sd[l + j] < p) { kk = j; p = sd[l + j]; }
+      if (kk != i) {
+        sd[l + kk] = sd[l + i];
+        sd[l + i] = p;
+        const int t = sperm[l + i]; sperm[l + i] = sperm[l + kk]; sperm[l + kk] = t;
+      }
+    }
+    // insertion sort by criterion on indices (dspriv.c:226-245), over positions [l, n)
+    int perm2[DS_MAXN];
+    for (int i = 0; i < n; ++i) perm2[i] = i;
+    for (int i = l + 1; i < ((flags & DS_DO_SORT) ? n : 0); ++i) {
+      const double re = sd[perm2[i]];
+      int j = i - 1;
+      int res = ds_compare(a.which, re, 0.0, sd[perm2[j]], 0.0);
+      while (res < 0 && j >= l) {
+        const int t = perm2[j]; perm2[j] = perm2[j + 1]; perm2[j + 1] = t;
+        --j;
+        if (j >= l) res = ds_compare(a.which, re, 0.0, sd[perm2[j]], 0.0);
+      }
+    }
+    // composite: final column i = original column sperm[perm2[i]]
+    double dtmp[DS_MAXN];
+    int comp[DS_MAXN];
+    for (int i = 0; i < n; ++i) { comp[i] = sperm[perm2[i]]; dtmp[i] = sd[perm2[i]]; }
+    for (int i = 0; i < n; ++i) sd[i] = dtmp[i];
+    // realise comp as a swap sequence on columns: position i must receive original column comp[i]
+    int where[DS_MAXN], at[DS_MAXN];  // where[c]: current position of original column c; at[p]: column at p
+    for (int i = 0; i < n; ++i) { where[i] = i; at[i] = i; }
+    int nsw = 0;
+    for (int i = 0; i < n; ++i) {
+      const int c = comp[i];
+      const int p = where[c];
+      if (p != i) {
+        sw_a[nsw] = i;
+        sw_b[nsw] = p;
+        ++nsw;
+        const int ci = at[i];
+        at[i] = c; where[c] = i;
+        at[p] = ci; where[ci] = p;
+      }
+    }
+    s_nsw = nsw;
+  }
+  __syncthreads();
+  for (int r = tid; r < nq; r += DS_THREADS) {
+    for (int t = 0; t < s_nsw; ++t) {
+      double *x = Qs + r + (size_t)sw_a[t] * n, *y = Qs + r + (size_t)sw_b[t] * n;
+      const double v = *x;
+      *x = *y;
+      *y = v;
+    }
+  }
+  __syncthreads();
+  // ---- extra row, convergence estimates ----
+  const double beta = st ? st->beta_out : 0.0;
+  const double beta_e = s_beta_e;
+  for (int i = tid; i < n; i += DS_THREADS) {
+    const double qlast = Qs[(n - 1) + (size_t)i * n];
+    if (flags & DS_DO_EXTRAROW) se[i] = beta_e * qlast;
+    else if ((flags & DS_DO_SOLVE) && i < n - 1) se[i] = 0.0;
+    const double w = fabs(sd[i]);
+    serr[i] = (w != 0.0) ? fabs(qlast) * beta / w : DBL_MAX;
+  }
+  __syncthreads();
+  // ---- write back ----
+  for (int i = tid; i < n; i += DS_THREADS) {
+    a.d[i] = sd[i];
+    a.e[i] = se[i];
+    a.eigr[i] = sd[i];
+    if (a.eigi) a.eigi[i] = 0.0;
+  }
+  for (int i = tid; i < n * n; i += DS_THREADS) a.Q[(i % n) + (size_t)(i / n) * a.ld] = Qs[i];
+  if (tid == 0 && (flags & DS_DO_CONTROL)) {
+    // EPSKrylovConvergence: first index from nconv whose estimate fails
+    int kk;
+    for (kk = l; kk < n; ++kk) {
+      a.errest[kk] = serr[kk];
+      if (serr[kk] >= a.tol) break;
+    }
+    for (int i = kk + 1; i < n; ++i) a.errest[i] = serr[i];
+    KSControl *ctl = a.ctl;
+    int reason = 0;
+    if (kk >= a.nev) reason = 1;
+    else if (a.its >= a.max_it) reason = -1;
+    const int breakdown = st->breakdown;
+    int lkeep;
+    if (reason != 0 || breakdown || kk == n) lkeep = 0;
+    else {
+      lkeep = (int)((n - kk) * a.keep);
+      if (lkeep < 1) lkeep = 1;
+    }
+    if (!a.lock && lkeep > 0) { lkeep += kk; kk = 0; }
+    ctl->nconv = kk;
+    ctl->l = lkeep;
+    ctl->reason = reason;
+    ctl->nv = n;
+    ctl->breakdown = breakdown;
+    ctl->need_start = (reason == 0 && (breakdown || kk == n) && kk < a.nev) ? 1 : 0;
+    ctl->ds_error = s_fail;
+    ctl->beta = beta;
+  }
+}
+
+cudaError_t launch_ds_hep(const DSArgs &a, int n_max, cudaStream_t s) {
+  if (n_max > DS_MAXN) return cudaErrorInvalidValue;
+  const size_t shm = (size_t)n_max * n_max * 8;
+  cudaError_t err = cudaFuncSetAttribute(k_ds_hep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+  if (err != cudaSuccess) return err;
+  k_ds_hep<<<1, DS_THREADS, shm, s>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace ksg

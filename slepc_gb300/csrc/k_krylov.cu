@@ -1,0 +1,712 @@
+// k_krylov.cu -- the Krylov factorisation kernels of the GB300 Krylov-Schur path.
+//
+//   k_spmv          y = sigma * A x                CSR, sub-warp per row, FP64 FMA    (MatMult, bvops.c:862-885)
+//   k_gs_dot        h = V^T [u w], u.u, u.w, w.w    half A of the Gram-Schmidt pair   (BVDotVec, bvblas.c:240-261)
+//   k_gs_update     [v w'] = [u w] - V [s g]        half B of the Gram-Schmidt pair   (BVMultVec, bvblas.c:56-67)
+//   k_restart       V(:,s:e) = V(:,a:b) Q(a:b,s:e)  thick restart, in place by rows    (BVMultInPlace, bvblas.c:74-106)
+//
+// Orthogonalisation is classical Gram-Schmidt with reorthogonalisation, arranged as DCGS2 (Bielich, Langou,
+// Thomas, Swirydowicz, Yamazaki, Boman, "Low-synch Gram-Schmidt with delayed reorthogonalization for Krylov
+// solvers", Parallel Computing 112, 2022): the reorthogonalisation of u_j is fused with the projection of
+// w = A u_j, so each Krylov step reads the basis twice (once per kernel) instead of four times.  The Hessenberg
+// column of A v_j is recovered as ([V_j^T w; v_j^T w] - H s) / nu, with u_j = nu v_j + V_j s.  Reductions are
+// deterministic: fixed row partition, fixed-order merge of per-block partials by the last block to finish.
+#include "common.cuh"
+#include "kernels.h"
+#include "ks_types.h"
+
+namespace ksg {
+
+// ------------------------------------------------------------------------------------------------------------
+// Arithmetic traits
+// ------------------------------------------------------------------------------------------------------------
+struct PairAr {
+  using val = f2x;
+  using acc = dfacc;
+  static KS_DEVICE val cvt(double v) { return split_f64(v); }
+  static KS_DEVICE void zero(acc &a) { acc_zero(a); }
+  static KS_DEVICE void fma(acc &a, val x, val y) { acc_fma(a, x, y); }
+  static KS_DEVICE void merge(acc &a, acc b) { acc_merge(a, b); }
+  static KS_DEVICE double value(acc a) { return acc_value(a); }
+  static KS_DEVICE acc shfl(acc a, int off) { return shfl_down_acc(a, off); }
+  static KS_DEVICE unsigned long long pack(acc a) {
+    return (unsigned long long)__float_as_uint(a.s) | ((unsigned long long)__float_as_uint(a.c) << 32);
+  }
+  static KS_DEVICE acc unpack(unsigned long long u) {
+    acc a;
+    a.s = __uint_as_float((unsigned)(u & 0xffffffffull));
+    a.c = __uint_as_float((unsigned)(u >> 32));
+    return a;
+  }
+};
+
+struct F64Ar {
+  using val = double;
+  using acc = double;
+  static KS_DEVICE val cvt(double v) { return v; }
+  static KS_DEVICE void zero(acc &a) { a = 0.0; }
+  static KS_DEVICE void fma(acc &a, val x, val y) { a = ::fma(x, y, a); }
+  static KS_DEVICE void merge(acc &a, acc b) { a += b; }
+  static KS_DEVICE double value(acc a) { return a; }
+  static KS_DEVICE acc shfl(acc a, int off) { return __shfl_down_sync(0xffffffffu, a, off); }
+  static KS_DEVICE unsigned long long pack(acc a) { return (unsigned long long)__double_as_longlong(a); }
+  static KS_DEVICE acc unpack(unsigned long long u) { return __longlong_as_double((long long)u); }
+};
+
+template <class Ar>
+KS_DEVICE typename Ar::acc warp_reduce(typename Ar::acc a) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) Ar::merge(a, Ar::shfl(a, off));
+  return a;
+}
+
+KS_DEVICE double warp_sum_f64(double v) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+  return v;
+}
+
+enum { TK_DOT = 0, TK_UPD = 1, TK_NRM = 2 };
+
+// ------------------------------------------------------------------------------------------------------------
+// SpMV: LANES threads per row, FP64 FMA.  Each warp owns 32/LANES consecutive rows per iteration.
+// ------------------------------------------------------------------------------------------------------------
+template <int LANES>
+__global__ void __launch_bounds__(256) k_spmv(const int *__restrict__ rp, const int *__restrict__ ci,
+                                              const double *__restrict__ va, const double *__restrict__ x,
+                                              double *__restrict__ y, int n, const KrylovState *st, double scale) {
+  if (st && st->stop) return;
+  const double sc = st ? st->sigma * scale : scale;
+  constexpr int RPW = 32 / LANES;
+  const int lane = threadIdx.x & 31;
+  const int sub = lane % LANES, grp = lane / LANES;
+  const long long warp_global = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long base = warp_global * RPW; base < n; base += nwarps * RPW) {
+    const long long row = base + grp;
+    int p0 = 0, p1 = 0;
+    if (row < n) {
+      p0 = rp[row];
+      p1 = rp[row + 1];
+    }
+    double sum = 0.0;
+    for (int p = p0 + sub; p < p1; p += LANES) sum = ::fma(va[p], __ldg(x + ci[p]), sum);
+#pragma unroll
+    for (int off = LANES / 2; off > 0; off >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, off, LANES);
+    if (sub == 0 && row < n) y[row] = sum * sc;
+  }
+}
+
+// ------------------------------------------------------------------------------------------------------------
+// Gram-Schmidt half A: partial sums of V^T u (and V^T w), plus u.u (u.w, w.w), per block, then the last block
+// merges them in block order and runs the coefficient algebra (epilogues below).
+// ------------------------------------------------------------------------------------------------------------
+constexpr int A_THREADS = 512;
+constexpr int A_WARPS = 16;
+constexpr int A_TILE = 512;
+constexpr int A_MAXJ = 272;
+
+// Coefficient algebra of one DCGS2 step (mode 0), the final reorthogonalisation (mode 1) or a plain CGS pass
+// used to orthonormalise a start vector (mode 2).  res[] holds the merged sums: s_raw/b interleaved per column
+// (NX = 2) or s_raw only (NX = 1), then the scalars.  Runs in the last block.
+template <int NX>
+__device__ void gs_epilogue(const StepArgs &a, const double *res, int mode) {
+  KrylovState *st = a.st;
+  // res[] already carries the scale sigma: kernel A stages u = sigma * u_raw
+  if (mode == GS_DOTS) {
+    for (int i = threadIdx.x; i < a.J * NX; i += blockDim.x) a.coef[i] = res[i];
+    if (threadIdx.x == 0) a.coef[a.J * NX] = res[a.J * NX];
+    return;
+  }
+  const int J = a.J, j = a.j;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  __shared__ double sh_nu, sh_bp, sh_tau, sh_invnu, sh_hj, sh_sigma;
+  __shared__ int sh_lindep, sh_first;
+  const double sigma = st->sigma;
+  if (warp == 0) {
+    double ss = 0.0, sb = 0.0;
+    for (int i = lane; i < J; i += 32) {
+      const double s = res[i * NX];
+      ss = ::fma(s, s, ss);
+      if (NX == 2) sb = ::fma(s, res[i * NX + 1], sb);
+      a.coef[i] = s;
+    }
+    ss = warp_sum_f64(ss);
+    sb = warp_sum_f64(sb);
+    if (lane == 0) {
+      const double aa = res[J * NX];
+      const double nu2 = aa - ss;
+      const double onorm = sqrt(aa > 0.0 ? aa : 0.0);
+      const double nu = nu2 > 0.0 ? sqrt(nu2) : 0.0;
+      const int lindep = !(nu2 > 0.0 && nu >= a.eta * onorm);
+      sh_nu = nu;
+      sh_lindep = lindep;
+      sh_sigma = sigma;
+      sh_bp = st->beta_prev;
+      sh_first = (j == st->k0) || mode == 2;
+      st->onorm = onorm;
+      if (mode == 2) {
+        // one CGS pass of an orthonormalisation: the caller judges linear dependence from nu and onorm
+        st->breakdown = !(nu2 > 0.0 && nu > 0.0);
+        if (!st->breakdown) st->invnu = 1.0 / nu;
+        else st->stop = 1;
+      } else if (lindep) {
+        st->stop = 1;
+        st->breakdown = 1;
+        if (mode == 0) st->m = j;
+        st->beta_out = st->beta_prev * nu;
+      } else {
+        const double invnu = 1.0 / nu;
+        sh_invnu = invnu;
+        st->invnu = invnu;
+        if (mode == 1) {
+          st->beta_out = st->beta_prev * nu;
+        } else {
+          const double c = res[J * NX + 1];
+          const double hj = (c - sb) * invnu;
+          const double tau = hj * invnu;
+          sh_hj = hj;
+          sh_tau = tau;
+          st->tau_sigma = tau * sigma;
+        }
+      }
+    }
+  }
+  __syncthreads();
+  if (mode == 2) return;
+  const int lindep = sh_lindep, first = sh_first;
+  const double bp = sh_bp, nu = sh_nu;
+  // 1. finalise column j-1 (columns of this segment only): H[0:j, j-1] += bp * s, H[j, j-1] = bp * nu
+  if (!first) {
+    if (a.hermitian) {
+      if (tid == 0) {
+        a.d[j - 1] += bp * a.coef[j - 1];
+        a.e[j - 1] = lindep ? 0.0 : bp * nu;
+      }
+    } else {
+      for (int i = tid; i < j; i += blockDim.x) a.H[i + (size_t)(j - 1) * a.ldh] += bp * a.coef[i];
+      if (tid == 0) a.H[j + (size_t)(j - 1) * a.ldh] = lindep ? 0.0 : bp * nu;
+    }
+  }
+  if (mode == 1 || lindep) return;
+  __syncthreads();
+  // 2. column j: H[0:j+1, j] = ([b; hj] - H[0:j+1, 0:j] s) / nu;  g = b - tau s
+  const double invnu = sh_invnu, tau = sh_tau, hj = sh_hj;
+  if (a.hermitian) {
+    if (warp == 0) {
+      // row j of H[0:j+1, 0:j]: the arrow (first step of a segment) or the subdiagonal entry
+      double hs = 0.0;
+      if (first) {
+        for (int i = lane; i < j; i += 32) hs = ::fma(a.e[i], a.coef[i], hs);
+        hs = warp_sum_f64(hs);
+      } else if (lane == 0) {
+        hs = a.e[j - 1] * a.coef[j - 1];
+      }
+      if (lane == 0) a.d[j] = (hj - hs) * invnu;
+    }
+  } else {
+    double *Hc = a.H + (size_t)j * a.ldh;
+    for (int i = tid; i <= j; i += blockDim.x) {
+      double hs = 0.0;
+      const int c0 = (i >= 2) ? 0 : 0;
+      for (int c = c0; c < j; ++c) hs = ::fma(a.H[i + (size_t)c * a.ldh], a.coef[c], hs);
+      const double y = (i < j) ? res[i * NX + 1] : hj;
+      Hc[i] = (y - hs) * invnu;
+    }
+  }
+  for (int i = tid; i < J; i += blockDim.x) a.coef[J + i] = res[i * NX + 1] - tau * a.coef[i];
+}
+
+template <int NX, int CPW, class Ar>
+__global__ void __launch_bounds__(A_THREADS, 1) k_gs_dot(StepArgs a, int mode) {
+  KrylovState *st = a.st;
+  if (st->stop) return;
+  using val = typename Ar::val;
+  using acc = typename Ar::acc;
+  __shared__ __align__(16) val sx[NX][A_TILE];
+  __shared__ acc sred[A_WARPS][3];
+  __shared__ double res[A_MAXJ * 2 + 4];
+  __shared__ int s_last;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int n = a.n, J = a.J;
+  const double sigma = st->sigma;
+  const double *U = a.U;
+  const double *W = a.W;
+  acc cacc[CPW][NX];
+#pragma unroll
+  for (int k = 0; k < CPW; ++k)
+#pragma unroll
+    for (int q = 0; q < NX; ++q) Ar::zero(cacc[k][q]);
+  acc sc0, sc1, sc2;
+  Ar::zero(sc0);
+  Ar::zero(sc1);
+  Ar::zero(sc2);
+  const int ntiles = (n + A_TILE - 1) / A_TILE;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int r0 = t * A_TILE;
+    const int rows = min(A_TILE, n - r0);
+    {
+      double u = 0.0, w = 0.0;
+      if (tid < rows) {
+        u = U[r0 + tid] * sigma;
+        if (NX == 2) w = W[r0 + tid];
+      }
+      const val us = Ar::cvt(u);
+      sx[0][tid] = us;
+      Ar::fma(sc0, us, us);
+      if (NX == 2) {
+        const val ws = Ar::cvt(w);
+        sx[NX - 1][tid] = ws;
+        Ar::fma(sc1, us, ws);
+        Ar::fma(sc2, ws, ws);
+      }
+    }
+    __syncthreads();
+    if (rows == A_TILE) {
+#pragma unroll
+      for (int k = 0; k < CPW; ++k) {
+        const int c = warp + k * A_WARPS;
+        if (c < J) {
+          const double *col = a.V + (size_t)c * a.ldv + r0 + lane * 2;
+          double2 v[8];
+#pragma unroll
+          for (int i = 0; i < 8; ++i) v[i] = ld_stream2(col + 64 * i);
+#pragma unroll
+          for (int i = 0; i < 8; ++i) {
+            const int rr = lane * 2 + 64 * i;
+            const val a0 = Ar::cvt(v[i].x), a1 = Ar::cvt(v[i].y);
+            Ar::fma(cacc[k][0], a0, sx[0][rr]);
+            Ar::fma(cacc[k][0], a1, sx[0][rr + 1]);
+            if (NX == 2) {
+              Ar::fma(cacc[k][NX - 1], a0, sx[NX - 1][rr]);
+              Ar::fma(cacc[k][NX - 1], a1, sx[NX - 1][rr + 1]);
+            }
+          }
+        }
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < CPW; ++k) {
+        const int c = warp + k * A_WARPS;
+        if (c < J) {
+          const double *col = a.V + (size_t)c * a.ldv + r0;
+          for (int rr = lane; rr < rows; rr += 32) {
+            const val a0 = Ar::cvt(col[rr]);
+            Ar::fma(cacc[k][0], a0, sx[0][rr]);
+            if (NX == 2) Ar::fma(cacc[k][NX - 1], a0, sx[NX - 1][rr]);
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+  // per-block partials
+  unsigned long long *pb = reinterpret_cast<unsigned long long *>(a.part) + (size_t)blockIdx.x * a.pstride;
+#pragma unroll
+  for (int k = 0; k < CPW; ++k) {
+    const int c = warp + k * A_WARPS;
+    if (c < J) {
+#pragma unroll
+      for (int q = 0; q < NX; ++q) {
+        const acc r = warp_reduce<Ar>(cacc[k][q]);
+        if (lane == 0) pb[c * NX + q] = Ar::pack(r);
+      }
+    }
+  }
+  {
+    acc r0 = warp_reduce<Ar>(sc0), r1 = warp_reduce<Ar>(sc1), r2 = warp_reduce<Ar>(sc2);
+    if (lane == 0) {
+      sred[warp][0] = r0;
+      sred[warp][1] = r1;
+      sred[warp][2] = r2;
+    }
+    __syncthreads();
+    if (warp == 0) {
+      const int nsc = (NX == 2) ? 3 : 1;
+      for (int i = 0; i < nsc; ++i) {
+        acc v;
+        Ar::zero(v);
+        if (lane < A_WARPS) v = sred[lane][i];
+        v = warp_reduce<Ar>(v);
+        if (lane == 0) pb[J * NX + i] = Ar::pack(v);
+      }
+    }
+  }
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) s_last = (atomicAdd(&st->tickets[TK_DOT], 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  const int nout = J * NX + ((NX == 2) ? 3 : 1);
+  const unsigned long long *pall = reinterpret_cast<const unsigned long long *>(a.part);
+  for (int o = tid; o < nout; o += A_THREADS) {
+    acc s;
+    Ar::zero(s);
+    for (int b = 0; b < (int)gridDim.x; ++b) Ar::merge(s, Ar::unpack(__ldcg(pall + (size_t)b * a.pstride + o)));
+    res[o] = Ar::value(s);
+  }
+  __syncthreads();
+  if (tid == 0) st->tickets[TK_DOT] = 0;
+  gs_epilogue<NX>(a, res, mode);
+}
+
+// ------------------------------------------------------------------------------------------------------------
+// Gram-Schmidt half B: per row, v_j = (sigma u - V s) / nu and (NX = 2) w' = w - V g - tau sigma u, with ||w'||^2
+// merged by the last block into the next step's scale.
+// ------------------------------------------------------------------------------------------------------------
+constexpr int B_THREADS = 256;
+constexpr int B_TILE = 2 * B_THREADS;
+
+template <int NX, class Ar>
+__global__ void __launch_bounds__(B_THREADS) k_gs_update(StepArgs a, int mode) {
+  KrylovState *st = a.st;
+  if (st->stop) return;
+  using val = typename Ar::val;
+  using acc = typename Ar::acc;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  val *cs = reinterpret_cast<val *>(smraw);  // s then g
+  __shared__ acc sred[B_THREADS / 32];
+  __shared__ int s_last;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int n = a.n, J = a.J;
+  for (int i = tid; i < NX * J; i += B_THREADS) cs[i] = Ar::cvt(a.coef[i]);
+  __syncthreads();
+  const double sigma = st->sigma, invnu = st->invnu, tsig = st->tau_sigma;
+  double *U = a.U;
+  double *W = a.W;
+  acc nrm;
+  Ar::zero(nrm);
+  const int ntiles = (n + B_TILE - 1) / B_TILE;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int r = t * B_TILE + tid * 2;
+    if (r + 1 < n) {
+      acc s0, s1, g0, g1;
+      Ar::zero(s0);
+      Ar::zero(s1);
+      Ar::zero(g0);
+      Ar::zero(g1);
+      const double *col = a.V + r;
+      int c = 0;
+      for (; c + 4 <= J; c += 4) {
+        double2 v[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) v[q] = ld_stream2(col + (size_t)(c + q) * a.ldv);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const val v0 = Ar::cvt(v[q].x), v1 = Ar::cvt(v[q].y);
+          Ar::fma(s0, v0, cs[c + q]);
+          Ar::fma(s1, v1, cs[c + q]);
+          if (NX == 2) {
+            Ar::fma(g0, v0, cs[J + c + q]);
+            Ar::fma(g1, v1, cs[J + c + q]);
+          }
+        }
+      }
+      for (; c < J; ++c) {
+        const double2 v = ld_stream2(col + (size_t)c * a.ldv);
+        const val v0 = Ar::cvt(v.x), v1 = Ar::cvt(v.y);
+        Ar::fma(s0, v0, cs[c]);
+        Ar::fma(s1, v1, cs[c]);
+        if (NX == 2) {
+          Ar::fma(g0, v0, cs[J + c]);
+          Ar::fma(g1, v1, cs[J + c]);
+        }
+      }
+      const double2 u = *reinterpret_cast<const double2 *>(U + r);
+      double2 vo;
+      vo.x = (sigma * u.x - Ar::value(s0)) * invnu;
+      vo.y = (sigma * u.y - Ar::value(s1)) * invnu;
+      *reinterpret_cast<double2 *>(U + r) = vo;
+      if (NX == 2) {
+        const double2 w = *reinterpret_cast<const double2 *>(W + r);
+        double2 wo;
+        wo.x = w.x - Ar::value(g0) - tsig * u.x;
+        wo.y = w.y - Ar::value(g1) - tsig * u.y;
+        *reinterpret_cast<double2 *>(W + r) = wo;
+        const val w0 = Ar::cvt(wo.x), w1 = Ar::cvt(wo.y);
+        Ar::fma(nrm, w0, w0);
+        Ar::fma(nrm, w1, w1);
+      }
+    } else if (r < n) {
+      acc s0, g0;
+      Ar::zero(s0);
+      Ar::zero(g0);
+      for (int c = 0; c < J; ++c) {
+        const val v0 = Ar::cvt(a.V[r + (size_t)c * a.ldv]);
+        Ar::fma(s0, v0, cs[c]);
+        if (NX == 2) Ar::fma(g0, v0, cs[J + c]);
+      }
+      const double u = U[r];
+      U[r] = (sigma * u - Ar::value(s0)) * invnu;
+      if (NX == 2) {
+        const double wo = W[r] - Ar::value(g0) - tsig * u;
+        W[r] = wo;
+        const val w0 = Ar::cvt(wo);
+        Ar::fma(nrm, w0, w0);
+      }
+    }
+  }
+  if (NX == 1) return;  // no norm needed after the final reorthogonalisation or a start-vector pass
+  nrm = warp_reduce<Ar>(nrm);
+  if (lane == 0) sred[warp] = nrm;
+  __syncthreads();
+  unsigned long long *pb = reinterpret_cast<unsigned long long *>(a.part);
+  if (warp == 0) {
+    acc v;
+    Ar::zero(v);
+    if (lane < B_THREADS / 32) v = sred[lane];
+    v = warp_reduce<Ar>(v);
+    if (lane == 0) pb[blockIdx.x] = Ar::pack(v);
+  }
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) s_last = (atomicAdd(&st->tickets[TK_UPD], 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  if (warp == 0) {
+    acc v;
+    Ar::zero(v);
+    for (int b = lane; b < (int)gridDim.x; b += 32) Ar::merge(v, Ar::unpack(__ldcg(pb + b)));
+    // merge lanes in a fixed order
+    v = warp_reduce<Ar>(v);
+    if (lane == 0) {
+      const double beta = sqrt(Ar::value(v));
+      st->tickets[TK_UPD] = 0;
+      if (beta == 0.0 || !(beta == beta)) {
+        st->stop = 1;
+        st->breakdown = 1;
+        st->m = a.j + 1;
+        st->beta_out = 0.0;
+        if (a.hermitian) a.e[a.j] = 0.0;
+        else a.H[(a.j + 1) + (size_t)a.j * a.ldh] = 0.0;
+      } else {
+        st->sigma = 1.0 / beta;
+        st->beta_prev = beta * st->invnu;
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------------------------------
+// Thick restart: V(:, s0:s0+N) = V(:, a0:a0+K) * Q(a0:a0+K, s0:s0+N), in place by row tiles.
+// ------------------------------------------------------------------------------------------------------------
+constexpr int R_THREADS = 256;
+constexpr int R_ROWS = 32;
+constexpr int R_MAXN = 144;
+
+template <class Ar>
+__global__ void __launch_bounds__(R_THREADS, 1) k_restart(double *V, long long ldv, int n, int a0, int K, int s0,
+                                                          int N, const double *Q, int ldq) {
+  using val = typename Ar::val;
+  using acc = typename Ar::acc;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  val *Qs = reinterpret_cast<val *>(smraw);  // K x N, row k contiguous
+  val *Vt = Qs + (size_t)K * N;              // K x R_ROWS, column k contiguous
+  const int tid = threadIdx.x;
+  for (int i = tid; i < K * N; i += R_THREADS) {
+    const int k = i / N, c = i % N;
+    Qs[i] = Ar::cvt(Q[(a0 + k) + (size_t)(s0 + c) * ldq]);
+  }
+  const int ty = tid / 16, tx = tid % 16;  // rows 2ty, 2ty+1; columns tx + 16q
+  constexpr int CQ = (R_MAXN + 15) / 16;
+  const int ntiles = (n + R_ROWS - 1) / R_ROWS;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int r0 = t * R_ROWS;
+    const int rows = min(R_ROWS, n - r0);
+    __syncthreads();
+    for (int i = tid; i < K * R_ROWS; i += R_THREADS) {
+      const int k = i / R_ROWS, r = i % R_ROWS;
+      Vt[i] = Ar::cvt(r < rows ? V[(r0 + r) + (size_t)(a0 + k) * ldv] : 0.0);
+    }
+    __syncthreads();
+    acc o0[CQ], o1[CQ];
+#pragma unroll
+    for (int q = 0; q < CQ; ++q) {
+      Ar::zero(o0[q]);
+      Ar::zero(o1[q]);
+    }
+    for (int k = 0; k < K; ++k) {
+      const val v0 = Vt[k * R_ROWS + 2 * ty], v1 = Vt[k * R_ROWS + 2 * ty + 1];
+#pragma unroll
+      for (int q = 0; q < CQ; ++q) {
+        const int c = tx + 16 * q;
+        if (c < N) {
+          const val qq = Qs[k * N + c];
+          Ar::fma(o0[q], v0, qq);
+          Ar::fma(o1[q], v1, qq);
+        }
+      }
+    }
+    __syncthreads();  // every read of this tile's V columns precedes the in-place writes
+#pragma unroll
+    for (int q = 0; q < CQ; ++q) {
+      const int c = tx + 16 * q;
+      if (c < N) {
+        if (2 * ty < rows) V[(r0 + 2 * ty) + (size_t)(s0 + c) * ldv] = Ar::value(o0[q]);
+        if (2 * ty + 1 < rows) V[(r0 + 2 * ty + 1) + (size_t)(s0 + c) * ldv] = Ar::value(o1[q]);
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------------------------------
+// Small helpers
+// ------------------------------------------------------------------------------------------------------------
+__global__ void k_segment_begin(KrylovState *st, int k0, int m) {
+  st->sigma = 1.0;
+  st->beta_prev = 0.0;
+  st->invnu = 1.0;
+  st->tau_sigma = 0.0;
+  st->beta_out = 0.0;
+  st->onorm = 0.0;
+  st->stop = 0;
+  st->m = m;
+  st->breakdown = 0;
+  st->k0 = k0;
+}
+
+__global__ void k_set_scales(KrylovState *st, double sigma, double invnu) {
+  st->sigma = sigma;
+  st->invnu = invnu;
+  st->stop = 0;
+}
+
+__global__ void k_scale_col(double *x, int n, double alpha) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    x[i] *= alpha;
+}
+
+// ------------------------------------------------------------------------------------------------------------
+// Host-side launchers
+// ------------------------------------------------------------------------------------------------------------
+static int g_num_sms = 0;
+
+int num_sms() {
+  if (!g_num_sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (g_num_sms <= 0) g_num_sms = 1;
+  }
+  return g_num_sms;
+}
+
+int spmv_lanes_for(double avg_nnz) {
+  int lanes = 1;
+  while (lanes < 32 && lanes < avg_nnz) lanes <<= 1;
+  return lanes;
+}
+
+cudaError_t launch_spmv(const int *rp, const int *ci, const double *va, const double *x, double *y, int n, int lanes,
+                        const KrylovState *st, double scale, cudaStream_t s) {
+  const int threads = 256;
+  long long rows_per_block = (threads / 32) * (32 / lanes);
+  long long blocks = (n + rows_per_block - 1) / rows_per_block;
+  long long cap = (long long)num_sms() * 8;
+  if (blocks > cap) blocks = cap;
+  if (blocks < 1) blocks = 1;
+  switch (lanes) {
+    case 1: k_spmv<1><<<(int)blocks, threads, 0, s>>>(rp, ci, va, x, y, n, st, scale); break;
+    case 2: k_spmv<2><<<(int)blocks, threads, 0, s>>>(rp, ci, va, x, y, n, st, scale); break;
+    case 4: k_spmv<4><<<(int)blocks, threads, 0, s>>>(rp, ci, va, x, y, n, st, scale); break;
+    case 8: k_spmv<8><<<(int)blocks, threads, 0, s>>>(rp, ci, va, x, y, n, st, scale); break;
+    case 16: k_spmv<16><<<(int)blocks, threads, 0, s>>>(rp, ci, va, x, y, n, st, scale); break;
+    default: k_spmv<32><<<(int)blocks, threads, 0, s>>>(rp, ci, va, x, y, n, st, scale); break;
+  }
+  return cudaGetLastError();
+}
+
+int gs_dot_blocks(int n) {
+  const int ntiles = (n + A_TILE - 1) / A_TILE;
+  int blocks = num_sms();
+  if (blocks > ntiles) blocks = ntiles;
+  return blocks < 1 ? 1 : blocks;
+}
+
+int gs_update_blocks(int n) {
+  const int ntiles = (n + B_TILE - 1) / B_TILE;
+  int blocks = num_sms() * 6;
+  if (blocks > ntiles) blocks = ntiles;
+  return blocks < 1 ? 1 : blocks;
+}
+
+int gs_max_columns() { return A_MAXJ; }
+
+template <int NX, class Ar>
+static cudaError_t dot_dispatch(const StepArgs &a, int mode, int blocks, cudaStream_t s) {
+  const int J = a.J;
+  if (J <= 16) k_gs_dot<NX, 1, Ar><<<blocks, A_THREADS, 0, s>>>(a, mode);
+  else if (J <= 32) k_gs_dot<NX, 2, Ar><<<blocks, A_THREADS, 0, s>>>(a, mode);
+  else if (J <= 64) k_gs_dot<NX, 4, Ar><<<blocks, A_THREADS, 0, s>>>(a, mode);
+  else if (J <= 144) k_gs_dot<NX, 9, Ar><<<blocks, A_THREADS, 0, s>>>(a, mode);
+  else if (J <= A_MAXJ) k_gs_dot<NX, 17, Ar><<<blocks, A_THREADS, 0, s>>>(a, mode);
+  else return cudaErrorInvalidValue;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gs_dot(const StepArgs &a, int nx, int mode, int arith, cudaStream_t s) {
+  const int blocks = gs_dot_blocks(a.n);
+  if (arith == ARITH_F64) return nx == 2 ? dot_dispatch<2, F64Ar>(a, mode, blocks, s) : dot_dispatch<1, F64Ar>(a, mode, blocks, s);
+  return nx == 2 ? dot_dispatch<2, PairAr>(a, mode, blocks, s) : dot_dispatch<1, PairAr>(a, mode, blocks, s);
+}
+
+cudaError_t launch_gs_update(const StepArgs &a, int nx, int mode, int arith, cudaStream_t s) {
+  const int blocks = gs_update_blocks(a.n);
+  const size_t shm = (size_t)nx * (a.J > 0 ? a.J : 1) * 8;
+  if (arith == ARITH_F64) {
+    if (nx == 2) k_gs_update<2, F64Ar><<<blocks, B_THREADS, shm, s>>>(a, mode);
+    else k_gs_update<1, F64Ar><<<blocks, B_THREADS, shm, s>>>(a, mode);
+  } else {
+    if (nx == 2) k_gs_update<2, PairAr><<<blocks, B_THREADS, shm, s>>>(a, mode);
+    else k_gs_update<1, PairAr><<<blocks, B_THREADS, shm, s>>>(a, mode);
+  }
+  return cudaGetLastError();
+}
+
+size_t restart_smem_bytes(int K, int N) { return ((size_t)K * N + (size_t)K * R_ROWS) * 8; }
+
+cudaError_t launch_restart(double *V, long long ldv, int n, int a0, int K, int s0, int N, const double *Q, int ldq,
+                           int arith, cudaStream_t s) {
+  if (N <= 0 || K <= 0) return cudaSuccess;
+  if (N > R_MAXN) return cudaErrorInvalidValue;
+  const size_t shm = restart_smem_bytes(K, N);
+  if (shm > 227 * 1024) return cudaErrorInvalidValue;
+  const int ntiles = (n + R_ROWS - 1) / R_ROWS;
+  int blocks = num_sms();
+  if (blocks > ntiles) blocks = ntiles;
+  cudaError_t err;
+  if (arith == ARITH_F64) {
+    err = cudaFuncSetAttribute(k_restart<F64Ar>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+    if (err != cudaSuccess) return err;
+    k_restart<F64Ar><<<blocks, R_THREADS, shm, s>>>(V, ldv, n, a0, K, s0, N, Q, ldq);
+  } else {
+    err = cudaFuncSetAttribute(k_restart<PairAr>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+    if (err != cudaSuccess) return err;
+    k_restart<PairAr><<<blocks, R_THREADS, shm, s>>>(V, ldv, n, a0, K, s0, N, Q, ldq);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_segment_begin(KrylovState *st, int k0, int m, cudaStream_t s) {
+  k_segment_begin<<<1, 1, 0, s>>>(st, k0, m);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_set_scales(KrylovState *st, double sigma, double invnu, cudaStream_t s) {
+  k_set_scales<<<1, 1, 0, s>>>(st, sigma, invnu);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_set_unit_scale(KrylovState *st, cudaStream_t s) { return launch_set_scales(st, 1.0, 1.0, s); }
+
+cudaError_t launch_scale(double *x, int n, double alpha, cudaStream_t s) {
+  int blocks = (n + 255) / 256;
+  if (blocks > num_sms() * 8) blocks = num_sms() * 8;
+  if (blocks < 1) blocks = 1;
+  k_scale_col<<<blocks, 256, 0, s>>>(x, n, alpha);
+  return cudaGetLastError();
+}
+
+}  // namespace ksg

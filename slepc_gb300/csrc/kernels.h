@@ -1,0 +1,55 @@
+// kernels.h -- host-side launchers of the CUDA kernels (no CUDA types beyond cudaStream_t / cudaError_t).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "ks_types.h"
+
+namespace ksg {
+
+// Arguments of the projected-problem kernels.
+struct DSArgs {
+  int ld;          // leading dimension of Q / H (ncv + 1)
+  int n;           // problem size when st is NULL (DS API); otherwise st->m is used
+  int flags;       // DS_DO_* operations to run
+  int l;           // locked columns (nconv)
+  int k;           // nconv + kept columns (start of the new Krylov segment)
+  int raw;         // 1 if the matrix still holds the arrow / Krylov-Schur form (kept columns > 0)
+  double *d, *e;   // symmetric: diagonal and off-diagonal / extra row (length ld)
+  double *H;       // non-symmetric: ld x ld matrix, extra row at row n
+  double *Q;       // ld x ld
+  double *eigr, *eigi, *errest;  // length ld
+  double *work;    // scratch (non-symmetric solver), 4 * ld doubles
+  int which;
+  double tol;
+  int nev, its, max_it;
+  double keep;
+  int lock;
+  const KrylovState *st;
+  KSControl *ctl;
+};
+
+enum { DS_DO_SOLVE = 1, DS_DO_SORT = 2, DS_DO_EXTRAROW = 4, DS_DO_CONTROL = 8, DS_DO_ALL = 15 };
+
+int num_sms();
+int spmv_lanes_for(double avg_nnz);
+int gs_dot_blocks(int n);
+int gs_update_blocks(int n);
+int gs_max_columns();
+size_t restart_smem_bytes(int K, int N);
+
+cudaError_t launch_spmv(const int *rp, const int *ci, const double *va, const double *x, double *y, int n, int lanes,
+                        const KrylovState *st, double scale, cudaStream_t s);
+cudaError_t launch_gs_dot(const StepArgs &a, int nx, int mode, int arith, cudaStream_t s);
+cudaError_t launch_gs_update(const StepArgs &a, int nx, int mode, int arith, cudaStream_t s);
+cudaError_t launch_restart(double *V, long long ldv, int n, int a0, int K, int s0, int N, const double *Q, int ldq,
+                           int arith, cudaStream_t s);
+cudaError_t launch_segment_begin(KrylovState *st, int k0, int m, cudaStream_t s);
+cudaError_t launch_set_unit_scale(KrylovState *st, cudaStream_t s);
+cudaError_t launch_set_scales(KrylovState *st, double sigma, double invnu, cudaStream_t s);
+cudaError_t launch_scale(double *x, int n, double alpha, cudaStream_t s);
+cudaError_t launch_ds_hep(const DSArgs &a, int n_max, cudaStream_t s);
+cudaError_t launch_ds_nhep(const DSArgs &a, int n_max, cudaStream_t s);
+cudaError_t launch_nhep_vectors(double *T, int ld, int n, double *X, cudaStream_t s);
+
+}  // namespace ksg

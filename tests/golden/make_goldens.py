@@ -1,0 +1,64 @@
+"""Regenerate reference_outputs.json from the reference's expected-output files (run in the build container only;
+the GPU machine uses the committed JSON).  Only the printed eigenvalues/norms of the Krylov-Schur-path tests are
+extracted; each entry records the file it came from and the options of that test."""
+import json
+import os
+import re
+
+REF = os.environ.get("SLEPC_REFERENCE", "/root/reference")
+OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_outputs.json")
+
+
+def read(rel):
+    with open(os.path.join(REF, rel)) as f:
+        return f.read()
+
+
+def floats(line):
+    return [float(x) for x in re.findall(r"-?\d+\.\d+", line)]
+
+
+def main():
+    g = {}
+    # 2-D Laplacian 72x72, -eps_nev 4 -eps_ncv 20 (src/eps/tutorials/ex2.c TEST 1)
+    txt = read("src/eps/tutorials/output/ex2_1.out")
+    line = [l for l in txt.splitlines() if re.search(r"\d\.\d{5}", l)][-1]
+    g["ex2_1"] = {"source": "src/eps/tutorials/output/ex2_1.out", "grid": [72, 72], "nev": 4, "ncv": 20,
+                  "which": "LM", "eigenvalues": floats(line)}
+    # 1-D Laplacian n=30, nev 4: largest, smallest (src/eps/tests/test2.c TEST 1_krylovschur)
+    txt = read("src/eps/tests/output/test2_1.out")
+    blocks = re.findall(r"- - - (\w+) eigenvalues - - -.*?\n.*?\n(.*?)\n", txt, flags=re.S)
+    g["test2_1"] = {"source": "src/eps/tests/output/test2_1.out", "n": 30, "nev": 4,
+                    "tol": max(1000 * 2.220446049250313e-16, 1e-9),
+                    "largest": floats(blocks[0][1]), "smallest": floats(blocks[1][1])}
+    txt = read("src/eps/tests/output/test2_3.out")
+    blocks = re.findall(r"- - - (\w+) eigenvalues - - -.*?\n.*?\n(.*?)\n", txt, flags=re.S)
+    g["test2_3"] = {"source": "src/eps/tests/output/test2_3.out", "n": 32, "nev": 4,
+                    "largest": floats(blocks[0][1]), "smallest": floats(blocks[1][1])}
+    # Brusselator n=50 (100 unknowns), nev 4, largest real (src/eps/tutorials/ex9.c TEST 1)
+    txt = read("src/eps/tutorials/output/ex9_1.out")
+    line = [l for l in txt.splitlines() if "i," in l or "i" in l and re.search(r"\d\.\d{5}", l)][-1]
+    pairs = re.findall(r"(-?\d+\.\d+)([+-]\d+\.\d+)i", line)
+    g["ex9_1"] = {"source": "src/eps/tutorials/output/ex9_1.out", "N": 50, "nev": 4, "which": "LR",
+                  "eigenvalues": [[float(a), float(b)] for a, b in pairs]}
+    # DSHEP compact arrow-tridiagonal n=9, l=2, k=5 (src/sys/classes/ds/tests/test3.c TEST 1)
+    txt = read("src/sys/classes/ds/tests/output/test3_1.out")
+    vals = txt.split("Computed eigenvalues =")[1].split()
+    g["ds_test3_1"] = {"source": "src/sys/classes/ds/tests/output/test3_1.out", "n": 9, "l": 2, "k": 5,
+                       "which": "LM", "eigenvalues": [float(v) for v in vals[:9]]}
+    # DSNHEP Grcar n=10 (src/sys/classes/ds/tests/test1.c TEST 1)
+    txt = read("src/sys/classes/ds/tests/output/test1_1.out")
+    body = txt.split("Computed eigenvalues =")[1]
+    pairs = re.findall(r"(-?\d+\.\d+)\+-(\d+\.\d+)i", body)
+    rn = re.search(r"rnorm for 3rd vector = (\d+\.\d+)", txt)
+    nv = re.search(r"Norm of 1st vector = (\d+\.\d+)", txt)
+    g["ds_test1_1"] = {"source": "src/sys/classes/ds/tests/output/test1_1.out", "n": 10, "which": "LM",
+                       "eigenvalues_abs_imag": [[float(a), float(b)] for a, b in pairs],
+                       "rnorm_3rd": float(rn.group(1)), "norm_1st": float(nv.group(1))}
+    with open(OUT, "w") as f:
+        json.dump(g, f, indent=1)
+    print("wrote", OUT)
+
+
+if __name__ == "__main__":
+    main()

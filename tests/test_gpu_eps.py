@@ -1,0 +1,146 @@
+"""GPU parity: EPSSolve through the C-ABI against the oracle, the reference's goldens and closed-form spectra.
+
+Tolerances: eigenvalues |lam - lam_ref| / |lam_ref| <= 1e-10 (set-based: degenerate spectra give one copy per
+distinct eigenvalue, as the reference's ex2_1.out shows), relative residual ||Ax - lam x|| / (||A|| |lam|) <= tol,
+||V^T V - I||_max <= 1e-12."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import slepc_gb300 as sg
+from slepc_gb300 import matgen
+
+pytestmark = pytest.mark.gpu
+G = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_outputs.json")))
+
+
+def run(csr, **kw):
+    return sg.solve(csr, **kw)
+
+
+def rel_match(vals, ref, tol):
+    ref = np.asarray(ref)
+    return max(np.min(np.abs(ref - v)) / abs(v) for v in vals) <= tol
+
+
+def check_residuals(csr, res, tol):
+    nrm = matgen_norm_inf(csr)
+    for i in range(res["nconv"]):
+        if res["eigi"][i] != 0.0:
+            continue
+        x = res["X"][:, i]
+        A = sg.Mat(*csr)
+        r = np.linalg.norm(A.mult(x) - res["eigr"][i] * x)
+        assert r / (nrm * abs(res["eigr"][i])) <= tol, (i, r)
+
+
+def matgen_norm_inf(csr):
+    rp, ci, va = csr
+    return max(np.add.reduceat(np.abs(va), rp[:-1])) if va.size else 0.0
+
+
+def test_config1_laplacian_100(lib, orc):
+    csr = matgen.laplacian_2d(100)
+    v0 = matgen.start_vector(10000, 1)
+    res = run(csr, hermitian=True, which="LM", nev=10, ncv=32, tol=1e-8, v0=v0)
+    ref = orc.solve(*csr, hermitian=True, which="LM", nev=10, ncv=32, tol=1e-8, v0=v0)
+    assert res["reason"] == 1 and res["nconv"] >= 10
+    exact = matgen.laplacian_eigenvalues([100, 100])
+    assert rel_match(res["eigr"], exact, 1e-10)
+    # every distinct eigenvalue the oracle found among the wanted ones is found on the GPU
+    for lam in np.unique(np.round(ref.eigr[:10], 9)):
+        assert np.min(np.abs(res["eigr"] - lam)) / abs(lam) <= 1e-9
+    check_residuals(csr, res, 1e-8)
+    assert res["eps"].orthogonalityError() <= 1e-12
+
+
+def test_ex2_golden_on_gpu(lib):
+    g = G["ex2_1"]
+    csr = matgen.laplacian_2d(*g["grid"])
+    res = run(csr, hermitian=True, which="LM", nev=g["nev"], ncv=g["ncv"], tol=1e-8,
+              v0=matgen.start_vector(72 * 72, 1))
+    got = np.unique(np.round(res["eigr"], 5))[::-1]
+    assert list(got[:4]) == g["eigenvalues"]
+
+
+@pytest.mark.parametrize("lock", [True, False])
+def test_test2_goldens_on_gpu(lib, lock):
+    g = G["test2_1"]
+    csr = matgen.laplacian_1d(g["n"])
+    for which, name in (("LR", "largest"), ("SR", "smallest")):
+        A = sg.Mat(*csr)
+        eps = sg.EPS().create()
+        eps.setOperators(A)
+        eps.setProblemType(sg.EPS.ProblemType.HEP)
+        eps.setDimensions(g["nev"])
+        eps.setTolerances(g["tol"])
+        eps.setWhichEigenpairs(which)
+        eps.setKrylovSchurLocking(lock)
+        eps.setInitialSpace(matgen.start_vector(g["n"], 1))
+        eps.solve()
+        assert eps.getConvergedReason() == 1
+        vals = [round(eps.getEigenvalue(i), 5) for i in range(g["nev"])]
+        assert vals == g[name]
+
+
+@pytest.mark.parametrize("arith", ["pair", "f64"])
+def test_lap3d_parity(lib, orc, arith):
+    m = 16
+    csr = matgen.laplacian_3d(m)
+    v0 = matgen.start_vector(m ** 3, 2)
+    res = run(csr, hermitian=True, which="LR", nev=20, ncv=48, tol=1e-10, v0=v0, arith=arith)
+    ref = orc.solve(*csr, hermitian=True, which="LR", nev=20, ncv=48, tol=1e-10, v0=v0)
+    assert res["reason"] == 1 and res["nconv"] >= 20
+    exact = matgen.laplacian_eigenvalues([m, m, m])
+    assert rel_match(res["eigr"], exact, 1e-10)
+    assert rel_match(res["eigr"][:20], ref.eigr, 1e-10) or rel_match(res["eigr"][:20], exact, 1e-12)
+    check_residuals(csr, res, 1e-10)
+    assert res["eps"].orthogonalityError() <= 1e-12
+
+
+def test_brusselator_golden_on_gpu(lib, orc):
+    g = G["ex9_1"]
+    csr = matgen.brusselator(g["N"])
+    res = run(csr, hermitian=False, which="LR", nev=g["nev"], tol=1e-8, v0=matgen.start_vector(100, 1))
+    assert res["reason"] == 1
+    got = [[round(a, 5), round(b, 5)] for a, b in zip(res["eigr"][:4], res["eigi"][:4])]
+    assert got == g["eigenvalues"]
+    dense = np.linalg.eigvals(matgen.csr_to_dense(*csr))
+    for a, b in zip(res["eigr"], res["eigi"]):
+        z = complex(a, b)
+        assert np.min(np.abs(dense - z)) / abs(z) < 1e-9
+    # residuals of the complex pairs through EPSComputeError
+    for i in range(res["nconv"]):
+        assert res["errors"][i] < 1e-7
+
+
+def test_convdiff_nhep_parity(lib, orc):
+    N, Pe = 40, 10.0
+    csr = matgen.convection_diffusion_2d(N, Pe)
+    v0 = matgen.start_vector(N * N, 3)
+    res = run(csr, hermitian=False, which="LR", nev=10, ncv=40, tol=1e-12, v0=v0)
+    assert res["reason"] == 1 and res["nconv"] >= 10
+    exact = matgen.convdiff_eigenvalues(N, Pe)
+    assert rel_match(res["eigr"], exact, 1e-10)
+    assert np.all(res["eigi"] == 0.0)
+    ref = orc.solve(*csr, hermitian=False, which="LR", nev=10, ncv=40, tol=1e-12, v0=v0)
+    assert rel_match(res["eigr"][:10], ref.eigr, 1e-10)
+    check_residuals(csr, res, 1e-10)
+
+
+def test_zero_start_vector_error(lib):
+    csr = matgen.laplacian_1d(50)
+    with pytest.raises(sg.SlepcError) as ei:
+        run(csr, hermitian=True, nev=2, v0=np.zeros(50))
+    assert ei.value.code == 77
+
+
+def test_repeatable(lib):
+    csr = matgen.laplacian_2d(40)
+    v0 = matgen.start_vector(1600, 5)
+    a = run(csr, hermitian=True, which="LR", nev=8, ncv=24, tol=1e-10, v0=v0)
+    b = run(csr, hermitian=True, which="LR", nev=8, ncv=24, tol=1e-10, v0=v0)
+    assert np.array_equal(a["eigr"], b["eigr"])
+    assert np.array_equal(a["X"], b["X"])

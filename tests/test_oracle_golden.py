@@ -1,0 +1,153 @@
+"""The oracle (CPU restatement of SLEPc's Krylov-Schur) pinned against the reference's own expected outputs and
+against closed-form spectra / dense LAPACK (numpy, scipy)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from slepc_gb300 import matgen
+
+G = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_outputs.json")))
+EPS64 = np.finfo(float).eps
+
+
+def r5(x):
+    return [round(float(v), 5) for v in x]
+
+
+def test_ds_hep_arrow_golden(orc):
+    g = G["ds_test3_1"]
+    n, l, k = g["n"], g["l"], g["k"]
+    d = np.arange(1, n + 1, dtype=float)
+    e = np.zeros(n)
+    e[l:n - 1] = 1.0
+    err, wr, Q, _ = orc.ds_hep(n, l, k, d, e, which="LM")
+    assert err == 0
+    assert r5(wr) == g["eigenvalues"]
+    # same spectrum as the dense arrow matrix
+    T = np.diag(d)
+    for i in range(l, k):
+        T[i, k] = T[k, i] = 1.0
+    for i in range(k, n - 1):
+        T[i, i + 1] = T[i + 1, i] = 1.0
+    assert np.allclose(np.sort(wr), np.sort(np.linalg.eigvalsh(T)), atol=1e-13)
+
+
+def test_ds_hep_extrarow(orc):
+    n, l, k = 9, 2, 5
+    d = np.arange(1, n + 1, dtype=float)
+    e = np.zeros(n)
+    e[l:n - 1] = 1.0
+    e[n - 1] = 1.0
+    err, wr, Q, eout = orc.ds_hep(n, l, k, d, e, which="LM", extrarow=True)
+    assert err == 0
+    assert abs(np.sum(eout[l:n] - Q[n - 1, l:n])) < 10 * EPS64
+
+
+def grcar(n):
+    A = np.zeros((n, n))
+    for i in range(1, n):
+        A[i, i - 1] = -1.0
+    for j in range(4):
+        for i in range(n - j):
+            A[i, i + j] = 1.0
+    return A
+
+
+def test_ds_nhep_golden(orc):
+    g = G["ds_test1_1"]
+    n = g["n"]
+    err, wr, wi, T, Q, rn, X = orc.ds_nhep(grcar(n), which="LM", vec_index=2)
+    assert err == 0
+    got = [[round(a, 5), round(abs(b), 5)] for a, b in zip(wr, wi)]
+    assert got == g["eigenvalues_abs_imag"]
+    assert round(rn, 3) == g["rnorm_3rd"]
+    assert round(np.hypot(np.linalg.norm(X[:n, 0]), np.linalg.norm(X[:n, 1])), 3) == g["norm_1st"]
+    # Schur relation A Q = Q T
+    A = grcar(n)
+    assert np.abs(A @ Q[:n, :n] - Q[:n, :n] @ T[:n, :n]).max() < 1e-13
+
+
+def test_ex2_golden(orc):
+    g = G["ex2_1"]
+    nx, ny = g["grid"]
+    csr = matgen.laplacian_2d(nx, ny)
+    r = orc.solve(*csr, hermitian=True, which=g["which"], nev=g["nev"], ncv=g["ncv"], tol=1e-8,
+                  v0=matgen.start_vector(nx * ny, 1))
+    assert r.err == 0 and r.reason == 1 and r.nconv >= g["nev"]
+    assert r5(r.eigr[: g["nev"]]) == g["eigenvalues"]
+
+
+@pytest.mark.parametrize("key", ["test2_1", "test2_3"])
+def test_test2_golden(orc, key):
+    g = G[key]
+    csr = matgen.laplacian_1d(g["n"])
+    tol = max(1000 * EPS64, 1e-9)
+    for which, name in (("LR", "largest"), ("SR", "smallest")):
+        for lock in (True, False):
+            r = orc.solve(*csr, hermitian=True, which=which, nev=g["nev"], tol=tol, lock=lock,
+                          v0=matgen.start_vector(g["n"], 1))
+            assert r.err == 0 and r.reason == 1
+            assert r5(r.eigr[: g["nev"]]) == g[name]
+
+
+def test_ex9_golden(orc):
+    g = G["ex9_1"]
+    csr = matgen.brusselator(g["N"])
+    r = orc.solve(*csr, hermitian=False, which=g["which"], nev=g["nev"], tol=1e-8,
+                  v0=matgen.start_vector(2 * g["N"], 1))
+    assert r.err == 0 and r.reason == 1
+    assert [[round(a, 5), round(b, 5)] for a, b in zip(r.eigr[:4], r.eigi[:4])] == g["eigenvalues"]
+
+
+def test_convdiff_analytic(orc):
+    N, Pe = 40, 10.0
+    csr = matgen.convection_diffusion_2d(N, Pe)
+    r = orc.solve(*csr, hermitian=False, which="LR", nev=10, ncv=40, tol=1e-12, v0=matgen.start_vector(N * N, 3))
+    assert r.err == 0 and r.reason == 1
+    ex = matgen.convdiff_eigenvalues(N, Pe)
+    for lam in r.eigr:
+        assert np.min(np.abs(ex - lam)) / abs(lam) < 1e-10
+    assert np.max(np.abs(r.eigi)) == 0.0
+
+
+def test_lap3d_analytic_and_orthogonality(orc):
+    m = 12
+    csr = matgen.laplacian_3d(m)
+    r = orc.solve(*csr, hermitian=True, which="LR", nev=20, ncv=48, tol=1e-10, v0=matgen.start_vector(m ** 3, 2))
+    assert r.err == 0 and r.reason == 1
+    ex = matgen.laplacian_eigenvalues([m, m, m])
+    assert max(np.min(np.abs(ex - l)) / abs(l) for l in r.eigr) < 1e-12
+    assert np.abs(r.X.T @ r.X - np.eye(r.nconv)).max() < 1e-12
+    A = matgen.csr_to_dense(*csr)
+    res = [np.linalg.norm(A @ r.X[:, i] - r.eigr[i] * r.X[:, i]) / (np.linalg.norm(A, 2) * abs(r.eigr[i]))
+           for i in range(r.nconv)]
+    assert max(res) < 1e-10
+
+
+def test_dense_nhep_against_numpy(orc):
+    rng = np.random.default_rng(7)
+    for n in (5, 17, 40):
+        A = rng.standard_normal((n, n))
+        err, T, Q, wr, wi = orc.schur(A)
+        assert err == 0
+        assert np.abs(Q.T @ Q - np.eye(n)).max() < 1e-13
+        assert np.abs(A @ Q - Q @ T).max() < 1e-12 * np.abs(A).max() * n
+        ev = np.linalg.eigvals(A)
+        got = wr + 1j * wi
+        for z in got:
+            assert np.min(np.abs(ev - z)) < 1e-10 * max(1, abs(z))
+
+
+def test_zero_start_vector_is_an_error(orc):
+    csr = matgen.laplacian_1d(40)
+    r = orc.solve(*csr, hermitian=True, which="LM", nev=2, v0=np.zeros(40))
+    assert r.err != 0
+
+
+def test_spmv(orc):
+    csr = matgen.convection_diffusion_2d(20, 5.0)
+    x = matgen.start_vector(400, 9)
+    A = matgen.csr_to_dense(*csr)
+    assert np.allclose(orc.spmv(*csr, x), A @ x, rtol=0, atol=1e-14)
