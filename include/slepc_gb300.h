@@ -52,6 +52,20 @@ PetscErrorCode EPSGB300GetDeviceBasis(EPS eps, const double **V, PetscInt *ld);
 /* Orthogonality ||V^T V - I||_max of the first nconv columns, computed on the device in FP64. */
 PetscErrorCode EPSGB300OrthogonalityError(EPS eps, PetscReal *err);
 
+/* y[0..k) = V(:, 0:k)^T x, with V (n x k, column-major, leading dimension ldv, 16-byte aligned, ldv even), x (n) and
+ * y (k) all in device memory, computed by the same kernel and arithmetic as BVDotVec -- and allocating nothing.
+ * No counterpart in the reference.  It is for callers that cannot allocate device memory while they run: programs
+ * that reserve the GPU's memory up front for their own pool allocator, and time-critical loops that cannot take the
+ * implicit device synchronisation of cudaMalloc/cudaFree.  Its scratch (partial sums, counter, staging; 344,448
+ * bytes) is a fixed static device array that every GPU loading this library holds until the process exits; the
+ * first call on a device looks up that array's address, so make that first call before any stream capture.
+ * Limits: k <= 256 (larger k returns PETSC_ERR_ARG_OUTOFRANGE).  The call is asynchronous on `stream` (a
+ * cudaStream_t, NULL for the legacy default stream).  All calls share the one scratch array: calls that overlap on
+ * the GPU (different streams, or different host threads without ordering) race and must be serialised by the
+ * caller. */
+PetscErrorCode BVGB300DotVecNoAlloc(const double *V, PetscInt ldv, PetscInt n, PetscInt k, const double *x, double *y,
+                                    void *stream);
+
 #ifdef __cplusplus
 }
 #endif
