@@ -39,6 +39,9 @@ WORKLOADS = {
     "lap2d100": dict(desc="2-D 5-point Laplacian 100x100 (n=10000, nnz=49600), EPS_HEP, nev=10 largest magnitude, "
                           "ncv=32, tol=1e-8, start vector seed 1",
                      gen=lambda mg: mg.laplacian_2d(100), hermitian=True, which="LM", nev=10, ncv=32, tol=1e-8, seed=1),
+    "lap3d64": dict(desc="3-D 7-point Laplacian 64^3 (n=262144, nnz=1810432), EPS_HEP, nev=50 largest algebraic, "
+                         "ncv=128, tol=1e-10, start vector seed 2 (the 128^3 solve's shape at 1/8 size, for profiling)",
+                    gen=lambda mg: mg.laplacian_3d(64), hermitian=True, which="LR", nev=50, ncv=128, tol=1e-10, seed=2),
     "convdiff1000": dict(desc="2-D upwind convection-diffusion 1000x1000 (n=1e6), Peclet 10, EPS_NHEP, nev=20 "
                               "largest real, ncv=64, tol=1e-10, start vector seed 3",
                          gen=lambda mg: mg.convection_diffusion_2d(1000, 10.0), hermitian=False, which="LR", nev=20,
@@ -184,6 +187,8 @@ def main():
     ap.add_argument("--arith", default="pair", choices=["pair", "f64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--profile-case", action="store_true",
+                    help="run exactly one solve limited to 2 restarts and exit (the ncu capture case)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     wl = WORKLOADS[args.workload]
@@ -238,6 +243,12 @@ def main():
 
     A = sg.Mat(*csr)
     eps = make_eps(A)
+    if args.profile_case:
+        eps.setTolerances(wl["tol"], 2)
+        eps.setUp()
+        eps.solve()
+        print(json.dumps({"profile_case": args.workload, "stats": eps.getStats()}), flush=True)
+        return
     eps.setUp()
     for _ in range(args.warmup):
         eps.solve()

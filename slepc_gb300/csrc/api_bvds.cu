@@ -736,8 +736,12 @@ extern "C" PetscErrorCode EPSGetBV(EPS eps, BV *V) {
     KSG_TRY(BVCreate(0, &eps->bv));
     KSG_TRY(BVSetSizes(eps->bv, eps->n, eps->n, eps->ncv_e + 1));
   }
-  // expose the solver's basis: copy it into the BV (the BV owns its storage)
-  KSG_CUDA(cudaMemcpy(eps->bv->V.p, eps->V.p, sizeof(double) * eps->ldv * (eps->ncv_e + 1), cudaMemcpyDeviceToDevice));
+  // expose the solver's basis: copy (or convert from pairs) into the BV, which owns FP64 storage
+  if (eps->storage == STORE_PAIR)
+    KSG_CUDA(launch_pair_to_f64(reinterpret_cast<const float2 *>(eps->V.p), eps->bv->V.p, eps->ldv * (eps->ncv_e + 1), 0));
+  else
+    KSG_CUDA(cudaMemcpy(eps->bv->V.p, eps->V.p, sizeof(double) * eps->ldv * (eps->ncv_e + 1), cudaMemcpyDeviceToDevice));
+  KSG_CUDA(cudaDeviceSynchronize());
   eps->bv->l = 0;
   eps->bv->k = eps->solved ? eps->nconv : eps->ncv_e;
   *V = eps->bv;

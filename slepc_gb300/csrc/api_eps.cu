@@ -154,6 +154,47 @@ PetscErrorCode ksg_mat_upload(Mat A) {
   return 0;
 }
 
+PetscErrorCode ksg_mat_upload_pairs(Mat A) {
+  KSG_TRY(ksg_mat_upload(A));
+  if (A->d_va2.p || A->nnz == 0) return 0;
+  std::vector<float2> h(A->nnz);
+  for (long long p = 0; p < A->nnz; ++p) {
+    const float hi = (float)A->aa[p];
+    h[p] = make_float2(hi, (float)(A->aa[p] - (double)hi));
+  }
+  KSG_CUDA(A->d_va2.alloc(A->nnz));
+  KSG_CUDA(cudaMemcpy(A->d_va2.p, h.data(), sizeof(float2) * A->nnz, cudaMemcpyHostToDevice));
+  return 0;
+}
+
+PetscErrorCode ksg_put_column(void *dst, const double *src, int n, int storage, cudaStream_t s) {
+  if (storage == STORE_F64) {
+    KSG_CUDA(cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    return 0;
+  }
+  std::vector<float2> h(n);
+  for (int i = 0; i < n; ++i) {
+    const float hi = (float)src[i];
+    h[i] = make_float2(hi, (float)(src[i] - (double)hi));
+  }
+  KSG_CUDA(cudaMemcpyAsync(dst, h.data(), sizeof(float2) * n, cudaMemcpyHostToDevice, s));
+  KSG_CUDA(cudaStreamSynchronize(s));
+  return 0;
+}
+
+PetscErrorCode ksg_get_column(double *dst, const void *src, int n, int storage, cudaStream_t s) {
+  if (storage == STORE_F64) {
+    KSG_CUDA(cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    KSG_CUDA(cudaStreamSynchronize(s));
+    return 0;
+  }
+  std::vector<float2> h(n);
+  KSG_CUDA(cudaMemcpyAsync(h.data(), src, sizeof(float2) * n, cudaMemcpyDeviceToHost, s));
+  KSG_CUDA(cudaStreamSynchronize(s));
+  for (int i = 0; i < n; ++i) dst[i] = (double)h[i].x + (double)h[i].y;
+  return 0;
+}
+
 double ksg_mat_norm_inf(Mat A) {
   if (A->norm_inf >= 0.0) return A->norm_inf;
   double mx = 0.0;
@@ -339,9 +380,9 @@ extern "C" PetscErrorCode VecDestroy(Vec *v) {
 size_t ksg_part_stride(int ld) { return (size_t)2 * ld + 8; }
 size_t ksg_part_blocks(int n) { return (size_t)std::max(gs_dot_blocks(n), gs_update_blocks(n)); }
 
-PetscErrorCode ksg_orthonormalize_column(double *V, long long ldv, int n, int j, double *coef, float2 *part,
+PetscErrorCode ksg_orthonormalize_column(void *V, long long ldv, int n, int j, double *coef, float2 *part,
                                          int pstride, KrylovState *st, int arith, cudaStream_t s, double *nrm,
-                                         int *lindep, int refine) {
+                                         int *lindep, int refine, int storage) {
   StepArgs a = {};
   a.V = V;
   a.ldv = ldv;
@@ -349,7 +390,7 @@ PetscErrorCode ksg_orthonormalize_column(double *V, long long ldv, int n, int j,
   a.J = j;
   a.j = j;
   a.hermitian = 1;
-  a.U = V + (size_t)j * ldv;
+  a.U = static_cast<double *>(V) + (size_t)j * ldv;  // 8 bytes per entry in both formats
   a.W = nullptr;
   a.eta = 0.7071;
   a.coef = coef;
@@ -362,8 +403,8 @@ PetscErrorCode ksg_orthonormalize_column(double *V, long long ldv, int n, int j,
   int ld = 0;
   for (int pass = 0; pass < passes_max; ++pass) {
     KSG_CUDA(launch_segment_begin(st, j, j, s));
-    KSG_CUDA(launch_gs_dot(a, 1, GS_ORTHO, arith, s));
-    KSG_CUDA(launch_gs_update(a, 1, GS_ORTHO, arith, s));
+    KSG_CUDA(launch_gs_dot(a, 1, GS_ORTHO, arith, s, storage));
+    KSG_CUDA(launch_gs_update(a, 1, GS_ORTHO, arith, s, storage));
     KrylovState h;
     KSG_CUDA(cudaMemcpyAsync(&h, st, sizeof(h), cudaMemcpyDeviceToHost, s));
     KSG_CUDA(cudaStreamSynchronize(s));
@@ -705,7 +746,9 @@ extern "C" PetscErrorCode EPSSetUp(EPS eps) {
   KSG_CUDA(cudaMemsetAsync(eps->d.p, 0, sizeof(double) * eps->d.count, eps->stream));
   KSG_CUDA(cudaMemsetAsync(eps->e.p, 0, sizeof(double) * eps->e.count, eps->stream));
   if (!eps->h_ctl) KSG_CUDA(cudaMallocHost((void **)&eps->h_ctl, sizeof(KSControl)));
+  eps->storage = (eps->arith == ARITH_PAIR) ? STORE_PAIR : STORE_F64;
   KSG_TRY(ksg_mat_upload(eps->A));
+  if (eps->storage == STORE_PAIR) KSG_TRY(ksg_mat_upload_pairs(eps->A));
   // power-of-two operator scaling keeps every vector inside the range of the FP32-pair arithmetic; it is exact
   const double nrm = ksg_mat_norm_inf(eps->A);
   eps->opscale = 1.0;
@@ -812,8 +855,8 @@ static PetscErrorCode eps_factorize(EPS eps, int k0, int nv, double *bytes) {
     double *w = u + eps->ldv;
     {
       LaunchScope ls(eps, EPS_GB300_K_SPMV, spmv_bytes(eps));
-      KSG_CUDA(launch_spmv(eps->A->d_rp.p, eps->A->d_ci.p, eps->A->d_va.p, u, w, n, eps->lanes, eps->st.p,
-                           eps->opscale, s));
+      KSG_CUDA(launch_spmv_storage(eps->A->d_rp.p, eps->A->d_ci.p, eps->A->d_va.p, eps->A->d_va2.p, u, w, n,
+                                   eps->lanes, eps->st.p, eps->opscale, eps->storage, s));
     }
     a.J = j;
     a.j = j;
@@ -821,11 +864,11 @@ static PetscErrorCode eps_factorize(EPS eps, int k0, int nv, double *bytes) {
     a.W = w;
     {
       LaunchScope ls(eps, EPS_GB300_K_GS_DOT, colb * (j + 2));
-      KSG_CUDA(launch_gs_dot(a, 2, GS_STEP, eps->arith, s));
+      KSG_CUDA(launch_gs_dot(a, 2, GS_STEP, eps->arith, s, eps->storage));
     }
     {
       LaunchScope ls(eps, EPS_GB300_K_GS_UPDATE, colb * (j + 4));
-      KSG_CUDA(launch_gs_update(a, 2, GS_STEP, eps->arith, s));
+      KSG_CUDA(launch_gs_update(a, 2, GS_STEP, eps->arith, s, eps->storage));
     }
     *bytes += spmv_bytes(eps) + colb * (j + 2) + colb * (j + 4);
   }
@@ -835,11 +878,11 @@ static PetscErrorCode eps_factorize(EPS eps, int k0, int nv, double *bytes) {
   a.W = nullptr;
   {
     LaunchScope ls(eps, EPS_GB300_K_GS_DOT, colb * (nv + 1));
-    KSG_CUDA(launch_gs_dot(a, 1, GS_FINAL, eps->arith, s));
+    KSG_CUDA(launch_gs_dot(a, 1, GS_FINAL, eps->arith, s, eps->storage));
   }
   {
     LaunchScope ls(eps, EPS_GB300_K_GS_UPDATE, colb * (nv + 2));
-    KSG_CUDA(launch_gs_update(a, 1, GS_FINAL, eps->arith, s));
+    KSG_CUDA(launch_gs_update(a, 1, GS_FINAL, eps->arith, s, eps->storage));
   }
   *bytes += colb * (nv + 1) + colb * (nv + 2);
   eps->stats.kernel_launches += 1;  // segment begin
@@ -851,11 +894,11 @@ static PetscErrorCode eps_new_start_vector(EPS eps, int col, int *breakdown) {
   std::vector<double> h(eps->n);
   ksg_random_fill(h.data(), eps->n, eps->seed, ++eps->rng_counter);
   double *dst = eps->V.p + (size_t)col * eps->ldv;
-  KSG_CUDA(cudaMemcpyAsync(dst, h.data(), sizeof(double) * eps->n, cudaMemcpyHostToDevice, eps->stream));
+  KSG_TRY(ksg_put_column(dst, h.data(), eps->n, eps->storage, eps->stream));
   double nrm = 0.0;
   int ld = 0;
   KSG_TRY(ksg_orthonormalize_column(eps->V.p, eps->ldv, eps->n, col, eps->coef.p, eps->part.p, eps->pstride,
-                                    eps->st.p, eps->arith, eps->stream, &nrm, &ld, 2));
+                                    eps->st.p, eps->arith, eps->stream, &nrm, &ld, 2, eps->storage));
   *breakdown = ld || nrm == 0.0;
   return 0;
 }
@@ -934,11 +977,11 @@ extern "C" PetscErrorCode EPSSolve(EPS eps) {
       ksg_random_fill(h.data(), n, eps->seed, 0);
       src = h.data();
     }
-    KSG_CUDA(cudaMemcpyAsync(eps->V.p, src, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    KSG_TRY(ksg_put_column(eps->V.p, src, n, eps->storage, s));
     double nrm = 0.0;
     int lindep = 0;
     KSG_TRY(ksg_orthonormalize_column(eps->V.p, eps->ldv, n, 0, eps->coef.p, eps->part.p, eps->pstride, eps->st.p,
-                                      eps->arith, s, &nrm, &lindep, 1));
+                                      eps->arith, s, &nrm, &lindep, 1, eps->storage));
     KSG_CHECK(!lindep && nrm != 0.0, PETSC_ERR_PLIB, "Initial vector is zero or belongs to the deflation space");
   }
   KSG_CUDA(cudaMemsetAsync(eps->d.p, 0, sizeof(double) * eps->d.count, s));
@@ -993,7 +1036,8 @@ extern "C" PetscErrorCode EPSSolve(EPS eps) {
     // thick restart: V(:, nconv:k+l) = V(:, nconv:nv) Q(nconv:nv, nconv:k+l)
     {
       LaunchScope ls(eps, EPS_GB300_K_RESTART, 8.0 * n * ((nv - nconv) + (k + l - nconv)));
-      KSG_CUDA(launch_restart(eps->V.p, eps->ldv, n, nconv, nv - nconv, nconv, k + l - nconv, eps->Q.p, ld, eps->arith, s));
+      KSG_CUDA(launch_restart(eps->V.p, eps->ldv, n, nconv, nv - nconv, nconv, k + l - nconv, eps->Q.p, ld, eps->arith,
+                              s, eps->storage));
     }
     bytes += 8.0 * n * ((nv - nconv) + (k + l - nconv));
     if (reason == 0) {
@@ -1015,7 +1059,7 @@ extern "C" PetscErrorCode EPSSolve(EPS eps) {
   // non-Hermitian: eigenvectors of the leading Schur block, V = V X (EPSComputeVectors_Schur, epsdefault.c:105-169)
   if (!herm && nconv > 0) {
     KSG_CUDA(launch_nhep_vectors(eps->H.p, ld, nconv, eps->X.p, s));
-    KSG_CUDA(launch_restart(eps->V.p, eps->ldv, n, 0, nconv, 0, nconv, eps->X.p, ld, eps->arith, s));
+    KSG_CUDA(launch_restart(eps->V.p, eps->ldv, n, 0, nconv, 0, nconv, eps->X.p, ld, eps->arith, s, eps->storage));
     bytes += 16.0 * n * nconv;
   }
   std::vector<double> er(ld), ei(ld), es(ld);
@@ -1037,7 +1081,9 @@ extern "C" PetscErrorCode EPSSolve(EPS eps) {
       if (eps->r_eigi[i] < 0.0) {
         eps->r_eigi[i] = -eps->r_eigi[i];
         eps->r_eigi[i + 1] = -eps->r_eigi[i + 1];
-        KSG_CUDA(launch_scale(eps->V.p + (size_t)(i + 1) * eps->ldv, n, -1.0, s));
+        // negate a basis column: both halves of a pair, or the double
+        KSG_CUDA(launch_negate(eps->V.p + (size_t)(i + 1) * eps->ldv, eps->storage == STORE_PAIR ? 2 * n : n,
+                               eps->storage == STORE_PAIR, s));
       }
       i++;
     }
@@ -1100,17 +1146,18 @@ extern "C" PetscErrorCode EPSGetEigenvector(EPS eps, PetscInt i, Vec Vr, Vec Vi)
   const double ei = eps->r_eigi[k];
   const double *col = eps->V.p + (size_t)k * eps->ldv;
   const size_t bytes = sizeof(double) * n;
+  const int sto = eps->storage;
   if (ei > 0.0) {
-    if (Vr) KSG_CUDA(cudaMemcpy(Vr->a, col, bytes, cudaMemcpyDeviceToHost));
-    if (Vi) KSG_CUDA(cudaMemcpy(Vi->a, col + eps->ldv, bytes, cudaMemcpyDeviceToHost));
+    if (Vr) KSG_TRY(ksg_get_column(Vr->a, col, n, sto, eps->stream));
+    if (Vi) KSG_TRY(ksg_get_column(Vi->a, col + eps->ldv, n, sto, eps->stream));
   } else if (ei < 0.0) {
-    if (Vr) KSG_CUDA(cudaMemcpy(Vr->a, col - eps->ldv, bytes, cudaMemcpyDeviceToHost));
+    if (Vr) KSG_TRY(ksg_get_column(Vr->a, col - eps->ldv, n, sto, eps->stream));
     if (Vi) {
-      KSG_CUDA(cudaMemcpy(Vi->a, col, bytes, cudaMemcpyDeviceToHost));
+      KSG_TRY(ksg_get_column(Vi->a, col, n, sto, eps->stream));
       for (int r = 0; r < n; ++r) Vi->a[r] = -Vi->a[r];
     }
   } else {
-    if (Vr) KSG_CUDA(cudaMemcpy(Vr->a, col, bytes, cudaMemcpyDeviceToHost));
+    if (Vr) KSG_TRY(ksg_get_column(Vr->a, col, n, sto, eps->stream));
     if (Vi) memset(Vi->a, 0, bytes);
   }
   return 0;
@@ -1173,12 +1220,22 @@ extern "C" PetscErrorCode EPSComputeError(EPS eps, PetscInt i, EPSErrorType type
     x = x - eps->ldv;
     ki = -ki;  // the stored pair is (x, xi) for the eigenvalue with positive imaginary part
   }
-  DBuf<double> y, yi, part;
+  DBuf<double> y, yi, part, xd, xid;
   const int blocks = std::min(1024, (n + 255) / 256);
   KSG_CUDA(y.alloc(n));
   if (xi) KSG_CUDA(yi.alloc(n));
   KSG_CUDA(part.alloc(2 * blocks));
   cudaStream_t s = eps->stream;
+  if (eps->storage == STORE_PAIR) {
+    KSG_CUDA(xd.alloc(n));
+    KSG_CUDA(launch_pair_to_f64(reinterpret_cast<const float2 *>(x), xd.p, n, s));
+    x = xd.p;
+    if (xi) {
+      KSG_CUDA(xid.alloc(n));
+      KSG_CUDA(launch_pair_to_f64(reinterpret_cast<const float2 *>(xi), xid.p, n, s));
+      xi = xid.p;
+    }
+  }
   KSG_CUDA(launch_spmv(eps->A->d_rp.p, eps->A->d_ci.p, eps->A->d_va.p, x, y.p, n, eps->lanes, nullptr, 1.0, s));
   if (xi) KSG_CUDA(launch_spmv(eps->A->d_rp.p, eps->A->d_ci.p, eps->A->d_va.p, xi, yi.p, n, eps->lanes, nullptr, 1.0, s));
   k_residual<<<blocks, 256, 0, s>>>(y.p, xi ? yi.p : nullptr, x, xi, kr, ki, n, part.p);
@@ -1238,7 +1295,8 @@ extern "C" PetscErrorCode EPSGB300OrthogonalityError(EPS eps, PetscReal *err) {
     a.J = j;
     a.j = j;
     a.U = eps->V.p + (size_t)j * eps->ldv;
-    KSG_CUDA(launch_gs_dot(a, 1, GS_DOTS, ARITH_F64, eps->stream));
+    KSG_CUDA(launch_gs_dot(a, 1, GS_DOTS, eps->storage == STORE_PAIR ? ARITH_PAIR : ARITH_F64, eps->stream,
+                           eps->storage));
     KSG_CUDA(cudaMemcpyAsync(h.data(), eps->coef.p, sizeof(double) * (j + 1), cudaMemcpyDeviceToHost, eps->stream));
     KSG_CUDA(cudaStreamSynchronize(eps->stream));
     for (int i = 0; i < j; ++i) worst = std::max(worst, fabs(h[i]));

@@ -71,6 +71,7 @@ struct _p_Mat {
   // device copy of the CSR arrays (uploaded on first use by a solver)
   DBuf<int> d_rp, d_ci;
   DBuf<double> d_va;
+  DBuf<float2> d_va2;  // values as FP32 pairs, for the pair-storage SpMV
   int device_ready = 0;
   double norm_inf = -1.0;
 };
@@ -102,6 +103,7 @@ struct _p_EPS {
   int lock = 1;
   int extraction = 0;
   int arith = ksg::ARITH_PAIR;
+  int storage = ksg::STORE_PAIR;  // basis format: pairs with pair arithmetic, doubles with FP64 arithmetic
   int device = -1;
   std::vector<double> v0;
   unsigned long long seed = 0x5EEDULL;
@@ -140,8 +142,13 @@ struct _p_EPS {
 
 // run the Gram-Schmidt pair kernels on one column (orthonormalise u = V[:, j] against V[:, 0:j]); returns the
 // norm of the orthogonalised vector in *nrm and the linear-dependence flag (two CGS passes)
-PetscErrorCode ksg_orthonormalize_column(double *V, long long ldv, int n, int j, double *coef, float2 *part,
+PetscErrorCode ksg_orthonormalize_column(void *V, long long ldv, int n, int j, double *coef, float2 *part,
                                          int pstride, ksg::KrylovState *st, int arith, cudaStream_t s, double *nrm,
-                                         int *lindep, int refine);
+                                         int *lindep, int refine, int storage = ksg::STORE_F64);
+PetscErrorCode ksg_mat_upload_pairs(Mat A);
+// host -> device copy of a double vector into a basis column of the given storage format
+PetscErrorCode ksg_put_column(void *dst, const double *src, int n, int storage, cudaStream_t s);
+// device basis column -> host doubles
+PetscErrorCode ksg_get_column(double *dst, const void *src, int n, int storage, cudaStream_t s);
 size_t ksg_part_stride(int ld);
 size_t ksg_part_blocks(int n);

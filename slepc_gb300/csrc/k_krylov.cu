@@ -15,6 +15,8 @@
 #include "kernels.h"
 #include "ks_types.h"
 
+#include <algorithm>
+
 namespace ksg {
 
 // ------------------------------------------------------------------------------------------------------------
@@ -53,6 +55,76 @@ struct F64Ar {
   static KS_DEVICE acc unpack(unsigned long long u) { return __longlong_as_double((long long)u); }
 };
 
+// ------------------------------------------------------------------------------------------------------------
+// Basis storage formats.  StF64: IEEE doubles.  StPair: FP32 pairs (hi, lo) with hi + lo the stored value (47-bit
+// significand, the same 8 bytes per entry), so the pair arithmetic reads them without any conversion.
+// load2 reads entries i and i+1 (i even, 16-byte aligned) in one vector load that bypasses L1 residency.
+// ------------------------------------------------------------------------------------------------------------
+struct StF64 {
+  using T = double;
+  template <class Ar>
+  static KS_DEVICE void load2(const T *p, typename Ar::val &a, typename Ar::val &b) {
+    const double2 v = __ldcs(reinterpret_cast<const double2 *>(p));
+    a = Ar::cvt(v.x);
+    b = Ar::cvt(v.y);
+  }
+  template <class Ar>
+  static KS_DEVICE typename Ar::val load1(const T *p) { return Ar::cvt(*p); }
+  static KS_DEVICE double get(const T *p) { return *p; }
+  static KS_DEVICE void put(T *p, double v) { *p = v; }
+  static KS_DEVICE void get2(const T *p, double &a, double &b) {
+    const double2 v = *reinterpret_cast<const double2 *>(p);
+    a = v.x;
+    b = v.y;
+  }
+  static KS_DEVICE void put2(T *p, double a, double b) { *reinterpret_cast<double2 *>(p) = make_double2(a, b); }
+};
+
+struct StPair {
+  using T = float2;
+  template <class Ar>
+  static KS_DEVICE void load2(const T *p, typename Ar::val &a, typename Ar::val &b) {
+    const float4 v = __ldcs(reinterpret_cast<const float4 *>(p));
+    a = pair_val<Ar>(v.x, v.y);
+    b = pair_val<Ar>(v.z, v.w);
+  }
+  template <class Ar>
+  static KS_DEVICE typename Ar::val load1(const T *p) {
+    const float2 v = *p;
+    return pair_val<Ar>(v.x, v.y);
+  }
+  template <class Ar>
+  static KS_DEVICE typename Ar::val pair_val(float hi, float lo);
+  static KS_DEVICE double get(const T *p) {
+    const float2 v = *p;
+    return (double)v.x + (double)v.y;
+  }
+  static KS_DEVICE void put(T *p, double v) {
+    const f2x s = split_f64(v);
+    *p = make_float2(s.hi, s.lo);
+  }
+  static KS_DEVICE void get2(const T *p, double &a, double &b) {
+    const float4 v = *reinterpret_cast<const float4 *>(p);
+    a = (double)v.x + (double)v.y;
+    b = (double)v.z + (double)v.w;
+  }
+  static KS_DEVICE void put2(T *p, double a, double b) {
+    const f2x x = split_f64(a), y = split_f64(b);
+    *reinterpret_cast<float4 *>(p) = make_float4(x.hi, x.lo, y.hi, y.lo);
+  }
+};
+template <>
+KS_DEVICE PairAr::val StPair::pair_val<PairAr>(float hi, float lo) {
+  f2x r;
+  r.hi = hi;
+  r.lo = lo;
+  return r;
+}
+template <>
+KS_DEVICE F64Ar::val StPair::pair_val<F64Ar>(float hi, float lo) {
+  return (double)hi + (double)lo;
+}
+
 template <class Ar>
 KS_DEVICE typename Ar::acc warp_reduce(typename Ar::acc a) {
 #pragma unroll
@@ -71,10 +143,11 @@ enum { TK_DOT = 0, TK_UPD = 1, TK_NRM = 2 };
 // ------------------------------------------------------------------------------------------------------------
 // SpMV: LANES threads per row, FP64 FMA.  Each warp owns 32/LANES consecutive rows per iteration.
 // ------------------------------------------------------------------------------------------------------------
-template <int LANES>
+template <int LANES, class S>
 __global__ void __launch_bounds__(256) k_spmv(const int *__restrict__ rp, const int *__restrict__ ci,
-                                              const double *__restrict__ va, const double *__restrict__ x,
-                                              double *__restrict__ y, int n, const KrylovState *st, double scale) {
+                                              const double *__restrict__ va, const typename S::T *__restrict__ x,
+                                              typename S::T *__restrict__ y, int n, const KrylovState *st,
+                                              double scale) {
   if (st && st->stop) return;
   const double sc = st ? st->sigma * scale : scale;
   constexpr int RPW = 32 / LANES;
@@ -90,11 +163,75 @@ __global__ void __launch_bounds__(256) k_spmv(const int *__restrict__ rp, const 
       p1 = rp[row + 1];
     }
     double sum = 0.0;
-    for (int p = p0 + sub; p < p1; p += LANES) sum = ::fma(va[p], __ldg(x + ci[p]), sum);
+    for (int p = p0 + sub; p < p1; p += LANES) sum = ::fma(va[p], S::get(x + ci[p]), sum);
 #pragma unroll
     for (int off = LANES / 2; off > 0; off >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, off, LANES);
-    if (sub == 0 && row < n) y[row] = sum * sc;
+    if (sub == 0 && row < n) S::put(y + row, sum * sc);
   }
+}
+
+// SpMV for pair storage: matrix values pre-split into pairs, x gathered as pairs, products and sums in pair
+// arithmetic, the scale applied as a pair product; nothing touches the FP64 pipe.
+template <int LANES>
+__global__ void __launch_bounds__(256) k_spmv_pair(const int *__restrict__ rp, const int *__restrict__ ci,
+                                                   const float2 *__restrict__ va, const float2 *__restrict__ x,
+                                                   float2 *__restrict__ y, int n, const KrylovState *st,
+                                                   double scale) {
+  if (st && st->stop) return;
+  const f2x sc = split_f64(st ? st->sigma * scale : scale);
+  constexpr int RPW = 32 / LANES;
+  const int lane = threadIdx.x & 31;
+  const int sub = lane % LANES, grp = lane / LANES;
+  const long long warp_global = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long base = warp_global * RPW; base < n; base += nwarps * RPW) {
+    const long long row = base + grp;
+    int p0 = 0, p1 = 0;
+    if (row < n) {
+      p0 = rp[row];
+      p1 = rp[row + 1];
+    }
+    dfacc acc;
+    acc_zero(acc);
+    for (int p = p0 + sub; p < p1; p += LANES) {
+      const float2 av = __ldg(va + p), xv = __ldg(x + __ldg(ci + p));
+      f2x a2, x2;
+      a2.hi = av.x; a2.lo = av.y;
+      x2.hi = xv.x; x2.lo = xv.y;
+      acc_fma(acc, a2, x2);
+    }
+#pragma unroll
+    for (int off = LANES / 2; off > 0; off >>= 1) {
+      dfacc o;
+      o.s = __shfl_down_sync(0xffffffffu, acc.s, off, LANES);
+      o.c = __shfl_down_sync(0xffffffffu, acc.c, off, LANES);
+      acc_merge(acc, o);
+    }
+    if (sub == 0 && row < n) {
+      // renormalise (s, c) into a pair, then multiply by the scale as pairs
+      f2x v;
+      v.hi = acc.s + acc.c;
+      v.lo = acc.c - (v.hi - acc.s);
+      dfacc pr;
+      acc_zero(pr);
+      acc_fma(pr, v, sc);
+      const float hi = pr.s + pr.c;
+      y[row] = make_float2(hi, pr.c - (hi - pr.s));
+    }
+  }
+}
+
+__global__ void k_f64_to_pair(const double *x, float2 *y, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double v = x[i];
+    const float hi = __double2float_rn(v);
+    y[i] = make_float2(hi, __double2float_rn(v - (double)hi));
+  }
+}
+
+__global__ void k_pair_to_f64(const float2 *x, double *y, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    y[i] = (double)x[i].x + (double)x[i].y;
 }
 
 // ------------------------------------------------------------------------------------------------------------
@@ -217,7 +354,7 @@ __device__ void gs_epilogue(const StepArgs &a, const double *res, int mode) {
   for (int i = tid; i < J; i += blockDim.x) a.coef[J + i] = res[i * NX + 1] - tau * a.coef[i];
 }
 
-template <int NX, int CPW, class Ar>
+template <int NX, int CPW, class Ar, class S>
 __global__ void __launch_bounds__(A_THREADS, 1) k_gs_dot(StepArgs a, int mode) {
   KrylovState *st = a.st;
   if (st->stop) return;
@@ -230,8 +367,10 @@ __global__ void __launch_bounds__(A_THREADS, 1) k_gs_dot(StepArgs a, int mode) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int n = a.n, J = a.J;
   const double sigma = st->sigma;
-  const double *U = a.U;
-  const double *W = a.W;
+  using ST = typename S::T;
+  const ST *Vb = static_cast<const ST *>(a.V);
+  const ST *U = static_cast<const ST *>(a.U);
+  const ST *W = static_cast<const ST *>(a.W);
   acc cacc[CPW][NX];
 #pragma unroll
   for (int k = 0; k < CPW; ++k)
@@ -242,14 +381,16 @@ __global__ void __launch_bounds__(A_THREADS, 1) k_gs_dot(StepArgs a, int mode) {
   Ar::zero(sc1);
   Ar::zero(sc2);
   const int ntiles = (n + A_TILE - 1) / A_TILE;
+  val na[8], nb[8];
+  bool have_next = false;
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const int r0 = t * A_TILE;
     const int rows = min(A_TILE, n - r0);
     {
       double u = 0.0, w = 0.0;
       if (tid < rows) {
-        u = U[r0 + tid] * sigma;
-        if (NX == 2) w = W[r0 + tid];
+        u = S::get(U + r0 + tid) * sigma;
+        if (NX == 2) w = S::get(W + r0 + tid);
       }
       const val us = Ar::cvt(u);
       sx[0][tid] = us;
@@ -263,23 +404,43 @@ __global__ void __launch_bounds__(A_THREADS, 1) k_gs_dot(StepArgs a, int mode) {
     }
     __syncthreads();
     if (rows == A_TILE) {
+      // software pipeline: the column of the next (k+1) iteration -- or the first column of this warp in the
+      // block's next tile -- is loaded before the current column is consumed
+      if (!have_next && warp < J) {
+        const ST *col = Vb + (size_t)warp * a.ldv + r0 + lane * 2;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) S::template load2<Ar>(col + 64 * i, na[i], nb[i]);
+      }
+      have_next = false;
 #pragma unroll
       for (int k = 0; k < CPW; ++k) {
         const int c = warp + k * A_WARPS;
         if (c < J) {
-          const double *col = a.V + (size_t)c * a.ldv + r0 + lane * 2;
-          double2 v[8];
+          val ca[8], cb[8];
 #pragma unroll
-          for (int i = 0; i < 8; ++i) v[i] = ld_stream2(col + 64 * i);
+          for (int i = 0; i < 8; ++i) {
+            ca[i] = na[i];
+            cb[i] = nb[i];
+          }
+          int cn = c + A_WARPS, tn = t;
+          if (cn >= J) {
+            cn = warp;
+            tn = t + gridDim.x;
+          }
+          if (tn < ntiles && (tn + 1) * A_TILE <= n) {
+            const ST *col = Vb + (size_t)cn * a.ldv + (size_t)tn * A_TILE + lane * 2;
+#pragma unroll
+            for (int i = 0; i < 8; ++i) S::template load2<Ar>(col + 64 * i, na[i], nb[i]);
+            if (tn != t) have_next = true;
+          }
 #pragma unroll
           for (int i = 0; i < 8; ++i) {
             const int rr = lane * 2 + 64 * i;
-            const val a0 = Ar::cvt(v[i].x), a1 = Ar::cvt(v[i].y);
-            Ar::fma(cacc[k][0], a0, sx[0][rr]);
-            Ar::fma(cacc[k][0], a1, sx[0][rr + 1]);
+            Ar::fma(cacc[k][0], ca[i], sx[0][rr]);
+            Ar::fma(cacc[k][0], cb[i], sx[0][rr + 1]);
             if (NX == 2) {
-              Ar::fma(cacc[k][NX - 1], a0, sx[NX - 1][rr]);
-              Ar::fma(cacc[k][NX - 1], a1, sx[NX - 1][rr + 1]);
+              Ar::fma(cacc[k][NX - 1], ca[i], sx[NX - 1][rr]);
+              Ar::fma(cacc[k][NX - 1], cb[i], sx[NX - 1][rr + 1]);
             }
           }
         }
@@ -289,9 +450,9 @@ __global__ void __launch_bounds__(A_THREADS, 1) k_gs_dot(StepArgs a, int mode) {
       for (int k = 0; k < CPW; ++k) {
         const int c = warp + k * A_WARPS;
         if (c < J) {
-          const double *col = a.V + (size_t)c * a.ldv + r0;
+          const ST *col = Vb + (size_t)c * a.ldv + r0;
           for (int rr = lane; rr < rows; rr += 32) {
-            const val a0 = Ar::cvt(col[rr]);
+            const val a0 = S::template load1<Ar>(col + rr);
             Ar::fma(cacc[k][0], a0, sx[0][rr]);
             if (NX == 2) Ar::fma(cacc[k][NX - 1], a0, sx[NX - 1][rr]);
           }
@@ -358,7 +519,7 @@ __global__ void __launch_bounds__(A_THREADS, 1) k_gs_dot(StepArgs a, int mode) {
 constexpr int B_THREADS = 256;
 constexpr int B_TILE = 2 * B_THREADS;
 
-template <int NX, class Ar>
+template <int NX, class Ar, class S>
 __global__ void __launch_bounds__(B_THREADS) k_gs_update(StepArgs a, int mode) {
   KrylovState *st = a.st;
   if (st->stop) return;
@@ -373,8 +534,10 @@ __global__ void __launch_bounds__(B_THREADS) k_gs_update(StepArgs a, int mode) {
   for (int i = tid; i < NX * J; i += B_THREADS) cs[i] = Ar::cvt(a.coef[i]);
   __syncthreads();
   const double sigma = st->sigma, invnu = st->invnu, tsig = st->tau_sigma;
-  double *U = a.U;
-  double *W = a.W;
+  using ST = typename S::T;
+  const ST *Vb = static_cast<const ST *>(a.V);
+  ST *U = static_cast<ST *>(a.U);
+  ST *W = static_cast<ST *>(a.W);
   acc nrm;
   Ar::zero(nrm);
   const int ntiles = (n + B_TILE - 1) / B_TILE;
@@ -386,45 +549,43 @@ __global__ void __launch_bounds__(B_THREADS) k_gs_update(StepArgs a, int mode) {
       Ar::zero(s1);
       Ar::zero(g0);
       Ar::zero(g1);
-      const double *col = a.V + r;
-      int c = 0;
-      for (; c + 4 <= J; c += 4) {
-        double2 v[4];
+      const ST *col = Vb + r;
+      // groups of 8 columns, the next group's loads in flight while the current one is consumed
+      val xa[8], xb[8];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) v[q] = ld_stream2(col + (size_t)(c + q) * a.ldv);
+      for (int q = 0; q < 8; ++q)
+        if (q < J) S::template load2<Ar>(col + (size_t)q * a.ldv, xa[q], xb[q]);
+      for (int c0 = 0; c0 < J; c0 += 8) {
+        val ca[8], cb[8];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const val v0 = Ar::cvt(v[q].x), v1 = Ar::cvt(v[q].y);
-          Ar::fma(s0, v0, cs[c + q]);
-          Ar::fma(s1, v1, cs[c + q]);
-          if (NX == 2) {
-            Ar::fma(g0, v0, cs[J + c + q]);
-            Ar::fma(g1, v1, cs[J + c + q]);
+        for (int q = 0; q < 8; ++q) {
+          ca[q] = xa[q];
+          cb[q] = xb[q];
+        }
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+          if (c0 + 8 + q < J) S::template load2<Ar>(col + (size_t)(c0 + 8 + q) * a.ldv, xa[q], xb[q]);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          if (c0 + q < J) {
+            Ar::fma(s0, ca[q], cs[c0 + q]);
+            Ar::fma(s1, cb[q], cs[c0 + q]);
+            if (NX == 2) {
+              Ar::fma(g0, ca[q], cs[J + c0 + q]);
+              Ar::fma(g1, cb[q], cs[J + c0 + q]);
+            }
           }
         }
       }
-      for (; c < J; ++c) {
-        const double2 v = ld_stream2(col + (size_t)c * a.ldv);
-        const val v0 = Ar::cvt(v.x), v1 = Ar::cvt(v.y);
-        Ar::fma(s0, v0, cs[c]);
-        Ar::fma(s1, v1, cs[c]);
-        if (NX == 2) {
-          Ar::fma(g0, v0, cs[J + c]);
-          Ar::fma(g1, v1, cs[J + c]);
-        }
-      }
-      const double2 u = *reinterpret_cast<const double2 *>(U + r);
-      double2 vo;
-      vo.x = (sigma * u.x - Ar::value(s0)) * invnu;
-      vo.y = (sigma * u.y - Ar::value(s1)) * invnu;
-      *reinterpret_cast<double2 *>(U + r) = vo;
+      double ux, uy;
+      S::get2(U + r, ux, uy);
+      S::put2(U + r, (sigma * ux - Ar::value(s0)) * invnu, (sigma * uy - Ar::value(s1)) * invnu);
       if (NX == 2) {
-        const double2 w = *reinterpret_cast<const double2 *>(W + r);
-        double2 wo;
-        wo.x = w.x - Ar::value(g0) - tsig * u.x;
-        wo.y = w.y - Ar::value(g1) - tsig * u.y;
-        *reinterpret_cast<double2 *>(W + r) = wo;
-        const val w0 = Ar::cvt(wo.x), w1 = Ar::cvt(wo.y);
+        double wx, wy;
+        S::get2(W + r, wx, wy);
+        const double ox = wx - Ar::value(g0) - tsig * ux, oy = wy - Ar::value(g1) - tsig * uy;
+        S::put2(W + r, ox, oy);
+        const val w0 = Ar::cvt(ox), w1 = Ar::cvt(oy);
         Ar::fma(nrm, w0, w0);
         Ar::fma(nrm, w1, w1);
       }
@@ -433,15 +594,15 @@ __global__ void __launch_bounds__(B_THREADS) k_gs_update(StepArgs a, int mode) {
       Ar::zero(s0);
       Ar::zero(g0);
       for (int c = 0; c < J; ++c) {
-        const val v0 = Ar::cvt(a.V[r + (size_t)c * a.ldv]);
+        const val v0 = S::template load1<Ar>(Vb + r + (size_t)c * a.ldv);
         Ar::fma(s0, v0, cs[c]);
         if (NX == 2) Ar::fma(g0, v0, cs[J + c]);
       }
-      const double u = U[r];
-      U[r] = (sigma * u - Ar::value(s0)) * invnu;
+      const double u = S::get(U + r);
+      S::put(U + r, (sigma * u - Ar::value(s0)) * invnu);
       if (NX == 2) {
-        const double wo = W[r] - Ar::value(g0) - tsig * u;
-        W[r] = wo;
+        const double wo = S::get(W + r) - Ar::value(g0) - tsig * u;
+        S::put(W + r, wo);
         const val w0 = Ar::cvt(wo);
         Ar::fma(nrm, w0, w0);
       }
@@ -496,9 +657,9 @@ constexpr int R_THREADS = 256;
 constexpr int R_ROWS = 32;
 constexpr int R_MAXN = 144;
 
-template <class Ar>
-__global__ void __launch_bounds__(R_THREADS, 1) k_restart(double *V, long long ldv, int n, int a0, int K, int s0,
-                                                          int N, const double *Q, int ldq) {
+template <class Ar, class S>
+__global__ void __launch_bounds__(R_THREADS, 1) k_restart(typename S::T *V, long long ldv, int n, int a0, int K,
+                                                          int s0, int N, const double *Q, int ldq) {
   using val = typename Ar::val;
   using acc = typename Ar::acc;
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -518,7 +679,7 @@ __global__ void __launch_bounds__(R_THREADS, 1) k_restart(double *V, long long l
     __syncthreads();
     for (int i = tid; i < K * R_ROWS; i += R_THREADS) {
       const int k = i / R_ROWS, r = i % R_ROWS;
-      Vt[i] = Ar::cvt(r < rows ? V[(r0 + r) + (size_t)(a0 + k) * ldv] : 0.0);
+      Vt[i] = (r < rows) ? S::template load1<Ar>(V + (r0 + r) + (size_t)(a0 + k) * ldv) : Ar::cvt(0.0);
     }
     __syncthreads();
     acc o0[CQ], o1[CQ];
@@ -544,8 +705,8 @@ __global__ void __launch_bounds__(R_THREADS, 1) k_restart(double *V, long long l
     for (int q = 0; q < CQ; ++q) {
       const int c = tx + 16 * q;
       if (c < N) {
-        if (2 * ty < rows) V[(r0 + 2 * ty) + (size_t)(s0 + c) * ldv] = Ar::value(o0[q]);
-        if (2 * ty + 1 < rows) V[(r0 + 2 * ty + 1) + (size_t)(s0 + c) * ldv] = Ar::value(o1[q]);
+        if (2 * ty < rows) S::put(V + (r0 + 2 * ty) + (size_t)(s0 + c) * ldv, Ar::value(o0[q]));
+        if (2 * ty + 1 < rows) S::put(V + (r0 + 2 * ty + 1) + (size_t)(s0 + c) * ldv, Ar::value(o1[q]));
       }
     }
   }
@@ -573,6 +734,15 @@ __global__ void k_set_scales(KrylovState *st, double sigma, double invnu) {
   st->stop = 0;
 }
 
+__global__ void k_negate(double *x, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    x[i] = -x[i];
+}
+__global__ void k_negate_f32(float *x, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    x[i] = -x[i];
+}
+
 __global__ void k_scale_col(double *x, int n, double alpha) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
     x[i] *= alpha;
@@ -593,28 +763,74 @@ int num_sms() {
   return g_num_sms;
 }
 
+// threads per row: one thread per row for short rows (one FP64/pair FMA per nonzero, no shuffles), wider groups
+// for long rows
 int spmv_lanes_for(double avg_nnz) {
-  int lanes = 1;
-  while (lanes < 32 && lanes < avg_nnz) lanes <<= 1;
-  return lanes;
+  if (avg_nnz <= 16.0) return 1;
+  if (avg_nnz <= 64.0) return 8;
+  return 32;
+}
+
+template <class S>
+static void spmv_dispatch(const int *rp, const int *ci, const double *va, const void *x, void *y, int n, int lanes,
+                          const KrylovState *st, double scale, int blocks, cudaStream_t s) {
+  using T = typename S::T;
+  const T *xx = static_cast<const T *>(x);
+  T *yy = static_cast<T *>(y);
+  switch (lanes) {
+    case 1: k_spmv<1, S><<<blocks, 256, 0, s>>>(rp, ci, va, xx, yy, n, st, scale); break;
+    case 2: k_spmv<2, S><<<blocks, 256, 0, s>>>(rp, ci, va, xx, yy, n, st, scale); break;
+    case 4: k_spmv<4, S><<<blocks, 256, 0, s>>>(rp, ci, va, xx, yy, n, st, scale); break;
+    case 8: k_spmv<8, S><<<blocks, 256, 0, s>>>(rp, ci, va, xx, yy, n, st, scale); break;
+    case 16: k_spmv<16, S><<<blocks, 256, 0, s>>>(rp, ci, va, xx, yy, n, st, scale); break;
+    default: k_spmv<32, S><<<blocks, 256, 0, s>>>(rp, ci, va, xx, yy, n, st, scale); break;
+  }
+}
+
+static int spmv_blocks(int n, int lanes) {
+  const long long rows_per_block = (256 / 32) * (32 / lanes);
+  long long blocks = (n + rows_per_block - 1) / rows_per_block;
+  const long long cap = (long long)num_sms() * 16;
+  if (blocks > cap) blocks = cap;
+  return blocks < 1 ? 1 : (int)blocks;
 }
 
 cudaError_t launch_spmv(const int *rp, const int *ci, const double *va, const double *x, double *y, int n, int lanes,
                         const KrylovState *st, double scale, cudaStream_t s) {
-  const int threads = 256;
-  long long rows_per_block = (threads / 32) * (32 / lanes);
-  long long blocks = (n + rows_per_block - 1) / rows_per_block;
-  long long cap = (long long)num_sms() * 8;
-  if (blocks > cap) blocks = cap;
-  if (blocks < 1) blocks = 1;
-  switch (lanes) {
-    case 1: k_spmv<1><<<(int)blocks, threads, 0, s>>>(rp, ci, va, x, y, n, st, scale); break;
-    case 2: k_spmv<2><<<(int)blocks, threads, 0, s>>>(rp, ci, va, x, y, n, st, scale); break;
-    case 4: k_spmv<4><<<(int)blocks, threads, 0, s>>>(rp, ci, va, x, y, n, st, scale); break;
-    case 8: k_spmv<8><<<(int)blocks, threads, 0, s>>>(rp, ci, va, x, y, n, st, scale); break;
-    case 16: k_spmv<16><<<(int)blocks, threads, 0, s>>>(rp, ci, va, x, y, n, st, scale); break;
-    default: k_spmv<32><<<(int)blocks, threads, 0, s>>>(rp, ci, va, x, y, n, st, scale); break;
+  spmv_dispatch<StF64>(rp, ci, va, x, y, n, lanes, st, scale, spmv_blocks(n, lanes), s);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_spmv_storage(const int *rp, const int *ci, const double *va, const float2 *va_pair, const void *x,
+                                void *y, int n, int lanes, const KrylovState *st, double scale, int storage,
+                                cudaStream_t s) {
+  const int blocks = spmv_blocks(n, lanes);
+  if (storage == STORE_F64) {
+    spmv_dispatch<StF64>(rp, ci, va, x, y, n, lanes, st, scale, blocks, s);
+  } else {
+    const float2 *xx = static_cast<const float2 *>(x);
+    float2 *yy = static_cast<float2 *>(y);
+    switch (lanes) {
+      case 1: k_spmv_pair<1><<<blocks, 256, 0, s>>>(rp, ci, va_pair, xx, yy, n, st, scale); break;
+      case 2: k_spmv_pair<2><<<blocks, 256, 0, s>>>(rp, ci, va_pair, xx, yy, n, st, scale); break;
+      case 4: k_spmv_pair<4><<<blocks, 256, 0, s>>>(rp, ci, va_pair, xx, yy, n, st, scale); break;
+      case 8: k_spmv_pair<8><<<blocks, 256, 0, s>>>(rp, ci, va_pair, xx, yy, n, st, scale); break;
+      case 16: k_spmv_pair<16><<<blocks, 256, 0, s>>>(rp, ci, va_pair, xx, yy, n, st, scale); break;
+      default: k_spmv_pair<32><<<blocks, 256, 0, s>>>(rp, ci, va_pair, xx, yy, n, st, scale); break;
+    }
   }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_f64_to_pair(const double *x, float2 *y, long long n, cudaStream_t s) {
+  int blocks = (int)std::min<long long>((n + 255) / 256, (long long)num_sms() * 8);
+  k_f64_to_pair<<<blocks < 1 ? 1 : blocks, 256, 0, s>>>(x, y, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pair_to_f64(const float2 *x, double *y, long long n, cudaStream_t s) {
+  int blocks = (int)std::min<long long>((n + 255) / 256, (long long)num_sms() * 8);
+  k_pair_to_f64<<<blocks < 1 ? 1 : blocks, 256, 0, s>>>(x, y, n);
   return cudaGetLastError();
 }
 
@@ -627,48 +843,55 @@ int gs_dot_blocks(int n) {
 
 int gs_update_blocks(int n) {
   const int ntiles = (n + B_TILE - 1) / B_TILE;
-  int blocks = num_sms() * 6;
+  int blocks = num_sms() * 2;  // two resident blocks per SM at ~120 registers per thread; persistent over tiles
   if (blocks > ntiles) blocks = ntiles;
   return blocks < 1 ? 1 : blocks;
 }
 
 int gs_max_columns() { return A_MAXJ; }
 
-template <int NX, class Ar>
+template <int NX, class Ar, class S>
 static cudaError_t dot_dispatch(const StepArgs &a, int mode, int blocks, cudaStream_t s) {
   const int J = a.J;
-  if (J <= 16) k_gs_dot<NX, 1, Ar><<<blocks, A_THREADS, 0, s>>>(a, mode);
-  else if (J <= 32) k_gs_dot<NX, 2, Ar><<<blocks, A_THREADS, 0, s>>>(a, mode);
-  else if (J <= 64) k_gs_dot<NX, 4, Ar><<<blocks, A_THREADS, 0, s>>>(a, mode);
-  else if (J <= 144) k_gs_dot<NX, 9, Ar><<<blocks, A_THREADS, 0, s>>>(a, mode);
-  else if (J <= A_MAXJ) k_gs_dot<NX, 17, Ar><<<blocks, A_THREADS, 0, s>>>(a, mode);
+  if (J <= 16) k_gs_dot<NX, 1, Ar, S><<<blocks, A_THREADS, 0, s>>>(a, mode);
+  else if (J <= 32) k_gs_dot<NX, 2, Ar, S><<<blocks, A_THREADS, 0, s>>>(a, mode);
+  else if (J <= 64) k_gs_dot<NX, 4, Ar, S><<<blocks, A_THREADS, 0, s>>>(a, mode);
+  else if (J <= 144) k_gs_dot<NX, 9, Ar, S><<<blocks, A_THREADS, 0, s>>>(a, mode);
+  else if (J <= A_MAXJ) k_gs_dot<NX, 17, Ar, S><<<blocks, A_THREADS, 0, s>>>(a, mode);
   else return cudaErrorInvalidValue;
   return cudaGetLastError();
 }
 
-cudaError_t launch_gs_dot(const StepArgs &a, int nx, int mode, int arith, cudaStream_t s) {
+// storage: STORE_F64 (doubles) or STORE_PAIR (FP32 pairs, pair arithmetic only)
+cudaError_t launch_gs_dot(const StepArgs &a, int nx, int mode, int arith, cudaStream_t s, int storage) {
   const int blocks = gs_dot_blocks(a.n);
-  if (arith == ARITH_F64) return nx == 2 ? dot_dispatch<2, F64Ar>(a, mode, blocks, s) : dot_dispatch<1, F64Ar>(a, mode, blocks, s);
-  return nx == 2 ? dot_dispatch<2, PairAr>(a, mode, blocks, s) : dot_dispatch<1, PairAr>(a, mode, blocks, s);
+  if (storage == STORE_PAIR)
+    return nx == 2 ? dot_dispatch<2, PairAr, StPair>(a, mode, blocks, s) : dot_dispatch<1, PairAr, StPair>(a, mode, blocks, s);
+  if (arith == ARITH_F64)
+    return nx == 2 ? dot_dispatch<2, F64Ar, StF64>(a, mode, blocks, s) : dot_dispatch<1, F64Ar, StF64>(a, mode, blocks, s);
+  return nx == 2 ? dot_dispatch<2, PairAr, StF64>(a, mode, blocks, s) : dot_dispatch<1, PairAr, StF64>(a, mode, blocks, s);
 }
 
-cudaError_t launch_gs_update(const StepArgs &a, int nx, int mode, int arith, cudaStream_t s) {
+cudaError_t launch_gs_update(const StepArgs &a, int nx, int mode, int arith, cudaStream_t s, int storage) {
   const int blocks = gs_update_blocks(a.n);
   const size_t shm = (size_t)nx * (a.J > 0 ? a.J : 1) * 8;
-  if (arith == ARITH_F64) {
-    if (nx == 2) k_gs_update<2, F64Ar><<<blocks, B_THREADS, shm, s>>>(a, mode);
-    else k_gs_update<1, F64Ar><<<blocks, B_THREADS, shm, s>>>(a, mode);
+  if (storage == STORE_PAIR) {
+    if (nx == 2) k_gs_update<2, PairAr, StPair><<<blocks, B_THREADS, shm, s>>>(a, mode);
+    else k_gs_update<1, PairAr, StPair><<<blocks, B_THREADS, shm, s>>>(a, mode);
+  } else if (arith == ARITH_F64) {
+    if (nx == 2) k_gs_update<2, F64Ar, StF64><<<blocks, B_THREADS, shm, s>>>(a, mode);
+    else k_gs_update<1, F64Ar, StF64><<<blocks, B_THREADS, shm, s>>>(a, mode);
   } else {
-    if (nx == 2) k_gs_update<2, PairAr><<<blocks, B_THREADS, shm, s>>>(a, mode);
-    else k_gs_update<1, PairAr><<<blocks, B_THREADS, shm, s>>>(a, mode);
+    if (nx == 2) k_gs_update<2, PairAr, StF64><<<blocks, B_THREADS, shm, s>>>(a, mode);
+    else k_gs_update<1, PairAr, StF64><<<blocks, B_THREADS, shm, s>>>(a, mode);
   }
   return cudaGetLastError();
 }
 
 size_t restart_smem_bytes(int K, int N) { return ((size_t)K * N + (size_t)K * R_ROWS) * 8; }
 
-cudaError_t launch_restart(double *V, long long ldv, int n, int a0, int K, int s0, int N, const double *Q, int ldq,
-                           int arith, cudaStream_t s) {
+cudaError_t launch_restart(void *V, long long ldv, int n, int a0, int K, int s0, int N, const double *Q, int ldq,
+                           int arith, cudaStream_t s, int storage) {
   if (N <= 0 || K <= 0) return cudaSuccess;
   if (N > R_MAXN) return cudaErrorInvalidValue;
   const size_t shm = restart_smem_bytes(K, N);
@@ -677,14 +900,18 @@ cudaError_t launch_restart(double *V, long long ldv, int n, int a0, int K, int s
   int blocks = num_sms();
   if (blocks > ntiles) blocks = ntiles;
   cudaError_t err;
-  if (arith == ARITH_F64) {
-    err = cudaFuncSetAttribute(k_restart<F64Ar>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+  if (storage == STORE_PAIR) {
+    err = cudaFuncSetAttribute(k_restart<PairAr, StPair>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
     if (err != cudaSuccess) return err;
-    k_restart<F64Ar><<<blocks, R_THREADS, shm, s>>>(V, ldv, n, a0, K, s0, N, Q, ldq);
+    k_restart<PairAr, StPair><<<blocks, R_THREADS, shm, s>>>(static_cast<float2 *>(V), ldv, n, a0, K, s0, N, Q, ldq);
+  } else if (arith == ARITH_F64) {
+    err = cudaFuncSetAttribute(k_restart<F64Ar, StF64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+    if (err != cudaSuccess) return err;
+    k_restart<F64Ar, StF64><<<blocks, R_THREADS, shm, s>>>(static_cast<double *>(V), ldv, n, a0, K, s0, N, Q, ldq);
   } else {
-    err = cudaFuncSetAttribute(k_restart<PairAr>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+    err = cudaFuncSetAttribute(k_restart<PairAr, StF64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
     if (err != cudaSuccess) return err;
-    k_restart<PairAr><<<blocks, R_THREADS, shm, s>>>(V, ldv, n, a0, K, s0, N, Q, ldq);
+    k_restart<PairAr, StF64><<<blocks, R_THREADS, shm, s>>>(static_cast<double *>(V), ldv, n, a0, K, s0, N, Q, ldq);
   }
   return cudaGetLastError();
 }
@@ -700,6 +927,14 @@ cudaError_t launch_set_scales(KrylovState *st, double sigma, double invnu, cudaS
 }
 
 cudaError_t launch_set_unit_scale(KrylovState *st, cudaStream_t s) { return launch_set_scales(st, 1.0, 1.0, s); }
+
+cudaError_t launch_negate(void *x, long long count, int as_float, cudaStream_t s) {
+  int blocks = (int)std::min<long long>((count + 255) / 256, (long long)num_sms() * 8);
+  if (blocks < 1) blocks = 1;
+  if (as_float) k_negate_f32<<<blocks, 256, 0, s>>>(static_cast<float *>(x), count);
+  else k_negate<<<blocks, 256, 0, s>>>(static_cast<double *>(x), count);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_scale(double *x, int n, double alpha, cudaStream_t s) {
   int blocks = (n + 255) / 256;

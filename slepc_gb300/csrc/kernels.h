@@ -40,14 +40,20 @@ size_t restart_smem_bytes(int K, int N);
 
 cudaError_t launch_spmv(const int *rp, const int *ci, const double *va, const double *x, double *y, int n, int lanes,
                         const KrylovState *st, double scale, cudaStream_t s);
-cudaError_t launch_gs_dot(const StepArgs &a, int nx, int mode, int arith, cudaStream_t s);
-cudaError_t launch_gs_update(const StepArgs &a, int nx, int mode, int arith, cudaStream_t s);
-cudaError_t launch_restart(double *V, long long ldv, int n, int a0, int K, int s0, int N, const double *Q, int ldq,
-                           int arith, cudaStream_t s);
+cudaError_t launch_spmv_storage(const int *rp, const int *ci, const double *va, const float2 *va_pair, const void *x,
+                                void *y, int n, int lanes, const KrylovState *st, double scale, int storage,
+                                cudaStream_t s);
+cudaError_t launch_f64_to_pair(const double *x, float2 *y, long long n, cudaStream_t s);
+cudaError_t launch_pair_to_f64(const float2 *x, double *y, long long n, cudaStream_t s);
+cudaError_t launch_gs_dot(const StepArgs &a, int nx, int mode, int arith, cudaStream_t s, int storage = STORE_F64);
+cudaError_t launch_gs_update(const StepArgs &a, int nx, int mode, int arith, cudaStream_t s, int storage = STORE_F64);
+cudaError_t launch_restart(void *V, long long ldv, int n, int a0, int K, int s0, int N, const double *Q, int ldq,
+                           int arith, cudaStream_t s, int storage = STORE_F64);
 cudaError_t launch_segment_begin(KrylovState *st, int k0, int m, cudaStream_t s);
 cudaError_t launch_set_unit_scale(KrylovState *st, cudaStream_t s);
 cudaError_t launch_set_scales(KrylovState *st, double sigma, double invnu, cudaStream_t s);
 cudaError_t launch_scale(double *x, int n, double alpha, cudaStream_t s);
+cudaError_t launch_negate(void *x, long long count, int as_float, cudaStream_t s);
 cudaError_t launch_ds_hep(const DSArgs &a, int n_max, cudaStream_t s);
 cudaError_t launch_ds_nhep(const DSArgs &a, int n_max, cudaStream_t s);
 cudaError_t launch_nhep_vectors(double *T, int ld, int n, double *X, cudaStream_t s);

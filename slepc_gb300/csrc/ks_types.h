@@ -11,6 +11,12 @@ enum Arith : int {
   ARITH_F64 = 1,   // FP64 storage, IEEE FP64 FMA (exact reference arithmetic, FP64-pipe bound on GB300)
 };
 
+// Storage format of the Krylov basis.
+enum Storage : int {
+  STORE_F64 = 0,   // IEEE doubles
+  STORE_PAIR = 1,  // FP32 pairs (hi, lo), value hi + lo: 47-bit significand in 8 bytes
+};
+
 // Per-factorisation state of the delayed-reorthogonalisation Gram-Schmidt (device resident).
 // The raw vector stored in V[:, j] at the start of step j is u_raw; the unit vector it stands for is
 // u = sigma * u_raw, already orthogonalised once against V[:, 0:j].
@@ -52,14 +58,14 @@ struct KSControl {
 
 // Arguments of one Gram-Schmidt step kernel (both halves of the fused pair).
 struct StepArgs {
-  const double *V;   // basis, column-major (columns 0..J-1 take part)
+  const void *V;     // basis, column-major (columns 0..J-1 take part); double or float2 per the storage format
   long long ldv;     // leading dimension (rows, padded)
   int n;             // rows
   int J;             // columns of V taking part (0..J-1)
   int j;             // Krylov index of u (Hessenberg column j); w is the vector of index j+1
   int hermitian;     // 1: write alpha/beta to (d, e); 0: write Hessenberg columns to H
-  double *U;         // u (raw, scaled by sigma); overwritten by kernel B with the orthonormal v_j
-  double *W;         // w = A u (NX = 2); overwritten by kernel B with w'
+  void *U;           // u (raw, scaled by sigma); overwritten by kernel B with the orthonormal v_j
+  void *W;           // w = A u (NX = 2); overwritten by kernel B with w'
   double *d, *e;     // tridiagonal storage (hermitian)
   double *H;         // Hessenberg storage (non-hermitian), column-major ldh
   int ldh;
