@@ -123,6 +123,14 @@ def committed_traffic(workload):
     return None
 
 
+def full_size_steps(workload):
+    """Krylov steps of the complete reference-algorithm solve (oracle/full_size_runs.py), 0 if not recorded."""
+    p = os.path.join(ROOT, "oracle", "full_size_runs.json")
+    if os.path.exists(p):
+        return int(json.load(open(p)).get(workload, {}).get("steps", 0))
+    return 0
+
+
 def cpu_baseline(csr, wl, steps_full, budget_s=20.0):
     """Oracle (CPU restatement of the reference) on all host cores for a bounded time; eigenpairs/s extrapolated
     by the number of Krylov steps of the full solve."""
@@ -157,8 +165,7 @@ def run_reference(args, wl):
     from slepc_gb300 import matgen
 
     csr = wl["gen"](matgen)
-    steps_full = int(json.load(open(os.path.join(ROOT, "profiles", "reference_steps.json"))).get(args.workload, 0)) \
-        if os.path.exists(os.path.join(ROOT, "profiles", "reference_steps.json")) else 0
+    steps_full = full_size_steps(args.workload)
     budget = 20.0 if args.workload == "lap3d128" else 10.0
     vals = []
     for i in range(args.warmup + args.steps):
@@ -319,7 +326,7 @@ def main():
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(csr, wl, steps_k[-1])
+        cpu = cpu_baseline(csr, wl, full_size_steps(args.workload) or steps_k[-1])
 
     if rank == 0:
         lat_sorted = sorted(lat)

@@ -70,6 +70,7 @@ def load():
         "EPSGetErrorEstimate": ([P, I, P], I),
         "EPSComputeError": ([P, I, I, P], I),
         "EPSGB300SetArithmetic": ([P, I], I),
+        "EPSGB300SetProjectedSolver": ([P, I], I),
         "EPSGB300GetStats": ([P, P], I),
         "EPSGB300OrthogonalityError": ([P, P], I),
         "EPSGB300SetProfiling": ([P, I], I),
@@ -253,6 +254,11 @@ class EPS:
         """'pair' (FP64 storage, error-free FP32-pair arithmetic) or 'f64' (IEEE FP64 FMA)."""
         _check(load().EPSGB300SetArithmetic(self.handle, 1 if arith == "f64" else 0), "EPSGB300SetArithmetic")
 
+    def setProjectedSolver(self, method):
+        """'refined' (FP32 QL + FP64 refinement, default) or 'qr' (FP64 QL) for the symmetric projected problem."""
+        _check(load().EPSGB300SetProjectedSolver(self.handle, 1 if method == "qr" else 0),
+               "EPSGB300SetProjectedSolver")
+
     def setUp(self):
         _check(load().EPSSetUp(self.handle), "EPSSetUp")
 
@@ -336,7 +342,7 @@ class EPS:
 
 
 def solve(csr, *, hermitian=True, which="LM", nev=1, ncv=None, mpd=None, tol=None, max_it=None, v0=None,
-          arith="pair", vectors=True):
+          arith="pair", vectors=True, ds=None, lock=None):
     """One-call convenience: returns dict(eigr, eigi, X, nconv, its, reason, errors, stats)."""
     A = Mat(*csr)
     eps = EPS().create()
@@ -346,6 +352,10 @@ def solve(csr, *, hermitian=True, which="LM", nev=1, ncv=None, mpd=None, tol=Non
     eps.setTolerances(tol if tol else -1.0, max_it if max_it else -1)
     eps.setWhichEigenpairs(which)
     eps.setArithmetic(arith)
+    if ds is not None:
+        eps.setProjectedSolver(ds)
+    if lock is not None:
+        eps.setKrylovSchurLocking(lock)
     if v0 is not None:
         eps.setInitialSpace(v0)
     eps.solve()

@@ -443,6 +443,7 @@ static PetscErrorCode eps_free_device(EPS eps) {
   eps->errest.release();
   eps->coef.release();
   eps->work.release();
+  eps->dsf.release();
   eps->part.release();
   eps->st.release();
   eps->ctl.release();
@@ -645,6 +646,18 @@ extern "C" PetscErrorCode EPSGB300GetArithmetic(EPS eps, EPSGB300Arith *arith) {
   *arith = (EPSGB300Arith)eps->arith;
   return 0;
 }
+extern "C" PetscErrorCode EPSGB300SetProjectedSolver(EPS eps, EPSGB300DSMethod method) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  KSG_CHECK(method == EPS_GB300_DS_REFINED || method == EPS_GB300_DS_QR, PETSC_ERR_ARG_OUTOFRANGE,
+            "Unknown projected solver");
+  eps->ds_method = method;
+  return 0;
+}
+extern "C" PetscErrorCode EPSGB300GetProjectedSolver(EPS eps, EPSGB300DSMethod *method) {
+  KSG_CHECK(eps && method, PETSC_ERR_ARG_NULL, "Null argument");
+  *method = (EPSGB300DSMethod)eps->ds_method;
+  return 0;
+}
 extern "C" PetscErrorCode EPSGB300SetDevice(EPS eps, int device) {
   KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
   int count = 0;
@@ -679,6 +692,8 @@ extern "C" PetscErrorCode EPSSetFromOptions(EPS eps) {
     else if (!strcmp(o, "-eps_type") && v) KSG_TRY(EPSSetType(eps, v));
     else if (!strcmp(o, "-eps_gb300_arith") && v)
       KSG_TRY(EPSGB300SetArithmetic(eps, !strcmp(v, "f64") ? EPS_GB300_ARITH_F64 : EPS_GB300_ARITH_PAIR));
+    else if (!strcmp(o, "-eps_gb300_ds") && v)
+      KSG_TRY(EPSGB300SetProjectedSolver(eps, !strcmp(v, "qr") ? EPS_GB300_DS_QR : EPS_GB300_DS_REFINED));
   }
   return 0;
 }
@@ -737,6 +752,7 @@ extern "C" PetscErrorCode EPSSetUp(EPS eps) {
   KSG_CUDA(eps->errest.alloc(ld));
   KSG_CUDA(eps->coef.alloc(2 * ld + 8));
   KSG_CUDA(eps->work.alloc(4 * ld + 8));
+  KSG_CUDA(eps->dsf.alloc(ds_fast_scratch_doubles(ld)));
   eps->pstride = (int)ksg_part_stride(ld);
   KSG_CUDA(eps->part.alloc(ksg_part_blocks(n) * eps->pstride));
   KSG_CUDA(eps->st.alloc(1));
@@ -1021,8 +1037,14 @@ extern "C" PetscErrorCode EPSSolve(EPS eps) {
     da.ctl = eps->ctl.p;
     {
       LaunchScope ls(eps, EPS_GB300_K_DS, 0.0);
-      if (herm) KSG_CUDA(launch_ds_hep(da, ld, s));
-      else KSG_CUDA(launch_ds_nhep(da, ld, s));
+      if (herm && eps->ds_method == EPS_GB300_DS_REFINED) {
+        KSG_CUDA(launch_ds_hep_fast(da, ds_fast_layout(eps->dsf.p, ld), ld, s));
+        eps->stats.kernel_launches += ds_fast_launches() - 1;
+      } else if (herm) {
+        KSG_CUDA(launch_ds_hep(da, ld, s));
+      } else {
+        KSG_CUDA(launch_ds_nhep(da, ld, s));
+      }
     }
     KSG_CUDA(cudaMemcpyAsync(eps->h_ctl, eps->ctl.p, sizeof(KSControl), cudaMemcpyDeviceToHost, s));
     KSG_CUDA(cudaStreamSynchronize(s));

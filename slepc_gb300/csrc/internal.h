@@ -104,6 +104,7 @@ struct _p_EPS {
   int extraction = 0;
   int arith = ksg::ARITH_PAIR;
   int storage = ksg::STORE_PAIR;  // basis format: pairs with pair arithmetic, doubles with FP64 arithmetic
+  int ds_method = 0;              // EPSGB300DSMethod
   int device = -1;
   std::vector<double> v0;
   unsigned long long seed = 0x5EEDULL;
@@ -116,7 +117,7 @@ struct _p_EPS {
   int lanes = 8;
   long long ldv = 0;
   cudaStream_t stream = nullptr;
-  DBuf<double> V, d, e, H, Q, X, eigr, eigi, errest, coef, work;
+  DBuf<double> V, d, e, H, Q, X, eigr, eigi, errest, coef, work, dsf;
   DBuf<float2> part;
   int pstride = 0;
   DBuf<ksg::KrylovState> st;

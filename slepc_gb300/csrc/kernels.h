@@ -31,6 +31,18 @@ struct DSArgs {
 
 enum { DS_DO_SOLVE = 1, DS_DO_SORT = 2, DS_DO_EXTRAROW = 4, DS_DO_CONTROL = 8, DS_DO_ALL = 15 };
 
+// Scratch of the mixed-precision symmetric projected solver (k_ds_fast.cu): five ld x ld FP64 matrices and a few
+// vectors, carved from one allocation by ds_fast_layout.  The problem fields are filled from DSArgs at launch.
+struct DSFArgs {
+  int ld, n, l, k, raw;
+  const double *d, *e;
+  double *T, *X, *P, *S, *G;  // ld x ld: projected matrix, eigenvectors, product, X^T T X, X^T X
+  double *W;                  // 2 * ld * 16: cluster rotations and cluster blocks
+  double *lam, *part, *scal;  // eigenvalue estimates, block partial sums, thresholds
+  const KrylovState *st;
+  KSControl *ctl;
+};
+
 int num_sms();
 int spmv_lanes_for(double avg_nnz);
 int gs_dot_blocks(int n);
@@ -56,6 +68,11 @@ cudaError_t launch_scale(double *x, int n, double alpha, cudaStream_t s);
 cudaError_t launch_negate(void *x, long long count, int as_float, cudaStream_t s);
 cudaError_t launch_ds_hep(const DSArgs &a, int n_max, cudaStream_t s);
 cudaError_t launch_ds_nhep(const DSArgs &a, int n_max, cudaStream_t s);
+size_t ds_fast_scratch_doubles(int ld);
+DSFArgs ds_fast_layout(double *scratch, int ld);
+int ds_fast_launches();
+// full DS_DO_ALL contract of launch_ds_hep for the Krylov-Schur loop (a.st and a.ctl required)
+cudaError_t launch_ds_hep_fast(const DSArgs &a, const DSFArgs &f, int n_max, cudaStream_t s);
 cudaError_t launch_nhep_vectors(double *T, int ld, int n, double *X, cudaStream_t s);
 
 }  // namespace ksg
