@@ -115,7 +115,7 @@ def measured_peaks():
 
 
 def committed_traffic(workload):
-    """Per-launch DRAM traffic of the dominant kernel from the committed ncu summary, if one exists."""
+    """DRAM traffic / algorithmic bytes per kernel class from the committed ncu captures, if recorded."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(p):
         d = json.load(open(p))
@@ -196,6 +196,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--profile-case", action="store_true",
                     help="run exactly one solve limited to 2 restarts and exit (the ncu capture case)")
+    ap.add_argument("--profile-solve", action="store_true",
+                    help="run exactly one complete solve and exit (the ncu launch-list case: same work as a step)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     wl = WORKLOADS[args.workload]
@@ -256,6 +258,11 @@ def main():
         eps.solve()
         print(json.dumps({"profile_case": args.workload, "stats": eps.getStats()}), flush=True)
         return
+    if args.profile_solve:
+        eps.setUp()
+        eps.solve()
+        print(json.dumps({"profile_solve": args.workload, "stats": eps.getStats()}), flush=True)
+        return
     eps.setUp()
     for _ in range(args.warmup):
         eps.solve()
@@ -310,10 +317,12 @@ def main():
     top = max(("gs_dot", "gs_update", "spmv", "restart"), key=lambda k: prof[k][0])
     ms_k, by_k, nl_k = prof[top]
     achieved = by_k / (ms_k / 1000.0) / 1e9 if ms_k > 0 else None
-    tr = committed_traffic(args.workload)
+    tr = (committed_traffic(args.workload) or {}).get(top)
+    traffic = tr * by_k / nl_k if (tr and nl_k) else None  # DRAM bytes per launch: ncu ratio x algorithmic bytes
     roofline = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak if achieved else None, "peak_source": peak_kind,
-                "traffic": (tr or {}).get(top), "launches": nl_k,
+                "traffic": traffic, "algorithmic_bytes_per_launch": by_k / nl_k if nl_k else None,
+                "launches": nl_k,
                 "per_class_ms": {k: round(v[0], 3) for k, v in prof.items()},
                 "per_class_GBps": {k: (round(v[1] / (v[0] / 1000.0) / 1e9, 1) if v[0] > 0 else None)
                                    for k, v in prof.items()}}
