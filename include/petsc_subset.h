@@ -48,6 +48,7 @@ typedef int MPI_Comm; /* one process per GPU: communicators carry no information
 #define PETSC_ERR_ARG_WRONG 62
 #define PETSC_ERR_ARG_OUTOFRANGE 63
 #define PETSC_ERR_ARG_WRONGSTATE 73
+#define PETSC_ERR_ARG_INCOMP 75
 #define PETSC_ERR_LIB 76
 #define PETSC_ERR_PLIB 77
 #define PETSC_ERR_CONV_FAILED 82

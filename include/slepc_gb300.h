@@ -60,6 +60,16 @@ PetscErrorCode EPSGB300GetProfile(EPS eps, EPSGB300KernelClass cls, double *ms, 
  * eigenvectors (Hermitian) or the Schur/eigen vectors (non-Hermitian) in solver order (see EPSGetEigenpair). */
 PetscErrorCode EPSGB300GetDeviceBasis(EPS eps, const double **V, PetscInt *ld);
 
+/* Solve `count` eigenproblems together: every EPS is configured as for EPSSolve (operators, problem type,
+ * dimensions, tolerances, which, initial space) and left in the state EPSSolve would leave it, so EPSGetConverged,
+ * EPSGetEigenpair, EPSGetIterationNumber and EPSGetConvergedReason read the results.  No counterpart in the
+ * reference (whose unit of work is one EPSSolve, krylovschur.c:227-337); each problem runs the same algorithm.
+ * The batch advances one Krylov step of every unconverged problem per kernel launch and runs a restart cycle of all
+ * of them as one CUDA graph; a problem's arithmetic depends only on the problem, so its results are the same in
+ * any batch, including a batch of one.  Requirements: pair arithmetic (the default), ncv <= 79, one device.
+ * The symmetric projected problems use the FP64 QR solver (EPS_GB300_DS_QR). */
+PetscErrorCode EPSGB300SolveBatch(PetscInt count, EPS *eps);
+
 /* Orthogonality ||V^T V - I||_max of the first nconv columns, computed on the device in FP64. */
 PetscErrorCode EPSGB300OrthogonalityError(EPS eps, PetscReal *err);
 

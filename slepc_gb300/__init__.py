@@ -71,6 +71,7 @@ def load():
         "EPSComputeError": ([P, I, I, P], I),
         "EPSGB300SetArithmetic": ([P, I], I),
         "EPSGB300SetProjectedSolver": ([P, I], I),
+        "EPSGB300SolveBatch": ([I, ctypes.POINTER(P)], I),
         "EPSGB300GetStats": ([P, P], I),
         "EPSGB300OrthogonalityError": ([P, P], I),
         "EPSGB300SetProfiling": ([P, I], I),
@@ -339,6 +340,12 @@ class EPS:
         v = ctypes.c_double()
         _check(load().EPSGB300OrthogonalityError(self.handle, ctypes.byref(v)), "EPSGB300OrthogonalityError")
         return v.value
+
+
+def solve_batch(eps_list):
+    """EPSGB300SolveBatch over configured EPS objects (the batched engine); results are read from each EPS."""
+    arr = (ctypes.c_void_p * len(eps_list))(*[e.handle for e in eps_list])
+    _check(load().EPSGB300SolveBatch(len(eps_list), arr), "EPSGB300SolveBatch")
 
 
 def solve(csr, *, hermitian=True, which="LM", nev=1, ncv=None, mpd=None, tol=None, max_it=None, v0=None,

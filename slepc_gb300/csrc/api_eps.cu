@@ -906,7 +906,22 @@ static PetscErrorCode eps_factorize(EPS eps, int k0, int nv, double *bytes) {
   return 0;
 }
 
-static PetscErrorCode eps_new_start_vector(EPS eps, int col, int *breakdown) {
+// the initial space, or a random vector, into column 0 of the basis (not yet normalised)
+PetscErrorCode ksg_eps_put_start(EPS eps, cudaStream_t s) {
+  std::vector<double> h;
+  const double *src;
+  if (!eps->v0.empty()) src = eps->v0.data();
+  else {
+    h.resize(eps->n);
+    ksg_random_fill(h.data(), eps->n, eps->seed, 0);
+    src = h.data();
+  }
+  KSG_TRY(ksg_put_column(eps->V.p, src, eps->n, eps->storage, s));
+  if (eps->v0.empty()) KSG_CUDA(cudaStreamSynchronize(s));  // h is pageable and goes out of scope
+  return 0;
+}
+
+PetscErrorCode ksg_eps_new_start_vector(EPS eps, int col, int *breakdown) {
   std::vector<double> h(eps->n);
   ksg_random_fill(h.data(), eps->n, eps->seed, ++eps->rng_counter);
   double *dst = eps->V.p + (size_t)col * eps->ldv;
@@ -963,6 +978,38 @@ static void sort_eigenvalues(int which, int n, const double *eigr, const double 
 }
 
 // EPSSolve (epssolve.c:119-208) with EPSSolve_KrylovSchur_Default (krylovschur.c:227-337) on the device
+// undo the operator scaling and order the results (epssolve.c:159-178); eigr/eigi/errest are the device arrays
+// already copied to the host; conjugate pairs with a negative first imaginary part are flipped on the device
+PetscErrorCode ksg_eps_assemble(EPS eps, int nconv, const double *er, const double *ei, const double *es,
+                                cudaStream_t s) {
+  const int n = eps->n;
+  const int herm = eps->problem == EPS_HEP;
+  eps->r_eigr.assign(er, er + nconv);
+  eps->r_eigi.assign(ei, ei + nconv);
+  eps->r_errest.assign(es, es + nconv);
+  if (herm) std::fill(eps->r_eigi.begin(), eps->r_eigi.end(), 0.0);
+  for (int i = 0; i < nconv; ++i) {
+    eps->r_eigr[i] /= eps->opscale;
+    eps->r_eigi[i] /= eps->opscale;
+  }
+  for (int i = 0; i < nconv - 1; ++i) {
+    if (eps->r_eigi[i] != 0.0) {
+      if (eps->r_eigi[i] < 0.0) {
+        eps->r_eigi[i] = -eps->r_eigi[i];
+        eps->r_eigi[i + 1] = -eps->r_eigi[i + 1];
+        // negate a basis column: both halves of a pair, or the double
+        KSG_CUDA(launch_negate(eps->V.p + (size_t)(i + 1) * eps->ldv, eps->storage == STORE_PAIR ? 2 * n : n,
+                               eps->storage == STORE_PAIR, s));
+      }
+      i++;
+    }
+  }
+  eps->perm.resize(std::max(nconv, 1));
+  for (int i = 0; i < nconv; ++i) eps->perm[i] = i;
+  sort_eigenvalues(eps->which, nconv, eps->r_eigr.data(), eps->r_eigi.data(), eps->perm.data());
+  return 0;
+}
+
 extern "C" PetscErrorCode EPSSolve(EPS eps) {
   KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
   KSG_TRY(EPSSetUp(eps));
@@ -985,15 +1032,7 @@ extern "C" PetscErrorCode EPSSolve(EPS eps) {
   eps->solved = 0;
   // start vector: the initial space, or a random vector (EPSGetStartVector, epssolve.c:841-873)
   {
-    std::vector<double> h;
-    const double *src;
-    if (!eps->v0.empty()) src = eps->v0.data();
-    else {
-      h.resize(n);
-      ksg_random_fill(h.data(), n, eps->seed, 0);
-      src = h.data();
-    }
-    KSG_TRY(ksg_put_column(eps->V.p, src, n, eps->storage, s));
+    KSG_TRY(ksg_eps_put_start(eps, s));
     double nrm = 0.0;
     int lindep = 0;
     KSG_TRY(ksg_orthonormalize_column(eps->V.p, eps->ldv, n, 0, eps->coef.p, eps->part.p, eps->pstride, eps->st.p,
@@ -1067,7 +1106,7 @@ extern "C" PetscErrorCode EPSSolve(EPS eps) {
         // start a new Krylov factorisation at column k (after the rotation of the converged vectors)
         if (k < nev) {
           int bd = 0;
-          KSG_TRY(eps_new_start_vector(eps, k, &bd));
+          KSG_TRY(ksg_eps_new_start_vector(eps, k, &bd));
           if (bd) reason = EPS_DIVERGED_BREAKDOWN;
         }
       } else {
@@ -1089,30 +1128,7 @@ extern "C" PetscErrorCode EPSSolve(EPS eps) {
   KSG_CUDA(cudaMemcpyAsync(ei.data(), eps->eigi.p, sizeof(double) * ld, cudaMemcpyDeviceToHost, s));
   KSG_CUDA(cudaMemcpyAsync(es.data(), eps->errest.p, sizeof(double) * ld, cudaMemcpyDeviceToHost, s));
   KSG_CUDA(cudaStreamSynchronize(s));
-  // undo the operator scaling and order the results (epssolve.c:159-178)
-  eps->r_eigr.assign(er.begin(), er.begin() + nconv);
-  eps->r_eigi.assign(ei.begin(), ei.begin() + nconv);
-  eps->r_errest.assign(es.begin(), es.begin() + nconv);
-  if (herm) std::fill(eps->r_eigi.begin(), eps->r_eigi.end(), 0.0);
-  for (int i = 0; i < nconv; ++i) {
-    eps->r_eigr[i] /= eps->opscale;
-    eps->r_eigi[i] /= eps->opscale;
-  }
-  for (int i = 0; i < nconv - 1; ++i) {
-    if (eps->r_eigi[i] != 0.0) {
-      if (eps->r_eigi[i] < 0.0) {
-        eps->r_eigi[i] = -eps->r_eigi[i];
-        eps->r_eigi[i + 1] = -eps->r_eigi[i + 1];
-        // negate a basis column: both halves of a pair, or the double
-        KSG_CUDA(launch_negate(eps->V.p + (size_t)(i + 1) * eps->ldv, eps->storage == STORE_PAIR ? 2 * n : n,
-                               eps->storage == STORE_PAIR, s));
-      }
-      i++;
-    }
-  }
-  eps->perm.resize(std::max(nconv, 1));
-  for (int i = 0; i < nconv; ++i) eps->perm[i] = i;
-  sort_eigenvalues(eps->which, nconv, eps->r_eigr.data(), eps->r_eigi.data(), eps->perm.data());
+  KSG_TRY(ksg_eps_assemble(eps, nconv, er.data(), ei.data(), es.data(), s));
   KSG_CUDA(cudaEventRecord(eps->ev_solve[1], s));
   KSG_CUDA(cudaStreamSynchronize(s));
   {

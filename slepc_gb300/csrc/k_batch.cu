@@ -1,0 +1,299 @@
+// k_batch.cu -- the batched Krylov-Schur engine: every live instance of a batch advances one Krylov step per launch.
+//
+// Each kernel runs a persistent grid over a list of virtual blocks (instance, b, nb): virtual block b of nb is the
+// share instance `inst` would get from block b of an nb-block launch of the single-problem kernel, and it runs the
+// same device body (krylov_body.cuh).  An instance's arithmetic therefore depends only on its own size -- the
+// result of a problem solved inside any mix equals its result solved alone in a batch of one.  Instances that
+// are not in the phase a launch serves skip their virtual blocks at once, so one captured sequence of launches (a
+// restart cycle) serves every cycle of every instance:
+//
+//   k_batch_zero + start pass (GS_ORTHO on column 0) + k_batch_start  -> newly admitted instances enter ITER
+//   slot s = 0 .. S:  k_batch_spmv(s), k_batch_dot(s), k_batch_update(s)   (instance steps if k0 <= s < nv,
+//                                                                            final reorthogonalisation if s == nv)
+//   projected problems (k_ds_hep.cu / k_ds_nhep.cu batched kernels), k_batch_restart, k_batch_control
+//
+// k_batch_control is the device copy of the host loop of EPSSolve_KrylovSchur_Default (krylovschur.c:227-337):
+// it reads the control record the projected solver wrote and sets up the next segment.
+#include "batch_types.h"
+#include "common.cuh"
+#include "kernels.h"
+#include "krylov_body.cuh"
+#include "ks_types.h"
+
+namespace ksg {
+
+KS_DEVICE void batch_segment_begin(KrylovState *st, int k0, int m) {
+  st->sigma = 1.0;
+  st->beta_prev = 0.0;
+  st->invnu = 1.0;
+  st->tau_sigma = 0.0;
+  st->beta_out = 0.0;
+  st->onorm = 0.0;
+  st->stop = 0;
+  st->m = m;
+  st->breakdown = 0;
+  st->k0 = k0;
+}
+
+// The Gram-Schmidt work of instance p in slot `slot`: mode and NX, or false if it has none.
+KS_DEVICE bool batch_slot(const BatchInst &p, int slot, int &mode, int &nx, int &j) {
+  if (slot < 0) {  // start pass: normalise column 0
+    if (p.phase != BP_START) return false;
+    mode = GS_ORTHO;
+    nx = 1;
+    j = 0;
+    return true;
+  }
+  if (p.phase != BP_ITER) return false;
+  if (slot >= p.k0 && slot < p.nv) {
+    mode = GS_STEP;
+    nx = 2;
+    j = slot;
+    return true;
+  }
+  if (slot == p.nv) {
+    mode = GS_FINAL;
+    nx = 1;
+    j = slot;
+    return true;
+  }
+  return false;
+}
+
+KS_DEVICE StepArgs batch_step_args(const BatchInst &p, int j, int nx) {
+  StepArgs a;
+  a.V = p.V;
+  a.ldv = p.ldv;
+  a.n = p.n;
+  a.J = j;
+  a.j = j;
+  a.hermitian = p.hermitian;
+  a.U = p.V + (size_t)j * p.ldv;
+  a.W = (nx == 2) ? (void *)(p.V + (size_t)(j + 1) * p.ldv) : nullptr;
+  a.d = p.d;
+  a.e = p.e;
+  a.H = p.H;
+  a.ldh = p.ld;
+  a.eta = 0.7071;
+  a.coef = p.coef;
+  a.part = p.part;
+  a.pstride = p.pstride;
+  a.st = p.st;
+  return a;
+}
+
+// zero d, e and H of newly admitted instances, reset their Krylov state for the start pass
+__global__ void k_batch_zero(BatchInst *I, const int *list, const BatchHdr *h) {
+  for (int v = blockIdx.x; v < h->n_inst; v += gridDim.x) {
+    BatchInst &p = I[list[v]];
+    if (p.phase != BP_START) continue;
+    const int ld = p.ld;
+    for (int i = threadIdx.x; i < ld + 1; i += blockDim.x) {
+      p.d[i] = 0.0;
+      p.e[i] = 0.0;
+    }
+    for (int i = threadIdx.x; i < (ld + 1) * (ld + 1); i += blockDim.x) p.H[i] = 0.0;
+    if (threadIdx.x == 0) batch_segment_begin(p.st, 0, 0);
+  }
+}
+
+// after the start pass: ITER, or FAILED if the start vector is zero (EPSSolve's "Initial vector is zero")
+__global__ void k_batch_start(BatchInst *I, const int *list, const BatchHdr *h) {
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < h->n_inst; v += gridDim.x * blockDim.x) {
+    BatchInst &p = I[list[v]];
+    if (p.phase != BP_START) continue;
+    if (p.st->breakdown) {
+      p.phase = BP_FAILED;
+      p.err = 77;  // PETSC_ERR_PLIB, as the single-problem path reports a zero initial vector
+      continue;
+    }
+    p.phase = BP_ITER;
+    p.nconv = 0;
+    p.l = 0;
+    p.its = 1;
+    p.reason = 0;
+    p.steps = 0;
+    p.k0 = 0;
+    p.nv = min(p.mpd, p.ncv);
+    batch_segment_begin(p.st, 0, p.nv);
+  }
+}
+
+template <int LANES>
+KS_DEVICE void batch_spmv_vb(const BatchInst &p, const BatchVB &m, int slot) {
+  const float2 *x = p.V + (size_t)slot * p.ldv;
+  float2 *y = p.V + (size_t)(slot + 1) * p.ldv;
+  const long long w0 = (long long)m.b * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const long long nw = (long long)m.nb * (blockDim.x >> 5);
+  spmv_pair_rows<LANES>(p.rp, p.ci, p.va2, x, y, p.n, p.st, p.opscale, w0, nw);
+}
+
+__global__ void __launch_bounds__(256) k_batch_spmv(const BatchInst *I, const BatchVB *map, const BatchHdr *h,
+                                                    int slot) {
+  const int nmap = h->n_spmv;
+  for (int v = blockIdx.x; v < nmap; v += gridDim.x) {
+    const BatchVB m = map[v];
+    const BatchInst &p = I[m.inst];
+    if (p.phase != BP_ITER || slot < p.k0 || slot >= p.nv) continue;
+    switch (p.lanes) {
+      case 1: batch_spmv_vb<1>(p, m, slot); break;
+      case 8: batch_spmv_vb<8>(p, m, slot); break;
+      default: batch_spmv_vb<32>(p, m, slot); break;
+    }
+  }
+}
+
+// Gram-Schmidt half A; CPW = 5 covers the batch limit of 80 columns (the per-column arithmetic does not depend on
+// CPW, so this matches the single-problem kernel's rounding)
+constexpr int BATCH_CPW = 5;
+constexpr int BATCH_MAXJ = A_WARPS * BATCH_CPW;
+
+__global__ void __launch_bounds__(A_THREADS, 1) k_batch_dot(const BatchInst *I, const BatchVB *map,
+                                                            const BatchHdr *h, int slot) {
+  const int nmap = h->n_dot;
+  for (int v = blockIdx.x; v < nmap; v += gridDim.x) {
+    const BatchVB m = map[v];
+    const BatchInst &p = I[m.inst];
+    int mode, nx, j;
+    if (!batch_slot(p, slot, mode, nx, j)) continue;
+    __syncthreads();  // shared staging of the previous virtual block is free
+    const StepArgs a = batch_step_args(p, j, nx);
+    if (nx == 2) gs_dot_body<2, BATCH_CPW, PairAr, StPair>(a, mode, m.b, m.nb);
+    else gs_dot_body<1, BATCH_CPW, PairAr, StPair>(a, mode, m.b, m.nb);
+  }
+}
+
+__global__ void __launch_bounds__(B_THREADS) k_batch_update(const BatchInst *I, const BatchVB *map,
+                                                            const BatchHdr *h, int slot) {
+  const int nmap = h->n_upd;
+  for (int v = blockIdx.x; v < nmap; v += gridDim.x) {
+    const BatchVB m = map[v];
+    const BatchInst &p = I[m.inst];
+    int mode, nx, j;
+    if (!batch_slot(p, slot, mode, nx, j)) continue;
+    __syncthreads();
+    const StepArgs a = batch_step_args(p, j, nx);
+    if (nx == 2) gs_update_body<2, PairAr, StPair>(a, mode, m.b, m.nb);
+    else gs_update_body<1, PairAr, StPair>(a, mode, m.b, m.nb);
+  }
+}
+
+// Thick restart V(:, nconv : k+l) = V(:, nconv : nv) Q(nconv : nv, nconv : k+l), then the residual column moves to
+// column k+l (krylovschur.c:300-329), for every instance whose projected problem was solved this cycle.
+__global__ void __launch_bounds__(R_THREADS, 1) k_batch_restart(const BatchInst *I, const BatchVB *map,
+                                                                const BatchHdr *h) {
+  const int nmap = h->n_rst;
+  for (int v = blockIdx.x; v < nmap; v += gridDim.x) {
+    const BatchVB m = map[v];
+    const BatchInst &p = I[m.inst];
+    if (p.phase != BP_ITER) continue;
+    const KSControl c = *p.ctl;
+    if (c.ds_error) continue;
+    const int k = c.nconv, l = c.l, nv = c.nv, nconv = p.nconv;
+    const int K = nv - nconv, N = k + l - nconv;
+    __syncthreads();
+    if (K > 0 && N > 0) restart_body<PairAr, StPair>(p.V, p.ldv, p.n, nconv, K, nconv, N, p.Q, p.ld, m.b, m.nb);
+    if (c.reason == 0 && !(c.breakdown || k == nv)) {
+      // this virtual block's rows only: the restart above already consumed column k+l for them
+      const int ntiles = (p.n + R_ROWS - 1) / R_ROWS;
+      const float2 *src = p.V + (size_t)nv * p.ldv;
+      float2 *dst = p.V + (size_t)(k + l) * p.ldv;
+      for (int t = m.b; t < ntiles; t += m.nb) {
+        const int r = t * R_ROWS + threadIdx.x;
+        if (threadIdx.x < R_ROWS && r < p.n) dst[r] = src[r];
+      }
+    }
+  }
+}
+
+// One thread per instance: the restart-loop bookkeeping of EPSSolve_KrylovSchur_Default after the restart.
+__global__ void k_batch_control(BatchInst *I, const int *list, const BatchHdr *h, BatchStatus *status) {
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < h->n_inst; v += gridDim.x * blockDim.x) {
+    const int i = list[v];
+    BatchInst &p = I[i];
+    if (p.phase == BP_ITER) {
+      const KSControl c = *p.ctl;
+      p.steps += (c.nv > p.k0) ? c.nv - p.k0 : 0;
+      if (c.ds_error) {
+        p.phase = BP_FAILED;
+        p.err = 76;  // PETSC_ERR_LIB: the projected eigenproblem solver did not converge
+      } else {
+        const int k = c.nconv;
+        p.nconv = k;
+        p.l = c.l;
+        p.reason = c.reason;
+        if (c.reason != 0) {
+          p.phase = BP_DONE;
+        } else {
+          p.its += 1;
+          p.k0 = k + c.l;
+          p.nv = min(k + p.mpd, p.ncv);
+          if (c.breakdown || k == c.nv) p.phase = BP_HOST;  // new start vector at column k (host)
+          else if (p.nv <= p.k0) {
+            p.phase = BP_FAILED;
+            p.err = 77;
+          } else batch_segment_begin(p.st, p.k0, p.nv);
+        }
+      }
+    }
+    BatchStatus s;
+    s.phase = p.phase;
+    s.nconv = p.nconv;
+    s.its = p.its;
+    s.reason = p.reason;
+    status[i] = s;
+  }
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------------------------------------------
+int batch_max_columns() { return BATCH_MAXJ; }
+
+cudaError_t launch_batch_begin(BatchInst *I, const int *list, const BatchHdr *h, int grid_inst, cudaStream_t s) {
+  k_batch_zero<<<grid_inst, 256, 0, s>>>(I, list, h);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_start(BatchInst *I, const int *list, const BatchHdr *h, int grid_inst, cudaStream_t s) {
+  k_batch_start<<<(grid_inst + 127) / 128, 128, 0, s>>>(I, list, h);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_spmv(const BatchInst *I, const BatchVB *map, const BatchHdr *h, int slot, int grid,
+                              cudaStream_t s) {
+  k_batch_spmv<<<grid, 256, 0, s>>>(I, map, h, slot);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_dot(const BatchInst *I, const BatchVB *map, const BatchHdr *h, int slot, int grid,
+                             cudaStream_t s) {
+  k_batch_dot<<<grid, A_THREADS, 0, s>>>(I, map, h, slot);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_update(const BatchInst *I, const BatchVB *map, const BatchHdr *h, int slot, int grid,
+                                int max_ld, cudaStream_t s) {
+  k_batch_update<<<grid, B_THREADS, (size_t)2 * max_ld * sizeof(f2x), s>>>(I, map, h, slot);
+  return cudaGetLastError();
+}
+
+// kernel attributes, set before a cycle is captured
+cudaError_t batch_prepare_restart(int max_ld) {
+  return cudaFuncSetAttribute(k_batch_restart, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)restart_smem_bytes(max_ld, max_ld));
+}
+
+cudaError_t launch_batch_restart(const BatchInst *I, const BatchVB *map, const BatchHdr *h, int grid, int max_ld,
+                                 cudaStream_t s) {
+  k_batch_restart<<<grid, R_THREADS, restart_smem_bytes(max_ld, max_ld), s>>>(I, map, h);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_control(BatchInst *I, const int *list, const BatchHdr *h, BatchStatus *status,
+                                 int grid_inst, cudaStream_t s) {
+  k_batch_control<<<(grid_inst + 127) / 128, 128, 0, s>>>(I, list, h, status);
+  return cudaGetLastError();
+}
+
+}  // namespace ksg

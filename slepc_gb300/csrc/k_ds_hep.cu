@@ -13,6 +13,7 @@
 // shared memory (n <= 144).
 #include <float.h>
 
+#include "batch_types.h"
 #include "common.cuh"
 #include "kernels.h"
 #include "ks_types.h"
@@ -49,8 +50,8 @@ KS_DEVICE int ds_compare(int which, double ar, double ai, double br, double bi) 
   }
 }
 
-__global__ void __launch_bounds__(DS_THREADS, 1) k_ds_hep(DSArgs a) {
-  extern __shared__ double Qs[];  // n x n, column-major with leading dimension n
+// Qs: n x n shared scratch, column-major with leading dimension n
+KS_DEVICE void ds_hep_body(const DSArgs &a, double *Qs) {
   __shared__ double sd[DS_MAXN], se[DS_MAXN], rc[DS_MAXN], rs[DS_MAXN], serr[DS_MAXN];
   __shared__ int sperm[DS_MAXN], sw_a[DS_MAXN], sw_b[DS_MAXN];
   __shared__ int s_cmd, s_lo, s_hi, s_nsw, s_fail;
@@ -297,6 +298,34 @@ __global__ void __launch_bounds__(DS_THREADS, 1) k_ds_hep(DSArgs a) {
     ctl->ds_error = s_fail;
     ctl->beta = beta;
   }
+}
+
+__global__ void __launch_bounds__(DS_THREADS, 1) k_ds_hep(DSArgs a) {
+  extern __shared__ double Qs[];
+  ds_hep_body(a, Qs);
+}
+
+// one block per instance of a batch whose projected problem is symmetric (grid-stride over the live list)
+__global__ void __launch_bounds__(DS_THREADS) k_batch_ds_hep(const BatchInst *I, const int *list, const BatchHdr *h) {
+  extern __shared__ double Qs[];
+  for (int v = blockIdx.x; v < h->n_inst; v += gridDim.x) {
+    const BatchInst &p = I[list[v]];
+    if (p.phase != BP_ITER || !p.hermitian) continue;
+    __syncthreads();
+    ds_hep_body(batch_ds_args(p), Qs);
+  }
+}
+
+cudaError_t batch_prepare_ds_hep(int max_ld) {
+  if (max_ld > DS_MAXN) return cudaErrorInvalidValue;
+  return cudaFuncSetAttribute(k_batch_ds_hep, cudaFuncAttributeMaxDynamicSharedMemorySize, max_ld * max_ld * 8);
+}
+
+cudaError_t launch_batch_ds_hep(const BatchInst *I, const int *list, const BatchHdr *h, int grid, int max_ld,
+                                cudaStream_t s) {
+  if (max_ld > DS_MAXN) return cudaErrorInvalidValue;
+  k_batch_ds_hep<<<grid, DS_THREADS, (size_t)max_ld * max_ld * 8, s>>>(I, list, h);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_ds_hep(const DSArgs &a, int n_max, cudaStream_t s) {

@@ -14,6 +14,7 @@
 // A and Q stay in global memory (they are at most 144 x 144 and L1/L2 resident).
 #include <float.h>
 
+#include "batch_types.h"
 #include "common.cuh"
 #include "kernels.h"
 #include "ks_types.h"
@@ -636,7 +637,7 @@ __device__ int nh_eigvec(const double *A, int ld, int n, int k, double tnorm, do
   return 1;
 }
 
-__global__ void __launch_bounds__(32) k_ds_nhep(DSArgs a) {
+KS_DEVICE void ds_nhep_body(const DSArgs &a) {
   __shared__ NhShared sh;
   __shared__ double wr[NH_MAXN], wi[NH_MAXN], errs[NH_MAXN];
   const int lane = lane_id();
@@ -795,6 +796,18 @@ __global__ void __launch_bounds__(32) k_ds_nhep(DSArgs a) {
   }
 }
 
+__global__ void __launch_bounds__(32) k_ds_nhep(DSArgs a) { ds_nhep_body(a); }
+
+// one warp per non-symmetric instance of a batch (grid-stride over the live list)
+__global__ void __launch_bounds__(32) k_batch_ds_nhep(const BatchInst *I, const int *list, const BatchHdr *h) {
+  for (int v = blockIdx.x; v < h->n_inst; v += gridDim.x) {
+    const BatchInst &p = I[list[v]];
+    if (p.phase != BP_ITER || p.hermitian) continue;
+    __syncwarp();
+    ds_nhep_body(batch_ds_args(p));
+  }
+}
+
 // eigenvectors of the leading n x n quasi-triangular block, normalised (DSVectors_NHEP_Eigen_All with back = "A")
 __global__ void __launch_bounds__(32) k_nhep_vectors(const double *A, int ld, int n, double *X) {
   const int lane = lane_id();
@@ -818,6 +831,13 @@ __global__ void __launch_bounds__(32) k_nhep_vectors(const double *A, int ld, in
 cudaError_t launch_ds_nhep(const DSArgs &a, int n_max, cudaStream_t s) {
   if (n_max > NH_MAXN) return cudaErrorInvalidValue;
   k_ds_nhep<<<1, 32, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_ds_nhep(const BatchInst *I, const int *list, const BatchHdr *h, int grid, int max_ld,
+                                 cudaStream_t s) {
+  if (max_ld > NH_MAXN) return cudaErrorInvalidValue;
+  k_batch_ds_nhep<<<grid, 32, 0, s>>>(I, list, h);
   return cudaGetLastError();
 }
 

@@ -108,7 +108,17 @@ static void spmv_dispatch(const int *rp, const int *ci, const double *va, const 
   }
 }
 
-static int spmv_blocks(int n, int lanes) {
+int spmv_blocks_for(int n, int lanes);
+static int spmv_blocks(int n, int lanes) { return spmv_blocks_for(n, lanes); }
+
+int restart_blocks_for(int n) {
+  const int ntiles = (n + R_ROWS - 1) / R_ROWS;
+  int blocks = num_sms();
+  if (blocks > ntiles) blocks = ntiles;
+  return blocks < 1 ? 1 : blocks;
+}
+
+int spmv_blocks_for(int n, int lanes) {
   const long long rows_per_block = (256 / 32) * (32 / lanes);
   long long blocks = (n + rows_per_block - 1) / rows_per_block;
   const long long cap = (long long)num_sms() * 16;

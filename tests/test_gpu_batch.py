@@ -1,0 +1,104 @@
+"""GPU: EPSGB300SolveBatch, the batched engine (many problems per launch, one restart cycle per CUDA graph).
+
+Every instance runs the single-problem path's device bodies with the same block partition, so a problem's results
+are bit-identical alone (EPSSolve with the FP64 QR projected solver, or a batch of one) and inside any mix; the
+eigenvalues are also checked against the oracle at 1e-10 and the residuals against tol."""
+import numpy as np
+import pytest
+
+import slepc_gb300 as sg
+from slepc_gb300 import matgen
+
+pytestmark = pytest.mark.gpu
+
+
+def make(csr, hermitian, which, nev, ncv, tol, seed, ds=None):
+    A = sg.Mat(*csr)
+    eps = sg.EPS().create()
+    eps.setOperators(A)
+    eps.setProblemType(sg.EPS.ProblemType.HEP if hermitian else sg.EPS.ProblemType.NHEP)
+    eps.setDimensions(nev, ncv)
+    eps.setTolerances(tol)
+    eps.setWhichEigenpairs(which)
+    if ds:
+        eps.setProjectedSolver(ds)
+    eps.setInitialSpace(matgen.start_vector(len(csr[0]) - 1, seed))
+    eps._A = A  # keep the matrix alive as long as the solver
+    return eps
+
+
+def results(eps):
+    nconv = eps.getConverged()
+    n = eps._A.m
+    vals, vecs = [], []
+    for i in range(nconv):
+        x = np.zeros(n)
+        v = eps.getEigenpair(i, x)
+        vals.append(v)
+        vecs.append(x)
+    return nconv, eps.getIterationNumber(), eps.getConvergedReason(), vals, vecs
+
+
+def mixed_problems():
+    probs = []
+    for i, n in enumerate([1000, 1500, 2304, 3000, 4096]):
+        probs.append((matgen.laplacian_2d_randdiag(n, 100 + i), True, "LM", 8, 24, 1e-10, 6 + i))
+    probs.append((matgen.convection_diffusion_2d(40, 10.0), False, "LR", 6, 24, 1e-10, 3))
+    probs.append((matgen.laplacian_3d(14), True, "SR", 6, 24, 1e-10, 9))
+    return probs
+
+
+def test_batch_equals_single_problem_path(lib):
+    probs = mixed_problems()
+    batch = [make(*p) for p in probs]
+    sg.solve_batch(batch)
+    for p, b in zip(probs, batch):
+        alone = make(*p, ds="qr")
+        alone.solve()
+        ra, rb = results(alone), results(b)
+        assert ra[0] == rb[0] and ra[1] == rb[1] and ra[2] == rb[2] == 1
+        assert ra[3] == rb[3], (ra[3], rb[3])
+        for xa, xb in zip(ra[4], rb[4]):
+            assert np.array_equal(xa, xb)
+
+
+def test_batch_alone_equals_in_mix(lib):
+    probs = mixed_problems()
+    mix = [make(*p) for p in probs]
+    sg.solve_batch(mix)
+    for k in (0, 3, 5):
+        one = [make(*probs[k])]
+        sg.solve_batch(one)
+        r1, rm = results(one[0]), results(mix[k])
+        assert r1[:3] == rm[:3] and r1[3] == rm[3]
+        for xa, xb in zip(r1[4], rm[4]):
+            assert np.array_equal(xa, xb)
+
+
+def test_batch_parity_with_oracle(lib, orc):
+    probs = mixed_problems()
+    batch = [make(*p) for p in probs]
+    sg.solve_batch(batch)
+    for (csr, herm, which, nev, ncv, tol, seed), b in zip(probs, batch):
+        nconv, its, reason, vals, vecs = results(b)
+        assert reason == 1 and nconv >= nev
+        ref = orc.solve(*csr, hermitian=herm, which=which, nev=nev, ncv=ncv, tol=tol,
+                        v0=matgen.start_vector(len(csr[0]) - 1, seed))
+        refv = np.asarray(ref.eigr[:ref.nconv]) + 1j * np.asarray(ref.eigi[:ref.nconv])
+        for v in vals[:nev]:
+            assert np.min(np.abs(refv - v)) / abs(v) <= 1e-10
+        A = sg.Mat(*csr)
+        nrm = max(np.add.reduceat(np.abs(csr[2]), csr[0][:-1]))
+        for v, x in zip(vals, vecs):
+            if isinstance(v, complex):
+                continue
+            assert np.linalg.norm(A.mult(x) - v * x) / (nrm * abs(v)) <= tol
+
+
+def test_batch_zero_start_vector_error(lib):
+    csr = matgen.laplacian_1d(200)
+    eps = make(csr, True, "LM", 2, 10, 1e-8, 1)
+    eps.setInitialSpace(np.zeros(200))
+    with pytest.raises(sg.SlepcError) as ei:
+        sg.solve_batch([eps])
+    assert ei.value.code == 77
