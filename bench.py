@@ -47,6 +47,10 @@ WORKLOADS = {
                          gen=lambda mg: mg.convection_diffusion_2d(1000, 10.0), hermitian=False, which="LR", nev=20,
                          ncv=64, tol=1e-10, seed=3),
 }
+BATCH = dict(desc="4096 independent EPS_HEP problems, n_i = round(exp(U[ln 1000, ln 65536])) (splitmix64 seed 6+i), "
+                  "2-D 5-point Laplacian on an r x c grid (r = floor(sqrt n_i), c = ceil(n_i/r)) plus diag(U[0,1]) "
+                  "(seed 6+i), nev=8 largest magnitude, ncv=24, tol=1e-10, start vector seed 6+i",
+             count=4096, nev=8, ncv=24, tol=1e-10, which="LM")
 METRIC = "converged eigenpairs/s at tol 1e-10 (plain Krylov-Schur, one solve per step)"
 UNIT = "eigenpairs/s"
 
@@ -184,22 +188,178 @@ def run_reference(args, wl):
     print(json.dumps(line), flush=True)
 
 
+def batch_instances(matgen, count):
+    """The batched workload's matrices (CSR) and start-vector seeds."""
+    out = []
+    for i in range(count):
+        u = matgen.uniform_01(6 + i, 1)[0]
+        n = int(round(np.exp(np.log(1000.0) + u * (np.log(65536.0) - np.log(1000.0)))))
+        out.append((matgen.laplacian_2d_randdiag(n, 6 + i), 6 + i))
+    return out
+
+
+def run_batch(args):
+    """Batched form: all problems in one EPSGB300SolveBatch per step, beside the one-problem-per-launch EPSSolve
+    path on a stratified sample of the same problems."""
+    import slepc_gb300 as sg
+    from slepc_gb300 import matgen
+    import ctypes
+
+    sg.build()
+    ctypes.CDLL("libcudart.so").cudaSetDevice(0)
+    count = args.batch_count or BATCH["count"]
+    t = time.time()
+    inst = batch_instances(matgen, count)
+    gen_s = time.time() - t
+    nsum = sum(len(c[0]) - 1 for c, _ in inst)
+
+    def make(csr, seed, A=None):
+        A = A or sg.Mat(*csr)
+        e = sg.EPS().create()
+        e.setOperators(A)
+        e.setProblemType(sg.EPS.ProblemType.HEP)
+        e.setDimensions(BATCH["nev"], BATCH["ncv"])
+        e.setTolerances(BATCH["tol"])
+        e.setWhichEigenpairs(BATCH["which"])
+        e.setInitialSpace(matgen.start_vector(len(csr[0]) - 1, seed))
+        e._A = A
+        return e
+
+    t = time.time()
+    tuning = sg.batch_tune(1, 7) if not args.no_tune else sg.batch_get_tuning()
+    tune_s = time.time() - t
+    t = time.time()
+    eps = [make(c, sd) for c, sd in inst]
+    for e in eps:
+        e.setUp()
+    setup_s = time.time() - t
+    for _ in range(args.warmup):
+        sg.solve_batch(eps)
+    clocks = ClockSampler(0)
+    clocks.start()
+    times, conv = [], []
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        sg.solve_batch(eps)
+        times.append(time.perf_counter() - t)
+        conv.append(sum(BATCH["nev"] for e in eps if e.getConvergedReason() == 1 and e.getConverged() >= BATCH["nev"]))
+    clk = clocks.stop()
+    value = sum(conv) / sum(times)
+    its = [e.getIterationNumber() for e in eps]
+    launches = eps[0].getStats()["kernel_launches"] * args.steps
+
+    # the plain path: EPSSolve one problem at a time, on every (count/sample)-th problem in order of size
+    order = sorted(range(count), key=lambda i: len(inst[i][0][0]))
+    sample = order[:: max(1, count // args.batch_plain_sample)]
+    plain_eps = [eps[i] for i in sample]
+    for e in plain_eps[:3]:
+        e.solve()
+    t = time.perf_counter()
+    pconv = 0
+    for e in plain_eps:
+        e.solve()
+        pconv += BATCH["nev"] if (e.getConvergedReason() == 1 and e.getConverged() >= BATCH["nev"]) else 0
+    plain_s = time.perf_counter() - t
+    plain_value = pconv / plain_s
+
+    # e2e: matrices from host CSR, setup, batched solve, every eigenpair back to the host
+    e2e = None
+    if not args.no_e2e:
+        t = time.perf_counter()
+        eps2 = [make(c, sd) for c, sd in inst]
+        sg.solve_batch(eps2)
+        d2h = 0
+        for e in eps2:
+            x = np.empty(e._A.m)
+            for i in range(BATCH["nev"]):
+                e.getEigenpair(i, x)
+            d2h += BATCH["nev"] * (x.nbytes + 16)
+        e2e_s = time.perf_counter() - t
+        h2d = sum(c[0].nbytes + c[1].nbytes + c[2].nbytes + 8 * (len(c[0]) - 1) for c, _ in inst)
+        e2e = {"value": sum(BATCH["nev"] for e in eps2 if e.getConvergedReason() == 1) / e2e_s, "unit": UNIT,
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+        for e in eps2:
+            e.destroy()
+    line = {"metric": METRIC.replace("plain Krylov-Schur", "batched Krylov-Schur"), "value": value, "unit": UNIT,
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * sum(times) / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": BATCH["desc"].replace("4096", str(count)), "instances": count, "sum_n": nsum,
+                       "arith": "pair", "parallelism": "replicas x1", "l2": "inputs larger than L2 (bases 13 GB)",
+                       "restarts_per_instance": {"min": min(its), "median": float(np.median(its)), "max": max(its)},
+                       "generate_s": round(gen_s, 1), "setup_s": round(setup_s, 1),
+                       "tuning": {"tiles_per_virtual_block_by_bucket": tuning, "tune_s": round(tune_s, 1)}},
+            "plain": {"value": plain_value, "unit": UNIT, "sample": f"{len(plain_eps)} of {count} problems "
+                      "(every k-th by size), EPSSolve one at a time", "seconds": plain_s},
+            "speedup_vs_plain": value / plain_value, "e2e": e2e, "clocks": clk, "gpu_launches": launches}
+    print(json.dumps(line), flush=True)
+
+
+def run_batch_reference(args):
+    """The reference algorithm (the oracle port of SLEPc's Krylov-Schur) on the host cores, one problem after
+    another as the reference would solve them, over a stratified sample of the batched workload."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import oracle
+    from slepc_gb300 import matgen
+
+    oracle.build()
+    count = args.batch_count or BATCH["count"]
+    inst = batch_instances(matgen, count)
+    order = sorted(range(count), key=lambda i: len(inst[i][0][0]))
+    sample = order[:: max(1, count // 64)]
+    cores = os.cpu_count() or 1
+    vals = []
+    for k in range(args.warmup + args.steps):
+        t = time.time()
+        conv = 0
+        for i in (sample[:4] if k < args.warmup else sample):
+            csr, seed = inst[i]
+            r = oracle.solve(*csr, hermitian=True, which=BATCH["which"], nev=BATCH["nev"], ncv=BATCH["ncv"],
+                             tol=BATCH["tol"], v0=matgen.start_vector(len(csr[0]) - 1, seed), nthreads=cores,
+                             vectors=False)
+            conv += BATCH["nev"] if (r.reason == 1 and r.nconv >= BATCH["nev"]) else 0
+        if k >= args.warmup:
+            vals.append(conv / (time.time() - t))
+    v = statistics.median(vals)
+    line = {"impl": "reference", "metric": METRIC.replace("plain Krylov-Schur", "batched Krylov-Schur"), "value": v,
+            "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 * BATCH["nev"] * len(sample) / v, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": BATCH["desc"].replace("4096", str(count)),
+                       "impl": "oracle port of SLEPc 3.22 Krylov-Schur, one problem at a time, OpenMP over rows"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{len(sample)} of {count} problems (every k-th by size), complete solves"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="lap3d128", choices=list(WORKLOADS))
+    ap.add_argument("--workload", default="lap3d128", choices=list(WORKLOADS) + ["batch4096"])
+    ap.add_argument("--batch-count", type=int, default=0, help="problems in the batched workload (default 4096)")
+    ap.add_argument("--batch-plain-sample", type=int, default=256,
+                    help="problems of the batched workload timed through the one-problem-per-launch path")
     ap.add_argument("--arith", default="pair", choices=["pair", "f64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="batched workload: keep the default tuning table")
     ap.add_argument("--profile-case", action="store_true",
                     help="run exactly one solve limited to 2 restarts and exit (the ncu capture case)")
     ap.add_argument("--profile-solve", action="store_true",
                     help="run exactly one complete solve and exit (the ncu launch-list case: same work as a step)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.workload == "batch4096":
+        if args.impl == "reference":
+            run_batch_reference(args)
+            return
+        run_batch(args)
+        return
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":
         run_reference(args, wl)

@@ -70,6 +70,14 @@ PetscErrorCode EPSGB300GetDeviceBasis(EPS eps, const double **V, PetscInt *ld);
  * The symmetric projected problems use the FP64 QR solver (EPS_GB300_DS_QR). */
 PetscErrorCode EPSGB300SolveBatch(PetscInt count, EPS *eps);
 
+/* Tuning of the batched engine: Gram-Schmidt tiles (512 rows) per virtual block for each size bucket b, which
+ * holds n in [2^(b+9), 2^(b+10)) (b = 0..13).  The table fixes each problem's summation partition, so results are
+ * reproducible for a given table.  EPSGB300BatchTune measures buckets first..last on one restart cycle of a batch
+ * that fills the GPU, trying 1, 2, 4, 8, 16 and 32 tiles, and keeps the fastest. */
+PetscErrorCode EPSGB300BatchTune(PetscInt first_bucket, PetscInt last_bucket);
+PetscErrorCode EPSGB300BatchGetTuning(PetscInt *tiles, PetscInt count);
+PetscErrorCode EPSGB300BatchSetTuning(const PetscInt *tiles, PetscInt count);
+
 /* Orthogonality ||V^T V - I||_max of the first nconv columns, computed on the device in FP64. */
 PetscErrorCode EPSGB300OrthogonalityError(EPS eps, PetscReal *err);
 

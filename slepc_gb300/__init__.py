@@ -72,6 +72,9 @@ def load():
         "EPSGB300SetArithmetic": ([P, I], I),
         "EPSGB300SetProjectedSolver": ([P, I], I),
         "EPSGB300SolveBatch": ([I, ctypes.POINTER(P)], I),
+        "EPSGB300BatchTune": ([I, I], I),
+        "EPSGB300BatchGetTuning": ([ctypes.POINTER(I), I], I),
+        "EPSGB300BatchSetTuning": ([ctypes.POINTER(I), I], I),
         "EPSGB300GetStats": ([P, P], I),
         "EPSGB300OrthogonalityError": ([P, P], I),
         "EPSGB300SetProfiling": ([P, I], I),
@@ -346,6 +349,26 @@ def solve_batch(eps_list):
     """EPSGB300SolveBatch over configured EPS objects (the batched engine); results are read from each EPS."""
     arr = (ctypes.c_void_p * len(eps_list))(*[e.handle for e in eps_list])
     _check(load().EPSGB300SolveBatch(len(eps_list), arr), "EPSGB300SolveBatch")
+
+
+BATCH_BUCKETS = 14
+
+
+def batch_tune(first_bucket=1, last_bucket=7):
+    """Measure the batched engine's tiles per virtual block for size buckets first..last; returns the table."""
+    _check(load().EPSGB300BatchTune(first_bucket, last_bucket), "EPSGB300BatchTune")
+    return batch_get_tuning()
+
+
+def batch_get_tuning():
+    arr = (ctypes.c_int * BATCH_BUCKETS)()
+    _check(load().EPSGB300BatchGetTuning(arr, BATCH_BUCKETS), "EPSGB300BatchGetTuning")
+    return list(arr)
+
+
+def batch_set_tuning(tiles):
+    arr = (ctypes.c_int * BATCH_BUCKETS)(*tiles)
+    _check(load().EPSGB300BatchSetTuning(arr, len(tiles)), "EPSGB300BatchSetTuning")
 
 
 def solve(csr, *, hermitian=True, which="LM", nev=1, ncv=None, mpd=None, tol=None, max_it=None, v0=None,

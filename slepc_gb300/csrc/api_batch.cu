@@ -6,6 +6,7 @@
 // per instance after each cycle, hands breakdowns back to the single-problem code, and retires solved instances.
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <cstring>
 #include <vector>
 
@@ -40,13 +41,37 @@ struct BatchEngine {
   }
 };
 
-// work lists of the live instances: virtual-block counts equal the single-problem kernels' grids for that n
+// Size buckets of the tuning table: bucket b holds n in [2^(b+9), 2^(b+10)), clamped to [0, BATCH_BUCKETS).
+constexpr int BATCH_BUCKETS = 14;
+constexpr int GS_TILE_ROWS = 512;  // rows per tile of both Gram-Schmidt kernels
+constexpr int SPMV_VB_ROWS = 256;  // rows per pass of one 256-thread SpMV block (one row per thread)
+
+// tiles per virtual block of the Gram-Schmidt kernels, per size bucket (EPSGB300BatchTune measures them)
+int g_gs_tpv[BATCH_BUCKETS] = {8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8};
+
+int batch_bucket(int n) {
+  int b = 0;
+  while (b + 1 < BATCH_BUCKETS && n >= (1 << (b + 10))) ++b;
+  return b;
+}
+
+// virtual blocks of instance n in each kernel.  The Gram-Schmidt counts decide the summation partition (and so
+// the rounding) of an instance; they depend on n and the tuning table only, never on the rest of the batch.
+int batch_gs_vbs(int n, int cap) {
+  const int ntiles = (n + GS_TILE_ROWS - 1) / GS_TILE_ROWS;
+  const int tpv = g_gs_tpv[batch_bucket(n)];
+  int nb = (ntiles + tpv - 1) / tpv;
+  return std::max(1, std::min(nb, cap));
+}
+
+// work lists of the live instances
 PetscErrorCode batch_upload_maps(BatchEngine &B, const std::vector<BatchInst> &hi, const std::vector<int> &live) {
   std::vector<BatchVB> ms, md, mu, mr;
   for (int i : live) {
     const BatchInst &p = hi[i];
-    const int ns = spmv_blocks_for(p.n, p.lanes), nd = gs_dot_blocks(p.n), nu = gs_update_blocks(p.n),
-              nr = restart_blocks_for(p.n);
+    const int ns = std::max(1, std::min(spmv_blocks_for(p.n, p.lanes), (p.n + 8 * SPMV_VB_ROWS - 1) / (8 * SPMV_VB_ROWS)));
+    const int nd = batch_gs_vbs(p.n, gs_dot_blocks(p.n)), nu = batch_gs_vbs(p.n, gs_update_blocks(p.n));
+    const int nr = std::max(1, std::min(restart_blocks_for(p.n), (p.n + 1023) / 1024));
     for (int b = 0; b < ns; ++b) ms.push_back({i, b, ns, 0});
     for (int b = 0; b < nd; ++b) md.push_back({i, b, nd, 0});
     for (int b = 0; b < nu; ++b) mu.push_back({i, b, nu, 0});
@@ -301,6 +326,93 @@ extern "C" PetscErrorCode EPSGB300SolveBatch(PetscInt count, EPS *eps) {
   for (int i = 0; i < count; ++i) {
     eps[i]->stats.solve_seconds = secs;
     eps[i]->stats.kernel_launches = cycles * B.launches_per_cycle;
+  }
+  return 0;
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// Autotuner: tiles per virtual block of the Gram-Schmidt kernels, per size bucket, measured on one restart cycle of
+// a GPU-filling batch of 2-D Laplacians (plus a fixed diagonal) of the bucket's middle size.
+// ---------------------------------------------------------------------------------------------------------------
+extern "C" PetscErrorCode EPSGB300BatchGetTuning(PetscInt *tiles, PetscInt count) {
+  KSG_CHECK(tiles, PETSC_ERR_ARG_NULL, "Null argument");
+  for (int b = 0; b < count && b < BATCH_BUCKETS; ++b) tiles[b] = g_gs_tpv[b];
+  return 0;
+}
+
+extern "C" PetscErrorCode EPSGB300BatchSetTuning(const PetscInt *tiles, PetscInt count) {
+  KSG_CHECK(tiles, PETSC_ERR_ARG_NULL, "Null argument");
+  for (int b = 0; b < count && b < BATCH_BUCKETS; ++b)
+    KSG_CHECK(tiles[b] >= 1 && tiles[b] <= 1024, PETSC_ERR_ARG_OUTOFRANGE, "tiles per block %d out of range",
+              (int)tiles[b]);
+  for (int b = 0; b < count && b < BATCH_BUCKETS; ++b) g_gs_tpv[b] = tiles[b];
+  return 0;
+}
+
+extern "C" PetscErrorCode EPSGB300BatchTune(PetscInt first_bucket, PetscInt last_bucket) {
+  KSG_CHECK(first_bucket >= 0 && last_bucket < BATCH_BUCKETS && first_bucket <= last_bucket,
+            PETSC_ERR_ARG_OUTOFRANGE, "buckets must lie in [0, %d]", BATCH_BUCKETS - 1);
+  const int cand[] = {1, 2, 4, 8, 16, 32};
+  for (int b = (int)first_bucket; b <= (int)last_bucket; ++b) {
+    const int nt = 3 << (b + 8);  // middle of [2^(b+9), 2^(b+10))
+    const int r = (int)std::sqrt((double)nt), c = (nt + r - 1) / r, n = r * c;
+    const int count = std::max(8, std::min(1024, (1 << 23) / n));
+    // CSR of the r x c 5-point Laplacian plus diag(0.5 + 0.5 sin(i))
+    std::vector<PetscInt> rp(n + 1), ci;
+    std::vector<PetscScalar> va;
+    ci.reserve(5 * (size_t)n);
+    va.reserve(5 * (size_t)n);
+    for (int i = 0; i < r; ++i)
+      for (int j = 0; j < c; ++j) {
+        const int row = i * c + j;
+        auto add = [&](int col, double v) { ci.push_back(col); va.push_back(v); };
+        if (i > 0) add(row - c, -1.0);
+        if (j > 0) add(row - 1, -1.0);
+        add(row, 4.0 + 0.5 + 0.5 * std::sin((double)row));
+        if (j < c - 1) add(row + 1, -1.0);
+        if (i < r - 1) add(row + c, -1.0);
+        rp[row + 1] = (PetscInt)ci.size();
+      }
+    std::vector<double> v0(n);
+    for (int i = 0; i < n; ++i) v0[i] = std::sin(0.37 * i + 1.0) + 0.25 * std::cos(1.91 * i);
+    std::vector<Mat> mats(count, nullptr);
+    std::vector<EPS> eps(count, nullptr);
+    std::vector<Vec> vecs(count, nullptr);
+    PetscErrorCode ierr = 0;
+    for (int k = 0; k < count && !ierr; ++k) {
+      ierr = MatCreateSeqAIJWithArrays(0, n, n, rp.data(), ci.data(), va.data(), &mats[k]);
+      if (!ierr) ierr = EPSCreate(0, &eps[k]);
+      if (!ierr) ierr = EPSSetOperators(eps[k], mats[k], nullptr);
+      if (!ierr) ierr = EPSSetProblemType(eps[k], EPS_HEP);
+      if (!ierr) ierr = EPSSetDimensions(eps[k], 8, 24, PETSC_DETERMINE);
+      if (!ierr) ierr = EPSSetTolerances(eps[k], 1e-10, 1);
+      if (!ierr) ierr = EPSSetWhichEigenpairs(eps[k], EPS_LARGEST_MAGNITUDE);
+      if (!ierr) ierr = VecCreateSeqWithArray(0, 1, n, v0.data(), &vecs[k]);
+      if (!ierr) ierr = EPSSetInitialSpace(eps[k], 1, &vecs[k]);
+    }
+    int best = g_gs_tpv[b];
+    double best_t = 1e30;
+    for (int ci_ = 0; ci_ < (int)(sizeof(cand) / sizeof(cand[0])) && !ierr; ++ci_) {
+      g_gs_tpv[b] = cand[ci_];
+      double t_min = 1e30;
+      for (int rep = 0; rep < 3 && !ierr; ++rep) {
+        auto t0 = std::chrono::steady_clock::now();
+        ierr = EPSGB300SolveBatch(count, eps.data());
+        const double t = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (rep > 0) t_min = std::min(t_min, t);
+      }
+      if (t_min < best_t) {
+        best_t = t_min;
+        best = cand[ci_];
+      }
+    }
+    g_gs_tpv[b] = best;
+    for (int k = 0; k < count; ++k) {
+      if (eps[k]) EPSDestroy(&eps[k]);
+      if (mats[k]) MatDestroy(&mats[k]);
+      if (vecs[k]) VecDestroy(&vecs[k]);
+    }
+    KSG_TRY(ierr);
   }
   return 0;
 }

@@ -163,7 +163,7 @@ __global__ void __launch_bounds__(A_THREADS, 1) k_batch_dot(const BatchInst *I, 
   }
 }
 
-__global__ void __launch_bounds__(B_THREADS) k_batch_update(const BatchInst *I, const BatchVB *map,
+__global__ void __launch_bounds__(B_THREADS, 2) k_batch_update(const BatchInst *I, const BatchVB *map,
                                                             const BatchHdr *h, int slot) {
   const int nmap = h->n_upd;
   for (int v = blockIdx.x; v < nmap; v += gridDim.x) {

@@ -49,17 +49,42 @@ def mixed_problems():
 
 
 def test_batch_equals_single_problem_path(lib):
+    """With one tile per virtual block the batch partitions every reduction exactly as the single-problem kernels
+    do, so the results are bit-identical to EPSSolve with the same (QR) projected solver."""
+    saved = sg.batch_get_tuning()
+    try:
+        sg.batch_set_tuning([1] * sg.BATCH_BUCKETS)
+        probs = mixed_problems()
+        batch = [make(*p) for p in probs]
+        sg.solve_batch(batch)
+        for p, b in zip(probs, batch):
+            alone = make(*p, ds="qr")
+            alone.solve()
+            ra, rb = results(alone), results(b)
+            assert ra[0] == rb[0] and ra[1] == rb[1] and ra[2] == rb[2] == 1
+            assert ra[3] == rb[3], (ra[3], rb[3])
+            for xa, xb in zip(ra[4], rb[4]):
+                assert np.array_equal(xa, xb)
+    finally:
+        sg.batch_set_tuning(saved)
+
+
+def test_batch_tuned_matches_single_problem_path(lib):
+    """With the default tuning (several tiles per virtual block) only the summation order changes; both runs
+    converge to tol 1e-10, and their eigenvalues agree within the parity tolerance 1e-10 (relative)."""
     probs = mixed_problems()
     batch = [make(*p) for p in probs]
     sg.solve_batch(batch)
     for p, b in zip(probs, batch):
+        nev = p[3]
         alone = make(*p, ds="qr")
         alone.solve()
         ra, rb = results(alone), results(b)
-        assert ra[0] == rb[0] and ra[1] == rb[1] and ra[2] == rb[2] == 1
-        assert ra[3] == rb[3], (ra[3], rb[3])
-        for xa, xb in zip(ra[4], rb[4]):
-            assert np.array_equal(xa, xb)
+        assert ra[2] == rb[2] == 1 and min(ra[0], rb[0]) >= nev
+        # set-based: degenerate spectra (the 3-D Laplacian) may gain copies in a different order
+        vb = np.asarray(rb[3])
+        for va in ra[3][:nev]:
+            assert np.min(np.abs(vb - va)) <= 1e-10 * abs(va)
 
 
 def test_batch_alone_equals_in_mix(lib):
