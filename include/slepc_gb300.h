@@ -70,6 +70,28 @@ PetscErrorCode EPSGB300GetDeviceBasis(EPS eps, const double **V, PetscInt *ld);
  * The symmetric projected problems use the FP64 QR solver (EPS_GB300_DS_QR). */
 PetscErrorCode EPSGB300SolveBatch(PetscInt count, EPS *eps);
 
+/* Serving: a request loop on its own host thread that solves eigenproblems as they arrive (continuous batching).
+ * EPSGB300ServerSubmit takes a configured EPS (operators, problem type, dimensions, tolerances, which, initial
+ * space; EPSSetUp is done by the server) and returns at once; the request is admitted when its footprint
+ * n (ncv+1) 8 + nnz 12 bytes fits the HBM budget next to the solves already admitted (a request larger than the
+ * budget is admitted alone), joins the solves on the GPU at their next restart cycle, and is retired when its
+ * restart loop ends.  EPSGB300ServerWait blocks until the EPS holds its results (timeout < 0: no limit), after which
+ * the usual EPSGet* calls read them and EPSGB300GetStats' solve_seconds is the latency from submission to result.
+ * The client must not touch a submitted EPS until Wait reports it done.  Results do not depend on what else is
+ * served at the same time.  max_requests bounds the solves admitted at once, max_ncv the ncv of any request
+ * (<= 79).  Destroy waits for every submitted request.  No counterpart in the reference. */
+typedef struct _p_EPSGB300Server *EPSGB300Server;
+typedef struct {
+  long long submitted, completed, failed, queued, live, max_live, cycles;
+  double bytes_in_use, peak_bytes;
+} EPSGB300ServerStats;
+PetscErrorCode EPSGB300ServerCreate(double hbm_budget_bytes, PetscInt max_requests, PetscInt max_ncv,
+                                    EPSGB300Server *server);
+PetscErrorCode EPSGB300ServerSubmit(EPSGB300Server server, EPS eps);
+PetscErrorCode EPSGB300ServerWait(EPSGB300Server server, EPS eps, double timeout_seconds, PetscBool *done);
+PetscErrorCode EPSGB300ServerGetStats(EPSGB300Server server, EPSGB300ServerStats *stats);
+PetscErrorCode EPSGB300ServerDestroy(EPSGB300Server *server);
+
 /* Tuning of the batched engine: Gram-Schmidt tiles (512 rows) per virtual block for each size bucket b, which
  * holds n in [2^(b+9), 2^(b+10)) (b = 0..13).  The table fixes each problem's summation partition, so results are
  * reproducible for a given table.  EPSGB300BatchTune measures buckets first..last on one restart cycle of a batch

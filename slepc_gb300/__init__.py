@@ -73,6 +73,11 @@ def load():
         "EPSGB300SetProjectedSolver": ([P, I], I),
         "EPSGB300SolveBatch": ([I, ctypes.POINTER(P)], I),
         "EPSGB300BatchTune": ([I, I], I),
+        "EPSGB300ServerCreate": ([D, I, I, PP], I),
+        "EPSGB300ServerSubmit": ([P, P], I),
+        "EPSGB300ServerWait": ([P, P, D, ctypes.POINTER(I)], I),
+        "EPSGB300ServerGetStats": ([P, P], I),
+        "EPSGB300ServerDestroy": ([PP], I),
         "EPSGB300BatchGetTuning": ([ctypes.POINTER(I), I], I),
         "EPSGB300BatchSetTuning": ([ctypes.POINTER(I), I], I),
         "EPSGB300GetStats": ([P, P], I),
@@ -352,6 +357,48 @@ def solve_batch(eps_list):
 
 
 BATCH_BUCKETS = 14
+
+
+class _ServerStats(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_longlong) for k in
+                ("submitted", "completed", "failed", "queued", "live", "max_live", "cycles")] + \
+               [("bytes_in_use", ctypes.c_double), ("peak_bytes", ctypes.c_double)]
+
+
+class Server:
+    """EPSGB300Server: continuous-batching request loop over the batched engine (its own host thread)."""
+
+    def __init__(self, hbm_budget_bytes, max_requests=4096, max_ncv=72):
+        h = ctypes.c_void_p()
+        _check(load().EPSGB300ServerCreate(float(hbm_budget_bytes), int(max_requests), int(max_ncv),
+                                           ctypes.byref(h)), "EPSGB300ServerCreate")
+        self.handle = h
+        self._inflight = {}
+
+    def submit(self, eps):
+        _check(load().EPSGB300ServerSubmit(self.handle, eps.handle), "EPSGB300ServerSubmit")
+        self._inflight[eps.handle.value] = eps
+
+    def wait(self, eps, timeout=-1.0):
+        done = ctypes.c_int(0)
+        try:
+            _check(load().EPSGB300ServerWait(self.handle, eps.handle, float(timeout), ctypes.byref(done)),
+                   "EPSGB300ServerWait")
+        finally:
+            if done.value:
+                self._inflight.pop(eps.handle.value, None)
+        return bool(done.value)
+
+    def stats(self):
+        st = _ServerStats()
+        _check(load().EPSGB300ServerGetStats(self.handle, ctypes.byref(st)), "EPSGB300ServerGetStats")
+        return {k: getattr(st, k) for k, _ in st._fields_}
+
+    def destroy(self):
+        if self.handle:
+            h = self.handle
+            self.handle = None
+            _check(load().EPSGB300ServerDestroy(ctypes.byref(h)), "EPSGB300ServerDestroy")
 
 
 def batch_tune(first_bucket=1, last_bucket=7):

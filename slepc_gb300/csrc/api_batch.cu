@@ -10,36 +10,12 @@
 #include <cstring>
 #include <vector>
 
+#include "batch_engine.h"
 #include "batch_types.h"
 #include "internal.h"
 #include "kernels.h"
 
-using namespace ksg;
-
-namespace {
-
-struct BatchEngine {
-  int device = 0;
-  cudaStream_t s = nullptr;
-  int cap = 0;          // instances
-  int slots = 0;        // slots per cycle: max ncv + 1 (steps 0..ncv-1, final pass at nv <= ncv)
-  int max_ld = 0;
-  int grid_spmv = 0, grid_dot = 0, grid_upd = 0, grid_rst = 0, grid_ds = 0, grid_inst = 0;
-  DBuf<BatchInst> inst;
-  DBuf<BatchVB> map_spmv, map_dot, map_upd, map_rst;
-  DBuf<int> list;
-  DBuf<BatchHdr> hdr;
-  DBuf<BatchStatus> status;
-  BatchStatus *h_status = nullptr;  // pinned
-  cudaGraphExec_t exec = nullptr;
-  long long launches_per_cycle = 0;
-
-  ~BatchEngine() {
-    if (exec) cudaGraphExecDestroy(exec);
-    if (h_status) cudaFreeHost(h_status);
-    if (s) cudaStreamDestroy(s);
-  }
-};
+namespace ksg {
 
 // Size buckets of the tuning table: bucket b holds n in [2^(b+9), 2^(b+10)), clamped to [0, BATCH_BUCKETS).
 constexpr int BATCH_BUCKETS = 14;
@@ -47,106 +23,30 @@ constexpr int GS_TILE_ROWS = 512;  // rows per tile of both Gram-Schmidt kernels
 constexpr int SPMV_VB_ROWS = 256;  // rows per pass of one 256-thread SpMV block (one row per thread)
 
 // tiles per virtual block of the Gram-Schmidt kernels, per size bucket (EPSGB300BatchTune measures them)
-int g_gs_tpv[BATCH_BUCKETS] = {8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8};
+static int g_gs_tpv[BATCH_BUCKETS] = {8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8, 8};
 
-int batch_bucket(int n) {
+static int batch_bucket(int n) {
   int b = 0;
   while (b + 1 < BATCH_BUCKETS && n >= (1 << (b + 10))) ++b;
   return b;
 }
 
-// virtual blocks of instance n in each kernel.  The Gram-Schmidt counts decide the summation partition (and so
-// the rounding) of an instance; they depend on n and the tuning table only, never on the rest of the batch.
-int batch_gs_vbs(int n, int cap) {
+// Virtual blocks of an instance of n rows.  The Gram-Schmidt counts decide the summation partition (and so the
+// rounding) of an instance; they depend on n and the tuning table only, never on the rest of the batch.
+static int batch_gs_vbs(int n, int cap) {
   const int ntiles = (n + GS_TILE_ROWS - 1) / GS_TILE_ROWS;
   const int tpv = g_gs_tpv[batch_bucket(n)];
-  int nb = (ntiles + tpv - 1) / tpv;
+  const int nb = (ntiles + tpv - 1) / tpv;
   return std::max(1, std::min(nb, cap));
 }
 
-// work lists of the live instances
-PetscErrorCode batch_upload_maps(BatchEngine &B, const std::vector<BatchInst> &hi, const std::vector<int> &live) {
-  std::vector<BatchVB> ms, md, mu, mr;
-  for (int i : live) {
-    const BatchInst &p = hi[i];
-    const int ns = std::max(1, std::min(spmv_blocks_for(p.n, p.lanes), (p.n + 8 * SPMV_VB_ROWS - 1) / (8 * SPMV_VB_ROWS)));
-    const int nd = batch_gs_vbs(p.n, gs_dot_blocks(p.n)), nu = batch_gs_vbs(p.n, gs_update_blocks(p.n));
-    const int nr = std::max(1, std::min(restart_blocks_for(p.n), (p.n + 1023) / 1024));
-    for (int b = 0; b < ns; ++b) ms.push_back({i, b, ns, 0});
-    for (int b = 0; b < nd; ++b) md.push_back({i, b, nd, 0});
-    for (int b = 0; b < nu; ++b) mu.push_back({i, b, nu, 0});
-    for (int b = 0; b < nr; ++b) mr.push_back({i, b, nr, 0});
-  }
-  auto up = [&](DBuf<BatchVB> &d, const std::vector<BatchVB> &h) -> cudaError_t {
-    if (h.size() > d.count) {
-      cudaError_t e = d.alloc(h.size() + h.size() / 4 + 16);
-      if (e != cudaSuccess) return e;
-    }
-    return h.empty() ? cudaSuccess
-                     : cudaMemcpyAsync(d.p, h.data(), h.size() * sizeof(BatchVB), cudaMemcpyHostToDevice, B.s);
-  };
-  KSG_CUDA(cudaStreamSynchronize(B.s));  // the previous lists may still be read by a running cycle
-  KSG_CUDA(up(B.map_spmv, ms));
-  KSG_CUDA(up(B.map_dot, md));
-  KSG_CUDA(up(B.map_upd, mu));
-  KSG_CUDA(up(B.map_rst, mr));
-  KSG_CUDA(cudaMemcpyAsync(B.list.p, live.data(), live.size() * sizeof(int), cudaMemcpyHostToDevice, B.s));
-  BatchHdr h = {};
-  h.n_spmv = (int)ms.size();
-  h.n_dot = (int)md.size();
-  h.n_upd = (int)mu.size();
-  h.n_rst = (int)mr.size();
-  h.n_inst = (int)live.size();
-  KSG_CUDA(cudaMemcpyAsync(B.hdr.p, &h, sizeof(h), cudaMemcpyHostToDevice, B.s));
-  KSG_CUDA(cudaStreamSynchronize(B.s));  // h is on the stack
-  return 0;
+BatchEngine::~BatchEngine() {
+  if (exec) cudaGraphExecDestroy(exec);
+  if (h_status) cudaFreeHost(h_status);
+  if (s) cudaStreamDestroy(s);
 }
 
-// the launches of one restart cycle, in stream order (captured once into a graph)
-PetscErrorCode batch_enqueue_cycle(BatchEngine &B, long long *launches) {
-  long long nl = 0;
-  cudaStream_t s = B.s;
-  KSG_CUDA(launch_batch_begin(B.inst.p, B.list.p, B.hdr.p, B.grid_inst, s));
-  KSG_CUDA(launch_batch_dot(B.inst.p, B.map_dot.p, B.hdr.p, -1, B.grid_dot, s));
-  KSG_CUDA(launch_batch_update(B.inst.p, B.map_upd.p, B.hdr.p, -1, B.grid_upd, B.max_ld, s));
-  KSG_CUDA(launch_batch_start(B.inst.p, B.list.p, B.hdr.p, B.grid_inst, s));
-  nl += 4;
-  for (int slot = 0; slot < B.slots; ++slot) {
-    KSG_CUDA(launch_batch_spmv(B.inst.p, B.map_spmv.p, B.hdr.p, slot, B.grid_spmv, s));
-    KSG_CUDA(launch_batch_dot(B.inst.p, B.map_dot.p, B.hdr.p, slot, B.grid_dot, s));
-    KSG_CUDA(launch_batch_update(B.inst.p, B.map_upd.p, B.hdr.p, slot, B.grid_upd, B.max_ld, s));
-    nl += 3;
-  }
-  KSG_CUDA(launch_batch_ds_hep(B.inst.p, B.list.p, B.hdr.p, B.grid_ds, B.max_ld, s));
-  KSG_CUDA(launch_batch_ds_nhep(B.inst.p, B.list.p, B.hdr.p, B.grid_ds, B.max_ld, s));
-  KSG_CUDA(launch_batch_restart(B.inst.p, B.map_rst.p, B.hdr.p, B.grid_rst, B.max_ld, s));
-  KSG_CUDA(launch_batch_control(B.inst.p, B.list.p, B.hdr.p, B.status.p, B.grid_inst, s));
-  nl += 4;
-  KSG_CUDA(cudaMemcpyAsync(B.h_status, B.status.p, sizeof(BatchStatus) * B.cap, cudaMemcpyDeviceToHost, s));
-  *launches = nl;
-  return 0;
-}
-
-PetscErrorCode batch_build_graph(BatchEngine &B) {
-  KSG_CUDA(batch_prepare_restart(B.max_ld));
-  KSG_CUDA(batch_prepare_ds_hep(B.max_ld));
-  cudaGraph_t g = nullptr;
-  KSG_CUDA(cudaStreamBeginCapture(B.s, cudaStreamCaptureModeThreadLocal));
-  long long nl = 0;
-  PetscErrorCode ierr = batch_enqueue_cycle(B, &nl);
-  cudaError_t ce = cudaStreamEndCapture(B.s, &g);
-  KSG_TRY(ierr);
-  KSG_CUDA(ce);
-  if (B.exec) cudaGraphExecDestroy(B.exec);
-  B.exec = nullptr;
-  ce = cudaGraphInstantiate(&B.exec, g, 0);
-  cudaGraphDestroy(g);
-  KSG_CUDA(ce);
-  B.launches_per_cycle = nl;
-  return 0;
-}
-
-BatchInst make_inst(EPS eps) {
+static BatchInst make_inst(EPS eps) {
   BatchInst p = {};
   p.n = eps->n;
   p.hermitian = eps->problem == EPS_HEP;
@@ -183,119 +83,209 @@ BatchInst make_inst(EPS eps) {
   return p;
 }
 
-}  // namespace
+PetscErrorCode ksg_engine_check(EPS e, int max_ncv) {
+  KSG_CHECK(e->storage == STORE_PAIR, PETSC_ERR_SUP,
+            "batched engine: the EPS uses EPS_GB300_ARITH_F64; the batched engine runs the pair arithmetic");
+  KSG_CHECK(e->ncv_e <= max_ncv, PETSC_ERR_SUP, "batched engine: ncv = %d exceeds the limit %d", e->ncv_e, max_ncv);
+  return 0;
+}
 
-extern "C" PetscErrorCode EPSGB300SolveBatch(PetscInt count, EPS *eps) {
-  KSG_CHECK(count >= 0, PETSC_ERR_ARG_OUTOFRANGE, "Negative count");
-  if (count == 0) return 0;
-  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS array");
-  auto t0 = std::chrono::steady_clock::now();
-  int device = -1;
-  for (int i = 0; i < count; ++i) {
-    KSG_CHECK(eps[i], PETSC_ERR_ARG_NULL, "Null EPS at position %d", i);
-    KSG_TRY(EPSSetUp(eps[i]));
-    KSG_CHECK(eps[i]->storage == STORE_PAIR, PETSC_ERR_SUP,
-              "EPSGB300SolveBatch: EPS %d uses EPS_GB300_ARITH_F64; the batched engine runs the pair arithmetic", i);
-    KSG_CHECK(eps[i]->ncv_e <= batch_max_columns() - 1, PETSC_ERR_SUP,
-              "EPSGB300SolveBatch: ncv = %d exceeds the batched limit %d", eps[i]->ncv_e, batch_max_columns() - 1);
-    if (device < 0) device = eps[i]->device;
-    KSG_CHECK(eps[i]->device == device, PETSC_ERR_ARG_INCOMP, "EPSGB300SolveBatch: all EPS must use one device");
-    for (int j = 0; j < i; ++j) KSG_CHECK(eps[j] != eps[i], PETSC_ERR_ARG_WRONG, "EPS %d appears twice", i);
-  }
-  KSG_CUDA(cudaSetDevice(device));
-  KSG_CUDA(cudaDeviceSynchronize());  // EPSSetUp work on the objects' own streams
-  BatchEngine B;
+PetscErrorCode ksg_engine_init(BatchEngine &B, int device, int cap, int max_ncv) {
+  KSG_CHECK(max_ncv >= 1 && max_ncv <= batch_max_columns() - 1, PETSC_ERR_ARG_OUTOFRANGE,
+            "batched engine: ncv limit %d outside [1, %d]", max_ncv, batch_max_columns() - 1);
   B.device = device;
-  B.cap = (int)count;
+  B.cap = cap;
+  B.slots = max_ncv + 1;
+  B.max_ld = max_ncv + 1;
+  KSG_CUDA(cudaSetDevice(device));
   KSG_CUDA(cudaStreamCreateWithFlags(&B.s, cudaStreamNonBlocking));
   const int sms = num_sms();
   B.grid_spmv = sms * 8;
   B.grid_dot = sms;
   B.grid_upd = sms;
   B.grid_rst = sms * 2;
-  B.grid_ds = std::min<int>((int)count, sms * 8);
-  B.grid_inst = std::min<int>((int)count, sms * 8);
-  std::vector<BatchInst> hi(count);
-  std::vector<std::vector<double>> rnd(count);
-  for (int i = 0; i < count; ++i) {
-    EPS e = eps[i];
-    hi[i] = make_inst(e);
-    B.slots = std::max(B.slots, e->ncv_e + 1);
-    B.max_ld = std::max(B.max_ld, e->ld);
-    e->solved = 0;
-    e->stats = EPSGB300Stats{};
-    // start vector in FP64 into column 1, converted to pairs in column 0 (column 1 is rewritten by the first SpMV)
-    const double *src;
-    if (!e->v0.empty()) src = e->v0.data();
-    else {
-      rnd[i].resize(e->n);
-      ksg_random_fill(rnd[i].data(), e->n, e->seed, 0);
-      src = rnd[i].data();
-    }
-    double *stage = e->V.p + e->ldv;
-    KSG_CUDA(cudaMemcpyAsync(stage, src, sizeof(double) * e->n, cudaMemcpyHostToDevice, B.s));
-    KSG_CUDA(launch_f64_to_pair(stage, reinterpret_cast<float2 *>(e->V.p), e->n, B.s));
-  }
-  KSG_CUDA(B.inst.alloc(count));
-  KSG_CUDA(B.list.alloc(count));
+  B.grid_ds = std::min(cap, sms * 8);
+  B.grid_inst = std::min(cap, sms * 8);
+  KSG_CUDA(B.inst.alloc(cap));
+  KSG_CUDA(B.list.alloc(cap));
   KSG_CUDA(B.hdr.alloc(1));
-  KSG_CUDA(B.status.alloc(count));
-  KSG_CUDA(cudaMallocHost((void **)&B.h_status, sizeof(BatchStatus) * count));
-  KSG_CUDA(cudaMemcpyAsync(B.inst.p, hi.data(), sizeof(BatchInst) * count, cudaMemcpyHostToDevice, B.s));
-  std::vector<int> live(count);
-  for (int i = 0; i < count; ++i) live[i] = i;
-  KSG_TRY(batch_upload_maps(B, hi, live));
-  KSG_TRY(batch_build_graph(B));
-  rnd.clear();
-  std::vector<int> phase(count, BP_START);
-  long long cycles = 0;
+  KSG_CUDA(B.status.alloc(cap));
+  KSG_CUDA(cudaMallocHost((void **)&B.h_status, sizeof(BatchStatus) * cap));
+  BatchHdr h = {};
+  KSG_CUDA(cudaMemcpy(B.hdr.p, &h, sizeof(h), cudaMemcpyHostToDevice));
+  B.hi.assign(cap, BatchInst{});
+  B.eps.assign(cap, nullptr);
+  B.free_slots.clear();
+  for (int i = cap - 1; i >= 0; --i) B.free_slots.push_back(i);
+  return 0;
+}
+
+// the launches of one restart cycle, in stream order (captured into a graph)
+static PetscErrorCode engine_enqueue_cycle(BatchEngine &B, long long *launches) {
+  long long nl = 0;
+  cudaStream_t s = B.s;
+  KSG_CUDA(launch_batch_begin(B.inst.p, B.list.p, B.hdr.p, B.grid_inst, s));
+  KSG_CUDA(launch_batch_dot(B.inst.p, B.map_dot.p, B.hdr.p, -1, B.grid_dot, s));
+  KSG_CUDA(launch_batch_update(B.inst.p, B.map_upd.p, B.hdr.p, -1, B.grid_upd, B.max_ld, s));
+  KSG_CUDA(launch_batch_start(B.inst.p, B.list.p, B.hdr.p, B.grid_inst, s));
+  nl += 4;
+  for (int slot = 0; slot < B.slots; ++slot) {
+    KSG_CUDA(launch_batch_spmv(B.inst.p, B.map_spmv.p, B.hdr.p, slot, B.grid_spmv, s));
+    KSG_CUDA(launch_batch_dot(B.inst.p, B.map_dot.p, B.hdr.p, slot, B.grid_dot, s));
+    KSG_CUDA(launch_batch_update(B.inst.p, B.map_upd.p, B.hdr.p, slot, B.grid_upd, B.max_ld, s));
+    nl += 3;
+  }
+  KSG_CUDA(launch_batch_ds_hep(B.inst.p, B.list.p, B.hdr.p, B.grid_ds, B.max_ld, s));
+  KSG_CUDA(launch_batch_ds_nhep(B.inst.p, B.list.p, B.hdr.p, B.grid_ds, B.max_ld, s));
+  KSG_CUDA(launch_batch_restart(B.inst.p, B.map_rst.p, B.hdr.p, B.grid_rst, B.max_ld, s));
+  KSG_CUDA(launch_batch_control(B.inst.p, B.list.p, B.hdr.p, B.status.p, B.grid_inst, s));
+  nl += 4;
+  KSG_CUDA(cudaMemcpyAsync(B.h_status, B.status.p, sizeof(BatchStatus) * B.cap, cudaMemcpyDeviceToHost, s));
+  *launches = nl;
+  return 0;
+}
+
+static PetscErrorCode engine_build_graph(BatchEngine &B) {
+  KSG_CUDA(batch_prepare_restart(B.max_ld));
+  KSG_CUDA(batch_prepare_ds_hep(B.max_ld));
+  cudaGraph_t g = nullptr;
+  KSG_CUDA(cudaStreamBeginCapture(B.s, cudaStreamCaptureModeThreadLocal));
+  long long nl = 0;
+  PetscErrorCode ierr = engine_enqueue_cycle(B, &nl);
+  cudaError_t ce = cudaStreamEndCapture(B.s, &g);
+  KSG_TRY(ierr);
+  KSG_CUDA(ce);
+  if (B.exec) cudaGraphExecDestroy(B.exec);
+  B.exec = nullptr;
+  ce = cudaGraphInstantiate(&B.exec, g, 0);
+  cudaGraphDestroy(g);
+  KSG_CUDA(ce);
+  B.launches_per_cycle = nl;
+  return 0;
+}
+
+// Work lists of the live instances (between cycles: the stream is idle).  A list buffer that has to grow is
+// reallocated, and the graph, which holds its address, is captured again.
+static PetscErrorCode engine_upload_maps(BatchEngine &B) {
+  std::vector<BatchVB> ms, md, mu, mr;
+  for (int i : B.live) {
+    const BatchInst &p = B.hi[i];
+    const int ns = std::max(1, std::min(spmv_blocks_for(p.n, p.lanes), (p.n + 8 * SPMV_VB_ROWS - 1) / (8 * SPMV_VB_ROWS)));
+    const int nd = batch_gs_vbs(p.n, gs_dot_blocks(p.n)), nu = batch_gs_vbs(p.n, gs_update_blocks(p.n));
+    const int nr = std::max(1, std::min(restart_blocks_for(p.n), (p.n + 1023) / 1024));
+    for (int b = 0; b < ns; ++b) ms.push_back({i, b, ns, 0});
+    for (int b = 0; b < nd; ++b) md.push_back({i, b, nd, 0});
+    for (int b = 0; b < nu; ++b) mu.push_back({i, b, nu, 0});
+    for (int b = 0; b < nr; ++b) mr.push_back({i, b, nr, 0});
+  }
+  bool regrown = false;
+  auto up = [&](DBuf<BatchVB> &d, const std::vector<BatchVB> &h) -> cudaError_t {
+    if (h.size() > d.count || !d.p) {
+      cudaError_t e = d.alloc(std::max<size_t>(h.size() + h.size() / 2 + 64, 1024));
+      if (e != cudaSuccess) return e;
+      regrown = true;
+    }
+    return h.empty() ? cudaSuccess
+                     : cudaMemcpyAsync(d.p, h.data(), h.size() * sizeof(BatchVB), cudaMemcpyHostToDevice, B.s);
+  };
+  KSG_CUDA(cudaStreamSynchronize(B.s));
+  KSG_CUDA(up(B.map_spmv, ms));
+  KSG_CUDA(up(B.map_dot, md));
+  KSG_CUDA(up(B.map_upd, mu));
+  KSG_CUDA(up(B.map_rst, mr));
+  if (!B.live.empty())
+    KSG_CUDA(cudaMemcpyAsync(B.list.p, B.live.data(), B.live.size() * sizeof(int), cudaMemcpyHostToDevice, B.s));
+  BatchHdr h = {};
+  h.n_spmv = (int)ms.size();
+  h.n_dot = (int)md.size();
+  h.n_upd = (int)mu.size();
+  h.n_rst = (int)mr.size();
+  h.n_inst = (int)B.live.size();
+  KSG_CUDA(cudaMemcpyAsync(B.hdr.p, &h, sizeof(h), cudaMemcpyHostToDevice, B.s));
+  KSG_CUDA(cudaStreamSynchronize(B.s));  // h is on the stack
+  if (regrown || !B.exec) KSG_TRY(engine_build_graph(B));
+  B.maps_dirty = false;
+  return 0;
+}
+
+// Take a set-up EPS into a free slot: start vector into column 0, instance record to the device, all on the EPS's
+// own stream (the engine's stream may be running a cycle).  The instance joins the live set at ksg_engine_activate.
+PetscErrorCode ksg_engine_admit(BatchEngine &B, EPS e, int *slot) {
+  KSG_CHECK(!B.free_slots.empty(), PETSC_ERR_GPU_RESOURCE, "batched engine: all %d slots are in use", B.cap);
+  const int i = B.free_slots.back();
+  B.free_slots.pop_back();
+  B.eps[i] = e;
+  B.hi[i] = make_inst(e);
+  e->solved = 0;
+  e->stats = EPSGB300Stats{};
+  cudaStream_t s = e->stream;
+  // the start vector in FP64 into column 1, converted to pairs in column 0 (column 1 is rewritten by the first SpMV)
+  std::vector<double> rnd;
+  const double *src;
+  if (!e->v0.empty()) src = e->v0.data();
+  else {
+    rnd.resize(e->n);
+    ksg_random_fill(rnd.data(), e->n, e->seed, 0);
+    src = rnd.data();
+  }
+  double *stage = e->V.p + e->ldv;
+  KSG_CUDA(cudaMemcpyAsync(stage, src, sizeof(double) * e->n, cudaMemcpyHostToDevice, s));
+  KSG_CUDA(launch_f64_to_pair(stage, reinterpret_cast<float2 *>(e->V.p), e->n, s));
+  KSG_CUDA(cudaMemcpyAsync(B.inst.p + i, &B.hi[i], sizeof(BatchInst), cudaMemcpyHostToDevice, s));
+  KSG_CUDA(cudaStreamSynchronize(s));  // rnd and the host record go out of scope / may change
+  *slot = i;
+  return 0;
+}
+
+PetscErrorCode ksg_engine_activate(BatchEngine &B, const std::vector<int> &slots) {
+  for (int i : slots) B.live.push_back(i);
+  if (!slots.empty()) B.maps_dirty = true;
+  return 0;
+}
+
+PetscErrorCode ksg_engine_launch(BatchEngine &B) {
+  if (B.maps_dirty || !B.exec) KSG_TRY(engine_upload_maps(B));
+  KSG_CUDA(cudaGraphLaunch(B.exec, B.s));
+  B.cycles++;
+  return 0;
+}
+
+// Wait for the cycle, then hand breakdowns to the single-problem code and retire solved or failed instances:
+// their results go into their EPS (EPSSolve's epilogue) and their slots become free.
+PetscErrorCode ksg_engine_finish(BatchEngine &B, std::vector<std::pair<int, int>> *retired) {
+  KSG_CUDA(cudaStreamSynchronize(B.s));
+  std::vector<int> still;
   std::vector<double> er, ei, es;
-  while (!live.empty()) {
-    KSG_CUDA(cudaGraphLaunch(B.exec, B.s));
-    KSG_CUDA(cudaStreamSynchronize(B.s));
-    ++cycles;
-    std::vector<int> still;
-    bool changed = false;
-    for (int i : live) {
-      const BatchStatus st = B.h_status[i];
-      EPS e = eps[i];
-      if (st.phase == BP_HOST) {
-        // breakdown: a new random start vector at column nconv, as the single-problem loop does
-        int bd = 0;
-        KSG_TRY(ksg_eps_new_start_vector(e, st.nconv, &bd));
-        BatchInst cur;
-        KSG_CUDA(cudaMemcpy(&cur, B.inst.p + i, sizeof(BatchInst), cudaMemcpyDeviceToHost));
-        if (bd) {
-          cur.phase = BP_DONE;
-          cur.reason = EPS_DIVERGED_BREAKDOWN;
-        } else {
-          KSG_CUDA(launch_segment_begin(e->st.p, cur.k0, cur.nv, e->stream));
-          cur.phase = BP_ITER;
-        }
-        KSG_CUDA(cudaStreamSynchronize(e->stream));
-        KSG_CUDA(cudaMemcpy(B.inst.p + i, &cur, sizeof(BatchInst), cudaMemcpyHostToDevice));
-        if (bd) {
-          B.h_status[i].phase = BP_DONE;
-          B.h_status[i].reason = EPS_DIVERGED_BREAKDOWN;
-        } else {
-          still.push_back(i);
-          continue;
-        }
+  for (int i : B.live) {
+    EPS e = B.eps[i];
+    int ph = B.h_status[i].phase;
+    if (ph == BP_HOST) {
+      // breakdown: a new random start vector at column nconv, as the single-problem loop does
+      int bd = 0;
+      KSG_TRY(ksg_eps_new_start_vector(e, B.h_status[i].nconv, &bd));
+      BatchInst cur;
+      KSG_CUDA(cudaMemcpy(&cur, B.inst.p + i, sizeof(BatchInst), cudaMemcpyDeviceToHost));
+      if (bd) {
+        cur.phase = BP_DONE;
+        cur.reason = EPS_DIVERGED_BREAKDOWN;
+      } else {
+        KSG_CUDA(launch_segment_begin(e->st.p, cur.k0, cur.nv, e->stream));
+        cur.phase = BP_ITER;
       }
-      const int ph = B.h_status[i].phase;
-      if (ph == BP_START || ph == BP_ITER) {
-        still.push_back(i);
-        continue;
-      }
-      changed = true;
-      BatchInst fin;
-      KSG_CUDA(cudaMemcpy(&fin, B.inst.p + i, sizeof(BatchInst), cudaMemcpyDeviceToHost));
-      if (ph == BP_FAILED) {
-        KSG_CHECK(false, fin.err, "EPSGB300SolveBatch: problem %d failed (%s)", i,
-                  fin.err == 77 ? "initial vector is zero or the Krylov segment is empty"
-                                : "the projected eigenproblem solver did not converge");
-      }
-      // retire: eigenvectors of the non-Hermitian Schur form, results into the EPS (EPSSolve's epilogue)
+      KSG_CUDA(cudaStreamSynchronize(e->stream));
+      KSG_CUDA(cudaMemcpy(B.inst.p + i, &cur, sizeof(BatchInst), cudaMemcpyHostToDevice));
+      ph = cur.phase;
+    }
+    if (ph == BP_START || ph == BP_ITER) {
+      still.push_back(i);
+      continue;
+    }
+    BatchInst fin;
+    KSG_CUDA(cudaMemcpy(&fin, B.inst.p + i, sizeof(BatchInst), cudaMemcpyDeviceToHost));
+    int err = 0;
+    if (ph == BP_FAILED) {
+      err = fin.err ? fin.err : PETSC_ERR_LIB;
+    } else {
       const int nconv = fin.nconv, ld = e->ld;
       if (!fin.hermitian && nconv > 0) {
         KSG_CUDA(launch_nhep_vectors(e->H.p, ld, nconv, e->X.p, B.s));
@@ -309,23 +299,74 @@ extern "C" PetscErrorCode EPSGB300SolveBatch(PetscInt count, EPS *eps) {
       KSG_CUDA(cudaMemcpyAsync(es.data(), e->errest.p, sizeof(double) * ld, cudaMemcpyDeviceToHost, B.s));
       KSG_CUDA(cudaStreamSynchronize(B.s));
       KSG_TRY(ksg_eps_assemble(e, nconv, er.data(), ei.data(), es.data(), B.s));
+      KSG_CUDA(cudaStreamSynchronize(B.s));
       e->nconv = nconv;
       e->its = fin.its;
       e->reason = fin.reason;
       e->stats.krylov_steps = fin.steps;
       e->stats.restarts = fin.its;
+      e->stats.kernel_launches = fin.its * B.launches_per_cycle;
       e->solved = 1;
     }
-    if (changed || still.size() != live.size()) {
-      live.swap(still);
-      if (!live.empty()) KSG_TRY(batch_upload_maps(B, hi, live));
-    }
+    retired->push_back({i, err});
+    B.eps[i] = nullptr;
+    B.free_slots.push_back(i);
+    B.maps_dirty = true;
   }
-  KSG_CUDA(cudaStreamSynchronize(B.s));
+  B.live.swap(still);
+  return 0;
+}
+
+}  // namespace ksg
+
+using namespace ksg;
+
+extern "C" PetscErrorCode EPSGB300SolveBatch(PetscInt count, EPS *eps) {
+  KSG_CHECK(count >= 0, PETSC_ERR_ARG_OUTOFRANGE, "Negative count");
+  if (count == 0) return 0;
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS array");
+  auto t0 = std::chrono::steady_clock::now();
+  int device = -1, max_ncv = 1;
+  for (int i = 0; i < count; ++i) {
+    KSG_CHECK(eps[i], PETSC_ERR_ARG_NULL, "Null EPS at position %d", i);
+    KSG_TRY(EPSSetUp(eps[i]));
+    KSG_TRY(ksg_engine_check(eps[i], batch_max_columns() - 1));
+    max_ncv = std::max(max_ncv, eps[i]->ncv_e);
+    if (device < 0) device = eps[i]->device;
+    KSG_CHECK(eps[i]->device == device, PETSC_ERR_ARG_INCOMP, "EPSGB300SolveBatch: all EPS must use one device");
+    for (int j = 0; j < i; ++j) KSG_CHECK(eps[j] != eps[i], PETSC_ERR_ARG_WRONG, "EPS %d appears twice", i);
+  }
+  KSG_CUDA(cudaSetDevice(device));
+  KSG_CUDA(cudaDeviceSynchronize());  // EPSSetUp work on the objects' own streams
+  BatchEngine B;
+  KSG_TRY(ksg_engine_init(B, device, (int)count, max_ncv));
+  std::vector<int> slots(count);
+  for (int i = 0; i < count; ++i) KSG_TRY(ksg_engine_admit(B, eps[i], &slots[i]));
+  KSG_TRY(ksg_engine_activate(B, slots));
+  std::vector<std::pair<int, int>> retired;
+  int first_err = 0, err_at = -1;
+  while (!B.live.empty()) {
+    KSG_TRY(ksg_engine_launch(B));
+    retired.clear();
+    KSG_TRY(ksg_engine_finish(B, &retired));
+    for (auto &r : retired)
+      if (r.second && !first_err) {
+        first_err = r.second;
+        err_at = r.first;
+      }
+  }
   const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   for (int i = 0; i < count; ++i) {
     eps[i]->stats.solve_seconds = secs;
-    eps[i]->stats.kernel_launches = cycles * B.launches_per_cycle;
+    eps[i]->stats.kernel_launches = B.cycles * B.launches_per_cycle;
+  }
+  if (first_err) {
+    int pos = 0;
+    for (int i = 0; i < count; ++i)
+      if (slots[i] == err_at) pos = i;
+    KSG_CHECK(false, first_err, "EPSGB300SolveBatch: problem %d failed (%s)", pos,
+              first_err == 77 ? "initial vector is zero or the Krylov segment is empty"
+                              : "the projected eigenproblem solver did not converge");
   }
   return 0;
 }
