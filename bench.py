@@ -294,6 +294,151 @@ def run_batch(args):
     print(json.dumps(line), flush=True)
 
 
+SERVED = dict(desc="served stream: requests n = exp(U[ln 2e3, ln 2e6]); 70% EPS_HEP Laplacian + diag(U[0,1]) "
+                   "(3-D m^3 when n > 2e5, else 2-D near-square), 30% EPS_NHEP upwind convection-diffusion N^2 with "
+                   "Pe ~ U[1,50]; nev ~ U{4..32}, ncv = max(2 nev + 8, 24), tol = 1e-10, largest real; seed 7",
+              pool_sizes=20, pe_levels=(1.0, 12.0, 25.0, 37.0, 50.0))
+
+
+def served_requests(matgen, count, seed=7):
+    """The request stream: (kind, size, Pe, nev, ncv, start seed) per request, and a pool of matrices shared by
+    requests of the same family and size (sizes quantised to a log grid, Pe to a few levels, so the stream's
+    matrices can be generated in seconds)."""
+    u = matgen.uniform_01(seed, 5 * count).reshape(count, 5)
+    grid = np.exp(np.linspace(np.log(2e3), np.log(2e6), SERVED["pool_sizes"]))
+    reqs = []
+    for i in range(count):
+        n = float(np.exp(np.log(2e3) + u[i, 0] * (np.log(2e6) - np.log(2e3))))
+        n = float(grid[np.argmin(np.abs(np.log(grid) - np.log(n)))])
+        nev = 4 + min(28, int(u[i, 2] * 29))
+        ncv = max(2 * nev + 8, 24)
+        if u[i, 1] < 0.7:
+            kind = "hep3" if n > 2e5 else "hep2"
+            pe = 0.0
+        else:
+            kind = "nhep"
+            pe = SERVED["pe_levels"][min(len(SERVED["pe_levels"]) - 1, int(u[i, 3] * len(SERVED["pe_levels"])))]
+        reqs.append((kind, int(round(n)), pe, nev, ncv, 1000 + i))
+    return reqs
+
+
+def served_matrix(matgen, cache, kind, n, pe):
+    key = (kind, n, pe)
+    if key not in cache:
+        if kind == "hep3":
+            m = max(2, int(round(n ** (1.0 / 3.0))))
+            cache[key] = matgen.laplacian_3d_randdiag(m, 7 + m)
+        elif kind == "hep2":
+            cache[key] = matgen.laplacian_2d_randdiag(n, 7 + n)
+        else:
+            N = max(2, int(round(np.sqrt(n))))
+            cache[key] = matgen.convection_diffusion_2d(N, pe)
+    return cache[key]
+
+
+def run_served(args):
+    """Served form: the request stream through EPSGB300Server -- capacity (every request submitted at once) and
+    latency under Poisson arrivals -- beside the one-problem-per-launch EPSSolve path on a sample of the stream."""
+    import slepc_gb300 as sg
+    from slepc_gb300 import matgen
+    import ctypes
+
+    sg.build()
+    ctypes.CDLL("libcudart.so").cudaSetDevice(0)
+    count = args.served_count
+    t = time.time()
+    reqs = served_requests(matgen, count)
+    cache, mats = {}, {}
+    for kind, n, pe, nev, ncv, sd in reqs:
+        csr = served_matrix(matgen, cache, kind, n, pe)
+        if (kind, n, pe) not in mats:
+            mats[(kind, n, pe)] = sg.Mat(*csr)
+    gen_s = time.time() - t
+    tuning = sg.batch_tune(1, 10) if not args.no_tune else sg.batch_get_tuning()
+
+    def make(r):
+        kind, n, pe, nev, ncv, sd = r
+        A = mats[(kind, n, pe)]
+        e = sg.EPS().create()
+        e.setOperators(A)
+        e.setProblemType(sg.EPS.ProblemType.NHEP if kind == "nhep" else sg.EPS.ProblemType.HEP)
+        e.setDimensions(nev, ncv)
+        e.setTolerances(1e-10)
+        e.setWhichEigenpairs("LR")
+        e.setInitialSpace(matgen.start_vector(A.m, sd))
+        e._A = A
+        return e
+
+    def ok(e, nev):
+        return e.getConvergedReason() == 1 and e.getConverged() >= nev
+
+    budget = args.served_budget_gb * 1e9
+    # 1. capacity: the whole stream submitted at once
+    srv = sg.Server(budget, max_requests=4096, max_ncv=72)
+    eps = [make(r) for r in reqs]
+    clocks = ClockSampler(0)
+    clocks.start()
+    t0 = time.perf_counter()
+    for e in eps:
+        srv.submit(e)
+    for e in eps:
+        srv.wait(e)
+    cap_s = time.perf_counter() - t0
+    clk = clocks.stop()
+    st_cap = srv.stats()
+    srv.destroy()
+    conv = sum(r[3] for r, e in zip(reqs, eps) if ok(e, r[3]))
+    cap_value = conv / cap_s
+    req_per_s = count / cap_s
+    # 2. latency: Poisson arrivals at a fraction of the measured capacity
+    rate = args.served_rate if args.served_rate > 0 else 0.5 * req_per_s
+    rng = np.random.default_rng(7)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=count))
+    srv = sg.Server(budget, max_requests=4096, max_ncv=72)
+    eps2 = [make(r) for r in reqs]
+    t0 = time.perf_counter()
+    for a, e in zip(arrivals, eps2):
+        d = t0 + a - time.perf_counter()
+        if d > 0:
+            time.sleep(d)
+        srv.submit(e)
+    for e in eps2:
+        srv.wait(e)
+    lat_s = time.perf_counter() - t0
+    st_lat = srv.stats()
+    srv.destroy()
+    lat = sorted(e.getStats()["solve_seconds"] * 1000.0 for e in eps2)
+    lat_conv = sum(r[3] for r, e in zip(reqs, eps2) if ok(e, r[3]))
+    # 3. the plain path: EPSSolve one request after another, on every k-th request of the stream
+    sample = list(range(0, count, max(1, count // args.served_plain_sample)))
+    pe_ = [make(reqs[i]) for i in sample]
+    t0 = time.perf_counter()
+    pconv = 0
+    for i, e in zip(sample, pe_):
+        e.solve()
+        pconv += reqs[i][3] if ok(e, reqs[i][3]) else 0
+    plain_s = time.perf_counter() - t0
+    plain_value = pconv / plain_s
+    line = {"metric": METRIC.replace("plain Krylov-Schur, one solve per step", "served Krylov-Schur stream"),
+            "value": cap_value, "unit": UNIT, "n_gpus": 1, "steps": 1, "warmup": 0,
+            "ms_per_step": 1000.0 * cap_s, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": SERVED["desc"], "requests": count, "matrices_in_pool": len(mats),
+                       "hbm_budget_gb": args.served_budget_gb, "generate_s": round(gen_s, 1),
+                       "tuning": tuning},
+            "capacity": {"requests_per_s": req_per_s, "eigenpairs_per_s": cap_value, "seconds": cap_s,
+                         "peak_admitted_bytes": st_cap["peak_bytes"], "max_live": st_cap["max_live"],
+                         "cycles": st_cap["cycles"]},
+            "latency_ms": {"arrival_rate_per_s": rate, "p50": float(np.percentile(lat, 50)),
+                           "p99": float(np.percentile(lat, 99)), "max": lat[-1],
+                           "eigenpairs_per_s": lat_conv / lat_s, "max_live": st_lat["max_live"]},
+            "plain": {"value": plain_value, "unit": UNIT, "sample": f"{len(sample)} of {count} requests, EPSSolve "
+                      "one at a time in arrival order", "seconds": plain_s},
+            "speedup_vs_plain": cap_value / plain_value, "clocks": clk,
+            "gpu_launches": st_cap["cycles"] * 0 + sum(e.getStats()["kernel_launches"] for e in eps)}
+    print(json.dumps(line), flush=True)
+
+
 def run_batch_reference(args):
     """The reference algorithm (the oracle port of SLEPc's Krylov-Schur) on the host cores, one problem after
     another as the reference would solve them, over a stratified sample of the batched workload."""
@@ -340,7 +485,12 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="lap3d128", choices=list(WORKLOADS) + ["batch4096"])
+    ap.add_argument("--workload", default="lap3d128", choices=list(WORKLOADS) + ["batch4096", "served"])
+    ap.add_argument("--served-count", type=int, default=200, help="requests in the served stream")
+    ap.add_argument("--served-rate", type=float, default=0.0,
+                    help="Poisson arrival rate of the latency run (default: half the measured capacity)")
+    ap.add_argument("--served-budget-gb", type=float, default=200.0, help="HBM budget of the server")
+    ap.add_argument("--served-plain-sample", type=int, default=40)
     ap.add_argument("--batch-count", type=int, default=0, help="problems in the batched workload (default 4096)")
     ap.add_argument("--batch-plain-sample", type=int, default=256,
                     help="problems of the batched workload timed through the one-problem-per-launch path")
@@ -354,6 +504,13 @@ def main():
                     help="run exactly one complete solve and exit (the ncu launch-list case: same work as a step)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.workload == "served":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the served stream has no CPU counterpart here; "
+                              "the reference arm is measured on the single-problem and batched workloads"}))
+            return
+        run_served(args)
+        return
     if args.workload == "batch4096":
         if args.impl == "reference":
             run_batch_reference(args)
