@@ -33,6 +33,11 @@ typedef enum { EPS_GB300_DS_REFINED = 0, EPS_GB300_DS_QR = 1 } EPSGB300DSMethod;
 PetscErrorCode EPSGB300SetProjectedSolver(EPS eps, EPSGB300DSMethod method);
 PetscErrorCode EPSGB300GetProjectedSolver(EPS eps, EPSGB300DSMethod *method);
 
+/* Wall-time budget of EPSSolve in seconds (0, the default: none).  Checked after each restart; when it has run out
+ * the solve stops with EPS_DIVERGED_ITS and the pairs converged so far.  A stopping test of the kind
+ * EPSSetStoppingTestFunction installs in the reference (epsdefault.c:290-302), for time-bounded callers. */
+PetscErrorCode EPSGB300SetTimeLimit(EPS eps, PetscReal seconds);
+
 /* CUDA device ordinal used by this EPS (default: the current device at EPSCreate). */
 PetscErrorCode EPSGB300SetDevice(EPS eps, int device);
 
@@ -90,6 +95,8 @@ PetscErrorCode EPSGB300ServerCreate(double hbm_budget_bytes, PetscInt max_reques
 PetscErrorCode EPSGB300ServerSubmit(EPSGB300Server server, EPS eps);
 PetscErrorCode EPSGB300ServerWait(EPSGB300Server server, EPS eps, double timeout_seconds, PetscBool *done);
 PetscErrorCode EPSGB300ServerGetStats(EPSGB300Server server, EPSGB300ServerStats *stats);
+/* Stop serving: queued and in-flight requests end at once with PETSC_ERR_ARG_WRONGSTATE (their Wait returns it). */
+PetscErrorCode EPSGB300ServerCancel(EPSGB300Server server);
 PetscErrorCode EPSGB300ServerDestroy(EPSGB300Server *server);
 
 /* Tuning of the batched engine: Gram-Schmidt tiles (512 rows) per virtual block for each size bucket b, which

@@ -78,6 +78,8 @@ def load():
         "EPSGB300ServerWait": ([P, P, D, ctypes.POINTER(I)], I),
         "EPSGB300ServerGetStats": ([P, P], I),
         "EPSGB300ServerDestroy": ([PP], I),
+        "EPSGB300ServerCancel": ([P], I),
+        "EPSGB300SetTimeLimit": ([P, D], I),
         "EPSGB300BatchGetTuning": ([ctypes.POINTER(I), I], I),
         "EPSGB300BatchSetTuning": ([ctypes.POINTER(I), I], I),
         "EPSGB300GetStats": ([P, P], I),
@@ -263,6 +265,10 @@ class EPS:
         """'pair' (FP64 storage, error-free FP32-pair arithmetic) or 'f64' (IEEE FP64 FMA)."""
         _check(load().EPSGB300SetArithmetic(self.handle, 1 if arith == "f64" else 0), "EPSGB300SetArithmetic")
 
+    def setTimeLimit(self, seconds):
+        """Wall-time budget of EPSSolve (checked after each restart; 0 = none)."""
+        _check(load().EPSGB300SetTimeLimit(self.handle, float(seconds)), "EPSGB300SetTimeLimit")
+
     def setProjectedSolver(self, method):
         """'refined' (FP32 QL + FP64 refinement, default) or 'qr' (FP64 QL) for the symmetric projected problem."""
         _check(load().EPSGB300SetProjectedSolver(self.handle, 1 if method == "qr" else 0),
@@ -388,6 +394,9 @@ class Server:
             if done.value:
                 self._inflight.pop(eps.handle.value, None)
         return bool(done.value)
+
+    def cancel(self):
+        _check(load().EPSGB300ServerCancel(self.handle), "EPSGB300ServerCancel")
 
     def stats(self):
         st = _ServerStats()

@@ -658,6 +658,11 @@ extern "C" PetscErrorCode EPSGB300GetProjectedSolver(EPS eps, EPSGB300DSMethod *
   *method = (EPSGB300DSMethod)eps->ds_method;
   return 0;
 }
+extern "C" PetscErrorCode EPSGB300SetTimeLimit(EPS eps, PetscReal seconds) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  eps->time_limit = seconds;
+  return 0;
+}
 extern "C" PetscErrorCode EPSGB300SetDevice(EPS eps, int device) {
   KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
   int count = 0;
@@ -1116,6 +1121,9 @@ extern "C" PetscErrorCode EPSSolve(EPS eps) {
     }
     nconv = k;
     eps->stats.restarts++;
+    if (reason == 0 && eps->time_limit > 0.0 &&
+        std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count() > eps->time_limit)
+      reason = EPS_DIVERGED_ITS;  // the caller's wall-time budget ran out (EPSGB300SetTimeLimit)
   }
   // non-Hermitian: eigenvectors of the leading Schur block, V = V X (EPSComputeVectors_Schur, epsdefault.c:105-169)
   if (!herm && nconv > 0) {

@@ -41,6 +41,7 @@ struct _p_EPSGB300Server {
   std::deque<EPS> queue;
   std::unordered_map<EPS, Request> req;
   bool stopping = false;
+  bool canceling = false;
   int loop_err = 0;
   long long submitted = 0, completed = 0, failed = 0, max_live = 0;
   long long live_now = 0, cycles_now = 0;  // copies of the engine's counters, under m
@@ -71,6 +72,30 @@ static void server_loop(EPSGB300Server S) {
     S->cv_done.notify_all();
   };
   for (;;) {
+    // 0. cancellation: every queued and live request ends now (the stream is idle between cycles)
+    {
+      std::unique_lock<std::mutex> lk(S->m);
+      if (S->canceling) {
+        const auto now = Clock::now();
+        for (auto &kv : S->req)
+          if (kv.second.state != 2) {
+            kv.second.state = 2;
+            kv.second.err = PETSC_ERR_ARG_WRONGSTATE;
+            kv.second.t_done = now;
+            S->failed++;
+          }
+        S->queue.clear();
+        S->in_use = 0.0;
+        for (int i : S->B.live) {
+          S->B.eps[i] = nullptr;
+          S->B.free_slots.push_back(i);
+        }
+        S->B.live.clear();
+        S->B.maps_dirty = true;
+        S->canceling = false;
+        S->cv_done.notify_all();
+      }
+    }
     // 1. admission: move queued requests whose footprint fits into free slots
     std::vector<EPS> take;
     {
@@ -228,6 +253,14 @@ extern "C" PetscErrorCode EPSGB300ServerGetStats(EPSGB300Server S, EPSGB300Serve
   st->cycles = S->cycles_now;
   st->bytes_in_use = S->in_use;
   st->peak_bytes = S->peak;
+  return 0;
+}
+
+extern "C" PetscErrorCode EPSGB300ServerCancel(EPSGB300Server S) {
+  KSG_CHECK(S, PETSC_ERR_ARG_NULL, "Null argument");
+  std::lock_guard<std::mutex> lk(S->m);
+  S->canceling = true;
+  S->cv_work.notify_all();
   return 0;
 }
 

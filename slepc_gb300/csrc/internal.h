@@ -105,6 +105,7 @@ struct _p_EPS {
   int arith = ksg::ARITH_PAIR;
   int storage = ksg::STORE_PAIR;  // basis format: pairs with pair arithmetic, doubles with FP64 arithmetic
   int ds_method = 0;              // EPSGB300DSMethod
+  double time_limit = 0.0;        // EPSGB300SetTimeLimit (0: none)
   int device = -1;
   std::vector<double> v0;
   unsigned long long seed = 0x5EEDULL;
