@@ -42,6 +42,11 @@ WORKLOADS = {
     "lap3d64": dict(desc="3-D 7-point Laplacian 64^3 (n=262144, nnz=1810432), EPS_HEP, nev=50 largest algebraic, "
                          "ncv=128, tol=1e-10, start vector seed 2 (the 128^3 solve's shape at 1/8 size, for profiling)",
                     gen=lambda mg: mg.laplacian_3d(64), hermitian=True, which="LR", nev=50, ncv=128, tol=1e-10, seed=2),
+    "chunglu4m": dict(desc="Chung-Lu power-law graph n=4194304, mean degree 32, gamma 2.1, max degree 1e5 (seed 4), "
+                           "weights U(0,1] (seed 5), normalised adjacency D^-1/2 A D^-1/2 (nnz 125,195,026), EPS_HEP, "
+                           "nev=16 largest algebraic, ncv=48, tol=1e-10, start vector seed 4",
+                      gen=lambda mg: mg.chung_lu(4194304), hermitian=True, which="LR", nev=16, ncv=48, tol=1e-10,
+                      seed=4),
     "convdiff1000": dict(desc="2-D upwind convection-diffusion 1000x1000 (n=1e6), Peclet 10, EPS_NHEP, nev=20 "
                               "largest real, ncv=64, tol=1e-10, start vector seed 3",
                          gen=lambda mg: mg.convection_diffusion_2d(1000, 10.0), hermitian=False, which="LR", nev=20,

@@ -34,7 +34,27 @@ def _newest_header() -> float:
     return max((os.path.getmtime(h) for h in hs), default=0.0)
 
 
+NATIVE_LIB = os.path.join(BUILD, "libmatgen_native.so")
+
+
+def build_native(force: bool = False) -> str:
+    """Host-only helpers of the matrix generators (gcc, no CUDA)."""
+    os.makedirs(BUILD, exist_ok=True)
+    src = os.path.join(HERE, "native", "matgen_native.c")
+    if force or not os.path.exists(NATIVE_LIB) or os.path.getmtime(NATIVE_LIB) < os.path.getmtime(src):
+        cc = shutil.which("gcc") or shutil.which("cc")
+        if not cc:
+            raise RuntimeError("no C compiler for the native generator helpers")
+        r = subprocess.run([cc, "-O2", "-std=c11", "-fopenmp", "-shared", "-fPIC", "-o", NATIVE_LIB + ".tmp", src, "-lm"],
+                           capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"gcc failed for matgen_native.c:\n{r.stdout}\n{r.stderr}")
+        os.replace(NATIVE_LIB + ".tmp", NATIVE_LIB)
+    return NATIVE_LIB
+
+
 def build(force: bool = False, verbose: bool = False, extra_flags=None) -> str:
+    build_native(force)
     os.makedirs(BUILD, exist_ok=True)
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
     hdr = _newest_header()

@@ -150,6 +150,36 @@ PetscErrorCode ksg_mat_upload(Mat A) {
     KSG_CUDA(cudaMemcpy(A->d_ci.p, A->aj, sizeof(int) * A->nnz, cudaMemcpyHostToDevice));
     KSG_CUDA(cudaMemcpy(A->d_va.p, A->aa, sizeof(double) * A->nnz, cudaMemcpyHostToDevice));
   }
+  // long rows -> segments (host side, once per matrix)
+  {
+    std::vector<int> sr, sb, se, lr, lf;
+    for (int r = 0; r < A->m; ++r) {
+      const int p0 = A->ai[r], p1 = A->ai[r + 1];
+      if (p1 - p0 <= LONG_ROW_T) continue;
+      lr.push_back(r);
+      lf.push_back((int)sr.size());
+      for (int p = p0; p < p1; p += LONG_SEG) {
+        sr.push_back(r);
+        sb.push_back(p);
+        se.push_back(std::min(p1, p + LONG_SEG));
+      }
+    }
+    A->n_long = (int)lr.size();
+    A->n_seg = (int)sr.size();
+    if (A->n_long > 0) {
+      lf.push_back(A->n_seg);
+      KSG_CUDA(A->d_seg_row.alloc(A->n_seg));
+      KSG_CUDA(A->d_seg_beg.alloc(A->n_seg));
+      KSG_CUDA(A->d_seg_end.alloc(A->n_seg));
+      KSG_CUDA(A->d_lrow.alloc(A->n_long));
+      KSG_CUDA(A->d_lfirst.alloc(A->n_long + 1));
+      KSG_CUDA(cudaMemcpy(A->d_seg_row.p, sr.data(), sizeof(int) * A->n_seg, cudaMemcpyHostToDevice));
+      KSG_CUDA(cudaMemcpy(A->d_seg_beg.p, sb.data(), sizeof(int) * A->n_seg, cudaMemcpyHostToDevice));
+      KSG_CUDA(cudaMemcpy(A->d_seg_end.p, se.data(), sizeof(int) * A->n_seg, cudaMemcpyHostToDevice));
+      KSG_CUDA(cudaMemcpy(A->d_lrow.p, lr.data(), sizeof(int) * A->n_long, cudaMemcpyHostToDevice));
+      KSG_CUDA(cudaMemcpy(A->d_lfirst.p, lf.data(), sizeof(int) * (A->n_long + 1), cudaMemcpyHostToDevice));
+    }
+  }
   A->device_ready = 1;
   return 0;
 }
@@ -444,6 +474,7 @@ static PetscErrorCode eps_free_device(EPS eps) {
   eps->coef.release();
   eps->work.release();
   eps->dsf.release();
+  eps->seg_part.release();
   eps->part.release();
   eps->st.release();
   eps->ctl.release();
@@ -769,6 +800,7 @@ extern "C" PetscErrorCode EPSSetUp(EPS eps) {
   if (!eps->h_ctl) KSG_CUDA(cudaMallocHost((void **)&eps->h_ctl, sizeof(KSControl)));
   eps->storage = (eps->arith == ARITH_PAIR) ? STORE_PAIR : STORE_F64;
   KSG_TRY(ksg_mat_upload(eps->A));
+  if (eps->A->n_seg > 0) KSG_CUDA(eps->seg_part.alloc(eps->A->n_seg));
   if (eps->storage == STORE_PAIR) KSG_TRY(ksg_mat_upload_pairs(eps->A));
   // power-of-two operator scaling keeps every vector inside the range of the FP32-pair arithmetic; it is exact
   const double nrm = ksg_mat_norm_inf(eps->A);
@@ -871,13 +903,25 @@ static PetscErrorCode eps_factorize(EPS eps, int k0, int nv, double *bytes) {
   a.pstride = eps->pstride;
   a.st = eps->st.p;
   const double colb = 8.0 * n;
+  LongRows lr;
+  if (eps->A->n_long > 0) {
+    lr.n_long = eps->A->n_long;
+    lr.n_seg = eps->A->n_seg;
+    lr.long_t = LONG_ROW_T;
+    lr.seg_row = eps->A->d_seg_row.p;
+    lr.seg_beg = eps->A->d_seg_beg.p;
+    lr.seg_end = eps->A->d_seg_end.p;
+    lr.lrow = eps->A->d_lrow.p;
+    lr.lfirst = eps->A->d_lfirst.p;
+    lr.part = eps->seg_part.p;
+  }
   for (int j = k0; j < nv; ++j) {
     double *u = eps->V.p + (size_t)j * eps->ldv;
     double *w = u + eps->ldv;
     {
       LaunchScope ls(eps, EPS_GB300_K_SPMV, spmv_bytes(eps));
       KSG_CUDA(launch_spmv_storage(eps->A->d_rp.p, eps->A->d_ci.p, eps->A->d_va.p, eps->A->d_va2.p, u, w, n,
-                                   eps->lanes, eps->st.p, eps->opscale, eps->storage, s));
+                                   eps->lanes, eps->st.p, eps->opscale, eps->storage, s, &lr));
     }
     a.J = j;
     a.j = j;

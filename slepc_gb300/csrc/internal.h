@@ -72,6 +72,9 @@ struct _p_Mat {
   DBuf<int> d_rp, d_ci;
   DBuf<double> d_va;
   DBuf<float2> d_va2;  // values as FP32 pairs, for the pair-storage SpMV
+  // rows longer than LONG_ROW_T nonzeros, cut into segments (the skew-aware SpMV of kernels.h)
+  DBuf<int> d_seg_row, d_seg_beg, d_seg_end, d_lrow, d_lfirst;
+  int n_long = 0, n_seg = 0;
   int device_ready = 0;
   double norm_inf = -1.0;
 };
@@ -119,6 +122,7 @@ struct _p_EPS {
   long long ldv = 0;
   cudaStream_t stream = nullptr;
   DBuf<double> V, d, e, H, Q, X, eigr, eigi, errest, coef, work, dsf;
+  DBuf<double> seg_part;  // one 8-byte partial per long-row segment of the operator
   DBuf<float2> part;
   int pstride = 0;
   DBuf<ksg::KrylovState> st;

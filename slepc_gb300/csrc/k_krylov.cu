@@ -94,17 +94,90 @@ int spmv_lanes_for(double avg_nnz) {
 
 template <class S>
 static void spmv_dispatch(const int *rp, const int *ci, const double *va, const void *x, void *y, int n, int lanes,
-                          const KrylovState *st, double scale, int blocks, cudaStream_t s) {
+                          const KrylovState *st, double scale, int blocks, cudaStream_t s, int long_t) {
   using T = typename S::T;
   const T *xx = static_cast<const T *>(x);
   T *yy = static_cast<T *>(y);
   switch (lanes) {
-    case 1: k_spmv<1, S><<<blocks, 256, 0, s>>>(rp, ci, va, xx, yy, n, st, scale); break;
-    case 2: k_spmv<2, S><<<blocks, 256, 0, s>>>(rp, ci, va, xx, yy, n, st, scale); break;
-    case 4: k_spmv<4, S><<<blocks, 256, 0, s>>>(rp, ci, va, xx, yy, n, st, scale); break;
-    case 8: k_spmv<8, S><<<blocks, 256, 0, s>>>(rp, ci, va, xx, yy, n, st, scale); break;
-    case 16: k_spmv<16, S><<<blocks, 256, 0, s>>>(rp, ci, va, xx, yy, n, st, scale); break;
-    default: k_spmv<32, S><<<blocks, 256, 0, s>>>(rp, ci, va, xx, yy, n, st, scale); break;
+    case 1: k_spmv<1, S><<<blocks, 256, 0, s>>>(rp, ci, va, xx, yy, n, st, scale, long_t); break;
+    case 2: k_spmv<2, S><<<blocks, 256, 0, s>>>(rp, ci, va, xx, yy, n, st, scale, long_t); break;
+    case 4: k_spmv<4, S><<<blocks, 256, 0, s>>>(rp, ci, va, xx, yy, n, st, scale, long_t); break;
+    case 8: k_spmv<8, S><<<blocks, 256, 0, s>>>(rp, ci, va, xx, yy, n, st, scale, long_t); break;
+    case 16: k_spmv<16, S><<<blocks, 256, 0, s>>>(rp, ci, va, xx, yy, n, st, scale, long_t); break;
+    default: k_spmv<32, S><<<blocks, 256, 0, s>>>(rp, ci, va, xx, yy, n, st, scale, long_t); break;
+  }
+}
+
+// ---- long rows: one warp per segment, then each long row merges its segment sums in order ----
+__global__ void __launch_bounds__(256) k_spmv_seg_pair(LongRows lr, const float2 *__restrict__ va,
+                                                       const int *__restrict__ ci, const float2 *__restrict__ x,
+                                                       const KrylovState *st) {
+  if (st && st->stop) return;
+  const int lane = threadIdx.x & 31;
+  const long long w0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  unsigned long long *part = static_cast<unsigned long long *>(lr.part);
+  for (long long sgi = w0; sgi < lr.n_seg; sgi += nw) {
+    dfacc acc;
+    acc_zero(acc);
+    for (int p = lr.seg_beg[sgi] + lane; p < lr.seg_end[sgi]; p += 32) {
+      const float2 av = __ldcs(va + p), xv = __ldg(x + __ldcs(ci + p));
+      f2x a2, x2;
+      a2.hi = av.x; a2.lo = av.y;
+      x2.hi = xv.x; x2.lo = xv.y;
+      acc_fma(acc, a2, x2);
+    }
+    acc = warp_reduce<PairAr>(acc);
+    if (lane == 0) part[sgi] = PairAr::pack(acc);
+  }
+}
+
+__global__ void k_spmv_longfix_pair(LongRows lr, float2 *__restrict__ y, const KrylovState *st, double scale) {
+  if (st && st->stop) return;
+  const f2x sc = split_f64(st ? st->sigma * scale : scale);
+  const unsigned long long *part = static_cast<const unsigned long long *>(lr.part);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < lr.n_long; i += gridDim.x * blockDim.x) {
+    dfacc acc;
+    acc_zero(acc);
+    for (int sgi = lr.lfirst[i]; sgi < lr.lfirst[i + 1]; ++sgi) acc_merge(acc, PairAr::unpack(part[sgi]));
+    f2x v;
+    v.hi = acc.s + acc.c;
+    v.lo = acc.c - (v.hi - acc.s);
+    dfacc pr;
+    acc_zero(pr);
+    acc_fma(pr, v, sc);
+    const float hi = pr.s + pr.c;
+    y[lr.lrow[i]] = make_float2(hi, pr.c - (hi - pr.s));
+  }
+}
+
+template <class S>
+__global__ void __launch_bounds__(256) k_spmv_seg_f64(LongRows lr, const double *__restrict__ va,
+                                                      const int *__restrict__ ci, const typename S::T *__restrict__ x,
+                                                      const KrylovState *st) {
+  if (st && st->stop) return;
+  const int lane = threadIdx.x & 31;
+  const long long w0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  double *part = static_cast<double *>(lr.part);
+  for (long long sgi = w0; sgi < lr.n_seg; sgi += nw) {
+    double sum = 0.0;
+    for (int p = lr.seg_beg[sgi] + lane; p < lr.seg_end[sgi]; p += 32)
+      sum = ::fma(__ldcs(va + p), S::get(x + __ldcs(ci + p)), sum);
+    sum = warp_sum_f64(sum);
+    if (lane == 0) part[sgi] = sum;
+  }
+}
+
+template <class S>
+__global__ void k_spmv_longfix_f64(LongRows lr, typename S::T *__restrict__ y, const KrylovState *st, double scale) {
+  if (st && st->stop) return;
+  const double sc = st ? st->sigma * scale : scale;
+  const double *part = static_cast<const double *>(lr.part);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < lr.n_long; i += gridDim.x * blockDim.x) {
+    double sum = 0.0;
+    for (int sgi = lr.lfirst[i]; sgi < lr.lfirst[i + 1]; ++sgi) sum += part[sgi];
+    S::put(y + lr.lrow[i], sum * sc);
   }
 }
 
@@ -128,26 +201,37 @@ int spmv_blocks_for(int n, int lanes) {
 
 cudaError_t launch_spmv(const int *rp, const int *ci, const double *va, const double *x, double *y, int n, int lanes,
                         const KrylovState *st, double scale, cudaStream_t s) {
-  spmv_dispatch<StF64>(rp, ci, va, x, y, n, lanes, st, scale, spmv_blocks(n, lanes), s);
+  spmv_dispatch<StF64>(rp, ci, va, x, y, n, lanes, st, scale, spmv_blocks(n, lanes), s, 0x7fffffff);
   return cudaGetLastError();
 }
 
 cudaError_t launch_spmv_storage(const int *rp, const int *ci, const double *va, const float2 *va_pair, const void *x,
                                 void *y, int n, int lanes, const KrylovState *st, double scale, int storage,
-                                cudaStream_t s) {
+                                cudaStream_t s, const LongRows *lr) {
   const int blocks = spmv_blocks(n, lanes);
+  const bool split = lr && lr->n_long > 0;
+  const int long_t = split ? lr->long_t : 0x7fffffff;
+  const int seg_blocks = split ? (int)std::min<long long>((lr->n_seg + 7) / 8, (long long)num_sms() * 8) : 0;
   if (storage == STORE_F64) {
-    spmv_dispatch<StF64>(rp, ci, va, x, y, n, lanes, st, scale, blocks, s);
+    spmv_dispatch<StF64>(rp, ci, va, x, y, n, lanes, st, scale, blocks, s, long_t);
+    if (split) {
+      k_spmv_seg_f64<StF64><<<seg_blocks, 256, 0, s>>>(*lr, va, ci, static_cast<const double *>(x), st);
+      k_spmv_longfix_f64<StF64><<<(lr->n_long + 127) / 128, 128, 0, s>>>(*lr, static_cast<double *>(y), st, scale);
+    }
   } else {
     const float2 *xx = static_cast<const float2 *>(x);
     float2 *yy = static_cast<float2 *>(y);
     switch (lanes) {
-      case 1: k_spmv_pair<1><<<blocks, 256, 0, s>>>(rp, ci, va_pair, xx, yy, n, st, scale); break;
-      case 2: k_spmv_pair<2><<<blocks, 256, 0, s>>>(rp, ci, va_pair, xx, yy, n, st, scale); break;
-      case 4: k_spmv_pair<4><<<blocks, 256, 0, s>>>(rp, ci, va_pair, xx, yy, n, st, scale); break;
-      case 8: k_spmv_pair<8><<<blocks, 256, 0, s>>>(rp, ci, va_pair, xx, yy, n, st, scale); break;
-      case 16: k_spmv_pair<16><<<blocks, 256, 0, s>>>(rp, ci, va_pair, xx, yy, n, st, scale); break;
-      default: k_spmv_pair<32><<<blocks, 256, 0, s>>>(rp, ci, va_pair, xx, yy, n, st, scale); break;
+      case 1: k_spmv_pair<1><<<blocks, 256, 0, s>>>(rp, ci, va_pair, xx, yy, n, st, scale, long_t); break;
+      case 2: k_spmv_pair<2><<<blocks, 256, 0, s>>>(rp, ci, va_pair, xx, yy, n, st, scale, long_t); break;
+      case 4: k_spmv_pair<4><<<blocks, 256, 0, s>>>(rp, ci, va_pair, xx, yy, n, st, scale, long_t); break;
+      case 8: k_spmv_pair<8><<<blocks, 256, 0, s>>>(rp, ci, va_pair, xx, yy, n, st, scale, long_t); break;
+      case 16: k_spmv_pair<16><<<blocks, 256, 0, s>>>(rp, ci, va_pair, xx, yy, n, st, scale, long_t); break;
+      default: k_spmv_pair<32><<<blocks, 256, 0, s>>>(rp, ci, va_pair, xx, yy, n, st, scale, long_t); break;
+    }
+    if (split) {
+      k_spmv_seg_pair<<<seg_blocks, 256, 0, s>>>(*lr, va_pair, ci, xx, st);
+      k_spmv_longfix_pair<<<(lr->n_long + 127) / 128, 128, 0, s>>>(*lr, yy, st, scale);
     }
   }
   return cudaGetLastError();

@@ -43,6 +43,18 @@ struct DSFArgs {
   KSControl *ctl;
 };
 
+// Rows of the operator longer than long_t nonzeros, cut into segments of at most LONG_SEG nonzeros: each segment is
+// summed by one warp, then each long row merges its segments in order (deterministic, no atomics).  Built once per
+// matrix (ksg_mat_upload); `part` is per-solver scratch (one 8-byte partial per segment).
+constexpr int LONG_ROW_T = 4096;
+constexpr int LONG_SEG = 2048;
+struct LongRows {
+  int n_long = 0, n_seg = 0, long_t = 0x7fffffff;
+  const int *seg_row = nullptr, *seg_beg = nullptr, *seg_end = nullptr;  // per segment
+  const int *lrow = nullptr, *lfirst = nullptr;                           // per long row: row, first segment
+  void *part = nullptr;
+};
+
 int num_sms();
 int spmv_lanes_for(double avg_nnz);
 int gs_dot_blocks(int n);
@@ -54,7 +66,7 @@ cudaError_t launch_spmv(const int *rp, const int *ci, const double *va, const do
                         const KrylovState *st, double scale, cudaStream_t s);
 cudaError_t launch_spmv_storage(const int *rp, const int *ci, const double *va, const float2 *va_pair, const void *x,
                                 void *y, int n, int lanes, const KrylovState *st, double scale, int storage,
-                                cudaStream_t s);
+                                cudaStream_t s, const LongRows *lr = nullptr);
 cudaError_t launch_f64_to_pair(const double *x, float2 *y, long long n, cudaStream_t s);
 cudaError_t launch_pair_to_f64(const float2 *x, double *y, long long n, cudaStream_t s);
 cudaError_t launch_gs_dot(const StepArgs &a, int nx, int mode, int arith, cudaStream_t s, int storage = STORE_F64);

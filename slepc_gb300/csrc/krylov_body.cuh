@@ -135,11 +135,12 @@ enum { TK_DOT = 0, TK_UPD = 1, TK_NRM = 2 };
 // ------------------------------------------------------------------------------------------------------------
 // SpMV: LANES threads per row, FP64 FMA.  Each warp owns 32/LANES consecutive rows per iteration.
 // ------------------------------------------------------------------------------------------------------------
+// Rows with more than long_t nonzeros are skipped: the segment kernels of k_krylov.cu compute them.
 template <int LANES, class S>
 __global__ void __launch_bounds__(256) k_spmv(const int *__restrict__ rp, const int *__restrict__ ci,
                                               const double *__restrict__ va, const typename S::T *__restrict__ x,
                                               typename S::T *__restrict__ y, int n, const KrylovState *st,
-                                              double scale) {
+                                              double scale, int long_t) {
   if (st && st->stop) return;
   const double sc = st ? st->sigma * scale : scale;
   constexpr int RPW = 32 / LANES;
@@ -150,15 +151,20 @@ __global__ void __launch_bounds__(256) k_spmv(const int *__restrict__ rp, const 
   for (long long base = warp_global * RPW; base < n; base += nwarps * RPW) {
     const long long row = base + grp;
     int p0 = 0, p1 = 0;
+    bool seg = false;  // a long row: computed by the segment kernels
     if (row < n) {
       p0 = rp[row];
       p1 = rp[row + 1];
+      if (p1 - p0 > long_t) {
+        seg = true;
+        p1 = p0;
+      }
     }
     double sum = 0.0;
-    for (int p = p0 + sub; p < p1; p += LANES) sum = ::fma(va[p], S::get(x + ci[p]), sum);
+    for (int p = p0 + sub; p < p1; p += LANES) sum = ::fma(__ldcs(va + p), S::get(x + __ldcs(ci + p)), sum);
 #pragma unroll
     for (int off = LANES / 2; off > 0; off >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, off, LANES);
-    if (sub == 0 && row < n) S::put(y + row, sum * sc);
+    if (sub == 0 && row < n && !seg) S::put(y + row, sum * sc);
   }
 }
 
@@ -169,7 +175,7 @@ __global__ void __launch_bounds__(256) k_spmv(const int *__restrict__ rp, const 
 template <int LANES>
 KS_DEVICE void spmv_pair_rows(const int *__restrict__ rp, const int *__restrict__ ci, const float2 *__restrict__ va,
                               const float2 *__restrict__ x, float2 *__restrict__ y, int n, const KrylovState *st,
-                              double scale, long long warp_global, long long nwarps) {
+                              double scale, long long warp_global, long long nwarps, int long_t = 0x7fffffff) {
   if (st && st->stop) return;
   const f2x sc = split_f64(st ? st->sigma * scale : scale);
   constexpr int RPW = 32 / LANES;
@@ -178,14 +184,20 @@ KS_DEVICE void spmv_pair_rows(const int *__restrict__ rp, const int *__restrict_
   for (long long base = warp_global * RPW; base < n; base += nwarps * RPW) {
     const long long row = base + grp;
     int p0 = 0, p1 = 0;
+    bool seg = false;  // a long row: computed by the segment kernels
     if (row < n) {
       p0 = rp[row];
       p1 = rp[row + 1];
+      if (p1 - p0 > long_t) {
+        seg = true;
+        p1 = p0;
+      }
     }
     dfacc acc;
     acc_zero(acc);
     for (int p = p0 + sub; p < p1; p += LANES) {
-      const float2 av = __ldg(va + p), xv = __ldg(x + __ldg(ci + p));
+      // the matrix streams through once per step (evict-first); the gathered x stays in L2
+      const float2 av = __ldcs(va + p), xv = __ldg(x + __ldcs(ci + p));
       f2x a2, x2;
       a2.hi = av.x; a2.lo = av.y;
       x2.hi = xv.x; x2.lo = xv.y;
@@ -198,7 +210,7 @@ KS_DEVICE void spmv_pair_rows(const int *__restrict__ rp, const int *__restrict_
       o.c = __shfl_down_sync(0xffffffffu, acc.c, off, LANES);
       acc_merge(acc, o);
     }
-    if (sub == 0 && row < n) {
+    if (sub == 0 && row < n && !seg) {
       // renormalise (s, c) into a pair, then multiply by the scale as pairs
       f2x v;
       v.hi = acc.s + acc.c;
@@ -216,9 +228,9 @@ template <int LANES>
 __global__ void __launch_bounds__(256) k_spmv_pair(const int *__restrict__ rp, const int *__restrict__ ci,
                                                    const float2 *__restrict__ va, const float2 *__restrict__ x,
                                                    float2 *__restrict__ y, int n, const KrylovState *st,
-                                                   double scale) {
+                                                   double scale, int long_t) {
   spmv_pair_rows<LANES>(rp, ci, va, x, y, n, st, scale, ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5,
-                        ((long long)gridDim.x * blockDim.x) >> 5);
+                        ((long long)gridDim.x * blockDim.x) >> 5, long_t);
 }
 
 // ------------------------------------------------------------------------------------------------------------

@@ -19,6 +19,7 @@ Random numbers come from counter-based splitmix64 so the same seed gives the sam
 """
 from __future__ import annotations
 
+import ctypes
 import math
 
 import numpy as np
@@ -134,8 +135,29 @@ def laplacian_3d_randdiag(m: int, seed: int):
     return rowptr, colidx, vals
 
 
+_NATIVE = None
+
+
+def _native_lib():
+    """ctypes handle of the C helpers (slepc_gb300/native/matgen_native.c), built on first use; None without gcc."""
+    global _NATIVE
+    if _NATIVE is None:
+        try:
+            from . import buildlib
+            lib = ctypes.CDLL(buildlib.build_native())
+            lib.chung_lu_build.argtypes = [ctypes.c_longlong, ctypes.c_void_p, ctypes.c_longlong, ctypes.c_ulonglong,
+                                           ctypes.c_ulonglong, ctypes.POINTER(ctypes.c_void_p)]
+            lib.chung_lu_build.restype = ctypes.c_longlong
+            lib.chung_lu_fetch.argtypes = [ctypes.c_void_p] * 4
+            lib.chung_lu_fetch.restype = None
+            _NATIVE = lib
+        except (OSError, RuntimeError):
+            _NATIVE = False
+    return _NATIVE or None
+
+
 def chung_lu(n: int, mean_degree: float = 32.0, gamma: float = 2.1, max_degree: float = 1e5,
-             seed: int = 4, weight_seed: int = 5, i0: float | None = None):
+             seed: int = 4, weight_seed: int = 5, i0: float | None = None, native: bool | None = None):
     """Normalised adjacency D^-1/2 A D^-1/2 of a Chung-Lu power-law graph.
 
     Expected degrees w_i proportional to (i + i0)^(-1/(gamma-1)), scaled to the requested mean and capped at
@@ -155,6 +177,19 @@ def chung_lu(n: int, mean_degree: float = 32.0, gamma: float = 2.1, max_degree: 
     m = int(round(n * mean_degree / 2.0))
     cdf = np.cumsum(w)
     cdf /= cdf[-1]
+    native = _native_lib() if native is None or native else None
+    if native is not None:
+        h = ctypes.c_void_p()
+        cdf_c = np.ascontiguousarray(cdf, dtype=np.float64)
+        nnz = native.chung_lu_build(n, cdf_c.ctypes.data_as(ctypes.c_void_p), m, seed, weight_seed, ctypes.byref(h))
+        if nnz < 0:
+            raise MemoryError("chung_lu: host allocation failed")
+        rowptr = np.empty(n + 1, dtype=np.int32)
+        cols = np.empty(nnz, dtype=np.int32)
+        vals = np.empty(nnz, dtype=np.float64)
+        native.chung_lu_fetch(h, rowptr.ctypes.data_as(ctypes.c_void_p), cols.ctypes.data_as(ctypes.c_void_p),
+                              vals.ctypes.data_as(ctypes.c_void_p))
+        return rowptr, cols, vals
     u = uniform_01(seed, 2 * m)
     ends = np.searchsorted(cdf, u, side="right").astype(np.int64)
     np.minimum(ends, n - 1, out=ends)

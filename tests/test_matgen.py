@@ -57,3 +57,12 @@ def test_randdiag():
     A = matgen.csr_to_dense(rp, ci, va)
     assert np.allclose(A, A.T)
     assert np.all(np.diag(A) >= 4.0) and np.all(np.diag(A) < 5.0)
+
+
+def test_chung_lu_native_matches_numpy():
+    """The C helper of the Chung-Lu generator reproduces the numpy algorithm bit for bit."""
+    for n in (3000, 40000):
+        a = matgen.chung_lu(n, native=False)
+        b = matgen.chung_lu(n, native=True)
+        for x, y in zip(a, b):
+            assert x.dtype == y.dtype and np.array_equal(x, y)
