@@ -534,7 +534,7 @@ def main():
     ap.add_argument("--batch-count", type=int, default=0, help="problems in the batched workload (default 4096)")
     ap.add_argument("--batch-plain-sample", type=int, default=256,
                     help="problems of the batched workload timed through the one-problem-per-launch path")
-    ap.add_argument("--arith", default="pair", choices=["pair", "f64"])
+    ap.add_argument("--arith", default="pair", choices=["pair", "f64", "f32"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="batched workload: keep the default tuning table")
@@ -703,6 +703,7 @@ def main():
                            "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (basis 2.2 GB)"
                            if args.workload == "lap3d128" else "small inputs",
                            "krylov_steps_per_solve": steps_k[-1], "restarts_per_solve": restarts[-1],
+                           "precision_phase_steps": eps.getStats()["precision_steps"],
                            "nconv": nconvs[-1]},
                 "latency_ms": {"p50": float(np.percentile(lat_sorted, 50)), "p99": float(np.percentile(lat_sorted, 99))},
                 "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches}

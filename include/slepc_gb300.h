@@ -18,7 +18,14 @@ extern "C" {
  *       transformations (relative error per product below 2^-46), the only form that reaches the HBM roofline on
  *       GB300, whose FP64 pipe runs at about 1.2 TFLOP/s.
  *   EPS_GB300_ARITH_F64: plain IEEE FP64 fused multiply-add everywhere (slower on GB300). */
-typedef enum { EPS_GB300_ARITH_PAIR = 0, EPS_GB300_ARITH_F64 = 1 } EPSGB300Arith;
+/*   EPS_GB300_ARITH_F32: the precision form.  Operator values and the Krylov basis are stored in FP32 (half the
+ *       bytes of the memory-bound SpMV and Gram-Schmidt); every dot product, norm and accumulation is still formed
+ *       exactly in FP32 pairs, the orthogonalisation coefficients, DS and residuals stay FP64.  The FP32 basis
+ *       limits this phase to about 1e-7, so it runs to max(tol, 1e-6); each converged pair is then rechecked in
+ *       FP64 (||A x - lambda x|| / |lambda|), and if one fails tol an FP64-class refinement sweep (a pair-storage
+ *       solve started from the sum of the phase-1 Ritz vectors) finishes to tol.  EPSGB300GetStats reports the
+ *       steps of each phase. */
+typedef enum { EPS_GB300_ARITH_PAIR = 0, EPS_GB300_ARITH_F64 = 1, EPS_GB300_ARITH_F32 = 2 } EPSGB300Arith;
 PetscErrorCode EPSGB300SetArithmetic(EPS eps, EPSGB300Arith arith);
 PetscErrorCode EPSGB300GetArithmetic(EPS eps, EPSGB300Arith *arith);
 
@@ -50,6 +57,8 @@ typedef struct {
   double setup_seconds;      /* EPSSetUp: allocation and matrix upload */
   long long kernel_launches; /* CUDA kernels launched by the last EPSSolve */
   double solve_device_ms;    /* EPSSolve measured with CUDA events on the EPS stream */
+  long long precision_steps;    /* EPS_GB300_ARITH_F32: Krylov steps of the FP32-storage phase (included above) */
+  long long precision_restarts; /* EPS_GB300_ARITH_F32: restarts of the FP32-storage phase */
 } EPSGB300Stats;
 PetscErrorCode EPSGB300GetStats(EPS eps, EPSGB300Stats *stats);
 

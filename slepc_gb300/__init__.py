@@ -262,8 +262,10 @@ class EPS:
         _check(load().EPSKrylovSchurSetLocking(self.handle, int(bool(lock))), "EPSKrylovSchurSetLocking")
 
     def setArithmetic(self, arith):
-        """'pair' (FP64 storage, error-free FP32-pair arithmetic) or 'f64' (IEEE FP64 FMA)."""
-        _check(load().EPSGB300SetArithmetic(self.handle, 1 if arith == "f64" else 0), "EPSGB300SetArithmetic")
+        """'pair' (pair storage, error-free FP32-pair arithmetic), 'f64' (IEEE FP64 FMA) or 'f32' (the precision
+        form: FP32 values and basis with pair accumulation, FP64 recheck and refinement sweep)."""
+        code = {"pair": 0, "f64": 1, "f32": 2}[arith]
+        _check(load().EPSGB300SetArithmetic(self.handle, code), "EPSGB300SetArithmetic")
 
     def setTimeLimit(self, seconds):
         """Wall-time budget of EPSSolve (checked after each restart; 0 = none)."""
@@ -325,15 +327,17 @@ class EPS:
         return v.value
 
     def getStats(self):
-        buf = (ctypes.c_char * 64)()
+        buf = (ctypes.c_char * 80)()
         _check(load().EPSGB300GetStats(self.handle, buf), "EPSGB300GetStats")
         steps, restarts = np.frombuffer(bytes(buf[:16]), dtype=np.int64)
         solve_s, bytes_moved, setup_s = np.frombuffer(bytes(buf[16:40]), dtype=np.float64)
         launches = np.frombuffer(bytes(buf[40:48]), dtype=np.int64)[0]
         dev_ms = np.frombuffer(bytes(buf[48:56]), dtype=np.float64)[0]
+        psteps, prestarts = np.frombuffer(bytes(buf[56:72]), dtype=np.int64)
         return {"krylov_steps": int(steps), "restarts": int(restarts), "solve_seconds": float(solve_s),
                 "bytes_moved": float(bytes_moved), "setup_seconds": float(setup_s), "kernel_launches": int(launches),
-                "solve_device_ms": float(dev_ms)}
+                "solve_device_ms": float(dev_ms), "precision_steps": int(psteps),
+                "precision_restarts": int(prestarts)}
 
     KERNEL_CLASSES = ("spmv", "gs_dot", "gs_update", "restart", "ds")
 

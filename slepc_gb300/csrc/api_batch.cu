@@ -84,8 +84,8 @@ static BatchInst make_inst(EPS eps) {
 }
 
 PetscErrorCode ksg_engine_check(EPS e, int max_ncv) {
-  KSG_CHECK(e->storage == STORE_PAIR, PETSC_ERR_SUP,
-            "batched engine: the EPS uses EPS_GB300_ARITH_F64; the batched engine runs the pair arithmetic");
+  KSG_CHECK(e->arith == ARITH_PAIR && e->storage == STORE_PAIR, PETSC_ERR_SUP,
+            "batched engine: the EPS must use the pair arithmetic (EPS_GB300_ARITH_PAIR)");
   KSG_CHECK(e->ncv_e <= max_ncv, PETSC_ERR_SUP, "batched engine: ncv = %d exceeds the limit %d", e->ncv_e, max_ncv);
   return 0;
 }

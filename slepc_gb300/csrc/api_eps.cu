@@ -197,9 +197,30 @@ PetscErrorCode ksg_mat_upload_pairs(Mat A) {
   return 0;
 }
 
+void *ksg_col(void *V, long long ldv, int j, int storage) {
+  return static_cast<char *>(V) + (size_t)j * (size_t)ldv * ksg_entry_bytes(storage);
+}
+
+PetscErrorCode ksg_mat_upload_f32(Mat A) {
+  KSG_TRY(ksg_mat_upload(A));
+  if (A->d_va32.p || A->nnz == 0) return 0;
+  std::vector<float> h(A->nnz);
+  for (long long p = 0; p < A->nnz; ++p) h[p] = (float)A->aa[p];
+  KSG_CUDA(A->d_va32.alloc(A->nnz));
+  KSG_CUDA(cudaMemcpy(A->d_va32.p, h.data(), sizeof(float) * A->nnz, cudaMemcpyHostToDevice));
+  return 0;
+}
+
 PetscErrorCode ksg_put_column(void *dst, const double *src, int n, int storage, cudaStream_t s) {
   if (storage == STORE_F64) {
     KSG_CUDA(cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    return 0;
+  }
+  if (storage == STORE_F32) {
+    std::vector<float> h(n);
+    for (int i = 0; i < n; ++i) h[i] = (float)src[i];
+    KSG_CUDA(cudaMemcpyAsync(dst, h.data(), sizeof(float) * n, cudaMemcpyHostToDevice, s));
+    KSG_CUDA(cudaStreamSynchronize(s));
     return 0;
   }
   std::vector<float2> h(n);
@@ -216,6 +237,13 @@ PetscErrorCode ksg_get_column(double *dst, const void *src, int n, int storage, 
   if (storage == STORE_F64) {
     KSG_CUDA(cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
     KSG_CUDA(cudaStreamSynchronize(s));
+    return 0;
+  }
+  if (storage == STORE_F32) {
+    std::vector<float> h(n);
+    KSG_CUDA(cudaMemcpyAsync(h.data(), src, sizeof(float) * n, cudaMemcpyDeviceToHost, s));
+    KSG_CUDA(cudaStreamSynchronize(s));
+    for (int i = 0; i < n; ++i) dst[i] = (double)h[i];
     return 0;
   }
   std::vector<float2> h(n);
@@ -420,7 +448,7 @@ PetscErrorCode ksg_orthonormalize_column(void *V, long long ldv, int n, int j, d
   a.J = j;
   a.j = j;
   a.hermitian = 1;
-  a.U = static_cast<double *>(V) + (size_t)j * ldv;  // 8 bytes per entry in both formats
+  a.U = ksg_col(V, ldv, j, storage);
   a.W = nullptr;
   a.eta = 0.7071;
   a.coef = coef;
@@ -668,7 +696,9 @@ extern "C" PetscErrorCode EPSKrylovSchurGetLocking(EPS eps, PetscBool *lock) {
 }
 extern "C" PetscErrorCode EPSGB300SetArithmetic(EPS eps, EPSGB300Arith arith) {
   KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
-  KSG_CHECK(arith == EPS_GB300_ARITH_PAIR || arith == EPS_GB300_ARITH_F64, PETSC_ERR_ARG_OUTOFRANGE, "Unknown arithmetic");
+  KSG_CHECK(arith == EPS_GB300_ARITH_PAIR || arith == EPS_GB300_ARITH_F64 || arith == EPS_GB300_ARITH_F32,
+            PETSC_ERR_ARG_OUTOFRANGE, "Unknown arithmetic");
+  KSG_CHECK(!eps->setup || eps->arith == (int)arith, PETSC_ERR_ORDER, "Set the arithmetic before EPSSetUp");
   eps->arith = arith;
   return 0;
 }
@@ -727,7 +757,9 @@ extern "C" PetscErrorCode EPSSetFromOptions(EPS eps) {
     else if (!strcmp(o, "-eps_krylovschur_locking") && v) KSG_TRY(EPSKrylovSchurSetLocking(eps, atoi(v) ? PETSC_TRUE : PETSC_FALSE));
     else if (!strcmp(o, "-eps_type") && v) KSG_TRY(EPSSetType(eps, v));
     else if (!strcmp(o, "-eps_gb300_arith") && v)
-      KSG_TRY(EPSGB300SetArithmetic(eps, !strcmp(v, "f64") ? EPS_GB300_ARITH_F64 : EPS_GB300_ARITH_PAIR));
+      KSG_TRY(EPSGB300SetArithmetic(eps, !strcmp(v, "f64")   ? EPS_GB300_ARITH_F64
+                                         : !strcmp(v, "f32") ? EPS_GB300_ARITH_F32
+                                                             : EPS_GB300_ARITH_PAIR));
     else if (!strcmp(o, "-eps_gb300_ds") && v)
       KSG_TRY(EPSGB300SetProjectedSolver(eps, !strcmp(v, "qr") ? EPS_GB300_DS_QR : EPS_GB300_DS_REFINED));
   }
@@ -798,10 +830,11 @@ extern "C" PetscErrorCode EPSSetUp(EPS eps) {
   KSG_CUDA(cudaMemsetAsync(eps->d.p, 0, sizeof(double) * eps->d.count, eps->stream));
   KSG_CUDA(cudaMemsetAsync(eps->e.p, 0, sizeof(double) * eps->e.count, eps->stream));
   if (!eps->h_ctl) KSG_CUDA(cudaMallocHost((void **)&eps->h_ctl, sizeof(KSControl)));
-  eps->storage = (eps->arith == ARITH_PAIR) ? STORE_PAIR : STORE_F64;
+  eps->storage = (eps->arith == ARITH_F64) ? STORE_F64 : STORE_PAIR;  // the precision form switches per phase
   KSG_TRY(ksg_mat_upload(eps->A));
   if (eps->A->n_seg > 0) KSG_CUDA(eps->seg_part.alloc(eps->A->n_seg));
   if (eps->storage == STORE_PAIR) KSG_TRY(ksg_mat_upload_pairs(eps->A));
+  if (eps->arith == ARITH_F32) KSG_TRY(ksg_mat_upload_f32(eps->A));
   // power-of-two operator scaling keeps every vector inside the range of the FP32-pair arithmetic; it is exact
   const double nrm = ksg_mat_norm_inf(eps->A);
   eps->opscale = 1.0;
@@ -916,12 +949,12 @@ static PetscErrorCode eps_factorize(EPS eps, int k0, int nv, double *bytes) {
     lr.part = eps->seg_part.p;
   }
   for (int j = k0; j < nv; ++j) {
-    double *u = eps->V.p + (size_t)j * eps->ldv;
-    double *w = u + eps->ldv;
+    void *u = ksg_col(eps->V.p, eps->ldv, j, eps->storage);
+    void *w = ksg_col(eps->V.p, eps->ldv, j + 1, eps->storage);
     {
       LaunchScope ls(eps, EPS_GB300_K_SPMV, spmv_bytes(eps));
       KSG_CUDA(launch_spmv_storage(eps->A->d_rp.p, eps->A->d_ci.p, eps->A->d_va.p, eps->A->d_va2.p, u, w, n,
-                                   eps->lanes, eps->st.p, eps->opscale, eps->storage, s, &lr));
+                                   eps->lanes, eps->st.p, eps->opscale, eps->storage, s, &lr, eps->A->d_va32.p));
     }
     a.J = j;
     a.j = j;
@@ -939,7 +972,7 @@ static PetscErrorCode eps_factorize(EPS eps, int k0, int nv, double *bytes) {
   }
   a.J = nv;
   a.j = nv;
-  a.U = eps->V.p + (size_t)nv * eps->ldv;
+  a.U = ksg_col(eps->V.p, eps->ldv, nv, eps->storage);
   a.W = nullptr;
   {
     LaunchScope ls(eps, EPS_GB300_K_GS_DOT, colb * (nv + 1));
@@ -959,21 +992,22 @@ static PetscErrorCode eps_factorize(EPS eps, int k0, int nv, double *bytes) {
 PetscErrorCode ksg_eps_put_start(EPS eps, cudaStream_t s) {
   std::vector<double> h;
   const double *src;
-  if (!eps->v0.empty()) src = eps->v0.data();
+  if (!eps->v0_internal.empty()) src = eps->v0_internal.data();  // the precision form's refinement sweep
+  else if (!eps->v0.empty()) src = eps->v0.data();
   else {
     h.resize(eps->n);
     ksg_random_fill(h.data(), eps->n, eps->seed, 0);
     src = h.data();
   }
   KSG_TRY(ksg_put_column(eps->V.p, src, eps->n, eps->storage, s));
-  if (eps->v0.empty()) KSG_CUDA(cudaStreamSynchronize(s));  // h is pageable and goes out of scope
+  KSG_CUDA(cudaStreamSynchronize(s));  // h is pageable and goes out of scope
   return 0;
 }
 
 PetscErrorCode ksg_eps_new_start_vector(EPS eps, int col, int *breakdown) {
   std::vector<double> h(eps->n);
   ksg_random_fill(h.data(), eps->n, eps->seed, ++eps->rng_counter);
-  double *dst = eps->V.p + (size_t)col * eps->ldv;
+  void *dst = ksg_col(eps->V.p, eps->ldv, col, eps->storage);
   KSG_TRY(ksg_put_column(dst, h.data(), eps->n, eps->storage, eps->stream));
   double nrm = 0.0;
   int ld = 0;
@@ -1046,9 +1080,9 @@ PetscErrorCode ksg_eps_assemble(EPS eps, int nconv, const double *er, const doub
       if (eps->r_eigi[i] < 0.0) {
         eps->r_eigi[i] = -eps->r_eigi[i];
         eps->r_eigi[i + 1] = -eps->r_eigi[i + 1];
-        // negate a basis column: both halves of a pair, or the double
-        KSG_CUDA(launch_negate(eps->V.p + (size_t)(i + 1) * eps->ldv, eps->storage == STORE_PAIR ? 2 * n : n,
-                               eps->storage == STORE_PAIR, s));
+        // negate a basis column: both halves of a pair, the float, or the double
+        KSG_CUDA(launch_negate(ksg_col(eps->V.p, eps->ldv, i + 1, eps->storage),
+                               eps->storage == STORE_PAIR ? 2 * n : n, eps->storage != STORE_F64, s));
       }
       i++;
     }
@@ -1059,26 +1093,13 @@ PetscErrorCode ksg_eps_assemble(EPS eps, int nconv, const double *er, const doub
   return 0;
 }
 
-extern "C" PetscErrorCode EPSSolve(EPS eps) {
-  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
-  KSG_TRY(EPSSetUp(eps));
-  KSG_CUDA(cudaSetDevice(eps->device));
+// One Krylov-Schur solve in the current storage format with tolerance tol (the body of EPSSolve): start vector,
+// restart loop, eigenvectors of the Schur form, results assembled into the EPS.
+static PetscErrorCode eps_solve_core(EPS eps, double tol, std::chrono::steady_clock::time_point t0, int *nconv_out,
+                                     int *its_out, int *reason_out, double *bytes_out) {
   cudaStream_t s = eps->stream;
-  auto t0 = std::chrono::steady_clock::now();
-  if (!eps->ev_solve[0]) {
-    KSG_CUDA(cudaEventCreate(&eps->ev_solve[0]));
-    KSG_CUDA(cudaEventCreate(&eps->ev_solve[1]));
-  }
-  KSG_CUDA(cudaEventRecord(eps->ev_solve[0], s));
   const int n = eps->n, ld = eps->ld, ncv = eps->ncv_e, mpd = eps->mpd_e, nev = eps->nev_e;
   const int herm = eps->problem == EPS_HEP;
-  eps->stats.krylov_steps = 0;
-  eps->stats.restarts = 0;
-  eps->stats.bytes_moved = 0.0;
-  eps->stats.kernel_launches = 0;
-  eps->ev_cls.clear();
-  eps->ev_used = 0;
-  eps->solved = 0;
   // start vector: the initial space, or a random vector (EPSGetStartVector, epssolve.c:841-873)
   {
     KSG_TRY(ksg_eps_put_start(eps, s));
@@ -1115,7 +1136,7 @@ extern "C" PetscErrorCode EPSSolve(EPS eps) {
     da.errest = eps->errest.p;
     da.work = eps->work.p;
     da.which = eps->which;
-    da.tol = eps->tol_e;
+    da.tol = tol;
     da.nev = nev;
     da.its = its;
     da.max_it = eps->maxit_e;
@@ -1159,8 +1180,9 @@ extern "C" PetscErrorCode EPSSolve(EPS eps) {
           if (bd) reason = EPS_DIVERGED_BREAKDOWN;
         }
       } else {
-        KSG_CUDA(cudaMemcpyAsync(eps->V.p + (size_t)(k + l) * eps->ldv, eps->V.p + (size_t)nv * eps->ldv,
-                                 sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+        KSG_CUDA(cudaMemcpyAsync(ksg_col(eps->V.p, eps->ldv, k + l, eps->storage),
+                                 ksg_col(eps->V.p, eps->ldv, nv, eps->storage), ksg_entry_bytes(eps->storage) * n,
+                                 cudaMemcpyDeviceToDevice, s));
       }
     }
     nconv = k;
@@ -1181,6 +1203,98 @@ extern "C" PetscErrorCode EPSSolve(EPS eps) {
   KSG_CUDA(cudaMemcpyAsync(es.data(), eps->errest.p, sizeof(double) * ld, cudaMemcpyDeviceToHost, s));
   KSG_CUDA(cudaStreamSynchronize(s));
   KSG_TRY(ksg_eps_assemble(eps, nconv, er.data(), ei.data(), es.data(), s));
+  *nconv_out = nconv;
+  *its_out = its;
+  *reason_out = reason;
+  *bytes_out = bytes;
+  return 0;
+}
+
+// in-place widening of basis columns [0, m) from FP32 to pairs (same leading dimension, twice the bytes); columns
+// are converted from the last down (column j's pairs overwrite the floats of columns 2j and 2j+1, converted
+// before it), column 0 through a temporary
+static PetscErrorCode eps_widen_f32_to_pair(EPS eps, int m) {
+  cudaStream_t s = eps->stream;
+  const int n = eps->n;
+  DBuf<double> tmp;
+  KSG_CUDA(tmp.alloc(n));
+  for (int j = m - 1; j >= 0; --j) {
+    const float *src = static_cast<const float *>(ksg_col(eps->V.p, eps->ldv, j, STORE_F32));
+    KSG_CUDA(launch_f32_to_f64(src, tmp.p, n, s));
+    KSG_CUDA(launch_f64_to_pair(tmp.p, static_cast<float2 *>(ksg_col(eps->V.p, eps->ldv, j, STORE_PAIR)), n, s));
+  }
+  KSG_CUDA(cudaStreamSynchronize(s));
+  return 0;
+}
+
+extern "C" PetscErrorCode EPSSolve(EPS eps) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  KSG_TRY(EPSSetUp(eps));
+  KSG_CUDA(cudaSetDevice(eps->device));
+  cudaStream_t s = eps->stream;
+  auto t0 = std::chrono::steady_clock::now();
+  if (!eps->ev_solve[0]) {
+    KSG_CUDA(cudaEventCreate(&eps->ev_solve[0]));
+    KSG_CUDA(cudaEventCreate(&eps->ev_solve[1]));
+  }
+  KSG_CUDA(cudaEventRecord(eps->ev_solve[0], s));
+  eps->stats.krylov_steps = 0;
+  eps->stats.restarts = 0;
+  eps->stats.bytes_moved = 0.0;
+  eps->stats.kernel_launches = 0;
+  eps->stats.precision_steps = 0;
+  eps->stats.precision_restarts = 0;
+  eps->ev_cls.clear();
+  eps->ev_used = 0;
+  eps->solved = 0;
+  int nconv = 0, its = 0, reason = 0;
+  double bytes = 0.0;
+  if (eps->arith != ARITH_F32) {
+    KSG_TRY(eps_solve_core(eps, eps->tol_e, t0, &nconv, &its, &reason, &bytes));
+  } else {
+    // The precision form.  Phase 1 stores the operator values and the basis in FP32 (half the bytes) with every
+    // product and sum accumulated exactly in pairs; its accuracy is limited by the FP32 basis (about 1e-7 relative),
+    // so it runs to max(tol, 1e-6).  Each converged pair is then rechecked in FP64 (||A x - lambda x|| / |lambda|);
+    // if one fails tol, an FP64-class refinement sweep -- a pair-storage Krylov-Schur solve started from the sum of
+    // the phase-1 Ritz vectors, whose Krylov space already holds the wanted directions -- finishes to tol.
+    const double tol1 = std::max(eps->tol_e, 1e-6);
+    eps->storage = STORE_F32;
+    KSG_TRY(eps_solve_core(eps, tol1, t0, &nconv, &its, &reason, &bytes));
+    eps->stats.precision_steps = eps->stats.krylov_steps;
+    eps->stats.precision_restarts = its;
+    eps->nconv = nconv;
+    eps->solved = 1;  // EPSComputeError reads the phase-1 results
+    bool pass = reason == 1;
+    const int check = std::min(nconv, eps->nev_e);
+    for (int i = 0; i < check && pass; ++i) {
+      double err = 0.0;
+      KSG_TRY(EPSComputeError(eps, i, EPS_ERROR_RELATIVE, &err));
+      if (!(err <= eps->tol_e)) pass = false;
+    }
+    eps->solved = 0;
+    if (pass) {
+      KSG_TRY(eps_widen_f32_to_pair(eps, nconv));
+      eps->storage = STORE_PAIR;
+    } else {
+      // start vector of the sweep: the sum of the phase-1 Ritz vectors of the wanted eigenvalues
+      std::vector<double> acc(eps->n, 0.0), col(eps->n);
+      const int use = std::max(1, std::min(nconv, eps->nev_e));
+      for (int i = 0; i < use && i < nconv; ++i) {
+        KSG_TRY(ksg_get_column(col.data(), ksg_col(eps->V.p, eps->ldv, eps->perm[i], STORE_F32), eps->n, STORE_F32,
+                               s));
+        for (int r = 0; r < eps->n; ++r) acc[r] += col[r];
+      }
+      eps->v0_internal.swap(acc);
+      eps->storage = STORE_PAIR;
+      int its2 = 0;
+      double bytes2 = 0.0;
+      PetscErrorCode ierr = eps_solve_core(eps, eps->tol_e, t0, &nconv, &its2, &reason, &bytes2);
+      eps->v0_internal.clear();
+      KSG_TRY(ierr);
+      its += its2;
+      bytes += bytes2;
+    }
+  }
   KSG_CUDA(cudaEventRecord(eps->ev_solve[1], s));
   KSG_CUDA(cudaStreamSynchronize(s));
   {
@@ -1302,21 +1416,27 @@ extern "C" PetscErrorCode EPSComputeError(EPS eps, PetscInt i, EPSErrorType type
   const int n = eps->n;
   const int k = eps->perm[i];
   double kr = eps->r_eigr[k], ki = eps->r_eigi[k];
-  const double *x = eps->V.p + (size_t)k * eps->ldv;
-  const double *xi = nullptr;
-  if (ki > 0.0) xi = x + eps->ldv;
-  else if (ki < 0.0) {
-    xi = x;
-    x = x - eps->ldv;
-    ki = -ki;  // the stored pair is (x, xi) for the eigenvalue with positive imaginary part
-  }
+  const int kx = (ki < 0.0) ? k - 1 : k;  // the stored pair is (x, xi) for the eigenvalue with positive imaginary part
+  const double *x = static_cast<const double *>(ksg_col(eps->V.p, eps->ldv, kx, eps->storage));
+  const double *xi = (ki != 0.0) ? static_cast<const double *>(ksg_col(eps->V.p, eps->ldv, kx + 1, eps->storage))
+                                  : nullptr;
+  if (ki < 0.0) ki = -ki;
   DBuf<double> y, yi, part, xd, xid;
   const int blocks = std::min(1024, (n + 255) / 256);
   KSG_CUDA(y.alloc(n));
   if (xi) KSG_CUDA(yi.alloc(n));
   KSG_CUDA(part.alloc(2 * blocks));
   cudaStream_t s = eps->stream;
-  if (eps->storage == STORE_PAIR) {
+  if (eps->storage == STORE_F32) {
+    KSG_CUDA(xd.alloc(n));
+    KSG_CUDA(launch_f32_to_f64(reinterpret_cast<const float *>(x), xd.p, n, s));
+    x = xd.p;
+    if (xi) {
+      KSG_CUDA(xid.alloc(n));
+      KSG_CUDA(launch_f32_to_f64(reinterpret_cast<const float *>(xi), xid.p, n, s));
+      xi = xid.p;
+    }
+  } else if (eps->storage == STORE_PAIR) {
     KSG_CUDA(xd.alloc(n));
     KSG_CUDA(launch_pair_to_f64(reinterpret_cast<const float2 *>(x), xd.p, n, s));
     x = xd.p;

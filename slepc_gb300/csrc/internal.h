@@ -72,6 +72,7 @@ struct _p_Mat {
   DBuf<int> d_rp, d_ci;
   DBuf<double> d_va;
   DBuf<float2> d_va2;  // values as FP32 pairs, for the pair-storage SpMV
+  DBuf<float> d_va32;  // values rounded to FP32, for the precision form
   // rows longer than LONG_ROW_T nonzeros, cut into segments (the skew-aware SpMV of kernels.h)
   DBuf<int> d_seg_row, d_seg_beg, d_seg_end, d_lrow, d_lfirst;
   int n_long = 0, n_seg = 0;
@@ -111,6 +112,7 @@ struct _p_EPS {
   double time_limit = 0.0;        // EPSGB300SetTimeLimit (0: none)
   int device = -1;
   std::vector<double> v0;
+  std::vector<double> v0_internal;  // start vector of the precision form's refinement sweep
   unsigned long long seed = 0x5EEDULL;
   unsigned long long rng_counter = 0;
   // state
@@ -152,6 +154,10 @@ PetscErrorCode ksg_orthonormalize_column(void *V, long long ldv, int n, int j, d
                                          int pstride, ksg::KrylovState *st, int arith, cudaStream_t s, double *nrm,
                                          int *lindep, int refine, int storage = ksg::STORE_F64);
 PetscErrorCode ksg_mat_upload_pairs(Mat A);
+PetscErrorCode ksg_mat_upload_f32(Mat A);
+// address of basis column j for the storage format (8 bytes per entry, 4 for STORE_F32; same leading dimension)
+inline size_t ksg_entry_bytes(int storage) { return storage == ksg::STORE_F32 ? 4 : 8; }
+void *ksg_col(void *V, long long ldv, int j, int storage);
 // host -> device copy of a double vector into a basis column of the given storage format
 PetscErrorCode ksg_put_column(void *dst, const double *src, int n, int storage, cudaStream_t s);
 // device basis column -> host doubles

@@ -151,6 +151,58 @@ __global__ void k_spmv_longfix_pair(LongRows lr, float2 *__restrict__ y, const K
   }
 }
 
+__global__ void __launch_bounds__(256) k_spmv_seg_f32(LongRows lr, const float *__restrict__ va,
+                                                      const int *__restrict__ ci, const float *__restrict__ x,
+                                                      const KrylovState *st) {
+  if (st && st->stop) return;
+  const int lane = threadIdx.x & 31;
+  const long long w0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  unsigned long long *part = static_cast<unsigned long long *>(lr.part);
+  for (long long sgi = w0; sgi < lr.n_seg; sgi += nw) {
+    dfacc acc;
+    acc_zero(acc);
+    for (int p = lr.seg_beg[sgi] + lane; p < lr.seg_end[sgi]; p += 32) {
+      f2x a2, x2;
+      a2.hi = __ldcs(va + p);
+      a2.lo = 0.0f;
+      x2.hi = __ldg(x + __ldcs(ci + p));
+      x2.lo = 0.0f;
+      acc_fma(acc, a2, x2);
+    }
+    acc = warp_reduce<PairAr>(acc);
+    if (lane == 0) part[sgi] = PairAr::pack(acc);
+  }
+}
+
+__global__ void k_spmv_longfix_f32(LongRows lr, float *__restrict__ y, const KrylovState *st, double scale) {
+  if (st && st->stop) return;
+  const f2x sc = split_f64(st ? st->sigma * scale : scale);
+  const unsigned long long *part = static_cast<const unsigned long long *>(lr.part);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < lr.n_long; i += gridDim.x * blockDim.x) {
+    dfacc acc;
+    acc_zero(acc);
+    for (int sgi = lr.lfirst[i]; sgi < lr.lfirst[i + 1]; ++sgi) acc_merge(acc, PairAr::unpack(part[sgi]));
+    f2x v;
+    v.hi = acc.s + acc.c;
+    v.lo = acc.c - (v.hi - acc.s);
+    dfacc pr;
+    acc_zero(pr);
+    acc_fma(pr, v, sc);
+    y[lr.lrow[i]] = pr.s + pr.c;
+  }
+}
+
+__global__ void k_f64_to_f32(const double *x, float *y, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    y[i] = __double2float_rn(x[i]);
+}
+
+__global__ void k_f32_to_f64(const float *x, double *y, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    y[i] = (double)x[i];
+}
+
 template <class S>
 __global__ void __launch_bounds__(256) k_spmv_seg_f64(LongRows lr, const double *__restrict__ va,
                                                       const int *__restrict__ ci, const typename S::T *__restrict__ x,
@@ -207,11 +259,26 @@ cudaError_t launch_spmv(const int *rp, const int *ci, const double *va, const do
 
 cudaError_t launch_spmv_storage(const int *rp, const int *ci, const double *va, const float2 *va_pair, const void *x,
                                 void *y, int n, int lanes, const KrylovState *st, double scale, int storage,
-                                cudaStream_t s, const LongRows *lr) {
+                                cudaStream_t s, const LongRows *lr, const float *va32) {
   const int blocks = spmv_blocks(n, lanes);
   const bool split = lr && lr->n_long > 0;
   const int long_t = split ? lr->long_t : 0x7fffffff;
   const int seg_blocks = split ? (int)std::min<long long>((lr->n_seg + 7) / 8, (long long)num_sms() * 8) : 0;
+  if (storage == STORE_F32) {
+    if (!va32) return cudaErrorInvalidValue;
+    const float *xx = static_cast<const float *>(x);
+    float *yy = static_cast<float *>(y);
+    switch (lanes) {
+      case 1: k_spmv_f32<1><<<blocks, 256, 0, s>>>(rp, ci, va32, xx, yy, n, st, scale, long_t); break;
+      case 8: k_spmv_f32<8><<<blocks, 256, 0, s>>>(rp, ci, va32, xx, yy, n, st, scale, long_t); break;
+      default: k_spmv_f32<32><<<blocks, 256, 0, s>>>(rp, ci, va32, xx, yy, n, st, scale, long_t); break;
+    }
+    if (split) {
+      k_spmv_seg_f32<<<seg_blocks, 256, 0, s>>>(*lr, va32, ci, xx, st);
+      k_spmv_longfix_f32<<<(lr->n_long + 127) / 128, 128, 0, s>>>(*lr, yy, st, scale);
+    }
+    return cudaGetLastError();
+  }
   if (storage == STORE_F64) {
     spmv_dispatch<StF64>(rp, ci, va, x, y, n, lanes, st, scale, blocks, s, long_t);
     if (split) {
@@ -240,6 +307,18 @@ cudaError_t launch_spmv_storage(const int *rp, const int *ci, const double *va, 
 cudaError_t launch_f64_to_pair(const double *x, float2 *y, long long n, cudaStream_t s) {
   int blocks = (int)std::min<long long>((n + 255) / 256, (long long)num_sms() * 8);
   k_f64_to_pair<<<blocks < 1 ? 1 : blocks, 256, 0, s>>>(x, y, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_f64_to_f32(const double *x, float *y, long long n, cudaStream_t s) {
+  int blocks = (int)std::min<long long>((n + 255) / 256, (long long)num_sms() * 8);
+  k_f64_to_f32<<<blocks < 1 ? 1 : blocks, 256, 0, s>>>(x, y, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_f32_to_f64(const float *x, double *y, long long n, cudaStream_t s) {
+  int blocks = (int)std::min<long long>((n + 255) / 256, (long long)num_sms() * 8);
+  k_f32_to_f64<<<blocks < 1 ? 1 : blocks, 256, 0, s>>>(x, y, n);
   return cudaGetLastError();
 }
 
@@ -280,6 +359,8 @@ static cudaError_t dot_dispatch(const StepArgs &a, int mode, int blocks, cudaStr
 // storage: STORE_F64 (doubles) or STORE_PAIR (FP32 pairs, pair arithmetic only)
 cudaError_t launch_gs_dot(const StepArgs &a, int nx, int mode, int arith, cudaStream_t s, int storage) {
   const int blocks = gs_dot_blocks(a.n);
+  if (storage == STORE_F32)
+    return nx == 2 ? dot_dispatch<2, PairAr, StF32>(a, mode, blocks, s) : dot_dispatch<1, PairAr, StF32>(a, mode, blocks, s);
   if (storage == STORE_PAIR)
     return nx == 2 ? dot_dispatch<2, PairAr, StPair>(a, mode, blocks, s) : dot_dispatch<1, PairAr, StPair>(a, mode, blocks, s);
   if (arith == ARITH_F64)
@@ -290,7 +371,10 @@ cudaError_t launch_gs_dot(const StepArgs &a, int nx, int mode, int arith, cudaSt
 cudaError_t launch_gs_update(const StepArgs &a, int nx, int mode, int arith, cudaStream_t s, int storage) {
   const int blocks = gs_update_blocks(a.n);
   const size_t shm = (size_t)nx * (a.J > 0 ? a.J : 1) * 8;
-  if (storage == STORE_PAIR) {
+  if (storage == STORE_F32) {
+    if (nx == 2) k_gs_update<2, PairAr, StF32><<<blocks, B_THREADS, shm, s>>>(a, mode);
+    else k_gs_update<1, PairAr, StF32><<<blocks, B_THREADS, shm, s>>>(a, mode);
+  } else if (storage == STORE_PAIR) {
     if (nx == 2) k_gs_update<2, PairAr, StPair><<<blocks, B_THREADS, shm, s>>>(a, mode);
     else k_gs_update<1, PairAr, StPair><<<blocks, B_THREADS, shm, s>>>(a, mode);
   } else if (arith == ARITH_F64) {
@@ -315,7 +399,11 @@ cudaError_t launch_restart(void *V, long long ldv, int n, int a0, int K, int s0,
   int blocks = num_sms();
   if (blocks > ntiles) blocks = ntiles;
   cudaError_t err;
-  if (storage == STORE_PAIR) {
+  if (storage == STORE_F32) {
+    err = cudaFuncSetAttribute(k_restart<PairAr, StF32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+    if (err != cudaSuccess) return err;
+    k_restart<PairAr, StF32><<<blocks, R_THREADS, shm, s>>>(static_cast<float *>(V), ldv, n, a0, K, s0, N, Q, ldq);
+  } else if (storage == STORE_PAIR) {
     err = cudaFuncSetAttribute(k_restart<PairAr, StPair>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
     if (err != cudaSuccess) return err;
     k_restart<PairAr, StPair><<<blocks, R_THREADS, shm, s>>>(static_cast<float2 *>(V), ldv, n, a0, K, s0, N, Q, ldq);

@@ -66,9 +66,11 @@ cudaError_t launch_spmv(const int *rp, const int *ci, const double *va, const do
                         const KrylovState *st, double scale, cudaStream_t s);
 cudaError_t launch_spmv_storage(const int *rp, const int *ci, const double *va, const float2 *va_pair, const void *x,
                                 void *y, int n, int lanes, const KrylovState *st, double scale, int storage,
-                                cudaStream_t s, const LongRows *lr = nullptr);
+                                cudaStream_t s, const LongRows *lr = nullptr, const float *va32 = nullptr);
 cudaError_t launch_f64_to_pair(const double *x, float2 *y, long long n, cudaStream_t s);
 cudaError_t launch_pair_to_f64(const float2 *x, double *y, long long n, cudaStream_t s);
+cudaError_t launch_f64_to_f32(const double *x, float *y, long long n, cudaStream_t s);
+cudaError_t launch_f32_to_f64(const float *x, double *y, long long n, cudaStream_t s);
 cudaError_t launch_gs_dot(const StepArgs &a, int nx, int mode, int arith, cudaStream_t s, int storage = STORE_F64);
 cudaError_t launch_gs_update(const StepArgs &a, int nx, int mode, int arith, cudaStream_t s, int storage = STORE_F64);
 cudaError_t launch_restart(void *V, long long ldv, int n, int a0, int K, int s0, int N, const double *Q, int ldq,

@@ -117,6 +117,43 @@ KS_DEVICE F64Ar::val StPair::pair_val<F64Ar>(float hi, float lo) {
   return (double)hi + (double)lo;
 }
 
+// StF32: FP32 entries (the precision form: half the bytes of the other formats).  Values widen exactly into the
+// pair arithmetic, so every product and sum is still accumulated at FP64-class accuracy; only storage rounds.
+struct StF32 {
+  using T = float;
+  template <class Ar>
+  static KS_DEVICE typename Ar::val widen(float v);
+  template <class Ar>
+  static KS_DEVICE void load2(const T *p, typename Ar::val &a, typename Ar::val &b) {
+    const float2 v = __ldcs(reinterpret_cast<const float2 *>(p));
+    a = widen<Ar>(v.x);
+    b = widen<Ar>(v.y);
+  }
+  template <class Ar>
+  static KS_DEVICE typename Ar::val load1(const T *p) { return widen<Ar>(*p); }
+  static KS_DEVICE double get(const T *p) { return (double)*p; }
+  static KS_DEVICE void put(T *p, double v) { *p = __double2float_rn(v); }
+  static KS_DEVICE void get2(const T *p, double &a, double &b) {
+    const float2 v = *reinterpret_cast<const float2 *>(p);
+    a = (double)v.x;
+    b = (double)v.y;
+  }
+  static KS_DEVICE void put2(T *p, double a, double b) {
+    *reinterpret_cast<float2 *>(p) = make_float2(__double2float_rn(a), __double2float_rn(b));
+  }
+};
+template <>
+KS_DEVICE PairAr::val StF32::widen<PairAr>(float v) {
+  f2x r;
+  r.hi = v;
+  r.lo = 0.0f;
+  return r;
+}
+template <>
+KS_DEVICE F64Ar::val StF32::widen<F64Ar>(float v) {
+  return (double)v;
+}
+
 template <class Ar>
 KS_DEVICE typename Ar::acc warp_reduce(typename Ar::acc a) {
 #pragma unroll
@@ -222,6 +259,67 @@ KS_DEVICE void spmv_pair_rows(const int *__restrict__ rp, const int *__restrict_
       y[row] = make_float2(hi, pr.c - (hi - pr.s));
     }
   }
+}
+
+// SpMV of the precision form: FP32 values and vectors, products exact in pairs, pair accumulation, result rounded
+// to FP32 once.
+template <int LANES>
+KS_DEVICE void spmv_f32_rows(const int *__restrict__ rp, const int *__restrict__ ci, const float *__restrict__ va,
+                             const float *__restrict__ x, float *__restrict__ y, int n, const KrylovState *st,
+                             double scale, long long warp_global, long long nwarps, int long_t = 0x7fffffff) {
+  if (st && st->stop) return;
+  const f2x sc = split_f64(st ? st->sigma * scale : scale);
+  constexpr int RPW = 32 / LANES;
+  const int lane = threadIdx.x & 31;
+  const int sub = lane % LANES, grp = lane / LANES;
+  for (long long base = warp_global * RPW; base < n; base += nwarps * RPW) {
+    const long long row = base + grp;
+    int p0 = 0, p1 = 0;
+    bool seg = false;
+    if (row < n) {
+      p0 = rp[row];
+      p1 = rp[row + 1];
+      if (p1 - p0 > long_t) {
+        seg = true;
+        p1 = p0;
+      }
+    }
+    dfacc acc;
+    acc_zero(acc);
+    for (int p = p0 + sub; p < p1; p += LANES) {
+      f2x a2, x2;
+      a2.hi = __ldcs(va + p);
+      a2.lo = 0.0f;
+      x2.hi = __ldg(x + __ldcs(ci + p));
+      x2.lo = 0.0f;
+      acc_fma(acc, a2, x2);
+    }
+#pragma unroll
+    for (int off = LANES / 2; off > 0; off >>= 1) {
+      dfacc o;
+      o.s = __shfl_down_sync(0xffffffffu, acc.s, off, LANES);
+      o.c = __shfl_down_sync(0xffffffffu, acc.c, off, LANES);
+      acc_merge(acc, o);
+    }
+    if (sub == 0 && row < n && !seg) {
+      f2x v;
+      v.hi = acc.s + acc.c;
+      v.lo = acc.c - (v.hi - acc.s);
+      dfacc pr;
+      acc_zero(pr);
+      acc_fma(pr, v, sc);
+      y[row] = pr.s + pr.c;
+    }
+  }
+}
+
+template <int LANES>
+__global__ void __launch_bounds__(256) k_spmv_f32(const int *__restrict__ rp, const int *__restrict__ ci,
+                                                  const float *__restrict__ va, const float *__restrict__ x,
+                                                  float *__restrict__ y, int n, const KrylovState *st, double scale,
+                                                  int long_t) {
+  spmv_f32_rows<LANES>(rp, ci, va, x, y, n, st, scale, ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5,
+                       ((long long)gridDim.x * blockDim.x) >> 5, long_t);
 }
 
 template <int LANES>

@@ -9,12 +9,14 @@ namespace ksg {
 enum Arith : int {
   ARITH_PAIR = 0,  // FP64 storage, products and sums on FP32 pairs with error-free transformations
   ARITH_F64 = 1,   // FP64 storage, IEEE FP64 FMA (exact reference arithmetic, FP64-pipe bound on GB300)
+  ARITH_F32 = 2,   // the precision form: FP32 values and basis with pair accumulation, then an FP64-class sweep
 };
 
 // Storage format of the Krylov basis.
 enum Storage : int {
   STORE_F64 = 0,   // IEEE doubles
   STORE_PAIR = 1,  // FP32 pairs (hi, lo), value hi + lo: 47-bit significand in 8 bytes
+  STORE_F32 = 2,   // FP32 (the precision form's first phase: half the bytes, exact widening into pairs)
 };
 
 // Per-factorisation state of the delayed-reorthogonalisation Gram-Schmidt (device resident).

@@ -144,3 +144,26 @@ def test_repeatable(lib):
     b = run(csr, hermitian=True, which="LR", nev=8, ncv=24, tol=1e-10, v0=v0)
     assert np.array_equal(a["eigr"], b["eigr"])
     assert np.array_equal(a["X"], b["X"])
+
+
+@pytest.mark.parametrize("tol", [1e-10, 1e-5])
+def test_precision_form(lib, orc, tol):
+    """FP32 values and basis with pair accumulation; the FP64 recheck passes at tol 1e-5 (no sweep) and fails at
+    1e-10, where the FP64-class refinement sweep finishes.  Error against the FP64 oracle stated per eigenpair."""
+    m = 14
+    csr = matgen.laplacian_3d_randdiag(m, 13)
+    v0 = matgen.start_vector(m ** 3, 6)
+    nev = 12
+    res = run(csr, hermitian=True, which="LR", nev=nev, ncv=40, tol=tol, v0=v0, arith="f32")
+    st = res["eps"].getStats()
+    assert res["reason"] == 1 and res["nconv"] >= nev
+    assert st["precision_steps"] > 0
+    if tol < 1e-6:
+        assert st["krylov_steps"] > st["precision_steps"]  # the refinement sweep ran
+    else:
+        assert st["krylov_steps"] == st["precision_steps"]
+    dense = np.linalg.eigvalsh(matgen.csr_to_dense(*csr))
+    errs = [np.min(np.abs(dense - v)) / abs(v) for v in res["eigr"][:nev]]
+    assert max(errs) <= max(tol, 1e-10), errs  # per-eigenpair error against the FP64 dense solve
+    check_residuals(csr, res, tol)
+    assert res["eps"].orthogonalityError() <= (1e-12 if tol < 1e-6 else 1e-6)
