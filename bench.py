@@ -562,22 +562,16 @@ def main():
         run_reference(args, wl)
         return
 
-    rank, world, local = dist_env()
+    import ctypes
+
     import slepc_gb300 as sg
     from slepc_gb300 import matgen
+    from slepc_gb300.replicas import Replicas
 
     sg.build()
-    dist = None
-    if world > 1:
-        import torch
-        import torch.distributed as td
-
-        torch.cuda.set_device(local)
-        td.init_process_group("nccl")
-        dist = (torch, td)
-    else:
-        import ctypes
-        ctypes.CDLL("libcudart.so").cudaSetDevice(local)
+    rep = Replicas()
+    rank, world, local = rep.rank, rep.world, rep.local
+    ctypes.CDLL("libcudart.so").cudaSetDevice(local)
 
     csr = wl["gen"](matgen)
     n = len(csr[0]) - 1
@@ -595,17 +589,8 @@ def main():
         eps.setInitialSpace(v0)
         return eps
 
-    def barrier():
-        if dist:
-            dist[1].barrier()
-            dist[0].cuda.synchronize()
-
-    def max_over_ranks(x):
-        if not dist:
-            return x
-        t = dist[0].tensor([x], dtype=dist[0].float64, device="cuda")
-        dist[1].all_reduce(t, op=dist[1].ReduceOp.MAX)
-        return float(t.item())
+    barrier = rep.barrier
+    max_over_ranks = rep.max
 
     A = sg.Mat(*csr)
     eps = make_eps(A)
@@ -708,8 +693,7 @@ def main():
                 "latency_ms": {"p50": float(np.percentile(lat_sorted, 50)), "p99": float(np.percentile(lat_sorted, 99))},
                 "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches}
         print(json.dumps(line), flush=True)
-    if dist:
-        dist[1].destroy_process_group()
+    rep.close()
 
 
 if __name__ == "__main__":
