@@ -43,7 +43,7 @@ def test_replicas_gloo_two_ranks():
     import oracle
 
     oracle.build()  # before the workers start
-    mgr = mp.Manager()
+    mgr = mp.get_context("spawn").Manager()
     out = mgr.dict()
     mp.start_processes(_worker, args=(2, _free_port(), out), nprocs=2, start_method="spawn", join=True)
     assert sorted(out.keys()) == [0, 1]
