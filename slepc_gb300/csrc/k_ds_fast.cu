@@ -56,18 +56,14 @@ DSFArgs ds_fast_layout(double *scratch, int ld) {
   return f;
 }
 
-KS_DEVICE int dsf_compare(int which, double ar, double br) {
-  double a, b;
-  switch (which) {
-    case 1: a = fabs(ar); b = fabs(br); return a < b ? 1 : (a > b ? -1 : 0);
-    case 2: a = fabs(ar); b = fabs(br); return a > b ? 1 : (a < b ? -1 : 0);
-    case 3: return ar < br ? 1 : (ar > br ? -1 : 0);
-    case 4: return ar > br ? 1 : (ar < br ? -1 : 0);
-    default: return 0;
-  }
-}
-
 KS_DEVICE int dsf_active(const DSFArgs &f) { return (f.st ? f.st->m : f.n) - f.l; }
+
+// a signed integer key with the order of the double (NaN-free input): negative values have all bits below the sign
+// flipped
+KS_DEVICE long long dsf_order_key(double x) {
+  const long long b = __double_as_longlong(x);
+  return b >= 0 ? b : (b ^ 0x7fffffffffffffffLL);
+}
 
 // Dense T of the active block from the compact storage: diagonal d; couplings e[i] for i in [l, n-1), between
 // rows i and k when i < k (arrow, raw form) and between rows i and i+1 otherwise.
@@ -496,6 +492,7 @@ __global__ void __launch_bounds__(DSF_THREADS, 1) k_dsf_step(DSFArgs f, int fina
 // restart control record (the tail of EPSSolve_KrylovSchur_Default for the symmetric case, krylovschur.c:270-322).
 __global__ void __launch_bounds__(DSF_THREADS, 1) k_dsf_finish(DSFArgs f, DSArgs a) {
   __shared__ double lam[DSF_MAXN], serr[DSF_MAXN];
+  __shared__ long long k_crit[DSF_MAXN], k_asc[DSF_MAXN];
   __shared__ int perm[DSF_MAXN];
   __shared__ double s_beta_e;
   const int tid = threadIdx.x;
@@ -503,25 +500,25 @@ __global__ void __launch_bounds__(DSF_THREADS, 1) k_dsf_finish(DSFArgs f, DSArgs
   if (tid == 0) s_beta_e = a.e[n - 1];
   for (int i = tid; i < m; i += DSF_THREADS) lam[i] = f.lam[i];
   __syncthreads();
-  if (tid == 0) {
-    // ascending order (steqr's contract) then insertion sort by the criterion (dspriv.c:226-245)
-    for (int i = 0; i < m; ++i) perm[i] = i;
-    for (int i = 1; i < m; ++i) {
-      const int pi = perm[i];
-      int j = i - 1;
-      while (j >= 0 && lam[perm[j]] > lam[pi]) { perm[j + 1] = perm[j]; --j; }
-      perm[j + 1] = pi;
+  // The order of steqr's ascending sort followed by the stable insertion sort by the criterion (dspriv.c:226-245):
+  // by the criterion first, ties by ascending value, then by index.  Each thread ranks its own eigenvalue with
+  // order-preserving integer keys (k_crit: the criterion's "goes first" order, k_asc: ascending value).
+  for (int i = tid; i < m; i += DSF_THREADS) {
+    const double v = lam[i] + 0.0;  // -0 -> +0, as the floating-point comparisons treat them
+    const double c = (a.which == 1 || a.which == 2) ? fabs(v) : v;
+    const long long kv = dsf_order_key(v), kc0 = dsf_order_key(c);
+    k_asc[i] = kv;
+    k_crit[i] = (a.which == 1 || a.which == 3) ? ~kc0 : kc0;  // largest first: reversed
+  }
+  __syncthreads();
+  for (int i = tid; i < m; i += DSF_THREADS) {
+    const long long ci = k_crit[i], ai = k_asc[i];
+    int r = 0;
+    for (int j = 0; j < m; ++j) {
+      const long long cj = k_crit[j], aj = k_asc[j];
+      r += (cj < ci) || (cj == ci && (aj < ai || (aj == ai && j < i)));
     }
-    for (int i = 1; i < m; ++i) {
-      const double re = lam[perm[i]];
-      int j = i - 1;
-      int res = dsf_compare(a.which, re, lam[perm[j]]);
-      while (res < 0 && j >= 0) {
-        const int t = perm[j]; perm[j] = perm[j + 1]; perm[j + 1] = t;
-        --j;
-        if (j >= 0) res = dsf_compare(a.which, re, lam[perm[j]]);
-      }
-    }
+    perm[r] = i;
   }
   __syncthreads();
   for (int idx = tid; idx < n * n; idx += DSF_THREADS) {

@@ -396,7 +396,9 @@ cudaError_t launch_restart(void *V, long long ldv, int n, int a0, int K, int s0,
   const size_t shm = restart_smem_bytes(K, N);
   if (shm > 227 * 1024) return cudaErrorInvalidValue;
   const int ntiles = (n + R_ROWS - 1) / R_ROWS;
-  int blocks = num_sms();
+  // two resident blocks per SM when shared memory allows (128 registers x 256 threads leaves room for two)
+  const int per_sm = shm * 2 <= (size_t)227 * 1024 ? 2 : 1;
+  int blocks = num_sms() * per_sm;
   if (blocks > ntiles) blocks = ntiles;
   cudaError_t err;
   if (storage == STORE_F32) {
