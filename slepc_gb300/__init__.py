@@ -80,6 +80,7 @@ def load():
         "EPSGB300ServerDestroy": ([PP], I),
         "EPSGB300ServerCancel": ([P], I),
         "EPSGB300SetTimeLimit": ([P, D], I),
+        "EPSGB300SetRestartMethod": ([P, I], I),
         "EPSGB300BatchGetTuning": ([ctypes.POINTER(I), I], I),
         "EPSGB300BatchSetTuning": ([ctypes.POINTER(I), I], I),
         "EPSGB300GetStats": ([P, P], I),
@@ -267,6 +268,10 @@ class EPS:
         code = {"pair": 0, "f64": 1, "f32": 2}[arith]
         _check(load().EPSGB300SetArithmetic(self.handle, code), "EPSGB300SetArithmetic")
 
+    def setRestartMethod(self, method):
+        """'tensor' (bf16 tensor cores with an error-free split, default) or 'pair' (CUDA-core pair arithmetic)."""
+        _check(load().EPSGB300SetRestartMethod(self.handle, 1 if method == "pair" else 0), "EPSGB300SetRestartMethod")
+
     def setTimeLimit(self, seconds):
         """Wall-time budget of EPSSolve (checked after each restart; 0 = none)."""
         _check(load().EPSGB300SetTimeLimit(self.handle, float(seconds)), "EPSGB300SetTimeLimit")
@@ -432,7 +437,7 @@ def batch_set_tuning(tiles):
 
 
 def solve(csr, *, hermitian=True, which="LM", nev=1, ncv=None, mpd=None, tol=None, max_it=None, v0=None,
-          arith="pair", vectors=True, ds=None, lock=None):
+          arith="pair", vectors=True, ds=None, lock=None, restart=None):
     """One-call convenience: returns dict(eigr, eigi, X, nconv, its, reason, errors, stats)."""
     A = Mat(*csr)
     eps = EPS().create()
@@ -444,6 +449,8 @@ def solve(csr, *, hermitian=True, which="LM", nev=1, ncv=None, mpd=None, tol=Non
     eps.setArithmetic(arith)
     if ds is not None:
         eps.setProjectedSolver(ds)
+    if restart is not None:
+        eps.setRestartMethod(restart)
     if lock is not None:
         eps.setKrylovSchurLocking(lock)
     if v0 is not None:

@@ -503,6 +503,7 @@ static PetscErrorCode eps_free_device(EPS eps) {
   eps->work.release();
   eps->dsf.release();
   eps->seg_part.release();
+  eps->rtc.release();
   eps->part.release();
   eps->st.release();
   eps->ctl.release();
@@ -719,6 +720,13 @@ extern "C" PetscErrorCode EPSGB300GetProjectedSolver(EPS eps, EPSGB300DSMethod *
   *method = (EPSGB300DSMethod)eps->ds_method;
   return 0;
 }
+extern "C" PetscErrorCode EPSGB300SetRestartMethod(EPS eps, EPSGB300RestartMethod method) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  KSG_CHECK(method == EPS_GB300_RESTART_TENSOR || method == EPS_GB300_RESTART_PAIR, PETSC_ERR_ARG_OUTOFRANGE,
+            "Unknown restart method");
+  eps->restart_method = method;
+  return 0;
+}
 extern "C" PetscErrorCode EPSGB300SetTimeLimit(EPS eps, PetscReal seconds) {
   KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
   eps->time_limit = seconds;
@@ -760,6 +768,8 @@ extern "C" PetscErrorCode EPSSetFromOptions(EPS eps) {
       KSG_TRY(EPSGB300SetArithmetic(eps, !strcmp(v, "f64")   ? EPS_GB300_ARITH_F64
                                          : !strcmp(v, "f32") ? EPS_GB300_ARITH_F32
                                                              : EPS_GB300_ARITH_PAIR));
+    else if (!strcmp(o, "-eps_gb300_restart") && v)
+      KSG_TRY(EPSGB300SetRestartMethod(eps, !strcmp(v, "pair") ? EPS_GB300_RESTART_PAIR : EPS_GB300_RESTART_TENSOR));
     else if (!strcmp(o, "-eps_gb300_ds") && v)
       KSG_TRY(EPSGB300SetProjectedSolver(eps, !strcmp(v, "qr") ? EPS_GB300_DS_QR : EPS_GB300_DS_REFINED));
   }
@@ -821,6 +831,7 @@ extern "C" PetscErrorCode EPSSetUp(EPS eps) {
   KSG_CUDA(eps->coef.alloc(2 * ld + 8));
   KSG_CUDA(eps->work.alloc(4 * ld + 8));
   KSG_CUDA(eps->dsf.alloc(ds_fast_scratch_doubles(ld)));
+  KSG_CUDA(eps->rtc.alloc(restart_tc_scratch_bytes(ld)));
   eps->pstride = (int)ksg_part_stride(ld);
   KSG_CUDA(eps->part.alloc(ksg_part_blocks(n) * eps->pstride));
   KSG_CUDA(eps->st.alloc(1));
@@ -1093,6 +1104,15 @@ PetscErrorCode ksg_eps_assemble(EPS eps, int nconv, const double *er, const doub
   return 0;
 }
 
+// V(:, s0:s0+N) = V(:, a0:a0+K) Q(a0:a0+K, s0:s0+N): the tensor-core restart for pair storage (default), the
+// pair-arithmetic CUDA-core kernel otherwise
+static cudaError_t eps_restart(EPS eps, int a0, int K, int s0, int N, const double *Q, cudaStream_t s) {
+  if (eps->storage == STORE_PAIR && eps->restart_method == EPS_GB300_RESTART_TENSOR)
+    return launch_restart_tc(reinterpret_cast<float2 *>(eps->V.p), eps->ldv, eps->n, a0, K, s0, N, Q, eps->ld,
+                             eps->rtc.p, eps->ld, s);
+  return launch_restart(eps->V.p, eps->ldv, eps->n, a0, K, s0, N, Q, eps->ld, eps->arith, s, eps->storage);
+}
+
 // One Krylov-Schur solve in the current storage format with tolerance tol (the body of EPSSolve): start vector,
 // restart loop, eigenvectors of the Schur form, results assembled into the EPS.
 static PetscErrorCode eps_solve_core(EPS eps, double tol, std::chrono::steady_clock::time_point t0, int *nconv_out,
@@ -1167,8 +1187,7 @@ static PetscErrorCode eps_solve_core(EPS eps, double tol, std::chrono::steady_cl
     // thick restart: V(:, nconv:k+l) = V(:, nconv:nv) Q(nconv:nv, nconv:k+l)
     {
       LaunchScope ls(eps, EPS_GB300_K_RESTART, 8.0 * n * ((nv - nconv) + (k + l - nconv)));
-      KSG_CUDA(launch_restart(eps->V.p, eps->ldv, n, nconv, nv - nconv, nconv, k + l - nconv, eps->Q.p, ld, eps->arith,
-                              s, eps->storage));
+      KSG_CUDA(eps_restart(eps, nconv, nv - nconv, nconv, k + l - nconv, eps->Q.p, s));
     }
     bytes += 8.0 * n * ((nv - nconv) + (k + l - nconv));
     if (reason == 0) {
@@ -1194,7 +1213,7 @@ static PetscErrorCode eps_solve_core(EPS eps, double tol, std::chrono::steady_cl
   // non-Hermitian: eigenvectors of the leading Schur block, V = V X (EPSComputeVectors_Schur, epsdefault.c:105-169)
   if (!herm && nconv > 0) {
     KSG_CUDA(launch_nhep_vectors(eps->H.p, ld, nconv, eps->X.p, s));
-    KSG_CUDA(launch_restart(eps->V.p, eps->ldv, n, 0, nconv, 0, nconv, eps->X.p, ld, eps->arith, s, eps->storage));
+    KSG_CUDA(eps_restart(eps, 0, nconv, 0, nconv, eps->X.p, s));
     bytes += 16.0 * n * nconv;
   }
   std::vector<double> er(ld), ei(ld), es(ld);

@@ -110,6 +110,7 @@ struct _p_EPS {
   int storage = ksg::STORE_PAIR;  // basis format: pairs with pair arithmetic, doubles with FP64 arithmetic
   int ds_method = 0;              // EPSGB300DSMethod
   double time_limit = 0.0;        // EPSGB300SetTimeLimit (0: none)
+  int restart_method = 0;         // EPSGB300RestartMethod
   int device = -1;
   std::vector<double> v0;
   std::vector<double> v0_internal;  // start vector of the precision form's refinement sweep
@@ -125,6 +126,7 @@ struct _p_EPS {
   cudaStream_t stream = nullptr;
   DBuf<double> V, d, e, H, Q, X, eigr, eigi, errest, coef, work, dsf;
   DBuf<double> seg_part;  // one 8-byte partial per long-row segment of the operator
+  DBuf<unsigned char> rtc;  // slices of Q for the tensor-core restart
   DBuf<float2> part;
   int pstride = 0;
   DBuf<ksg::KrylovState> st;

@@ -75,6 +75,10 @@ cudaError_t launch_gs_dot(const StepArgs &a, int nx, int mode, int arith, cudaSt
 cudaError_t launch_gs_update(const StepArgs &a, int nx, int mode, int arith, cudaStream_t s, int storage = STORE_F64);
 cudaError_t launch_restart(void *V, long long ldv, int n, int a0, int K, int s0, int N, const double *Q, int ldq,
                            int arith, cudaStream_t s, int storage = STORE_F64);
+// the restart on the bf16 tensor cores (pair storage, k_restart_tc.cu); scratch of restart_tc_scratch_bytes(ld)
+size_t restart_tc_scratch_bytes(int ld);
+cudaError_t launch_restart_tc(float2 *V, long long ldv, int n, int a0, int K, int s0, int N, const double *Q, int ldq,
+                              void *scratch, int ld, cudaStream_t s);
 cudaError_t launch_segment_begin(KrylovState *st, int k0, int m, cudaStream_t s);
 cudaError_t launch_set_unit_scale(KrylovState *st, cudaStream_t s);
 cudaError_t launch_set_scales(KrylovState *st, double sigma, double invnu, cudaStream_t s);

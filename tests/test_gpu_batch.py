@@ -12,7 +12,7 @@ from slepc_gb300 import matgen
 pytestmark = pytest.mark.gpu
 
 
-def make(csr, hermitian, which, nev, ncv, tol, seed, ds=None):
+def make(csr, hermitian, which, nev, ncv, tol, seed, ds=None, restart=None):
     A = sg.Mat(*csr)
     eps = sg.EPS().create()
     eps.setOperators(A)
@@ -22,6 +22,8 @@ def make(csr, hermitian, which, nev, ncv, tol, seed, ds=None):
     eps.setWhichEigenpairs(which)
     if ds:
         eps.setProjectedSolver(ds)
+    if restart:
+        eps.setRestartMethod(restart)
     eps.setInitialSpace(matgen.start_vector(len(csr[0]) - 1, seed))
     eps._A = A  # keep the matrix alive as long as the solver
     return eps
@@ -50,7 +52,8 @@ def mixed_problems():
 
 def test_batch_equals_single_problem_path(lib):
     """With one tile per virtual block the batch partitions every reduction exactly as the single-problem kernels
-    do, so the results are bit-identical to EPSSolve with the same (QR) projected solver."""
+    do, so the results are bit-identical to EPSSolve with the same (QR) projected solver and the same (CUDA-core)
+    restart kernel."""
     saved = sg.batch_get_tuning()
     try:
         sg.batch_set_tuning([1] * sg.BATCH_BUCKETS)
@@ -58,7 +61,7 @@ def test_batch_equals_single_problem_path(lib):
         batch = [make(*p) for p in probs]
         sg.solve_batch(batch)
         for p, b in zip(probs, batch):
-            alone = make(*p, ds="qr")
+            alone = make(*p, ds="qr", restart="pair")
             alone.solve()
             ra, rb = results(alone), results(b)
             assert ra[0] == rb[0] and ra[1] == rb[1] and ra[2] == rb[2] == 1
