@@ -28,7 +28,9 @@ constexpr int OZ_L = 8;          // levels s + t kept
 constexpr int OZ_ROWS = 64;      // rows of V per tile
 constexpr int OZ_THREADS = 256;  // 8 warps: 4 row groups of 16 x 2 column halves of a chunk
 constexpr int OZ_NC = 32;        // output columns per chunk (4 mma n-tiles)
-constexpr int OZ_PAD = 8;        // bf16 padding per smem row (conflict-free fragment loads)
+constexpr int OZ_PAD = 8;        // bf16 padding per row of the Q slices (rows stay 16-byte aligned for 16-byte copies)
+constexpr int OZ_PADA = 2;       // bf16 padding per row of the V slices: an odd word stride, so the slicing pass's
+                                 // stores from 32 consecutive rows hit 32 banks
 
 size_t restart_tc_scratch_bytes(int ld) {
   const int kp = (ld + 15) / 16 * 16, np = (ld + OZ_NC - 1) / OZ_NC * OZ_NC;
@@ -36,8 +38,9 @@ size_t restart_tc_scratch_bytes(int ld) {
 }
 
 static size_t oz_smem_bytes(int kp) {
-  return ((size_t)OZ_SA * OZ_ROWS * (kp + OZ_PAD) + (size_t)OZ_S * OZ_NC * (kp + OZ_PAD)) * sizeof(__nv_bfloat16) +
-         OZ_ROWS * sizeof(int);
+  return ((size_t)OZ_SA * OZ_ROWS * (kp + OZ_PADA) + (size_t)OZ_S * OZ_NC * (kp + OZ_PAD)) *
+             sizeof(__nv_bfloat16) +
+         OZ_ROWS * sizeof(int) + 16;
 }
 
 // Column exponents and slices of Q(a0 + k, s0 + c), k < K, c < N (zero-padded to kp x np): one block per column.
@@ -107,10 +110,12 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_restart_tc(float2 *__restrict
                                                                const __nv_bfloat16 *__restrict__ Bsl,
                                                                const int *__restrict__ fcol) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  const int lda = kp + OZ_PAD;
+  const int lda = kp + OZ_PADA, ldb = kp + OZ_PAD;
   __nv_bfloat16 *As = reinterpret_cast<__nv_bfloat16 *>(smraw);  // [s][r][k]
-  __nv_bfloat16 *Bs = As + (size_t)OZ_SA * OZ_ROWS * lda;        // [t][c][k]
-  int *erow = reinterpret_cast<int *>(Bs + (size_t)OZ_S * OZ_NC * lda);
+  // Q slices after the V slices, rounded up to a 16-byte boundary
+  const size_t aoff = ((size_t)OZ_SA * OZ_ROWS * lda * sizeof(__nv_bfloat16) + 15) / 16 * 16;
+  __nv_bfloat16 *Bs = reinterpret_cast<__nv_bfloat16 *>(smraw + aoff);  // [t][c][k]
+  int *erow = reinterpret_cast<int *>(Bs + (size_t)OZ_S * OZ_NC * ldb);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int g = lane >> 2, tq = lane & 3;
   const int rg = warp >> 1, half = warp & 1;
@@ -155,7 +160,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_restart_tc(float2 *__restrict
       for (int i = tid; i < OZ_S * OZ_NC * kv; i += OZ_THREADS) {
         const int q = i % kv, cr = (i / kv) % OZ_NC, t = i / (kv * OZ_NC);
         const uint4 w = *reinterpret_cast<const uint4 *>(Bsl + ((size_t)t * np + c0 + cr) * kp + q * 8);
-        *reinterpret_cast<uint4 *>(Bs + ((size_t)t * OZ_NC + cr) * lda + q * 8) = w;
+        *reinterpret_cast<uint4 *>(Bs + ((size_t)t * OZ_NC + cr) * ldb + q * 8) = w;
       }
       __syncthreads();
       float acc[2][OZ_L][4];
@@ -182,7 +187,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_restart_tc(float2 *__restrict
           unsigned bf[OZ_S][2];
 #pragma unroll
           for (int t = 0; t < OZ_S; ++t) {
-            const __nv_bfloat16 *base = Bs + ((size_t)t * OZ_NC + bcol) * lda + k0 + 2 * tq;
+            const __nv_bfloat16 *base = Bs + ((size_t)t * OZ_NC + bcol) * ldb + k0 + 2 * tq;
             bf[t][0] = *reinterpret_cast<const unsigned *>(base);
             bf[t][1] = *reinterpret_cast<const unsigned *>(base + 8);
           }

@@ -178,7 +178,7 @@ def test_tensor_restart_matches_pair_restart(lib, herm):
     if herm:
         csr, kw = matgen.laplacian_3d_randdiag(18, 3), dict(hermitian=True, which="LR", nev=16, ncv=56)
     else:
-        csr, kw = matgen.convection_diffusion_2d(60, 20.0), dict(hermitian=False, which="LR", nev=10, ncv=40)
+        csr, kw = matgen.convection_diffusion_2d(40, 2.0), dict(hermitian=False, which="LR", nev=10, ncv=40)
     n = len(csr[0]) - 1
     v0 = matgen.start_vector(n, 21)
     a = run(csr, tol=1e-10, v0=v0, restart="tensor", **kw)
@@ -188,9 +188,9 @@ def test_tensor_restart_matches_pair_restart(lib, herm):
         check_residuals(csr, r, 1e-10)
         if herm:
             assert r["eps"].orthogonalityError() <= 1e-12
-    # symmetric: 1e-12.  The convection-diffusion operator is strongly non-normal with doubly degenerate eigenvalues,
-    # whose two computed copies move by ~1e-9 under any rounding change; they agree to that conditioning.
-    agree = 1e-12 if herm else 1e-8
+    # symmetric: 1e-12.  The convection-diffusion operator (mildly non-normal at Pe = 2) has doubly degenerate
+    # eigenvalues whose computed copies move with the rounding; 1e-10 is the parity bound of the closed form.
+    agree = 1e-12 if herm else 1e-10
     vb = np.asarray(b["eigr"]) + 1j * np.asarray(b["eigi"])
     for x, y in zip(a["eigr"][:kw["nev"]], a["eigi"][:kw["nev"]]):
         z = complex(x, y)
