@@ -227,6 +227,8 @@ def run_batch(args):
         e.setTolerances(BATCH["tol"])
         e.setWhichEigenpairs(BATCH["which"])
         e.setInitialSpace(matgen.start_vector(len(csr[0]) - 1, seed))
+        if args.arith == "f32":
+            e.setArithmetic("f32")  # the FP32-storage variant
         e._A = A
         return e
 
@@ -289,7 +291,7 @@ def run_batch(args):
             "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * sum(times) / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": BATCH["desc"].replace("4096", str(count)), "instances": count, "sum_n": nsum,
-                       "arith": "pair", "parallelism": "replicas x1", "l2": "inputs larger than L2 (bases 13 GB)",
+                       "arith": args.arith, "parallelism": "replicas x1", "l2": "inputs larger than L2 (bases 13 GB)",
                        "restarts_per_instance": {"min": min(its), "median": float(np.median(its)), "max": max(its)},
                        "generate_s": round(gen_s, 1), "setup_s": round(setup_s, 1),
                        "tuning": {"tiles_per_virtual_block_by_bucket": tuning, "tune_s": round(tune_s, 1)}},

@@ -64,6 +64,8 @@ static BatchInst make_inst(EPS eps) {
   p.rp = eps->A->d_rp.p;
   p.ci = eps->A->d_ci.p;
   p.va2 = eps->A->d_va2.p;
+  p.va32 = eps->A->d_va32.p;
+  p.storage = eps->storage;
   p.V = reinterpret_cast<float2 *>(eps->V.p);
   p.ldv = eps->ldv;
   p.d = eps->d.p;
@@ -83,18 +85,19 @@ static BatchInst make_inst(EPS eps) {
   return p;
 }
 
-PetscErrorCode ksg_engine_check(EPS e, int max_ncv) {
-  KSG_CHECK(e->arith == ARITH_PAIR && e->storage == STORE_PAIR, PETSC_ERR_SUP,
-            "batched engine: the EPS must use the pair arithmetic (EPS_GB300_ARITH_PAIR)");
+PetscErrorCode ksg_engine_check(EPS e, int max_ncv, bool allow_f32) {
+  KSG_CHECK(e->arith == ARITH_PAIR || (allow_f32 && e->arith == ARITH_F32), PETSC_ERR_SUP,
+            "batched engine: the EPS must use the pair arithmetic%s", allow_f32 ? " or the precision form" : "");
   KSG_CHECK(e->ncv_e <= max_ncv, PETSC_ERR_SUP, "batched engine: ncv = %d exceeds the limit %d", e->ncv_e, max_ncv);
   return 0;
 }
 
-PetscErrorCode ksg_engine_init(BatchEngine &B, int device, int cap, int max_ncv) {
+PetscErrorCode ksg_engine_init(BatchEngine &B, int device, int cap, int max_ncv, bool with_f32) {
   KSG_CHECK(max_ncv >= 1 && max_ncv <= batch_max_columns() - 1, PETSC_ERR_ARG_OUTOFRANGE,
             "batched engine: ncv limit %d outside [1, %d]", max_ncv, batch_max_columns() - 1);
   B.device = device;
   B.cap = cap;
+  B.has_f32 = with_f32;
   B.slots = max_ncv + 1;
   B.max_ld = max_ncv + 1;
   KSG_CUDA(cudaSetDevice(device));
@@ -125,19 +128,30 @@ static PetscErrorCode engine_enqueue_cycle(BatchEngine &B, long long *launches) 
   long long nl = 0;
   cudaStream_t s = B.s;
   KSG_CUDA(launch_batch_begin(B.inst.p, B.list.p, B.hdr.p, B.grid_inst, s));
-  KSG_CUDA(launch_batch_dot(B.inst.p, B.map_dot.p, B.hdr.p, -1, B.grid_dot, s));
-  KSG_CUDA(launch_batch_update(B.inst.p, B.map_upd.p, B.hdr.p, -1, B.grid_upd, B.max_ld, s));
+  for (int q = 0; q < (B.has_f32 ? 2 : 1); ++q) {
+    const int st = q ? STORE_F32 : STORE_PAIR;
+    KSG_CUDA(launch_batch_dot(B.inst.p, B.map_dot.p, B.hdr.p, -1, B.grid_dot, s, st));
+    KSG_CUDA(launch_batch_update(B.inst.p, B.map_upd.p, B.hdr.p, -1, B.grid_upd, B.max_ld, s, st));
+    nl += 2;
+  }
   KSG_CUDA(launch_batch_start(B.inst.p, B.list.p, B.hdr.p, B.grid_inst, s));
-  nl += 4;
+  nl += 2;
+  // the FP32 kernels are captured only when the engine holds precision-form instances
+  const int nsto = B.has_f32 ? 2 : 1;
+  const int sto[2] = {STORE_PAIR, STORE_F32};
   for (int slot = 0; slot < B.slots; ++slot) {
-    KSG_CUDA(launch_batch_spmv(B.inst.p, B.map_spmv.p, B.hdr.p, slot, B.grid_spmv, s));
-    KSG_CUDA(launch_batch_dot(B.inst.p, B.map_dot.p, B.hdr.p, slot, B.grid_dot, s));
-    KSG_CUDA(launch_batch_update(B.inst.p, B.map_upd.p, B.hdr.p, slot, B.grid_upd, B.max_ld, s));
-    nl += 3;
+    for (int q = 0; q < nsto; ++q) {
+      KSG_CUDA(launch_batch_spmv(B.inst.p, B.map_spmv.p, B.hdr.p, slot, B.grid_spmv, s, sto[q]));
+      KSG_CUDA(launch_batch_dot(B.inst.p, B.map_dot.p, B.hdr.p, slot, B.grid_dot, s, sto[q]));
+      KSG_CUDA(launch_batch_update(B.inst.p, B.map_upd.p, B.hdr.p, slot, B.grid_upd, B.max_ld, s, sto[q]));
+      nl += 3;
+    }
   }
   KSG_CUDA(launch_batch_ds_hep(B.inst.p, B.list.p, B.hdr.p, B.grid_ds, B.max_ld, s));
   KSG_CUDA(launch_batch_ds_nhep(B.inst.p, B.list.p, B.hdr.p, B.grid_ds, B.max_ld, s));
-  KSG_CUDA(launch_batch_restart(B.inst.p, B.map_rst.p, B.hdr.p, B.grid_rst, B.max_ld, s));
+  for (int q = 0; q < nsto; ++q)
+    KSG_CUDA(launch_batch_restart(B.inst.p, B.map_rst.p, B.hdr.p, B.grid_rst, B.max_ld, s, sto[q]));
+  nl += nsto - 1;
   KSG_CUDA(launch_batch_control(B.inst.p, B.list.p, B.hdr.p, B.status.p, B.grid_inst, s));
   nl += 4;
   KSG_CUDA(cudaMemcpyAsync(B.h_status, B.status.p, sizeof(BatchStatus) * B.cap, cudaMemcpyDeviceToHost, s));
@@ -210,27 +224,31 @@ static PetscErrorCode engine_upload_maps(BatchEngine &B) {
 
 // Take a set-up EPS into a free slot: start vector into column 0, instance record to the device, all on the EPS's
 // own stream (the engine's stream may be running a cycle).  The instance joins the live set at ksg_engine_activate.
-PetscErrorCode ksg_engine_admit(BatchEngine &B, EPS e, int *slot) {
+PetscErrorCode ksg_engine_admit(BatchEngine &B, EPS e, int *slot, double tol) {
   KSG_CHECK(!B.free_slots.empty(), PETSC_ERR_GPU_RESOURCE, "batched engine: all %d slots are in use", B.cap);
+  KSG_CHECK(e->storage != STORE_F32 || B.has_f32, PETSC_ERR_PLIB, "batched engine built without the FP32 kernels");
   const int i = B.free_slots.back();
   B.free_slots.pop_back();
   B.eps[i] = e;
   B.hi[i] = make_inst(e);
+  if (tol > 0.0) B.hi[i].tol = tol;
   e->solved = 0;
   e->stats = EPSGB300Stats{};
   cudaStream_t s = e->stream;
   // the start vector in FP64 into column 1, converted to pairs in column 0 (column 1 is rewritten by the first SpMV)
   std::vector<double> rnd;
   const double *src;
-  if (!e->v0.empty()) src = e->v0.data();
+  if (!e->v0_internal.empty()) src = e->v0_internal.data();  // the precision form's refinement sweep
+  else if (!e->v0.empty()) src = e->v0.data();
   else {
     rnd.resize(e->n);
     ksg_random_fill(rnd.data(), e->n, e->seed, 0);
     src = rnd.data();
   }
-  double *stage = e->V.p + e->ldv;
+  double *stage = e->V.p + e->ldv;  // bytes [8 ldv, 16 ldv): clear of column 0 in either format
   KSG_CUDA(cudaMemcpyAsync(stage, src, sizeof(double) * e->n, cudaMemcpyHostToDevice, s));
-  KSG_CUDA(launch_f64_to_pair(stage, reinterpret_cast<float2 *>(e->V.p), e->n, s));
+  if (e->storage == STORE_F32) KSG_CUDA(launch_f64_to_f32(stage, reinterpret_cast<float *>(e->V.p), e->n, s));
+  else KSG_CUDA(launch_f64_to_pair(stage, reinterpret_cast<float2 *>(e->V.p), e->n, s));
   KSG_CUDA(cudaMemcpyAsync(B.inst.p + i, &B.hi[i], sizeof(BatchInst), cudaMemcpyHostToDevice, s));
   KSG_CUDA(cudaStreamSynchronize(s));  // rnd and the host record go out of scope / may change
   *slot = i;
@@ -327,10 +345,12 @@ extern "C" PetscErrorCode EPSGB300SolveBatch(PetscInt count, EPS *eps) {
   KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS array");
   auto t0 = std::chrono::steady_clock::now();
   int device = -1, max_ncv = 1;
+  bool any_f32 = false;
   for (int i = 0; i < count; ++i) {
     KSG_CHECK(eps[i], PETSC_ERR_ARG_NULL, "Null EPS at position %d", i);
     KSG_TRY(EPSSetUp(eps[i]));
-    KSG_TRY(ksg_engine_check(eps[i], batch_max_columns() - 1));
+    KSG_TRY(ksg_engine_check(eps[i], batch_max_columns() - 1, true));
+    any_f32 = any_f32 || eps[i]->arith == ARITH_F32;
     max_ncv = std::max(max_ncv, eps[i]->ncv_e);
     if (device < 0) device = eps[i]->device;
     KSG_CHECK(eps[i]->device == device, PETSC_ERR_ARG_INCOMP, "EPSGB300SolveBatch: all EPS must use one device");
@@ -339,35 +359,94 @@ extern "C" PetscErrorCode EPSGB300SolveBatch(PetscInt count, EPS *eps) {
   KSG_CUDA(cudaSetDevice(device));
   KSG_CUDA(cudaDeviceSynchronize());  // EPSSetUp work on the objects' own streams
   BatchEngine B;
-  KSG_TRY(ksg_engine_init(B, device, (int)count, max_ncv));
-  std::vector<int> slots(count);
-  for (int i = 0; i < count; ++i) KSG_TRY(ksg_engine_admit(B, eps[i], &slots[i]));
-  KSG_TRY(ksg_engine_activate(B, slots));
+  KSG_TRY(ksg_engine_init(B, device, (int)count, max_ncv, any_f32));
+  // the precision form runs its FP32 phase first (to max(tol, 1e-6)), then, after the FP64 recheck, either widens
+  // the basis or goes through the engine again as an FP64-class refinement sweep (EPSSolve's precision driver)
+  std::vector<int> slot_of(count), stage(count, 0);  // stage: 0 plain, 1 FP32 phase, 2 refinement sweep
+  std::vector<long long> psteps(count, 0), pits(count, 0);
+  std::vector<int> owner(count, -1);
+  std::vector<int> first;
+  for (int i = 0; i < count; ++i) {
+    EPS e = eps[i];
+    double tol = 0.0;
+    if (e->arith == ARITH_F32) {
+      e->storage = STORE_F32;
+      stage[i] = 1;
+      tol = std::max(e->tol_e, 1e-6);
+    }
+    KSG_TRY(ksg_engine_admit(B, e, &slot_of[i], tol));
+    owner[slot_of[i]] = i;
+    first.push_back(slot_of[i]);
+  }
+  KSG_TRY(ksg_engine_activate(B, first));
   std::vector<std::pair<int, int>> retired;
   int first_err = 0, err_at = -1;
   while (!B.live.empty()) {
     KSG_TRY(ksg_engine_launch(B));
     retired.clear();
     KSG_TRY(ksg_engine_finish(B, &retired));
-    for (auto &r : retired)
-      if (r.second && !first_err) {
-        first_err = r.second;
-        err_at = r.first;
+    std::vector<int> again;
+    for (auto &r : retired) {
+      const int i = owner[r.first];
+      owner[r.first] = -1;
+      if (r.second) {
+        if (!first_err) {
+          first_err = r.second;
+          err_at = i;
+        }
+        continue;
       }
+      EPS e = eps[i];
+      if (stage[i] == 1) {
+        psteps[i] = e->stats.krylov_steps;
+        pits[i] = e->its;
+        bool pass = e->reason == 1;
+        for (int k = 0; k < std::min(e->nconv, e->nev_e) && pass; ++k) {
+          double err = 0.0;
+          KSG_TRY(EPSComputeError(e, k, EPS_ERROR_RELATIVE, &err));
+          if (!(err <= e->tol_e)) pass = false;
+        }
+        if (pass) {
+          KSG_TRY(ksg_eps_widen_f32(e, e->nconv));
+          e->storage = STORE_PAIR;
+          e->stats.precision_steps = psteps[i];
+          e->stats.precision_restarts = pits[i];
+          stage[i] = 0;
+        } else {
+          std::vector<double> acc(e->n, 0.0), col(e->n);
+          const int use = std::max(1, std::min(e->nconv, e->nev_e));
+          for (int k = 0; k < use && k < e->nconv; ++k) {
+            KSG_TRY(ksg_get_column(col.data(), ksg_col(e->V.p, e->ldv, e->perm[k], STORE_F32), e->n, STORE_F32,
+                                   e->stream));
+            for (int r2 = 0; r2 < e->n; ++r2) acc[r2] += col[r2];
+          }
+          e->v0_internal.swap(acc);
+          e->storage = STORE_PAIR;
+          stage[i] = 2;
+          int sl = -1;
+          KSG_TRY(ksg_engine_admit(B, e, &sl, 0.0));
+          owner[sl] = i;
+          again.push_back(sl);
+        }
+      } else if (stage[i] == 2) {
+        e->v0_internal.clear();
+        e->stats.precision_steps = psteps[i];
+        e->stats.precision_restarts = pits[i];
+        e->stats.krylov_steps += psteps[i];
+        e->its += (int)pits[i];
+        stage[i] = 0;
+      }
+    }
+    if (!again.empty()) KSG_TRY(ksg_engine_activate(B, again));
   }
   const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   for (int i = 0; i < count; ++i) {
     eps[i]->stats.solve_seconds = secs;
     eps[i]->stats.kernel_launches = B.cycles * B.launches_per_cycle;
   }
-  if (first_err) {
-    int pos = 0;
-    for (int i = 0; i < count; ++i)
-      if (slots[i] == err_at) pos = i;
-    KSG_CHECK(false, first_err, "EPSGB300SolveBatch: problem %d failed (%s)", pos,
-              first_err == 77 ? "initial vector is zero or the Krylov segment is empty"
-                              : "the projected eigenproblem solver did not converge");
-  }
+  KSG_CHECK(!first_err, first_err, "EPSGB300SolveBatch: problem %d failed (%s)", err_at,
+            first_err == 77 ? "initial vector is zero or the Krylov segment is empty"
+                            : "the projected eigenproblem solver did not converge");
   return 0;
 }
 

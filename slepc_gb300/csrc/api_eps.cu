@@ -1232,7 +1232,7 @@ static PetscErrorCode eps_solve_core(EPS eps, double tol, std::chrono::steady_cl
 // in-place widening of basis columns [0, m) from FP32 to pairs (same leading dimension, twice the bytes); columns
 // are converted from the last down (column j's pairs overwrite the floats of columns 2j and 2j+1, converted
 // before it), column 0 through a temporary
-static PetscErrorCode eps_widen_f32_to_pair(EPS eps, int m) {
+PetscErrorCode ksg_eps_widen_f32(EPS eps, int m) {
   cudaStream_t s = eps->stream;
   const int n = eps->n;
   DBuf<double> tmp;
@@ -1292,7 +1292,7 @@ extern "C" PetscErrorCode EPSSolve(EPS eps) {
     }
     eps->solved = 0;
     if (pass) {
-      KSG_TRY(eps_widen_f32_to_pair(eps, nconv));
+      KSG_TRY(ksg_eps_widen_f32(eps, nconv));
       eps->storage = STORE_PAIR;
     } else {
       // start vector of the sweep: the sum of the phase-1 Ritz vectors of the wanted eigenvalues

@@ -132,7 +132,7 @@ static void server_loop(EPSGB300Server S) {
     std::vector<int> new_slots;
     for (EPS e : take) {
       PetscErrorCode ierr = EPSSetUp(e);
-      if (!ierr) ierr = ksg_engine_check(e, S->B.max_ld - 1);
+      if (!ierr) ierr = ksg_engine_check(e, S->B.max_ld - 1, false);
       int slot = -1;
       if (!ierr) ierr = ksg_engine_admit(S->B, e, &slot);
       std::lock_guard<std::mutex> lk(S->m);

@@ -31,6 +31,7 @@ struct BatchEngine {
   long long launches_per_cycle = 0;
   long long cycles = 0;
   bool maps_dirty = true;
+  bool has_f32 = false;  // the cycle graph includes the FP32-storage kernels
   std::vector<BatchInst> hi;  // host copy of each slot's problem fields
   std::vector<EPS> eps;       // slot -> EPS (nullptr when free)
   std::vector<int> live;      // slots in the live set
@@ -38,9 +39,10 @@ struct BatchEngine {
   ~BatchEngine();
 };
 
-PetscErrorCode ksg_engine_check(EPS e, int max_ncv);
-PetscErrorCode ksg_engine_init(BatchEngine &B, int device, int cap, int max_ncv);
-PetscErrorCode ksg_engine_admit(BatchEngine &B, EPS e, int *slot);
+PetscErrorCode ksg_engine_check(EPS e, int max_ncv, bool allow_f32);
+PetscErrorCode ksg_engine_init(BatchEngine &B, int device, int cap, int max_ncv, bool with_f32 = false);
+// tol > 0 overrides the EPS tolerance (the precision form's FP32 phase)
+PetscErrorCode ksg_engine_admit(BatchEngine &B, EPS e, int *slot, double tol = 0.0);
 PetscErrorCode ksg_engine_activate(BatchEngine &B, const std::vector<int> &slots);
 PetscErrorCode ksg_engine_launch(BatchEngine &B);
 // retired: (slot, PETSc error code or 0) of every instance whose restart loop ended in this cycle

@@ -20,8 +20,10 @@ struct BatchInst {
   double tol, keep, opscale;
   const int *rp, *ci;
   const float2 *va2;
-  float2 *V;
+  const float *va32;  // the precision form's FP32 values (storage STORE_F32)
+  float2 *V;          // the basis; STORE_F32 instances read it as float with the same leading dimension
   long long ldv;
+  int storage;        // STORE_PAIR or STORE_F32
   double *d, *e, *H, *Q, *eigr, *eigi, *errest, *coef, *work;
   float2 *part;
   int pstride;
@@ -55,14 +57,15 @@ struct BatchStatus {
 int batch_max_columns();
 cudaError_t launch_batch_begin(BatchInst *I, const int *list, const BatchHdr *h, int grid_inst, cudaStream_t s);
 cudaError_t launch_batch_start(BatchInst *I, const int *list, const BatchHdr *h, int grid_inst, cudaStream_t s);
+// the Krylov-step and restart launchers serve the instances of one storage format (STORE_PAIR or STORE_F32)
 cudaError_t launch_batch_spmv(const BatchInst *I, const BatchVB *map, const BatchHdr *h, int slot, int grid,
-                              cudaStream_t s);
+                              cudaStream_t s, int storage);
 cudaError_t launch_batch_dot(const BatchInst *I, const BatchVB *map, const BatchHdr *h, int slot, int grid,
-                             cudaStream_t s);
+                             cudaStream_t s, int storage);
 cudaError_t launch_batch_update(const BatchInst *I, const BatchVB *map, const BatchHdr *h, int slot, int grid,
-                                int max_ld, cudaStream_t s);
+                                int max_ld, cudaStream_t s, int storage);
 cudaError_t launch_batch_restart(const BatchInst *I, const BatchVB *map, const BatchHdr *h, int grid, int max_ld,
-                                 cudaStream_t s);
+                                 cudaStream_t s, int storage);
 cudaError_t launch_batch_control(BatchInst *I, const int *list, const BatchHdr *h, BatchStatus *status,
                                  int grid_inst, cudaStream_t s);
 cudaError_t launch_batch_ds_hep(const BatchInst *I, const int *list, const BatchHdr *h, int grid, int max_ld,

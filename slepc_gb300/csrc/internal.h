@@ -166,6 +166,7 @@ PetscErrorCode ksg_put_column(void *dst, const double *src, int n, int storage, 
 PetscErrorCode ksg_get_column(double *dst, const void *src, int n, int storage, cudaStream_t s);
 // pieces of EPSSolve shared with the batched engine (api_batch.cu)
 PetscErrorCode ksg_eps_put_start(EPS eps, cudaStream_t s);
+PetscErrorCode ksg_eps_widen_f32(EPS eps, int m);  // basis columns [0, m): FP32 -> pairs, in place
 PetscErrorCode ksg_eps_new_start_vector(EPS eps, int col, int *breakdown);
 PetscErrorCode ksg_eps_assemble(EPS eps, int nconv, const double *er, const double *ei, const double *es,
                                 cudaStream_t s);

@@ -60,6 +60,14 @@ KS_DEVICE bool batch_slot(const BatchInst &p, int slot, int &mode, int &nx, int 
   return false;
 }
 
+// basis column j of instance p (8 bytes per entry, 4 for the precision form's FP32 phase)
+template <int STO = -1>
+KS_DEVICE void *batch_col(const BatchInst &p, int j) {
+  const size_t es = (STO == STORE_F32 || (STO < 0 && p.storage == STORE_F32)) ? 4 : 8;
+  return reinterpret_cast<char *>(p.V) + (size_t)j * (size_t)p.ldv * es;
+}
+
+template <int STO>
 KS_DEVICE StepArgs batch_step_args(const BatchInst &p, int j, int nx) {
   StepArgs a;
   a.V = p.V;
@@ -68,8 +76,8 @@ KS_DEVICE StepArgs batch_step_args(const BatchInst &p, int j, int nx) {
   a.J = j;
   a.j = j;
   a.hermitian = p.hermitian;
-  a.U = p.V + (size_t)j * p.ldv;
-  a.W = (nx == 2) ? (void *)(p.V + (size_t)(j + 1) * p.ldv) : nullptr;
+  a.U = batch_col<STO>(p, j);
+  a.W = (nx == 2) ? batch_col<STO>(p, j + 1) : nullptr;
   a.d = p.d;
   a.e = p.e;
   a.H = p.H;
@@ -121,20 +129,25 @@ __global__ void k_batch_start(BatchInst *I, const int *list, const BatchHdr *h) 
 
 template <int LANES>
 KS_DEVICE void batch_spmv_vb(const BatchInst &p, const BatchVB &m, int slot) {
-  const float2 *x = p.V + (size_t)slot * p.ldv;
-  float2 *y = p.V + (size_t)(slot + 1) * p.ldv;
   const long long w0 = (long long)m.b * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const long long nw = (long long)m.nb * (blockDim.x >> 5);
-  spmv_pair_rows<LANES>(p.rp, p.ci, p.va2, x, y, p.n, p.st, p.opscale, w0, nw);
+  if (p.storage == STORE_F32)
+    spmv_f32_rows<LANES>(p.rp, p.ci, p.va32, static_cast<const float *>(batch_col(p, slot)),
+                         static_cast<float *>(batch_col(p, slot + 1)), p.n, p.st, p.opscale, w0, nw);
+  else
+    spmv_pair_rows<LANES>(p.rp, p.ci, p.va2, static_cast<const float2 *>(batch_col(p, slot)),
+                          static_cast<float2 *>(batch_col(p, slot + 1)), p.n, p.st, p.opscale, w0, nw);
 }
 
+// each batched kernel serves the instances of one storage format (STO); the others skip their virtual blocks
+template <int STO>
 __global__ void __launch_bounds__(256) k_batch_spmv(const BatchInst *I, const BatchVB *map, const BatchHdr *h,
                                                     int slot) {
   const int nmap = h->n_spmv;
   for (int v = blockIdx.x; v < nmap; v += gridDim.x) {
     const BatchVB m = map[v];
     const BatchInst &p = I[m.inst];
-    if (p.phase != BP_ITER || slot < p.k0 || slot >= p.nv) continue;
+    if (p.storage != STO || p.phase != BP_ITER || slot < p.k0 || slot >= p.nv) continue;
     switch (p.lanes) {
       case 1: batch_spmv_vb<1>(p, m, slot); break;
       case 8: batch_spmv_vb<8>(p, m, slot); break;
@@ -148,6 +161,7 @@ __global__ void __launch_bounds__(256) k_batch_spmv(const BatchInst *I, const Ba
 constexpr int BATCH_CPW = 5;
 constexpr int BATCH_MAXJ = A_WARPS * BATCH_CPW;
 
+template <int STO, class S>
 __global__ void __launch_bounds__(A_THREADS, 1) k_batch_dot(const BatchInst *I, const BatchVB *map,
                                                             const BatchHdr *h, int slot) {
   const int nmap = h->n_dot;
@@ -155,14 +169,15 @@ __global__ void __launch_bounds__(A_THREADS, 1) k_batch_dot(const BatchInst *I, 
     const BatchVB m = map[v];
     const BatchInst &p = I[m.inst];
     int mode, nx, j;
-    if (!batch_slot(p, slot, mode, nx, j)) continue;
+    if (p.storage != STO || !batch_slot(p, slot, mode, nx, j)) continue;
     __syncthreads();  // shared staging of the previous virtual block is free
-    const StepArgs a = batch_step_args(p, j, nx);
-    if (nx == 2) gs_dot_body<2, BATCH_CPW, PairAr, StPair>(a, mode, m.b, m.nb);
-    else gs_dot_body<1, BATCH_CPW, PairAr, StPair>(a, mode, m.b, m.nb);
+    const StepArgs a = batch_step_args<STO>(p, j, nx);
+    if (nx == 2) gs_dot_body<2, BATCH_CPW, PairAr, S>(a, mode, m.b, m.nb);
+    else gs_dot_body<1, BATCH_CPW, PairAr, S>(a, mode, m.b, m.nb);
   }
 }
 
+template <int STO, class S>
 __global__ void __launch_bounds__(B_THREADS, 2) k_batch_update(const BatchInst *I, const BatchVB *map,
                                                             const BatchHdr *h, int slot) {
   const int nmap = h->n_upd;
@@ -170,37 +185,46 @@ __global__ void __launch_bounds__(B_THREADS, 2) k_batch_update(const BatchInst *
     const BatchVB m = map[v];
     const BatchInst &p = I[m.inst];
     int mode, nx, j;
-    if (!batch_slot(p, slot, mode, nx, j)) continue;
+    if (p.storage != STO || !batch_slot(p, slot, mode, nx, j)) continue;
     __syncthreads();
-    const StepArgs a = batch_step_args(p, j, nx);
-    if (nx == 2) gs_update_body<2, PairAr, StPair>(a, mode, m.b, m.nb);
-    else gs_update_body<1, PairAr, StPair>(a, mode, m.b, m.nb);
+    const StepArgs a = batch_step_args<STO>(p, j, nx);
+    if (nx == 2) gs_update_body<2, PairAr, S>(a, mode, m.b, m.nb);
+    else gs_update_body<1, PairAr, S>(a, mode, m.b, m.nb);
   }
 }
 
 // Thick restart V(:, nconv : k+l) = V(:, nconv : nv) Q(nconv : nv, nconv : k+l), then the residual column moves to
 // column k+l (krylovschur.c:300-329), for every instance whose projected problem was solved this cycle.
+template <int STO>
 __global__ void __launch_bounds__(R_THREADS, 1) k_batch_restart(const BatchInst *I, const BatchVB *map,
                                                                 const BatchHdr *h) {
   const int nmap = h->n_rst;
   for (int v = blockIdx.x; v < nmap; v += gridDim.x) {
     const BatchVB m = map[v];
     const BatchInst &p = I[m.inst];
-    if (p.phase != BP_ITER) continue;
+    if (p.storage != STO || p.phase != BP_ITER) continue;
     const KSControl c = *p.ctl;
     if (c.ds_error) continue;
     const int k = c.nconv, l = c.l, nv = c.nv, nconv = p.nconv;
     const int K = nv - nconv, N = k + l - nconv;
     __syncthreads();
-    if (K > 0 && N > 0) restart_body<PairAr, StPair>(p.V, p.ldv, p.n, nconv, K, nconv, N, p.Q, p.ld, m.b, m.nb);
+    if (K > 0 && N > 0) {
+      if (STO == STORE_F32)
+        restart_body<PairAr, StF32>(static_cast<float *>(batch_col(p, 0)), p.ldv, p.n, nconv, K, nconv, N, p.Q, p.ld,
+                                    m.b, m.nb);
+      else
+        restart_body<PairAr, StPair>(p.V, p.ldv, p.n, nconv, K, nconv, N, p.Q, p.ld, m.b, m.nb);
+    }
     if (c.reason == 0 && !(c.breakdown || k == nv)) {
       // this virtual block's rows only: the restart above already consumed column k+l for them
       const int ntiles = (p.n + R_ROWS - 1) / R_ROWS;
-      const float2 *src = p.V + (size_t)nv * p.ldv;
-      float2 *dst = p.V + (size_t)(k + l) * p.ldv;
+      const bool f32 = STO == STORE_F32;
       for (int t = m.b; t < ntiles; t += m.nb) {
         const int r = t * R_ROWS + threadIdx.x;
-        if (threadIdx.x < R_ROWS && r < p.n) dst[r] = src[r];
+        if (threadIdx.x < R_ROWS && r < p.n) {
+          if (f32) static_cast<float *>(batch_col(p, k + l))[r] = static_cast<const float *>(batch_col(p, nv))[r];
+          else static_cast<float2 *>(batch_col(p, k + l))[r] = static_cast<const float2 *>(batch_col(p, nv))[r];
+        }
       }
     }
   }
@@ -261,32 +285,41 @@ cudaError_t launch_batch_start(BatchInst *I, const int *list, const BatchHdr *h,
 }
 
 cudaError_t launch_batch_spmv(const BatchInst *I, const BatchVB *map, const BatchHdr *h, int slot, int grid,
-                              cudaStream_t s) {
-  k_batch_spmv<<<grid, 256, 0, s>>>(I, map, h, slot);
+                              cudaStream_t s, int storage) {
+  if (storage == STORE_F32) k_batch_spmv<STORE_F32><<<grid, 256, 0, s>>>(I, map, h, slot);
+  else k_batch_spmv<STORE_PAIR><<<grid, 256, 0, s>>>(I, map, h, slot);
   return cudaGetLastError();
 }
 
 cudaError_t launch_batch_dot(const BatchInst *I, const BatchVB *map, const BatchHdr *h, int slot, int grid,
-                             cudaStream_t s) {
-  k_batch_dot<<<grid, A_THREADS, 0, s>>>(I, map, h, slot);
+                             cudaStream_t s, int storage) {
+  if (storage == STORE_F32) k_batch_dot<STORE_F32, StF32><<<grid, A_THREADS, 0, s>>>(I, map, h, slot);
+  else k_batch_dot<STORE_PAIR, StPair><<<grid, A_THREADS, 0, s>>>(I, map, h, slot);
   return cudaGetLastError();
 }
 
 cudaError_t launch_batch_update(const BatchInst *I, const BatchVB *map, const BatchHdr *h, int slot, int grid,
-                                int max_ld, cudaStream_t s) {
-  k_batch_update<<<grid, B_THREADS, (size_t)2 * max_ld * sizeof(f2x), s>>>(I, map, h, slot);
+                                int max_ld, cudaStream_t s, int storage) {
+  const size_t shm = (size_t)2 * max_ld * sizeof(f2x);
+  if (storage == STORE_F32) k_batch_update<STORE_F32, StF32><<<grid, B_THREADS, shm, s>>>(I, map, h, slot);
+  else k_batch_update<STORE_PAIR, StPair><<<grid, B_THREADS, shm, s>>>(I, map, h, slot);
   return cudaGetLastError();
 }
 
 // kernel attributes, set before a cycle is captured
 cudaError_t batch_prepare_restart(int max_ld) {
-  return cudaFuncSetAttribute(k_batch_restart, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaError_t e = cudaFuncSetAttribute(k_batch_restart<STORE_PAIR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)restart_smem_bytes(max_ld, max_ld));
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_batch_restart<STORE_F32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)restart_smem_bytes(max_ld, max_ld));
 }
 
 cudaError_t launch_batch_restart(const BatchInst *I, const BatchVB *map, const BatchHdr *h, int grid, int max_ld,
-                                 cudaStream_t s) {
-  k_batch_restart<<<grid, R_THREADS, restart_smem_bytes(max_ld, max_ld), s>>>(I, map, h);
+                                 cudaStream_t s, int storage) {
+  const size_t shm = restart_smem_bytes(max_ld, max_ld);
+  if (storage == STORE_F32) k_batch_restart<STORE_F32><<<grid, R_THREADS, shm, s>>>(I, map, h);
+  else k_batch_restart<STORE_PAIR><<<grid, R_THREADS, shm, s>>>(I, map, h);
   return cudaGetLastError();
 }
 

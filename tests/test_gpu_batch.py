@@ -130,3 +130,28 @@ def test_batch_zero_start_vector_error(lib):
     with pytest.raises(sg.SlepcError) as ei:
         sg.solve_batch([eps])
     assert ei.value.code == 77
+
+
+def test_batch_precision_form(lib):
+    """The FP32-storage variant in the batch: FP32 phase, FP64 recheck, refinement sweep through the engine again;
+    mixed with pair-arithmetic problems in the same batch.  Eigenvalues against dense FP64 solves."""
+    probs = [(matgen.laplacian_2d_randdiag(n, 300 + n % 97), True, "LM", 8, 24, 1e-10, 40 + k)
+             for k, n in enumerate([1500, 2600, 3600])]
+    eps = [make(*p) for p in probs]
+    for e in eps[:2]:
+        e.setArithmetic("f32")
+    sg.solve_batch(eps)
+    for p, e in zip(probs, eps):
+        nconv, its, reason, vals, vecs = results(e)
+        assert reason == 1 and nconv >= p[3]
+        dense = np.linalg.eigvalsh(matgen.csr_to_dense(*p[0]))
+        for v in vals[:p[3]]:
+            assert np.min(np.abs(dense - v)) / abs(v) <= 1e-10
+        A = sg.Mat(*p[0])
+        nrm = max(np.add.reduceat(np.abs(p[0][2]), p[0][0][:-1]))
+        for v, x in zip(vals, vecs):
+            assert np.linalg.norm(A.mult(x) - v * x) / (nrm * abs(v)) <= 1e-10
+    for e in eps[:2]:
+        st = e.getStats()
+        assert 0 < st["precision_steps"] < st["krylov_steps"]
+    assert eps[2].getStats()["precision_steps"] == 0
