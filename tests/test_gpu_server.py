@@ -102,3 +102,41 @@ def test_server_budget_admission(lib):
         srv.destroy()
     for e in eps:
         assert e.getConvergedReason() == 1
+
+
+def test_server_two_lanes(lib):
+    """Small and large requests run in separate lanes (engines, graphs, streams) under one budget: each result is
+    bit-identical to the same problem solved alone, and the admitted footprint of both lanes together stays within
+    the budget while the large requests' reservation keeps the small ones from starving them."""
+    small = requests()[:4]
+    large = [(matgen.laplacian_3d_randdiag(64, 90 + i), True, "LR", 6, 24, 1e-10, 92 + i) for i in range(2)]
+    reqs = [small[0], large[0], small[1], small[2], large[1], small[3]]
+
+    def foot(p):
+        return (len(p[0][0]) - 1) * (p[4] + 1) * 8 + len(p[0][1]) * 12
+
+    assert min(foot(p) for p in large) > 64 * 1024 * 1024 >= max(foot(p) for p in small)
+    alone = []
+    for p in reqs:
+        e = make(*p)
+        sg.solve_batch([e])
+        alone.append(results(e))
+    budget = max(foot(p) for p in large) + 2 * max(foot(p) for p in small)
+    srv = sg.Server(hbm_budget_bytes=budget, max_requests=16, max_ncv=48)
+    try:
+        served = [make(*p) for p in reqs]
+        for e in served:
+            srv.submit(e)
+        for e in served:
+            assert srv.wait(e, timeout=300.0)
+        st = srv.stats()
+        assert st["completed"] == len(reqs) and st["failed"] == 0
+        assert st["peak_bytes"] <= budget and st["bytes_in_use"] == 0.0
+    finally:
+        srv.destroy()
+    for a, e in zip(alone, served):
+        r = results(e)
+        assert r[0] == a[0] and r[1] == a[1] and r[2] == a[2] == 1
+        assert r[3] == a[3]
+        for xa, xb in zip(a[4], r[4]):
+            assert np.array_equal(xa, xb)
