@@ -140,14 +140,14 @@ def full_size_steps(workload):
     return 0
 
 
-def cpu_baseline(csr, wl, steps_full, budget_s=20.0):
-    """Oracle (CPU restatement of the reference) on all host cores for a bounded time; eigenpairs/s extrapolated
-    by the number of Krylov steps of the full solve."""
+def cpu_baseline(csr, wl, steps_full, budget_s=20.0, nthreads=0):
+    """Oracle (CPU restatement of the reference) on all host cores (or nthreads) for a bounded time; eigenpairs/s
+    extrapolated by the number of Krylov steps of the full solve."""
     import oracle
     from slepc_gb300 import matgen
 
     oracle.build()
-    cores = os.cpu_count() or 1
+    cores = nthreads or os.cpu_count() or 1
     n = len(csr[0]) - 1
     t = time.time()
     r = oracle.solve(*csr, hermitian=wl["hermitian"], which=wl["which"], nev=wl["nev"], ncv=wl["ncv"], tol=wl["tol"],
@@ -680,6 +680,8 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(csr, wl, full_size_steps(args.workload) or steps_k[-1])
+        one = cpu_baseline(csr, wl, full_size_steps(args.workload) or steps_k[-1], budget_s=10.0, nthreads=1)
+        cpu["one_thread"] = {"value": one["value"], "cores": 1, "sample": one["sample"]}
 
     if rank == 0:
         lat_sorted = sorted(lat)

@@ -101,6 +101,7 @@ PetscErrorCode ksg_engine_init(BatchEngine &B, int device, int cap, int max_ncv,
   B.slots = max_ncv + 1;
   B.max_ld = max_ncv + 1;
   KSG_CUDA(cudaSetDevice(device));
+  KSG_CUDA(prepare_ds_nhep());
   KSG_CUDA(cudaStreamCreateWithFlags(&B.s, cudaStreamNonBlocking));
   const int sms = num_sms();
   B.grid_spmv = sms * 8;

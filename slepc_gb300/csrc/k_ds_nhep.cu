@@ -1,8 +1,8 @@
 // k_ds_nhep.cu -- projected problem of the non-symmetric Krylov-Schur iteration, solved on the device in FP64.
 //
-// One warp per projected problem (lane 0 runs the scalar recurrences, all lanes apply the transformations), so
-// the same code serves the single large solve and, later, many small solves side by side.  It follows the
-// reference's DSNHEP path:
+// One 128-thread block per projected problem (thread 0 or warp 0 runs the scalar recurrences, the block applies the
+// transformations), so the same code serves the single large solve and many small solves side by side.  It follows
+// the reference's DSNHEP path:
 //   DSSolve_NHEP_Private (src/sys/classes/ds/impls/dsutil.c:21-87): Householder reduction to Hessenberg form of the
 //     rows/columns from l on (gehrd with ILO = l+1) when the matrix holds the Krylov-Schur form, then the real
 //     Schur form by Francis double-shift QR (the algorithm of hseqr/lahqr) with standardised 2x2 blocks (lanv2);
@@ -11,7 +11,11 @@
 //   DSUpdateExtraRow_NHEP (dsnhep.c:318-340), DSVectors_NHEP_Eigen_Some (dsnhep.c:101-166) for the residual
 //     estimates of EPSKrylovConvergence (epskrylov.c:207-295), DSGetTruncateSize (dsops.c:329-344) and
 //     DSTruncate_NHEP (dsnhep.c:394-425).
-// A and Q stay in global memory (they are at most 144 x 144 and L1/L2 resident).
+// The solver is a long chain of short FP64 steps (one bulge reflector, then its application), and one warp issues
+// FP64 instructions at a fraction of the SM's rate: four warps, one per SM sub-partition, apply each transformation
+// together, and every thread computes the small reflectors itself instead of waiting for a broadcast.  A (and Q,
+// when both fit) are staged in shared memory with odd strides, so threads walking rows or columns of a
+// column-major array hit distinct banks.
 #include <float.h>
 
 #include "batch_types.h"
@@ -22,22 +26,40 @@
 namespace ksg {
 
 constexpr int NH_MAXN = 144;
+constexpr int NH_T = 128;  // threads of one solver: four warps, one per SM sub-partition (each has its own FP64 pipe)
 
-#define AH(i, j) A[(i) + (size_t)(j) * ld]
-#define QH(i, j) Q[(i) + (size_t)(j) * ld]
+constexpr int NH_PAIRS = NH_MAXN / 2 + 1;
+constexpr int NH_SMEM_MAX = 220 * 1024;  // dynamic shared memory of one solver (A, and Q when both fit)
+
+#define AH(i, j) A[(i) + (size_t)(j) * lda]
+#define QH(i, j) Q[(i) + (size_t)(j) * ldq]
 
 struct NhShared {
   double v[NH_MAXN + 4];
   double G[16];
+  double red[NH_T / 32];
   double tau, beta, cs, sn;
+  double pc[NH_PAIRS], ps[NH_PAIRS];  // Givens rotations of one round of the parallel sort
+  int pf[NH_PAIRS];
   int cmd, i0, i1, i2, i3;
   int fail;
 };
 
-KS_DEVICE int lane_id() { return threadIdx.x & 31; }
+// odd strides >= rows: consecutive columns of a column-major array start in distinct banks
+KS_DEVICE int nh_stride_a(int n) { return (n + 1) | 1; }  // A holds rows 0..n (the extra row n)
+KS_DEVICE int nh_stride_q(int n) { return n | 1; }
+__host__ __device__ inline size_t nh_smem_a(int n) { return (size_t)((n + 1) | 1) * n * sizeof(double); }
+__host__ __device__ inline size_t nh_smem_q(int n) { return (size_t)(n | 1) * n * sizeof(double); }
 
-// Householder vector of x[0..m-1] (lane 0): x becomes v with v[0] = 1; returns tau, *beta = resulting head
-__device__ double nh_house(int m, double *x, double *beta) {
+KS_DEVICE int lane_id() { return threadIdx.x & 31; }
+KS_DEVICE int nh_tid() { return threadIdx.x; }
+KS_DEVICE void nh_sync() { __syncthreads(); }
+
+// Householder vector of x[0..m-1] (one thread): x becomes v with v[0] = 1; returns tau, *beta = resulting head.
+// H = I - tau v v^T maps x to (beta, 0, ..., 0) (the convention of LAPACK's larfg).  The norm is a plain sum of
+// squares and one square root; the scaled sum (no divisions on the common path otherwise) is used only when the
+// squares leave the safe range.
+__device__ double nh_house_scaled(int m, double *x, double *beta) {
   const double alpha = x[0];
   double scale = 0.0, ssq = 1.0;
   for (int i = 1; i < m; ++i) {
@@ -64,40 +86,118 @@ __device__ double nh_house(int m, double *x, double *beta) {
   return tau;
 }
 
-// warp-parallel reflector applications (v, tau in shared memory)
-__device__ void nh_refl_left(double *A, int ld, int r0, int m, int c0, int c1, const double *v, double tau) {
-  for (int j = c0 + lane_id(); j <= c1; j += 32) {
-    double s = 0.0;
-    for (int i = 0; i < m; ++i) s = fma(v[i], AH(r0 + i, j), s);
-    s *= tau;
-    for (int i = 0; i < m; ++i) AH(r0 + i, j) -= s * v[i];
+constexpr double NH_SQ_LO = 1e-280, NH_SQ_HI = 1e280;
+
+__device__ double nh_house(int m, double *x, double *beta) {
+  const double alpha = x[0];
+  double s2 = 0.0;
+  for (int i = 1; i < m; ++i) s2 = fma(x[i], x[i], s2);
+  const double t = fma(alpha, alpha, s2);
+  if (s2 == 0.0 || t < NH_SQ_LO || t > NH_SQ_HI) return nh_house_scaled(m, x, beta);
+  const double b = -copysign(sqrt(t), alpha);
+  const double tau = (b - alpha) / b;
+  const double sc = 1.0 / (alpha - b);
+  for (int i = 1; i < m; ++i) x[i] *= sc;
+  x[0] = 1.0;
+  *beta = b;
+  return tau;
+}
+
+KS_DEVICE double warp_sum_all(double v) {
+  // butterfly: every lane ends with the same bits (each level adds the same two operands on both partners)
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// sum over the block, the same bits in every thread (warp butterflies, then the warp sums in a fixed order)
+KS_DEVICE double nh_block_sum(double v, double *red) {
+  v = warp_sum_all(v);
+  if (lane_id() == 0) red[threadIdx.x >> 5] = v;
+  nh_sync();
+  double s = red[0];
+  for (int w = 1; w < NH_T / 32; ++w) s += red[w];
+  nh_sync();
+  return s;
+}
+
+// the reflector of a long vector computed by the whole block (x in shared memory, the Hessenberg reduction);
+// every thread returns tau, sh.beta holds beta
+__device__ double nh_house_block(int m, double *x, NhShared &sh) {
+  const int tid = nh_tid();
+  double s2 = 0.0;
+  for (int i = 1 + tid; i < m; i += NH_T) s2 = fma(x[i], x[i], s2);
+  s2 = nh_block_sum(s2, sh.red);
+  const double alpha = x[0];
+  const double t = fma(alpha, alpha, s2);
+  if (s2 == 0.0 || t < NH_SQ_LO || t > NH_SQ_HI) {
+    if (tid == 0) {
+      double beta;
+      sh.tau = nh_house_scaled(m, x, &beta);
+      sh.beta = beta;
+    }
+    nh_sync();
+    return sh.tau;
+  }
+  const double b = -copysign(sqrt(t), alpha);
+  const double tau = (b - alpha) / b;
+  const double sc = 1.0 / (alpha - b);
+  for (int i = 1 + tid; i < m; i += NH_T) x[i] *= sc;
+  if (tid == 0) {
+    x[0] = 1.0;
+    sh.beta = b;
+  }
+  nh_sync();
+  return tau;
+}
+
+// block-parallel reflector applications (v, tau in shared memory); long dot products use four partial sums
+__device__ void nh_refl_left(double *A, int lda, int r0, int m, int c0, int c1, const double *v, double tau) {
+  for (int j = c0 + nh_tid(); j <= c1; j += NH_T) {
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    int i = 0;
+    for (; i + 3 < m; i += 4) {
+      s0 = fma(v[i], AH(r0 + i, j), s0);
+      s1 = fma(v[i + 1], AH(r0 + i + 1, j), s1);
+      s2 = fma(v[i + 2], AH(r0 + i + 2, j), s2);
+      s3 = fma(v[i + 3], AH(r0 + i + 3, j), s3);
+    }
+    for (; i < m; ++i) s0 = fma(v[i], AH(r0 + i, j), s0);
+    const double s = ((s0 + s1) + (s2 + s3)) * tau;
+    for (int i2 = 0; i2 < m; ++i2) AH(r0 + i2, j) -= s * v[i2];
   }
 }
-__device__ void nh_refl_right(double *A, int ld, int c0, int m, int r0, int r1, const double *v, double tau) {
-  for (int i = r0 + lane_id(); i <= r1; i += 32) {
-    double s = 0.0;
-    for (int j = 0; j < m; ++j) s = fma(AH(i, c0 + j), v[j], s);
-    s *= tau;
-    for (int j = 0; j < m; ++j) AH(i, c0 + j) -= s * v[j];
+__device__ void nh_refl_right(double *A, int lda, int c0, int m, int r0, int r1, const double *v, double tau) {
+  for (int i = r0 + nh_tid(); i <= r1; i += NH_T) {
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    int j = 0;
+    for (; j + 3 < m; j += 4) {
+      s0 = fma(AH(i, c0 + j), v[j], s0);
+      s1 = fma(AH(i, c0 + j + 1), v[j + 1], s1);
+      s2 = fma(AH(i, c0 + j + 2), v[j + 2], s2);
+      s3 = fma(AH(i, c0 + j + 3), v[j + 3], s3);
+    }
+    for (; j < m; ++j) s0 = fma(AH(i, c0 + j), v[j], s0);
+    const double s = ((s0 + s1) + (s2 + s3)) * tau;
+    for (int j2 = 0; j2 < m; ++j2) AH(i, c0 + j2) -= s * v[j2];
   }
 }
 // BLAS rot on rows (x: row p, y: row p+1, columns c0..c1) or columns (rows r0..r1)
-__device__ void nh_rot_rows(double *A, int ld, int p, int c0, int c1, double c, double s) {
-  for (int j = c0 + lane_id(); j <= c1; j += 32) {
+__device__ void nh_rot_rows(double *A, int lda, int p, int c0, int c1, double c, double s) {
+  for (int j = c0 + nh_tid(); j <= c1; j += NH_T) {
     const double x = AH(p, j), y = AH(p + 1, j);
     AH(p, j) = c * x + s * y;
     AH(p + 1, j) = c * y - s * x;
   }
 }
-__device__ void nh_rot_cols(double *A, int ld, int p, int r0, int r1, double c, double s) {
-  for (int i = r0 + lane_id(); i <= r1; i += 32) {
+__device__ void nh_rot_cols(double *A, int lda, int p, int r0, int r1, double c, double s) {
+  for (int i = r0 + nh_tid(); i <= r1; i += NH_T) {
     const double x = AH(i, p), y = AH(i, p + 1);
     AH(i, p) = c * x + s * y;
     AH(i, p + 1) = c * y - s * x;
   }
 }
 
-// 2x2 standardisation (lane 0): [a b; c d] -> G^T [a b; c d] G, G = [cs -sn; sn cs]
+// 2x2 standardisation (one thread): [a b; c d] -> G^T [a b; c d] G, G = [cs -sn; sn cs]
 __device__ void nh_std2x2(double &a, double &b, double &c, double &d, double &cs, double &sn) {
   const double eps = DBL_EPSILON;
   if (c == 0.0) { cs = 1.0; sn = 0.0; return; }
@@ -162,97 +262,126 @@ __device__ void nh_std2x2(double &a, double &b, double &c, double &d, double &cs
   }
 }
 
-// standardise the 2x2 block at (i, i+1) and propagate to T and Q (whole warp)
-__device__ void nh_std_block(double *A, double *Q, int ld, int n, int i, NhShared &sh) {
-  if (lane_id() == 0) {
+// standardise the 2x2 block at (i, i+1) and propagate to T and Q (whole block)
+__device__ void nh_std_block(double *A, int lda, double *Q, int ldq, int n, int i, NhShared &sh) {
+  if (nh_tid() == 0) {
     double a = AH(i, i), b = AH(i, i + 1), c = AH(i + 1, i), d = AH(i + 1, i + 1), cs, sn;
     nh_std2x2(a, b, c, d, cs, sn);
     AH(i, i) = a; AH(i, i + 1) = b; AH(i + 1, i) = c; AH(i + 1, i + 1) = d;
     sh.cs = cs;
     sh.sn = sn;
   }
-  __syncwarp();
+  nh_sync();
   const double cs = sh.cs, sn = sh.sn;
-  if (i + 2 < n) nh_rot_rows(A, ld, i, i + 2, n - 1, cs, sn);
-  if (i > 0) nh_rot_cols(A, ld, i, 0, i - 1, cs, sn);
-  nh_rot_cols(Q, ld, i, 0, n - 1, cs, sn);
-  __syncwarp();
+  if (i + 2 < n) nh_rot_rows(A, lda, i, i + 2, n - 1, cs, sn);
+  if (i > 0) nh_rot_cols(A, lda, i, 0, i - 1, cs, sn);
+  nh_rot_cols(Q, ldq, i, 0, n - 1, cs, sn);
+  nh_sync();
 }
 
 // Hessenberg reduction from column ilo (rows/columns before ilo already triangular), accumulated into Q
-__device__ void nh_hessenberg(double *A, double *Q, int ld, int n, int ilo, NhShared &sh) {
+__device__ void nh_hessenberg(double *A, int lda, double *Q, int ldq, int n, int ilo, NhShared &sh) {
   for (int c = ilo; c < n - 2; ++c) {
     const int m = n - c - 1;
-    if (lane_id() == 0) {
-      for (int i = 0; i < m; ++i) sh.v[i] = AH(c + 1 + i, c);
-      double beta;
-      sh.tau = nh_house(m, sh.v, &beta);
-      sh.beta = beta;
-    }
-    __syncwarp();
-    const double tau = sh.tau;
+    for (int i = nh_tid(); i < m; i += NH_T) sh.v[i] = AH(c + 1 + i, c);
+    nh_sync();
+    const double tau = nh_house_block(m, sh.v, sh);
     if (tau != 0.0) {
-      nh_refl_left(A, ld, c + 1, m, c, n - 1, sh.v, tau);
-      __syncwarp();
-      nh_refl_right(A, ld, c + 1, m, 0, n - 1, sh.v, tau);
-      nh_refl_right(Q, ld, c + 1, m, 0, n - 1, sh.v, tau);
-      __syncwarp();
-      if (lane_id() == 0) {
-        AH(c + 1, c) = sh.beta;
-        for (int i = 1; i < m; ++i) AH(c + 1 + i, c) = 0.0;
-      }
+      nh_refl_left(A, lda, c + 1, m, c + 1, n - 1, sh.v, tau);
+      nh_sync();
+      nh_refl_right(A, lda, c + 1, m, 0, n - 1, sh.v, tau);
+      nh_refl_right(Q, ldq, c + 1, m, 0, n - 1, sh.v, tau);
+      nh_sync();
+      for (int i = nh_tid(); i < m; i += NH_T) AH(c + 1 + i, c) = i ? 0.0 : sh.beta;
     }
-    __syncwarp();
+    nh_sync();
   }
 }
 
-// real Schur form of the Hessenberg matrix (rows/columns before ilo triangular); returns 0 or 1 (no convergence)
-__device__ int nh_francis(double *A, double *Q, int ld, int n, int ilo, NhShared &sh) {
+// deflation test of the double-shift QR (lahqr) for the subdiagonal entry H(l, l-1), ilo < l <= ihi
+KS_DEVICE bool nh_negligible(const double *A, int lda, int l, int ilo, int ihi, double smlnum) {
   const double eps = DBL_EPSILON;
-  const double smlnum = DBL_MIN * ((double)n / eps);
-  for (int i = ilo + 2 + lane_id(); i < n; i += 32)
+  const double hll = fabs(AH(l, l - 1));
+  if (hll <= smlnum) return true;
+  double tst = fabs(AH(l - 1, l - 1)) + fabs(AH(l, l));
+  if (tst == 0.0) {
+    if (l - 2 >= ilo) tst += fabs(AH(l - 1, l - 2));
+    if (l + 1 <= ihi) tst += fabs(AH(l + 1, l));
+  }
+  if (hll <= eps * tst) {
+    const double ab = fmax(hll, fabs(AH(l - 1, l)));
+    const double ba = fmin(hll, fabs(AH(l - 1, l)));
+    const double aa = fmax(fabs(AH(l, l)), fabs(AH(l - 1, l - 1) - AH(l, l)));
+    const double bb = fmin(fabs(AH(l, l)), fabs(AH(l - 1, l - 1) - AH(l, l)));
+    const double s = aa + ab;
+    if (ba * (ab / s) <= fmax(smlnum, eps * (bb * (aa / s)))) return true;
+  }
+  return false;
+}
+
+// reflector of (x0, x1, x2) with v = (1, v1, v2) (x2 = 0 for a 2-element reflector), computed identically by every
+// thread from the same inputs
+KS_DEVICE void nh_house3(double x0, double x1, double x2, double &tau, double &v1, double &v2, double &beta) {
+  const double s2 = fma(x2, x2, x1 * x1);
+  const double t = fma(x0, x0, s2);
+  if (s2 == 0.0 || t < NH_SQ_LO || t > NH_SQ_HI) {
+    double x[3] = {x0, x1, x2};
+    tau = nh_house_scaled(3, x, &beta);
+    v1 = x[1];
+    v2 = x[2];
+    return;
+  }
+  beta = -copysign(sqrt(t), x0);
+  tau = (beta - x0) / beta;
+  const double sc = 1.0 / (x0 - beta);
+  v1 = x1 * sc;
+  v2 = x2 * sc;
+}
+
+// Real Schur form of the Hessenberg matrix (rows/columns before ilo triangular) by the double-shift QR algorithm
+// (lahqr: deflation test, exceptional shifts at 10 and 20 iterations, bulge chase with 3-element reflectors);
+// returns 0 or 1 (no convergence).  Warp 0 runs the deflation scan (32 subdiagonals per ballot) and the shift
+// computation in lockstep, every thread computes each bulge reflector, and the block applies it.
+__device__ int nh_francis(double *A, int lda, double *Q, int ldq, int n, int ilo, NhShared &sh) {
+  const double smlnum = DBL_MIN * ((double)n / DBL_EPSILON);
+  const int tid = nh_tid();
+  for (int i = ilo + 2 + tid; i < n; i += NH_T)
     for (int j = ilo; j < i - 1; ++j) AH(i, j) = 0.0;
-  __syncwarp();
-  int ihi = n - 1, its = 0, totits = 0;
+  nh_sync();
+  int ihi = n - 1, its = 0, totits = 0;  // warp 0's copies (the same in every lane)
   const int maxtot = 40 * (n > 10 ? n : 10);
   for (;;) {
-    // lane 0 decides: cmd 0 done, 1 standardise block at i0, 2 Francis sweep on [i0, i1]
-    if (lane_id() == 0) {
-      sh.cmd = 0;
+    if (tid < 32) {
+      int cmd = 0, i0 = 0, i1 = 0, fail = 0;
+      double v0 = 0.0, v1 = 0.0, v2 = 0.0;
       while (ihi >= ilo) {
-        int l;
-        for (l = ihi; l > ilo; --l) {
-          const double hll = fabs(AH(l, l - 1));
-          if (hll <= smlnum) break;
-          double tst = fabs(AH(l - 1, l - 1)) + fabs(AH(l, l));
-          if (tst == 0.0) {
-            if (l - 2 >= ilo) tst += fabs(AH(l - 1, l - 2));
-            if (l + 1 <= ihi) tst += fabs(AH(l + 1, l));
-          }
-          if (hll <= eps * tst) {
-            const double ab = fmax(hll, fabs(AH(l - 1, l)));
-            const double ba = fmin(hll, fabs(AH(l - 1, l)));
-            const double aa = fmax(fabs(AH(l, l)), fabs(AH(l - 1, l - 1) - AH(l, l)));
-            const double bb = fmin(fabs(AH(l, l)), fabs(AH(l - 1, l - 1) - AH(l, l)));
-            const double s = aa + ab;
-            if (ba * (ab / s) <= fmax(smlnum, eps * (bb * (aa / s)))) break;
+        // the largest l in (ilo, ihi] whose subdiagonal is negligible, else ilo
+        int l = ilo;
+        for (int top = ihi; top > ilo; top -= 32) {
+          const int cand = top - tid;
+          const bool ok = cand > ilo && nh_negligible(A, lda, cand, ilo, ihi, smlnum);
+          const unsigned bal = __ballot_sync(0xffffffffu, ok);
+          if (bal) {
+            l = top - (__ffs(bal) - 1);
+            break;
           }
         }
-        if (l > ilo) AH(l, l - 1) = 0.0;
+        if (l > ilo && tid == 0) AH(l, l - 1) = 0.0;
+        __syncwarp();
         if (l >= ihi) {
           ihi -= 1;
           its = 0;
           continue;
         }
         if (l == ihi - 1) {
-          sh.cmd = 1;
-          sh.i0 = l;
+          cmd = 1;
+          i0 = l;
           ihi -= 2;
           its = 0;
           break;
         }
         if (++totits > maxtot) {
-          sh.fail = 1;
+          fail = 1;
           break;
         }
         its++;
@@ -298,57 +427,98 @@ __device__ int nh_francis(double *A, double *Q, int ld, int n, int ilo, NhShared
         double h21s = AH(m + 1, m);
         double sc = fabs(AH(m, m) - rt2r) + fabs(rt2i) + fabs(h21s);
         h21s /= sc;
-        double v0 = h21s * AH(m, m + 1) + (AH(m, m) - rt1r) * ((AH(m, m) - rt2r) / sc) - rt1i * (rt2i / sc);
-        double v1 = h21s * (AH(m, m) + AH(m + 1, m + 1) - rt1r - rt2r);
-        double v2 = h21s * AH(m + 2, m + 1);
-        sc = fabs(v0) + fabs(v1) + fabs(v2);
-        sh.v[0] = v0 / sc;
-        sh.v[1] = v1 / sc;
-        sh.v[2] = v2 / sc;
-        sh.cmd = 2;
-        sh.i0 = m;
-        sh.i1 = ihi;
+        const double w0 = h21s * AH(m, m + 1) + (AH(m, m) - rt1r) * ((AH(m, m) - rt2r) / sc) - rt1i * (rt2i / sc);
+        const double w1 = h21s * (AH(m, m) + AH(m + 1, m + 1) - rt1r - rt2r);
+        const double w2 = h21s * AH(m + 2, m + 1);
+        sc = fabs(w0) + fabs(w1) + fabs(w2);
+        v0 = w0 / sc;
+        v1 = w1 / sc;
+        v2 = w2 / sc;
+        cmd = 2;
+        i0 = m;
+        i1 = ihi;
         break;
       }
+      if (tid == 0) {
+        sh.cmd = cmd;
+        sh.i0 = i0;
+        sh.i1 = i1;
+        sh.v[0] = v0;
+        sh.v[1] = v1;
+        sh.v[2] = v2;
+        if (fail) sh.fail = 1;
+      }
     }
-    __syncwarp();
+    nh_sync();
     const int cmd = sh.cmd;
     if (cmd == 0) break;
     if (cmd == 1) {
-      nh_std_block(A, Q, ld, n, sh.i0, sh);
+      nh_std_block(A, lda, Q, ldq, n, sh.i0, sh);
       continue;
     }
     // bulge chase over [m, hi]
     const int m = sh.i0, hi = sh.i1;
+    double x0 = sh.v[0], x1 = sh.v[1], x2 = sh.v[2];
     for (int k = m; k <= hi - 1; ++k) {
       const int nr = (3 < hi - k + 1) ? 3 : hi - k + 1;
-      if (lane_id() == 0) {
-        if (k > m)
-          for (int i = 0; i < nr; ++i) sh.v[i] = AH(k + i, k - 1);
-        double beta;
-        sh.tau = nh_house(nr, sh.v, &beta);
-        if (k > m) {
-          AH(k, k - 1) = beta;
-          AH(k + 1, k - 1) = 0.0;
-          if (k < hi - 1) AH(k + 2, k - 1) = 0.0;
+      if (k > m) {
+        x0 = AH(k, k - 1);
+        x1 = AH(k + 1, k - 1);
+        x2 = nr == 3 ? AH(k + 2, k - 1) : 0.0;
+      }
+      double tau, v1, v2, beta;
+      nh_house3(x0, x1, nr == 3 ? x2 : 0.0, tau, v1, v2, beta);
+      if (tau == 0.0) continue;  // x is already (x0, 0, 0): nothing changes
+      const double w0 = tau, w1 = tau * v1, w2 = tau * v2;
+      // rows k..k+nr-1 over columns k..n-1
+      for (int j = k + tid; j < n; j += NH_T) {
+        const double a0 = AH(k, j), a1 = AH(k + 1, j);
+        if (nr == 3) {
+          const double a2 = AH(k + 2, j);
+          const double d = fma(v2, a2, fma(v1, a1, a0));
+          AH(k, j) = fma(-d, w0, a0);
+          AH(k + 1, j) = fma(-d, w1, a1);
+          AH(k + 2, j) = fma(-d, w2, a2);
+        } else {
+          const double d = fma(v1, a1, a0);
+          AH(k, j) = fma(-d, w0, a0);
+          AH(k + 1, j) = fma(-d, w1, a1);
         }
       }
-      __syncwarp();
-      const double tau = sh.tau;
-      if (tau != 0.0) {
-        nh_refl_left(A, ld, k, nr, k, n - 1, sh.v, tau);
-        __syncwarp();
-        const int r1 = (k + 3 < hi) ? k + 3 : hi;
-        nh_refl_right(A, ld, k, nr, 0, r1, sh.v, tau);
-        nh_refl_right(Q, ld, k, nr, 0, n - 1, sh.v, tau);
+      nh_sync();
+      // column k-1 of the bulge (read by every thread above) becomes (beta, 0, 0)
+      if (tid == 0 && k > m) {
+        AH(k, k - 1) = beta;
+        AH(k + 1, k - 1) = 0.0;
+        if (nr == 3) AH(k + 2, k - 1) = 0.0;
       }
-      __syncwarp();
+      // columns k..k+nr-1 over rows 0..r1 of the matrix and all rows of the Schur vectors
+      const int r1 = (k + 3 < hi) ? k + 3 : hi;
+      for (int t = tid; t <= r1 + n; t += NH_T) {
+        double *row;
+        int ldm;
+        if (t <= r1) { row = A + t; ldm = lda; }
+        else { row = Q + (t - r1 - 1); ldm = ldq; }
+        const double a0 = row[(size_t)k * ldm], a1 = row[(size_t)(k + 1) * ldm];
+        if (nr == 3) {
+          const double a2 = row[(size_t)(k + 2) * ldm];
+          const double d = fma(a2, v2, fma(a1, v1, a0));
+          row[(size_t)k * ldm] = fma(-d, w0, a0);
+          row[(size_t)(k + 1) * ldm] = fma(-d, w1, a1);
+          row[(size_t)(k + 2) * ldm] = fma(-d, w2, a2);
+        } else {
+          const double d = fma(a1, v1, a0);
+          row[(size_t)k * ldm] = fma(-d, w0, a0);
+          row[(size_t)(k + 1) * ldm] = fma(-d, w1, a1);
+        }
+      }
+      nh_sync();
     }
   }
   return sh.fail;
 }
 
-// small Sylvester solve T11 X - X T22 = B (Kronecker system, complete pivoting), lane 0
+// small Sylvester solve T11 X - X T22 = B (Kronecker system, complete pivoting), one thread
 __device__ void nh_sylv(int n1, int n2, const double *D, double *X, double smin) {
   const int m = n1 * n2;
   double K[4][4], rhs[4];
@@ -397,11 +567,11 @@ __device__ void nh_sylv(int n1, int n2, const double *D, double *X, double smin)
 }
 
 // swap adjacent blocks of sizes n1 (at j1) and n2 (at j1+n1); returns 1 if rejected
-__device__ int nh_swap(double *A, double *Q, int ld, int n, int j1, int n1, int n2, NhShared &sh) {
+__device__ int nh_swap(double *A, int lda, double *Q, int ldq, int n, int j1, int n1, int n2, NhShared &sh) {
   const int m = n1 + n2;
   if (n1 == 1 && n2 == 1) {
     const int j2 = j1 + 1;
-    if (lane_id() == 0) {
+    if (nh_tid() == 0) {
       const double t11 = AH(j1, j1), t22 = AH(j2, j2);
       const double f = AH(j1, j2), g = t22 - t11;
       double c, s;
@@ -417,20 +587,20 @@ __device__ int nh_swap(double *A, double *Q, int ld, int n, int j1, int n1, int 
       sh.G[0] = t11;
       sh.G[1] = t22;
     }
-    __syncwarp();
+    nh_sync();
     const double c = sh.cs, s = sh.sn;
-    if (j2 + 1 < n) nh_rot_rows(A, ld, j1, j2 + 1, n - 1, c, s);
-    if (j1 > 0) nh_rot_cols(A, ld, j1, 0, j1 - 1, c, s);
-    nh_rot_cols(Q, ld, j1, 0, n - 1, c, s);
-    __syncwarp();
-    if (lane_id() == 0) {
+    if (j2 + 1 < n) nh_rot_rows(A, lda, j1, j2 + 1, n - 1, c, s);
+    if (j1 > 0) nh_rot_cols(A, lda, j1, 0, j1 - 1, c, s);
+    nh_rot_cols(Q, ldq, j1, 0, n - 1, c, s);
+    nh_sync();
+    if (nh_tid() == 0) {
       AH(j1, j1) = sh.G[1];
       AH(j2, j2) = sh.G[0];
     }
-    __syncwarp();
+    nh_sync();
     return 0;
   }
-  if (lane_id() == 0) {
+  if (nh_tid() == 0) {
     const double eps = DBL_EPSILON;
     double D[16], dnorm = 0.0;
     for (int j = 0; j < m; ++j)
@@ -487,11 +657,11 @@ __device__ int nh_swap(double *A, double *Q, int ld, int n, int j1, int n1, int 
       for (int j = 0; j < n2; ++j) resid = fmax(resid, fabs(D2[i + j * 4]));
     sh.cmd = resid > thresh;
   }
-  __syncwarp();
+  nh_sync();
   if (sh.cmd) return 1;
   const double *G = sh.G;
   // left: rows j1..j1+m-1 over columns j1..n-1
-  for (int j = j1 + lane_id(); j < n; j += 32) {
+  for (int j = j1 + nh_tid(); j < n; j += NH_T) {
     double t[4];
     for (int i = 0; i < m; ++i) {
       double s = 0.0;
@@ -500,9 +670,9 @@ __device__ int nh_swap(double *A, double *Q, int ld, int n, int j1, int n1, int 
     }
     for (int i = 0; i < m; ++i) AH(j1 + i, j) = t[i];
   }
-  __syncwarp();
+  nh_sync();
   // right: columns j1..j1+m-1 over rows 0..j1+m-1; Q over all rows
-  for (int i = lane_id(); i < j1 + m; i += 32) {
+  for (int i = nh_tid(); i < j1 + m; i += NH_T) {
     double t[4];
     for (int j = 0; j < m; ++j) {
       double s = 0.0;
@@ -511,7 +681,7 @@ __device__ int nh_swap(double *A, double *Q, int ld, int n, int j1, int n1, int 
     }
     for (int j = 0; j < m; ++j) AH(i, j1 + j) = t[j];
   }
-  for (int i = lane_id(); i < n; i += 32) {
+  for (int i = nh_tid(); i < n; i += NH_T) {
     double t[4];
     for (int j = 0; j < m; ++j) {
       double s = 0.0;
@@ -520,37 +690,37 @@ __device__ int nh_swap(double *A, double *Q, int ld, int n, int j1, int n1, int 
     }
     for (int j = 0; j < m; ++j) QH(i, j1 + j) = t[j];
   }
-  __syncwarp();
-  if (lane_id() == 0)
+  nh_sync();
+  if (nh_tid() == 0)
     for (int i = n2; i < m; ++i)
       for (int j = 0; j < n2; ++j) AH(j1 + i, j1 + j) = 0.0;
-  __syncwarp();
-  if (n2 == 2) nh_std_block(A, Q, ld, n, j1, sh);
+  nh_sync();
+  if (n2 == 2) nh_std_block(A, lda, Q, ldq, n, j1, sh);
   else {
-    if (lane_id() == 0) AH(j1 + 1, j1) = 0.0;
-    __syncwarp();
+    if (nh_tid() == 0) AH(j1 + 1, j1) = 0.0;
+    nh_sync();
   }
-  if (n1 == 2) nh_std_block(A, Q, ld, n, j1 + n2, sh);
+  if (n1 == 2) nh_std_block(A, lda, Q, ldq, n, j1 + n2, sh);
   return 0;
 }
 
 // move the block at ifst up to ilst (ifst > ilst); 0 or 1 (rejected swap)
-__device__ int nh_move(double *A, double *Q, int ld, int n, int ifst, int ilst, NhShared &sh) {
+__device__ int nh_move(double *A, int lda, double *Q, int ldq, int n, int ifst, int ilst, NhShared &sh) {
   if (ifst > 0 && AH(ifst, ifst - 1) != 0.0) ifst--;
   int nbf = (ifst < n - 1 && AH(ifst + 1, ifst) != 0.0) ? 2 : 1;
   if (ilst > 0 && AH(ilst, ilst - 1) != 0.0) ilst--;
   int here = ifst;
   while (here > ilst) {
     const int nbnext = (here >= 2 && AH(here - 1, here - 2) != 0.0) ? 2 : 1;
-    if (nh_swap(A, Q, ld, n, here - nbnext, nbnext, nbf, sh)) return 1;
-    __syncwarp();
+    if (nh_swap(A, lda, Q, ldq, n, here - nbnext, nbnext, nbf, sh)) return 1;
+    nh_sync();
     if (nbf == 2 && AH(here - nbnext + 1, here - nbnext) == 0.0) nbf = 1;
     here -= nbnext;
   }
   return 0;
 }
 
-__device__ void nh_eigs(const double *A, int ld, int n, int from, double *wr, double *wi) {
+__device__ void nh_eigs(const double *A, int lda, int n, int from, double *wr, double *wi) {
   for (int j = from; j < n; ++j) {
     wr[j] = AH(j, j);
     if (j < n - 1 && AH(j + 1, j) != 0.0) {
@@ -563,7 +733,7 @@ __device__ void nh_eigs(const double *A, int ld, int n, int from, double *wr, do
 }
 
 // right eigenvector of the quasi-triangular T for the block starting at k (single thread, trevc conventions)
-__device__ int nh_eigvec(const double *A, int ld, int n, int k, double tnorm, double *xr, double *xi) {
+__device__ int nh_eigvec(const double *A, int lda, int n, int k, double tnorm, double *xr, double *xi) {
   const double eps = DBL_EPSILON;
   const double smin = fmax(eps * tnorm, DBL_MIN / eps);
   for (int i = 0; i < n; ++i) { xr[i] = 0.0; xi[i] = 0.0; }
@@ -637,179 +807,294 @@ __device__ int nh_eigvec(const double *A, int ld, int n, int k, double tnorm, do
   return 1;
 }
 
-KS_DEVICE void ds_nhep_body(const DSArgs &a) {
+// ordering of two eigenvalues by the criterion: > 0 when (r2, i2) goes before (r1, i1) (SlepcSCCompare, which
+// values as in EPSWhich: 1 largest magnitude, 2 smallest magnitude, 3 largest real, 4 smallest real, 5 largest
+// imaginary, 6 smallest imaginary)
+KS_DEVICE int nh_cmp(int which, double r1, double i1, double r2, double i2) {
+  double av, bv;
+  switch (which) {
+    case 1: av = hypot(r1, i1); bv = hypot(r2, i2); return av < bv ? 1 : (av > bv ? -1 : 0);
+    case 2: av = hypot(r1, i1); bv = hypot(r2, i2); return av > bv ? 1 : (av < bv ? -1 : 0);
+    case 3: return r1 < r2 ? 1 : (r1 > r2 ? -1 : 0);
+    case 4: return r1 > r2 ? 1 : (r1 < r2 ? -1 : 0);
+    case 5: av = fabs(i1); bv = fabs(i2); return av < bv ? 1 : (av > bv ? -1 : 0);
+    case 6: av = fabs(i1); bv = fabs(i2); return av > bv ? 1 : (av < bv ? -1 : 0);
+    default: return 0;
+  }
+}
+
+// Sort of a real Schur form with 1x1 blocks only (rows l..n-1) by odd-even transposition: in each round the
+// out-of-order pairs (j, j+1) of one parity are exchanged by the 1x1 swap of the direct swapping method (a Givens
+// rotation from T(j, j+1) and T(j+1, j+1) - T(j, j), trexc/laexc with n1 = n2 = 1).  Pairs of one round are
+// disjoint, so their rotations commute: all row rotations are applied, then all column rotations (T and Q), then
+// the diagonal exchanges.  The final order is the stable order of the criterion, as the selection sort's.
+__device__ void nh_sort_real(double *A, int lda, double *Q, int ldq, int n, int l, int which, double *wr,
+                             NhShared &sh) {
+  const int tid = nh_tid();
+  int quiet = 0;
+  for (int round = 0; round < 2 * (n - l) + 2 && quiet < 2; ++round) {
+    const int j0 = l + (round & 1);
+    const int np = (n - j0) / 2;  // pairs (j0 + 2p, j0 + 2p + 1)
+    int any = 0;
+    for (int p = tid; p < np; p += NH_T) {
+      const int j = j0 + 2 * p;
+      const int sw = nh_cmp(which, wr[j], 0.0, wr[j + 1], 0.0) > 0;
+      sh.pf[p] = sw;
+      if (sw) {
+        any = 1;
+        const double t11 = AH(j, j), t22 = AH(j + 1, j + 1);
+        const double f = AH(j, j + 1), g = t22 - t11;
+        double c, sn;
+        if (g == 0.0) { c = 1.0; sn = 0.0; }
+        else if (f == 0.0) { c = 0.0; sn = copysign(1.0, g); }
+        else {
+          const double d = hypot(f, g);
+          c = fabs(f) / d;
+          sn = g / copysign(d, f);
+        }
+        sh.pc[p] = c;
+        sh.ps[p] = sn;
+      }
+    }
+    if (!__syncthreads_or(any)) {
+      quiet++;
+      continue;
+    }
+    quiet = 0;
+    // rows j, j+1 over columns j+2..n-1
+    for (int col = tid; col < n; col += NH_T)
+      for (int p = 0; p < np; ++p) {
+        const int j = j0 + 2 * p;
+        if (j + 2 > col) break;
+        if (!sh.pf[p]) continue;
+        const double c = sh.pc[p], sn = sh.ps[p];
+        const double x = AH(j, col), y = AH(j + 1, col);
+        AH(j, col) = c * x + sn * y;
+        AH(j + 1, col) = c * y - sn * x;
+      }
+    nh_sync();
+    // columns j, j+1 over rows 0..j-1, and the Schur vectors
+    for (int r = tid; r < n; r += NH_T)
+      for (int p = 0; p < np; ++p) {
+        if (!sh.pf[p]) continue;
+        const int j = j0 + 2 * p;
+        const double c = sh.pc[p], sn = sh.ps[p];
+        if (r < j) {
+          const double x = AH(r, j), y = AH(r, j + 1);
+          AH(r, j) = c * x + sn * y;
+          AH(r, j + 1) = c * y - sn * x;
+        }
+        const double x = QH(r, j), y = QH(r, j + 1);
+        QH(r, j) = c * x + sn * y;
+        QH(r, j + 1) = c * y - sn * x;
+      }
+    nh_sync();
+    for (int p = tid; p < np; p += NH_T)
+      if (sh.pf[p]) {
+        const int j = j0 + 2 * p;
+        const double t = AH(j, j);
+        AH(j, j) = AH(j + 1, j + 1);
+        AH(j + 1, j + 1) = t;
+        const double w = wr[j];
+        wr[j] = wr[j + 1];
+        wr[j + 1] = w;
+      }
+    nh_sync();
+  }
+}
+
+KS_DEVICE void ds_nhep_body(const DSArgs &a, double *smem, int smem_bytes) {
   __shared__ NhShared sh;
   __shared__ double wr[NH_MAXN], wi[NH_MAXN], errs[NH_MAXN];
-  const int lane = lane_id();
+  const int tid = nh_tid();
   const int n = a.st ? a.st->m : a.n;
   const int ld = a.ld, l = a.l, flags = a.flags;
-  double *A = a.H, *Q = a.Q;
-  if (lane == 0) {
+  // stage A (rows 0..n) and, when it fits too, Q in shared memory
+  const bool sa = smem && nh_smem_a(n) <= (size_t)smem_bytes;
+  const bool sq = sa && nh_smem_a(n) + nh_smem_q(n) <= (size_t)smem_bytes;
+  double *A = sa ? smem : a.H;
+  const int lda = sa ? nh_stride_a(n) : ld;
+  double *Q = sq ? smem + (size_t)lda * n : a.Q;
+  const int ldq = sq ? nh_stride_q(n) : ld;
+  if (sa)
+    for (int i = tid; i < (n + 1) * n; i += NH_T) AH(i % (n + 1), i / (n + 1)) = a.H[i % (n + 1) + (size_t)(i / (n + 1)) * ld];
+  if (sq && !(flags & DS_DO_SOLVE))
+    for (int i = tid; i < n * n; i += NH_T) QH(i % n, i / n) = a.Q[i % n + (size_t)(i / n) * ld];
+  if (tid == 0) {
     sh.fail = 0;
     sh.cmd = 0;
   }
-  __syncwarp();
+  nh_sync();
   if (flags & DS_DO_SOLVE) {
-    for (int i = lane; i < n * n; i += 32) QH(i % n, i / n) = ((i % n) == (i / n)) ? 1.0 : 0.0;
-    __syncwarp();
+    for (int i = tid; i < n * n; i += NH_T) QH(i % n, i / n) = ((i % n) == (i / n)) ? 1.0 : 0.0;
+    nh_sync();
     if (n > 1) {
-      if (a.raw) nh_hessenberg(A, Q, ld, n, l, sh);
-      nh_francis(A, Q, ld, n, l, sh);
+      if (a.raw) nh_hessenberg(A, lda, Q, ldq, n, l, sh);
+      nh_francis(A, lda, Q, ldq, n, l, sh);
     }
-    __syncwarp();
+    nh_sync();
   }
-  if (lane == 0) nh_eigs(A, ld, n, 0, wr, wi);
-  __syncwarp();
+  if (tid == 0) nh_eigs(A, lda, n, 0, wr, wi);
+  nh_sync();
   if ((flags & DS_DO_SORT) && !sh.fail) {
-    // selection sort (DSSort_NHEP_Total), lane 0 chooses, the warp moves blocks
-    for (int i = l; i < n - 1; ++i) {
-      if (lane == 0) {
-        double re = wr[i], im = wi[i];
-        int pos = 0;
-        int j = (im != 0.0) ? i + 2 : i + 1;
-        for (; j < n; ++j) {
-          int res;
-          {
-            double av, bv;
-            switch (a.which) {
-              case 1: av = hypot(re, im); bv = hypot(wr[j], wi[j]); res = av < bv ? 1 : (av > bv ? -1 : 0); break;
-              case 2: av = hypot(re, im); bv = hypot(wr[j], wi[j]); res = av > bv ? 1 : (av < bv ? -1 : 0); break;
-              case 3: res = re < wr[j] ? 1 : (re > wr[j] ? -1 : 0); break;
-              case 4: res = re > wr[j] ? 1 : (re < wr[j] ? -1 : 0); break;
-              case 5: av = fabs(im); bv = fabs(wi[j]); res = av < bv ? 1 : (av > bv ? -1 : 0); break;
-              case 6: av = fabs(im); bv = fabs(wi[j]); res = av > bv ? 1 : (av < bv ? -1 : 0); break;
-              default: res = 0;
-            }
+    int cplx = 0;
+    for (int i = l + tid; i + 1 < n; i += NH_T) cplx |= AH(i + 1, i) != 0.0;
+    if (!__syncthreads_or(cplx)) {
+      nh_sort_real(A, lda, Q, ldq, n, l, a.which, wr, sh);
+    } else {
+      // selection sort (DSSort_NHEP_Total), thread 0 chooses, the block moves blocks
+      for (int i = l; i < n - 1; ++i) {
+        if (tid == 0) {
+          double re = wr[i], im = wi[i];
+          int pos = 0;
+          int j = (im != 0.0) ? i + 2 : i + 1;
+          for (; j < n; ++j) {
+            if (nh_cmp(a.which, re, im, wr[j], wi[j]) > 0) { re = wr[j]; im = wi[j]; pos = j; }
+            if (wi[j] != 0.0) j++;
           }
-          if (res > 0) { re = wr[j]; im = wi[j]; pos = j; }
-          if (wi[j] != 0.0) j++;
+          sh.i2 = pos;
         }
-        sh.i2 = pos;
-      }
-      __syncwarp();
-      const int pos = sh.i2;
-      if (pos) {
-        if (nh_move(A, Q, ld, n, pos, i, sh)) {
-          if (lane == 0) sh.fail = 2;
-          __syncwarp();
-          break;
+        nh_sync();
+        const int pos = sh.i2;
+        if (pos) {
+          if (nh_move(A, lda, Q, ldq, n, pos, i, sh)) {
+            if (tid == 0) sh.fail = 2;
+            nh_sync();
+            break;
+          }
+          nh_sync();
+          if (tid == 0) nh_eigs(A, lda, n, i, wr, wi);
+          nh_sync();
         }
-        __syncwarp();
-        if (lane == 0) nh_eigs(A, ld, n, i, wr, wi);
-        __syncwarp();
+        if (wi[i] != 0.0) i++;
       }
-      if (wi[i] != 0.0) i++;
     }
   }
-  __syncwarp();
+  nh_sync();
   if (flags & DS_DO_EXTRAROW) {
     // A(n, :) = Q^T A(n, :)
     double *x = sh.v;
-    for (int i = lane; i < n; i += 32) x[i] = AH(n, i);
-    __syncwarp();
-    for (int i = lane; i < n; i += 32) {
-      double s = 0.0;
-      for (int j = 0; j < n; ++j) s = fma(QH(j, i), x[j], s);
-      errs[i] = s;
+    for (int i = tid; i < n; i += NH_T) x[i] = AH(n, i);
+    nh_sync();
+    for (int i = tid; i < n; i += NH_T) {
+      double s0 = 0.0, s1 = 0.0;
+      int j = 0;
+      for (; j + 1 < n; j += 2) {
+        s0 = fma(QH(j, i), x[j], s0);
+        s1 = fma(QH(j + 1, i), x[j + 1], s1);
+      }
+      if (j < n) s0 = fma(QH(j, i), x[j], s0);
+      errs[i] = s0 + s1;
     }
-    __syncwarp();
-    for (int i = lane; i < n; i += 32) AH(n, i) = errs[i];
-    __syncwarp();
+    nh_sync();
+    for (int i = tid; i < n; i += NH_T) AH(n, i) = errs[i];
+    nh_sync();
   }
-  for (int i = lane; i < n; i += 32) {
+  for (int i = tid; i < n; i += NH_T) {
     a.eigr[i] = wr[i];
     if (a.eigi) a.eigi[i] = wi[i];
   }
   if (!(flags & DS_DO_CONTROL)) {
-    if (lane == 0 && a.ctl) a.ctl->ds_error = sh.fail;
-    return;
-  }
-  // residual estimates for k = l..n-1, one eigenvector per lane (DSVectors_NHEP_Eigen_Some)
-  const double beta = a.st ? a.st->beta_out : 0.0;
-  double tnorm = 0.0;
-  for (int j = 0; j < n; ++j)
-    for (int i = 0; i <= j + 1 && i < n; ++i) tnorm = fmax(tnorm, fabs(AH(i, j)));
-  double xr[NH_MAXN], xi[NH_MAXN];
-  for (int k = l + lane; k < n; k += 32) {
-    errs[k] = -1.0;
-    if (k > 0 && AH(k, k - 1) != 0.0) continue;  // second row of a 2x2 block: handled by the first
-    const int cplx = nh_eigvec(A, ld, n, k, tnorm, xr, xi);
-    double yl_r = 0.0, yl_i = 0.0, nr2 = 0.0, ni2 = 0.0;
-    for (int i = 0; i < n; ++i) {
-      double sr = 0.0, si = 0.0;
+    if (tid == 0 && a.ctl) a.ctl->ds_error = sh.fail;
+  } else {
+    // residual estimates for k = l..n-1, one eigenvector per thread (DSVectors_NHEP_Eigen_Some): the Ritz vector
+    // is Q x with x the eigenvector of the quasi-triangular T, so its norm is ||x|| (Q is orthogonal) and only
+    // its last entry Q(n-1, :) x is formed
+    const double beta = a.st ? a.st->beta_out : 0.0;
+    double tnorm = 0.0;
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i <= j + 1 && i < n; ++i) tnorm = fmax(tnorm, fabs(AH(i, j)));
+    double xr[NH_MAXN], xi[NH_MAXN];
+    for (int k = l + tid; k < n; k += NH_T) {
+      errs[k] = -1.0;
+      if (k > 0 && AH(k, k - 1) != 0.0) continue;  // second row of a 2x2 block: handled by the first
+      const int cplx = nh_eigvec(A, lda, n, k, tnorm, xr, xi);
+      double yl_r = 0.0, yl_i = 0.0, nr2 = 0.0, ni2 = 0.0;
       for (int j = 0; j <= k + cplx; ++j) {
-        sr = fma(QH(i, j), xr[j], sr);
-        if (cplx) si = fma(QH(i, j), xi[j], si);
+        yl_r = fma(QH(n - 1, j), xr[j], yl_r);
+        nr2 = fma(xr[j], xr[j], nr2);
+        if (cplx) {
+          yl_i = fma(QH(n - 1, j), xi[j], yl_i);
+          ni2 = fma(xi[j], xi[j], ni2);
+        }
       }
-      nr2 += sr * sr;
-      ni2 += si * si;
-      if (i == n - 1) { yl_r = sr; yl_i = si; }
+      const double nrm = sqrt(nr2 + ni2);
+      const double rn = (cplx ? hypot(yl_r, yl_i) : fabs(yl_r)) / nrm * beta;
+      const double w = hypot(wr[k], wi[k]);
+      errs[k] = (w != 0.0) ? rn / w : DBL_MAX;
+      if (cplx) errs[k + 1] = errs[k];
     }
-    const double nrm = sqrt(nr2 + ni2);
-    const double rn = (cplx ? hypot(yl_r, yl_i) : fabs(yl_r)) / nrm * beta;
-    const double w = hypot(wr[k], wi[k]);
-    errs[k] = (w != 0.0) ? rn / w : DBL_MAX;
-    if (cplx) errs[k + 1] = errs[k];
+    nh_sync();
+    if (tid == 0) {
+      int kk;
+      for (kk = l; kk < n; ++kk) {
+        a.errest[kk] = errs[kk];
+        if (errs[kk] >= a.tol) break;
+        if (wi[kk] != 0.0 && kk + 1 < n) {
+          a.errest[kk + 1] = errs[kk];
+          kk++;
+        }
+      }
+      KSControl *ctl = a.ctl;
+      int reason = 0;
+      if (kk >= a.nev) reason = 1;
+      else if (a.its >= a.max_it) reason = -1;
+      const int breakdown = a.st ? a.st->breakdown : 0;
+      int lkeep;
+      if (reason != 0 || breakdown || kk == n) lkeep = 0;
+      else {
+        lkeep = (int)((n - kk) * a.keep);
+        if (lkeep < 1) lkeep = 1;
+        // DSGetTruncateSize_Default: do not split a 2x2 block
+        if (AH(kk + lkeep, kk + lkeep - 1) != 0.0) {
+          if (kk + lkeep < n - 1) lkeep++;
+          else lkeep--;
+        }
+      }
+      if (!a.lock && lkeep > 0) { lkeep += kk; kk = 0; }
+      if (reason == 0 && !(breakdown || kk == n)) {
+        // DSTruncate_NHEP: move the extra row to row kk+lkeep
+        const int nn = kk + lkeep;
+        for (int i = l; i < nn; ++i) AH(nn, i) = AH(n, i);
+        for (int i = l; i < n; ++i) AH(n, i) = 0.0;
+      }
+      ctl->nconv = kk;
+      ctl->l = lkeep;
+      ctl->reason = reason;
+      ctl->nv = n;
+      ctl->breakdown = breakdown;
+      ctl->need_start = (reason == 0 && (breakdown || kk == n) && kk < a.nev) ? 1 : 0;
+      ctl->ds_error = sh.fail;
+      ctl->beta = beta;
+    }
   }
-  __syncwarp();
-  if (lane == 0) {
-    int kk;
-    for (kk = l; kk < n; ++kk) {
-      a.errest[kk] = errs[kk];
-      if (errs[kk] >= a.tol) break;
-      if (wi[kk] != 0.0 && kk + 1 < n) {
-        a.errest[kk + 1] = errs[kk];
-        kk++;
-      }
-    }
-    KSControl *ctl = a.ctl;
-    int reason = 0;
-    if (kk >= a.nev) reason = 1;
-    else if (a.its >= a.max_it) reason = -1;
-    const int breakdown = a.st ? a.st->breakdown : 0;
-    int lkeep;
-    if (reason != 0 || breakdown || kk == n) lkeep = 0;
-    else {
-      lkeep = (int)((n - kk) * a.keep);
-      if (lkeep < 1) lkeep = 1;
-      // DSGetTruncateSize_Default: do not split a 2x2 block
-      if (AH(kk + lkeep, kk + lkeep - 1) != 0.0) {
-        if (kk + lkeep < n - 1) lkeep++;
-        else lkeep--;
-      }
-    }
-    if (!a.lock && lkeep > 0) { lkeep += kk; kk = 0; }
-    if (reason == 0 && !(breakdown || kk == n)) {
-      // DSTruncate_NHEP: move the extra row to row kk+lkeep
-      const int nn = kk + lkeep;
-      for (int i = l; i < nn; ++i) AH(nn, i) = AH(n, i);
-      for (int i = l; i < n; ++i) AH(n, i) = 0.0;
-    }
-    ctl->nconv = kk;
-    ctl->l = lkeep;
-    ctl->reason = reason;
-    ctl->nv = n;
-    ctl->breakdown = breakdown;
-    ctl->need_start = (reason == 0 && (breakdown || kk == n) && kk < a.nev) ? 1 : 0;
-    ctl->ds_error = sh.fail;
-    ctl->beta = beta;
-  }
+  nh_sync();
+  if (sa)
+    for (int i = tid; i < (n + 1) * n; i += NH_T) a.H[i % (n + 1) + (size_t)(i / (n + 1)) * ld] = AH(i % (n + 1), i / (n + 1));
+  if (sq)
+    for (int i = tid; i < n * n; i += NH_T) a.Q[i % n + (size_t)(i / n) * ld] = QH(i % n, i / n);
+  nh_sync();
 }
 
-__global__ void __launch_bounds__(32) k_ds_nhep(DSArgs a) { ds_nhep_body(a); }
+__global__ void __launch_bounds__(NH_T) k_ds_nhep(DSArgs a, int smem_bytes) {
+  extern __shared__ double nh_dyn[];
+  ds_nhep_body(a, nh_dyn, smem_bytes);
+}
 
-// one warp per non-symmetric instance of a batch (grid-stride over the live list)
-__global__ void __launch_bounds__(32) k_batch_ds_nhep(const BatchInst *I, const int *list, const BatchHdr *h) {
+// one block per non-symmetric instance of a batch (grid-stride over the live list)
+__global__ void __launch_bounds__(NH_T) k_batch_ds_nhep(const BatchInst *I, const int *list, const BatchHdr *h,
+                                                         int smem_bytes) {
+  extern __shared__ double nh_dyn[];
   for (int v = blockIdx.x; v < h->n_inst; v += gridDim.x) {
     const BatchInst &p = I[list[v]];
     if (p.phase != BP_ITER || p.hermitian) continue;
-    __syncwarp();
-    ds_nhep_body(batch_ds_args(p));
+    nh_sync();
+    ds_nhep_body(batch_ds_args(p), nh_dyn, smem_bytes);
   }
 }
 
 // eigenvectors of the leading n x n quasi-triangular block, normalised (DSVectors_NHEP_Eigen_All with back = "A")
-__global__ void __launch_bounds__(32) k_nhep_vectors(const double *A, int ld, int n, double *X) {
+__global__ void __launch_bounds__(32) k_nhep_vectors(const double *A, int lda, int n, double *X) {
   const int lane = lane_id();
   double tnorm = 0.0;
   for (int j = 0; j < n; ++j)
@@ -817,27 +1102,54 @@ __global__ void __launch_bounds__(32) k_nhep_vectors(const double *A, int ld, in
   double xr[NH_MAXN], xi[NH_MAXN];
   for (int k = lane; k < n; k += 32) {
     if (k > 0 && AH(k, k - 1) != 0.0) continue;
-    const int cplx = nh_eigvec(A, ld, n, k, tnorm, xr, xi);
+    const int cplx = nh_eigvec(A, lda, n, k, tnorm, xr, xi);
     double s = 0.0;
     for (int i = 0; i < n; ++i) s += xr[i] * xr[i] + xi[i] * xi[i];
     const double inv = 1.0 / sqrt(s);
     for (int i = 0; i < n; ++i) {
-      X[i + (size_t)k * ld] = xr[i] * inv;
-      if (cplx) X[i + (size_t)(k + 1) * ld] = xi[i] * inv;
+      X[i + (size_t)k * lda] = xr[i] * inv;
+      if (cplx) X[i + (size_t)(k + 1) * lda] = xi[i] * inv;
     }
   }
 }
 
+// dynamic shared memory for problems of size up to n_max: A, and Q when both fit
+static int nh_smem_bytes(int n_max) {
+  size_t b = nh_smem_a(n_max);
+  if (b + nh_smem_q(n_max) <= (size_t)NH_SMEM_MAX) b += nh_smem_q(n_max);
+  return b <= (size_t)NH_SMEM_MAX ? (int)b : 0;
+}
+
+template <typename K>
+static cudaError_t nh_allow_smem(K kernel) {
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, NH_SMEM_MAX);
+}
+
+// kernel attributes set once per process, before any launch is captured into a graph
+cudaError_t prepare_ds_nhep() {
+  static cudaError_t attr = [] {
+    cudaError_t e = nh_allow_smem(k_ds_nhep);
+    return e != cudaSuccess ? e : nh_allow_smem(k_batch_ds_nhep);
+  }();
+  return attr;
+}
+
 cudaError_t launch_ds_nhep(const DSArgs &a, int n_max, cudaStream_t s) {
   if (n_max > NH_MAXN) return cudaErrorInvalidValue;
-  k_ds_nhep<<<1, 32, 0, s>>>(a);
+  const cudaError_t attr = prepare_ds_nhep();
+  if (attr != cudaSuccess) return attr;
+  const int bytes = nh_smem_bytes(n_max);
+  k_ds_nhep<<<1, NH_T, bytes, s>>>(a, bytes);
   return cudaGetLastError();
 }
 
 cudaError_t launch_batch_ds_nhep(const BatchInst *I, const int *list, const BatchHdr *h, int grid, int max_ld,
                                  cudaStream_t s) {
   if (max_ld > NH_MAXN) return cudaErrorInvalidValue;
-  k_batch_ds_nhep<<<grid, 32, 0, s>>>(I, list, h);
+  const cudaError_t attr = prepare_ds_nhep();
+  if (attr != cudaSuccess) return attr;
+  const int bytes = nh_smem_bytes(max_ld);
+  k_batch_ds_nhep<<<grid, NH_T, bytes, s>>>(I, list, h, bytes);
   return cudaGetLastError();
 }
 

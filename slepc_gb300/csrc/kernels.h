@@ -86,6 +86,7 @@ cudaError_t launch_scale(double *x, int n, double alpha, cudaStream_t s);
 cudaError_t launch_negate(void *x, long long count, int as_float, cudaStream_t s);
 cudaError_t launch_ds_hep(const DSArgs &a, int n_max, cudaStream_t s);
 cudaError_t launch_ds_nhep(const DSArgs &a, int n_max, cudaStream_t s);
+cudaError_t prepare_ds_nhep();  // shared-memory attributes of the NHEP solver kernels (call outside graph capture)
 size_t ds_fast_scratch_doubles(int ld);
 DSFArgs ds_fast_layout(double *scratch, int ld);
 int ds_fast_launches();
