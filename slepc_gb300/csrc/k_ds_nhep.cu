@@ -321,19 +321,26 @@ KS_DEVICE bool nh_negligible(const double *A, int lda, int l, int ilo, int ihi, 
 
 // reflector of (x0, x1, x2) with v = (1, v1, v2) (x2 = 0 for a 2-element reflector), computed identically by every
 // thread from the same inputs
+// With r = 1/sqrt(t), t = x0^2 + x1^2 + x2^2: beta = -sign(x0) t r, tau = (beta - x0)/beta = 1 + |x0| r, and the
+// vector scale 1/(x0 - beta) = sign(x0)/(|x0| + t r): one reciprocal square root and one reciprocal.  The range
+// tests read the bit pattern of t (non-negative doubles order as integers).
 KS_DEVICE void nh_house3(double x0, double x1, double x2, double &tau, double &v1, double &v2, double &beta) {
   const double s2 = fma(x2, x2, x1 * x1);
   const double t = fma(x0, x0, s2);
-  if (s2 == 0.0 || t < NH_SQ_LO || t > NH_SQ_HI) {
+  const long long tb = __double_as_longlong(t);
+  if (__double_as_longlong(s2) == 0 || tb < __double_as_longlong(NH_SQ_LO) || tb > __double_as_longlong(NH_SQ_HI)) {
     double x[3] = {x0, x1, x2};
     tau = nh_house_scaled(3, x, &beta);
     v1 = x[1];
     v2 = x[2];
     return;
   }
-  beta = -copysign(sqrt(t), x0);
-  tau = (beta - x0) / beta;
-  const double sc = 1.0 / (x0 - beta);
+  const double r = rsqrt(t);
+  const double root = t * r;
+  const double ax0 = fabs(x0);
+  beta = copysign(root, -x0);
+  tau = fma(ax0, r, 1.0);
+  const double sc = copysign(__drcp_rn(ax0 + root), x0);
   v1 = x1 * sc;
   v2 = x2 * sc;
 }
@@ -741,7 +748,9 @@ __device__ int nh_eigvec(const double *A, int lda, int n, int k, double tnorm, d
   if (!cplx) {
     const double lam = AH(k, k);
     xr[k] = 1.0;
+    double mx = 1.0;
     for (int i = k - 1; i >= 0; --i) {
+      bool twice = false;  // a 2x2 block set xr[i-1] and xr[i]; i now indexes its first row
       if (i > 0 && AH(i, i - 1) != 0.0) {
         double r0 = 0.0, r1 = 0.0;
         for (int j = i + 1; j <= k; ++j) { r0 -= AH(i - 1, j) * xr[j]; r1 -= AH(i, j) * xr[j]; }
@@ -751,6 +760,7 @@ __device__ int nh_eigvec(const double *A, int lda, int n, int k, double tnorm, d
         xr[i - 1] = (r0 * d - b * r1) / det;
         xr[i] = (a * r1 - c * r0) / det;
         i--;
+        twice = true;
       } else {
         double s = 0.0;
         for (int j = i + 1; j <= k; ++j) s -= AH(i, j) * xr[j];
@@ -758,10 +768,14 @@ __device__ int nh_eigvec(const double *A, int lda, int n, int k, double tnorm, d
         if (fabs(den) < smin) den = smin;
         xr[i] = s / den;
       }
-      double mx = 0.0;
-      for (int j = i; j <= k; ++j) mx = fmax(mx, fabs(xr[j]));
-      if (mx > 1e150)
+      // max |xr[i..k]|, kept as a running maximum (entries below i are still zero)
+      mx = fmax(mx, fabs(xr[i]));
+      if (i + 1 <= k && twice) mx = fmax(mx, fabs(xr[i + 1]));
+      if (mx > 1e150) {
         for (int j = 0; j <= k; ++j) xr[j] /= mx;
+        mx = 0.0;
+        for (int j = i; j <= k; ++j) mx = fmax(mx, fabs(xr[j]));
+      }
     }
     return 0;
   }
@@ -770,7 +784,9 @@ __device__ int nh_eigvec(const double *A, int lda, int n, int k, double tnorm, d
   const double wim = sqrt(fabs(AH(k, ki))) * sqrt(fabs(AH(ki, k)));
   if (fabs(AH(k, ki)) >= fabs(AH(ki, k))) { xr[k] = 1.0; xi[ki] = wim / AH(k, ki); }
   else { xr[k] = -wim / AH(ki, k); xi[ki] = 1.0; }
+  double mx = fmax(fabs(xr[k]) + fabs(xi[k]), fabs(xr[ki]) + fabs(xi[ki]));
   for (int i = k - 1; i >= 0; --i) {
+    bool twice = false;
     if (i > 0 && AH(i, i - 1) != 0.0) {
       double r0r = 0.0, r0i = 0.0, r1r = 0.0, r1i = 0.0;
       for (int j = i + 1; j <= ki; ++j) {
@@ -790,6 +806,7 @@ __device__ int nh_eigvec(const double *A, int lda, int n, int k, double tnorm, d
       xr[i] = (nr * detr + ni * deti) / dd;
       xi[i] = (ni * detr - nr * deti) / dd;
       i--;
+      twice = true;
     } else {
       double sr = 0.0, si = 0.0;
       for (int j = i + 1; j <= ki; ++j) { sr -= AH(i, j) * xr[j]; si -= AH(i, j) * xi[j]; }
@@ -799,10 +816,14 @@ __device__ int nh_eigvec(const double *A, int lda, int n, int k, double tnorm, d
       xr[i] = (sr * denr + si * deni) / dd;
       xi[i] = (si * denr - sr * deni) / dd;
     }
-    double mx = 0.0;
-    for (int j = i; j <= ki; ++j) mx = fmax(mx, fabs(xr[j]) + fabs(xi[j]));
-    if (mx > 1e150)
+    // max |xr[j]| + |xi[j]| over j = i..ki, kept as a running maximum
+    mx = fmax(mx, fabs(xr[i]) + fabs(xi[i]));
+    if (twice) mx = fmax(mx, fabs(xr[i + 1]) + fabs(xi[i + 1]));
+    if (mx > 1e150) {
       for (int j = 0; j <= ki; ++j) { xr[j] /= mx; xi[j] /= mx; }
+      mx = 0.0;
+      for (int j = i; j <= ki; ++j) mx = fmax(mx, fabs(xr[j]) + fabs(xi[j]));
+    }
   }
   return 1;
 }
@@ -873,21 +894,22 @@ __device__ void nh_sort_real(double *A, int lda, double *Q, int ldq, int n, int 
         AH(j + 1, col) = c * y - sn * x;
       }
     nh_sync();
-    // columns j, j+1 over rows 0..j-1, and the Schur vectors
-    for (int r = tid; r < n; r += NH_T)
+    // columns j, j+1 over rows 0..j-1 of T (tasks 0..n-1) and over all rows of the Schur vectors (tasks n..2n-1)
+    for (int t = tid; t < 2 * n; t += NH_T) {
+      const bool isq = t >= n;
+      const int r = isq ? t - n : t;
+      double *row = isq ? Q + r : A + r;
+      const int ldm = isq ? ldq : lda;
       for (int p = 0; p < np; ++p) {
         if (!sh.pf[p]) continue;
         const int j = j0 + 2 * p;
+        if (!isq && r >= j) continue;
         const double c = sh.pc[p], sn = sh.ps[p];
-        if (r < j) {
-          const double x = AH(r, j), y = AH(r, j + 1);
-          AH(r, j) = c * x + sn * y;
-          AH(r, j + 1) = c * y - sn * x;
-        }
-        const double x = QH(r, j), y = QH(r, j + 1);
-        QH(r, j) = c * x + sn * y;
-        QH(r, j + 1) = c * y - sn * x;
+        const double x = row[(size_t)j * ldm], y = row[(size_t)(j + 1) * ldm];
+        row[(size_t)j * ldm] = c * x + sn * y;
+        row[(size_t)(j + 1) * ldm] = c * y - sn * x;
       }
+    }
     nh_sync();
     for (int p = tid; p < np; p += NH_T)
       if (sh.pf[p]) {
@@ -1001,9 +1023,15 @@ KS_DEVICE void ds_nhep_body(const DSArgs &a, double *smem, int smem_bytes) {
     // is Q x with x the eigenvector of the quasi-triangular T, so its norm is ||x|| (Q is orthogonal) and only
     // its last entry Q(n-1, :) x is formed
     const double beta = a.st ? a.st->beta_out : 0.0;
+    // max |T(i, j)| over the upper Hessenberg part: columns split over the block, then a max over the warps
     double tnorm = 0.0;
-    for (int j = 0; j < n; ++j)
+    for (int j = tid; j < n; j += NH_T)
       for (int i = 0; i <= j + 1 && i < n; ++i) tnorm = fmax(tnorm, fabs(AH(i, j)));
+    for (int o = 16; o > 0; o >>= 1) tnorm = fmax(tnorm, __shfl_xor_sync(0xffffffffu, tnorm, o));
+    if (lane_id() == 0) sh.red[tid >> 5] = tnorm;
+    nh_sync();
+    tnorm = sh.red[0];
+    for (int w = 1; w < NH_T / 32; ++w) tnorm = fmax(tnorm, sh.red[w]);
     double xr[NH_MAXN], xi[NH_MAXN];
     for (int k = l + tid; k < n; k += NH_T) {
       errs[k] = -1.0;
