@@ -47,10 +47,14 @@ typedef int MPI_Comm; /* one process per GPU: communicators carry no information
 #define PETSC_ERR_ARG_SIZ 60
 #define PETSC_ERR_ARG_WRONG 62
 #define PETSC_ERR_ARG_OUTOFRANGE 63
+#define PETSC_ERR_FILE_OPEN 65
+#define PETSC_ERR_FILE_READ 66
+#define PETSC_ERR_FILE_WRITE 67
 #define PETSC_ERR_ARG_WRONGSTATE 73
 #define PETSC_ERR_ARG_INCOMP 75
 #define PETSC_ERR_LIB 76
 #define PETSC_ERR_PLIB 77
+#define PETSC_ERR_FILE_UNEXPECTED 79
 #define PETSC_ERR_CONV_FAILED 82
 #define PETSC_ERR_ARG_NULL 85
 #define PETSC_ERR_USER_INPUT 91
@@ -61,6 +65,10 @@ typedef enum { NORM_1 = 0, NORM_2 = 1, NORM_FROBENIUS = 2, NORM_INFINITY = 3, NO
 
 typedef struct _p_Mat *Mat;
 typedef struct _p_Vec *Vec;
+typedef struct _p_PetscViewer *PetscViewer;
+typedef enum { FILE_MODE_UNDEFINED = -1, FILE_MODE_READ = 0, FILE_MODE_WRITE, FILE_MODE_APPEND } PetscFileMode;
+#define MAT_FILE_CLASSID 1211216
+#define VEC_FILE_CLASSID 1211214
 
 /* SlepcInitialize/PetscInitialize: a no-op shim (selects the current CUDA device lazily). */
 PetscErrorCode PetscInitialize(int *argc, char ***argv, const char file[], const char help[]);
@@ -84,6 +92,26 @@ PetscErrorCode MatMult(Mat A, Vec x, Vec y);
 PetscErrorCode MatNorm(Mat A, NormType type, PetscReal *nrm);
 PetscErrorCode MatCreateVecs(Mat A, Vec *right, Vec *left);
 PetscErrorCode MatDestroy(Mat *A);
+/* CSR arrays of an AIJ matrix, read-only (shift must be 0; the arrays stay valid until the Mat is destroyed). */
+PetscErrorCode MatGetRowIJ(Mat A, PetscInt shift, PetscBool symmetric, PetscBool inodecompressed, PetscInt *n,
+                           const PetscInt *ia[], const PetscInt *ja[], PetscBool *done);
+PetscErrorCode MatRestoreRowIJ(Mat A, PetscInt shift, PetscBool symmetric, PetscBool inodecompressed, PetscInt *n,
+                               const PetscInt *ia[], const PetscInt *ja[], PetscBool *done);
+PetscErrorCode MatSeqAIJGetArrayRead(Mat A, const PetscScalar *array[]);
+PetscErrorCode MatSeqAIJRestoreArrayRead(Mat A, const PetscScalar *array[]);
+
+/* --- binary files (petscviewer.h, MatLoad/MatView/VecLoad/VecView): PETSc's big-endian binary format, so the
+ * reference's data files (share/slepc/datafiles/matrices/NAME.petsc) load unchanged.  MatCreate gives an empty AIJ
+ * matrix that MatLoad fills and then owns. --- */
+PetscErrorCode PetscViewerBinaryOpen(MPI_Comm comm, const char name[], PetscFileMode mode, PetscViewer *viewer);
+PetscErrorCode PetscViewerDestroy(PetscViewer *viewer);
+PetscErrorCode MatCreate(MPI_Comm comm, Mat *A);
+PetscErrorCode MatSetType(Mat A, const char *type);
+PetscErrorCode MatSetFromOptions(Mat A);
+PetscErrorCode MatLoad(Mat A, PetscViewer viewer);
+PetscErrorCode MatView(Mat A, PetscViewer viewer);
+PetscErrorCode VecLoad(Vec x, PetscViewer viewer);
+PetscErrorCode VecView(Vec x, PetscViewer viewer);
 
 /* --- Vec (petscvec.h) --- */
 PetscErrorCode VecCreateSeq(MPI_Comm comm, PetscInt n, Vec *v);

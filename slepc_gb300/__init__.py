@@ -144,6 +144,50 @@ class Mat:
     def createAIJ(cls, csr):
         return cls(*csr)
 
+    @classmethod
+    def load(cls, path):
+        """MatLoad from a PETSc binary file (PetscViewerBinaryOpen + MatCreate + MatLoad); the library owns the
+        arrays, and rowptr/colidx/vals are copies of them."""
+        lib = load()
+        viewer, h = ctypes.c_void_p(), ctypes.c_void_p()
+        _check(lib.PetscViewerBinaryOpen(0, os.fsencode(path), 0, ctypes.byref(viewer)), "PetscViewerBinaryOpen")
+        try:
+            _check(lib.MatCreate(0, ctypes.byref(h)), "MatCreate")
+            rc = lib.MatLoad(h, viewer)
+            if rc:
+                lib.MatDestroy(ctypes.byref(h))
+                _check(rc, "MatLoad")
+        finally:
+            lib.PetscViewerDestroy(ctypes.byref(viewer))
+        m = ctypes.c_int()
+        ia, ja = ctypes.POINTER(ctypes.c_int)(), ctypes.POINTER(ctypes.c_int)()
+        aa = ctypes.POINTER(ctypes.c_double)()
+        done = ctypes.c_int()
+        _check(lib.MatGetRowIJ(h, 0, 0, 0, ctypes.byref(m), ctypes.byref(ia), ctypes.byref(ja), ctypes.byref(done)),
+               "MatGetRowIJ")
+        _check(lib.MatSeqAIJGetArrayRead(h, ctypes.byref(aa)), "MatSeqAIJGetArrayRead")
+        obj = cls.__new__(cls)
+        obj.handle = h
+        obj.m = m.value
+        rows, cols = ctypes.c_int(), ctypes.c_int()
+        _check(lib.MatGetSize(h, ctypes.byref(rows), ctypes.byref(cols)), "MatGetSize")
+        obj.n = cols.value
+        obj.rowptr = np.ctypeslib.as_array(ia, (obj.m + 1,)).copy()
+        nnz = int(obj.rowptr[-1])
+        obj.colidx = np.ctypeslib.as_array(ja, (nnz,)).copy() if nnz else np.zeros(0, np.int32)
+        obj.vals = np.ctypeslib.as_array(aa, (nnz,)).copy() if nnz else np.zeros(0)
+        return obj
+
+    def save(self, path):
+        """MatView into a PETSc binary file (the format MatLoad and PETSc read)."""
+        lib = load()
+        viewer = ctypes.c_void_p()
+        _check(lib.PetscViewerBinaryOpen(0, os.fsencode(path), 1, ctypes.byref(viewer)), "PetscViewerBinaryOpen")
+        try:
+            _check(lib.MatView(self.handle, viewer), "MatView")
+        finally:
+            _check(lib.PetscViewerDestroy(ctypes.byref(viewer)), "PetscViewerDestroy")
+
     def mult(self, x):
         y = np.zeros(self.m)
         vx, vy = Vec(x), Vec(y)

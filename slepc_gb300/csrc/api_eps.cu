@@ -306,6 +306,7 @@ extern "C" PetscErrorCode MatNorm(Mat A, NormType type, PetscReal *nrm) {
 
 extern "C" PetscErrorCode MatMult(Mat A, Vec x, Vec y) {
   KSG_CHECK(A && x && y, PETSC_ERR_ARG_NULL, "Null argument");
+  KSG_CHECK(!A->empty, PETSC_ERR_ARG_WRONGSTATE, "The Mat holds no data (MatCreate without MatLoad)");
   KSG_CHECK(x->n == A->n && y->n == A->m, PETSC_ERR_ARG_SIZ, "Nonconforming sizes");
   if (A->dense) return ksg_set_error(PETSC_ERR_SUP, "MatMult on a dense Mat is not provided");
   KSG_TRY(ksg_mat_upload(A));
@@ -564,6 +565,7 @@ extern "C" PetscErrorCode EPSGetType(EPS eps, EPSType *type) {
 extern "C" PetscErrorCode EPSSetOperators(EPS eps, Mat A, Mat B) {
   KSG_CHECK(eps && A, PETSC_ERR_ARG_NULL, "Null argument");
   KSG_CHECK(!B, PETSC_ERR_SUP, "Generalised problems (B != NULL) are not provided");
+  KSG_CHECK(!A->empty, PETSC_ERR_ARG_WRONGSTATE, "The Mat holds no data (MatCreate without MatLoad)");
   KSG_CHECK(A->m == A->n, PETSC_ERR_ARG_WRONG, "A must be square");
   A->refs++;
   if (eps->A) MatDestroy(&eps->A);

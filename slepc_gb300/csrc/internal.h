@@ -59,10 +59,13 @@ struct DBuf {
 struct _p_Mat {
   int m = 0, n = 0;
   int dense = 0;
-  // AIJ (caller-owned arrays)
+  int empty = 0;  // created by MatCreate, not yet filled by MatLoad
+  // AIJ (caller-owned arrays, or the own_* arrays of a loaded matrix)
   const PetscInt *ai = nullptr, *aj = nullptr;
   const PetscScalar *aa = nullptr;
   long long nnz = 0;
+  std::vector<PetscInt> own_i, own_j;
+  std::vector<double> own_a;
   // dense
   std::vector<double> dbuf;
   double *data = nullptr;

@@ -1,9 +1,13 @@
 """Regenerate reference_outputs.json from the reference's expected-output files (run in the build container only;
 the GPU machine uses the committed JSON).  Only the printed eigenvalues/norms of the Krylov-Schur-path tests are
-extracted; each entry records the file it came from and the options of that test."""
+extracted; each entry records the file it came from and the options of that test.  The real matrix those tests
+read from a PETSc binary file (share/slepc/datafiles/matrices/rdb200.petsc) is converted to CSR arrays in
+rdb200.npz by an independent big-endian reader."""
 import json
 import os
 import re
+
+import numpy as np
 
 REF = os.environ.get("SLEPC_REFERENCE", "/root/reference")
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_outputs.json")
@@ -55,6 +59,21 @@ def main():
     g["ds_test1_1"] = {"source": "src/sys/classes/ds/tests/output/test1_1.out", "n": 10, "which": "LM",
                        "eigenvalues_abs_imag": [[float(a), float(b)] for a, b in pairs],
                        "rnorm_3rd": float(rn.group(1)), "norm_1st": float(nv.group(1))}
+    # rdb200 (200 x 200, non-symmetric), EPS_NHEP defaults, -eps_nev 4 (src/eps/tutorials/ex4.c TEST 1)
+    txt = read("src/eps/tutorials/output/ex4_1.out")
+    line = [l for l in txt.splitlines() if re.search(r"\d\.\d{5}", l)][-1]
+    its = int(re.search(r"Number of iterations of the method: (\d+)", txt).group(1))
+    g["ex4_1"] = {"source": "src/eps/tutorials/output/ex4_1.out", "matrix": "rdb200.npz", "nev": 4, "tol": 1e-8,
+                  "which": "LM", "iterations": its, "eigenvalues": floats(line)}
+    raw = open(os.path.join(REF, "share/slepc/datafiles/matrices/rdb200.petsc"), "rb").read()
+    classid, m, n, nz = np.frombuffer(raw[:16], dtype=">i4")
+    assert classid == 1211216 and len(raw) == 16 + 4 * m + 12 * nz
+    lens = np.frombuffer(raw[16:16 + 4 * m], dtype=">i4").astype(np.int32)
+    cols = np.frombuffer(raw[16 + 4 * m:16 + 4 * m + 4 * nz], dtype=">i4").astype(np.int32)
+    vals = np.frombuffer(raw[16 + 4 * m + 4 * nz:], dtype=">f8").astype(np.float64)
+    rowptr = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
+    np.savez(os.path.join(os.path.dirname(OUT), "rdb200.npz"), rowptr=rowptr, colidx=cols, vals=vals,
+             shape=np.array([m, n], dtype=np.int32))
     with open(OUT, "w") as f:
         json.dump(g, f, indent=1)
     print("wrote", OUT)

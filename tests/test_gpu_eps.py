@@ -116,6 +116,30 @@ def test_brusselator_golden_on_gpu(lib, orc):
         assert res["errors"][i] < 1e-7
 
 
+def test_rdb200_from_petsc_file_on_gpu(lib, orc, tmp_path):
+    """The reference's real non-symmetric matrix, written in PETSc's binary format and read back by MatLoad, solved
+    as ex4 does (EPS_NHEP, largest magnitude, nev 4, tol 1e-8): the digits of ex4_1.out; then at tol 1e-10 against
+    the oracle and a dense solve."""
+    g = G["ex4_1"]
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "rdb200.npz"))
+    path = str(tmp_path / "rdb200.petsc")
+    sg.Mat(d["rowptr"], d["colidx"], d["vals"]).save(path)
+    A = sg.Mat.load(path)
+    csr = (A.rowptr, A.colidx, A.vals)
+    v0 = matgen.start_vector(200, 1)
+    res = run(csr, hermitian=False, which=g["which"], nev=g["nev"], tol=g["tol"], v0=v0)
+    assert res["reason"] == 1
+    assert [round(v, 5) for v in res["eigr"][:4]] == g["eigenvalues"]
+    res = run(csr, hermitian=False, which=g["which"], nev=g["nev"], tol=1e-10, v0=v0)
+    ref = orc.solve(*csr, hermitian=False, which=g["which"], nev=g["nev"], tol=1e-10, v0=v0)
+    assert res["reason"] == 1 and ref.reason == 1
+    dense = np.linalg.eigvals(matgen.csr_to_dense(*csr))
+    for i in range(4):
+        assert abs(res["eigr"][i] - ref.eigr[i]) <= 1e-10 * abs(ref.eigr[i])
+        assert np.min(np.abs(dense - res["eigr"][i])) <= 1e-10 * abs(res["eigr"][i])
+    check_residuals(csr, res, 1e-10)
+
+
 def test_convdiff_nhep_parity(lib, orc):
     N, Pe = 40, 10.0
     csr = matgen.convection_diffusion_2d(N, Pe)
