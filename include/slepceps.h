@@ -48,7 +48,13 @@ PetscErrorCode EPSSetOperators(EPS eps, Mat A, Mat B);
 PetscErrorCode EPSGetOperators(EPS eps, Mat *A, Mat *B);
 PetscErrorCode EPSSetProblemType(EPS eps, EPSProblemType type);
 PetscErrorCode EPSGetProblemType(EPS eps, EPSProblemType *type);
+/* extraction (epsopts.c:1090-1130): EPS_RITZ, or EPS_HARMONIC for eigenvalues near the target (krylovschur.c:238-240,
+ * 270-319: the Krylov decomposition is translated for the target before each projected solve and recovered before
+ * the restart); the target serves EPS_TARGET_MAGNITUDE / EPS_TARGET_REAL (epsopts.c:560-600) */
 PetscErrorCode EPSSetExtraction(EPS eps, EPSExtraction extr);
+PetscErrorCode EPSGetExtraction(EPS eps, EPSExtraction *extr);
+PetscErrorCode EPSSetTarget(EPS eps, PetscScalar target);
+PetscErrorCode EPSGetTarget(EPS eps, PetscScalar *target);
 PetscErrorCode EPSSetDimensions(EPS eps, PetscInt nev, PetscInt ncv, PetscInt mpd);     /* epsopts.c:392-417 */
 PetscErrorCode EPSGetDimensions(EPS eps, PetscInt *nev, PetscInt *ncv, PetscInt *mpd);
 PetscErrorCode EPSSetTolerances(EPS eps, PetscReal tol, PetscInt maxits);               /* epsopts.c:300-323 */

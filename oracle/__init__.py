@@ -19,7 +19,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(LIB_DIR, "libksoracle.so")
 
-WHICH = {"LM": 1, "SM": 2, "LR": 3, "SR": 4, "LI": 5, "SI": 6}
+WHICH = {"LM": 1, "SM": 2, "LR": 3, "SR": 4, "LI": 5, "SI": 6, "TM": 7, "TR": 8}
 INFO_LEN = 16
 _lib = None
 
@@ -43,7 +43,7 @@ def load():
         lib = ctypes.CDLL(LIB_PATH)
         P = ctypes.c_void_p
         i, d, ull = ctypes.c_int, ctypes.c_double, ctypes.c_ulonglong
-        lib.ksor_solve.argtypes = [i, P, P, P, i, i, i, i, i, d, i, d, i, i, P, ull, d, P, i, P, P, P, P]
+        lib.ksor_solve.argtypes = [i, P, P, P, i, i, i, i, i, d, i, d, i, i, P, ull, d, P, i, P, P, P, P, i, d]
         lib.ksor_solve.restype = i
         lib.ksor_spmv.argtypes = [i, P, P, P, P, P, i]
         lib.ksor_spmv.restype = None
@@ -81,7 +81,8 @@ class Result:
 
 
 def solve(rowptr, colidx, vals, *, hermitian=True, which="LM", nev=1, ncv=0, mpd=0, tol=1e-8, max_it=0,
-          keep=0.5, lock=True, v0=None, nthreads=1, seed=0x5EED, time_budget=0.0, vectors=True) -> Result:
+          keep=0.5, lock=True, v0=None, nthreads=1, seed=0x5EED, time_budget=0.0, vectors=True, harmonic=False,
+          target=0.0) -> Result:
     lib = load()
     n = len(rowptr) - 1
     rowptr = np.ascontiguousarray(rowptr, dtype=np.int32)
@@ -99,7 +100,7 @@ def solve(rowptr, colidx, vals, *, hermitian=True, which="LM", nev=1, ncv=0, mpd
     err = lib.ksor_solve(n, _ptr(rowptr), _ptr(colidx), _ptr(vals), int(bool(hermitian)), WHICH[which], int(nev),
                          int(ncv), int(mpd), float(tol), int(max_it), float(keep), int(bool(lock)), int(nthreads),
                          _ptr(v0a), int(seed), float(time_budget), _ptr(info), int(cap), _ptr(eigr), _ptr(eigi),
-                         _ptr(errest), _ptr(X))
+                         _ptr(errest), _ptr(X), int(bool(harmonic)), float(target))
     return Result(info, eigr, eigi, errest, X, err)
 
 

@@ -64,9 +64,12 @@ static double urand_pm1(unsigned long long *s) {
 /* ------------------------------------------------------------------------------------------------------------
  * Sorting criteria (slepcsc.c:152-245).  Returns -1 if a goes first, 1 if b goes first, 0 if tied.
  * ------------------------------------------------------------------------------------------------------------ */
-static int sc_compare(int which, double ar, double ai, double br, double bi) {
+static int sc_compare(int which, double target, double ar, double ai, double br, double bi) {
   double a, b;
   switch (which) {
+    /* SlepcCompareTargetMagnitude / SlepcCompareTargetReal (slepcsc.c:240-267), real scalars */
+    case KSOR_TARGET_MAGNITUDE: a = hypot(ar - target, ai); b = hypot(br - target, bi); return a > b ? 1 : (a < b ? -1 : 0);
+    case KSOR_TARGET_REAL: a = fabs(ar - target); b = fabs(br - target); return a > b ? 1 : (a < b ? -1 : 0);
     case KSOR_LARGEST_MAGNITUDE: a = hypot(ar, ai); b = hypot(br, bi); return a < b ? 1 : (a > b ? -1 : 0);
     case KSOR_SMALLEST_MAGNITUDE: a = hypot(ar, ai); b = hypot(br, bi); return a > b ? 1 : (a < b ? -1 : 0);
     case KSOR_LARGEST_REAL: a = ar; b = br; return a < b ? 1 : (a > b ? -1 : 0);
@@ -211,15 +214,15 @@ static int tridiag_ql(int n, double *d, double *e, double *Q, int ld, int nq) {
 }
 
 /* Insertion sort of real eigenvalues on [l, t) (dspriv.c:226-245) */
-static void sort_real_perm(int which, int l, int t, const double *eig, int *perm) {
+static void sort_real_perm(int which, double target, int l, int t, const double *eig, int *perm) {
   for (int i = l + 1; i < t; i++) {
     double re = eig[perm[i]];
     int j = i - 1;
-    int res = sc_compare(which, re, 0.0, eig[perm[j]], 0.0);
+    int res = sc_compare(which, target, re, 0.0, eig[perm[j]], 0.0);
     while (res < 0 && j >= l) {
       int tmp = perm[j]; perm[j] = perm[j + 1]; perm[j + 1] = tmp;
       j--;
-      if (j >= l) res = sc_compare(which, re, 0.0, eig[perm[j]], 0.0);
+      if (j >= l) res = sc_compare(which, target, re, 0.0, eig[perm[j]], 0.0);
     }
   }
 }
@@ -276,10 +279,10 @@ static int ds_hep_solve(ds_t *ds, double *wr, double *wi) {
 }
 
 /* DSSort_HEP (dshep.c:323-347) */
-static void ds_hep_sort(ds_t *ds, int which, double *wr) {
+static void ds_hep_sort(ds_t *ds, int which, double target, double *wr) {
   int n = ds->n, l = ds->l;
   for (int i = 0; i < n; i++) ds->perm[i] = i;
-  sort_real_perm(which, l, ds->t, ds->d, ds->perm);
+  sort_real_perm(which, target, l, ds->t, ds->d, ds->perm);
   for (int i = l; i < n; i++) wr[i] = ds->d[ds->perm[i]];
   permute_columns(l, n, n, ds->Q, ds->ld, ds->perm);
   for (int i = l; i < n; i++) ds->d[i] = wr[i];
@@ -753,7 +756,7 @@ static int ds_nhep_solve(ds_t *ds, double *wr, double *wi) {
 }
 
 /* DSSort_NHEP_Total (dsutil.c:93-171): selection sort with block moves */
-static int ds_nhep_sort(ds_t *ds, int which, double *wr, double *wi) {
+static int ds_nhep_sort(ds_t *ds, int which, double target, double *wr, double *wi) {
   int n = ds->n, ld = ds->ld;
   for (int i = ds->l; i < n - 1; i++) {
     double re = wr[i], im = wi[i];
@@ -761,7 +764,7 @@ static int ds_nhep_sort(ds_t *ds, int which, double *wr, double *wi) {
     int j = i + 1;
     if (im != 0.0) j = i + 2;
     for (; j < n; j++) {
-      if (sc_compare(which, re, im, wr[j], wi[j]) > 0) { re = wr[j]; im = wi[j]; pos = j; }
+      if (sc_compare(which, target, re, im, wr[j], wi[j]) > 0) { re = wr[j]; im = wi[j]; pos = j; }
       if (wi[j] != 0.0) j++;
     }
     if (pos) {
@@ -1107,6 +1110,67 @@ typedef struct {
   int n; const int *rp, *ci; const double *va;
 } csr_t;
 
+/* DSTranslateHarmonic_NHEP, translation (dsnhep.c:466-507): g = (A - tau I)^T \ (beta e_n), A(:, n-1) += beta g,
+ * returns gamma = sqrt(1 + g'g).  The reference factors A - tau I (getrf) and solves with its transpose (getrs "C");
+ * here the transpose is factored with partial pivoting, which solves the same system. */
+static int harmonic_translate(ds_t *ds, double tau, double beta, double *g, double *gamma) {
+  int n = ds->n, ld = ds->ld;
+  double *B = (double *)malloc(sizeof(double) * (size_t)n * n);
+  if (!B) return 55;
+  for (int j = 0; j < n; j++)
+    for (int i = 0; i < n; i++) B[i + (size_t)j * n] = ds->A[IDX(j, i, ld)] - (i == j ? tau : 0.0);
+  for (int i = 0; i < n; i++) g[i] = 0.0;
+  g[n - 1] = beta;
+  int err = 0;
+  for (int c = 0; c < n; c++) {
+    int p = c;
+    for (int i = c + 1; i < n; i++) if (fabs(B[i + (size_t)c * n]) > fabs(B[p + (size_t)c * n])) p = i;
+    if (B[p + (size_t)c * n] == 0.0) { err = 76; break; }
+    if (p != c) {
+      for (int j = 0; j < n; j++) { double t = B[c + (size_t)j * n]; B[c + (size_t)j * n] = B[p + (size_t)j * n]; B[p + (size_t)j * n] = t; }
+      double t = g[c]; g[c] = g[p]; g[p] = t;
+    }
+    for (int i = c + 1; i < n; i++) {
+      double f = B[i + (size_t)c * n] / B[c + (size_t)c * n];
+      for (int j = c + 1; j < n; j++) B[i + (size_t)j * n] -= f * B[c + (size_t)j * n];
+      g[i] -= f * g[c];
+    }
+  }
+  if (!err)
+    for (int i = n - 1; i >= 0; i--) {
+      double s = g[i];
+      for (int j = i + 1; j < n; j++) s -= B[i + (size_t)j * n] * g[j];
+      g[i] = s / B[i + (size_t)i * n];
+    }
+  free(B);
+  if (err) return err;
+  for (int i = 0; i < n; i++) ds->A[IDX(i, n - 1, ld)] += g[i] * beta;
+  *gamma = hypot(1.0, nrm2(n, g));
+  return 0;
+}
+
+/* DSTranslateHarmonic_NHEP, recovery (dsnhep.c:508-535) with DSSetDimensions(n, k, l): ghat = -Q(:,0:k+l)' g;
+ * A(i, j) += ghat_i Q(n-1, j) beta for i < k+l, k <= j < k+l; g <- g + Q(:,0:k+l) ghat; gamma = sqrt(1 + g'g);
+ * the extra row entries k..k+l-1 are multiplied by gamma. */
+static void harmonic_recover(ds_t *ds, int k, int l, double beta, double *g, double *gamma) {
+  int n = ds->n, ld = ds->ld, ncol = k + l;
+  double *gh = ds->work;
+  for (int j = 0; j < ncol; j++) {
+    double s = 0.0;
+    for (int i = 0; i < n; i++) s += ds->Q[IDX(i, j, ld)] * g[i];
+    gh[j] = -s;
+  }
+  for (int i = 0; i < ncol; i++)
+    for (int j = k; j < ncol; j++) ds->A[IDX(i, j, ld)] += gh[i] * ds->Q[IDX(n - 1, j, ld)] * beta;
+  for (int i = 0; i < n; i++) {
+    double s = 0.0;
+    for (int j = 0; j < ncol; j++) s += ds->Q[IDX(i, j, ld)] * gh[j];
+    g[i] += s;
+  }
+  *gamma = hypot(1.0, nrm2(n, g));
+  for (int j = k; j < ncol; j++) ds->A[IDX(n, j, ld)] *= *gamma;
+}
+
 /* BVMatLanczos / BVMatArnoldi (bvkrylov.c:56-226): steps j = k..m-1 */
 static int krylov_factor(bv_t *bv, const csr_t *A, int hermitian, ds_t *ds, int k, int *m, double *beta,
                          int *breakdown, long long *nsteps) {
@@ -1140,8 +1204,11 @@ int ksor_solve(int n, const int *rowptr, const int *colidx, const double *vals,
                int hermitian, int which, int nev, int ncv, int mpd, double tol, int max_it,
                double keep, int lock, int nthreads, const double *v0, unsigned long long seed,
                double time_budget_s,
-               int *info, int ncv_cap, double *eigr_out, double *eigi_out, double *errest_out, double *X) {
+               int *info, int ncv_cap, double *eigr_out, double *eigi_out, double *errest_out, double *X,
+               int harmonic, double target) {
   double t_start = now_s();
+  /* EPSSolve_KrylovSchur_Default (krylovschur.c:238-239): harmonic extraction runs the non-symmetric variant */
+  if (harmonic) hermitian = 0;
   if (n <= 0 || nev <= 0) return 63;
   if (nthreads <= 0) nthreads = 1;
   /* EPSSetDimensions_Default (epssetup.c:648-671) */
@@ -1177,6 +1244,7 @@ int ksor_solve(int n, const int *rowptr, const int *colidx, const double *vals,
   double *eigr = (double *)calloc(ld, sizeof(double)), *eigi = (double *)calloc(ld, sizeof(double));
   double *errest = (double *)calloc(ld, sizeof(double));
   int *perm = (int *)calloc(ld, sizeof(int));
+  double *hg = (double *)calloc(ld, sizeof(double));
   int err = 0, reason = KSOR_ITERATING, its = 0, nconv = 0;
   long long nsteps = 0;
   if (!bv.V || !bv.h || !bv.c || !ds.A || !ds.Q || !ds.X) { err = 55; goto done; }
@@ -1202,14 +1270,20 @@ int ksor_solve(int n, const int *rowptr, const int *colidx, const double *vals,
     if (err) goto done;
     ds.n = nv; ds.t = nv; ds.l = nconv; ds.k = nconv + l;
     ds.state = l ? ST_RAW : ST_INTERMEDIATE;
+    /* translation of the Krylov decomposition for harmonic extraction (krylovschur.c:270-271) */
+    double gamma = 1.0;
+    if (harmonic) {
+      if ((err = harmonic_translate(&ds, target, beta, hg, &gamma))) goto done;
+      ds.state = ST_RAW;
+    }
     /* solve, sort, extra row */
     if (hermitian) {
       if (ds_hep_solve(&ds, eigr, eigi)) { err = 76; goto done; }
-      ds_hep_sort(&ds, which, eigr);
+      ds_hep_sort(&ds, which, target, eigr);
       ds_hep_extrarow(&ds);
     } else {
       if (ds_nhep_solve(&ds, eigr, eigi)) { err = 76; goto done; }
-      if (ds_nhep_sort(&ds, which, eigr, eigi)) { err = 76; goto done; }
+      if (ds_nhep_sort(&ds, which, target, eigr, eigi)) { err = 76; goto done; }
       ds_nhep_extrarow(&ds);
     }
     /* EPSKrylovConvergence (epskrylov.c:207-295) */
@@ -1220,7 +1294,7 @@ int ksor_solve(int n, const int *rowptr, const int *colidx, const double *vals,
       double resnorm;
       if (hermitian) resnorm = fabs(ds.Q[IDX(nv - 1, k, ld)]);
       else ds_nhep_vector(&ds, &newk, &resnorm);
-      resnorm *= beta;
+      resnorm *= beta * gamma;  /* corrf = gamma (epskrylov.c:265) */
       double w = hypot(re, im);
       errest[k] = (w != 0.0) ? resnorm / w : DBL_MAX;
       if (marker == -1 && errest[k] >= tol) marker = k;
@@ -1256,6 +1330,16 @@ int ksor_solve(int n, const int *rowptr, const int *colidx, const double *vals,
           else bv_scale(&bv, k, 1.0 / nrm);
         }
       } else {
+        if (harmonic) {
+          /* undo the translation (krylovschur.c:306-316): gamma u^ = u - V(:,0:nv) g~ */
+          harmonic_recover(&ds, k, l, beta, hg, &gamma);
+          double *u = VCOL(&bv, nv);
+          for (int i = 0; i < n; i++) {
+            double s = 0.0;
+            for (int j = 0; j < nv; j++) s += VCOL(&bv, j)[i] * hg[j];
+            u[i] = (u[i] - s) / gamma;
+          }
+        }
         /* DSTruncate(k+l) */
         int nn = k + l;
         if (!hermitian) {
@@ -1295,7 +1379,7 @@ int ksor_solve(int n, const int *rowptr, const int *colidx, const double *vals,
     int j = i + 1;
     if (im != 0.0) { i--; im = eigi[perm[i]]; }
     while (j < nconv) {
-      if (sc_compare(which, re, im, eigr[perm[j]], eigi[perm[j]]) <= 0) break;
+      if (sc_compare(which, target, re, im, eigr[perm[j]], eigi[perm[j]]) <= 0) break;
       int tmp;
       if (im == 0.0) {
         if (eigi[perm[j]] == 0.0) { tmp = perm[j - 1]; perm[j - 1] = perm[j]; perm[j] = tmp; j++; }
@@ -1329,7 +1413,7 @@ done:
   }
   free(bv.V); free(bv.h); free(bv.c);
   free(ds.d); free(ds.e); free(ds.A); free(ds.Q); free(ds.X); free(ds.perm); free(ds.work);
-  free(eigr); free(eigi); free(errest); free(perm);
+  free(eigr); free(eigi); free(errest); free(perm); free(hg);
   return err;
 }
 
@@ -1349,7 +1433,7 @@ int ksor_ds_hep(int n, int l, int k, int ld, const double *d, const double *e, i
   ds.state = state_raw ? ST_RAW : ST_INTERMEDIATE;
   int err = ds_hep_solve(&ds, wr, NULL);
   if (!err) {
-    ds_hep_sort(&ds, which, wr);
+    ds_hep_sort(&ds, which, 0.0, wr);
     if (extrarow) ds_hep_extrarow(&ds);
     if (e_out) memcpy(e_out, ds.e, sizeof(double) * n);
   }
@@ -1366,7 +1450,7 @@ int ksor_ds_nhep(int n, int ld, double *A, int state_intermediate, int which, in
   ds.work = (double *)calloc((size_t)4 * ld, sizeof(double));
   ds.state = state_intermediate ? ST_INTERMEDIATE : ST_RAW;
   int err = ds_nhep_solve(&ds, wr, wi);
-  if (!err) err = ds_nhep_sort(&ds, which, wr, wi);
+  if (!err) err = ds_nhep_sort(&ds, which, 0.0, wr, wi);
   if (!err) {
     if (extrarow) ds_nhep_extrarow(&ds);
     if (vec_index >= 0 && rnorm) { int j = vec_index; ds_nhep_vector(&ds, &j, rnorm); }

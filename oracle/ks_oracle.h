@@ -16,7 +16,7 @@ extern "C" {
 
 /* which: same numbering as SLEPc's EPSWhich (include/slepceps.h:109) */
 enum { KSOR_LARGEST_MAGNITUDE = 1, KSOR_SMALLEST_MAGNITUDE, KSOR_LARGEST_REAL, KSOR_SMALLEST_REAL,
-       KSOR_LARGEST_IMAGINARY, KSOR_SMALLEST_IMAGINARY };
+       KSOR_LARGEST_IMAGINARY, KSOR_SMALLEST_IMAGINARY, KSOR_TARGET_MAGNITUDE, KSOR_TARGET_REAL };
 
 /* converged reasons (include/slepceps.h:174-180) */
 enum { KSOR_CONVERGED_TOL = 1, KSOR_DIVERGED_ITS = -1, KSOR_DIVERGED_BREAKDOWN = -2, KSOR_ITERATING = 0 };
@@ -25,7 +25,7 @@ enum { KSOR_CONVERGED_TOL = 1, KSOR_DIVERGED_ITS = -1, KSOR_DIVERGED_BREAKDOWN =
 enum { KSOR_INFO_NCONV = 0, KSOR_INFO_ITS, KSOR_INFO_REASON, KSOR_INFO_NSTEPS, KSOR_INFO_NPASSES,
        KSOR_INFO_NCV, KSOR_INFO_MPD, KSOR_INFO_MAXIT, KSOR_INFO_LEN = 16 };
 
-/* Full Krylov-Schur solve (EPSSolve with EPSKRYLOVSCHUR, ST shift 0, Ritz extraction).
+/* Full Krylov-Schur solve (EPSSolve with EPSKRYLOVSCHUR, ST shift 0, Ritz or harmonic extraction).
  *   CSR matrix (n, rowptr[n+1], colidx[nnz], vals[nnz]); hermitian selects Lanczos+DSHEP vs Arnoldi+DSNHEP.
  *   ncv/mpd/max_it <= 0 select the reference defaults.  keep <= 0 selects 0.5.  lock: 1 locking, 0 not.
  *   v0: start vector (n), copied into V[:,0] as EPSSetInitialSpace does; NULL draws a random one.
@@ -33,12 +33,15 @@ enum { KSOR_INFO_NCONV = 0, KSOR_INFO_ITS, KSOR_INFO_REASON, KSOR_INFO_NSTEPS, K
  *   X (n x ncv_cap column-major, may be NULL) receives the eigenvectors in the same order (complex pairs as
  *   consecutive real/imag columns, as in the reference's V layout).
  *   time_budget_s > 0 stops after that many seconds (reason stays ITERATING): used for bounded CPU samples.
+ *   harmonic: harmonic Rayleigh-Ritz extraction for the given target (EPSSetExtraction(EPS_HARMONIC),
+ *   EPSSetTarget); target also serves the target sorting criteria.
  * Returns 0 on success, nonzero error code otherwise. */
 int ksor_solve(int n, const int *rowptr, const int *colidx, const double *vals,
                int hermitian, int which, int nev, int ncv, int mpd, double tol, int max_it,
                double keep, int lock, int nthreads, const double *v0, unsigned long long seed,
                double time_budget_s,
-               int *info, int ncv_cap, double *eigr, double *eigi, double *errest, double *X);
+               int *info, int ncv_cap, double *eigr, double *eigi, double *errest, double *X,
+               int harmonic, double target);
 
 /* y = A x (CSR), the operation MatMult performs for AIJ. */
 void ksor_spmv(int n, const int *rowptr, const int *colidx, const double *vals, const double *x, double *y,

@@ -87,6 +87,15 @@ def load():
         "EPSGB300OrthogonalityError": ([P, P], I),
         "EPSGB300SetProfiling": ([P, I], I),
         "EPSGB300GetProfile": ([P, I, P, P, P], I),
+        "EPSSetExtraction": ([P, I], I),
+        "EPSGetExtraction": ([P, P], I),
+        "EPSSetTarget": ([P, D], I),
+        "EPSGetTarget": ([P, P], I),
+        "PetscViewerBinaryOpen": ([I, ctypes.c_char_p, I, PP], I),
+        "PetscViewerDestroy": ([PP], I),
+        "MatCreate": ([I, PP], I),
+        "MatLoad": ([P, P], I),
+        "MatView": ([P, P], I),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -231,7 +240,11 @@ class EPS:
         DIVERGED_BREAKDOWN = -2
         CONVERGED_ITERATING = 0
 
-    WHICH_NAMES = {"LM": 1, "SM": 2, "LR": 3, "SR": 4, "LI": 5, "SI": 6}
+    WHICH_NAMES = {"LM": 1, "SM": 2, "LR": 3, "SR": 4, "LI": 5, "SI": 6, "TM": 7, "TR": 8}
+
+    class Extraction:
+        RITZ = 0
+        HARMONIC = 1
 
     def __init__(self):
         self.handle = ctypes.c_void_p()
@@ -302,6 +315,25 @@ class EPS:
 
     def setKrylovSchurRestart(self, keep):
         _check(load().EPSKrylovSchurSetRestart(self.handle, float(keep)), "EPSKrylovSchurSetRestart")
+
+    def setExtraction(self, extraction):
+        """'ritz' or 'harmonic' (or EPS.Extraction.*): harmonic Rayleigh-Ritz for eigenvalues near the target."""
+        if isinstance(extraction, str):
+            extraction = {"ritz": 0, "harmonic": 1}[extraction]
+        _check(load().EPSSetExtraction(self.handle, int(extraction)), "EPSSetExtraction")
+
+    def getExtraction(self):
+        v = ctypes.c_int()
+        _check(load().EPSGetExtraction(self.handle, ctypes.byref(v)), "EPSGetExtraction")
+        return v.value
+
+    def setTarget(self, target):
+        _check(load().EPSSetTarget(self.handle, ctypes.c_double(float(target))), "EPSSetTarget")
+
+    def getTarget(self):
+        v = ctypes.c_double()
+        _check(load().EPSGetTarget(self.handle, ctypes.byref(v)), "EPSGetTarget")
+        return v.value
 
     def setKrylovSchurLocking(self, lock):
         _check(load().EPSKrylovSchurSetLocking(self.handle, int(bool(lock))), "EPSKrylovSchurSetLocking")
@@ -481,7 +513,7 @@ def batch_set_tuning(tiles):
 
 
 def solve(csr, *, hermitian=True, which="LM", nev=1, ncv=None, mpd=None, tol=None, max_it=None, v0=None,
-          arith="pair", vectors=True, ds=None, lock=None, restart=None):
+          arith="pair", vectors=True, ds=None, lock=None, restart=None, harmonic=False, target=None):
     """One-call convenience: returns dict(eigr, eigi, X, nconv, its, reason, errors, stats)."""
     A = Mat(*csr)
     eps = EPS().create()
@@ -491,6 +523,10 @@ def solve(csr, *, hermitian=True, which="LM", nev=1, ncv=None, mpd=None, tol=Non
     eps.setTolerances(tol if tol else -1.0, max_it if max_it else -1)
     eps.setWhichEigenpairs(which)
     eps.setArithmetic(arith)
+    if target is not None:
+        eps.setTarget(target)
+    if harmonic:
+        eps.setExtraction("harmonic")
     if ds is not None:
         eps.setProjectedSolver(ds)
     if restart is not None:

@@ -89,6 +89,8 @@ PetscErrorCode ksg_engine_check(EPS e, int max_ncv, bool allow_f32) {
   KSG_CHECK(e->arith == ARITH_PAIR || (allow_f32 && e->arith == ARITH_F32), PETSC_ERR_SUP,
             "batched engine: the EPS must use the pair arithmetic%s", allow_f32 ? " or the precision form" : "");
   KSG_CHECK(e->ncv_e <= max_ncv, PETSC_ERR_SUP, "batched engine: ncv = %d exceeds the limit %d", e->ncv_e, max_ncv);
+  KSG_CHECK(e->extraction == EPS_RITZ && e->which <= EPS_SMALLEST_IMAGINARY, PETSC_ERR_SUP,
+            "batched engine: Ritz extraction with the largest/smallest criteria only (use EPSSolve for targets)");
   return 0;
 }
 

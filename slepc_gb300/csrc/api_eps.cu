@@ -595,8 +595,28 @@ extern "C" PetscErrorCode EPSGetProblemType(EPS eps, EPSProblemType *type) {
 }
 extern "C" PetscErrorCode EPSSetExtraction(EPS eps, EPSExtraction extr) {
   KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
-  KSG_CHECK(extr == EPS_RITZ, PETSC_ERR_SUP, "Only Ritz extraction is provided");
+  // EPSSetUp_KrylovSchur (krylovschur.c:120) admits Ritz and harmonic extraction
+  KSG_CHECK(extr == EPS_RITZ || extr == EPS_HARMONIC, PETSC_ERR_SUP, "Unsupported extraction type");
   eps->extraction = extr;
+  eps->setup = 0;
+  eps->solved = 0;
+  return 0;
+}
+extern "C" PetscErrorCode EPSGetExtraction(EPS eps, EPSExtraction *extr) {
+  KSG_CHECK(eps && extr, PETSC_ERR_ARG_NULL, "Null argument");
+  *extr = (EPSExtraction)eps->extraction;
+  return 0;
+}
+extern "C" PetscErrorCode EPSSetTarget(EPS eps, PetscScalar target) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  KSG_CHECK(std::isfinite(target), PETSC_ERR_ARG_WRONG, "The target must be finite");
+  eps->target = target;
+  eps->solved = 0;
+  return 0;
+}
+extern "C" PetscErrorCode EPSGetTarget(EPS eps, PetscScalar *target) {
+  KSG_CHECK(eps && target, PETSC_ERR_ARG_NULL, "Null argument");
+  *target = eps->target;
   return 0;
 }
 extern "C" PetscErrorCode EPSSetDimensions(EPS eps, PetscInt nev, PetscInt ncv, PetscInt mpd) {
@@ -651,8 +671,9 @@ extern "C" PetscErrorCode EPSGetTolerances(EPS eps, PetscReal *tol, PetscInt *ma
 }
 extern "C" PetscErrorCode EPSSetWhichEigenpairs(EPS eps, EPSWhich which) {
   KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
-  KSG_CHECK(which >= EPS_LARGEST_MAGNITUDE && which <= EPS_SMALLEST_IMAGINARY, PETSC_ERR_SUP,
-            "Only EPS_LARGEST/SMALLEST_MAGNITUDE/REAL/IMAGINARY are provided");
+  KSG_CHECK(which >= EPS_LARGEST_MAGNITUDE && which <= EPS_TARGET_REAL, PETSC_ERR_SUP,
+            "Only EPS_LARGEST/SMALLEST_MAGNITUDE/REAL/IMAGINARY and EPS_TARGET_MAGNITUDE/REAL are provided "
+            "(EPS_TARGET_IMAGINARY needs complex scalars)");
   eps->which = which;
   eps->solved = 0;
   return 0;
@@ -761,6 +782,14 @@ extern "C" PetscErrorCode EPSSetFromOptions(EPS eps) {
     else if (!strcmp(o, "-eps_smallest_real")) KSG_TRY(EPSSetWhichEigenpairs(eps, EPS_SMALLEST_REAL));
     else if (!strcmp(o, "-eps_largest_imaginary")) KSG_TRY(EPSSetWhichEigenpairs(eps, EPS_LARGEST_IMAGINARY));
     else if (!strcmp(o, "-eps_smallest_imaginary")) KSG_TRY(EPSSetWhichEigenpairs(eps, EPS_SMALLEST_IMAGINARY));
+    else if (!strcmp(o, "-eps_target_magnitude")) KSG_TRY(EPSSetWhichEigenpairs(eps, EPS_TARGET_MAGNITUDE));
+    else if (!strcmp(o, "-eps_target_real")) KSG_TRY(EPSSetWhichEigenpairs(eps, EPS_TARGET_REAL));
+    else if (!strcmp(o, "-eps_target") && v) {
+      // epsopts.c: giving a target also selects EPS_TARGET_MAGNITUDE unless a target criterion is already set
+      KSG_TRY(EPSSetTarget(eps, atof(v)));
+      if (eps->which != EPS_TARGET_REAL) KSG_TRY(EPSSetWhichEigenpairs(eps, EPS_TARGET_MAGNITUDE));
+    } else if (!strcmp(o, "-eps_harmonic")) KSG_TRY(EPSSetExtraction(eps, EPS_HARMONIC));
+    else if (!strcmp(o, "-eps_ritz")) KSG_TRY(EPSSetExtraction(eps, EPS_RITZ));
     else if (!strcmp(o, "-eps_hermitian")) KSG_TRY(EPSSetProblemType(eps, EPS_HEP));
     else if (!strcmp(o, "-eps_non_hermitian")) KSG_TRY(EPSSetProblemType(eps, EPS_NHEP));
     else if (!strcmp(o, "-eps_krylovschur_restart") && v) KSG_TRY(EPSKrylovSchurSetRestart(eps, atof(v)));
@@ -813,6 +842,7 @@ extern "C" PetscErrorCode EPSSetUp(EPS eps) {
   eps->maxit_e = (eps->max_it == PETSC_DETERMINE) ? std::max(100, 2 * n / ncv) : eps->max_it;
   eps->tol_e = (eps->tol == (double)PETSC_DETERMINE) ? 1e-8 : eps->tol;
   if (!eps->which) eps->which = EPS_LARGEST_MAGNITUDE;
+  KSG_CHECK(eps->extraction == EPS_RITZ || eps->extraction == EPS_HARMONIC, PETSC_ERR_SUP, "Unsupported extraction type");
   eps->n = n;
   eps->ld = ncv + 1;
   // the device basis: columns 512-byte aligned
@@ -932,7 +962,7 @@ static double spmv_bytes(EPS eps) {
 static PetscErrorCode eps_factorize(EPS eps, int k0, int nv, double *bytes) {
   cudaStream_t s = eps->stream;
   const int n = eps->n;
-  const int herm = eps->problem == EPS_HEP;
+  const int herm = ksg_eps_lanczos(eps);
   KSG_CUDA(launch_segment_begin(eps->st.p, k0, nv, s));
   StepArgs a = {};
   a.V = eps->V.p;
@@ -1030,9 +1060,11 @@ PetscErrorCode ksg_eps_new_start_vector(EPS eps, int col, int *breakdown) {
   return 0;
 }
 
-static int compare_which(int which, double ar, double ai, double br, double bi) {
+static int compare_which(int which, double target, double ar, double ai, double br, double bi) {
   double a, b;
   switch (which) {
+    case EPS_TARGET_MAGNITUDE: a = hypot(ar - target, ai); b = hypot(br - target, bi); return a > b ? 1 : (a < b ? -1 : 0);
+    case EPS_TARGET_REAL: a = fabs(ar - target); b = fabs(br - target); return a > b ? 1 : (a < b ? -1 : 0);
     case EPS_LARGEST_MAGNITUDE: a = hypot(ar, ai); b = hypot(br, bi); return a < b ? 1 : (a > b ? -1 : 0);
     case EPS_SMALLEST_MAGNITUDE: a = hypot(ar, ai); b = hypot(br, bi); return a > b ? 1 : (a < b ? -1 : 0);
     case EPS_LARGEST_REAL: return ar < br ? 1 : (ar > br ? -1 : 0);
@@ -1044,7 +1076,7 @@ static int compare_which(int which, double ar, double ai, double br, double bi) 
 }
 
 // SlepcSortEigenvalues (slepcsc.c:89-140): insertion sort keeping conjugate pairs together
-static void sort_eigenvalues(int which, int n, const double *eigr, const double *eigi, int *perm) {
+static void sort_eigenvalues(int which, double target, int n, const double *eigr, const double *eigi, int *perm) {
   for (int i = n - 1; i >= 0; i--) {
     double re = eigr[perm[i]], im = eigi[perm[i]];
     int j = i + 1;
@@ -1053,7 +1085,7 @@ static void sort_eigenvalues(int which, int n, const double *eigr, const double 
       im = eigi[perm[i]];
     }
     while (j < n) {
-      if (compare_which(which, re, im, eigr[perm[j]], eigi[perm[j]]) <= 0) break;
+      if (compare_which(which, target, re, im, eigr[perm[j]], eigi[perm[j]]) <= 0) break;
       int tmp;
       if (im == 0.0) {
         if (eigi[perm[j]] == 0.0) {
@@ -1102,7 +1134,7 @@ PetscErrorCode ksg_eps_assemble(EPS eps, int nconv, const double *er, const doub
   }
   eps->perm.resize(std::max(nconv, 1));
   for (int i = 0; i < nconv; ++i) eps->perm[i] = i;
-  sort_eigenvalues(eps->which, nconv, eps->r_eigr.data(), eps->r_eigi.data(), eps->perm.data());
+  sort_eigenvalues(eps->which, eps->target, nconv, eps->r_eigr.data(), eps->r_eigi.data(), eps->perm.data());
   return 0;
 }
 
@@ -1121,7 +1153,8 @@ static PetscErrorCode eps_solve_core(EPS eps, double tol, std::chrono::steady_cl
                                      int *its_out, int *reason_out, double *bytes_out) {
   cudaStream_t s = eps->stream;
   const int n = eps->n, ld = eps->ld, ncv = eps->ncv_e, mpd = eps->mpd_e, nev = eps->nev_e;
-  const int herm = eps->problem == EPS_HEP;
+  const int herm = ksg_eps_lanczos(eps);
+  const int harmonic = eps->extraction == EPS_HARMONIC;
   // start vector: the initial space, or a random vector (EPSGetStartVector, epssolve.c:841-873)
   {
     KSG_TRY(ksg_eps_put_start(eps, s));
@@ -1166,6 +1199,8 @@ static PetscErrorCode eps_solve_core(EPS eps, double tol, std::chrono::steady_cl
     da.lock = eps->lock;
     da.st = eps->st.p;
     da.ctl = eps->ctl.p;
+    da.target = eps->target * eps->opscale;  // the projected problem holds the scaled operator
+    da.harmonic = harmonic;
     {
       LaunchScope ls(eps, EPS_GB300_K_DS, 0.0);
       if (herm && eps->ds_method == EPS_GB300_DS_REFINED) {
@@ -1186,6 +1221,28 @@ static PetscErrorCode eps_solve_core(EPS eps, double tol, std::chrono::steady_cl
     l = c.l;
     reason = c.reason;
     nv = c.nv;
+    if (harmonic && reason == 0 && !(c.breakdown || k == nv)) {
+      // undo the harmonic translation on the residual vector (krylovschur.c:312-315): gamma u^ = u - V(:,0:nv) g~,
+      // with g~ from the projected solver (work) and gamma in the control block; the BVMultVec form of the
+      // Gram-Schmidt update kernel
+      StepArgs ha = {};
+      ha.V = eps->V.p;
+      ha.ldv = eps->ldv;
+      ha.n = n;
+      ha.J = nv;
+      ha.j = nv;
+      ha.hermitian = 1;
+      ha.U = ksg_col(eps->V.p, eps->ldv, nv, eps->storage);
+      ha.eta = 0.7071;
+      ha.coef = eps->work.p;
+      ha.part = eps->part.p;
+      ha.pstride = eps->pstride;
+      ha.st = eps->st.p;
+      KSG_CUDA(launch_set_scales(eps->st.p, 1.0, 1.0 / c.hgamma, s));
+      KSG_CUDA(launch_gs_update(ha, 1, GS_COMBINE, eps->arith, s, eps->storage));
+      eps->stats.kernel_launches += 2;
+      bytes += 8.0 * n * (nv + 2);
+    }
     // thick restart: V(:, nconv:k+l) = V(:, nconv:nv) Q(nconv:nv, nconv:k+l)
     {
       LaunchScope ls(eps, EPS_GB300_K_RESTART, 8.0 * n * ((nv - nconv) + (k + l - nconv)));
@@ -1212,7 +1269,8 @@ static PetscErrorCode eps_solve_core(EPS eps, double tol, std::chrono::steady_cl
         std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count() > eps->time_limit)
       reason = EPS_DIVERGED_ITS;  // the caller's wall-time budget ran out (EPSGB300SetTimeLimit)
   }
-  // non-Hermitian: eigenvectors of the leading Schur block, V = V X (EPSComputeVectors_Schur, epsdefault.c:105-169)
+  // non-Hermitian or harmonic: eigenvectors of the leading Schur block, V = V X (EPSComputeVectors_Schur,
+  // epsdefault.c:105-169)
   if (!herm && nconv > 0) {
     KSG_CUDA(launch_nhep_vectors(eps->H.p, ld, nconv, eps->X.p, s));
     KSG_CUDA(eps_restart(eps, 0, nconv, 0, nconv, eps->X.p, s));

@@ -108,7 +108,8 @@ struct _p_EPS {
   int max_it = PETSC_DETERMINE;
   double keep = 0.5;
   int lock = 1;
-  int extraction = 0;
+  int extraction = 0;  // EPSExtraction: EPS_RITZ or EPS_HARMONIC
+  double target = 0.0;
   int arith = ksg::ARITH_PAIR;
   int storage = ksg::STORE_PAIR;  // basis format: pairs with pair arithmetic, doubles with FP64 arithmetic
   int ds_method = 0;              // EPSGB300DSMethod
@@ -136,6 +137,7 @@ struct _p_EPS {
   DBuf<ksg::KSControl> ctl;
   ksg::KSControl *h_ctl = nullptr;  // pinned
   cudaEvent_t ev_solve[2] = {nullptr, nullptr};
+
   // results
   int nconv = 0, its = 0, reason = 0;
   std::vector<double> r_eigr, r_eigi, r_errest;
@@ -152,6 +154,10 @@ struct _p_EPS {
   BV bv = nullptr;
   DS ds = nullptr;
 };
+
+// the Lanczos (symmetric) variant runs for EPS_HEP with Ritz extraction; harmonic extraction runs the Arnoldi
+// variant with the non-symmetric projected solver (krylovschur.c:238-239)
+inline int ksg_eps_lanczos(EPS e) { return e->problem == EPS_HEP && e->extraction != EPS_HARMONIC; }
 
 // run the Gram-Schmidt pair kernels on one column (orthonormalise u = V[:, j] against V[:, 0:j]); returns the
 // norm of the orthogonalised vector in *nrm and the linear-dependence flag (two CGS passes)

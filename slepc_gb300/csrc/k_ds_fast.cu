@@ -505,10 +505,10 @@ __global__ void __launch_bounds__(DSF_THREADS, 1) k_dsf_finish(DSFArgs f, DSArgs
   // order-preserving integer keys (k_crit: the criterion's "goes first" order, k_asc: ascending value).
   for (int i = tid; i < m; i += DSF_THREADS) {
     const double v = lam[i] + 0.0;  // -0 -> +0, as the floating-point comparisons treat them
-    const double c = (a.which == 1 || a.which == 2) ? fabs(v) : v;
+    const double c = (a.which == 1 || a.which == 2) ? fabs(v) : (a.which >= 7 ? fabs(v - a.target) : v);
     const long long kv = dsf_order_key(v), kc0 = dsf_order_key(c);
     k_asc[i] = kv;
-    k_crit[i] = (a.which == 1 || a.which == 3) ? ~kc0 : kc0;  // largest first: reversed
+    k_crit[i] = (a.which == 1 || a.which == 3) ? ~kc0 : kc0;  // largest first: reversed; targets: nearest first
   }
   __syncthreads();
   for (int i = tid; i < m; i += DSF_THREADS) {

@@ -36,10 +36,13 @@ KS_DEVICE void ds_givens(double f, double g, double &c, double &s, double &r) {
   }
 }
 
-// criterion comparison (slepcsc.c): -1 if a goes first, 1 if b goes first, 0 if tied
-KS_DEVICE int ds_compare(int which, double ar, double ai, double br, double bi) {
+// criterion comparison (slepcsc.c:152-267): -1 if a goes first, 1 if b goes first, 0 if tied; 7 and 8 measure
+// the distance to the target
+KS_DEVICE int ds_compare(int which, double target, double ar, double ai, double br, double bi) {
   double a, b;
   switch (which) {
+    case 7: a = hypot(ar - target, ai); b = hypot(br - target, bi); return a > b ? 1 : (a < b ? -1 : 0);
+    case 8: a = fabs(ar - target); b = fabs(br - target); return a > b ? 1 : (a < b ? -1 : 0);
     case 1: a = hypot(ar, ai); b = hypot(br, bi); return a < b ? 1 : (a > b ? -1 : 0);
     case 2: a = hypot(ar, ai); b = hypot(br, bi); return a > b ? 1 : (a < b ? -1 : 0);
     case 3: return ar < br ? 1 : (ar > br ? -1 : 0);
@@ -210,11 +213,11 @@ KS_DEVICE void ds_hep_body(const DSArgs &a, double *Qs) {
     for (int i = l + 1; i < ((flags & DS_DO_SORT) ? n : 0); ++i) {
       const double re = sd[perm2[i]];
       int j = i - 1;
-      int res = ds_compare(a.which, re, 0.0, sd[perm2[j]], 0.0);
+      int res = ds_compare(a.which, a.target, re, 0.0, sd[perm2[j]], 0.0);
       while (res < 0 && j >= l) {
         const int t = perm2[j]; perm2[j] = perm2[j + 1]; perm2[j + 1] = t;
         --j;
-        if (j >= l) res = ds_compare(a.which, re, 0.0, sd[perm2[j]], 0.0);
+        if (j >= l) res = ds_compare(a.which, a.target, re, 0.0, sd[perm2[j]], 0.0);
       }
     }
     // composite: final column i = original column sperm[perm2[i]]

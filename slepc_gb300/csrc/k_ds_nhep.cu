@@ -830,10 +830,12 @@ __device__ int nh_eigvec(const double *A, int lda, int n, int k, double tnorm, d
 
 // ordering of two eigenvalues by the criterion: > 0 when (r2, i2) goes before (r1, i1) (SlepcSCCompare, which
 // values as in EPSWhich: 1 largest magnitude, 2 smallest magnitude, 3 largest real, 4 smallest real, 5 largest
-// imaginary, 6 smallest imaginary)
-KS_DEVICE int nh_cmp(int which, double r1, double i1, double r2, double i2) {
+// imaginary, 6 smallest imaginary, 7 closest to the target, 8 real part closest to the target; slepcsc.c:152-267)
+KS_DEVICE int nh_cmp(int which, double target, double r1, double i1, double r2, double i2) {
   double av, bv;
   switch (which) {
+    case 7: av = hypot(r1 - target, i1); bv = hypot(r2 - target, i2); return av > bv ? 1 : (av < bv ? -1 : 0);
+    case 8: av = fabs(r1 - target); bv = fabs(r2 - target); return av > bv ? 1 : (av < bv ? -1 : 0);
     case 1: av = hypot(r1, i1); bv = hypot(r2, i2); return av < bv ? 1 : (av > bv ? -1 : 0);
     case 2: av = hypot(r1, i1); bv = hypot(r2, i2); return av > bv ? 1 : (av < bv ? -1 : 0);
     case 3: return r1 < r2 ? 1 : (r1 > r2 ? -1 : 0);
@@ -849,8 +851,8 @@ KS_DEVICE int nh_cmp(int which, double r1, double i1, double r2, double i2) {
 // rotation from T(j, j+1) and T(j+1, j+1) - T(j, j), trexc/laexc with n1 = n2 = 1).  Pairs of one round are
 // disjoint, so their rotations commute: all row rotations are applied, then all column rotations (T and Q), then
 // the diagonal exchanges.  The final order is the stable order of the criterion, as the selection sort's.
-__device__ void nh_sort_real(double *A, int lda, double *Q, int ldq, int n, int l, int which, double *wr,
-                             NhShared &sh) {
+__device__ void nh_sort_real(double *A, int lda, double *Q, int ldq, int n, int l, int which, double target,
+                             double *wr, NhShared &sh) {
   const int tid = nh_tid();
   int quiet = 0;
   for (int round = 0; round < 2 * (n - l) + 2 && quiet < 2; ++round) {
@@ -859,7 +861,7 @@ __device__ void nh_sort_real(double *A, int lda, double *Q, int ldq, int n, int 
     int any = 0;
     for (int p = tid; p < np; p += NH_T) {
       const int j = j0 + 2 * p;
-      const int sw = nh_cmp(which, wr[j], 0.0, wr[j + 1], 0.0) > 0;
+      const int sw = nh_cmp(which, target, wr[j], 0.0, wr[j + 1], 0.0) > 0;
       sh.pf[p] = sw;
       if (sw) {
         any = 1;
@@ -925,9 +927,115 @@ __device__ void nh_sort_real(double *A, int lda, double *Q, int ldq, int n, int 
   }
 }
 
+// Harmonic extraction, translation (DSTranslateHarmonic_NHEP, dsnhep.c:466-507): g = (A - tau I)^T \ (beta e_n)
+// and A(:, n-1) += beta g; returns gamma = sqrt(1 + g'g), the correction factor of the residual estimates.  The
+// reference factors A - tau I and solves with its transpose; here the transpose is copied into the scratch C
+// (ldc >= n) and eliminated with partial pivoting (the row of largest magnitude, the first one on ties), which
+// solves the same system.  A zero pivot (tau an eigenvalue of A) sets sh.fail.
+__device__ double nh_harmonic_translate(double *A, int lda, int n, double tau, double beta, double *C, int ldc,
+                                        double *g, NhShared &sh) {
+  const int tid = nh_tid();
+  for (int t = tid; t < n * n; t += NH_T) {
+    const int r = t % n, c = t / n;
+    C[r + (size_t)c * ldc] = AH(c, r) - (r == c ? tau : 0.0);
+  }
+  for (int i = tid; i < n; i += NH_T) g[i] = (i == n - 1) ? beta : 0.0;
+  nh_sync();
+  for (int c = 0; c < n; ++c) {
+    if (tid < 32) {
+      double best = -1.0;
+      int bi = c;
+      for (int i = c + tid; i < n; i += 32) {
+        const double v = fabs(C[i + (size_t)c * ldc]);
+        if (v > best) { best = v; bi = i; }
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+      }
+      if (tid == 0) {
+        sh.i2 = bi;
+        sh.tau = best;
+      }
+    }
+    nh_sync();
+    const int p = sh.i2;
+    if (sh.tau == 0.0) {
+      if (tid == 0) sh.fail = 3;
+      nh_sync();
+      return 1.0;
+    }
+    if (p != c) {
+      for (int j = c + tid; j < n; j += NH_T) {
+        const double t = C[c + (size_t)j * ldc];
+        C[c + (size_t)j * ldc] = C[p + (size_t)j * ldc];
+        C[p + (size_t)j * ldc] = t;
+      }
+      if (tid == 0) {
+        const double t = g[c];
+        g[c] = g[p];
+        g[p] = t;
+      }
+      nh_sync();
+    }
+    const double piv = C[c + (size_t)c * ldc], gc = g[c];
+    for (int i = c + 1 + tid; i < n; i += NH_T) {
+      const double f = C[i + (size_t)c * ldc] / piv;
+      for (int j = c + 1; j < n; ++j) C[i + (size_t)j * ldc] -= f * C[c + (size_t)j * ldc];
+      g[i] -= f * gc;
+    }
+    nh_sync();
+  }
+  // back substitution, one column of U at a time
+  for (int i = n - 1; i >= 0; --i) {
+    if (tid == 0) g[i] /= C[i + (size_t)i * ldc];
+    nh_sync();
+    const double gi = g[i];
+    for (int r = tid; r < i; r += NH_T) g[r] -= C[r + (size_t)i * ldc] * gi;
+    nh_sync();
+  }
+  for (int i = tid; i < n; i += NH_T) AH(i, n - 1) += g[i] * beta;
+  double s2 = 0.0;
+  for (int i = tid; i < n; i += NH_T) s2 = fma(g[i], g[i], s2);
+  s2 = nh_block_sum(s2, sh.red);
+  return hypot(1.0, sqrt(s2));
+}
+
+// Harmonic extraction, recovery before the restart (dsnhep.c:508-535 with DSSetDimensions(n, k, l)):
+// ghat = -Q(:, 0:k+l)^T g; A(i, j) += ghat_i Q(n-1, j) beta for i < k+l, k <= j < k+l; g <- g + Q(:, 0:k+l) ghat;
+// gamma = sqrt(1 + g'g) scales the extra-row entries k..k+l-1.  Returns gamma; g holds g~.
+__device__ double nh_harmonic_recover(double *A, int lda, const double *Q, int ldq, int n, int k, int l,
+                                      double beta, double *g, double *gh, NhShared &sh) {
+  const int tid = nh_tid(), ncol = k + l;
+  for (int j = tid; j < ncol; j += NH_T) {
+    double s = 0.0;
+    for (int i = 0; i < n; ++i) s = fma(QH(i, j), g[i], s);
+    gh[j] = -s;
+  }
+  nh_sync();
+  for (int t = tid; t < ncol * l; t += NH_T) {
+    const int i = t % ncol, j = k + t / ncol;
+    AH(i, j) += gh[i] * QH(n - 1, j) * beta;
+  }
+  for (int i = tid; i < n; i += NH_T) {
+    double s = 0.0;
+    for (int j = 0; j < ncol; ++j) s = fma(QH(i, j), gh[j], s);
+    g[i] += s;
+  }
+  double s2 = 0.0;
+  for (int i = tid; i < n; i += NH_T) s2 = fma(g[i], g[i], s2);
+  s2 = nh_block_sum(s2, sh.red);
+  const double gamma = hypot(1.0, sqrt(s2));
+  for (int j = k + tid; j < ncol; j += NH_T) AH(n, j) *= gamma;
+  nh_sync();
+  return gamma;
+}
+
 KS_DEVICE void ds_nhep_body(const DSArgs &a, double *smem, int smem_bytes) {
   __shared__ NhShared sh;
   __shared__ double wr[NH_MAXN], wi[NH_MAXN], errs[NH_MAXN];
+  __shared__ double hg[NH_MAXN], hgh[NH_MAXN];  // harmonic extraction: g and ghat
   const int tid = nh_tid();
   const int n = a.st ? a.st->m : a.n;
   const int ld = a.ld, l = a.l, flags = a.flags;
@@ -947,11 +1055,16 @@ KS_DEVICE void ds_nhep_body(const DSArgs &a, double *smem, int smem_bytes) {
     sh.cmd = 0;
   }
   nh_sync();
+  const double beta = a.st ? a.st->beta_out : 0.0;
+  double hgamma = 1.0;  // correction factor of the residual estimates (1 for Ritz extraction)
   if (flags & DS_DO_SOLVE) {
+    // harmonic translation, with the Schur-vector storage as scratch before it is set to the identity
+    if (a.harmonic && n > 1) hgamma = nh_harmonic_translate(A, lda, n, a.target, beta, Q, ldq, hg, sh);
+    nh_sync();
     for (int i = tid; i < n * n; i += NH_T) QH(i % n, i / n) = ((i % n) == (i / n)) ? 1.0 : 0.0;
     nh_sync();
-    if (n > 1) {
-      if (a.raw) nh_hessenberg(A, lda, Q, ldq, n, l, sh);
+    if (n > 1 && !sh.fail) {
+      if (a.raw || a.harmonic) nh_hessenberg(A, lda, Q, ldq, n, l, sh);
       nh_francis(A, lda, Q, ldq, n, l, sh);
     }
     nh_sync();
@@ -962,7 +1075,7 @@ KS_DEVICE void ds_nhep_body(const DSArgs &a, double *smem, int smem_bytes) {
     int cplx = 0;
     for (int i = l + tid; i + 1 < n; i += NH_T) cplx |= AH(i + 1, i) != 0.0;
     if (!__syncthreads_or(cplx)) {
-      nh_sort_real(A, lda, Q, ldq, n, l, a.which, wr, sh);
+      nh_sort_real(A, lda, Q, ldq, n, l, a.which, a.target, wr, sh);
     } else {
       // selection sort (DSSort_NHEP_Total), thread 0 chooses, the block moves blocks
       for (int i = l; i < n - 1; ++i) {
@@ -971,7 +1084,7 @@ KS_DEVICE void ds_nhep_body(const DSArgs &a, double *smem, int smem_bytes) {
           int pos = 0;
           int j = (im != 0.0) ? i + 2 : i + 1;
           for (; j < n; ++j) {
-            if (nh_cmp(a.which, re, im, wr[j], wi[j]) > 0) { re = wr[j]; im = wi[j]; pos = j; }
+            if (nh_cmp(a.which, a.target, re, im, wr[j], wi[j]) > 0) { re = wr[j]; im = wi[j]; pos = j; }
             if (wi[j] != 0.0) j++;
           }
           sh.i2 = pos;
@@ -1021,8 +1134,7 @@ KS_DEVICE void ds_nhep_body(const DSArgs &a, double *smem, int smem_bytes) {
   } else {
     // residual estimates for k = l..n-1, one eigenvector per thread (DSVectors_NHEP_Eigen_Some): the Ritz vector
     // is Q x with x the eigenvector of the quasi-triangular T, so its norm is ||x|| (Q is orthogonal) and only
-    // its last entry Q(n-1, :) x is formed
-    const double beta = a.st ? a.st->beta_out : 0.0;
+    // its last entry Q(n-1, :) x is formed; harmonic extraction scales the estimate by gamma (epskrylov.c:265)
     // max |T(i, j)| over the upper Hessenberg part: columns split over the block, then a max over the warps
     double tnorm = 0.0;
     for (int j = tid; j < n; j += NH_T)
@@ -1047,12 +1159,13 @@ KS_DEVICE void ds_nhep_body(const DSArgs &a, double *smem, int smem_bytes) {
         }
       }
       const double nrm = sqrt(nr2 + ni2);
-      const double rn = (cplx ? hypot(yl_r, yl_i) : fabs(yl_r)) / nrm * beta;
+      const double rn = (cplx ? hypot(yl_r, yl_i) : fabs(yl_r)) / nrm * (beta * hgamma);
       const double w = hypot(wr[k], wi[k]);
       errs[k] = (w != 0.0) ? rn / w : DBL_MAX;
       if (cplx) errs[k + 1] = errs[k];
     }
     nh_sync();
+    // convergence marker, restart sizes and stopping test (thread 0), then the harmonic recovery (block)
     if (tid == 0) {
       int kk;
       for (kk = l; kk < n; ++kk) {
@@ -1063,7 +1176,6 @@ KS_DEVICE void ds_nhep_body(const DSArgs &a, double *smem, int smem_bytes) {
           kk++;
         }
       }
-      KSControl *ctl = a.ctl;
       int reason = 0;
       if (kk >= a.nev) reason = 1;
       else if (a.its >= a.max_it) reason = -1;
@@ -1080,7 +1192,24 @@ KS_DEVICE void ds_nhep_body(const DSArgs &a, double *smem, int smem_bytes) {
         }
       }
       if (!a.lock && lkeep > 0) { lkeep += kk; kk = 0; }
-      if (reason == 0 && !(breakdown || kk == n)) {
+      sh.i0 = kk;
+      sh.i1 = lkeep;
+      sh.i3 = reason;
+      sh.cmd = (reason == 0 && !(breakdown || kk == n)) ? 1 : 0;  // restart with truncation
+      sh.G[0] = 1.0;
+    }
+    nh_sync();
+    if (a.harmonic && sh.cmd && !sh.fail) {
+      const double g2 = nh_harmonic_recover(A, lda, Q, ldq, n, sh.i0, sh.i1, beta, hg, hgh, sh);
+      for (int i = tid; i < n; i += NH_T) a.work[i] = hg[i];  // g~ for the residual-vector update
+      if (tid == 0) sh.G[0] = g2;
+      nh_sync();
+    }
+    if (tid == 0) {
+      const int kk = sh.i0, lkeep = sh.i1, reason = sh.i3;
+      const int breakdown = a.st ? a.st->breakdown : 0;
+      KSControl *ctl = a.ctl;
+      if (sh.cmd) {
         // DSTruncate_NHEP: move the extra row to row kk+lkeep
         const int nn = kk + lkeep;
         for (int i = l; i < nn; ++i) AH(nn, i) = AH(n, i);
@@ -1094,6 +1223,7 @@ KS_DEVICE void ds_nhep_body(const DSArgs &a, double *smem, int smem_bytes) {
       ctl->need_start = (reason == 0 && (breakdown || kk == n) && kk < a.nev) ? 1 : 0;
       ctl->ds_error = sh.fail;
       ctl->beta = beta;
+      ctl->hgamma = sh.G[0];
     }
   }
   nh_sync();
@@ -1141,23 +1271,34 @@ __global__ void __launch_bounds__(32) k_nhep_vectors(const double *A, int lda, i
   }
 }
 
-// dynamic shared memory for problems of size up to n_max: A, and Q when both fit
-static int nh_smem_bytes(int n_max) {
-  size_t b = nh_smem_a(n_max);
-  if (b + nh_smem_q(n_max) <= (size_t)NH_SMEM_MAX) b += nh_smem_q(n_max);
-  return b <= (size_t)NH_SMEM_MAX ? (int)b : 0;
-}
+// dynamic shared memory of each solver kernel: at most NH_SMEM_MAX, and what the device's opt-in limit leaves
+// beside the kernel's own static shared memory (set once, before any launch is captured into a graph)
+static int g_nh_dyn[2] = {-1, -1};  // k_ds_nhep, k_batch_ds_nhep
 
 template <typename K>
-static cudaError_t nh_allow_smem(K kernel) {
-  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, NH_SMEM_MAX);
+static cudaError_t nh_allow_smem(K kernel, int *dyn) {
+  int dev = 0, optin = 0;
+  cudaFuncAttributes fa;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, kernel);
+  if (e != cudaSuccess) return e;
+  const int room = optin - (int)fa.sharedSizeBytes;
+  *dyn = room < NH_SMEM_MAX ? (room > 0 ? room : 0) : NH_SMEM_MAX;
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, *dyn);
 }
 
-// kernel attributes set once per process, before any launch is captured into a graph
+// dynamic shared memory for problems of size up to n_max: A, and Q when both fit in the kernel's allowance
+static int nh_smem_bytes(int n_max, int allowed) {
+  size_t b = nh_smem_a(n_max);
+  if (b + nh_smem_q(n_max) <= (size_t)allowed) b += nh_smem_q(n_max);
+  return b <= (size_t)allowed ? (int)b : 0;
+}
+
 cudaError_t prepare_ds_nhep() {
   static cudaError_t attr = [] {
-    cudaError_t e = nh_allow_smem(k_ds_nhep);
-    return e != cudaSuccess ? e : nh_allow_smem(k_batch_ds_nhep);
+    cudaError_t e = nh_allow_smem(k_ds_nhep, &g_nh_dyn[0]);
+    return e != cudaSuccess ? e : nh_allow_smem(k_batch_ds_nhep, &g_nh_dyn[1]);
   }();
   return attr;
 }
@@ -1166,7 +1307,7 @@ cudaError_t launch_ds_nhep(const DSArgs &a, int n_max, cudaStream_t s) {
   if (n_max > NH_MAXN) return cudaErrorInvalidValue;
   const cudaError_t attr = prepare_ds_nhep();
   if (attr != cudaSuccess) return attr;
-  const int bytes = nh_smem_bytes(n_max);
+  const int bytes = nh_smem_bytes(n_max, g_nh_dyn[0]);
   k_ds_nhep<<<1, NH_T, bytes, s>>>(a, bytes);
   return cudaGetLastError();
 }
@@ -1176,7 +1317,7 @@ cudaError_t launch_batch_ds_nhep(const BatchInst *I, const int *list, const Batc
   if (max_ld > NH_MAXN) return cudaErrorInvalidValue;
   const cudaError_t attr = prepare_ds_nhep();
   if (attr != cudaSuccess) return attr;
-  const int bytes = nh_smem_bytes(max_ld);
+  const int bytes = nh_smem_bytes(max_ld, g_nh_dyn[1]);
   k_batch_ds_nhep<<<grid, NH_T, bytes, s>>>(I, list, h, bytes);
   return cudaGetLastError();
 }

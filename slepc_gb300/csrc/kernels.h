@@ -27,6 +27,8 @@ struct DSArgs {
   int lock;
   const KrylovState *st;
   KSControl *ctl;
+  double target;   // target of the EPS_TARGET_* criteria (operator scale applied)
+  int harmonic;    // non-symmetric solver: harmonic Rayleigh-Ritz translation for the target
 };
 
 enum { DS_DO_SOLVE = 1, DS_DO_SORT = 2, DS_DO_EXTRAROW = 4, DS_DO_CONTROL = 8, DS_DO_ALL = 15 };

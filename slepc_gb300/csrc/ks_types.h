@@ -56,6 +56,7 @@ struct KSControl {
   int ds_error;     // nonzero if the dense solver did not converge
   int pad;
   double beta;      // residual norm used in the convergence test
+  double hgamma;    // harmonic extraction: the scale gamma of the recovered residual vector (work holds g~)
 };
 
 // Arguments of one Gram-Schmidt step kernel (both halves of the fused pair).

@@ -34,7 +34,9 @@ def main():
     blocks = re.findall(r"- - - (\w+) eigenvalues - - -.*?\n.*?\n(.*?)\n", txt, flags=re.S)
     g["test2_1"] = {"source": "src/eps/tests/output/test2_1.out", "n": 30, "nev": 4,
                     "tol": max(1000 * 2.220446049250313e-16, 1e-9),
-                    "largest": floats(blocks[0][1]), "smallest": floats(blocks[1][1])}
+                    "largest": floats(blocks[0][1]), "smallest": floats(blocks[1][1]),
+                    # EPS_TARGET_MAGNITUDE, target 2.1, EPSSetExtraction(EPS_HARMONIC) for Krylov-Schur
+                    "interior": floats(blocks[2][1]), "target": 2.1}
     txt = read("src/eps/tests/output/test2_3.out")
     blocks = re.findall(r"- - - (\w+) eigenvalues - - -.*?\n.*?\n(.*?)\n", txt, flags=re.S)
     g["test2_3"] = {"source": "src/eps/tests/output/test2_3.out", "n": 32, "nev": 4,

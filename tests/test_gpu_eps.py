@@ -219,3 +219,77 @@ def test_tensor_restart_matches_pair_restart(lib, herm):
     for x, y in zip(a["eigr"][:kw["nev"]], a["eigi"][:kw["nev"]]):
         z = complex(x, y)
         assert np.min(np.abs(vb - z)) / abs(z) <= agree
+
+
+@pytest.mark.parametrize("lock", [True, False])
+def test_test2_interior_harmonic_golden_on_gpu(lib, lock):
+    """test2.c's third solve on the device: harmonic extraction for the eigenvalues closest to 2.1."""
+    g = G["test2_1"]
+    csr = matgen.laplacian_1d(g["n"])
+    res = run(csr, hermitian=True, which="TM", nev=g["nev"], tol=g["tol"], v0=matgen.start_vector(g["n"], 1),
+              harmonic=True, target=g["target"], lock=lock)
+    assert res["reason"] == 1
+    assert [round(v, 5) for v in res["eigr"][:4]] == g["interior"]
+    assert res["eps"].getExtraction() == 1 and res["eps"].getTarget() == g["target"]
+
+
+@pytest.mark.parametrize("arith", ["pair", "f64"])
+def test_harmonic_hep_parity(lib, orc, arith):
+    n, tgt = 400, 1.0
+    csr = matgen.laplacian_1d(n)
+    v0 = matgen.start_vector(n, 1)
+    kw = dict(hermitian=True, which="TM", nev=4, ncv=30, tol=1e-10, v0=v0, harmonic=True, target=tgt)
+    res = run(csr, arith=arith, **kw)
+    ref = orc.solve(*csr, **kw)
+    assert res["reason"] == 1 and ref.reason == 1
+    ex = 2 - 2 * np.cos(np.arange(1, n + 1) * np.pi / (n + 1))
+    want = ex[np.argsort(np.abs(ex - tgt))][:4]
+    got = np.asarray(res["eigr"][:4])
+    assert np.max(np.abs(got - want) / want) <= 1e-10
+    assert np.max(np.abs(got - np.asarray(ref.eigr[:4])) / want) <= 1e-10
+    assert np.all(np.abs(got[:-1] - tgt) <= np.abs(got[1:] - tgt))  # nearest to the target first
+    check_residuals(csr, res, 1e-10)
+    assert res["eps"].orthogonalityError() <= 1e-12
+
+
+def test_harmonic_nhep_parity(lib, orc):
+    N, Pe, tgt = 20, 2.0, 4.0
+    csr = matgen.convection_diffusion_2d(N, Pe)
+    v0 = matgen.start_vector(N * N, 3)
+    kw = dict(hermitian=False, which="TM", nev=4, ncv=30, tol=1e-10, v0=v0, harmonic=True, target=tgt)
+    res = run(csr, **kw)
+    ref = orc.solve(*csr, **kw)
+    assert res["reason"] == 1 and ref.reason == 1
+    ex = matgen.convdiff_eigenvalues(N, Pe)
+    for v in res["eigr"][:4]:
+        assert np.min(np.abs(ex - v)) <= 1e-10 * abs(v)
+        assert np.min(np.abs(np.asarray(ref.eigr[:4]) - v)) <= 1e-10 * abs(v)
+    assert np.max(np.abs(res["eigi"][:4])) == 0.0
+
+
+@pytest.mark.parametrize("ds", ["refined", "qr"])
+def test_ritz_target_criterion(lib, ds):
+    """EPS_TARGET_MAGNITUDE with Ritz extraction orders by distance to the target in both symmetric projected
+    solvers: a target below the spectrum selects the smallest eigenvalues, nearest first."""
+    n = 100
+    csr = matgen.laplacian_1d(n)
+    res = run(csr, hermitian=True, which="TM", nev=4, ncv=20, tol=1e-10, v0=matgen.start_vector(n, 1), target=-0.5,
+              ds=ds)
+    assert res["reason"] == 1
+    ex = np.sort(2 - 2 * np.cos(np.arange(1, n + 1) * np.pi / (n + 1)))[:4]
+    assert np.max(np.abs(np.asarray(res["eigr"][:4]) - ex) / ex) <= 1e-10
+
+
+def test_batch_rejects_targets(lib):
+    csr = matgen.laplacian_1d(200)
+    A = sg.Mat(*csr)
+    eps = sg.EPS().create()
+    eps.setOperators(A)
+    eps.setProblemType(sg.EPS.ProblemType.HEP)
+    eps.setDimensions(4, 20)
+    eps.setWhichEigenpairs("TM")
+    eps.setTarget(1.0)
+    eps.setExtraction("harmonic")
+    with pytest.raises(sg.SlepcError) as e:
+        sg.solve_batch([eps])
+    assert e.value.code == 56  # PETSC_ERR_SUP

@@ -151,3 +151,25 @@ def test_spmv(orc):
     x = matgen.start_vector(400, 9)
     A = matgen.csr_to_dense(*csr)
     assert np.allclose(orc.spmv(*csr, x), A @ x, rtol=0, atol=1e-14)
+
+
+@pytest.mark.parametrize("lock", [True, False])
+def test_test2_interior_harmonic_golden(orc, lock):
+    """src/eps/tests/test2.c third solve: EPS_TARGET_MAGNITUDE, target 2.1, EPSSetExtraction(EPS_HARMONIC)."""
+    g = G["test2_1"]
+    csr = matgen.laplacian_1d(g["n"])
+    r = orc.solve(*csr, hermitian=True, which="TM", nev=g["nev"], tol=g["tol"], v0=matgen.start_vector(g["n"], 1),
+                  harmonic=True, target=g["target"], lock=lock)
+    assert r.err == 0 and r.reason == 1
+    assert [round(v, 5) for v in r.eigr[:4]] == g["interior"]
+
+
+def test_harmonic_interior_analytic(orc):
+    n, tgt = 200, 2.1
+    csr = matgen.laplacian_1d(n)
+    r = orc.solve(*csr, hermitian=True, which="TM", nev=4, ncv=24, tol=1e-10, v0=matgen.start_vector(n, 1),
+                  harmonic=True, target=tgt)
+    assert r.err == 0 and r.reason == 1
+    ex = 2 - 2 * np.cos(np.arange(1, n + 1) * np.pi / (n + 1))
+    want = ex[np.argsort(np.abs(ex - tgt))][:4]
+    assert np.max(np.abs(np.asarray(r.eigr[:4]) - want) / want) < 1e-12
