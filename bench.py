@@ -232,6 +232,15 @@ def run_batch(args):
         e._A = A
         return e
 
+    if args.profile_solve:
+        # the ncu launch-list case: one batched solve with the default tuning table
+        eps = [make(c, sd) for c, sd in inst]
+        for e in eps:
+            e.setUp()
+        sg.solve_batch(eps)
+        print(json.dumps({"profile_solve": "batch", "instances": count,
+                          "converged": sum(1 for e in eps if e.getConvergedReason() == 1)}), flush=True)
+        return
     t = time.time()
     tuning = sg.batch_tune(1, 7) if not args.no_tune else sg.batch_get_tuning()
     tune_s = time.time() - t

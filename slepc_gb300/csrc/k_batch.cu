@@ -195,9 +195,10 @@ __global__ void __launch_bounds__(B_THREADS, 2) k_batch_update(const BatchInst *
 
 // Thick restart V(:, nconv : k+l) = V(:, nconv : nv) Q(nconv : nv, nconv : k+l), then the residual column moves to
 // column k+l (krylovschur.c:300-329), for every instance whose projected problem was solved this cycle.
-template <int STO>
-__global__ void __launch_bounds__(R_THREADS, 1) k_batch_restart(const BatchInst *I, const BatchVB *map,
+template <int STO, int CQ>
+__global__ void __launch_bounds__(R_THREADS, 2) k_batch_restart(const BatchInst *I, const BatchVB *map,
                                                                 const BatchHdr *h) {
+  constexpr int TR = restart_tile_rows<CQ>();
   const int nmap = h->n_rst;
   for (int v = blockIdx.x; v < nmap; v += gridDim.x) {
     const BatchVB m = map[v];
@@ -210,18 +211,19 @@ __global__ void __launch_bounds__(R_THREADS, 1) k_batch_restart(const BatchInst 
     __syncthreads();
     if (K > 0 && N > 0) {
       if (STO == STORE_F32)
-        restart_body<PairAr, StF32>(static_cast<float *>(batch_col(p, 0)), p.ldv, p.n, nconv, K, nconv, N, p.Q, p.ld,
-                                    m.b, m.nb);
+        restart_body<PairAr, StF32, CQ>(static_cast<float *>(batch_col(p, 0)), p.ldv, p.n, nconv, K, nconv, N, p.Q,
+                                        p.ld, m.b, m.nb);
       else
-        restart_body<PairAr, StPair>(p.V, p.ldv, p.n, nconv, K, nconv, N, p.Q, p.ld, m.b, m.nb);
+        restart_body<PairAr, StPair, CQ>(p.V, p.ldv, p.n, nconv, K, nconv, N, p.Q, p.ld, m.b, m.nb);
     }
     if (c.reason == 0 && !(c.breakdown || k == nv)) {
-      // this virtual block's rows only: the restart above already consumed column k+l for them
-      const int ntiles = (p.n + R_ROWS - 1) / R_ROWS;
+      // this virtual block's rows only (the restart's row tiles): the restart above already consumed column k+l
+      // for them
+      const int ntiles = (p.n + TR - 1) / TR;
       const bool f32 = STO == STORE_F32;
       for (int t = m.b; t < ntiles; t += m.nb) {
-        const int r = t * R_ROWS + threadIdx.x;
-        if (threadIdx.x < R_ROWS && r < p.n) {
+        const int rend = min(p.n, (t + 1) * TR);
+        for (int r = t * TR + threadIdx.x; r < rend; r += R_THREADS) {
           if (f32) static_cast<float *>(batch_col(p, k + l))[r] = static_cast<const float *>(batch_col(p, nv))[r];
           else static_cast<float2 *>(batch_col(p, k + l))[r] = static_cast<const float2 *>(batch_col(p, nv))[r];
         }
@@ -306,21 +308,43 @@ cudaError_t launch_batch_update(const BatchInst *I, const BatchVB *map, const Ba
   return cudaGetLastError();
 }
 
+// the restart variant for the engine's widest instance: N <= max_ld - 1 columns
+template <int CQ>
+static size_t batch_restart_smem(int max_ld) { return restart_smem_bytes(max_ld, max_ld, restart_tile_rows<CQ>()); }
+
+template <int CQ>
+static cudaError_t batch_restart_attrs(int max_ld) {
+  const int shm = (int)batch_restart_smem<CQ>(max_ld);
+  cudaError_t e = cudaFuncSetAttribute(k_batch_restart<STORE_PAIR, CQ>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_batch_restart<STORE_F32, CQ>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm);
+}
+
+template <int CQ>
+static cudaError_t batch_restart_go(const BatchInst *I, const BatchVB *map, const BatchHdr *h, int grid, int max_ld,
+                                    cudaStream_t s, int storage) {
+  const size_t shm = batch_restart_smem<CQ>(max_ld);
+  if (storage == STORE_F32) k_batch_restart<STORE_F32, CQ><<<grid, R_THREADS, shm, s>>>(I, map, h);
+  else k_batch_restart<STORE_PAIR, CQ><<<grid, R_THREADS, shm, s>>>(I, map, h);
+  return cudaGetLastError();
+}
+
 // kernel attributes, set before a cycle is captured
 cudaError_t batch_prepare_restart(int max_ld) {
-  cudaError_t e = cudaFuncSetAttribute(k_batch_restart<STORE_PAIR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)restart_smem_bytes(max_ld, max_ld));
-  if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_batch_restart<STORE_F32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)restart_smem_bytes(max_ld, max_ld));
+  const int nmax = max_ld - 1;
+  if (nmax <= 16) return batch_restart_attrs<1>(max_ld);
+  if (nmax <= 32) return batch_restart_attrs<2>(max_ld);
+  if (nmax <= 64) return batch_restart_attrs<4>(max_ld);
+  return batch_restart_attrs<9>(max_ld);
 }
 
 cudaError_t launch_batch_restart(const BatchInst *I, const BatchVB *map, const BatchHdr *h, int grid, int max_ld,
                                  cudaStream_t s, int storage) {
-  const size_t shm = restart_smem_bytes(max_ld, max_ld);
-  if (storage == STORE_F32) k_batch_restart<STORE_F32><<<grid, R_THREADS, shm, s>>>(I, map, h);
-  else k_batch_restart<STORE_PAIR><<<grid, R_THREADS, shm, s>>>(I, map, h);
-  return cudaGetLastError();
+  const int nmax = max_ld - 1;
+  if (nmax <= 16) return batch_restart_go<1>(I, map, h, grid, max_ld, s, storage);
+  if (nmax <= 32) return batch_restart_go<2>(I, map, h, grid, max_ld, s, storage);
+  if (nmax <= 64) return batch_restart_go<4>(I, map, h, grid, max_ld, s, storage);
+  return batch_restart_go<9>(I, map, h, grid, max_ld, s, storage);
 }
 
 cudaError_t launch_batch_control(BatchInst *I, const int *list, const BatchHdr *h, BatchStatus *status,

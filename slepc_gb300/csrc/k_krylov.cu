@@ -387,38 +387,46 @@ cudaError_t launch_gs_update(const StepArgs &a, int nx, int mode, int arith, cud
   return cudaGetLastError();
 }
 
-size_t restart_smem_bytes(int K, int N) { return ((size_t)K * N + (size_t)K * R_ROWS) * 8; }
+size_t restart_smem_bytes(int K, int N, int tile_rows) { return ((size_t)K * N + (size_t)K * tile_rows) * 8; }
+
+// one restart launch with CQ column chunks (N <= 16 CQ)
+template <class Ar, class S, int CQ>
+static cudaError_t restart_go(typename S::T *V, long long ldv, int n, int a0, int K, int s0, int N, const double *Q,
+                              int ldq, cudaStream_t s) {
+  constexpr int TR = restart_tile_rows<CQ>();
+  const size_t shm = restart_smem_bytes(K, N, TR);
+  if (shm > 227 * 1024) return cudaErrorInvalidValue;
+  const int ntiles = (n + TR - 1) / TR;
+  // two resident blocks per SM when shared memory allows
+  const int per_sm = shm * 2 <= (size_t)227 * 1024 ? 2 : 1;
+  int blocks = num_sms() * per_sm;
+  if (blocks > ntiles) blocks = ntiles;
+  const cudaError_t err = cudaFuncSetAttribute(k_restart<Ar, S, CQ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+  if (err != cudaSuccess) return err;
+  k_restart<Ar, S, CQ><<<blocks, R_THREADS, shm, s>>>(V, ldv, n, a0, K, s0, N, Q, ldq);
+  return cudaGetLastError();
+}
+
+template <class Ar, class S>
+static cudaError_t restart_dispatch(typename S::T *V, long long ldv, int n, int a0, int K, int s0, int N,
+                                    const double *Q, int ldq, cudaStream_t s) {
+  if (N <= 16) return restart_go<Ar, S, 1>(V, ldv, n, a0, K, s0, N, Q, ldq, s);
+  if (N <= 32) return restart_go<Ar, S, 2>(V, ldv, n, a0, K, s0, N, Q, ldq, s);
+  if (N <= 64) return restart_go<Ar, S, 4>(V, ldv, n, a0, K, s0, N, Q, ldq, s);
+  return restart_go<Ar, S, 9>(V, ldv, n, a0, K, s0, N, Q, ldq, s);
+}
 
 cudaError_t launch_restart(void *V, long long ldv, int n, int a0, int K, int s0, int N, const double *Q, int ldq,
                            int arith, cudaStream_t s, int storage) {
   if (N <= 0 || K <= 0) return cudaSuccess;
   if (N > R_MAXN) return cudaErrorInvalidValue;
-  const size_t shm = restart_smem_bytes(K, N);
-  if (shm > 227 * 1024) return cudaErrorInvalidValue;
-  const int ntiles = (n + R_ROWS - 1) / R_ROWS;
-  // two resident blocks per SM when shared memory allows (128 registers x 256 threads leaves room for two)
-  const int per_sm = shm * 2 <= (size_t)227 * 1024 ? 2 : 1;
-  int blocks = num_sms() * per_sm;
-  if (blocks > ntiles) blocks = ntiles;
-  cudaError_t err;
-  if (storage == STORE_F32) {
-    err = cudaFuncSetAttribute(k_restart<PairAr, StF32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
-    if (err != cudaSuccess) return err;
-    k_restart<PairAr, StF32><<<blocks, R_THREADS, shm, s>>>(static_cast<float *>(V), ldv, n, a0, K, s0, N, Q, ldq);
-  } else if (storage == STORE_PAIR) {
-    err = cudaFuncSetAttribute(k_restart<PairAr, StPair>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
-    if (err != cudaSuccess) return err;
-    k_restart<PairAr, StPair><<<blocks, R_THREADS, shm, s>>>(static_cast<float2 *>(V), ldv, n, a0, K, s0, N, Q, ldq);
-  } else if (arith == ARITH_F64) {
-    err = cudaFuncSetAttribute(k_restart<F64Ar, StF64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
-    if (err != cudaSuccess) return err;
-    k_restart<F64Ar, StF64><<<blocks, R_THREADS, shm, s>>>(static_cast<double *>(V), ldv, n, a0, K, s0, N, Q, ldq);
-  } else {
-    err = cudaFuncSetAttribute(k_restart<PairAr, StF64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
-    if (err != cudaSuccess) return err;
-    k_restart<PairAr, StF64><<<blocks, R_THREADS, shm, s>>>(static_cast<double *>(V), ldv, n, a0, K, s0, N, Q, ldq);
-  }
-  return cudaGetLastError();
+  if (storage == STORE_F32)
+    return restart_dispatch<PairAr, StF32>(static_cast<float *>(V), ldv, n, a0, K, s0, N, Q, ldq, s);
+  if (storage == STORE_PAIR)
+    return restart_dispatch<PairAr, StPair>(static_cast<float2 *>(V), ldv, n, a0, K, s0, N, Q, ldq, s);
+  if (arith == ARITH_F64)
+    return restart_dispatch<F64Ar, StF64>(static_cast<double *>(V), ldv, n, a0, K, s0, N, Q, ldq, s);
+  return restart_dispatch<PairAr, StF64>(static_cast<double *>(V), ldv, n, a0, K, s0, N, Q, ldq, s);
 }
 
 cudaError_t launch_segment_begin(KrylovState *st, int k0, int m, cudaStream_t s) {

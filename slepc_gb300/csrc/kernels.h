@@ -62,7 +62,7 @@ int spmv_lanes_for(double avg_nnz);
 int gs_dot_blocks(int n);
 int gs_update_blocks(int n);
 int gs_max_columns();
-size_t restart_smem_bytes(int K, int N);
+size_t restart_smem_bytes(int K, int N, int tile_rows);
 
 cudaError_t launch_spmv(const int *rp, const int *ci, const double *va, const double *x, double *y, int n, int lanes,
                         const KrylovState *st, double scale, cudaStream_t s);

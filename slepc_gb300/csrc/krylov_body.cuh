@@ -765,46 +765,64 @@ constexpr int R_THREADS = 256;
 constexpr int R_ROWS = 32;
 constexpr int R_MAXN = 144;
 
-template <class Ar, class S>
+// Thread (ty, tx) of a restart block owns rows 2ty + 32p and 2ty + 1 + 32p of a tile (p < RP) and columns
+// tx + 16q (q < CQ): CQ = ceil(N / 16) column chunks, and RP row pairs per thread, more when N is small, so a tile
+// holds 32 RP rows.  Every output element is one thread's sum over k in increasing order, whatever the tiling.
+template <int CQ>
+__host__ __device__ constexpr int restart_rp() { return CQ <= 2 ? 4 : (CQ <= 4 ? 2 : 1); }
+template <int CQ>
+__host__ __device__ constexpr int restart_tile_rows() { return 32 * restart_rp<CQ>(); }
+
+template <class Ar, class S, int CQ>
 KS_DEVICE void restart_body(typename S::T *V, long long ldv, int n, int a0, int K, int s0, int N, const double *Q,
                             int ldq, int bid, int nblk) {
   using val = typename Ar::val;
   using acc = typename Ar::acc;
+  constexpr int RP = restart_rp<CQ>(), TR = restart_tile_rows<CQ>();
   extern __shared__ __align__(16) unsigned char smraw[];
   val *Qs = reinterpret_cast<val *>(smraw);  // K x N, row k contiguous
-  val *Vt = Qs + (size_t)K * N;              // K x R_ROWS, column k contiguous
+  val *Vt = Qs + (size_t)K * N;              // K x TR, column k contiguous
   const int tid = threadIdx.x;
   for (int i = tid; i < K * N; i += R_THREADS) {
     const int k = i / N, c = i % N;
     Qs[i] = Ar::cvt(Q[(a0 + k) + (size_t)(s0 + c) * ldq]);
   }
-  const int ty = tid / 16, tx = tid % 16;  // rows 2ty, 2ty+1; columns tx + 16q
-  constexpr int CQ = (R_MAXN + 15) / 16;
-  const int ntiles = (n + R_ROWS - 1) / R_ROWS;
+  const int ty = tid / 16, tx = tid % 16;
+  const int ntiles = (n + TR - 1) / TR;
   for (int t = bid; t < ntiles; t += nblk) {
-    const int r0 = t * R_ROWS;
-    const int rows = min(R_ROWS, n - r0);
+    const int r0 = t * TR;
+    const int rows = min(TR, n - r0);
     __syncthreads();
-    for (int i = tid; i < K * R_ROWS; i += R_THREADS) {
-      const int k = i / R_ROWS, r = i % R_ROWS;
+    for (int i = tid; i < K * TR; i += R_THREADS) {
+      const int k = i / TR, r = i % TR;
       Vt[i] = (r < rows) ? S::template load1<Ar>(V + (r0 + r) + (size_t)(a0 + k) * ldv) : Ar::cvt(0.0);
     }
     __syncthreads();
-    acc o0[CQ], o1[CQ];
+    acc o0[CQ][RP], o1[CQ][RP];
 #pragma unroll
-    for (int q = 0; q < CQ; ++q) {
-      Ar::zero(o0[q]);
-      Ar::zero(o1[q]);
-    }
+    for (int q = 0; q < CQ; ++q)
+#pragma unroll
+      for (int p = 0; p < RP; ++p) {
+        Ar::zero(o0[q][p]);
+        Ar::zero(o1[q][p]);
+      }
     for (int k = 0; k < K; ++k) {
-      const val v0 = Vt[k * R_ROWS + 2 * ty], v1 = Vt[k * R_ROWS + 2 * ty + 1];
+      val v0[RP], v1[RP];
+#pragma unroll
+      for (int p = 0; p < RP; ++p) {
+        v0[p] = Vt[k * TR + 2 * ty + 32 * p];
+        v1[p] = Vt[k * TR + 2 * ty + 1 + 32 * p];
+      }
 #pragma unroll
       for (int q = 0; q < CQ; ++q) {
         const int c = tx + 16 * q;
         if (c < N) {
           const val qq = Qs[k * N + c];
-          Ar::fma(o0[q], v0, qq);
-          Ar::fma(o1[q], v1, qq);
+#pragma unroll
+          for (int p = 0; p < RP; ++p) {
+            Ar::fma(o0[q][p], v0[p], qq);
+            Ar::fma(o1[q][p], v1[p], qq);
+          }
         }
       }
     }
@@ -813,17 +831,21 @@ KS_DEVICE void restart_body(typename S::T *V, long long ldv, int n, int a0, int 
     for (int q = 0; q < CQ; ++q) {
       const int c = tx + 16 * q;
       if (c < N) {
-        if (2 * ty < rows) S::put(V + (r0 + 2 * ty) + (size_t)(s0 + c) * ldv, Ar::value(o0[q]));
-        if (2 * ty + 1 < rows) S::put(V + (r0 + 2 * ty + 1) + (size_t)(s0 + c) * ldv, Ar::value(o1[q]));
+#pragma unroll
+        for (int p = 0; p < RP; ++p) {
+          const int r = 2 * ty + 32 * p;
+          if (r < rows) S::put(V + (r0 + r) + (size_t)(s0 + c) * ldv, Ar::value(o0[q][p]));
+          if (r + 1 < rows) S::put(V + (r0 + r + 1) + (size_t)(s0 + c) * ldv, Ar::value(o1[q][p]));
+        }
       }
     }
   }
 }
 
-template <class Ar, class S>
-__global__ void __launch_bounds__(R_THREADS, 1) k_restart(typename S::T *V, long long ldv, int n, int a0, int K,
+template <class Ar, class S, int CQ>
+__global__ void __launch_bounds__(R_THREADS, 2) k_restart(typename S::T *V, long long ldv, int n, int a0, int K,
                                                           int s0, int N, const double *Q, int ldq) {
-  restart_body<Ar, S>(V, ldv, n, a0, K, s0, N, Q, ldq, blockIdx.x, gridDim.x);
+  restart_body<Ar, S, CQ>(V, ldv, n, a0, K, s0, N, Q, ldq, blockIdx.x, gridDim.x);
 }
 
 }  // namespace ksg
