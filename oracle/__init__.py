@@ -1,6 +1,6 @@
 """The oracle: a CPU restatement of SLEPc 3.22's Krylov-Schur path (ks_oracle.c), loaded through ctypes.
 
-TEST INFRASTRUCTURE ONLY.  It is the checker the CUDA path is compared against and the timed CPU baseline.
+TEST INFRASTRUCTURE ONLY.  It is what the CUDA path is compared against in the tests, and the timed CPU baseline.
 Only tests/, __graft_entry__.smoke() and bench.py (its cpu_baseline leg and its reference arm) may import it;
 the product package slepc_gb300 never does.
 

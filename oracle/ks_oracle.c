@@ -1,7 +1,7 @@
 /*
  * ks_oracle.c -- CPU restatement of SLEPc 3.22's Krylov-Schur path, used as the ORACLE.
  *
- * TEST INFRASTRUCTURE ONLY: the checker for the CUDA path and the timed CPU baseline.  Nothing under
+ * TEST INFRASTRUCTURE ONLY: the reference results for the CUDA path's tests and the timed CPU baseline.  Nothing under
  * slepc_gb300/ links, loads or calls this file.  Written from the reference's algorithms in our own code:
  *
  *   Krylov-Schur restart loop ........ src/eps/impls/krylov/krylovschur/krylovschur.c:227-337

@@ -1,7 +1,7 @@
 /*
  * ks_oracle.h -- CPU restatement of SLEPc 3.22's Krylov-Schur path (the oracle).
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker the CUDA path is compared against and the
+ * TEST INFRASTRUCTURE ONLY.  This library is what the CUDA path is compared against in the tests, and the
  * timed CPU baseline.  Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline / reference arm may
  * load it.  The product (slepc_gb300/) never links, loads or calls it.
  *

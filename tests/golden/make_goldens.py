@@ -1,5 +1,5 @@
 """Regenerate reference_outputs.json from the reference's expected-output files (run in the build container only;
-the GPU machine uses the committed JSON).  Only the printed eigenvalues/norms of the Krylov-Schur-path tests are
+other machines use the committed JSON).  Only the printed eigenvalues/norms of the Krylov-Schur-path tests are
 extracted; each entry records the file it came from and the options of that test.  The real matrix those tests
 read from a PETSc binary file (share/slepc/datafiles/matrices/rdb200.petsc) is converted to CSR arrays in
 rdb200.npz by an independent big-endian reader."""
