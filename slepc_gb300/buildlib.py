@@ -18,7 +18,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libslepc_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
-         "-Xcompiler", "-Wall", "-I", os.path.join(HERE, "..", "include")]
+         "-Xcompiler", "-Wall", "-Xcompiler", "-fopenmp", "-I", os.path.join(HERE, "..", "include")]
 
 
 def nvcc() -> str:
@@ -81,7 +81,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags=None) -> str:
             list(ex.map(compile_one, jobs))
     objs = [os.path.join(BUILD, os.path.basename(s) + ".o") for s in srcs]
     if force or jobs or not os.path.exists(LIB):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs + ["-lcudart"]
+        cmd = [nvcc()] + ARCH + ["-shared", "-Xcompiler", "-fopenmp", "-o", LIB + ".tmp"] + objs + ["-lcudart"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

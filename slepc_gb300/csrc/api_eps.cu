@@ -71,13 +71,22 @@ extern "C" PetscErrorCode MatCreateSeqAIJWithArrays(MPI_Comm, PetscInt m, PetscI
   KSG_CHECK(m >= 0 && n >= 0, PETSC_ERR_ARG_OUTOFRANGE, "Negative dimension");
   KSG_CHECK(i && (i[m] == 0 || (j && a)), PETSC_ERR_ARG_NULL, "Null CSR array");
   KSG_CHECK(i[0] == 0, PETSC_ERR_ARG_WRONG, "i (row pointers) must start with 0");
-  for (int r = 0; r < m; ++r) {
+  for (int r = 0; r < m; ++r)
     KSG_CHECK(i[r + 1] >= i[r], PETSC_ERR_ARG_WRONG, "Row pointers must be nondecreasing (row %d)", r);
-    for (int p = i[r]; p < i[r + 1]; ++p) {
-      KSG_CHECK(j[p] >= 0 && j[p] < n, PETSC_ERR_ARG_OUTOFRANGE, "Column index %d out of range in row %d", j[p], r);
-      KSG_CHECK(isfinite(a[p]), PETSC_ERR_ARG_WRONG, "Matrix entry (%d,%d) is not finite", r, j[p]);
+  // entries checked in parallel; the first failing row (in row order) is the one reported
+  int bad = m;
+#pragma omp parallel for reduction(min : bad) schedule(static)
+  for (int r = 0; r < m; ++r)
+    for (int p = i[r]; p < i[r + 1]; ++p)
+      if (!(j[p] >= 0 && j[p] < n) || !isfinite(a[p])) {
+        bad = std::min(bad, r);
+        break;
+      }
+  if (bad < m)
+    for (int p = i[bad]; p < i[bad + 1]; ++p) {
+      KSG_CHECK(j[p] >= 0 && j[p] < n, PETSC_ERR_ARG_OUTOFRANGE, "Column index %d out of range in row %d", j[p], bad);
+      KSG_CHECK(isfinite(a[p]), PETSC_ERR_ARG_WRONG, "Matrix entry (%d,%d) is not finite", bad, j[p]);
     }
-  }
   Mat M = new _p_Mat();
   M->m = m;
   M->n = n;
@@ -187,13 +196,11 @@ PetscErrorCode ksg_mat_upload(Mat A) {
 PetscErrorCode ksg_mat_upload_pairs(Mat A) {
   KSG_TRY(ksg_mat_upload(A));
   if (A->d_va2.p || A->nnz == 0) return 0;
-  std::vector<float2> h(A->nnz);
-  for (long long p = 0; p < A->nnz; ++p) {
-    const float hi = (float)A->aa[p];
-    h[p] = make_float2(hi, (float)(A->aa[p] - (double)hi));
-  }
+  // split on the device from the FP64 values already there (hi = fl32(v), lo = fl32(v - hi)); the solver streams do
+  // not order themselves after the legacy stream, hence the synchronisation
   KSG_CUDA(A->d_va2.alloc(A->nnz));
-  KSG_CUDA(cudaMemcpy(A->d_va2.p, h.data(), sizeof(float2) * A->nnz, cudaMemcpyHostToDevice));
+  KSG_CUDA(launch_f64_to_pair(A->d_va.p, A->d_va2.p, A->nnz, 0));
+  KSG_CUDA(cudaStreamSynchronize(0));
   return 0;
 }
 
@@ -204,10 +211,9 @@ void *ksg_col(void *V, long long ldv, int j, int storage) {
 PetscErrorCode ksg_mat_upload_f32(Mat A) {
   KSG_TRY(ksg_mat_upload(A));
   if (A->d_va32.p || A->nnz == 0) return 0;
-  std::vector<float> h(A->nnz);
-  for (long long p = 0; p < A->nnz; ++p) h[p] = (float)A->aa[p];
   KSG_CUDA(A->d_va32.alloc(A->nnz));
-  KSG_CUDA(cudaMemcpy(A->d_va32.p, h.data(), sizeof(float) * A->nnz, cudaMemcpyHostToDevice));
+  KSG_CUDA(launch_f64_to_f32(A->d_va.p, A->d_va32.p, A->nnz, 0));
+  KSG_CUDA(cudaStreamSynchronize(0));
   return 0;
 }
 
@@ -263,6 +269,8 @@ double ksg_mat_norm_inf(Mat A) {
       mx = std::max(mx, s);
     }
   } else {
+    // rows in parallel; each row summed in order, so the maximum is the same as a sequential pass
+#pragma omp parallel for reduction(max : mx) schedule(static)
     for (int r = 0; r < A->m; ++r) {
       double s = 0.0;
       for (int p = A->ai[r]; p < A->ai[r + 1]; ++p) s += fabs(A->aa[p]);
