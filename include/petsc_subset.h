@@ -113,6 +113,23 @@ PetscErrorCode MatView(Mat A, PetscViewer viewer);
 PetscErrorCode VecLoad(Vec x, PetscViewer viewer);
 PetscErrorCode VecView(Vec x, PetscViewer viewer);
 
+/* --- ASCII viewers (petscviewer.h): text reports on stdout or a file, with a format stack.  The format names are
+ * PETSc's; only DEFAULT, ASCII_INFO, ASCII_INFO_DETAIL and FAILED change what the EPS reports print.  Binary-file
+ * calls (MatLoad, MatView, VecLoad, VecView) on an ASCII viewer return PETSC_ERR_SUP. --- */
+typedef enum { PETSC_VIEWER_DEFAULT, PETSC_VIEWER_ASCII_MATLAB, PETSC_VIEWER_ASCII_MATHEMATICA, PETSC_VIEWER_ASCII_IMPL,
+               PETSC_VIEWER_ASCII_INFO, PETSC_VIEWER_ASCII_INFO_DETAIL, PETSC_VIEWER_ASCII_COMMON,
+               PETSC_VIEWER_ASCII_SYMMODU, PETSC_VIEWER_ASCII_INDEX, PETSC_VIEWER_ASCII_DENSE,
+               PETSC_VIEWER_ASCII_MATRIXMARKET, PETSC_VIEWER_FAILED } PetscViewerFormat;
+PetscViewer PETSC_VIEWER_STDOUT_(MPI_Comm comm);
+#define PETSC_VIEWER_STDOUT_WORLD PETSC_VIEWER_STDOUT_(PETSC_COMM_WORLD)
+#define PETSC_VIEWER_STDOUT_SELF PETSC_VIEWER_STDOUT_(PETSC_COMM_SELF)
+PetscErrorCode PetscViewerASCIIGetStdout(MPI_Comm comm, PetscViewer *viewer);
+PetscErrorCode PetscViewerASCIIOpen(MPI_Comm comm, const char name[], PetscViewer *viewer);
+PetscErrorCode PetscViewerPushFormat(PetscViewer viewer, PetscViewerFormat format);
+PetscErrorCode PetscViewerPopFormat(PetscViewer viewer);
+PetscErrorCode PetscViewerGetFormat(PetscViewer viewer, PetscViewerFormat *format);
+PetscErrorCode PetscViewerASCIIPrintf(PetscViewer viewer, const char format[], ...);
+
 /* --- Vec (petscvec.h) --- */
 PetscErrorCode VecCreateSeq(MPI_Comm comm, PetscInt n, Vec *v);
 PetscErrorCode VecCreateSeqWithArray(MPI_Comm comm, PetscInt bs, PetscInt n, const PetscScalar array[], Vec *v);

@@ -80,6 +80,10 @@ PetscErrorCode EPSGetEigenvalue(EPS eps, PetscInt i, PetscScalar *eigr, PetscSca
 PetscErrorCode EPSGetEigenvector(EPS eps, PetscInt i, Vec Vr, Vec Vi);
 PetscErrorCode EPSGetErrorEstimate(EPS eps, PetscInt i, PetscReal *errest);
 PetscErrorCode EPSComputeError(EPS eps, PetscInt i, EPSErrorType type, PetscReal *error);
+/* text reports of the solution (epsview.c:243-262, 297-447, 603-617); a NULL viewer means stdout */
+PetscErrorCode EPSConvergedReasonView(EPS eps, PetscViewer viewer);
+PetscErrorCode EPSErrorView(EPS eps, EPSErrorType etype, PetscViewer viewer);
+PetscErrorCode EPSValuesView(EPS eps, PetscViewer viewer);
 PetscErrorCode EPSGetBV(EPS eps, BV *V);
 PetscErrorCode EPSGetDS(EPS eps, DS *ds);
 

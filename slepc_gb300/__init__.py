@@ -96,6 +96,12 @@ def load():
         "MatCreate": ([I, PP], I),
         "MatLoad": ([P, P], I),
         "MatView": ([P, P], I),
+        "PetscViewerASCIIOpen": ([I, ctypes.c_char_p, PP], I),
+        "PetscViewerPushFormat": ([P, I], I),
+        "PetscViewerPopFormat": ([P], I),
+        "EPSErrorView": ([P, I, P], I),
+        "EPSConvergedReasonView": ([P, P], I),
+        "EPSValuesView": ([P, P], I),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -406,6 +412,40 @@ class EPS:
         v = ctypes.c_double()
         _check(load().EPSComputeError(self.handle, int(i), int(etype), ctypes.byref(v)), "EPSComputeError")
         return v.value
+
+    # text reports through an ASCII viewer (petsc4py: EPS.errorView / valuesView / convergedReasonView).  With
+    # path=None the text is returned (written through a temporary ASCII viewer); otherwise it goes to that file, or
+    # to the process's stdout for path="stdout".  detail=True pushes PETSC_VIEWER_ASCII_INFO_DETAIL.
+    def _view(self, fn, args, path, detail):
+        import tempfile
+        lib = load()
+        tmp = None
+        if path is None:
+            fd, tmp = tempfile.mkstemp(suffix=".txt")
+            os.close(fd)
+        viewer = ctypes.c_void_p()
+        _check(lib.PetscViewerASCIIOpen(0, os.fsencode(tmp or path), ctypes.byref(viewer)), "PetscViewerASCIIOpen")
+        try:
+            if detail:
+                _check(lib.PetscViewerPushFormat(viewer, 5), "PetscViewerPushFormat")
+            _check(getattr(lib, fn)(self.handle, *args, viewer), fn)
+        finally:
+            _check(lib.PetscViewerDestroy(ctypes.byref(viewer)), "PetscViewerDestroy")
+        if tmp is None:
+            return None
+        with open(tmp) as f:
+            text = f.read()
+        os.unlink(tmp)
+        return text
+
+    def errorView(self, etype=ErrorType.RELATIVE, path=None, detail=False):
+        return self._view("EPSErrorView", (int(etype),), path, detail)
+
+    def convergedReasonView(self, path=None):
+        return self._view("EPSConvergedReasonView", (), path, False)
+
+    def valuesView(self, path=None):
+        return self._view("EPSValuesView", (), path, False)
 
     def getStats(self):
         buf = (ctypes.c_char * 80)()

@@ -1,4 +1,5 @@
-// api_io.cu -- PETSc binary matrix and vector files (PetscViewerBinaryOpen, MatLoad, MatView, VecLoad, VecView).
+// api_io.cu -- viewers: PETSc binary matrix and vector files (PetscViewerBinaryOpen, MatLoad, MatView, VecLoad,
+// VecView) and the ASCII result reports of EPS (EPSErrorView, EPSConvergedReasonView, EPSValuesView).
 //
 // The reference's tutorials read their operators this way (src/eps/tutorials/ex4.c:45-49, ex7.c:52, ex31.c:551-562),
 // and its data files (share/slepc/datafiles/matrices/*.petsc) use PETSc's binary format: every item big-endian,
@@ -9,6 +10,7 @@
 // matrix owns its CSR arrays; everything else about it (device upload on first solve, MatMult, MatDestroy) is the
 // same as for MatCreateSeqAIJWithArrays.
 #include <cmath>
+#include <cstdarg>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -20,6 +22,9 @@ struct _p_PetscViewer {
   FILE *f = nullptr;
   PetscFileMode mode = FILE_MODE_READ;
   std::string name;
+  int ascii = 0;     // PETSCVIEWERASCII (text reports) rather than PETSCVIEWERBINARY
+  int borrowed = 0;  // the process-wide stdout viewer: never closed, PetscViewerDestroy only clears the handle
+  std::vector<PetscViewerFormat> formats;  // PetscViewerPushFormat stack
 };
 
 namespace {
@@ -78,7 +83,11 @@ extern "C" PetscErrorCode PetscViewerBinaryOpen(MPI_Comm, const char name[], Pet
 extern "C" PetscErrorCode PetscViewerDestroy(PetscViewer *viewer) {
   if (!viewer || !*viewer) return 0;
   PetscViewer v = *viewer;
-  const int rc = v->f ? std::fclose(v->f) : 0;
+  if (v->borrowed) {
+    *viewer = nullptr;
+    return 0;
+  }
+  const int rc = (v->f && v->f != stdout && v->f != stderr) ? std::fclose(v->f) : 0;
   const std::string name = v->name;
   delete v;
   *viewer = nullptr;
@@ -143,6 +152,7 @@ extern "C" PetscErrorCode MatSeqAIJRestoreArrayRead(Mat A, const PetscScalar *ar
 // MatLoad_SeqAIJ_Binary: rows, columns, row lengths, column indices, values (PETSc's binary format).
 extern "C" PetscErrorCode MatLoad(Mat A, PetscViewer v) {
   KSG_CHECK(A && v, PETSC_ERR_ARG_NULL, "Null argument");
+  KSG_CHECK(!v->ascii, PETSC_ERR_SUP, "Only binary viewers are supported here");
   KSG_CHECK(v->mode == FILE_MODE_READ, PETSC_ERR_ARG_WRONGSTATE, "%s is not open for reading", v->name.c_str());
   KSG_CHECK(A->empty && !A->dense, PETSC_ERR_ARG_WRONGSTATE, "MatLoad needs a Mat from MatCreate that holds no data");
   std::vector<unsigned char> buf;
@@ -195,6 +205,7 @@ extern "C" PetscErrorCode MatLoad(Mat A, PetscViewer v) {
 // MatView with a binary viewer: the same layout MatLoad reads
 extern "C" PetscErrorCode MatView(Mat A, PetscViewer v) {
   KSG_CHECK(A && v, PETSC_ERR_ARG_NULL, "Null argument");
+  KSG_CHECK(!v->ascii, PETSC_ERR_SUP, "Only binary viewers are supported here");
   KSG_CHECK(v->mode != FILE_MODE_READ, PETSC_ERR_ARG_WRONGSTATE, "%s is not open for writing", v->name.c_str());
   KSG_CHECK(!A->dense && !A->empty, PETSC_ERR_SUP, "MatView writes AIJ matrices only");
   std::vector<unsigned char> out;
@@ -213,6 +224,7 @@ extern "C" PetscErrorCode MatView(Mat A, PetscViewer v) {
 
 extern "C" PetscErrorCode VecLoad(Vec x, PetscViewer v) {
   KSG_CHECK(x && v, PETSC_ERR_ARG_NULL, "Null argument");
+  KSG_CHECK(!v->ascii, PETSC_ERR_SUP, "Only binary viewers are supported here");
   KSG_CHECK(v->mode == FILE_MODE_READ, PETSC_ERR_ARG_WRONGSTATE, "%s is not open for reading", v->name.c_str());
   std::vector<unsigned char> buf;
   KSG_TRY(read_bytes(v, 8, buf, "the vector header"));
@@ -234,6 +246,7 @@ extern "C" PetscErrorCode VecLoad(Vec x, PetscViewer v) {
 
 extern "C" PetscErrorCode VecView(Vec x, PetscViewer v) {
   KSG_CHECK(x && v, PETSC_ERR_ARG_NULL, "Null argument");
+  KSG_CHECK(!v->ascii, PETSC_ERR_SUP, "Only binary viewers are supported here");
   KSG_CHECK(v->mode != FILE_MODE_READ, PETSC_ERR_ARG_WRONGSTATE, "%s is not open for writing", v->name.c_str());
   std::vector<unsigned char> out;
   put_be(out, (uint32_t)VEC_FILE_CLASSID, 4);
@@ -242,4 +255,214 @@ extern "C" PetscErrorCode VecView(Vec x, PetscViewer v) {
   KSG_CHECK(std::fwrite(out.data(), 1, out.size(), v->f) == out.size(), PETSC_ERR_FILE_WRITE,
             "%s: write failed", v->name.c_str());
   return 0;
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// ASCII viewers (PetscViewerASCIIOpen, PetscViewerASCIIGetStdout, PETSC_VIEWER_STDOUT_WORLD/SELF) with a format
+// stack, and the EPS result reports the reference's tutorials print (src/eps/interface/epsview.c)
+// ---------------------------------------------------------------------------------------------------------------
+namespace {
+
+_p_PetscViewer *stdout_viewer() {
+  static _p_PetscViewer v = [] {
+    _p_PetscViewer w;
+    w.f = stdout;
+    w.mode = FILE_MODE_WRITE;
+    w.name = "stdout";
+    w.ascii = 1;
+    w.borrowed = 1;
+    return w;
+  }();
+  return &v;
+}
+
+PetscViewerFormat top_format(PetscViewer v) { return v->formats.empty() ? PETSC_VIEWER_DEFAULT : v->formats.back(); }
+
+struct Text {
+  std::string s;
+  void add(const char *fmt, ...) {
+    char buf[256];
+    va_list ap;
+    va_start(ap, fmt);
+    const int n = std::vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (n > 0) s.append(buf, std::min<size_t>((size_t)n, sizeof(buf) - 1));
+  }
+  // one eigenvalue as SlepcPrintEigenvalueASCII prints it (include/slepc/private/slepcimpl.h:92-112): five decimals,
+  // a part below 1e-10 (PETSC_SMALL) of the other printed as zero, real when the imaginary part is zero
+  void eig(double re, double im) {
+    const double small = 1e-10;
+    if (im != 0.0 && std::fabs(re) / std::fabs(im) < small) re = 0.0;
+    if (re != 0.0 && std::fabs(im) / std::fabs(re) < small) im = 0.0;
+    if (im != 0.0) add("%.5f%+.5fi", re, im);
+    else add("%.5f", re);
+  }
+};
+
+PetscErrorCode emit(PetscViewer v, const Text &t) {
+  if (t.s.empty()) return 0;
+  KSG_CHECK(std::fwrite(t.s.data(), 1, t.s.size(), v->f) == t.s.size(), PETSC_ERR_FILE_WRITE, "%s: write failed",
+            v->name.c_str());
+  std::fflush(v->f);
+  return 0;
+}
+
+const char *reason_name(int reason) {
+  switch (reason) {
+    case EPS_CONVERGED_TOL: return "CONVERGED_TOL";
+    case EPS_CONVERGED_USER: return "CONVERGED_USER";
+    case EPS_DIVERGED_ITS: return "DIVERGED_ITS";
+    case EPS_DIVERGED_BREAKDOWN: return "DIVERGED_BREAKDOWN";
+    case EPS_DIVERGED_SYMMETRY_LOST: return "DIVERGED_SYMMETRY_LOST";
+    default: return "CONVERGED_ITERATING";
+  }
+}
+
+}  // namespace
+
+extern "C" PetscViewer PETSC_VIEWER_STDOUT_(MPI_Comm) { return stdout_viewer(); }
+
+extern "C" PetscErrorCode PetscViewerASCIIGetStdout(MPI_Comm, PetscViewer *viewer) {
+  KSG_CHECK(viewer, PETSC_ERR_ARG_NULL, "Null argument");
+  *viewer = stdout_viewer();
+  return 0;
+}
+
+// PetscViewerASCIIOpen: a text file written from the start; the names "stdout" and "stderr" give those streams
+extern "C" PetscErrorCode PetscViewerASCIIOpen(MPI_Comm, const char name[], PetscViewer *viewer) {
+  KSG_CHECK(name && viewer, PETSC_ERR_ARG_NULL, "Null argument");
+  FILE *f = !std::strcmp(name, "stdout") ? stdout : !std::strcmp(name, "stderr") ? stderr : std::fopen(name, "w");
+  KSG_CHECK(f, PETSC_ERR_FILE_OPEN, "Cannot open file %s", name);
+  PetscViewer v = new _p_PetscViewer();
+  v->f = f;
+  v->mode = FILE_MODE_WRITE;
+  v->name = name;
+  v->ascii = 1;
+  *viewer = v;
+  return 0;
+}
+
+extern "C" PetscErrorCode PetscViewerPushFormat(PetscViewer v, PetscViewerFormat format) {
+  KSG_CHECK(v, PETSC_ERR_ARG_NULL, "Null viewer");
+  KSG_CHECK(v->formats.size() < 10, PETSC_ERR_ARG_OUTOFRANGE, "Too many PetscViewerPushFormat() calls");
+  v->formats.push_back(format);
+  return 0;
+}
+
+extern "C" PetscErrorCode PetscViewerPopFormat(PetscViewer v) {
+  KSG_CHECK(v, PETSC_ERR_ARG_NULL, "Null viewer");
+  if (!v->formats.empty()) v->formats.pop_back();
+  return 0;
+}
+
+extern "C" PetscErrorCode PetscViewerGetFormat(PetscViewer v, PetscViewerFormat *format) {
+  KSG_CHECK(v && format, PETSC_ERR_ARG_NULL, "Null argument");
+  *format = top_format(v);
+  return 0;
+}
+
+extern "C" PetscErrorCode PetscViewerASCIIPrintf(PetscViewer v, const char format[], ...) {
+  KSG_CHECK(v && format, PETSC_ERR_ARG_NULL, "Null argument");
+  KSG_CHECK(v->ascii, PETSC_ERR_ARG_WRONG, "%s is not an ASCII viewer", v->name.c_str());
+  va_list ap;
+  va_start(ap, format);
+  const int rc = std::vfprintf(v->f, format, ap);
+  va_end(ap);
+  KSG_CHECK(rc >= 0, PETSC_ERR_FILE_WRITE, "%s: write failed", v->name.c_str());
+  std::fflush(v->f);
+  return 0;
+}
+
+// EPSConvergedReasonView (epsview.c:243-262): one line with the number of converged pairs, the reason and the
+// number of restarts; PETSC_VIEWER_FAILED prints only a failure
+extern "C" PetscErrorCode EPSConvergedReasonView(EPS eps, PetscViewer v) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  if (!v) v = stdout_viewer();
+  if (!v->ascii) return 0;
+  const int nconv = eps->nconv, its = eps->its, reason = eps->reason;  // before EPSSolve: 0, CONVERGED_ITERATING
+  Text t;
+  if (reason > 0 && top_format(v) != PETSC_VIEWER_FAILED)
+    t.add(" Linear eigensolve converged (%d eigenpair%s) due to %s; iterations %d\n", nconv, nconv > 1 ? "s" : "",
+          reason_name(reason), its);
+  else if (reason <= 0)
+    t.add(" Linear eigensolve did not converge due to %s; iterations %d\n", reason_name(reason), its);
+  return emit(v, t);
+}
+
+// EPSErrorView (epsview.c:297-447).  Default / ASCII_INFO format: the first nev eigenvalues, eight to a line, when
+// all of them converged with errors below 5*tol, else a one-line diagnosis.  ASCII_INFO_DETAIL: a table of every
+// converged eigenvalue with its error.  Other formats print nothing.
+extern "C" PetscErrorCode EPSErrorView(EPS eps, EPSErrorType etype, PetscViewer v) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  KSG_CHECK(eps->solved, PETSC_ERR_ORDER, "Must call EPSSolve() first");
+  if (!v) v = stdout_viewer();
+  if (!v->ascii) return 0;
+  PetscInt nconv = 0, nev = 0;
+  PetscReal tol = 0.0;
+  KSG_TRY(EPSGetConverged(eps, &nconv));
+  KSG_TRY(EPSGetDimensions(eps, &nev, nullptr, nullptr));
+  KSG_TRY(EPSGetTolerances(eps, &tol, nullptr));
+  const PetscViewerFormat fmt = top_format(v);
+  Text t;
+  if (fmt == PETSC_VIEWER_DEFAULT || fmt == PETSC_VIEWER_ASCII_INFO) {
+    if (nconv < nev) {
+      t.add(" Problem: less than %d eigenvalues converged\n\n", (int)nev);
+      return emit(v, t);
+    }
+    for (PetscInt i = 0; i < nev; ++i) {
+      PetscReal err = 0.0;
+      KSG_TRY(EPSComputeError(eps, i, etype, &err));
+      if (err >= 5.0 * tol) {
+        t.add(" Problem: some of the first %d relative errors are higher than the tolerance\n\n", (int)nev);
+        return emit(v, t);
+      }
+    }
+    t.add(" All requested eigenvalues computed up to the required tolerance:");
+    for (PetscInt i = 0; i < nev; ++i) {
+      if (i % 8 == 0) t.add("\n     ");
+      PetscScalar kr = 0.0, ki = 0.0;
+      KSG_TRY(EPSGetEigenvalue(eps, i, &kr, &ki));
+      t.eig(kr, ki);
+      if (i + 1 < nev) t.add(", ");
+    }
+    t.add("\n\n");
+  } else if (fmt == PETSC_VIEWER_ASCII_INFO_DETAIL) {
+    if (!nconv) return 0;
+    const char *sep = " ---------------------- --------------------\n";
+    const char *head = etype == EPS_ERROR_ABSOLUTE   ? "   ||Ax-kx||"
+                       : etype == EPS_ERROR_RELATIVE ? "||Ax-kx||/||kx||"
+                                                     : "    eta(x,k)";
+    t.add("%s            k             %s\n%s", sep, head, sep);
+    for (PetscInt i = 0; i < nconv; ++i) {
+      PetscScalar kr = 0.0, ki = 0.0;
+      PetscReal err = 0.0;
+      KSG_TRY(EPSGetEigenvalue(eps, i, &kr, &ki));
+      KSG_TRY(EPSComputeError(eps, i, etype, &err));
+      if (ki != 0.0) t.add("  % 9f%+9fi      %12g\n", kr, ki, err);
+      else t.add("    % 12f           %12g\n", kr, err);
+    }
+    t.add("%s", sep);
+  }
+  return emit(v, t);
+}
+
+// EPSValuesView (epsview.c:603-617), ASCII: every converged eigenvalue on its own line
+extern "C" PetscErrorCode EPSValuesView(EPS eps, PetscViewer v) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  KSG_CHECK(eps->solved, PETSC_ERR_ORDER, "Must call EPSSolve() first");
+  if (!v) v = stdout_viewer();
+  if (!v->ascii) return 0;
+  PetscInt nconv = 0;
+  KSG_TRY(EPSGetConverged(eps, &nconv));
+  Text t;
+  t.add("Eigenvalues = \n");
+  for (PetscInt i = 0; i < nconv; ++i) {
+    PetscScalar kr = 0.0, ki = 0.0;
+    KSG_TRY(EPSGetEigenvalue(eps, i, &kr, &ki));
+    t.add("   ");
+    t.eig(kr, ki);
+    t.add("\n");
+  }
+  t.add("\n");
+  return emit(v, t);
 }

@@ -1,8 +1,8 @@
 """Regenerate reference_outputs.json from the reference's expected-output files (run in the build container only;
 other machines use the committed JSON).  Only the printed eigenvalues/norms of the Krylov-Schur-path tests are
-extracted; each entry records the file it came from and the options of that test.  The real matrix those tests
-read from a PETSc binary file (share/slepc/datafiles/matrices/rdb200.petsc) is converted to CSR arrays in
-rdb200.npz by an independent big-endian reader."""
+extracted, with the lines EPSErrorView printed; each entry records the file it came from and the options of that
+test.  The real matrix those tests read from a PETSc binary file (share/slepc/datafiles/matrices/rdb200.petsc)
+is converted to CSR arrays in rdb200.npz by an independent big-endian reader."""
 import json
 import os
 import re
@@ -76,6 +76,11 @@ def main():
     rowptr = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
     np.savez(os.path.join(os.path.dirname(OUT), "rdb200.npz"), rowptr=rowptr, colidx=cols, vals=vals,
              shape=np.array([m, n], dtype=np.int32))
+    # the text EPSErrorView prints (the "All requested ..." line and the eigenvalue line), per solve of each test
+    for key in ("ex2_1", "ex9_1", "ex4_1", "test2_1", "test2_3"):
+        lines = read(g[key]["source"]).splitlines()
+        g[key]["errorview"] = [[lines[i], lines[i + 1]] for i, l in enumerate(lines)
+                               if l.startswith(" All requested eigenvalues")]
     with open(OUT, "w") as f:
         json.dump(g, f, indent=1)
     print("wrote", OUT)

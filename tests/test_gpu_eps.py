@@ -293,3 +293,51 @@ def test_batch_rejects_targets(lib):
     with pytest.raises(sg.SlepcError) as e:
         sg.solve_batch([eps])
     assert e.value.code == 56  # PETSC_ERR_SUP
+
+
+def test_error_view_prints_the_reference_text(lib, tmp_path):
+    """EPSErrorView's default report (epsview.c:297-333) against the lines the reference's tests printed: ex2
+    (symmetric), ex9 (complex pairs: 0.00007+2.13946i), ex4 (rdb200 read by MatLoad), and test2's three solves
+    (largest, smallest, harmonic interior around 2.1).  The INFO_DETAIL table and EPSConvergedReasonView follow
+    the reference's layout."""
+    cases = []
+    g = G["ex2_1"]
+    cases.append((matgen.laplacian_2d(*g["grid"]), dict(hermitian=True, which="LM", nev=4, ncv=20, tol=1e-8),
+                  g["errorview"][0]))
+    g = G["ex9_1"]
+    cases.append((matgen.brusselator(g["N"]), dict(hermitian=False, which="LR", nev=4, tol=1e-8), g["errorview"][0]))
+    g = G["ex4_1"]
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "rdb200.npz"))
+    path = str(tmp_path / "rdb200.petsc")
+    sg.Mat(d["rowptr"], d["colidx"], d["vals"]).save(path)
+    A = sg.Mat.load(path)
+    cases.append(((A.rowptr, A.colidx, A.vals), dict(hermitian=False, which="LM", nev=4, tol=1e-8),
+                  g["errorview"][0]))
+    g = G["test2_1"]
+    lap = matgen.laplacian_1d(g["n"])
+    for kw, want in ((dict(which="LR"), g["errorview"][0]), (dict(which="SR"), g["errorview"][1]),
+                     (dict(which="TM", harmonic=True, target=g["target"]), g["errorview"][2])):
+        cases.append((lap, dict(hermitian=True, nev=4, tol=g["tol"], **kw), want))
+    for csr, kw, want in cases:
+        n = len(csr[0]) - 1
+        res = run(csr, v0=matgen.start_vector(n, 1), **kw)
+        eps = res["eps"]
+        text = eps.errorView()
+        assert text.splitlines()[:2] == want, (text, want)
+        assert text.endswith("\n\n")
+        nconv = eps.getConverged()
+        assert eps.convergedReasonView() == (f" Linear eigensolve converged ({nconv} eigenpairs) due to "
+                                             f"CONVERGED_TOL; iterations {eps.getIterationNumber()}\n")
+        detail = eps.errorView(detail=True).splitlines()
+        sep = " ---------------------- --------------------"
+        assert detail[0] == sep and detail[2] == sep and detail[-1] == sep
+        assert detail[1] == "            k             ||Ax-kx||/||kx||"
+        assert len(detail) == nconv + 4
+        for i, line in enumerate(detail[3:-1]):
+            z = complex(eps.getEigenvalue(i))
+            kr, ki = z.real, z.imag
+            err = eps.computeError(i)
+            want_line = (f"  {kr: 9f}{ki:+9f}i      {err:12g}" if ki != 0.0 else f"    {kr: 12f}           {err:12g}")
+            assert line == want_line
+        values = eps.valuesView().splitlines()
+        assert values[0] == "Eigenvalues = " and len(values) == nconv + 1
