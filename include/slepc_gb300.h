@@ -80,7 +80,8 @@ PetscErrorCode EPSGB300SetProfiling(EPS eps, PetscBool on);
 PetscErrorCode EPSGB300GetProfile(EPS eps, EPSGB300KernelClass cls, double *ms, double *bytes, long long *launches);
 
 /* Device pointer to the basis (column-major, leading dimension *ld) after EPSSolve: columns 0..nconv-1 hold the
- * eigenvectors (Hermitian) or the Schur/eigen vectors (non-Hermitian) in solver order (see EPSGetEigenpair). */
+ * eigenvectors (Hermitian) or the Schur/eigen vectors (non-Hermitian) in solver order (see EPSGetEigenpair).  For
+ * EPS_GHEP the columns are y = B^1/2 x (EPSGetEigenvector returns x). */
 PetscErrorCode EPSGB300GetDeviceBasis(EPS eps, const double **V, PetscInt *ld);
 
 /* Solve `count` eigenproblems together: every EPS is configured as for EPSSolve (operators, problem type,

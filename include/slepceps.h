@@ -32,6 +32,7 @@ typedef enum { EPS_LARGEST_MAGNITUDE = 1, EPS_SMALLEST_MAGNITUDE, EPS_LARGEST_RE
 typedef enum { EPS_CONVERGED_TOL = 1, EPS_CONVERGED_USER = 2, EPS_DIVERGED_ITS = -1, EPS_DIVERGED_BREAKDOWN = -2,
                EPS_DIVERGED_SYMMETRY_LOST = -3, EPS_CONVERGED_ITERATING = 0 } EPSConvergedReason;
 typedef enum { EPS_ERROR_ABSOLUTE, EPS_ERROR_RELATIVE, EPS_ERROR_BACKWARD } EPSErrorType;
+typedef enum { EPS_CONV_ABS, EPS_CONV_REL, EPS_CONV_NORM, EPS_CONV_USER } EPSConv;
 
 /* SlepcInitialize / SlepcFinalize (src/sys/slepcinit.c): no-op shims */
 PetscErrorCode SlepcInitialize(int *argc, char ***argv, const char file[], const char help[]);
@@ -43,7 +44,10 @@ PetscErrorCode EPSDestroy(EPS *eps);
 PetscErrorCode EPSReset(EPS eps);
 PetscErrorCode EPSSetType(EPS eps, EPSType type);
 PetscErrorCode EPSGetType(EPS eps, EPSType *type);
-/* problem definition: epssetup.c:470-520 (EPSSetOperators), epsopts.c */
+/* problem definition: epssetup.c:470-520 (EPSSetOperators), epsopts.c.  B != NULL gives a generalised problem
+ * A x = lambda B x (EPS_GHEP or EPS_GNHEP; EPS_GNHEP is the default with B).  B must be diagonal here -- positive
+ * for EPS_GHEP, nonzero for EPS_GNHEP -- and the solve runs Krylov-Schur on an operator with the same Krylov spaces
+ * as the reference's B^-1 A with the B-inner product (STSHIFT, shift 0); other B return PETSC_ERR_SUP. */
 PetscErrorCode EPSSetOperators(EPS eps, Mat A, Mat B);
 PetscErrorCode EPSGetOperators(EPS eps, Mat *A, Mat *B);
 PetscErrorCode EPSSetProblemType(EPS eps, EPSProblemType type);
@@ -59,6 +63,13 @@ PetscErrorCode EPSSetDimensions(EPS eps, PetscInt nev, PetscInt ncv, PetscInt mp
 PetscErrorCode EPSGetDimensions(EPS eps, PetscInt *nev, PetscInt *ncv, PetscInt *mpd);
 PetscErrorCode EPSSetTolerances(EPS eps, PetscReal tol, PetscInt maxits);               /* epsopts.c:300-323 */
 PetscErrorCode EPSGetTolerances(EPS eps, PetscReal *tol, PetscInt *maxits);
+/* convergence test (epsopts.c:640-700, epsdefault.c:180-230): EPS_CONV_REL (default) errest/|k|, EPS_CONV_ABS
+ * errest, EPS_CONV_NORM errest/(||A|| + |k| ||B||) with infinity norms; EPS_CONV_USER is not provided */
+PetscErrorCode EPSSetConvergenceTest(EPS eps, EPSConv conv);
+PetscErrorCode EPSGetConvergenceTest(EPS eps, EPSConv *conv);
+/* purification of the eigenvectors of EPS_GHEP (epsdefault.c:28-50): x <- B^-1 A x, B-normalised (default on) */
+PetscErrorCode EPSSetPurify(EPS eps, PetscBool purify);
+PetscErrorCode EPSGetPurify(EPS eps, PetscBool *purify);
 PetscErrorCode EPSSetWhichEigenpairs(EPS eps, EPSWhich which);
 PetscErrorCode EPSGetWhichEigenpairs(EPS eps, EPSWhich *which);
 PetscErrorCode EPSSetInitialSpace(EPS eps, PetscInt n, Vec is[]);                          /* epssetup.c:592 */

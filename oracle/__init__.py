@@ -45,6 +45,9 @@ def load():
         i, d, ull = ctypes.c_int, ctypes.c_double, ctypes.c_ulonglong
         lib.ksor_solve.argtypes = [i, P, P, P, i, i, i, i, i, d, i, d, i, i, P, ull, d, P, i, P, P, P, P, i, d]
         lib.ksor_solve.restype = i
+        lib.ksor_solve_gen.argtypes = [i, P, P, P, P, i, i, i, i, i, d, i, d, i, i, P, ull, d, P, i, P, P, P, P, i, d,
+                                       i, d, d, i]
+        lib.ksor_solve_gen.restype = i
         lib.ksor_spmv.argtypes = [i, P, P, P, P, P, i]
         lib.ksor_spmv.restype = None
         lib.ksor_ds_hep.argtypes = [i, i, i, i, P, P, i, i, i, P, P, P]
@@ -80,9 +83,14 @@ class Result:
         self.X = X[:, : self.nconv] if X is not None else None
 
 
+CONV = {"abs": 0, "rel": 1, "norm": 2}
+
+
 def solve(rowptr, colidx, vals, *, hermitian=True, which="LM", nev=1, ncv=0, mpd=0, tol=1e-8, max_it=0,
           keep=0.5, lock=True, v0=None, nthreads=1, seed=0x5EED, time_budget=0.0, vectors=True, harmonic=False,
-          target=0.0) -> Result:
+          target=0.0, bdiag=None, conv="rel", purify=True) -> Result:
+    """bdiag: the diagonal of B for A x = k B x (EPS_GHEP when hermitian, else EPS_GNHEP); conv: "rel", "abs" or
+    "norm" (EPS_CONV_NORM with the infinity norms of A and of B, or 0 for ||B|| without B, as EPSSetUp leaves it)."""
     lib = load()
     n = len(rowptr) - 1
     rowptr = np.ascontiguousarray(rowptr, dtype=np.int32)
@@ -97,10 +105,15 @@ def solve(rowptr, colidx, vals, *, hermitian=True, which="LM", nev=1, ncv=0, mpd
     errest = np.zeros(cap)
     X = np.asfortranarray(np.zeros((n, cap))) if vectors else None  # column-major n x cap
     v0a = None if v0 is None else np.ascontiguousarray(v0, dtype=np.float64)
-    err = lib.ksor_solve(n, _ptr(rowptr), _ptr(colidx), _ptr(vals), int(bool(hermitian)), WHICH[which], int(nev),
-                         int(ncv), int(mpd), float(tol), int(max_it), float(keep), int(bool(lock)), int(nthreads),
-                         _ptr(v0a), int(seed), float(time_budget), _ptr(info), int(cap), _ptr(eigr), _ptr(eigi),
-                         _ptr(errest), _ptr(X), int(bool(harmonic)), float(target))
+    bd = None if bdiag is None else np.ascontiguousarray(bdiag, dtype=np.float64)
+    rows = np.repeat(np.arange(n), np.diff(rowptr))
+    nrma = float(np.bincount(rows, weights=np.abs(vals), minlength=n).max()) if conv == "norm" and n else 0.0
+    nrmb = float(np.max(np.abs(bd))) if conv == "norm" and bd is not None else 0.0
+    err = lib.ksor_solve_gen(n, _ptr(rowptr), _ptr(colidx), _ptr(vals), _ptr(bd), int(bool(hermitian)), WHICH[which],
+                             int(nev), int(ncv), int(mpd), float(tol), int(max_it), float(keep), int(bool(lock)),
+                             int(nthreads), _ptr(v0a), int(seed), float(time_budget), _ptr(info), int(cap), _ptr(eigr),
+                             _ptr(eigi), _ptr(errest), _ptr(X), int(bool(harmonic)), float(target), CONV[conv],
+                             nrma, nrmb, int(bool(purify)))
     return Result(info, eigr, eigi, errest, X, err)
 
 

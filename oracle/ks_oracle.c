@@ -942,12 +942,16 @@ typedef struct {
   int nthreads;
   unsigned long long rng;
   long long npasses;
+  const double *bw;  /* diagonal of the inner-product matrix B (BVSetMatrix), NULL: Euclidean */
 } bv_t;
 
 #define VCOL(bv, j) ((bv)->V + (size_t)(j) * (size_t)(bv)->n)
 
-/* c[0..j-1] = V[:,0:j]^T w, c[j] = w^T w  (BVDotColumnInc, bvorthog.c:32-47) */
+/* c[0..j-1] = V[:,0:j]^T w, c[j] = w^T w  (BVDotColumnInc, bvorthog.c:32-47); with an inner-product matrix B the
+ * dots are against B w (BV_IPMatMult, bvimpl.h:147-157), B diagonal here */
+static void bv_dot_inc_b(bv_t *bv, int j, const double *w, double *c);
 static void bv_dot_inc(bv_t *bv, int j, const double *w, double *c) {
+  if (bv->bw) { bv_dot_inc_b(bv, j, w, c); return; }
   int n = bv->n;
   for (int i = 0; i <= j; i++) c[i] = 0.0;
 #pragma omp parallel num_threads(bv->nthreads)
@@ -966,6 +970,34 @@ static void bv_dot_inc(bv_t *bv, int j, const double *w, double *c) {
       }
       double s = 0.0;
       for (int r = r0; r < r1; r++) s += w[r] * w[r];
+      lp[j] += s;
+    }
+#pragma omp critical
+    for (int i = 0; i <= j; i++) c[i] += lp[i];
+    if (lp != loc) free(lp);
+  }
+}
+
+static void bv_dot_inc_b(bv_t *bv, int j, const double *w, double *c) {
+  int n = bv->n;
+  const double *b = bv->bw;
+  for (int i = 0; i <= j; i++) c[i] = 0.0;
+#pragma omp parallel num_threads(bv->nthreads)
+  {
+    double loc[1024];
+    double *lp = (j + 1 <= 1024) ? loc : (double *)calloc((size_t)j + 1, sizeof(double));
+    for (int i = 0; i <= j; i++) lp[i] = 0.0;
+#pragma omp for schedule(static)
+    for (int r0 = 0; r0 < n; r0 += 256) {
+      int r1 = r0 + 256 < n ? r0 + 256 : n;
+      for (int i = 0; i < j; i++) {
+        const double *vi = VCOL(bv, i);
+        double s = 0.0;
+        for (int r = r0; r < r1; r++) s += vi[r] * (b[r] * w[r]);
+        lp[i] += s;
+      }
+      double s = 0.0;
+      for (int r = r0; r < r1; r++) s += w[r] * (b[r] * w[r]);
       lp[j] += s;
     }
 #pragma omp critical
@@ -995,6 +1027,15 @@ static double vec_norm(int n, const double *w, int nthreads) {
   return sqrt(s);
 }
 
+/* the norm of the BV's inner product (BVNormColumn with a matrix: sqrt(w^T B w)) */
+static double bv_vec_norm(const bv_t *bv, const double *w) {
+  if (!bv->bw) return vec_norm(bv->n, w, bv->nthreads);
+  double s = 0.0;
+#pragma omp parallel for reduction(+ : s) num_threads(bv->nthreads)
+  for (int r = 0; r < bv->n; r++) s += w[r] * (bv->bw[r] * w[r]);
+  return sqrt(s);
+}
+
 /* One CGS pass (BVOrthogonalizeCGS1, bvorthog.c:91-132).  Returns 0, or an error code for a negative inner
  * product (BV_SafeSqrt).  onorm/norm optional. */
 static int bv_cgs1(bv_t *bv, int j, double *h, double *onorm, double *norm) {
@@ -1013,7 +1054,7 @@ static int bv_cgs1(bv_t *bv, int j, double *h, double *onorm, double *norm) {
     double sum = 0.0;
     for (int i = 0; i < j; i++) sum += c[i] * c[i];
     double nn = beta * beta - sum;
-    if (nn <= 0.0) *norm = vec_norm(bv->n, w, bv->nthreads);
+    if (nn <= 0.0) *norm = bv_vec_norm(bv, w);
     else *norm = sqrt(nn);
   }
   for (int i = 0; i < j; i++) h[i] += c[i];
@@ -1036,7 +1077,7 @@ static int bv_orthogonalize_gs(bv_t *bv, int j, double *nrm_out, int *lindep) {
     *lindep = !(nrm != 0.0 && fabs(nrm) >= bv->eta * fabs(onrm));
   } else if (bv->refine == 0) {
     if ((err = bv_cgs1(bv, j, h, NULL, NULL))) return err;
-    nrm = vec_norm(bv->n, VCOL(bv, j), bv->nthreads);
+    nrm = bv_vec_norm(bv, VCOL(bv, j));
     *lindep = (nrm == 0.0);
   } else {
     if ((err = bv_cgs1(bv, j, h, NULL, NULL))) return err;
@@ -1172,13 +1213,21 @@ static void harmonic_recover(ds_t *ds, int k, int l, double beta, double *g, dou
 }
 
 /* BVMatLanczos / BVMatArnoldi (bvkrylov.c:56-226): steps j = k..m-1 */
-static int krylov_factor(bv_t *bv, const csr_t *A, int hermitian, ds_t *ds, int k, int *m, double *beta,
-                         int *breakdown, long long *nsteps) {
+/* STApply of STSHIFT with shift 0 (st/impls/shift/shift.c): w = A v, then w = B^-1 w for a generalised problem (a
+ * direct solve with the diagonal B: one division per entry) */
+static void st_apply(const csr_t *A, const double *bdiv, const double *v, double *w, int nthreads) {
+  ksor_spmv(A->n, A->rp, A->ci, A->va, v, w, nthreads);
+  if (bdiv)
+    for (int r = 0; r < A->n; r++) w[r] /= bdiv[r];
+}
+
+static int krylov_factor(bv_t *bv, const csr_t *A, const double *bdiv, int hermitian, ds_t *ds, int k, int *m,
+                         double *beta, int *breakdown, long long *nsteps) {
   int lindep = 0, err;
   double nrm = 0.0;
   int j;
   for (j = k; j < *m; j++) {
-    ksor_spmv(A->n, A->rp, A->ci, A->va, VCOL(bv, j), VCOL(bv, j + 1), bv->nthreads);
+    st_apply(A, bdiv, VCOL(bv, j), VCOL(bv, j + 1), bv->nthreads);
     (*nsteps)++;
     if ((err = bv_orthonormalize(bv, j + 1, &nrm, &lindep))) return err;
     if (lindep) { *m = j + 1; break; }
@@ -1206,7 +1255,23 @@ int ksor_solve(int n, const int *rowptr, const int *colidx, const double *vals,
                double time_budget_s,
                int *info, int ncv_cap, double *eigr_out, double *eigi_out, double *errest_out, double *X,
                int harmonic, double target) {
+  return ksor_solve_gen(n, rowptr, colidx, vals, NULL, hermitian, which, nev, ncv, mpd, tol, max_it, keep, lock,
+                        nthreads, v0, seed, time_budget_s, info, ncv_cap, eigr_out, eigi_out, errest_out, X, harmonic,
+                        target, KSOR_CONV_REL, 0.0, 0.0, 1);
+}
+
+int ksor_solve_gen(int n, const int *rowptr, const int *colidx, const double *vals, const double *bdiag,
+                   int hermitian, int which, int nev, int ncv, int mpd, double tol, int max_it,
+                   double keep, int lock, int nthreads, const double *v0, unsigned long long seed,
+                   double time_budget_s,
+                   int *info, int ncv_cap, double *eigr_out, double *eigi_out, double *errest_out, double *X,
+                   int harmonic, double target, int conv, double nrma, double nrmb, int purify) {
   double t_start = now_s();
+  /* generalised problems (epssetup.c:321-329): B^-1 A, with the B-inner product when Hermitian (GHEP); start
+   * vectors forced into the range of the operator and eigenvectors purified for GHEP (epssolve.c:855-862,
+   * epsdefault.c:28-50) */
+  const int ghep = bdiag && hermitian;
+  const csr_t Acsr = {n, rowptr, colidx, vals};
   /* EPSSolve_KrylovSchur_Default (krylovschur.c:238-239): harmonic extraction runs the non-symmetric variant */
   if (harmonic) hermitian = 0;
   if (n <= 0 || nev <= 0) return 63;
@@ -1229,6 +1294,7 @@ int ksor_solve(int n, const int *rowptr, const int *colidx, const double *vals,
   bv_t bv = {0};
   bv.n = n; bv.m = ncv + 1; bv.eta = 0.7071; bv.refine = 1; bv.nthreads = nthreads;
   bv.rng = seed ? seed : 0x5eed;
+  bv.bw = ghep ? bdiag : NULL;
   bv.V = (double *)calloc((size_t)n * bv.m, sizeof(double));
   bv.h = (double *)calloc((size_t)(bv.m + 1) * (bv.m + 1), sizeof(double));
   bv.c = (double *)calloc((size_t)bv.m + 1, sizeof(double));
@@ -1252,8 +1318,14 @@ int ksor_solve(int n, const int *rowptr, const int *colidx, const double *vals,
   /* start vector: EPSSetInitialSpace copy, or a random one; then orthonormalise (EPSGetStartVector) */
   if (v0) memcpy(bv.V, v0, sizeof(double) * n);
   else bv_random_column(&bv, 0);
+  if (ghep) {
+    double *t = (double *)malloc(sizeof(double) * n);
+    memcpy(t, bv.V, sizeof(double) * n);
+    st_apply(&Acsr, bdiag, t, bv.V, nthreads);
+    free(t);
+  }
   {
-    double nrm = vec_norm(n, bv.V, nthreads);
+    double nrm = bv_vec_norm(&bv, bv.V);
     if (nrm == 0.0) { err = 77; goto done; } /* initial vector is zero */
     bv_scale(&bv, 0, 1.0 / nrm);
   }
@@ -1266,7 +1338,7 @@ int ksor_solve(int n, const int *rowptr, const int *colidx, const double *vals,
     ds.n = nv; ds.t = nv; ds.l = nconv; ds.k = nconv + l;
     double beta = 0.0;
     int breakdown = 0;
-    err = krylov_factor(&bv, &(csr_t){n, rowptr, colidx, vals}, hermitian, &ds, nconv + l, &nv, &beta, &breakdown, &nsteps);
+    err = krylov_factor(&bv, &Acsr, bdiag, hermitian, &ds, nconv + l, &nv, &beta, &breakdown, &nsteps);
     if (err) goto done;
     ds.n = nv; ds.t = nv; ds.l = nconv; ds.k = nconv + l;
     ds.state = l ? ST_RAW : ST_INTERMEDIATE;
@@ -1296,7 +1368,10 @@ int ksor_solve(int n, const int *rowptr, const int *colidx, const double *vals,
       else ds_nhep_vector(&ds, &newk, &resnorm);
       resnorm *= beta * gamma;  /* corrf = gamma (epskrylov.c:265) */
       double w = hypot(re, im);
-      errest[k] = (w != 0.0) ? resnorm / w : DBL_MAX;
+      /* EPSConvergedRelative / Absolute / Norm (epsdefault.c:224-256) */
+      if (conv == KSOR_CONV_ABS) errest[k] = resnorm;
+      else if (conv == KSOR_CONV_NORM) errest[k] = resnorm / (nrma + w * nrmb);
+      else errest[k] = (w != 0.0) ? resnorm / w : DBL_MAX;
       if (marker == -1 && errest[k] >= tol) marker = k;
       if (newk == k + 1) { errest[k + 1] = errest[k]; k++; }
       if (marker != -1) break;
@@ -1323,6 +1398,12 @@ int ksor_solve(int n, const int *rowptr, const int *colidx, const double *vals,
         if (k < nev) {
           /* EPSGetStartVector(k): random vector orthogonalised against V[:,0:k] */
           bv_random_column(&bv, k);
+          if (ghep) {
+            double *t = (double *)malloc(sizeof(double) * n);
+            memcpy(t, VCOL(&bv, k), sizeof(double) * n);
+            st_apply(&Acsr, bdiag, t, VCOL(&bv, k), nthreads);
+            free(t);
+          }
           double nrm;
           int ld2;
           if ((err = bv_orthogonalize_gs(&bv, k, &nrm, &ld2))) goto done;
@@ -1364,6 +1445,17 @@ int ksor_solve(int n, const int *rowptr, const int *colidx, const double *vals,
     for (int i = 0; i < nconv; i++) for (int j = 0; j < nconv; j++) ds.X[IDX(i, j, ld)] = 0.0;
     ds_nhep_vectors_all(&ds);
     bv_mult_in_place(&bv, ds.X, ld, 0, nconv, 0, nconv);
+  }
+  /* EPS_Purify + BVNormalize for GHEP: x = B^-1 A x / ||B^-1 A x||_B */
+  if (ghep && purify && nconv > 0) {
+    double *t = (double *)malloc(sizeof(double) * n);
+    for (int j = 0; j < nconv; j++) {
+      memcpy(t, VCOL(&bv, j), sizeof(double) * n);
+      st_apply(&Acsr, bdiag, t, VCOL(&bv, j), nthreads);
+      double nrm = bv_vec_norm(&bv, VCOL(&bv, j));
+      if (nrm > 0.0) bv_scale(&bv, j, 1.0 / nrm);
+    }
+    free(t);
   }
   /* reorder conjugate pairs (positive imaginary first) and final sort (epssolve.c:160-178) */
   for (int i = 0; i < nconv - 1; i++) {

@@ -43,6 +43,20 @@ int ksor_solve(int n, const int *rowptr, const int *colidx, const double *vals,
                int *info, int ncv_cap, double *eigr, double *eigi, double *errest, double *X,
                int harmonic, double target);
 
+/* convergence tests (EPSConv, include/slepceps.h) */
+enum { KSOR_CONV_ABS = 0, KSOR_CONV_REL = 1, KSOR_CONV_NORM = 2 };
+
+/* ksor_solve for A x = k B x with a diagonal B (bdiag[n]; NULL: standard problem), as the reference runs it with
+ * STSHIFT (shift 0) and a direct solve with B: the operator B^-1 A, the B-inner product and purified eigenvectors
+ * when hermitian (EPS_GHEP), the Euclidean inner product otherwise (EPS_GNHEP).  conv selects the convergence test
+ * (nrma, nrmb: the norms of EPS_CONV_NORM); purify applies to EPS_GHEP.  Eigenvectors X are B-normalised. */
+int ksor_solve_gen(int n, const int *rowptr, const int *colidx, const double *vals, const double *bdiag,
+                   int hermitian, int which, int nev, int ncv, int mpd, double tol, int max_it,
+                   double keep, int lock, int nthreads, const double *v0, unsigned long long seed,
+                   double time_budget_s,
+                   int *info, int ncv_cap, double *eigr, double *eigi, double *errest, double *X,
+                   int harmonic, double target, int conv, double nrma, double nrmb, int purify);
+
 /* y = A x (CSR), the operation MatMult performs for AIJ. */
 void ksor_spmv(int n, const int *rowptr, const int *colidx, const double *vals, const double *x, double *y,
                int nthreads);

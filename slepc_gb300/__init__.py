@@ -90,6 +90,9 @@ def load():
         "EPSSetExtraction": ([P, I], I),
         "EPSGetExtraction": ([P, P], I),
         "EPSSetTarget": ([P, D], I),
+        "EPSSetConvergenceTest": ([P, I], I),
+        "EPSGetConvergenceTest": ([P, P], I),
+        "EPSSetPurify": ([P, I], I),
         "EPSGetTarget": ([P, P], I),
         "PetscViewerBinaryOpen": ([I, ctypes.c_char_p, I, PP], I),
         "PetscViewerDestroy": ([PP], I),
@@ -225,7 +228,14 @@ class EPS:
 
     class ProblemType:
         HEP = 1
+        GHEP = 2
         NHEP = 3
+        GNHEP = 4
+
+    class Conv:
+        ABS = 0
+        REL = 1
+        NORM = 2
 
     class Which:
         LARGEST_MAGNITUDE = 1
@@ -276,10 +286,23 @@ class EPS:
         _check(load().EPSSetType(self.handle, t.encode()), "EPSSetType")
 
     def setOperators(self, A, B=None):
-        if B is not None:
-            raise SlepcError(56, "EPSSetOperators", "generalised problems are not provided")
+        """A, and B for a generalised problem A x = k B x (B diagonal on this path)."""
         self._A = A
-        _check(load().EPSSetOperators(self.handle, A.handle, None), "EPSSetOperators")
+        self._B = B
+        _check(load().EPSSetOperators(self.handle, A.handle, B.handle if B is not None else None), "EPSSetOperators")
+
+    def setConvergenceTest(self, conv):
+        if isinstance(conv, str):
+            conv = {"abs": 0, "rel": 1, "norm": 2}[conv]
+        _check(load().EPSSetConvergenceTest(self.handle, int(conv)), "EPSSetConvergenceTest")
+
+    def getConvergenceTest(self):
+        v = ctypes.c_int()
+        _check(load().EPSGetConvergenceTest(self.handle, ctypes.byref(v)), "EPSGetConvergenceTest")
+        return v.value
+
+    def setPurify(self, purify=True):
+        _check(load().EPSSetPurify(self.handle, int(bool(purify))), "EPSSetPurify")
 
     def setProblemType(self, ptype):
         _check(load().EPSSetProblemType(self.handle, int(ptype)), "EPSSetProblemType")
@@ -553,12 +576,22 @@ def batch_set_tuning(tiles):
 
 
 def solve(csr, *, hermitian=True, which="LM", nev=1, ncv=None, mpd=None, tol=None, max_it=None, v0=None,
-          arith="pair", vectors=True, ds=None, lock=None, restart=None, harmonic=False, target=None):
-    """One-call convenience: returns dict(eigr, eigi, X, nconv, its, reason, errors, stats)."""
+          arith="pair", vectors=True, ds=None, lock=None, restart=None, harmonic=False, target=None, B=None,
+          conv=None, purify=None):
+    """One-call convenience: returns dict(eigr, eigi, X, nconv, its, reason, errors, stats).  B (CSR arrays of a
+    diagonal matrix) makes the problem generalised: EPS_GHEP when hermitian, else EPS_GNHEP."""
     A = Mat(*csr)
+    Bm = Mat(*B) if B is not None else None
     eps = EPS().create()
-    eps.setOperators(A)
-    eps.setProblemType(EPS.ProblemType.HEP if hermitian else EPS.ProblemType.NHEP)
+    eps.setOperators(A, Bm)
+    if Bm is None:
+        eps.setProblemType(EPS.ProblemType.HEP if hermitian else EPS.ProblemType.NHEP)
+    else:
+        eps.setProblemType(EPS.ProblemType.GHEP if hermitian else EPS.ProblemType.GNHEP)
+    if conv is not None:
+        eps.setConvergenceTest(conv)
+    if purify is not None:
+        eps.setPurify(purify)
     eps.setDimensions(nev, ncv if ncv else -1, mpd if mpd else -1)
     eps.setTolerances(tol if tol else -1.0, max_it if max_it else -1)
     eps.setWhichEigenpairs(which)
@@ -590,5 +623,5 @@ def solve(csr, *, hermitian=True, which="LM", nev=1, ncv=None, mpd=None, tol=Non
             X[:, i] = xr
     out = {"eigr": eigr, "eigi": eigi, "X": X, "nconv": nconv, "its": eps.getIterationNumber(),
            "reason": eps.getConvergedReason(), "stats": eps.getStats(),
-           "errors": np.array([eps.computeError(i) for i in range(nconv)]), "eps": eps, "A": A}
+           "errors": np.array([eps.computeError(i) for i in range(nconv)]), "eps": eps, "A": A, "B": Bm}
     return out

@@ -91,6 +91,8 @@ PetscErrorCode ksg_engine_check(EPS e, int max_ncv, bool allow_f32) {
   KSG_CHECK(e->ncv_e <= max_ncv, PETSC_ERR_SUP, "batched engine: ncv = %d exceeds the limit %d", e->ncv_e, max_ncv);
   KSG_CHECK(e->extraction == EPS_RITZ && e->which <= EPS_SMALLEST_IMAGINARY, PETSC_ERR_SUP,
             "batched engine: Ritz extraction with the largest/smallest criteria only (use EPSSolve for targets)");
+  KSG_CHECK(!e->B && e->conv == EPS_CONV_REL, PETSC_ERR_SUP,
+            "batched engine: standard problems with the relative convergence test only (use EPSSolve)");
   return 0;
 }
 

@@ -752,7 +752,7 @@ extern "C" PetscErrorCode EPSGetDS(EPS eps, DS *ds) {
   KSG_CHECK(eps && ds, PETSC_ERR_ARG_NULL, "Null argument");
   if (!eps->ds) {
     KSG_TRY(DSCreate(0, &eps->ds));
-    KSG_TRY(DSSetType(eps->ds, eps->problem == EPS_HEP ? DSHEP : DSNHEP));
+    KSG_TRY(DSSetType(eps->ds, ksg_eps_hermitian(eps) ? DSHEP : DSNHEP));
     if (eps->setup) KSG_TRY(DSAllocate(eps->ds, eps->ld));
   }
   *ds = eps->ds;

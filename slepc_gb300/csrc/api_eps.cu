@@ -542,6 +542,12 @@ extern "C" PetscErrorCode EPSReset(EPS eps) {
   return 0;
 }
 
+// the operator the solver iterates on is A itself or an EPS-owned scaled copy (generalised problems)
+static void eps_drop_operator(EPS e) {
+  if (e->op && e->op != e->A) MatDestroy(&e->op);
+  e->op = nullptr;
+}
+
 extern "C" PetscErrorCode EPSDestroy(EPS *eps) {
   if (!eps || !*eps) return 0;
   EPS e = *eps;
@@ -553,7 +559,9 @@ extern "C" PetscErrorCode EPSDestroy(EPS *eps) {
   if (e->bv) BVDestroy(&e->bv);
   if (e->ds) DSDestroy(&e->ds);
   if (e->stream) cudaStreamDestroy(e->stream);
+  eps_drop_operator(e);
   if (e->A) MatDestroy(&e->A);
+  if (e->B) MatDestroy(&e->B);
   delete e;
   *eps = nullptr;
   return 0;
@@ -570,14 +578,24 @@ extern "C" PetscErrorCode EPSGetType(EPS eps, EPSType *type) {
   *type = EPSKRYLOVSCHUR;
   return 0;
 }
+// EPSSetOperators (epssetup.c:440-500): A, and B for a generalised problem (sizes checked as there)
 extern "C" PetscErrorCode EPSSetOperators(EPS eps, Mat A, Mat B) {
   KSG_CHECK(eps && A, PETSC_ERR_ARG_NULL, "Null argument");
-  KSG_CHECK(!B, PETSC_ERR_SUP, "Generalised problems (B != NULL) are not provided");
   KSG_CHECK(!A->empty, PETSC_ERR_ARG_WRONGSTATE, "The Mat holds no data (MatCreate without MatLoad)");
-  KSG_CHECK(A->m == A->n, PETSC_ERR_ARG_WRONG, "A must be square");
+  KSG_CHECK(A->m == A->n, PETSC_ERR_ARG_WRONG, "A does not have equal row and column sizes (%d, %d)", A->m, A->n);
+  if (B) {
+    KSG_CHECK(!B->empty, PETSC_ERR_ARG_WRONGSTATE, "The Mat B holds no data (MatCreate without MatLoad)");
+    KSG_CHECK(B->m == B->n, PETSC_ERR_ARG_WRONG, "B is a non-square matrix (%d rows, %d cols)", B->m, B->n);
+    KSG_CHECK(A->m == B->m, PETSC_ERR_ARG_INCOMP, "Dimensions of A and B do not match (%d, %d)", A->m, B->m);
+    B->refs++;
+  }
   A->refs++;
+  eps_drop_operator(eps);
   if (eps->A) MatDestroy(&eps->A);
+  if (eps->B) MatDestroy(&eps->B);
   eps->A = A;
+  eps->B = B;
+  eps->nrma = eps->nrmb = 0.0;
   eps->setup = 0;
   eps->solved = 0;
   return 0;
@@ -585,12 +603,13 @@ extern "C" PetscErrorCode EPSSetOperators(EPS eps, Mat A, Mat B) {
 extern "C" PetscErrorCode EPSGetOperators(EPS eps, Mat *A, Mat *B) {
   KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
   if (A) *A = eps->A;
-  if (B) *B = nullptr;
+  if (B) *B = eps->B;
   return 0;
 }
 extern "C" PetscErrorCode EPSSetProblemType(EPS eps, EPSProblemType type) {
   KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
-  KSG_CHECK(type == EPS_HEP || type == EPS_NHEP, PETSC_ERR_SUP, "Only EPS_HEP and EPS_NHEP are provided");
+  KSG_CHECK(type == EPS_HEP || type == EPS_NHEP || type == EPS_GHEP || type == EPS_GNHEP, PETSC_ERR_SUP,
+            "Only EPS_HEP, EPS_NHEP, EPS_GHEP and EPS_GNHEP are provided");
   eps->problem = type;
   eps->setup = 0;
   eps->solved = 0;
@@ -599,6 +618,32 @@ extern "C" PetscErrorCode EPSSetProblemType(EPS eps, EPSProblemType type) {
 extern "C" PetscErrorCode EPSGetProblemType(EPS eps, EPSProblemType *type) {
   KSG_CHECK(eps && type, PETSC_ERR_ARG_NULL, "Null argument");
   *type = (EPSProblemType)eps->problem;
+  return 0;
+}
+// EPSSetConvergenceTest (epsopts.c:682-700)
+extern "C" PetscErrorCode EPSSetConvergenceTest(EPS eps, EPSConv conv) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  KSG_CHECK(conv != EPS_CONV_USER, PETSC_ERR_SUP, "EPS_CONV_USER (a convergence test function) is not provided");
+  KSG_CHECK(conv == EPS_CONV_ABS || conv == EPS_CONV_REL || conv == EPS_CONV_NORM, PETSC_ERR_ARG_OUTOFRANGE,
+            "Invalid 'conv' value");
+  eps->conv = conv;
+  eps->setup = 0;
+  return 0;
+}
+extern "C" PetscErrorCode EPSGetConvergenceTest(EPS eps, EPSConv *conv) {
+  KSG_CHECK(eps && conv, PETSC_ERR_ARG_NULL, "Null argument");
+  *conv = (EPSConv)eps->conv;
+  return 0;
+}
+extern "C" PetscErrorCode EPSSetPurify(EPS eps, PetscBool purify) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  eps->purify = purify ? 1 : 0;
+  eps->setup = 0;
+  return 0;
+}
+extern "C" PetscErrorCode EPSGetPurify(EPS eps, PetscBool *purify) {
+  KSG_CHECK(eps && purify, PETSC_ERR_ARG_NULL, "Null argument");
+  *purify = eps->purify ? PETSC_TRUE : PETSC_FALSE;
   return 0;
 }
 extern "C" PetscErrorCode EPSSetExtraction(EPS eps, EPSExtraction extr) {
@@ -800,6 +845,13 @@ extern "C" PetscErrorCode EPSSetFromOptions(EPS eps) {
     else if (!strcmp(o, "-eps_ritz")) KSG_TRY(EPSSetExtraction(eps, EPS_RITZ));
     else if (!strcmp(o, "-eps_hermitian")) KSG_TRY(EPSSetProblemType(eps, EPS_HEP));
     else if (!strcmp(o, "-eps_non_hermitian")) KSG_TRY(EPSSetProblemType(eps, EPS_NHEP));
+    else if (!strcmp(o, "-eps_gen_hermitian")) KSG_TRY(EPSSetProblemType(eps, EPS_GHEP));
+    else if (!strcmp(o, "-eps_gen_non_hermitian")) KSG_TRY(EPSSetProblemType(eps, EPS_GNHEP));
+    else if (!strcmp(o, "-eps_conv_abs")) KSG_TRY(EPSSetConvergenceTest(eps, EPS_CONV_ABS));
+    else if (!strcmp(o, "-eps_conv_rel")) KSG_TRY(EPSSetConvergenceTest(eps, EPS_CONV_REL));
+    else if (!strcmp(o, "-eps_conv_norm")) KSG_TRY(EPSSetConvergenceTest(eps, EPS_CONV_NORM));
+    else if (!strcmp(o, "-eps_purify"))
+      KSG_TRY(EPSSetPurify(eps, (v && (!strcmp(v, "0") || !strcmp(v, "false"))) ? PETSC_FALSE : PETSC_TRUE));
     else if (!strcmp(o, "-eps_krylovschur_restart") && v) KSG_TRY(EPSKrylovSchurSetRestart(eps, atof(v)));
     else if (!strcmp(o, "-eps_krylovschur_locking") && v) KSG_TRY(EPSKrylovSchurSetLocking(eps, atoi(v) ? PETSC_TRUE : PETSC_FALSE));
     else if (!strcmp(o, "-eps_type") && v) KSG_TRY(EPSSetType(eps, v));
@@ -815,14 +867,93 @@ extern "C" PetscErrorCode EPSSetFromOptions(EPS eps) {
   return 0;
 }
 
+// Generalised problems A x = lambda B x with a diagonal B = D.  The reference runs Krylov-Schur on B^-1 A (STSHIFT,
+// shift 0) with the B-inner product for EPS_GHEP and the Euclidean one for EPS_GNHEP (epssetup.c:321-329,
+// st/impls/shift/shift.c).  Here the iteration runs on a scaled copy of A:
+//   GHEP:  C = D^-1/2 A D^-1/2 (symmetric when A is), y = D^1/2 x.  B^-1 A = D^-1/2 C D^1/2, so the Krylov space
+//          of C from D^1/2 v0 is D^1/2 times that of B^-1 A from v0, and the Euclidean inner product of y-vectors
+//          is the B-inner product of x-vectors: the Lanczos coefficients, Ritz values and residual estimates are
+//          those of the reference; eigenvectors come back as x = D^-1/2 y.
+//   GNHEP: C = D^-1 A = B^-1 A itself; vectors are unchanged.
+// Each entry of C is a_rc (s_r s_c) with s = D^-1/2, one rounding per product, so C is exactly symmetric when A is.
+static PetscErrorCode eps_setup_operator(EPS eps) {
+  eps_drop_operator(eps);
+  eps->bdiag.clear();
+  eps->d_bdiag.release();
+  eps->d_bisqrt.release();
+  if (!eps->B) {
+    eps->op = eps->A;
+    return 0;
+  }
+  const Mat A = eps->A, B = eps->B;
+  const int n = A->m;
+  const int ghep = eps->problem == EPS_GHEP;
+  KSG_CHECK(!A->dense, PETSC_ERR_SUP, "Generalised problems need an AIJ matrix A");
+  std::vector<double> d(n, 0.0);
+  if (B->dense) {
+    for (int c = 0; c < n; ++c)
+      for (int r = 0; r < n; ++r) {
+        const double v = B->data[r + (size_t)c * B->lda];
+        if (r == c) d[r] = v;
+        else KSG_CHECK(v == 0.0, PETSC_ERR_SUP, "B must be diagonal on this path (entry (%d,%d) is %g)", r, c, v);
+      }
+  } else {
+    for (int r = 0; r < n; ++r)
+      for (int p = B->ai[r]; p < B->ai[r + 1]; ++p) {
+        if (B->aj[p] == r) d[r] += B->aa[p];
+        else KSG_CHECK(B->aa[p] == 0.0, PETSC_ERR_SUP, "B must be diagonal on this path (entry (%d,%d) is %g)", r,
+                       (int)B->aj[p], B->aa[p]);
+      }
+  }
+  std::vector<double> sc(n);
+  for (int r = 0; r < n; ++r) {
+    if (ghep) {
+      KSG_CHECK(d[r] > 0.0, PETSC_ERR_ARG_WRONG, "EPS_GHEP needs a positive definite B (B(%d,%d) = %g)", r, r, d[r]);
+      sc[r] = 1.0 / sqrt(d[r]);
+    } else {
+      KSG_CHECK(d[r] != 0.0, PETSC_ERR_ARG_WRONG, "B is singular (B(%d,%d) = 0)", r, r);
+      sc[r] = 1.0 / d[r];
+    }
+  }
+  Mat C = new _p_Mat();
+  C->m = C->n = n;
+  C->own_i.assign(A->ai, A->ai + n + 1);
+  C->own_j.assign(A->aj, A->aj + A->nnz);
+  C->own_a.resize(A->nnz);
+  for (int r = 0; r < n; ++r)
+    for (int p = A->ai[r]; p < A->ai[r + 1]; ++p)
+      C->own_a[p] = ghep ? A->aa[p] * (sc[r] * sc[A->aj[p]]) : A->aa[p] * sc[r];
+  C->ai = C->own_i.data();
+  C->aj = C->own_j.data();
+  C->aa = C->own_a.data();
+  C->nnz = A->nnz;
+  eps->op = C;
+  eps->bdiag.swap(d);
+  KSG_CUDA(eps->d_bdiag.alloc(n));
+  KSG_CUDA(cudaMemcpy(eps->d_bdiag.p, eps->bdiag.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+  if (ghep) {
+    KSG_CUDA(eps->d_bisqrt.alloc(n));
+    KSG_CUDA(cudaMemcpy(eps->d_bisqrt.p, sc.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+  }
+  return 0;
+}
+
 // EPSSetUp (epssetup.c:286-418 with EPSSetUp_KrylovSchur, krylovschur.c:93-194)
 extern "C" PetscErrorCode EPSSetUp(EPS eps) {
   KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
   if (eps->setup) return 0;
   auto t0 = std::chrono::steady_clock::now();
   KSG_CHECK(eps->A, PETSC_ERR_ORDER, "EPSSetOperators must be called first");
-  if (!eps->problem) eps->problem = EPS_NHEP;  // the reference default for a single matrix
-  KSG_CHECK(eps->problem == EPS_HEP || eps->problem == EPS_NHEP, PETSC_ERR_SUP, "Unsupported problem type");
+  // the problem type against the number of matrices (epssetup.c:321-329)
+  if (!eps->problem) eps->problem = eps->B ? EPS_GNHEP : EPS_NHEP;
+  else if (!eps->B && (eps->problem == EPS_GHEP || eps->problem == EPS_GNHEP))
+    eps->problem = (eps->problem == EPS_GHEP) ? EPS_HEP : EPS_NHEP;  // generalised without B: standard problem
+  KSG_CHECK(eps->problem == EPS_HEP || eps->problem == EPS_NHEP || eps->problem == EPS_GHEP ||
+                eps->problem == EPS_GNHEP, PETSC_ERR_SUP, "Unsupported problem type");
+  KSG_CHECK(!eps->B || eps->problem == EPS_GHEP || eps->problem == EPS_GNHEP, PETSC_ERR_ARG_INCOMP,
+            "Inconsistent EPS state: the problem type does not match the number of matrices");
+  KSG_CHECK(!eps->B || eps->arith != ARITH_F32, PETSC_ERR_SUP,
+            "The precision form (EPS_GB300_ARITH_F32) is provided for standard problems only");
   const int n = eps->A->m;
   KSG_CHECK(n > 0, PETSC_ERR_ARG_WRONG, "Empty operator");
   int nev = eps->nev, ncv = eps->ncv, mpd = eps->mpd;
@@ -882,15 +1013,22 @@ extern "C" PetscErrorCode EPSSetUp(EPS eps) {
   KSG_CUDA(cudaMemsetAsync(eps->e.p, 0, sizeof(double) * eps->e.count, eps->stream));
   if (!eps->h_ctl) KSG_CUDA(cudaMallocHost((void **)&eps->h_ctl, sizeof(KSControl)));
   eps->storage = (eps->arith == ARITH_F64) ? STORE_F64 : STORE_PAIR;  // the precision form switches per phase
-  KSG_TRY(ksg_mat_upload(eps->A));
-  if (eps->A->n_seg > 0) KSG_CUDA(eps->seg_part.alloc(eps->A->n_seg));
-  if (eps->storage == STORE_PAIR) KSG_TRY(ksg_mat_upload_pairs(eps->A));
-  if (eps->arith == ARITH_F32) KSG_TRY(ksg_mat_upload_f32(eps->A));
+  KSG_TRY(eps_setup_operator(eps));
+  Mat op = eps->op;
+  KSG_TRY(ksg_mat_upload(op));
+  if (op->n_seg > 0) KSG_CUDA(eps->seg_part.alloc(op->n_seg));
+  if (eps->storage == STORE_PAIR) KSG_TRY(ksg_mat_upload_pairs(op));
+  if (eps->arith == ARITH_F32) KSG_TRY(ksg_mat_upload_f32(op));
   // power-of-two operator scaling keeps every vector inside the range of the FP32-pair arithmetic; it is exact
-  const double nrm = ksg_mat_norm_inf(eps->A);
+  const double nrm = ksg_mat_norm_inf(op);
   eps->opscale = 1.0;
   if (nrm > 0.0 && (nrm > 1048576.0 || nrm < 1.0 / 1048576.0)) eps->opscale = ldexp(1.0, -ilogb(nrm));
-  eps->lanes = spmv_lanes_for((double)eps->A->nnz / n);
+  eps->lanes = spmv_lanes_for((double)op->nnz / n);
+  // matrix norms of EPS_CONV_NORM (epssetup.c:343-353): ||B|| only for generalised problems, else 0
+  if (eps->conv == EPS_CONV_NORM) {
+    eps->nrma = ksg_mat_norm_inf(eps->A);
+    eps->nrmb = eps->B ? ksg_mat_norm_inf(eps->B) : 0.0;
+  }
   KSG_CUDA(cudaStreamSynchronize(eps->stream));
   eps->setup = 1;
   eps->stats.setup_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -962,7 +1100,7 @@ extern "C" PetscErrorCode EPSGB300GetProfile(EPS eps, EPSGB300KernelClass cls, d
 }
 
 static double spmv_bytes(EPS eps) {
-  const double n = eps->n, nnz = (double)eps->A->nnz;
+  const double n = eps->n, nnz = (double)eps->op->nnz;
   return nnz * 12.0 + 4.0 * (n + 1) + 16.0 * n;
 }
 
@@ -987,16 +1125,17 @@ static PetscErrorCode eps_factorize(EPS eps, int k0, int nv, double *bytes) {
   a.pstride = eps->pstride;
   a.st = eps->st.p;
   const double colb = 8.0 * n;
+  const Mat op = eps->op;
   LongRows lr;
-  if (eps->A->n_long > 0) {
-    lr.n_long = eps->A->n_long;
-    lr.n_seg = eps->A->n_seg;
+  if (op->n_long > 0) {
+    lr.n_long = op->n_long;
+    lr.n_seg = op->n_seg;
     lr.long_t = LONG_ROW_T;
-    lr.seg_row = eps->A->d_seg_row.p;
-    lr.seg_beg = eps->A->d_seg_beg.p;
-    lr.seg_end = eps->A->d_seg_end.p;
-    lr.lrow = eps->A->d_lrow.p;
-    lr.lfirst = eps->A->d_lfirst.p;
+    lr.seg_row = op->d_seg_row.p;
+    lr.seg_beg = op->d_seg_beg.p;
+    lr.seg_end = op->d_seg_end.p;
+    lr.lrow = op->d_lrow.p;
+    lr.lfirst = op->d_lfirst.p;
     lr.part = eps->seg_part.p;
   }
   for (int j = k0; j < nv; ++j) {
@@ -1004,8 +1143,8 @@ static PetscErrorCode eps_factorize(EPS eps, int k0, int nv, double *bytes) {
     void *w = ksg_col(eps->V.p, eps->ldv, j + 1, eps->storage);
     {
       LaunchScope ls(eps, EPS_GB300_K_SPMV, spmv_bytes(eps));
-      KSG_CUDA(launch_spmv_storage(eps->A->d_rp.p, eps->A->d_ci.p, eps->A->d_va.p, eps->A->d_va2.p, u, w, n,
-                                   eps->lanes, eps->st.p, eps->opscale, eps->storage, s, &lr, eps->A->d_va32.p));
+      KSG_CUDA(launch_spmv_storage(op->d_rp.p, op->d_ci.p, op->d_va.p, op->d_va2.p, u, w, n, eps->lanes, eps->st.p,
+                                   eps->opscale, eps->storage, s, &lr, op->d_va32.p));
     }
     a.J = j;
     a.j = j;
@@ -1039,19 +1178,54 @@ static PetscErrorCode eps_factorize(EPS eps, int k0, int nv, double *bytes) {
   return 0;
 }
 
-// the initial space, or a random vector, into column 0 of the basis (not yet normalised)
+// basis column <-> FP64 device vector, for the pair and FP64 storage formats
+static cudaError_t eps_column_to_f64(EPS eps, int col, double *x, cudaStream_t s) {
+  const void *c = ksg_col(eps->V.p, eps->ldv, col, eps->storage);
+  if (eps->storage == STORE_PAIR) return launch_pair_to_f64(static_cast<const float2 *>(c), x, eps->n, s);
+  return cudaMemcpyAsync(x, c, sizeof(double) * eps->n, cudaMemcpyDeviceToDevice, s);
+}
+static cudaError_t eps_f64_to_column(EPS eps, const double *x, int col, cudaStream_t s) {
+  void *c = ksg_col(eps->V.p, eps->ldv, col, eps->storage);
+  if (eps->storage == STORE_PAIR) return launch_f64_to_pair(x, static_cast<float2 *>(c), eps->n, s);
+  return cudaMemcpyAsync(c, x, sizeof(double) * eps->n, cudaMemcpyDeviceToDevice, s);
+}
+
+// EPSGetStartVector's "force the vector into the range of OP" for definite generalised problems
+// (epssolve.c:855-862): basis column col <- C column col, in FP64 on the device
+static PetscErrorCode eps_apply_op_column(EPS eps, int col, cudaStream_t s) {
+  DBuf<double> x, y;
+  KSG_CUDA(x.alloc(eps->n));
+  KSG_CUDA(y.alloc(eps->n));
+  KSG_CUDA(eps_column_to_f64(eps, col, x.p, s));
+  KSG_CUDA(launch_spmv(eps->op->d_rp.p, eps->op->d_ci.p, eps->op->d_va.p, x.p, y.p, eps->n, eps->lanes, nullptr,
+                       eps->opscale, s));
+  KSG_CUDA(eps_f64_to_column(eps, y.p, col, s));
+  KSG_CUDA(cudaStreamSynchronize(s));  // x and y are freed on return
+  eps->stats.kernel_launches += 1 + (eps->storage == STORE_PAIR ? 2 : 0);
+  return 0;
+}
+
+// the initial space, or a random vector, into column 0 of the basis (not yet normalised); for EPS_GHEP the user's
+// vector v0 becomes D^1/2 v0 (the basis holds y = D^1/2 x) and is then mapped into the range of the operator
 PetscErrorCode ksg_eps_put_start(EPS eps, cudaStream_t s) {
   std::vector<double> h;
   const double *src;
   if (!eps->v0_internal.empty()) src = eps->v0_internal.data();  // the precision form's refinement sweep
-  else if (!eps->v0.empty()) src = eps->v0.data();
-  else {
+  else if (!eps->v0.empty()) {
+    src = eps->v0.data();
+    if (eps->problem == EPS_GHEP && eps->B) {
+      h.resize(eps->n);
+      for (int r = 0; r < eps->n; ++r) h[r] = eps->v0[r] * sqrt(eps->bdiag[r]);
+      src = h.data();
+    }
+  } else {
     h.resize(eps->n);
     ksg_random_fill(h.data(), eps->n, eps->seed, 0);
     src = h.data();
   }
   KSG_TRY(ksg_put_column(eps->V.p, src, eps->n, eps->storage, s));
   KSG_CUDA(cudaStreamSynchronize(s));  // h is pageable and goes out of scope
+  if (eps->problem == EPS_GHEP && eps->B) KSG_TRY(eps_apply_op_column(eps, 0, s));
   return 0;
 }
 
@@ -1060,6 +1234,7 @@ PetscErrorCode ksg_eps_new_start_vector(EPS eps, int col, int *breakdown) {
   ksg_random_fill(h.data(), eps->n, eps->seed, ++eps->rng_counter);
   void *dst = ksg_col(eps->V.p, eps->ldv, col, eps->storage);
   KSG_TRY(ksg_put_column(dst, h.data(), eps->n, eps->storage, eps->stream));
+  if (eps->problem == EPS_GHEP && eps->B) KSG_TRY(eps_apply_op_column(eps, col, eps->stream));
   double nrm = 0.0;
   int ld = 0;
   KSG_TRY(ksg_orthonormalize_column(eps->V.p, eps->ldv, eps->n, col, eps->coef.p, eps->part.p, eps->pstride,
@@ -1119,7 +1294,7 @@ static void sort_eigenvalues(int which, double target, int n, const double *eigr
 PetscErrorCode ksg_eps_assemble(EPS eps, int nconv, const double *er, const double *ei, const double *es,
                                 cudaStream_t s) {
   const int n = eps->n;
-  const int herm = eps->problem == EPS_HEP;
+  const int herm = ksg_eps_hermitian(eps);
   eps->r_eigr.assign(er, er + nconv);
   eps->r_eigi.assign(ei, ei + nconv);
   eps->r_errest.assign(es, es + nconv);
@@ -1153,6 +1328,39 @@ static cudaError_t eps_restart(EPS eps, int a0, int K, int s0, int N, const doub
     return launch_restart_tc(reinterpret_cast<float2 *>(eps->V.p), eps->ldv, eps->n, a0, K, s0, N, Q, eps->ld,
                              eps->rtc.p, eps->ld, s);
   return launch_restart(eps->V.p, eps->ldv, eps->n, a0, K, s0, N, Q, eps->ld, eps->arith, s, eps->storage);
+}
+
+__global__ void k_residual(const double *y, const double *yi, const double *x, const double *xi, const double *b,
+                           double kr, double ki, int n, double *part);
+
+// EPS_Purify + BVNormalize for EPS_GHEP (epsdefault.c:28-50, epsimpl.h:297-312): x <- B^-1 A x, B-normalised.  In
+// the basis y = D^1/2 x this is y <- C y / ||C y||, on the device for the first m columns.
+static PetscErrorCode eps_purify(EPS eps, int m, cudaStream_t s, double *bytes) {
+  const int n = eps->n;
+  const int blocks = std::min(1024, (n + 255) / 256);
+  DBuf<double> x, y, part;
+  KSG_CUDA(x.alloc(n));
+  KSG_CUDA(y.alloc(n));
+  KSG_CUDA(part.alloc(3 * blocks));
+  std::vector<double> h(3 * blocks);
+  for (int j = 0; j < m; ++j) {
+    KSG_CUDA(eps_column_to_f64(eps, j, x.p, s));
+    KSG_CUDA(launch_spmv(eps->op->d_rp.p, eps->op->d_ci.p, eps->op->d_va.p, x.p, y.p, n, eps->lanes, nullptr, 1.0,
+                         s));
+    k_residual<<<blocks, 256, 0, s>>>(y.p, nullptr, y.p, nullptr, nullptr, 0.0, 0.0, n, part.p);
+    KSG_CUDA(cudaGetLastError());
+    KSG_CUDA(cudaMemcpyAsync(h.data(), part.p, sizeof(double) * 3 * blocks, cudaMemcpyDeviceToHost, s));
+    KSG_CUDA(cudaStreamSynchronize(s));
+    double ss = 0.0;
+    for (int b = 0; b < blocks; ++b) ss += h[3 * b];
+    KSG_CHECK(ss > 0.0, PETSC_ERR_PLIB, "Purification gave a zero vector (column %d)", j);
+    KSG_CUDA(launch_scale(y.p, n, 1.0 / sqrt(ss), s));
+    KSG_CUDA(eps_f64_to_column(eps, y.p, j, s));
+    eps->stats.kernel_launches += 4 + (eps->storage == STORE_PAIR ? 2 : 0);
+    *bytes += 8.0 * n * 8 + spmv_bytes(eps);
+  }
+  KSG_CUDA(cudaStreamSynchronize(s));
+  return 0;
 }
 
 // One Krylov-Schur solve in the current storage format with tolerance tol (the body of EPSSolve): start vector,
@@ -1209,6 +1417,9 @@ static PetscErrorCode eps_solve_core(EPS eps, double tol, std::chrono::steady_cl
     da.ctl = eps->ctl.p;
     da.target = eps->target * eps->opscale;  // the projected problem holds the scaled operator
     da.harmonic = harmonic;
+    da.conv = eps->conv == EPS_CONV_ABS ? DS_CONV_ABS : eps->conv == EPS_CONV_NORM ? DS_CONV_NORM : DS_CONV_REL;
+    da.conv_a = eps->conv == EPS_CONV_NORM ? eps->nrma * eps->opscale : eps->opscale;
+    da.conv_b = eps->nrmb;
     {
       LaunchScope ls(eps, EPS_GB300_K_DS, 0.0);
       if (herm && eps->ds_method == EPS_GB300_DS_REFINED) {
@@ -1284,6 +1495,7 @@ static PetscErrorCode eps_solve_core(EPS eps, double tol, std::chrono::steady_cl
     KSG_CUDA(eps_restart(eps, 0, nconv, 0, nconv, eps->X.p, s));
     bytes += 16.0 * n * nconv;
   }
+  if (eps->problem == EPS_GHEP && eps->B && eps->purify && nconv > 0) KSG_TRY(eps_purify(eps, nconv, s, &bytes));
   std::vector<double> er(ld), ei(ld), es(ld);
   KSG_CUDA(cudaMemcpyAsync(er.data(), eps->eigr.p, sizeof(double) * ld, cudaMemcpyDeviceToHost, s));
   KSG_CUDA(cudaMemcpyAsync(ei.data(), eps->eigi.p, sizeof(double) * ld, cudaMemcpyDeviceToHost, s));
@@ -1451,6 +1663,8 @@ extern "C" PetscErrorCode EPSGetEigenvector(EPS eps, PetscInt i, Vec Vr, Vec Vi)
     if (Vr) KSG_TRY(ksg_get_column(Vr->a, col, n, sto, eps->stream));
     if (Vi) memset(Vi->a, 0, bytes);
   }
+  if (Vr && eps->B && eps->problem == EPS_GHEP)  // the basis holds y = D^1/2 x
+    for (int r = 0; r < n; ++r) Vr->a[r] *= 1.0 / sqrt(eps->bdiag[r]);
   return 0;
 }
 extern "C" PetscErrorCode EPSGetEigenpair(EPS eps, PetscInt i, PetscScalar *eigr, PetscScalar *eigi, Vec Vr, Vec Vi) {
@@ -1466,36 +1680,50 @@ extern "C" PetscErrorCode EPSGetErrorEstimate(EPS eps, PetscInt i, PetscReal *er
   return 0;
 }
 
-// residual norms on the device: sums of (y - kr x + ki xi)^2 and (yi - kr xi - ki x)^2, FP64
-__global__ void k_residual(const double *y, const double *yi, const double *x, const double *xi, double kr, double ki,
-                           int n, double *part) {
-  __shared__ double s0[256], s1[256];
-  double a0 = 0.0, a1 = 0.0;
+// residual norms on the device: per block, the sums of (y - kr Bx + ki Bxi)^2, of (yi - kr Bxi - ki Bx)^2 and of
+// x^2, FP64; b is the diagonal of B, or null for B = I
+__global__ void k_residual(const double *y, const double *yi, const double *x, const double *xi, const double *b,
+                           double kr, double ki, int n, double *part) {
+  __shared__ double s0[256], s1[256], s2[256];
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0;
   for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long long)gridDim.x * blockDim.x) {
-    double u = y[r] - kr * x[r] + (xi ? ki * xi[r] : 0.0);
+    const double bx = b ? b[r] * x[r] : x[r];
+    const double bxi = xi ? (b ? b[r] * xi[r] : xi[r]) : 0.0;
+    double u = y[r] - kr * bx + (xi ? ki * bxi : 0.0);
     a0 = fma(u, u, a0);
     if (yi) {
-      double v = yi[r] - kr * xi[r] - ki * x[r];
+      double v = yi[r] - kr * bxi - ki * bx;
       a1 = fma(v, v, a1);
     }
+    a2 = fma(x[r], x[r], a2);
   }
   s0[threadIdx.x] = a0;
   s1[threadIdx.x] = a1;
+  s2[threadIdx.x] = a2;
   __syncthreads();
   for (int off = 128; off > 0; off >>= 1) {
     if (threadIdx.x < off) {
       s0[threadIdx.x] += s0[threadIdx.x + off];
       s1[threadIdx.x] += s1[threadIdx.x + off];
+      s2[threadIdx.x] += s2[threadIdx.x + off];
     }
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    part[2 * blockIdx.x] = s0[0];
-    part[2 * blockIdx.x + 1] = s1[0];
+    part[3 * blockIdx.x] = s0[0];
+    part[3 * blockIdx.x + 1] = s1[0];
+    part[3 * blockIdx.x + 2] = s2[0];
   }
 }
 
-// EPSComputeError / EPSComputeResidualNorm_Private (epssolve.c:666-815)
+// x <- d .* x (the map y -> x = D^-1/2 y of EPS_GHEP)
+__global__ void k_diag_mul(double *x, const double *d, int n) {
+  for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long long)gridDim.x * blockDim.x)
+    x[r] *= d[r];
+}
+
+// EPSComputeError / EPSComputeResidualNorm_Private (epssolve.c:666-815): ||A x - k B x|| with the user's A and B;
+// for EPS_GHEP the basis column holds y = D^1/2 x and the relative and backward errors divide by ||x||
 extern "C" PetscErrorCode EPSComputeError(EPS eps, PetscInt i, EPSErrorType type, PetscReal *error) {
   KSG_CHECK(eps && error, PETSC_ERR_ARG_NULL, "Null argument");
   KSG_CHECK(eps->solved, PETSC_ERR_ORDER, "Must call EPSSolve() first");
@@ -1508,11 +1736,14 @@ extern "C" PetscErrorCode EPSComputeError(EPS eps, PetscInt i, EPSErrorType type
   const double *xi = (ki != 0.0) ? static_cast<const double *>(ksg_col(eps->V.p, eps->ldv, kx + 1, eps->storage))
                                   : nullptr;
   if (ki < 0.0) ki = -ki;
+  const int gen = eps->B != nullptr;
+  const int ghep = gen && eps->problem == EPS_GHEP;
+  if (gen) KSG_TRY(ksg_mat_upload(eps->A));  // the iteration ran on the scaled operator
   DBuf<double> y, yi, part, xd, xid;
   const int blocks = std::min(1024, (n + 255) / 256);
   KSG_CUDA(y.alloc(n));
   if (xi) KSG_CUDA(yi.alloc(n));
-  KSG_CUDA(part.alloc(2 * blocks));
+  KSG_CUDA(part.alloc(3 * blocks));
   cudaStream_t s = eps->stream;
   if (eps->storage == STORE_F32) {
     KSG_CUDA(xd.alloc(n));
@@ -1532,25 +1763,39 @@ extern "C" PetscErrorCode EPSComputeError(EPS eps, PetscInt i, EPSErrorType type
       KSG_CUDA(launch_pair_to_f64(reinterpret_cast<const float2 *>(xi), xid.p, n, s));
       xi = xid.p;
     }
+  } else if (ghep) {
+    KSG_CUDA(xd.alloc(n));
+    KSG_CUDA(cudaMemcpyAsync(xd.p, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+    x = xd.p;
   }
-  KSG_CUDA(launch_spmv(eps->A->d_rp.p, eps->A->d_ci.p, eps->A->d_va.p, x, y.p, n, eps->lanes, nullptr, 1.0, s));
-  if (xi) KSG_CUDA(launch_spmv(eps->A->d_rp.p, eps->A->d_ci.p, eps->A->d_va.p, xi, yi.p, n, eps->lanes, nullptr, 1.0, s));
-  k_residual<<<blocks, 256, 0, s>>>(y.p, xi ? yi.p : nullptr, x, xi, kr, ki, n, part.p);
+  if (ghep) {  // eigenvalues of EPS_GHEP are real: no xi
+    k_diag_mul<<<blocks, 256, 0, s>>>(xd.p, eps->d_bisqrt.p, n);
+    KSG_CUDA(cudaGetLastError());
+  }
+  const Mat A = eps->A;
+  KSG_CUDA(launch_spmv(A->d_rp.p, A->d_ci.p, A->d_va.p, x, y.p, n, eps->lanes, nullptr, 1.0, s));
+  if (xi) KSG_CUDA(launch_spmv(A->d_rp.p, A->d_ci.p, A->d_va.p, xi, yi.p, n, eps->lanes, nullptr, 1.0, s));
+  k_residual<<<blocks, 256, 0, s>>>(y.p, xi ? yi.p : nullptr, x, xi, gen ? eps->d_bdiag.p : nullptr, kr, ki, n,
+                                    part.p);
   KSG_CUDA(cudaGetLastError());
-  std::vector<double> h(2 * blocks);
-  KSG_CUDA(cudaMemcpyAsync(h.data(), part.p, sizeof(double) * 2 * blocks, cudaMemcpyDeviceToHost, s));
+  std::vector<double> h(3 * blocks);
+  KSG_CUDA(cudaMemcpyAsync(h.data(), part.p, sizeof(double) * 3 * blocks, cudaMemcpyDeviceToHost, s));
   KSG_CUDA(cudaStreamSynchronize(s));
-  double s0 = 0.0, s1 = 0.0;
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0;
   for (int b = 0; b < blocks; ++b) {
-    s0 += h[2 * b];
-    s1 += h[2 * b + 1];
+    s0 += h[3 * b];
+    s1 += h[3 * b + 1];
+    s2 += h[3 * b + 2];
   }
   double nrm = xi ? hypot(sqrt(s0), sqrt(s1)) : sqrt(s0);
   const double lam = hypot(kr, ki);
+  const double vecnorm = ghep ? sqrt(s2) : 1.0;  // epssolve.c:767
   switch (type) {
     case EPS_ERROR_ABSOLUTE: break;
-    case EPS_ERROR_RELATIVE: nrm /= lam; break;
-    case EPS_ERROR_BACKWARD: nrm /= (ksg_mat_norm_inf(eps->A) + lam); break;
+    case EPS_ERROR_RELATIVE: nrm /= lam * vecnorm; break;
+    case EPS_ERROR_BACKWARD:
+      nrm /= (ksg_mat_norm_inf(A) + lam * (gen ? ksg_mat_norm_inf(eps->B) : 1.0)) * vecnorm;
+      break;
     default: return ksg_set_error(PETSC_ERR_ARG_OUTOFRANGE, "Invalid error type");
   }
   *error = nrm;

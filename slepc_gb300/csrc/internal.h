@@ -100,6 +100,7 @@ struct _p_BV;
 struct _p_EPS {
   // configuration
   Mat A = nullptr;
+  Mat B = nullptr;  // generalised problems: a diagonal B (EPSSetOperators)
   int problem = 0;  // EPSProblemType
   std::string type = "krylovschur";
   int which = 0;
@@ -110,6 +111,8 @@ struct _p_EPS {
   int lock = 1;
   int extraction = 0;  // EPSExtraction: EPS_RITZ or EPS_HARMONIC
   double target = 0.0;
+  int conv = EPS_CONV_REL;  // EPSConv
+  int purify = 1;           // EPSSetPurify: GHEP eigenvectors x <- B^-1 A x, B-normalised
   int arith = ksg::ARITH_PAIR;
   int storage = ksg::STORE_PAIR;  // basis format: pairs with pair arithmetic, doubles with FP64 arithmetic
   int ds_method = 0;              // EPSGB300DSMethod
@@ -125,6 +128,12 @@ struct _p_EPS {
   int n = 0, ncv_e = 0, mpd_e = 0, maxit_e = 0, nev_e = 0, ld = 0;
   double tol_e = 1e-8;
   double opscale = 1.0;
+  // the operator the Krylov iteration runs on: A itself, or for a generalised problem with diagonal B a scaled
+  // copy owned by the EPS (GHEP: D^-1/2 A D^-1/2 with D = B; GNHEP: D^-1 A)
+  Mat op = nullptr;
+  std::vector<double> bdiag;       // the diagonal of B (generalised problems)
+  DBuf<double> d_bdiag, d_bisqrt;  // device copies of diag(B) and diag(B)^-1/2
+  double nrma = 0.0, nrmb = 0.0;   // infinity norms for EPS_CONV_NORM (nrmb stays 0 for standard problems)
   int lanes = 8;
   long long ldv = 0;
   cudaStream_t stream = nullptr;
@@ -157,7 +166,8 @@ struct _p_EPS {
 
 // the Lanczos (symmetric) variant runs for EPS_HEP with Ritz extraction; harmonic extraction runs the Arnoldi
 // variant with the non-symmetric projected solver (krylovschur.c:238-239)
-inline int ksg_eps_lanczos(EPS e) { return e->problem == EPS_HEP && e->extraction != EPS_HARMONIC; }
+inline int ksg_eps_hermitian(EPS e) { return e->problem == EPS_HEP || e->problem == EPS_GHEP; }
+inline int ksg_eps_lanczos(EPS e) { return ksg_eps_hermitian(e) && e->extraction != EPS_HARMONIC; }
 
 // run the Gram-Schmidt pair kernels on one column (orthonormalise u = V[:, j] against V[:, 0:j]); returns the
 // norm of the orthogonalised vector in *nrm and the linear-dependence flag (two CGS passes)

@@ -534,7 +534,7 @@ __global__ void __launch_bounds__(DSF_THREADS, 1) k_dsf_finish(DSFArgs f, DSArgs
     const double di = (i < l) ? a.d[i] : lam[perm[i - l]];
     const double qlast = (i < l) ? ((i == n - 1) ? 1.0 : 0.0) : f.X[(m - 1) + (size_t)perm[i - l] * ld];
     const double w = fabs(di);
-    serr[i] = (w != 0.0) ? fabs(qlast) * beta / w : DBL_MAX;
+    serr[i] = ds_conv_errest(a, fabs(qlast) * beta, w);
     a.eigr[i] = di;
     if (a.eigi) a.eigi[i] = 0.0;
   }

@@ -261,7 +261,7 @@ KS_DEVICE void ds_hep_body(const DSArgs &a, double *Qs) {
     if (flags & DS_DO_EXTRAROW) se[i] = beta_e * qlast;
     else if ((flags & DS_DO_SOLVE) && i < n - 1) se[i] = 0.0;
     const double w = fabs(sd[i]);
-    serr[i] = (w != 0.0) ? fabs(qlast) * beta / w : DBL_MAX;
+    serr[i] = ds_conv_errest(a, fabs(qlast) * beta, w);
   }
   __syncthreads();
   // ---- write back ----

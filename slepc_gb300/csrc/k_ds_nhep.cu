@@ -1161,7 +1161,7 @@ KS_DEVICE void ds_nhep_body(const DSArgs &a, double *smem, int smem_bytes) {
       const double nrm = sqrt(nr2 + ni2);
       const double rn = (cplx ? hypot(yl_r, yl_i) : fabs(yl_r)) / nrm * (beta * hgamma);
       const double w = hypot(wr[k], wi[k]);
-      errs[k] = (w != 0.0) ? rn / w : DBL_MAX;
+      errs[k] = ds_conv_errest(a, rn, w);
       if (cplx) errs[k + 1] = errs[k];
     }
     nh_sync();

@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include <cfloat>
+
 #include "ks_types.h"
 
 namespace ksg {
@@ -29,7 +31,21 @@ struct DSArgs {
   KSControl *ctl;
   double target;   // target of the EPS_TARGET_* criteria (operator scale applied)
   int harmonic;    // non-symmetric solver: harmonic Rayleigh-Ritz translation for the target
+  int conv;        // DS_CONV_*: the error estimate of the convergence test
+  double conv_a, conv_b;  // DS_CONV_ABS: res / conv_a; DS_CONV_NORM: res / (conv_a + conv_b |k|)
 };
+
+// convergence tests (EPSConvergedRelative / Absolute / Norm, epsdefault.c:224-256) on the scaled operator: the
+// residual norm res and the eigenvalue modulus w are both scaled by the operator scale s, so ABS divides by s and
+// NORM by ||A|| s + ||B|| w
+enum { DS_CONV_REL = 0, DS_CONV_ABS = 1, DS_CONV_NORM = 2 };
+#ifdef __CUDACC__
+__device__ __forceinline__ double ds_conv_errest(const DSArgs &a, double res, double w) {
+  if (a.conv == DS_CONV_REL) return (w != 0.0) ? res / w : DBL_MAX;
+  const double den = (a.conv == DS_CONV_ABS) ? a.conv_a : a.conv_a + a.conv_b * w;
+  return (den != 0.0) ? res / den : DBL_MAX;
+}
+#endif
 
 enum { DS_DO_SOLVE = 1, DS_DO_SORT = 2, DS_DO_EXTRAROW = 4, DS_DO_CONTROL = 8, DS_DO_ALL = 15 };
 

@@ -236,6 +236,18 @@ def convdiff_eigenvalues(N: int, peclet: float) -> np.ndarray:
     return (ev[:, None] + ev[None, :]).ravel()
 
 
+def diagonal(d):
+    """CSR arrays of diag(d) (the B of a generalised problem)."""
+    d = np.asarray(d, dtype=np.float64)
+    n = d.size
+    return np.arange(n + 1, dtype=np.int32), np.arange(n, dtype=np.int32), d.copy()
+
+
+def log_mass(n: int) -> np.ndarray:
+    """B(i,i) = 2 / log(i + 2): the diagonal B of the reference's generalised test (src/eps/tests/test1.c)."""
+    return 2.0 / np.log(np.arange(n, dtype=np.float64) + 2.0)
+
+
 def csr_to_dense(rowptr, colidx, vals, n=None) -> np.ndarray:
     n = len(rowptr) - 1 if n is None else n
     A = np.zeros((n, n))

@@ -76,8 +76,15 @@ def main():
     rowptr = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
     np.savez(os.path.join(os.path.dirname(OUT), "rdb200.npz"), rowptr=rowptr, colidx=cols, vals=vals,
              shape=np.array([m, n], dtype=np.int32))
+    # GHEP: 2-D Laplacian 18x18 with B = diag(2/log(i+2)), nev 4, tol PETSC_SMALL, EPS_CONV_NORM, EPSErrorView with
+    # EPS_ERROR_BACKWARD (src/eps/tests/test1.c TEST 1, krylovschur)
+    txt = read("src/eps/tests/output/test1_1.out")
+    line = [l for l in txt.splitlines() if re.search(r"\d\.\d{5}", l)][-1]
+    g["test1_1"] = {"source": "src/eps/tests/output/test1_1.out", "grid": [18, 18], "nev": 4, "tol": 1e-10,
+                    "conv": "norm", "max_it": 1500, "which": "LM", "eigenvalues": floats(line),
+                    "orthogonality": "Level of orthogonality below the tolerance" in txt}
     # the text EPSErrorView prints (the "All requested ..." line and the eigenvalue line), per solve of each test
-    for key in ("ex2_1", "ex9_1", "ex4_1", "test2_1", "test2_3"):
+    for key in ("ex2_1", "ex9_1", "ex4_1", "test2_1", "test2_3", "test1_1"):
         lines = read(g[key]["source"]).splitlines()
         g[key]["errorview"] = [[lines[i], lines[i + 1]] for i, l in enumerate(lines)
                                if l.startswith(" All requested eigenvalues")]

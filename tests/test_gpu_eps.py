@@ -340,4 +340,5 @@ def test_error_view_prints_the_reference_text(lib, tmp_path):
             want_line = (f"  {kr: 9f}{ki:+9f}i      {err:12g}" if ki != 0.0 else f"    {kr: 12f}           {err:12g}")
             assert line == want_line
         values = eps.valuesView().splitlines()
-        assert values[0] == "Eigenvalues = " and len(values) == nconv + 1
+        assert values[0] == "Eigenvalues = " and len(values) == nconv + 2 and values[-1] == ""
+        assert values[1] == "   " + want[1].split(",")[0].strip()

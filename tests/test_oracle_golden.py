@@ -173,3 +173,61 @@ def test_harmonic_interior_analytic(orc):
     ex = 2 - 2 * np.cos(np.arange(1, n + 1) * np.pi / (n + 1))
     want = ex[np.argsort(np.abs(ex - tgt))][:4]
     assert np.max(np.abs(np.asarray(r.eigr[:4]) - want) / want) < 1e-12
+
+
+def test_ghep_test1_golden(orc):
+    """test1.c: A x = k B x with the 2-D Laplacian and B = diag(2/log(i+2)), EPS_GHEP, EPS_CONV_NORM, tol 1e-10:
+    the digits of test1_1.out, B-orthonormal purified eigenvectors, and scipy's dense generalised solver."""
+    import scipy.linalg as sl
+    g = G["test1_1"]
+    csr = matgen.laplacian_2d(*g["grid"])
+    n = g["grid"][0] * g["grid"][1]
+    b = matgen.log_mass(n)
+    r = orc.solve(*csr, hermitian=True, which=g["which"], nev=g["nev"], tol=g["tol"], max_it=g["max_it"],
+                  conv=g["conv"], bdiag=b, v0=matgen.start_vector(n, 1))
+    assert r.err == 0 and r.reason == 1
+    assert r5(r.eigr[:4]) == g["eigenvalues"]
+    X = r.X[:, :r.nconv]
+    assert np.abs(X.T @ (b[:, None] * X) - np.eye(r.nconv)).max() < 10 * g["tol"]  # test1.c's orthogonality check
+    w = np.sort(sl.eigh(matgen.csr_to_dense(*csr), np.diag(b), eigvals_only=True))[::-1]
+    for lam in r.eigr[:r.nconv]:
+        assert np.min(np.abs(w - lam)) / abs(lam) < 1e-11
+
+
+def test_gnhep_against_scipy(orc):
+    """EPS_GNHEP with a diagonal B: B^-1 A with the Euclidean inner product, against scipy.linalg.eig(A, B)."""
+    import scipy.linalg as sl
+    N = 20
+    csr = matgen.convection_diffusion_2d(N, 2.0)
+    n = N * N
+    b = 1.0 + matgen.uniform_01(11, n)
+    r = orc.solve(*csr, hermitian=False, which="LR", nev=6, tol=1e-11, bdiag=b, v0=matgen.start_vector(n, 2))
+    assert r.err == 0 and r.reason == 1
+    w = sl.eig(matgen.csr_to_dense(*csr), np.diag(b), right=False)
+    for a, c in zip(r.eigr[:r.nconv], r.eigi[:r.nconv]):
+        z = complex(a, c)
+        assert np.min(np.abs(w - z)) / abs(z) < 1e-10
+
+
+@pytest.mark.parametrize("conv", ["abs", "norm"])
+def test_convergence_tests(orc, conv):
+    """EPS_CONV_ABS and EPS_CONV_NORM on a standard problem: every converged pair's true residual ||A x - k x||
+    meets tol in the test's own scale (absolute, or relative to ||A||_inf = 12 since ||B|| stays 0 for one matrix),
+    and every converged value is an exact eigenvalue.  The stricter absolute test runs longer, so rounding can let
+    a second copy of a degenerate eigenvalue converge."""
+    m = 10
+    csr = matgen.laplacian_3d(m)
+    A = matgen.csr_to_dense(*csr)
+    kw = dict(hermitian=True, which="LR", nev=6, ncv=24, tol=1e-9, v0=matgen.start_vector(m ** 3, 2))
+    rel = orc.solve(*csr, **kw)
+    other = orc.solve(*csr, conv=conv, **kw)
+    assert rel.reason == 1 and other.reason == 1
+    scale = 1.0 if conv == "abs" else 12.0
+    for i in range(other.nconv):
+        x, lam = other.X[:, i], other.eigr[i]
+        assert other.errest[i] < kw["tol"]
+        assert np.linalg.norm(A @ x - lam * x) / scale < 10 * kw["tol"]
+    ex = matgen.laplacian_eigenvalues([m, m, m])
+    for lam in other.eigr[:other.nconv]:  # degenerate copies may appear once rounding splits them
+        assert np.min(np.abs(ex - lam)) < 1e-9 * abs(lam)
+    assert abs(other.eigr[0] - rel.eigr[0]) < 1e-9 * abs(rel.eigr[0])
