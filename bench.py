@@ -546,6 +546,8 @@ def main():
     ap.add_argument("--batch-plain-sample", type=int, default=256,
                     help="problems of the batched workload timed through the one-problem-per-launch path")
     ap.add_argument("--arith", default="pair", choices=["pair", "f64", "f32"])
+    ap.add_argument("--restart", default="tensor", choices=["tensor", "pair", "mma_sync", "tcgen05"],
+                    help="kernel of the thick restart (EPSGB300SetRestartMethod)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="batched workload: keep the default tuning table")
@@ -597,6 +599,7 @@ def main():
         eps.setTolerances(wl["tol"])
         eps.setWhichEigenpairs(wl["which"])
         eps.setArithmetic(args.arith)
+        eps.setRestartMethod(args.restart)
         eps.setInitialSpace(v0)
         return eps
 
@@ -613,8 +616,11 @@ def main():
         return
     if args.profile_solve:
         eps.setUp()
+        eps.setProfiling(True)
         eps.solve()
-        print(json.dumps({"profile_solve": args.workload, "stats": eps.getStats()}), flush=True)
+        prof = eps.getProfile()
+        print(json.dumps({"profile_solve": args.workload, "restart": args.restart, "stats": eps.getStats(),
+                          "per_class_ms": {k: round(v[0], 3) for k, v in prof.items()}}), flush=True)
         return
     eps.setUp()
     for _ in range(args.warmup):
@@ -697,7 +703,7 @@ def main():
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": {"workload": wl["desc"], "n": n, "nnz": nnz, "arith": args.arith,
+                "config": {"workload": wl["desc"], "n": n, "nnz": nnz, "arith": args.arith, "restart": args.restart,
                            "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (basis 2.2 GB)"
                            if args.workload == "lap3d128" else "small inputs",
                            "krylov_steps_per_solve": steps_k[-1], "restarts_per_solve": restarts[-1],

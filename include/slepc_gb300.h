@@ -41,12 +41,17 @@ PetscErrorCode EPSGB300SetProjectedSolver(EPS eps, EPSGB300DSMethod method);
 PetscErrorCode EPSGB300GetProjectedSolver(EPS eps, EPSGB300DSMethod *method);
 
 /* Kernel of the thick restart V(:, s:s+N) = V(:, a:a+K) Q for the pair-storage basis.
- *   EPS_GB300_RESTART_TENSOR (default): the bf16 tensor cores, to FP64-class accuracy by an error-free split of V and
- *       Q into seven 7-bit slices each (Ozaki scheme): the 28 slice products accumulate exactly in FP32 and are
- *       recombined in FP32 pairs (relative error about 2^-47, as the pair arithmetic).
+ *   EPS_GB300_RESTART_TENSOR (default): the bf16 tensor cores, to FP64-class accuracy by an error-free split of V
+ *       (eight 7-bit slices) and Q (seven) (Ozaki scheme): the 35 slice products of the eight levels kept
+ *       accumulate exactly in FP32 and are recombined in FP32 pairs (relative error about 2^-47, as the pair
+ *       arithmetic).  It runs on the mma.sync or the tcgen05 kernel below, whichever is the default.
+ *   EPS_GB300_RESTART_MMA_SYNC, EPS_GB300_RESTART_TCGEN05: that product on mma.sync (registers) or on tcgen05.mma
+ *       (TMEM accumulators) explicitly.  Both give bit-identical results.
  *   EPS_GB300_RESTART_PAIR: FP32-pair arithmetic on the CUDA cores.
- * The reference's BVMultInPlace (bvblas.c:74-106) is a DGEMM.  Option -eps_gb300_restart tensor|pair. */
-typedef enum { EPS_GB300_RESTART_TENSOR = 0, EPS_GB300_RESTART_PAIR = 1 } EPSGB300RestartMethod;
+ * The reference's BVMultInPlace (bvblas.c:74-106) is a DGEMM.  Option -eps_gb300_restart
+ * tensor|pair|mma_sync|tcgen05. */
+typedef enum { EPS_GB300_RESTART_TENSOR = 0, EPS_GB300_RESTART_PAIR = 1, EPS_GB300_RESTART_MMA_SYNC = 2,
+               EPS_GB300_RESTART_TCGEN05 = 3 } EPSGB300RestartMethod;
 PetscErrorCode EPSGB300SetRestartMethod(EPS eps, EPSGB300RestartMethod method);
 
 /* Wall-time budget of EPSSolve in seconds (0, the default: none).  Checked after each restart; when it has run out

@@ -373,9 +373,12 @@ class EPS:
         code = {"pair": 0, "f64": 1, "f32": 2}[arith]
         _check(load().EPSGB300SetArithmetic(self.handle, code), "EPSGB300SetArithmetic")
 
+    RESTART_METHODS = {"tensor": 0, "pair": 1, "mma_sync": 2, "tcgen05": 3}
+
     def setRestartMethod(self, method):
-        """'tensor' (bf16 tensor cores with an error-free split, default) or 'pair' (CUDA-core pair arithmetic)."""
-        _check(load().EPSGB300SetRestartMethod(self.handle, 1 if method == "pair" else 0), "EPSGB300SetRestartMethod")
+        """'tensor' (bf16 tensor cores with an error-free split, default), 'pair' (CUDA-core pair arithmetic), or the
+        tensor-core kernel explicitly: 'mma_sync' or 'tcgen05' (bit-identical results)."""
+        _check(load().EPSGB300SetRestartMethod(self.handle, self.RESTART_METHODS[method]), "EPSGB300SetRestartMethod")
 
     def setTimeLimit(self, seconds):
         """Wall-time budget of EPSSolve (checked after each restart; 0 = none)."""

@@ -798,7 +798,7 @@ extern "C" PetscErrorCode EPSGB300GetProjectedSolver(EPS eps, EPSGB300DSMethod *
 }
 extern "C" PetscErrorCode EPSGB300SetRestartMethod(EPS eps, EPSGB300RestartMethod method) {
   KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
-  KSG_CHECK(method == EPS_GB300_RESTART_TENSOR || method == EPS_GB300_RESTART_PAIR, PETSC_ERR_ARG_OUTOFRANGE,
+  KSG_CHECK(method >= EPS_GB300_RESTART_TENSOR && method <= EPS_GB300_RESTART_TCGEN05, PETSC_ERR_ARG_OUTOFRANGE,
             "Unknown restart method");
   eps->restart_method = method;
   return 0;
@@ -860,7 +860,10 @@ extern "C" PetscErrorCode EPSSetFromOptions(EPS eps) {
                                          : !strcmp(v, "f32") ? EPS_GB300_ARITH_F32
                                                              : EPS_GB300_ARITH_PAIR));
     else if (!strcmp(o, "-eps_gb300_restart") && v)
-      KSG_TRY(EPSGB300SetRestartMethod(eps, !strcmp(v, "pair") ? EPS_GB300_RESTART_PAIR : EPS_GB300_RESTART_TENSOR));
+      KSG_TRY(EPSGB300SetRestartMethod(eps, !strcmp(v, "pair")       ? EPS_GB300_RESTART_PAIR
+                                            : !strcmp(v, "mma_sync") ? EPS_GB300_RESTART_MMA_SYNC
+                                            : !strcmp(v, "tcgen05")  ? EPS_GB300_RESTART_TCGEN05
+                                                                     : EPS_GB300_RESTART_TENSOR));
     else if (!strcmp(o, "-eps_gb300_ds") && v)
       KSG_TRY(EPSGB300SetProjectedSolver(eps, !strcmp(v, "qr") ? EPS_GB300_DS_QR : EPS_GB300_DS_REFINED));
   }
@@ -1002,7 +1005,7 @@ extern "C" PetscErrorCode EPSSetUp(EPS eps) {
   KSG_CUDA(eps->coef.alloc(2 * ld + 8));
   KSG_CUDA(eps->work.alloc(4 * ld + 8));
   KSG_CUDA(eps->dsf.alloc(ds_fast_scratch_doubles(ld)));
-  KSG_CUDA(eps->rtc.alloc(restart_tc_scratch_bytes(ld)));
+  KSG_CUDA(eps->rtc.alloc(restart_tc_scratch_bytes(ld)));  // grown on the first tcgen05 restart
   eps->pstride = (int)ksg_part_stride(ld);
   KSG_CUDA(eps->part.alloc(ksg_part_blocks(n) * eps->pstride));
   KSG_CUDA(eps->st.alloc(1));
@@ -1323,10 +1326,25 @@ PetscErrorCode ksg_eps_assemble(EPS eps, int nconv, const double *er, const doub
 
 // V(:, s0:s0+N) = V(:, a0:a0+K) Q(a0:a0+K, s0:s0+N): the tensor-core restart for pair storage (default), the
 // pair-arithmetic CUDA-core kernel otherwise
+// the tensor-core kernel of EPS_GB300_RESTART_TENSOR
+static const bool kRestartTensorIsTcgen05 = false;
+
 static cudaError_t eps_restart(EPS eps, int a0, int K, int s0, int N, const double *Q, cudaStream_t s) {
-  if (eps->storage == STORE_PAIR && eps->restart_method == EPS_GB300_RESTART_TENSOR)
+  const int m = eps->restart_method;
+  if (eps->storage == STORE_PAIR && m != EPS_GB300_RESTART_PAIR) {
+    if (m == EPS_GB300_RESTART_TCGEN05 || (m == EPS_GB300_RESTART_TENSOR && kRestartTensorIsTcgen05)) {
+      const size_t need = restart_t5_scratch_bytes(eps->ld);  // about 2 KB per SM and basis column
+      if (eps->rtc.count < need) {
+        cudaError_t e = eps->rtc.alloc(need);
+        if (e == cudaSuccess) e = cudaMemsetAsync(eps->rtc.p, 0, need, s);
+        if (e != cudaSuccess) return e;
+      }
+      return launch_restart_t5(reinterpret_cast<float2 *>(eps->V.p), eps->ldv, eps->n, a0, K, s0, N, Q, eps->ld,
+                               eps->rtc.p, eps->ld, s);
+    }
     return launch_restart_tc(reinterpret_cast<float2 *>(eps->V.p), eps->ldv, eps->n, a0, K, s0, N, Q, eps->ld,
                              eps->rtc.p, eps->ld, s);
+  }
   return launch_restart(eps->V.p, eps->ldv, eps->n, a0, K, s0, N, Q, eps->ld, eps->arith, s, eps->storage);
 }
 
@@ -1596,6 +1614,11 @@ extern "C" PetscErrorCode EPSSolve(EPS eps) {
   }
   KSG_CUDA(cudaEventRecord(eps->ev_solve[1], s));
   KSG_CUDA(cudaStreamSynchronize(s));
+  if (eps->rtc.count >= restart_t5_scratch_bytes(eps->ld)) {
+    int flag = 0;  // a bounded wait of the tcgen05 restart ran out (the kernel freed its TMEM and returned)
+    KSG_CUDA(cudaMemcpy(&flag, restart_t5_errflag(eps->rtc.p, eps->ld), sizeof(int), cudaMemcpyDeviceToHost));
+    KSG_CHECK(!flag, PETSC_ERR_GPU, "tcgen05 restart: a bounded wait ran out; results are not valid");
+  }
   {
     float ms = 0.0f;
     KSG_CUDA(cudaEventElapsedTime(&ms, eps->ev_solve[0], eps->ev_solve[1]));

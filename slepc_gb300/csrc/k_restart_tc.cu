@@ -221,6 +221,319 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_restart_tc(float2 *__restrict
   }
 }
 
+// ---------------------------------------------------------------------------------------------------------------
+// The same product on the 5th-generation tensor cores: tcgen05.mma (kind::f16, bf16 x bf16 -> FP32) issued by one
+// thread, operands in shared memory in the canonical K-major core-matrix layout (8 rows x 16 bytes per core
+// matrix, no swizzle), the eight level sums accumulated in TMEM (8 levels x 64 columns = all 512 columns of the
+// SM's tensor memory, 128 lanes = the 128 rows of a tile).  Every level sum is exact in FP32, so the result is
+// bit-identical to k_restart_tc's whatever the summation order.
+//
+// Per tile of 128 rows: the row exponents, then all slices of the tile into this CTA's scratch in global memory
+// (L2-resident, 2 KB per K column), so that the output chunks -- which overwrite V in place -- never read a
+// column that an earlier chunk already wrote.  Per chunk of 64 output columns: K in stages of 32 (two MMA K-steps),
+// double-buffered in shared memory; while the tensor cores run 35 MMAs per K-step on one stage, the block copies
+// the next one.  tcgen05.commit arrives on the stage's mbarrier when the MMAs that read it are done.  The
+// epilogue reads TMEM with tcgen05.ld (warp w owns lanes 32 (w mod 4) .. +31), recombines the levels as pairs and
+// stores.  Every wait is bounded: on a timeout the kernel sets *err, frees its TMEM and returns.
+// ---------------------------------------------------------------------------------------------------------------
+constexpr int T5_M = 128;                                  // rows per tile (MMA M)
+constexpr int T5_NC = 64;                                  // output columns per chunk (MMA N <= 64)
+constexpr int T5_KC = 32;                                  // K per shared-memory stage
+constexpr int T5_THREADS = 256;
+constexpr int T5_ASL = T5_M * T5_KC * 2;                   // bytes of one V slice in a stage
+constexpr int T5_BSL = T5_NC * T5_KC * 2;                  // bytes of one Q slice in a stage
+constexpr int T5_STAGE = OZ_SA * T5_ASL + OZ_S * T5_BSL;   // 94208
+constexpr uint32_t T5_TMEM_COLS = OZ_L * T5_NC;            // 512
+constexpr size_t T5_SMEM = 2 * (size_t)T5_STAGE + 2 * T5_M * sizeof(int) + 2 * sizeof(unsigned long long) + 16;
+constexpr int T5_WAIT_LIMIT = 1 << 22;
+
+KS_DEVICE uint32_t t5_smem(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor (sm_100 family): start address, leading-dimension byte offset (between core
+// matrices adjacent in K), stride byte offset (between 8-row groups), version 1, no swizzle
+KS_DEVICE uint64_t t5_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+KS_DEVICE void t5_mma(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dtmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+KS_DEVICE void t5_commit(unsigned long long *bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(t5_smem(bar))
+               : "memory");
+}
+
+KS_DEVICE void t5_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+KS_DEVICE void t5_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// bounded wait for the completion of the mbarrier phase with this parity; false on timeout
+KS_DEVICE bool t5_wait(unsigned long long *bar, uint32_t parity) {
+  const uint32_t a = t5_smem(bar);
+  for (int it = 0; it < T5_WAIT_LIMIT; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+// 16 consecutive TMEM columns of the warp's 32 lanes (one FP32 per thread and column)
+KS_DEVICE void t5_ld16(uint32_t taddr, float *v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+KS_DEVICE uint32_t t5_bf16_pair(int lo, int hi) {
+  return (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn((float)lo)) |
+         ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn((float)hi)) << 16);
+}
+
+__global__ void __launch_bounds__(T5_THREADS, 1)
+    k_restart_t5(float2 *__restrict__ V, long long ldv, int n, int a0, int K, int s0, int N, int kp, int np,
+                 const __nv_bfloat16 *__restrict__ Bsl, const int *__restrict__ fcol, __nv_bfloat16 *__restrict__ Ascr,
+                 int *__restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  int *erow = reinterpret_cast<int *>(sm + 2 * T5_STAGE);
+  int *etmp = erow + T5_M;
+  unsigned long long *bar = reinterpret_cast<unsigned long long *>(etmp + T5_M);
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 2);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int nk8 = kp / 8;                                  // core matrices along K (kp is a multiple of 16)
+  const int nkc = (kp + T5_KC - 1) / T5_KC;                // stages per chunk
+  __nv_bfloat16 *As = Ascr + (size_t)blockIdx.x * OZ_SA * nk8 * 16 * 64;  // [s][k8][m8][8 rows][8 k]
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(t5_smem(tslot)),
+                 "r"(T5_TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(t5_smem(&bar[0])) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(t5_smem(&bar[1])) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  t5_fence_before();
+  __syncthreads();
+  t5_fence_after();
+  const uint32_t tbase = *tslot;
+  uint32_t phase[2] = {0u, 0u};
+  int pend[2] = {0, 0};
+  int ok = 1;
+  // D = FP32, A = B = bf16, both K-major, M = 128 (N filled in per chunk)
+  const uint32_t idesc_m = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(T5_M >> 4) << 24);
+  const int ntiles = (n + T5_M - 1) / T5_M;
+  for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+    const int r0 = tile * T5_M;
+    const int rows = min(T5_M, n - r0);
+    // 1. row exponents: e_r = 1 + floor(log2 max_k |hi|) from the float exponent fields (two threads per row)
+    {
+      const int m = tid & (T5_M - 1), h = tid >> 7;
+      int E = 0;
+      if (m < rows)
+        for (int k = h; k < K; k += 2) {
+          const float hi = V[(size_t)(r0 + m) + (size_t)(a0 + k) * ldv].x;
+          E = max(E, (int)((__float_as_uint(hi) >> 23) & 0xFFu));
+        }
+      if (h) etmp[m] = E;
+      __syncthreads();
+      if (!h) erow[m] = max(E, etmp[m]);
+      __syncthreads();
+    }
+    // 2. all slices of the tile into the scratch, one core-matrix row (8 consecutive k of one row) per item
+    for (int it = tid; it < T5_M * nk8; it += T5_THREADS) {
+      const int m = it & (T5_M - 1), k8 = it >> 7;
+      const int er = erow[m];
+      unsigned long long mag[8];
+      unsigned negm = 0;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int k = 8 * k8 + j;
+        long long x = 0;
+        if (m < rows && k < K && er) {
+          const float2 v = V[(size_t)(r0 + m) + (size_t)(a0 + k) * ldv];
+          x = oz_fix56(v.x, er - 126) + oz_fix56(v.y, er - 126);
+        }
+        if (x < 0) negm |= 1u << j;
+        mag[j] = x < 0 ? (unsigned long long)(-x) : (unsigned long long)x;
+      }
+#pragma unroll
+      for (int sl = 0; sl < OZ_SA; ++sl) {
+        int q[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const int v = (int)((mag[j] >> (49 - 7 * sl)) & 127ull);
+          q[j] = ((negm >> j) & 1u) ? -v : v;
+        }
+        uint4 w;
+        w.x = t5_bf16_pair(q[0], q[1]);
+        w.y = t5_bf16_pair(q[2], q[3]);
+        w.z = t5_bf16_pair(q[4], q[5]);
+        w.w = t5_bf16_pair(q[6], q[7]);
+        *reinterpret_cast<uint4 *>(As + (((size_t)sl * nk8 + k8) * 16 + (m >> 3)) * 64 + (m & 7) * 8) = w;
+      }
+    }
+    __syncthreads();
+    // 3. output columns in chunks of 64
+    for (int c0 = 0; c0 < N && ok; c0 += T5_NC) {
+      const int nch = min(T5_NC, (N - c0 + 15) / 16 * 16);
+      const uint32_t idesc = idesc_m | ((uint32_t)(nch >> 3) << 17);
+      uint32_t initmask = 0;  // levels already written in this chunk (thread 0)
+      for (int i = 0; i < nkc; ++i) {
+        const int b = i & 1;
+        if (pend[b]) {
+          ok = t5_wait(&bar[b], phase[b]) ? ok : 0;
+          phase[b] ^= 1u;
+          pend[b] = 0;
+        }
+        ok = __syncthreads_and(ok);
+        if (!ok) break;
+        const int kc8 = i * (T5_KC / 8);
+        const int sk8 = min(T5_KC / 8, nk8 - kc8);  // 4, or 2 for a last stage of 16
+        unsigned char *st = sm + b * T5_STAGE;
+        const int aq = sk8 * 16 * 8;  // uint4 per V slice in this stage
+        for (int q = tid; q < OZ_SA * aq; q += T5_THREADS) {
+          const int sl = q / aq, w = q - sl * aq;
+          const uint4 *src = reinterpret_cast<const uint4 *>(As + ((size_t)sl * nk8 + kc8) * 16 * 64) + w;
+          reinterpret_cast<uint4 *>(st + sl * T5_ASL)[w] = *src;
+        }
+        const int bq = OZ_S * sk8 * nch;
+        for (int q = tid; q < bq; q += T5_THREADS) {
+          const int nn = q % nch, rr = q / nch, k8 = rr % sk8, t = rr / sk8;
+          const uint4 w = *reinterpret_cast<const uint4 *>(Bsl + ((size_t)t * np + c0 + nn) * kp + (kc8 + k8) * 8);
+          *reinterpret_cast<uint4 *>(st + OZ_SA * T5_ASL + t * T5_BSL + (k8 * (T5_NC / 8) + (nn >> 3)) * 128 +
+                                     (nn & 7) * 16) = w;
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+          t5_fence_after();
+          const uint32_t abase = t5_smem(st), bbase = abase + OZ_SA * T5_ASL;
+          for (int j = 0; j < sk8 / 2; ++j)
+#pragma unroll
+            for (int sa = 0; sa < OZ_SA; ++sa)
+#pragma unroll
+              for (int tb = 0; tb < OZ_S; ++tb) {
+                if (sa + tb >= OZ_L) continue;
+                const int L = sa + tb;
+                const uint64_t ad = t5_desc(abase + sa * T5_ASL + j * 2 * (16 * 128), 16 * 128, 128);
+                const uint64_t bd = t5_desc(bbase + tb * T5_BSL + j * 2 * ((T5_NC / 8) * 128), (T5_NC / 8) * 128, 128);
+                t5_mma(tbase + (uint32_t)(L * T5_NC), ad, bd, idesc, (initmask >> L) & 1u);
+                initmask |= 1u << L;
+              }
+          t5_commit(&bar[b]);
+        }
+        pend[b] = 1;
+      }
+      // every MMA of the chunk done
+      for (int b = 0; b < 2; ++b)
+        if (pend[b]) {
+          ok = t5_wait(&bar[b], phase[b]) ? ok : 0;
+          phase[b] ^= 1u;
+          pend[b] = 0;
+        }
+      ok = __syncthreads_and(ok);
+      if (!ok) break;
+      t5_fence_after();
+      // 4. epilogue: warp w reads lanes 32 (w mod 4) .. +31 (tile rows), columns 32 (w / 4) .. +31 of the chunk
+      {
+        const int qd = warp & 3, hh = warp >> 2;
+        const int m = 32 * qd + lane;
+        const int er = erow[m];
+#pragma unroll 1
+        for (int g = 0; g < 2; ++g) {
+          const int col = 32 * hh + 16 * g;
+          if (col >= nch) continue;  // warp-uniform
+          float sh[16], sl[16];
+#pragma unroll
+          for (int i2 = 0; i2 < 16; ++i2) sh[i2] = sl[i2] = 0.0f;
+#pragma unroll 1
+          for (int L = OZ_L - 1; L >= 0; --L) {
+            float v[16];
+            t5_ld16(tbase + ((uint32_t)(32 * qd) << 16) + (uint32_t)(L * T5_NC + col), v);
+#pragma unroll
+            for (int i2 = 0; i2 < 16; ++i2) oz_add(sh[i2], sl[i2], ldexpf(v[i2], -7 * (L + 2)));
+          }
+          if (m < rows) {
+#pragma unroll
+            for (int i2 = 0; i2 < 16; ++i2) {
+              const int c = c0 + col + i2;
+              if (c >= N) break;
+              float2 out = make_float2(0.0f, 0.0f);  // an all-zero row stays zero
+              if (er) {
+                const float hi = sh[i2] + sl[i2];
+                const float lo = sl[i2] - (hi - sh[i2]);
+                const int sc = (er - 126) + fcol[c];
+                out = make_float2(ldexpf(hi, sc), ldexpf(lo, sc));
+              }
+              V[(size_t)(r0 + m) + (size_t)(s0 + c) * ldv] = out;
+            }
+          }
+        }
+      }
+      t5_fence_before();
+      __syncthreads();  // TMEM is read out before the next chunk's MMAs overwrite it
+    }
+  }
+  t5_fence_before();
+  __syncthreads();
+  t5_fence_after();
+  if (!ok && tid == 0) atomicExch(err, 1);
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(T5_TMEM_COLS) : "memory");
+}
+
+// scratch of the tcgen05 restart: the Q slices (as for k_restart_tc), then per CTA the V slices of a tile
+// (OZ_SA x ldp x 128 bf16), then the timeout flag
+static size_t t5_qbytes(int ld) { return (restart_tc_scratch_bytes(ld) + 255) / 256 * 256; }
+static size_t t5_abytes(int ld) {
+  const int ldp = (ld + 15) / 16 * 16;
+  return (size_t)num_sms() * OZ_SA * ldp * 128 * sizeof(__nv_bfloat16);
+}
+size_t restart_t5_scratch_bytes(int ld) { return t5_qbytes(ld) + t5_abytes(ld) + 256; }
+int *restart_t5_errflag(void *scratch, int ld) {
+  return reinterpret_cast<int *>(static_cast<unsigned char *>(scratch) + t5_qbytes(ld) + t5_abytes(ld));
+}
+
+cudaError_t launch_restart_t5(float2 *V, long long ldv, int n, int a0, int K, int s0, int N, const double *Q, int ldq,
+                              void *scratch, int ld, cudaStream_t s) {
+  if (N <= 0 || K <= 0) return cudaSuccess;
+  if (K > ld || N > ld) return cudaErrorInvalidValue;
+  const int kp = (K + 15) / 16 * 16;
+  const int ldp = (ld + 15) / 16 * 16;
+  const int np = (ld + OZ_NC - 1) / OZ_NC * OZ_NC;
+  if (kp > ldp || np < (N + 15) / 16 * 16) return cudaErrorInvalidValue;
+  __nv_bfloat16 *B = static_cast<__nv_bfloat16 *>(scratch);
+  int *fcol = reinterpret_cast<int *>(B + (size_t)OZ_S * np * kp);
+  __nv_bfloat16 *Ascr = reinterpret_cast<__nv_bfloat16 *>(static_cast<unsigned char *>(scratch) + t5_qbytes(ld));
+  int *err = restart_t5_errflag(scratch, ld);
+  cudaError_t e = cudaFuncSetAttribute(k_restart_t5, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T5_SMEM);
+  if (e != cudaSuccess) return e;
+  k_oz_qslice<<<np, 128, 0, s>>>(Q, ldq, a0, s0, K, N, kp, np, B, fcol);
+  const int ntiles = (n + T5_M - 1) / T5_M;
+  int blocks = num_sms();
+  if (blocks > ntiles) blocks = ntiles;
+  k_restart_t5<<<blocks, T5_THREADS, T5_SMEM, s>>>(V, ldv, n, a0, K, s0, N, kp, np, B, fcol, Ascr, err);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_restart_tc(float2 *V, long long ldv, int n, int a0, int K, int s0, int N, const double *Q, int ldq,
                               void *scratch, int ld, cudaStream_t s) {
   if (N <= 0 || K <= 0) return cudaSuccess;

@@ -95,6 +95,12 @@ cudaError_t launch_restart(void *V, long long ldv, int n, int a0, int K, int s0,
                            int arith, cudaStream_t s, int storage = STORE_F64);
 // the restart on the bf16 tensor cores (pair storage, k_restart_tc.cu); scratch of restart_tc_scratch_bytes(ld)
 size_t restart_tc_scratch_bytes(int ld);
+// the same restart on tcgen05 (TMEM accumulators), bit-identical results; scratch of restart_t5_scratch_bytes(ld),
+// zeroed once (it holds the flag restart_t5_errflag, set when a bounded wait of the kernel ran out)
+size_t restart_t5_scratch_bytes(int ld);
+int *restart_t5_errflag(void *scratch, int ld);
+cudaError_t launch_restart_t5(float2 *V, long long ldv, int n, int a0, int K, int s0, int N, const double *Q, int ldq,
+                              void *scratch, int ld, cudaStream_t s);
 cudaError_t launch_restart_tc(float2 *V, long long ldv, int n, int a0, int K, int s0, int N, const double *Q, int ldq,
                               void *scratch, int ld, cudaStream_t s);
 cudaError_t launch_segment_begin(KrylovState *st, int k0, int m, cudaStream_t s);

@@ -221,6 +221,28 @@ def test_tensor_restart_matches_pair_restart(lib, herm):
         assert np.min(np.abs(vb - z)) / abs(z) <= agree
 
 
+@pytest.mark.parametrize("case", ["lap3d_wide", "lap3d_narrow", "convdiff"])
+def test_tcgen05_restart_is_bit_identical(lib, case):
+    """The restart on tcgen05 (TMEM accumulators) against the same error-free split on mma.sync: every level sum is
+    exact in FP32, so whole solves agree bit for bit (eigenvalues, restart counts, eigenvectors).  The cases cover
+    output chunks wider than 64 columns (two TMEM passes), a last K stage of 16, row counts that are not multiples
+    of the 128-row tile, and the non-symmetric solver."""
+    if case == "lap3d_wide":
+        csr, kw = matgen.laplacian_3d_randdiag(30, 3), dict(hermitian=True, which="LR", nev=40, ncv=110)
+    elif case == "lap3d_narrow":
+        csr, kw = matgen.laplacian_3d_randdiag(23, 5), dict(hermitian=True, which="LR", nev=12, ncv=40)
+    else:
+        csr, kw = matgen.convection_diffusion_2d(45, 2.0), dict(hermitian=False, which="LR", nev=10, ncv=40)
+    n = len(csr[0]) - 1
+    v0 = matgen.start_vector(n, 21)
+    a = run(csr, tol=1e-10, v0=v0, restart="tcgen05", **kw)
+    b = run(csr, tol=1e-10, v0=v0, restart="mma_sync", **kw)
+    assert a["reason"] == 1 and b["reason"] == 1
+    assert a["its"] == b["its"] and a["nconv"] == b["nconv"]
+    assert np.array_equal(a["eigr"], b["eigr"]) and np.array_equal(a["eigi"], b["eigi"])
+    assert np.array_equal(a["X"], b["X"])
+
+
 @pytest.mark.parametrize("lock", [True, False])
 def test_test2_interior_harmonic_golden_on_gpu(lib, lock):
     """test2.c's third solve on the device: harmonic extraction for the eigenvalues closest to 2.1."""
