@@ -44,8 +44,10 @@ static size_t oz_smem_bytes(int kp) {
 }
 
 // Column exponents and slices of Q(a0 + k, s0 + c), k < K, c < N (zero-padded to kp x np): one block per column.
+// Layout of slice t: [c][k] (cm = 0, the mma.sync kernel), or K-major core matrices [k/8][c/8][c%8][k%8] (cm = 1, the
+// tcgen05 kernel: the 8-column groups of one k-group are contiguous, so a stage is a few bulk copies).
 __global__ void k_oz_qslice(const double *__restrict__ Q, int ldq, int a0, int s0, int K, int N, int kp, int np,
-                            __nv_bfloat16 *__restrict__ B, int *__restrict__ fcol) {
+                            __nv_bfloat16 *__restrict__ B, int *__restrict__ fcol, int cmlayout) {
   __shared__ double red[32];
   const int c = blockIdx.x;
   const bool col_ok = c < N;
@@ -72,7 +74,9 @@ __global__ void k_oz_qslice(const double *__restrict__ Q, int ldq, int a0, int s
     for (int t = 0; t < OZ_S; ++t) {
       // 7-bit slices; only the top one may reach 128 (when |q| 2^(49-f) rounds up to 2^49)
       const int sl = (int)((a >> (42 - 7 * t)) & (t == 0 ? 255ull : 127ull));
-      B[((size_t)t * np + c) * kp + k] = __float2bfloat16_rn(neg ? -(float)sl : (float)sl);
+      const size_t at = cmlayout ? (((size_t)t * (kp / 8) + k / 8) * (np / 8) + c / 8) * 64 + (c % 8) * 8 + (k % 8)
+                           : ((size_t)t * np + c) * kp + k;
+      B[at] = __float2bfloat16_rn(neg ? -(float)sl : (float)sl);
     }
   }
 }
@@ -231,10 +235,12 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_restart_tc(float2 *__restrict
 // Per tile of 128 rows: the row exponents, then all slices of the tile into this CTA's scratch in global memory
 // (L2-resident, 2 KB per K column), so that the output chunks -- which overwrite V in place -- never read a
 // column that an earlier chunk already wrote.  Per chunk of 64 output columns: K in stages of 32 (two MMA K-steps),
-// double-buffered in shared memory; while the tensor cores run 35 MMAs per K-step on one stage, the block copies
-// the next one.  tcgen05.commit arrives on the stage's mbarrier when the MMAs that read it are done.  The
-// epilogue reads TMEM with tcgen05.ld (warp w owns lanes 32 (w mod 4) .. +31), recombines the levels as pairs and
-// stores.  Every wait is bounded: on a timeout the kernel sets *err, frees its TMEM and returns.
+// double-buffered in shared memory and filled by bulk copies of the TMA engine (cp.async.bulk, completion counted
+// in bytes on the stage's "full" mbarrier).  One thread runs the pipeline: the copies of stage i+1 are in flight
+// while the tensor cores run the 35 MMAs per K-step of stage i; tcgen05.commit arrives on the stage's "empty"
+// mbarrier when the MMAs that read it are done.  The epilogue reads TMEM with tcgen05.ld (warp w owns lanes
+// 32 (w mod 4) .. +31), recombines the levels as pairs and stores.  Every wait is bounded: on a timeout the kernel
+// sets *err, waits (bounded) for its copies and MMAs in flight, frees its TMEM and returns.
 // ---------------------------------------------------------------------------------------------------------------
 constexpr int T5_M = 128;                                  // rows per tile (MMA M)
 constexpr int T5_NC = 64;                                  // output columns per chunk (MMA N <= 64)
@@ -244,7 +250,7 @@ constexpr int T5_ASL = T5_M * T5_KC * 2;                   // bytes of one V sli
 constexpr int T5_BSL = T5_NC * T5_KC * 2;                  // bytes of one Q slice in a stage
 constexpr int T5_STAGE = OZ_SA * T5_ASL + OZ_S * T5_BSL;   // 94208
 constexpr uint32_t T5_TMEM_COLS = OZ_L * T5_NC;            // 512
-constexpr size_t T5_SMEM = 2 * (size_t)T5_STAGE + 2 * T5_M * sizeof(int) + 2 * sizeof(unsigned long long) + 16;
+constexpr size_t T5_SMEM = 2 * (size_t)T5_STAGE + 2 * T5_M * sizeof(int) + 4 * sizeof(unsigned long long) + 16;
 constexpr int T5_WAIT_LIMIT = 1 << 22;
 
 KS_DEVICE uint32_t t5_smem(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -306,6 +312,19 @@ KS_DEVICE uint32_t t5_bf16_pair(int lo, int hi) {
          ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn((float)hi)) << 16);
 }
 
+KS_DEVICE void t5_expect_tx(unsigned long long *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(t5_smem(bar)), "r"(bytes) : "memory");
+}
+
+// global -> shared bulk copy (TMA engine), completion counted in bytes on the mbarrier; 16-byte aligned, size a
+// multiple of 16
+KS_DEVICE void t5_bulk(void *dst, const void *src, uint32_t bytes, unsigned long long *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(t5_smem(dst)),
+      "l"(src), "r"(bytes), "r"(t5_smem(bar))
+      : "memory");
+}
+
 __global__ void __launch_bounds__(T5_THREADS, 1)
     k_restart_t5(float2 *__restrict__ V, long long ldv, int n, int a0, int K, int s0, int N, int kp, int np,
                  const __nv_bfloat16 *__restrict__ Bsl, const int *__restrict__ fcol, __nv_bfloat16 *__restrict__ Ascr,
@@ -313,11 +332,12 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
   extern __shared__ __align__(1024) unsigned char sm[];
   int *erow = reinterpret_cast<int *>(sm + 2 * T5_STAGE);
   int *etmp = erow + T5_M;
-  unsigned long long *bar = reinterpret_cast<unsigned long long *>(etmp + T5_M);
-  uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 2);
+  unsigned long long *full = reinterpret_cast<unsigned long long *>(etmp + T5_M);  // stage loaded (TMA bytes)
+  unsigned long long *empty = full + 2;                                             // stage consumed (MMA commit)
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(empty + 2);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int nk8 = kp / 8;                                  // core matrices along K (kp is a multiple of 16)
-  const int nkc = (kp + T5_KC - 1) / T5_KC;                // stages per chunk
+  const int nk8 = kp / 8;                    // core matrices along K (kp is a multiple of 16)
+  const int nkc = (kp + T5_KC - 1) / T5_KC;  // stages per chunk
   __nv_bfloat16 *As = Ascr + (size_t)blockIdx.x * OZ_SA * nk8 * 16 * 64;  // [s][k8][m8][8 rows][8 k]
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(t5_smem(tslot)),
@@ -326,16 +346,19 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(t5_smem(&bar[0])) : "memory");
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(t5_smem(&bar[1])) : "memory");
+    for (int b = 0; b < 2; ++b) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(t5_smem(&full[b])) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(t5_smem(&empty[b])) : "memory");
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   t5_fence_before();
   __syncthreads();
   t5_fence_after();
   const uint32_t tbase = *tslot;
-  uint32_t phase[2] = {0u, 0u};
-  int pend[2] = {0, 0};
+  // barrier phases and outstanding completions (used by thread 0 only)
+  uint32_t fph[2] = {0u, 0u}, eph[2] = {0u, 0u};
+  int epend[2] = {0, 0}, fpend[2] = {0, 0};
   int ok = 1;
   // D = FP32, A = B = bf16, both K-major, M = 128 (N filled in per chunk)
   const uint32_t idesc_m = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(T5_M >> 4) << 24);
@@ -343,89 +366,123 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
   for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
     const int r0 = tile * T5_M;
     const int rows = min(T5_M, n - r0);
-    // 1. row exponents: e_r = 1 + floor(log2 max_k |hi|) from the float exponent fields (two threads per row)
+    // 1. row exponents: e_r = 1 + floor(log2 max_k |hi|) from the float exponent fields (two threads per row, 16
+    //    loads in flight each)
     {
       const int m = tid & (T5_M - 1), h = tid >> 7;
       int E = 0;
-      if (m < rows)
-        for (int k = h; k < K; k += 2) {
-          const float hi = V[(size_t)(r0 + m) + (size_t)(a0 + k) * ldv].x;
-          E = max(E, (int)((__float_as_uint(hi) >> 23) & 0xFFu));
+      if (m < rows) {
+        const float2 *col = V + (size_t)(r0 + m) + (size_t)a0 * ldv;
+        for (int k0 = h; k0 < K; k0 += 32) {
+          float hv[16];
+#pragma unroll
+          for (int u = 0; u < 16; ++u) {
+            const int k = k0 + 2 * u;
+            hv[u] = (k < K) ? col[(size_t)k * ldv].x : 0.0f;
+          }
+#pragma unroll
+          for (int u = 0; u < 16; ++u) E = max(E, (int)((__float_as_uint(hv[u]) >> 23) & 0xFFu));
         }
+      }
       if (h) etmp[m] = E;
       __syncthreads();
       if (!h) erow[m] = max(E, etmp[m]);
       __syncthreads();
     }
-    // 2. all slices of the tile into the scratch, one core-matrix row (8 consecutive k of one row) per item
-    for (int it = tid; it < T5_M * nk8; it += T5_THREADS) {
-      const int m = it & (T5_M - 1), k8 = it >> 7;
-      const int er = erow[m];
-      unsigned long long mag[8];
-      unsigned negm = 0;
+    // 2. all slices of the tile into the scratch, one core-matrix row (8 consecutive k of one row) per item, two
+    //    items per pass
+    for (int it0 = tid; it0 < T5_M * nk8; it0 += 2 * T5_THREADS) {
+      float2 v[2][8];
 #pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        const int k = 8 * k8 + j;
-        long long x = 0;
-        if (m < rows && k < K && er) {
-          const float2 v = V[(size_t)(r0 + m) + (size_t)(a0 + k) * ldv];
-          x = oz_fix56(v.x, er - 126) + oz_fix56(v.y, er - 126);
-        }
-        if (x < 0) negm |= 1u << j;
-        mag[j] = x < 0 ? (unsigned long long)(-x) : (unsigned long long)x;
-      }
-#pragma unroll
-      for (int sl = 0; sl < OZ_SA; ++sl) {
-        int q[8];
+      for (int p2 = 0; p2 < 2; ++p2) {
+        const int it = it0 + p2 * T5_THREADS;
+        const int m = it & (T5_M - 1), k8 = it >> 7;
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
-          const int v = (int)((mag[j] >> (49 - 7 * sl)) & 127ull);
-          q[j] = ((negm >> j) & 1u) ? -v : v;
+          const int k = 8 * k8 + j;
+          v[p2][j] = (it < T5_M * nk8 && m < rows && k < K)
+                         ? V[(size_t)(r0 + m) + (size_t)(a0 + k) * ldv]
+                         : make_float2(0.0f, 0.0f);
         }
-        uint4 w;
-        w.x = t5_bf16_pair(q[0], q[1]);
-        w.y = t5_bf16_pair(q[2], q[3]);
-        w.z = t5_bf16_pair(q[4], q[5]);
-        w.w = t5_bf16_pair(q[6], q[7]);
-        *reinterpret_cast<uint4 *>(As + (((size_t)sl * nk8 + k8) * 16 + (m >> 3)) * 64 + (m & 7) * 8) = w;
+      }
+#pragma unroll
+      for (int p2 = 0; p2 < 2; ++p2) {
+        const int it = it0 + p2 * T5_THREADS;
+        if (it >= T5_M * nk8) break;
+        const int m = it & (T5_M - 1), k8 = it >> 7;
+        const int er = erow[m];
+        unsigned long long mag[8];
+        unsigned negm = 0;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          long long x = 0;
+          if (er) x = oz_fix56(v[p2][j].x, er - 126) + oz_fix56(v[p2][j].y, er - 126);
+          if (x < 0) negm |= 1u << j;
+          mag[j] = x < 0 ? (unsigned long long)(-x) : (unsigned long long)x;
+        }
+#pragma unroll
+        for (int sl = 0; sl < OZ_SA; ++sl) {
+          int q[8];
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            const int vv = (int)((mag[j] >> (49 - 7 * sl)) & 127ull);
+            q[j] = ((negm >> j) & 1u) ? -vv : vv;
+          }
+          uint4 w;
+          w.x = t5_bf16_pair(q[0], q[1]);
+          w.y = t5_bf16_pair(q[2], q[3]);
+          w.z = t5_bf16_pair(q[4], q[5]);
+          w.w = t5_bf16_pair(q[6], q[7]);
+          *reinterpret_cast<uint4 *>(As + (((size_t)sl * nk8 + k8) * 16 + (m >> 3)) * 64 + (m & 7) * 8) = w;
+        }
       }
     }
+    asm volatile("fence.proxy.async;" ::: "memory");  // the scratch is read next by the TMA engine
     __syncthreads();
-    // 3. output columns in chunks of 64
+    // 3. output columns in chunks of 64.  Thread 0 runs the pipeline: bulk copies of stage i+1 in flight while the
+    //    MMAs of stage i run; the other threads wait for the epilogue.
     for (int c0 = 0; c0 < N && ok; c0 += T5_NC) {
       const int nch = min(T5_NC, (N - c0 + 15) / 16 * 16);
-      const uint32_t idesc = idesc_m | ((uint32_t)(nch >> 3) << 17);
-      uint32_t initmask = 0;  // levels already written in this chunk (thread 0)
-      for (int i = 0; i < nkc; ++i) {
-        const int b = i & 1;
-        if (pend[b]) {
-          ok = t5_wait(&bar[b], phase[b]) ? ok : 0;
-          phase[b] ^= 1u;
-          pend[b] = 0;
-        }
-        ok = __syncthreads_and(ok);
-        if (!ok) break;
-        const int kc8 = i * (T5_KC / 8);
-        const int sk8 = min(T5_KC / 8, nk8 - kc8);  // 4, or 2 for a last stage of 16
-        unsigned char *st = sm + b * T5_STAGE;
-        const int aq = sk8 * 16 * 8;  // uint4 per V slice in this stage
-        for (int q = tid; q < OZ_SA * aq; q += T5_THREADS) {
-          const int sl = q / aq, w = q - sl * aq;
-          const uint4 *src = reinterpret_cast<const uint4 *>(As + ((size_t)sl * nk8 + kc8) * 16 * 64) + w;
-          reinterpret_cast<uint4 *>(st + sl * T5_ASL)[w] = *src;
-        }
-        const int bq = OZ_S * sk8 * nch;
-        for (int q = tid; q < bq; q += T5_THREADS) {
-          const int nn = q % nch, rr = q / nch, k8 = rr % sk8, t = rr / sk8;
-          const uint4 w = *reinterpret_cast<const uint4 *>(Bsl + ((size_t)t * np + c0 + nn) * kp + (kc8 + k8) * 8);
-          *reinterpret_cast<uint4 *>(st + OZ_SA * T5_ASL + t * T5_BSL + (k8 * (T5_NC / 8) + (nn >> 3)) * 128 +
-                                     (nn & 7) * 16) = w;
-        }
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-        if (tid == 0) {
+      if (tid == 0) {
+        const uint32_t idesc = idesc_m | ((uint32_t)(nch >> 3) << 17);
+        uint32_t initmask = 0;  // levels already written in this chunk
+        auto load = [&](int i) {  // stage i into buffer i & 1, once the MMAs that read the buffer are done
+          const int b = i & 1;
+          if (epend[b]) {
+            if (!t5_wait(&empty[b], eph[b])) {
+              ok = 0;  // the buffer may still be read: issue nothing
+              return;
+            }
+            eph[b] ^= 1u;
+            epend[b] = 0;
+          }
+          const int kc8 = i * (T5_KC / 8);
+          const int sk8 = min(T5_KC / 8, nk8 - kc8);
+          unsigned char *st = sm + b * T5_STAGE;
+          const uint32_t abytes = sk8 * 16 * 128, bbytes = (nch / 8) * 128;
+          t5_expect_tx(&full[b], OZ_SA * abytes + OZ_S * sk8 * bbytes);
+          for (int sl = 0; sl < OZ_SA; ++sl)
+            t5_bulk(st + sl * T5_ASL, As + ((size_t)sl * nk8 + kc8) * 16 * 64, abytes, &full[b]);
+          for (int t = 0; t < OZ_S; ++t)
+            for (int k8 = 0; k8 < sk8; ++k8)
+              t5_bulk(st + OZ_SA * T5_ASL + t * T5_BSL + k8 * (T5_NC / 8) * 128,
+                      Bsl + (((size_t)t * nk8 + kc8 + k8) * (np / 8) + c0 / 8) * 64, bbytes, &full[b]);
+          fpend[b] = 1;
+        };
+        load(0);
+        for (int i = 0; i < nkc && ok; ++i) {
+          const int b = i & 1;
+          if (i + 1 < nkc) load(i + 1);
+          if (!ok) break;
+          if (!t5_wait(&full[b], fph[b])) {
+            ok = 0;
+            break;
+          }
+          fph[b] ^= 1u;
+          fpend[b] = 0;
           t5_fence_after();
-          const uint32_t abase = t5_smem(st), bbase = abase + OZ_SA * T5_ASL;
+          const int sk8 = min(T5_KC / 8, nk8 - i * (T5_KC / 8));
+          const uint32_t abase = t5_smem(sm + b * T5_STAGE), bbase = abase + OZ_SA * T5_ASL;
           for (int j = 0; j < sk8 / 2; ++j)
 #pragma unroll
             for (int sa = 0; sa < OZ_SA; ++sa)
@@ -438,17 +495,24 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
                 t5_mma(tbase + (uint32_t)(L * T5_NC), ad, bd, idesc, (initmask >> L) & 1u);
                 initmask |= 1u << L;
               }
-          t5_commit(&bar[b]);
+          t5_commit(&empty[b]);
+          epend[b] = 1;
         }
-        pend[b] = 1;
+        // every MMA of the chunk done (the commits track all earlier MMAs of this thread); after a timeout, also
+        // every bulk copy still in flight (bounded waits)
+        for (int b = 0; b < 2; ++b) {
+          if (epend[b]) {
+            if (!t5_wait(&empty[b], eph[b])) ok = 0;
+            eph[b] ^= 1u;
+            epend[b] = 0;
+          }
+          if (fpend[b]) {
+            if (!t5_wait(&full[b], fph[b])) ok = 0;
+            fph[b] ^= 1u;
+            fpend[b] = 0;
+          }
+        }
       }
-      // every MMA of the chunk done
-      for (int b = 0; b < 2; ++b)
-        if (pend[b]) {
-          ok = t5_wait(&bar[b], phase[b]) ? ok : 0;
-          phase[b] ^= 1u;
-          pend[b] = 0;
-        }
       ok = __syncthreads_and(ok);
       if (!ok) break;
       t5_fence_after();
@@ -526,7 +590,7 @@ cudaError_t launch_restart_t5(float2 *V, long long ldv, int n, int a0, int K, in
   int *err = restart_t5_errflag(scratch, ld);
   cudaError_t e = cudaFuncSetAttribute(k_restart_t5, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T5_SMEM);
   if (e != cudaSuccess) return e;
-  k_oz_qslice<<<np, 128, 0, s>>>(Q, ldq, a0, s0, K, N, kp, np, B, fcol);
+  k_oz_qslice<<<np, 128, 0, s>>>(Q, ldq, a0, s0, K, N, kp, np, B, fcol, 1);
   const int ntiles = (n + T5_M - 1) / T5_M;
   int blocks = num_sms();
   if (blocks > ntiles) blocks = ntiles;
@@ -548,7 +612,7 @@ cudaError_t launch_restart_tc(float2 *V, long long ldv, int n, int a0, int K, in
   if (shm > (size_t)227 * 1024) return cudaErrorInvalidValue;
   cudaError_t err = cudaFuncSetAttribute(k_restart_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
   if (err != cudaSuccess) return err;
-  k_oz_qslice<<<np, 128, 0, s>>>(Q, ldq, a0, s0, K, N, kp, np, B, fcol);
+  k_oz_qslice<<<np, 128, 0, s>>>(Q, ldq, a0, s0, K, N, kp, np, B, fcol, 0);
   const int ntiles = (n + OZ_ROWS - 1) / OZ_ROWS;
   int blocks = num_sms();
   if (blocks > ntiles) blocks = ntiles;
