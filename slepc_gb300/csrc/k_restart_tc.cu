@@ -307,9 +307,22 @@ KS_DEVICE void t5_ld16(uint32_t taddr, float *v) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-KS_DEVICE uint32_t t5_bf16_pair(int lo, int hi) {
-  return (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn((float)lo)) |
-         ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn((float)hi)) << 16);
+// Two signed 7-bit slices as a bf16x2 word, with the encoding of __float2bfloat16_rn(neg ? -(float)u : (float)u)
+// (a negative value's zero slice is -0): 0x4300 | u is the bf16 of 128 + u, one exact bf16x2 subtraction of 128
+// leaves u, and the sign bits are set after it.  Integer and FMA-pipe operations only.
+KS_DEVICE uint32_t t5_slice_pair(uint32_t u0, uint32_t u1, uint32_t neg0, uint32_t neg1) {
+  const uint32_t biased = 0x43004300u | u0 | (u1 << 16);
+  const __nv_bfloat162 d = __hsub2(*reinterpret_cast<const __nv_bfloat162 *>(&biased),
+                                   __floats2bfloat162_rn(128.0f, 128.0f));
+  return *reinterpret_cast<const uint32_t *>(&d) | (neg0 << 15) | (neg1 << 31);
+}
+
+// the 7-bit field s of a 56-bit magnitude held as (hi, lo) 32-bit halves: bits [49 - 7 s, 56 - 7 s)
+KS_DEVICE uint32_t t5_field(uint32_t hi, uint32_t lo, int sl) {
+  const int b = 49 - 7 * sl;  // compile-time after unrolling
+  if (b >= 32) return (hi >> (b - 32)) & 127u;
+  if (b + 7 <= 32) return (lo >> b) & 127u;
+  return __funnelshift_r(lo, hi, b) & 127u;
 }
 
 KS_DEVICE void t5_expect_tx(unsigned long long *bar, uint32_t bytes) {
@@ -411,28 +424,26 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
         if (it >= T5_M * nk8) break;
         const int m = it & (T5_M - 1), k8 = it >> 7;
         const int er = erow[m];
-        unsigned long long mag[8];
-        unsigned negm = 0;
+        uint32_t mh[8], ml[8], ng[8];
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
           long long x = 0;
           if (er) x = oz_fix56(v[p2][j].x, er - 126) + oz_fix56(v[p2][j].y, er - 126);
-          if (x < 0) negm |= 1u << j;
-          mag[j] = x < 0 ? (unsigned long long)(-x) : (unsigned long long)x;
+          ng[j] = x < 0 ? 1u : 0u;
+          const unsigned long long a = x < 0 ? (unsigned long long)(-x) : (unsigned long long)x;
+          mh[j] = (uint32_t)(a >> 32);
+          ml[j] = (uint32_t)a;
         }
 #pragma unroll
         for (int sl = 0; sl < OZ_SA; ++sl) {
-          int q[8];
+          uint32_t u[8];
 #pragma unroll
-          for (int j = 0; j < 8; ++j) {
-            const int vv = (int)((mag[j] >> (49 - 7 * sl)) & 127ull);
-            q[j] = ((negm >> j) & 1u) ? -vv : vv;
-          }
+          for (int j = 0; j < 8; ++j) u[j] = t5_field(mh[j], ml[j], sl);
           uint4 w;
-          w.x = t5_bf16_pair(q[0], q[1]);
-          w.y = t5_bf16_pair(q[2], q[3]);
-          w.z = t5_bf16_pair(q[4], q[5]);
-          w.w = t5_bf16_pair(q[6], q[7]);
+          w.x = t5_slice_pair(u[0], u[1], ng[0], ng[1]);
+          w.y = t5_slice_pair(u[2], u[3], ng[2], ng[3]);
+          w.z = t5_slice_pair(u[4], u[5], ng[4], ng[5]);
+          w.w = t5_slice_pair(u[6], u[7], ng[6], ng[7]);
           *reinterpret_cast<uint4 *>(As + (((size_t)sl * nk8 + k8) * 16 + (m >> 3)) * 64 + (m & 7) * 8) = w;
         }
       }
@@ -532,8 +543,11 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
           for (int L = OZ_L - 1; L >= 0; --L) {
             float v[16];
             t5_ld16(tbase + ((uint32_t)(32 * qd) << 16) + (uint32_t)(L * T5_NC + col), v);
+            // 2^(-7(L+2)) as a float (exponent field 127 - 7(L+2) >= 64): the level sums are integers below 2^24,
+            // so the product is exact and equals ldexpf(v, -7(L+2))
+            const float scale = __uint_as_float((uint32_t)(127 - 7 * (L + 2)) << 23);
 #pragma unroll
-            for (int i2 = 0; i2 < 16; ++i2) oz_add(sh[i2], sl[i2], ldexpf(v[i2], -7 * (L + 2)));
+            for (int i2 = 0; i2 < 16; ++i2) oz_add(sh[i2], sl[i2], v[i2] * scale);
           }
           if (m < rows) {
 #pragma unroll
