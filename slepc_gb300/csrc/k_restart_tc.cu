@@ -250,7 +250,7 @@ constexpr int T5_ASL = T5_M * T5_KC * 2;                   // bytes of one V sli
 constexpr int T5_BSL = T5_NC * T5_KC * 2;                  // bytes of one Q slice in a stage
 constexpr int T5_STAGE = OZ_SA * T5_ASL + OZ_S * T5_BSL;   // 94208
 constexpr uint32_t T5_TMEM_COLS = OZ_L * T5_NC;            // 512
-constexpr size_t T5_SMEM = 2 * (size_t)T5_STAGE + 2 * T5_M * sizeof(int) + 4 * sizeof(unsigned long long) + 16;
+constexpr size_t T5_SMEM = 2 * (size_t)T5_STAGE + 2 * T5_M * sizeof(int) + 5 * sizeof(unsigned long long) + 16;
 constexpr int T5_WAIT_LIMIT = 1 << 22;
 
 KS_DEVICE uint32_t t5_smem(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -347,7 +347,8 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
   int *etmp = erow + T5_M;
   unsigned long long *full = reinterpret_cast<unsigned long long *>(etmp + T5_M);  // stage loaded (TMA bytes)
   unsigned long long *empty = full + 2;                                             // stage consumed (MMA commit)
-  uint32_t *tslot = reinterpret_cast<uint32_t *>(empty + 2);
+  unsigned long long *vbar = empty + 2;                                             // V tile loaded (TMA bytes)
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(vbar + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nk8 = kp / 8;                    // core matrices along K (kp is a multiple of 16)
   const int nkc = (kp + T5_KC - 1) / T5_KC;  // stages per chunk
@@ -363,6 +364,7 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(t5_smem(&full[b])) : "memory");
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(t5_smem(&empty[b])) : "memory");
     }
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(t5_smem(vbar)) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   t5_fence_before();
@@ -376,27 +378,37 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
   // D = FP32, A = B = bf16, both K-major, M = 128 (N filled in per chunk)
   const uint32_t idesc_m = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(T5_M >> 4) << 24);
   const int ntiles = (n + T5_M - 1) / T5_M;
+  // The V tile (K columns of up to 128 rows, [k][128] float2, at most 144 KB) is loaded by bulk copies into the
+  // stage region, which is free until the tile's slices exist.  The rows are rounded up to even (16-byte copies):
+  // the extra row is inside the basis' row padding (the leading dimension is a multiple of 64).
+  const float2 *vt = reinterpret_cast<const float2 *>(sm);
+  uint32_t vph = 0;
+  int vpend = 0;  // thread 0: a V tile load it issued has not been waited for
+  auto issue_v = [&](int tl) {  // thread 0
+    const int rr = min(T5_M, n - tl * T5_M);
+    const uint32_t bytes = (uint32_t)((rr + 1) & ~1) * 8u;
+    t5_expect_tx(vbar, (uint32_t)K * bytes);
+    for (int k = 0; k < K; ++k)
+      t5_bulk(sm + (size_t)k * T5_M * 8, V + (size_t)tl * T5_M + (size_t)(a0 + k) * ldv, bytes, vbar);
+  };
+  if (tid == 0 && blockIdx.x < ntiles) {
+    issue_v(blockIdx.x);
+    vpend = 1;
+  }
   for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
     const int r0 = tile * T5_M;
     const int rows = min(T5_M, n - r0);
-    // 1. row exponents: e_r = 1 + floor(log2 max_k |hi|) from the float exponent fields (two threads per row, 16
-    //    loads in flight each)
+    if (!t5_wait(vbar, vph)) ok = 0;
+    vph ^= 1u;
+    vpend = 0;  // (every thread waited)
+    ok = __syncthreads_and(ok);
+    if (!ok) break;
+    // 1. row exponents: e_r = 1 + floor(log2 max_k |hi|) from the float exponent fields (two threads per row)
     {
       const int m = tid & (T5_M - 1), h = tid >> 7;
       int E = 0;
-      if (m < rows) {
-        const float2 *col = V + (size_t)(r0 + m) + (size_t)a0 * ldv;
-        for (int k0 = h; k0 < K; k0 += 32) {
-          float hv[16];
-#pragma unroll
-          for (int u = 0; u < 16; ++u) {
-            const int k = k0 + 2 * u;
-            hv[u] = (k < K) ? col[(size_t)k * ldv].x : 0.0f;
-          }
-#pragma unroll
-          for (int u = 0; u < 16; ++u) E = max(E, (int)((__float_as_uint(hv[u]) >> 23) & 0xFFu));
-        }
-      }
+      if (m < rows)
+        for (int k = h; k < K; k += 2) E = max(E, (int)((__float_as_uint(vt[(size_t)k * T5_M + m].x) >> 23) & 0xFFu));
       if (h) etmp[m] = E;
       __syncthreads();
       if (!h) erow[m] = max(E, etmp[m]);
@@ -413,9 +425,7 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
           const int k = 8 * k8 + j;
-          v[p2][j] = (it < T5_M * nk8 && m < rows && k < K)
-                         ? V[(size_t)(r0 + m) + (size_t)(a0 + k) * ldv]
-                         : make_float2(0.0f, 0.0f);
+          v[p2][j] = (it < T5_M * nk8 && m < rows && k < K) ? vt[(size_t)k * T5_M + m] : make_float2(0.0f, 0.0f);
         }
       }
 #pragma unroll
@@ -448,7 +458,8 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
         }
       }
     }
-    asm volatile("fence.proxy.async;" ::: "memory");  // the scratch is read next by the TMA engine
+    // the scratch is read next by the TMA engine, and the V tile's shared memory is overwritten by it
+    asm volatile("fence.proxy.async;" ::: "memory");
     __syncthreads();
     // 3. output columns in chunks of 64.  Thread 0 runs the pipeline: bulk copies of stage i+1 in flight while the
     //    MMAs of stage i run; the other threads wait for the epilogue.
@@ -523,6 +534,11 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
             fpend[b] = 0;
           }
         }
+        // after the last chunk's MMAs the stage region is free: the next tile's V loads during this epilogue
+        if (ok && c0 + T5_NC >= N && tile + (int)gridDim.x < ntiles) {
+          issue_v(tile + gridDim.x);
+          vpend = 1;
+        }
       }
       ok = __syncthreads_and(ok);
       if (!ok) break;
@@ -570,6 +586,8 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
       __syncthreads();  // TMEM is read out before the next chunk's MMAs overwrite it
     }
   }
+  // a V tile load still in flight after a timeout (bounded wait)
+  if (tid == 0 && vpend && !t5_wait(vbar, vph)) ok = 0;
   t5_fence_before();
   __syncthreads();
   t5_fence_after();
@@ -598,6 +616,7 @@ cudaError_t launch_restart_t5(float2 *V, long long ldv, int n, int a0, int K, in
   const int ldp = (ld + 15) / 16 * 16;
   const int np = (ld + OZ_NC - 1) / OZ_NC * OZ_NC;
   if (kp > ldp || np < (N + 15) / 16 * 16) return cudaErrorInvalidValue;
+  if ((size_t)K * T5_M * sizeof(float2) > 2 * (size_t)T5_STAGE) return cudaErrorInvalidValue;  // the V tile's room
   __nv_bfloat16 *B = static_cast<__nv_bfloat16 *>(scratch);
   int *fcol = reinterpret_cast<int *>(B + (size_t)OZ_S * np * kp);
   __nv_bfloat16 *Ascr = reinterpret_cast<__nv_bfloat16 *>(static_cast<unsigned char *>(scratch) + t5_qbytes(ld));
