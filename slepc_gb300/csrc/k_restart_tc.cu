@@ -245,12 +245,13 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_restart_tc(float2 *__restrict
 constexpr int T5_M = 128;                                  // rows per tile (MMA M)
 constexpr int T5_NC = 64;                                  // output columns per chunk (MMA N <= 64)
 constexpr int T5_KC = 32;                                  // K per shared-memory stage
-constexpr int T5_THREADS = 256;
+constexpr int T5_THREADS = 512;                            // 16 warps: 4 lane quarters x 4 column groups
 constexpr int T5_ASL = T5_M * T5_KC * 2;                   // bytes of one V slice in a stage
 constexpr int T5_BSL = T5_NC * T5_KC * 2;                  // bytes of one Q slice in a stage
 constexpr int T5_STAGE = OZ_SA * T5_ASL + OZ_S * T5_BSL;   // 94208
 constexpr uint32_t T5_TMEM_COLS = OZ_L * T5_NC;            // 512
-constexpr size_t T5_SMEM = 2 * (size_t)T5_STAGE + 2 * T5_M * sizeof(int) + 5 * sizeof(unsigned long long) + 16;
+constexpr size_t T5_SMEM = 2 * (size_t)T5_STAGE + (T5_THREADS / T5_M + 1) * T5_M * sizeof(int) +
+                           5 * sizeof(unsigned long long) + 16;
 constexpr int T5_WAIT_LIMIT = 1 << 22;
 
 KS_DEVICE uint32_t t5_smem(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -344,8 +345,8 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
                  int *__restrict__ err) {
   extern __shared__ __align__(1024) unsigned char sm[];
   int *erow = reinterpret_cast<int *>(sm + 2 * T5_STAGE);
-  int *etmp = erow + T5_M;
-  unsigned long long *full = reinterpret_cast<unsigned long long *>(etmp + T5_M);  // stage loaded (TMA bytes)
+  int *etmp = erow + T5_M;  // (T5_THREADS / T5_M - 1) x 128 partial maxima
+  unsigned long long *full = reinterpret_cast<unsigned long long *>(etmp + (T5_THREADS / T5_M - 1) * T5_M);
   unsigned long long *empty = full + 2;                                             // stage consumed (MMA commit)
   unsigned long long *vbar = empty + 2;                                             // V tile loaded (TMA bytes)
   uint32_t *tslot = reinterpret_cast<uint32_t *>(vbar + 1);
@@ -403,15 +404,20 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
     vpend = 0;  // (every thread waited)
     ok = __syncthreads_and(ok);
     if (!ok) break;
-    // 1. row exponents: e_r = 1 + floor(log2 max_k |hi|) from the float exponent fields (two threads per row)
+    // 1. row exponents: e_r = 1 + floor(log2 max_k |hi|) from the float exponent fields (four threads per row)
     {
+      constexpr int H = T5_THREADS / T5_M;
       const int m = tid & (T5_M - 1), h = tid >> 7;
       int E = 0;
       if (m < rows)
-        for (int k = h; k < K; k += 2) E = max(E, (int)((__float_as_uint(vt[(size_t)k * T5_M + m].x) >> 23) & 0xFFu));
-      if (h) etmp[m] = E;
+        for (int k = h; k < K; k += H) E = max(E, (int)((__float_as_uint(vt[(size_t)k * T5_M + m].x) >> 23) & 0xFFu));
+      if (h) etmp[(h - 1) * T5_M + m] = E;
       __syncthreads();
-      if (!h) erow[m] = max(E, etmp[m]);
+      if (!h) {
+#pragma unroll
+        for (int q = 0; q < H - 1; ++q) E = max(E, etmp[q * T5_M + m]);
+        erow[m] = E;
+      }
       __syncthreads();
     }
     // 2. all slices of the tile into the scratch, one core-matrix row (8 consecutive k of one row) per item, two
@@ -543,42 +549,37 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
       ok = __syncthreads_and(ok);
       if (!ok) break;
       t5_fence_after();
-      // 4. epilogue: warp w reads lanes 32 (w mod 4) .. +31 (tile rows), columns 32 (w / 4) .. +31 of the chunk
-      {
-        const int qd = warp & 3, hh = warp >> 2;
+      // 4. epilogue: warp w reads lanes 32 (w mod 4) .. +31 (tile rows), columns 16 (w / 4) .. +15 of the chunk
+      const int qd = warp & 3, col = 16 * (warp >> 2);
+      if (col < nch) {  // warp-uniform
         const int m = 32 * qd + lane;
         const int er = erow[m];
+        float sh[16], sl[16];
+#pragma unroll
+        for (int i2 = 0; i2 < 16; ++i2) sh[i2] = sl[i2] = 0.0f;
 #pragma unroll 1
-        for (int g = 0; g < 2; ++g) {
-          const int col = 32 * hh + 16 * g;
-          if (col >= nch) continue;  // warp-uniform
-          float sh[16], sl[16];
+        for (int L = OZ_L - 1; L >= 0; --L) {
+          float v[16];
+          t5_ld16(tbase + ((uint32_t)(32 * qd) << 16) + (uint32_t)(L * T5_NC + col), v);
+          // 2^(-7(L+2)) as a float (exponent field 127 - 7(L+2) >= 64): the level sums are integers below 2^24, so
+          // the product is exact and equals ldexpf(v, -7(L+2))
+          const float scale = __uint_as_float((uint32_t)(127 - 7 * (L + 2)) << 23);
 #pragma unroll
-          for (int i2 = 0; i2 < 16; ++i2) sh[i2] = sl[i2] = 0.0f;
-#pragma unroll 1
-          for (int L = OZ_L - 1; L >= 0; --L) {
-            float v[16];
-            t5_ld16(tbase + ((uint32_t)(32 * qd) << 16) + (uint32_t)(L * T5_NC + col), v);
-            // 2^(-7(L+2)) as a float (exponent field 127 - 7(L+2) >= 64): the level sums are integers below 2^24,
-            // so the product is exact and equals ldexpf(v, -7(L+2))
-            const float scale = __uint_as_float((uint32_t)(127 - 7 * (L + 2)) << 23);
+          for (int i2 = 0; i2 < 16; ++i2) oz_add(sh[i2], sl[i2], v[i2] * scale);
+        }
+        if (m < rows) {
 #pragma unroll
-            for (int i2 = 0; i2 < 16; ++i2) oz_add(sh[i2], sl[i2], v[i2] * scale);
-          }
-          if (m < rows) {
-#pragma unroll
-            for (int i2 = 0; i2 < 16; ++i2) {
-              const int c = c0 + col + i2;
-              if (c >= N) break;
-              float2 out = make_float2(0.0f, 0.0f);  // an all-zero row stays zero
-              if (er) {
-                const float hi = sh[i2] + sl[i2];
-                const float lo = sl[i2] - (hi - sh[i2]);
-                const int sc = (er - 126) + fcol[c];
-                out = make_float2(ldexpf(hi, sc), ldexpf(lo, sc));
-              }
-              V[(size_t)(r0 + m) + (size_t)(s0 + c) * ldv] = out;
+          for (int i2 = 0; i2 < 16; ++i2) {
+            const int c = c0 + col + i2;
+            if (c >= N) break;
+            float2 out = make_float2(0.0f, 0.0f);  // an all-zero row stays zero
+            if (er) {
+              const float hi = sh[i2] + sl[i2];
+              const float lo = sl[i2] - (hi - sh[i2]);
+              const int sc = (er - 126) + fcol[c];
+              out = make_float2(ldexpf(hi, sc), ldexpf(lo, sc));
             }
+            V[(size_t)(r0 + m) + (size_t)(s0 + c) * ldv] = out;
           }
         }
       }
