@@ -497,11 +497,11 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
                       Bsl + (((size_t)t * nk8 + kc8 + k8) * (np / 8) + c0 / 8) * 64, bbytes, &full[b]);
           fpend[b] = 1;
         };
+        // stage i's MMAs are queued before stage i+1 is loaded: the load waits for stage i-1's MMAs (its buffer),
+        // while the tensor pipe already holds stage i's
         load(0);
         for (int i = 0; i < nkc && ok; ++i) {
           const int b = i & 1;
-          if (i + 1 < nkc) load(i + 1);
-          if (!ok) break;
           if (!t5_wait(&full[b], fph[b])) {
             ok = 0;
             break;
@@ -511,6 +511,10 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
           t5_fence_after();
           const int sk8 = min(T5_KC / 8, nk8 - i * (T5_KC / 8));
           const uint32_t abase = t5_smem(sm + b * T5_STAGE), bbase = abase + OZ_SA * T5_ASL;
+          // descriptors of slice 0 at K-step 0; the others add their byte offset / 16 to the start-address field
+          // (shared addresses stay below 2^18, so the 14-bit field never carries)
+          const uint64_t ad0 = t5_desc(abase, 16 * 128, 128);
+          const uint64_t bd0 = t5_desc(bbase, (T5_NC / 8) * 128, 128);
           for (int j = 0; j < sk8 / 2; ++j)
 #pragma unroll
             for (int sa = 0; sa < OZ_SA; ++sa)
@@ -518,13 +522,14 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
               for (int tb = 0; tb < OZ_S; ++tb) {
                 if (sa + tb >= OZ_L) continue;
                 const int L = sa + tb;
-                const uint64_t ad = t5_desc(abase + sa * T5_ASL + j * 2 * (16 * 128), 16 * 128, 128);
-                const uint64_t bd = t5_desc(bbase + tb * T5_BSL + j * 2 * ((T5_NC / 8) * 128), (T5_NC / 8) * 128, 128);
+                const uint64_t ad = ad0 + (uint64_t)((sa * T5_ASL + j * 2 * (16 * 128)) >> 4);
+                const uint64_t bd = bd0 + (uint64_t)((tb * T5_BSL + j * 2 * ((T5_NC / 8) * 128)) >> 4);
                 t5_mma(tbase + (uint32_t)(L * T5_NC), ad, bd, idesc, (initmask >> L) & 1u);
                 initmask |= 1u << L;
               }
           t5_commit(&empty[b]);
           epend[b] = 1;
+          if (i + 1 < nkc) load(i + 1);
         }
         // every MMA of the chunk done (the commits track all earlier MMAs of this thread); after a timeout, also
         // every bulk copy still in flight (bounded waits)
