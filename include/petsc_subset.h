@@ -56,6 +56,7 @@ typedef int MPI_Comm; /* one process per GPU: communicators carry no information
 #define PETSC_ERR_PLIB 77
 #define PETSC_ERR_FILE_UNEXPECTED 79
 #define PETSC_ERR_CONV_FAILED 82
+#define PETSC_ERR_USER 83
 #define PETSC_ERR_ARG_NULL 85
 #define PETSC_ERR_USER_INPUT 91
 #define PETSC_ERR_GPU_RESOURCE 96
@@ -129,6 +130,21 @@ PetscErrorCode PetscViewerPushFormat(PetscViewer viewer, PetscViewerFormat forma
 PetscErrorCode PetscViewerPopFormat(PetscViewer viewer);
 PetscErrorCode PetscViewerGetFormat(PetscViewer viewer, PetscViewerFormat *format);
 PetscErrorCode PetscViewerASCIIPrintf(PetscViewer viewer, const char format[], ...);
+
+/* a viewer with the format a monitor prints in (petscviewer.h), and the context-destroy callback type */
+typedef struct {
+  PetscViewer viewer;
+  PetscViewerFormat format;
+  void *data; /* monitor-private state (EPSMonitorConverged: the previous nconv) */
+} PetscViewerAndFormat;
+PetscErrorCode PetscViewerAndFormatCreate(PetscViewer viewer, PetscViewerFormat format, PetscViewerAndFormat **vf);
+PetscErrorCode PetscViewerAndFormatDestroy(PetscViewerAndFormat **vf);
+typedef PetscErrorCode PetscCtxDestroyFn(void **ctx);
+
+/* object names (PetscObjectSetName): kept for EPS objects, whose MATLAB-format reports print them */
+typedef void *PetscObject;
+PetscErrorCode PetscObjectSetName(PetscObject obj, const char name[]);
+PetscErrorCode PetscObjectGetName(PetscObject obj, const char *name[]);
 
 /* --- Vec (petscvec.h) --- */
 PetscErrorCode VecCreateSeq(MPI_Comm comm, PetscInt n, Vec *v);

@@ -95,6 +95,24 @@ PetscErrorCode EPSComputeError(EPS eps, PetscInt i, EPSErrorType type, PetscReal
 PetscErrorCode EPSConvergedReasonView(EPS eps, PetscViewer viewer);
 PetscErrorCode EPSErrorView(EPS eps, EPSErrorType etype, PetscViewer viewer);
 PetscErrorCode EPSValuesView(EPS eps, PetscViewer viewer);
+/* monitors (epsmon.c): called after every restart with the restart count, the number converged, the nest current
+ * Ritz values (operator scaling undone) and their error estimates.  Up to 5 per EPS.  The built-ins print one line
+ * per restart to the viewer of their PetscViewerAndFormat: the first unconverged value (EPSMonitorFirst, option
+ * -eps_monitor), all values (EPSMonitorAll, -eps_monitor_all), or each value as it converges (EPSMonitorConverged,
+ * -eps_monitor_conv, whose context comes from EPSMonitorConvergedCreate). */
+typedef PetscErrorCode EPSMonitorFn(EPS eps, PetscInt its, PetscInt nconv, PetscScalar eigr[], PetscScalar eigi[],
+                                    PetscReal errest[], PetscInt nest, void *ctx);
+PetscErrorCode EPSMonitorSet(EPS eps, EPSMonitorFn *monitor, void *mctx, PetscCtxDestroyFn *monitordestroy);
+PetscErrorCode EPSMonitorCancel(EPS eps);
+PetscErrorCode EPSMonitorFirst(EPS eps, PetscInt its, PetscInt nconv, PetscScalar eigr[], PetscScalar eigi[],
+                               PetscReal errest[], PetscInt nest, PetscViewerAndFormat *vf);
+PetscErrorCode EPSMonitorAll(EPS eps, PetscInt its, PetscInt nconv, PetscScalar eigr[], PetscScalar eigi[],
+                             PetscReal errest[], PetscInt nest, PetscViewerAndFormat *vf);
+PetscErrorCode EPSMonitorConverged(EPS eps, PetscInt its, PetscInt nconv, PetscScalar eigr[], PetscScalar eigi[],
+                                   PetscReal errest[], PetscInt nest, PetscViewerAndFormat *vf);
+PetscErrorCode EPSMonitorConvergedCreate(PetscViewer viewer, PetscViewerFormat format, void *ctx,
+                                         PetscViewerAndFormat **vf);
+PetscErrorCode EPSMonitorConvergedDestroy(PetscViewerAndFormat **vf);
 PetscErrorCode EPSGetBV(EPS eps, BV *V);
 PetscErrorCode EPSGetDS(EPS eps, DS *ds);
 

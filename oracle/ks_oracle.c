@@ -1260,6 +1260,13 @@ int ksor_solve(int n, const int *rowptr, const int *colidx, const double *vals,
                         target, KSOR_CONV_REL, 0.0, 0.0, 1);
 }
 
+static ksor_monitor_fn g_monitor = NULL;
+static void *g_monitor_ctx = NULL;
+void ksor_set_monitor(ksor_monitor_fn fn, void *ctx) {
+  g_monitor = fn;
+  g_monitor_ctx = ctx;
+}
+
 int ksor_solve_gen(int n, const int *rowptr, const int *colidx, const double *vals, const double *bdiag,
                    int hermitian, int which, int nev, int ncv, int mpd, double tol, int max_it,
                    double keep, int lock, int nthreads, const double *v0, unsigned long long seed,
@@ -1377,6 +1384,8 @@ int ksor_solve_gen(int n, const int *rowptr, const int *colidx, const double *va
       if (marker != -1) break;
     }
     if (marker != -1) k = marker;
+    /* EPSMonitor (krylovschur.c, after EPSKrylovConvergence): its, nconv, all nv values and estimates */
+    if (g_monitor) g_monitor(its, k, eigr, eigi, errest, nv, g_monitor_ctx);
     /* EPSStoppingBasic */
     if (k >= nev) reason = KSOR_CONVERGED_TOL;
     else if (its >= max_it) reason = KSOR_DIVERGED_ITS;

@@ -57,6 +57,12 @@ int ksor_solve_gen(int n, const int *rowptr, const int *colidx, const double *va
                    int *info, int ncv_cap, double *eigr, double *eigi, double *errest, double *X,
                    int harmonic, double target, int conv, double nrma, double nrmb, int purify);
 
+/* A monitor called by the solves after every restart, as EPSMonitor is (epsmon.c:40-48): restart count, number
+ * converged, the nest current values and error estimates.  NULL turns it off.  Not thread-safe (one global). */
+typedef void (*ksor_monitor_fn)(int its, int nconv, const double *eigr, const double *eigi, const double *errest,
+                                int nest, void *ctx);
+void ksor_set_monitor(ksor_monitor_fn fn, void *ctx);
+
 /* y = A x (CSR), the operation MatMult performs for AIJ. */
 void ksor_spmv(int n, const int *rowptr, const int *colidx, const double *vals, const double *x, double *y,
                int nthreads);

@@ -103,6 +103,11 @@ def load():
         "PetscViewerPushFormat": ([P, I], I),
         "PetscViewerPopFormat": ([P], I),
         "EPSErrorView": ([P, I, P], I),
+        "SlepcInitialize": ([ctypes.POINTER(I), ctypes.POINTER(ctypes.POINTER(ctypes.c_char_p)), P, P], I),
+        "EPSSetFromOptions": ([P], I),
+        "PetscObjectSetName": ([P, ctypes.c_char_p], I),
+        "EPSMonitorSet": ([P, P, P, P], I),
+        "EPSMonitorCancel": ([P], I),
         "EPSConvergedReasonView": ([P, P], I),
         "EPSValuesView": ([P, P], I),
     }
@@ -112,6 +117,25 @@ def load():
         f.restype = res
     _lib = lib
     return lib
+
+
+_argv_keep = None
+
+
+def initialize(argv):
+    """SlepcInitialize with this argument list (argv[0] is the program name); EPS.setFromOptions reads it."""
+    global _argv_keep
+    arr = (ctypes.c_char_p * (len(argv) + 1))(*[a.encode() for a in argv], None)
+    argc = ctypes.c_int(len(argv))
+    parr = ctypes.cast(arr, ctypes.POINTER(ctypes.c_char_p))
+    _argv_keep = (arr, argc, parr)
+    _check(load().SlepcInitialize(ctypes.byref(argc), ctypes.byref(parr), None, None), "SlepcInitialize")
+
+
+# EPSMonitorFn: (eps, its, nconv, eigr, eigi, errest, nest, ctx) -> PetscErrorCode
+MONITOR_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                              ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                              ctypes.POINTER(ctypes.c_double), ctypes.c_int, ctypes.c_void_p)
 
 
 def _check(code, where):
@@ -330,6 +354,30 @@ class EPS:
         if isinstance(which, str):
             which = self.WHICH_NAMES[which]
         _check(load().EPSSetWhichEigenpairs(self.handle, int(which)), "EPSSetWhichEigenpairs")
+
+    def setFromOptions(self):
+        _check(load().EPSSetFromOptions(self.handle), "EPSSetFromOptions")
+
+    def setName(self, name):
+        """PetscObjectSetName: the name MATLAB-format reports print."""
+        _check(load().PetscObjectSetName(self.handle, name.encode()), "PetscObjectSetName")
+
+    def monitorSet(self, fn):
+        """EPSMonitorSet with a Python callable fn(its, nconv, eigr, eigi, errest) called after every restart."""
+        def _c(_eps, its, nconv, er, ei, es, nest, _ctx):
+            try:
+                fn(its, nconv, np.ctypeslib.as_array(er, (nest,)).copy(), np.ctypeslib.as_array(ei, (nest,)).copy(),
+                   np.ctypeslib.as_array(es, (nest,)).copy())
+                return 0
+            except Exception:  # a failing monitor aborts the solve with PETSC_ERR_USER
+                return 83
+        cb = MONITOR_FN(_c)
+        self._monitors = getattr(self, "_monitors", []) + [cb]
+        _check(load().EPSMonitorSet(self.handle, ctypes.cast(cb, ctypes.c_void_p), None, None), "EPSMonitorSet")
+
+    def monitorCancel(self):
+        _check(load().EPSMonitorCancel(self.handle), "EPSMonitorCancel")
+        self._monitors = []
 
     def setInitialSpace(self, space):
         if space is None or (isinstance(space, (list, tuple)) and len(space) == 0):

@@ -548,9 +548,52 @@ static void eps_drop_operator(EPS e) {
   e->op = nullptr;
 }
 
+// EPSMonitorSet / EPSMonitorCancel (epsmon.c:62-130): up to 5 monitors, called after every restart
+extern "C" PetscErrorCode EPSMonitorSet(EPS eps, EPSMonitorFn *monitor, void *mctx, PetscCtxDestroyFn *monitordestroy) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  KSG_CHECK(eps->mon.size() < 5, PETSC_ERR_ARG_OUTOFRANGE, "Too many EPS monitors set");
+  if (!monitor) return 0;
+  eps->mon.push_back(monitor);
+  eps->mon_ctx.push_back(mctx);
+  eps->mon_destroy.push_back(monitordestroy);
+  return 0;
+}
+extern "C" PetscErrorCode EPSMonitorCancel(EPS eps) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  PetscErrorCode first = 0;
+  for (size_t i = 0; i < eps->mon.size(); ++i)
+    if (eps->mon_destroy[i]) {
+      void *c = eps->mon_ctx[i];
+      const PetscErrorCode e = eps->mon_destroy[i](&c);
+      if (e && !first) first = e;
+    }
+  eps->mon.clear();
+  eps->mon_ctx.clear();
+  eps->mon_destroy.clear();
+  return first;
+}
+
+// EPSMonitor (epsmon.c:40-48) after a restart: the nest current Ritz values (operator scaling undone) and their error
+// estimates, read from the device
+static PetscErrorCode eps_run_monitors(EPS eps, int its, int nconv, int nest, cudaStream_t s) {
+  std::vector<double> er(nest), ei(nest), es(nest);
+  KSG_CUDA(cudaMemcpyAsync(er.data(), eps->eigr.p, sizeof(double) * nest, cudaMemcpyDeviceToHost, s));
+  KSG_CUDA(cudaMemcpyAsync(ei.data(), eps->eigi.p, sizeof(double) * nest, cudaMemcpyDeviceToHost, s));
+  KSG_CUDA(cudaMemcpyAsync(es.data(), eps->errest.p, sizeof(double) * nest, cudaMemcpyDeviceToHost, s));
+  KSG_CUDA(cudaStreamSynchronize(s));
+  for (int i = 0; i < nest; ++i) {
+    er[i] /= eps->opscale;
+    ei[i] = ksg_eps_hermitian(eps) && eps->extraction != EPS_HARMONIC ? 0.0 : ei[i] / eps->opscale;
+  }
+  for (size_t m = 0; m < eps->mon.size(); ++m)
+    KSG_TRY(eps->mon[m](eps, its, nconv, er.data(), ei.data(), es.data(), nest, eps->mon_ctx[m]));
+  return 0;
+}
+
 extern "C" PetscErrorCode EPSDestroy(EPS *eps) {
   if (!eps || !*eps) return 0;
   EPS e = *eps;
+  EPSMonitorCancel(e);
   if (e->device >= 0) cudaSetDevice(e->device);
   eps_free_device(e);
   for (cudaEvent_t ev : e->ev_pool) cudaEventDestroy(ev);
@@ -850,7 +893,33 @@ extern "C" PetscErrorCode EPSSetFromOptions(EPS eps) {
     else if (!strcmp(o, "-eps_conv_abs")) KSG_TRY(EPSSetConvergenceTest(eps, EPS_CONV_ABS));
     else if (!strcmp(o, "-eps_conv_rel")) KSG_TRY(EPSSetConvergenceTest(eps, EPS_CONV_REL));
     else if (!strcmp(o, "-eps_conv_norm")) KSG_TRY(EPSSetConvergenceTest(eps, EPS_CONV_NORM));
-    else if (!strcmp(o, "-eps_purify"))
+    else if (!strcmp(o, "-eps_monitor") || !strcmp(o, "-eps_monitor_all") || !strcmp(o, "-eps_monitor_conv")) {
+      const bool has_spec = v && v[0] != '-';
+      KSG_TRY(ksg_eps_monitor_from_spec(eps, !strcmp(o, "-eps_monitor") ? 0 : !strcmp(o, "-eps_monitor_all") ? 1 : 2,
+                                        has_spec ? v : nullptr));
+    } else if (!strcmp(o, "-eps_converged_reason") || !strcmp(o, "-eps_error_absolute") ||
+               !strcmp(o, "-eps_error_relative") || !strcmp(o, "-eps_error_backward") ||
+               !strcmp(o, "-eps_view_values")) {
+      // reports printed at the end of EPSSolve (EPSConvergedReasonViewFromOptions, EPSErrorViewFromOptions,
+      // EPSValuesViewFromOptions); the value is a viewer "[ascii][:file][:format]"
+      const bool has_spec = v && v[0] != '-';
+      PetscViewer pv_viewer;
+      PetscViewerFormat fmt;
+      int ok = 0;
+      KSG_TRY(ksg_viewer_from_spec(has_spec ? v : nullptr, &pv_viewer, &fmt, &ok));
+      std::string file = pv_viewer->borrowed ? std::string() : std::string(pv_viewer->name);
+      if (!pv_viewer->borrowed) KSG_TRY(PetscViewerDestroy(&pv_viewer));
+      if (ok) {
+        EPSPostView pv;
+        pv.kind = !strcmp(o, "-eps_converged_reason") ? 0 : !strcmp(o, "-eps_view_values") ? 2 : 1;
+        pv.etype = !strcmp(o, "-eps_error_absolute") ? EPS_ERROR_ABSOLUTE
+                   : !strcmp(o, "-eps_error_backward") ? EPS_ERROR_BACKWARD
+                                                       : EPS_ERROR_RELATIVE;
+        pv.format = fmt;
+        pv.file = file;
+        eps->post_views.push_back(pv);
+      }
+    } else if (!strcmp(o, "-eps_purify"))
       KSG_TRY(EPSSetPurify(eps, (v && (!strcmp(v, "0") || !strcmp(v, "false"))) ? PETSC_FALSE : PETSC_TRUE));
     else if (!strcmp(o, "-eps_krylovschur_restart") && v) KSG_TRY(EPSKrylovSchurSetRestart(eps, atof(v)));
     else if (!strcmp(o, "-eps_krylovschur_locking") && v) KSG_TRY(EPSKrylovSchurSetLocking(eps, atoi(v) ? PETSC_TRUE : PETSC_FALSE));
@@ -1459,6 +1528,7 @@ static PetscErrorCode eps_solve_core(EPS eps, double tol, std::chrono::steady_cl
     l = c.l;
     reason = c.reason;
     nv = c.nv;
+    if (!eps->mon.empty()) KSG_TRY(eps_run_monitors(eps, its, k, nv, s));
     if (harmonic && reason == 0 && !(c.breakdown || k == nv)) {
       // undo the harmonic translation on the residual vector (krylovschur.c:312-315): gamma u^ = u - V(:,0:nv) g~,
       // with g~ from the projected solver (work) and gamma in the control block; the BVMultVec form of the
@@ -1632,6 +1702,7 @@ extern "C" PetscErrorCode EPSSolve(EPS eps) {
   eps->solved = 1;
   eps->stats.bytes_moved = bytes;
   eps->stats.solve_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (!eps->post_views.empty()) KSG_TRY(ksg_eps_post_views(eps));
   return 0;
 }
 

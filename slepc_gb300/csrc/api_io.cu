@@ -18,14 +18,6 @@
 
 #include "internal.h"
 
-struct _p_PetscViewer {
-  FILE *f = nullptr;
-  PetscFileMode mode = FILE_MODE_READ;
-  std::string name;
-  int ascii = 0;     // PETSCVIEWERASCII (text reports) rather than PETSCVIEWERBINARY
-  int borrowed = 0;  // the process-wide stdout viewer: never closed, PetscViewerDestroy only clears the handle
-  std::vector<PetscViewerFormat> formats;  // PetscViewerPushFormat stack
-};
 
 namespace {
 
@@ -307,6 +299,17 @@ PetscErrorCode emit(PetscViewer v, const Text &t) {
   return 0;
 }
 
+// the name MATLAB-format reports print: the one given by PetscObjectSetName, else "eps"
+const char *eps_name(EPS eps) { return eps->name.empty() ? "eps" : eps->name.c_str(); }
+
+// %g as PETSc's ASCII viewers print it: a value that prints as an integer gets a trailing decimal point ("20.")
+void add_g(Text &t, double x) {
+  char buf[64];
+  std::snprintf(buf, sizeof(buf), "%g", x);
+  if (!std::strpbrk(buf, ".eEni")) std::strncat(buf, ".", sizeof(buf) - std::strlen(buf) - 1);
+  t.s += buf;
+}
+
 const char *reason_name(int reason) {
   switch (reason) {
     case EPS_CONVERGED_TOL: return "CONVERGED_TOL";
@@ -429,8 +432,9 @@ extern "C" PetscErrorCode EPSErrorView(EPS eps, EPSErrorType etype, PetscViewer 
   } else if (fmt == PETSC_VIEWER_ASCII_INFO_DETAIL) {
     if (!nconv) return 0;
     const char *sep = " ---------------------- --------------------\n";
-    const char *head = etype == EPS_ERROR_ABSOLUTE   ? "   ||Ax-kx||"
-                       : etype == EPS_ERROR_RELATIVE ? "||Ax-kx||/||kx||"
+    const bool gen = eps->B != nullptr;
+    const char *head = etype == EPS_ERROR_ABSOLUTE   ? (gen ? "   ||Ax-kBx||" : "   ||Ax-kx||")
+                       : etype == EPS_ERROR_RELATIVE ? (gen ? "||Ax-kBx||/||kx||" : "||Ax-kx||/||kx||")
                                                      : "    eta(x,k)";
     t.add("%s            k             %s\n%s", sep, head, sep);
     for (PetscInt i = 0; i < nconv; ++i) {
@@ -442,6 +446,15 @@ extern "C" PetscErrorCode EPSErrorView(EPS eps, EPSErrorType etype, PetscViewer 
       else t.add("    % 12f           %12g\n", kr, err);
     }
     t.add("%s", sep);
+  } else if (fmt == PETSC_VIEWER_ASCII_MATLAB) {
+    // EPSErrorView_MATLAB (epsview.c:372-388)
+    t.add("Error_%s = [\n", eps_name(eps));
+    for (PetscInt i = 0; i < nconv; ++i) {
+      PetscReal err = 0.0;
+      KSG_TRY(EPSComputeError(eps, i, etype, &err));
+      t.add("%18.16e\n", err);
+    }
+    t.add("];\n");
   }
   return emit(v, t);
 }
@@ -455,6 +468,18 @@ extern "C" PetscErrorCode EPSValuesView(EPS eps, PetscViewer v) {
   PetscInt nconv = 0;
   KSG_TRY(EPSGetConverged(eps, &nconv));
   Text t;
+  if (top_format(v) == PETSC_VIEWER_ASCII_MATLAB) {
+    // EPSValuesView_MATLAB (epsview.c:619-646)
+    t.add("Lambda_%s = [\n", eps_name(eps));
+    for (PetscInt i = 0; i < nconv; ++i) {
+      PetscScalar kr = 0.0, ki = 0.0;
+      KSG_TRY(EPSGetEigenvalue(eps, i, &kr, &ki));
+      if (ki != 0.0) t.add("%18.16e%+18.16ei\n", kr, ki);
+      else t.add("%18.16e\n", kr);
+    }
+    t.add("];\n");
+    return emit(v, t);
+  }
   t.add("Eigenvalues = \n");
   for (PetscInt i = 0; i < nconv; ++i) {
     PetscScalar kr = 0.0, ki = 0.0;
@@ -465,4 +490,205 @@ extern "C" PetscErrorCode EPSValuesView(EPS eps, PetscViewer v) {
   }
   t.add("\n");
   return emit(v, t);
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// object names, viewer-and-format pairs, and the EPS monitors of epsmon.c
+// ---------------------------------------------------------------------------------------------------------------
+extern "C" PetscErrorCode PetscObjectSetName(PetscObject obj, const char name[]) {
+  KSG_CHECK(obj && name, PETSC_ERR_ARG_NULL, "Null argument");
+  if (*static_cast<const unsigned *>(obj) == KSG_EPS_COOKIE) static_cast<EPS>(obj)->name = name;
+  return 0;  // names of other objects are not printed anywhere
+}
+
+extern "C" PetscErrorCode PetscObjectGetName(PetscObject obj, const char *name[]) {
+  KSG_CHECK(obj && name, PETSC_ERR_ARG_NULL, "Null argument");
+  *name = (*static_cast<const unsigned *>(obj) == KSG_EPS_COOKIE) ? eps_name(static_cast<EPS>(obj)) : "";
+  return 0;
+}
+
+namespace {
+// every PetscViewerAndFormat is allocated with this tail: whether it owns its viewer (options-created file viewers)
+struct VfBox {
+  PetscViewerAndFormat vf;
+  int owns_viewer;
+  PetscInt oldnconv;  // EPSMonitorConverged
+};
+}  // namespace
+
+extern "C" PetscErrorCode PetscViewerAndFormatCreate(PetscViewer viewer, PetscViewerFormat format,
+                                                     PetscViewerAndFormat **vf) {
+  KSG_CHECK(vf, PETSC_ERR_ARG_NULL, "Null argument");
+  VfBox *b = new VfBox();
+  b->vf.viewer = viewer ? viewer : stdout_viewer();
+  b->vf.format = format;
+  b->vf.data = nullptr;
+  *vf = &b->vf;
+  return 0;
+}
+
+extern "C" PetscErrorCode PetscViewerAndFormatDestroy(PetscViewerAndFormat **vf) {
+  if (!vf || !*vf) return 0;
+  VfBox *b = reinterpret_cast<VfBox *>(*vf);
+  if (b->owns_viewer) KSG_TRY(PetscViewerDestroy(&b->vf.viewer));
+  delete b;
+  *vf = nullptr;
+  return 0;
+}
+
+extern "C" PetscErrorCode EPSMonitorConvergedCreate(PetscViewer viewer, PetscViewerFormat format, void *,
+                                                    PetscViewerAndFormat **vf) {
+  KSG_TRY(PetscViewerAndFormatCreate(viewer, format, vf));
+  reinterpret_cast<VfBox *>(*vf)->vf.data = &reinterpret_cast<VfBox *>(*vf)->oldnconv;
+  return 0;
+}
+
+extern "C" PetscErrorCode EPSMonitorConvergedDestroy(PetscViewerAndFormat **vf) {
+  return PetscViewerAndFormatDestroy(vf);
+}
+
+namespace {
+// one monitor line's eigenvalue: " %g", then "%+gi" for a nonzero imaginary part (epsmon.c:205-212)
+void add_monitor_value(Text &t, double er, double ei) {
+  t.s += ' ';
+  add_g(t, er);
+  if (ei != 0.0) {
+    char buf[64];
+    std::snprintf(buf, sizeof(buf), "%+g", ei);
+    t.s += buf;
+    if (!std::strpbrk(buf + 1, ".eEni")) t.s += '.';
+    t.s += 'i';
+  }
+}
+
+PetscErrorCode monitor_viewer(EPS eps, PetscViewerAndFormat *vf, PetscViewer *v) {
+  KSG_CHECK(eps && vf, PETSC_ERR_ARG_NULL, "Null argument");
+  *v = vf->viewer ? vf->viewer : stdout_viewer();
+  return 0;
+}
+}  // namespace
+
+// EPSMonitorFirst (epsmon.c:183-220): the first unconverged value and its error estimate
+extern "C" PetscErrorCode EPSMonitorFirst(EPS eps, PetscInt its, PetscInt nconv, PetscScalar eigr[],
+                                          PetscScalar eigi[], PetscReal errest[], PetscInt nest,
+                                          PetscViewerAndFormat *vf) {
+  PetscViewer v;
+  KSG_TRY(monitor_viewer(eps, vf, &v));
+  if (!v->ascii || nconv >= nest) return 0;
+  Text t;
+  t.add("%3d EPS nconv=%d first unconverged value (error)", (int)its, (int)nconv);
+  add_monitor_value(t, eigr[nconv], eigi[nconv]);
+  t.add(" (%10.8e)\n", errest[nconv]);
+  return emit(v, t);
+}
+
+// EPSMonitorAll (epsmon.c:236-270): every current value and error estimate
+extern "C" PetscErrorCode EPSMonitorAll(EPS eps, PetscInt its, PetscInt nconv, PetscScalar eigr[], PetscScalar eigi[],
+                                        PetscReal errest[], PetscInt nest, PetscViewerAndFormat *vf) {
+  PetscViewer v;
+  KSG_TRY(monitor_viewer(eps, vf, &v));
+  if (!v->ascii) return 0;
+  Text t;
+  t.add("%3d EPS nconv=%d Values (Errors)", (int)its, (int)nconv);
+  for (PetscInt i = 0; i < nest; ++i) {
+    add_monitor_value(t, eigr[i], eigi[i]);
+    t.add(" (%10.8e)", errest[i]);
+  }
+  t.add("\n");
+  return emit(v, t);
+}
+
+// EPSMonitorConverged (epsmon.c:291-330): each value once, in the restart where it converged
+extern "C" PetscErrorCode EPSMonitorConverged(EPS eps, PetscInt its, PetscInt nconv, PetscScalar eigr[],
+                                              PetscScalar eigi[], PetscReal errest[], PetscInt,
+                                              PetscViewerAndFormat *vf) {
+  PetscViewer v;
+  KSG_TRY(monitor_viewer(eps, vf, &v));
+  KSG_CHECK(vf->data, PETSC_ERR_ARG_WRONG, "EPSMonitorConverged needs the context of EPSMonitorConvergedCreate");
+  PetscInt *old = static_cast<PetscInt *>(vf->data);
+  if (its == 1) *old = 0;
+  if (!v->ascii || *old == nconv) return 0;
+  Text t;
+  for (PetscInt i = *old; i < nconv; ++i) {
+    t.add("%3d EPS converged value (error) #%d", (int)its, (int)i);
+    add_monitor_value(t, eigr[i], eigi[i]);
+    t.add(" (%10.8e)\n", errest[i]);
+  }
+  *old = nconv;
+  return emit(v, t);
+}
+
+// A viewer from an options value "[ascii][:file][:format]" (PetscOptionsCreateViewer): stdout unless a file is
+// named (opened for appending, owned by the caller); the draw and binary viewer types are not provided (*ok = 0)
+PetscErrorCode ksg_viewer_from_spec(const char *spec, PetscViewer *viewer, PetscViewerFormat *format, int *ok) {
+  *viewer = stdout_viewer();
+  *format = PETSC_VIEWER_DEFAULT;
+  *ok = 1;
+  if (!spec || !*spec) return 0;
+  std::string sp(spec), type, file, fmt;
+  const size_t c1 = sp.find(':');
+  type = sp.substr(0, c1);
+  if (c1 != std::string::npos) {
+    const size_t c2 = sp.find(':', c1 + 1);
+    file = sp.substr(c1 + 1, c2 == std::string::npos ? std::string::npos : c2 - c1 - 1);
+    if (c2 != std::string::npos) fmt = sp.substr(c2 + 1);
+  }
+  if (!type.empty() && type != "ascii") {
+    *ok = 0;
+    return 0;
+  }
+  if (fmt == "ascii_info") *format = PETSC_VIEWER_ASCII_INFO;
+  else if (fmt == "ascii_info_detail") *format = PETSC_VIEWER_ASCII_INFO_DETAIL;
+  else if (fmt == "ascii_matlab") *format = PETSC_VIEWER_ASCII_MATLAB;
+  else if (fmt == "failed") *format = PETSC_VIEWER_FAILED;
+  else KSG_CHECK(fmt.empty() || fmt == "default", PETSC_ERR_SUP, "Unsupported viewer format %s", fmt.c_str());
+  if (!file.empty() && file != "stdout") {
+    FILE *f = file == "stderr" ? stderr : std::fopen(file.c_str(), "a");
+    KSG_CHECK(f, PETSC_ERR_FILE_OPEN, "Cannot open file %s", file.c_str());
+    PetscViewer v = new _p_PetscViewer();
+    v->f = f;
+    v->mode = FILE_MODE_APPEND;
+    v->name = file;
+    v->ascii = 1;
+    *viewer = v;
+  }
+  return 0;
+}
+
+// a monitor from the options database (-eps_monitor[_all|_conv] [spec]): kind 0 first, 1 all, 2 converged
+PetscErrorCode ksg_eps_monitor_from_spec(EPS eps, int kind, const char *spec) {
+  PetscViewer v;
+  PetscViewerFormat f;
+  int ok;
+  KSG_TRY(ksg_viewer_from_spec(spec, &v, &f, &ok));
+  if (!ok) return 0;  // draw and binary monitors are not provided: nothing is printed
+  PetscViewerAndFormat *vf;
+  if (kind == 2) KSG_TRY(EPSMonitorConvergedCreate(v, f, nullptr, &vf));
+  else KSG_TRY(PetscViewerAndFormatCreate(v, f, &vf));
+  reinterpret_cast<VfBox *>(vf)->owns_viewer = !v->borrowed;
+  EPSMonitorFn *fn = kind == 0   ? reinterpret_cast<EPSMonitorFn *>(EPSMonitorFirst)
+                     : kind == 1 ? reinterpret_cast<EPSMonitorFn *>(EPSMonitorAll)
+                                 : reinterpret_cast<EPSMonitorFn *>(EPSMonitorConverged);
+  PetscErrorCode ierr = EPSMonitorSet(eps, fn, vf, reinterpret_cast<PetscCtxDestroyFn *>(PetscViewerAndFormatDestroy));
+  if (ierr) PetscViewerAndFormatDestroy(&vf);
+  return ierr;
+}
+
+// the reports EPSSolve prints when it ends (epssolve.c:182-186: converged reason, errors, values)
+PetscErrorCode ksg_eps_post_views(EPS eps) {
+  for (const EPSPostView &pv : eps->post_views) {
+    PetscViewer v;
+    PetscViewerFormat f;
+    int ok;
+    std::string spec = pv.file.empty() ? std::string() : "ascii:" + pv.file;
+    KSG_TRY(ksg_viewer_from_spec(spec.c_str(), &v, &f, &ok));
+    v->formats.push_back(pv.format);
+    PetscErrorCode ierr = pv.kind == 0   ? EPSConvergedReasonView(eps, v)
+                          : pv.kind == 1 ? EPSErrorView(eps, (EPSErrorType)pv.etype, v)
+                                         : EPSValuesView(eps, v);
+    v->formats.pop_back();
+    if (!v->borrowed) PetscViewerDestroy(&v);
+    KSG_TRY(ierr);
+  }
+  return 0;
 }

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <cstdio>
 #include <string>
 #include <vector>
 
@@ -83,6 +84,15 @@ struct _p_Mat {
   double norm_inf = -1.0;
 };
 
+struct _p_PetscViewer {
+  FILE *f = nullptr;
+  PetscFileMode mode = FILE_MODE_READ;
+  std::string name;
+  int ascii = 0;     // PETSCVIEWERASCII (text reports) rather than PETSCVIEWERBINARY
+  int borrowed = 0;  // the process-wide stdout viewer: never closed, PetscViewerDestroy only clears the handle
+  std::vector<PetscViewerFormat> formats;  // PetscViewerPushFormat stack
+};
+
 struct _p_Vec {
   int n = 0;
   std::vector<double> own;
@@ -97,7 +107,19 @@ PetscErrorCode ksg_random_fill(double *host, int n, unsigned long long seed, uns
 struct _p_DS;
 struct _p_BV;
 
+constexpr unsigned KSG_EPS_COOKIE = 0x31535045u;  // the first word of every EPS (PetscObjectSetName checks it)
+
+// a report EPSSolve prints when it ends (options -eps_converged_reason, -eps_error_*, -eps_view_values)
+struct EPSPostView {
+  int kind;  // 0 converged reason, 1 error view (etype), 2 values view
+  int etype;
+  PetscViewerFormat format;
+  std::string file;  // empty: stdout
+};
+
 struct _p_EPS {
+  unsigned cookie = KSG_EPS_COOKIE;
+  std::string name;  // PetscObjectSetName
   // configuration
   Mat A = nullptr;
   Mat B = nullptr;  // generalised problems: a diagonal B (EPSSetOperators)
@@ -162,6 +184,11 @@ struct _p_EPS {
   long long prof_launches[EPS_GB300_K_COUNT] = {0};
   BV bv = nullptr;
   DS ds = nullptr;
+  // monitors (EPSMonitorSet) and the reports to print at the end of EPSSolve
+  std::vector<EPSMonitorFn *> mon;
+  std::vector<void *> mon_ctx;
+  std::vector<PetscCtxDestroyFn *> mon_destroy;
+  std::vector<EPSPostView> post_views;
 };
 
 // the Lanczos (symmetric) variant runs for EPS_HEP with Ritz extraction; harmonic extraction runs the Arnoldi
@@ -190,4 +217,9 @@ PetscErrorCode ksg_eps_new_start_vector(EPS eps, int col, int *breakdown);
 PetscErrorCode ksg_eps_assemble(EPS eps, int nconv, const double *er, const double *ei, const double *es,
                                 cudaStream_t s);
 size_t ksg_part_stride(int ld);
+// options support (api_io.cu): a viewer from "[ascii][:file][:format]"; a built-in monitor (kind 0 first, 1 all,
+// 2 converged); the reports requested for the end of EPSSolve
+PetscErrorCode ksg_viewer_from_spec(const char *spec, PetscViewer *viewer, PetscViewerFormat *format, int *ok);
+PetscErrorCode ksg_eps_monitor_from_spec(EPS eps, int kind, const char *spec);
+PetscErrorCode ksg_eps_post_views(EPS eps);
 size_t ksg_part_blocks(int n);

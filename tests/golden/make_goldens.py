@@ -83,6 +83,13 @@ def main():
     g["test1_1"] = {"source": "src/eps/tests/output/test1_1.out", "grid": [18, 18], "nev": 4, "tol": 1e-10,
                     "conv": "norm", "max_it": 1500, "which": "LM", "eigenvalues": floats(line),
                     "orthogonality": "Level of orthogonality below the tolerance" in txt}
+    # -eps_monitor and -eps_view_values ::ascii_matlab on diag(1..20), LR, nev 1 (src/eps/tests/test23.c TEST 2);
+    # the test's filter replaced the error estimates with "removed"
+    lines = read("src/eps/tests/output/test23_2.out").splitlines()
+    g["test23_2"] = {"source": "src/eps/tests/output/test23_2.out", "n": 20, "which": "LR", "nev": 1,
+                     "monitor": [l for l in lines if "EPS nconv=" in l],
+                     "values_matlab": [l.strip() for l in lines if "Lambda_" in l or l.strip().endswith("e+01")
+                                       or l.strip() == "];"]}
     # the text EPSErrorView prints (the "All requested ..." line and the eigenvalue line), per solve of each test
     for key in ("ex2_1", "ex9_1", "ex4_1", "test2_1", "test2_3", "test1_1"):
         lines = read(g[key]["source"]).splitlines()

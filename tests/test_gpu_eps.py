@@ -4,6 +4,7 @@ Tolerances: eigenvalues |lam - lam_ref| / |lam_ref| <= 1e-10 (set-based: degener
 distinct eigenvalue, as the reference's ex2_1.out shows), relative residual ||Ax - lam x|| / (||A|| |lam|) <= tol,
 ||V^T V - I||_max <= 1e-12."""
 import json
+import re
 import os
 
 import numpy as np
@@ -364,3 +365,42 @@ def test_error_view_prints_the_reference_text(lib, tmp_path):
         values = eps.valuesView().splitlines()
         assert values[0] == "Eigenvalues = " and len(values) == nconv + 2 and values[-1] == ""
         assert values[1] == "   " + want[1].split(",")[0].strip()
+
+
+def test_monitor_and_matlab_values_test23(lib, orc, tmp_path):
+    """test23.c TEST 2 on the device: diag(1..20), -eps_largest_real -eps_monitor -eps_view_values ::ascii_matlab
+    given as options.  The monitor lines, after the test's own filter of the error estimates, are the reference's
+    two lines; the restart-by-restart values follow the oracle's monitor; the MATLAB values report is the
+    reference's."""
+    g = G["test23_2"]
+    n = g["n"]
+    rp, ci, va = np.arange(n + 1, dtype=np.int32), np.arange(n, dtype=np.int32), np.arange(1, n + 1, dtype=float)
+    v0 = matgen.start_vector(n, 1)
+    mon, val = tmp_path / "mon.txt", tmp_path / "val.txt"
+    sg.initialize(["test23", "-eps_largest_real", "-eps_monitor", ":" + str(mon),
+                   "-eps_view_values", ":" + str(val) + ":ascii_matlab"])
+    try:
+        A = sg.Mat(rp, ci, va)
+        eps = sg.EPS().create()
+        eps.setOperators(A)
+        eps.setName("eps")
+        eps.setFromOptions()
+        eps.setInitialSpace(v0)
+        seen = []
+        eps.monitorSet(lambda its, nconv, er, ei, es: seen.append((its, nconv, er.copy(), es.copy())))
+        eps.solve()
+        assert eps.getConvergedReason() == 1
+    finally:
+        sg.initialize(["prog"])
+    lines = mon.read_text().splitlines()
+    assert [re.sub(r"[0-9]\.[0-9]*e-([0-9]*)", "removed", l) for l in lines] == g["monitor"]
+    ref = []
+    r = orc.solve(rp, ci, va, hermitian=False, which="LR", nev=1, tol=1e-8, v0=v0,
+                  monitor=lambda its, nconv, er, ei, es, nest: ref.append((its, nconv, list(er), list(es))))
+    assert r.reason == 1 and len(seen) == len(ref) == eps.getIterationNumber()
+    for (its, k, er, es), (its_r, k_r, er_r, es_r) in zip(seen, ref):
+        assert its == its_r and k == k_r and len(er) == len(er_r)
+        assert np.allclose(er, er_r, rtol=1e-9, atol=0)
+    vals = [l.strip() for l in val.read_text().splitlines()]
+    fixed = [re.sub(r"^(2\.[0-9]*e\+01|1\.9999999999[0-9]*e\+01)$", "2.0000000000000000e+01", l) for l in vals]
+    assert fixed == g["values_matlab"]

@@ -75,3 +75,100 @@ def test_binary_calls_reject_ascii_viewers(lib, tmp_path):
     assert lib.MatLoad(A, v) == PETSC_ERR_SUP
     assert lib.MatDestroy(ctypes.byref(A)) == 0
     assert lib.PetscViewerDestroy(ctypes.byref(v)) == 0
+
+
+# -------------------------------------------------------------------------------------------------------------
+# monitors: the built-in printers called directly (host code), against the reference's printed monitor lines
+# -------------------------------------------------------------------------------------------------------------
+import json  # noqa: E402
+import os  # noqa: E402
+import re  # noqa: E402
+
+G = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_outputs.json")))
+D = ctypes.c_double
+
+
+def removed(line):
+    """test23.c's output filter: error estimates become 'removed'."""
+    return re.sub(r"[0-9]\.[0-9]*e-([0-9]*)", "removed", line)
+
+
+def call_monitor(lib, name, vf, its, nconv, er, ei, es):
+    n = len(er)
+    f = getattr(lib, name)
+    f.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(D), ctypes.POINTER(D), ctypes.POINTER(D),
+                  ctypes.c_int, P]
+    eps = sg.EPS().create()
+    rc = f(eps.handle, its, nconv, (D * n)(*er), (D * n)(*ei), (D * n)(*es), n, vf)
+    eps.destroy()
+    return rc
+
+
+def vf_on(lib, path, creator="PetscViewerAndFormatCreate"):
+    v = open_ascii(lib, path)
+    vf = P()
+    getattr(lib, creator).argtypes = [P, ctypes.c_int, ctypes.POINTER(P)] if creator == "PetscViewerAndFormatCreate" \
+        else [P, ctypes.c_int, P, ctypes.POINTER(P)]
+    if creator == "PetscViewerAndFormatCreate":
+        assert lib.PetscViewerAndFormatCreate(v, PETSC_VIEWER_DEFAULT, ctypes.byref(vf)) == 0
+    else:
+        assert lib.EPSMonitorConvergedCreate(v, PETSC_VIEWER_DEFAULT, None, ctypes.byref(vf)) == 0
+    return v, vf
+
+
+def test_monitor_first_prints_the_reference_lines(lib, tmp_path):
+    g = G["test23_2"]
+    path = tmp_path / "mon.txt"
+    v, vf = vf_on(lib, path)
+    er, ei = [20.0 - 1e-9] + [19.0 - 1e-12] + [18.0] * 14, [0.0] * 16
+    assert call_monitor(lib, "EPSMonitorFirst", vf, 1, 0, er, ei, [1.2e-4, 3e-5] + [1.0] * 14) == 0
+    assert call_monitor(lib, "EPSMonitorFirst", vf, 2, 1, er, ei, [1e-12, 1.7e-8] + [1.0] * 14) == 0
+    assert call_monitor(lib, "EPSMonitorFirst", vf, 3, 16, er, ei, [0.0] * 16) == 0  # all converged: no line
+    assert lib.PetscViewerAndFormatDestroy(ctypes.byref(vf)) == 0
+    assert lib.PetscViewerDestroy(ctypes.byref(v)) == 0
+    assert [removed(l) for l in path.read_text().splitlines()] == g["monitor"]
+
+
+def test_monitor_all_and_converged_formats(lib, tmp_path):
+    path = tmp_path / "all.txt"
+    v, vf = vf_on(lib, path)
+    assert call_monitor(lib, "EPSMonitorAll", vf, 3, 1, [6.0, 2.5, -1.25], [0.0, 0.5, -0.5],
+                        [0.0, 1e-3, 1e-3]) == 0
+    assert lib.PetscViewerAndFormatDestroy(ctypes.byref(vf)) == 0
+    assert lib.PetscViewerDestroy(ctypes.byref(v)) == 0
+    assert path.read_text() == ("  3 EPS nconv=1 Values (Errors) 6. (0.00000000e+00) 2.5+0.5i (1.00000000e-03)"
+                                " -1.25-0.5i (1.00000000e-03)\n")
+    path = tmp_path / "conv.txt"
+    v, vf = vf_on(lib, path, "EPSMonitorConvergedCreate")
+    er, ei = [6.0, 5.0, 4.0], [0.0] * 3
+    assert call_monitor(lib, "EPSMonitorConverged", vf, 1, 0, er, ei, [1e-3] * 3) == 0
+    assert call_monitor(lib, "EPSMonitorConverged", vf, 2, 2, er, ei, [0.0, 0.0, 1e-3]) == 0
+    assert call_monitor(lib, "EPSMonitorConverged", vf, 3, 2, er, ei, [0.0, 0.0, 1e-3]) == 0
+    assert lib.EPSMonitorConvergedDestroy(ctypes.byref(vf)) == 0
+    assert lib.PetscViewerDestroy(ctypes.byref(v)) == 0
+    assert path.read_text() == ("  2 EPS converged value (error) #0 6. (0.00000000e+00)\n"
+                                "  2 EPS converged value (error) #1 5. (0.00000000e+00)\n")
+
+
+def test_options_monitors_names_and_views(lib, tmp_path):
+    """-eps_monitor*, -eps_view_values, -eps_error_*, -eps_converged_reason parse with viewer specs; draw viewers
+    are ignored; an unknown format is an error; PetscObjectSetName is what MATLAB reports print."""
+    sg.initialize(["prog", "-eps_monitor", ":" + str(tmp_path / "m.txt"), "-eps_monitor_all", "draw::draw_lg",
+                   "-eps_monitor_conv", "-eps_view_values", ":" + str(tmp_path / "v.txt") + ":ascii_matlab",
+                   "-eps_error_relative", "::ascii_info_detail", "-eps_converged_reason", "-eps_nev", "3"])
+    eps = sg.EPS().create()
+    eps.setFromOptions()
+    assert eps.getDimensions()[0] == 3
+    eps.setName("myeps")
+    lib.PetscObjectGetName.argtypes = [P, ctypes.POINTER(ctypes.c_char_p)]
+    name = ctypes.c_char_p()
+    assert lib.PetscObjectGetName(eps.handle, ctypes.byref(name)) == 0 and name.value == b"myeps"
+    eps.monitorCancel()
+    eps.destroy()
+    sg.initialize(["prog", "-eps_view_values", "::ascii_nonsense"])
+    eps = sg.EPS().create()
+    with pytest.raises(sg.SlepcError) as e:
+        eps.setFromOptions()
+    assert e.value.code == PETSC_ERR_SUP
+    eps.destroy()
+    sg.initialize(["prog"])
