@@ -236,6 +236,43 @@ def convdiff_eigenvalues(N: int, peclet: float) -> np.ndarray:
     return (ev[:, None] + ev[None, :]).ravel()
 
 
+def markov_walk(m: int):
+    """CSR arrays of the random walk on a triangular grid of m points per side (G. W. Stewart, SRRIT, TR-514,
+    University of Maryland, 1978): n = m(m+1)/2 states numbered along the grid's rows; from point (i, j) the walk
+    moves up or right with probability pd = (i + j - 1) / (2(m - 1)) each (doubled on the boundary row/column) and
+    down or left with pu = 1/2 - (i + j - 3) / (2(m - 1)).  The matrix is the transpose of the transition matrix,
+    as the reference's ex5.c builds it; 1 is an exact eigenvalue."""
+    cst = 0.5 / (m - 1)
+    rows, cols, vals = [], [], []
+    ix = 0
+    for i in range(1, m + 1):
+        jmax = m - i + 1
+        for j in range(1, jmax + 1):
+            ix += 1
+            r = ix - 1
+            if j != jmax:
+                pd = cst * (i + j - 1)
+                rows += [r, r]
+                cols += [ix, ix + jmax - 1]
+                vals += [2 * pd if i == 1 else pd, 2 * pd if j == 1 else pd]
+            pu = 0.5 - cst * (i + j - 3)
+            if j > 1:
+                rows.append(r)
+                cols.append(ix - 2)
+                vals.append(pu)
+            if i > 1:
+                rows.append(r)
+                cols.append(ix - jmax - 2)
+                vals.append(pu)
+    n = m * (m + 1) // 2
+    rows, cols, vals = np.array(rows), np.array(cols), np.array(vals, dtype=np.float64)
+    order = np.lexsort((cols, rows))
+    rows, cols, vals = rows[order], cols[order], vals[order]
+    rowptr = np.zeros(n + 1, dtype=np.int32)
+    np.add.at(rowptr, rows + 1, 1)
+    return np.cumsum(rowptr).astype(np.int32), cols.astype(np.int32), vals
+
+
 def diagonal(d):
     """CSR arrays of diag(d) (the B of a generalised problem)."""
     d = np.asarray(d, dtype=np.float64)

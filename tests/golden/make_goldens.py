@@ -90,8 +90,24 @@ def main():
                      "monitor": [l for l in lines if "EPS nconv=" in l],
                      "values_matlab": [l.strip() for l in lines if "Lambda_" in l or l.strip().endswith("e+01")
                                        or l.strip() == "];"]}
+    # Markov random walk m=15 (n=120), NHEP, largest real, nev 4, with and without locking (src/eps/tutorials/ex5.c
+    # TEST 1; its filter maps 0.90424 -> 0.90423 and 0.85715 -> 0.85714)
+    txt = read("src/eps/tutorials/output/ex5_1.out")
+    line = [l for l in txt.splitlines() if re.search(r"\d\.\d{5}", l)][-1]
+    g["ex5_1"] = {"source": "src/eps/tutorials/output/ex5_1.out", "m": 15, "nev": 4, "which": "LR", "tol": 1e-8,
+                  "eigenvalues": floats(line), "filter": [["0.90424", "0.90423"], ["0.85715", "0.85714"]]}
+    # 1-D Laplacian n=30, HEP, nev 4, largest magnitude, tol 1000 eps (src/eps/tests/test4.c TEST 1, krylovschur)
+    txt = read("src/eps/tests/output/test4_1.out")
+    line = [l for l in txt.splitlines() if re.search(r"\d\.\d{5}", l)][-1]
+    g["test4_1"] = {"source": "src/eps/tests/output/test4_1.out", "n": 30, "nev": 4, "which": "LM",
+                    "tol": 1000 * 2.220446049250313e-16, "eigenvalues": floats(line)}
+    # diag(1..30), HEP, nev 4, largest magnitude, tol PETSC_SMALL (src/eps/tests/test6.c TEST 1, krylovschur)
+    txt = read("src/eps/tests/output/test6_1.out")
+    line = [l for l in txt.splitlines() if re.search(r"\d\.\d{5}", l)][-1]
+    g["test6_1"] = {"source": "src/eps/tests/output/test6_1.out", "n": 30, "nev": 4, "which": "LM", "tol": 1e-10,
+                    "eigenvalues": floats(line)}
     # the text EPSErrorView prints (the "All requested ..." line and the eigenvalue line), per solve of each test
-    for key in ("ex2_1", "ex9_1", "ex4_1", "test2_1", "test2_3", "test1_1"):
+    for key in ("ex2_1", "ex9_1", "ex4_1", "test2_1", "test2_3", "test1_1", "ex5_1", "test4_1", "test6_1"):
         lines = read(g[key]["source"]).splitlines()
         g[key]["errorview"] = [[lines[i], lines[i + 1]] for i, l in enumerate(lines)
                                if l.startswith(" All requested eigenvalues")]

@@ -404,3 +404,40 @@ def test_monitor_and_matlab_values_test23(lib, orc, tmp_path):
     vals = [l.strip() for l in val.read_text().splitlines()]
     fixed = [re.sub(r"^(2\.[0-9]*e\+01|1\.9999999999[0-9]*e\+01)$", "2.0000000000000000e+01", l) for l in vals]
     assert fixed == g["values_matlab"]
+
+
+@pytest.mark.parametrize("lock", [True, False])
+def test_ex5_markov_golden_on_gpu(lib, orc, lock):
+    """ex5.c on the device: the Markov random walk (n = 120), non-Hermitian, largest real, nev 4: the digits of
+    ex5_1.out (after its filter), the EPSErrorView line, and the oracle's eigenvalues to 1e-10 at tol 1e-10."""
+    g = G["ex5_1"]
+    csr = matgen.markov_walk(g["m"])
+    n = len(csr[0]) - 1
+    v0 = matgen.start_vector(n, 1)
+    res = run(csr, hermitian=False, which=g["which"], nev=g["nev"], tol=g["tol"], lock=lock, v0=v0)
+    assert res["reason"] == 1
+    got = [f"{v:.5f}" for v in res["eigr"][:4]]
+    for a, b in g["filter"]:
+        got = [b if x == a else x for x in got]
+    assert [float(x) for x in got] == g["eigenvalues"]
+    text = res["eps"].errorView().splitlines()[:2]
+    for a, b in g["filter"]:
+        text = [t.replace(a, b) for t in text]
+    assert text == g["errorview"][0]
+    res = run(csr, hermitian=False, which=g["which"], nev=g["nev"], tol=1e-10, lock=lock, v0=v0)
+    ref = orc.solve(*csr, hermitian=False, which=g["which"], nev=g["nev"], tol=1e-10, lock=lock, v0=v0)
+    assert ref.reason == 1
+    for i in range(4):
+        assert abs(res["eigr"][i] - ref.eigr[i]) <= 1e-10 * abs(ref.eigr[i])
+
+
+@pytest.mark.parametrize("key,gen", [("test4_1", "lap1d"), ("test6_1", "diag")])
+def test_test4_test6_goldens_on_gpu(lib, key, gen):
+    """test4.c and test6.c on the device: HEP, nev 4, largest magnitude; digits and the EPSErrorView line."""
+    g = G[key]
+    n = g["n"]
+    csr = matgen.laplacian_1d(n) if gen == "lap1d" else matgen.diagonal(np.arange(1, n + 1, dtype=float))
+    res = run(csr, hermitian=True, which=g["which"], nev=g["nev"], tol=g["tol"], v0=matgen.start_vector(n, 1))
+    assert res["reason"] == 1
+    assert [round(v, 5) for v in res["eigr"][:4]] == g["eigenvalues"]
+    assert res["eps"].errorView().splitlines()[:2] == g["errorview"][0]

@@ -231,3 +231,74 @@ def test_convergence_tests(orc, conv):
     for lam in other.eigr[:other.nconv]:  # degenerate copies may appear once rounding splits them
         assert np.min(np.abs(ex - lam)) < 1e-9 * abs(lam)
     assert abs(other.eigr[0] - rel.eigr[0]) < 1e-9 * abs(rel.eigr[0])
+
+
+def _filtered(vals, g):
+    out = [f"{v:.5f}" for v in vals]
+    for a, b in g.get("filter", []):
+        out = [b if x == a else x for x in out]
+    return [float(x) for x in out]
+
+
+@pytest.mark.parametrize("lock", [True, False])
+def test_ex5_markov_golden(orc, lock):
+    """ex5.c: the random walk on a triangular grid (m = 15, n = 120), non-Hermitian, largest real, nev 4, with and
+    without locking: the digits of ex5_1.out (after the test's own filter)."""
+    g = G["ex5_1"]
+    csr = matgen.markov_walk(g["m"])
+    n = len(csr[0]) - 1
+    r = orc.solve(*csr, hermitian=False, which=g["which"], nev=g["nev"], tol=g["tol"], lock=lock,
+                  v0=matgen.start_vector(n, 1))
+    assert r.err == 0 and r.reason == 1
+    assert _filtered(r.eigr[:4], g) == g["eigenvalues"] and not np.any(r.eigi[:4])
+
+
+@pytest.mark.parametrize("key,gen", [("test4_1", "lap1d"), ("test6_1", "diag")])
+def test_test4_test6_goldens(orc, key, gen):
+    """test4.c (1-D Laplacian n = 30) and test6.c (diag(1..30)): HEP, nev 4, largest magnitude."""
+    g = G[key]
+    n = g["n"]
+    csr = matgen.laplacian_1d(n) if gen == "lap1d" else matgen.diagonal(np.arange(1, n + 1, dtype=float))
+    r = orc.solve(*csr, hermitian=True, which=g["which"], nev=g["nev"], tol=g["tol"], v0=matgen.start_vector(n, 1))
+    assert r.err == 0 and r.reason == 1
+    assert r5(r.eigr[:4]) == g["eigenvalues"]
+
+
+def test_oracle_monitor_through_the_c_printer(orc):
+    """test23.c TEST 2 on the CPU: the oracle's restart-by-restart values, printed by the library's EPSMonitorFirst,
+    are the two lines of test23_2.out after that test's filter."""
+    import ctypes
+    import re
+    import tempfile
+
+    import slepc_gb300 as sg
+    sg.build()
+    lib = sg.load()
+    g = G["test23_2"]
+    n = g["n"]
+    P, D = ctypes.c_void_p, ctypes.c_double
+    rp, ci, va = np.arange(n + 1, dtype=np.int32), np.arange(n, dtype=np.int32), np.arange(1, n + 1, dtype=float)
+    hist = []
+    r = orc.solve(rp, ci, va, hermitian=False, which="LR", nev=1, tol=1e-8, v0=matgen.start_vector(n, 1),
+                  monitor=lambda its, nconv, er, ei, es, nest: hist.append((its, nconv, er, ei, es, nest)))
+    assert r.reason == 1
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "mon.txt")
+        v, vf = P(), P()
+        lib.PetscViewerASCIIOpen.argtypes = [ctypes.c_int, ctypes.c_char_p, ctypes.POINTER(P)]
+        lib.PetscViewerAndFormatCreate.argtypes = [P, ctypes.c_int, ctypes.POINTER(P)]
+        lib.EPSMonitorFirst.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(D), ctypes.POINTER(D),
+                                        ctypes.POINTER(D), ctypes.c_int, P]
+        lib.PetscViewerAndFormatDestroy.argtypes = [ctypes.POINTER(P)]
+        lib.PetscViewerDestroy.argtypes = [ctypes.POINTER(P)]
+        assert lib.PetscViewerASCIIOpen(0, path.encode(), ctypes.byref(v)) == 0
+        assert lib.PetscViewerAndFormatCreate(v, 0, ctypes.byref(vf)) == 0
+        eps = sg.EPS().create()
+        for its, nconv, er, ei, es, nest in hist:
+            assert lib.EPSMonitorFirst(eps.handle, its, nconv, (D * nest)(*er), (D * nest)(*ei), (D * nest)(*es),
+                                       nest, vf) == 0
+        eps.destroy()
+        assert lib.PetscViewerAndFormatDestroy(ctypes.byref(vf)) == 0
+        assert lib.PetscViewerDestroy(ctypes.byref(v)) == 0
+        lines = open(path).read().splitlines()
+    assert [re.sub(r"[0-9]\.[0-9]*e-([0-9]*)", "removed", l) for l in lines] == g["monitor"]
