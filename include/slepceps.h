@@ -95,6 +95,7 @@ PetscErrorCode EPSComputeError(EPS eps, PetscInt i, EPSErrorType type, PetscReal
 PetscErrorCode EPSConvergedReasonView(EPS eps, PetscViewer viewer);
 PetscErrorCode EPSErrorView(EPS eps, EPSErrorType etype, PetscViewer viewer);
 PetscErrorCode EPSValuesView(EPS eps, PetscViewer viewer);
+PetscErrorCode EPSView(EPS eps, PetscViewer viewer); /* epsview.c:40-190; option -eps_view (after EPSSolve) */
 /* monitors (epsmon.c): called after every restart with the restart count, the number converged, the nest current
  * Ritz values (operator scaling undone) and their error estimates.  Up to 5 per EPS.  The built-ins print one line
  * per restart to the viewer of their PetscViewerAndFormat: the first unconverged value (EPSMonitorFirst, option

@@ -110,6 +110,7 @@ def load():
         "EPSMonitorCancel": ([P], I),
         "EPSConvergedReasonView": ([P, P], I),
         "EPSValuesView": ([P, P], I),
+        "EPSView": ([P, P], I),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -520,6 +521,10 @@ class EPS:
 
     def valuesView(self, path=None):
         return self._view("EPSValuesView", (), path, False)
+
+    def view(self, path=None):
+        """EPSView: the solver configuration (before EPSSetUp the values set, after it the values in use)."""
+        return self._view("EPSView", (), path, False)
 
     def getStats(self):
         buf = (ctypes.c_char * 80)()

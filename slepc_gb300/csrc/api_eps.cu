@@ -899,7 +899,7 @@ extern "C" PetscErrorCode EPSSetFromOptions(EPS eps) {
                                         has_spec ? v : nullptr));
     } else if (!strcmp(o, "-eps_converged_reason") || !strcmp(o, "-eps_error_absolute") ||
                !strcmp(o, "-eps_error_relative") || !strcmp(o, "-eps_error_backward") ||
-               !strcmp(o, "-eps_view_values")) {
+               !strcmp(o, "-eps_view_values") || !strcmp(o, "-eps_view")) {
       // reports printed at the end of EPSSolve (EPSConvergedReasonViewFromOptions, EPSErrorViewFromOptions,
       // EPSValuesViewFromOptions); the value is a viewer "[ascii][:file][:format]"
       const bool has_spec = v && v[0] != '-';
@@ -911,7 +911,10 @@ extern "C" PetscErrorCode EPSSetFromOptions(EPS eps) {
       if (!pv_viewer->borrowed) KSG_TRY(PetscViewerDestroy(&pv_viewer));
       if (ok) {
         EPSPostView pv;
-        pv.kind = !strcmp(o, "-eps_converged_reason") ? 0 : !strcmp(o, "-eps_view_values") ? 2 : 1;
+        pv.kind = !strcmp(o, "-eps_converged_reason") ? 0
+                  : !strcmp(o, "-eps_view_values")    ? 2
+                  : !strcmp(o, "-eps_view")           ? 3
+                                                      : 1;
         pv.etype = !strcmp(o, "-eps_error_absolute") ? EPS_ERROR_ABSOLUTE
                    : !strcmp(o, "-eps_error_backward") ? EPS_ERROR_BACKWARD
                                                        : EPS_ERROR_RELATIVE;

@@ -9,6 +9,7 @@
 // Items are assembled byte by byte, so the files read and write the same on little- and big-endian hosts.  A loaded
 // matrix owns its CSR arrays; everything else about it (device upload on first solve, MatMult, MatDestroy) is the
 // same as for MatCreateSeqAIJWithArrays.
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -674,9 +675,14 @@ PetscErrorCode ksg_eps_monitor_from_spec(EPS eps, int kind, const char *spec) {
   return ierr;
 }
 
-// the reports EPSSolve prints when it ends (epssolve.c:182-186: converged reason, errors, values)
+// the reports EPSSolve prints when it ends, in the order of epssolve.c:182-186: view, converged reason, errors,
+// values
 PetscErrorCode ksg_eps_post_views(EPS eps) {
-  for (const EPSPostView &pv : eps->post_views) {
+  std::vector<EPSPostView> views = eps->post_views;
+  std::stable_sort(views.begin(), views.end(), [](const EPSPostView &a, const EPSPostView &b) {
+    return (a.kind + 1) % 4 < (b.kind + 1) % 4;  // view (3), converged reason (0), errors (1), values (2)
+  });
+  for (const EPSPostView &pv : views) {
     PetscViewer v;
     PetscViewerFormat f;
     int ok;
@@ -685,10 +691,80 @@ PetscErrorCode ksg_eps_post_views(EPS eps) {
     v->formats.push_back(pv.format);
     PetscErrorCode ierr = pv.kind == 0   ? EPSConvergedReasonView(eps, v)
                           : pv.kind == 1 ? EPSErrorView(eps, (EPSErrorType)pv.etype, v)
-                                         : EPSValuesView(eps, v);
+                          : pv.kind == 2 ? EPSValuesView(eps, v)
+                                         : EPSView(eps, v);
     v->formats.pop_back();
     if (!v->borrowed) PetscViewerDestroy(&v);
     KSG_TRY(ierr);
   }
   return 0;
+}
+
+// EPSView (epsview.c:40-190 with EPSView_KrylovSchur, krylovschur.c:1490-1500): the solver configuration, then the
+// basis, projected-problem and spectral-transformation objects.  Before EPSSetUp the values are the ones set;
+// after it, the ones in use.  The BV lines state this library's basis (device, pair or FP64 storage, two-pass
+// delayed classical Gram-Schmidt) rather than the reference's default settings.
+extern "C" PetscErrorCode EPSView(EPS eps, PetscViewer v) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  if (!v) v = stdout_viewer();
+  if (!v->ascii) return 0;
+  Text t;
+  t.add("EPS Object: %s%s1 MPI process\n", eps->name.c_str(), eps->name.empty() ? "" : " ");
+  t.add("  type: krylovschur\n");
+  t.add("    %d%% of basis vectors kept after restart\n", (int)(100 * eps->keep));
+  t.add("    using the %slocking variant\n", eps->lock ? "" : "non-");
+  const char *ptype = "not yet set";
+  switch (eps->problem) {
+    case EPS_HEP: ptype = "symmetric eigenvalue problem"; break;
+    case EPS_GHEP: ptype = "generalized symmetric eigenvalue problem"; break;
+    case EPS_NHEP: ptype = "non-symmetric eigenvalue problem"; break;
+    case EPS_GNHEP: ptype = "generalized non-symmetric eigenvalue problem"; break;
+    default: break;
+  }
+  t.add("  problem type: %s\n", ptype);
+  if (eps->extraction == EPS_HARMONIC) t.add("  extraction type: harmonic Ritz\n");
+  t.add("  selected portion of the spectrum: ");
+  char tg[64];
+  std::snprintf(tg, sizeof(tg), "%g", eps->target);
+  if (!std::strpbrk(tg, ".eEni")) std::strncat(tg, ".", sizeof(tg) - std::strlen(tg) - 1);
+  switch (eps->which) {
+    case EPS_TARGET_MAGNITUDE: t.add("closest to target: %s (in magnitude)\n", tg); break;
+    case EPS_TARGET_REAL: t.add("closest to target: %s (along the real axis)\n", tg); break;
+    case EPS_LARGEST_MAGNITUDE: t.add("largest eigenvalues in magnitude\n"); break;
+    case EPS_SMALLEST_MAGNITUDE: t.add("smallest eigenvalues in magnitude\n"); break;
+    case EPS_LARGEST_REAL: t.add("largest real parts\n"); break;
+    case EPS_SMALLEST_REAL: t.add("smallest real parts\n"); break;
+    case EPS_LARGEST_IMAGINARY: t.add("largest imaginary parts\n"); break;
+    case EPS_SMALLEST_IMAGINARY: t.add("smallest imaginary parts\n"); break;
+    default: t.add("not yet set\n"); break;
+  }
+  // purification applies to definite generalised problems only (epssetup.c:359-368)
+  const bool purify = eps->purify && (!eps->setup || (eps->B && eps->problem == EPS_GHEP));
+  if (purify) t.add("  postprocessing eigenvectors with purification\n");
+  t.add("  number of eigenvalues (nev): %d\n", eps->setup ? eps->nev_e : eps->nev);
+  t.add("  number of column vectors (ncv): %d\n", eps->setup ? eps->ncv_e : eps->ncv);
+  t.add("  maximum dimension of projected problem (mpd): %d\n", eps->setup ? eps->mpd_e : eps->mpd);
+  t.add("  maximum number of iterations: %d\n", eps->setup ? eps->maxit_e : eps->max_it);
+  t.add("  tolerance: %g\n", eps->setup ? eps->tol_e : eps->tol);
+  t.add("  convergence test: ");
+  if (eps->conv == EPS_CONV_ABS) t.add("absolute\n");
+  else if (eps->conv == EPS_CONV_NORM) {
+    t.add("relative to the eigenvalue and matrix norms\n");
+    t.add("  computed matrix norms: norm(A)=%g", eps->nrma);
+    if (eps->B) t.add(", norm(B)=%g", eps->nrmb);
+    t.add("\n");
+  } else t.add("relative to the eigenvalue\n");
+  if (!eps->v0.empty()) t.add("  dimension of user-provided initial space: 1\n");
+  const int ncv = eps->setup ? eps->ncv_e : eps->ncv;
+  t.add("BV Object: 1 MPI process\n");
+  t.add("  type: device (GB300), %s storage\n", eps->storage == ksg::STORE_F64 ? "FP64" : "FP32-pair");
+  if (ncv > 0 && eps->A) t.add("  %d columns of global length %d\n", ncv + 1, eps->A->m);
+  t.add("  vector orthogonalization method: classical Gram-Schmidt, two passes (delayed)\n");
+  t.add("DS Object: 1 MPI process\n");
+  t.add("  type: %s\n", ksg_eps_lanczos(eps) ? "hep" : "nhep");
+  t.add("ST Object: 1 MPI process\n");
+  t.add("  type: shift\n");
+  t.add("  shift: 0.\n");
+  t.add("  number of matrices: %d\n", eps->B ? 2 : 1);
+  return emit(v, t);
 }

@@ -111,7 +111,7 @@ constexpr unsigned KSG_EPS_COOKIE = 0x31535045u;  // the first word of every EPS
 
 // a report EPSSolve prints when it ends (options -eps_converged_reason, -eps_error_*, -eps_view_values)
 struct EPSPostView {
-  int kind;  // 0 converged reason, 1 error view (etype), 2 values view
+  int kind;  // 0 converged reason, 1 error view (etype), 2 values view, 3 EPSView
   int etype;
   PetscViewerFormat format;
   std::string file;  // empty: stdout

@@ -106,6 +106,11 @@ def main():
     line = [l for l in txt.splitlines() if re.search(r"\d\.\d{5}", l)][-1]
     g["test6_1"] = {"source": "src/eps/tests/output/test6_1.out", "n": 30, "nev": 4, "which": "LM", "tol": 1e-10,
                     "eigenvalues": floats(line)}
+    # EPSView of a Krylov-Schur NHEP solve, largest real (src/eps/tests/test23.c TEST 1): the EPS Object block
+    lines = read("src/eps/tests/output/test23_1.out").splitlines()
+    i0 = next(i for i, l in enumerate(lines) if l.startswith("EPS Object"))
+    i1 = next(i for i, l in enumerate(lines) if l.startswith("BV Object"))
+    g["test23_1"] = {"source": "src/eps/tests/output/test23_1.out", "eps_view": lines[i0:i1]}
     # the text EPSErrorView prints (the "All requested ..." line and the eigenvalue line), per solve of each test
     for key in ("ex2_1", "ex9_1", "ex4_1", "test2_1", "test2_3", "test1_1", "ex5_1", "test4_1", "test6_1"):
         lines = read(g[key]["source"]).splitlines()

@@ -172,3 +172,25 @@ def test_options_monitors_names_and_views(lib, tmp_path):
     assert e.value.code == PETSC_ERR_SUP
     eps.destroy()
     sg.initialize(["prog"])
+
+
+def test_eps_view_matches_the_reference_block(lib):
+    """EPSView of test23.c's configuration (named "eps", NHEP, largest real, nev 1, ncv = mpd = 6, 100 iterations)
+    before EPSSetUp: the EPS Object block of test23_1.out, apart from its balancing and residual-tracking lines
+    (options not provided here), the tolerance (the test filters it) and purification (on until EPSSetUp turns it
+    off for a standard problem); then the BV, DS and ST objects."""
+    A = sg.Mat(*__import__("slepc_gb300.matgen", fromlist=["x"]).laplacian_1d(30))
+    eps = sg.EPS().create()
+    eps.setOperators(A)
+    eps.setProblemType(sg.EPS.ProblemType.NHEP)
+    eps.setName("eps")
+    eps.setWhichEigenpairs("LR")
+    eps.setDimensions(1, 6, 6)
+    eps.setTolerances(max_it=100)
+    text = eps.view().splitlines()
+    skip = ("balancing", "computing all residuals", "tolerance", "purification")
+    ours = [l for l in text[:text.index("BV Object: 1 MPI process")] if not any(k in l for k in skip)]
+    ref = [l for l in G["test23_1"]["eps_view"] if not any(k in l for k in skip)]
+    assert ours == ref
+    assert "DS Object: 1 MPI process" in text and "  type: nhep" in text and "  type: shift" in text
+    eps.destroy()
