@@ -74,6 +74,11 @@ PetscErrorCode EPSSetWhichEigenpairs(EPS eps, EPSWhich which);
 PetscErrorCode EPSGetWhichEigenpairs(EPS eps, EPSWhich *which);
 PetscErrorCode EPSSetInitialSpace(EPS eps, PetscInt n, Vec is[]);                          /* epssetup.c:592 */
 PetscErrorCode EPSSetFromOptions(EPS eps);
+/* options prefix (epsopts.c:1320-1400): the EPS's options are then -<prefix>eps_...; -st_type other than shift and
+ * nonzero -st_shift are PETSC_ERR_SUP (the spectral transformation is the shift of 0) */
+PetscErrorCode EPSSetOptionsPrefix(EPS eps, const char prefix[]);
+PetscErrorCode EPSAppendOptionsPrefix(EPS eps, const char prefix[]);
+PetscErrorCode EPSGetOptionsPrefix(EPS eps, const char *prefix[]);
 /* Krylov-Schur knobs: krylovschur.c:339-489 */
 PetscErrorCode EPSKrylovSchurSetRestart(EPS eps, PetscReal keep);
 PetscErrorCode EPSKrylovSchurGetRestart(EPS eps, PetscReal *keep);

@@ -111,6 +111,9 @@ def load():
         "EPSConvergedReasonView": ([P, P], I),
         "EPSValuesView": ([P, P], I),
         "EPSView": ([P, P], I),
+        "EPSSetOptionsPrefix": ([P, ctypes.c_char_p], I),
+        "EPSAppendOptionsPrefix": ([P, ctypes.c_char_p], I),
+        "EPSGetOptionsPrefix": ([P, ctypes.POINTER(ctypes.c_char_p)], I),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -358,6 +361,17 @@ class EPS:
 
     def setFromOptions(self):
         _check(load().EPSSetFromOptions(self.handle), "EPSSetFromOptions")
+
+    def setOptionsPrefix(self, prefix):
+        _check(load().EPSSetOptionsPrefix(self.handle, prefix.encode() if prefix else None), "EPSSetOptionsPrefix")
+
+    def appendOptionsPrefix(self, prefix):
+        _check(load().EPSAppendOptionsPrefix(self.handle, prefix.encode()), "EPSAppendOptionsPrefix")
+
+    def getOptionsPrefix(self):
+        v = ctypes.c_char_p()
+        _check(load().EPSGetOptionsPrefix(self.handle, ctypes.byref(v)), "EPSGetOptionsPrefix")
+        return v.value.decode() if v.value else None
 
     def setName(self, name):
         """PetscObjectSetName: the name MATLAB-format reports print."""

@@ -862,12 +862,44 @@ extern "C" PetscErrorCode EPSGB300SetDevice(EPS eps, int device) {
 }
 
 // -eps_* options from the argv given to SlepcInitialize (epsopts.c:84-260, krylovschur.c:1440-1475)
+// EPSSetOptionsPrefix / EPSAppendOptionsPrefix / EPSGetOptionsPrefix (epsopts.c:1320-1400): options of this EPS are
+// then spelled -<prefix>eps_..., and the reports name the prefix
+extern "C" PetscErrorCode EPSSetOptionsPrefix(EPS eps, const char prefix[]) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  KSG_CHECK(!prefix || prefix[0] != '-', PETSC_ERR_ARG_WRONG, "Options prefix should not begin with a hyphen");
+  eps->prefix = prefix ? prefix : "";
+  return 0;
+}
+extern "C" PetscErrorCode EPSAppendOptionsPrefix(EPS eps, const char prefix[]) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  KSG_CHECK(!prefix || prefix[0] != '-', PETSC_ERR_ARG_WRONG, "Options prefix should not begin with a hyphen");
+  if (prefix) eps->prefix += prefix;
+  return 0;
+}
+extern "C" PetscErrorCode EPSGetOptionsPrefix(EPS eps, const char *prefix[]) {
+  KSG_CHECK(eps && prefix, PETSC_ERR_ARG_NULL, "Null argument");
+  *prefix = eps->prefix.empty() ? nullptr : eps->prefix.c_str();
+  return 0;
+}
+
 extern "C" PetscErrorCode EPSSetFromOptions(EPS eps) {
   KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  std::string unpre;
   for (int i = 1; i < g_argc; ++i) {
     const char *o = g_argv[i];
     const char *v = (i + 1 < g_argc) ? g_argv[i + 1] : nullptr;
-    if (!strcmp(o, "-eps_nev") && v) KSG_TRY(EPSSetDimensions(eps, atoi(v), PETSC_CURRENT, PETSC_CURRENT));
+    if (!o || o[0] != '-') continue;
+    if (!eps->prefix.empty()) {  // -<prefix>name becomes -name; options without the prefix are not this EPS's
+      if (strncmp(o + 1, eps->prefix.c_str(), eps->prefix.size())) continue;
+      unpre = std::string("-") + (o + 1 + eps->prefix.size());
+      o = unpre.c_str();
+    }
+    if (!strcmp(o, "-st_type") && v) {
+      // the spectral transformation is the shift of 0 (STSHIFT); the others need linear solves
+      KSG_CHECK(!strcmp(v, "shift"), PETSC_ERR_SUP, "ST type %s is not provided: the shift transformation only", v);
+    } else if (!strcmp(o, "-st_shift") && v) {
+      KSG_CHECK(atof(v) == 0.0, PETSC_ERR_SUP, "Nonzero shifts of the spectral transformation are not provided");
+    } else if (!strcmp(o, "-eps_nev") && v) KSG_TRY(EPSSetDimensions(eps, atoi(v), PETSC_CURRENT, PETSC_CURRENT));
     else if (!strcmp(o, "-eps_ncv") && v) KSG_TRY(EPSSetDimensions(eps, PETSC_CURRENT, atoi(v), PETSC_CURRENT));
     else if (!strcmp(o, "-eps_mpd") && v) KSG_TRY(EPSSetDimensions(eps, PETSC_CURRENT, PETSC_CURRENT, atoi(v)));
     else if (!strcmp(o, "-eps_tol") && v) KSG_TRY(EPSSetTolerances(eps, atof(v), PETSC_CURRENT));

@@ -386,10 +386,11 @@ extern "C" PetscErrorCode EPSConvergedReasonView(EPS eps, PetscViewer v) {
   const int nconv = eps->nconv, its = eps->its, reason = eps->reason;  // before EPSSolve: 0, CONVERGED_ITERATING
   Text t;
   if (reason > 0 && top_format(v) != PETSC_VIEWER_FAILED)
-    t.add(" Linear eigensolve converged (%d eigenpair%s) due to %s; iterations %d\n", nconv, nconv > 1 ? "s" : "",
-          reason_name(reason), its);
+    t.add("%s Linear eigensolve converged (%d eigenpair%s) due to %s; iterations %d\n", eps->prefix.c_str(), nconv,
+          nconv > 1 ? "s" : "", reason_name(reason), its);
   else if (reason <= 0)
-    t.add(" Linear eigensolve did not converge due to %s; iterations %d\n", reason_name(reason), its);
+    t.add("%s Linear eigensolve did not converge due to %s; iterations %d\n", eps->prefix.c_str(), reason_name(reason),
+          its);
   return emit(v, t);
 }
 
@@ -575,8 +576,11 @@ extern "C" PetscErrorCode EPSMonitorFirst(EPS eps, PetscInt its, PetscInt nconv,
                                           PetscViewerAndFormat *vf) {
   PetscViewer v;
   KSG_TRY(monitor_viewer(eps, vf, &v));
-  if (!v->ascii || nconv >= nest) return 0;
+  if (!v->ascii) return 0;
   Text t;
+  if (its == 1 && !eps->prefix.empty())
+    t.add("  Eigenvalue approximations and residual norms for %s solve.\n", eps->prefix.c_str());
+  if (nconv >= nest) return emit(v, t);
   t.add("%3d EPS nconv=%d first unconverged value (error)", (int)its, (int)nconv);
   add_monitor_value(t, eigr[nconv], eigi[nconv]);
   t.add(" (%10.8e)\n", errest[nconv]);
@@ -590,6 +594,8 @@ extern "C" PetscErrorCode EPSMonitorAll(EPS eps, PetscInt its, PetscInt nconv, P
   KSG_TRY(monitor_viewer(eps, vf, &v));
   if (!v->ascii) return 0;
   Text t;
+  if (its == 1 && !eps->prefix.empty())
+    t.add("  Eigenvalue approximations and residual norms for %s solve.\n", eps->prefix.c_str());
   t.add("%3d EPS nconv=%d Values (Errors)", (int)its, (int)nconv);
   for (PetscInt i = 0; i < nest; ++i) {
     add_monitor_value(t, eigr[i], eigi[i]);
@@ -607,9 +613,11 @@ extern "C" PetscErrorCode EPSMonitorConverged(EPS eps, PetscInt its, PetscInt nc
   KSG_TRY(monitor_viewer(eps, vf, &v));
   KSG_CHECK(vf->data, PETSC_ERR_ARG_WRONG, "EPSMonitorConverged needs the context of EPSMonitorConvergedCreate");
   PetscInt *old = static_cast<PetscInt *>(vf->data);
-  if (its == 1) *old = 0;
-  if (!v->ascii || *old == nconv) return 0;
+  if (!v->ascii) return 0;
   Text t;
+  if (its == 1 && !eps->prefix.empty()) t.add("  Convergence history for %s solve.\n", eps->prefix.c_str());
+  if (its == 1) *old = 0;
+  if (*old == nconv) return emit(v, t);
   for (PetscInt i = *old; i < nconv; ++i) {
     t.add("%3d EPS converged value (error) #%d", (int)its, (int)i);
     add_monitor_value(t, eigr[i], eigi[i]);

@@ -119,7 +119,8 @@ struct EPSPostView {
 
 struct _p_EPS {
   unsigned cookie = KSG_EPS_COOKIE;
-  std::string name;  // PetscObjectSetName
+  std::string name;    // PetscObjectSetName
+  std::string prefix;  // EPSSetOptionsPrefix
   // configuration
   Mat A = nullptr;
   Mat B = nullptr;  // generalised problems: a diagonal B (EPSSetOperators)

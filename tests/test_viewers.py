@@ -194,3 +194,30 @@ def test_eps_view_matches_the_reference_block(lib):
     assert ours == ref
     assert "DS Object: 1 MPI process" in text and "  type: nhep" in text and "  type: shift" in text
     eps.destroy()
+
+
+def test_options_prefix_as_test19(lib):
+    """test19.c's prefix handling: "check_" + "myprefix_", options -check_myprefix_eps_nev 2 (an unprefixed -eps_nev
+    belongs to no-prefix objects); the converged-reason line names the prefix; -check_myprefix_st_type sinvert is
+    not provided (the spectral transformation is the shift of 0)."""
+    eps = sg.EPS().create()
+    eps.setOptionsPrefix("check_")
+    eps.appendOptionsPrefix("myprefix_")
+    assert eps.getOptionsPrefix() == "check_myprefix_"
+    sg.initialize(["test19", "-check_myprefix_eps_nev", "2", "-eps_nev", "7"])
+    try:
+        eps.setFromOptions()
+        assert eps.getDimensions()[0] == 2
+        assert eps.convergedReasonView() == ("check_myprefix_ Linear eigensolve did not converge due to "
+                                             "CONVERGED_ITERATING; iterations 0\n")
+        sg.initialize(["test19", "-check_myprefix_st_type", "sinvert"])
+        with pytest.raises(sg.SlepcError) as e:
+            eps.setFromOptions()
+        assert e.value.code == PETSC_ERR_SUP
+        sg.initialize(["test19", "-check_myprefix_st_type", "shift", "-check_myprefix_st_shift", "0"])
+        eps.setFromOptions()
+    finally:
+        sg.initialize(["prog"])
+    eps.setOptionsPrefix(None)
+    assert eps.getOptionsPrefix() is None
+    eps.destroy()
