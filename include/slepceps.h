@@ -14,6 +14,7 @@
 #include "petsc_subset.h"
 #include "slepcbv.h"
 #include "slepcds.h"
+#include "slepcst.h"
 
 #ifdef __cplusplus
 extern "C" {
@@ -120,6 +121,11 @@ PetscErrorCode EPSMonitorConvergedCreate(PetscViewer viewer, PetscViewerFormat f
                                          PetscViewerAndFormat **vf);
 PetscErrorCode EPSMonitorConvergedDestroy(PetscViewerAndFormat **vf);
 PetscErrorCode EPSGetBV(EPS eps, BV *V);
+PetscErrorCode EPSGetST(EPS eps, ST *st); /* the shift-0 transformation (slepcst.h) */
+/* problem properties after EPSSetProblemType (epsbasic.c:1000-1080) */
+PetscErrorCode EPSIsHermitian(EPS eps, PetscBool *is);
+PetscErrorCode EPSIsGeneralized(EPS eps, PetscBool *is);
+PetscErrorCode EPSIsPositive(EPS eps, PetscBool *is);
 PetscErrorCode EPSGetDS(EPS eps, DS *ds);
 
 #ifdef __cplusplus

@@ -1,0 +1,37 @@
+/*
+ * slepcst.h -- ST (spectral transformation) subset.
+ *
+ * Same names and enum strings as SLEPc 3.22's include/slepcst.h (:42-103).  The Krylov-Schur path here runs the
+ * shift transformation with shift 0 (STSHIFT; the operator is A, or the generalised operator of EPSSetOperators):
+ * EPSGetST returns that object so that programs which query or confirm it work unchanged.  The transformations that
+ * need linear solves (sinvert, cayley, precond, filter, shell) and nonzero shifts return PETSC_ERR_SUP.
+ */
+#ifndef SLEPC_GB300_SLEPCST_H
+#define SLEPC_GB300_SLEPCST_H
+
+#include "petsc_subset.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct _p_ST *ST;
+typedef const char *STType;
+#define STSHELL "shell"
+#define STSHIFT "shift"
+#define STSINVERT "sinvert"
+#define STCAYLEY "cayley"
+#define STPRECOND "precond"
+#define STFILTER "filter"
+
+PetscErrorCode STSetType(ST st, STType type);
+PetscErrorCode STGetType(ST st, STType *type);
+PetscErrorCode STSetShift(ST st, PetscScalar shift);
+PetscErrorCode STGetShift(ST st, PetscScalar *shift);
+PetscErrorCode STGetNumMatrices(ST st, PetscInt *n);
+PetscErrorCode STView(ST st, PetscViewer viewer);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

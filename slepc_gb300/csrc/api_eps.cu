@@ -663,6 +663,23 @@ extern "C" PetscErrorCode EPSGetProblemType(EPS eps, EPSProblemType *type) {
   *type = (EPSProblemType)eps->problem;
   return 0;
 }
+// EPSIsHermitian / EPSIsGeneralized / EPSIsPositive (epsbasic.c): from the problem type
+extern "C" PetscErrorCode EPSIsHermitian(EPS eps, PetscBool *is) {
+  KSG_CHECK(eps && is, PETSC_ERR_ARG_NULL, "Null argument");
+  *is = ksg_eps_hermitian(eps) ? PETSC_TRUE : PETSC_FALSE;
+  return 0;
+}
+extern "C" PetscErrorCode EPSIsGeneralized(EPS eps, PetscBool *is) {
+  KSG_CHECK(eps && is, PETSC_ERR_ARG_NULL, "Null argument");
+  *is = (eps->problem == EPS_GHEP || eps->problem == EPS_GNHEP) ? PETSC_TRUE : PETSC_FALSE;
+  return 0;
+}
+extern "C" PetscErrorCode EPSIsPositive(EPS eps, PetscBool *is) {
+  KSG_CHECK(eps && is, PETSC_ERR_ARG_NULL, "Null argument");
+  *is = eps->problem == EPS_GHEP ? PETSC_TRUE : PETSC_FALSE;  // B positive definite (PGNHEP is not provided)
+  return 0;
+}
+
 // EPSSetConvergenceTest (epsopts.c:682-700)
 extern "C" PetscErrorCode EPSSetConvergenceTest(EPS eps, EPSConv conv) {
   KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");

@@ -770,9 +770,61 @@ extern "C" PetscErrorCode EPSView(EPS eps, PetscViewer v) {
   t.add("  vector orthogonalization method: classical Gram-Schmidt, two passes (delayed)\n");
   t.add("DS Object: 1 MPI process\n");
   t.add("  type: %s\n", ksg_eps_lanczos(eps) ? "hep" : "nhep");
+  KSG_TRY(emit(v, t));
+  eps->stobj.eps = eps;
+  return STView(&eps->stobj, v);
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// ST: the shift transformation with shift 0, owned by its EPS
+// ---------------------------------------------------------------------------------------------------------------
+extern "C" PetscErrorCode EPSGetST(EPS eps, ST *st) {
+  KSG_CHECK(eps && st, PETSC_ERR_ARG_NULL, "Null argument");
+  eps->stobj.eps = eps;
+  *st = &eps->stobj;
+  return 0;
+}
+
+extern "C" PetscErrorCode STSetType(ST st, STType type) {
+  KSG_CHECK(st && type, PETSC_ERR_ARG_NULL, "Null argument");
+  KSG_CHECK(!std::strcmp(type, STSHIFT), PETSC_ERR_SUP,
+            "ST type %s is not provided: the Krylov-Schur path runs the shift transformation (STSHIFT)", type);
+  return 0;
+}
+
+extern "C" PetscErrorCode STGetType(ST st, STType *type) {
+  KSG_CHECK(st && type, PETSC_ERR_ARG_NULL, "Null argument");
+  *type = STSHIFT;
+  return 0;
+}
+
+extern "C" PetscErrorCode STSetShift(ST st, PetscScalar shift) {
+  KSG_CHECK(st, PETSC_ERR_ARG_NULL, "Null ST");
+  KSG_CHECK(shift == 0.0, PETSC_ERR_SUP, "Nonzero shifts (%g) are not provided", shift);
+  return 0;
+}
+
+extern "C" PetscErrorCode STGetShift(ST st, PetscScalar *shift) {
+  KSG_CHECK(st && shift, PETSC_ERR_ARG_NULL, "Null argument");
+  *shift = 0.0;
+  return 0;
+}
+
+extern "C" PetscErrorCode STGetNumMatrices(ST st, PetscInt *n) {
+  KSG_CHECK(st && st->eps && n, PETSC_ERR_ARG_NULL, "Null argument");
+  *n = st->eps->B ? 2 : 1;
+  return 0;
+}
+
+// STView (stfunc.c): type, shift, number of matrices
+extern "C" PetscErrorCode STView(ST st, PetscViewer v) {
+  KSG_CHECK(st && st->eps, PETSC_ERR_ARG_NULL, "Null ST");
+  if (!v) v = stdout_viewer();
+  if (!v->ascii) return 0;
+  Text t;
   t.add("ST Object: 1 MPI process\n");
   t.add("  type: shift\n");
   t.add("  shift: 0.\n");
-  t.add("  number of matrices: %d\n", eps->B ? 2 : 1);
+  t.add("  number of matrices: %d\n", st->eps->B ? 2 : 1);
   return emit(v, t);
 }

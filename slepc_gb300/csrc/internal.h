@@ -106,6 +106,9 @@ PetscErrorCode ksg_random_fill(double *host, int n, unsigned long long seed, uns
 
 struct _p_DS;
 struct _p_BV;
+struct _p_ST {
+  EPS eps = nullptr;  // the owner
+};
 
 constexpr unsigned KSG_EPS_COOKIE = 0x31535045u;  // the first word of every EPS (PetscObjectSetName checks it)
 
@@ -185,6 +188,7 @@ struct _p_EPS {
   long long prof_launches[EPS_GB300_K_COUNT] = {0};
   BV bv = nullptr;
   DS ds = nullptr;
+  _p_ST stobj;  // EPSGetST
   // monitors (EPSMonitorSet) and the reports to print at the end of EPSSolve
   std::vector<EPSMonitorFn *> mon;
   std::vector<void *> mon_ctx;

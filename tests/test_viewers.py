@@ -4,6 +4,7 @@ EPSErrorView before EPSSolve (PETSC_ERR_ORDER) and binary calls on an ASCII view
 of solved problems are checked against the reference's printed text in test_gpu_eps.py."""
 import ctypes
 
+import numpy as np
 import pytest
 
 import slepc_gb300 as sg
@@ -220,4 +221,39 @@ def test_options_prefix_as_test19(lib):
         sg.initialize(["prog"])
     eps.setOptionsPrefix(None)
     assert eps.getOptionsPrefix() is None
+    eps.destroy()
+
+
+def test_st_object_and_problem_queries(lib):
+    """EPSGetST gives the shift-0 transformation: STSetType(shift) and STSetShift(0) are accepted, sinvert and
+    nonzero shifts are PETSC_ERR_SUP; EPSIsHermitian/Generalized/Positive follow the problem type."""
+    from slepc_gb300 import matgen
+    A = sg.Mat(*matgen.laplacian_1d(20))
+    B = sg.Mat(*matgen.diagonal(np.ones(20)))
+    eps = sg.EPS().create()
+    eps.setOperators(A, B)
+    st = P()
+    lib.EPSGetST.argtypes = [P, ctypes.POINTER(P)]
+    assert lib.EPSGetST(eps.handle, ctypes.byref(st)) == 0 and st.value
+    for f, a in (("STSetType", [P, ctypes.c_char_p]), ("STSetShift", [P, ctypes.c_double]),
+                 ("STGetNumMatrices", [P, ctypes.POINTER(ctypes.c_int)]), ("STGetType", [P, ctypes.POINTER(ctypes.c_char_p)]),
+                 ("EPSIsHermitian", [P, ctypes.POINTER(ctypes.c_int)]), ("EPSIsGeneralized", [P, ctypes.POINTER(ctypes.c_int)]),
+                 ("EPSIsPositive", [P, ctypes.POINTER(ctypes.c_int)])):
+        getattr(lib, f).argtypes = a
+    assert lib.STSetType(st, b"shift") == 0 and lib.STSetShift(st, 0.0) == 0
+    assert lib.STSetType(st, b"sinvert") == PETSC_ERR_SUP and lib.STSetShift(st, 1.5) == PETSC_ERR_SUP
+    t, nm = ctypes.c_char_p(), ctypes.c_int()
+    assert lib.STGetType(st, ctypes.byref(t)) == 0 and t.value == b"shift"
+    assert lib.STGetNumMatrices(st, ctypes.byref(nm)) == 0 and nm.value == 2
+    flags = {}
+    for ptype, want in ((sg.EPS.ProblemType.GHEP, (1, 1, 1)), (sg.EPS.ProblemType.GNHEP, (0, 1, 0)),
+                        (sg.EPS.ProblemType.HEP, (1, 0, 0)), (sg.EPS.ProblemType.NHEP, (0, 0, 0))):
+        eps.setProblemType(ptype)
+        got = []
+        for f in ("EPSIsHermitian", "EPSIsGeneralized", "EPSIsPositive"):
+            b = ctypes.c_int(-1)
+            assert getattr(lib, f)(eps.handle, ctypes.byref(b)) == 0
+            got.append(b.value)
+        flags[ptype] = tuple(got)
+        assert tuple(got) == want, (ptype, got)
     eps.destroy()
