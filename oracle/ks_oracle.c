@@ -1282,6 +1282,10 @@ int ksor_solve_gen(int n, const int *rowptr, const int *colidx, const double *va
   /* EPSSolve_KrylovSchur_Default (krylovschur.c:238-239): harmonic extraction runs the non-symmetric variant */
   if (harmonic) hermitian = 0;
   if (n <= 0 || nev <= 0) return 63;
+  /* EPSSetUp clamps the dimensions to the problem size (epssetup.c:337-338); ncv = n is a full basis whose last
+   * factorisation step breaks down with every eigenvalue converged */
+  if (nev > n) nev = n;
+  if (ncv > n) ncv = n;
   if (nthreads <= 0) nthreads = 1;
   /* EPSSetDimensions_Default (epssetup.c:648-671) */
   if (ncv <= 0) {
@@ -1294,7 +1298,6 @@ int ksor_solve_gen(int n, const int *rowptr, const int *colidx, const double *va
   if (max_it <= 0) max_it = (2 * n / ncv) > 100 ? 2 * n / ncv : 100;
   if (tol <= 0.0) tol = 1e-8;
   if (keep <= 0.0) keep = 0.5;
-  if (ncv >= n) return 56; /* full-basis safeguard path not restated */
   if (ncv_cap < ncv) return 60;
 
   int ld = ncv + 1;

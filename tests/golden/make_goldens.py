@@ -111,6 +111,12 @@ def main():
     i0 = next(i for i, l in enumerate(lines) if l.startswith("EPS Object"))
     i1 = next(i for i, l in enumerate(lines) if l.startswith("BV Object"))
     g["test23_1"] = {"source": "src/eps/tests/output/test23_1.out", "eps_view": lines[i0:i1]}
+    # 1-D Laplacian n=18, smallest real, nev 1: the default ncv (16), then ncv + 2 = 18 = n, a full basis
+    # (src/eps/tests/test20.c TEST 1, krylovschur)
+    lines = read("src/eps/tests/output/test20_1.out").splitlines()
+    g["test20_1"] = {"source": "src/eps/tests/output/test20_1.out", "n": 18, "nev": 1, "which": "SR",
+                     "tol": max(1000 * 2.220446049250313e-16, 1e-9), "ncv": [16, 18],
+                     "eigenvalues": [floats(l)[0] for l in lines if re.search(r"\d\.\d{5}", l)]}
     # the text EPSErrorView prints (the "All requested ..." line and the eigenvalue line), per solve of each test
     for key in ("ex2_1", "ex9_1", "ex4_1", "test2_1", "test2_3", "test1_1", "ex5_1", "test4_1", "test6_1"):
         lines = read(g[key]["source"]).splitlines()

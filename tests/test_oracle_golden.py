@@ -302,3 +302,18 @@ def test_oracle_monitor_through_the_c_printer(orc):
         assert lib.PetscViewerDestroy(ctypes.byref(v)) == 0
         lines = open(path).read().splitlines()
     assert [re.sub(r"[0-9]\.[0-9]*e-([0-9]*)", "removed", l) for l in lines] == g["monitor"]
+
+
+def test_test20_full_basis_golden(orc):
+    """test20.c: the smallest eigenvalue of the 1-D Laplacian n = 18 with the default ncv (16) and then with
+    ncv = 18 = n (a full basis: the factorisation ends in a breakdown with every eigenvalue converged)."""
+    g = G["test20_1"]
+    csr = matgen.laplacian_1d(g["n"])
+    for ncv, want in zip(g["ncv"], g["eigenvalues"]):
+        r = orc.solve(*csr, hermitian=True, which=g["which"], nev=g["nev"], ncv=ncv, tol=g["tol"],
+                      v0=matgen.start_vector(g["n"], 1))
+        assert r.err == 0 and r.reason == 1
+        assert round(float(r.eigr[0]), 5) == want
+    # ncv above n is clamped to n (epssetup.c:337-338)
+    r = orc.solve(*csr, hermitian=True, which="SR", nev=2, ncv=40, tol=g["tol"], v0=matgen.start_vector(g["n"], 1))
+    assert r.err == 0 and r.reason == 1 and r.ncv == g["n"]
