@@ -48,6 +48,9 @@ def load():
         lib.ksor_solve_gen.argtypes = [i, P, P, P, P, i, i, i, i, i, d, i, d, i, i, P, ull, d, P, i, P, P, P, P, i, d,
                                        i, d, d, i]
         lib.ksor_solve_gen.restype = i
+        lib.ksor_solve_genb.argtypes = [i, P, P, P, P, P, P, i, i, i, i, i, d, i, d, i, i, P, ull, d, P, i, P, P, P,
+                                        P, i, d, i, d, d, i]
+        lib.ksor_solve_genb.restype = i
         lib.ksor_set_monitor.argtypes = [MONITOR_FN, P]
         lib.ksor_set_monitor.restype = None
         lib.ksor_spmv.argtypes = [i, P, P, P, P, P, i]
@@ -95,7 +98,7 @@ MONITOR_FN = ctypes.CFUNCTYPE(None, ctypes.c_int, ctypes.c_int, ctypes.POINTER(c
 
 def solve(rowptr, colidx, vals, *, hermitian=True, which="LM", nev=1, ncv=0, mpd=0, tol=1e-8, max_it=0,
           keep=0.5, lock=True, v0=None, nthreads=1, seed=0x5EED, time_budget=0.0, vectors=True, harmonic=False,
-          target=0.0, bdiag=None, conv="rel", purify=True, monitor=None) -> Result:
+          target=0.0, bdiag=None, conv="rel", purify=True, monitor=None, B=None) -> Result:
     """bdiag: the diagonal of B for A x = k B x (EPS_GHEP when hermitian, else EPS_GNHEP); conv: "rel", "abs" or
     "norm" (EPS_CONV_NORM with the infinity norms of A and of B, or 0 for ||B|| without B, as EPSSetUp leaves it)."""
     lib = load()
@@ -116,6 +119,12 @@ def solve(rowptr, colidx, vals, *, hermitian=True, which="LM", nev=1, ncv=0, mpd
     rows = np.repeat(np.arange(n), np.diff(rowptr))
     nrma = float(np.bincount(rows, weights=np.abs(vals), minlength=n).max()) if conv == "norm" and n else 0.0
     nrmb = float(np.max(np.abs(bd))) if conv == "norm" and bd is not None else 0.0
+    if B is not None:
+        brp, bci, bva = (np.ascontiguousarray(B[0], np.int32), np.ascontiguousarray(B[1], np.int32),
+                         np.ascontiguousarray(B[2], np.float64))
+        brows = np.repeat(np.arange(n), np.diff(brp))
+        if conv == "norm":
+            nrmb = float(np.bincount(brows, weights=np.abs(bva), minlength=n).max())
     cb = None
     if monitor is not None:
         def _mon(its, nconv, er, ei, es, nest, _ctx):
@@ -123,11 +132,19 @@ def solve(rowptr, colidx, vals, *, hermitian=True, which="LM", nev=1, ncv=0, mpd
                     [es[i] for i in range(nest)], nest)
         cb = MONITOR_FN(_mon)
     lib.ksor_set_monitor(cb if cb is not None else MONITOR_FN(), None)
-    err = lib.ksor_solve_gen(n, _ptr(rowptr), _ptr(colidx), _ptr(vals), _ptr(bd), int(bool(hermitian)), WHICH[which],
-                             int(nev), int(ncv), int(mpd), float(tol), int(max_it), float(keep), int(bool(lock)),
-                             int(nthreads), _ptr(v0a), int(seed), float(time_budget), _ptr(info), int(cap), _ptr(eigr),
-                             _ptr(eigi), _ptr(errest), _ptr(X), int(bool(harmonic)), float(target), CONV[conv],
-                             nrma, nrmb, int(bool(purify)))
+    if B is None:
+        err = lib.ksor_solve_gen(n, _ptr(rowptr), _ptr(colidx), _ptr(vals), _ptr(bd), int(bool(hermitian)),
+                                 WHICH[which], int(nev), int(ncv), int(mpd), float(tol), int(max_it), float(keep),
+                                 int(bool(lock)), int(nthreads), _ptr(v0a), int(seed), float(time_budget), _ptr(info),
+                                 int(cap), _ptr(eigr), _ptr(eigi), _ptr(errest), _ptr(X), int(bool(harmonic)),
+                                 float(target), CONV[conv], nrma, nrmb, int(bool(purify)))
+    else:
+        err = lib.ksor_solve_genb(n, _ptr(rowptr), _ptr(colidx), _ptr(vals), _ptr(brp), _ptr(bci), _ptr(bva),
+                                  int(bool(hermitian)), WHICH[which], int(nev), int(ncv), int(mpd), float(tol),
+                                  int(max_it), float(keep), int(bool(lock)), int(nthreads), _ptr(v0a), int(seed),
+                                  float(time_budget), _ptr(info), int(cap), _ptr(eigr), _ptr(eigi), _ptr(errest),
+                                  _ptr(X), int(bool(harmonic)), float(target), CONV[conv], nrma, nrmb,
+                                  int(bool(purify)))
     lib.ksor_set_monitor(MONITOR_FN(), None)
     return Result(info, eigr, eigi, errest, X, err)
 

@@ -928,6 +928,10 @@ static void ds_nhep_vectors_all(ds_t *ds) {
   }
 }
 
+typedef struct {
+  int n; const int *rp, *ci; const double *va;
+} csr_t;
+
 /* ------------------------------------------------------------------------------------------------------------
  * BV: basis of m columns of length n (column-major, ld = n) with the reference's coefficient buffer layout:
  * column j of `h` (length m+1) holds the orthogonalisation coefficients of vector j, h[j] its norm.
@@ -943,6 +947,8 @@ typedef struct {
   unsigned long long rng;
   long long npasses;
   const double *bw;  /* diagonal of the inner-product matrix B (BVSetMatrix), NULL: Euclidean */
+  const csr_t *bm;   /* or a general inner-product matrix B (CSR) */
+  double *bt;        /* scratch for B w (n) */
 } bv_t;
 
 #define VCOL(bv, j) ((bv)->V + (size_t)(j) * (size_t)(bv)->n)
@@ -950,8 +956,12 @@ typedef struct {
 /* c[0..j-1] = V[:,0:j]^T w, c[j] = w^T w  (BVDotColumnInc, bvorthog.c:32-47); with an inner-product matrix B the
  * dots are against B w (BV_IPMatMult, bvimpl.h:147-157), B diagonal here */
 static void bv_dot_inc_b(bv_t *bv, int j, const double *w, double *c);
+void ksor_spmv(int n, const int *rowptr, const int *colidx, const double *vals, const double *x, double *y,
+               int nthreads);
+static void bv_dot_inc_general(bv_t *bv, int j, const double *w, double *c);
 static void bv_dot_inc(bv_t *bv, int j, const double *w, double *c) {
   if (bv->bw) { bv_dot_inc_b(bv, j, w, c); return; }
+  if (bv->bm) { bv_dot_inc_general(bv, j, w, c); return; }
   int n = bv->n;
   for (int i = 0; i <= j; i++) c[i] = 0.0;
 #pragma omp parallel num_threads(bv->nthreads)
@@ -1006,6 +1016,36 @@ static void bv_dot_inc_b(bv_t *bv, int j, const double *w, double *c) {
   }
 }
 
+/* the same with a general B: t = B w (BV_IPMatMult, a MatMult), then V^T t and w^T t */
+static void bv_dot_inc_general(bv_t *bv, int j, const double *w, double *c) {
+  int n = bv->n;
+  const double *t = bv->bt;
+  ksor_spmv(n, bv->bm->rp, bv->bm->ci, bv->bm->va, w, bv->bt, bv->nthreads);
+  for (int i = 0; i <= j; i++) c[i] = 0.0;
+#pragma omp parallel num_threads(bv->nthreads)
+  {
+    double loc[1024];
+    double *lp = (j + 1 <= 1024) ? loc : (double *)calloc((size_t)j + 1, sizeof(double));
+    for (int i = 0; i <= j; i++) lp[i] = 0.0;
+#pragma omp for schedule(static)
+    for (int r0 = 0; r0 < n; r0 += 256) {
+      int r1 = r0 + 256 < n ? r0 + 256 : n;
+      for (int i = 0; i < j; i++) {
+        const double *vi = VCOL(bv, i);
+        double s = 0.0;
+        for (int r = r0; r < r1; r++) s += vi[r] * t[r];
+        lp[i] += s;
+      }
+      double s = 0.0;
+      for (int r = r0; r < r1; r++) s += w[r] * t[r];
+      lp[j] += s;
+    }
+#pragma omp critical
+    for (int i = 0; i <= j; i++) c[i] += lp[i];
+    if (lp != loc) free(lp);
+  }
+}
+
 /* w -= V[:,0:j] c  (BVMultColumn / gemv "N") */
 static void bv_mult_sub(bv_t *bv, int j, double *w, const double *c) {
   int n = bv->n;
@@ -1029,6 +1069,12 @@ static double vec_norm(int n, const double *w, int nthreads) {
 
 /* the norm of the BV's inner product (BVNormColumn with a matrix: sqrt(w^T B w)) */
 static double bv_vec_norm(const bv_t *bv, const double *w) {
+  if (bv->bm) {
+    ksor_spmv(bv->n, bv->bm->rp, bv->bm->ci, bv->bm->va, w, bv->bt, bv->nthreads);
+    double s = 0.0;
+    for (int r = 0; r < bv->n; r++) s += w[r] * bv->bt[r];
+    return sqrt(s > 0.0 ? s : 0.0);
+  }
   if (!bv->bw) return vec_norm(bv->n, w, bv->nthreads);
   double s = 0.0;
 #pragma omp parallel for reduction(+ : s) num_threads(bv->nthreads)
@@ -1147,9 +1193,6 @@ void ksor_spmv(int n, const int *rowptr, const int *colidx, const double *vals, 
 /* ------------------------------------------------------------------------------------------------------------
  * The Krylov-Schur solver
  * ------------------------------------------------------------------------------------------------------------ */
-typedef struct {
-  int n; const int *rp, *ci; const double *va;
-} csr_t;
 
 /* DSTranslateHarmonic_NHEP, translation (dsnhep.c:466-507): g = (A - tau I)^T \ (beta e_n), A(:, n-1) += beta g,
  * returns gamma = sqrt(1 + g'g).  The reference factors A - tau I (getrf) and solves with its transpose (getrs "C");
@@ -1215,19 +1258,75 @@ static void harmonic_recover(ds_t *ds, int k, int l, double beta, double *g, dou
 /* BVMatLanczos / BVMatArnoldi (bvkrylov.c:56-226): steps j = k..m-1 */
 /* STApply of STSHIFT with shift 0 (st/impls/shift/shift.c): w = A v, then w = B^-1 w for a generalised problem (a
  * direct solve with the diagonal B: one division per entry) */
-static void st_apply(const csr_t *A, const double *bdiv, const double *v, double *w, int nthreads) {
-  ksor_spmv(A->n, A->rp, A->ci, A->va, v, w, nthreads);
-  if (bdiv)
-    for (int r = 0; r < A->n; r++) w[r] /= bdiv[r];
+/* the operator of STSHIFT with shift 0: A, or B^-1 A with a direct solve with B -- a division per entry for a
+ * diagonal B, or a dense LU factorisation with partial pivoting for a general one (the reference's default
+ * KSPPREONLY + PCLU) */
+typedef struct {
+  const double *bdiv;     /* diagonal B, or NULL */
+  const double *lu;       /* general B: n x n row-major LU factors (unit lower L below the diagonal), or NULL */
+  const int *piv;         /* its row interchanges */
+} stop_t;
+
+/* LU factorisation with partial pivoting (Doolittle, row interchanges as in LAPACK's getrf); 0, or the first
+ * zero pivot + 1 */
+static int lu_factor(int n, double *a, int *piv) {
+  for (int k = 0; k < n; k++) {
+    int p = k;
+    for (int i = k + 1; i < n; i++)
+      if (fabs(a[(size_t)i * n + k]) > fabs(a[(size_t)p * n + k])) p = i;
+    piv[k] = p;
+    if (a[(size_t)p * n + k] == 0.0) return k + 1;
+    if (p != k)
+      for (int j = 0; j < n; j++) {
+        double t = a[(size_t)k * n + j];
+        a[(size_t)k * n + j] = a[(size_t)p * n + j];
+        a[(size_t)p * n + j] = t;
+      }
+    const double d = a[(size_t)k * n + k];
+    for (int i = k + 1; i < n; i++) {
+      double l = a[(size_t)i * n + k] / d;
+      a[(size_t)i * n + k] = l;
+      if (l != 0.0)
+        for (int j = k + 1; j < n; j++) a[(size_t)i * n + j] -= l * a[(size_t)k * n + j];
+    }
+  }
+  return 0;
 }
 
-static int krylov_factor(bv_t *bv, const csr_t *A, const double *bdiv, int hermitian, ds_t *ds, int k, int *m,
+static void lu_solve(int n, const double *a, const int *piv, double *x) {
+  for (int k = 0; k < n; k++)
+    if (piv[k] != k) {
+      double t = x[k];
+      x[k] = x[piv[k]];
+      x[piv[k]] = t;
+    }
+  for (int i = 1; i < n; i++) {
+    double s = x[i];
+    for (int j = 0; j < i; j++) s -= a[(size_t)i * n + j] * x[j];
+    x[i] = s;
+  }
+  for (int i = n - 1; i >= 0; i--) {
+    double s = x[i];
+    for (int j = i + 1; j < n; j++) s -= a[(size_t)i * n + j] * x[j];
+    x[i] = s / a[(size_t)i * n + i];
+  }
+}
+
+static void st_apply(const csr_t *A, const stop_t *op, const double *v, double *w, int nthreads) {
+  ksor_spmv(A->n, A->rp, A->ci, A->va, v, w, nthreads);
+  if (op->bdiv)
+    for (int r = 0; r < A->n; r++) w[r] /= op->bdiv[r];
+  else if (op->lu)
+    lu_solve(A->n, op->lu, op->piv, w);
+}
+
+static int krylov_factor(bv_t *bv, const csr_t *A, const stop_t *op, int hermitian, ds_t *ds, int k, int *m,
                          double *beta, int *breakdown, long long *nsteps) {
   int lindep = 0, err;
   double nrm = 0.0;
   int j;
   for (j = k; j < *m; j++) {
-    st_apply(A, bdiv, VCOL(bv, j), VCOL(bv, j + 1), bv->nthreads);
+    st_apply(A, op, VCOL(bv, j), VCOL(bv, j + 1), bv->nthreads);
     (*nsteps)++;
     if ((err = bv_orthonormalize(bv, j + 1, &nrm, &lindep))) return err;
     if (lindep) { *m = j + 1; break; }
@@ -1267,18 +1366,51 @@ void ksor_set_monitor(ksor_monitor_fn fn, void *ctx) {
   g_monitor_ctx = ctx;
 }
 
+static int solve_impl(int n, const int *rowptr, const int *colidx, const double *vals, const double *bdiag,
+                      const csr_t *bcsr, int hermitian, int which, int nev, int ncv, int mpd, double tol, int max_it,
+                      double keep, int lock, int nthreads, const double *v0, unsigned long long seed,
+                      double time_budget_s, int *info, int ncv_cap, double *eigr_out, double *eigi_out,
+                      double *errest_out, double *X, int harmonic, double target, int conv, double nrma,
+                      double nrmb, int purify);
+
 int ksor_solve_gen(int n, const int *rowptr, const int *colidx, const double *vals, const double *bdiag,
                    int hermitian, int which, int nev, int ncv, int mpd, double tol, int max_it,
                    double keep, int lock, int nthreads, const double *v0, unsigned long long seed,
                    double time_budget_s,
                    int *info, int ncv_cap, double *eigr_out, double *eigi_out, double *errest_out, double *X,
                    int harmonic, double target, int conv, double nrma, double nrmb, int purify) {
+  return solve_impl(n, rowptr, colidx, vals, bdiag, NULL, hermitian, which, nev, ncv, mpd, tol, max_it, keep, lock,
+                    nthreads, v0, seed, time_budget_s, info, ncv_cap, eigr_out, eigi_out, errest_out, X, harmonic,
+                    target, conv, nrma, nrmb, purify);
+}
+
+int ksor_solve_genb(int n, const int *rowptr, const int *colidx, const double *vals, const int *browptr,
+                    const int *bcolidx, const double *bvals, int hermitian, int which, int nev, int ncv, int mpd,
+                    double tol, int max_it, double keep, int lock, int nthreads, const double *v0,
+                    unsigned long long seed, double time_budget_s, int *info, int ncv_cap, double *eigr_out,
+                    double *eigi_out, double *errest_out, double *X, int harmonic, double target, int conv,
+                    double nrma, double nrmb, int purify) {
+  const csr_t B = {n, browptr, bcolidx, bvals};
+  return solve_impl(n, rowptr, colidx, vals, NULL, &B, hermitian, which, nev, ncv, mpd, tol, max_it, keep, lock,
+                    nthreads, v0, seed, time_budget_s, info, ncv_cap, eigr_out, eigi_out, errest_out, X, harmonic,
+                    target, conv, nrma, nrmb, purify);
+}
+
+static int solve_impl(int n, const int *rowptr, const int *colidx, const double *vals, const double *bdiag,
+                      const csr_t *bcsr, int hermitian, int which, int nev, int ncv, int mpd, double tol, int max_it,
+                      double keep, int lock, int nthreads, const double *v0, unsigned long long seed,
+                      double time_budget_s, int *info, int ncv_cap, double *eigr_out, double *eigi_out,
+                      double *errest_out, double *X, int harmonic, double target, int conv, double nrma,
+                      double nrmb, int purify) {
   double t_start = now_s();
   /* generalised problems (epssetup.c:321-329): B^-1 A, with the B-inner product when Hermitian (GHEP); start
    * vectors forced into the range of the operator and eigenvectors purified for GHEP (epssolve.c:855-862,
    * epsdefault.c:28-50) */
-  const int ghep = bdiag && hermitian;
+  const int ghep = (bdiag || bcsr) && hermitian;
   const csr_t Acsr = {n, rowptr, colidx, vals};
+  stop_t op = {bdiag, NULL, NULL};
+  double *lu = NULL;
+  int *piv = NULL;
   /* EPSSolve_KrylovSchur_Default (krylovschur.c:238-239): harmonic extraction runs the non-symmetric variant */
   if (harmonic) hermitian = 0;
   if (n <= 0 || nev <= 0) return 63;
@@ -1305,6 +1437,7 @@ int ksor_solve_gen(int n, const int *rowptr, const int *colidx, const double *va
   bv.n = n; bv.m = ncv + 1; bv.eta = 0.7071; bv.refine = 1; bv.nthreads = nthreads;
   bv.rng = seed ? seed : 0x5eed;
   bv.bw = ghep ? bdiag : NULL;
+  bv.bm = ghep ? bcsr : NULL;
   bv.V = (double *)calloc((size_t)n * bv.m, sizeof(double));
   bv.h = (double *)calloc((size_t)(bv.m + 1) * (bv.m + 1), sizeof(double));
   bv.c = (double *)calloc((size_t)bv.m + 1, sizeof(double));
@@ -1324,6 +1457,19 @@ int ksor_solve_gen(int n, const int *rowptr, const int *colidx, const double *va
   int err = 0, reason = KSOR_ITERATING, its = 0, nconv = 0;
   long long nsteps = 0;
   if (!bv.V || !bv.h || !bv.c || !ds.A || !ds.Q || !ds.X) { err = 55; goto done; }
+  if (bcsr) {
+    /* the dense LU of B (n^2 doubles: the oracle's general-B path is for test sizes) */
+    if (n > 8192) { err = 56; goto done; }
+    lu = (double *)calloc((size_t)n * n, sizeof(double));
+    piv = (int *)calloc((size_t)n, sizeof(int));
+    bv.bt = (double *)calloc((size_t)n, sizeof(double));
+    if (!lu || !piv || !bv.bt) { err = 55; goto done; }
+    for (int r = 0; r < n; r++)
+      for (int p = bcsr->rp[r]; p < bcsr->rp[r + 1]; p++) lu[(size_t)r * n + bcsr->ci[p]] += bcsr->va[p];
+    if (lu_factor(n, lu, piv)) { err = 71; goto done; } /* PETSC_ERR_MAT_LU_ZRPVT: B is singular */
+    op.lu = lu;
+    op.piv = piv;
+  }
 
   /* start vector: EPSSetInitialSpace copy, or a random one; then orthonormalise (EPSGetStartVector) */
   if (v0) memcpy(bv.V, v0, sizeof(double) * n);
@@ -1331,7 +1477,7 @@ int ksor_solve_gen(int n, const int *rowptr, const int *colidx, const double *va
   if (ghep) {
     double *t = (double *)malloc(sizeof(double) * n);
     memcpy(t, bv.V, sizeof(double) * n);
-    st_apply(&Acsr, bdiag, t, bv.V, nthreads);
+    st_apply(&Acsr, &op, t, bv.V, nthreads);
     free(t);
   }
   {
@@ -1348,7 +1494,7 @@ int ksor_solve_gen(int n, const int *rowptr, const int *colidx, const double *va
     ds.n = nv; ds.t = nv; ds.l = nconv; ds.k = nconv + l;
     double beta = 0.0;
     int breakdown = 0;
-    err = krylov_factor(&bv, &Acsr, bdiag, hermitian, &ds, nconv + l, &nv, &beta, &breakdown, &nsteps);
+    err = krylov_factor(&bv, &Acsr, &op, hermitian, &ds, nconv + l, &nv, &beta, &breakdown, &nsteps);
     if (err) goto done;
     ds.n = nv; ds.t = nv; ds.l = nconv; ds.k = nconv + l;
     ds.state = l ? ST_RAW : ST_INTERMEDIATE;
@@ -1413,7 +1559,7 @@ int ksor_solve_gen(int n, const int *rowptr, const int *colidx, const double *va
           if (ghep) {
             double *t = (double *)malloc(sizeof(double) * n);
             memcpy(t, VCOL(&bv, k), sizeof(double) * n);
-            st_apply(&Acsr, bdiag, t, VCOL(&bv, k), nthreads);
+            st_apply(&Acsr, &op, t, VCOL(&bv, k), nthreads);
             free(t);
           }
           double nrm;
@@ -1463,7 +1609,7 @@ int ksor_solve_gen(int n, const int *rowptr, const int *colidx, const double *va
     double *t = (double *)malloc(sizeof(double) * n);
     for (int j = 0; j < nconv; j++) {
       memcpy(t, VCOL(&bv, j), sizeof(double) * n);
-      st_apply(&Acsr, bdiag, t, VCOL(&bv, j), nthreads);
+      st_apply(&Acsr, &op, t, VCOL(&bv, j), nthreads);
       double nrm = bv_vec_norm(&bv, VCOL(&bv, j));
       if (nrm > 0.0) bv_scale(&bv, j, 1.0 / nrm);
     }
@@ -1515,7 +1661,7 @@ done:
     info[KSOR_INFO_MPD] = mpd;
     info[KSOR_INFO_MAXIT] = max_it;
   }
-  free(bv.V); free(bv.h); free(bv.c);
+  free(bv.V); free(bv.h); free(bv.c); free(bv.bt); free(lu); free(piv);
   free(ds.d); free(ds.e); free(ds.A); free(ds.Q); free(ds.X); free(ds.perm); free(ds.work);
   free(eigr); free(eigi); free(errest); free(perm); free(hg);
   return err;

@@ -57,6 +57,16 @@ int ksor_solve_gen(int n, const int *rowptr, const int *colidx, const double *va
                    int *info, int ncv_cap, double *eigr, double *eigi, double *errest, double *X,
                    int harmonic, double target, int conv, double nrma, double nrmb, int purify);
 
+/* ksor_solve_gen for a general B in CSR (B rowptr/colidx/vals): the direct solve with B is a dense LU factorisation
+ * with partial pivoting (n <= 8192; a singular B returns 71), and for hermitian (EPS_GHEP) the B-inner products
+ * multiply by B in CSR. */
+int ksor_solve_genb(int n, const int *rowptr, const int *colidx, const double *vals, const int *browptr,
+                    const int *bcolidx, const double *bvals, int hermitian, int which, int nev, int ncv, int mpd,
+                    double tol, int max_it, double keep, int lock, int nthreads, const double *v0,
+                    unsigned long long seed, double time_budget_s, int *info, int ncv_cap, double *eigr,
+                    double *eigi, double *errest, double *X, int harmonic, double target, int conv, double nrma,
+                    double nrmb, int purify);
+
 /* A monitor called by the solves after every restart, as EPSMonitor is (epsmon.c:40-48): restart count, number
  * converged, the nest current values and error estimates.  NULL turns it off.  Not thread-safe (one global). */
 typedef void (*ksor_monitor_fn)(int its, int nconv, const double *eigr, const double *eigi, const double *errest,

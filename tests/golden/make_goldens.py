@@ -2,7 +2,7 @@
 other machines use the committed JSON).  Only the printed eigenvalues/norms of the Krylov-Schur-path tests are
 extracted, with the lines EPSErrorView printed; each entry records the file it came from and the options of that
 test.  The real matrix those tests read from a PETSc binary file (share/slepc/datafiles/matrices/rdb200.petsc)
-is converted to CSR arrays in rdb200.npz by an independent big-endian reader."""
+is converted to CSR arrays in rdb200.npz by an independent big-endian reader, as are bfw62a/bfw62b (ex7.c)."""
 import json
 import os
 import re
@@ -117,8 +117,29 @@ def main():
     g["test20_1"] = {"source": "src/eps/tests/output/test20_1.out", "n": 18, "nev": 1, "which": "SR",
                      "tol": max(1000 * 2.220446049250313e-16, 1e-9), "ncv": [16, 18],
                      "eigenvalues": [floats(l)[0] for l in lines if re.search(r"\d\.\d{5}", l)]}
+    # GNHEP from PETSc binary files bfw62a / bfw62b (62 x 62, B not diagonal), nev 4, largest magnitude, tol 1e-8
+    # (src/eps/tutorials/ex7.c TEST 1), and the pencil (A, A) whose eigenvalues are all 1 (TEST 3)
+    for key, src in (("ex7_1", "src/eps/tutorials/output/ex7_1.out"), ("ex7_3", "src/eps/tutorials/output/ex7_3.out")):
+        txt = read(src)
+        line = [l for l in txt.splitlines() if re.search(r"\d\.\d{5}", l)][-1]
+        pairs = re.findall(r"(-?\d+\.\d+)(?:([+-]\d+\.\d+)i)?", line)
+        g[key] = {"source": src, "matrices": ["bfw62a.npz", "bfw62b.npz" if key == "ex7_1" else "bfw62a.npz"],
+                  "nev": 4, "which": "LM", "tol": 1e-8,
+                  "iterations": int(re.search(r"Number of iterations of the method: (\d+)", txt).group(1)),
+                  "eigenvalues": [[float(a), float(b) if b else 0.0] for a, b in pairs]}
+    for name in ("bfw62a", "bfw62b"):
+        raw = open(os.path.join(REF, "share/slepc/datafiles/matrices/%s.petsc" % name), "rb").read()
+        classid, m, n, nz = np.frombuffer(raw[:16], dtype=">i4")
+        assert classid == 1211216 and len(raw) == 16 + 4 * m + 12 * nz
+        lens = np.frombuffer(raw[16:16 + 4 * m], dtype=">i4").astype(np.int32)
+        cols = np.frombuffer(raw[16 + 4 * m:16 + 4 * m + 4 * nz], dtype=">i4").astype(np.int32)
+        vals = np.frombuffer(raw[16 + 4 * m + 4 * nz:], dtype=">f8").astype(np.float64)
+        np.savez(os.path.join(os.path.dirname(OUT), name + ".npz"),
+                 rowptr=np.concatenate([[0], np.cumsum(lens)]).astype(np.int32), colidx=cols, vals=vals,
+                 shape=np.array([m, n], dtype=np.int32))
     # the text EPSErrorView prints (the "All requested ..." line and the eigenvalue line), per solve of each test
-    for key in ("ex2_1", "ex9_1", "ex4_1", "test2_1", "test2_3", "test1_1", "ex5_1", "test4_1", "test6_1"):
+    for key in ("ex2_1", "ex9_1", "ex4_1", "test2_1", "test2_3", "test1_1", "ex5_1", "test4_1", "test6_1", "ex7_1",
+                "ex7_3"):
         lines = read(g[key]["source"]).splitlines()
         g[key]["errorview"] = [[lines[i], lines[i + 1]] for i, l in enumerate(lines)
                                if l.startswith(" All requested eigenvalues")]

@@ -317,3 +317,67 @@ def test_test20_full_basis_golden(orc):
     # ncv above n is clamped to n (epssetup.c:337-338)
     r = orc.solve(*csr, hermitian=True, which="SR", nev=2, ncv=40, tol=g["tol"], v0=matgen.start_vector(g["n"], 1))
     assert r.err == 0 and r.reason == 1 and r.ncv == g["n"]
+
+
+def _npz(name):
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", name))
+    return d["rowptr"], d["colidx"], d["vals"]
+
+
+def test_ex7_general_b_goldens(orc):
+    """ex7.c: the GNHEP pencil of the reference's data files bfw62a / bfw62b (B symmetric, not diagonal), B^-1 A with
+    a direct solve: the golden eigenvalues within the run's tolerance (tol 1e-8 fixes about 3 decimals of values
+    near 2e5) and the dense generalised solve at tol 1e-12; then the pencil (A, A), all eigenvalues 1 in one restart
+    as the reference reports."""
+    import scipy.linalg as sl
+    g = G["ex7_1"]
+    A, B = _npz("bfw62a.npz"), _npz("bfw62b.npz")
+    v0 = matgen.start_vector(62, 1)
+    r = orc.solve(*A, hermitian=False, which=g["which"], nev=g["nev"], tol=g["tol"], B=B, v0=v0)
+    assert r.err == 0 and r.reason == 1
+    for (a, b), x, y in zip(g["eigenvalues"], r.eigr, r.eigi):
+        assert abs(complex(x, y) - complex(a, b)) <= 10 * g["tol"] * abs(complex(a, b)) + 1e-5
+    r = orc.solve(*A, hermitian=False, which=g["which"], nev=g["nev"], tol=1e-12, B=B, v0=v0)
+    w = sl.eig(matgen.csr_to_dense(*A), matgen.csr_to_dense(*B), right=False)
+    for x, y in zip(r.eigr[:4], r.eigi[:4]):
+        z = complex(x, y)
+        assert np.min(np.abs(w - z)) <= 1e-10 * abs(z)
+    g3 = G["ex7_3"]
+    r = orc.solve(*A, hermitian=False, which=g3["which"], nev=g3["nev"], tol=g3["tol"], B=A, v0=v0)
+    assert r.err == 0 and r.reason == 1 and r.its == g3["iterations"]
+    assert [[round(float(x), 5), round(float(y), 5)] for x, y in zip(r.eigr[:4], r.eigi[:4])] == g3["eigenvalues"]
+
+
+def test_general_b_ghep(orc):
+    """EPS_GHEP with a general SPD B (a tridiagonal mass matrix): against scipy.linalg.eigh(A, B), B-orthonormal
+    purified eigenvectors; and a diagonal B through the general path gives the diagonal path's solve exactly."""
+    import scipy.linalg as sl
+    m = 12
+    csr = matgen.laplacian_2d(m, m)
+    n = m * m
+    rp = [0]
+    ci, va = [], []
+    for r in range(n):
+        for c, v in ((r - 1, 1.0), (r, 4.0), (r + 1, 1.0)):
+            if 0 <= c < n:
+                ci.append(c)
+                va.append(v / 6.0)
+        rp.append(len(ci))
+    Bc = (np.array(rp, np.int32), np.array(ci, np.int32), np.array(va))
+    v0 = matgen.start_vector(n, 3)
+    for which in ("LR", "SR"):
+        r = orc.solve(*csr, hermitian=True, which=which, nev=5, tol=1e-12, B=Bc, v0=v0)
+        assert r.err == 0 and r.reason == 1
+        Bd = matgen.csr_to_dense(*Bc)
+        w = sl.eigh(matgen.csr_to_dense(*csr), Bd, eigvals_only=True)
+        for lam in r.eigr[:5]:
+            assert np.min(np.abs(w - lam)) <= 1e-10 * abs(lam)
+        X = r.X[:, :r.nconv]
+        assert np.abs(X.T @ Bd @ X - np.eye(r.nconv)).max() < 1e-10
+    g = G["test1_1"]
+    csr = matgen.laplacian_2d(*g["grid"])
+    b = matgen.log_mass(324)
+    kw = dict(hermitian=True, which="LM", nev=4, tol=g["tol"], conv="norm", v0=matgen.start_vector(324, 1))
+    r1 = orc.solve(*csr, bdiag=b, **kw)
+    r2 = orc.solve(*csr, B=matgen.diagonal(b), **kw)
+    assert r1.its == r2.its and np.array_equal(r1.eigr, r2.eigr)
