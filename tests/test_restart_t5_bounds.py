@@ -1,0 +1,121 @@
+"""CPU model of the tcgen05 restart kernel's addressing (k_restart_t5 in slepc_gb300/csrc/k_restart_tc.cu): for a sweep
+of problem sizes and restart shapes, every shared-memory, tensor-memory, scratch, Q-slice and basis access the
+kernel makes stays inside its allocation, every bulk copy is 16-byte aligned with a size that is a multiple of 16,
+and the mbarrier transaction counts stay below 2^20.  The constants and formulas are the kernel's; a change there
+must be mirrored here."""
+import itertools
+
+import pytest
+
+# kernel constants
+OZ_SA, OZ_S, OZ_L, OZ_NC = 8, 7, 8, 32
+T5_M, T5_NC, T5_KC, T5_THREADS = 128, 64, 32, 512
+T5_ASL = T5_M * T5_KC * 2
+T5_BSL = T5_NC * T5_KC * 2
+T5_STAGE = OZ_SA * T5_ASL + OZ_S * T5_BSL
+T5_SMEM = 2 * T5_STAGE + (T5_THREADS // T5_M + 1) * T5_M * 4 + 5 * 8 + 16
+TMEM_COLS = OZ_L * T5_NC
+NUM_SMS = 152
+BF16 = 2
+
+
+def rup(x, m):
+    return (x + m - 1) // m * m
+
+
+def scratch_layout(ld):
+    """restart_tc_scratch_bytes / t5_qbytes / t5_abytes / restart_t5_scratch_bytes"""
+    kp_max, np_ = rup(ld, 16), rup(ld, OZ_NC)
+    tc = OZ_S * np_ * kp_max * BF16 + np_ * 4 + 256
+    q = rup(tc, 256)
+    a = NUM_SMS * OZ_SA * rup(ld, 16) * 128 * BF16
+    return {"np": np_, "tc": tc, "q": q, "a": a, "total": q + a + 256}
+
+
+def check(n, ld, K, N):
+    assert 0 < K <= ld and 0 < N <= ld and ld <= 144
+    lay = scratch_layout(ld)
+    np_ = lay["np"]
+    kp, ldp = rup(K, 16), rup(ld, 16)
+    assert kp <= ldp and np_ >= rup(N, 16)            # the launch's own checks
+    assert K * T5_M * 8 <= 2 * T5_STAGE                # the V tile fits the stage region
+    assert T5_SMEM <= 227 * 1024
+    # shared layout: stages, erow + etmp, five mbarriers (8-byte aligned), the TMEM slot
+    erow = 2 * T5_STAGE
+    bars = erow + (T5_THREADS // T5_M) * T5_M * 4
+    assert bars % 8 == 0 and bars + 5 * 8 + 4 <= T5_SMEM
+    nk8 = kp // 8
+    ntiles = -(-n // T5_M)
+    blocks = min(NUM_SMS, ntiles)
+    ldv = rup(n, 64)
+    v_elems = ldv * (ld + 1)                           # float2 entries of the basis
+    # Q slices (cm layout) written by k_oz_qslice: element (t, c, k)
+    q_max = ((OZ_S - 1) * nk8 + (kp - 1) // 8) * (np_ // 8) * 64 + ((np_ - 1) // 8) * 64 + 7 * 8 + 7
+    assert (q_max + 1) * BF16 <= OZ_S * np_ * kp * BF16 <= lay["tc"]
+    # per-CTA slice scratch
+    per_cta = OZ_SA * nk8 * 16 * 64 * BF16
+    assert blocks * per_cta <= lay["a"]
+    assert lay["q"] % 16 == 0 and per_cta % 16 == 0
+    for tile in range(ntiles):
+        r0 = tile * T5_M
+        rows = min(T5_M, n - r0)
+        rows2 = (rows + 1) & ~1
+        # V tile bulk copies: column k at r0 + (a0 + k) ldv, rows2 entries; a0 + K <= ld
+        for a0 in (0, ld - K):
+            first = r0 + a0 * ldv
+            last = r0 + (a0 + K - 1) * ldv + rows2 - 1
+            assert first * 8 % 16 == 0 and rows2 * 8 % 16 == 0 and last < v_elems
+        assert K * rows2 * 8 < (1 << 20)               # mbarrier transaction count
+        # slicing stores: item (m, k8) -> ((s nk8 + k8) 16 + m / 8) 64 + (m % 8) 8, 16 bytes
+        top = ((OZ_SA - 1) * nk8 + nk8 - 1) * 16 * 64 + 15 * 64 + 7 * 8 + 8
+        assert top * BF16 <= per_cta
+    # chunks and stages
+    nkc = -(-kp // T5_KC)
+    for c0 in range(0, N, T5_NC):
+        nch = min(T5_NC, rup(N - c0, 16))
+        assert nch % 16 == 0 and 16 <= nch <= 256       # MMA N for M = 128
+        assert (OZ_L - 1) * T5_NC + nch <= TMEM_COLS    # level accumulators
+        for i in range(nkc):
+            kc8 = i * (T5_KC // 8)
+            sk8 = min(T5_KC // 8, nk8 - kc8)
+            assert sk8 in (2, 4)
+            abytes = sk8 * 16 * 128
+            bbytes = (nch // 8) * 128
+            assert abytes % 16 == 0 and bbytes % 16 == 0
+            assert OZ_SA * abytes + OZ_S * sk8 * bbytes < (1 << 20)
+            # A copies: source inside the CTA's slice scratch, destination inside its slice of the stage
+            for sl in range(OZ_SA):
+                src_end = ((sl * nk8 + kc8) * 16 * 64) * BF16 + abytes
+                assert src_end <= per_cta and abytes <= T5_ASL
+            # B copies: source inside the Q slices, destination inside the slice of the stage
+            for t, k8 in itertools.product(range(OZ_S), range(sk8)):
+                src = (((t * nk8 + kc8 + k8) * (np_ // 8) + c0 // 8) * 64) * BF16
+                assert src % 16 == 0 and src + bbytes <= OZ_S * np_ * kp * BF16
+                assert k8 * (T5_NC // 8) * 128 + bbytes <= T5_BSL
+            # what the tensor cores read per MMA (K-major, no swizzle: 8-row groups at SBO, K core matrices at LBO)
+            for j in range(sk8 // 2):
+                a_lo = j * 2 * 16 * 128
+                a_hi = a_lo + 15 * 128 + 1 * (16 * 128) + 128
+                b_lo = j * 2 * (T5_NC // 8) * 128
+                b_hi = b_lo + (nch // 8 - 1) * 128 + 1 * (T5_NC // 8) * 128 + 128
+                assert a_hi <= T5_ASL and b_hi <= T5_BSL
+                assert (2 * T5_STAGE) >> 4 < (1 << 14)  # descriptor start-address field
+        # epilogue: warp w reads lanes 32 (w % 4) .. +31 and columns L 64 + 16 (w / 4) .. +15 when below nch
+        for w in range(T5_THREADS // 32):
+            col = 16 * (w // 4)
+            if col < nch:
+                assert 32 * (w % 4) + 31 < 128 and (OZ_L - 1) * T5_NC + col + 16 <= TMEM_COLS
+                assert c0 + col < rup(N, 16) <= np_     # fcol entries read are written by k_oz_qslice
+
+
+@pytest.mark.parametrize("n", [1, 2, 127, 128, 129, 1000, 4095, 12167, 27000])
+@pytest.mark.parametrize("ld,K,N", [(24, 24, 17), (41, 40, 30), (111, 110, 70), (129, 128, 64), (129, 128, 96),
+                                    (129, 75, 128), (144, 143, 143), (144, 16, 16), (33, 1, 1)])
+def test_t5_addressing_in_bounds(n, ld, K, N):
+    check(n, ld, K, N)
+
+
+def test_t5_shared_memory_and_registers_fit():
+    # 512 threads x at most 112 registers (ptxas -v: 110) fit the SM's 65,536 registers; one CTA per SM by TMEM and shared memory
+    assert T5_THREADS * 112 <= 65536
+    assert 2 * T5_SMEM > 228 * 1024
