@@ -398,12 +398,11 @@ class EPS:
         if space is None or (isinstance(space, (list, tuple)) and len(space) == 0):
             _check(load().EPSSetInitialSpace(self.handle, 0, None), "EPSSetInitialSpace")
             return
-        if isinstance(space, (list, tuple)):
-            space = space[0]
-        v = space if isinstance(space, Vec) else Vec(space)
-        self._v0 = v
-        arr = (ctypes.c_void_p * 1)(v.handle.value)
-        _check(load().EPSSetInitialSpace(self.handle, 1, arr), "EPSSetInitialSpace")
+        vecs = list(space) if isinstance(space, (list, tuple)) else [space]
+        vecs = [x if isinstance(x, Vec) else Vec(x) for x in vecs]
+        self._v0 = vecs
+        arr = (ctypes.c_void_p * len(vecs))(*[x.handle.value for x in vecs])
+        _check(load().EPSSetInitialSpace(self.handle, len(vecs), arr), "EPSSetInitialSpace")
 
     def setKrylovSchurRestart(self, keep):
         _check(load().EPSKrylovSchurSetRestart(self.handle, float(keep)), "EPSKrylovSchurSetRestart")

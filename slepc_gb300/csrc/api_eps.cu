@@ -796,14 +796,19 @@ extern "C" PetscErrorCode EPSGetWhichEigenpairs(EPS eps, EPSWhich *which) {
   *which = (EPSWhich)(eps->which ? eps->which : EPS_LARGEST_MAGNITUDE);
   return 0;
 }
+// EPSSetInitialSpace (epssetup.c:592-602, consumed at :400-406): the reference inserts the n vectors into the basis
+// (at most ncv of them), and Krylov-Schur's factorisation starts from the first (EPSGetStartVector(eps, 0)), so the
+// first vector is the one kept
 extern "C" PetscErrorCode EPSSetInitialSpace(EPS eps, PetscInt n, Vec is[]) {
   KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
-  KSG_CHECK(n >= 0 && n <= 1, PETSC_ERR_SUP, "An initial space of at most one vector is provided");
+  KSG_CHECK(n >= 0, PETSC_ERR_ARG_OUTOFRANGE, "Argument n cannot be negative");
   if (n == 0) eps->v0.clear();
   else {
-    KSG_CHECK(is && is[0], PETSC_ERR_ARG_NULL, "Null initial vector");
+    KSG_CHECK(is, PETSC_ERR_ARG_NULL, "Null initial space");
+    for (PetscInt i = 0; i < n; ++i) KSG_CHECK(is[i], PETSC_ERR_ARG_NULL, "Null initial vector %d", (int)i);
     eps->v0.assign(is[0]->a, is[0]->a + is[0]->n);
   }
+  eps->nini = (int)n;
   eps->solved = 0;
   return 0;
 }
@@ -1099,6 +1104,7 @@ extern "C" PetscErrorCode EPSSetUp(EPS eps) {
   KSG_CHECK(ncv + 1 <= 144, PETSC_ERR_SUP, "ncv (%d) above 143 is not provided by the device projected solver", ncv);
   KSG_CHECK(eps->lock || mpd >= ncv, PETSC_ERR_SUP, "Should not use mpd parameter in non-locking variant");
   KSG_CHECK(eps->v0.empty() || (int)eps->v0.size() == n, PETSC_ERR_ARG_SIZ, "Initial vector has the wrong length");
+  KSG_CHECK(eps->nini <= ncv, PETSC_ERR_USER_INPUT, "The number of initial vectors is larger than ncv");
   eps->nev_e = nev;
   eps->ncv_e = ncv;
   eps->mpd_e = mpd;

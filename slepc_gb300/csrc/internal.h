@@ -145,7 +145,8 @@ struct _p_EPS {
   double time_limit = 0.0;        // EPSGB300SetTimeLimit (0: none)
   int restart_method = 0;         // EPSGB300RestartMethod
   int device = -1;
-  std::vector<double> v0;
+  std::vector<double> v0;  // the first vector of the initial space
+  int nini = 0;            // the size of the initial space given
   std::vector<double> v0_internal;  // start vector of the precision form's refinement sweep
   unsigned long long seed = 0x5EEDULL;
   unsigned long long rng_counter = 0;

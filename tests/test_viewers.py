@@ -257,3 +257,13 @@ def test_st_object_and_problem_queries(lib):
         flags[ptype] = tuple(got)
         assert tuple(got) == want, (ptype, got)
     eps.destroy()
+
+
+def test_initial_space_of_several_vectors(lib):
+    """EPSSetInitialSpace with several vectors is accepted (the factorisation starts from the first, as in the
+    reference); a negative count is an error."""
+    eps = sg.EPS().create()
+    eps.setInitialSpace([np.ones(20), np.arange(20.0), np.zeros(20)])
+    lib.EPSSetInitialSpace.argtypes = [P, ctypes.c_int, P]
+    assert lib.EPSSetInitialSpace(eps.handle, -1, None) == 63
+    eps.destroy()
