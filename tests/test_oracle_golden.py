@@ -381,3 +381,21 @@ def test_general_b_ghep(orc):
     r1 = orc.solve(*csr, bdiag=b, **kw)
     r2 = orc.solve(*csr, B=matgen.diagonal(b), **kw)
     assert r1.its == r2.its and np.array_equal(r1.eigr, r2.eigr)
+
+
+def test_ghep_harmonic_interior(orc):
+    """Interior eigenvalues of a definite pencil: EPS_GHEP with harmonic extraction around a target (the Arnoldi
+    variant with the B-inner product, as the reference runs Krylov-Schur with harmonic extraction on a Hermitian
+    problem), against scipy.linalg.eigh(A, B): the eigenvalues closest to the target."""
+    import scipy.linalg as sl
+    m = 14
+    csr = matgen.laplacian_2d(m, m)
+    n = m * m
+    b = 1.0 + matgen.uniform_01(9, n)
+    target = 2.05
+    r = orc.solve(*csr, hermitian=True, which="TM", nev=4, ncv=40, tol=1e-11, bdiag=b, harmonic=True, target=target,
+                  v0=matgen.start_vector(n, 2))
+    assert r.err == 0 and r.reason == 1
+    w = sl.eigh(matgen.csr_to_dense(*csr), np.diag(b), eigvals_only=True)
+    want = w[np.argsort(np.abs(w - target))][:4]
+    assert np.allclose(np.sort(r.eigr[:4]), np.sort(want), rtol=1e-9, atol=0)
