@@ -1,0 +1,90 @@
+"""The boundary's argument checks without a GPU: the PETSc error codes the reference's PetscCheck sites return
+(epssetup.c:440-500 EPSSetOperators, epsopts.c EPSSet*, epsmon.c EPSMonitorSet), raised by the library before any
+device work."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import slepc_gb300 as sg
+from slepc_gb300 import matgen
+
+P = ctypes.c_void_p
+PETSC_ERR_SUP, PETSC_ERR_ARG_WRONG, PETSC_ERR_ARG_OUTOFRANGE = 56, 62, 63
+PETSC_ERR_ARG_WRONGSTATE, PETSC_ERR_ARG_INCOMP, PETSC_ERR_ARG_NULL = 73, 75, 85
+
+
+@pytest.fixture(scope="module")
+def lib():
+    sg.build()
+    return sg.load()
+
+
+def code(fn, *a):
+    with pytest.raises(sg.SlepcError) as e:
+        fn(*a)
+    return e.value.code
+
+
+def test_operator_checks(lib):
+    eps = sg.EPS().create()
+    A = sg.Mat(*matgen.laplacian_1d(10))
+    B = sg.Mat(*matgen.diagonal(np.ones(12)))
+    assert code(eps.setOperators, A, B) == PETSC_ERR_ARG_INCOMP        # "Dimensions of A and B do not match"
+    rect = sg.Mat(np.array([0, 1, 2], np.int32), np.array([0, 2], np.int32), np.array([1.0, 2.0]), ncols=3)
+    assert code(eps.setOperators, rect) == PETSC_ERR_ARG_WRONG        # "A does not have equal row and column sizes"
+    empty = P()
+    assert lib.MatCreate(0, ctypes.byref(empty)) == 0
+    lib.EPSSetOperators.argtypes = [P, P, P]
+    assert lib.EPSSetOperators(eps.handle, empty, None) == PETSC_ERR_ARG_WRONGSTATE  # MatCreate without MatLoad
+    assert lib.EPSSetOperators(eps.handle, None, None) == PETSC_ERR_ARG_NULL
+    assert lib.MatDestroy(ctypes.byref(empty)) == 0
+    eps.setOperators(A, sg.Mat(*matgen.diagonal(np.ones(10))))        # a consistent pencil is accepted
+    eps.destroy()
+
+
+def test_setting_checks(lib):
+    eps = sg.EPS().create()
+    lib.EPSSetProblemType.argtypes = [P, ctypes.c_int]
+    assert lib.EPSSetProblemType(eps.handle, 6) == PETSC_ERR_SUP       # EPS_GHIEP is not provided
+    lib.EPSSetWhichEigenpairs.argtypes = [P, ctypes.c_int]
+    assert lib.EPSSetWhichEigenpairs(eps.handle, 9) == PETSC_ERR_SUP   # EPS_TARGET_IMAGINARY
+    assert lib.EPSSetWhichEigenpairs(eps.handle, 10) == PETSC_ERR_SUP  # EPS_ALL
+    lib.EPSSetConvergenceTest.argtypes = [P, ctypes.c_int]
+    assert lib.EPSSetConvergenceTest(eps.handle, 3) == PETSC_ERR_SUP   # EPS_CONV_USER
+    assert lib.EPSSetConvergenceTest(eps.handle, 7) == PETSC_ERR_ARG_OUTOFRANGE
+    lib.EPSKrylovSchurSetRestart.argtypes = [P, ctypes.c_double]
+    assert lib.EPSKrylovSchurSetRestart(eps.handle, 0.95) == PETSC_ERR_ARG_OUTOFRANGE  # keep in [0.1, 0.9]
+    lib.EPSSetExtraction.argtypes = [P, ctypes.c_int]
+    assert lib.EPSSetExtraction(eps.handle, 5) == PETSC_ERR_SUP        # EPS_REFINED
+    lib.EPSSetOptionsPrefix.argtypes = [P, ctypes.c_char_p]
+    assert lib.EPSSetOptionsPrefix(eps.handle, b"-bad_") == PETSC_ERR_ARG_WRONG
+    eps.setConvergenceTest("norm")
+    assert eps.getConvergenceTest() == 2
+    eps.destroy()
+
+
+def test_queries_before_solve(lib):
+    """Results before EPSSolve are an ordering error (EPSCheckSolved), as in the reference."""
+    eps = sg.EPS().create()
+    PETSC_ERR_ORDER = 58
+    for f, args in (("EPSGetConverged", [P, P]), ("EPSGetConvergedReason", [P, P])):
+        getattr(lib, f).argtypes = args
+        out = ctypes.c_int()
+        assert getattr(lib, f)(eps.handle, ctypes.byref(out)) == PETSC_ERR_ORDER
+    lib.EPSComputeError.argtypes = [P, ctypes.c_int, ctypes.c_int, P]
+    err = ctypes.c_double()
+    assert lib.EPSComputeError(eps.handle, 0, 1, ctypes.byref(err)) == PETSC_ERR_ORDER
+    eps.destroy()
+
+
+def test_monitor_limit(lib):
+    eps = sg.EPS().create()
+    for _ in range(5):
+        eps.monitorSet(lambda *a: None)
+    with pytest.raises(sg.SlepcError) as e:
+        eps.monitorSet(lambda *a: None)
+    assert e.value.code == PETSC_ERR_ARG_OUTOFRANGE                    # "Too many EPS monitors set"
+    eps.monitorCancel()
+    eps.monitorSet(lambda *a: None)
+    eps.destroy()
