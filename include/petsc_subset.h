@@ -93,6 +93,33 @@ PetscErrorCode MatMult(Mat A, Vec x, Vec y);
 PetscErrorCode MatNorm(Mat A, NormType type, PetscReal *nrm);
 PetscErrorCode MatCreateVecs(Mat A, Vec *right, Vec *left);
 PetscErrorCode MatDestroy(Mat *A);
+/* Assembly (petscmat.h), sequential AIJ: MatCreate + MatSetSizes (+ MatSetFromOptions / MatSetUp / preallocation,
+ * accepted), MatSetValue(s) with INSERT_VALUES or ADD_VALUES (negative indices skipped, as in PETSc), then
+ * MatAssemblyBegin/End builds the CSR arrays (columns ascending, duplicates combined in call order).  Values may be
+ * set again after assembly (new nonzeros included) and take effect at the next MatAssemblyEnd.  A matrix made by
+ * MatCreateSeqAIJWithArrays becomes library-owned when modified (the caller's arrays are left as they were). */
+typedef enum { NOT_SET_VALUES, INSERT_VALUES, ADD_VALUES, MAX_VALUES, MIN_VALUES } InsertMode;
+typedef enum { MAT_FINAL_ASSEMBLY = 0, MAT_FLUSH_ASSEMBLY = 1 } MatAssemblyType;
+typedef enum { MAT_SYMMETRIC, MAT_HERMITIAN, MAT_STRUCTURALLY_SYMMETRIC, MAT_SPD, MAT_NEW_NONZERO_LOCATIONS,
+               MAT_NEW_NONZERO_ALLOCATION_ERR, MAT_IGNORE_ZERO_ENTRIES, MAT_KEEP_NONZERO_PATTERN,
+               MAT_SYMMETRY_ETERNAL } MatOption;
+#define MATAIJ "aij"
+#define MATSEQAIJ "seqaij"
+PetscErrorCode MatSetSizes(Mat A, PetscInt m, PetscInt n, PetscInt M, PetscInt N);
+PetscErrorCode MatSetUp(Mat A);
+PetscErrorCode MatSeqAIJSetPreallocation(Mat A, PetscInt nz, const PetscInt nnz[]);
+PetscErrorCode MatGetOwnershipRange(Mat A, PetscInt *rstart, PetscInt *rend);
+PetscErrorCode MatGetLocalSize(Mat A, PetscInt *m, PetscInt *n);
+PetscErrorCode MatSetValue(Mat A, PetscInt i, PetscInt j, PetscScalar v, InsertMode mode);
+PetscErrorCode MatSetValues(Mat A, PetscInt m, const PetscInt idxm[], PetscInt n, const PetscInt idxn[],
+                            const PetscScalar v[], InsertMode mode);
+PetscErrorCode MatAssemblyBegin(Mat A, MatAssemblyType type);
+PetscErrorCode MatAssemblyEnd(Mat A, MatAssemblyType type);
+PetscErrorCode MatAssembled(Mat A, PetscBool *assembled);
+PetscErrorCode MatSetOption(Mat A, MatOption op, PetscBool flg);
+PetscErrorCode MatZeroEntries(Mat A);
+PetscErrorCode MatScale(Mat A, PetscScalar a);
+PetscErrorCode MatShift(Mat A, PetscScalar a);
 /* CSR arrays of an AIJ matrix, read-only (shift must be 0; the arrays stay valid until the Mat is destroyed). */
 PetscErrorCode MatGetRowIJ(Mat A, PetscInt shift, PetscBool symmetric, PetscBool inodecompressed, PetscInt *n,
                            const PetscInt *ia[], const PetscInt *ja[], PetscBool *done);
@@ -147,6 +174,20 @@ PetscErrorCode PetscObjectSetName(PetscObject obj, const char name[]);
 PetscErrorCode PetscObjectGetName(PetscObject obj, const char *name[]);
 
 /* --- Vec (petscvec.h) --- */
+PetscErrorCode VecCreate(MPI_Comm comm, Vec *v);
+PetscErrorCode VecSetSizes(Vec v, PetscInt n, PetscInt N);
+PetscErrorCode VecSetFromOptions(Vec v);
+PetscErrorCode VecSetValue(Vec v, PetscInt i, PetscScalar y, InsertMode mode);
+PetscErrorCode VecSetValues(Vec v, PetscInt ni, const PetscInt ix[], const PetscScalar y[], InsertMode mode);
+PetscErrorCode VecAssemblyBegin(Vec v);
+PetscErrorCode VecAssemblyEnd(Vec v);
+PetscErrorCode VecZeroEntries(Vec v);
+PetscErrorCode VecDuplicateVecs(Vec v, PetscInt m, Vec *V[]);
+PetscErrorCode VecDestroyVecs(PetscInt m, Vec *V[]);
+PetscErrorCode VecPlaceArray(Vec v, const PetscScalar array[]);
+PetscErrorCode VecResetArray(Vec v);
+PetscErrorCode VecConjugate(Vec v);
+PetscErrorCode VecGetOwnershipRange(Vec v, PetscInt *low, PetscInt *high);
 PetscErrorCode VecCreateSeq(MPI_Comm comm, PetscInt n, Vec *v);
 PetscErrorCode VecCreateSeqWithArray(MPI_Comm comm, PetscInt bs, PetscInt n, const PetscScalar array[], Vec *v);
 PetscErrorCode VecDuplicate(Vec v, Vec *newv);

@@ -624,10 +624,10 @@ extern "C" PetscErrorCode EPSGetType(EPS eps, EPSType *type) {
 // EPSSetOperators (epssetup.c:440-500): A, and B for a generalised problem (sizes checked as there)
 extern "C" PetscErrorCode EPSSetOperators(EPS eps, Mat A, Mat B) {
   KSG_CHECK(eps && A, PETSC_ERR_ARG_NULL, "Null argument");
-  KSG_CHECK(!A->empty, PETSC_ERR_ARG_WRONGSTATE, "The Mat holds no data (MatCreate without MatLoad)");
+  KSG_CHECK(!A->empty, PETSC_ERR_ARG_WRONGSTATE, "Not for unassembled matrix (A)");
   KSG_CHECK(A->m == A->n, PETSC_ERR_ARG_WRONG, "A does not have equal row and column sizes (%d, %d)", A->m, A->n);
   if (B) {
-    KSG_CHECK(!B->empty, PETSC_ERR_ARG_WRONGSTATE, "The Mat B holds no data (MatCreate without MatLoad)");
+    KSG_CHECK(!B->empty, PETSC_ERR_ARG_WRONGSTATE, "Not for unassembled matrix (B)");
     KSG_CHECK(B->m == B->n, PETSC_ERR_ARG_WRONG, "B is a non-square matrix (%d rows, %d cols)", B->m, B->n);
     KSG_CHECK(A->m == B->m, PETSC_ERR_ARG_INCOMP, "Dimensions of A and B do not match (%d, %d)", A->m, B->m);
     B->refs++;
@@ -1070,7 +1070,11 @@ static PetscErrorCode eps_setup_operator(EPS eps) {
 // EPSSetUp (epssetup.c:286-418 with EPSSetUp_KrylovSchur, krylovschur.c:93-194)
 extern "C" PetscErrorCode EPSSetUp(EPS eps) {
   KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
-  if (eps->setup) return 0;
+  if (eps->setup) {
+    // set up again when an operator's values changed since (the object-state check of STSetUp)
+    if (eps->A->state == eps->a_state && (!eps->B || eps->B->state == eps->b_state)) return 0;
+    eps->setup = 0;
+  }
   auto t0 = std::chrono::steady_clock::now();
   KSG_CHECK(eps->A, PETSC_ERR_ORDER, "EPSSetOperators must be called first");
   // the problem type against the number of matrices (epssetup.c:321-329)
@@ -1160,6 +1164,8 @@ extern "C" PetscErrorCode EPSSetUp(EPS eps) {
     eps->nrmb = eps->B ? ksg_mat_norm_inf(eps->B) : 0.0;
   }
   KSG_CUDA(cudaStreamSynchronize(eps->stream));
+  eps->a_state = eps->A->state;
+  eps->b_state = eps->B ? eps->B->state : -1;
   eps->setup = 1;
   eps->stats.setup_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   return 0;

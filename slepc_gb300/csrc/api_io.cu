@@ -192,6 +192,7 @@ extern "C" PetscErrorCode MatLoad(Mat A, PetscViewer v) {
   A->aa = A->own_a.data();
   A->nnz = nz;
   A->empty = 0;
+  A->state++;
   return 0;
 }
 

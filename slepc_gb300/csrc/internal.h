@@ -57,10 +57,19 @@ struct DBuf {
   ~DBuf() { release(); }
 };
 
+// one MatSetValue(s) entry waiting for MatAssemblyEnd
+struct MatEntry {
+  int row, col;
+  double v;
+  int add;  // ADD_VALUES (else INSERT_VALUES)
+};
+
 struct _p_Mat {
   int m = 0, n = 0;
   int dense = 0;
-  int empty = 0;  // created by MatCreate, not yet filled by MatLoad
+  int empty = 0;  // created by MatCreate, not yet filled (MatLoad, or MatSetSizes + MatSetValues + assembly)
+  int sized = 0;  // MatSetSizes given
+  std::vector<MatEntry> pending;  // MatSetValue(s) since the last assembly
   // AIJ (caller-owned arrays, or the own_* arrays of a loaded matrix)
   const PetscInt *ai = nullptr, *aj = nullptr;
   const PetscScalar *aa = nullptr;
@@ -82,6 +91,7 @@ struct _p_Mat {
   int n_long = 0, n_seg = 0;
   int device_ready = 0;
   double norm_inf = -1.0;
+  long long state = 0;  // bumped when the values change (assembly, MatLoad, MatScale, ...)
 };
 
 struct _p_PetscViewer {
@@ -97,7 +107,9 @@ struct _p_Vec {
   int n = 0;
   std::vector<double> own;
   double *a = nullptr;
+  double *placed_from = nullptr;  // VecPlaceArray: the array to return to at VecResetArray
 };
+
 
 // device helpers used by more than one object
 PetscErrorCode ksg_mat_upload(Mat A);
@@ -161,6 +173,7 @@ struct _p_EPS {
   std::vector<double> bdiag;       // the diagonal of B (generalised problems)
   DBuf<double> d_bdiag, d_bisqrt;  // device copies of diag(B) and diag(B)^-1/2
   double nrma = 0.0, nrmb = 0.0;   // infinity norms for EPS_CONV_NORM (nrmb stays 0 for standard problems)
+  long long a_state = -1, b_state = -1;  // the matrices' states at EPSSetUp
   int lanes = 8;
   long long ldv = 0;
   cudaStream_t stream = nullptr;
