@@ -13,6 +13,11 @@
 #ifndef SLEPC_GB300_PETSC_SUBSET_H
 #define SLEPC_GB300_PETSC_SUBSET_H
 
+#include <float.h>
+#include <math.h>
+#include <stddef.h>
+#include <stdio.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -70,6 +75,94 @@ typedef struct _p_PetscViewer *PetscViewer;
 typedef enum { FILE_MODE_UNDEFINED = -1, FILE_MODE_READ = 0, FILE_MODE_WRITE, FILE_MODE_APPEND } PetscFileMode;
 #define MAT_FILE_CLASSID 1211216
 #define VEC_FILE_CLASSID 1211214
+
+/* --- the basics programs written against PETSc use (petscsys.h, petscmath.h, petscerror.h) --- */
+#define PetscInt_FMT "d"
+#define PETSC_MACHINE_EPSILON DBL_EPSILON
+#define PETSC_SMALL 1.e-10
+#define PETSC_MAX_REAL DBL_MAX
+#define PETSC_MIN_REAL (-DBL_MAX)
+#define PETSC_PI 3.14159265358979323846
+#define PetscMax(a, b) (((a) < (b)) ? (b) : (a))
+#define PetscMin(a, b) (((a) < (b)) ? (a) : (b))
+#define PetscAbs(a) (((a) >= 0) ? (a) : (-(a)))
+#define PetscAbsInt(a) (((a) < 0) ? (-(a)) : (a))
+#define PetscAbsReal(a) fabs(a)
+#define PetscAbsScalar(a) fabs(a)
+#define PetscRealPart(a) (a)
+#define PetscImaginaryPart(a) ((PetscReal)0.0)
+#define PetscConj(a) (a)
+#define PetscSqrtReal(a) sqrt(a)
+#define PetscSqrtScalar(a) sqrt(a)
+#define PetscLogReal(a) log(a)
+#define PetscLogScalar(a) log(a)
+#define PetscExpReal(a) exp(a)
+#define PetscCosReal(a) cos(a)
+#define PetscSinReal(a) sin(a)
+#define PetscPowReal(a, b) pow(a, b)
+#define PetscSqr(a) ((a) * (a))
+/* error handling: a failing call prints where it failed and returns its code from the caller */
+void PetscGB300ReportError(PetscErrorCode ierr, const char *call, const char *file, int line);
+#define PetscCall(...)                                                                \
+  do {                                                                                \
+    PetscErrorCode ierr_petsc_call_ = (__VA_ARGS__);                                  \
+    if (ierr_petsc_call_) {                                                           \
+      PetscGB300ReportError(ierr_petsc_call_, #__VA_ARGS__, __FILE__, __LINE__);      \
+      return ierr_petsc_call_;                                                        \
+    }                                                                                 \
+  } while (0)
+#define PetscCheck(cond, comm, ierr, ...)                                             \
+  do {                                                                                \
+    if (!(cond)) {                                                                    \
+      fprintf(stderr, __VA_ARGS__);                                                   \
+      fprintf(stderr, "\n");                                                          \
+      return ierr;                                                                    \
+    }                                                                                 \
+  } while (0)
+#define SETERRQ(comm, ierr, ...)                                                      \
+  do {                                                                                \
+    fprintf(stderr, __VA_ARGS__);                                                     \
+    fprintf(stderr, "\n");                                                            \
+    return ierr;                                                                      \
+  } while (0)
+#define PetscFunctionBegin
+#define PetscFunctionBeginUser
+#define PetscFunctionReturn(x) return (x)
+#define PETSC_MAX_PATH_LEN 4096
+PetscErrorCode PetscStrcmp(const char a[], const char b[], PetscBool *flg);
+/* MPI on one process: rank 0 of 1 */
+#define MPI_SUCCESS 0
+int MPI_Comm_rank(MPI_Comm comm, int *rank);
+int MPI_Comm_size(MPI_Comm comm, int *size);
+#define PetscCallMPI(...) PetscCall(__VA_ARGS__)
+/* random numbers (PetscRandom): uniform in [0, 1) from a counter-based splitmix64 stream; PETSc's default generator
+ * is another one, so the values differ from PETSc's for the same seed */
+typedef struct _p_PetscRandom *PetscRandom;
+PetscErrorCode PetscRandomCreate(MPI_Comm comm, PetscRandom *r);
+PetscErrorCode PetscRandomSetFromOptions(PetscRandom r);
+PetscErrorCode PetscRandomSetSeed(PetscRandom r, unsigned long seed);
+PetscErrorCode PetscRandomSeed(PetscRandom r);
+PetscErrorCode PetscRandomGetValue(PetscRandom r, PetscScalar *value);
+PetscErrorCode PetscRandomDestroy(PetscRandom *r);
+/* type of an object (EPS: "krylovschur", ST: "shift", Mat: "seqaij" or "seqdense") against one name, or against a
+ * list of names ended by "" */
+PetscErrorCode PetscObjectTypeCompare(void *obj, const char type[], PetscBool *same);
+PetscErrorCode PetscObjectTypeCompareAny(void *obj, PetscBool *match, const char type[], ...);
+/* output on the first (only) process */
+PetscErrorCode PetscPrintf(MPI_Comm comm, const char format[], ...);
+/* the options database is the argument list given to SlepcInitialize/PetscInitialize (PetscOptions: NULL) */
+typedef void *PetscOptions;
+PetscErrorCode PetscOptionsHasName(PetscOptions options, const char pre[], const char name[], PetscBool *set);
+PetscErrorCode PetscOptionsGetInt(PetscOptions options, const char pre[], const char name[], PetscInt *ivalue,
+                                  PetscBool *set);
+PetscErrorCode PetscOptionsGetReal(PetscOptions options, const char pre[], const char name[], PetscReal *dvalue,
+                                   PetscBool *set);
+PetscErrorCode PetscOptionsGetScalar(PetscOptions options, const char pre[], const char name[], PetscScalar *dvalue,
+                                     PetscBool *set);
+PetscErrorCode PetscOptionsGetBool(PetscOptions options, const char pre[], const char name[], PetscBool *ivalue,
+                                   PetscBool *set);
+PetscErrorCode PetscOptionsGetString(PetscOptions options, const char pre[], const char name[], char string[],
+                                     size_t len, PetscBool *set);
 
 /* SlepcInitialize/PetscInitialize: a no-op shim (selects the current CUDA device lazily). */
 PetscErrorCode PetscInitialize(int *argc, char ***argv, const char file[], const char help[]);
@@ -188,6 +281,11 @@ PetscErrorCode VecPlaceArray(Vec v, const PetscScalar array[]);
 PetscErrorCode VecResetArray(Vec v);
 PetscErrorCode VecConjugate(Vec v);
 PetscErrorCode VecGetOwnershipRange(Vec v, PetscInt *low, PetscInt *high);
+PetscErrorCode VecSetRandom(Vec v, PetscRandom r);
+/* SLEPc's VecCheckOrthonormality (src/sys/vec/vecutil.c): lev = max |Y_j^T B X_i - delta_ij| over the nx x ny Gram
+ * matrix (Y = X when y is NULL, B = I when NULL); the viewer is not used */
+PetscErrorCode VecCheckOrthonormality(Vec x[], PetscInt nx, Vec y[], PetscInt ny, Mat B, PetscViewer viewer,
+                                      PetscReal *lev);
 PetscErrorCode VecCreateSeq(MPI_Comm comm, PetscInt n, Vec *v);
 PetscErrorCode VecCreateSeqWithArray(MPI_Comm comm, PetscInt bs, PetscInt n, const PetscScalar array[], Vec *v);
 PetscErrorCode VecDuplicate(Vec v, Vec *newv);

@@ -23,6 +23,26 @@ extern "C" {
 typedef struct _p_EPS *EPS;
 typedef const char *EPSType;
 #define EPSKRYLOVSCHUR "krylovschur"
+/* the other solver types' names (slepceps.h:31-56), so that programs which compare or select types compile;
+ * EPSSetType accepts EPSKRYLOVSCHUR only */
+#define EPSPOWER "power"
+#define EPSSUBSPACE "subspace"
+#define EPSARNOLDI "arnoldi"
+#define EPSLANCZOS "lanczos"
+#define EPSGD "gd"
+#define EPSJD "jd"
+#define EPSRQCG "rqcg"
+#define EPSLOBPCG "lobpcg"
+#define EPSCISS "ciss"
+#define EPSLYAPII "lyapii"
+#define EPSLAPACK "lapack"
+#define EPSARPACK "arpack"
+typedef enum { EPS_POWER_SHIFT_CONSTANT, EPS_POWER_SHIFT_RAYLEIGH, EPS_POWER_SHIFT_WILKINSON } EPSPowerShiftType;
+extern const char *EPSPowerShiftTypes[];
+typedef enum { EPS_LANCZOS_REORTHOG_LOCAL, EPS_LANCZOS_REORTHOG_FULL, EPS_LANCZOS_REORTHOG_SELECTIVE,
+               EPS_LANCZOS_REORTHOG_PERIODIC, EPS_LANCZOS_REORTHOG_PARTIAL,
+               EPS_LANCZOS_REORTHOG_DELAYED } EPSLanczosReorthogType;
+extern const char *EPSLanczosReorthogTypes[];
 
 typedef enum { EPS_HEP = 1, EPS_GHEP, EPS_NHEP, EPS_GNHEP, EPS_PGNHEP, EPS_GHIEP, EPS_BSE } EPSProblemType;
 typedef enum { EPS_RITZ, EPS_HARMONIC, EPS_HARMONIC_RELATIVE, EPS_HARMONIC_RIGHT, EPS_HARMONIC_LARGEST,
@@ -122,6 +142,16 @@ PetscErrorCode EPSMonitorConvergedCreate(PetscViewer viewer, PetscViewerFormat f
 PetscErrorCode EPSMonitorConvergedDestroy(PetscViewerAndFormat **vf);
 PetscErrorCode EPSGetBV(EPS eps, BV *V);
 PetscErrorCode EPSGetST(EPS eps, ST *st); /* the shift-0 transformation (slepcst.h) */
+/* options of other solver types, as SLEPc dispatches them on a Krylov-Schur EPS: the setters do nothing
+ * (PetscTryMethod), the getters return PETSC_ERR_SUP (PetscUseMethod) */
+PetscErrorCode EPSPowerSetShiftType(EPS eps, EPSPowerShiftType shift);
+PetscErrorCode EPSPowerGetShiftType(EPS eps, EPSPowerShiftType *shift);
+PetscErrorCode EPSLanczosSetReorthog(EPS eps, EPSLanczosReorthogType reorthog);
+PetscErrorCode EPSLanczosGetReorthog(EPS eps, EPSLanczosReorthogType *reorthog);
+PetscErrorCode EPSGDSetDoubleExpansion(EPS eps, PetscBool doubleexp);
+PetscErrorCode EPSGDGetDoubleExpansion(EPS eps, PetscBool *doubleexp);
+/* a deflation space (epsdefl.c) is not provided: an empty one is accepted */
+PetscErrorCode EPSSetDeflationSpace(EPS eps, PetscInt n, Vec v[]);
 /* problem properties after EPSSetProblemType (epsbasic.c:1000-1080) */
 PetscErrorCode EPSIsHermitian(EPS eps, PetscBool *is);
 PetscErrorCode EPSIsGeneralized(EPS eps, PetscBool *is);

@@ -30,6 +30,10 @@ PetscErrorCode STSetShift(ST st, PetscScalar shift);
 PetscErrorCode STGetShift(ST st, PetscScalar *shift);
 PetscErrorCode STGetNumMatrices(ST st, PetscInt *n);
 PetscErrorCode STView(ST st, PetscViewer viewer);
+/* the linear solver of the transformation: the shift of 0 has none to run, so its iteration count is 0 */
+typedef struct _p_KSP *KSP;
+PetscErrorCode STGetKSP(ST st, KSP *ksp);
+PetscErrorCode KSPGetTotalIterations(KSP ksp, PetscInt *its);
 
 #ifdef __cplusplus
 }

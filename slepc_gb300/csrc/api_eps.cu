@@ -12,7 +12,11 @@
 #include <string.h>
 
 #include <algorithm>
+#include <cctype>
 #include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
 
 #include "internal.h"
 
@@ -46,6 +50,124 @@ extern "C" PetscErrorCode SlepcInitialize(int *argc, char ***argv, const char[],
   return 0;
 }
 extern "C" PetscErrorCode SlepcFinalize(void) { return 0; }
+
+// ---------------------------------------------------------------------------------------------------------------
+// PETSc basics: PetscPrintf, the PetscCall error report, and the options database read from the argument list of
+// SlepcInitialize (PetscOptionsGet*, petsc/src/sys/objects/options.c semantics: the last occurrence wins; an option
+// name carries its dash, the prefix does not)
+// ---------------------------------------------------------------------------------------------------------------
+extern "C" void PetscGB300ReportError(PetscErrorCode ierr, const char *call, const char *file, int line) {
+  std::fprintf(stderr, "[0]PETSC ERROR: %s returned %d at %s:%d\n[0]PETSC ERROR: %s\n", call, ierr, file, line,
+               PetscGB300LastError());
+}
+
+extern "C" PetscErrorCode PetscPrintf(MPI_Comm, const char format[], ...) {
+  KSG_CHECK(format, PETSC_ERR_ARG_NULL, "Null format");
+  va_list ap;
+  va_start(ap, format);
+  std::vfprintf(stdout, format, ap);
+  va_end(ap);
+  std::fflush(stdout);
+  return 0;
+}
+
+// the value of option -<pre><name without its dash>: nullptr if absent; *val the following argument, if it is one
+static const char *opt_find(const char *pre, const char *name, const char **val) {
+  *val = nullptr;
+  if (!name || name[0] != '-') return nullptr;
+  std::string key = std::string("-") + (pre ? pre : "") + (name + 1);
+  const char *found = nullptr;
+  for (int i = 1; i < g_argc; ++i) {
+    if (!g_argv[i] || key != g_argv[i]) continue;
+    found = g_argv[i];
+    *val = nullptr;
+    if (i + 1 < g_argc && g_argv[i + 1]) {
+      const char *nx = g_argv[i + 1];
+      const bool number = nx[0] == '-' && (std::isdigit((unsigned char)nx[1]) || nx[1] == '.');
+      if (nx[0] != '-' || number) *val = nx;
+    }
+  }
+  return found;
+}
+
+extern "C" PetscErrorCode PetscOptionsHasName(PetscOptions, const char pre[], const char name[], PetscBool *set) {
+  KSG_CHECK(name && set, PETSC_ERR_ARG_NULL, "Null argument");
+  const char *v;
+  *set = opt_find(pre, name, &v) ? PETSC_TRUE : PETSC_FALSE;
+  return 0;
+}
+
+extern "C" PetscErrorCode PetscOptionsGetInt(PetscOptions, const char pre[], const char name[], PetscInt *ivalue,
+                                             PetscBool *set) {
+  KSG_CHECK(name && ivalue, PETSC_ERR_ARG_NULL, "Null argument");
+  const char *v;
+  const char *f = opt_find(pre, name, &v);
+  if (set) *set = PETSC_FALSE;
+  if (!f) return 0;
+  KSG_CHECK(v, PETSC_ERR_ARG_WRONG, "Missing value for option %s", f);
+  char *end = nullptr;
+  const long x = std::strtol(v, &end, 10);
+  KSG_CHECK(end && *end == 0, PETSC_ERR_ARG_WRONG, "Input string %s has no integer value", v);
+  *ivalue = (PetscInt)x;
+  if (set) *set = PETSC_TRUE;
+  return 0;
+}
+
+extern "C" PetscErrorCode PetscOptionsGetReal(PetscOptions, const char pre[], const char name[], PetscReal *dvalue,
+                                              PetscBool *set) {
+  KSG_CHECK(name && dvalue, PETSC_ERR_ARG_NULL, "Null argument");
+  const char *v;
+  const char *f = opt_find(pre, name, &v);
+  if (set) *set = PETSC_FALSE;
+  if (!f) return 0;
+  KSG_CHECK(v, PETSC_ERR_ARG_WRONG, "Missing value for option %s", f);
+  char *end = nullptr;
+  const double x = std::strtod(v, &end);
+  KSG_CHECK(end && *end == 0, PETSC_ERR_ARG_WRONG, "Input string %s has no numeric value", v);
+  *dvalue = x;
+  if (set) *set = PETSC_TRUE;
+  return 0;
+}
+
+extern "C" PetscErrorCode PetscOptionsGetScalar(PetscOptions o, const char pre[], const char name[],
+                                                PetscScalar *dvalue, PetscBool *set) {
+  return PetscOptionsGetReal(o, pre, name, dvalue, set);
+}
+
+extern "C" PetscErrorCode PetscOptionsGetBool(PetscOptions, const char pre[], const char name[], PetscBool *ivalue,
+                                              PetscBool *set) {
+  KSG_CHECK(name, PETSC_ERR_ARG_NULL, "Null argument");
+  const char *v;
+  const char *f = opt_find(pre, name, &v);
+  if (set) *set = PETSC_FALSE;
+  if (!f) return 0;
+  PetscBool b = PETSC_TRUE;  // the bare option means true
+  if (v) {
+    std::string t(v);
+    for (char &c : t) c = (char)std::tolower((unsigned char)c);
+    if (t == "0" || t == "false" || t == "no" || t == "off") b = PETSC_FALSE;
+    else KSG_CHECK(t == "1" || t == "true" || t == "yes" || t == "on", PETSC_ERR_ARG_WRONG,
+                   "Unknown logical value: %s", v);
+  }
+  if (ivalue) *ivalue = b;
+  if (set) *set = PETSC_TRUE;
+  return 0;
+}
+
+extern "C" PetscErrorCode PetscOptionsGetString(PetscOptions, const char pre[], const char name[], char string[],
+                                                size_t len, PetscBool *set) {
+  KSG_CHECK(name && string, PETSC_ERR_ARG_NULL, "Null argument");
+  const char *v;
+  const char *f = opt_find(pre, name, &v);
+  if (set) *set = PETSC_FALSE;
+  if (!f) return 0;
+  if (len > 0) {
+    std::strncpy(string, v ? v : "", len - 1);
+    string[len - 1] = 0;
+  }
+  if (set) *set = PETSC_TRUE;
+  return 0;
+}
 
 // ---------------------------------------------------------------------------------------------------------------
 // random vectors: splitmix64 uniform in [-1, 1), counter-based so that any column can be regenerated

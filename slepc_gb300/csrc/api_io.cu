@@ -829,3 +829,83 @@ extern "C" PetscErrorCode STView(ST st, PetscViewer v) {
   t.add("  number of matrices: %d\n", st->eps->B ? 2 : 1);
   return emit(v, t);
 }
+
+// ---------------------------------------------------------------------------------------------------------------
+// type queries and the options of other solver types (PetscTryMethod setters do nothing, PetscUseMethod getters fail)
+// ---------------------------------------------------------------------------------------------------------------
+const char *EPSPowerShiftTypes[] = {"CONSTANT", "RAYLEIGH", "WILKINSON", "EPSPowerShiftType", "EPS_POWER_SHIFT_",
+                                    nullptr};
+const char *EPSLanczosReorthogTypes[] = {"LOCAL", "FULL", "SELECTIVE", "PERIODIC", "PARTIAL", "DELAYED",
+                                         "EPSLanczosReorthogType", "EPS_LANCZOS_REORTHOG_", nullptr};
+
+namespace {
+// the type name of an object of this library, by the cookie its struct begins with
+const char *object_type(void *obj) {
+  const unsigned c = *static_cast<const unsigned *>(obj);
+  if (c == KSG_EPS_COOKIE) return static_cast<EPS>(obj)->type.c_str();
+  if (c == KSG_ST_COOKIE) return STSHIFT;
+  if (c == KSG_MAT_COOKIE) return static_cast<Mat>(obj)->dense ? "seqdense" : "seqaij";
+  return "";
+}
+}  // namespace
+
+extern "C" PetscErrorCode PetscObjectTypeCompare(void *obj, const char type[], PetscBool *same) {
+  KSG_CHECK(same, PETSC_ERR_ARG_NULL, "Null argument");
+  *same = (obj && type && !std::strcmp(object_type(obj), type)) ? PETSC_TRUE : PETSC_FALSE;
+  return 0;
+}
+
+extern "C" PetscErrorCode PetscObjectTypeCompareAny(void *obj, PetscBool *match, const char type[], ...) {
+  KSG_CHECK(match, PETSC_ERR_ARG_NULL, "Null argument");
+  *match = PETSC_FALSE;
+  va_list ap;
+  va_start(ap, type);
+  for (const char *t = type; t && t[0]; t = va_arg(ap, const char *))
+    if (obj && !std::strcmp(object_type(obj), t)) *match = PETSC_TRUE;
+  va_end(ap);
+  return 0;
+}
+
+extern "C" PetscErrorCode EPSPowerSetShiftType(EPS eps, EPSPowerShiftType) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  return 0;
+}
+extern "C" PetscErrorCode EPSPowerGetShiftType(EPS eps, EPSPowerShiftType *) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  return ksg_set_error(PETSC_ERR_SUP, "EPSPowerGetShiftType: the EPS type is krylovschur, not power");
+}
+extern "C" PetscErrorCode EPSLanczosSetReorthog(EPS eps, EPSLanczosReorthogType) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  return 0;
+}
+extern "C" PetscErrorCode EPSLanczosGetReorthog(EPS eps, EPSLanczosReorthogType *) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  return ksg_set_error(PETSC_ERR_SUP, "EPSLanczosGetReorthog: the EPS type is krylovschur, not lanczos");
+}
+extern "C" PetscErrorCode EPSGDSetDoubleExpansion(EPS eps, PetscBool) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  return 0;
+}
+extern "C" PetscErrorCode EPSGDGetDoubleExpansion(EPS eps, PetscBool *) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  return ksg_set_error(PETSC_ERR_SUP, "EPSGDGetDoubleExpansion: the EPS type is krylovschur, not gd");
+}
+
+extern "C" PetscErrorCode EPSSetDeflationSpace(EPS eps, PetscInt n, Vec[]) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  KSG_CHECK(n >= 0, PETSC_ERR_ARG_OUTOFRANGE, "Argument n cannot be negative");
+  KSG_CHECK(n == 0, PETSC_ERR_SUP, "A deflation space is not provided");
+  return 0;
+}
+
+// the shift of 0 runs no linear solver: its KSP handle is the ST's, and its iteration count 0
+extern "C" PetscErrorCode STGetKSP(ST st, KSP *ksp) {
+  KSG_CHECK(st && ksp, PETSC_ERR_ARG_NULL, "Null argument");
+  *ksp = reinterpret_cast<KSP>(st);
+  return 0;
+}
+extern "C" PetscErrorCode KSPGetTotalIterations(KSP ksp, PetscInt *its) {
+  KSG_CHECK(ksp && its, PETSC_ERR_ARG_NULL, "Null argument");
+  *its = 0;
+  return 0;
+}

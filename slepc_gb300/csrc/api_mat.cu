@@ -343,3 +343,115 @@ extern "C" PetscErrorCode VecGetOwnershipRange(Vec v, PetscInt *low, PetscInt *h
   if (high) *high = v->n;
   return 0;
 }
+
+// ---------------------------------------------------------------------------------------------------------------
+// small PETSc utilities the examples use: string compare, MPI on one process, random numbers, orthonormality check
+// ---------------------------------------------------------------------------------------------------------------
+extern "C" PetscErrorCode PetscStrcmp(const char a[], const char b[], PetscBool *flg) {
+  KSG_CHECK(flg, PETSC_ERR_ARG_NULL, "Null argument");
+  *flg = ((!a && !b) || (a && b && !std::strcmp(a, b))) ? PETSC_TRUE : PETSC_FALSE;
+  return 0;
+}
+
+extern "C" int MPI_Comm_rank(MPI_Comm, int *rank) {
+  if (rank) *rank = 0;
+  return 0;
+}
+
+extern "C" int MPI_Comm_size(MPI_Comm, int *size) {
+  if (size) *size = 1;
+  return 0;
+}
+
+struct _p_PetscRandom {
+  unsigned long long seed = 0x5EEDULL;
+  unsigned long long counter = 0;
+};
+
+extern "C" PetscErrorCode PetscRandomCreate(MPI_Comm, PetscRandom *r) {
+  KSG_CHECK(r, PETSC_ERR_ARG_NULL, "Null argument");
+  *r = new _p_PetscRandom();
+  return 0;
+}
+
+extern "C" PetscErrorCode PetscRandomSetFromOptions(PetscRandom r) {
+  KSG_CHECK(r, PETSC_ERR_ARG_NULL, "Null PetscRandom");
+  return 0;
+}
+
+extern "C" PetscErrorCode PetscRandomSetSeed(PetscRandom r, unsigned long seed) {
+  KSG_CHECK(r, PETSC_ERR_ARG_NULL, "Null PetscRandom");
+  r->seed = seed;
+  return 0;
+}
+
+extern "C" PetscErrorCode PetscRandomSeed(PetscRandom r) {
+  KSG_CHECK(r, PETSC_ERR_ARG_NULL, "Null PetscRandom");
+  r->counter = 0;  // restart the stream of the current seed
+  return 0;
+}
+
+// the next value of the stream, uniform in [0, 1) (splitmix64, the top 53 bits)
+static double random_next(PetscRandom r) {
+  unsigned long long z = r->seed + (++r->counter) * 0x9E3779B97F4A7C15ULL;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  z ^= z >> 31;
+  return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+}
+
+extern "C" PetscErrorCode PetscRandomGetValue(PetscRandom r, PetscScalar *value) {
+  KSG_CHECK(r && value, PETSC_ERR_ARG_NULL, "Null argument");
+  *value = random_next(r);
+  return 0;
+}
+
+extern "C" PetscErrorCode PetscRandomDestroy(PetscRandom *r) {
+  if (!r || !*r) return 0;
+  delete *r;
+  *r = nullptr;
+  return 0;
+}
+
+extern "C" PetscErrorCode VecSetRandom(Vec v, PetscRandom r) {
+  KSG_CHECK(v, PETSC_ERR_ARG_NULL, "Null Vec");
+  _p_PetscRandom local;
+  PetscRandom rr = r ? r : &local;
+  for (int i = 0; i < v->n; ++i) v->a[i] = random_next(rr);
+  return 0;
+}
+
+// VecCheckOrthonormality (src/sys/vec/vecutil.c): the largest entry of |Y^T B X - I| (host arithmetic)
+extern "C" PetscErrorCode VecCheckOrthonormality(Vec x[], PetscInt nx, Vec y[], PetscInt ny, Mat B, PetscViewer,
+                                                 PetscReal *lev) {
+  KSG_CHECK(x && lev, PETSC_ERR_ARG_NULL, "Null argument");
+  if (!y) {
+    y = x;
+    ny = nx;
+  }
+  const int n = nx > 0 ? x[0]->n : 0;
+  std::vector<double> bx((size_t)n);
+  double worst = 0.0;
+  for (PetscInt i = 0; i < nx; ++i) {
+    KSG_CHECK(x[i] && x[i]->n == n, PETSC_ERR_ARG_SIZ, "Vectors of different sizes");
+    const double *xi = x[i]->a;
+    if (B) {  // b = B x_i
+      KSG_CHECK(!B->empty && !B->dense && B->m == n && B->n == n, PETSC_ERR_ARG_WRONG,
+                "B must be an assembled square AIJ matrix of the vectors' size");
+      for (int r = 0; r < n; ++r) {
+        double s = 0.0;
+        for (PetscInt p = B->ai[r]; p < B->ai[r + 1]; ++p) s += B->aa[p] * xi[B->aj[p]];
+        bx[r] = s;
+      }
+      xi = bx.data();
+    }
+    for (PetscInt j = 0; j < ny; ++j) {
+      KSG_CHECK(y[j] && y[j]->n == n, PETSC_ERR_ARG_SIZ, "Vectors of different sizes");
+      double d = 0.0;
+      for (int r = 0; r < n; ++r) d += y[j]->a[r] * xi[r];
+      worst = std::max(worst, std::fabs(d - (i == j ? 1.0 : 0.0)));
+    }
+  }
+  *lev = worst;
+  return 0;
+}

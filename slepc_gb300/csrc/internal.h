@@ -64,7 +64,11 @@ struct MatEntry {
   int add;  // ADD_VALUES (else INSERT_VALUES)
 };
 
+// the first word of every EPS, ST and Mat (PetscObjectSetName, PetscObjectTypeCompare read it)
+constexpr unsigned KSG_EPS_COOKIE = 0x31535045u, KSG_ST_COOKIE = 0x31315453u, KSG_MAT_COOKIE = 0x3154414Du;
+
 struct _p_Mat {
+  unsigned cookie = KSG_MAT_COOKIE;
   int m = 0, n = 0;
   int dense = 0;
   int empty = 0;  // created by MatCreate, not yet filled (MatLoad, or MatSetSizes + MatSetValues + assembly)
@@ -119,10 +123,11 @@ PetscErrorCode ksg_random_fill(double *host, int n, unsigned long long seed, uns
 struct _p_DS;
 struct _p_BV;
 struct _p_ST {
+  unsigned cookie = KSG_ST_COOKIE;
   EPS eps = nullptr;  // the owner
 };
 
-constexpr unsigned KSG_EPS_COOKIE = 0x31535045u;  // the first word of every EPS (PetscObjectSetName checks it)
+
 
 // a report EPSSolve prints when it ends (options -eps_converged_reason, -eps_error_*, -eps_view_values)
 struct EPSPostView {

@@ -1,0 +1,50 @@
+"""The reference's own EPS programs compile and link unchanged against include/ and libslepc_gb300.so.
+
+Where the reference tree is present (environment variable SLEPC_REFERENCE, default /root/reference), each program is
+compiled in place from its source with gcc -Wall -Werror and linked against the library; nothing is copied.  Run
+without a GPU, a program builds its matrices and options and then stops at EPSSolve with PETSC_ERR_GPU (97) and the
+CUDA error: there is no CPU fallback.  With a GPU it solves."""
+import os
+import shutil
+import subprocess
+
+import pytest
+
+import slepc_gb300 as sg
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REF = os.environ.get("SLEPC_REFERENCE", "/root/reference")
+PROGRAMS = ["tutorials/ex2", "tutorials/ex4", "tutorials/ex5", "tutorials/ex7", "tests/test1", "tests/test2",
+            "tests/test4", "tests/test6", "tests/test19", "tests/test20", "tests/test23"]
+
+pytestmark = pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "src", "eps")) or not shutil.which("gcc"),
+                                reason="the reference's sources or gcc are not available here")
+
+
+@pytest.fixture(scope="module")
+def libdir():
+    sg.build()
+    return os.path.dirname(sg.LIB_PATH)
+
+
+@pytest.mark.parametrize("prog", PROGRAMS)
+def test_program_compiles_and_links(prog, libdir, tmp_path):
+    src = os.path.join(REF, "src", "eps", prog + ".c")
+    exe = tmp_path / os.path.basename(prog)
+    r = subprocess.run(["gcc", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), src, "-o", str(exe),
+                        "-L", libdir, "-lslepc_gb300", "-lm", "-Wl,-rpath," + libdir],
+                       capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr[-2000:]
+
+
+def test_program_runs_to_the_solve(libdir, tmp_path):
+    """ex2 -n 10: the header line, then EPSSolve -- on a machine without a GPU it reports PETSC_ERR_GPU."""
+    exe = tmp_path / "ex2"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), os.path.join(REF, "src/eps/tutorials/ex2.c"), "-o",
+                    str(exe), "-L", libdir, "-lslepc_gb300", "-lm", "-Wl,-rpath," + libdir], check=True, timeout=120)
+    r = subprocess.run([str(exe), "-n", "10", "-eps_nev", "4", "-terse"], capture_output=True, text=True, timeout=600)
+    assert "2-D Laplacian Eigenproblem, N=100 (10x10 grid)" in r.stdout
+    if r.returncode == 97:
+        assert "PETSC ERROR" in r.stderr and "CUDA error" in r.stderr
+    else:
+        assert r.returncode == 0 and "All requested eigenvalues computed up to the required tolerance" in r.stdout
