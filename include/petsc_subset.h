@@ -144,6 +144,12 @@ PetscErrorCode PetscRandomSetSeed(PetscRandom r, unsigned long seed);
 PetscErrorCode PetscRandomSeed(PetscRandom r);
 PetscErrorCode PetscRandomGetValue(PetscRandom r, PetscScalar *value);
 PetscErrorCode PetscRandomDestroy(PetscRandom *r);
+PetscErrorCode PetscRandomSetInterval(PetscRandom r, PetscScalar low, PetscScalar high);
+PetscErrorCode PetscRandomGetValueReal(PetscRandom r, PetscReal *value);
+PetscErrorCode PetscStrendswith(const char a[], const char b[], PetscBool *flg);
+/* one process owns everything: a PETSC_DECIDE size becomes the other one */
+PetscErrorCode PetscSplitOwnership(MPI_Comm comm, PetscInt *n, PetscInt *N);
+#define PETSC_ERR_WRONG_MPI_SIZE 94
 /* type of an object (EPS: "krylovschur", ST: "shift", Mat: "seqaij" or "seqdense") against one name, or against a
  * list of names ended by "" */
 PetscErrorCode PetscObjectTypeCompare(void *obj, const char type[], PetscBool *same);
@@ -213,6 +219,10 @@ PetscErrorCode MatSetOption(Mat A, MatOption op, PetscBool flg);
 PetscErrorCode MatZeroEntries(Mat A);
 PetscErrorCode MatScale(Mat A, PetscScalar a);
 PetscErrorCode MatShift(Mat A, PetscScalar a);
+typedef enum { MAT_DO_NOT_COPY_VALUES, MAT_COPY_VALUES, MAT_SHARE_NONZERO_PATTERN } MatDuplicateOption;
+typedef enum { DIFFERENT_NONZERO_PATTERN, SUBSET_NONZERO_PATTERN, SAME_NONZERO_PATTERN, UNKNOWN_NONZERO_PATTERN } MatStructure;
+PetscErrorCode MatDuplicate(Mat A, MatDuplicateOption op, Mat *B);
+PetscErrorCode MatDiagonalSet(Mat A, Vec D, InsertMode mode);
 /* CSR arrays of an AIJ matrix, read-only (shift must be 0; the arrays stay valid until the Mat is destroyed). */
 PetscErrorCode MatGetRowIJ(Mat A, PetscInt shift, PetscBool symmetric, PetscBool inodecompressed, PetscInt *n,
                            const PetscInt *ia[], const PetscInt *ja[], PetscBool *done);

@@ -43,6 +43,8 @@ PetscErrorCode SlepcCompareSmallestImaginary(PetscScalar, PetscScalar, PetscScal
 /* life cycle and dimensions: src/sys/classes/ds/interface/dsbasic.c, dsops.c:130-165 */
 PetscErrorCode DSCreate(MPI_Comm comm, DS *ds);
 PetscErrorCode DSSetType(DS ds, DSType type);
+PetscErrorCode DSGetType(DS ds, DSType *type);  /* dsbasic.c:275; NULL until a type is set */
+PetscErrorCode DSView(DS ds, PetscViewer viewer); /* type line (dsbasic.c DSView, ASCII) */
 PetscErrorCode DSAllocate(DS ds, PetscInt ld);
 PetscErrorCode DSGetLeadingDimension(DS ds, PetscInt *ld);
 PetscErrorCode DSSetDimensions(DS ds, PetscInt n, PetscInt l, PetscInt k);

@@ -150,6 +150,18 @@ PetscErrorCode EPSLanczosSetReorthog(EPS eps, EPSLanczosReorthogType reorthog);
 PetscErrorCode EPSLanczosGetReorthog(EPS eps, EPSLanczosReorthogType *reorthog);
 PetscErrorCode EPSGDSetDoubleExpansion(EPS eps, PetscBool doubleexp);
 PetscErrorCode EPSGDGetDoubleExpansion(EPS eps, PetscBool *doubleexp);
+/* balancing (epsopts.c:1010-1090) and the stopping test (epsopts.c:780-860): the defaults, EPS_BALANCE_NONE and
+ * EPS_STOP_BASIC, are what this path runs; other values return PETSC_ERR_SUP.  Track-all is stored (the error
+ * estimates of all current values are computed in any case). */
+typedef enum { EPS_BALANCE_NONE, EPS_BALANCE_ONESIDE, EPS_BALANCE_TWOSIDE, EPS_BALANCE_USER } EPSBalance;
+extern const char *EPSBalanceTypes[];
+typedef enum { EPS_STOP_BASIC, EPS_STOP_USER, EPS_STOP_THRESHOLD } EPSStop;
+PetscErrorCode EPSSetBalance(EPS eps, EPSBalance bal, PetscInt its, PetscReal cutoff);
+PetscErrorCode EPSGetBalance(EPS eps, EPSBalance *bal, PetscInt *its, PetscReal *cutoff);
+PetscErrorCode EPSSetStoppingTest(EPS eps, EPSStop stop);
+PetscErrorCode EPSGetStoppingTest(EPS eps, EPSStop *stop);
+PetscErrorCode EPSSetTrackAll(EPS eps, PetscBool trackall);
+PetscErrorCode EPSGetTrackAll(EPS eps, PetscBool *trackall);
 /* a deflation space (epsdefl.c) is not provided: an empty one is accepted */
 PetscErrorCode EPSSetDeflationSpace(EPS eps, PetscInt n, Vec v[]);
 /* problem properties after EPSSetProblemType (epsbasic.c:1000-1080) */

@@ -34,6 +34,7 @@ PetscErrorCode STView(ST st, PetscViewer viewer);
 typedef struct _p_KSP *KSP;
 PetscErrorCode STGetKSP(ST st, KSP *ksp);
 PetscErrorCode KSPGetTotalIterations(KSP ksp, PetscInt *its);
+PetscErrorCode KSPSetTolerances(KSP ksp, PetscReal rtol, PetscReal abstol, PetscReal dtol, PetscInt maxits);
 
 #ifdef __cplusplus
 }

@@ -751,10 +751,28 @@ extern "C" PetscErrorCode EPSGetBV(EPS eps, BV *V) {
 extern "C" PetscErrorCode EPSGetDS(EPS eps, DS *ds) {
   KSG_CHECK(eps && ds, PETSC_ERR_ARG_NULL, "Null argument");
   if (!eps->ds) {
-    KSG_TRY(DSCreate(0, &eps->ds));
-    KSG_TRY(DSSetType(eps->ds, ksg_eps_hermitian(eps) ? DSHEP : DSNHEP));
-    if (eps->setup) KSG_TRY(DSAllocate(eps->ds, eps->ld));
+    KSG_TRY(DSCreate(0, &eps->ds));  // typed by EPSSetFromOptions (DSNHEP) or EPSSetUp, as the reference's
+    if (eps->setup) {
+      KSG_TRY(DSSetType(eps->ds, ksg_eps_lanczos(eps) ? DSHEP : DSNHEP));
+      KSG_TRY(DSAllocate(eps->ds, eps->ld));
+    }
   }
   *ds = eps->ds;
+  return 0;
+}
+
+extern "C" PetscErrorCode DSGetType(DS ds, DSType *type) {
+  KSG_CHECK(ds && type, PETSC_ERR_ARG_NULL, "Null argument");
+  *type = ds->type == 1 ? DSHEP : ds->type == 2 ? DSNHEP : nullptr;
+  return 0;
+}
+
+// DSView, ASCII: "DS Object: 1 MPI process" and the type
+extern "C" PetscErrorCode DSView(DS ds, PetscViewer viewer) {
+  KSG_CHECK(ds, PETSC_ERR_ARG_NULL, "Null DS");
+  if (!viewer) KSG_TRY(PetscViewerASCIIGetStdout(PETSC_COMM_SELF, &viewer));
+  if (!viewer->ascii) return 0;
+  KSG_TRY(PetscViewerASCIIPrintf(viewer, "DS Object: 1 MPI process\n  %s\n",
+                                 ds->type == 1 ? "type: hep" : ds->type == 2 ? "type: nhep" : "type not yet set"));
   return 0;
 }

@@ -1028,6 +1028,13 @@ extern "C" PetscErrorCode EPSGetOptionsPrefix(EPS eps, const char *prefix[]) {
 
 extern "C" PetscErrorCode EPSSetFromOptions(EPS eps) {
   KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  // STSetFromOptions and DSSetFromOptions give the default types (stset.c:125, dsbasic.c:738)
+  eps->stobj.typeset = 1;
+  DS ds = nullptr;
+  KSG_TRY(EPSGetDS(eps, &ds));
+  DSType dtype = nullptr;
+  KSG_TRY(DSGetType(ds, &dtype));
+  if (!dtype) KSG_TRY(DSSetType(ds, DSNHEP));
   std::string unpre;
   for (int i = 1; i < g_argc; ++i) {
     const char *o = g_argv[i];
@@ -1209,6 +1216,8 @@ extern "C" PetscErrorCode EPSSetUp(EPS eps) {
             "Inconsistent EPS state: the problem type does not match the number of matrices");
   KSG_CHECK(!eps->B || eps->arith != ARITH_F32, PETSC_ERR_SUP,
             "The precision form (EPS_GB300_ARITH_F32) is provided for standard problems only");
+  KSG_CHECK(ksg_eps_hermitian(eps) || (eps->balance != EPS_BALANCE_ONESIDE && eps->balance != EPS_BALANCE_TWOSIDE),
+            PETSC_ERR_SUP, "Balancing of a non-Hermitian problem is not provided");
   const int n = eps->A->m;
   KSG_CHECK(n > 0, PETSC_ERR_ARG_WRONG, "Empty operator");
   int nev = eps->nev, ncv = eps->ncv, mpd = eps->mpd;
@@ -1288,6 +1297,12 @@ extern "C" PetscErrorCode EPSSetUp(EPS eps) {
   KSG_CUDA(cudaStreamSynchronize(eps->stream));
   eps->a_state = eps->A->state;
   eps->b_state = eps->B ? eps->B->state : -1;
+  // the ST and the DS the caller can query get their types here (EPSSetUp_KrylovSchur: DSHEP or DSNHEP)
+  eps->stobj.typeset = 1;
+  if (eps->ds) {
+    KSG_TRY(DSSetType(eps->ds, ksg_eps_lanczos(eps) ? DSHEP : DSNHEP));
+    KSG_TRY(DSAllocate(eps->ds, eps->ld));
+  }
   eps->setup = 1;
   eps->stats.setup_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   return 0;

@@ -196,10 +196,16 @@ extern "C" PetscErrorCode MatLoad(Mat A, PetscViewer v) {
   return 0;
 }
 
-// MatView with a binary viewer: the same layout MatLoad reads
+namespace {
+PetscErrorCode mat_view_ascii(Mat A, PetscViewer v);
+}
+
+// MatView: a binary viewer writes the layout MatLoad reads; an ASCII viewer (NULL is PETSC_VIEWER_STDOUT_WORLD)
+// prints the rows as PETSc's seqaij viewer does
 extern "C" PetscErrorCode MatView(Mat A, PetscViewer v) {
-  KSG_CHECK(A && v, PETSC_ERR_ARG_NULL, "Null argument");
-  KSG_CHECK(!v->ascii, PETSC_ERR_SUP, "Only binary viewers are supported here");
+  KSG_CHECK(A, PETSC_ERR_ARG_NULL, "Null argument");
+  KSG_CHECK(A->pending.empty() && !A->empty, PETSC_ERR_ARG_WRONGSTATE, "Not for unassembled matrix");
+  if (!v || v->ascii) return mat_view_ascii(A, v);
   KSG_CHECK(v->mode != FILE_MODE_READ, PETSC_ERR_ARG_WRONGSTATE, "%s is not open for writing", v->name.c_str());
   KSG_CHECK(!A->dense && !A->empty, PETSC_ERR_SUP, "MatView writes AIJ matrices only");
   std::vector<unsigned char> out;
@@ -310,6 +316,34 @@ void add_g(Text &t, double x) {
   std::snprintf(buf, sizeof(buf), "%g", x);
   if (!std::strpbrk(buf, ".eEni")) std::strncat(buf, ".", sizeof(buf) - std::strlen(buf) - 1);
   t.s += buf;
+}
+
+// MatView_SeqAIJ_ASCII / MatView_SeqDense_ASCII in the default format: the object header, then one line per row,
+// " (column, value) " for each stored entry of an AIJ matrix, every value of a dense one
+PetscErrorCode mat_view_ascii(Mat A, PetscViewer v) {
+  if (!v) v = stdout_viewer();
+  Text t;
+  t.add("Mat Object: 1 MPI process\n  type: %s\n", A->dense ? "seqdense" : "seqaij");
+  const PetscViewerFormat fmt = top_format(v);
+  if (fmt == PETSC_VIEWER_ASCII_INFO || fmt == PETSC_VIEWER_ASCII_INFO_DETAIL) {
+    const long long nz = A->dense ? (long long)A->m * A->n : A->nnz;
+    t.add("  rows=%d, cols=%d\n  total: nonzeros=%lld, allocated nonzeros=%lld\n", A->m, A->n, nz, nz);
+    return emit(v, t);
+  }
+  for (int r = 0; r < A->m; ++r) {
+    if (A->dense) {
+      for (int c = 0; c < A->n; ++c) t.add("%18.16e ", A->data[(size_t)c * A->lda + r]);
+    } else {
+      t.add("row %d:", r);
+      for (PetscInt p = A->ai[r]; p < A->ai[r + 1]; ++p) {
+        t.add(" (%d, ", (int)A->aj[p]);
+        add_g(t, A->aa[p]);
+        t.s += ") ";
+      }
+    }
+    t.s += "\n";
+  }
+  return emit(v, t);
 }
 
 const char *reason_name(int reason) {
@@ -769,8 +803,13 @@ extern "C" PetscErrorCode EPSView(EPS eps, PetscViewer v) {
   t.add("  type: device (GB300), %s storage\n", eps->storage == ksg::STORE_F64 ? "FP64" : "FP32-pair");
   if (ncv > 0 && eps->A) t.add("  %d columns of global length %d\n", ncv + 1, eps->A->m);
   t.add("  vector orthogonalization method: classical Gram-Schmidt, two passes (delayed)\n");
+  // the DS as the reference's EPSView shows it: typed by EPSSetUp (or EPSSetFromOptions), untyped before
+  DSType dtype = nullptr;
+  if (eps->setup) dtype = ksg_eps_lanczos(eps) ? DSHEP : DSNHEP;
+  else if (eps->ds) KSG_TRY(DSGetType(eps->ds, &dtype));
   t.add("DS Object: 1 MPI process\n");
-  t.add("  type: %s\n", ksg_eps_lanczos(eps) ? "hep" : "nhep");
+  if (dtype) t.add("  type: %s\n", dtype);
+  else t.add("  type not yet set\n");
   KSG_TRY(emit(v, t));
   eps->stobj.eps = eps;
   return STView(&eps->stobj, v);
@@ -790,12 +829,13 @@ extern "C" PetscErrorCode STSetType(ST st, STType type) {
   KSG_CHECK(st && type, PETSC_ERR_ARG_NULL, "Null argument");
   KSG_CHECK(!std::strcmp(type, STSHIFT), PETSC_ERR_SUP,
             "ST type %s is not provided: the Krylov-Schur path runs the shift transformation (STSHIFT)", type);
+  st->typeset = 1;
   return 0;
 }
 
 extern "C" PetscErrorCode STGetType(ST st, STType *type) {
   KSG_CHECK(st && type, PETSC_ERR_ARG_NULL, "Null argument");
-  *type = STSHIFT;
+  *type = st->typeset ? STSHIFT : nullptr;  // no type until one is set, as the reference (stset.c:93)
   return 0;
 }
 
@@ -824,7 +864,7 @@ extern "C" PetscErrorCode STView(ST st, PetscViewer v) {
   if (!v->ascii) return 0;
   Text t;
   t.add("ST Object: 1 MPI process\n");
-  t.add("  type: shift\n");
+  t.add(st->typeset ? "  type: shift\n" : "  type not yet set\n");
   t.add("  shift: 0.\n");
   t.add("  number of matrices: %d\n", st->eps->B ? 2 : 1);
   return emit(v, t);
@@ -908,4 +948,61 @@ extern "C" PetscErrorCode KSPGetTotalIterations(KSP ksp, PetscInt *its) {
   KSG_CHECK(ksp && its, PETSC_ERR_ARG_NULL, "Null argument");
   *its = 0;
   return 0;
+}
+
+// balancing, stopping test and track-all (epsopts.c): the defaults are this path's
+const char *EPSBalanceTypes[] = {"NONE", "ONESIDE", "TWOSIDE", "USER", "EPSBalance", "EPS_BALANCE_", nullptr};
+
+// EPSSetBalance (epsopts.c:1062-1092): the settings are stored and checked as the reference does.  A Hermitian
+// problem is never balanced (epssetup.c:378-385); balancing a non-Hermitian one is refused by EPSSetUp.
+extern "C" PetscErrorCode EPSSetBalance(EPS eps, EPSBalance bal, PetscInt its, PetscReal cutoff) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  KSG_CHECK(bal == EPS_BALANCE_NONE || bal == EPS_BALANCE_ONESIDE || bal == EPS_BALANCE_TWOSIDE ||
+                bal == EPS_BALANCE_USER, PETSC_ERR_ARG_OUTOFRANGE, "Invalid value of argument 'bal'");
+  if (eps->balance != (int)bal) {
+    eps->balance = bal;
+    eps->setup = 0;
+  }
+  if (its == PETSC_DETERMINE) eps->balance_its = 5;
+  else if (its != PETSC_CURRENT) {
+    KSG_CHECK(its > 0, PETSC_ERR_ARG_OUTOFRANGE, "Illegal value of its. Must be > 0");
+    eps->balance_its = its;
+  }
+  if (cutoff == (PetscReal)PETSC_DETERMINE) eps->balance_cutoff = 1e-8;
+  else if (cutoff != (PetscReal)PETSC_CURRENT) {
+    KSG_CHECK(cutoff > 0.0, PETSC_ERR_ARG_OUTOFRANGE, "Illegal value of cutoff. Must be > 0");
+    eps->balance_cutoff = cutoff;
+  }
+  return 0;
+}
+extern "C" PetscErrorCode EPSGetBalance(EPS eps, EPSBalance *bal, PetscInt *its, PetscReal *cutoff) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  if (bal) *bal = (EPSBalance)eps->balance;
+  if (its) *its = eps->balance_its;
+  if (cutoff) *cutoff = eps->balance_cutoff;
+  return 0;
+}
+extern "C" PetscErrorCode EPSSetStoppingTest(EPS eps, EPSStop stop) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  KSG_CHECK(stop == EPS_STOP_BASIC, PETSC_ERR_SUP, "Only EPS_STOP_BASIC is provided");
+  return 0;
+}
+extern "C" PetscErrorCode EPSGetStoppingTest(EPS eps, EPSStop *stop) {
+  KSG_CHECK(eps && stop, PETSC_ERR_ARG_NULL, "Null argument");
+  *stop = EPS_STOP_BASIC;
+  return 0;
+}
+extern "C" PetscErrorCode EPSSetTrackAll(EPS eps, PetscBool trackall) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  eps->trackall = trackall ? 1 : 0;
+  return 0;
+}
+extern "C" PetscErrorCode EPSGetTrackAll(EPS eps, PetscBool *trackall) {
+  KSG_CHECK(eps && trackall, PETSC_ERR_ARG_NULL, "Null argument");
+  *trackall = eps->trackall ? PETSC_TRUE : PETSC_FALSE;
+  return 0;
+}
+extern "C" PetscErrorCode KSPSetTolerances(KSP ksp, PetscReal, PetscReal, PetscReal, PetscInt) {
+  KSG_CHECK(ksp, PETSC_ERR_ARG_NULL, "Null KSP");
+  return 0;  // the shift of 0 runs no linear solver
 }

@@ -366,6 +366,7 @@ extern "C" int MPI_Comm_size(MPI_Comm, int *size) {
 struct _p_PetscRandom {
   unsigned long long seed = 0x5EEDULL;
   unsigned long long counter = 0;
+  double low = 0.0, width = 1.0;  // PetscRandomSetInterval
 };
 
 extern "C" PetscErrorCode PetscRandomCreate(MPI_Comm, PetscRandom *r) {
@@ -402,7 +403,38 @@ static double random_next(PetscRandom r) {
 
 extern "C" PetscErrorCode PetscRandomGetValue(PetscRandom r, PetscScalar *value) {
   KSG_CHECK(r && value, PETSC_ERR_ARG_NULL, "Null argument");
-  *value = random_next(r);
+  *value = r->low + r->width * random_next(r);
+  return 0;
+}
+
+extern "C" PetscErrorCode PetscRandomGetValueReal(PetscRandom r, PetscReal *value) {
+  return PetscRandomGetValue(r, value);
+}
+
+extern "C" PetscErrorCode PetscRandomSetInterval(PetscRandom r, PetscScalar low, PetscScalar high) {
+  KSG_CHECK(r, PETSC_ERR_ARG_NULL, "Null PetscRandom");
+  KSG_CHECK(low < high, PETSC_ERR_ARG_OUTOFRANGE, "only low < high");
+  r->low = low;
+  r->width = high - low;
+  return 0;
+}
+
+extern "C" PetscErrorCode PetscStrendswith(const char a[], const char b[], PetscBool *flg) {
+  KSG_CHECK(flg, PETSC_ERR_ARG_NULL, "Null argument");
+  *flg = PETSC_FALSE;
+  if (a && b) {
+    const size_t la = std::strlen(a), lb = std::strlen(b);
+    *flg = (la >= lb && !std::strcmp(a + la - lb, b)) ? PETSC_TRUE : PETSC_FALSE;
+  }
+  return 0;
+}
+
+extern "C" PetscErrorCode PetscSplitOwnership(MPI_Comm, PetscInt *n, PetscInt *N) {
+  KSG_CHECK(n && N, PETSC_ERR_ARG_NULL, "Null argument");
+  KSG_CHECK(*n != PETSC_DECIDE || *N != PETSC_DECIDE, PETSC_ERR_ARG_INCOMP, "Both n and N cannot be PETSC_DECIDE");
+  if (*n == PETSC_DECIDE) *n = *N;
+  if (*N == PETSC_DECIDE) *N = *n;
+  KSG_CHECK(*n == *N, PETSC_ERR_ARG_SIZ, "Sum of local lengths %d does not equal global length %d", (int)*n, (int)*N);
   return 0;
 }
 
@@ -417,7 +449,7 @@ extern "C" PetscErrorCode VecSetRandom(Vec v, PetscRandom r) {
   KSG_CHECK(v, PETSC_ERR_ARG_NULL, "Null Vec");
   _p_PetscRandom local;
   PetscRandom rr = r ? r : &local;
-  for (int i = 0; i < v->n; ++i) v->a[i] = random_next(rr);
+  for (int i = 0; i < v->n; ++i) v->a[i] = rr->low + rr->width * random_next(rr);
   return 0;
 }
 
@@ -454,4 +486,35 @@ extern "C" PetscErrorCode VecCheckOrthonormality(Vec x[], PetscInt nx, Vec y[], 
   }
   *lev = worst;
   return 0;
+}
+
+// MatDuplicate: a library-owned copy (values or zeros); MatDiagonalSet: the diagonal from a Vec
+extern "C" PetscErrorCode MatDuplicate(Mat A, MatDuplicateOption op, Mat *B) {
+  KSG_CHECK(A && B, PETSC_ERR_ARG_NULL, "Null argument");
+  KSG_CHECK(!A->empty, PETSC_ERR_ARG_WRONGSTATE, "Not for unassembled matrix");
+  KSG_CHECK(!A->dense, PETSC_ERR_SUP, "MatDuplicate of a dense Mat is not provided");
+  Mat C = new _p_Mat();
+  C->m = A->m;
+  C->n = A->n;
+  C->sized = 1;
+  C->own_i.assign(A->ai, A->ai + A->m + 1);
+  C->own_j.assign(A->aj, A->aj + A->nnz);
+  if (op == MAT_COPY_VALUES) C->own_a.assign(A->aa, A->aa + A->nnz);
+  else C->own_a.assign((size_t)A->nnz, 0.0);
+  C->ai = C->own_i.data();
+  C->aj = C->own_j.data();
+  C->aa = C->own_a.data();
+  C->nnz = A->nnz;
+  *B = C;
+  return 0;
+}
+
+extern "C" PetscErrorCode MatDiagonalSet(Mat A, Vec D, InsertMode mode) {
+  KSG_CHECK(A && D, PETSC_ERR_ARG_NULL, "Null argument");
+  KSG_CHECK(!A->empty, PETSC_ERR_ARG_WRONGSTATE, "Not for unassembled matrix");
+  KSG_CHECK(!A->dense && D->n == std::min(A->m, A->n), PETSC_ERR_ARG_SIZ, "Nonconforming sizes");
+  KSG_CHECK(mode == INSERT_VALUES || mode == ADD_VALUES, PETSC_ERR_SUP, "Only INSERT_VALUES and ADD_VALUES");
+  own_arrays(A);
+  for (int r = 0; r < D->n; ++r) A->pending.push_back({r, r, D->a[r], mode == ADD_VALUES});
+  return MatAssemblyEnd(A, MAT_FINAL_ASSEMBLY);
 }

@@ -125,6 +125,7 @@ struct _p_BV;
 struct _p_ST {
   unsigned cookie = KSG_ST_COOKIE;
   EPS eps = nullptr;  // the owner
+  int typeset = 0;    // STSetType, EPSSetFromOptions or EPSSetUp gave the type (STSHIFT)
 };
 
 
@@ -156,6 +157,9 @@ struct _p_EPS {
   double target = 0.0;
   int conv = EPS_CONV_REL;  // EPSConv
   int purify = 1;           // EPSSetPurify: GHEP eigenvectors x <- B^-1 A x, B-normalised
+  int balance = 0, balance_its = 5;  // EPSSetBalance: EPS_BALANCE_NONE, 5 iterations, cutoff 1e-8 (epsbasic.c:72-74)
+  double balance_cutoff = 1e-8;
+  int trackall = 0;         // EPSSetTrackAll (stored; every current estimate is computed anyway)
   int arith = ksg::ARITH_PAIR;
   int storage = ksg::STORE_PAIR;  // basis format: pairs with pair arithmetic, doubles with FP64 arithmetic
   int ds_method = 0;              // EPSGB300DSMethod

@@ -15,7 +15,8 @@ import slepc_gb300 as sg
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 REF = os.environ.get("SLEPC_REFERENCE", "/root/reference")
 PROGRAMS = ["tutorials/ex2", "tutorials/ex4", "tutorials/ex5", "tutorials/ex7", "tests/test1", "tests/test2",
-            "tests/test4", "tests/test6", "tests/test19", "tests/test20", "tests/test23"]
+            "tests/test3", "tests/test4", "tests/test6", "tests/test14", "tests/test19", "tests/test20", "tests/test23",
+            "tests/test26", "tests/test39", "tests/test42"]
 
 pytestmark = pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "src", "eps")) or not shutil.which("gcc"),
                                 reason="the reference's sources or gcc are not available here")
@@ -48,3 +49,19 @@ def test_program_runs_to_the_solve(libdir, tmp_path):
         assert "PETSC ERROR" in r.stderr and "CUDA error" in r.stderr
     else:
         assert r.returncode == 0 and "All requested eigenvalues computed up to the required tolerance" in r.stdout
+
+
+def test_interface_queries_print_as_the_reference(libdir, tmp_path):
+    """test14 (src/eps/tests/test14.c) sets and queries every EPS setting, views the operator, the ST and the DS
+    before the solve: everything it prints up to EPSSolve matches the reference's output file line for line."""
+    exe = tmp_path / "test14"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), os.path.join(REF, "src/eps/tests/test14.c"), "-o",
+                    str(exe), "-L", libdir, "-lslepc_gb300", "-lm", "-Wl,-rpath," + libdir], check=True, timeout=120)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=600)
+    with open(os.path.join(REF, "src/eps/tests/output/test14_1.out")) as f:
+        expected = f.read()
+    before_solve = expected[:expected.index(" Finished")]
+    if r.returncode == 97:
+        assert r.stdout == before_solve and "CUDA error" in r.stderr
+    else:
+        assert r.returncode == 0 and r.stdout == expected

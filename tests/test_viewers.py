@@ -177,7 +177,7 @@ def test_options_monitors_names_and_views(lib, tmp_path):
 
 def test_eps_view_matches_the_reference_block(lib):
     """EPSView of test23.c's configuration (named "eps", NHEP, largest real, nev 1, ncv = mpd = 6, 100 iterations)
-    before EPSSetUp: the EPS Object block of test23_1.out, apart from its balancing and residual-tracking lines
+    after EPSSetFromOptions and before EPSSetUp: the EPS Object block of test23_1.out, apart from its balancing and residual-tracking lines
     (options not provided here), the tolerance (the test filters it) and purification (on until EPSSetUp turns it
     off for a standard problem); then the BV, DS and ST objects."""
     A = sg.Mat(*__import__("slepc_gb300.matgen", fromlist=["x"]).laplacian_1d(30))
@@ -188,6 +188,10 @@ def test_eps_view_matches_the_reference_block(lib):
     eps.setWhichEigenpairs("LR")
     eps.setDimensions(1, 6, 6)
     eps.setTolerances(max_it=100)
+    text = eps.view().splitlines()
+    # before EPSSetFromOptions (test23.c:43) the ST and DS have no type yet, as in the reference
+    assert "  type not yet set" in text and "  type: nhep" not in text
+    eps.setFromOptions()
     text = eps.view().splitlines()
     skip = ("balancing", "computing all residuals", "tolerance", "purification")
     ours = [l for l in text[:text.index("BV Object: 1 MPI process")] if not any(k in l for k in skip)]
