@@ -14,9 +14,13 @@ import slepc_gb300 as sg
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 REF = os.environ.get("SLEPC_REFERENCE", "/root/reference")
-PROGRAMS = ["tutorials/ex2", "tutorials/ex4", "tutorials/ex5", "tutorials/ex7", "tests/test1", "tests/test2",
-            "tests/test3", "tests/test4", "tests/test6", "tests/test14", "tests/test19", "tests/test20", "tests/test23",
-            "tests/test26", "tests/test39", "tests/test42"]
+PROGRAMS = ["tutorials/ex1", "tutorials/ex2", "tutorials/ex4", "tutorials/ex5", "tutorials/ex7", "tutorials/ex11",
+            "tutorials/ex13", "tutorials/ex44", "tests/test1", "tests/test2", "tests/test3", "tests/test4",
+            "tests/test6", "tests/test10", "tests/test14", "tests/test18", "tests/test19", "tests/test20",
+            "tests/test23", "tests/test26", "tests/test27", "tests/test28", "tests/test39", "tests/test42"]
+# these build their problem and reach EPSSolve on a machine without a GPU (PETSC_ERR_GPU there)
+RUN_TO_SOLVE = ["tutorials/ex1", "tutorials/ex13", "tutorials/ex44", "tests/test27", "tests/test28", "tests/test3",
+                "tests/test42"]
 
 pytestmark = pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "src", "eps")) or not shutil.which("gcc"),
                                 reason="the reference's sources or gcc are not available here")
@@ -65,3 +69,16 @@ def test_interface_queries_print_as_the_reference(libdir, tmp_path):
         assert r.stdout == before_solve and "CUDA error" in r.stderr
     else:
         assert r.returncode == 0 and r.stdout == expected
+
+
+@pytest.mark.parametrize("prog", RUN_TO_SOLVE)
+def test_program_reaches_the_solve(prog, libdir, tmp_path):
+    """Every call before EPSSolve succeeds; the solve itself needs the GPU (PETSC_ERR_GPU without one)."""
+    exe = tmp_path / os.path.basename(prog)
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), os.path.join(REF, "src", "eps", prog + ".c"), "-o",
+                    str(exe), "-L", libdir, "-lslepc_gb300", "-lm", "-Wl,-rpath," + libdir], check=True, timeout=120)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=600)
+    if r.returncode == 97:
+        assert "EPSSolve(eps) returned 97" in r.stderr and "CUDA error" in r.stderr, r.stderr[-2000:]
+    else:
+        assert r.returncode == 0, r.stderr[-2000:]
