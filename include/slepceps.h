@@ -150,9 +150,11 @@ PetscErrorCode EPSLanczosSetReorthog(EPS eps, EPSLanczosReorthogType reorthog);
 PetscErrorCode EPSLanczosGetReorthog(EPS eps, EPSLanczosReorthogType *reorthog);
 PetscErrorCode EPSGDSetDoubleExpansion(EPS eps, PetscBool doubleexp);
 PetscErrorCode EPSGDGetDoubleExpansion(EPS eps, PetscBool *doubleexp);
-/* balancing (epsopts.c:1010-1090) and the stopping test (epsopts.c:780-860): the defaults, EPS_BALANCE_NONE and
- * EPS_STOP_BASIC, are what this path runs; other values return PETSC_ERR_SUP.  Track-all is stored (the error
- * estimates of all current values are computed in any case). */
+/* balancing (epsopts.c:1010-1090) and the stopping test (epsopts.c:780-860).  The balancing settings are stored and
+ * checked as the reference does; a Hermitian problem is never balanced (epssetup.c:378-385), and EPSSetUp returns
+ * PETSC_ERR_SUP for one-sided or two-sided balancing of a non-Hermitian problem.  The stopping test is
+ * EPS_STOP_BASIC; other values return PETSC_ERR_SUP.  Track-all is stored (the error estimates of all current
+ * values are computed in any case). */
 typedef enum { EPS_BALANCE_NONE, EPS_BALANCE_ONESIDE, EPS_BALANCE_TWOSIDE, EPS_BALANCE_USER } EPSBalance;
 extern const char *EPSBalanceTypes[];
 typedef enum { EPS_STOP_BASIC, EPS_STOP_USER, EPS_STOP_THRESHOLD } EPSStop;

@@ -444,7 +444,8 @@ extern "C" PetscErrorCode DSSetType(DS ds, DSType type) {
 extern "C" PetscErrorCode DSAllocate(DS ds, PetscInt ld) {
   KSG_CHECK(ds, PETSC_ERR_ARG_NULL, "Null DS");
   KSG_CHECK(ds->type, PETSC_ERR_ORDER, "Must call DSSetType() first");
-  KSG_CHECK(ld > 0 && ld <= 144, PETSC_ERR_ARG_OUTOFRANGE, "Leading dimension must be in 1..144");
+  KSG_CHECK(ld > 0 && ld <= KSG_HOST_DS_MAX_LD, PETSC_ERR_ARG_OUTOFRANGE, "Leading dimension must be in 1..%d",
+            KSG_HOST_DS_MAX_LD);
   ds->ld = ld;
   ds->A.assign((size_t)ld * ld, 0.0);
   ds->Q.assign((size_t)ld * ld, 0.0);
@@ -754,7 +755,7 @@ extern "C" PetscErrorCode EPSGetDS(EPS eps, DS *ds) {
     KSG_TRY(DSCreate(0, &eps->ds));  // typed by EPSSetFromOptions (DSNHEP) or EPSSetUp, as the reference's
     if (eps->setup) {
       KSG_TRY(DSSetType(eps->ds, ksg_eps_lanczos(eps) ? DSHEP : DSNHEP));
-      KSG_TRY(DSAllocate(eps->ds, eps->ld));
+      if (eps->ld <= KSG_HOST_DS_MAX_LD) KSG_TRY(DSAllocate(eps->ds, eps->ld));
     }
   }
   *ds = eps->ds;

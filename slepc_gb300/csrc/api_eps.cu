@@ -1301,7 +1301,7 @@ extern "C" PetscErrorCode EPSSetUp(EPS eps) {
   eps->stobj.typeset = 1;
   if (eps->ds) {
     KSG_TRY(DSSetType(eps->ds, ksg_eps_lanczos(eps) ? DSHEP : DSNHEP));
-    KSG_TRY(DSAllocate(eps->ds, eps->ld));
+    if (eps->ld <= KSG_HOST_DS_MAX_LD) KSG_TRY(DSAllocate(eps->ds, eps->ld));  // the host DS is for small ld only
   }
   eps->setup = 1;
   eps->stats.setup_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

@@ -221,6 +221,10 @@ struct _p_EPS {
 
 // the Lanczos (symmetric) variant runs for EPS_HEP with Ritz extraction; harmonic extraction runs the Arnoldi
 // variant with the non-symmetric projected solver (krylovschur.c:238-239)
+// the largest leading dimension of the host-side DS object (DSAllocate); the solver's projected problems live on
+// the device and have no such limit
+constexpr int KSG_HOST_DS_MAX_LD = 144;
+
 inline int ksg_eps_hermitian(EPS e) { return e->problem == EPS_HEP || e->problem == EPS_GHEP; }
 inline int ksg_eps_lanczos(EPS e) { return ksg_eps_hermitian(e) && e->extraction != EPS_HARMONIC; }
 
