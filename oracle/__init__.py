@@ -53,6 +53,8 @@ def load():
         lib.ksor_solve_genb.restype = i
         lib.ksor_set_monitor.argtypes = [MONITOR_FN, P]
         lib.ksor_set_monitor.restype = None
+        lib.ksor_set_deflation.argtypes = [i, P]
+        lib.ksor_set_deflation.restype = None
         lib.ksor_spmv.argtypes = [i, P, P, P, P, P, i]
         lib.ksor_spmv.restype = None
         lib.ksor_ds_hep.argtypes = [i, i, i, i, P, P, i, i, i, P, P, P]
@@ -98,9 +100,10 @@ MONITOR_FN = ctypes.CFUNCTYPE(None, ctypes.c_int, ctypes.c_int, ctypes.POINTER(c
 
 def solve(rowptr, colidx, vals, *, hermitian=True, which="LM", nev=1, ncv=0, mpd=0, tol=1e-8, max_it=0,
           keep=0.5, lock=True, v0=None, nthreads=1, seed=0x5EED, time_budget=0.0, vectors=True, harmonic=False,
-          target=0.0, bdiag=None, conv="rel", purify=True, monitor=None, B=None) -> Result:
+          target=0.0, bdiag=None, conv="rel", purify=True, monitor=None, B=None, deflation=None) -> Result:
     """bdiag: the diagonal of B for A x = k B x (EPS_GHEP when hermitian, else EPS_GNHEP); conv: "rel", "abs" or
-    "norm" (EPS_CONV_NORM with the infinity norms of A and of B, or 0 for ||B|| without B, as EPSSetUp leaves it)."""
+    "norm" (EPS_CONV_NORM with the infinity norms of A and of B, or 0 for ||B|| without B, as EPSSetUp leaves it);
+    deflation: an n x nds array whose columns span the deflation space (EPSSetDeflationSpace)."""
     lib = load()
     n = len(rowptr) - 1
     rowptr = np.ascontiguousarray(rowptr, dtype=np.int32)
@@ -132,6 +135,8 @@ def solve(rowptr, colidx, vals, *, hermitian=True, which="LM", nev=1, ncv=0, mpd
                     [es[i] for i in range(nest)], nest)
         cb = MONITOR_FN(_mon)
     lib.ksor_set_monitor(cb if cb is not None else MONITOR_FN(), None)
+    W = None if deflation is None else np.asfortranarray(np.asarray(deflation, np.float64).reshape(n, -1))
+    lib.ksor_set_deflation(0 if W is None else W.shape[1], _ptr(W))
     if B is None:
         err = lib.ksor_solve_gen(n, _ptr(rowptr), _ptr(colidx), _ptr(vals), _ptr(bd), int(bool(hermitian)),
                                  WHICH[which], int(nev), int(ncv), int(mpd), float(tol), int(max_it), float(keep),
@@ -146,6 +151,7 @@ def solve(rowptr, colidx, vals, *, hermitian=True, which="LM", nev=1, ncv=0, mpd
                                   _ptr(X), int(bool(harmonic)), float(target), CONV[conv], nrma, nrmb,
                                   int(bool(purify)))
     lib.ksor_set_monitor(MONITOR_FN(), None)
+    lib.ksor_set_deflation(0, None)
     return Result(info, eigr, eigi, errest, X, err)
 
 

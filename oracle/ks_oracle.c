@@ -949,6 +949,9 @@ typedef struct {
   const double *bw;  /* diagonal of the inner-product matrix B (BVSetMatrix), NULL: Euclidean */
   const csr_t *bm;   /* or a general inner-product matrix B (CSR) */
   double *bt;        /* scratch for B w (n) */
+  int nc;            /* constraint columns (the deflation space, BVInsertConstraints), orthonormal, before V */
+  double *W;         /* n x nc */
+  double *cw;        /* their coefficients (nc) */
 } bv_t;
 
 #define VCOL(bv, j) ((bv)->V + (size_t)(j) * (size_t)(bv)->n)
@@ -1084,20 +1087,40 @@ static double bv_vec_norm(const bv_t *bv, const double *w) {
 
 /* One CGS pass (BVOrthogonalizeCGS1, bvorthog.c:91-132).  Returns 0, or an error code for a negative inner
  * product (BV_SafeSqrt).  onorm/norm optional. */
+/* constraint part of one CGS pass (BVOrthogonalizeCGS1 runs over columns -nc..j-1, bvorthog.c): cw = W^T w against
+ * the same w as the basis dots, subtracted with them, and counted in the square sum */
+static void bv_constraint_dots(bv_t *bv, const double *w) {
+  for (int i = 0; i < bv->nc; i++) {
+    const double *wi = bv->W + (size_t)i * bv->n;
+    double s = 0.0;
+    for (int r = 0; r < bv->n; r++) s += wi[r] * w[r];
+    bv->cw[i] = s;
+  }
+}
+static void bv_constraint_sub(bv_t *bv, double *w) {
+  for (int i = 0; i < bv->nc; i++) {
+    const double *wi = bv->W + (size_t)i * bv->n;
+    for (int r = 0; r < bv->n; r++) w[r] -= wi[r] * bv->cw[i];
+  }
+}
+
 static int bv_cgs1(bv_t *bv, int j, double *h, double *onorm, double *norm) {
   double *w = VCOL(bv, j), *c = bv->c;
   double beta = 0.0;
   bv->npasses++;
   bv_dot_inc(bv, j, w, c);
+  bv_constraint_dots(bv, w);
   if (onorm || norm) {
     double alpha = c[j];
     if (alpha < -10.0 * DEPS) return 62; /* PETSC_ERR_USER_INPUT: invalid inner product */
     beta = alpha < 0.0 ? 0.0 : sqrt(alpha);
   }
   bv_mult_sub(bv, j, w, c);
+  bv_constraint_sub(bv, w);
   if (onorm) *onorm = beta;
   if (norm) {
     double sum = 0.0;
+    for (int i = 0; i < bv->nc; i++) sum += bv->cw[i] * bv->cw[i];
     for (int i = 0; i < j; i++) sum += c[i] * c[i];
     double nn = beta * beta - sum;
     if (nn <= 0.0) *norm = bv_vec_norm(bv, w);
@@ -1359,6 +1382,40 @@ int ksor_solve(int n, const int *rowptr, const int *colidx, const double *vals,
                         target, KSOR_CONV_REL, 0.0, 0.0, 1);
 }
 
+/* the deflation space of the next solve (EPSSetDeflationSpace, epssetup.c:523-560): nds vectors of length n,
+ * column-major; the caller keeps them alive until the solve returns */
+static int g_defl_n = 0;
+static const double *g_defl = NULL;
+void ksor_set_deflation(int nds, const double *W) {
+  g_defl_n = W ? nds : 0;
+  g_defl = W;
+}
+
+/* BVInsertConstraints (bvbasic.c): each vector orthonormalised against the ones kept before it (classical
+ * Gram-Schmidt, refined if needed, as BVOrthonormalizeColumn); a linearly dependent one is dropped */
+static void insert_constraints(bv_t *bv, int nds, const double *U) {
+  const int n = bv->n;
+  bv->nc = 0;
+  for (int k = 0; k < nds; k++) {
+    double *w = bv->W + (size_t)bv->nc * n;
+    memcpy(w, U + (size_t)k * n, sizeof(double) * n);
+    double onrm = 0.0, nrm = 0.0;
+    for (int pass = 0; pass < 3; pass++) {
+      double a = 0.0, sum = 0.0;
+      for (int r = 0; r < n; r++) a += w[r] * w[r];
+      bv_constraint_dots(bv, w);
+      bv_constraint_sub(bv, w);
+      for (int i = 0; i < bv->nc; i++) sum += bv->cw[i] * bv->cw[i];
+      onrm = sqrt(a);
+      nrm = (a - sum > 0.0) ? sqrt(a - sum) : nrm2(n, w);
+      if (!(nrm != 0.0 && nrm < bv->eta * onrm)) break;
+    }
+    if (nrm == 0.0 || nrm < bv->eta * onrm) continue;  /* linearly dependent */
+    for (int r = 0; r < n; r++) w[r] /= nrm;
+    bv->nc++;
+  }
+}
+
 static ksor_monitor_fn g_monitor = NULL;
 static void *g_monitor_ctx = NULL;
 void ksor_set_monitor(ksor_monitor_fn fn, void *ctx) {
@@ -1439,6 +1496,12 @@ static int solve_impl(int n, const int *rowptr, const int *colidx, const double 
   bv.bw = ghep ? bdiag : NULL;
   bv.bm = ghep ? bcsr : NULL;
   bv.V = (double *)calloc((size_t)n * bv.m, sizeof(double));
+  if (g_defl_n > 0) {
+    if (bdiag || bcsr) { free(bv.V); return 56; } /* deflation spaces of generalised problems: not restated */
+    bv.W = (double *)calloc((size_t)n * g_defl_n, sizeof(double));
+    bv.cw = (double *)calloc((size_t)g_defl_n, sizeof(double));
+    insert_constraints(&bv, g_defl_n, g_defl);
+  }
   bv.h = (double *)calloc((size_t)(bv.m + 1) * (bv.m + 1), sizeof(double));
   bv.c = (double *)calloc((size_t)bv.m + 1, sizeof(double));
   ds_t ds = {0};
@@ -1480,7 +1543,13 @@ static int solve_impl(int n, const int *rowptr, const int *colidx, const double 
     st_apply(&Acsr, &op, t, bv.V, nthreads);
     free(t);
   }
-  {
+  if (bv.nc) {
+    /* EPSGetStartVector (epssolve.c): orthonormalised against the deflation space */
+    double nrm = 0.0;
+    int lindep = 0;
+    if ((err = bv_orthonormalize(&bv, 0, &nrm, &lindep))) goto done;
+    if (lindep || nrm == 0.0) { err = 77; goto done; } /* the initial vector belongs to the deflation space */
+  } else {
     double nrm = bv_vec_norm(&bv, bv.V);
     if (nrm == 0.0) { err = 77; goto done; } /* initial vector is zero */
     bv_scale(&bv, 0, 1.0 / nrm);
@@ -1661,7 +1730,7 @@ done:
     info[KSOR_INFO_MPD] = mpd;
     info[KSOR_INFO_MAXIT] = max_it;
   }
-  free(bv.V); free(bv.h); free(bv.c); free(bv.bt); free(lu); free(piv);
+  free(bv.V); free(bv.h); free(bv.c); free(bv.bt); free(bv.W); free(bv.cw); free(lu); free(piv);
   free(ds.d); free(ds.e); free(ds.A); free(ds.Q); free(ds.X); free(ds.perm); free(ds.work);
   free(eigr); free(eigi); free(errest); free(perm); free(hg);
   return err;

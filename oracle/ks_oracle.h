@@ -72,6 +72,9 @@ int ksor_solve_genb(int n, const int *rowptr, const int *colidx, const double *v
 typedef void (*ksor_monitor_fn)(int its, int nconv, const double *eigr, const double *eigi, const double *errest,
                                 int nest, void *ctx);
 void ksor_set_monitor(ksor_monitor_fn fn, void *ctx);
+/* the deflation space of the next solves (EPSSetDeflationSpace): nds column-major vectors of length n, orthonormalised
+ * on entry to each solve; NULL clears it.  Standard problems only (a generalised one returns 56). */
+void ksor_set_deflation(int nds, const double *W);
 
 /* y = A x (CSR), the operation MatMult performs for AIJ. */
 void ksor_spmv(int n, const int *rowptr, const int *colidx, const double *vals, const double *x, double *y,

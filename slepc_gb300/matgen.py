@@ -96,6 +96,17 @@ def laplacian_2d(nx: int, ny: int | None = None):
     return _stencil_csr((nx, ny), 4.0, [(0, -1, -1.0), (0, 1, -1.0), (1, -1, -1.0), (1, 1, -1.0)])
 
 
+def graph_laplacian_2d(nx: int, ny: int | None = None):
+    """Graph Laplacian of an nx x ny mesh: -1 per mesh edge, the vertex degree on the diagonal (ex11.c's matrix,
+    src/eps/tutorials/ex11.c:49-57).  Singular, with the constant vector as null space."""
+    rowptr, colidx, vals = laplacian_2d(nx, ny)
+    n = len(rowptr) - 1
+    rows = np.repeat(np.arange(n), np.diff(rowptr))
+    vals = vals.copy()
+    vals[colidx == rows] = np.diff(rowptr)[rows[colidx == rows]] - 1.0
+    return rowptr, colidx, vals
+
+
 def laplacian_3d(n: int):
     offs = [(a, s, -1.0) for a in range(3) for s in (-1, 1)]
     return _stencil_csr((n, n, n), 6.0, offs)

@@ -106,6 +106,12 @@ def main():
     line = [l for l in txt.splitlines() if re.search(r"\d\.\d{5}", l)][-1]
     g["test6_1"] = {"source": "src/eps/tests/output/test6_1.out", "n": 30, "nev": 4, "which": "LM", "tol": 1e-10,
                     "eigenvalues": floats(line)}
+    # graph Laplacian of a 10 x 10 mesh (degree on the diagonal), HEP, smallest real, nev 4, restart 0.2, the
+    # constant vector as deflation space (src/eps/tutorials/ex11.c TEST 1)
+    txt = read("src/eps/tutorials/output/ex11_1.out")
+    line = [l for l in txt.splitlines() if re.search(r"\d\.\d{5}", l)][-1]
+    g["ex11_1"] = {"source": "src/eps/tutorials/output/ex11_1.out", "grid": [10, 10], "nev": 4, "which": "SR",
+                   "keep": 0.2, "tol": 1e-8, "eigenvalues": floats(line)}
     # EPSView of a Krylov-Schur NHEP solve, largest real (src/eps/tests/test23.c TEST 1): the EPS Object block
     lines = read("src/eps/tests/output/test23_1.out").splitlines()
     i0 = next(i for i, l in enumerate(lines) if l.startswith("EPS Object"))
@@ -139,7 +145,7 @@ def main():
                  shape=np.array([m, n], dtype=np.int32))
     # the text EPSErrorView prints (the "All requested ..." line and the eigenvalue line), per solve of each test
     for key in ("ex2_1", "ex9_1", "ex4_1", "test2_1", "test2_3", "test1_1", "ex5_1", "test4_1", "test6_1", "ex7_1",
-                "ex7_3"):
+                "ex7_3", "ex11_1"):
         lines = read(g[key]["source"]).splitlines()
         g[key]["errorview"] = [[lines[i], lines[i + 1]] for i, l in enumerate(lines)
                                if l.startswith(" All requested eigenvalues")]

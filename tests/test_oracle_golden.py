@@ -399,3 +399,21 @@ def test_ghep_harmonic_interior(orc):
     w = sl.eigh(matgen.csr_to_dense(*csr), np.diag(b), eigvals_only=True)
     want = w[np.argsort(np.abs(w - target))][:4]
     assert np.allclose(np.sort(r.eigr[:4]), np.sort(want), rtol=1e-9, atol=0)
+
+
+def test_ex11_deflation_space_golden(orc):
+    """ex11.c: the Fiedler vector of a 10 x 10 mesh's graph Laplacian, smallest real, nev 4, restart 0.2, with the
+    constant vector (the null space) as deflation space: the eigenvalues ex11_1.out prints, and every computed
+    eigenvector orthogonal to the deflation space."""
+    g = G["ex11_1"]
+    csr = matgen.graph_laplacian_2d(*g["grid"])
+    n = len(csr[0]) - 1
+    assert np.allclose(np.add.reduceat(csr[2], csr[0][:-1]), 0.0)  # rows sum to zero: the constant is a null vector
+    r = orc.solve(*csr, hermitian=True, which=g["which"], nev=g["nev"], keep=g["keep"], tol=g["tol"],
+                     deflation=np.ones(n))
+    assert r.reason == 1 and r.nconv >= g["nev"]
+    assert [round(v, 5) for v in r.eigr[:g["nev"]]] == g["eigenvalues"]
+    assert np.abs(r.X[:, :g["nev"]].sum(axis=0)).max() < 1e-10 * np.sqrt(n)
+    # without the deflation space the zero eigenvalue comes first
+    r0 = orc.solve(*csr, hermitian=True, which=g["which"], nev=g["nev"], keep=g["keep"], tol=g["tol"])
+    assert abs(r0.eigr[0]) < 1e-8 and round(r0.eigr[1], 5) == g["eigenvalues"][0]
