@@ -10,6 +10,7 @@
 #include <stdarg.h>
 #include <stdio.h>
 #include <string.h>
+#include <strings.h>
 
 #include <algorithm>
 #include <cctype>
@@ -1055,6 +1056,17 @@ extern "C" PetscErrorCode EPSSetFromOptions(EPS eps) {
     else if (!strcmp(o, "-eps_mpd") && v) KSG_TRY(EPSSetDimensions(eps, PETSC_CURRENT, PETSC_CURRENT, atoi(v)));
     else if (!strcmp(o, "-eps_tol") && v) KSG_TRY(EPSSetTolerances(eps, atof(v), PETSC_CURRENT));
     else if (!strcmp(o, "-eps_max_it") && v) KSG_TRY(EPSSetTolerances(eps, PETSC_CURRENT, atoi(v)));
+    else if (!strcmp(o, "-eps_balance") && v) {  // epsopts.c:132-137: the EPSBalance names in lower case
+      const char *names[] = {"none", "oneside", "twoside", "user"};
+      int b = -1;
+      for (int k = 0; k < 4; ++k)
+        if (!strcasecmp(v, names[k])) b = k;
+      KSG_CHECK(b >= 0, PETSC_ERR_USER_INPUT, "Unknown balancing method %s", v);
+      KSG_TRY(EPSSetBalance(eps, (EPSBalance)b, PETSC_CURRENT, PETSC_CURRENT));
+    } else if (!strcmp(o, "-eps_balance_its") && v)
+      KSG_TRY(EPSSetBalance(eps, (EPSBalance)eps->balance, atoi(v), PETSC_CURRENT));
+    else if (!strcmp(o, "-eps_balance_cutoff") && v)
+      KSG_TRY(EPSSetBalance(eps, (EPSBalance)eps->balance, PETSC_CURRENT, atof(v)));
     else if (!strcmp(o, "-eps_largest_magnitude")) KSG_TRY(EPSSetWhichEigenpairs(eps, EPS_LARGEST_MAGNITUDE));
     else if (!strcmp(o, "-eps_smallest_magnitude")) KSG_TRY(EPSSetWhichEigenpairs(eps, EPS_SMALLEST_MAGNITUDE));
     else if (!strcmp(o, "-eps_largest_real")) KSG_TRY(EPSSetWhichEigenpairs(eps, EPS_LARGEST_REAL));

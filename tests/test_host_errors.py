@@ -88,3 +88,31 @@ def test_monitor_limit(lib):
     eps.monitorCancel()
     eps.monitorSet(lambda *a: None)
     eps.destroy()
+
+
+def test_balance_settings(lib):
+    """EPSSetBalance/EPSGetBalance (epsopts.c:1062-1092) and -eps_balance*: stored as the reference stores them."""
+    eps = sg.EPS().create()
+    lib.EPSSetBalance.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_double]
+    lib.EPSGetBalance.argtypes = [P, P, P, P]
+    bal, its, cut = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+
+    def get():
+        assert lib.EPSGetBalance(eps.handle, ctypes.byref(bal), ctypes.byref(its), ctypes.byref(cut)) == 0
+        return bal.value, its.value, cut.value
+
+    assert get() == (0, 5, 1e-8)                                            # EPS_BALANCE_NONE, 5, 1e-8
+    assert lib.EPSSetBalance(eps.handle, 1, 8, 1e-6) == 0 and get() == (1, 8, 1e-6)
+    assert lib.EPSSetBalance(eps.handle, 2, -1, -1.0) == 0 and get() == (2, 5, 1e-8)   # PETSC_DETERMINE
+    assert lib.EPSSetBalance(eps.handle, 2, -2, -2.0) == 0 and get() == (2, 5, 1e-8)   # PETSC_CURRENT
+    assert lib.EPSSetBalance(eps.handle, 7, -2, -2.0) == PETSC_ERR_ARG_OUTOFRANGE
+    assert lib.EPSSetBalance(eps.handle, 1, 0, -2.0) == PETSC_ERR_ARG_OUTOFRANGE        # its must be > 0
+    eps.destroy()
+    sg.initialize(["prog", "-eps_balance", "oneside", "-eps_balance_its", "3"])
+    try:
+        eps = sg.EPS().create()
+        eps.setFromOptions()
+        assert get() == (1, 3, 1e-8)
+        eps.destroy()
+    finally:
+        sg.initialize(["prog"])
