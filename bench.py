@@ -6,7 +6,12 @@ uniform[-1,1] (splitmix64, seed 2).  The basis alone is 2.2 GB, far larger than 
 between steps.
 
   value      nev converged eigenpairs per solve / device time of EPSSolve (CUDA events on the solver's stream),
-             matrix resident in HBM since EPSSetUp (the start vector's 16.8 MB upload is inside EPSSolve)
+             matrix resident in HBM since EPSSetUp (the start vector's 16.8 MB upload is inside EPSSolve).
+             Arithmetic: IEEE FP64 storage and products (--arith f64, the default)
+  parity     after the timed solves, on the host: every converged eigenvalue against the closed-form spectrum
+             (set-based over distinct values), ||Ax - lam x|| / (||A||_inf |lam|) with scipy.sparse on the CSR
+             arrays, ||X^T X - I|| in numpy, from the eigenvectors EPSGetEigenpair returns; exit code 3 if a bound fails
+  pair       the same workload in FP32-pair arithmetic (narrower than FP64), reported beside the headline
   e2e        the same metric through the public C-ABI from host buffers: MatCreateSeqAIJWithArrays + EPSSetUp (CSR
              host->device) + EPSSolve + EPSGetEigenpair for all nev (eigenvectors device->host), host wall clock
   roofline   the dominant kernel class of one profiled solve: algorithmic bytes / summed CUDA-event time
@@ -34,14 +39,16 @@ sys.path.insert(0, ROOT)
 WORKLOADS = {
     "lap3d128": dict(desc="3-D 7-point Laplacian 128^3 (n=2097152, nnz=14581760, FP64 CSR), EPS_HEP, nev=50 "
                           "largest algebraic, ncv=128, tol=1e-10, start vector uniform[-1,1] seed 2",
-                     gen=lambda mg: mg.laplacian_3d(128), hermitian=True, which="LR", nev=50, ncv=128, tol=1e-10,
-                     seed=2),
+                     gen=lambda mg: mg.laplacian_3d(128), exact=lambda mg: mg.laplacian_eigenvalues([128] * 3),
+                     hermitian=True, which="LR", nev=50, ncv=128, tol=1e-10, seed=2),
     "lap2d100": dict(desc="2-D 5-point Laplacian 100x100 (n=10000, nnz=49600), EPS_HEP, nev=10 largest magnitude, "
                           "ncv=32, tol=1e-8, start vector seed 1",
-                     gen=lambda mg: mg.laplacian_2d(100), hermitian=True, which="LM", nev=10, ncv=32, tol=1e-8, seed=1),
+                     gen=lambda mg: mg.laplacian_2d(100), exact=lambda mg: mg.laplacian_eigenvalues([100, 100]),
+                     hermitian=True, which="LM", nev=10, ncv=32, tol=1e-8, seed=1),
     "lap3d64": dict(desc="3-D 7-point Laplacian 64^3 (n=262144, nnz=1810432), EPS_HEP, nev=50 largest algebraic, "
                          "ncv=128, tol=1e-10, start vector seed 2 (the 128^3 solve's shape at 1/8 size, for profiling)",
-                    gen=lambda mg: mg.laplacian_3d(64), hermitian=True, which="LR", nev=50, ncv=128, tol=1e-10, seed=2),
+                    gen=lambda mg: mg.laplacian_3d(64), exact=lambda mg: mg.laplacian_eigenvalues([64] * 3),
+                    hermitian=True, which="LR", nev=50, ncv=128, tol=1e-10, seed=2),
     "chunglu4m": dict(desc="Chung-Lu power-law graph n=4194304, mean degree 32, gamma 2.1, max degree 1e5 (seed 4), "
                            "weights U(0,1] (seed 5), normalised adjacency D^-1/2 A D^-1/2 (nnz 125,195,026), EPS_HEP, "
                            "nev=16 largest algebraic, ncv=48, tol=1e-10, start vector seed 4",
@@ -49,7 +56,8 @@ WORKLOADS = {
                       seed=4),
     "convdiff1000": dict(desc="2-D upwind convection-diffusion 1000x1000 (n=1e6), Peclet 10, EPS_NHEP, nev=20 "
                               "largest real, ncv=64, tol=1e-10, start vector seed 3",
-                         gen=lambda mg: mg.convection_diffusion_2d(1000, 10.0), hermitian=False, which="LR", nev=20,
+                         gen=lambda mg: mg.convection_diffusion_2d(1000, 10.0),
+                         exact=lambda mg: mg.convdiff_eigenvalues(1000, 10.0), hermitian=False, which="LR", nev=20,
                          ncv=64, tol=1e-10, seed=3),
 }
 BATCH = dict(desc="4096 independent EPS_HEP problems, n_i = round(exp(U[ln 1000, ln 65536])) (splitmix64 seed 6+i), "
@@ -545,11 +553,15 @@ def main():
     ap.add_argument("--batch-count", type=int, default=0, help="problems in the batched workload (default 4096)")
     ap.add_argument("--batch-plain-sample", type=int, default=256,
                     help="problems of the batched workload timed through the one-problem-per-launch path")
-    ap.add_argument("--arith", default="pair", choices=["pair", "f64", "f32"])
+    ap.add_argument("--arith", default="f64", choices=["pair", "f64", "f32"],
+                    help="f64: IEEE FP64 storage and FMA (the headline); pair: FP32-pair arithmetic (reported beside "
+                         "it); f32: the precision form")
     ap.add_argument("--restart", default="tensor", choices=["tensor", "pair", "mma_sync", "tcgen05"],
                     help="kernel of the thick restart (EPSGB300SetRestartMethod)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-parity", action="store_true", help="skip the host-side parity block")
+    ap.add_argument("--no-pair", action="store_true", help="skip the pair-arithmetic line beside the FP64 one")
     ap.add_argument("--no-tune", action="store_true", help="batched workload: keep the default tuning table")
     ap.add_argument("--profile-case", action="store_true",
                     help="run exactly one solve limited to 2 restarts and exit (the ncu capture case)")
@@ -574,7 +586,55 @@ def main():
     if args.impl == "reference":
         run_reference(args, wl)
         return
+    run_plain(args, wl)
 
+
+# FP64 FMA throughput of this GPU (DFMA microbenchmark: 1.20 TFLOP/s).  A Gram-Schmidt half does two FMAs per 8-byte
+# basis entry (0.5 flop/byte), so IEEE FP64 Gram-Schmidt is bounded at 1.20e12 * 2 = 2.4 TB/s, below the HBM rate.
+DFMA_TFLOPS = 1.20
+ARITH_LABEL = {"f64": "IEEE FP64 storage and FMA",
+               "pair": "FP32-pair storage and arithmetic (hi+lo floats, 47-bit significand, ~2^-46 per product)",
+               "f32": "FP32 storage, pair accumulation, FP64-class refinement sweep"}
+
+
+def eigenpairs(eps, n, count):
+    """The first `count` converged eigenpairs through EPSGetEigenpair (real parts; vectors as returned)."""
+    lams = np.zeros(count)
+    imag = np.zeros(count)
+    X = np.empty((n, count))
+    x = np.empty(n)
+    for i in range(count):
+        lam = eps.getEigenpair(i, x)
+        lams[i] = lam.real if isinstance(lam, complex) else lam
+        imag[i] = lam.imag if isinstance(lam, complex) else 0.0
+        X[:, i] = x
+    return lams, imag, X
+
+
+def parity_of(eps, csr, wl, n):
+    """Host-side parity of the solve left in `eps`: eigenvalues against the closed-form spectrum (set-based),
+    residuals with scipy.sparse on the caller's CSR and ||X^T X - I|| in numpy (slepc_gb300.verify)."""
+    from slepc_gb300 import matgen, verify
+
+    nconv = eps.getConverged()
+    lams, imag, X = eigenpairs(eps, n, nconv)
+    real = imag == 0.0
+    exact = wl["exact"](matgen) if wl.get("exact") else None
+    if exact is not None:
+        p = verify.parity_block(csr, lams[real], X[:, real], exact, wl["which"], wl["nev"], wl["tol"],
+                                hermitian=wl["hermitian"])
+    else:
+        r_a, r_l = verify.residuals(csr, lams[real], X[:, real])
+        p = {"checked": "residuals and orthogonality (no closed form)", "converged": int(nconv),
+             "max_rel_residual": float(r_a.max()), "max_residual_over_lambda": float(r_l.max()),
+             "orth_err": verify.orthogonality(X) if wl["hermitian"] else None, "tol": wl["tol"]}
+        p["ok"] = bool(p["max_rel_residual"] <= wl["tol"] and (p["orth_err"] is None or p["orth_err"] <= 1e-12))
+    p["complex_pairs"] = int(np.sum(~real))
+    del X
+    return p
+
+
+def run_plain(args, wl):
     import ctypes
 
     import slepc_gb300 as sg
@@ -591,14 +651,14 @@ def main():
     nnz = len(csr[1])
     v0 = matgen.start_vector(n, wl["seed"])
 
-    def make_eps(A):
+    def make_eps(A, arith):
         eps = sg.EPS().create()
         eps.setOperators(A)
         eps.setProblemType(sg.EPS.ProblemType.HEP if wl["hermitian"] else sg.EPS.ProblemType.NHEP)
         eps.setDimensions(wl["nev"], wl["ncv"])
         eps.setTolerances(wl["tol"])
         eps.setWhichEigenpairs(wl["which"])
-        eps.setArithmetic(args.arith)
+        eps.setArithmetic(arith)
         eps.setRestartMethod(args.restart)
         eps.setInitialSpace(v0)
         return eps
@@ -607,7 +667,7 @@ def main():
     max_over_ranks = rep.max
 
     A = sg.Mat(*csr)
-    eps = make_eps(A)
+    eps = make_eps(A, args.arith)
     if args.profile_case:
         eps.setTolerances(wl["tol"], 2)
         eps.setUp()
@@ -619,30 +679,73 @@ def main():
         eps.setProfiling(True)
         eps.solve()
         prof = eps.getProfile()
-        print(json.dumps({"profile_solve": args.workload, "restart": args.restart, "stats": eps.getStats(),
-                          "per_class_ms": {k: round(v[0], 3) for k, v in prof.items()}}), flush=True)
+        print(json.dumps({"profile_solve": args.workload, "arith": args.arith, "restart": args.restart,
+                          "stats": eps.getStats(), "per_class_ms": {k: round(v[0], 3) for k, v in prof.items()}}),
+              flush=True)
         return
-    eps.setUp()
-    for _ in range(args.warmup):
-        eps.solve()
+
+    def timed(e, steps, warmup, clocks=None):
+        """warmup untimed solves, then `steps` solves: device time (CUDA events on the solver's stream), wall
+        latency, launches, converged counts."""
+        e.setUp()
+        for _ in range(warmup):
+            e.solve()
+        barrier()
+        if clocks:
+            clocks.start()
+        r = {"dev_ms": [], "lat": [], "launches": 0, "nconv": [], "steps": [], "restarts": []}
+        for _ in range(steps):
+            e.solve()
+            st = e.getStats()
+            r["dev_ms"].append(st["solve_device_ms"])
+            r["lat"].append(st["solve_seconds"] * 1000.0)
+            r["launches"] += st["kernel_launches"]
+            r["nconv"].append(e.getConverged())
+            r["steps"].append(st["krylov_steps"])
+            r["restarts"].append(st["restarts"])
+        barrier()
+        r["clk"] = clocks.stop() if clocks else None
+        r["total_ms"] = max_over_ranks(sum(r["dev_ms"]))
+        assert min(r["nconv"]) >= wl["nev"], f"solve did not converge ({r['nconv']})"
+        r["value"] = world * steps * wl["nev"] / (r["total_ms"] / 1000.0)
+        return r
+
+    def roofline_of(e, arith):
+        """One profiled solve: per kernel class device time and algorithmic bytes; the dominant class's rate."""
+        e.setProfiling(True)
+        e.solve()
+        prof = e.getProfile()
+        e.setProfiling(False)
+        peak, peak_kind = measured_peaks()
+        top = max(("gs_dot", "gs_update", "spmv", "restart"), key=lambda k: prof[k][0])
+        ms_k, by_k, nl_k = prof[top]
+        achieved = by_k / (ms_k / 1000.0) / 1e9 if ms_k > 0 else None
+        tr = (committed_traffic(args.workload + ("" if arith == "pair" else "_" + arith)) or {}).get(top)
+        traffic = tr * by_k / nl_k if (tr and nl_k) else None  # DRAM bytes per launch: ncu ratio x algorithmic
+        roof = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak if achieved else None, "peak_source": peak_kind,
+                "traffic": traffic, "algorithmic_bytes_per_launch": by_k / nl_k if nl_k else None,
+                "launches": nl_k,
+                "per_class_ms": {k: round(v[0], 3) for k, v in prof.items()},
+                "per_class_GBps": {k: (round(v[1] / (v[0] / 1000.0) / 1e9, 1) if v[0] > 0 else None)
+                                   for k, v in prof.items()}}
+        krylov_ms = sum(prof[k][0] for k in ("spmv", "gs_dot", "gs_update"))
+        krylov_bytes = sum(prof[k][1] for k in ("spmv", "gs_dot", "gs_update"))
+        roof["krylov_step_GBps"] = round(krylov_bytes / (krylov_ms / 1000.0) / 1e9, 1) if krylov_ms > 0 else None
+        roof["krylov_step_frac"] = round(roof["krylov_step_GBps"] / peak, 4) if krylov_ms > 0 else None
+        roof["solve_bytes"] = sum(v[1] for v in prof.values())
+        if arith == "f64":
+            # the FP64 pipe bounds IEEE Gram-Schmidt before HBM does: 2 DFMA per 8-byte entry
+            bound = DFMA_TFLOPS * 1e12 * 2.0 / 1e9
+            roof["fp64_fma_bound"] = {
+                "dfma_tflops": DFMA_TFLOPS, "gs_flop_per_byte": 0.5, "bound_GBps": bound,
+                "gs_dot_frac": (roof["per_class_GBps"]["gs_dot"] or 0.0) / bound,
+                "gs_update_frac": (roof["per_class_GBps"]["gs_update"] or 0.0) / bound}
+        return roof
+
     clocks = ClockSampler(local)
-    barrier()
-    clocks.start()
-    dev_ms, lat, launches, nconvs, steps_k, restarts = [], [], 0, [], [], []
-    for _ in range(args.steps):
-        eps.solve()
-        st = eps.getStats()
-        dev_ms.append(st["solve_device_ms"])
-        lat.append(st["solve_seconds"] * 1000.0)
-        launches += st["kernel_launches"]
-        nconvs.append(eps.getConverged())
-        steps_k.append(st["krylov_steps"])
-        restarts.append(st["restarts"])
-    barrier()
-    clk = clocks.stop()
-    total_ms = max_over_ranks(sum(dev_ms))
-    assert min(nconvs) >= wl["nev"], f"solve did not converge ({nconvs})"
-    value = world * args.steps * wl["nev"] / (total_ms / 1000.0)
+    main_run = timed(eps, args.steps, args.warmup, clocks)
+    par = parity_of(eps, csr, wl, n) if (rank == 0 and not args.no_parity) else None
 
     # e2e: public API from host buffers, per step: CSR + start vector host->device, solve, eigenpairs device->host
     e2e = None
@@ -654,7 +757,7 @@ def main():
             barrier()
             t = time.perf_counter()
             Ae = sg.Mat(*csr)
-            e = make_eps(Ae)
+            e = make_eps(Ae, args.arith)
             e.solve()
             x = np.empty(n)
             for i in range(wl["nev"]):
@@ -667,51 +770,54 @@ def main():
         e2e = {"value": world * args.steps * wl["nev"] / e2e_t, "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h}
 
-    # roofline: one profiled solve
-    eps.setProfiling(True)
-    eps.solve()
-    prof = eps.getProfile()
-    eps.setProfiling(False)
-    peak, peak_kind = measured_peaks()
-    top = max(("gs_dot", "gs_update", "spmv", "restart"), key=lambda k: prof[k][0])
-    ms_k, by_k, nl_k = prof[top]
-    achieved = by_k / (ms_k / 1000.0) / 1e9 if ms_k > 0 else None
-    tr = (committed_traffic(args.workload) or {}).get(top)
-    traffic = tr * by_k / nl_k if (tr and nl_k) else None  # DRAM bytes per launch: ncu ratio x algorithmic bytes
-    roofline = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak if achieved else None, "peak_source": peak_kind,
-                "traffic": traffic, "algorithmic_bytes_per_launch": by_k / nl_k if nl_k else None,
-                "launches": nl_k,
-                "per_class_ms": {k: round(v[0], 3) for k, v in prof.items()},
-                "per_class_GBps": {k: (round(v[1] / (v[0] / 1000.0) / 1e9, 1) if v[0] > 0 else None)
-                                   for k, v in prof.items()}}
-    step_bytes = sum(v[1] for k, v in prof.items())
-    krylov_ms = sum(prof[k][0] for k in ("spmv", "gs_dot", "gs_update"))
-    krylov_bytes = sum(prof[k][1] for k in ("spmv", "gs_dot", "gs_update"))
-    roofline["krylov_step_GBps"] = round(krylov_bytes / (krylov_ms / 1000.0) / 1e9, 1) if krylov_ms > 0 else None
-    roofline["krylov_step_frac"] = round(roofline["krylov_step_GBps"] / peak, 4) if krylov_ms > 0 else None
-    roofline["solve_bytes"] = step_bytes
+    roofline = roofline_of(eps, args.arith)
+    stats = eps.getStats()
+
+    # the pair arithmetic beside the headline, labelled as what it is (narrower than IEEE FP64)
+    pair = None
+    if args.arith != "pair" and not args.no_pair and args.workload in ("lap3d128", "lap3d64", "lap2d100"):
+        ep = make_eps(A, "pair")
+        pr = timed(ep, max(1, min(args.steps, 2)), 1)
+        pair = {"value": pr["value"], "unit": UNIT, "arith": "pair", "dtype": ARITH_LABEL["pair"],
+                "ms_per_step": pr["total_ms"] / len(pr["dev_ms"]), "steps": len(pr["dev_ms"]),
+                "krylov_steps_per_solve": pr["steps"][-1], "restarts_per_solve": pr["restarts"][-1],
+                "nconv": pr["nconv"][-1]}
+        rp = roofline_of(ep, "pair")
+        pair["roofline"] = {k: rp[k] for k in ("kernel", "achieved", "peak", "frac", "per_class_ms",
+                                               "per_class_GBps", "krylov_step_frac")}
+        if rank == 0 and not args.no_parity:
+            pair["parity"] = parity_of(ep, csr, wl, n)
+        ep.destroy()
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(csr, wl, full_size_steps(args.workload) or steps_k[-1])
-        one = cpu_baseline(csr, wl, full_size_steps(args.workload) or steps_k[-1], budget_s=10.0, nthreads=1)
+        cpu = cpu_baseline(csr, wl, full_size_steps(args.workload) or main_run["steps"][-1])
+        one = cpu_baseline(csr, wl, full_size_steps(args.workload) or main_run["steps"][-1], budget_s=10.0,
+                           nthreads=1)
         cpu["one_thread"] = {"value": one["value"], "cores": 1, "sample": one["sample"]}
 
     if rank == 0:
-        lat_sorted = sorted(lat)
-        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": {"workload": wl["desc"], "n": n, "nnz": nnz, "arith": args.arith, "restart": args.restart,
+        lat_sorted = sorted(main_run["lat"])
+        line = {"metric": METRIC, "value": main_run["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": main_run["total_ms"] / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.arith == "f64" else args.arith,
+                "data": "synthetic",
+                "config": {"workload": wl["desc"], "n": n, "nnz": nnz, "arith": args.arith,
+                           "arith_detail": ARITH_LABEL[args.arith], "restart": args.restart,
                            "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (basis 2.2 GB)"
                            if args.workload == "lap3d128" else "small inputs",
-                           "krylov_steps_per_solve": steps_k[-1], "restarts_per_solve": restarts[-1],
-                           "precision_phase_steps": eps.getStats()["precision_steps"],
-                           "nconv": nconvs[-1]},
-                "latency_ms": {"p50": float(np.percentile(lat_sorted, 50)), "p99": float(np.percentile(lat_sorted, 99))},
-                "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches}
+                           "krylov_steps_per_solve": main_run["steps"][-1],
+                           "restarts_per_solve": main_run["restarts"][-1],
+                           "precision_phase_steps": stats["precision_steps"], "nconv": main_run["nconv"][-1]},
+                "latency_ms": {"p50": float(np.percentile(lat_sorted, 50)),
+                               "p99": float(np.percentile(lat_sorted, 99))},
+                "parity": par, "e2e": e2e, "roofline": roofline, "pair": pair, "cpu_baseline": cpu,
+                "clocks": main_run["clk"], "gpu_launches": main_run["launches"]}
         print(json.dumps(line), flush=True)
+        if par is not None and not par["ok"]:
+            print(f"parity check failed: {par}", file=sys.stderr, flush=True)
+            rep.close()
+            sys.exit(3)
     rep.close()
 
 

@@ -84,9 +84,15 @@ typedef enum { EPS_GB300_K_SPMV = 0, EPS_GB300_K_GS_DOT, EPS_GB300_K_GS_UPDATE, 
 PetscErrorCode EPSGB300SetProfiling(EPS eps, PetscBool on);
 PetscErrorCode EPSGB300GetProfile(EPS eps, EPSGB300KernelClass cls, double *ms, double *bytes, long long *launches);
 
-/* Device pointer to the basis (column-major, leading dimension *ld) after EPSSolve: columns 0..nconv-1 hold the
- * eigenvectors (Hermitian) or the Schur/eigen vectors (non-Hermitian) in solver order (see EPSGetEigenpair).  For
- * EPS_GHEP the columns are y = B^1/2 x (EPSGetEigenvector returns x). */
+/* The converged eigenvectors on the device, as IEEE doubles, without a host copy: column i (leading dimension *ld)
+ * is the vector EPSGetEigenvector(eps, i, ...) returns in Vr (for EPS_GHEP the eigenvector x itself); a complex
+ * pair listed as i, i+1 has its real part in column i and its imaginary part in column i+1, as the reference's
+ * basis after EPSComputeVectors_Schur (src/eps/interface/epsdefault.c:105-169).  The values are converted from the
+ * basis' storage format (FP32 pairs in the default arithmetic, FP32 in the precision form) into an EPS-owned FP64
+ * array on the first call after each EPSSolve; the pointer stays valid until the next EPSSolve, EPSSetUp, EPSReset
+ * or EPSDestroy.  Counterpart of EPSGetEigenvector (src/eps/interface/epssolve.c:516) for all i at once. */
+PetscErrorCode EPSGB300GetDeviceEigenvectors(EPS eps, const double **X, PetscInt *ld);
+/* The same array as EPSGB300GetDeviceEigenvectors (kept for existing callers). */
 PetscErrorCode EPSGB300GetDeviceBasis(EPS eps, const double **V, PetscInt *ld);
 
 /* Solve `count` eigenproblems together: every EPS is configured as for EPSSolve (operators, problem type,

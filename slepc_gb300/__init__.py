@@ -85,6 +85,7 @@ def load():
         "EPSGB300BatchSetTuning": ([ctypes.POINTER(I), I], I),
         "EPSGB300GetStats": ([P, P], I),
         "EPSGB300OrthogonalityError": ([P, P], I),
+        "EPSGB300GetDeviceEigenvectors": ([P, PP, P], I),
         "EPSGB300SetProfiling": ([P, I], I),
         "EPSGB300GetProfile": ([P, I, P, P, P], I),
         "EPSSetExtraction": ([P, I], I),
@@ -566,6 +567,27 @@ class EPS:
                    "EPSGB300GetProfile")
             out[name] = (ms.value, by.value, nl.value)
         return out
+
+    def getDeviceEigenvectors(self):
+        """(device address, leading dimension) of the FP64 eigenvector array (EPSGB300GetDeviceEigenvectors)."""
+        p, ld = ctypes.c_void_p(), ctypes.c_int()
+        _check(load().EPSGB300GetDeviceEigenvectors(self.handle, ctypes.byref(p), ctypes.byref(ld)),
+               "EPSGB300GetDeviceEigenvectors")
+        return p.value, ld.value
+
+    def copyDeviceEigenvectors(self):
+        """The device eigenvector array copied to the host (n x nconv), one cudaMemcpy of the columns."""
+        ptr, ld = self.getDeviceEigenvectors()
+        m = self.getConverged()
+        n = self._A.m
+        out = np.empty((m, ld))
+        if m:
+            rt = ctypes.CDLL("libcudart.so")
+            rt.cudaMemcpy.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int]
+            err = rt.cudaMemcpy(out.ctypes.data, ctypes.c_void_p(ptr), out.nbytes, 2)  # cudaMemcpyDeviceToHost
+            if err != 0:
+                raise SlepcError(err, "cudaMemcpy", "device eigenvector copy failed")
+        return np.ascontiguousarray(out[:, :n].T)
 
     def orthogonalityError(self):
         v = ctypes.c_double()

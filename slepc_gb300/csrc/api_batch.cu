@@ -330,6 +330,7 @@ PetscErrorCode ksg_engine_finish(BatchEngine &B, std::vector<std::pair<int, int>
       e->stats.restarts = fin.its;
       e->stats.kernel_launches = fin.its * B.launches_per_cycle;
       e->solved = 1;
+      e->xvec_valid = 0;
     }
     retired->push_back({i, err});
     B.eps[i] = nullptr;

@@ -635,6 +635,9 @@ static PetscErrorCode eps_free_device(EPS eps) {
   eps->work.release();
   eps->dsf.release();
   eps->seg_part.release();
+  eps->xvec.release();
+  eps->d_perm.release();
+  eps->xvec_valid = 0;
   eps->rtc.release();
   eps->part.release();
   eps->st.release();
@@ -1833,6 +1836,7 @@ extern "C" PetscErrorCode EPSSolve(EPS eps) {
   KSG_TRY(EPSSetUp(eps));
   KSG_CUDA(cudaSetDevice(eps->device));
   cudaStream_t s = eps->stream;
+  eps->xvec_valid = 0;  // the device eigenvectors of an earlier solve are stale
   auto t0 = std::chrono::steady_clock::now();
   if (!eps->ev_solve[0]) {
     KSG_CUDA(cudaEventCreate(&eps->ev_solve[0]));
@@ -2116,12 +2120,65 @@ extern "C" PetscErrorCode EPSGB300GetStats(EPS eps, EPSGB300Stats *stats) {
   return 0;
 }
 
-extern "C" PetscErrorCode EPSGB300GetDeviceBasis(EPS eps, const double **V, PetscInt *ld) {
-  KSG_CHECK(eps && V && ld, PETSC_ERR_ARG_NULL, "Null argument");
-  KSG_CHECK(eps->setup, PETSC_ERR_ORDER, "Must call EPSSetUp() first");
-  *V = eps->V.p;
-  *ld = (PetscInt)eps->ldv;
+// Column i of X = the real eigenvector of pair i as EPSGetEigenvector(i) returns it; for a complex pair listed as
+// i, i+1 the real part and the imaginary part (of the eigenvalue with positive imaginary part) in columns i and i+1,
+// the layout of the reference's basis after EPSComputeVectors_Schur (epsdefault.c:105-169).  Values are converted
+// to IEEE doubles from the basis' storage format and, for EPS_GHEP, mapped back from y = D^1/2 x.
+__global__ void k_gather_eigvecs(const void *V, long long ldv, int storage, const int *cols, const double *bisqrt,
+                                 int n, int nconv, double *X, long long ldx) {
+  const int i = blockIdx.y;
+  if (i >= nconv) return;
+  const size_t k = (size_t)cols[i];
+  for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long long)gridDim.x * blockDim.x) {
+    double v;
+    if (storage == STORE_F64) v = static_cast<const double *>(V)[r + k * ldv];
+    else if (storage == STORE_F32) v = (double)static_cast<const float *>(V)[r + k * ldv];
+    else {
+      const float2 p = static_cast<const float2 *>(V)[r + k * ldv];
+      v = (double)p.x + (double)p.y;
+    }
+    if (bisqrt) v *= bisqrt[r];
+    X[r + (size_t)i * ldx] = v;
+  }
+}
+
+// the device-side counterpart of EPSGetEigenvector for every converged pair at once
+extern "C" PetscErrorCode EPSGB300GetDeviceEigenvectors(EPS eps, const double **X, PetscInt *ld) {
+  KSG_CHECK(eps && X && ld, PETSC_ERR_ARG_NULL, "Null argument");
+  KSG_CHECK(eps->solved, PETSC_ERR_ORDER, "Must call EPSSolve() first");
+  const int n = eps->n, m = eps->nconv;
+  const long long ldx = ((long long)n + 63) / 64 * 64;
+  if (!eps->xvec_valid) {
+    KSG_CUDA(cudaSetDevice(eps->device));
+    if (m > 0) {
+      if (eps->xvec.count < (size_t)ldx * m) KSG_CUDA(eps->xvec.alloc((size_t)ldx * m));
+      if (eps->d_perm.count < (size_t)m) KSG_CUDA(eps->d_perm.alloc(m));
+      std::vector<int> cols(m);
+      for (int i = 0; i < m; ++i) {
+        const int k = eps->perm[i];
+        cols[i] = k;
+        // the second of a complex pair follows its first: column k holds the imaginary part; a conjugate listed
+        // without its partner just before it gives its real part, column k - 1
+        if (eps->r_eigi[k] < 0.0 && !(i > 0 && eps->perm[i - 1] == k - 1)) cols[i] = k - 1;
+      }
+      KSG_CUDA(cudaMemcpyAsync(eps->d_perm.p, cols.data(), sizeof(int) * m, cudaMemcpyHostToDevice, eps->stream));
+      const double *bis = (eps->B && eps->problem == EPS_GHEP) ? eps->d_bisqrt.p : nullptr;
+      dim3 grid((unsigned)std::min<long long>((n + 255) / 256, 1024), (unsigned)m);
+      k_gather_eigvecs<<<grid, 256, 0, eps->stream>>>(eps->V.p, eps->ldv, eps->storage, eps->d_perm.p, bis, n, m,
+                                                      eps->xvec.p, ldx);
+      KSG_CUDA(cudaGetLastError());
+      KSG_CUDA(cudaStreamSynchronize(eps->stream));
+    }
+    eps->xvec_valid = 1;
+  }
+  *X = eps->xvec.p;
+  *ld = (PetscInt)ldx;
   return 0;
+}
+
+// kept for existing callers: the same FP64 eigenvector array as EPSGB300GetDeviceEigenvectors
+extern "C" PetscErrorCode EPSGB300GetDeviceBasis(EPS eps, const double **V, PetscInt *ld) {
+  return EPSGB300GetDeviceEigenvectors(eps, V, ld);
 }
 
 // ||V^T V - I||_max over the first nconv columns (solver order), with the GS_DOTS kernel in the EPS arithmetic

@@ -188,6 +188,9 @@ struct _p_EPS {
   cudaStream_t stream = nullptr;
   DBuf<double> V, d, e, H, Q, X, eigr, eigi, errest, coef, work, dsf;
   DBuf<double> seg_part;  // one 8-byte partial per long-row segment of the operator
+  DBuf<double> xvec;      // EPSGB300GetDeviceEigenvectors: FP64 eigenvectors in EPSGetEigenpair order
+  DBuf<int> d_perm;       // its column map
+  int xvec_valid = 0;     // xvec holds the current solve's vectors
   DBuf<unsigned char> rtc;  // slices of Q for the tensor-core restart
   DBuf<float2> part;
   int pstride = 0;

@@ -1,5 +1,5 @@
-"""Regenerate reference_outputs.json from the reference's expected-output files (run in the build container only;
-other machines use the committed JSON).  Only the printed eigenvalues/norms of the Krylov-Schur-path tests are
+"""Regenerate reference_outputs.json from the reference's expected-output files (run with SLEPC_REFERENCE set to a SLEPc
+source tree; other machines use the committed JSON).  Only the printed eigenvalues/norms of the Krylov-Schur-path tests are
 extracted, with the lines EPSErrorView printed; each entry records the file it came from and the options of that
 test.  The real matrix those tests read from a PETSc binary file (share/slepc/datafiles/matrices/rdb200.petsc)
 is converted to CSR arrays in rdb200.npz by an independent big-endian reader, as are bfw62a/bfw62b (ex7.c)."""
@@ -9,7 +9,9 @@ import re
 
 import numpy as np
 
-REF = os.environ.get("SLEPC_REFERENCE", "/root/reference")
+REF = os.environ.get("SLEPC_REFERENCE", "")
+if not REF:
+    raise SystemExit("set SLEPC_REFERENCE to the root of the SLEPc 3.22 source tree")
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_outputs.json")
 
 

@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 import slepc_gb300 as sg
-from slepc_gb300 import matgen
+from slepc_gb300 import matgen, verify
 
 pytestmark = pytest.mark.gpu
 
@@ -117,12 +117,10 @@ def test_batch_parity_with_oracle(lib, orc):
         refv = np.asarray(ref.eigr[:ref.nconv]) + 1j * np.asarray(ref.eigi[:ref.nconv])
         for v in vals[:nev]:
             assert np.min(np.abs(refv - v)) / abs(v) <= 1e-10
-        A = sg.Mat(*csr)
-        nrm = max(np.add.reduceat(np.abs(csr[2]), csr[0][:-1]))
-        for v, x in zip(vals, vecs):
-            if isinstance(v, complex):
-                continue
-            assert np.linalg.norm(A.mult(x) - v * x) / (nrm * abs(v)) <= tol
+        real = [(v, x) for v, x in zip(vals, vecs) if not isinstance(v, complex)]
+        if real:  # host check: scipy.sparse on the CSR arrays
+            r_a, _ = verify.residuals(csr, [v for v, _ in real], np.stack([x for _, x in real], axis=1))
+            assert r_a.max() <= tol
 
 
 def test_batch_zero_start_vector_error(lib):
@@ -149,10 +147,8 @@ def test_batch_precision_form(lib):
         dense = np.linalg.eigvalsh(matgen.csr_to_dense(*p[0]))
         for v in vals[:p[3]]:
             assert np.min(np.abs(dense - v)) / abs(v) <= 1e-10
-        A = sg.Mat(*p[0])
-        nrm = max(np.add.reduceat(np.abs(p[0][2]), p[0][0][:-1]))
-        for v, x in zip(vals, vecs):
-            assert np.linalg.norm(A.mult(x) - v * x) / (nrm * abs(v)) <= 1e-10
+        r_a, _ = verify.residuals(p[0], list(vals), np.stack(vecs, axis=1))  # host, scipy.sparse
+        assert r_a.max() <= 1e-10
     for e in eps[:2]:
         st = e.getStats()
         assert 0 < st["precision_steps"] < st["krylov_steps"]

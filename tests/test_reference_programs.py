@@ -1,7 +1,7 @@
 """The reference's own EPS programs compile and link unchanged against include/ and libslepc_gb300.so.
 
-Where the reference tree is present (environment variable SLEPC_REFERENCE, default /root/reference), each program is
-compiled in place from its source with gcc -Wall -Werror and linked against the library; nothing is copied.  Run
+Where the reference tree is given (environment variable SLEPC_REFERENCE, the root of a SLEPc 3.22 source tree; the
+tests skip when it is unset), each program is compiled in place from its source with gcc -Wall -Werror and linked against the library; nothing is copied.  Run
 without a GPU, a program builds its matrices and options and then stops at EPSSolve with PETSC_ERR_GPU (97) and the
 CUDA error: there is no CPU fallback.  With a GPU it solves."""
 import os
@@ -13,7 +13,7 @@ import pytest
 import slepc_gb300 as sg
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = os.environ.get("SLEPC_REFERENCE", "/root/reference")
+REF = os.environ.get("SLEPC_REFERENCE", "")
 PROGRAMS = ["tutorials/ex1", "tutorials/ex2", "tutorials/ex4", "tutorials/ex5", "tutorials/ex7", "tutorials/ex11",
             "tutorials/ex13", "tutorials/ex44", "tests/test1", "tests/test2", "tests/test3", "tests/test4",
             "tests/test6", "tests/test10", "tests/test14", "tests/test18", "tests/test19", "tests/test20",
@@ -22,8 +22,8 @@ PROGRAMS = ["tutorials/ex1", "tutorials/ex2", "tutorials/ex4", "tutorials/ex5", 
 RUN_TO_SOLVE = ["tutorials/ex1", "tutorials/ex13", "tutorials/ex44", "tests/test27", "tests/test28", "tests/test3",
                 "tests/test42"]
 
-pytestmark = pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "src", "eps")) or not shutil.which("gcc"),
-                                reason="the reference's sources or gcc are not available here")
+pytestmark = pytest.mark.skipif(not REF or not os.path.isdir(os.path.join(REF, "src", "eps")) or not shutil.which("gcc"),
+                                reason="SLEPC_REFERENCE (a SLEPc source tree) is unset, or gcc is missing")
 
 
 @pytest.fixture(scope="module")
