@@ -73,6 +73,8 @@ typedef struct {
   double solve_device_ms;    /* EPSSolve measured with CUDA events on the EPS stream */
   long long precision_steps;    /* EPS_GB300_ARITH_F32: Krylov steps of the FP32-storage phase (included above) */
   long long precision_restarts; /* EPS_GB300_ARITH_F32: restarts of the FP32-storage phase */
+  long long ds_fallbacks;       /* restarts whose mixed-precision projected solve failed its accuracy check and was
+                                   redone by the FP64 QR solver */
 } EPSGB300Stats;
 PetscErrorCode EPSGB300GetStats(EPS eps, EPSGB300Stats *stats);
 

@@ -547,11 +547,11 @@ class EPS:
         solve_s, bytes_moved, setup_s = np.frombuffer(bytes(buf[16:40]), dtype=np.float64)
         launches = np.frombuffer(bytes(buf[40:48]), dtype=np.int64)[0]
         dev_ms = np.frombuffer(bytes(buf[48:56]), dtype=np.float64)[0]
-        psteps, prestarts = np.frombuffer(bytes(buf[56:72]), dtype=np.int64)
+        psteps, prestarts, dsfb = np.frombuffer(bytes(buf[56:80]), dtype=np.int64)
         return {"krylov_steps": int(steps), "restarts": int(restarts), "solve_seconds": float(solve_s),
                 "bytes_moved": float(bytes_moved), "setup_seconds": float(setup_s), "kernel_launches": int(launches),
                 "solve_device_ms": float(dev_ms), "precision_steps": int(psteps),
-                "precision_restarts": int(prestarts)}
+                "precision_restarts": int(prestarts), "ds_fallbacks": int(dsfb)}
 
     KERNEL_CLASSES = ("spmv", "gs_dot", "gs_update", "restart", "ds")
 

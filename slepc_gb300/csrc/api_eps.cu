@@ -1609,22 +1609,25 @@ PetscErrorCode ksg_eps_assemble(EPS eps, int nconv, const double *er, const doub
   return 0;
 }
 
-// V(:, s0:s0+N) = V(:, a0:a0+K) Q(a0:a0+K, s0:s0+N): the tensor-core restart for pair storage (default), the
-// pair-arithmetic CUDA-core kernel otherwise
+// V(:, s0:s0+N) = V(:, a0:a0+K) Q(a0:a0+K, s0:s0+N): the tensor-core restart for pair storage and (tcgen05) for FP64
+// storage, the CUDA-core kernel of the storage's arithmetic otherwise
 // the tensor-core kernel of EPS_GB300_RESTART_TENSOR: tcgen05 (bit-identical to mma.sync; the 128^3 Laplacian's
 // restarts take 417 ms per solve against 782 ms)
 static const bool kRestartTensorIsTcgen05 = true;
 
 static cudaError_t eps_restart(EPS eps, int a0, int K, int s0, int N, const double *Q, cudaStream_t s) {
   const int m = eps->restart_method;
-  if (eps->storage == STORE_PAIR && m != EPS_GB300_RESTART_PAIR) {
-    if (m == EPS_GB300_RESTART_TCGEN05 || (m == EPS_GB300_RESTART_TENSOR && kRestartTensorIsTcgen05)) {
+  const bool t5 = m == EPS_GB300_RESTART_TCGEN05 || (m == EPS_GB300_RESTART_TENSOR && kRestartTensorIsTcgen05);
+  if ((eps->storage == STORE_PAIR && m != EPS_GB300_RESTART_PAIR) || (eps->storage == STORE_F64 && t5)) {
+    if (t5) {
       const size_t need = restart_t5_scratch_bytes(eps->ld);  // about 2 KB per SM and basis column
       if (eps->rtc.count < need) {
         cudaError_t e = eps->rtc.alloc(need);
         if (e == cudaSuccess) e = cudaMemsetAsync(eps->rtc.p, 0, need, s);
         if (e != cudaSuccess) return e;
       }
+      if (eps->storage == STORE_F64)
+        return launch_restart_t5_f64(eps->V.p, eps->ldv, eps->n, a0, K, s0, N, Q, eps->ld, eps->rtc.p, eps->ld, s);
       return launch_restart_t5(reinterpret_cast<float2 *>(eps->V.p), eps->ldv, eps->n, a0, K, s0, N, Q, eps->ld,
                                eps->rtc.p, eps->ld, s);
     }
@@ -1740,6 +1743,7 @@ static PetscErrorCode eps_solve_core(EPS eps, double tol, std::chrono::steady_cl
     prof_collect(eps);
     const KSControl c = *eps->h_ctl;
     KSG_CHECK(!c.ds_error, PETSC_ERR_LIB, "The projected eigenproblem solver did not converge (restart %d)", its);
+    if (herm && eps->ds_method == EPS_GB300_DS_REFINED && c.ds_fallback) eps->stats.ds_fallbacks++;
     const int k = c.nconv;
     l = c.l;
     reason = c.reason;
@@ -1845,6 +1849,7 @@ extern "C" PetscErrorCode EPSSolve(EPS eps) {
   KSG_CUDA(cudaEventRecord(eps->ev_solve[0], s));
   eps->stats.krylov_steps = 0;
   eps->stats.restarts = 0;
+  eps->stats.ds_fallbacks = 0;
   eps->stats.bytes_moved = 0.0;
   eps->stats.kernel_launches = 0;
   eps->stats.precision_steps = 0;

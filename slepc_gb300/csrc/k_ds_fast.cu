@@ -19,6 +19,11 @@
 //   3. a final cluster pass, one Newton-Schulz step X (3I - X^T X) / 2 that makes X orthogonal to rounding, and the
 //      sort by criterion, extra row, convergence test and restart control (k_dsf_finish, the same contract as the
 //      FP64 kernel in k_ds_hep.cu).
+//   4. an accuracy check before the final cluster pass: outside the clusters every off-diagonal entry of X^T T X must
+//      be at rounding level of ||T||, and X^T X at rounding level of I.  Pairs whose gap is just above the cluster
+//      threshold can stay mixed after the refinement steps (measured on the 128^3 Laplacian: pairs 1.7e-4 apart at
+//      |lambda| ~ 12 left residuals of 1e-7); when the check fails, the FP64 QR solver of k_ds_hep.cu solves the
+//      projected problem again from the untouched compact form, so every restart gets FP64-accurate Ritz pairs.
 #include <float.h>
 
 #include "common.cuh"
@@ -33,6 +38,7 @@ constexpr int DSF_CL = 16;     // largest cluster diagonalised as one block (lon
 constexpr int DSF_TILE = 16;   // output tile of the small FP64 products
 constexpr int DSF_ITERS = 4;   // refinement steps
 constexpr double DSF_TAU = 1e-5;
+constexpr double DSF_CHECK = 1024.0;  // accuracy check: |s_ij| <= 1024 eps ||T||_F outside clusters, |G - I| <= 1024 eps
 
 size_t ds_fast_scratch_doubles(int ld) {
   const int nt = (ld + DSF_TILE - 1) / DSF_TILE;
@@ -53,6 +59,7 @@ DSFArgs ds_fast_layout(double *scratch, int ld) {
   f.lam = f.W + (size_t)2 * ld * DSF_CL;
   f.part = f.lam + ld;
   f.scal = f.part + 2 * (size_t)nt * nt;
+  f.fallback = reinterpret_cast<int *>(f.scal + 4);
   return f;
 }
 
@@ -69,6 +76,7 @@ KS_DEVICE long long dsf_order_key(double x) {
 // rows i and k when i < k (arrow, raw form) and between rows i and i+1 otherwise.
 __global__ void k_dsf_build(DSFArgs f) {
   const int m = dsf_active(f), l = f.l, k = f.k, ld = f.ld;
+  if (blockIdx.x == 0 && threadIdx.x == 0) *f.fallback = 0;
   for (int idx = threadIdx.x + blockIdx.x * blockDim.x; idx < m * m; idx += blockDim.x * gridDim.x) {
     const int i = idx % m, j = idx / m;
     const int gi = i + l, gj = j + l;
@@ -356,9 +364,9 @@ KS_DEVICE void dsf_jacobi(int len, double *A, double *W, int lda) {
 // The scalar part of one refinement step (one block): lambda, delta, the threshold, clusters and their rotations.
 __global__ void __launch_bounds__(DSF_THREADS, 1) k_dsf_step(DSFArgs f, int final_pass) {
   __shared__ double lam[DSF_MAXN], red[DSF_THREADS / 32][4];
-  __shared__ int by_rank[DSF_MAXN], close_next[DSF_MAXN], cl_start[DSF_MAXN], cl_len[DSF_MAXN];
+  __shared__ int by_rank[DSF_MAXN], close_next[DSF_MAXN], cl_start[DSF_MAXN], cl_len[DSF_MAXN], cl_of[DSF_MAXN];
   __shared__ int s_ncl;
-  __shared__ double s_tau;
+  __shared__ double s_tau, s_tnorm;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int m = dsf_active(f), ld = f.ld, l = f.l;
   double *S = f.S, *G = f.G, *X = f.X;
@@ -399,6 +407,7 @@ __global__ void __launch_bounds__(DSF_THREADS, 1) k_dsf_step(DSFArgs f, int fina
     }
     const double tau = DSF_TAU * bm;
     s_tau = tau;
+    s_tnorm = sqrt(b2);
     const double delta = 2.0 * (sqrt(b0) + sqrt(b2) * sqrt(b1));
     if (!final_pass) f.scal[0] = fmax(delta, tau);
   }
@@ -419,6 +428,38 @@ __global__ void __launch_bounds__(DSF_THREADS, 1) k_dsf_step(DSFArgs f, int fina
   }
   __syncthreads();
   const int ncl = s_ncl;
+  if (final_pass) {
+    // Accuracy check of the refined pairs: outside the clusters (diagonalised next by FP64 Jacobi) every
+    // off-diagonal entry of S = X^T T X must be at rounding level of ||T||, and G = X^T X at rounding level of I.
+    // A pair whose gap is too small for the refinement to converge in DSF_ITERS steps stays mixed and fails here;
+    // the FP64 QR solver (k_ds_hep) then redoes the whole projected problem.
+    for (int i = tid; i < m; i += DSF_THREADS) cl_of[i] = -1;
+    __syncthreads();
+    for (int c = 0; c < ncl; ++c)
+      for (int q = tid; q < cl_len[c]; q += DSF_THREADS) cl_of[by_rank[cl_start[c] + q]] = c;
+    __syncthreads();
+    double ms = 0.0, mg = 0.0;
+    for (int idx = tid; idx < m * m; idx += DSF_THREADS) {
+      const int i = idx % m, j = idx / m;
+      const double g = G[i + (size_t)j * ld] - (i == j ? 1.0 : 0.0);
+      mg = fmax(mg, fabs(g));
+      if (i != j && !(cl_of[i] >= 0 && cl_of[i] == cl_of[j])) ms = fmax(ms, fabs(S[i + (size_t)j * ld]));
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+      ms = fmax(ms, __shfl_down_sync(0xffffffffu, ms, off));
+      mg = fmax(mg, __shfl_down_sync(0xffffffffu, mg, off));
+    }
+    if (lane == 0) { red[warp][0] = ms; red[warp][1] = mg; }
+    __syncthreads();
+    if (tid == 0) {
+      double bs = 0.0, bg = 0.0;
+      for (int w = 0; w < DSF_THREADS / 32; ++w) { bs = fmax(bs, red[w][0]); bg = fmax(bg, red[w][1]); }
+      const int bad = !(bs <= DSF_CHECK * DBL_EPSILON * s_tnorm) || !(bg <= DSF_CHECK * DBL_EPSILON);
+      *f.fallback = bad;
+      f.ctl->ds_fallback = bad;
+    }
+    __syncthreads();
+  }
   if (ncl > 0) {
     // one thread per cluster: Jacobi on the symmetrised block of S; W and the block copy live in f.W, indexed
     // by rank (rows s0 .. s0+len-1 of an ld x DSF_CL array), so clusters never overlap
@@ -491,6 +532,7 @@ __global__ void __launch_bounds__(DSF_THREADS, 1) k_dsf_step(DSFArgs f, int fina
 // Sort by the criterion, write Q (identity on the locked block), d, the extra row, the error estimates and the
 // restart control record (the tail of EPSSolve_KrylovSchur_Default for the symmetric case, krylovschur.c:270-322).
 __global__ void __launch_bounds__(DSF_THREADS, 1) k_dsf_finish(DSFArgs f, DSArgs a) {
+  if (*f.fallback) return;  // the FP64 QR solver redoes this projected problem (launched next)
   __shared__ double lam[DSF_MAXN], serr[DSF_MAXN];
   __shared__ long long k_crit[DSF_MAXN], k_asc[DSF_MAXN];
   __shared__ int perm[DSF_MAXN];
@@ -575,7 +617,7 @@ __global__ void __launch_bounds__(DSF_THREADS, 1) k_dsf_finish(DSFArgs f, DSArgs
   }
 }
 
-int ds_fast_launches() { return 2 + 3 * (DSF_ITERS + 1) + DSF_ITERS + 3; }
+int ds_fast_launches() { return 2 + 3 * (DSF_ITERS + 1) + DSF_ITERS + 4; }
 
 cudaError_t launch_ds_hep_fast(const DSArgs &a, const DSFArgs &f0, int n_max, cudaStream_t s) {
   if (n_max > DSF_MAXN || f0.ld < n_max || a.ld != f0.ld || !a.st || !a.ctl) return cudaErrorInvalidValue;
@@ -612,7 +654,10 @@ cudaError_t launch_ds_hep_fast(const DSArgs &a, const DSFArgs &f0, int n_max, cu
   k_dsf_mm<DSF_MM_NS><<<grid, 256, 0, s>>>(f, f.X, f.G, f.P, nullptr);
   { double *t = f.X; f.X = f.P; f.P = t; }
   k_dsf_finish<<<1, DSF_THREADS, 0, s>>>(f, a);
-  return cudaGetLastError();
+  // the fallback: the reference's FP64 algorithm on the untouched compact form, only when the check failed
+  DSArgs q = a;
+  q.run_if = f.fallback;
+  return launch_ds_hep(q, n_max, s);
 }
 
 }  // namespace ksg

@@ -16,6 +16,8 @@
 // FP64 pipe in the main kernel.
 #include <cuda_bf16.h>
 
+#include <type_traits>
+
 #include "common.cuh"
 #include "kernels.h"
 #include "ks_types.h"
@@ -23,7 +25,8 @@
 namespace ksg {
 
 constexpr int OZ_SA = 8;         // slices of V (56 bits)
-constexpr int OZ_S = 7;          // slices of Q (49 bits)
+constexpr int OZ_S = 7;          // slices of Q (49 bits) for pair storage and for FP64 storage with K > 128
+constexpr int OZ_QMAX = 8;       // slices of Q (56 bits) for FP64 storage with K <= 128; the scratch holds 8
 constexpr int OZ_L = 8;          // levels s + t kept
 constexpr int OZ_ROWS = 64;      // rows of V per tile
 constexpr int OZ_THREADS = 256;  // 8 warps: 4 row groups of 16 x 2 column halves of a chunk
@@ -34,7 +37,7 @@ constexpr int OZ_PADA = 2;       // bf16 padding per row of the V slices: an odd
 
 size_t restart_tc_scratch_bytes(int ld) {
   const int kp = (ld + 15) / 16 * 16, np = (ld + OZ_NC - 1) / OZ_NC * OZ_NC;
-  return (size_t)OZ_S * np * kp * sizeof(__nv_bfloat16) + (size_t)np * sizeof(int) + 256;
+  return (size_t)OZ_QMAX * np * kp * sizeof(__nv_bfloat16) + (size_t)np * sizeof(int) + 256;
 }
 
 static size_t oz_smem_bytes(int kp) {
@@ -43,11 +46,12 @@ static size_t oz_smem_bytes(int kp) {
          OZ_ROWS * sizeof(int) + 16;
 }
 
-// Column exponents and slices of Q(a0 + k, s0 + c), k < K, c < N (zero-padded to kp x np): one block per column.
+// Column exponents and qs slices of Q(a0 + k, s0 + c), k < K, c < N (zero-padded to kp x np): one block per column.
+// q / 2^f is rounded to a 7 qs-bit fixed point and cut into 7-bit slices, most significant first.
 // Layout of slice t: [c][k] (cm = 0, the mma.sync kernel), or K-major core matrices [k/8][c/8][c%8][k%8] (cm = 1, the
 // tcgen05 kernel: the 8-column groups of one k-group are contiguous, so a stage is a few bulk copies).
 __global__ void k_oz_qslice(const double *__restrict__ Q, int ldq, int a0, int s0, int K, int N, int kp, int np,
-                            __nv_bfloat16 *__restrict__ B, int *__restrict__ fcol, int cmlayout) {
+                            __nv_bfloat16 *__restrict__ B, int *__restrict__ fcol, int cmlayout, int qs) {
   __shared__ double red[32];
   const int c = blockIdx.x;
   const bool col_ok = c < N;
@@ -66,14 +70,15 @@ __global__ void k_oz_qslice(const double *__restrict__ Q, int ldq, int a0, int s
   const double cm = red[0];
   const int f = (cm > 0.0) ? ilogb(cm) + 1 : 0;  // |q| / 2^f < 1
   if (threadIdx.x == 0) fcol[c] = f;
+  const int bits = 7 * qs;
   for (int k = threadIdx.x; k < kp; k += blockDim.x) {
     long long y = 0;
-    if (col_ok && k < K) y = __double2ll_rn(scalbn(Q[(a0 + k) + (size_t)(s0 + c) * ldq], 49 - f));
+    if (col_ok && k < K) y = __double2ll_rn(scalbn(Q[(a0 + k) + (size_t)(s0 + c) * ldq], bits - f));
     const bool neg = y < 0;
     const unsigned long long a = neg ? (unsigned long long)(-y) : (unsigned long long)y;
-    for (int t = 0; t < OZ_S; ++t) {
-      // 7-bit slices; only the top one may reach 128 (when |q| 2^(49-f) rounds up to 2^49)
-      const int sl = (int)((a >> (42 - 7 * t)) & (t == 0 ? 255ull : 127ull));
+    for (int t = 0; t < qs; ++t) {
+      // 7-bit slices; only the top one may reach 128 (when |q| 2^(bits-f) rounds up to 2^bits)
+      const int sl = (int)((a >> (bits - 7 - 7 * t)) & (t == 0 ? 255ull : 127ull));
       const size_t at = cmlayout ? (((size_t)t * (kp / 8) + k / 8) * (np / 8) + c / 8) * 64 + (c % 8) * 8 + (k % 8)
                            : ((size_t)t * np + c) * kp + k;
       B[at] = __float2bfloat16_rn(neg ? -(float)sl : (float)sl);
@@ -248,7 +253,7 @@ constexpr int T5_KC = 32;                                  // K per shared-memor
 constexpr int T5_THREADS = 512;                            // 16 warps: 4 lane quarters x 4 column groups
 constexpr int T5_ASL = T5_M * T5_KC * 2;                   // bytes of one V slice in a stage
 constexpr int T5_BSL = T5_NC * T5_KC * 2;                  // bytes of one Q slice in a stage
-constexpr int T5_STAGE = OZ_SA * T5_ASL + OZ_S * T5_BSL;   // 94208
+constexpr int T5_STAGE = OZ_SA * T5_ASL + OZ_QMAX * T5_BSL;  // 98304
 constexpr uint32_t T5_TMEM_COLS = OZ_L * T5_NC;            // 512
 constexpr size_t T5_SMEM = 2 * (size_t)T5_STAGE + (T5_THREADS / T5_M + 1) * T5_M * sizeof(int) +
                            5 * sizeof(unsigned long long) + 16;
@@ -339,10 +344,47 @@ KS_DEVICE void t5_bulk(void *dst, const void *src, uint32_t bytes, unsigned long
       : "memory");
 }
 
+// 2^k as a double (bit construction in the normal range)
+KS_DEVICE double t5_pow2(int k) {
+  if (k >= -1022 && k <= 1023) return __longlong_as_double((long long)(1023 + k) << 52);
+  return ldexp(1.0, k);
+}
+
+// Basis storage of the tcgen05 restart.  T5Pair: FP32 pairs (hi, lo); the row exponent comes from hi, the fixed
+// point is the sum of both parts', and the result is written back as a pair.  T5F64: IEEE doubles; the fixed point
+// holds the 53-bit significand (truncated only below 2^-56 of the row maximum), and the result is the exact level
+// sum rounded once to a double.  Both keep 8 bytes per entry, so the V tile and its copies are the same.
+struct T5Pair {
+  using T = float2;
+  static KS_DEVICE int expo(float2 v) { return (int)((__float_as_uint(v.x) >> 23) & 0xFFu); }
+  static KS_DEVICE int escale(int E) { return E - 126; }  // 2^(E-127) <= |hi| < 2^(E-126)
+  static KS_DEVICE long long fix56(float2 v, int e) { return oz_fix56(v.x, e) + oz_fix56(v.y, e); }
+};
+struct T5F64 {
+  using T = double;
+  static KS_DEVICE int expo(double v) { return (int)((__double_as_longlong(v) >> 52) & 0x7FF); }
+  static KS_DEVICE int escale(int E) { return E - 1022; }  // 2^(E-1023) <= |v| < 2^(E-1022)
+  // signed 56-bit fixed point of v * 2^(56 - e), |v| < 2^e (so the shift is at most 3); zero for zeros and
+  // subnormals, truncated toward zero below 2^-56 of the row maximum
+  static KS_DEVICE long long fix56(double v, int e) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+    const int E = (int)((u >> 52) & 0x7FF);
+    if (E == 0) return 0;
+    const long long m = (long long)((u & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull);
+    const int sh = (E - 1075) + 56 - e;
+    long long r;
+    if (sh >= 0) r = sh <= 3 ? (m << sh) : 0;
+    else r = sh > -60 ? (m >> (-sh)) : 0;
+    return (u >> 63) ? -r : r;
+  }
+};
+
+template <class S, int QS>
 __global__ void __launch_bounds__(T5_THREADS, 1)
-    k_restart_t5(float2 *__restrict__ V, long long ldv, int n, int a0, int K, int s0, int N, int kp, int np,
+    k_restart_t5(typename S::T *__restrict__ V, long long ldv, int n, int a0, int K, int s0, int N, int kp, int np,
                  const __nv_bfloat16 *__restrict__ Bsl, const int *__restrict__ fcol, __nv_bfloat16 *__restrict__ Ascr,
                  int *__restrict__ err) {
+  using T = typename S::T;
   extern __shared__ __align__(1024) unsigned char sm[];
   int *erow = reinterpret_cast<int *>(sm + 2 * T5_STAGE);
   int *etmp = erow + T5_M;  // (T5_THREADS / T5_M - 1) x 128 partial maxima
@@ -382,7 +424,7 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
   // The V tile (K columns of up to 128 rows, [k][128] float2, at most 144 KB) is loaded by bulk copies into the
   // stage region, which is free until the tile's slices exist.  The rows are rounded up to even (16-byte copies):
   // the extra row is inside the basis' row padding (the leading dimension is a multiple of 64).
-  const float2 *vt = reinterpret_cast<const float2 *>(sm);
+  const T *vt = reinterpret_cast<const T *>(sm);
   uint32_t vph = 0;
   int vpend = 0;  // thread 0: a V tile load it issued has not been waited for
   auto issue_v = [&](int tl) {  // thread 0
@@ -410,7 +452,7 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
       const int m = tid & (T5_M - 1), h = tid >> 7;
       int E = 0;
       if (m < rows)
-        for (int k = h; k < K; k += H) E = max(E, (int)((__float_as_uint(vt[(size_t)k * T5_M + m].x) >> 23) & 0xFFu));
+        for (int k = h; k < K; k += H) E = max(E, S::expo(vt[(size_t)k * T5_M + m]));
       if (h) etmp[(h - 1) * T5_M + m] = E;
       __syncthreads();
       if (!h) {
@@ -423,7 +465,7 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
     // 2. all slices of the tile into the scratch, one core-matrix row (8 consecutive k of one row) per item, two
     //    items per pass
     for (int it0 = tid; it0 < T5_M * nk8; it0 += 2 * T5_THREADS) {
-      float2 v[2][8];
+      T v[2][8];
 #pragma unroll
       for (int p2 = 0; p2 < 2; ++p2) {
         const int it = it0 + p2 * T5_THREADS;
@@ -431,7 +473,7 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
           const int k = 8 * k8 + j;
-          v[p2][j] = (it < T5_M * nk8 && m < rows && k < K) ? vt[(size_t)k * T5_M + m] : make_float2(0.0f, 0.0f);
+          v[p2][j] = (it < T5_M * nk8 && m < rows && k < K) ? vt[(size_t)k * T5_M + m] : T{};
         }
       }
 #pragma unroll
@@ -444,7 +486,7 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
           long long x = 0;
-          if (er) x = oz_fix56(v[p2][j].x, er - 126) + oz_fix56(v[p2][j].y, er - 126);
+          if (er) x = S::fix56(v[p2][j], S::escale(er));
           ng[j] = x < 0 ? 1u : 0u;
           const unsigned long long a = x < 0 ? (unsigned long long)(-x) : (unsigned long long)x;
           mh[j] = (uint32_t)(a >> 32);
@@ -488,10 +530,10 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
           const int sk8 = min(T5_KC / 8, nk8 - kc8);
           unsigned char *st = sm + b * T5_STAGE;
           const uint32_t abytes = sk8 * 16 * 128, bbytes = (nch / 8) * 128;
-          t5_expect_tx(&full[b], OZ_SA * abytes + OZ_S * sk8 * bbytes);
+          t5_expect_tx(&full[b], OZ_SA * abytes + QS * sk8 * bbytes);
           for (int sl = 0; sl < OZ_SA; ++sl)
             t5_bulk(st + sl * T5_ASL, As + ((size_t)sl * nk8 + kc8) * 16 * 64, abytes, &full[b]);
-          for (int t = 0; t < OZ_S; ++t)
+          for (int t = 0; t < QS; ++t)
             for (int k8 = 0; k8 < sk8; ++k8)
               t5_bulk(st + OZ_SA * T5_ASL + t * T5_BSL + k8 * (T5_NC / 8) * 128,
                       Bsl + (((size_t)t * nk8 + kc8 + k8) * (np / 8) + c0 / 8) * 64, bbytes, &full[b]);
@@ -519,7 +561,7 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
 #pragma unroll
             for (int sa = 0; sa < OZ_SA; ++sa)
 #pragma unroll
-              for (int tb = 0; tb < OZ_S; ++tb) {
+              for (int tb = 0; tb < QS; ++tb) {
                 if (sa + tb >= OZ_L) continue;
                 const int L = sa + tb;
                 const uint64_t ad = ad0 + (uint64_t)((sa * T5_ASL + j * 2 * (16 * 128)) >> 4);
@@ -559,32 +601,65 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
       if (col < nch) {  // warp-uniform
         const int m = 32 * qd + lane;
         const int er = erow[m];
-        float sh[16], sl[16];
+        if constexpr (std::is_same<S, T5Pair>::value) {
+          float sh[16], sl[16];
 #pragma unroll
-        for (int i2 = 0; i2 < 16; ++i2) sh[i2] = sl[i2] = 0.0f;
+          for (int i2 = 0; i2 < 16; ++i2) sh[i2] = sl[i2] = 0.0f;
 #pragma unroll 1
-        for (int L = OZ_L - 1; L >= 0; --L) {
-          float v[16];
-          t5_ld16(tbase + ((uint32_t)(32 * qd) << 16) + (uint32_t)(L * T5_NC + col), v);
-          // 2^(-7(L+2)) as a float (exponent field 127 - 7(L+2) >= 64): the level sums are integers below 2^24, so
-          // the product is exact and equals ldexpf(v, -7(L+2))
-          const float scale = __uint_as_float((uint32_t)(127 - 7 * (L + 2)) << 23);
+          for (int L = OZ_L - 1; L >= 0; --L) {
+            float v[16];
+            t5_ld16(tbase + ((uint32_t)(32 * qd) << 16) + (uint32_t)(L * T5_NC + col), v);
+            // 2^(-7(L+2)) as a float (exponent field 127 - 7(L+2) >= 64): the level sums are integers below 2^24,
+            // so the product is exact and equals ldexpf(v, -7(L+2))
+            const float scale = __uint_as_float((uint32_t)(127 - 7 * (L + 2)) << 23);
 #pragma unroll
-          for (int i2 = 0; i2 < 16; ++i2) oz_add(sh[i2], sl[i2], v[i2] * scale);
-        }
-        if (m < rows) {
+            for (int i2 = 0; i2 < 16; ++i2) oz_add(sh[i2], sl[i2], v[i2] * scale);
+          }
+          if (m < rows) {
 #pragma unroll
-          for (int i2 = 0; i2 < 16; ++i2) {
-            const int c = c0 + col + i2;
-            if (c >= N) break;
-            float2 out = make_float2(0.0f, 0.0f);  // an all-zero row stays zero
-            if (er) {
-              const float hi = sh[i2] + sl[i2];
-              const float lo = sl[i2] - (hi - sh[i2]);
-              const int sc = (er - 126) + fcol[c];
-              out = make_float2(ldexpf(hi, sc), ldexpf(lo, sc));
+            for (int i2 = 0; i2 < 16; ++i2) {
+              const int c = c0 + col + i2;
+              if (c >= N) break;
+              float2 out = make_float2(0.0f, 0.0f);  // an all-zero row stays zero
+              if (er) {
+                const float hi = sh[i2] + sl[i2];
+                const float lo = sl[i2] - (hi - sh[i2]);
+                const int sc = S::escale(er) + fcol[c];
+                out = make_float2(ldexpf(hi, sc), ldexpf(lo, sc));
+              }
+              V[(size_t)(r0 + m) + (size_t)(s0 + c) * ldv] = out;
             }
-            V[(size_t)(r0 + m) + (size_t)(s0 + c) * ldv] = out;
+          }
+        } else {
+          // the level sums as exact integers: X = sum_L P_L 2^(7(7-L)) = H 2^42 + R with H = 128 P_0 + P_1
+          // (|H| < 2^32) and R = sum_{L>=2} P_L 2^(7(7-L)) (|R| < 2^60); v q = 2^(e_r + f_c - 63) X, rounded once
+          long long Hs[16], Rs[16];
+#pragma unroll
+          for (int i2 = 0; i2 < 16; ++i2) Hs[i2] = Rs[i2] = 0;
+#pragma unroll 1
+          for (int L = OZ_L - 1; L >= 0; --L) {
+            float v[16];
+            t5_ld16(tbase + ((uint32_t)(32 * qd) << 16) + (uint32_t)(L * T5_NC + col), v);
+            const long long w = L >= 2 ? (1ll << (7 * (7 - L))) : (L == 1 ? 1ll : 128ll);
+#pragma unroll
+            for (int i2 = 0; i2 < 16; ++i2) {
+              const long long pl = (long long)__float2int_rn(v[i2]);  // an integer below 2^24 in magnitude
+              if (L >= 2) Rs[i2] += pl * w;
+              else Hs[i2] += pl * w;
+            }
+          }
+          if (m < rows) {
+#pragma unroll
+            for (int i2 = 0; i2 < 16; ++i2) {
+              const int c = c0 + col + i2;
+              if (c >= N) break;
+              double out = 0.0;  // an all-zero row stays zero
+              if (er) {
+                const int sc = S::escale(er) + fcol[c] - 63;
+                out = fma((double)Hs[i2], t5_pow2(sc + 42), (double)Rs[i2] * t5_pow2(sc));
+              }
+              V[(size_t)(r0 + m) + (size_t)(s0 + c) * ldv] = out;
+            }
           }
         }
       }
@@ -614,27 +689,42 @@ int *restart_t5_errflag(void *scratch, int ld) {
   return reinterpret_cast<int *>(static_cast<unsigned char *>(scratch) + t5_qbytes(ld) + t5_abytes(ld));
 }
 
-cudaError_t launch_restart_t5(float2 *V, long long ldv, int n, int a0, int K, int s0, int N, const double *Q, int ldq,
-                              void *scratch, int ld, cudaStream_t s) {
+template <class S, int QS>
+static cudaError_t restart_t5_go(typename S::T *V, long long ldv, int n, int a0, int K, int s0, int N,
+                                 const double *Q, int ldq, void *scratch, int ld, cudaStream_t s) {
   if (N <= 0 || K <= 0) return cudaSuccess;
   if (K > ld || N > ld) return cudaErrorInvalidValue;
   const int kp = (K + 15) / 16 * 16;
   const int ldp = (ld + 15) / 16 * 16;
   const int np = (ld + OZ_NC - 1) / OZ_NC * OZ_NC;
   if (kp > ldp || np < (N + 15) / 16 * 16) return cudaErrorInvalidValue;
-  if ((size_t)K * T5_M * sizeof(float2) > 2 * (size_t)T5_STAGE) return cudaErrorInvalidValue;  // the V tile's room
+  if ((size_t)K * T5_M * 8 > 2 * (size_t)T5_STAGE) return cudaErrorInvalidValue;  // the V tile's room
+  // level sums exact in FP32: at most min(QS, 8) products of magnitude <= 127 * 128 per level and k
+  if ((long long)(QS > OZ_L ? OZ_L : QS) * 127 * 128 * kp >= (1ll << 24)) return cudaErrorInvalidValue;
   __nv_bfloat16 *B = static_cast<__nv_bfloat16 *>(scratch);
-  int *fcol = reinterpret_cast<int *>(B + (size_t)OZ_S * np * kp);
+  int *fcol = reinterpret_cast<int *>(B + (size_t)OZ_QMAX * np * kp);
   __nv_bfloat16 *Ascr = reinterpret_cast<__nv_bfloat16 *>(static_cast<unsigned char *>(scratch) + t5_qbytes(ld));
   int *err = restart_t5_errflag(scratch, ld);
-  cudaError_t e = cudaFuncSetAttribute(k_restart_t5, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T5_SMEM);
+  cudaError_t e = cudaFuncSetAttribute(k_restart_t5<S, QS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T5_SMEM);
   if (e != cudaSuccess) return e;
-  k_oz_qslice<<<np, 128, 0, s>>>(Q, ldq, a0, s0, K, N, kp, np, B, fcol, 1);
+  k_oz_qslice<<<np, 128, 0, s>>>(Q, ldq, a0, s0, K, N, kp, np, B, fcol, 1, QS);
   const int ntiles = (n + T5_M - 1) / T5_M;
   int blocks = num_sms();
   if (blocks > ntiles) blocks = ntiles;
-  k_restart_t5<<<blocks, T5_THREADS, T5_SMEM, s>>>(V, ldv, n, a0, K, s0, N, kp, np, B, fcol, Ascr, err);
+  k_restart_t5<S, QS><<<blocks, T5_THREADS, T5_SMEM, s>>>(V, ldv, n, a0, K, s0, N, kp, np, B, fcol, Ascr, err);
   return cudaGetLastError();
+}
+
+cudaError_t launch_restart_t5(float2 *V, long long ldv, int n, int a0, int K, int s0, int N, const double *Q, int ldq,
+                              void *scratch, int ld, cudaStream_t s) {
+  return restart_t5_go<T5Pair, OZ_S>(V, ldv, n, a0, K, s0, N, Q, ldq, scratch, ld, s);
+}
+
+// FP64 storage: Q in 8 slices (56 bits) while the level sums stay exact (K <= 128), else 7
+cudaError_t launch_restart_t5_f64(double *V, long long ldv, int n, int a0, int K, int s0, int N, const double *Q,
+                                  int ldq, void *scratch, int ld, cudaStream_t s) {
+  if ((K + 15) / 16 * 16 <= 128) return restart_t5_go<T5F64, OZ_QMAX>(V, ldv, n, a0, K, s0, N, Q, ldq, scratch, ld, s);
+  return restart_t5_go<T5F64, OZ_S>(V, ldv, n, a0, K, s0, N, Q, ldq, scratch, ld, s);
 }
 
 cudaError_t launch_restart_tc(float2 *V, long long ldv, int n, int a0, int K, int s0, int N, const double *Q, int ldq,
@@ -646,12 +736,12 @@ cudaError_t launch_restart_tc(float2 *V, long long ldv, int n, int a0, int K, in
   const int np = (ld + OZ_NC - 1) / OZ_NC * OZ_NC;  // layout of the scratch (fixed per EPS)
   if (kp > ldp) return cudaErrorInvalidValue;
   __nv_bfloat16 *B = static_cast<__nv_bfloat16 *>(scratch);
-  int *fcol = reinterpret_cast<int *>(B + (size_t)OZ_S * np * kp);
+  int *fcol = reinterpret_cast<int *>(B + (size_t)OZ_QMAX * np * kp);
   const size_t shm = oz_smem_bytes(kp);
   if (shm > (size_t)227 * 1024) return cudaErrorInvalidValue;
   cudaError_t err = cudaFuncSetAttribute(k_restart_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
   if (err != cudaSuccess) return err;
-  k_oz_qslice<<<np, 128, 0, s>>>(Q, ldq, a0, s0, K, N, kp, np, B, fcol, 0);
+  k_oz_qslice<<<np, 128, 0, s>>>(Q, ldq, a0, s0, K, N, kp, np, B, fcol, 0, OZ_S);
   const int ntiles = (n + OZ_ROWS - 1) / OZ_ROWS;
   int blocks = num_sms();
   if (blocks > ntiles) blocks = ntiles;

@@ -33,6 +33,7 @@ struct DSArgs {
   int harmonic;    // non-symmetric solver: harmonic Rayleigh-Ritz translation for the target
   int conv;        // DS_CONV_*: the error estimate of the convergence test
   double conv_a, conv_b;  // DS_CONV_ABS: res / conv_a; DS_CONV_NORM: res / (conv_a + conv_b |k|)
+  const int *run_if = nullptr;  // the FP64 QR kernel runs only when this device flag is nonzero (null: always)
 };
 
 // convergence tests (EPSConvergedRelative / Absolute / Norm, epsdefault.c:224-256) on the scaled operator: the
@@ -57,6 +58,7 @@ struct DSFArgs {
   double *T, *X, *P, *S, *G;  // ld x ld: projected matrix, eigenvectors, product, X^T T X, X^T X
   double *W;                  // 2 * ld * 16: cluster rotations and cluster blocks
   double *lam, *part, *scal;  // eigenvalue estimates, block partial sums, thresholds
+  int *fallback;              // set by the final step when the refined pairs fail the accuracy check
   const KrylovState *st;
   KSControl *ctl;
 };
@@ -101,6 +103,10 @@ size_t restart_t5_scratch_bytes(int ld);
 int *restart_t5_errflag(void *scratch, int ld);
 cudaError_t launch_restart_t5(float2 *V, long long ldv, int n, int a0, int K, int s0, int N, const double *Q, int ldq,
                               void *scratch, int ld, cudaStream_t s);
+// the tcgen05 restart for FP64 storage: Q in 8 slices (7 when K > 128), the exact level sums rounded once to
+// doubles; the same scratch and timeout flag
+cudaError_t launch_restart_t5_f64(double *V, long long ldv, int n, int a0, int K, int s0, int N, const double *Q,
+                                  int ldq, void *scratch, int ld, cudaStream_t s);
 cudaError_t launch_restart_tc(float2 *V, long long ldv, int n, int a0, int K, int s0, int N, const double *Q, int ldq,
                               void *scratch, int ld, cudaStream_t s);
 cudaError_t launch_segment_begin(KrylovState *st, int k0, int m, cudaStream_t s);

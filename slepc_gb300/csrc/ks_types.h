@@ -54,7 +54,7 @@ struct KSControl {
   int breakdown;    // the factorisation broke down
   int need_start;   // a new start vector is needed at column nconv (breakdown or k == nv with k < nev)
   int ds_error;     // nonzero if the dense solver did not converge
-  int pad;
+  int ds_fallback;  // the mixed-precision symmetric solver failed its accuracy check; the FP64 QR solver ran
   double beta;      // residual norm used in the convergence test
   double hgamma;    // harmonic extraction: the scale gamma of the recovered residual vector (work holds g~)
 };

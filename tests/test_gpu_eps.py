@@ -249,6 +249,35 @@ def test_tcgen05_restart_is_bit_identical(lib, case):
     assert np.array_equal(a["X"], b["X"])
 
 
+@pytest.mark.parametrize("case", ["lap3d_wide", "lap3d_narrow", "convdiff"])
+def test_tcgen05_restart_fp64_storage(lib, case):
+    """The tcgen05 restart on IEEE-double storage (Q in 8 slices for K <= 128, exact level sums rounded once to a
+    double) against the CUDA-core FP64 FMA restart: the same eigenvalues to 1e-12, both at 1e-10 against the closed
+    form where there is one, host-side residuals at tol and orthonormal eigenvectors.  The wide case has K up to 110
+    and two output chunks; the narrow one a last K stage of 16."""
+    if case == "lap3d_wide":
+        csr, kw = matgen.laplacian_3d(30), dict(hermitian=True, which="LR", nev=40, ncv=110)
+        exact = matgen.laplacian_eigenvalues([30, 30, 30])
+    elif case == "lap3d_narrow":
+        csr, kw = matgen.laplacian_3d_randdiag(23, 5), dict(hermitian=True, which="LR", nev=12, ncv=40)
+        exact = None
+    else:
+        csr, kw = matgen.convection_diffusion_2d(45, 2.0), dict(hermitian=False, which="LR", nev=10, ncv=40)
+        exact = matgen.convdiff_eigenvalues(45, 2.0)
+    n = len(csr[0]) - 1
+    v0 = matgen.start_vector(n, 21)
+    a = run(csr, tol=1e-10, v0=v0, arith="f64", restart="tcgen05", **kw)
+    b = run(csr, tol=1e-10, v0=v0, arith="f64", restart="pair", **kw)
+    assert a["reason"] == 1 and b["reason"] == 1 and a["nconv"] >= kw["nev"]
+    m = min(a["nconv"], b["nconv"], kw["nev"])
+    assert np.max(np.abs(a["eigr"][:m] - b["eigr"][:m]) / np.abs(b["eigr"][:m])) <= 1e-12
+    if exact is not None:
+        assert rel_match(a["eigr"][:a["nconv"]], exact, 1e-10)
+    check_residuals(csr, a, 1e-10)
+    if kw["hermitian"]:
+        assert host_orth(a) <= 1e-12
+
+
 @pytest.mark.parametrize("lock", [True, False])
 def test_test2_interior_harmonic_golden_on_gpu(lib, lock):
     """test2.c's third solve on the device: harmonic extraction for the eigenvalues closest to 2.1."""

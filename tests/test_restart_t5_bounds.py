@@ -8,11 +8,11 @@ import itertools
 import pytest
 
 # kernel constants
-OZ_SA, OZ_S, OZ_L, OZ_NC = 8, 7, 8, 32
+OZ_SA, OZ_S, OZ_QMAX, OZ_L, OZ_NC = 8, 7, 8, 8, 32
 T5_M, T5_NC, T5_KC, T5_THREADS = 128, 64, 32, 512
 T5_ASL = T5_M * T5_KC * 2
 T5_BSL = T5_NC * T5_KC * 2
-T5_STAGE = OZ_SA * T5_ASL + OZ_S * T5_BSL
+T5_STAGE = OZ_SA * T5_ASL + OZ_QMAX * T5_BSL
 T5_SMEM = 2 * T5_STAGE + (T5_THREADS // T5_M + 1) * T5_M * 4 + 5 * 8 + 16
 TMEM_COLS = OZ_L * T5_NC
 NUM_SMS = 152
@@ -26,18 +26,21 @@ def rup(x, m):
 def scratch_layout(ld):
     """restart_tc_scratch_bytes / t5_qbytes / t5_abytes / restart_t5_scratch_bytes"""
     kp_max, np_ = rup(ld, 16), rup(ld, OZ_NC)
-    tc = OZ_S * np_ * kp_max * BF16 + np_ * 4 + 256
+    tc = OZ_QMAX * np_ * kp_max * BF16 + np_ * 4 + 256
     q = rup(tc, 256)
     a = NUM_SMS * OZ_SA * rup(ld, 16) * 128 * BF16
     return {"np": np_, "tc": tc, "q": q, "a": a, "total": q + a + 256}
 
 
-def check(n, ld, K, N):
+def check(n, ld, K, N, f64=False):
+    """f64: the FP64-storage kernel (Q in 8 slices when K <= 128, else 7); otherwise pair storage (7 slices)."""
     assert 0 < K <= ld and 0 < N <= ld and ld <= 144
     lay = scratch_layout(ld)
     np_ = lay["np"]
     kp, ldp = rup(K, 16), rup(ld, 16)
+    QS = OZ_QMAX if (f64 and kp <= 128) else OZ_S
     assert kp <= ldp and np_ >= rup(N, 16)            # the launch's own checks
+    assert min(QS, OZ_L) * 127 * 128 * kp < (1 << 24)  # every level sum exact in FP32
     assert K * T5_M * 8 <= 2 * T5_STAGE                # the V tile fits the stage region
     assert T5_SMEM <= 227 * 1024
     # shared layout: stages, erow + etmp, five mbarriers (8-byte aligned), the TMEM slot
@@ -50,8 +53,9 @@ def check(n, ld, K, N):
     ldv = rup(n, 64)
     v_elems = ldv * (ld + 1)                           # float2 entries of the basis
     # Q slices (cm layout) written by k_oz_qslice: element (t, c, k)
-    q_max = ((OZ_S - 1) * nk8 + (kp - 1) // 8) * (np_ // 8) * 64 + ((np_ - 1) // 8) * 64 + 7 * 8 + 7
-    assert (q_max + 1) * BF16 <= OZ_S * np_ * kp * BF16 <= lay["tc"]
+    q_max = ((QS - 1) * nk8 + (kp - 1) // 8) * (np_ // 8) * 64 + ((np_ - 1) // 8) * 64 + 7 * 8 + 7
+    assert (q_max + 1) * BF16 <= OZ_QMAX * np_ * kp * BF16
+    assert OZ_QMAX * np_ * kp * BF16 + np_ * 4 <= lay["tc"]  # the slices, then the column exponents
     # per-CTA slice scratch
     per_cta = OZ_SA * nk8 * 16 * 64 * BF16
     assert blocks * per_cta <= lay["a"]
@@ -82,16 +86,17 @@ def check(n, ld, K, N):
             abytes = sk8 * 16 * 128
             bbytes = (nch // 8) * 128
             assert abytes % 16 == 0 and bbytes % 16 == 0
-            assert OZ_SA * abytes + OZ_S * sk8 * bbytes < (1 << 20)
+            assert OZ_SA * abytes + QS * sk8 * bbytes < (1 << 20)
             # A copies: source inside the CTA's slice scratch, destination inside its slice of the stage
             for sl in range(OZ_SA):
                 src_end = ((sl * nk8 + kc8) * 16 * 64) * BF16 + abytes
                 assert src_end <= per_cta and abytes <= T5_ASL
             # B copies: source inside the Q slices, destination inside the slice of the stage
-            for t, k8 in itertools.product(range(OZ_S), range(sk8)):
+            for t, k8 in itertools.product(range(QS), range(sk8)):
                 src = (((t * nk8 + kc8 + k8) * (np_ // 8) + c0 // 8) * 64) * BF16
-                assert src % 16 == 0 and src + bbytes <= OZ_S * np_ * kp * BF16
+                assert src % 16 == 0 and src + bbytes <= QS * np_ * kp * BF16
                 assert k8 * (T5_NC // 8) * 128 + bbytes <= T5_BSL
+                assert OZ_SA * T5_ASL + t * T5_BSL + T5_BSL <= T5_STAGE
             # what the tensor cores read per MMA (K-major, no swizzle: 8-row groups at SBO, K core matrices at LBO)
             for j in range(sk8 // 2):
                 a_lo = j * 2 * 16 * 128
@@ -111,11 +116,13 @@ def check(n, ld, K, N):
 @pytest.mark.parametrize("n", [1, 2, 127, 128, 129, 1000, 4095, 12167, 27000])
 @pytest.mark.parametrize("ld,K,N", [(24, 24, 17), (41, 40, 30), (111, 110, 70), (129, 128, 64), (129, 128, 96),
                                     (129, 75, 128), (144, 143, 143), (144, 16, 16), (33, 1, 1)])
-def test_t5_addressing_in_bounds(n, ld, K, N):
-    check(n, ld, K, N)
+@pytest.mark.parametrize("f64", [False, True])
+def test_t5_addressing_in_bounds(n, ld, K, N, f64):
+    check(n, ld, K, N, f64)
 
 
 def test_t5_shared_memory_and_registers_fit():
-    # 512 threads x at most 112 registers (ptxas -v: 110) fit the SM's 65,536 registers; one CTA per SM by TMEM and shared memory
-    assert T5_THREADS * 112 <= 65536
+    # 512 threads x at most 128 registers (ptxas -v: 110 for pair storage, 127 for FP64) fit the SM's 65,536
+    # registers; one CTA per SM by TMEM and shared memory
+    assert T5_THREADS * 128 <= 65536
     assert 2 * T5_SMEM > 228 * 1024
