@@ -30,13 +30,15 @@ PetscErrorCode EPSGB300SetArithmetic(EPS eps, EPSGB300Arith arith);
 PetscErrorCode EPSGB300GetArithmetic(EPS eps, EPSGB300Arith *arith);
 
 /* Solver of the symmetric projected problem inside EPSSolve.
- *   EPS_GB300_DS_REFINED (default): FP32 arrowhead reduction and implicit QL, then FP64 eigenvector refinement
- *       (Ogita-Aishima iterations with clustered eigenvalues diagonalised by Jacobi, and a Newton-Schulz step), whose
- *       matrix products run on the whole GPU.  Same results as the QR solver to FP64 rounding, a fraction of its
- *       time: GB300's FP64 scalar latency makes a one-thread FP64 QL chain the slowest part of a restart.
- *   EPS_GB300_DS_QR: the reference's algorithm (arrowhead reduction, implicit QL) in FP64 in one thread block.
+ *   EPS_GB300_DS_QR (default): the reference's algorithm (arrowhead reduction, implicit QL) in FP64 in one thread
+ *       block.
+ *   EPS_GB300_DS_REFINED: FP32 arrowhead reduction and implicit QL, then FP64 eigenvector refinement (Ogita-Aishima
+ *       iterations with clustered eigenvalues diagonalised by Jacobi, and a Newton-Schulz step), whose matrix
+ *       products run on the whole GPU, then an accuracy check of every pair; a restart whose pairs fail the check is
+ *       solved again by the QR solver (EPSGB300Stats.ds_fallbacks counts them).  Faster when the wanted end of the
+ *       spectrum is well separated; on dense clusters (the 3-D Laplacians) every restart falls back.
  * The non-Hermitian solver and the DS object always use the FP64 algorithms.  Option -eps_gb300_ds refined|qr. */
-typedef enum { EPS_GB300_DS_REFINED = 0, EPS_GB300_DS_QR = 1 } EPSGB300DSMethod;
+typedef enum { EPS_GB300_DS_REFINED = 0, EPS_GB300_DS_QR = 1 } EPSGB300DSMethod;  /* default: EPS_GB300_DS_QR */
 PetscErrorCode EPSGB300SetProjectedSolver(EPS eps, EPSGB300DSMethod method);
 PetscErrorCode EPSGB300GetProjectedSolver(EPS eps, EPSGB300DSMethod *method);
 

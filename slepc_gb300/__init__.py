@@ -448,7 +448,8 @@ class EPS:
         _check(load().EPSGB300SetTimeLimit(self.handle, float(seconds)), "EPSGB300SetTimeLimit")
 
     def setProjectedSolver(self, method):
-        """'refined' (FP32 QL + FP64 refinement, default) or 'qr' (FP64 QL) for the symmetric projected problem."""
+        """'qr' (FP64 QL, default) or 'refined' (FP32 QL + FP64 refinement with a checked fallback to 'qr') for the
+        symmetric projected problem."""
         _check(load().EPSGB300SetProjectedSolver(self.handle, 1 if method == "qr" else 0),
                "EPSGB300SetProjectedSolver")
 

@@ -1,0 +1,835 @@
+// k_gs_tc.cu -- the DCGS2 Gram-Schmidt pair for IEEE-double storage on the bf16 tensor cores (tcgen05 + TMEM), by
+// the error-free slice split of Ozaki, Ogita, Oishi and Rump ("Error-free transformations of matrix multiplication
+// by using fast routines of matrix multiplication and its applications", Numer. Algorithms 59, 2012).
+//
+// GB300's FP64 pipe issues about 0.6 T FMA/s, so the FP64-FMA Gram-Schmidt kernels (two FMAs per 8-byte basis
+// entry) stop near 2.4 TB/s, a third of the HBM rate.  Here every product runs exactly on the bf16 tensor cores:
+//
+//   a value v with |v| < 2^e is the 56-bit fixed point  v 2^(56-e) = sum_{p<8} a_p 2^(7(7-p)),  a_p in [-127, 127]
+//   (the 53-bit significand truncated only below 2^-56 of the scale), each a_p exact in bf16;
+//   sum_r v_r u_r = 2^(e_v + e_u - 112) sum_{p,q} D_pq 2^(7(14-p-q)),  D_pq = sum_r a_p(v_r) b_q(u_r),
+//
+// every D_pq an exact FP32 sum of exact integer products (|D_pq| <= 1024 * 127^2 < 2^24).  The 64 slice products
+// recombine exactly as a 128-bit integer, rounded once to a double.
+//
+// Scales.  Basis columns (unit vectors) carry one exponent per column and 128-row tile, recorded by the kernels that
+// write them (this file's update half, the tcgen05 restart) in an int8 table [column][tile]; a value's scale is the
+// maximum over the tiles it is summed with, so small entries keep their relative precision where the column is
+// small.  u, w (half A) get a scale per row chunk, the coefficient vectors s, g (half B) one per vector, computed on
+// the fly.  A value at or above its recorded scale sets the error flag (the host reports PETSC_ERR_PLIB).
+//
+// Half A (dot): s = V^T u, b = V^T w over chunks of ct 128-row tiles.  MMA M = 128 = 16 basis columns x 8 slices
+// (row jl * 8 + p), N = 16 = 2 vectors x 8 slices, K = the rows of a tile.  Exact chunk sums, recombined per column
+// as 128-bit integers (a butterfly over the 8 lanes of a column), are accumulated across chunks in double-double;
+// the block partials are merged in block order by the last block, which runs the DCGS2 coefficient algebra
+// (gs_epilogue).  Rounding: one rounding per chunk and column and a double-double sum, far below the FP64 dot's.
+//
+// Half B (update): [v w'] = [(sigma u - V s) / nu, w - V g - tau sigma u].  Per tile of 128 rows: MMA M = 128 rows,
+// N = 16 (s, g x 8 slices), K = the basis columns, one TMEM accumulator per V slice p; the thread of row r sums the
+// 15 levels p + q exactly and rounds the product once; the FP64 update, the norm of w' and the recorded exponents of
+// v follow.  Results are deterministic: fixed partitions, fixed orders, no floating-point atomics.
+//
+// Warp roles (13 warps): 0-3 epilogue and vector staging (TMEM lanes 0-127), 4 the MMA issuer (one thread), 5-12
+// slicers (global loads of V, slicing into a ring of four 32 KB shared-memory stages).  Stages, B buffers and TMEM
+// buffers hand over on mbarriers; tcgen05.commit releases what the tensor cores have read.  Every wait is bounded:
+// on a timeout the kernel records it, stops issuing, waits (bounded) for the MMAs in flight, frees TMEM and returns.
+#include <float.h>
+
+#include <type_traits>
+
+#include "common.cuh"
+#include "kernels.h"
+#include "krylov_body.cuh"
+#include "ks_types.h"
+#include "tc_common.cuh"
+
+namespace ksg {
+
+constexpr int GT_R = 128;                                 // rows per tile
+constexpr int GT_NA = 4;                                  // A stages
+constexpr int GT_STAGE = 32768;                           // 128 x 16 values x 8 slices x bf16
+constexpr int GT_BT = 4096;                               // dot: B slices of one tile (16 k8 x 2 n8 x 128 B)
+constexpr int GT_CTMAX = 8;                               // tiles per chunk (dot)
+constexpr int GT_EW = 4, GT_SW = 8;                       // epilogue warps, slicer warps
+constexpr int GT_MWARP = GT_EW;                           // the MMA warp
+constexpr int GT_SW0 = GT_EW + 1;                         // first slicer warp
+constexpr int GT_THREADS = 32 * (GT_EW + 1 + GT_SW);      // 416
+constexpr int GT_MAXJ = 144;
+constexpr uint32_t GT_TMEM = 512;
+// barriers: afull[4] aempty[4] bfull[2] cdone[2] tfree[2] fin
+constexpr int GB_AFULL = 0, GB_AEMPTY = 4, GB_BFULL = 8, GB_CDONE = 10, GB_TFREE = 12, GB_FIN = 14, GB_N = 15;
+
+// dynamic shared memory: A ring, then (dot) two chunk B buffers / (update) the coefficient slices, then bookkeeping
+constexpr size_t GT_AOFF = 0;
+constexpr size_t GT_BOFF = GT_AOFF + (size_t)GT_NA * GT_STAGE;
+constexpr size_t GT_DOT_MISC = GT_BOFF + 2 * (size_t)GT_CTMAX * GT_BT;  // dd partials [J][2][2] after the B buffers
+constexpr size_t GT_UPD_MISC = GT_BOFF + (size_t)(GT_MAXJ / 8) * 2 * 128;
+constexpr size_t GT_MISC_BYTES = (size_t)GT_MAXJ * 4 * 8 + 64 * 8 + GB_N * 8 + 64 * 4 + 16;
+constexpr size_t GT_DOT_SMEM = GT_DOT_MISC + GT_MISC_BYTES;
+constexpr size_t GT_UPD_SMEM = GT_UPD_MISC + GT_MISC_BYTES;
+
+struct GTShared {
+  double *pdd;          // [GT_MAXJ][2 vectors][hi, lo]
+  double *red;          // 64 doubles of reduction scratch
+  unsigned long long *bar;
+  int *ints;            // [0] abort, [1] epilogue-warp barrier counter, [4..7] and [8..11] per-warp maxima,
+                        // [12..15] per-tile-slot arrival counters, [16..31] per-tile-slot warp maxima
+  uint32_t *tslot;
+};
+
+KS_DEVICE GTShared gt_shared(unsigned char *sm, size_t misc) {
+  GTShared s;
+  s.pdd = reinterpret_cast<double *>(sm + misc);
+  s.red = s.pdd + GT_MAXJ * 4;
+  s.bar = reinterpret_cast<unsigned long long *>(s.red + 64);
+  s.ints = reinterpret_cast<int *>(s.bar + GB_N);
+  s.tslot = reinterpret_cast<uint32_t *>(s.ints + 64);
+  return s;
+}
+
+// bounded wait that gives up at once when another role has aborted; false on timeout or abort
+KS_DEVICE bool gt_wait(unsigned long long *bar, uint32_t parity, volatile int *abort) {
+  const uint32_t a = t5_smem(bar);
+  for (int it = 0; it < T5_WAIT_LIMIT; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if ((it & 63) == 63 && *abort) return false;
+  }
+  *abort = 1;
+  return false;
+}
+
+KS_DEVICE void gt_arrive(unsigned long long *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(t5_smem(bar)) : "memory");
+}
+
+KS_DEVICE void gt_fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// Barrier of the four epilogue warps on a shared counter: each warp adds one arrival, then waits (bounded, giving up
+// on an abort) until the counter reaches 4 * gen.  Unlike a named barrier it cannot hang when another role has
+// stopped early.  Returns false on timeout or abort.
+KS_DEVICE bool gt_ebar(int *cnt, int gen, volatile int *abort) {
+  __syncwarp();
+  __threadfence_block();
+  if ((threadIdx.x & 31) == 0) atomicAdd(cnt, 1);
+  bool ok = true;
+  for (int it = 0;; ++it) {
+    if (*(volatile int *)cnt >= GT_EW * gen) break;
+    if (it >= T5_WAIT_LIMIT || ((it & 63) == 63 && *abort)) {
+      *abort = 1;
+      ok = false;
+      break;
+    }
+  }
+  __syncwarp();
+  __threadfence_block();
+  return ok;
+}
+
+// Eight doubles that are consecutive along the MMA's K dimension -> eight slices of 8 bf16 (one 16-byte core-matrix
+// row each) of their 56-bit fixed point relative to 2^e; *ovf is set when some |v| >= 2^e.
+KS_DEVICE void gt_slice8(const double *v, int e, uint4 *out, int *ovf) {
+  uint32_t mh[8], ml[8], ng[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(v[j]);
+    const int E = (int)((u >> 52) & 0x7FF);
+    unsigned long long x = 0;
+    if (E) {
+      const int sh = (E - 1075) + 56 - e;
+      const unsigned long long m = (u & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+      if (sh > 3) *ovf = 1;
+      x = sh >= 0 ? (sh <= 3 ? (m << sh) : 0ull) : (sh > -60 ? (m >> (-sh)) : 0ull);
+    }
+    ng[j] = (uint32_t)(u >> 63);
+    mh[j] = (uint32_t)(x >> 32);
+    ml[j] = (uint32_t)x;
+  }
+#pragma unroll
+  for (int sl = 0; sl < 8; ++sl) {
+    uint32_t f[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) f[j] = t5_field(mh[j], ml[j], sl);
+    out[sl].x = t5_slice_pair(f[0], f[1], ng[0], ng[1]);
+    out[sl].y = t5_slice_pair(f[2], f[3], ng[2], ng[3]);
+    out[sl].z = t5_slice_pair(f[4], f[5], ng[4], ng[5]);
+    out[sl].w = t5_slice_pair(f[6], f[7], ng[6], ng[7]);
+  }
+}
+
+// scale exponent of a value: |v| < 2^(E - 1022) for its biased exponent E >= 1; recorded in [-127, 127], -128 for zero
+KS_DEVICE int gt_expo(double v) { return (int)(((unsigned long long)__double_as_longlong(v) >> 52) & 0x7FF); }
+KS_DEVICE int gt_escale(int Emax) {
+  if (Emax == 0) return -128;
+  const int e = Emax - 1022;
+  return e < -127 ? -127 : (e > 127 ? 127 : e);
+}
+
+// 2^k as a double over the whole exponent range used here (|k| < 1100)
+KS_DEVICE double gt_pow2(int k) { return t5_pow2(k); }
+
+// 128-bit two's complement (hi, lo) helpers
+KS_DEVICE void gt_add128(long long &hi, unsigned long long &lo, long long bhi, unsigned long long blo) {
+  const unsigned long long s = lo + blo;
+  hi = hi + bhi + (s < lo ? 1 : 0);
+  lo = s;
+}
+// (hi, lo) = Y * 2^sh for a signed Y = H 2^42 + R (|H| < 2^33, |R| < 2^61), 0 <= sh < 64
+KS_DEVICE void gt_make128(long long H, long long R, int sh, long long &hi, unsigned long long &lo) {
+  hi = H >> 22;
+  lo = (unsigned long long)H << 42;
+  gt_add128(hi, lo, R >> 63, (unsigned long long)R);
+  if (sh > 0) {
+    hi = (long long)(((unsigned long long)hi << sh) | (lo >> (64 - sh)));
+    lo <<= sh;
+  }
+}
+// the value of a 128-bit integer as a double (two roundings at most: within 1 ulp)
+KS_DEVICE double gt_to_double(long long hi, unsigned long long lo) {
+  return fma(__ll2double_rn(hi), 18446744073709551616.0, __ull2double_rn(lo));
+}
+
+// double-double accumulation (TwoSum)
+KS_DEVICE void gt_dd_add(double &hi, double &lo, double x) {
+  const double s = hi + x;
+  const double bb = s - hi;
+  lo += (hi - (s - bb)) + (x - bb);
+  hi = s;
+}
+
+// the recorded scale of V column j over tiles [t0, t0 + nt): the largest exponent (-128 when every tile is zero)
+KS_DEVICE int gt_vscale(const GTArgs &g, int j, int t0, int nt) {
+  int e = -128;
+  const signed char *p = g.vexp + (size_t)j * g.ldt + t0;
+  for (int t = 0; t < nt; ++t) e = max(e, (int)p[t]);
+  return e;
+}
+
+KS_DEVICE void gt_init_barriers(const GTShared &S) {
+  const int counts[GB_N] = {GT_SW, GT_SW, GT_SW, GT_SW, 1, 1, 1, 1, GT_EW, GT_EW, 1, 1, GT_EW, GT_EW, 1};
+  for (int i = 0; i < GB_N; ++i)
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(t5_smem(&S.bar[i])), "r"(counts[i]) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// Half A
+// ---------------------------------------------------------------------------------------------------------------
+template <int NX>
+__global__ void __maxnreg__(152) k_gs_dot_tc(StepArgs a, int mode, GTArgs g) {
+  KrylovState *st = a.st;
+  if (st->stop) return;
+  extern __shared__ __align__(1024) unsigned char sm[];
+  __shared__ double res[GT_MAXJ * 2 + 4];
+  __shared__ int s_last;
+  const GTShared S = gt_shared(sm, GT_DOT_MISC);
+  volatile int *abort = S.ints;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int n = a.n, J = a.J, NMB = (J + 15) / 16, ct = g.ct;
+  const double sigma = st->sigma;
+  const double *U = static_cast<const double *>(a.U);
+  const double *W = static_cast<const double *>(a.W);
+  const double *V = static_cast<const double *>(a.V);
+  const int ntiles = (n + GT_R - 1) / GT_R;
+  const int nchunks = (ntiles + ct - 1) / ct;
+  const int my = blockIdx.x < nchunks ? (nchunks - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+  if (tid == 0) {
+    for (int i = 0; i < 64; ++i) S.ints[i] = 0;
+    gt_init_barriers(S);
+  }
+  for (int i = tid; i < GT_MAXJ * 4; i += GT_THREADS) S.pdd[i] = 0.0;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(t5_smem(S.tslot)),
+                 "r"(GT_TMEM)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  t5_fence_before();
+  __syncthreads();
+  t5_fence_after();
+  const uint32_t tbase = *S.tslot;
+  unsigned char *As = sm + GT_AOFF;
+  unsigned char *Bs = sm + GT_BOFF;
+  double sc0 = 0.0, sc1 = 0.0, sc2 = 0.0;  // u.u, u.w, w.w (epilogue threads)
+
+  if (warp < GT_EW) {
+    // ---------------- epilogue warps: u/w staging and TMEM drain ----------------
+    const int e = tid;  // 0..127: the 8-row group of a chunk this thread stages, and its TMEM lane
+    int ebar_gen = 0;
+    int eu0 = 0, ew0 = 0, eu1 = 0, ew1 = 0;  // chunk scales of the two B buffers
+    auto stage_uw = [&](int i) -> bool {
+      const int b = i & 1;
+      const int c = blockIdx.x + i * gridDim.x;
+      const long long r0 = (long long)c * ct * GT_R + 8 * e;
+      double uv[8], wv[8];
+      int Eu = 0, Ew = 0;
+      const bool mine = e < ct * 16;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const long long r = r0 + k;
+        double u = 0.0, w = 0.0;
+        if (mine && r < n) {
+          u = U[r] * sigma;
+          if (NX == 2) w = W[r];
+        }
+        uv[k] = u;
+        wv[k] = w;
+        sc0 = fma(u, u, sc0);
+        if (NX == 2) {
+          sc1 = fma(u, w, sc1);
+          sc2 = fma(w, w, sc2);
+        }
+        Eu = max(Eu, gt_expo(u));
+        Ew = max(Ew, gt_expo(w));
+      }
+      // chunk scales: the largest exponent over the 128 staging threads (every thread keeps its own copy)
+      for (int off = 16; off > 0; off >>= 1) {
+        Eu = max(Eu, __shfl_xor_sync(0xffffffffu, Eu, off));
+        Ew = max(Ew, __shfl_xor_sync(0xffffffffu, Ew, off));
+      }
+      if (lane == 0) {
+        S.ints[4 + warp] = Eu;
+        S.ints[8 + warp] = Ew;
+      }
+      if (!gt_ebar(&S.ints[1], ++ebar_gen, abort)) return false;
+      int eu = 0, ew = 0;
+#pragma unroll
+      for (int q = 0; q < GT_EW; ++q) {
+        eu = max(eu, S.ints[4 + q]);
+        ew = max(ew, S.ints[8 + q]);
+      }
+      if (!gt_ebar(&S.ints[1], ++ebar_gen, abort)) return false;  // read by all before the next staging
+      eu = gt_escale(eu);
+      ew = gt_escale(ew);
+      if (b == 0) { eu0 = eu; ew0 = ew; } else { eu1 = eu; ew1 = ew; }
+      if (mine) {
+        uint4 sl[8];
+        int ovf = 0;
+        const int t = e >> 4, k8 = e & 15;
+        unsigned char *base = Bs + (size_t)b * GT_CTMAX * GT_BT + (size_t)((t * 16 + k8) * 2) * 128;
+        gt_slice8(uv, eu, sl, &ovf);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) *reinterpret_cast<uint4 *>(base + q * 16) = sl[q];
+        if (NX == 2) gt_slice8(wv, ew, sl, &ovf);
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+          *reinterpret_cast<uint4 *>(base + 128 + q * 16) = NX == 2 ? sl[q] : make_uint4(0u, 0u, 0u, 0u);
+      }
+      gt_fence_async_smem();
+      __syncwarp();
+      if (lane == 0) gt_arrive(&S.bar[GB_BFULL + b]);
+      return true;
+    };
+    bool eok = true;
+    if (my > 0) eok = stage_uw(0);
+    if (my > 1 && eok) eok = stage_uw(1);
+    const int jl = e >> 3, p = e & 7;
+    for (int i = 0; i < my && eok; ++i) {
+      const int b = i & 1;
+      const int c = blockIdx.x + i * gridDim.x;
+      if (!gt_wait(&S.bar[GB_CDONE + b], (uint32_t)((i >> 1) & 1), abort)) break;
+      t5_fence_after();
+      const int eu = b ? eu1 : eu0, ew = b ? ew1 : ew0;
+      for (int mb = 0; mb < NMB; ++mb) {
+        float v[16];
+        t5_ld16(tbase + ((uint32_t)(32 * warp) << 16) + (uint32_t)(b * NMB * 16 + mb * 16), v);
+        const int j = mb * 16 + jl;
+        const int ej = (j < J) ? gt_vscale(g, j, c * ct, min(ct, ntiles - c * ct)) : -128;
+#pragma unroll
+        for (int x = 0; x < NX; ++x) {
+          long long H = 0, R = 0;
+          H = (long long)__float2int_rn(v[x * 8 + 0]) * 128 + (long long)__float2int_rn(v[x * 8 + 1]);
+#pragma unroll
+          for (int q = 2; q < 8; ++q) R += (long long)__float2int_rn(v[x * 8 + q]) << (7 * (7 - q));
+          long long hi;
+          unsigned long long lo;
+          gt_make128(H, R, 7 * (7 - p), hi, lo);
+#pragma unroll
+          for (int off = 4; off > 0; off >>= 1) {
+            const long long ohi = __shfl_xor_sync(0xffffffffu, hi, off);
+            const unsigned long long olo = __shfl_xor_sync(0xffffffffu, lo, off);
+            gt_add128(hi, lo, ohi, olo);
+          }
+          if (p == 0 && j < J && ej > -128) {
+            const double val = gt_to_double(hi, lo) * gt_pow2(ej + (x ? ew : eu) - 112);
+            gt_dd_add(S.pdd[(j * 2 + x) * 2], S.pdd[(j * 2 + x) * 2 + 1], val);
+          }
+        }
+      }
+      t5_fence_before();
+      __syncwarp();
+      if (lane == 0) gt_arrive(&S.bar[GB_TFREE + b]);
+      if (i + 2 < my) eok = stage_uw(i + 2);
+    }
+  } else if (warp == GT_MWARP) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(16 >> 3) << 17) |
+                             ((uint32_t)(GT_R >> 4) << 24);
+      int q = 0;
+      bool ok = true;
+      for (int i = 0; i < my && ok; ++i) {
+        const int b = i & 1, u = i >> 1;
+        if (!gt_wait(&S.bar[GB_BFULL + b], (uint32_t)(u & 1), abort)) { ok = false; break; }
+        if (u >= 1 && !gt_wait(&S.bar[GB_TFREE + b], (uint32_t)((u - 1) & 1), abort)) { ok = false; break; }
+        t5_fence_after();
+        const uint32_t bbase = t5_smem(Bs + (size_t)b * GT_CTMAX * GT_BT);
+        for (int t = 0; t < ct && ok; ++t)
+          for (int mb = 0; mb < NMB; ++mb, ++q) {
+            const int sa = q % GT_NA;
+            if (!gt_wait(&S.bar[GB_AFULL + sa], (uint32_t)((q / GT_NA) & 1), abort)) { ok = false; break; }
+            t5_fence_after();
+            const uint32_t abase = t5_smem(As + (size_t)sa * GT_STAGE);
+            const uint32_t dcol = tbase + (uint32_t)(b * NMB * 16 + mb * 16);
+#pragma unroll
+            for (int ks = 0; ks < 8; ++ks) {
+              const uint64_t ad = t5_desc(abase + ks * 2 * 2048, 2048, 128);
+              const uint64_t bd = t5_desc(bbase + (uint32_t)((t * 16 + 2 * ks) * 256), 256, 128);
+              t5_mma(dcol, ad, bd, idesc, (t > 0 || ks > 0) ? 1u : 0u);
+            }
+            t5_commit(&S.bar[GB_AEMPTY + sa]);
+          }
+        if (ok) t5_commit(&S.bar[GB_CDONE + b]);
+      }
+      // every MMA issued has completed before TMEM is freed (bounded)
+      t5_commit(&S.bar[GB_FIN]);
+      if (!t5_wait(&S.bar[GB_FIN], 0)) *abort = 1;
+    }
+  } else {
+    // ---------------- slicers ----------------
+    const int s = tid - 32 * GT_SW0;  // 0..255
+    const int jl = s >> 4, k8 = s & 15;
+    int q = 0, ovf = 0;
+    bool ok = true;
+    for (int i = 0; i < my && ok; ++i) {
+      const int c = blockIdx.x + i * gridDim.x;
+      const int tch = min(ct, ntiles - c * ct);
+      for (int t = 0; t < ct && ok; ++t)
+        for (int mb = 0; mb < NMB; ++mb, ++q) {
+          const int sa = q % GT_NA;
+          const int j = mb * 16 + jl;
+          const long long r0 = ((long long)c * ct + t) * GT_R + 8 * k8;
+          double v[8];
+          if (j < J && t < tch) {
+            const double *col = V + (size_t)j * a.ldv + r0;
+            if (r0 + 8 <= n) {
+#pragma unroll
+              for (int k = 0; k < 4; ++k) {
+                const double2 d2 = __ldcs(reinterpret_cast<const double2 *>(col) + k);
+                v[2 * k] = d2.x;
+                v[2 * k + 1] = d2.y;
+              }
+            } else {
+#pragma unroll
+              for (int k = 0; k < 8; ++k) v[k] = (r0 + k < n) ? col[k] : 0.0;
+            }
+          } else {
+#pragma unroll
+            for (int k = 0; k < 8; ++k) v[k] = 0.0;
+          }
+          const int ej = (j < J && t < tch) ? gt_vscale(g, j, c * ct, tch) : 0;
+          uint4 sl[8];
+          gt_slice8(v, ej, sl, &ovf);
+          if (q >= GT_NA && !gt_wait(&S.bar[GB_AEMPTY + sa], (uint32_t)(((q / GT_NA) - 1) & 1), abort)) {
+            ok = false;
+            break;
+          }
+          unsigned char *dst = As + (size_t)sa * GT_STAGE + (size_t)(k8 * 16 + jl) * 128;
+#pragma unroll
+          for (int p = 0; p < 8; ++p) *reinterpret_cast<uint4 *>(dst + p * 16) = sl[p];
+          gt_fence_async_smem();
+          __syncwarp();
+          if (lane == 0) gt_arrive(&S.bar[GB_AFULL + sa]);
+        }
+    }
+    if (ovf) atomicExch(g.err, 2);
+  }
+  // ---------------- teardown, partials, merge ----------------
+  t5_fence_before();
+  __syncthreads();
+  t5_fence_after();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(GT_TMEM) : "memory");
+  if (*abort && tid == 0) atomicExch(g.err, 1);
+  // scalars: reduce the epilogue threads' sums (fixed order)
+  if (warp < GT_EW) {
+    for (int off = 16; off > 0; off >>= 1) {
+      sc0 += __shfl_down_sync(0xffffffffu, sc0, off);
+      sc1 += __shfl_down_sync(0xffffffffu, sc1, off);
+      sc2 += __shfl_down_sync(0xffffffffu, sc2, off);
+    }
+    if (lane == 0) {
+      S.red[8 + warp * 3] = sc0;
+      S.red[9 + warp * 3] = sc1;
+      S.red[10 + warp * 3] = sc2;
+    }
+  }
+  __syncthreads();
+  const int nsc = NX == 2 ? 3 : 1;
+  double *pb = g.part + (size_t)blockIdx.x * g.pstride;  // [J * NX][hi, lo], then the scalars
+  for (int o = tid; o < J * NX; o += GT_THREADS) {
+    const int j = o / NX, x = o % NX;
+    pb[2 * o] = S.pdd[(j * 2 + x) * 2];
+    pb[2 * o + 1] = S.pdd[(j * 2 + x) * 2 + 1];
+  }
+  if (tid < nsc) {
+    double v = 0.0;
+    for (int w = 0; w < GT_EW; ++w) v += S.red[8 + w * 3 + tid];
+    pb[2 * J * NX + tid] = v;
+  }
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) s_last = (atomicAdd(&st->tickets[TK_DOT], 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  for (int o = tid; o < J * NX + nsc; o += GT_THREADS) {
+    if (o < J * NX) {
+      double hi = 0.0, lo = 0.0;
+      for (int b2 = 0; b2 < (int)gridDim.x; ++b2) {
+        const double *q2 = g.part + (size_t)b2 * g.pstride + 2 * o;
+        gt_dd_add(hi, lo, __ldcg(q2));
+        gt_dd_add(hi, lo, __ldcg(q2 + 1));
+      }
+      res[o] = hi + lo;
+    } else {
+      double v = 0.0;
+      for (int b2 = 0; b2 < (int)gridDim.x; ++b2) v += __ldcg(g.part + (size_t)b2 * g.pstride + 2 * J * NX + (o - J * NX));
+      res[o] = v;
+    }
+  }
+  __syncthreads();
+  if (tid == 0) st->tickets[TK_DOT] = 0;
+  gs_epilogue<NX>(a, res, mode);
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// Half B
+// ---------------------------------------------------------------------------------------------------------------
+template <int NX, bool LEVELS32>
+__global__ void __maxnreg__(152) k_gs_update_tc(StepArgs a, int mode, GTArgs g) {
+  KrylovState *st = a.st;
+  if (st->stop) return;
+  extern __shared__ __align__(1024) unsigned char sm[];
+  __shared__ int s_last, s_es[2];
+  const GTShared S = gt_shared(sm, GT_UPD_MISC);
+  volatile int *abort = S.ints;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int n = a.n, J = a.J, NKS = (J + 15) / 16;
+  const double sigma = st->sigma, invnu = st->invnu, tsig = st->tau_sigma;
+  double *U = static_cast<double *>(a.U);
+  double *W = static_cast<double *>(a.W);
+  const double *V = static_cast<const double *>(a.V);
+  const int ntiles = (n + GT_R - 1) / GT_R;
+  const int my = blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+  if (tid == 0) {
+    for (int i = 0; i < 64; ++i) S.ints[i] = 0;
+    s_es[0] = s_es[1] = 0;
+    gt_init_barriers(S);
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(t5_smem(S.tslot)),
+                 "r"(GT_TMEM)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  __syncthreads();
+  unsigned char *As = sm + GT_AOFF;
+  unsigned char *Bs = sm + GT_BOFF;
+  // the scales of s and g (all threads), then their slices: [k8][x][8 slices][8 columns]
+  {
+    int Es = 0, Eg = 0;
+    for (int j = tid; j < J; j += GT_THREADS) {
+      Es = max(Es, gt_expo(a.coef[j]));
+      if (NX == 2) Eg = max(Eg, gt_expo(a.coef[J + j]));
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+      Es = max(Es, __shfl_xor_sync(0xffffffffu, Es, off));
+      Eg = max(Eg, __shfl_xor_sync(0xffffffffu, Eg, off));
+    }
+    if (lane == 0) {
+      atomicMax(&s_es[0], Es);
+      atomicMax(&s_es[1], Eg);
+    }
+  }
+  __syncthreads();
+  const int es = gt_escale(s_es[0]), eg = gt_escale(s_es[1]);
+  for (int it = tid; it < 2 * NKS * 2; it += GT_THREADS) {
+    const int x = it & 1, k8 = it >> 1;  // coefficients j = 8 k8 .. 8 k8 + 7 of vector x
+    double cv[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const int j = 8 * k8 + k;
+      cv[k] = (j < J && (x == 0 || NX == 2)) ? a.coef[x * J + j] : 0.0;
+    }
+    uint4 sl[8];
+    int ovf = 0;
+    gt_slice8(cv, x ? eg : es, sl, &ovf);
+    unsigned char *base = Bs + (size_t)(k8 * 2 + x) * 128;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) *reinterpret_cast<uint4 *>(base + q * 16) = sl[q];
+  }
+  gt_fence_async_smem();
+  t5_fence_before();
+  __syncthreads();
+  t5_fence_after();
+  const uint32_t tbase = *S.tslot;
+  double nrm = 0.0;
+
+  if (warp < GT_EW) {
+    // ---------------- epilogue warps: row e of each tile ----------------
+    const int e = tid;
+    for (int i = 0; i < my; ++i) {
+      const int b = i & 1, slot = i & 3;
+      const int T = blockIdx.x + i * gridDim.x;
+      const long long r = (long long)T * GT_R + e;
+      double u = 0.0, w = 0.0;
+      if (r < n) {
+        u = U[r];
+        if (NX == 2) w = W[r];
+      }
+      // the tile's row scale: the largest recorded exponent of its columns (each warp on its own; the slicers
+      // compute the same value)
+      int etile = -128;
+      for (int j = lane; j < J; j += 32) etile = max(etile, (int)g.vexp[(size_t)j * g.ldt + T]);
+      for (int off = 16; off > 0; off >>= 1) etile = max(etile, __shfl_xor_sync(0xffffffffu, etile, off));
+      if (!gt_wait(&S.bar[GB_CDONE + b], (uint32_t)((i >> 1) & 1), abort)) break;
+      t5_fence_after();
+      // the 15 levels p + q of each vector: FP32 sums (exact while J <= 128: |level| <= 8 * 128 * 127^2 < 2^24),
+      // else 64-bit integer sums
+      using LT = typename std::conditional<LEVELS32, float, long long>::type;
+      LT lev[NX][15];
+#pragma unroll
+      for (int x = 0; x < NX; ++x)
+#pragma unroll
+        for (int L = 0; L < 15; ++L) lev[x][L] = 0;
+#pragma unroll
+      for (int p = 0; p < 8; ++p) {
+        float v[16];
+        t5_ld16(tbase + ((uint32_t)(32 * warp) << 16) + (uint32_t)(b * 128 + p * 16), v);
+#pragma unroll
+        for (int x = 0; x < NX; ++x)
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            if constexpr (LEVELS32) lev[x][p + q] += v[x * 8 + q];
+            else lev[x][p + q] += (long long)__float2int_rn(v[x * 8 + q]);
+          }
+      }
+      t5_fence_before();
+      __syncwarp();
+      if (lane == 0) gt_arrive(&S.bar[GB_TFREE + b]);
+      double prod[2] = {0.0, 0.0};
+#pragma unroll
+      for (int x = 0; x < NX; ++x) {
+        long long A3 = 0, B3 = 0, C3 = 0;  // levels 0-4, 5-9, 10-14, each sum below 2^53 in magnitude
+#pragma unroll
+        for (int L = 0; L < 15; ++L) {
+          long long t;
+          if constexpr (LEVELS32) t = (long long)__float2int_rn(lev[x][L]);
+          else t = lev[x][L];
+          if (L < 5) A3 += t * (1ll << (7 * (4 - L)));
+          else if (L < 10) B3 += t * (1ll << (7 * (9 - L)));
+          else C3 += t * (1ll << (7 * (14 - L)));
+        }
+        // X = A3 2^70 + B3 2^35 + C3;  (V c)_r = 2^(etile + e_c - 112) X
+        const double xs = fma(__ll2double_rn(A3), 1180591620717411303424.0,
+                              fma(__ll2double_rn(B3), 34359738368.0, __ll2double_rn(C3)));
+        prod[x] = (etile > -128) ? xs * gt_pow2(etile + (x ? eg : es) - 112) : 0.0;
+      }
+      int Eu = 0;
+      if (r < n) {
+        const double un = (sigma * u - prod[0]) * invnu;
+        U[r] = un;
+        Eu = gt_expo(un);
+        if (NX == 2) {
+          const double wo = w - prod[1] - tsig * u;
+          W[r] = wo;
+          nrm = fma(wo, wo, nrm);
+        }
+      }
+      // the exponent of the new column v_j over this tile, read by later launches: the warps' maxima meet in a
+      // per-tile slot; the last of the four warps to arrive writes the table entry
+      for (int off = 16; off > 0; off >>= 1) Eu = max(Eu, __shfl_xor_sync(0xffffffffu, Eu, off));
+      if (lane == 0) {
+        S.ints[16 + 4 * slot + warp] = Eu;
+        __threadfence_block();
+        if (atomicAdd(&S.ints[12 + slot], 1) == GT_EW - 1) {
+          int m = 0;
+#pragma unroll
+          for (int q = 0; q < GT_EW; ++q) m = max(m, *(volatile int *)&S.ints[16 + 4 * slot + q]);
+          g.vexp[(size_t)a.j * g.ldt + T] = (signed char)gt_escale(m);
+          S.ints[12 + slot] = 0;
+        }
+      }
+    }
+  } else if (warp == GT_MWARP) {
+    if (lane == 0) {
+      const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(16 >> 3) << 17) |
+                             ((uint32_t)(GT_R >> 4) << 24);
+      const uint32_t bbase = t5_smem(Bs);
+      int q = 0;
+      bool ok = true;
+      for (int i = 0; i < my && ok; ++i) {
+        const int b = i & 1, u = i >> 1;
+        if (u >= 1 && !gt_wait(&S.bar[GB_TFREE + b], (uint32_t)((u - 1) & 1), abort)) { ok = false; break; }
+        for (int ks = 0; ks < NKS; ++ks, ++q) {
+          const int sa = q % GT_NA;
+          if (!gt_wait(&S.bar[GB_AFULL + sa], (uint32_t)((q / GT_NA) & 1), abort)) { ok = false; break; }
+          t5_fence_after();
+          const uint32_t abase = t5_smem(As + (size_t)sa * GT_STAGE);
+          const uint64_t bd = t5_desc(bbase + (uint32_t)(ks * 2 * 256), 256, 128);
+#pragma unroll
+          for (int p = 0; p < 8; ++p) {
+            const uint64_t ad = t5_desc(abase + p * 4096, 2048, 128);
+            t5_mma(tbase + (uint32_t)(b * 128 + p * 16), ad, bd, idesc, ks > 0 ? 1u : 0u);
+          }
+          t5_commit(&S.bar[GB_AEMPTY + sa]);
+        }
+        if (ok) t5_commit(&S.bar[GB_CDONE + b]);
+      }
+      t5_commit(&S.bar[GB_FIN]);
+      if (!t5_wait(&S.bar[GB_FIN], 0)) *abort = 1;
+    }
+  } else {
+    // ---------------- slicers: item = (row rl, 8-column group kg) of a 16-column stage ----------------
+    const int s = tid - 32 * GT_SW0;
+    const int rl = s & 127, kg = s >> 7;
+    int q = 0, ovf = 0;
+    bool ok = true;
+    for (int i = 0; i < my && ok; ++i) {
+      const int T = blockIdx.x + i * gridDim.x;
+      const long long r = (long long)T * GT_R + rl;
+      int etile = -128;  // as the epilogue warps compute it
+      for (int j = lane; j < J; j += 32) etile = max(etile, (int)g.vexp[(size_t)j * g.ldt + T]);
+      for (int off = 16; off > 0; off >>= 1) etile = max(etile, __shfl_xor_sync(0xffffffffu, etile, off));
+      for (int ks = 0; ks < NKS && ok; ++ks, ++q) {
+        const int sa = q % GT_NA;
+        double v[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          const int j = ks * 16 + kg * 8 + k;
+          v[k] = (j < J && r < n) ? __ldcs(V + (size_t)j * a.ldv + r) : 0.0;
+        }
+        uint4 sl[8];
+        gt_slice8(v, etile, sl, &ovf);
+        if (q >= GT_NA && !gt_wait(&S.bar[GB_AEMPTY + sa], (uint32_t)(((q / GT_NA) - 1) & 1), abort)) {
+          ok = false;
+          break;
+        }
+        unsigned char *dst = As + (size_t)sa * GT_STAGE + (size_t)((kg * 16 + (rl >> 3)) * 128 + (rl & 7) * 16);
+#pragma unroll
+        for (int p = 0; p < 8; ++p) *reinterpret_cast<uint4 *>(dst + p * 4096) = sl[p];
+        gt_fence_async_smem();
+        __syncwarp();
+        if (lane == 0) gt_arrive(&S.bar[GB_AFULL + sa]);
+      }
+    }
+    if (ovf) atomicExch(g.err, 2);
+  }
+  t5_fence_before();
+  __syncthreads();
+  t5_fence_after();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(GT_TMEM) : "memory");
+  if (*abort && tid == 0) atomicExch(g.err, 1);
+  if (NX == 1) return;
+  // ||w'||^2: the epilogue threads' sums in a fixed order, per block, then the last block (as k_gs_update)
+  if (warp < GT_EW) {
+    for (int off = 16; off > 0; off >>= 1) nrm += __shfl_down_sync(0xffffffffu, nrm, off);
+    if (lane == 0) S.red[warp] = nrm;
+  }
+  __syncthreads();
+  double *pb = g.part;
+  if (tid == 0) {
+    double v = 0.0;
+    for (int w = 0; w < GT_EW; ++w) v += S.red[w];
+    pb[blockIdx.x] = v;
+  }
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) s_last = (atomicAdd(&st->tickets[TK_UPD], 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  if (tid == 0) {
+    double v = 0.0;
+    for (int b2 = 0; b2 < (int)gridDim.x; ++b2) v += __ldcg(pb + b2);
+    const double beta = sqrt(v);
+    st->tickets[TK_UPD] = 0;
+    if (beta == 0.0 || !(beta == beta)) {
+      st->stop = 1;
+      st->breakdown = 1;
+      st->m = a.j + 1;
+      st->beta_out = 0.0;
+      if (a.hermitian) a.e[a.j] = 0.0;
+      else a.H[(a.j + 1) + (size_t)a.j * a.ldh] = 0.0;
+    } else {
+      st->sigma = 1.0 / beta;
+      st->beta_prev = beta * st->invnu;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------------------------------------------
+int gs_tc_max_columns() { return GT_MAXJ; }
+
+// tiles per chunk of half A: the longest chunk that still leaves three chunks per block
+static int gs_tc_chunk_tiles(int n, int grid) {
+  const int ntiles = (n + GT_R - 1) / GT_R;
+  for (int ct = GT_CTMAX; ct > 1; ct >>= 1)
+    if ((ntiles + ct - 1) / ct >= 3 * grid) return ct;
+  return 1;
+}
+
+size_t gs_tc_part_doubles() { return (size_t)num_sms() * (4 * GT_MAXJ + 8); }
+
+cudaError_t launch_gs_dot_tc(const StepArgs &a, int nx, int mode, const GTArgs &g0, cudaStream_t s) {
+  if (a.J < 1 || a.J > GT_MAXJ || nx < 1 || nx > 2) return cudaErrorInvalidValue;
+  GTArgs g = g0;
+  const int ntiles = (a.n + GT_R - 1) / GT_R;
+  int grid = num_sms();
+  g.ct = gs_tc_chunk_tiles(a.n, grid);
+  const int nchunks = (ntiles + g.ct - 1) / g.ct;
+  if (grid > nchunks) grid = nchunks;
+  g.pstride = 4 * GT_MAXJ + 8;
+  cudaError_t e;
+  if (nx == 2) {
+    e = cudaFuncSetAttribute(k_gs_dot_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GT_DOT_SMEM);
+    if (e != cudaSuccess) return e;
+    k_gs_dot_tc<2><<<grid, GT_THREADS, GT_DOT_SMEM, s>>>(a, mode, g);
+  } else {
+    e = cudaFuncSetAttribute(k_gs_dot_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GT_DOT_SMEM);
+    if (e != cudaSuccess) return e;
+    k_gs_dot_tc<1><<<grid, GT_THREADS, GT_DOT_SMEM, s>>>(a, mode, g);
+  }
+  return cudaGetLastError();
+}
+
+template <int NX, bool L32>
+static cudaError_t upd_go(const StepArgs &a, int mode, const GTArgs &g, int grid, cudaStream_t s) {
+  const cudaError_t e =
+      cudaFuncSetAttribute(k_gs_update_tc<NX, L32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GT_UPD_SMEM);
+  if (e != cudaSuccess) return e;
+  k_gs_update_tc<NX, L32><<<grid, GT_THREADS, GT_UPD_SMEM, s>>>(a, mode, g);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gs_update_tc(const StepArgs &a, int nx, int mode, const GTArgs &g, cudaStream_t s) {
+  if (a.J < 1 || a.J > GT_MAXJ || nx < 1 || nx > 2) return cudaErrorInvalidValue;
+  const int ntiles = (a.n + GT_R - 1) / GT_R;
+  int grid = num_sms();
+  if (grid > ntiles) grid = ntiles;
+  // level sums exact in FP32 while 8 * J * 127^2 < 2^24, i.e. J <= 128
+  const bool l32 = a.J <= 128;
+  if (nx == 2) return l32 ? upd_go<2, true>(a, mode, g, grid, s) : upd_go<2, false>(a, mode, g, grid, s);
+  return l32 ? upd_go<1, true>(a, mode, g, grid, s) : upd_go<1, false>(a, mode, g, grid, s);
+}
+
+}  // namespace ksg

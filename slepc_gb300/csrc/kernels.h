@@ -75,6 +75,22 @@ struct LongRows {
   void *part = nullptr;
 };
 
+// The Gram-Schmidt pair for IEEE-double storage on the tensor cores (k_gs_tc.cu).  The basis columns' scales live in
+// an int8 table [column][128-row tile] (leading dimension ldt, a multiple of 8): the update half and the tcgen05
+// restart record the exponents of the columns they write.
+struct GTArgs {
+  signed char *vexp;  // exponent e of each (column, tile): every |v| < 2^e there; -128 for an all-zero tile
+  int ldt;            // tiles per column in the table (a multiple of 8)
+  int ct;             // half A: tiles per chunk (set by the launcher)
+  double *part;       // per-block partials (gs_tc_part_doubles() doubles)
+  int pstride;        // half A: doubles per block in part (set by the launcher)
+  int *err;           // set to 1 when a bounded wait ran out, to 2 when a value reached its recorded scale
+};
+int gs_tc_max_columns();
+size_t gs_tc_part_doubles();
+cudaError_t launch_gs_dot_tc(const StepArgs &a, int nx, int mode, const GTArgs &g, cudaStream_t s);
+cudaError_t launch_gs_update_tc(const StepArgs &a, int nx, int mode, const GTArgs &g, cudaStream_t s);
+
 int num_sms();
 int spmv_lanes_for(double avg_nnz);
 int gs_dot_blocks(int n);

@@ -82,16 +82,17 @@ def test_refined_nearly_degenerate_pairs(lib, lock):
     assert verify.orthogonality(res["X"][:, :res["nconv"]]) <= 1e-12
 
 
-@pytest.mark.parametrize("arith", ["f64", "pair"])
-def test_lap3d64_nev50_ncv128_host_parity(lib, arith):
-    """The 128^3 workload's shape at 64^3 (nev 50, ncv 128, tol 1e-10, largest algebraic) with the default
-    mixed-precision projected solver: a degenerate spectrum with pairs just outside the cluster threshold, where the
-    refinement alone left mixed Ritz vectors.  Checked on the host: eigenvalues against the closed form (set-based
-    over distinct values), residuals with scipy.sparse, ||X^T X - I|| in numpy."""
+@pytest.mark.parametrize("arith,ds", [("f64", "qr"), ("pair", "qr"), ("f64", "refined")])
+def test_lap3d64_nev50_ncv128_host_parity(lib, arith, ds):
+    """The 128^3 workload's shape at 64^3 (nev 50, ncv 128, tol 1e-10, largest algebraic): a degenerate spectrum
+    with pairs just outside the cluster threshold of the mixed-precision projected solver, where its refinement
+    alone left mixed Ritz vectors (now caught by its check and redone in FP64).  Checked on the host: eigenvalues
+    against the closed form (set-based over distinct values), residuals with scipy.sparse, ||X^T X - I|| in
+    numpy."""
     m = 64
     csr = matgen.laplacian_3d(m)
     res = sg.solve(csr, hermitian=True, which="LR", nev=50, ncv=128, tol=1e-10, v0=matgen.start_vector(m ** 3, 2),
-                   arith=arith)
+                   arith=arith, ds=ds)
     assert res["reason"] == 1 and res["nconv"] >= 50
     k = res["nconv"]
     p = verify.parity_block(csr, res["eigr"][:k], res["X"][:, :k], matgen.laplacian_eigenvalues([m] * 3), "LR", 50,
