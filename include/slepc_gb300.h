@@ -39,6 +39,19 @@ PetscErrorCode EPSGB300GetArithmetic(EPS eps, EPSGB300Arith *arith);
  *       spectrum is well separated; on dense clusters (the 3-D Laplacians) every restart falls back.
  * The non-Hermitian solver and the DS object always use the FP64 algorithms.  Option -eps_gb300_ds refined|qr. */
 typedef enum { EPS_GB300_DS_REFINED = 0, EPS_GB300_DS_QR = 1 } EPSGB300DSMethod;  /* default: EPS_GB300_DS_QR */
+
+/* Gram-Schmidt of IEEE-double storage (EPS_GB300_ARITH_F64) inside EPSSolve.  No counterpart in the reference, whose
+ * orthogonalisation (BVOrthogonalizeCGS1, src/sys/classes/bv/interface/bvorthog.c:91-132) calls FP64 BLAS gemv.
+ *   EPS_GB300_GS_TENSOR (default): every product of the two Gram-Schmidt halves exact on the bf16 tensor cores
+ *       (an error-free 8 x 7-bit slice split of the 56-bit fixed point of each value against its column/tile
+ *       exponent), the slice sums recombined as exact integers, rounded once per 1024-row chunk and accumulated in
+ *       double-double: more accurate than FP64 FMA, and not bound by GB300's FP64 pipe.  Used for the symmetric
+ *       (Lanczos) variant with the tcgen05 restart; the other cases use the FMA kernels.
+ *   EPS_GB300_GS_FMA: IEEE FP64 FMA in every product (FP64-pipe bound on GB300).
+ * Option -eps_gb300_gs tensor|fma. */
+typedef enum { EPS_GB300_GS_TENSOR = 0, EPS_GB300_GS_FMA = 1 } EPSGB300GSMethod;
+PetscErrorCode EPSGB300SetGSMethod(EPS eps, EPSGB300GSMethod method);
+PetscErrorCode EPSGB300GetGSMethod(EPS eps, EPSGB300GSMethod *method);
 PetscErrorCode EPSGB300SetProjectedSolver(EPS eps, EPSGB300DSMethod method);
 PetscErrorCode EPSGB300GetProjectedSolver(EPS eps, EPSGB300DSMethod *method);
 

@@ -81,6 +81,7 @@ def load():
         "EPSGB300ServerCancel": ([P], I),
         "EPSGB300SetTimeLimit": ([P, D], I),
         "EPSGB300SetRestartMethod": ([P, I], I),
+        "EPSGB300SetGSMethod": ([P, I], I),
         "EPSGB300BatchGetTuning": ([ctypes.POINTER(I), I], I),
         "EPSGB300BatchSetTuning": ([ctypes.POINTER(I), I], I),
         "EPSGB300GetStats": ([P, P], I),
@@ -443,6 +444,11 @@ class EPS:
         tensor-core kernel explicitly: 'mma_sync' or 'tcgen05' (bit-identical results)."""
         _check(load().EPSGB300SetRestartMethod(self.handle, self.RESTART_METHODS[method]), "EPSGB300SetRestartMethod")
 
+    def setGSMethod(self, method):
+        """'tensor' (exact slice products on the tensor cores, the default for IEEE-double storage) or 'fma' (IEEE
+        FP64 FMA) for the Gram-Schmidt pair (EPSGB300SetGSMethod)."""
+        _check(load().EPSGB300SetGSMethod(self.handle, 1 if method == "fma" else 0), "EPSGB300SetGSMethod")
+
     def setTimeLimit(self, seconds):
         """Wall-time budget of EPSSolve (checked after each restart; 0 = none)."""
         _check(load().EPSGB300SetTimeLimit(self.handle, float(seconds)), "EPSGB300SetTimeLimit")
@@ -669,7 +675,7 @@ def batch_set_tuning(tiles):
 
 def solve(csr, *, hermitian=True, which="LM", nev=1, ncv=None, mpd=None, tol=None, max_it=None, v0=None,
           arith="pair", vectors=True, ds=None, lock=None, restart=None, harmonic=False, target=None, B=None,
-          conv=None, purify=None):
+          conv=None, purify=None, gs=None):
     """One-call convenience: returns dict(eigr, eigi, X, nconv, its, reason, errors, stats).  B (CSR arrays of a
     diagonal matrix) makes the problem generalised: EPS_GHEP when hermitian, else EPS_GNHEP."""
     A = Mat(*csr)
@@ -696,6 +702,8 @@ def solve(csr, *, hermitian=True, which="LM", nev=1, ncv=None, mpd=None, tol=Non
         eps.setProjectedSolver(ds)
     if restart is not None:
         eps.setRestartMethod(restart)
+    if gs is not None:
+        eps.setGSMethod(gs)
     if lock is not None:
         eps.setKrylovSchurLocking(lock)
     if v0 is not None:

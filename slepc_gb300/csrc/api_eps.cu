@@ -572,8 +572,9 @@ size_t ksg_part_blocks(int n) { return (size_t)std::max(gs_dot_blocks(n), gs_upd
 
 PetscErrorCode ksg_orthonormalize_column(void *V, long long ldv, int n, int j, double *coef, float2 *part,
                                          int pstride, KrylovState *st, int arith, cudaStream_t s, double *nrm,
-                                         int *lindep, int refine, int storage) {
+                                         int *lindep, int refine, int storage, const GTArgs *tc) {
   StepArgs a = {};
+  a.tc = tc;
   a.V = V;
   a.ldv = ldv;
   a.n = n;
@@ -637,6 +638,10 @@ static PetscErrorCode eps_free_device(EPS eps) {
   eps->seg_part.release();
   eps->xvec.release();
   eps->d_perm.release();
+  eps->vexp.release();
+  eps->gtpart.release();
+  eps->gterr.release();
+  eps->gs_tc_on = 0;
   eps->xvec_valid = 0;
   eps->rtc.release();
   eps->part.release();
@@ -987,6 +992,18 @@ extern "C" PetscErrorCode EPSGB300GetProjectedSolver(EPS eps, EPSGB300DSMethod *
   *method = (EPSGB300DSMethod)eps->ds_method;
   return 0;
 }
+extern "C" PetscErrorCode EPSGB300SetGSMethod(EPS eps, EPSGB300GSMethod method) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  KSG_CHECK(method == EPS_GB300_GS_TENSOR || method == EPS_GB300_GS_FMA, PETSC_ERR_ARG_OUTOFRANGE,
+            "Unknown Gram-Schmidt method");
+  eps->gs_method = method;
+  return 0;
+}
+extern "C" PetscErrorCode EPSGB300GetGSMethod(EPS eps, EPSGB300GSMethod *method) {
+  KSG_CHECK(eps && method, PETSC_ERR_ARG_NULL, "Null argument");
+  *method = (EPSGB300GSMethod)eps->gs_method;
+  return 0;
+}
 extern "C" PetscErrorCode EPSGB300SetRestartMethod(EPS eps, EPSGB300RestartMethod method) {
   KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
   KSG_CHECK(method >= EPS_GB300_RESTART_TENSOR && method <= EPS_GB300_RESTART_TCGEN05, PETSC_ERR_ARG_OUTOFRANGE,
@@ -1136,6 +1153,8 @@ extern "C" PetscErrorCode EPSSetFromOptions(EPS eps) {
                                                                      : EPS_GB300_RESTART_TENSOR));
     else if (!strcmp(o, "-eps_gb300_ds") && v)
       KSG_TRY(EPSGB300SetProjectedSolver(eps, !strcmp(v, "qr") ? EPS_GB300_DS_QR : EPS_GB300_DS_REFINED));
+    else if (!strcmp(o, "-eps_gb300_gs") && v)
+      KSG_TRY(EPSGB300SetGSMethod(eps, !strcmp(v, "fma") ? EPS_GB300_GS_FMA : EPS_GB300_GS_TENSOR));
   }
   return 0;
 }
@@ -1293,6 +1312,20 @@ extern "C" PetscErrorCode EPSSetUp(EPS eps) {
   KSG_CUDA(cudaMemsetAsync(eps->e.p, 0, sizeof(double) * eps->e.count, eps->stream));
   if (!eps->h_ctl) KSG_CUDA(cudaMallocHost((void **)&eps->h_ctl, sizeof(KSControl)));
   eps->storage = (eps->arith == ARITH_F64) ? STORE_F64 : STORE_PAIR;  // the precision form switches per phase
+  if (eps->storage == STORE_F64) {
+    // tensor-core Gram-Schmidt: the exponent table (every entry 1 until written: |v| < 2 holds for unit columns),
+    // the per-block partials and the error flag
+    const int ldt = ((n + 127) / 128 + 7) / 8 * 8;
+    KSG_CUDA(eps->vexp.alloc((size_t)ldt * (ld + 1)));
+    KSG_CUDA(cudaMemsetAsync(eps->vexp.p, 1, eps->vexp.count, eps->stream));
+    KSG_CUDA(eps->gtpart.alloc(gs_tc_part_doubles()));
+    KSG_CUDA(eps->gterr.alloc(1));
+    KSG_CUDA(cudaMemsetAsync(eps->gterr.p, 0, sizeof(int), eps->stream));
+    eps->gt.vexp = eps->vexp.p;
+    eps->gt.ldt = ldt;
+    eps->gt.part = eps->gtpart.p;
+    eps->gt.err = eps->gterr.p;
+  }
   KSG_TRY(eps_setup_operator(eps));
   Mat op = eps->op;
   KSG_TRY(ksg_mat_upload(op));
@@ -1412,6 +1445,7 @@ static PetscErrorCode eps_factorize(EPS eps, int k0, int nv, double *bytes) {
   a.part = eps->part.p;
   a.pstride = eps->pstride;
   a.st = eps->st.p;
+  a.tc = eps->gs_tc_on ? &eps->gt : nullptr;
   const double colb = 8.0 * n;
   const Mat op = eps->op;
   LongRows lr;
@@ -1526,7 +1560,8 @@ PetscErrorCode ksg_eps_new_start_vector(EPS eps, int col, int *breakdown) {
   double nrm = 0.0;
   int ld = 0;
   KSG_TRY(ksg_orthonormalize_column(eps->V.p, eps->ldv, eps->n, col, eps->coef.p, eps->part.p, eps->pstride,
-                                    eps->st.p, eps->arith, eps->stream, &nrm, &ld, 2, eps->storage));
+                                    eps->st.p, eps->arith, eps->stream, &nrm, &ld, 2, eps->storage,
+                                    eps->gs_tc_on ? &eps->gt : nullptr));
   *breakdown = ld || nrm == 0.0;
   return 0;
 }
@@ -1627,7 +1662,8 @@ static cudaError_t eps_restart(EPS eps, int a0, int K, int s0, int N, const doub
         if (e != cudaSuccess) return e;
       }
       if (eps->storage == STORE_F64)
-        return launch_restart_t5_f64(eps->V.p, eps->ldv, eps->n, a0, K, s0, N, Q, eps->ld, eps->rtc.p, eps->ld, s);
+        return launch_restart_t5_f64(eps->V.p, eps->ldv, eps->n, a0, K, s0, N, Q, eps->ld, eps->rtc.p, eps->ld, s,
+                                     eps->vexp.p, eps->gt.ldt);
       return launch_restart_t5(reinterpret_cast<float2 *>(eps->V.p), eps->ldv, eps->n, a0, K, s0, N, Q, eps->ld,
                                eps->rtc.p, eps->ld, s);
     }
@@ -1678,13 +1714,23 @@ static PetscErrorCode eps_solve_core(EPS eps, double tol, std::chrono::steady_cl
   const int n = eps->n, ld = eps->ld, ncv = eps->ncv_e, mpd = eps->mpd_e, nev = eps->nev_e;
   const int herm = ksg_eps_lanczos(eps);
   const int harmonic = eps->extraction == EPS_HARMONIC;
+  // IEEE-double Gram-Schmidt on the tensor cores: the symmetric (Lanczos) variant with the tcgen05 restart, whose
+  // kernels and this one keep the basis columns' exponent table up to date
+  {
+    const int rm = eps->restart_method;
+    eps->gs_tc_on = eps->storage == STORE_F64 && eps->arith == ARITH_F64 && eps->gs_method == EPS_GB300_GS_TENSOR &&
+                    herm && eps->vexp.p && ld <= gs_tc_max_columns() &&
+                    (rm == EPS_GB300_RESTART_TCGEN05 || (rm == EPS_GB300_RESTART_TENSOR && kRestartTensorIsTcgen05));
+    if (eps->gs_tc_on) KSG_CUDA(cudaMemsetAsync(eps->gterr.p, 0, sizeof(int), s));
+  }
   // start vector: the initial space, or a random vector (EPSGetStartVector, epssolve.c:841-873)
   {
     KSG_TRY(ksg_eps_put_start(eps, s));
     double nrm = 0.0;
     int lindep = 0;
     KSG_TRY(ksg_orthonormalize_column(eps->V.p, eps->ldv, n, 0, eps->coef.p, eps->part.p, eps->pstride, eps->st.p,
-                                      eps->arith, s, &nrm, &lindep, 1, eps->storage));
+                                      eps->arith, s, &nrm, &lindep, 1, eps->storage,
+                                      eps->gs_tc_on ? &eps->gt : nullptr));
     KSG_CHECK(!lindep && nrm != 0.0, PETSC_ERR_PLIB, "Initial vector is zero or belongs to the deflation space");
   }
   KSG_CUDA(cudaMemsetAsync(eps->d.p, 0, sizeof(double) * eps->d.count, s));
@@ -1911,6 +1957,13 @@ extern "C" PetscErrorCode EPSSolve(EPS eps) {
     int flag = 0;  // a bounded wait of the tcgen05 restart ran out (the kernel freed its TMEM and returned)
     KSG_CUDA(cudaMemcpy(&flag, restart_t5_errflag(eps->rtc.p, eps->ld), sizeof(int), cudaMemcpyDeviceToHost));
     KSG_CHECK(!flag, PETSC_ERR_GPU, "tcgen05 restart: a bounded wait ran out; results are not valid");
+  }
+  if (eps->gs_tc_on) {
+    int flag = 0;  // 1: a bounded wait of a tensor-core Gram-Schmidt kernel ran out; 2: a value reached its scale
+    KSG_CUDA(cudaMemcpy(&flag, eps->gterr.p, sizeof(int), cudaMemcpyDeviceToHost));
+    KSG_CHECK(flag != 1, PETSC_ERR_GPU, "tensor-core Gram-Schmidt: a bounded wait ran out; results are not valid");
+    KSG_CHECK(flag != 2, PETSC_ERR_PLIB,
+              "tensor-core Gram-Schmidt: a basis value exceeded its recorded exponent; results are not valid");
   }
   {
     float ms = 0.0f;

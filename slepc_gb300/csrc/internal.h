@@ -163,6 +163,7 @@ struct _p_EPS {
   int arith = ksg::ARITH_PAIR;
   int storage = ksg::STORE_PAIR;  // basis format: pairs with pair arithmetic, doubles with FP64 arithmetic
   int ds_method = EPS_GB300_DS_QR;  // EPSGB300DSMethod
+  int gs_method = EPS_GB300_GS_TENSOR;  // EPSGB300GSMethod
   double time_limit = 0.0;        // EPSGB300SetTimeLimit (0: none)
   int restart_method = 0;         // EPSGB300RestartMethod
   int device = -1;
@@ -188,6 +189,11 @@ struct _p_EPS {
   cudaStream_t stream = nullptr;
   DBuf<double> V, d, e, H, Q, X, eigr, eigi, errest, coef, work, dsf;
   DBuf<double> seg_part;  // one 8-byte partial per long-row segment of the operator
+  DBuf<signed char> vexp;  // tensor-core Gram-Schmidt: exponents of the basis columns per 128-row tile
+  DBuf<double> gtpart;     // its per-block partials
+  DBuf<int> gterr;         // its error flag
+  ksg::GTArgs gt = {};
+  int gs_tc_on = 0;        // the current solve runs the tensor-core Gram-Schmidt
   DBuf<double> xvec;      // EPSGB300GetDeviceEigenvectors: FP64 eigenvectors in EPSGetEigenpair order
   DBuf<int> d_perm;       // its column map
   int xvec_valid = 0;     // xvec holds the current solve's vectors
@@ -235,7 +241,8 @@ inline int ksg_eps_lanczos(EPS e) { return ksg_eps_hermitian(e) && e->extraction
 // norm of the orthogonalised vector in *nrm and the linear-dependence flag (two CGS passes)
 PetscErrorCode ksg_orthonormalize_column(void *V, long long ldv, int n, int j, double *coef, float2 *part,
                                          int pstride, ksg::KrylovState *st, int arith, cudaStream_t s, double *nrm,
-                                         int *lindep, int refine, int storage = ksg::STORE_F64);
+                                         int *lindep, int refine, int storage = ksg::STORE_F64,
+                                         const ksg::GTArgs *tc = nullptr);
 PetscErrorCode ksg_mat_upload_pairs(Mat A);
 PetscErrorCode ksg_mat_upload_f32(Mat A);
 // address of basis column j for the storage format (8 bytes per entry, 4 for STORE_F32; same leading dimension)

@@ -775,6 +775,27 @@ __global__ void __maxnreg__(152) k_gs_update_tc(StepArgs a, int mode, GTArgs g) 
   }
 }
 
+// the exponent of each 128-row tile of one basis column written by another kernel (one block per tile)
+__global__ void k_record_vexp(const double *col, int n, signed char *vexp_col) {
+  const long long r = (long long)blockIdx.x * GT_R + threadIdx.x;
+  int E = r < n ? gt_expo(col[r]) : 0;
+  for (int off = 16; off > 0; off >>= 1) E = max(E, __shfl_xor_sync(0xffffffffu, E, off));
+  __shared__ int wm[GT_R / 32];
+  if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = E;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int m = 0;
+    for (int w = 0; w < GT_R / 32; ++w) m = max(m, wm[w]);
+    vexp_col[blockIdx.x] = (signed char)gt_escale(m);
+  }
+}
+
+cudaError_t launch_record_vexp(const double *col, int n, signed char *vexp_col, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_record_vexp<<<(n + GT_R - 1) / GT_R, GT_R, 0, s>>>(col, n, vexp_col);
+  return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------------------------------------------

@@ -357,7 +357,13 @@ static cudaError_t dot_dispatch(const StepArgs &a, int mode, int blocks, cudaStr
 }
 
 // storage: STORE_F64 (doubles) or STORE_PAIR (FP32 pairs, pair arithmetic only)
+// the tensor-core pair runs IEEE-double Gram-Schmidt when the caller supplies its arguments and the basis has columns
+static bool gs_use_tc(const StepArgs &a, int arith, int storage) {
+  return a.tc && storage == STORE_F64 && arith == ARITH_F64 && a.J >= 1 && a.J <= gs_tc_max_columns();
+}
+
 cudaError_t launch_gs_dot(const StepArgs &a, int nx, int mode, int arith, cudaStream_t s, int storage) {
+  if (gs_use_tc(a, arith, storage)) return launch_gs_dot_tc(a, nx, mode, *a.tc, s);
   const int blocks = gs_dot_blocks(a.n);
   if (storage == STORE_F32)
     return nx == 2 ? dot_dispatch<2, PairAr, StF32>(a, mode, blocks, s) : dot_dispatch<1, PairAr, StF32>(a, mode, blocks, s);
@@ -369,6 +375,16 @@ cudaError_t launch_gs_dot(const StepArgs &a, int nx, int mode, int arith, cudaSt
 }
 
 cudaError_t launch_gs_update(const StepArgs &a, int nx, int mode, int arith, cudaStream_t s, int storage) {
+  if (gs_use_tc(a, arith, storage)) return launch_gs_update_tc(a, nx, mode, *a.tc, s);
+  if (a.tc && storage == STORE_F64 && arith == ARITH_F64 && mode != GS_COMBINE) {
+    // the FP64-FMA kernel writes the column (no basis columns to project out): record its tile exponents for the
+    // tensor-core launches that read it later
+    StepArgs b = a;
+    b.tc = nullptr;
+    const cudaError_t e = launch_gs_update(b, nx, mode, arith, s, storage);
+    if (e != cudaSuccess) return e;
+    return launch_record_vexp(static_cast<const double *>(a.U), a.n, a.tc->vexp + (size_t)a.j * a.tc->ldt, s);
+  }
   const int blocks = gs_update_blocks(a.n);
   const size_t shm = (size_t)nx * (a.J > 0 ? a.J : 1) * 8;
   if (storage == STORE_F32) {

@@ -257,7 +257,7 @@ constexpr int T5_BSL = T5_NC * T5_KC * 2;                  // bytes of one Q sli
 constexpr int T5_STAGE = OZ_SA * T5_ASL + OZ_QMAX * T5_BSL;  // 98304
 constexpr uint32_t T5_TMEM_COLS = OZ_L * T5_NC;            // 512
 constexpr size_t T5_SMEM = 2 * (size_t)T5_STAGE + (T5_THREADS / T5_M + 1) * T5_M * sizeof(int) +
-                           5 * sizeof(unsigned long long) + 16;
+                           5 * sizeof(unsigned long long) + 16 + T5_NC * sizeof(int);
 // Basis storage of the tcgen05 restart.  T5Pair: FP32 pairs (hi, lo); the row exponent comes from hi, the fixed
 // point is the sum of both parts', and the result is written back as a pair.  T5F64: IEEE doubles; the fixed point
 // holds the 53-bit significand (truncated only below 2^-56 of the row maximum), and the result is the exact level
@@ -291,7 +291,7 @@ template <class S, int QS>
 __global__ void __launch_bounds__(T5_THREADS, 1)
     k_restart_t5(typename S::T *__restrict__ V, long long ldv, int n, int a0, int K, int s0, int N, int kp, int np,
                  const __nv_bfloat16 *__restrict__ Bsl, const int *__restrict__ fcol, __nv_bfloat16 *__restrict__ Ascr,
-                 int *__restrict__ err) {
+                 int *__restrict__ err, signed char *__restrict__ vexp, int ldt) {
   using T = typename S::T;
   extern __shared__ __align__(1024) unsigned char sm[];
   int *erow = reinterpret_cast<int *>(sm + 2 * T5_STAGE);
@@ -300,7 +300,11 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
   unsigned long long *empty = full + 2;                                             // stage consumed (MMA commit)
   unsigned long long *vbar = empty + 2;                                             // V tile loaded (TMA bytes)
   uint32_t *tslot = reinterpret_cast<uint32_t *>(vbar + 1);
+  // FP64 storage with a column-exponent table: per output column of a chunk, the largest biased exponent of the
+  // tile's new values (recorded for the tensor-core Gram-Schmidt kernels)
+  int *cmax = reinterpret_cast<int *>(tslot + 4);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid < T5_NC) cmax[tid] = 0;
   const int nk8 = kp / 8;                    // core matrices along K (kp is a multiple of 16)
   const int nkc = (kp + T5_KC - 1) / T5_KC;  // stages per chunk
   __nv_bfloat16 *As = Ascr + (size_t)blockIdx.x * OZ_SA * nk8 * 16 * 64;  // [s][k8][m8][8 rows][8 k]
@@ -556,6 +560,9 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
               else Hs[i2] += pl * w;
             }
           }
+          int ex[16];
+#pragma unroll
+          for (int i2 = 0; i2 < 16; ++i2) ex[i2] = 0;
           if (m < rows) {
 #pragma unroll
             for (int i2 = 0; i2 < 16; ++i2) {
@@ -567,12 +574,32 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
                 out = fma((double)Hs[i2], t5_pow2(sc + 42), (double)Rs[i2] * t5_pow2(sc));
               }
               V[(size_t)(r0 + m) + (size_t)(s0 + c) * ldv] = out;
+              ex[i2] = (int)(((unsigned long long)__double_as_longlong(out) >> 52) & 0x7FF);
+            }
+          }
+          if (vexp) {
+#pragma unroll
+            for (int i2 = 0; i2 < 16; ++i2) {
+              int x = ex[i2];
+#pragma unroll
+              for (int off = 16; off > 0; off >>= 1) x = max(x, __shfl_xor_sync(0xffffffffu, x, off));
+              if (lane == 0 && x) atomicMax(&cmax[col + i2], x);
             }
           }
         }
       }
       t5_fence_before();
       __syncthreads();  // TMEM is read out before the next chunk's MMAs overwrite it
+      if (vexp && tid < nch) {
+        // the exponent of each output column over this tile: |v| < 2^(E - 1022), -128 for an all-zero tile
+        const int c = c0 + tid;
+        if (c < N) {
+          const int E = cmax[tid];
+          const int e = E == 0 ? -128 : (E - 1022 < -127 ? -127 : (E - 1022 > 127 ? 127 : E - 1022));
+          vexp[(size_t)(s0 + c) * ldt + tile] = (signed char)e;
+        }
+        cmax[tid] = 0;
+      }
     }
   }
   // a V tile load still in flight after a timeout (bounded wait)
@@ -599,7 +626,8 @@ int *restart_t5_errflag(void *scratch, int ld) {
 
 template <class S, int QS>
 static cudaError_t restart_t5_go(typename S::T *V, long long ldv, int n, int a0, int K, int s0, int N,
-                                 const double *Q, int ldq, void *scratch, int ld, cudaStream_t s) {
+                                 const double *Q, int ldq, void *scratch, int ld, cudaStream_t s,
+                                 signed char *vexp = nullptr, int ldt = 0) {
   if (N <= 0 || K <= 0) return cudaSuccess;
   if (K > ld || N > ld) return cudaErrorInvalidValue;
   const int kp = (K + 15) / 16 * 16;
@@ -619,7 +647,8 @@ static cudaError_t restart_t5_go(typename S::T *V, long long ldv, int n, int a0,
   const int ntiles = (n + T5_M - 1) / T5_M;
   int blocks = num_sms();
   if (blocks > ntiles) blocks = ntiles;
-  k_restart_t5<S, QS><<<blocks, T5_THREADS, T5_SMEM, s>>>(V, ldv, n, a0, K, s0, N, kp, np, B, fcol, Ascr, err);
+  k_restart_t5<S, QS><<<blocks, T5_THREADS, T5_SMEM, s>>>(V, ldv, n, a0, K, s0, N, kp, np, B, fcol, Ascr, err, vexp,
+                                                          ldt);
   return cudaGetLastError();
 }
 
@@ -630,9 +659,10 @@ cudaError_t launch_restart_t5(float2 *V, long long ldv, int n, int a0, int K, in
 
 // FP64 storage: Q in 8 slices (56 bits) while the level sums stay exact (K <= 128), else 7
 cudaError_t launch_restart_t5_f64(double *V, long long ldv, int n, int a0, int K, int s0, int N, const double *Q,
-                                  int ldq, void *scratch, int ld, cudaStream_t s) {
-  if ((K + 15) / 16 * 16 <= 128) return restart_t5_go<T5F64, OZ_QMAX>(V, ldv, n, a0, K, s0, N, Q, ldq, scratch, ld, s);
-  return restart_t5_go<T5F64, OZ_S>(V, ldv, n, a0, K, s0, N, Q, ldq, scratch, ld, s);
+                                  int ldq, void *scratch, int ld, cudaStream_t s, signed char *vexp, int ldt) {
+  if ((K + 15) / 16 * 16 <= 128)
+    return restart_t5_go<T5F64, OZ_QMAX>(V, ldv, n, a0, K, s0, N, Q, ldq, scratch, ld, s, vexp, ldt);
+  return restart_t5_go<T5F64, OZ_S>(V, ldv, n, a0, K, s0, N, Q, ldq, scratch, ld, s, vexp, ldt);
 }
 
 cudaError_t launch_restart_tc(float2 *V, long long ldv, int n, int a0, int K, int s0, int N, const double *Q, int ldq,

@@ -90,6 +90,8 @@ int gs_tc_max_columns();
 size_t gs_tc_part_doubles();
 cudaError_t launch_gs_dot_tc(const StepArgs &a, int nx, int mode, const GTArgs &g, cudaStream_t s);
 cudaError_t launch_gs_update_tc(const StepArgs &a, int nx, int mode, const GTArgs &g, cudaStream_t s);
+// the exponents of the 128-row tiles of one IEEE-double column (vexp_col = the table row of that column)
+cudaError_t launch_record_vexp(const double *col, int n, signed char *vexp_col, cudaStream_t s);
 
 int num_sms();
 int spmv_lanes_for(double avg_nnz);
@@ -122,7 +124,8 @@ cudaError_t launch_restart_t5(float2 *V, long long ldv, int n, int a0, int K, in
 // the tcgen05 restart for FP64 storage: Q in 8 slices (7 when K > 128), the exact level sums rounded once to
 // doubles; the same scratch and timeout flag
 cudaError_t launch_restart_t5_f64(double *V, long long ldv, int n, int a0, int K, int s0, int N, const double *Q,
-                                  int ldq, void *scratch, int ld, cudaStream_t s);
+                                  int ldq, void *scratch, int ld, cudaStream_t s, signed char *vexp = nullptr,
+                                  int ldt = 0);
 cudaError_t launch_restart_tc(float2 *V, long long ldv, int n, int a0, int K, int s0, int N, const double *Q, int ldq,
                               void *scratch, int ld, cudaStream_t s);
 cudaError_t launch_segment_begin(KrylovState *st, int k0, int m, cudaStream_t s);

@@ -5,6 +5,8 @@
 
 namespace ksg {
 
+struct GTArgs;
+
 // Arithmetic used by the bandwidth-bound kernels (Gram-Schmidt, restart, residual norms).
 enum Arith : int {
   ARITH_PAIR = 0,  // FP64 storage, products and sums on FP32 pairs with error-free transformations
@@ -77,6 +79,7 @@ struct StepArgs {
   float2 *part;      // per-block partial sums
   int pstride;       // stride between blocks in part (float2 units)
   KrylovState *st;
+  const GTArgs *tc;  // host side: non-null routes IEEE-double Gram-Schmidt to the tensor-core kernels (k_gs_tc.cu)
 };
 
 }  // namespace ksg

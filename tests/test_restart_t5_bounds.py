@@ -13,7 +13,7 @@ T5_M, T5_NC, T5_KC, T5_THREADS = 128, 64, 32, 512
 T5_ASL = T5_M * T5_KC * 2
 T5_BSL = T5_NC * T5_KC * 2
 T5_STAGE = OZ_SA * T5_ASL + OZ_QMAX * T5_BSL
-T5_SMEM = 2 * T5_STAGE + (T5_THREADS // T5_M + 1) * T5_M * 4 + 5 * 8 + 16
+T5_SMEM = 2 * T5_STAGE + (T5_THREADS // T5_M + 1) * T5_M * 4 + 5 * 8 + 16 + T5_NC * 4
 TMEM_COLS = OZ_L * T5_NC
 NUM_SMS = 152
 BF16 = 2
@@ -47,6 +47,8 @@ def check(n, ld, K, N, f64=False):
     erow = 2 * T5_STAGE
     bars = erow + (T5_THREADS // T5_M) * T5_M * 4
     assert bars % 8 == 0 and bars + 5 * 8 + 4 <= T5_SMEM
+    cmax = bars + 5 * 8 + 16                           # per-column exponent maxima (FP64 storage), 64 ints
+    assert cmax % 4 == 0 and cmax + T5_NC * 4 <= T5_SMEM
     nk8 = kp // 8
     ntiles = -(-n // T5_M)
     blocks = min(NUM_SMS, ntiles)
