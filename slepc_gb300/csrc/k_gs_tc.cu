@@ -221,7 +221,7 @@ KS_DEVICE void gt_init_barriers(const GTShared &S) {
 // Half A
 // ---------------------------------------------------------------------------------------------------------------
 template <int NX>
-__global__ void __maxnreg__(152) k_gs_dot_tc(StepArgs a, int mode, GTArgs g) {
+__global__ void __maxnreg__(136) k_gs_dot_tc(StepArgs a, int mode, GTArgs g) {
   KrylovState *st = a.st;
   if (st->stop) return;
   extern __shared__ __align__(1024) unsigned char sm[];
@@ -512,7 +512,7 @@ __global__ void __maxnreg__(152) k_gs_dot_tc(StepArgs a, int mode, GTArgs g) {
 // Half B
 // ---------------------------------------------------------------------------------------------------------------
 template <int NX, bool LEVELS32>
-__global__ void __maxnreg__(152) k_gs_update_tc(StepArgs a, int mode, GTArgs g) {
+__global__ void __maxnreg__(136) k_gs_update_tc(StepArgs a, int mode, GTArgs g) {
   KrylovState *st = a.st;
   if (st->stop) return;
   extern __shared__ __align__(1024) unsigned char sm[];
@@ -600,38 +600,31 @@ __global__ void __maxnreg__(152) k_gs_update_tc(StepArgs a, int mode, GTArgs g) 
       for (int off = 16; off > 0; off >>= 1) etile = max(etile, __shfl_xor_sync(0xffffffffu, etile, off));
       if (!gt_wait(&S.bar[GB_CDONE + b], (uint32_t)((i >> 1) & 1), abort)) break;
       t5_fence_after();
-      // the 15 levels p + q of each vector: FP32 sums (exact while J <= 128: |level| <= 8 * 128 * 127^2 < 2^24),
-      // else 64-bit integer sums
+      // per vector, the 15 levels p + q: FP32 sums (exact while J <= 128: |level| <= 8 * 128 * 127^2 < 2^24), else
+      // 64-bit integer sums
       using LT = typename std::conditional<LEVELS32, float, long long>::type;
-      LT lev[NX][15];
-#pragma unroll
-      for (int x = 0; x < NX; ++x)
-#pragma unroll
-        for (int L = 0; L < 15; ++L) lev[x][L] = 0;
-#pragma unroll
-      for (int p = 0; p < 8; ++p) {
-        float v[16];
-        t5_ld16(tbase + ((uint32_t)(32 * warp) << 16) + (uint32_t)(b * 128 + p * 16), v);
-#pragma unroll
-        for (int x = 0; x < NX; ++x)
-#pragma unroll
-          for (int q = 0; q < 8; ++q) {
-            if constexpr (LEVELS32) lev[x][p + q] += v[x * 8 + q];
-            else lev[x][p + q] += (long long)__float2int_rn(v[x * 8 + q]);
-          }
-      }
-      t5_fence_before();
-      __syncwarp();
-      if (lane == 0) gt_arrive(&S.bar[GB_TFREE + b]);
       double prod[2] = {0.0, 0.0};
 #pragma unroll
       for (int x = 0; x < NX; ++x) {
+        LT lev[15];
+#pragma unroll
+        for (int L = 0; L < 15; ++L) lev[L] = 0;
+#pragma unroll
+        for (int p = 0; p < 8; ++p) {
+          float v[16];
+          t5_ld16(tbase + ((uint32_t)(32 * warp) << 16) + (uint32_t)(b * 128 + p * 16), v);
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            if constexpr (LEVELS32) lev[p + q] += v[x * 8 + q];
+            else lev[p + q] += (long long)__float2int_rn(v[x * 8 + q]);
+          }
+        }
         long long A3 = 0, B3 = 0, C3 = 0;  // levels 0-4, 5-9, 10-14, each sum below 2^53 in magnitude
 #pragma unroll
         for (int L = 0; L < 15; ++L) {
           long long t;
-          if constexpr (LEVELS32) t = (long long)__float2int_rn(lev[x][L]);
-          else t = lev[x][L];
+          if constexpr (LEVELS32) t = (long long)__float2int_rn(lev[L]);
+          else t = lev[L];
           if (L < 5) A3 += t * (1ll << (7 * (4 - L)));
           else if (L < 10) B3 += t * (1ll << (7 * (9 - L)));
           else C3 += t * (1ll << (7 * (14 - L)));
@@ -641,6 +634,9 @@ __global__ void __maxnreg__(152) k_gs_update_tc(StepArgs a, int mode, GTArgs g) 
                               fma(__ll2double_rn(B3), 34359738368.0, __ll2double_rn(C3)));
         prod[x] = (etile > -128) ? xs * gt_pow2(etile + (x ? eg : es) - 112) : 0.0;
       }
+      t5_fence_before();
+      __syncwarp();
+      if (lane == 0) gt_arrive(&S.bar[GB_TFREE + b]);
       int Eu = 0;
       if (r < n) {
         const double un = (sigma * u - prod[0]) * invnu;
