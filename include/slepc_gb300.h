@@ -162,9 +162,12 @@ PetscErrorCode EPSGB300OrthogonalityError(EPS eps, PetscReal *err);
  * No counterpart in the reference.  It is for callers that cannot allocate device memory while they run: programs
  * that reserve the GPU's memory up front for their own pool allocator, and time-critical loops that cannot take the
  * implicit device synchronisation of cudaMalloc/cudaFree.  Its scratch (partial sums, counter, staging; 344,448
- * bytes) is a fixed static device array that every GPU loading this library holds until the process exits; the
- * first call on a device looks up that array's address, so make that first call before any stream capture.
- * Limits: k <= 256 (larger k returns PETSC_ERR_ARG_OUTOFRANGE).  The call is asynchronous on `stream` (a
+ * bytes) is a fixed static device array that every GPU loading this library holds until the process exits.  The
+ * first call on a device is a warm-up: it looks up that array's address and, with CUDA's lazy module loading, may
+ * make the driver load this library's kernels and allocate driver memory for them; make it before reserving your
+ * memory pool, before entering the time-critical loop, and before any stream capture.  Later calls allocate
+ * nothing.  Limits: k <= 256 (larger k returns PETSC_ERR_ARG_OUTOFRANGE); any n (the kernel's grid is capped at
+ * 160 blocks, which loop over the rows).  The call is asynchronous on `stream` (a
  * cudaStream_t, NULL for the legacy default stream).  All calls share the one scratch array: calls that overlap on
  * the GPU (different streams, or different host threads without ordering) race and must be serialised by the
  * caller. */

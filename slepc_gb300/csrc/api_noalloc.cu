@@ -16,7 +16,7 @@ using namespace ksg;
 
 namespace {
 constexpr int NA_MAX_COLS = 256;     // largest k accepted
-constexpr int NA_MAX_BLOCKS = 160;   // largest grid of the dot kernel (one block per SM, GB300 has 152)
+constexpr int NA_MAX_BLOCKS = 160;   // the dot kernel's grid is capped here (one block per SM on GB300's 152 SMs)
 constexpr int NA_PART_STRIDE = NA_MAX_COLS + 8;  // partial sums per block (k values + u.u), 8-byte units
 constexpr size_t NA_STATE_BYTES = 256;
 constexpr size_t NA_COEF_BYTES = (size_t)(2 * NA_MAX_COLS + 8) * 8;
@@ -59,9 +59,6 @@ extern "C" PetscErrorCode BVGB300DotVecNoAlloc(const double *V, PetscInt ldv, Pe
             "k = %d columns exceeds the fixed scratch of this entry point (at most %d)", k, NA_MAX_COLS);
   KSG_CHECK(ldv >= n && (ldv % 2) == 0, PETSC_ERR_ARG_WRONG, "ldv must be even and at least n");
   KSG_CHECK(((uintptr_t)V % 16) == 0, PETSC_ERR_ARG_WRONG, "V must be 16-byte aligned");
-  const int blocks = gs_dot_blocks(n);
-  KSG_CHECK(blocks <= NA_MAX_BLOCKS, PETSC_ERR_SUP, "the dot kernel would use %d blocks, above the scratch's %d",
-            blocks, NA_MAX_BLOCKS);
   if (k == 0) return 0;
   unsigned char *base = nullptr;
   KSG_TRY(na_scratch(&base));
@@ -86,7 +83,9 @@ extern "C" PetscErrorCode BVGB300DotVecNoAlloc(const double *V, PetscInt ldv, Pe
   a.part = part;
   a.pstride = NA_PART_STRIDE;
   a.st = st;
-  KSG_CUDA(launch_gs_dot(a, 1, GS_DOTS, ARITH_PAIR, s));
+  // a device with more SMs than the scratch has block slots runs the kernel on NA_MAX_BLOCKS blocks, which loop
+  // over the row tiles: any n works on any device
+  KSG_CUDA(launch_gs_dot(a, 1, GS_DOTS, ARITH_PAIR, s, STORE_F64, NA_MAX_BLOCKS));
   KSG_CUDA(cudaMemcpyAsync(y, coef, sizeof(double) * k, cudaMemcpyDeviceToDevice, s));
   return 0;
 }

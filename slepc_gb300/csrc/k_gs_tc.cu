@@ -221,7 +221,7 @@ KS_DEVICE void gt_init_barriers(const GTShared &S) {
 // Half A
 // ---------------------------------------------------------------------------------------------------------------
 template <int NX>
-__global__ void __maxnreg__(136) k_gs_dot_tc(StepArgs a, int mode, GTArgs g) {
+__global__ void __maxnreg__(128) k_gs_dot_tc(StepArgs a, int mode, GTArgs g) {
   KrylovState *st = a.st;
   if (st->stop) return;
   extern __shared__ __align__(1024) unsigned char sm[];
@@ -512,7 +512,7 @@ __global__ void __maxnreg__(136) k_gs_dot_tc(StepArgs a, int mode, GTArgs g) {
 // Half B
 // ---------------------------------------------------------------------------------------------------------------
 template <int NX, bool LEVELS32>
-__global__ void __maxnreg__(136) k_gs_update_tc(StepArgs a, int mode, GTArgs g) {
+__global__ void __maxnreg__(128) k_gs_update_tc(StepArgs a, int mode, GTArgs g) {
   KrylovState *st = a.st;
   if (st->stop) return;
   extern __shared__ __align__(1024) unsigned char sm[];

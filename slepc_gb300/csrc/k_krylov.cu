@@ -362,9 +362,11 @@ static bool gs_use_tc(const StepArgs &a, int arith, int storage) {
   return a.tc && storage == STORE_F64 && arith == ARITH_F64 && a.J >= 1 && a.J <= gs_tc_max_columns();
 }
 
-cudaError_t launch_gs_dot(const StepArgs &a, int nx, int mode, int arith, cudaStream_t s, int storage) {
+cudaError_t launch_gs_dot(const StepArgs &a, int nx, int mode, int arith, cudaStream_t s, int storage,
+                          int max_blocks) {
   if (gs_use_tc(a, arith, storage)) return launch_gs_dot_tc(a, nx, mode, *a.tc, s);
-  const int blocks = gs_dot_blocks(a.n);
+  int blocks = gs_dot_blocks(a.n);
+  if (max_blocks > 0 && blocks > max_blocks) blocks = max_blocks;
   if (storage == STORE_F32)
     return nx == 2 ? dot_dispatch<2, PairAr, StF32>(a, mode, blocks, s) : dot_dispatch<1, PairAr, StF32>(a, mode, blocks, s);
   if (storage == STORE_PAIR)

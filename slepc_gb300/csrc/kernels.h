@@ -109,7 +109,10 @@ cudaError_t launch_f64_to_pair(const double *x, float2 *y, long long n, cudaStre
 cudaError_t launch_pair_to_f64(const float2 *x, double *y, long long n, cudaStream_t s);
 cudaError_t launch_f64_to_f32(const double *x, float *y, long long n, cudaStream_t s);
 cudaError_t launch_f32_to_f64(const float *x, double *y, long long n, cudaStream_t s);
-cudaError_t launch_gs_dot(const StepArgs &a, int nx, int mode, int arith, cudaStream_t s, int storage = STORE_F64);
+// max_blocks > 0 caps the grid (the blocks loop over the row tiles, so any grid size gives the same sums' partition
+// per block count)
+cudaError_t launch_gs_dot(const StepArgs &a, int nx, int mode, int arith, cudaStream_t s, int storage = STORE_F64,
+                          int max_blocks = 0);
 cudaError_t launch_gs_update(const StepArgs &a, int nx, int mode, int arith, cudaStream_t s, int storage = STORE_F64);
 cudaError_t launch_restart(void *V, long long ldv, int n, int a0, int K, int s0, int N, const double *Q, int ldq,
                            int arith, cudaStream_t s, int storage = STORE_F64);

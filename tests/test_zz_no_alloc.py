@@ -1,6 +1,7 @@
 """BVGB300DotVecNoAlloc -- the dot kernel with its scratch in a static device array, for callers that cannot
 allocate device memory while they run -- checked through the C-ABI against BVDotVec, twice in a row (the second
-call must not see the first call's scratch contents).  This file is named to run last."""
+call must not see the first call's scratch contents); after those warm-up calls, more calls leave the device's free
+memory unchanged; bad sizes and alignment are refused with an error.  This file is named to run last."""
 import ctypes
 
 import numpy as np
@@ -17,7 +18,14 @@ def _cudart():
     rt.cudaMemcpy.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int]
     rt.cudaFree.argtypes = [ctypes.c_void_p]
     rt.cudaDeviceSynchronize.argtypes = []
+    rt.cudaMemGetInfo.argtypes = [ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)]
     return rt
+
+
+def _free_bytes(rt):
+    free, total = ctypes.c_size_t(), ctypes.c_size_t()
+    assert rt.cudaMemGetInfo(ctypes.byref(free), ctypes.byref(total)) == 0
+    return free.value
 
 
 def _bvdotvec(lib, V, x):
@@ -70,8 +78,18 @@ def test_no_alloc_dot_matches_bvdotvec(lib):
             scale = np.abs(V).T @ np.abs(x)
             assert np.all(np.abs(y - ref) <= 1e-13 * scale), (call, np.max(np.abs(y - ref) / scale))
             assert np.all(np.abs(y - V.T @ x) <= 1e-12 * scale)
-        # sizes beyond the fixed scratch are refused with an error, not a fault
+        # after the warm-up calls above, further calls allocate no device memory
+        before = _free_bytes(rt)
+        for _ in range(4):
+            assert f(dV, n, n, k, dx, dy, None) == 0
+            assert rt.cudaDeviceSynchronize() == 0
+        assert _free_bytes(rt) == before
+        # sizes beyond the fixed scratch, an odd leading dimension and a V that is not 16-byte aligned are refused
+        # with an error before any launch
         assert f(dV, n, n, 257, dx, dy, None) != 0
+        assert f(dV, n + 1, n, k, dx, dy, None) != 0
+        assert f(ctypes.c_void_p(dV.value + 8), n, n, k, dx, dy, None) != 0
+        assert rt.cudaDeviceSynchronize() == 0
     finally:
         rt.cudaFree(dV)
         rt.cudaFree(dx)
