@@ -570,6 +570,8 @@ def main():
                          "it); f32: the precision form")
     ap.add_argument("--restart", default="tensor", choices=["tensor", "pair", "mma_sync", "tcgen05"],
                     help="kernel of the thick restart (EPSGB300SetRestartMethod)")
+    ap.add_argument("--gs", default="tensor", choices=["tensor", "fma"],
+                    help="Gram-Schmidt of the f64 arithmetic: exact slice products on the tensor cores, or FP64 FMA")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-parity", action="store_true", help="skip the host-side parity block")
@@ -672,6 +674,8 @@ def run_plain(args, wl):
         eps.setWhichEigenpairs(wl["which"])
         eps.setArithmetic(arith)
         eps.setRestartMethod(args.restart)
+        if arith == "f64":
+            eps.setGSMethod(args.gs)
         eps.setInitialSpace(v0)
         return eps
 
@@ -691,7 +695,7 @@ def run_plain(args, wl):
         eps.setProfiling(True)
         eps.solve()
         prof = eps.getProfile()
-        print(json.dumps({"profile_solve": args.workload, "arith": args.arith, "restart": args.restart,
+        print(json.dumps({"profile_solve": args.workload, "arith": args.arith, "gs": args.gs, "restart": args.restart,
                           "stats": eps.getStats(), "per_class_ms": {k: round(v[0], 3) for k, v in prof.items()}}),
               flush=True)
         return

@@ -1,16 +1,17 @@
-// k_gs_tc.cu -- the DCGS2 Gram-Schmidt pair for IEEE-double storage on the bf16 tensor cores (tcgen05 + TMEM), by
+// k_gs_tc.cu -- the DCGS2 Gram-Schmidt pair for IEEE-double storage on the 16-bit tensor cores (tcgen05 + TMEM), by
 // the error-free slice split of Ozaki, Ogita, Oishi and Rump ("Error-free transformations of matrix multiplication
 // by using fast routines of matrix multiplication and its applications", Numer. Algorithms 59, 2012).
 //
 // GB300's FP64 pipe issues about 0.6 T FMA/s, so the FP64-FMA Gram-Schmidt kernels (two FMAs per 8-byte basis
-// entry) stop near 2.4 TB/s, a third of the HBM rate.  Here every product runs exactly on the bf16 tensor cores:
+// entry) stop near 2.4 TB/s, a third of the HBM rate.  Here every product runs exactly on the tensor cores:
 //
-//   a value v with |v| < 2^e is the 56-bit fixed point  v 2^(56-e) = sum_{p<8} a_p 2^(7(7-p)),  a_p in [-127, 127]
-//   (the 53-bit significand truncated only below 2^-56 of the scale), each a_p exact in bf16;
-//   sum_r v_r u_r = 2^(e_v + e_u - 112) sum_{p,q} D_pq 2^(7(14-p-q)),  D_pq = sum_r a_p(v_r) b_q(u_r),
-//
-// every D_pq an exact FP32 sum of exact integer products (|D_pq| <= 1024 * 127^2 < 2^24).  The 64 slice products
-// recombine exactly as a 128-bit integer, rounded once to a double.
+//   a basis value v with |v| < 2^e is the 55-bit two's complement fixed point X = trunc(v 2^(55-e)) (the 53-bit
+//   significand truncated only below 2^-55 of the scale), cut into seven bytes B_0 (signed) .. B_6 (unsigned) with
+//   X = sum_k B_k 2^(8(6-k)); a vector value u (half A) is cut into eight signed 7-bit slices of its 56-bit fixed
+//   point, a coefficient value (half B) into seven bytes like v.  Every slice is an integer below 256 in magnitude,
+//   exact in FP16 (the bytes come out of the fixed point's words by byte permutes: FP16(1024 + b) has the bits
+//   0x6400 | b, and one exact FP16 subtraction leaves b), every product of two slices is exact, and the tensor
+//   cores' FP32 sums of them stay exact below 2^24.
 //
 // Scales.  Basis columns (unit vectors) carry one exponent per column and 128-row tile, recorded by the kernels that
 // write them (this file's update half, the tcgen05 restart) in an int8 table [column][tile]; a value's scale is the
@@ -18,21 +19,28 @@
 // small.  u, w (half A) get a scale per row chunk, the coefficient vectors s, g (half B) one per vector, computed on
 // the fly.  A value at or above its recorded scale sets the error flag (the host reports PETSC_ERR_PLIB).
 //
-// Half A (dot): s = V^T u, b = V^T w over chunks of ct 128-row tiles.  MMA M = 128 = 16 basis columns x 8 slices
-// (row jl * 8 + p), N = 16 = 2 vectors x 8 slices, K = the rows of a tile.  Exact chunk sums, recombined per column
-// as 128-bit integers (a butterfly over the 8 lanes of a column), are accumulated across chunks in double-double;
-// the block partials are merged in block order by the last block, which runs the DCGS2 coefficient algebra
-// (gs_epilogue).  Rounding: one rounding per chunk and column and a double-double sum, far below the FP64 dot's.
+// Half A (dot): s = V^T u, b = V^T w over chunks of ct <= 4 tiles of 128 rows (|D| <= 512 * 255 * 127 < 2^24).
+// MMA M = 128 = 16 basis columns x 8 slice slots (row jl * 8 + k; slot 7 stays zero), N = 16 = 2 vectors x 8
+// slices, K = the rows.  The exact chunk sums of one column, recombined by a butterfly over its 8 lanes as a
+// 128-bit integer, are rounded once and accumulated across chunks in double-double; the last block merges the block
+// partials in block order and runs the DCGS2 coefficient algebra (gs_epilogue).
 //
 // Half B (update): [v w'] = [(sigma u - V s) / nu, w - V g - tau sigma u].  Per tile of 128 rows: MMA M = 128 rows,
-// N = 16 (s, g x 8 slices), K = the basis columns, one TMEM accumulator per V slice p; the thread of row r sums the
-// 15 levels p + q exactly and rounds the product once; the FP64 update, the norm of w' and the recorded exponents of
-// v follow.  Results are deterministic: fixed partitions, fixed orders, no floating-point atomics.
+// N = 16 (s, g x 8 byte slots), K = the basis columns, one TMEM accumulator per V byte; the thread of row r sums the
+// 13 levels k + q exactly in 32-bit integers and rounds the product once; the FP64 update, the norm of w' and the
+// recorded exponents of v follow.  Results are deterministic: fixed partitions, fixed orders, no floating-point
+// atomics.
 //
-// Warp roles (13 warps): 0-3 epilogue and vector staging (TMEM lanes 0-127), 4 the MMA issuer (one thread), 5-12
-// slicers (global loads of V, slicing into a ring of four 32 KB shared-memory stages).  Stages, B buffers and TMEM
-// buffers hand over on mbarriers; tcgen05.commit releases what the tensor cores have read.  Every wait is bounded:
-// on a timeout the kernel records it, stops issuing, waits (bounded) for the MMAs in flight, frees TMEM and returns.
+// Shared-memory layouts are the canonical K-major core matrices (8 rows x 16 bytes, no swizzle).  In half A the
+// core matrices adjacent along K sit 2064 bytes apart instead of 2048, so the slicers' 16-byte stores of one warp
+// spread over all bank groups (the unpadded stride put every store of a warp in the same four banks).
+//
+// Warp roles (13 warps, at most 128 registers each: 4 warps share a sub-partition's 16K registers): 0-3 epilogue
+// and vector staging (TMEM lanes 0-127), 4 the MMA issuer (one thread), 5-12 slicers (global loads of V, one stage
+// ahead, slicing into a ring of four shared-memory stages).  Stages, B buffers and TMEM buffers hand over on
+// mbarriers; tcgen05.commit releases what the tensor cores have read.  Every wait is bounded: on a timeout the
+// kernel records it, stops issuing, waits (bounded) for the MMAs in flight, frees TMEM and returns.
+#include <cuda_fp16.h>
 #include <float.h>
 
 #include <type_traits>
@@ -47,15 +55,21 @@ namespace ksg {
 
 constexpr int GT_R = 128;                                 // rows per tile
 constexpr int GT_NA = 4;                                  // A stages
-constexpr int GT_STAGE = 32768;                           // 128 x 16 values x 8 slices x bf16
-constexpr int GT_BT = 4096;                               // dot: B slices of one tile (16 k8 x 2 n8 x 128 B)
-constexpr int GT_CTMAX = 8;                               // tiles per chunk (dot)
+constexpr int GT_DLBO = 2064;                             // half A: bytes between core matrices adjacent in K
+constexpr int GT_DSTAGE = 16 * GT_DLBO;                   // half A stage: 128 rows of 16 columns (8 slots)
+constexpr int GT_USTAGE = 7 * 4096;                       // half B stage: 7 byte matrices of 128 rows x 16 columns
+constexpr int GT_STAGE = GT_DSTAGE > GT_USTAGE ? GT_DSTAGE : GT_USTAGE;
+constexpr int GT_BLBO = 272;                              // half A B-operand: bytes between core matrices along K
+constexpr int GT_BT = 16 * GT_BLBO;                       // half A: u/w slices of one tile
+constexpr int GT_CTMAX = 4;                               // tiles per chunk (half A): 512 rows keep sums exact
 constexpr int GT_EW = 4, GT_SW = 8;                       // epilogue warps, slicer warps
 constexpr int GT_MWARP = GT_EW;                           // the MMA warp
 constexpr int GT_SW0 = GT_EW + 1;                         // first slicer warp
 constexpr int GT_THREADS = 32 * (GT_EW + 1 + GT_SW);      // 416
 constexpr int GT_MAXJ = 144;
 constexpr uint32_t GT_TMEM = 512;
+// FP16 instruction descriptor: D = FP32, A = B = FP16, both K-major, N = 16, M = 128
+constexpr uint32_t GT_IDESC = (1u << 4) | ((uint32_t)(16 >> 3) << 17) | ((uint32_t)(GT_R >> 4) << 24);
 // barriers: afull[4] aempty[4] bfull[2] cdone[2] tfree[2] fin
 constexpr int GB_AFULL = 0, GB_AEMPTY = 4, GB_BFULL = 8, GB_CDONE = 10, GB_TFREE = 12, GB_FIN = 14, GB_N = 15;
 
@@ -131,9 +145,63 @@ KS_DEVICE bool gt_ebar(int *cnt, int gen, volatile int *abort) {
   return ok;
 }
 
-// Eight doubles that are consecutive along the MMA's K dimension -> eight slices of 8 bf16 (one 16-byte core-matrix
-// row each) of their 56-bit fixed point relative to 2^e; *ovf is set when some |v| >= 2^e.
-KS_DEVICE void gt_slice8(const double *v, int e, uint4 *out, int *ovf) {
+// 55-bit two's complement fixed point of v relative to 2^e: trunc(v 2^(55-e)); *ovf is set when |v| >= 2^e
+KS_DEVICE long long gt_fix55(double v, int e, int *ovf) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+  const int E = (int)((u >> 52) & 0x7FF);
+  if (E == 0) return 0;  // zero (or subnormal: below 2^-1022, far below any recorded scale's 2^-55)
+  const int sh = (E - 1075) + 55 - e;
+  const unsigned long long m = (u & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+  if (sh > 2) *ovf = 1;
+  const unsigned long long x = sh >= 0 ? (sh <= 2 ? (m << sh) : 0ull) : (sh > -60 ? (m >> (-sh)) : 0ull);
+  return (u >> 63) ? -(long long)x : (long long)x;
+}
+
+// Seven byte slices of eight fixed points X_0..X_7 (consecutive along K): out[k] = the 16-byte core-matrix row of byte
+// B_k (k = 0 the signed top byte) of the eight values, as FP16 integers.  Byte permutes put each byte of two values
+// beside the exponent byte 0x64 (FP16(1024 + b) = 0x6400 | b); one exact FP16 subtraction per pair leaves b
+// (1152 for the top byte, whose sign bit was flipped to make it 128 + B_0).
+KS_DEVICE void gt_bytes7(const long long *X, uint4 *out) {
+  const uint32_t C = 0x64646464u;
+  const __half2 k1024 = __floats2half2_rn(1024.0f, 1024.0f), k1152 = __floats2half2_rn(1152.0f, 1152.0f);
+  uint32_t w[7][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const uint32_t l0 = (uint32_t)X[2 * i], l1 = (uint32_t)X[2 * i + 1];
+    const uint32_t h0 = (uint32_t)((unsigned long long)X[2 * i] >> 32) ^ 0x00800000u;
+    const uint32_t h1 = (uint32_t)((unsigned long long)X[2 * i + 1] >> 32) ^ 0x00800000u;
+    const uint32_t tl01 = __byte_perm(l0, l1, 0x5140), tl23 = __byte_perm(l0, l1, 0x7362);
+    const uint32_t th01 = __byte_perm(h0, h1, 0x5140), th2 = __byte_perm(h0, h1, 0x7362);
+    uint32_t r[7];
+    r[6] = __byte_perm(tl01, C, 0x5140);  // byte 0 of the low word: B_6
+    r[5] = __byte_perm(tl01, C, 0x5342);  // byte 1: B_5
+    r[4] = __byte_perm(tl23, C, 0x5140);  // byte 2: B_4
+    r[3] = __byte_perm(tl23, C, 0x5342);  // byte 3: B_3
+    r[2] = __byte_perm(th01, C, 0x5140);  // high word byte 0: B_2
+    r[1] = __byte_perm(th01, C, 0x5342);  // byte 1: B_1
+    r[0] = __byte_perm(th2, C, 0x5140);   // byte 2: 128 + B_0
+#pragma unroll
+    for (int k = 0; k < 7; ++k) {
+      __half2 hv = *reinterpret_cast<const __half2 *>(&r[k]);
+      hv = __hsub2(hv, k == 0 ? k1152 : k1024);
+      w[k][i] = *reinterpret_cast<const uint32_t *>(&hv);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 7; ++k) out[k] = make_uint4(w[k][0], w[k][1], w[k][2], w[k][3]);
+}
+
+// Two signed 7-bit slices as an FP16x2 word: 0x6400 | u is FP16(1024 + u), one exact subtraction leaves u, then the
+// sign bits (a negative value's zero slice is -0)
+KS_DEVICE uint32_t gt_h_pair(uint32_t u0, uint32_t u1, uint32_t neg0, uint32_t neg1) {
+  const uint32_t biased = 0x64006400u | u0 | (u1 << 16);
+  const __half2 d = __hsub2(*reinterpret_cast<const __half2 *>(&biased), __floats2half2_rn(1024.0f, 1024.0f));
+  return *reinterpret_cast<const uint32_t *>(&d) | (neg0 << 15) | (neg1 << 31);
+}
+
+// Eight doubles (consecutive along K) -> eight 7-bit slices (sign and magnitude) of their 56-bit fixed point
+// relative to 2^e, as FP16 core-matrix rows; *ovf is set when some |v| >= 2^e.  Used for the vectors u, w of half A.
+KS_DEVICE void gt_slice8h(const double *v, int e, uint4 *out, int *ovf) {
   uint32_t mh[8], ml[8], ng[8];
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
@@ -155,10 +223,10 @@ KS_DEVICE void gt_slice8(const double *v, int e, uint4 *out, int *ovf) {
     uint32_t f[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) f[j] = t5_field(mh[j], ml[j], sl);
-    out[sl].x = t5_slice_pair(f[0], f[1], ng[0], ng[1]);
-    out[sl].y = t5_slice_pair(f[2], f[3], ng[2], ng[3]);
-    out[sl].z = t5_slice_pair(f[4], f[5], ng[4], ng[5]);
-    out[sl].w = t5_slice_pair(f[6], f[7], ng[6], ng[7]);
+    out[sl].x = gt_h_pair(f[0], f[1], ng[0], ng[1]);
+    out[sl].y = gt_h_pair(f[2], f[3], ng[2], ng[3]);
+    out[sl].z = gt_h_pair(f[4], f[5], ng[4], ng[5]);
+    out[sl].w = gt_h_pair(f[6], f[7], ng[6], ng[7]);
   }
 }
 
@@ -217,6 +285,20 @@ KS_DEVICE void gt_init_barriers(const GTShared &S) {
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
+KS_DEVICE void gt_load8(const double *col, long long r0, int n, bool valid, double *v) {
+  if (valid && r0 + 8 <= n) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const double2 d2 = __ldcs(reinterpret_cast<const double2 *>(col) + k);
+      v[2 * k] = d2.x;
+      v[2 * k + 1] = d2.y;
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v[k] = (valid && r0 + k < n) ? col[k] : 0.0;
+  }
+}
+
 // ---------------------------------------------------------------------------------------------------------------
 // Half A
 // ---------------------------------------------------------------------------------------------------------------
@@ -243,6 +325,10 @@ __global__ void __maxnreg__(128) k_gs_dot_tc(StepArgs a, int mode, GTArgs g) {
     gt_init_barriers(S);
   }
   for (int i = tid; i < GT_MAXJ * 4; i += GT_THREADS) S.pdd[i] = 0.0;
+  // slot 7 of every column in the A stages is never written: the whole ring starts at zero
+  for (int i = tid; i < GT_NA * GT_STAGE / 16; i += GT_THREADS)
+    reinterpret_cast<uint4 *>(sm + GT_AOFF)[i] = make_uint4(0u, 0u, 0u, 0u);
+  gt_fence_async_smem();
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(t5_smem(S.tslot)),
                  "r"(GT_TMEM)
@@ -311,11 +397,11 @@ __global__ void __maxnreg__(128) k_gs_dot_tc(StepArgs a, int mode, GTArgs g) {
         uint4 sl[8];
         int ovf = 0;
         const int t = e >> 4, k8 = e & 15;
-        unsigned char *base = Bs + (size_t)b * GT_CTMAX * GT_BT + (size_t)((t * 16 + k8) * 2) * 128;
-        gt_slice8(uv, eu, sl, &ovf);
+        unsigned char *base = Bs + (size_t)b * GT_CTMAX * GT_BT + (size_t)(t * 16 + k8) * GT_BLBO;
+        gt_slice8h(uv, eu, sl, &ovf);
 #pragma unroll
         for (int q = 0; q < 8; ++q) *reinterpret_cast<uint4 *>(base + q * 16) = sl[q];
-        if (NX == 2) gt_slice8(wv, ew, sl, &ovf);
+        if (NX == 2) gt_slice8h(wv, ew, sl, &ovf);
 #pragma unroll
         for (int q = 0; q < 8; ++q)
           *reinterpret_cast<uint4 *>(base + 128 + q * 16) = NX == 2 ? sl[q] : make_uint4(0u, 0u, 0u, 0u);
@@ -342,13 +428,15 @@ __global__ void __maxnreg__(128) k_gs_dot_tc(StepArgs a, int mode, GTArgs g) {
         const int ej = (j < J) ? gt_vscale(g, j, c * ct, min(ct, ntiles - c * ct)) : -128;
 #pragma unroll
         for (int x = 0; x < NX; ++x) {
-          long long H = 0, R = 0;
-          H = (long long)__float2int_rn(v[x * 8 + 0]) * 128 + (long long)__float2int_rn(v[x * 8 + 1]);
+          // Y_k = sum_q D_kq 2^(7(7-q)) = H 2^42 + R, then weight 2^(8(6-k)) of byte k (slot 7 holds zeros)
+          const long long H =
+              (long long)__float2int_rn(v[x * 8 + 0]) * 128 + (long long)__float2int_rn(v[x * 8 + 1]);
+          long long R = 0;
 #pragma unroll
-          for (int q = 2; q < 8; ++q) R += (long long)__float2int_rn(v[x * 8 + q]) << (7 * (7 - q));
+          for (int q = 2; q < 8; ++q) R += (long long)__float2int_rn(v[x * 8 + q]) * (1ll << (7 * (7 - q)));
           long long hi;
           unsigned long long lo;
-          gt_make128(H, R, 7 * (7 - p), hi, lo);
+          gt_make128(H, R, p < 7 ? 8 * (6 - p) : 0, hi, lo);
 #pragma unroll
           for (int off = 4; off > 0; off >>= 1) {
             const long long ohi = __shfl_xor_sync(0xffffffffu, hi, off);
@@ -356,7 +444,7 @@ __global__ void __maxnreg__(128) k_gs_dot_tc(StepArgs a, int mode, GTArgs g) {
             gt_add128(hi, lo, ohi, olo);
           }
           if (p == 0 && j < J && ej > -128) {
-            const double val = gt_to_double(hi, lo) * gt_pow2(ej + (x ? ew : eu) - 112);
+            const double val = gt_to_double(hi, lo) * gt_pow2(ej + (x ? ew : eu) - 111);
             gt_dd_add(S.pdd[(j * 2 + x) * 2], S.pdd[(j * 2 + x) * 2 + 1], val);
           }
         }
@@ -369,8 +457,6 @@ __global__ void __maxnreg__(128) k_gs_dot_tc(StepArgs a, int mode, GTArgs g) {
   } else if (warp == GT_MWARP) {
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
-      const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(16 >> 3) << 17) |
-                             ((uint32_t)(GT_R >> 4) << 24);
       int q = 0;
       bool ok = true;
       for (int i = 0; i < my && ok; ++i) {
@@ -388,9 +474,9 @@ __global__ void __maxnreg__(128) k_gs_dot_tc(StepArgs a, int mode, GTArgs g) {
             const uint32_t dcol = tbase + (uint32_t)(b * NMB * 16 + mb * 16);
 #pragma unroll
             for (int ks = 0; ks < 8; ++ks) {
-              const uint64_t ad = t5_desc(abase + ks * 2 * 2048, 2048, 128);
-              const uint64_t bd = t5_desc(bbase + (uint32_t)((t * 16 + 2 * ks) * 256), 256, 128);
-              t5_mma(dcol, ad, bd, idesc, (t > 0 || ks > 0) ? 1u : 0u);
+              const uint64_t ad = t5_desc(abase + ks * 2 * GT_DLBO, GT_DLBO, 128);
+              const uint64_t bd = t5_desc(bbase + (uint32_t)((t * 16 + 2 * ks) * GT_BLBO), GT_BLBO, 128);
+              t5_mma(dcol, ad, bd, GT_IDESC, (t > 0 || ks > 0) ? 1u : 0u);
             }
             t5_commit(&S.bar[GB_AEMPTY + sa]);
           }
@@ -401,51 +487,56 @@ __global__ void __maxnreg__(128) k_gs_dot_tc(StepArgs a, int mode, GTArgs g) {
       if (!t5_wait(&S.bar[GB_FIN], 0)) *abort = 1;
     }
   } else {
-    // ---------------- slicers ----------------
+    // ---------------- slicers: item = (column jl, 8-row group k8) of a 16-column stage, loads one stage ahead ----
     const int s = tid - 32 * GT_SW0;  // 0..255
     const int jl = s >> 4, k8 = s & 15;
-    int q = 0, ovf = 0;
-    bool ok = true;
-    for (int i = 0; i < my && ok; ++i) {
-      const int c = blockIdx.x + i * gridDim.x;
-      const int tch = min(ct, ntiles - c * ct);
-      for (int t = 0; t < ct && ok; ++t)
-        for (int mb = 0; mb < NMB; ++mb, ++q) {
-          const int sa = q % GT_NA;
-          const int j = mb * 16 + jl;
-          const long long r0 = ((long long)c * ct + t) * GT_R + 8 * k8;
-          double v[8];
-          if (j < J && t < tch) {
-            const double *col = V + (size_t)j * a.ldv + r0;
-            if (r0 + 8 <= n) {
+    const int total = my * ct * NMB;
+    int ovf = 0;
+    auto where = [&](int q, int &c, int &t, int &j, long long &r0, bool &valid) {
+      const int mb = q % NMB, tq = q / NMB;
+      t = tq % ct;
+      c = blockIdx.x + (tq / ct) * gridDim.x;
+      j = mb * 16 + jl;
+      r0 = ((long long)c * ct + t) * GT_R + 8 * k8;
+      valid = j < J && c * ct + t < ntiles;
+    };
+    double vn[8];
+    if (total > 0) {
+      int c, t, j;
+      long long r0;
+      bool valid;
+      where(0, c, t, j, r0, valid);
+      gt_load8(V + (size_t)j * a.ldv + r0, r0, n, valid, vn);
+    }
+    for (int q = 0; q < total; ++q) {
+      const int sa = q % GT_NA;
+      int c, t, j;
+      long long r0;
+      bool valid;
+      where(q, c, t, j, r0, valid);
+      double v[8];
 #pragma unroll
-              for (int k = 0; k < 4; ++k) {
-                const double2 d2 = __ldcs(reinterpret_cast<const double2 *>(col) + k);
-                v[2 * k] = d2.x;
-                v[2 * k + 1] = d2.y;
-              }
-            } else {
+      for (int k = 0; k < 8; ++k) v[k] = vn[k];
+      if (q + 1 < total) {
+        int c2, t2, j2;
+        long long r2;
+        bool v2;
+        where(q + 1, c2, t2, j2, r2, v2);
+        gt_load8(V + (size_t)j2 * a.ldv + r2, r2, n, v2, vn);
+      }
+      const int ej = valid ? gt_vscale(g, j, c * ct, min(ct, ntiles - c * ct)) : 0;
+      long long X[8];
 #pragma unroll
-              for (int k = 0; k < 8; ++k) v[k] = (r0 + k < n) ? col[k] : 0.0;
-            }
-          } else {
+      for (int k = 0; k < 8; ++k) X[k] = gt_fix55(v[k], ej, &ovf);
+      uint4 sl[7];
+      gt_bytes7(X, sl);
+      if (q >= GT_NA && !gt_wait(&S.bar[GB_AEMPTY + sa], (uint32_t)(((q / GT_NA) - 1) & 1), abort)) break;
+      unsigned char *dst = As + (size_t)sa * GT_STAGE + (size_t)k8 * GT_DLBO + (size_t)jl * 128;
 #pragma unroll
-            for (int k = 0; k < 8; ++k) v[k] = 0.0;
-          }
-          const int ej = (j < J && t < tch) ? gt_vscale(g, j, c * ct, tch) : 0;
-          uint4 sl[8];
-          gt_slice8(v, ej, sl, &ovf);
-          if (q >= GT_NA && !gt_wait(&S.bar[GB_AEMPTY + sa], (uint32_t)(((q / GT_NA) - 1) & 1), abort)) {
-            ok = false;
-            break;
-          }
-          unsigned char *dst = As + (size_t)sa * GT_STAGE + (size_t)(k8 * 16 + jl) * 128;
-#pragma unroll
-          for (int p = 0; p < 8; ++p) *reinterpret_cast<uint4 *>(dst + p * 16) = sl[p];
-          gt_fence_async_smem();
-          __syncwarp();
-          if (lane == 0) gt_arrive(&S.bar[GB_AFULL + sa]);
-        }
+      for (int k = 0; k < 7; ++k) *reinterpret_cast<uint4 *>(dst + k * 16) = sl[k];
+      gt_fence_async_smem();
+      __syncwarp();
+      if (lane == 0) gt_arrive(&S.bar[GB_AFULL + sa]);
     }
     if (ovf) atomicExch(g.err, 2);
   }
@@ -511,7 +602,7 @@ __global__ void __maxnreg__(128) k_gs_dot_tc(StepArgs a, int mode, GTArgs g) {
 // ---------------------------------------------------------------------------------------------------------------
 // Half B
 // ---------------------------------------------------------------------------------------------------------------
-template <int NX, bool LEVELS32>
+template <int NX>
 __global__ void __maxnreg__(128) k_gs_update_tc(StepArgs a, int mode, GTArgs g) {
   KrylovState *st = a.st;
   if (st->stop) return;
@@ -541,7 +632,7 @@ __global__ void __maxnreg__(128) k_gs_update_tc(StepArgs a, int mode, GTArgs g) 
   __syncthreads();
   unsigned char *As = sm + GT_AOFF;
   unsigned char *Bs = sm + GT_BOFF;
-  // the scales of s and g (all threads), then their slices: [k8][x][8 slices][8 columns]
+  // the scales of s and g (all threads), then their byte slices: [k8][x][8 slots (7 bytes, slot 7 zero)][8 columns]
   {
     int Es = 0, Eg = 0;
     for (int j = tid; j < J; j += GT_THREADS) {
@@ -561,18 +652,20 @@ __global__ void __maxnreg__(128) k_gs_update_tc(StepArgs a, int mode, GTArgs g) 
   const int es = gt_escale(s_es[0]), eg = gt_escale(s_es[1]);
   for (int it = tid; it < 2 * NKS * 2; it += GT_THREADS) {
     const int x = it & 1, k8 = it >> 1;  // coefficients j = 8 k8 .. 8 k8 + 7 of vector x
-    double cv[8];
+    long long X[8];
+    int ovf = 0;
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
       const int j = 8 * k8 + k;
-      cv[k] = (j < J && (x == 0 || NX == 2)) ? a.coef[x * J + j] : 0.0;
+      const double cv = (j < J && (x == 0 || NX == 2)) ? a.coef[x * J + j] : 0.0;
+      X[k] = gt_fix55(cv, x ? eg : es, &ovf);
     }
-    uint4 sl[8];
-    int ovf = 0;
-    gt_slice8(cv, x ? eg : es, sl, &ovf);
+    uint4 sl[7];
+    gt_bytes7(X, sl);
     unsigned char *base = Bs + (size_t)(k8 * 2 + x) * 128;
 #pragma unroll
-    for (int q = 0; q < 8; ++q) *reinterpret_cast<uint4 *>(base + q * 16) = sl[q];
+    for (int q = 0; q < 7; ++q) *reinterpret_cast<uint4 *>(base + q * 16) = sl[q];
+    *reinterpret_cast<uint4 *>(base + 7 * 16) = make_uint4(0u, 0u, 0u, 0u);
   }
   gt_fence_async_smem();
   t5_fence_before();
@@ -600,39 +693,33 @@ __global__ void __maxnreg__(128) k_gs_update_tc(StepArgs a, int mode, GTArgs g) 
       for (int off = 16; off > 0; off >>= 1) etile = max(etile, __shfl_xor_sync(0xffffffffu, etile, off));
       if (!gt_wait(&S.bar[GB_CDONE + b], (uint32_t)((i >> 1) & 1), abort)) break;
       t5_fence_after();
-      // per vector, the 15 levels p + q: FP32 sums (exact while J <= 128: |level| <= 8 * 128 * 127^2 < 2^24), else
-      // 64-bit integer sums
-      using LT = typename std::conditional<LEVELS32, float, long long>::type;
+      // per vector, the 13 levels k + q of the byte products, as exact 32-bit integer sums
+      // (|D| <= 144 * 255^2 < 2^24, at most 7 products per level)
       double prod[2] = {0.0, 0.0};
 #pragma unroll
       for (int x = 0; x < NX; ++x) {
-        LT lev[15];
+        int lev[13];
 #pragma unroll
-        for (int L = 0; L < 15; ++L) lev[L] = 0;
+        for (int L = 0; L < 13; ++L) lev[L] = 0;
 #pragma unroll
-        for (int p = 0; p < 8; ++p) {
+        for (int k = 0; k < 7; ++k) {
           float v[16];
-          t5_ld16(tbase + ((uint32_t)(32 * warp) << 16) + (uint32_t)(b * 128 + p * 16), v);
+          t5_ld16(tbase + ((uint32_t)(32 * warp) << 16) + (uint32_t)(b * 128 + k * 16), v);
 #pragma unroll
-          for (int q = 0; q < 8; ++q) {
-            if constexpr (LEVELS32) lev[p + q] += v[x * 8 + q];
-            else lev[p + q] += (long long)__float2int_rn(v[x * 8 + q]);
-          }
+          for (int q = 0; q < 7; ++q) lev[k + q] += __float2int_rn(v[x * 8 + q]);
         }
-        long long A3 = 0, B3 = 0, C3 = 0;  // levels 0-4, 5-9, 10-14, each sum below 2^53 in magnitude
+        // X = sum_L lev_L 2^(8(12-L)) = A3 2^64 + B3 2^32 + C3, each part below 2^59 in magnitude
+        long long A3 = 0, B3 = 0, C3 = 0;
 #pragma unroll
-        for (int L = 0; L < 15; ++L) {
-          long long t;
-          if constexpr (LEVELS32) t = (long long)__float2int_rn(lev[L]);
-          else t = lev[L];
-          if (L < 5) A3 += t * (1ll << (7 * (4 - L)));
-          else if (L < 10) B3 += t * (1ll << (7 * (9 - L)));
-          else C3 += t * (1ll << (7 * (14 - L)));
+        for (int L = 0; L < 13; ++L) {
+          if (L < 5) A3 += (long long)lev[L] * (1ll << (8 * (4 - L)));
+          else if (L < 9) B3 += (long long)lev[L] * (1ll << (8 * (8 - L)));
+          else C3 += (long long)lev[L] * (1ll << (8 * (12 - L)));
         }
-        // X = A3 2^70 + B3 2^35 + C3;  (V c)_r = 2^(etile + e_c - 112) X
-        const double xs = fma(__ll2double_rn(A3), 1180591620717411303424.0,
-                              fma(__ll2double_rn(B3), 34359738368.0, __ll2double_rn(C3)));
-        prod[x] = (etile > -128) ? xs * gt_pow2(etile + (x ? eg : es) - 112) : 0.0;
+        const double xs = fma(__ll2double_rn(A3), 18446744073709551616.0,
+                              fma(__ll2double_rn(B3), 4294967296.0, __ll2double_rn(C3)));
+        // (V c)_r = 2^(etile + e_c - 110) X
+        prod[x] = (etile > -128) ? xs * gt_pow2(etile + (x ? eg : es) - 110) : 0.0;
       }
       t5_fence_before();
       __syncwarp();
@@ -665,8 +752,6 @@ __global__ void __maxnreg__(128) k_gs_update_tc(StepArgs a, int mode, GTArgs g) 
     }
   } else if (warp == GT_MWARP) {
     if (lane == 0) {
-      const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(16 >> 3) << 17) |
-                             ((uint32_t)(GT_R >> 4) << 24);
       const uint32_t bbase = t5_smem(Bs);
       int q = 0;
       bool ok = true;
@@ -680,9 +765,9 @@ __global__ void __maxnreg__(128) k_gs_update_tc(StepArgs a, int mode, GTArgs g) 
           const uint32_t abase = t5_smem(As + (size_t)sa * GT_STAGE);
           const uint64_t bd = t5_desc(bbase + (uint32_t)(ks * 2 * 256), 256, 128);
 #pragma unroll
-          for (int p = 0; p < 8; ++p) {
-            const uint64_t ad = t5_desc(abase + p * 4096, 2048, 128);
-            t5_mma(tbase + (uint32_t)(b * 128 + p * 16), ad, bd, idesc, ks > 0 ? 1u : 0u);
+          for (int k = 0; k < 7; ++k) {
+            const uint64_t ad = t5_desc(abase + k * 4096, 2048, 128);
+            t5_mma(tbase + (uint32_t)(b * 128 + k * 16), ad, bd, GT_IDESC, ks > 0 ? 1u : 0u);
           }
           t5_commit(&S.bar[GB_AEMPTY + sa]);
         }
@@ -692,38 +777,47 @@ __global__ void __maxnreg__(128) k_gs_update_tc(StepArgs a, int mode, GTArgs g) 
       if (!t5_wait(&S.bar[GB_FIN], 0)) *abort = 1;
     }
   } else {
-    // ---------------- slicers: item = (row rl, 8-column group kg) of a 16-column stage ----------------
+    // ---------------- slicers: item = (row rl, 8-column group kg) of a 16-column stage, loads one stage ahead ----
     const int s = tid - 32 * GT_SW0;
     const int rl = s & 127, kg = s >> 7;
-    int q = 0, ovf = 0;
-    bool ok = true;
-    for (int i = 0; i < my && ok; ++i) {
-      const int T = blockIdx.x + i * gridDim.x;
+    const int total = my * NKS;
+    int ovf = 0;
+    double vn[8];
+    auto load = [&](int q, double *v) {
+      const int T = blockIdx.x + (q / NKS) * gridDim.x, ks = q % NKS;
       const long long r = (long long)T * GT_R + rl;
-      int etile = -128;  // as the epilogue warps compute it
-      for (int j = lane; j < J; j += 32) etile = max(etile, (int)g.vexp[(size_t)j * g.ldt + T]);
-      for (int off = 16; off > 0; off >>= 1) etile = max(etile, __shfl_xor_sync(0xffffffffu, etile, off));
-      for (int ks = 0; ks < NKS && ok; ++ks, ++q) {
-        const int sa = q % GT_NA;
-        double v[8];
 #pragma unroll
-        for (int k = 0; k < 8; ++k) {
-          const int j = ks * 16 + kg * 8 + k;
-          v[k] = (j < J && r < n) ? __ldcs(V + (size_t)j * a.ldv + r) : 0.0;
-        }
-        uint4 sl[8];
-        gt_slice8(v, etile, sl, &ovf);
-        if (q >= GT_NA && !gt_wait(&S.bar[GB_AEMPTY + sa], (uint32_t)(((q / GT_NA) - 1) & 1), abort)) {
-          ok = false;
-          break;
-        }
-        unsigned char *dst = As + (size_t)sa * GT_STAGE + (size_t)((kg * 16 + (rl >> 3)) * 128 + (rl & 7) * 16);
-#pragma unroll
-        for (int p = 0; p < 8; ++p) *reinterpret_cast<uint4 *>(dst + p * 4096) = sl[p];
-        gt_fence_async_smem();
-        __syncwarp();
-        if (lane == 0) gt_arrive(&S.bar[GB_AFULL + sa]);
+      for (int k = 0; k < 8; ++k) {
+        const int j = ks * 16 + kg * 8 + k;
+        v[k] = (j < J && r < n) ? __ldcs(V + (size_t)j * a.ldv + r) : 0.0;
       }
+    };
+    if (total > 0) load(0, vn);
+    int etile = -128;
+    for (int q = 0; q < total; ++q) {
+      const int sa = q % GT_NA;
+      const int T = blockIdx.x + (q / NKS) * gridDim.x;
+      if (q % NKS == 0) {
+        etile = -128;  // as the epilogue warps compute it
+        for (int j = lane; j < J; j += 32) etile = max(etile, (int)g.vexp[(size_t)j * g.ldt + T]);
+        for (int off = 16; off > 0; off >>= 1) etile = max(etile, __shfl_xor_sync(0xffffffffu, etile, off));
+      }
+      double v[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) v[k] = vn[k];
+      if (q + 1 < total) load(q + 1, vn);
+      long long X[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) X[k] = gt_fix55(v[k], etile, &ovf);
+      uint4 sl[7];
+      gt_bytes7(X, sl);
+      if (q >= GT_NA && !gt_wait(&S.bar[GB_AEMPTY + sa], (uint32_t)(((q / GT_NA) - 1) & 1), abort)) break;
+      unsigned char *dst = As + (size_t)sa * GT_STAGE + (size_t)((kg * 16 + (rl >> 3)) * 128 + (rl & 7) * 16);
+#pragma unroll
+      for (int k = 0; k < 7; ++k) *reinterpret_cast<uint4 *>(dst + k * 4096) = sl[k];
+      gt_fence_async_smem();
+      __syncwarp();
+      if (lane == 0) gt_arrive(&S.bar[GB_AFULL + sa]);
     }
     if (ovf) atomicExch(g.err, 2);
   }
@@ -829,12 +923,12 @@ cudaError_t launch_gs_dot_tc(const StepArgs &a, int nx, int mode, const GTArgs &
   return cudaGetLastError();
 }
 
-template <int NX, bool L32>
+template <int NX>
 static cudaError_t upd_go(const StepArgs &a, int mode, const GTArgs &g, int grid, cudaStream_t s) {
   const cudaError_t e =
-      cudaFuncSetAttribute(k_gs_update_tc<NX, L32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GT_UPD_SMEM);
+      cudaFuncSetAttribute(k_gs_update_tc<NX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GT_UPD_SMEM);
   if (e != cudaSuccess) return e;
-  k_gs_update_tc<NX, L32><<<grid, GT_THREADS, GT_UPD_SMEM, s>>>(a, mode, g);
+  k_gs_update_tc<NX><<<grid, GT_THREADS, GT_UPD_SMEM, s>>>(a, mode, g);
   return cudaGetLastError();
 }
 
@@ -843,10 +937,7 @@ cudaError_t launch_gs_update_tc(const StepArgs &a, int nx, int mode, const GTArg
   const int ntiles = (a.n + GT_R - 1) / GT_R;
   int grid = num_sms();
   if (grid > ntiles) grid = ntiles;
-  // level sums exact in FP32 while 8 * J * 127^2 < 2^24, i.e. J <= 128
-  const bool l32 = a.J <= 128;
-  if (nx == 2) return l32 ? upd_go<2, true>(a, mode, g, grid, s) : upd_go<2, false>(a, mode, g, grid, s);
-  return l32 ? upd_go<1, true>(a, mode, g, grid, s) : upd_go<1, false>(a, mode, g, grid, s);
+  return nx == 2 ? upd_go<2>(a, mode, g, grid, s) : upd_go<1>(a, mode, g, grid, s);
 }
 
 }  // namespace ksg
