@@ -42,12 +42,13 @@ typedef enum { EPS_GB300_DS_REFINED = 0, EPS_GB300_DS_QR = 1 } EPSGB300DSMethod;
 
 /* Gram-Schmidt of IEEE-double storage (EPS_GB300_ARITH_F64) inside EPSSolve.  No counterpart in the reference, whose
  * orthogonalisation (BVOrthogonalizeCGS1, src/sys/classes/bv/interface/bvorthog.c:91-132) calls FP64 BLAS gemv.
- *   EPS_GB300_GS_TENSOR (default): every product of the two Gram-Schmidt halves exact on the bf16 tensor cores
- *       (an error-free 8 x 7-bit slice split of the 56-bit fixed point of each value against its column/tile
- *       exponent), the slice sums recombined as exact integers, rounded once per 1024-row chunk and accumulated in
- *       double-double: more accurate than FP64 FMA, and not bound by GB300's FP64 pipe.  Used for the symmetric
- *       (Lanczos) variant with the tcgen05 restart; the other cases use the FMA kernels.
- *   EPS_GB300_GS_FMA: IEEE FP64 FMA in every product (FP64-pipe bound on GB300).
+ *   EPS_GB300_GS_FMA (default): IEEE FP64 FMA in every product (bound by GB300's FP64 pipe near 2.4 TB/s).
+ *   EPS_GB300_GS_TENSOR: every product of the two Gram-Schmidt halves exact on the FP16 tensor cores (an
+ *       error-free split of each value's 55/56-bit fixed point, against its column/tile exponent, into byte or
+ *       7-bit slices), the slice sums recombined as exact integers, rounded once per chunk of at most 512 rows and
+ *       accumulated in double-double: more accurate than FP64 FMA.  On the 128^3 Laplacian it is still slower
+ *       than the FMA kernels (the slicing on the CUDA cores bounds it).  Used for the symmetric (Lanczos) variant
+ *       with the tcgen05 restart; the other cases use the FMA kernels.
  * Option -eps_gb300_gs tensor|fma. */
 typedef enum { EPS_GB300_GS_TENSOR = 0, EPS_GB300_GS_FMA = 1 } EPSGB300GSMethod;
 PetscErrorCode EPSGB300SetGSMethod(EPS eps, EPSGB300GSMethod method);

@@ -445,8 +445,8 @@ class EPS:
         _check(load().EPSGB300SetRestartMethod(self.handle, self.RESTART_METHODS[method]), "EPSGB300SetRestartMethod")
 
     def setGSMethod(self, method):
-        """'tensor' (exact slice products on the tensor cores, the default for IEEE-double storage) or 'fma' (IEEE
-        FP64 FMA) for the Gram-Schmidt pair (EPSGB300SetGSMethod)."""
+        """'fma' (IEEE FP64 FMA, the default) or 'tensor' (exact slice products on the tensor cores) for the
+        Gram-Schmidt pair of IEEE-double storage (EPSGB300SetGSMethod)."""
         _check(load().EPSGB300SetGSMethod(self.handle, 1 if method == "fma" else 0), "EPSGB300SetGSMethod")
 
     def setTimeLimit(self, seconds):

@@ -54,7 +54,7 @@
 namespace ksg {
 
 constexpr int GT_R = 128;                                 // rows per tile
-constexpr int GT_NA = 4;                                  // A stages
+constexpr int GT_NA = 4;                                  // A stages (a power of two: slot = q & 3)
 constexpr int GT_DLBO = 2064;                             // half A: bytes between core matrices adjacent in K
 constexpr int GT_DSTAGE = 16 * GT_DLBO;                   // half A stage: 128 rows of 16 columns (8 slots)
 constexpr int GT_USTAGE = 7 * 4096;                       // half B stage: 7 byte matrices of 128 rows x 16 columns
@@ -101,18 +101,20 @@ KS_DEVICE GTShared gt_shared(unsigned char *sm, size_t misc) {
   return s;
 }
 
-// bounded wait that gives up at once when another role has aborted; false on timeout or abort
+// Bounded wait that gives up at once when another role has aborted; false on timeout or abort.  Each try suspends
+// the thread for up to 0.5 us instead of spinning, so waiting warps leave their issue slots to the slicers; at most
+// T5_WAIT_LIMIT / 16 tries.
 KS_DEVICE bool gt_wait(unsigned long long *bar, uint32_t parity, volatile int *abort) {
   const uint32_t a = t5_smem(bar);
-  for (int it = 0; it < T5_WAIT_LIMIT; ++it) {
+  for (int it = 0; it < T5_WAIT_LIMIT / 16; ++it) {
     uint32_t done;
     asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
         : "=r"(done)
-        : "r"(a), "r"(parity)
+        : "r"(a), "r"(parity), "r"(500u)
         : "memory");
     if (done) return true;
-    if ((it & 63) == 63 && *abort) return false;
+    if ((it & 15) == 15 && *abort) return false;
   }
   *abort = 1;
   return false;
@@ -492,45 +494,59 @@ __global__ void __maxnreg__(128) k_gs_dot_tc(StepArgs a, int mode, GTArgs g) {
     const int jl = s >> 4, k8 = s & 15;
     const int total = my * ct * NMB;
     int ovf = 0;
-    auto where = [&](int q, int &c, int &t, int &j, long long &r0, bool &valid) {
-      const int mb = q % NMB, tq = q / NMB;
-      t = tq % ct;
-      c = blockIdx.x + (tq / ct) * gridDim.x;
-      j = mb * 16 + jl;
+    // stage q -> (chunk c, tile t, column block mb), advanced without divisions: a cursor per look-ahead slot
+    struct Cur {
+      int mb, t, i;
+    };
+    auto step = [&](Cur &u) {
+      if (++u.mb == NMB) {
+        u.mb = 0;
+        if (++u.t == ct) {
+          u.t = 0;
+          ++u.i;
+        }
+      }
+    };
+    auto where_c = [&](const Cur &u, int &c, int &t, int &j, long long &r0, bool &valid) {
+      t = u.t;
+      c = blockIdx.x + u.i * gridDim.x;
+      j = u.mb * 16 + jl;
       r0 = ((long long)c * ct + t) * GT_R + 8 * k8;
       valid = j < J && c * ct + t < ntiles;
     };
-    double vn[8];
-    if (total > 0) {
+    Cur cq = {0, 0, 0}, cn = {0, 0, 0};  // the stage being sliced, the next stage to load
+    // the loads of the next two stages are in flight while a stage is sliced (about 32 KB per SM)
+    double vn1[8], vn2[8];
+    auto issue = [&](double *dst) {  // loads the stage at cursor cn, then advances it
+      int c2, t2, j2;
+      long long r2;
+      bool v2;
+      where_c(cn, c2, t2, j2, r2, v2);
+      gt_load8(V + (size_t)j2 * a.ldv + r2, r2, n, v2, dst);
+      step(cn);
+    };
+    if (total > 0) issue(vn1);
+    if (total > 1) issue(vn2);
+    for (int q = 0; q < total; ++q, step(cq)) {
+      const int sa = q & (GT_NA - 1);
       int c, t, j;
       long long r0;
       bool valid;
-      where(0, c, t, j, r0, valid);
-      gt_load8(V + (size_t)j * a.ldv + r0, r0, n, valid, vn);
-    }
-    for (int q = 0; q < total; ++q) {
-      const int sa = q % GT_NA;
-      int c, t, j;
-      long long r0;
-      bool valid;
-      where(q, c, t, j, r0, valid);
+      where_c(cq, c, t, j, r0, valid);
       double v[8];
 #pragma unroll
-      for (int k = 0; k < 8; ++k) v[k] = vn[k];
-      if (q + 1 < total) {
-        int c2, t2, j2;
-        long long r2;
-        bool v2;
-        where(q + 1, c2, t2, j2, r2, v2);
-        gt_load8(V + (size_t)j2 * a.ldv + r2, r2, n, v2, vn);
+      for (int k = 0; k < 8; ++k) {
+        v[k] = vn1[k];
+        vn1[k] = vn2[k];
       }
+      if (q + 2 < total) issue(vn2);
       const int ej = valid ? gt_vscale(g, j, c * ct, min(ct, ntiles - c * ct)) : 0;
       long long X[8];
 #pragma unroll
       for (int k = 0; k < 8; ++k) X[k] = gt_fix55(v[k], ej, &ovf);
       uint4 sl[7];
       gt_bytes7(X, sl);
-      if (q >= GT_NA && !gt_wait(&S.bar[GB_AEMPTY + sa], (uint32_t)(((q / GT_NA) - 1) & 1), abort)) break;
+      if (q >= GT_NA && !gt_wait(&S.bar[GB_AEMPTY + sa], (uint32_t)(((q >> 2) - 1) & 1), abort)) break;
       unsigned char *dst = As + (size_t)sa * GT_STAGE + (size_t)k8 * GT_DLBO + (size_t)jl * 128;
 #pragma unroll
       for (int k = 0; k < 7; ++k) *reinterpret_cast<uint4 *>(dst + k * 16) = sl[k];
@@ -782,9 +798,15 @@ __global__ void __maxnreg__(128) k_gs_update_tc(StepArgs a, int mode, GTArgs g) 
     const int rl = s & 127, kg = s >> 7;
     const int total = my * NKS;
     int ovf = 0;
-    double vn[8];
-    auto load = [&](int q, double *v) {
-      const int T = blockIdx.x + (q / NKS) * gridDim.x, ks = q % NKS;
+    // the loads of the next two stages are in flight while a stage is sliced
+    double vn1[8], vn2[8];
+    int lks = 0, li = 0;  // the next stage to load: column step lks of the tile li
+    auto load = [&](double *v) {
+      const int T = blockIdx.x + li * gridDim.x, ks = lks;
+      if (++lks == NKS) {
+        lks = 0;
+        ++li;
+      }
       const long long r = (long long)T * GT_R + rl;
 #pragma unroll
       for (int k = 0; k < 8; ++k) {
@@ -792,26 +814,35 @@ __global__ void __maxnreg__(128) k_gs_update_tc(StepArgs a, int mode, GTArgs g) 
         v[k] = (j < J && r < n) ? __ldcs(V + (size_t)j * a.ldv + r) : 0.0;
       }
     };
-    if (total > 0) load(0, vn);
+    if (total > 0) load(vn1);
+    if (total > 1) load(vn2);
     int etile = -128;
+    int cks = 0, ci = 0;  // the stage being sliced
     for (int q = 0; q < total; ++q) {
-      const int sa = q % GT_NA;
-      const int T = blockIdx.x + (q / NKS) * gridDim.x;
-      if (q % NKS == 0) {
+      const int sa = q & (GT_NA - 1);
+      const int T = blockIdx.x + ci * gridDim.x;
+      if (cks == 0) {
         etile = -128;  // as the epilogue warps compute it
         for (int j = lane; j < J; j += 32) etile = max(etile, (int)g.vexp[(size_t)j * g.ldt + T]);
         for (int off = 16; off > 0; off >>= 1) etile = max(etile, __shfl_xor_sync(0xffffffffu, etile, off));
       }
       double v[8];
 #pragma unroll
-      for (int k = 0; k < 8; ++k) v[k] = vn[k];
-      if (q + 1 < total) load(q + 1, vn);
+      for (int k = 0; k < 8; ++k) {
+        v[k] = vn1[k];
+        vn1[k] = vn2[k];
+      }
+      if (q + 2 < total) load(vn2);
+      if (++cks == NKS) {
+        cks = 0;
+        ++ci;
+      }
       long long X[8];
 #pragma unroll
       for (int k = 0; k < 8; ++k) X[k] = gt_fix55(v[k], etile, &ovf);
       uint4 sl[7];
       gt_bytes7(X, sl);
-      if (q >= GT_NA && !gt_wait(&S.bar[GB_AEMPTY + sa], (uint32_t)(((q / GT_NA) - 1) & 1), abort)) break;
+      if (q >= GT_NA && !gt_wait(&S.bar[GB_AEMPTY + sa], (uint32_t)(((q >> 2) - 1) & 1), abort)) break;
       unsigned char *dst = As + (size_t)sa * GT_STAGE + (size_t)((kg * 16 + (rl >> 3)) * 128 + (rl & 7) * 16);
 #pragma unroll
       for (int k = 0; k < 7; ++k) *reinterpret_cast<uint4 *>(dst + k * 4096) = sl[k];
