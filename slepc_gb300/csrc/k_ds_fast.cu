@@ -38,7 +38,11 @@ constexpr int DSF_CL = 16;     // largest cluster diagonalised as one block (lon
 constexpr int DSF_TILE = 16;   // output tile of the small FP64 products
 constexpr int DSF_ITERS = 4;   // refinement steps
 constexpr double DSF_TAU = 1e-5;
-constexpr double DSF_CHECK = 1024.0;  // accuracy check: |s_ij| <= 1024 eps ||T||_F outside clusters, |G - I| <= 1024 eps
+// accuracy check before the final cluster pass: |s_ij| <= 256 eps ||T||_F outside clusters; |G - I| <= 1e-12 (the
+// refinement's own rounding floor for X^T X is near 2e-13 at ld = 129; the Newton-Schulz step that follows the
+// check takes the orthogonality error of X from there to rounding level)
+constexpr double DSF_CHECK = 256.0;
+constexpr double DSF_CHECK_G = 1e-12;
 
 size_t ds_fast_scratch_doubles(int ld) {
   const int nt = (ld + DSF_TILE - 1) / DSF_TILE;
@@ -406,9 +410,12 @@ __global__ void __launch_bounds__(DSF_THREADS, 1) k_dsf_step(DSFArgs f, int fina
       b0 += red[w][0]; b1 += red[w][1]; b2 += red[w][2]; bm = fmax(bm, red[w][3]);
     }
     const double tau = DSF_TAU * bm;
-    s_tau = tau;
     s_tnorm = sqrt(b2);
     const double delta = 2.0 * (sqrt(b0) + sqrt(b2) * sqrt(b1));
+    // pairs closer than max(delta, tau) get no first-order correction in the update: they are clustered, so the
+    // cluster pass diagonalises them (the clustered-eigenvalue form of the refinement); a fixed tau alone left pairs
+    // between tau and delta neither corrected nor rotated
+    s_tau = fmax(delta, tau);
     if (!final_pass) f.scal[0] = fmax(delta, tau);
   }
   __syncthreads();
@@ -430,7 +437,8 @@ __global__ void __launch_bounds__(DSF_THREADS, 1) k_dsf_step(DSFArgs f, int fina
   const int ncl = s_ncl;
   if (final_pass) {
     // Accuracy check of the refined pairs: outside the clusters (diagonalised next by FP64 Jacobi) every
-    // off-diagonal entry of S = X^T T X must be at rounding level of ||T||, and G = X^T X at rounding level of I.
+    // off-diagonal entry of S = X^T T X must be at rounding level of ||T||, and G = X^T X close enough to I for the
+    // Newton-Schulz step.
     // A pair whose gap is too small for the refinement to converge in DSF_ITERS steps stays mixed and fails here;
     // the FP64 QR solver (k_ds_hep) then redoes the whole projected problem.
     for (int i = tid; i < m; i += DSF_THREADS) cl_of[i] = -1;
@@ -454,7 +462,7 @@ __global__ void __launch_bounds__(DSF_THREADS, 1) k_dsf_step(DSFArgs f, int fina
     if (tid == 0) {
       double bs = 0.0, bg = 0.0;
       for (int w = 0; w < DSF_THREADS / 32; ++w) { bs = fmax(bs, red[w][0]); bg = fmax(bg, red[w][1]); }
-      const int bad = !(bs <= DSF_CHECK * DBL_EPSILON * s_tnorm) || !(bg <= DSF_CHECK * DBL_EPSILON);
+      const int bad = !(bs <= DSF_CHECK * DBL_EPSILON * s_tnorm) || !(bg <= DSF_CHECK_G);
       *f.fallback = bad;
       f.ctl->ds_fallback = bad;
     }
