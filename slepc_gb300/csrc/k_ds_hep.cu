@@ -41,7 +41,7 @@ KS_DEVICE void ds_givens(double f, double g, double &c, double &s, double &r) {
       const double di = rsqrt(t2);
       c = fabs(f) * di;
       r = copysign(t2 * di, f);
-      s = copysign(g * di, f);  // g / r
+      s = (f < 0.0 ? -g : g) * di;  // g / r, r carrying the sign of f
     }
   }
 }
