@@ -269,10 +269,12 @@ def test_tcgen05_restart_fp64_storage(lib, case):
     a = run(csr, tol=1e-10, v0=v0, arith="f64", restart="tcgen05", **kw)
     b = run(csr, tol=1e-10, v0=v0, arith="f64", restart="pair", **kw)
     assert a["reason"] == 1 and b["reason"] == 1 and a["nconv"] >= kw["nev"]
-    # set-based: a degenerate spectrum may converge different numbers of copies
+    # set-based: a degenerate spectrum may converge different numbers of copies; the non-normal convection-diffusion
+    # operator's Ritz values are sensitive at the level of its tolerance, so that case uses the parity bound 1e-10
+    agree = 1e-12 if kw["hermitian"] else 1e-10
     for x, y in ((a, b), (b, a)):
         for v in x["eigr"][:kw["nev"]]:
-            assert np.min(np.abs(y["eigr"][:y["nconv"]] - v)) / abs(v) <= 1e-12
+            assert np.min(np.abs(y["eigr"][:y["nconv"]] - v)) / abs(v) <= agree
     if exact is not None:
         assert rel_match(a["eigr"][:a["nconv"]], exact, 1e-10)
     check_residuals(csr, a, 1e-10)
