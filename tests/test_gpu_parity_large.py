@@ -1,0 +1,104 @@
+"""GPU parity at the benchmarked workloads' shapes, checked independently of the device path.
+
+Each case solves through the C-ABI and checks the results on the host: eigenvalues against a closed-form spectrum or
+the oracle (the CPU restatement of the reference's Krylov-Schur), set-based over distinct values where the spectrum
+is degenerate; residuals ||A x - lam x|| / (||A||_inf |lam|) with scipy.sparse on the CSR arrays; ||X^T X - I|| in
+numpy for Hermitian problems.  Tolerances: eigenvalues 1e-10 relative, residuals the solve's tol, orthogonality
+1e-12.
+
+  convection-diffusion 200^2 (n = 40,000), EPS_NHEP, nev 20, ncv 64: the 1000^2 workload's operator and sizes of
+      the projected problem at 1/25 of the rows, against the closed form
+  Chung-Lu graph n = 2^20, nev 16, ncv 48: the 4M workload's generator at 1/4 of the rows (long rows segmented),
+      against the oracle, in IEEE FP64 and in pair arithmetic
+  512 problems of the batched workload's distribution (n log-uniform in [1000, 65536]) in one batched solve: every
+      problem's residuals and eigenvectors on the host, and a stratified sample of 24 against the oracle
+"""
+import os
+
+import numpy as np
+import pytest
+
+import slepc_gb300 as sg
+from slepc_gb300 import matgen, verify
+
+pytestmark = pytest.mark.gpu
+
+
+def test_convdiff_200_nhep(lib):
+    N, pe = 200, 10.0
+    csr = matgen.convection_diffusion_2d(N, pe)
+    n = N * N
+    res = sg.solve(csr, hermitian=False, which="LR", nev=20, ncv=64, tol=1e-10, v0=matgen.start_vector(n, 3),
+                   arith="f64")
+    assert res["reason"] == 1 and res["nconv"] >= 20
+    k = res["nconv"]
+    assert np.all(res["eigi"][:k] == 0.0)  # the operator is similar to a symmetric one: a real spectrum
+    exact = matgen.convdiff_eigenvalues(N, pe)
+    m = verify.match_spectrum(res["eigr"][:k], exact, "LR", 20)
+    assert m["ok"], m
+    r_a, _ = verify.residuals(csr, res["eigr"][:k], res["X"][:, :k])
+    assert r_a.max() <= 1e-10, r_a.max()
+
+
+@pytest.mark.parametrize("arith", ["f64", "pair"])
+def test_chung_lu_1m_against_oracle(lib, orc, arith):
+    n = 1 << 20
+    csr = matgen.chung_lu(n)
+    assert (np.diff(csr[0]) > 4096).sum() > 0  # long rows: the segmented SpMV path
+    v0 = matgen.start_vector(n, 4)
+    res = sg.solve(csr, hermitian=True, which="LR", nev=16, ncv=48, tol=1e-10, v0=v0, arith=arith)
+    ref = orc.solve(*csr, hermitian=True, which="LR", nev=16, ncv=48, tol=1e-10, v0=v0, nthreads=os.cpu_count() or 1,
+                    vectors=False)
+    assert res["reason"] == 1 and res["nconv"] >= 16 and ref.reason == 1
+    k = res["nconv"]
+    refv = np.asarray(ref.eigr[:ref.nconv])
+    # eigenvalue 1 has one copy per connected component: compare distinct values both ways
+    for v in verify.distinct(np.sort(res["eigr"][:16])[::-1], 1e-12):
+        assert np.min(np.abs(refv - v)) / abs(v) <= 1e-10
+    for v in verify.distinct(np.sort(refv[:16])[::-1], 1e-12):
+        assert np.min(np.abs(res["eigr"][:k] - v)) / abs(v) <= 1e-10
+    r_a, _ = verify.residuals(csr, res["eigr"][:k], res["X"][:, :k])
+    assert r_a.max() <= 1e-10, r_a.max()
+    assert verify.orthogonality(res["X"][:, :k]) <= 1e-12
+
+
+def test_batch_512_against_oracle(lib, orc):
+    count, nev, ncv, tol = 512, 8, 24, 1e-10
+    probs = []
+    for i in range(count):
+        u = matgen.uniform_01(6 + i, 1)[0]
+        n = int(round(np.exp(np.log(1000.0) + u * (np.log(65536.0) - np.log(1000.0)))))
+        probs.append((matgen.laplacian_2d_randdiag(n, 6 + i), 6 + i))
+    eps, mats = [], []
+    for csr, seed in probs:
+        A = sg.Mat(*csr)
+        e = sg.EPS().create()
+        e.setOperators(A)
+        e.setProblemType(sg.EPS.ProblemType.HEP)
+        e.setDimensions(nev, ncv)
+        e.setTolerances(tol)
+        e.setWhichEigenpairs("LM")
+        e.setInitialSpace(matgen.start_vector(len(csr[0]) - 1, seed))
+        eps.append(e)
+        mats.append(A)
+    sg.solve_batch(eps)
+    order = sorted(range(count), key=lambda i: len(probs[i][0][0]))
+    sample = set(order[:: count // 24])
+    for i, ((csr, seed), e) in enumerate(zip(probs, eps)):
+        n = len(csr[0]) - 1
+        assert e.getConvergedReason() == 1 and e.getConverged() >= nev, i
+        k = e.getConverged()
+        vals, X = np.zeros(k), np.zeros((n, k))
+        x = np.zeros(n)
+        for j in range(k):
+            vals[j] = e.getEigenpair(j, x)
+            X[:, j] = x
+        r_a, _ = verify.residuals(csr, vals, X)
+        assert r_a.max() <= tol, (i, r_a.max())
+        assert verify.orthogonality(X) <= 1e-12, i
+        if i in sample:
+            ref = orc.solve(*csr, hermitian=True, which="LM", nev=nev, ncv=ncv, tol=tol,
+                            v0=matgen.start_vector(n, seed), vectors=False)
+            refv = np.asarray(ref.eigr[:ref.nconv])
+            for v in vals[:nev]:
+                assert np.min(np.abs(refv - v)) / abs(v) <= 1e-10, (i, v)
