@@ -330,183 +330,145 @@ def run_batch(args):
     rep.close()
 
 
-SERVED = dict(desc="served stream: requests n = exp(U[ln 2e3, ln 2e6]); 70% EPS_HEP Laplacian + diag(U[0,1]) "
-                   "(3-D m^3 when n > 2e5, else 2-D near-square), 30% EPS_NHEP upwind convection-diffusion N^2 with "
-                   "Pe ~ U[1,50]; nev ~ U{4..32}, ncv = max(2 nev + 8, 24), tol = 1e-10, largest real; seed 7",
-              pool_sizes=20, pe_levels=(1.0, 12.0, 25.0, 37.0, 50.0))
+SERVED = dict(desc="served stream: Poisson arrivals at each rate for the window; per request n = exp(U[ln 2e3, ln 2e6]); "
+                   "70% EPS_HEP Laplacian + diag(U[0,1]) (3-D m^3 when n > 2e5, else 2-D near-square), 30% EPS_NHEP "
+                   "upwind convection-diffusion N^2 with Pe ~ U[1,50]; nev ~ U{4..32}, ncv = max(2 nev + 8, 24), "
+                   "tol = 1e-10, largest real; every request's matrix generated for it on arrival (no shared pool); "
+                   "seed 7")
 
 
-def served_requests(matgen, count, seed=7):
-    """The request stream: (kind, size, Pe, nev, ncv, start seed) per request, and a pool of matrices shared by
-    requests of the same family and size (sizes quantised to a log grid, Pe to a few levels, so the stream's
-    matrices can be generated in seconds)."""
-    u = matgen.uniform_01(seed, 5 * count).reshape(count, 5)
-    grid = np.exp(np.linspace(np.log(2e3), np.log(2e6), SERVED["pool_sizes"]))
-    reqs = []
-    for i in range(count):
-        n = float(np.exp(np.log(2e3) + u[i, 0] * (np.log(2e6) - np.log(2e3))))
-        n = float(grid[np.argmin(np.abs(np.log(grid) - np.log(n)))])
-        nev = 4 + min(28, int(u[i, 2] * 29))
-        ncv = max(2 * nev + 8, 24)
-        if u[i, 1] < 0.7:
-            kind = "hep3" if n > 2e5 else "hep2"
-            pe = 0.0
-        else:
-            kind = "nhep"
-            pe = SERVED["pe_levels"][min(len(SERVED["pe_levels"]) - 1, int(u[i, 3] * len(SERVED["pe_levels"])))]
-        reqs.append((kind, int(round(n)), pe, nev, ncv, 1000 + i))
-    return reqs
+def served_request(matgen, i, seed=7):
+    """Request i of the stream: (kind, n, Pe, nev, ncv, start seed), from its own splitmix64 draws."""
+    u = matgen.uniform_01(seed * 1000003 + i, 5)
+    n = float(np.exp(np.log(2e3) + u[0] * (np.log(2e6) - np.log(2e3))))
+    nev = 4 + min(28, int(u[2] * 29))
+    ncv = max(2 * nev + 8, 24)
+    if u[1] < 0.7:
+        kind = "hep3" if n > 2e5 else "hep2"
+        pe = 0.0
+    else:
+        kind = "nhep"
+        pe = 1.0 + 49.0 * float(u[3])
+    return kind, int(round(n)), pe, nev, ncv, 1000 + i
 
 
-def served_matrix(matgen, cache, kind, n, pe):
-    key = (kind, n, pe)
-    if key not in cache:
-        if kind == "hep3":
-            m = max(2, int(round(n ** (1.0 / 3.0))))
-            cache[key] = matgen.laplacian_3d_randdiag(m, 7 + m)
-        elif kind == "hep2":
-            cache[key] = matgen.laplacian_2d_randdiag(n, 7 + n)
-        else:
-            N = max(2, int(round(np.sqrt(n))))
-            cache[key] = matgen.convection_diffusion_2d(N, pe)
-    return cache[key]
+def served_matrix(matgen, kind, n, pe, i):
+    if kind == "hep3":
+        m = max(2, int(round(n ** (1.0 / 3.0))))
+        return matgen.laplacian_3d_randdiag(m, 7 + i)
+    if kind == "hep2":
+        return matgen.laplacian_2d_randdiag(n, 7 + i)
+    N = max(2, int(round(np.sqrt(n))))
+    return matgen.convection_diffusion_2d(N, pe)
 
 
 def run_served(args):
-    """Served form: the request stream through EPSGB300Server -- capacity (every request submitted at once) and
-    latency under Poisson arrivals -- beside the one-problem-per-launch EPSSolve path on a sample of the stream."""
+    """Served form at the stated arrival rates: for each rate, Poisson arrivals for one window, every request's
+    matrix generated when it arrives and submitted to EPSGB300Server (continuous batching, HBM-budget admission),
+    then a bounded drain.  Latency runs from the scheduled arrival to the result, so generator lag and queueing
+    count.  A request that arrives while the host queue holds max_queue unfinished requests is refused at the door
+    and counted as dropped."""
     import slepc_gb300 as sg
     from slepc_gb300 import matgen
     import ctypes
 
     sg.build()
     ctypes.CDLL("libcudart.so").cudaSetDevice(0)
-    count = args.served_count
-    t = time.time()
-    reqs = served_requests(matgen, count)
-    cache, mats = {}, {}
-    for kind, n, pe, nev, ncv, sd in reqs:
-        csr = served_matrix(matgen, cache, kind, n, pe)
-        if (kind, n, pe) not in mats:
-            mats[(kind, n, pe)] = sg.Mat(*csr)
-    gen_s = time.time() - t
-    tuning = sg.batch_tune(1, 10) if not args.no_tune else sg.batch_get_tuning()
-
-    def make(r):
-        kind, n, pe, nev, ncv, sd = r
-        A = mats[(kind, n, pe)]
-        e = sg.EPS().create()
-        e.setOperators(A)
-        e.setProblemType(sg.EPS.ProblemType.NHEP if kind == "nhep" else sg.EPS.ProblemType.HEP)
-        e.setDimensions(nev, ncv)
-        e.setTolerances(1e-10)
-        e.setWhichEigenpairs("LR")
-        e.setInitialSpace(matgen.start_vector(A.m, sd))
-        e._A = A
-        return e
-
-    def ok(e, nev):
-        return e.getConvergedReason() == 1 and e.getConverged() >= nev
-
-    budget = args.served_budget_gb * 1e9
-    W = args.served_window
-
-    def drain(srv, eps):
-        """Wait for every request; the ones the cancel ended raise and count as incomplete."""
-        done = []
-        for r, e in zip(reqs, eps):
-            try:
-                srv.wait(e)
-                done.append(ok(e, r[3]))
-            except sg.SlepcError:
-                done.append(None)
-        return done
-
-    # 1. capacity: the whole stream is queued at t = 0; eigenpairs of the requests completed within the window
-    srv = sg.Server(budget, max_requests=4096, max_ncv=72)
-    eps = [make(r) for r in reqs]
+    rates = [float(r) for r in args.served_rates.split(",")]
+    W, drain, budget = args.served_window, args.served_drain, args.served_budget_gb * 1e9
+    max_queue = args.served_max_queue
     clocks = ClockSampler(0)
     clocks.start()
-    for e in eps:
-        srv.submit(e)
-    time.sleep(W)
-    srv.cancel()
-    st_cap = srv.stats()
-    done = drain(srv, eps)
+    per_rate = []
+    base = 0
+    for rate in rates:
+        srv = sg.Server(budget, max_requests=4096, max_ncv=72)
+        rng = np.random.default_rng(7 + int(rate))
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, size=int(rate * W * 1.5) + 16))
+        arrivals = arrivals[arrivals < W]
+        live = []          # (request, eps, scheduled arrival, submit time)
+        finished = []      # (request, latency s, converged)
+        dropped = 0
+        lock = threading.Lock()
+        t0 = time.perf_counter()
+
+        def reap(block_until=None):
+            """Collect finished requests without blocking (or until a deadline)."""
+            nonlocal live
+            keep = []
+            for r, e, arr, sub in live:
+                try:
+                    done = srv.wait(e, 0.0 if block_until is None else max(0.0, block_until - time.perf_counter()))
+                except sg.SlepcError:
+                    done = True
+                if done:
+                    st = e.getStats()
+                    ok = e.getConvergedReason() == 1 and e.getConverged() >= r[3]
+                    finished.append((r, (sub - t0 - arr) + st["solve_seconds"], ok))
+                    e.destroy()
+                else:
+                    keep.append((r, e, arr, sub))
+            live = keep
+
+        gen_s = 0.0
+        for k, arr in enumerate(arrivals):
+            r = served_request(matgen, base + k)
+            now = time.perf_counter() - t0
+            if now > W:
+                dropped += len(arrivals) - k  # arrivals the generator could not reach within the window
+                break
+            reap()
+            if len(live) >= max_queue:
+                dropped += 1
+                continue
+            g0 = time.perf_counter()
+            csr = served_matrix(matgen, r[0], r[1], r[2], base + k)
+            A = sg.Mat(*csr)
+            e = sg.EPS().create()
+            e.setOperators(A)
+            e.setProblemType(sg.EPS.ProblemType.NHEP if r[0] == "nhep" else sg.EPS.ProblemType.HEP)
+            e.setDimensions(r[3], r[4])
+            e.setTolerances(1e-10)
+            e.setWhichEigenpairs("LR")
+            e.setInitialSpace(matgen.start_vector(A.m, r[5]))
+            e._A = A
+            gen_s += time.perf_counter() - g0
+            wait = t0 + arr - time.perf_counter()
+            if wait > 0:
+                time.sleep(wait)
+            srv.submit(e)
+            live.append((r, e, arr, time.perf_counter()))
+        base += len(arrivals)
+        end = t0 + W + drain
+        while live and time.perf_counter() < end:
+            reap(block_until=min(end, time.perf_counter() + 0.5))
+        incomplete = len(live)
+        srv.cancel()
+        for r, e, arr, sub in live:
+            try:
+                srv.wait(e)
+            except sg.SlepcError:
+                pass
+        st = srv.stats()
+        srv.destroy()
+        lat = sorted(x[1] for x in finished if x[2])
+        conv = sum(x[0][3] for x in finished if x[2])
+        per_rate.append({"rate_per_s": rate, "offered": int(len(arrivals)), "submitted": int(len(arrivals) - dropped),
+                         "dropped_at_door": int(dropped), "completed": len(lat), "incomplete_after_drain": incomplete,
+                         "p50_ms": 1000.0 * float(np.percentile(lat, 50)) if lat else None,
+                         "p99_ms": 1000.0 * float(np.percentile(lat, 99)) if lat else None,
+                         "eigenpairs_per_s": conv / (W + drain), "peak_admitted_bytes": st["peak_bytes"],
+                         "max_live": st["max_live"], "host_generate_s": round(gen_s, 1)})
+        print(json.dumps({"served_rate": per_rate[-1]}), file=sys.stderr, flush=True)
     clk = clocks.stop()
-    srv.destroy()
-    cap_conv = sum(r[3] for r, d in zip(reqs, done) if d)
-    cap_value = cap_conv / W
-    cap_done = sum(1 for d in done if d is not None)
-    # 2. the plain path over the same window: EPSSolve one request after another in arrival order, each solve bounded
-    #    by the time left, only converged solves counted
-    t0 = time.perf_counter()
-    pconv, pdone = 0, 0
-    for r in reqs:
-        left = W - (time.perf_counter() - t0)
-        if left <= 0:
-            break
-        e = make(r)
-        e.setTimeLimit(left)
-        e.solve()
-        if ok(e, r[3]) and time.perf_counter() - t0 <= W:
-            pconv += r[3]
-            pdone += 1
-        e.destroy()
-    plain_value = pconv / W
-    # 3. latency: Poisson arrivals at a fraction of the capacity measured above, for one window, then a drain of
-    #    half a window; latency = submission to result (server clock)
-    rate = args.served_rate if args.served_rate > 0 else max(0.05, 0.5 * cap_done / W)
-    rng = np.random.default_rng(7)
-    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=count))
-    srv = sg.Server(budget, max_requests=4096, max_ncv=72)
-    eps2 = [make(r) for r in reqs]
-    t0 = time.perf_counter()
-    submitted = []
-    for a, e in zip(arrivals, eps2):
-        if a > W:
-            break
-        d = t0 + a - time.perf_counter()
-        if d > 0:
-            time.sleep(d)
-        srv.submit(e)
-        submitted.append(e)
-    rest = t0 + 1.5 * W - time.perf_counter()
-    if rest > 0:
-        time.sleep(rest)
-    srv.cancel()
-    st_lat = srv.stats()
-    lat, lat_conv, incomplete = [], 0, 0
-    for r, e in zip(reqs, submitted):
-        try:
-            srv.wait(e)
-            lat.append(e.getStats()["solve_seconds"] * 1000.0)
-            lat_conv += r[3] if ok(e, r[3]) else 0
-        except sg.SlepcError:
-            incomplete += 1
-    srv.destroy()
-    lat.sort()
-    lat_s = 1.5 * W
+    best = max(per_rate, key=lambda x: x["eigenpairs_per_s"])
     line = {"metric": METRIC.replace("plain Krylov-Schur, one solve per step", "served Krylov-Schur stream"),
-            "value": cap_value, "unit": UNIT, "n_gpus": 1, "steps": 1, "warmup": 0,
-            "ms_per_step": 1000.0 * W, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic",
-            "config": {"workload": SERVED["desc"], "requests_in_stream": count, "matrices_in_pool": len(mats),
-                       "window_s": W, "hbm_budget_gb": args.served_budget_gb, "generate_s": round(gen_s, 1),
-                       "tuning": tuning},
-            "capacity": {"eigenpairs_per_s": cap_value, "requests_completed": cap_done,
-                         "peak_admitted_bytes": st_cap["peak_bytes"], "max_live": st_cap["max_live"],
-                         "cycles": st_cap["cycles"], "note": "whole stream queued at t=0; completions in the window"},
-            "latency_ms": {"arrival_rate_per_s": rate, "submitted": len(submitted), "completed": len(lat),
-                           "incomplete_after_drain": incomplete,
-                           "p50": float(np.percentile(lat, 50)) if lat else None,
-                           "p99": float(np.percentile(lat, 99)) if lat else None, "max": lat[-1] if lat else None,
-                           "eigenpairs_per_s": lat_conv / lat_s, "max_live": st_lat["max_live"]},
-            "plain": {"value": plain_value, "unit": UNIT, "requests_completed": pdone,
-                      "sample": "the same stream in arrival order, EPSSolve one at a time, over the same window"},
-            "speedup_vs_plain": cap_value / plain_value if plain_value > 0 else None, "clocks": clk,
-            # kernels per restart cycle of a server with ncv limit 72: start pass 4, 73 slots x 3, DS 2, restart, control
-            "gpu_launches": st_cap["cycles"] * (4 + 3 * 73 + 4)}
+            "value": best["eigenpairs_per_s"], "unit": UNIT, "n_gpus": 1, "steps": len(rates), "warmup": 0,
+            "ms_per_step": 1000.0 * (W + drain), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "pair", "data": "synthetic",
+            "config": {"workload": SERVED["desc"], "window_s": W, "drain_s": drain, "hbm_budget_gb": args.served_budget_gb,
+                       "max_queue": max_queue, "arith": "pair (the batched engine's arithmetic)"},
+            "rates": per_rate, "clocks": clk}
     print(json.dumps(line), flush=True)
 
 
@@ -557,9 +519,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="lap3d128", choices=list(WORKLOADS) + ["batch4096", "served"])
-    ap.add_argument("--served-count", type=int, default=200, help="requests in the served stream")
-    ap.add_argument("--served-rate", type=float, default=0.0,
-                    help="Poisson arrival rate of the latency run (default: half the measured capacity)")
+    ap.add_argument("--served-rates", default="50,100,200,500,1000,2000",
+                    help="Poisson arrival rates (requests/s) of the served runs, one window each")
+    ap.add_argument("--served-drain", type=float, default=30.0, help="seconds of drain after each window")
+    ap.add_argument("--served-max-queue", type=int, default=256,
+                    help="unfinished requests the host holds before refusing arrivals at the door")
     ap.add_argument("--served-budget-gb", type=float, default=200.0, help="HBM budget of the server")
     ap.add_argument("--served-window", type=float, default=60.0, help="seconds of each served measurement")
     ap.add_argument("--batch-count", type=int, default=0, help="problems in the batched workload (default 4096)")
