@@ -362,12 +362,21 @@ def served_matrix(matgen, kind, n, pe, i):
     return matgen.convection_diffusion_2d(N, pe)
 
 
+def served_lane(r):
+    """The server's lane of a request (its admission footprint n (ncv+1) 8 + 12 nnz against 64 MB), from the
+    request's parameters before its matrix exists (nnz: 7 per row for the 3-D operators, 5 for the 2-D ones)."""
+    kind, n, _, _, ncv, _ = r
+    nnz = n * (7 if kind == "hep3" else 5)
+    return 0 if n * (ncv + 1) * 8.0 + 12.0 * nnz <= 64.0 * 1024 * 1024 else 1
+
+
 def run_served(args):
     """Served form at the stated arrival rates: for each rate, Poisson arrivals for one window, every request's
     matrix generated when it arrives and submitted to EPSGB300Server (continuous batching, HBM-budget admission),
     then a bounded drain.  Latency runs from the scheduled arrival to the result, so generator lag and queueing
-    count.  A request that arrives while the host queue holds max_queue unfinished requests is refused at the door
-    and counted as dropped."""
+    count.  A request that arrives while its lane (small or large footprint, the server's two lanes) holds
+    max_queue unfinished requests is refused at the door and counted as dropped: per-lane backpressure, so that
+    long solves filling the queue do not shut out the short ones."""
     import slepc_gb300 as sg
     from slepc_gb300 import matgen
     import ctypes
@@ -381,6 +390,23 @@ def run_served(args):
     clocks.start()
     per_rate = []
     base = 0
+    # finished requests are released on a thread of their own: freeing device memory waits for the device to go
+    # idle, which would stall the arrival loop behind the solves in flight (the client hands results off)
+    import queue
+    grave = queue.Queue()
+
+    def release():
+        while True:
+            e = grave.get()
+            if e is None:
+                return
+            A = getattr(e, "_A", None)
+            e.destroy()
+            if A is not None:
+                A.destroy()
+
+    releaser = threading.Thread(target=release, daemon=True)
+    releaser.start()
     for rate in rates:
         srv = sg.Server(budget, max_requests=4096, max_ncv=72)
         rng = np.random.default_rng(7 + int(rate))
@@ -405,7 +431,7 @@ def run_served(args):
                     st = e.getStats()
                     ok = e.getConvergedReason() == 1 and e.getConverged() >= r[3]
                     finished.append((r, (sub - t0 - arr) + st["solve_seconds"], ok))
-                    e.destroy()
+                    grave.put(e)
                 else:
                     keep.append((r, e, arr, sub))
             live = keep
@@ -418,7 +444,8 @@ def run_served(args):
                 dropped += len(arrivals) - k  # arrivals the generator could not reach within the window
                 break
             reap()
-            if len(live) >= max_queue:
+            lane = served_lane(r)
+            if sum(1 for x in live if served_lane(x[0]) == lane) >= max_queue:
                 dropped += 1
                 continue
             g0 = time.perf_counter()
@@ -451,6 +478,9 @@ def run_served(args):
                 pass
         st = srv.stats()
         srv.destroy()
+        for r, e, arr, sub in live:
+            grave.put(e)
+        live = []
         lat = sorted(x[1] for x in finished if x[2])
         conv = sum(x[0][3] for x in finished if x[2])
         per_rate.append({"rate_per_s": rate, "offered": int(len(arrivals)), "submitted": int(len(arrivals) - dropped),
@@ -460,6 +490,8 @@ def run_served(args):
                          "eigenpairs_per_s": conv / (W + drain), "peak_admitted_bytes": st["peak_bytes"],
                          "max_live": st["max_live"], "host_generate_s": round(gen_s, 1)})
         print(json.dumps({"served_rate": per_rate[-1]}), file=sys.stderr, flush=True)
+    grave.put(None)
+    releaser.join()
     clk = clocks.stop()
     best = max(per_rate, key=lambda x: x["eigenpairs_per_s"])
     line = {"metric": METRIC.replace("plain Krylov-Schur, one solve per step", "served Krylov-Schur stream"),
@@ -467,7 +499,7 @@ def run_served(args):
             "ms_per_step": 1000.0 * (W + drain), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "pair", "data": "synthetic",
             "config": {"workload": SERVED["desc"], "window_s": W, "drain_s": drain, "hbm_budget_gb": args.served_budget_gb,
-                       "max_queue": max_queue, "arith": "pair (the batched engine's arithmetic)"},
+                       "max_queue_per_lane": max_queue, "arith": "pair (the batched engine's arithmetic)"},
             "rates": per_rate, "clocks": clk}
     print(json.dumps(line), flush=True)
 

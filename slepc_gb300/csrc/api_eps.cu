@@ -1255,6 +1255,10 @@ extern "C" PetscErrorCode EPSSetUp(EPS eps) {
   const int n = eps->A->m;
   KSG_CHECK(n > 0, PETSC_ERR_ARG_WRONG, "Empty operator");
   int nev = eps->nev, ncv = eps->ncv, mpd = eps->mpd;
+  // the dimensions clamped to the problem size (epssetup.c:336-337): ncv = n is a full basis, whose last
+  // factorisation step orthogonalises A v_(n-1) against all n columns and ends in a breakdown with beta = 0
+  if (nev > n) nev = n;
+  if (ncv != PETSC_DETERMINE && ncv > n) ncv = n;
   // EPSSetDimensions_Default (epssetup.c:648-671)
   if (ncv != PETSC_DETERMINE) {
     KSG_CHECK(ncv >= nev + 1 || (ncv == nev && ncv == n), PETSC_ERR_USER_INPUT, "The value of ncv must be at least nev+1");
@@ -1269,8 +1273,13 @@ extern "C" PetscErrorCode EPSSetUp(EPS eps) {
   }
   if (mpd == PETSC_DETERMINE) mpd = ncv;
   KSG_CHECK(ncv <= nev + mpd, PETSC_ERR_USER_INPUT, "The value of ncv must not be larger than nev+mpd");
-  KSG_CHECK(ncv < n, PETSC_ERR_SUP, "ncv (%d) must be smaller than the problem size (%d) on this path", ncv, n);
-  KSG_CHECK(ncv + 1 <= 144, PETSC_ERR_SUP, "ncv (%d) above 143 is not provided by the device projected solver", ncv);
+  // projected problems: shared memory to ld = 144, then in place in the EPS's own arrays (the symmetric solver to
+  // ld = 1024, the non-symmetric one to 640)
+  {
+    const int dsmax = ksg_eps_lanczos(eps) ? ds_hep_max_n() : ds_nhep_max_n();
+    KSG_CHECK(ncv + 1 <= dsmax, PETSC_ERR_SUP,
+              "ncv (%d) above %d is not provided by the device projected solver of this problem type", ncv, dsmax - 1);
+  }
   KSG_CHECK(eps->lock || mpd >= ncv, PETSC_ERR_SUP, "Should not use mpd parameter in non-locking variant");
   KSG_CHECK(eps->v0.empty() || (int)eps->v0.size() == n, PETSC_ERR_ARG_SIZ, "Initial vector has the wrong length");
   KSG_CHECK(eps->nini <= ncv, PETSC_ERR_USER_INPUT, "The number of initial vectors is larger than ncv");
@@ -1653,7 +1662,9 @@ static const bool kRestartTensorIsTcgen05 = true;
 static cudaError_t eps_restart(EPS eps, int a0, int K, int s0, int N, const double *Q, cudaStream_t s) {
   const int m = eps->restart_method;
   const bool t5 = m == EPS_GB300_RESTART_TCGEN05 || (m == EPS_GB300_RESTART_TENSOR && kRestartTensorIsTcgen05);
-  if ((eps->storage == STORE_PAIR && m != EPS_GB300_RESTART_PAIR) || (eps->storage == STORE_F64 && t5)) {
+  // the tensor-core restarts stage up to 144 columns of Q; wider bases take the CUDA-core kernel
+  const bool narrow = eps->ld <= 144;
+  if (narrow && ((eps->storage == STORE_PAIR && m != EPS_GB300_RESTART_PAIR) || (eps->storage == STORE_F64 && t5))) {
     if (t5) {
       const size_t need = restart_t5_scratch_bytes(eps->ld);  // about 2 KB per SM and basis column
       if (eps->rtc.count < need) {
@@ -1719,7 +1730,7 @@ static PetscErrorCode eps_solve_core(EPS eps, double tol, std::chrono::steady_cl
   {
     const int rm = eps->restart_method;
     eps->gs_tc_on = eps->storage == STORE_F64 && eps->arith == ARITH_F64 && eps->gs_method == EPS_GB300_GS_TENSOR &&
-                    herm && eps->vexp.p && ld <= gs_tc_max_columns() &&
+                    herm && eps->vexp.p && ld <= gs_tc_max_columns() && ncv < n &&
                     (rm == EPS_GB300_RESTART_TCGEN05 || (rm == EPS_GB300_RESTART_TENSOR && kRestartTensorIsTcgen05));
     if (eps->gs_tc_on) KSG_CUDA(cudaMemsetAsync(eps->gterr.p, 0, sizeof(int), s));
   }
@@ -1775,7 +1786,7 @@ static PetscErrorCode eps_solve_core(EPS eps, double tol, std::chrono::steady_cl
     da.conv_b = eps->nrmb;
     {
       LaunchScope ls(eps, EPS_GB300_K_DS, 0.0);
-      if (herm && eps->ds_method == EPS_GB300_DS_REFINED) {
+      if (herm && eps->ds_method == EPS_GB300_DS_REFINED && ld <= 144) {
         KSG_CUDA(launch_ds_hep_fast(da, ds_fast_layout(eps->dsf.p, ld), ld, s));
         eps->stats.kernel_launches += ds_fast_launches() - 1;
       } else if (herm) {
@@ -1789,7 +1800,7 @@ static PetscErrorCode eps_solve_core(EPS eps, double tol, std::chrono::steady_cl
     prof_collect(eps);
     const KSControl c = *eps->h_ctl;
     KSG_CHECK(!c.ds_error, PETSC_ERR_LIB, "The projected eigenproblem solver did not converge (restart %d)", its);
-    if (herm && eps->ds_method == EPS_GB300_DS_REFINED && c.ds_fallback) eps->stats.ds_fallbacks++;
+    if (herm && eps->ds_method == EPS_GB300_DS_REFINED && ld <= 144 && c.ds_fallback) eps->stats.ds_fallbacks++;
     const int k = c.nconv;
     l = c.l;
     reason = c.reason;

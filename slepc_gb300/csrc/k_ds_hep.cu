@@ -10,7 +10,7 @@
 // epsdefault.c:224-232,290-302) are evaluated so the host reads only a small control record.
 //
 // The rotation sequences are computed by one thread and applied to the rows of Q by all threads; Q lives in
-// shared memory (n <= 144).
+// shared memory for n <= 144, and in place in the caller's Q (global memory, L2-resident) up to n = 1024.
 #include <float.h>
 
 #include "batch_types.h"
@@ -22,6 +22,31 @@ namespace ksg {
 
 constexpr int DS_THREADS = 256;
 constexpr int DS_MAXN = 144;
+constexpr int DS_WIDE_MAXN = 1024;
+
+// per-index scratch of one projected solve: shared arrays for n <= 144, carved from dynamic shared memory above
+struct DSHepMem {
+  double *sd, *se, *rc, *rs, *serr, *dtmp;
+  int *sperm, *sw_a, *sw_b, *perm2, *comp, *where, *at;
+  double *Qs;  // n x n, column-major with leading dimension ldq
+  int ldq;
+  int inplace;  // Qs is a.Q itself (ldq = a.ld): no copy in or out
+};
+
+static inline size_t ds_wide_smem(int n) { return (size_t)n * (6 * sizeof(double) + 7 * sizeof(int)); }
+
+KS_DEVICE DSHepMem ds_wide_mem(unsigned char *raw, int n, double *Q, int ld) {
+  DSHepMem m;
+  double *dp = reinterpret_cast<double *>(raw);
+  m.sd = dp; m.se = dp + n; m.rc = dp + 2 * n; m.rs = dp + 3 * n; m.serr = dp + 4 * n; m.dtmp = dp + 5 * n;
+  int *ip = reinterpret_cast<int *>(dp + 6 * n);
+  m.sperm = ip; m.sw_a = ip + n; m.sw_b = ip + 2 * n; m.perm2 = ip + 3 * n; m.comp = ip + 4 * n;
+  m.where = ip + 5 * n; m.at = ip + 6 * n;
+  m.Qs = Q;
+  m.ldq = ld;
+  m.inplace = 1;
+  return m;
+}
 
 KS_DEVICE void ds_givens(double f, double g, double &c, double &s, double &r) {
   if (g == 0.0) {
@@ -63,15 +88,23 @@ KS_DEVICE int ds_compare(int which, double target, double ar, double ai, double 
   }
 }
 
-// Qs: n x n shared scratch, column-major with leading dimension n
-KS_DEVICE void ds_hep_body(const DSArgs &a, double *Qs) {
-  __shared__ double sd[DS_MAXN], se[DS_MAXN], rc[DS_MAXN], rs[DS_MAXN], serr[DS_MAXN];
-  __shared__ int sperm[DS_MAXN], sw_a[DS_MAXN], sw_b[DS_MAXN];
+// the small solver's scratch: shared arrays, Q in dynamic shared memory with leading dimension n
+#define DS_SMALL_MEM(m, Qshared, nn)                                                                          \
+  __shared__ double sd_[DS_MAXN], se_[DS_MAXN], rc_[DS_MAXN], rs_[DS_MAXN], serr_[DS_MAXN], dtmp_[DS_MAXN];  \
+  __shared__ int sperm_[DS_MAXN], swa_[DS_MAXN], swb_[DS_MAXN], perm2_[DS_MAXN], comp_[DS_MAXN],              \
+      where_[DS_MAXN], at_[DS_MAXN];                                                                         \
+  DSHepMem m = {sd_, se_, rc_, rs_, serr_, dtmp_, sperm_, swa_, swb_, perm2_, comp_, where_, at_, Qshared, nn, 0}
+
+KS_DEVICE void ds_hep_body(const DSArgs &a, const DSHepMem &mem) {
   __shared__ int s_cmd, s_lo, s_hi, s_nsw, s_fail;
   __shared__ double s_beta_e;
+  double *sd = mem.sd, *se = mem.se, *rc = mem.rc, *rs = mem.rs, *serr = mem.serr;
+  int *sperm = mem.sperm, *sw_a = mem.sw_a, *sw_b = mem.sw_b;
+  double *Qs = mem.Qs;
   const int tid = threadIdx.x;
   const KrylovState *st = a.st;
   const int n = st ? st->m : a.n;  // actual size of the factorisation
+  const size_t lq = mem.inplace ? (size_t)mem.ldq : (size_t)n;  // leading dimension of Qs
   const int flags = a.flags;
   const int l = a.l, k = a.k;
   const int nq = n;
@@ -80,8 +113,8 @@ KS_DEVICE void ds_hep_body(const DSArgs &a, double *Qs) {
     se[i] = a.e[i];
   }
   if (flags & DS_DO_SOLVE) {
-    for (int i = tid; i < n * n; i += DS_THREADS) Qs[i] = ((i % n) == (i / n)) ? 1.0 : 0.0;
-  } else {
+    for (int i = tid; i < n * n; i += DS_THREADS) Qs[(i % n) + (i / n) * lq] = ((i % n) == (i / n)) ? 1.0 : 0.0;
+  } else if (!mem.inplace) {
     for (int i = tid; i < n * n; i += DS_THREADS) Qs[i] = a.Q[(i % n) + (size_t)(i / n) * a.ld];
   }
   if (tid == 0) s_fail = 0;
@@ -125,7 +158,7 @@ KS_DEVICE void ds_hep_body(const DSArgs &a, double *Qs) {
       for (int t = 0; t <= j; ++t) {
         const int p = (t == 0) ? j : j - t;
         const double c = rc[t], s = rs[t];
-        double *x = row + (size_t)(l + p) * n, *y = row + (size_t)(l + p + 1) * n;
+        double *x = row + (size_t)(l + p) * lq, *y = row + (size_t)(l + p + 1) * lq;
         const double xv = *x, yv = *y;
         *x = c * xv + s * yv;
         *y = c * yv - s * xv;
@@ -200,13 +233,15 @@ KS_DEVICE void ds_hep_body(const DSArgs &a, double *Qs) {
       const int lo = s_lo, hi = s_hi;
       for (int r = tid; r < nq; r += DS_THREADS) {
         double *row = Qs + r;
+        // column l+i+1 of rotation i is column l+i of rotation i+1: carried in a register down the sweep
+        double t = row[(size_t)(l + hi) * lq];
         for (int i = hi - 1; i >= lo; --i) {
           const double c = rc[i], s = rs[i];
-          double *qi = row + (size_t)(l + i) * n, *qi1 = row + (size_t)(l + i + 1) * n;
-          const double t = *qi1;
-          *qi1 = s * (*qi) + c * t;
-          *qi = c * (*qi) - s * t;
+          const double qi = row[(size_t)(l + i) * lq];
+          row[(size_t)(l + i + 1) * lq] = s * qi + c * t;
+          t = c * qi - s * t;
         }
+        row[(size_t)(l + lo) * lq] = t;
       }
       __syncthreads();
     }
@@ -230,7 +265,7 @@ KS_DEVICE void ds_hep_body(const DSArgs &a, double *Qs) {
       }
     }
     // insertion sort by criterion on indices (dspriv.c:226-245), over positions [l, n)
-    int perm2[DS_MAXN];
+    int *perm2 = mem.perm2;
     for (int i = 0; i < n; ++i) perm2[i] = i;
     for (int i = l + 1; i < ((flags & DS_DO_SORT) ? n : 0); ++i) {
       const double re = sd[perm2[i]];
@@ -243,12 +278,12 @@ KS_DEVICE void ds_hep_body(const DSArgs &a, double *Qs) {
       }
     }
     // composite: final column i = original column sperm[perm2[i]]
-    double dtmp[DS_MAXN];
-    int comp[DS_MAXN];
+    double *dtmp = mem.dtmp;
+    int *comp = mem.comp;
     for (int i = 0; i < n; ++i) { comp[i] = sperm[perm2[i]]; dtmp[i] = sd[perm2[i]]; }
     for (int i = 0; i < n; ++i) sd[i] = dtmp[i];
     // realise comp as a swap sequence on columns: position i must receive original column comp[i]
-    int where[DS_MAXN], at[DS_MAXN];  // where[c]: current position of original column c; at[p]: column at p
+    int *where = mem.where, *at = mem.at;  // where[c]: current position of original column c; at[p]: column at p
     for (int i = 0; i < n; ++i) { where[i] = i; at[i] = i; }
     int nsw = 0;
     for (int i = 0; i < n; ++i) {
@@ -268,7 +303,7 @@ KS_DEVICE void ds_hep_body(const DSArgs &a, double *Qs) {
   __syncthreads();
   for (int r = tid; r < nq; r += DS_THREADS) {
     for (int t = 0; t < s_nsw; ++t) {
-      double *x = Qs + r + (size_t)sw_a[t] * n, *y = Qs + r + (size_t)sw_b[t] * n;
+      double *x = Qs + r + (size_t)sw_a[t] * lq, *y = Qs + r + (size_t)sw_b[t] * lq;
       const double v = *x;
       *x = *y;
       *y = v;
@@ -279,7 +314,7 @@ KS_DEVICE void ds_hep_body(const DSArgs &a, double *Qs) {
   const double beta = st ? st->beta_out : 0.0;
   const double beta_e = s_beta_e;
   for (int i = tid; i < n; i += DS_THREADS) {
-    const double qlast = Qs[(n - 1) + (size_t)i * n];
+    const double qlast = Qs[(n - 1) + (size_t)i * lq];
     if (flags & DS_DO_EXTRAROW) se[i] = beta_e * qlast;
     else if ((flags & DS_DO_SOLVE) && i < n - 1) se[i] = 0.0;
     const double w = fabs(sd[i]);
@@ -293,7 +328,8 @@ KS_DEVICE void ds_hep_body(const DSArgs &a, double *Qs) {
     a.eigr[i] = sd[i];
     if (a.eigi) a.eigi[i] = 0.0;
   }
-  for (int i = tid; i < n * n; i += DS_THREADS) a.Q[(i % n) + (size_t)(i / n) * a.ld] = Qs[i];
+  if (!mem.inplace)
+    for (int i = tid; i < n * n; i += DS_THREADS) a.Q[(i % n) + (size_t)(i / n) * a.ld] = Qs[i];
   if (tid == 0 && (flags & DS_DO_CONTROL)) {
     // EPSKrylovConvergence: first index from nconv whose estimate fails
     int kk;
@@ -328,7 +364,15 @@ KS_DEVICE void ds_hep_body(const DSArgs &a, double *Qs) {
 __global__ void __launch_bounds__(DS_THREADS, 1) k_ds_hep(DSArgs a) {
   extern __shared__ double Qs[];
   if (a.run_if && *a.run_if == 0) return;  // the fallback of the mixed-precision solver, not needed this restart
-  ds_hep_body(a, Qs);
+  DS_SMALL_MEM(m, Qs, 0);
+  ds_hep_body(a, m);
+}
+
+// projected problems above 144: Q rotated in place in the caller's array, per-index scratch in dynamic shared memory
+__global__ void __launch_bounds__(DS_THREADS, 1) k_ds_hep_wide(DSArgs a) {
+  extern __shared__ __align__(16) unsigned char dsraw[];
+  const int n = a.st ? a.st->m : a.n;
+  ds_hep_body(a, ds_wide_mem(dsraw, n, a.Q, a.ld));
 }
 
 // one block per instance of a batch whose projected problem is symmetric (grid-stride over the live list)
@@ -338,7 +382,8 @@ __global__ void __launch_bounds__(DS_THREADS) k_batch_ds_hep(const BatchInst *I,
     const BatchInst &p = I[list[v]];
     if (p.phase != BP_ITER || !p.hermitian) continue;
     __syncthreads();
-    ds_hep_body(batch_ds_args(p), Qs);
+    DS_SMALL_MEM(m, Qs, 0);
+    ds_hep_body(batch_ds_args(p), m);
   }
 }
 
@@ -354,8 +399,17 @@ cudaError_t launch_batch_ds_hep(const BatchInst *I, const int *list, const Batch
   return cudaGetLastError();
 }
 
+int ds_hep_max_n() { return DS_WIDE_MAXN; }
+
 cudaError_t launch_ds_hep(const DSArgs &a, int n_max, cudaStream_t s) {
-  if (n_max > DS_MAXN) return cudaErrorInvalidValue;
+  if (n_max > DS_WIDE_MAXN || a.ld < n_max) return cudaErrorInvalidValue;
+  if (n_max > DS_MAXN) {
+    const size_t shm = ds_wide_smem(n_max);
+    cudaError_t err = cudaFuncSetAttribute(k_ds_hep_wide, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+    if (err != cudaSuccess) return err;
+    k_ds_hep_wide<<<1, DS_THREADS, shm, s>>>(a);
+    return cudaGetLastError();
+  }
   const size_t shm = (size_t)n_max * n_max * 8;
   cudaError_t err = cudaFuncSetAttribute(k_ds_hep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
   if (err != cudaSuccess) return err;

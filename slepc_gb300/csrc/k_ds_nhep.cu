@@ -26,21 +26,22 @@
 namespace ksg {
 
 constexpr int NH_MAXN = 144;
+constexpr int NH_WIDE_MAXN = 640;  // the wide solver: A and Q in the caller's arrays (global memory, L2-resident)
 constexpr int NH_T = 128;  // threads of one solver: four warps, one per SM sub-partition (each has its own FP64 pipe)
 
-constexpr int NH_PAIRS = NH_MAXN / 2 + 1;
 constexpr int NH_SMEM_MAX = 220 * 1024;  // dynamic shared memory of one solver (A, and Q when both fit)
 
 #define AH(i, j) A[(i) + (size_t)(j) * lda]
 #define QH(i, j) Q[(i) + (size_t)(j) * ldq]
 
+template <int MAXN>
 struct NhShared {
-  double v[NH_MAXN + 4];
+  double v[MAXN + 4];
   double G[16];
   double red[NH_T / 32];
   double tau, beta, cs, sn;
-  double pc[NH_PAIRS], ps[NH_PAIRS];  // Givens rotations of one round of the parallel sort
-  int pf[NH_PAIRS];
+  double pc[MAXN / 2 + 1], ps[MAXN / 2 + 1];  // Givens rotations of one round of the parallel sort
+  int pf[MAXN / 2 + 1];
   int cmd, i0, i1, i2, i3;
   int fail;
 };
@@ -122,7 +123,8 @@ KS_DEVICE double nh_block_sum(double v, double *red) {
 
 // the reflector of a long vector computed by the whole block (x in shared memory, the Hessenberg reduction);
 // every thread returns tau, sh.beta holds beta
-__device__ double nh_house_block(int m, double *x, NhShared &sh) {
+template <class SH>
+__device__ double nh_house_block(int m, double *x, SH &sh) {
   const int tid = nh_tid();
   double s2 = 0.0;
   for (int i = 1 + tid; i < m; i += NH_T) s2 = fma(x[i], x[i], s2);
@@ -263,7 +265,8 @@ __device__ void nh_std2x2(double &a, double &b, double &c, double &d, double &cs
 }
 
 // standardise the 2x2 block at (i, i+1) and propagate to T and Q (whole block)
-__device__ void nh_std_block(double *A, int lda, double *Q, int ldq, int n, int i, NhShared &sh) {
+template <class SH>
+__device__ void nh_std_block(double *A, int lda, double *Q, int ldq, int n, int i, SH &sh) {
   if (nh_tid() == 0) {
     double a = AH(i, i), b = AH(i, i + 1), c = AH(i + 1, i), d = AH(i + 1, i + 1), cs, sn;
     nh_std2x2(a, b, c, d, cs, sn);
@@ -280,7 +283,8 @@ __device__ void nh_std_block(double *A, int lda, double *Q, int ldq, int n, int 
 }
 
 // Hessenberg reduction from column ilo (rows/columns before ilo already triangular), accumulated into Q
-__device__ void nh_hessenberg(double *A, int lda, double *Q, int ldq, int n, int ilo, NhShared &sh) {
+template <class SH>
+__device__ void nh_hessenberg(double *A, int lda, double *Q, int ldq, int n, int ilo, SH &sh) {
   for (int c = ilo; c < n - 2; ++c) {
     const int m = n - c - 1;
     for (int i = nh_tid(); i < m; i += NH_T) sh.v[i] = AH(c + 1 + i, c);
@@ -349,7 +353,8 @@ KS_DEVICE void nh_house3(double x0, double x1, double x2, double &tau, double &v
 // (lahqr: deflation test, exceptional shifts at 10 and 20 iterations, bulge chase with 3-element reflectors);
 // returns 0 or 1 (no convergence).  Warp 0 runs the deflation scan (32 subdiagonals per ballot) and the shift
 // computation in lockstep, every thread computes each bulge reflector, and the block applies it.
-__device__ int nh_francis(double *A, int lda, double *Q, int ldq, int n, int ilo, NhShared &sh) {
+template <class SH>
+__device__ int nh_francis(double *A, int lda, double *Q, int ldq, int n, int ilo, SH &sh) {
   const double smlnum = DBL_MIN * ((double)n / DBL_EPSILON);
   const int tid = nh_tid();
   for (int i = ilo + 2 + tid; i < n; i += NH_T)
@@ -574,7 +579,8 @@ __device__ void nh_sylv(int n1, int n2, const double *D, double *X, double smin)
 }
 
 // swap adjacent blocks of sizes n1 (at j1) and n2 (at j1+n1); returns 1 if rejected
-__device__ int nh_swap(double *A, int lda, double *Q, int ldq, int n, int j1, int n1, int n2, NhShared &sh) {
+template <class SH>
+__device__ int nh_swap(double *A, int lda, double *Q, int ldq, int n, int j1, int n1, int n2, SH &sh) {
   const int m = n1 + n2;
   if (n1 == 1 && n2 == 1) {
     const int j2 = j1 + 1;
@@ -712,7 +718,8 @@ __device__ int nh_swap(double *A, int lda, double *Q, int ldq, int n, int j1, in
 }
 
 // move the block at ifst up to ilst (ifst > ilst); 0 or 1 (rejected swap)
-__device__ int nh_move(double *A, int lda, double *Q, int ldq, int n, int ifst, int ilst, NhShared &sh) {
+template <class SH>
+__device__ int nh_move(double *A, int lda, double *Q, int ldq, int n, int ifst, int ilst, SH &sh) {
   if (ifst > 0 && AH(ifst, ifst - 1) != 0.0) ifst--;
   int nbf = (ifst < n - 1 && AH(ifst + 1, ifst) != 0.0) ? 2 : 1;
   if (ilst > 0 && AH(ilst, ilst - 1) != 0.0) ilst--;
@@ -851,8 +858,9 @@ KS_DEVICE int nh_cmp(int which, double target, double r1, double i1, double r2, 
 // rotation from T(j, j+1) and T(j+1, j+1) - T(j, j), trexc/laexc with n1 = n2 = 1).  Pairs of one round are
 // disjoint, so their rotations commute: all row rotations are applied, then all column rotations (T and Q), then
 // the diagonal exchanges.  The final order is the stable order of the criterion, as the selection sort's.
+template <class SH>
 __device__ void nh_sort_real(double *A, int lda, double *Q, int ldq, int n, int l, int which, double target,
-                             double *wr, NhShared &sh) {
+                             double *wr, SH &sh) {
   const int tid = nh_tid();
   int quiet = 0;
   for (int round = 0; round < 2 * (n - l) + 2 && quiet < 2; ++round) {
@@ -932,8 +940,9 @@ __device__ void nh_sort_real(double *A, int lda, double *Q, int ldq, int n, int 
 // reference factors A - tau I and solves with its transpose; here the transpose is copied into the scratch C
 // (ldc >= n) and eliminated with partial pivoting (the row of largest magnitude, the first one on ties), which
 // solves the same system.  A zero pivot (tau an eigenvalue of A) sets sh.fail.
+template <class SH>
 __device__ double nh_harmonic_translate(double *A, int lda, int n, double tau, double beta, double *C, int ldc,
-                                        double *g, NhShared &sh) {
+                                        double *g, SH &sh) {
   const int tid = nh_tid();
   for (int t = tid; t < n * n; t += NH_T) {
     const int r = t % n, c = t / n;
@@ -1005,8 +1014,9 @@ __device__ double nh_harmonic_translate(double *A, int lda, int n, double tau, d
 // Harmonic extraction, recovery before the restart (dsnhep.c:508-535 with DSSetDimensions(n, k, l)):
 // ghat = -Q(:, 0:k+l)^T g; A(i, j) += ghat_i Q(n-1, j) beta for i < k+l, k <= j < k+l; g <- g + Q(:, 0:k+l) ghat;
 // gamma = sqrt(1 + g'g) scales the extra-row entries k..k+l-1.  Returns gamma; g holds g~.
+template <class SH>
 __device__ double nh_harmonic_recover(double *A, int lda, const double *Q, int ldq, int n, int k, int l,
-                                      double beta, double *g, double *gh, NhShared &sh) {
+                                      double beta, double *g, double *gh, SH &sh) {
   const int tid = nh_tid(), ncol = k + l;
   for (int j = tid; j < ncol; j += NH_T) {
     double s = 0.0;
@@ -1032,10 +1042,11 @@ __device__ double nh_harmonic_recover(double *A, int lda, const double *Q, int l
   return gamma;
 }
 
+template <int MAXN>
 KS_DEVICE void ds_nhep_body(const DSArgs &a, double *smem, int smem_bytes) {
-  __shared__ NhShared sh;
-  __shared__ double wr[NH_MAXN], wi[NH_MAXN], errs[NH_MAXN];
-  __shared__ double hg[NH_MAXN], hgh[NH_MAXN];  // harmonic extraction: g and ghat
+  __shared__ NhShared<MAXN> sh;
+  __shared__ double wr[MAXN], wi[MAXN], errs[MAXN];
+  __shared__ double hg[MAXN], hgh[MAXN];  // harmonic extraction: g and ghat
   const int tid = nh_tid();
   const int n = a.st ? a.st->m : a.n;
   const int ld = a.ld, l = a.l, flags = a.flags;
@@ -1144,7 +1155,7 @@ KS_DEVICE void ds_nhep_body(const DSArgs &a, double *smem, int smem_bytes) {
     nh_sync();
     tnorm = sh.red[0];
     for (int w = 1; w < NH_T / 32; ++w) tnorm = fmax(tnorm, sh.red[w]);
-    double xr[NH_MAXN], xi[NH_MAXN];
+    double xr[MAXN], xi[MAXN];
     for (int k = l + tid; k < n; k += NH_T) {
       errs[k] = -1.0;
       if (k > 0 && AH(k, k - 1) != 0.0) continue;  // second row of a 2x2 block: handled by the first
@@ -1236,8 +1247,11 @@ KS_DEVICE void ds_nhep_body(const DSArgs &a, double *smem, int smem_bytes) {
 
 __global__ void __launch_bounds__(NH_T) k_ds_nhep(DSArgs a, int smem_bytes) {
   extern __shared__ double nh_dyn[];
-  ds_nhep_body(a, nh_dyn, smem_bytes);
+  ds_nhep_body<NH_MAXN>(a, nh_dyn, smem_bytes);
 }
+
+// projected problems above 144 rows: A and Q transformed in place in the caller's arrays
+__global__ void __launch_bounds__(NH_T) k_ds_nhep_wide(DSArgs a) { ds_nhep_body<NH_WIDE_MAXN>(a, nullptr, 0); }
 
 // one block per non-symmetric instance of a batch (grid-stride over the live list)
 __global__ void __launch_bounds__(NH_T) k_batch_ds_nhep(const BatchInst *I, const int *list, const BatchHdr *h,
@@ -1247,17 +1261,18 @@ __global__ void __launch_bounds__(NH_T) k_batch_ds_nhep(const BatchInst *I, cons
     const BatchInst &p = I[list[v]];
     if (p.phase != BP_ITER || p.hermitian) continue;
     nh_sync();
-    ds_nhep_body(batch_ds_args(p), nh_dyn, smem_bytes);
+    ds_nhep_body<NH_MAXN>(batch_ds_args(p), nh_dyn, smem_bytes);
   }
 }
 
 // eigenvectors of the leading n x n quasi-triangular block, normalised (DSVectors_NHEP_Eigen_All with back = "A")
+template <int MAXN>
 __global__ void __launch_bounds__(32) k_nhep_vectors(const double *A, int lda, int n, double *X) {
   const int lane = lane_id();
   double tnorm = 0.0;
   for (int j = 0; j < n; ++j)
     for (int i = 0; i <= j + 1 && i < n; ++i) tnorm = fmax(tnorm, fabs(AH(i, j)));
-  double xr[NH_MAXN], xi[NH_MAXN];
+  double xr[MAXN], xi[MAXN];
   for (int k = lane; k < n; k += 32) {
     if (k > 0 && AH(k, k - 1) != 0.0) continue;
     const int cplx = nh_eigvec(A, lda, n, k, tnorm, xr, xi);
@@ -1303,8 +1318,14 @@ cudaError_t prepare_ds_nhep() {
   return attr;
 }
 
+int ds_nhep_max_n() { return NH_WIDE_MAXN; }
+
 cudaError_t launch_ds_nhep(const DSArgs &a, int n_max, cudaStream_t s) {
-  if (n_max > NH_MAXN) return cudaErrorInvalidValue;
+  if (n_max > NH_WIDE_MAXN || a.ld < n_max) return cudaErrorInvalidValue;
+  if (n_max > NH_MAXN) {
+    k_ds_nhep_wide<<<1, NH_T, 0, s>>>(a);
+    return cudaGetLastError();
+  }
   const cudaError_t attr = prepare_ds_nhep();
   if (attr != cudaSuccess) return attr;
   const int bytes = nh_smem_bytes(n_max, g_nh_dyn[0]);
@@ -1323,8 +1344,9 @@ cudaError_t launch_batch_ds_nhep(const BatchInst *I, const int *list, const Batc
 }
 
 cudaError_t launch_nhep_vectors(double *T, int ld, int n, double *X, cudaStream_t s) {
-  if (n > NH_MAXN) return cudaErrorInvalidValue;
-  k_nhep_vectors<<<1, 32, 0, s>>>(T, ld, n, X);
+  if (n > NH_WIDE_MAXN) return cudaErrorInvalidValue;
+  if (n > NH_MAXN) k_nhep_vectors<NH_WIDE_MAXN><<<1, 32, 0, s>>>(T, ld, n, X);
+  else k_nhep_vectors<NH_MAXN><<<1, 32, 0, s>>>(T, ld, n, X);
   return cudaGetLastError();
 }
 

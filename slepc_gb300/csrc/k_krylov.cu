@@ -343,6 +343,8 @@ int gs_update_blocks(int n) {
 }
 
 int gs_max_columns() { return A_MAXJ; }
+int gs_wide_max_columns() { return GW_MAXJ; }
+int restart_wide_max_columns() { return RW_MAXK; }
 
 template <int NX, class Ar, class S>
 static cudaError_t dot_dispatch(const StepArgs &a, int mode, int blocks, cudaStream_t s) {
@@ -352,6 +354,7 @@ static cudaError_t dot_dispatch(const StepArgs &a, int mode, int blocks, cudaStr
   else if (J <= 64) k_gs_dot<NX, 4, Ar, S><<<blocks, A_THREADS, 0, s>>>(a, mode);
   else if (J <= 144) k_gs_dot<NX, 9, Ar, S><<<blocks, A_THREADS, 0, s>>>(a, mode);
   else if (J <= A_MAXJ) k_gs_dot<NX, 17, Ar, S><<<blocks, A_THREADS, 0, s>>>(a, mode);
+  else if (J <= GW_MAXJ) k_gs_dot_wide<NX, Ar, S><<<blocks, A_THREADS, (size_t)(2 * J + 4) * 8, s>>>(a, mode);
   else return cudaErrorInvalidValue;
   return cudaGetLastError();
 }
@@ -426,8 +429,24 @@ static cudaError_t restart_go(typename S::T *V, long long ldv, int n, int a0, in
 }
 
 template <class Ar, class S>
+static cudaError_t restart_wide_go(typename S::T *V, long long ldv, int n, int a0, int K, int s0, int N,
+                                   const double *Q, int ldq, cudaStream_t s) {
+  if (K > RW_MAXK) return cudaErrorInvalidValue;
+  const size_t shm = (size_t)K * RW_ROWS * sizeof(typename Ar::val);
+  const int ntiles = (n + RW_ROWS - 1) / RW_ROWS;
+  int blocks = num_sms() * (shm * 2 <= (size_t)227 * 1024 ? 2 : 1);
+  if (blocks > ntiles) blocks = ntiles;
+  const cudaError_t err = cudaFuncSetAttribute(k_restart_wide<Ar, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)shm);
+  if (err != cudaSuccess) return err;
+  k_restart_wide<Ar, S><<<blocks, R_THREADS, shm, s>>>(V, ldv, n, a0, K, s0, N, Q, ldq);
+  return cudaGetLastError();
+}
+
+template <class Ar, class S>
 static cudaError_t restart_dispatch(typename S::T *V, long long ldv, int n, int a0, int K, int s0, int N,
                                     const double *Q, int ldq, cudaStream_t s) {
+  if (K > R_MAXN || N > R_MAXN) return restart_wide_go<Ar, S>(V, ldv, n, a0, K, s0, N, Q, ldq, s);
   if (N <= 16) return restart_go<Ar, S, 1>(V, ldv, n, a0, K, s0, N, Q, ldq, s);
   if (N <= 32) return restart_go<Ar, S, 2>(V, ldv, n, a0, K, s0, N, Q, ldq, s);
   if (N <= 64) return restart_go<Ar, S, 4>(V, ldv, n, a0, K, s0, N, Q, ldq, s);
@@ -437,7 +456,7 @@ static cudaError_t restart_dispatch(typename S::T *V, long long ldv, int n, int 
 cudaError_t launch_restart(void *V, long long ldv, int n, int a0, int K, int s0, int N, const double *Q, int ldq,
                            int arith, cudaStream_t s, int storage) {
   if (N <= 0 || K <= 0) return cudaSuccess;
-  if (N > R_MAXN) return cudaErrorInvalidValue;
+  if (N > RW_MAXK || K > RW_MAXK) return cudaErrorInvalidValue;
   if (storage == STORE_F32)
     return restart_dispatch<PairAr, StF32>(static_cast<float *>(V), ldv, n, a0, K, s0, N, Q, ldq, s);
   if (storage == STORE_PAIR)

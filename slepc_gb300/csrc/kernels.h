@@ -97,8 +97,10 @@ int num_sms();
 int spmv_lanes_for(double avg_nnz);
 int gs_dot_blocks(int n);
 int gs_update_blocks(int n);
-int gs_max_columns();
+int gs_max_columns();  // columns of the register-tiled dot kernel; wider bases take the column-group kernel
+int gs_wide_max_columns();
 size_t restart_smem_bytes(int K, int N, int tile_rows);
+int restart_wide_max_columns();
 
 cudaError_t launch_spmv(const int *rp, const int *ci, const double *va, const double *x, double *y, int n, int lanes,
                         const KrylovState *st, double scale, cudaStream_t s);
@@ -136,8 +138,12 @@ cudaError_t launch_set_unit_scale(KrylovState *st, cudaStream_t s);
 cudaError_t launch_set_scales(KrylovState *st, double sigma, double invnu, cudaStream_t s);
 cudaError_t launch_scale(double *x, int n, double alpha, cudaStream_t s);
 cudaError_t launch_negate(void *x, long long count, int as_float, cudaStream_t s);
+// n_max <= 144: Q in shared memory; up to ds_hep_max_n(): Q rotated in place in a.Q (a.ld >= n_max)
 cudaError_t launch_ds_hep(const DSArgs &a, int n_max, cudaStream_t s);
+int ds_hep_max_n();
+// n_max <= 144: A (and Q when it fits) in shared memory; up to ds_nhep_max_n(): in place in a.H and a.Q
 cudaError_t launch_ds_nhep(const DSArgs &a, int n_max, cudaStream_t s);
+int ds_nhep_max_n();
 cudaError_t prepare_ds_nhep();  // shared-memory attributes of the NHEP solver kernels (call outside graph capture)
 size_t ds_fast_scratch_doubles(int ld);
 DSFArgs ds_fast_layout(double *scratch, int ld);

@@ -372,7 +372,10 @@ __device__ void gs_epilogue(const StepArgs &a, const double *res, int mode) {
       const double nu2 = aa - ss;
       const double onorm = sqrt(aa > 0.0 ? aa : 0.0);
       const double nu = nu2 > 0.0 ? sqrt(nu2) : 0.0;
-      const int lindep = !(nu2 > 0.0 && nu >= a.eta * onorm);
+      // a column orthogonalised against n columns (a full basis) is zero: breakdown with beta = 0, as the
+      // reference's safe orthogonalisation of the last column (bvkrylov.c:90, bvimpl.h:452-465)
+      const int full = J >= a.n && mode != 2;
+      const int lindep = full || !(nu2 > 0.0 && nu >= a.eta * onorm);
       sh_nu = nu;
       sh_lindep = lindep;
       sh_sigma = sigma;
@@ -388,7 +391,7 @@ __device__ void gs_epilogue(const StepArgs &a, const double *res, int mode) {
         st->stop = 1;
         st->breakdown = 1;
         if (mode == 0) st->m = j;
-        st->beta_out = st->beta_prev * nu;
+        st->beta_out = full ? 0.0 : st->beta_prev * nu;
       } else {
         const double invnu = 1.0 / nu;
         sh_invnu = invnu;
@@ -613,6 +616,150 @@ KS_DEVICE void gs_dot_body(const StepArgs &a, int mode, int bid, int nblk) {
 template <int NX, int CPW, class Ar, class S>
 __global__ void __launch_bounds__(A_THREADS, 1) k_gs_dot(StepArgs a, int mode) {
   gs_dot_body<NX, CPW, Ar, S>(a, mode, blockIdx.x, gridDim.x);
+}
+
+// Gram-Schmidt half A for bases wider than A_MAXJ columns: the columns in groups of A_WARPS * GW_CPW, each group a
+// pass over the block's row tiles (u and w restaged per pass, one column's extra read per 128); per column the sum
+// runs over the same rows in the same order as above.  The merged sums live in dynamic shared memory (2 J + 4
+// doubles).
+constexpr int GW_CPW = 8;
+constexpr int GW_MAXJ = 1024;
+
+template <int NX, class Ar, class S>
+KS_DEVICE void gs_dot_wide_body(const StepArgs &a, int mode, int bid, int nblk) {
+  KrylovState *st = a.st;
+  if (st->stop) return;
+  using val = typename Ar::val;
+  using acc = typename Ar::acc;
+  __shared__ __align__(16) val sx[NX][A_TILE];
+  __shared__ acc sred[A_WARPS][3];
+  __shared__ int s_last;
+  extern __shared__ __align__(16) unsigned char gwraw[];
+  double *res = reinterpret_cast<double *>(gwraw);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int n = a.n, J = a.J;
+  const double sigma = st->sigma;
+  using ST = typename S::T;
+  const ST *Vb = static_cast<const ST *>(a.V);
+  const ST *U = static_cast<const ST *>(a.U);
+  const ST *W = static_cast<const ST *>(a.W);
+  unsigned long long *pb = reinterpret_cast<unsigned long long *>(a.part) + (size_t)bid * a.pstride;
+  acc sc0, sc1, sc2;
+  Ar::zero(sc0);
+  Ar::zero(sc1);
+  Ar::zero(sc2);
+  const int ntiles = (n + A_TILE - 1) / A_TILE;
+  for (int g0 = 0; g0 < J; g0 += A_WARPS * GW_CPW) {
+    acc cacc[GW_CPW][NX];
+#pragma unroll
+    for (int k = 0; k < GW_CPW; ++k)
+#pragma unroll
+      for (int q = 0; q < NX; ++q) Ar::zero(cacc[k][q]);
+    for (int t = bid; t < ntiles; t += nblk) {
+      const int r0 = t * A_TILE;
+      const int rows = min(A_TILE, n - r0);
+      {
+        double u = 0.0, w = 0.0;
+        if (tid < rows) {
+          u = S::get(U + r0 + tid) * sigma;
+          if (NX == 2) w = S::get(W + r0 + tid);
+        }
+        const val us = Ar::cvt(u);
+        sx[0][tid] = us;
+        if (g0 == 0) Ar::fma(sc0, us, us);
+        if (NX == 2) {
+          const val ws = Ar::cvt(w);
+          sx[NX - 1][tid] = ws;
+          if (g0 == 0) {
+            Ar::fma(sc1, us, ws);
+            Ar::fma(sc2, ws, ws);
+          }
+        }
+      }
+      __syncthreads();
+#pragma unroll
+      for (int k = 0; k < GW_CPW; ++k) {
+        const int c = g0 + warp + k * A_WARPS;
+        if (c < J) {
+          const ST *col = Vb + (size_t)c * a.ldv + r0;
+          if (rows == A_TILE) {
+            val ca[8], cb[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) S::template load2<Ar>(col + lane * 2 + 64 * i, ca[i], cb[i]);
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+              const int rr = lane * 2 + 64 * i;
+              Ar::fma(cacc[k][0], ca[i], sx[0][rr]);
+              Ar::fma(cacc[k][0], cb[i], sx[0][rr + 1]);
+              if (NX == 2) {
+                Ar::fma(cacc[k][NX - 1], ca[i], sx[NX - 1][rr]);
+                Ar::fma(cacc[k][NX - 1], cb[i], sx[NX - 1][rr + 1]);
+              }
+            }
+          } else {
+            for (int rr = lane; rr < rows; rr += 32) {
+              const val a0 = S::template load1<Ar>(col + rr);
+              Ar::fma(cacc[k][0], a0, sx[0][rr]);
+              if (NX == 2) Ar::fma(cacc[k][NX - 1], a0, sx[NX - 1][rr]);
+            }
+          }
+        }
+      }
+      __syncthreads();
+    }
+#pragma unroll
+    for (int k = 0; k < GW_CPW; ++k) {
+      const int c = g0 + warp + k * A_WARPS;
+      if (c < J) {
+#pragma unroll
+        for (int q = 0; q < NX; ++q) {
+          const acc r = warp_reduce<Ar>(cacc[k][q]);
+          if (lane == 0) pb[c * NX + q] = Ar::pack(r);
+        }
+      }
+    }
+  }
+  {
+    acc r0 = warp_reduce<Ar>(sc0), r1 = warp_reduce<Ar>(sc1), r2 = warp_reduce<Ar>(sc2);
+    if (lane == 0) {
+      sred[warp][0] = r0;
+      sred[warp][1] = r1;
+      sred[warp][2] = r2;
+    }
+    __syncthreads();
+    if (warp == 0) {
+      const int nsc = (NX == 2) ? 3 : 1;
+      for (int i = 0; i < nsc; ++i) {
+        acc v;
+        Ar::zero(v);
+        if (lane < A_WARPS) v = sred[lane][i];
+        v = warp_reduce<Ar>(v);
+        if (lane == 0) pb[J * NX + i] = Ar::pack(v);
+      }
+    }
+  }
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) s_last = (atomicAdd(&st->tickets[TK_DOT], 1u) == nblk - 1);
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  const int nout = J * NX + ((NX == 2) ? 3 : 1);
+  const unsigned long long *pall = reinterpret_cast<const unsigned long long *>(a.part);
+  for (int o = tid; o < nout; o += A_THREADS) {
+    acc s;
+    Ar::zero(s);
+    for (int b = 0; b < nblk; ++b) Ar::merge(s, Ar::unpack(__ldcg(pall + (size_t)b * a.pstride + o)));
+    res[o] = Ar::value(s);
+  }
+  __syncthreads();
+  if (tid == 0) st->tickets[TK_DOT] = 0;
+  gs_epilogue<NX>(a, res, mode);
+}
+
+template <int NX, class Ar, class S>
+__global__ void __launch_bounds__(A_THREADS, 1) k_gs_dot_wide(StepArgs a, int mode) {
+  gs_dot_wide_body<NX, Ar, S>(a, mode, blockIdx.x, gridDim.x);
 }
 
 // ------------------------------------------------------------------------------------------------------------
@@ -840,6 +987,64 @@ KS_DEVICE void restart_body(typename S::T *V, long long ldv, int n, int a0, int 
       }
     }
   }
+}
+
+// The restart for K or N above R_MAXN: tiles of RW_ROWS rows, the tile's K values per row staged in shared memory
+// (K x RW_ROWS, up to 128 KB), Q read through the cache.  Thread (cl, r) owns row r of the tile and output columns
+// cl + 16 q, in chunks of RW_CQ; every output element is one thread's sum over k in increasing order.  All reads of
+// the tile's rows precede the block's in-place writes (the tile is in shared memory), and no two blocks share a row.
+constexpr int RW_ROWS = 16;
+constexpr int RW_CQ = 8;
+constexpr int RW_MAXK = 1024;
+
+template <class Ar, class S>
+KS_DEVICE void restart_wide_body(typename S::T *V, long long ldv, int n, int a0, int K, int s0, int N,
+                                 const double *__restrict__ Q, int ldq, int bid, int nblk) {
+  using val = typename Ar::val;
+  using acc = typename Ar::acc;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  val *Vt = reinterpret_cast<val *>(smraw);  // K x RW_ROWS, column k contiguous
+  const int tid = threadIdx.x;
+  const int r = tid % RW_ROWS, cl = tid / RW_ROWS;
+  constexpr int NCL = R_THREADS / RW_ROWS;
+  const int ntiles = (n + RW_ROWS - 1) / RW_ROWS;
+  for (int t = bid; t < ntiles; t += nblk) {
+    const int r0 = t * RW_ROWS;
+    const int rows = min(RW_ROWS, n - r0);
+    __syncthreads();
+    for (int i = tid; i < K * RW_ROWS; i += R_THREADS) {
+      const int k = i / RW_ROWS, rr = i % RW_ROWS;
+      Vt[i] = (rr < rows) ? S::template load1<Ar>(V + (r0 + rr) + (size_t)(a0 + k) * ldv) : Ar::cvt(0.0);
+    }
+    __syncthreads();
+    for (int cb = 0; cb < N; cb += NCL * RW_CQ) {
+      acc o[RW_CQ];
+#pragma unroll
+      for (int q = 0; q < RW_CQ; ++q) Ar::zero(o[q]);
+      for (int k = 0; k < K; ++k) {
+        const val v = Vt[k * RW_ROWS + r];
+        const double *qk = Q + (a0 + k) + (size_t)s0 * ldq;
+#pragma unroll
+        for (int q = 0; q < RW_CQ; ++q) {
+          const int c = cb + cl + NCL * q;
+          if (c < N) Ar::fma(o[q], v, Ar::cvt(__ldg(qk + (size_t)c * ldq)));
+        }
+      }
+      if (r < rows) {
+#pragma unroll
+        for (int q = 0; q < RW_CQ; ++q) {
+          const int c = cb + cl + NCL * q;
+          if (c < N) S::put(V + (r0 + r) + (size_t)(s0 + c) * ldv, Ar::value(o[q]));
+        }
+      }
+    }
+  }
+}
+
+template <class Ar, class S>
+__global__ void __launch_bounds__(R_THREADS, 1) k_restart_wide(typename S::T *V, long long ldv, int n, int a0, int K,
+                                                               int s0, int N, const double *Q, int ldq) {
+  restart_wide_body<Ar, S>(V, ldv, n, a0, K, s0, N, Q, ldq, blockIdx.x, gridDim.x);
 }
 
 template <class Ar, class S, int CQ>

@@ -516,3 +516,97 @@ def test_device_eigenvectors_match_getEigenpair(lib, arith, kind):
     # the array is refreshed by the next solve
     eps.solve()
     assert np.allclose(eps.copyDeviceEigenvectors()[:, 0], Xd[:, 0], rtol=0, atol=1e-12)
+
+
+@pytest.mark.parametrize("arith", ["f64", "pair"])
+def test_test20_full_basis_on_gpu(lib, arith):
+    """test20.c: the smallest eigenvalue of the 1-D Laplacian n = 18 with the default ncv (16) and with ncv = 18 = n,
+    a full basis whose last factorisation step ends in a breakdown (beta = 0) with every Ritz value converged; ncv
+    above n is clamped to n (epssetup.c:336-337)."""
+    g = G["test20_1"]
+    n = g["n"]
+    csr = matgen.laplacian_1d(n)
+    for ncv, want in zip(g["ncv"], g["eigenvalues"]):
+        res = run(csr, hermitian=True, which=g["which"], nev=g["nev"], ncv=ncv, tol=g["tol"],
+                  v0=matgen.start_vector(n, 1), arith=arith)
+        assert res["reason"] == 1 and res["nconv"] >= 1
+        assert round(float(res["eigr"][0]), 5) == want
+        check_residuals(csr, res, g["tol"])
+    res = run(csr, hermitian=True, which="SR", nev=2, ncv=40, tol=g["tol"], v0=matgen.start_vector(n, 1),
+              arith=arith)
+    assert res["reason"] == 1 and res["eps"].getDimensions()[1] == n
+
+
+def test_full_basis_every_eigenpair(lib):
+    """ncv = nev = n: one restart gives the whole spectrum (HEP against LAPACK's eigh; NHEP against eigvals of a
+    dense non-normal matrix with complex pairs)."""
+    import scipy.linalg as sl
+
+    csr = matgen.laplacian_3d_randdiag(4, 2)  # n = 64, distinct eigenvalues
+    n = len(csr[0]) - 1
+    res = run(csr, hermitian=True, which="LR", nev=n, ncv=n, tol=1e-12, v0=matgen.start_vector(n, 2), arith="f64")
+    assert res["reason"] == 1 and res["nconv"] == n and res["its"] == 1
+    w = sl.eigh(matgen.csr_to_dense(*csr), eigvals_only=True)
+    assert np.max(np.abs(np.sort(res["eigr"]) - np.sort(w))) <= 1e-12 * np.max(np.abs(w))
+    check_residuals(csr, res, 1e-12)
+    assert host_orth(res) <= 1e-12
+    # non-Hermitian: the Brusselator at n = 40 (complex pairs), all eigenvalues
+    csr = matgen.brusselator(20)
+    n = len(csr[0]) - 1
+    res = run(csr, hermitian=False, which="LM", nev=n, ncv=n, tol=1e-12, v0=matgen.start_vector(n, 2), arith="f64")
+    assert res["reason"] == 1 and res["nconv"] == n
+    w = np.linalg.eigvals(matgen.csr_to_dense(*csr))
+    got = res["eigr"] + 1j * res["eigi"]
+    for lam in w:
+        assert np.min(np.abs(got - lam)) <= 1e-10 * np.max(np.abs(w)), lam
+
+
+@pytest.mark.parametrize("arith,ds", [("f64", "qr"), ("pair", "qr"), ("f64", "refined")])
+def test_wide_basis_nev100_default_ncv(lib, arith, ds):
+    """nev = 100 with the default ncv = 2 nev = 200 (EPSSetDimensions_Default, epssetup.c:663): a projected problem
+    of 201 rows, past the shared-memory solver (Q rotated in place), the column-group Gram-Schmidt and the wide
+    restart.  The 3-D Laplacian 32^3's closed-form spectrum, host residuals and orthogonality."""
+    csr = matgen.laplacian_3d(32)
+    n = 32 ** 3
+    res = run(csr, hermitian=True, which="LR", nev=100, tol=1e-10, v0=matgen.start_vector(n, 7), arith=arith, ds=ds)
+    assert res["eps"].getDimensions()[1] == 200
+    assert res["reason"] == 1 and res["nconv"] >= 100
+    m = verify.match_spectrum(res["eigr"][:res["nconv"]], matgen.laplacian_eigenvalues([32, 32, 32]), "LR", 100)
+    assert m["ok"], m
+    check_residuals(csr, res, 1e-10)
+    assert host_orth(res) <= 1e-12
+
+
+def test_wide_basis_nev500(lib):
+    """nev = 500: the default ncv is nev + mpd = 1000 with mpd = 500 (epssetup.c:664-667), a projected problem of
+    1001 rows.  The 2-D Laplacian 120 x 97 against its closed form."""
+    csr = matgen.laplacian_2d(120, 97)
+    n = 120 * 97
+    res = run(csr, hermitian=True, which="SR", nev=500, tol=1e-9, v0=matgen.start_vector(n, 8), arith="f64")
+    assert res["eps"].getDimensions() == (500, 1000, 500)
+    assert res["reason"] == 1 and res["nconv"] >= 500
+    m = verify.match_spectrum(res["eigr"][:res["nconv"]], matgen.laplacian_eigenvalues([120, 97]), "SR", 500,
+                              rel_tol=1e-9)
+    assert m["ok"], m
+    check_residuals(csr, res, 1e-9)
+    assert host_orth(res) <= 1e-12
+
+
+def test_wide_basis_nonsymmetric(lib):
+    """NHEP with nev = 100 and the default ncv = 200: the non-symmetric projected solver in place in the EPS's arrays
+    (201 rows).  Convection-diffusion 40^2 at Pe = 1 (the similarity to a symmetric matrix is well conditioned, so
+    the closed form pins the eigenvalues to 1e-9); ncv above 639 is PETSC_ERR_SUP at setup."""
+    N, pe = 40, 1.0
+    csr = matgen.convection_diffusion_2d(N, pe)
+    n = N * N
+    res = run(csr, hermitian=False, which="LR", nev=100, tol=1e-10, v0=matgen.start_vector(n, 9), arith="f64")
+    assert res["eps"].getDimensions()[1] == 200
+    assert res["reason"] == 1 and res["nconv"] >= 100
+    k = res["nconv"]
+    assert np.max(np.abs(res["eigi"][:k])) <= 1e-9 * np.max(np.abs(res["eigr"][:k]))
+    m = verify.match_spectrum(res["eigr"][:k], matgen.convdiff_eigenvalues(N, pe), "LR", 100, rel_tol=1e-9)
+    assert m["ok"], m
+    check_residuals(csr, res, 1e-10)
+    with pytest.raises(sg.SlepcError) as e:
+        run(matgen.convection_diffusion_2d(30, pe), hermitian=False, which="LR", nev=10, ncv=700, tol=1e-8)
+    assert e.value.code == 56
