@@ -30,15 +30,20 @@ PetscErrorCode EPSGB300SetArithmetic(EPS eps, EPSGB300Arith arith);
 PetscErrorCode EPSGB300GetArithmetic(EPS eps, EPSGB300Arith *arith);
 
 /* Solver of the symmetric projected problem inside EPSSolve.
- *   EPS_GB300_DS_QR (default): the reference's algorithm (arrowhead reduction, implicit QL) in FP64 in one thread
+ *   EPS_GB300_DS_AUTO (default): EPS_GB300_DS_REFINED while its accuracy checks pass; after two restarts in a row
+ *       whose pairs failed the check (each redone by the QR solver), EPS_GB300_DS_QR for the rest of the solve.
+ *       Problems whose wanted end is well separated keep the fast solver; dense clusters (the 3-D Laplacians) cost
+ *       two extra attempts per solve.
+ *   EPS_GB300_DS_QR: the reference's algorithm (arrowhead reduction, implicit QL) in FP64 in one thread
  *       block.
  *   EPS_GB300_DS_REFINED: FP32 arrowhead reduction and implicit QL, then FP64 eigenvector refinement (Ogita-Aishima
  *       iterations with clustered eigenvalues diagonalised by Jacobi, and a Newton-Schulz step), whose matrix
  *       products run on the whole GPU, then an accuracy check of every pair; a restart whose pairs fail the check is
  *       solved again by the QR solver (EPSGB300Stats.ds_fallbacks counts them).  Faster when the wanted end of the
  *       spectrum is well separated; on dense clusters (the 3-D Laplacians) every restart falls back.
- * The non-Hermitian solver and the DS object always use the FP64 algorithms.  Option -eps_gb300_ds refined|qr. */
-typedef enum { EPS_GB300_DS_REFINED = 0, EPS_GB300_DS_QR = 1 } EPSGB300DSMethod;  /* default: EPS_GB300_DS_QR */
+ * The non-Hermitian solver and the DS object always use the FP64 algorithms. */
+typedef enum { EPS_GB300_DS_REFINED = 0, EPS_GB300_DS_QR = 1, EPS_GB300_DS_AUTO = 2 } EPSGB300DSMethod;
+/* default: EPS_GB300_DS_AUTO; option -eps_gb300_ds auto|refined|qr */
 
 /* Gram-Schmidt of IEEE-double storage (EPS_GB300_ARITH_F64) inside EPSSolve.  No counterpart in the reference, whose
  * orthogonalisation (BVOrthogonalizeCGS1, src/sys/classes/bv/interface/bvorthog.c:91-132) calls FP64 BLAS gemv.
@@ -75,6 +80,14 @@ PetscErrorCode EPSGB300SetRestartMethod(EPS eps, EPSGB300RestartMethod method);
  * EPSSetStoppingTestFunction installs in the reference (epsdefault.c:290-302), for time-bounded callers. */
 PetscErrorCode EPSGB300SetTimeLimit(EPS eps, PetscReal seconds);
 
+/* Factorisation segments as CUDA graphs.  The launch sequence of one Krylov factorisation segment (from column k
+ * to nv: SpMV and the two Gram-Schmidt halves per step, then the final reorthogonalisation) depends only on k, nv
+ * and the EPS's buffers, so a segment seen a second time is captured once and replayed afterwards: the kernels and
+ * their results are the same, without the per-launch host work between them.  mode -1 (default): on for problems
+ * of at most 262144 rows, where launch gaps are a visible share of each step; 0: off; 1: on.  Graphs are dropped
+ * by EPSSetUp and EPSDestroy.  Off while per-kernel profiling is on.  Option -eps_gb300_graphs -1|0|1. */
+PetscErrorCode EPSGB300SetGraphCapture(EPS eps, PetscInt mode);
+
 /* CUDA device ordinal used by this EPS (default: the current device at EPSCreate). */
 PetscErrorCode EPSGB300SetDevice(EPS eps, int device);
 
@@ -91,6 +104,7 @@ typedef struct {
   long long precision_restarts; /* EPS_GB300_ARITH_F32: restarts of the FP32-storage phase */
   long long ds_fallbacks;       /* restarts whose mixed-precision projected solve failed its accuracy check and was
                                    redone by the FP64 QR solver */
+  long long graph_segments;     /* factorisation segments replayed from captured CUDA graphs */
 } EPSGB300Stats;
 PetscErrorCode EPSGB300GetStats(EPS eps, EPSGB300Stats *stats);
 

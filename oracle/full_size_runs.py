@@ -6,7 +6,10 @@ running the complete solve, and records it in full_size_runs.json beside this fi
 restatement of SLEPc 3.22's Krylov-Schur (CGS with IFNEEDED refinement, FP64 LAPACK-style projected solvers), so
 the counts are those of the reference algorithm on the same matrix and start vector.
 
-  python oracle/full_size_runs.py lap3d128 [lap3d64 convdiff1000 ...] [--threads T]
+  python oracle/full_size_runs.py lap3d128 [lap3d64 convdiff1000 ...] [--threads T] [--out FILE]
+
+--out writes the records to another file (a run on another host, merged into full_size_runs.json under the
+workload's "hosts" entry by hand).
 """
 import argparse
 import json
@@ -26,9 +29,10 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("workloads", nargs="+")
     ap.add_argument("--threads", type=int, default=os.cpu_count() or 1)
+    ap.add_argument("--out", default=os.path.join(HERE, "full_size_runs.json"))
     args = ap.parse_args()
     oracle.build()
-    path = os.path.join(HERE, "full_size_runs.json")
+    path = args.out
     out = json.load(open(path)) if os.path.exists(path) else {}
     for name in args.workloads:
         wl = bench.WORKLOADS[name]

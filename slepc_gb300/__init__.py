@@ -80,6 +80,7 @@ def load():
         "EPSGB300ServerDestroy": ([PP], I),
         "EPSGB300ServerCancel": ([P], I),
         "EPSGB300SetTimeLimit": ([P, D], I),
+        "EPSGB300SetGraphCapture": ([P, I], I),
         "EPSGB300SetRestartMethod": ([P, I], I),
         "EPSGB300SetGSMethod": ([P, I], I),
         "EPSGB300BatchGetTuning": ([ctypes.POINTER(I), I], I),
@@ -453,11 +454,15 @@ class EPS:
         """Wall-time budget of EPSSolve (checked after each restart; 0 = none)."""
         _check(load().EPSGB300SetTimeLimit(self.handle, float(seconds)), "EPSGB300SetTimeLimit")
 
+    def setGraphCapture(self, mode):
+        """Factorisation segments as CUDA graphs: -1 auto (n <= 262144), 0 off, 1 on (EPSGB300SetGraphCapture)."""
+        _check(load().EPSGB300SetGraphCapture(self.handle, int(mode)), "EPSGB300SetGraphCapture")
+
     def setProjectedSolver(self, method):
-        """'qr' (FP64 QL, default) or 'refined' (FP32 QL + FP64 refinement with a checked fallback to 'qr') for the
-        symmetric projected problem."""
-        _check(load().EPSGB300SetProjectedSolver(self.handle, 1 if method == "qr" else 0),
-               "EPSGB300SetProjectedSolver")
+        """'auto' (default: 'refined' until two restarts in a row fall back, then 'qr'), 'qr' (FP64 QL) or
+        'refined' (FP32 QL + FP64 refinement with a checked fallback to 'qr') for the symmetric projected problem."""
+        code = {"refined": 0, "qr": 1, "auto": 2}[method]
+        _check(load().EPSGB300SetProjectedSolver(self.handle, code), "EPSGB300SetProjectedSolver")
 
     def setUp(self):
         _check(load().EPSSetUp(self.handle), "EPSSetUp")
@@ -548,17 +553,17 @@ class EPS:
         return self._view("EPSView", (), path, False)
 
     def getStats(self):
-        buf = (ctypes.c_char * 80)()
+        buf = (ctypes.c_char * 88)()
         _check(load().EPSGB300GetStats(self.handle, buf), "EPSGB300GetStats")
         steps, restarts = np.frombuffer(bytes(buf[:16]), dtype=np.int64)
         solve_s, bytes_moved, setup_s = np.frombuffer(bytes(buf[16:40]), dtype=np.float64)
         launches = np.frombuffer(bytes(buf[40:48]), dtype=np.int64)[0]
         dev_ms = np.frombuffer(bytes(buf[48:56]), dtype=np.float64)[0]
-        psteps, prestarts, dsfb = np.frombuffer(bytes(buf[56:80]), dtype=np.int64)
+        psteps, prestarts, dsfb, graphs = np.frombuffer(bytes(buf[56:88]), dtype=np.int64)
         return {"krylov_steps": int(steps), "restarts": int(restarts), "solve_seconds": float(solve_s),
                 "bytes_moved": float(bytes_moved), "setup_seconds": float(setup_s), "kernel_launches": int(launches),
                 "solve_device_ms": float(dev_ms), "precision_steps": int(psteps),
-                "precision_restarts": int(prestarts), "ds_fallbacks": int(dsfb)}
+                "precision_restarts": int(prestarts), "ds_fallbacks": int(dsfb), "graph_segments": int(graphs)}
 
     KERNEL_CLASSES = ("spmv", "gs_dot", "gs_update", "restart", "ds")
 

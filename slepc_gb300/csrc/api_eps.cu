@@ -622,7 +622,14 @@ PetscErrorCode ksg_orthonormalize_column(void *V, long long ldv, int n, int j, d
 // ---------------------------------------------------------------------------------------------------------------
 // EPS
 // ---------------------------------------------------------------------------------------------------------------
+static void eps_clear_graphs(EPS eps) {
+  for (auto &kv : eps->seg_graphs)
+    if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+  eps->seg_graphs.clear();
+}
+
 static PetscErrorCode eps_free_device(EPS eps) {
+  eps_clear_graphs(eps);
   eps->V.release();
   eps->d.release();
   eps->e.release();
@@ -982,8 +989,8 @@ extern "C" PetscErrorCode EPSGB300GetArithmetic(EPS eps, EPSGB300Arith *arith) {
 }
 extern "C" PetscErrorCode EPSGB300SetProjectedSolver(EPS eps, EPSGB300DSMethod method) {
   KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
-  KSG_CHECK(method == EPS_GB300_DS_REFINED || method == EPS_GB300_DS_QR, PETSC_ERR_ARG_OUTOFRANGE,
-            "Unknown projected solver");
+  KSG_CHECK(method == EPS_GB300_DS_REFINED || method == EPS_GB300_DS_QR || method == EPS_GB300_DS_AUTO,
+            PETSC_ERR_ARG_OUTOFRANGE, "Unknown projected solver");
   eps->ds_method = method;
   return 0;
 }
@@ -1011,6 +1018,13 @@ extern "C" PetscErrorCode EPSGB300SetRestartMethod(EPS eps, EPSGB300RestartMetho
   eps->restart_method = method;
   return 0;
 }
+extern "C" PetscErrorCode EPSGB300SetGraphCapture(EPS eps, PetscInt mode) {
+  KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
+  KSG_CHECK(mode >= -1 && mode <= 1, PETSC_ERR_ARG_OUTOFRANGE, "Graph capture mode must be -1, 0 or 1");
+  eps->graph_mode = (int)mode;
+  return 0;
+}
+
 extern "C" PetscErrorCode EPSGB300SetTimeLimit(EPS eps, PetscReal seconds) {
   KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
   eps->time_limit = seconds;
@@ -1152,9 +1166,13 @@ extern "C" PetscErrorCode EPSSetFromOptions(EPS eps) {
                                             : !strcmp(v, "tcgen05")  ? EPS_GB300_RESTART_TCGEN05
                                                                      : EPS_GB300_RESTART_TENSOR));
     else if (!strcmp(o, "-eps_gb300_ds") && v)
-      KSG_TRY(EPSGB300SetProjectedSolver(eps, !strcmp(v, "qr") ? EPS_GB300_DS_QR : EPS_GB300_DS_REFINED));
+      KSG_TRY(EPSGB300SetProjectedSolver(eps, !strcmp(v, "qr")        ? EPS_GB300_DS_QR
+                                               : !strcmp(v, "refined") ? EPS_GB300_DS_REFINED
+                                                                       : EPS_GB300_DS_AUTO));
     else if (!strcmp(o, "-eps_gb300_gs") && v)
       KSG_TRY(EPSGB300SetGSMethod(eps, !strcmp(v, "fma") ? EPS_GB300_GS_FMA : EPS_GB300_GS_TENSOR));
+    else if (!strcmp(o, "-eps_gb300_graphs") && v)
+      KSG_TRY(EPSGB300SetGraphCapture(eps, atoi(v)));
   }
   return 0;
 }
@@ -1296,6 +1314,7 @@ extern "C" PetscErrorCode EPSSetUp(EPS eps) {
   eps->ldv = ((long long)n + 63) / 64 * 64;
   KSG_CUDA(cudaSetDevice(eps->device));
   if (!eps->stream) KSG_CUDA(cudaStreamCreateWithFlags(&eps->stream, cudaStreamNonBlocking));
+  eps_clear_graphs(eps);  // captured segments hold the old buffers' addresses
   const int ld = eps->ld;
   KSG_CUDA(eps->V.alloc((size_t)eps->ldv * (ld + 1)));
   KSG_CUDA(cudaMemsetAsync(eps->V.p, 0, sizeof(double) * eps->V.count, eps->stream));
@@ -1435,7 +1454,7 @@ static double spmv_bytes(EPS eps) {
 }
 
 // one Krylov factorisation segment: steps k0..nv-1 plus the final reorthogonalisation of the residual vector
-static PetscErrorCode eps_factorize(EPS eps, int k0, int nv, double *bytes) {
+static PetscErrorCode eps_factorize_launch(EPS eps, int k0, int nv, double *bytes) {
   cudaStream_t s = eps->stream;
   const int n = eps->n;
   const int herm = ksg_eps_lanczos(eps);
@@ -1506,6 +1525,54 @@ static PetscErrorCode eps_factorize(EPS eps, int k0, int nv, double *bytes) {
   *bytes += colb * (nv + 1) + colb * (nv + 2);
   eps->stats.kernel_launches += 1;  // segment begin
   eps->stats.krylov_steps += nv - k0;
+  return 0;
+}
+
+// One factorisation segment: direct launches the first time a (k, nv) segment runs, a captured CUDA graph from the
+// second time on (the same kernels with the same arguments; the stop flag in the device state ends a segment early
+// in either form).  A capture that fails turns graphs off for this EPS and runs the launches directly.
+static PetscErrorCode eps_factorize(EPS eps, int k0, int nv, double *bytes) {
+  const bool on = eps->graph_mode == 1 || (eps->graph_mode == -1 && eps->n <= 262144);
+  if (!on || eps->prof || eps->gs_tc_on) return eps_factorize_launch(eps, k0, nv, bytes);
+  const std::array<int, 4> key = {k0, nv, eps->storage, eps->arith};
+  auto it = eps->seg_graphs.find(key);
+  if (it == eps->seg_graphs.end()) {
+    if (eps->seg_graphs.size() >= 512) return eps_factorize_launch(eps, k0, nv, bytes);
+    it = eps->seg_graphs.emplace(key, _p_EPS::SegGraph()).first;
+  }
+  _p_EPS::SegGraph &g = it->second;
+  if (!g.exec) {
+    if (++g.seen < 2) return eps_factorize_launch(eps, k0, nv, bytes);
+    const long long l0 = eps->stats.kernel_launches, s0 = eps->stats.krylov_steps;
+    double b = 0.0;
+    cudaGraph_t graph = nullptr;
+    cudaError_t ce = cudaStreamBeginCapture(eps->stream, cudaStreamCaptureModeThreadLocal);
+    PetscErrorCode ierr = 0;
+    if (ce == cudaSuccess) {
+      ierr = eps_factorize_launch(eps, k0, nv, &b);
+      ce = cudaStreamEndCapture(eps->stream, &graph);
+    }
+    cudaGraphExec_t exec = nullptr;
+    if (!ierr && ce == cudaSuccess && graph) ce = cudaGraphInstantiate(&exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    const long long captured = eps->stats.kernel_launches - l0;  // the kernels the capture recorded
+    eps->stats.kernel_launches = l0;
+    eps->stats.krylov_steps = s0;
+    if (ierr || ce != cudaSuccess || !exec) {
+      if (exec) cudaGraphExecDestroy(exec);
+      cudaGetLastError();  // the capture's error is not the solve's: the launches run directly from here on
+      eps->graph_mode = 0;
+      return eps_factorize_launch(eps, k0, nv, bytes);
+    }
+    g.exec = exec;
+    g.launches = captured;
+    g.bytes = b;
+  }
+  KSG_CUDA(cudaGraphLaunch(g.exec, eps->stream));
+  eps->stats.kernel_launches += g.launches;
+  eps->stats.krylov_steps += nv - k0;
+  eps->stats.graph_segments++;
+  *bytes += g.bytes;
   return 0;
 }
 
@@ -1749,6 +1816,11 @@ static PetscErrorCode eps_solve_core(EPS eps, double tol, std::chrono::steady_cl
   KSG_CUDA(cudaMemsetAsync(eps->H.p, 0, sizeof(double) * eps->H.count, s));
   int nconv = 0, l = 0, its = 0, reason = 0;
   double bytes = 0.0;
+  // the mixed-precision projected solver while it passes its checks (EPS_GB300_DS_AUTO: until two restarts in a
+  // row fall back to the QR solver)
+  bool ds_refined =
+      herm && ld <= 144 && (eps->ds_method == EPS_GB300_DS_REFINED || eps->ds_method == EPS_GB300_DS_AUTO);
+  int ds_fb_run = 0;
   while (reason == 0) {
     its++;
     int nv = std::min(nconv + mpd, ncv);
@@ -1786,7 +1858,7 @@ static PetscErrorCode eps_solve_core(EPS eps, double tol, std::chrono::steady_cl
     da.conv_b = eps->nrmb;
     {
       LaunchScope ls(eps, EPS_GB300_K_DS, 0.0);
-      if (herm && eps->ds_method == EPS_GB300_DS_REFINED && ld <= 144) {
+      if (ds_refined) {
         KSG_CUDA(launch_ds_hep_fast(da, ds_fast_layout(eps->dsf.p, ld), ld, s));
         eps->stats.kernel_launches += ds_fast_launches() - 1;
       } else if (herm) {
@@ -1800,7 +1872,14 @@ static PetscErrorCode eps_solve_core(EPS eps, double tol, std::chrono::steady_cl
     prof_collect(eps);
     const KSControl c = *eps->h_ctl;
     KSG_CHECK(!c.ds_error, PETSC_ERR_LIB, "The projected eigenproblem solver did not converge (restart %d)", its);
-    if (herm && eps->ds_method == EPS_GB300_DS_REFINED && ld <= 144 && c.ds_fallback) eps->stats.ds_fallbacks++;
+    if (ds_refined) {
+      if (c.ds_fallback) {
+        eps->stats.ds_fallbacks++;
+        if (++ds_fb_run >= 2 && eps->ds_method == EPS_GB300_DS_AUTO) ds_refined = false;
+      } else {
+        ds_fb_run = 0;
+      }
+    }
     const int k = c.nconv;
     l = c.l;
     reason = c.reason;
@@ -1907,6 +1986,7 @@ extern "C" PetscErrorCode EPSSolve(EPS eps) {
   eps->stats.krylov_steps = 0;
   eps->stats.restarts = 0;
   eps->stats.ds_fallbacks = 0;
+  eps->stats.graph_segments = 0;
   eps->stats.bytes_moved = 0.0;
   eps->stats.kernel_launches = 0;
   eps->stats.precision_steps = 0;

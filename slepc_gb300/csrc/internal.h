@@ -3,7 +3,9 @@
 
 #include <cuda_runtime.h>
 
+#include <array>
 #include <cstdio>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -162,7 +164,7 @@ struct _p_EPS {
   int trackall = 0;         // EPSSetTrackAll (stored; every current estimate is computed anyway)
   int arith = ksg::ARITH_PAIR;
   int storage = ksg::STORE_PAIR;  // basis format: pairs with pair arithmetic, doubles with FP64 arithmetic
-  int ds_method = EPS_GB300_DS_QR;  // EPSGB300DSMethod
+  int ds_method = EPS_GB300_DS_AUTO;  // EPSGB300DSMethod
   int gs_method = EPS_GB300_GS_FMA;  // EPSGB300GSMethod
   double time_limit = 0.0;        // EPSGB300SetTimeLimit (0: none)
   int restart_method = 0;         // EPSGB300RestartMethod
@@ -197,6 +199,15 @@ struct _p_EPS {
   DBuf<double> xvec;      // EPSGB300GetDeviceEigenvectors: FP64 eigenvectors in EPSGetEigenpair order
   DBuf<int> d_perm;       // its column map
   int xvec_valid = 0;     // xvec holds the current solve's vectors
+  // factorisation segments captured as CUDA graphs, keyed by (k, nv, storage, arithmetic)
+  struct SegGraph {
+    cudaGraphExec_t exec = nullptr;
+    int seen = 0;               // direct runs so far (captured on the second)
+    long long launches = 0;     // kernels in the graph
+    double bytes = 0.0;         // algorithmic bytes of the segment
+  };
+  std::map<std::array<int, 4>, SegGraph> seg_graphs;
+  int graph_mode = -1;  // EPSGB300SetGraphCapture
   DBuf<unsigned char> rtc;  // slices of Q for the tensor-core restart
   DBuf<float2> part;
   int pstride = 0;

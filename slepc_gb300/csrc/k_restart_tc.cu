@@ -21,6 +21,7 @@
 #include "common.cuh"
 #include "kernels.h"
 #include "ks_types.h"
+#include "oz_round.h"
 #include "tc_common.cuh"
 
 namespace ksg {
@@ -244,20 +245,17 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_restart_tc(float2 *__restrict
 // double-buffered in shared memory and filled by bulk copies of the TMA engine (cp.async.bulk, completion counted
 // in bytes on the stage's "full" mbarrier).  One thread runs the pipeline: the copies of stage i+1 are in flight
 // while the tensor cores run the 35 MMAs per K-step of stage i; tcgen05.commit arrives on the stage's "empty"
-// mbarrier when the MMAs that read it are done.  The epilogue reads TMEM with tcgen05.ld (warp w owns lanes
-// 32 (w mod 4) .. +31), recombines the levels as pairs and stores.  Every wait is bounded: on a timeout the kernel
-// sets *err, waits (bounded) for its copies and MMAs in flight, frees its TMEM and returns.
+// mbarrier when the MMAs that read it are done.  The epilogue reads TMEM with tcgen05.ld and recombines the levels
+// (as pairs, or for FP64 storage as exact integers rounded once, on the integer units: oz_round.h).
 // ---------------------------------------------------------------------------------------------------------------
 constexpr int T5_M = 128;                                  // rows per tile (MMA M)
 constexpr int T5_NC = 64;                                  // output columns per chunk (MMA N <= 64)
 constexpr int T5_KC = 32;                                  // K per shared-memory stage
-constexpr int T5_THREADS = 512;                            // 16 warps: 4 lane quarters x 4 column groups
+constexpr int T5_THREADS = 512;                            // 16 warps: 4 tensor warps, 12 slicing warps
 constexpr int T5_ASL = T5_M * T5_KC * 2;                   // bytes of one V slice in a stage
 constexpr int T5_BSL = T5_NC * T5_KC * 2;                  // bytes of one Q slice in a stage
 constexpr int T5_STAGE = OZ_SA * T5_ASL + OZ_QMAX * T5_BSL;  // 98304
 constexpr uint32_t T5_TMEM_COLS = OZ_L * T5_NC;            // 512
-constexpr size_t T5_SMEM = 2 * (size_t)T5_STAGE + (T5_THREADS / T5_M + 1) * T5_M * sizeof(int) +
-                           5 * sizeof(unsigned long long) + 16 + T5_NC * sizeof(int);
 // Basis storage of the tcgen05 restart.  T5Pair: FP32 pairs (hi, lo); the row exponent comes from hi, the fixed
 // point is the sum of both parts', and the result is written back as a pair.  T5F64: IEEE doubles; the fixed point
 // holds the 53-bit significand (truncated only below 2^-56 of the row maximum), and the result is the exact level
@@ -287,27 +285,67 @@ struct T5F64 {
   }
 };
 
+// ---------------------------------------------------------------------------------------------------------------
+// The kernel is warp-specialised, so that the phases of consecutive tiles overlap:
+//   warps 0-3, the tensor warps: thread 0 runs a chunk's operand-stage pipeline and MMAs (as above) and commits to
+//     tmem_full; the four warps then read the level sums out of TMEM (warp w: lanes 32 w .. +31, every 16-column
+//     group of the chunk) and write the outputs.
+//   warps 4-15, the slicing warps (384 threads): the row exponents and slices of the CTA's next tile, read from V
+//     in global memory and written to the CTA's scratch buffer (tile j in buffer j mod 2), while the tensor warps
+//     run the tile before it.
+// Hand-offs by mbarriers: ready[b] completes when the 384 slicing threads have filled buffer b (slices and row
+// exponents); done[b] when the four tensor warps have written back the tile of buffer b, so that the tile after
+// next may replace it.  Named barriers (1: tensor warps, 2: slicing warps) order each group's own phases.  The
+// slicing warps read rows of later tiles than the ones the tensor warps write, and a tile's rows are all read (its
+// slices complete) before its own outputs are written, so the in-place update stays safe.  Every wait is bounded;
+// a timeout in either group ends both (the other group's next wait runs out), the MMA thread then waits (bounded)
+// for its copies and MMAs in flight, and the kernel frees its TMEM and sets *err.
+// ---------------------------------------------------------------------------------------------------------------
+constexpr int T5W_TENSOR = 128;                       // threads of the tensor warps
+constexpr int T5W_SLICERS = T5_THREADS - T5W_TENSOR;  // 384
+constexpr int T5W_H = T5W_SLICERS / T5_M;             // slicing threads per row in the exponent pass
+constexpr size_t T5W_SMEM = 2 * (size_t)T5_STAGE + (2 + T5W_H) * T5_M * sizeof(int) +
+                            9 * sizeof(unsigned long long) + 16 + T5_NC * sizeof(int);
+
+KS_DEVICE void t5_bar(int id, int count) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory"); }
+
+// named barrier that also ANDs a flag over the participating threads
+KS_DEVICE int t5_bar_and(int id, int count, int v) {
+  uint32_t out;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.and.pred q, %2, %3, p;\n\tselp.u32 %0, 1, 0, q;\n\t}\n"
+      : "=r"(out)
+      : "r"((uint32_t)v), "r"(id), "r"(count)
+      : "memory");
+  return (int)out;
+}
+
+KS_DEVICE void t5_arrive(unsigned long long *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(t5_smem(bar)) : "memory");
+}
+
 template <class S, int QS>
 __global__ void __launch_bounds__(T5_THREADS, 1)
-    k_restart_t5(typename S::T *__restrict__ V, long long ldv, int n, int a0, int K, int s0, int N, int kp, int np,
-                 const __nv_bfloat16 *__restrict__ Bsl, const int *__restrict__ fcol, __nv_bfloat16 *__restrict__ Ascr,
-                 int *__restrict__ err, signed char *__restrict__ vexp, int ldt) {
+    k_restart_t5w(typename S::T *__restrict__ V, long long ldv, int n, int a0, int K, int s0, int N, int kp, int np,
+                  const __nv_bfloat16 *__restrict__ Bsl, const int *__restrict__ fcol,
+                  __nv_bfloat16 *__restrict__ Ascr, int *__restrict__ err, signed char *__restrict__ vexp, int ldt) {
   using T = typename S::T;
   extern __shared__ __align__(1024) unsigned char sm[];
-  int *erow = reinterpret_cast<int *>(sm + 2 * T5_STAGE);
-  int *etmp = erow + T5_M;  // (T5_THREADS / T5_M - 1) x 128 partial maxima
-  unsigned long long *full = reinterpret_cast<unsigned long long *>(etmp + (T5_THREADS / T5_M - 1) * T5_M);
-  unsigned long long *empty = full + 2;                                             // stage consumed (MMA commit)
-  unsigned long long *vbar = empty + 2;                                             // V tile loaded (TMA bytes)
-  uint32_t *tslot = reinterpret_cast<uint32_t *>(vbar + 1);
-  // FP64 storage with a column-exponent table: per output column of a chunk, the largest biased exponent of the
-  // tile's new values (recorded for the tensor-core Gram-Schmidt kernels)
+  int *erow = reinterpret_cast<int *>(sm + 2 * T5_STAGE);  // [2][128]: row exponents of the tile in buffer b
+  int *etmp = erow + 2 * T5_M;                             // [T5W_H][128]: partial maxima
+  unsigned long long *full = reinterpret_cast<unsigned long long *>(etmp + T5W_H * T5_M);  // stage loaded
+  unsigned long long *empty = full + 2;                                                     // stage consumed
+  unsigned long long *tfull = empty + 2;   // a chunk's MMAs done
+  unsigned long long *ready = tfull + 1;   // [2] a tile's slices in buffer b
+  unsigned long long *done = ready + 2;    // [2] buffer b's tile written back
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(done + 2);
   int *cmax = reinterpret_cast<int *>(tslot + 4);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid < T5_NC) cmax[tid] = 0;
-  const int nk8 = kp / 8;                    // core matrices along K (kp is a multiple of 16)
-  const int nkc = (kp + T5_KC - 1) / T5_KC;  // stages per chunk
-  __nv_bfloat16 *As = Ascr + (size_t)blockIdx.x * OZ_SA * nk8 * 16 * 64;  // [s][k8][m8][8 rows][8 k]
+  const int nk8 = kp / 8;
+  const int nkc = (kp + T5_KC - 1) / T5_KC;
+  const size_t abuf = (size_t)OZ_SA * nk8 * 16 * 64;       // bf16 elements of one slice buffer
+  __nv_bfloat16 *As0 = Ascr + (size_t)blockIdx.x * 2 * abuf;
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(t5_smem(tslot)),
                  "r"(T5_TMEM_COLS)
@@ -318,296 +356,316 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
     for (int b = 0; b < 2; ++b) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(t5_smem(&full[b])) : "memory");
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(t5_smem(&empty[b])) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(t5_smem(&ready[b])), "r"(T5W_SLICERS) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(t5_smem(&done[b])), "r"(T5W_TENSOR / 32)
+                   : "memory");
     }
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(t5_smem(vbar)) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(t5_smem(tfull)) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   t5_fence_before();
   __syncthreads();
   t5_fence_after();
   const uint32_t tbase = *tslot;
-  // barrier phases and outstanding completions (used by thread 0 only)
-  uint32_t fph[2] = {0u, 0u}, eph[2] = {0u, 0u};
-  int epend[2] = {0, 0}, fpend[2] = {0, 0};
-  int ok = 1;
-  // D = FP32, A = B = bf16, both K-major, M = 128 (N filled in per chunk)
-  const uint32_t idesc_m = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(T5_M >> 4) << 24);
   const int ntiles = (n + T5_M - 1) / T5_M;
-  // The V tile (K columns of up to 128 rows, [k][128] float2, at most 144 KB) is loaded by bulk copies into the
-  // stage region, which is free until the tile's slices exist.  The rows are rounded up to even (16-byte copies):
-  // the extra row is inside the basis' row padding (the leading dimension is a multiple of 64).
-  const T *vt = reinterpret_cast<const T *>(sm);
-  uint32_t vph = 0;
-  int vpend = 0;  // thread 0: a V tile load it issued has not been waited for
-  auto issue_v = [&](int tl) {  // thread 0
-    const int rr = min(T5_M, n - tl * T5_M);
-    const uint32_t bytes = (uint32_t)((rr + 1) & ~1) * 8u;
-    t5_expect_tx(vbar, (uint32_t)K * bytes);
-    for (int k = 0; k < K; ++k)
-      t5_bulk(sm + (size_t)k * T5_M * 8, V + (size_t)tl * T5_M + (size_t)(a0 + k) * ldv, bytes, vbar);
-  };
-  if (tid == 0 && blockIdx.x < ntiles) {
-    issue_v(blockIdx.x);
-    vpend = 1;
-  }
-  for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-    const int r0 = tile * T5_M;
-    const int rows = min(T5_M, n - r0);
-    if (!t5_wait(vbar, vph)) ok = 0;
-    vph ^= 1u;
-    vpend = 0;  // (every thread waited)
-    ok = __syncthreads_and(ok);
-    if (!ok) break;
-    // 1. row exponents: e_r = 1 + floor(log2 max_k |hi|) from the float exponent fields (four threads per row)
-    {
-      constexpr int H = T5_THREADS / T5_M;
-      const int m = tid & (T5_M - 1), h = tid >> 7;
-      int E = 0;
-      if (m < rows)
-        for (int k = h; k < K; k += H) E = max(E, S::expo(vt[(size_t)k * T5_M + m]));
-      if (h) etmp[(h - 1) * T5_M + m] = E;
-      __syncthreads();
-      if (!h) {
-#pragma unroll
-        for (int q = 0; q < H - 1; ++q) E = max(E, etmp[q * T5_M + m]);
-        erow[m] = E;
-      }
-      __syncthreads();
-    }
-    // 2. all slices of the tile into the scratch, one core-matrix row (8 consecutive k of one row) per item, two
-    //    items per pass
-    for (int it0 = tid; it0 < T5_M * nk8; it0 += 2 * T5_THREADS) {
-      T v[2][8];
-#pragma unroll
-      for (int p2 = 0; p2 < 2; ++p2) {
-        const int it = it0 + p2 * T5_THREADS;
-        const int m = it & (T5_M - 1), k8 = it >> 7;
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          const int k = 8 * k8 + j;
-          v[p2][j] = (it < T5_M * nk8 && m < rows && k < K) ? vt[(size_t)k * T5_M + m] : T{};
-        }
-      }
-#pragma unroll
-      for (int p2 = 0; p2 < 2; ++p2) {
-        const int it = it0 + p2 * T5_THREADS;
-        if (it >= T5_M * nk8) break;
-        const int m = it & (T5_M - 1), k8 = it >> 7;
-        const int er = erow[m];
-        uint32_t mh[8], ml[8], ng[8];
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          long long x = 0;
-          if (er) x = S::fix56(v[p2][j], S::escale(er));
-          ng[j] = x < 0 ? 1u : 0u;
-          const unsigned long long a = x < 0 ? (unsigned long long)(-x) : (unsigned long long)x;
-          mh[j] = (uint32_t)(a >> 32);
-          ml[j] = (uint32_t)a;
-        }
-#pragma unroll
-        for (int sl = 0; sl < OZ_SA; ++sl) {
-          uint32_t u[8];
-#pragma unroll
-          for (int j = 0; j < 8; ++j) u[j] = t5_field(mh[j], ml[j], sl);
-          uint4 w;
-          w.x = t5_slice_pair(u[0], u[1], ng[0], ng[1]);
-          w.y = t5_slice_pair(u[2], u[3], ng[2], ng[3]);
-          w.z = t5_slice_pair(u[4], u[5], ng[4], ng[5]);
-          w.w = t5_slice_pair(u[6], u[7], ng[6], ng[7]);
-          *reinterpret_cast<uint4 *>(As + (((size_t)sl * nk8 + k8) * 16 + (m >> 3)) * 64 + (m & 7) * 8) = w;
-        }
-      }
-    }
-    // the scratch is read next by the TMA engine, and the V tile's shared memory is overwritten by it
-    asm volatile("fence.proxy.async;" ::: "memory");
-    __syncthreads();
-    // 3. output columns in chunks of 64.  Thread 0 runs the pipeline: bulk copies of stage i+1 in flight while the
-    //    MMAs of stage i run; the other threads wait for the epilogue.
-    for (int c0 = 0; c0 < N && ok; c0 += T5_NC) {
-      const int nch = min(T5_NC, (N - c0 + 15) / 16 * 16);
-      if (tid == 0) {
-        const uint32_t idesc = idesc_m | ((uint32_t)(nch >> 3) << 17);
-        uint32_t initmask = 0;  // levels already written in this chunk
-        auto load = [&](int i) {  // stage i into buffer i & 1, once the MMAs that read the buffer are done
-          const int b = i & 1;
-          if (epend[b]) {
-            if (!t5_wait(&empty[b], eph[b])) {
-              ok = 0;  // the buffer may still be read: issue nothing
-              return;
-            }
-            eph[b] ^= 1u;
-            epend[b] = 0;
-          }
-          const int kc8 = i * (T5_KC / 8);
-          const int sk8 = min(T5_KC / 8, nk8 - kc8);
-          unsigned char *st = sm + b * T5_STAGE;
-          const uint32_t abytes = sk8 * 16 * 128, bbytes = (nch / 8) * 128;
-          t5_expect_tx(&full[b], OZ_SA * abytes + QS * sk8 * bbytes);
-          for (int sl = 0; sl < OZ_SA; ++sl)
-            t5_bulk(st + sl * T5_ASL, As + ((size_t)sl * nk8 + kc8) * 16 * 64, abytes, &full[b]);
-          for (int t = 0; t < QS; ++t)
-            for (int k8 = 0; k8 < sk8; ++k8)
-              t5_bulk(st + OZ_SA * T5_ASL + t * T5_BSL + k8 * (T5_NC / 8) * 128,
-                      Bsl + (((size_t)t * nk8 + kc8 + k8) * (np / 8) + c0 / 8) * 64, bbytes, &full[b]);
-          fpend[b] = 1;
-        };
-        // stage i's MMAs are queued before stage i+1 is loaded: the load waits for stage i-1's MMAs (its buffer),
-        // while the tensor pipe already holds stage i's
-        load(0);
-        for (int i = 0; i < nkc && ok; ++i) {
-          const int b = i & 1;
-          if (!t5_wait(&full[b], fph[b])) {
-            ok = 0;
-            break;
-          }
-          fph[b] ^= 1u;
-          fpend[b] = 0;
-          t5_fence_after();
-          const int sk8 = min(T5_KC / 8, nk8 - i * (T5_KC / 8));
-          const uint32_t abase = t5_smem(sm + b * T5_STAGE), bbase = abase + OZ_SA * T5_ASL;
-          // descriptors of slice 0 at K-step 0; the others add their byte offset / 16 to the start-address field
-          // (shared addresses stay below 2^18, so the 14-bit field never carries)
-          const uint64_t ad0 = t5_desc(abase, 16 * 128, 128);
-          const uint64_t bd0 = t5_desc(bbase, (T5_NC / 8) * 128, 128);
-          for (int j = 0; j < sk8 / 2; ++j)
-#pragma unroll
-            for (int sa = 0; sa < OZ_SA; ++sa)
-#pragma unroll
-              for (int tb = 0; tb < QS; ++tb) {
-                if (sa + tb >= OZ_L) continue;
-                const int L = sa + tb;
-                const uint64_t ad = ad0 + (uint64_t)((sa * T5_ASL + j * 2 * (16 * 128)) >> 4);
-                const uint64_t bd = bd0 + (uint64_t)((tb * T5_BSL + j * 2 * ((T5_NC / 8) * 128)) >> 4);
-                t5_mma(tbase + (uint32_t)(L * T5_NC), ad, bd, idesc, (initmask >> L) & 1u);
-                initmask |= 1u << L;
-              }
-          t5_commit(&empty[b]);
-          epend[b] = 1;
-          if (i + 1 < nkc) load(i + 1);
-        }
-        // every MMA of the chunk done (the commits track all earlier MMAs of this thread); after a timeout, also
-        // every bulk copy still in flight (bounded waits)
-        for (int b = 0; b < 2; ++b) {
-          if (epend[b]) {
-            if (!t5_wait(&empty[b], eph[b])) ok = 0;
-            eph[b] ^= 1u;
-            epend[b] = 0;
-          }
-          if (fpend[b]) {
-            if (!t5_wait(&full[b], fph[b])) ok = 0;
-            fph[b] ^= 1u;
-            fpend[b] = 0;
-          }
-        }
-        // after the last chunk's MMAs the stage region is free: the next tile's V loads during this epilogue
-        if (ok && c0 + T5_NC >= N && tile + (int)gridDim.x < ntiles) {
-          issue_v(tile + gridDim.x);
-          vpend = 1;
-        }
-      }
-      ok = __syncthreads_and(ok);
+  int ok = 1;
+  if (warp < T5W_TENSOR / 32) {
+    // ---- tensor warps ----
+    uint32_t fph[2] = {0u, 0u}, eph[2] = {0u, 0u};  // thread 0: barrier phases and outstanding completions
+    int epend[2] = {0, 0}, fpend[2] = {0, 0};
+    uint32_t tph = 0u;
+    const uint32_t idesc_m = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(T5_M >> 4) << 24);
+    int j = 0;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++j) {
+      const int b = j & 1;
+      const int r0 = tile * T5_M;
+      const int rows = min(T5_M, n - r0);
+      if (!t5_wait(&ready[b], (uint32_t)((j >> 1) & 1))) ok = 0;
+      ok = t5_bar_and(1, T5W_TENSOR, ok);
       if (!ok) break;
-      t5_fence_after();
-      // 4. epilogue: warp w reads lanes 32 (w mod 4) .. +31 (tile rows), columns 16 (w / 4) .. +15 of the chunk
-      const int qd = warp & 3, col = 16 * (warp >> 2);
-      if (col < nch) {  // warp-uniform
-        const int m = 32 * qd + lane;
-        const int er = erow[m];
-        if constexpr (std::is_same<S, T5Pair>::value) {
-          float sh[16], sl[16];
-#pragma unroll
-          for (int i2 = 0; i2 < 16; ++i2) sh[i2] = sl[i2] = 0.0f;
-#pragma unroll 1
-          for (int L = OZ_L - 1; L >= 0; --L) {
-            float v[16];
-            t5_ld16(tbase + ((uint32_t)(32 * qd) << 16) + (uint32_t)(L * T5_NC + col), v);
-            // 2^(-7(L+2)) as a float (exponent field 127 - 7(L+2) >= 64): the level sums are integers below 2^24,
-            // so the product is exact and equals ldexpf(v, -7(L+2))
-            const float scale = __uint_as_float((uint32_t)(127 - 7 * (L + 2)) << 23);
-#pragma unroll
-            for (int i2 = 0; i2 < 16; ++i2) oz_add(sh[i2], sl[i2], v[i2] * scale);
-          }
-          if (m < rows) {
-#pragma unroll
-            for (int i2 = 0; i2 < 16; ++i2) {
-              const int c = c0 + col + i2;
-              if (c >= N) break;
-              float2 out = make_float2(0.0f, 0.0f);  // an all-zero row stays zero
-              if (er) {
-                const float hi = sh[i2] + sl[i2];
-                const float lo = sl[i2] - (hi - sh[i2]);
-                const int sc = S::escale(er) + fcol[c];
-                out = make_float2(ldexpf(hi, sc), ldexpf(lo, sc));
+      const __nv_bfloat16 *As = As0 + (size_t)b * abuf;
+      const int *er_b = erow + b * T5_M;
+      for (int c0 = 0; c0 < N && ok; c0 += T5_NC) {
+        const int nch = min(T5_NC, (N - c0 + 15) / 16 * 16);
+        if (tid == 0) {
+          const uint32_t idesc = idesc_m | ((uint32_t)(nch >> 3) << 17);
+          uint32_t initmask = 0;  // levels already written in this chunk
+          auto load = [&](int i) {  // stage i into buffer i & 1, once the MMAs that read the buffer are done
+            const int sb = i & 1;
+            if (epend[sb]) {
+              if (!t5_wait(&empty[sb], eph[sb])) {
+                ok = 0;  // the buffer may still be read: issue nothing
+                return;
               }
-              V[(size_t)(r0 + m) + (size_t)(s0 + c) * ldv] = out;
+              eph[sb] ^= 1u;
+              epend[sb] = 0;
             }
-          }
-        } else {
-          // the level sums as exact integers: X = sum_L P_L 2^(7(7-L)) = H 2^42 + R with H = 128 P_0 + P_1
-          // (|H| < 2^32) and R = sum_{L>=2} P_L 2^(7(7-L)) (|R| < 2^60); v q = 2^(e_r + f_c - 63) X, rounded once
-          long long Hs[16], Rs[16];
-#pragma unroll
-          for (int i2 = 0; i2 < 16; ++i2) Hs[i2] = Rs[i2] = 0;
-#pragma unroll 1
-          for (int L = OZ_L - 1; L >= 0; --L) {
-            float v[16];
-            t5_ld16(tbase + ((uint32_t)(32 * qd) << 16) + (uint32_t)(L * T5_NC + col), v);
-            const long long w = L >= 2 ? (1ll << (7 * (7 - L))) : (L == 1 ? 1ll : 128ll);
-#pragma unroll
-            for (int i2 = 0; i2 < 16; ++i2) {
-              const long long pl = (long long)__float2int_rn(v[i2]);  // an integer below 2^24 in magnitude
-              if (L >= 2) Rs[i2] += pl * w;
-              else Hs[i2] += pl * w;
+            const int kc8 = i * (T5_KC / 8);
+            const int sk8 = min(T5_KC / 8, nk8 - kc8);
+            unsigned char *st = sm + sb * T5_STAGE;
+            const uint32_t abytes = sk8 * 16 * 128, bbytes = (nch / 8) * 128;
+            t5_expect_tx(&full[sb], OZ_SA * abytes + QS * sk8 * bbytes);
+            for (int sl = 0; sl < OZ_SA; ++sl)
+              t5_bulk(st + sl * T5_ASL, As + ((size_t)sl * nk8 + kc8) * 16 * 64, abytes, &full[sb]);
+            for (int t = 0; t < QS; ++t)
+              for (int k8 = 0; k8 < sk8; ++k8)
+                t5_bulk(st + OZ_SA * T5_ASL + t * T5_BSL + k8 * (T5_NC / 8) * 128,
+                        Bsl + (((size_t)t * nk8 + kc8 + k8) * (np / 8) + c0 / 8) * 64, bbytes, &full[sb]);
+            fpend[sb] = 1;
+          };
+          load(0);
+          for (int i = 0; i < nkc && ok; ++i) {
+            const int sb = i & 1;
+            if (!t5_wait(&full[sb], fph[sb])) {
+              ok = 0;
+              break;
             }
+            fph[sb] ^= 1u;
+            fpend[sb] = 0;
+            t5_fence_after();
+            const int sk8 = min(T5_KC / 8, nk8 - i * (T5_KC / 8));
+            const uint32_t abase = t5_smem(sm + sb * T5_STAGE), bbase = abase + OZ_SA * T5_ASL;
+            const uint64_t ad0 = t5_desc(abase, 16 * 128, 128);
+            const uint64_t bd0 = t5_desc(bbase, (T5_NC / 8) * 128, 128);
+            for (int jj = 0; jj < sk8 / 2; ++jj)
+#pragma unroll
+              for (int sa = 0; sa < OZ_SA; ++sa)
+#pragma unroll
+                for (int tb = 0; tb < QS; ++tb) {
+                  if (sa + tb >= OZ_L) continue;
+                  const int L = sa + tb;
+                  const uint64_t ad = ad0 + (uint64_t)((sa * T5_ASL + jj * 2 * (16 * 128)) >> 4);
+                  const uint64_t bd = bd0 + (uint64_t)((tb * T5_BSL + jj * 2 * ((T5_NC / 8) * 128)) >> 4);
+                  t5_mma(tbase + (uint32_t)(L * T5_NC), ad, bd, idesc, (initmask >> L) & 1u);
+                  initmask |= 1u << L;
+                }
+            t5_commit(&empty[sb]);
+            epend[sb] = 1;
+            if (i + 1 < nkc) load(i + 1);
           }
-          int ex[16];
-#pragma unroll
-          for (int i2 = 0; i2 < 16; ++i2) ex[i2] = 0;
-          if (m < rows) {
-#pragma unroll
-            for (int i2 = 0; i2 < 16; ++i2) {
-              const int c = c0 + col + i2;
-              if (c >= N) break;
-              double out = 0.0;  // an all-zero row stays zero
-              if (er) {
-                const int sc = S::escale(er) + fcol[c] - 63;
-                out = fma((double)Hs[i2], t5_pow2(sc + 42), (double)Rs[i2] * t5_pow2(sc));
-              }
-              V[(size_t)(r0 + m) + (size_t)(s0 + c) * ldv] = out;
-              ex[i2] = (int)(((unsigned long long)__double_as_longlong(out) >> 52) & 0x7FF);
+          // the chunk's level sums are complete when every MMA issued so far is
+          if (ok) t5_commit(tfull);
+          for (int sb = 0; sb < 2; ++sb) {
+            if (epend[sb]) {
+              if (!t5_wait(&empty[sb], eph[sb])) ok = 0;
+              eph[sb] ^= 1u;
+              epend[sb] = 0;
             }
-          }
-          if (vexp) {
-#pragma unroll
-            for (int i2 = 0; i2 < 16; ++i2) {
-              int x = ex[i2];
-#pragma unroll
-              for (int off = 16; off > 0; off >>= 1) x = max(x, __shfl_xor_sync(0xffffffffu, x, off));
-              if (lane == 0 && x) atomicMax(&cmax[col + i2], x);
+            if (fpend[sb]) {
+              if (!t5_wait(&full[sb], fph[sb])) ok = 0;
+              fph[sb] ^= 1u;
+              fpend[sb] = 0;
             }
           }
         }
-      }
-      t5_fence_before();
-      __syncthreads();  // TMEM is read out before the next chunk's MMAs overwrite it
-      if (vexp && tid < nch) {
-        // the exponent of each output column over this tile: |v| < 2^(E - 1022), -128 for an all-zero tile
-        const int c = c0 + tid;
-        if (c < N) {
-          const int E = cmax[tid];
-          const int e = E == 0 ? -128 : (E - 1022 < -127 ? -127 : (E - 1022 > 127 ? 127 : E - 1022));
-          vexp[(size_t)(s0 + c) * ldt + tile] = (signed char)e;
+        __syncwarp();
+        // thread 0's pipeline state joins the vote: after a failure it committed nothing to tmem_full
+        ok = t5_bar_and(1, T5W_TENSOR, ok);
+        if (!ok) break;
+        if (!t5_wait(tfull, tph)) ok = 0;
+        tph ^= 1u;
+        ok = t5_bar_and(1, T5W_TENSOR, ok);
+        if (!ok) break;
+        t5_fence_after();
+        // epilogue: warp w reads lanes 32 w .. +31 (tile rows), every 16-column group of the chunk
+        const int m = 32 * warp + lane;
+        const int er = er_b[m];
+#pragma unroll 1
+        for (int col = 0; col < nch; col += 16) {
+          if constexpr (std::is_same<S, T5Pair>::value) {
+            float sh[16], sl[16];
+#pragma unroll
+            for (int i2 = 0; i2 < 16; ++i2) sh[i2] = sl[i2] = 0.0f;
+#pragma unroll 1
+            for (int L = OZ_L - 1; L >= 0; --L) {
+              float v[16];
+              t5_ld16(tbase + ((uint32_t)(32 * warp) << 16) + (uint32_t)(L * T5_NC + col), v);
+              const float scale = __uint_as_float((uint32_t)(127 - 7 * (L + 2)) << 23);
+#pragma unroll
+              for (int i2 = 0; i2 < 16; ++i2) oz_add(sh[i2], sl[i2], v[i2] * scale);
+            }
+            if (m < rows) {
+#pragma unroll
+              for (int i2 = 0; i2 < 16; ++i2) {
+                const int c = c0 + col + i2;
+                if (c >= N) break;
+                float2 out = make_float2(0.0f, 0.0f);  // an all-zero row stays zero
+                if (er) {
+                  const float hi = sh[i2] + sl[i2];
+                  const float lo = sl[i2] - (hi - sh[i2]);
+                  const int sc = S::escale(er) + fcol[c];
+                  out = make_float2(ldexpf(hi, sc), ldexpf(lo, sc));
+                }
+                V[(size_t)(r0 + m) + (size_t)(s0 + c) * ldv] = out;
+              }
+            }
+          } else {
+            long long Hs[16], Rs[16];
+#pragma unroll
+            for (int i2 = 0; i2 < 16; ++i2) Hs[i2] = Rs[i2] = 0;
+#pragma unroll 1
+            for (int L = OZ_L - 1; L >= 0; --L) {
+              float v[16];
+              t5_ld16(tbase + ((uint32_t)(32 * warp) << 16) + (uint32_t)(L * T5_NC + col), v);
+              const long long w = L >= 2 ? (1ll << (7 * (7 - L))) : (L == 1 ? 1ll : 128ll);
+#pragma unroll
+              for (int i2 = 0; i2 < 16; ++i2) {
+                const long long pl = (long long)oz_f2i_exact(v[i2]);  // an integer below 2^24 in magnitude
+                if (L >= 2) Rs[i2] += pl * w;
+                else Hs[i2] += pl * w;
+              }
+            }
+            int ex[16];
+#pragma unroll
+            for (int i2 = 0; i2 < 16; ++i2) ex[i2] = 0;
+            if (m < rows) {
+#pragma unroll
+              for (int i2 = 0; i2 < 16; ++i2) {
+                const int c = c0 + col + i2;
+                if (c >= N) break;
+                double out = 0.0;  // an all-zero row stays zero
+                if (er) {
+                  // X 2^sc rounded once, on the integer units; FP64 only outside the normal range
+                  const int sc = S::escale(er) + fcol[c] - 63;
+                  if (!oz_round_x(Hs[i2], Rs[i2], sc, &out))
+                    out = fma((double)Hs[i2], t5_pow2(sc + 42), (double)Rs[i2] * t5_pow2(sc));
+                }
+                V[(size_t)(r0 + m) + (size_t)(s0 + c) * ldv] = out;
+                ex[i2] = (int)(((unsigned long long)__double_as_longlong(out) >> 52) & 0x7FF);
+              }
+            }
+            if (vexp) {
+#pragma unroll
+              for (int i2 = 0; i2 < 16; ++i2) {
+                int x = ex[i2];
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) x = max(x, __shfl_xor_sync(0xffffffffu, x, off));
+                if (lane == 0 && x) atomicMax(&cmax[col + i2], x);
+              }
+            }
+          }
         }
-        cmax[tid] = 0;
+        t5_fence_before();
+        t5_bar(1, T5W_TENSOR);  // TMEM is read out before the next chunk's MMAs overwrite it
+        if (vexp) {
+          if (tid < nch) {
+            // the exponent of each output column over this tile: |v| < 2^(E - 1022), -128 for an all-zero tile
+            const int c = c0 + tid;
+            if (c < N) {
+              const int E = cmax[tid];
+              const int e = E == 0 ? -128 : (E - 1022 < -127 ? -127 : (E - 1022 > 127 ? 127 : E - 1022));
+              vexp[(size_t)(s0 + c) * ldt + tile] = (signed char)e;
+            }
+            cmax[tid] = 0;
+          }
+          t5_bar(1, T5W_TENSOR);
+        }
       }
+      if (!ok) break;
+      // the tile is written back: its buffer may take the tile after next
+      __syncwarp();
+      if (lane == 0) t5_arrive(&done[b]);
+    }
+  } else {
+    // ---- slicing warps ----
+    const int st = tid - T5W_TENSOR;
+    int j = 0;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++j) {
+      const int b = j & 1;
+      const int r0 = tile * T5_M;
+      const int rows = min(T5_M, n - r0);
+      if (j >= 2 && !t5_wait(&done[b], (uint32_t)(((j - 2) >> 1) & 1))) ok = 0;
+      ok = t5_bar_and(2, T5W_SLICERS, ok);
+      if (!ok) break;
+      int *er_b = erow + b * T5_M;
+      // 1. row exponents: e_r = 1 + floor(log2 max_k |v|) from the exponent fields (T5W_H threads per row; eight
+      //    loads in flight per thread: this pass is the tile's first touch of V)
+      {
+        const int m = st & (T5_M - 1), h = st >> 7;
+        int E = 0;
+        if (m < rows)
+          for (int k0 = h; k0 < K; k0 += 8 * T5W_H) {
+            T vv[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+              const int k = k0 + u * T5W_H;
+              vv[u] = k < K ? V[(size_t)(r0 + m) + (size_t)(a0 + k) * ldv] : T{};
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) E = max(E, S::expo(vv[u]));
+          }
+        etmp[h * T5_M + m] = E;
+        t5_bar(2, T5W_SLICERS);
+        if (h == 0) {
+#pragma unroll
+          for (int q = 1; q < T5W_H; ++q) E = max(E, etmp[q * T5_M + m]);
+          er_b[m] = E;
+        }
+        t5_bar(2, T5W_SLICERS);
+      }
+      // the CTA's next tile into L2 while this one is sliced (one 128-byte line per 16 rows and column)
+      {
+        const int rn = r0 + (int)gridDim.x * T5_M;
+        if (rn < n)
+          for (int q = st; q < K * 8; q += T5W_SLICERS) {
+            const int r = rn + 16 * (q & 7);
+            if (r < n) asm volatile("prefetch.global.L2 [%0];" ::"l"(V + (size_t)r + (size_t)(a0 + (q >> 3)) * ldv));
+          }
+      }
+      // 2. all slices of the tile into buffer b, one core-matrix row (8 consecutive k of one row) per item, two
+      //    items per pass (32 consecutive rows per warp: every load of a column is one coalesced 256-byte access)
+      __nv_bfloat16 *As = As0 + (size_t)b * abuf;
+      for (int it0 = st; it0 < T5_M * nk8; it0 += 2 * T5W_SLICERS) {
+        T v[2][8];
+#pragma unroll
+        for (int p2 = 0; p2 < 2; ++p2) {
+          const int it = it0 + p2 * T5W_SLICERS;
+          const int m = it & (T5_M - 1), k8 = it >> 7;
+#pragma unroll
+          for (int jj = 0; jj < 8; ++jj) {
+            const int k = 8 * k8 + jj;
+            v[p2][jj] = (it < T5_M * nk8 && m < rows && k < K) ? V[(size_t)(r0 + m) + (size_t)(a0 + k) * ldv] : T{};
+          }
+        }
+#pragma unroll
+        for (int p2 = 0; p2 < 2; ++p2) {
+          const int it = it0 + p2 * T5W_SLICERS;
+          if (it >= T5_M * nk8) break;
+          const int m = it & (T5_M - 1), k8 = it >> 7;
+          const int er = er_b[m];
+          uint32_t mh[8], ml[8], ng[8];
+#pragma unroll
+          for (int jj = 0; jj < 8; ++jj) {
+            long long x = 0;
+            if (er) x = S::fix56(v[p2][jj], S::escale(er));
+            ng[jj] = x < 0 ? 1u : 0u;
+            const unsigned long long a = x < 0 ? (unsigned long long)(-x) : (unsigned long long)x;
+            mh[jj] = (uint32_t)(a >> 32);
+            ml[jj] = (uint32_t)a;
+          }
+#pragma unroll
+          for (int sl = 0; sl < OZ_SA; ++sl) {
+            uint32_t u[8];
+#pragma unroll
+            for (int jj = 0; jj < 8; ++jj) u[jj] = t5_field(mh[jj], ml[jj], sl);
+            uint4 w;
+            w.x = t5_slice_pair(u[0], u[1], ng[0], ng[1]);
+            w.y = t5_slice_pair(u[2], u[3], ng[2], ng[3]);
+            w.z = t5_slice_pair(u[4], u[5], ng[4], ng[5]);
+            w.w = t5_slice_pair(u[6], u[7], ng[6], ng[7]);
+            *reinterpret_cast<uint4 *>(As + (((size_t)sl * nk8 + k8) * 16 + (m >> 3)) * 64 + (m & 7) * 8) = w;
+          }
+        }
+      }
+      // the TMA engine reads the buffer next (async proxy): order this thread's writes before the hand-off
+      asm volatile("fence.proxy.async;" ::: "memory");
+      t5_arrive(&ready[b]);
     }
   }
-  // a V tile load still in flight after a timeout (bounded wait)
-  if (tid == 0 && vpend && !t5_wait(vbar, vph)) ok = 0;
   t5_fence_before();
-  __syncthreads();
+  const int bad = __syncthreads_or(!ok);
   t5_fence_after();
-  if (!ok && tid == 0) atomicExch(err, 1);
+  if (bad && tid == 0) atomicExch(err, 1);
   if (warp == 0)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(T5_TMEM_COLS) : "memory");
 }
@@ -617,7 +675,7 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
 static size_t t5_qbytes(int ld) { return (restart_tc_scratch_bytes(ld) + 255) / 256 * 256; }
 static size_t t5_abytes(int ld) {
   const int ldp = (ld + 15) / 16 * 16;
-  return (size_t)num_sms() * OZ_SA * ldp * 128 * sizeof(__nv_bfloat16);
+  return (size_t)num_sms() * 2 * OZ_SA * ldp * 128 * sizeof(__nv_bfloat16);  // two buffers per CTA
 }
 size_t restart_t5_scratch_bytes(int ld) { return t5_qbytes(ld) + t5_abytes(ld) + 256; }
 int *restart_t5_errflag(void *scratch, int ld) {
@@ -641,14 +699,15 @@ static cudaError_t restart_t5_go(typename S::T *V, long long ldv, int n, int a0,
   int *fcol = reinterpret_cast<int *>(B + (size_t)OZ_QMAX * np * kp);
   __nv_bfloat16 *Ascr = reinterpret_cast<__nv_bfloat16 *>(static_cast<unsigned char *>(scratch) + t5_qbytes(ld));
   int *err = restart_t5_errflag(scratch, ld);
-  cudaError_t e = cudaFuncSetAttribute(k_restart_t5<S, QS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T5_SMEM);
+  cudaError_t e = cudaFuncSetAttribute(k_restart_t5w<S, QS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)T5W_SMEM);
   if (e != cudaSuccess) return e;
   k_oz_qslice<<<np, 128, 0, s>>>(Q, ldq, a0, s0, K, N, kp, np, B, fcol, 1, QS);
   const int ntiles = (n + T5_M - 1) / T5_M;
   int blocks = num_sms();
   if (blocks > ntiles) blocks = ntiles;
-  k_restart_t5<S, QS><<<blocks, T5_THREADS, T5_SMEM, s>>>(V, ldv, n, a0, K, s0, N, kp, np, B, fcol, Ascr, err, vexp,
-                                                          ldt);
+  k_restart_t5w<S, QS><<<blocks, T5_THREADS, T5W_SMEM, s>>>(V, ldv, n, a0, K, s0, N, kp, np, B, fcol, Ascr, err,
+                                                            vexp, ldt);
   return cudaGetLastError();
 }
 

@@ -82,7 +82,8 @@ def test_refined_nearly_degenerate_pairs(lib, lock):
     assert verify.orthogonality(res["X"][:, :res["nconv"]]) <= 1e-12
 
 
-@pytest.mark.parametrize("arith,ds", [("f64", "qr"), ("pair", "qr"), ("f64", "refined")])
+@pytest.mark.parametrize("arith,ds", [("f64", "qr"), ("pair", "qr"), ("f64", "refined"), ("f64", "auto"),
+                                     ("pair", "auto")])
 def test_lap3d64_nev50_ncv128_host_parity(lib, arith, ds):
     """The 128^3 workload's shape at 64^3 (nev 50, ncv 128, tol 1e-10, largest algebraic): a degenerate spectrum
     with pairs just outside the cluster threshold of the mixed-precision projected solver, where its refinement
@@ -100,3 +101,20 @@ def test_lap3d64_nev50_ncv128_host_parity(lib, arith, ds):
     assert p["ok"], p
     _, r_l = verify.residuals(csr, res["eigr"][:k], res["X"][:, :k])
     assert r_l.max() <= 2e-10, r_l.max()  # ||Ax - lam x|| / |lam|: the convergence test's own measure, at tol
+
+
+def test_auto_projected_solver_is_the_default_and_matches_qr(lib):
+    """The default projected solver (auto) on the 100^2 Laplacian of the small workload, beside the FP64 QR solver:
+    both pass the parity block against the closed form (the spectrum has multiplicity 2, so which copies converge
+    first differs with rounding; the distinct wanted values are found by both), host residuals at tol."""
+    csr = matgen.laplacian_2d(100)
+    v0 = matgen.start_vector(10000, 1)
+    exact = matgen.laplacian_eigenvalues([100, 100])
+    for ds in (None, "qr"):
+        r = sg.solve(csr, hermitian=True, which="LM", nev=10, ncv=32, tol=1e-10, v0=v0, arith="f64", ds=ds)
+        assert r["reason"] == 1 and r["nconv"] >= 10
+        k = r["nconv"]
+        p = verify.parity_block(csr, r["eigr"][:k], r["X"][:, :k], exact, "LM", 10, 1e-10)
+        assert p["ok"], (ds, p)
+        if ds == "qr":
+            assert r["stats"]["ds_fallbacks"] == 0

@@ -610,3 +610,44 @@ def test_wide_basis_nonsymmetric(lib):
     with pytest.raises(sg.SlepcError) as e:
         run(matgen.convection_diffusion_2d(30, pe), hermitian=False, which="LR", nev=10, ncv=700, tol=1e-8)
     assert e.value.code == 56
+
+
+@pytest.mark.parametrize("arith,herm", [("f64", True), ("pair", True), ("f64", False)])
+def test_graph_segments_match_direct_launches(lib, arith, herm):
+    """Factorisation segments replayed from captured CUDA graphs give the same bits as direct launches: three
+    solves with graphs on (the second and third replay the segments seen before) against one with them off."""
+    if herm:
+        csr, kw = matgen.laplacian_2d(100), dict(hermitian=True, which="LM", nev=10, ncv=32)
+    else:
+        csr, kw = matgen.convection_diffusion_2d(60, 10.0), dict(hermitian=False, which="LR", nev=8, ncv=32)
+    n = len(csr[0]) - 1
+    A = sg.Mat(*csr)
+
+    def make(mode):
+        e = sg.EPS().create()
+        e.setOperators(A)
+        e.setProblemType(sg.EPS.ProblemType.HEP if kw["hermitian"] else sg.EPS.ProblemType.NHEP)
+        e.setDimensions(kw["nev"], kw["ncv"])
+        e.setTolerances(1e-10)
+        e.setWhichEigenpairs(kw["which"])
+        e.setArithmetic(arith)
+        e.setGraphCapture(mode)
+        e.setInitialSpace(matgen.start_vector(n, 4))
+        return e
+
+    def vals(e):
+        k = e.getConverged()
+        return np.array([complex(e.getEigenvalue(i)) for i in range(k)]), e.getIterationNumber()
+
+    ref = make(0)
+    ref.solve()
+    want = vals(ref)
+    assert ref.getStats()["graph_segments"] == 0
+    e = make(1)
+    replays = []
+    for _ in range(3):
+        e.solve()
+        got = vals(e)
+        assert got[1] == want[1] and np.array_equal(got[0], want[0])
+        replays.append(e.getStats()["graph_segments"])
+    assert replays[2] > 0 and replays[2] >= replays[0]
