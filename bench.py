@@ -144,7 +144,9 @@ def full_size_steps(workload):
     """Krylov steps of the complete reference-algorithm solve (oracle/full_size_runs.py), 0 if not recorded."""
     p = os.path.join(ROOT, "oracle", "full_size_runs.json")
     if os.path.exists(p):
-        return int(json.load(open(p)).get(workload, {}).get("steps", 0))
+        rec = json.load(open(p)).get(workload, {})
+        here = rec.get("hosts", {}).get(os.uname().machine, {})  # the count of a solve on this kind of host
+        return int(here.get("steps", rec.get("steps", 0)))
     return 0
 
 

@@ -135,7 +135,7 @@ static PetscErrorCode engine_enqueue_cycle(BatchEngine &B, long long *launches) 
   KSG_CUDA(launch_batch_begin(B.inst.p, B.list.p, B.hdr.p, B.grid_inst, s));
   for (int q = 0; q < (B.has_f32 ? 2 : 1); ++q) {
     const int st = q ? STORE_F32 : STORE_PAIR;
-    KSG_CUDA(launch_batch_dot(B.inst.p, B.map_dot.p, B.hdr.p, -1, B.grid_dot, s, st));
+    KSG_CUDA(launch_batch_dot(B.inst.p, B.map_dot.p, B.hdr.p, -1, B.grid_dot, s, st, B.max_ld));
     KSG_CUDA(launch_batch_update(B.inst.p, B.map_upd.p, B.hdr.p, -1, B.grid_upd, B.max_ld, s, st));
     nl += 2;
   }
@@ -147,7 +147,7 @@ static PetscErrorCode engine_enqueue_cycle(BatchEngine &B, long long *launches) 
   for (int slot = 0; slot < B.slots; ++slot) {
     for (int q = 0; q < nsto; ++q) {
       KSG_CUDA(launch_batch_spmv(B.inst.p, B.map_spmv.p, B.hdr.p, slot, B.grid_spmv, s, sto[q]));
-      KSG_CUDA(launch_batch_dot(B.inst.p, B.map_dot.p, B.hdr.p, slot, B.grid_dot, s, sto[q]));
+      KSG_CUDA(launch_batch_dot(B.inst.p, B.map_dot.p, B.hdr.p, slot, B.grid_dot, s, sto[q], B.max_ld));
       KSG_CUDA(launch_batch_update(B.inst.p, B.map_upd.p, B.hdr.p, slot, B.grid_upd, B.max_ld, s, sto[q]));
       nl += 3;
     }

@@ -60,8 +60,9 @@ cudaError_t launch_batch_start(BatchInst *I, const int *list, const BatchHdr *h,
 // the Krylov-step and restart launchers serve the instances of one storage format (STORE_PAIR or STORE_F32)
 cudaError_t launch_batch_spmv(const BatchInst *I, const BatchVB *map, const BatchHdr *h, int slot, int grid,
                               cudaStream_t s, int storage);
+// the engine's widest basis max_ld selects the column tiling (up to 80 or up to 144 columns)
 cudaError_t launch_batch_dot(const BatchInst *I, const BatchVB *map, const BatchHdr *h, int slot, int grid,
-                             cudaStream_t s, int storage);
+                             cudaStream_t s, int storage, int max_ld);
 cudaError_t launch_batch_update(const BatchInst *I, const BatchVB *map, const BatchHdr *h, int slot, int grid,
                                 int max_ld, cudaStream_t s, int storage);
 cudaError_t launch_batch_restart(const BatchInst *I, const BatchVB *map, const BatchHdr *h, int grid, int max_ld,

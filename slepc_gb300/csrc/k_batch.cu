@@ -156,12 +156,13 @@ __global__ void __launch_bounds__(256) k_batch_spmv(const BatchInst *I, const Ba
   }
 }
 
-// Gram-Schmidt half A; CPW = 5 covers the batch limit of 80 columns (the per-column arithmetic does not depend on
-// CPW, so this matches the single-problem kernel's rounding)
+// Gram-Schmidt half A; CPW = 5 covers engines of up to 80 columns, CPW = 9 up to 144 (the per-column arithmetic
+// does not depend on CPW, so both match the single-problem kernel's rounding)
 constexpr int BATCH_CPW = 5;
-constexpr int BATCH_MAXJ = A_WARPS * BATCH_CPW;
+constexpr int BATCH_CPW_WIDE = 9;
+constexpr int BATCH_MAXJ = A_WARPS * BATCH_CPW_WIDE;
 
-template <int STO, class S>
+template <int STO, class S, int CPW>
 __global__ void __launch_bounds__(A_THREADS, 1) k_batch_dot(const BatchInst *I, const BatchVB *map,
                                                             const BatchHdr *h, int slot) {
   const int nmap = h->n_dot;
@@ -172,8 +173,8 @@ __global__ void __launch_bounds__(A_THREADS, 1) k_batch_dot(const BatchInst *I, 
     if (p.storage != STO || !batch_slot(p, slot, mode, nx, j)) continue;
     __syncthreads();  // shared staging of the previous virtual block is free
     const StepArgs a = batch_step_args<STO>(p, j, nx);
-    if (nx == 2) gs_dot_body<2, BATCH_CPW, PairAr, S>(a, mode, m.b, m.nb);
-    else gs_dot_body<1, BATCH_CPW, PairAr, S>(a, mode, m.b, m.nb);
+    if (nx == 2) gs_dot_body<2, CPW, PairAr, S>(a, mode, m.b, m.nb);
+    else gs_dot_body<1, CPW, PairAr, S>(a, mode, m.b, m.nb);
   }
 }
 
@@ -294,9 +295,16 @@ cudaError_t launch_batch_spmv(const BatchInst *I, const BatchVB *map, const Batc
 }
 
 cudaError_t launch_batch_dot(const BatchInst *I, const BatchVB *map, const BatchHdr *h, int slot, int grid,
-                             cudaStream_t s, int storage) {
-  if (storage == STORE_F32) k_batch_dot<STORE_F32, StF32><<<grid, A_THREADS, 0, s>>>(I, map, h, slot);
-  else k_batch_dot<STORE_PAIR, StPair><<<grid, A_THREADS, 0, s>>>(I, map, h, slot);
+                             cudaStream_t s, int storage, int max_ld) {
+  if (max_ld > BATCH_MAXJ) return cudaErrorInvalidValue;
+  if (max_ld <= A_WARPS * BATCH_CPW) {
+    if (storage == STORE_F32) k_batch_dot<STORE_F32, StF32, BATCH_CPW><<<grid, A_THREADS, 0, s>>>(I, map, h, slot);
+    else k_batch_dot<STORE_PAIR, StPair, BATCH_CPW><<<grid, A_THREADS, 0, s>>>(I, map, h, slot);
+  } else {
+    if (storage == STORE_F32)
+      k_batch_dot<STORE_F32, StF32, BATCH_CPW_WIDE><<<grid, A_THREADS, 0, s>>>(I, map, h, slot);
+    else k_batch_dot<STORE_PAIR, StPair, BATCH_CPW_WIDE><<<grid, A_THREADS, 0, s>>>(I, map, h, slot);
+  }
   return cudaGetLastError();
 }
 

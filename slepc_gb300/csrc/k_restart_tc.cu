@@ -21,7 +21,6 @@
 #include "common.cuh"
 #include "kernels.h"
 #include "ks_types.h"
-#include "oz_round.h"
 #include "tc_common.cuh"
 
 namespace ksg {
@@ -246,7 +245,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_restart_tc(float2 *__restrict
 // in bytes on the stage's "full" mbarrier).  One thread runs the pipeline: the copies of stage i+1 are in flight
 // while the tensor cores run the 35 MMAs per K-step of stage i; tcgen05.commit arrives on the stage's "empty"
 // mbarrier when the MMAs that read it are done.  The epilogue reads TMEM with tcgen05.ld and recombines the levels
-// (as pairs, or for FP64 storage as exact integers rounded once, on the integer units: oz_round.h).
+// (as pairs, or for FP64 storage as exact integers scaled into one FP64 fused multiply-add).
 // ---------------------------------------------------------------------------------------------------------------
 constexpr int T5_M = 128;                                  // rows per tile (MMA M)
 constexpr int T5_NC = 64;                                  // output columns per chunk (MMA N <= 64)
@@ -287,22 +286,22 @@ struct T5F64 {
 
 // ---------------------------------------------------------------------------------------------------------------
 // The kernel is warp-specialised, so that the phases of consecutive tiles overlap:
-//   warps 0-3, the tensor warps: thread 0 runs a chunk's operand-stage pipeline and MMAs (as above) and commits to
-//     tmem_full; the four warps then read the level sums out of TMEM (warp w: lanes 32 w .. +31, every 16-column
-//     group of the chunk) and write the outputs.
-//   warps 4-15, the slicing warps (384 threads): the row exponents and slices of the CTA's next tile, read from V
+//   warps 0-7, the tensor warps: thread 0 runs a chunk's operand-stage pipeline and MMAs (as above) and commits to
+//     tmem_full; the eight warps then read the level sums out of TMEM (warp w: lanes 32 (w mod 4) .. +31, every
+//     other 16-column group from 16 (w / 4)) and write the outputs.
+//   warps 8-15, the slicing warps (256 threads): the row exponents and slices of the CTA's next tile, read from V
 //     in global memory and written to the CTA's scratch buffer (tile j in buffer j mod 2), while the tensor warps
 //     run the tile before it.
-// Hand-offs by mbarriers: ready[b] completes when the 384 slicing threads have filled buffer b (slices and row
-// exponents); done[b] when the four tensor warps have written back the tile of buffer b, so that the tile after
+// Hand-offs by mbarriers: ready[b] completes when the 256 slicing threads have filled buffer b (slices and row
+// exponents); done[b] when the eight tensor warps have written back the tile of buffer b, so that the tile after
 // next may replace it.  Named barriers (1: tensor warps, 2: slicing warps) order each group's own phases.  The
 // slicing warps read rows of later tiles than the ones the tensor warps write, and a tile's rows are all read (its
 // slices complete) before its own outputs are written, so the in-place update stays safe.  Every wait is bounded;
 // a timeout in either group ends both (the other group's next wait runs out), the MMA thread then waits (bounded)
 // for its copies and MMAs in flight, and the kernel frees its TMEM and sets *err.
 // ---------------------------------------------------------------------------------------------------------------
-constexpr int T5W_TENSOR = 128;                       // threads of the tensor warps
-constexpr int T5W_SLICERS = T5_THREADS - T5W_TENSOR;  // 384
+constexpr int T5W_TENSOR = 256;                       // threads of the tensor warps
+constexpr int T5W_SLICERS = T5_THREADS - T5W_TENSOR;  // 256
 constexpr int T5W_H = T5W_SLICERS / T5_M;             // slicing threads per row in the exponent pass
 constexpr size_t T5W_SMEM = 2 * (size_t)T5_STAGE + (2 + T5W_H) * T5_M * sizeof(int) +
                             9 * sizeof(unsigned long long) + 16 + T5_NC * sizeof(int);
@@ -324,6 +323,25 @@ KS_DEVICE void t5_arrive(unsigned long long *bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(t5_smem(bar)) : "memory");
 }
 
+// bounded wait that suspends the warp (up to 500 ns per try) instead of polling, so that waiting warps leave the
+// issue slots of their sub-partition to the working ones; a timeout, or another thread's, sets *abort and ends it.
+// With abort null the wait runs to its own bound (the MMA thread's waits for copies and MMAs in flight).
+KS_DEVICE bool t5w_wait(unsigned long long *bar, uint32_t parity, volatile int *abort) {
+  const uint32_t a = t5_smem(bar);
+  for (int it = 0; it < T5_WAIT_LIMIT / 16; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity), "r"(500u)
+        : "memory");
+    if (done) return true;
+    if ((it & 15) == 15 && abort && *abort) return false;
+  }
+  if (abort) *abort = 1;
+  return false;
+}
+
 template <class S, int QS>
 __global__ void __launch_bounds__(T5_THREADS, 1)
     k_restart_t5w(typename S::T *__restrict__ V, long long ldv, int n, int a0, int K, int s0, int N, int kp, int np,
@@ -339,9 +357,11 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
   unsigned long long *ready = tfull + 1;   // [2] a tile's slices in buffer b
   unsigned long long *done = ready + 2;    // [2] buffer b's tile written back
   uint32_t *tslot = reinterpret_cast<uint32_t *>(done + 2);
+  volatile int *abortf = reinterpret_cast<volatile int *>(tslot + 1);  // a wait of this CTA timed out
   int *cmax = reinterpret_cast<int *>(tslot + 4);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid < T5_NC) cmax[tid] = 0;
+  if (tid == 0) *abortf = 0;
   const int nk8 = kp / 8;
   const int nkc = (kp + T5_KC - 1) / T5_KC;
   const size_t abuf = (size_t)OZ_SA * nk8 * 16 * 64;       // bf16 elements of one slice buffer
@@ -380,7 +400,7 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
       const int b = j & 1;
       const int r0 = tile * T5_M;
       const int rows = min(T5_M, n - r0);
-      if (!t5_wait(&ready[b], (uint32_t)((j >> 1) & 1))) ok = 0;
+      if (!t5w_wait(&ready[b], (uint32_t)((j >> 1) & 1), abortf)) ok = 0;
       ok = t5_bar_and(1, T5W_TENSOR, ok);
       if (!ok) break;
       const __nv_bfloat16 *As = As0 + (size_t)b * abuf;
@@ -393,7 +413,7 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
           auto load = [&](int i) {  // stage i into buffer i & 1, once the MMAs that read the buffer are done
             const int sb = i & 1;
             if (epend[sb]) {
-              if (!t5_wait(&empty[sb], eph[sb])) {
+              if (!t5w_wait(&empty[sb], eph[sb], abortf)) {
                 ok = 0;  // the buffer may still be read: issue nothing
                 return;
               }
@@ -416,7 +436,7 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
           load(0);
           for (int i = 0; i < nkc && ok; ++i) {
             const int sb = i & 1;
-            if (!t5_wait(&full[sb], fph[sb])) {
+            if (!t5w_wait(&full[sb], fph[sb], abortf)) {
               ok = 0;
               break;
             }
@@ -446,13 +466,14 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
           // the chunk's level sums are complete when every MMA issued so far is
           if (ok) t5_commit(tfull);
           for (int sb = 0; sb < 2; ++sb) {
+            // every copy and MMA in flight completes before the stage buffers or TMEM are reused or freed
             if (epend[sb]) {
-              if (!t5_wait(&empty[sb], eph[sb])) ok = 0;
+              if (!t5w_wait(&empty[sb], eph[sb], nullptr)) ok = 0;
               eph[sb] ^= 1u;
               epend[sb] = 0;
             }
             if (fpend[sb]) {
-              if (!t5_wait(&full[sb], fph[sb])) ok = 0;
+              if (!t5w_wait(&full[sb], fph[sb], nullptr)) ok = 0;
               fph[sb] ^= 1u;
               fpend[sb] = 0;
             }
@@ -462,16 +483,19 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
         // thread 0's pipeline state joins the vote: after a failure it committed nothing to tmem_full
         ok = t5_bar_and(1, T5W_TENSOR, ok);
         if (!ok) break;
-        if (!t5_wait(tfull, tph)) ok = 0;
+        if (!t5w_wait(tfull, tph, abortf)) ok = 0;
         tph ^= 1u;
         ok = t5_bar_and(1, T5W_TENSOR, ok);
         if (!ok) break;
         t5_fence_after();
         // epilogue: warp w reads lanes 32 w .. +31 (tile rows), every 16-column group of the chunk
-        const int m = 32 * warp + lane;
+        // tensor warp w reads TMEM lanes 32 (w mod 4) .. +31 (tile rows) and every other 16-column group from
+        // 16 (w / 4): two warps per sub-partition share the TMEM latency of the level loads
+        const int qd = warp & 3;
+        const int m = 32 * qd + lane;
         const int er = er_b[m];
 #pragma unroll 1
-        for (int col = 0; col < nch; col += 16) {
+        for (int col = 16 * (warp >> 2); col < nch; col += 16 * (T5W_TENSOR / 128)) {
           if constexpr (std::is_same<S, T5Pair>::value) {
             float sh[16], sl[16];
 #pragma unroll
@@ -479,7 +503,7 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
 #pragma unroll 1
             for (int L = OZ_L - 1; L >= 0; --L) {
               float v[16];
-              t5_ld16(tbase + ((uint32_t)(32 * warp) << 16) + (uint32_t)(L * T5_NC + col), v);
+              t5_ld16(tbase + ((uint32_t)(32 * qd) << 16) + (uint32_t)(L * T5_NC + col), v);
               const float scale = __uint_as_float((uint32_t)(127 - 7 * (L + 2)) << 23);
 #pragma unroll
               for (int i2 = 0; i2 < 16; ++i2) oz_add(sh[i2], sl[i2], v[i2] * scale);
@@ -506,11 +530,11 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
 #pragma unroll 1
             for (int L = OZ_L - 1; L >= 0; --L) {
               float v[16];
-              t5_ld16(tbase + ((uint32_t)(32 * warp) << 16) + (uint32_t)(L * T5_NC + col), v);
+              t5_ld16(tbase + ((uint32_t)(32 * qd) << 16) + (uint32_t)(L * T5_NC + col), v);
               const long long w = L >= 2 ? (1ll << (7 * (7 - L))) : (L == 1 ? 1ll : 128ll);
 #pragma unroll
               for (int i2 = 0; i2 < 16; ++i2) {
-                const long long pl = (long long)oz_f2i_exact(v[i2]);  // an integer below 2^24 in magnitude
+                const long long pl = (long long)__float2int_rn(v[i2]);  // an integer below 2^24 in magnitude
                 if (L >= 2) Rs[i2] += pl * w;
                 else Hs[i2] += pl * w;
               }
@@ -525,10 +549,8 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
                 if (c >= N) break;
                 double out = 0.0;  // an all-zero row stays zero
                 if (er) {
-                  // X 2^sc rounded once, on the integer units; FP64 only outside the normal range
                   const int sc = S::escale(er) + fcol[c] - 63;
-                  if (!oz_round_x(Hs[i2], Rs[i2], sc, &out))
-                    out = fma((double)Hs[i2], t5_pow2(sc + 42), (double)Rs[i2] * t5_pow2(sc));
+                  out = fma((double)Hs[i2], t5_pow2(sc + 42), (double)Rs[i2] * t5_pow2(sc));
                 }
                 V[(size_t)(r0 + m) + (size_t)(s0 + c) * ldv] = out;
                 ex[i2] = (int)(((unsigned long long)__double_as_longlong(out) >> 52) & 0x7FF);
@@ -574,7 +596,7 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
       const int b = j & 1;
       const int r0 = tile * T5_M;
       const int rows = min(T5_M, n - r0);
-      if (j >= 2 && !t5_wait(&done[b], (uint32_t)(((j - 2) >> 1) & 1))) ok = 0;
+      if (j >= 2 && !t5w_wait(&done[b], (uint32_t)(((j - 2) >> 1) & 1), abortf)) ok = 0;
       ok = t5_bar_and(2, T5W_SLICERS, ok);
       if (!ok) break;
       int *er_b = erow + b * T5_M;

@@ -153,3 +153,27 @@ def test_batch_precision_form(lib):
         st = e.getStats()
         assert 0 < st["precision_steps"] < st["krylov_steps"]
     assert eps[2].getStats()["precision_steps"] == 0
+
+
+def test_wide_batch_equals_single_problem_path(lib):
+    """An engine wider than 80 columns (ncv 100: the dot kernel's 144-column tiling) stays bit-identical to EPSSolve
+    with the same projected solver and restart kernel, for symmetric and non-symmetric instances."""
+    saved = sg.batch_get_tuning()
+    try:
+        sg.batch_set_tuning([1] * sg.BATCH_BUCKETS)
+        probs = [(matgen.laplacian_2d_randdiag(n, 200 + i), True, "LR", 40, 100, 1e-10, 20 + i)
+                 for i, n in enumerate([3000, 5000, 8000])]
+        probs.append((matgen.convection_diffusion_2d(60, 2.0), False, "LR", 30, 100, 1e-10, 5))
+        probs.append((matgen.laplacian_2d_randdiag(2000, 7), True, "LM", 8, 24, 1e-10, 8))  # a narrow one beside
+        batch = [make(*p) for p in probs]
+        sg.solve_batch(batch)
+        for p, b in zip(probs, batch):
+            alone = make(*p, ds="qr", restart="pair")
+            alone.solve()
+            ra, rb = results(alone), results(b)
+            assert ra[0] == rb[0] and ra[1] == rb[1] and ra[2] == rb[2] == 1
+            assert ra[3] == rb[3], (ra[3], rb[3])
+            for xa, xb in zip(ra[4], rb[4]):
+                assert np.array_equal(xa, xb)
+    finally:
+        sg.batch_set_tuning(saved)

@@ -14,7 +14,7 @@ T5_M, T5_NC, T5_KC, T5_THREADS = 128, 64, 32, 512
 T5_ASL = T5_M * T5_KC * 2
 T5_BSL = T5_NC * T5_KC * 2
 T5_STAGE = OZ_SA * T5_ASL + OZ_QMAX * T5_BSL
-T5W_TENSOR = 128
+T5W_TENSOR = 256
 T5W_SLICERS = T5_THREADS - T5W_TENSOR
 T5W_H = T5W_SLICERS // T5_M
 T5_SMEM = 2 * T5_STAGE + (2 + T5W_H) * T5_M * 4 + 9 * 8 + 16 + T5_NC * 4
@@ -112,11 +112,16 @@ def check(n, ld, K, N, f64=False):
                 b_hi = b_lo + (nch // 8 - 1) * 128 + 1 * (T5_NC // 8) * 128 + 128
                 assert a_hi <= T5_ASL and b_hi <= T5_BSL
                 assert (2 * T5_STAGE) >> 4 < (1 << 14)  # descriptor start-address field
-        # epilogue: tensor warp w reads lanes 32 w .. +31 and columns L 64 + col .. +15 for col = 0, 16, .. < nch
+        # epilogue: tensor warp w reads lanes 32 (w % 4) .. +31 and columns L 64 + col .. +15 for
+        # col = 16 (w / 4), + 16 (T5W_TENSOR / 128), .. < nch; every column group is read by one warp per lane quarter
+        seen = set()
         for w in range(T5W_TENSOR // 32):
-            for col in range(0, nch, 16):
-                assert 32 * w + 31 < 128 and (OZ_L - 1) * T5_NC + col + 16 <= TMEM_COLS
+            for col in range(16 * (w // 4), nch, 16 * (T5W_TENSOR // 128)):
+                assert 32 * (w % 4) + 31 < 128 and (OZ_L - 1) * T5_NC + col + 16 <= TMEM_COLS
                 assert c0 + col < rup(N, 16) <= np_     # fcol entries read are written by k_oz_qslice
+                assert (w % 4, col) not in seen
+                seen.add((w % 4, col))
+        assert seen == {(q, col) for q in range(4) for col in range(0, nch, 16)}
         assert nch <= T5W_TENSOR                        # the column-exponent threads (tid < nch) are tensor threads
 
 
