@@ -30,10 +30,10 @@ PetscErrorCode EPSGB300SetArithmetic(EPS eps, EPSGB300Arith arith);
 PetscErrorCode EPSGB300GetArithmetic(EPS eps, EPSGB300Arith *arith);
 
 /* Solver of the symmetric projected problem inside EPSSolve.
- *   EPS_GB300_DS_AUTO (default): EPS_GB300_DS_REFINED while its accuracy checks pass; after two restarts in a row
- *       whose pairs failed the check (each redone by the QR solver), EPS_GB300_DS_QR for the rest of the solve.
+ *   EPS_GB300_DS_AUTO (default): EPS_GB300_DS_REFINED while its accuracy checks pass; from the first restart whose
+ *       pairs fail the check (that restart redone by the QR solver), EPS_GB300_DS_QR for the rest of the solve.
  *       Problems whose wanted end is well separated keep the fast solver; dense clusters (the 3-D Laplacians) cost
- *       two extra attempts per solve.
+ *       one extra attempt per solve and follow the QR solver's iteration exactly.
  *   EPS_GB300_DS_QR: the reference's algorithm (arrowhead reduction, implicit QL) in FP64 in one thread
  *       block.
  *   EPS_GB300_DS_REFINED: FP32 arrowhead reduction and implicit QL, then FP64 eigenvector refinement (Ogita-Aishima

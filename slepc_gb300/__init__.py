@@ -459,7 +459,7 @@ class EPS:
         _check(load().EPSGB300SetGraphCapture(self.handle, int(mode)), "EPSGB300SetGraphCapture")
 
     def setProjectedSolver(self, method):
-        """'auto' (default: 'refined' until two restarts in a row fall back, then 'qr'), 'qr' (FP64 QL) or
+        """'auto' (default: 'refined' until a restart falls back, then 'qr'), 'qr' (FP64 QL) or
         'refined' (FP32 QL + FP64 refinement with a checked fallback to 'qr') for the symmetric projected problem."""
         code = {"refined": 0, "qr": 1, "auto": 2}[method]
         _check(load().EPSGB300SetProjectedSolver(self.handle, code), "EPSGB300SetProjectedSolver")

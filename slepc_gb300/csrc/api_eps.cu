@@ -1816,8 +1816,8 @@ static PetscErrorCode eps_solve_core(EPS eps, double tol, std::chrono::steady_cl
   KSG_CUDA(cudaMemsetAsync(eps->H.p, 0, sizeof(double) * eps->H.count, s));
   int nconv = 0, l = 0, its = 0, reason = 0;
   double bytes = 0.0;
-  // the mixed-precision projected solver while it passes its checks (EPS_GB300_DS_AUTO: until two restarts in a
-  // row fall back to the QR solver)
+  // the mixed-precision projected solver while it passes its checks (EPS_GB300_DS_AUTO: until a restart falls back
+  // to the QR solver, whose result that restart then uses)
   bool ds_refined =
       herm && ld <= 144 && (eps->ds_method == EPS_GB300_DS_REFINED || eps->ds_method == EPS_GB300_DS_AUTO);
   int ds_fb_run = 0;
@@ -1875,7 +1875,7 @@ static PetscErrorCode eps_solve_core(EPS eps, double tol, std::chrono::steady_cl
     if (ds_refined) {
       if (c.ds_fallback) {
         eps->stats.ds_fallbacks++;
-        if (++ds_fb_run >= 2 && eps->ds_method == EPS_GB300_DS_AUTO) ds_refined = false;
+        if (++ds_fb_run >= 1 && eps->ds_method == EPS_GB300_DS_AUTO) ds_refined = false;
       } else {
         ds_fb_run = 0;
       }

@@ -26,20 +26,21 @@ constexpr int DS_WIDE_MAXN = 1024;
 
 // per-index scratch of one projected solve: shared arrays for n <= 144, carved from dynamic shared memory above
 struct DSHepMem {
-  double *sd, *se, *rc, *rs, *serr, *dtmp;
+  double *sd, *se, *rc, *rs, *serr, *dtmp, *rc2, *rs2;  // rc2, rs2: the second buffer of QL sweep rotations
   int *sperm, *sw_a, *sw_b, *perm2, *comp, *where, *at;
   double *Qs;  // n x n, column-major with leading dimension ldq
   int ldq;
   int inplace;  // Qs is a.Q itself (ldq = a.ld): no copy in or out
 };
 
-static inline size_t ds_wide_smem(int n) { return (size_t)n * (6 * sizeof(double) + 7 * sizeof(int)); }
+static inline size_t ds_wide_smem(int n) { return (size_t)n * (8 * sizeof(double) + 7 * sizeof(int)); }
 
 KS_DEVICE DSHepMem ds_wide_mem(unsigned char *raw, int n, double *Q, int ld) {
   DSHepMem m;
   double *dp = reinterpret_cast<double *>(raw);
   m.sd = dp; m.se = dp + n; m.rc = dp + 2 * n; m.rs = dp + 3 * n; m.serr = dp + 4 * n; m.dtmp = dp + 5 * n;
-  int *ip = reinterpret_cast<int *>(dp + 6 * n);
+  m.rc2 = dp + 6 * n; m.rs2 = dp + 7 * n;
+  int *ip = reinterpret_cast<int *>(dp + 8 * n);
   m.sperm = ip; m.sw_a = ip + n; m.sw_b = ip + 2 * n; m.perm2 = ip + 3 * n; m.comp = ip + 4 * n;
   m.where = ip + 5 * n; m.at = ip + 6 * n;
   m.Qs = Q;
@@ -90,13 +91,15 @@ KS_DEVICE int ds_compare(int which, double target, double ar, double ai, double 
 
 // the small solver's scratch: shared arrays, Q in dynamic shared memory with leading dimension n
 #define DS_SMALL_MEM(m, Qshared, nn)                                                                          \
-  __shared__ double sd_[DS_MAXN], se_[DS_MAXN], rc_[DS_MAXN], rs_[DS_MAXN], serr_[DS_MAXN], dtmp_[DS_MAXN];  \
+  __shared__ double sd_[DS_MAXN], se_[DS_MAXN], rc_[DS_MAXN], rs_[DS_MAXN], serr_[DS_MAXN], dtmp_[DS_MAXN],  \
+      rc2_[DS_MAXN], rs2_[DS_MAXN];                                                                          \
   __shared__ int sperm_[DS_MAXN], swa_[DS_MAXN], swb_[DS_MAXN], perm2_[DS_MAXN], comp_[DS_MAXN],              \
       where_[DS_MAXN], at_[DS_MAXN];                                                                         \
-  DSHepMem m = {sd_, se_, rc_, rs_, serr_, dtmp_, sperm_, swa_, swb_, perm2_, comp_, where_, at_, Qshared, nn, 0}
+  DSHepMem m = {sd_,    se_,    rc_,   rs_,    serr_,  dtmp_, rc2_,    rs2_, sperm_,                          \
+                swa_,   swb_,   perm2_, comp_, where_, at_,   Qshared, nn,   0}
 
 KS_DEVICE void ds_hep_body(const DSArgs &a, const DSHepMem &mem) {
-  __shared__ int s_cmd, s_lo, s_hi, s_nsw, s_fail;
+  __shared__ int s_cmd2[2], s_lo2[2], s_hi2[2], s_nsw, s_fail;
   __shared__ double s_beta_e;
   double *sd = mem.sd, *se = mem.se, *rc = mem.rc, *rs = mem.rs, *serr = mem.serr;
   int *sperm = mem.sperm, *sw_a = mem.sw_a, *sw_b = mem.sw_b;
@@ -168,80 +171,94 @@ KS_DEVICE void ds_hep_body(const DSArgs &a, const DSHepMem &mem) {
   }
   // ---- implicit QL on [l, n) ----
   {
-    // thread 0 drives; other threads apply the recorded sweeps
-    int ll = 0, total = 0;       // thread 0 state (block-relative indices)
+    // Thread 0 computes each sweep's rotations (the serial FP64 chain) into one of two buffers while the warps on
+    // sub-partitions 1-3 apply the previous sweep's rotations to the rows of Q: the two overlap, and sub-partition
+    // 0's FP64 pipe (thread 0's warp and warp 4) stays with the chain.
+    int ll = 0, total = 0;  // thread 0 state (block-relative indices)
     const int m_blk = (flags & DS_DO_SOLVE) ? n - l : 0;
     double *d = sd + l, *e = se + l;
+    double *rcb[2] = {rc, mem.rc2}, *rsb[2] = {rs, mem.rs2};
     if (tid == 0 && m_blk > 0) e[m_blk - 1] = 0.0;
-    for (;;) {
-      if (tid == 0) {
-        s_cmd = 0;
-        while (ll < m_blk) {
-          int m;
-          for (m = ll; m < m_blk - 1; ++m) {
-            const double dd = fabs(d[m]) + fabs(d[m + 1]);
-            if (fabs(e[m]) <= DBL_EPSILON * dd) break;
-          }
-          if (m == ll) { ++ll; continue; }
-          if (++total > 30 * m_blk) { s_fail = 1; break; }
-          double g = (d[ll + 1] - d[ll]) / (2.0 * e[ll]);
-          double r = hypot(g, 1.0);
-          g = d[m] - d[ll] + e[ll] / (g + copysign(r, g));
-          double s = 1.0, c = 1.0, p = 0.0;
-          int i;
-          int under = 0;
-          for (i = m - 1; i >= ll; --i) {
-            const double f = s * e[i], b = c * e[i];
-            // r = hypot(f, g), s = f / r, c = g / r by one reciprocal square root: on GB300 a dependent FP64
-            // square root costs about 690 cycles and a division 440, and this recurrence is the solver's serial
-            // chain (sums of squares far from overflow here: the operator is scaled into [2^-20, 2^20])
-            const double t2 = fma(f, f, g * g);
-            if (t2 < 1e-280) {
-              r = hypot(f, g);
-              e[i + 1] = r;
-              if (r == 0.0) { d[i + 1] -= p; e[m] = 0.0; under = 1; break; }
-              s = f / r;
-              c = g / r;
-            } else {
-              const double ri = rsqrt(t2);
-              r = t2 * ri;
-              e[i + 1] = r;
-              s = f * ri;
-              c = g * ri;
-            }
-            g = d[i + 1] - p;
-            r = (d[i] - g) * s + 2.0 * c * b;
-            p = s * r;
-            d[i + 1] = g + p;
-            g = c * r - b;
-            rc[i] = c;
-            rs[i] = s;
-          }
-          if (!under) {
-            d[ll] -= p;
-            e[ll] = g;
-            e[m] = 0.0;
-          }
-          s_lo = under ? i + 1 : ll;
-          s_hi = m;  // rotations i = s_hi-1 down to s_lo
-          s_cmd = 1;
-          break;
+    auto sweep = [&](int buf) {  // thread 0: the next sweep's rotations into buffer buf, or s_cmd2[buf] = 0
+      double *rcw = rcb[buf], *rsw = rsb[buf];
+      s_cmd2[buf] = 0;
+      while (ll < m_blk) {
+        int m;
+        for (m = ll; m < m_blk - 1; ++m) {
+          const double dd = fabs(d[m]) + fabs(d[m + 1]);
+          if (fabs(e[m]) <= DBL_EPSILON * dd) break;
         }
+        if (m == ll) { ++ll; continue; }
+        if (++total > 30 * m_blk) { s_fail = 1; break; }
+        double g = (d[ll + 1] - d[ll]) / (2.0 * e[ll]);
+        double r = hypot(g, 1.0);
+        g = d[m] - d[ll] + e[ll] / (g + copysign(r, g));
+        double s = 1.0, c = 1.0, p = 0.0;
+        int i;
+        int under = 0;
+        for (i = m - 1; i >= ll; --i) {
+          const double f = s * e[i], b = c * e[i];
+          // r = hypot(f, g), s = f / r, c = g / r by one reciprocal square root: on GB300 a dependent FP64
+          // square root costs about 690 cycles and a division 440, and this recurrence is the solver's serial
+          // chain (sums of squares far from overflow here: the operator is scaled into [2^-20, 2^20])
+          const double t2 = fma(f, f, g * g);
+          if (t2 < 1e-280) {
+            r = hypot(f, g);
+            e[i + 1] = r;
+            if (r == 0.0) { d[i + 1] -= p; e[m] = 0.0; under = 1; break; }
+            s = f / r;
+            c = g / r;
+          } else {
+            const double ri = rsqrt(t2);
+            r = t2 * ri;
+            e[i + 1] = r;
+            s = f * ri;
+            c = g * ri;
+          }
+          g = d[i + 1] - p;
+          r = (d[i] - g) * s + 2.0 * c * b;
+          p = s * r;
+          d[i + 1] = g + p;
+          g = c * r - b;
+          rcw[i] = c;
+          rsw[i] = s;
+        }
+        if (!under) {
+          d[ll] -= p;
+          e[ll] = g;
+          e[m] = 0.0;
+        }
+        s_lo2[buf] = under ? i + 1 : ll;
+        s_hi2[buf] = m;  // rotations i = s_hi-1 down to s_lo
+        s_cmd2[buf] = 1;
+        break;
       }
-      __syncthreads();
-      if (s_cmd == 0) break;
-      const int lo = s_lo, hi = s_hi;
-      for (int r = tid; r < nq; r += DS_THREADS) {
-        double *row = Qs + r;
-        // column l+i+1 of rotation i is column l+i of rotation i+1: carried in a register down the sweep
-        double t = row[(size_t)(l + hi) * lq];
-        for (int i = hi - 1; i >= lo; --i) {
-          const double c = rc[i], s = rs[i];
-          const double qi = row[(size_t)(l + i) * lq];
-          row[(size_t)(l + i + 1) * lq] = s * qi + c * t;
-          t = c * qi - s * t;
+    };
+    if (tid == 0) sweep(0);
+    __syncthreads();
+    const int warp = tid >> 5, lane = tid & 31;
+    const int aw = (warp & 3) ? (warp >> 2) * 3 + (warp & 3) - 1 : -1;  // warps 1-3, 5-7 -> 0..5
+    constexpr int DS_APPLIERS = 6 * 32;
+    for (int k = 0;; ++k) {
+      const int cur = k & 1;
+      if (s_cmd2[cur] == 0) break;
+      if (tid == 0) {
+        sweep(cur ^ 1);
+      } else if (aw >= 0) {
+        const int lo = s_lo2[cur], hi = s_hi2[cur];
+        const double *rcr = rcb[cur], *rsr = rsb[cur];
+        for (int r = aw * 32 + lane; r < nq; r += DS_APPLIERS) {
+          double *row = Qs + r;
+          // column l+i+1 of rotation i is column l+i of rotation i+1: carried in a register down the sweep
+          double t = row[(size_t)(l + hi) * lq];
+          for (int i = hi - 1; i >= lo; --i) {
+            const double c = rcr[i], s = rsr[i];
+            const double qi = row[(size_t)(l + i) * lq];
+            row[(size_t)(l + i + 1) * lq] = s * qi + c * t;
+            t = c * qi - s * t;
+          }
+          row[(size_t)(l + lo) * lq] = t;
         }
-        row[(size_t)(l + lo) * lq] = t;
       }
       __syncthreads();
     }
