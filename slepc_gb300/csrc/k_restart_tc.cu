@@ -520,7 +520,7 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
                   const int sc = S::escale(er) + fcol[c];
                   out = make_float2(ldexpf(hi, sc), ldexpf(lo, sc));
                 }
-                V[(size_t)(r0 + m) + (size_t)(s0 + c) * ldv] = out;
+                __stcs(V + (size_t)(r0 + m) + (size_t)(s0 + c) * ldv, out);  // streamed out (evict-first)
               }
             }
           } else {
@@ -552,7 +552,7 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
                   const int sc = S::escale(er) + fcol[c] - 63;
                   out = fma((double)Hs[i2], t5_pow2(sc + 42), (double)Rs[i2] * t5_pow2(sc));
                 }
-                V[(size_t)(r0 + m) + (size_t)(s0 + c) * ldv] = out;
+                __stcs(V + (size_t)(r0 + m) + (size_t)(s0 + c) * ldv, out);  // streamed out (evict-first)
                 ex[i2] = (int)(((unsigned long long)__double_as_longlong(out) >> 52) & 0x7FF);
               }
             }
@@ -646,7 +646,9 @@ __global__ void __launch_bounds__(T5_THREADS, 1)
 #pragma unroll
           for (int jj = 0; jj < 8; ++jj) {
             const int k = 8 * k8 + jj;
-            v[p2][jj] = (it < T5_M * nk8 && m < rows && k < K) ? V[(size_t)(r0 + m) + (size_t)(a0 + k) * ldv] : T{};
+            // the tile's second and last read of V: evict-first, so the slice scratch keeps its L2 lines
+            v[p2][jj] = (it < T5_M * nk8 && m < rows && k < K) ? __ldcs(V + (size_t)(r0 + m) + (size_t)(a0 + k) * ldv)
+                                                               : T{};
           }
         }
 #pragma unroll
