@@ -40,6 +40,7 @@ struct NhShared {
   double G[16];
   double red[NH_T / 32];
   double tau, beta, cs, sn;
+  double rf[2][4];  // bulge-chase reflectors (tau, v1, v2) of steps k and k+1
   double pc[MAXN / 2 + 1], ps[MAXN / 2 + 1];  // Givens rotations of one round of the parallel sort
   int pf[MAXN / 2 + 1];
   int cmd, i0, i1, i2, i3;
@@ -468,60 +469,122 @@ __device__ int nh_francis(double *A, int lda, double *Q, int ldq, int n, int ilo
       nh_std_block(A, lda, Q, ldq, n, sh.i0, sh);
       continue;
     }
-    // bulge chase over [m, hi]
+    // bulge chase over [m, hi].  Warp 0 owns the critical path of each step: the update of the 4 x 3 block that
+    // the next reflector depends on (rows k..k+3, columns k..k+2, both sides), then that reflector and the zeros
+    // of its column; warps 1-3 meanwhile apply the step to the rest of A (the rows' remaining columns, the
+    // columns' rows above k) and to Q.  The regions are disjoint, so one barrier per step suffices, and every
+    // entry gets the same operations as in a block-wide update.
     const int m = sh.i0, hi = sh.i1;
-    double x0 = sh.v[0], x1 = sh.v[1], x2 = sh.v[2];
+    const int warp = tid >> 5, lane = tid & 31;
+    if (warp == 0) {
+      const int nr = (3 < hi - m + 1) ? 3 : hi - m + 1;
+      double tau, v1, v2, beta;
+      nh_house3(sh.v[0], sh.v[1], nr == 3 ? sh.v[2] : 0.0, tau, v1, v2, beta);
+      if (lane == 0) {
+        sh.rf[m & 1][0] = tau;
+        sh.rf[m & 1][1] = v1;
+        sh.rf[m & 1][2] = v2;
+      }
+    }
+    nh_sync();
     for (int k = m; k <= hi - 1; ++k) {
       const int nr = (3 < hi - k + 1) ? 3 : hi - k + 1;
-      if (k > m) {
-        x0 = AH(k, k - 1);
-        x1 = AH(k + 1, k - 1);
-        x2 = nr == 3 ? AH(k + 2, k - 1) : 0.0;
-      }
-      double tau, v1, v2, beta;
-      nh_house3(x0, x1, nr == 3 ? x2 : 0.0, tau, v1, v2, beta);
-      if (tau == 0.0) continue;  // x is already (x0, 0, 0): nothing changes
-      const double w0 = tau, w1 = tau * v1, w2 = tau * v2;
-      // rows k..k+nr-1 over columns k..n-1
-      for (int j = k + tid; j < n; j += NH_T) {
-        const double a0 = AH(k, j), a1 = AH(k + 1, j);
-        if (nr == 3) {
-          const double a2 = AH(k + 2, j);
-          const double d = fma(v2, a2, fma(v1, a1, a0));
-          AH(k, j) = fma(-d, w0, a0);
-          AH(k + 1, j) = fma(-d, w1, a1);
-          AH(k + 2, j) = fma(-d, w2, a2);
+      const int cb = k + nr;                    // first column right of the reflector's
+      const int r1 = (k + 3 < hi) ? k + 3 : hi;  // last row the column update reaches
+      const double tau = sh.rf[k & 1][0], v1 = sh.rf[k & 1][1], v2 = sh.rf[k & 1][2];
+      if (tau != 0.0) {  // else x was already (x0, 0, 0): nothing changes
+        const double w0 = tau, w1 = tau * v1, w2 = tau * v2;
+        if (warp == 0) {
+          // rows k..k+nr-1 over the block's columns k..cb-1
+          if (lane < nr) {
+            const int j = k + lane;
+            const double a0 = AH(k, j), a1 = AH(k + 1, j);
+            if (nr == 3) {
+              const double a2 = AH(k + 2, j);
+              const double d = fma(v2, a2, fma(v1, a1, a0));
+              AH(k, j) = fma(-d, w0, a0);
+              AH(k + 1, j) = fma(-d, w1, a1);
+              AH(k + 2, j) = fma(-d, w2, a2);
+            } else {
+              const double d = fma(v1, a1, a0);
+              AH(k, j) = fma(-d, w0, a0);
+              AH(k + 1, j) = fma(-d, w1, a1);
+            }
+          }
+          __syncwarp();
+          // columns k..cb-1 over the block's rows k..r1
+          if (lane <= r1 - k) {
+            double *row = A + (k + lane);
+            const double a0 = row[(size_t)k * lda], a1 = row[(size_t)(k + 1) * lda];
+            if (nr == 3) {
+              const double a2 = row[(size_t)(k + 2) * lda];
+              const double d = fma(a2, v2, fma(a1, v1, a0));
+              row[(size_t)k * lda] = fma(-d, w0, a0);
+              row[(size_t)(k + 1) * lda] = fma(-d, w1, a1);
+              row[(size_t)(k + 2) * lda] = fma(-d, w2, a2);
+            } else {
+              const double d = fma(a1, v1, a0);
+              row[(size_t)k * lda] = fma(-d, w0, a0);
+              row[(size_t)(k + 1) * lda] = fma(-d, w1, a1);
+            }
+          }
+          __syncwarp();
         } else {
-          const double d = fma(v1, a1, a0);
-          AH(k, j) = fma(-d, w0, a0);
-          AH(k + 1, j) = fma(-d, w1, a1);
+          const int bt = tid - 32;
+          constexpr int NB = NH_T - 32;
+          // rows k..k+nr-1 over columns cb..n-1
+          for (int j = cb + bt; j < n; j += NB) {
+            const double a0 = AH(k, j), a1 = AH(k + 1, j);
+            if (nr == 3) {
+              const double a2 = AH(k + 2, j);
+              const double d = fma(v2, a2, fma(v1, a1, a0));
+              AH(k, j) = fma(-d, w0, a0);
+              AH(k + 1, j) = fma(-d, w1, a1);
+              AH(k + 2, j) = fma(-d, w2, a2);
+            } else {
+              const double d = fma(v1, a1, a0);
+              AH(k, j) = fma(-d, w0, a0);
+              AH(k + 1, j) = fma(-d, w1, a1);
+            }
+          }
+          // columns k..cb-1 over rows 0..k-1 of the matrix and all rows of the Schur vectors
+          for (int t = bt; t < k + n; t += NB) {
+            double *row;
+            int ldm;
+            if (t < k) { row = A + t; ldm = lda; }
+            else { row = Q + (t - k); ldm = ldq; }
+            const double a0 = row[(size_t)k * ldm], a1 = row[(size_t)(k + 1) * ldm];
+            if (nr == 3) {
+              const double a2 = row[(size_t)(k + 2) * ldm];
+              const double d = fma(a2, v2, fma(a1, v1, a0));
+              row[(size_t)k * ldm] = fma(-d, w0, a0);
+              row[(size_t)(k + 1) * ldm] = fma(-d, w1, a1);
+              row[(size_t)(k + 2) * ldm] = fma(-d, w2, a2);
+            } else {
+              const double d = fma(a1, v1, a0);
+              row[(size_t)k * ldm] = fma(-d, w0, a0);
+              row[(size_t)(k + 1) * ldm] = fma(-d, w1, a1);
+            }
+          }
         }
       }
-      nh_sync();
-      // column k-1 of the bulge (read by every thread above) becomes (beta, 0, 0)
-      if (tid == 0 && k > m) {
-        AH(k, k - 1) = beta;
-        AH(k + 1, k - 1) = 0.0;
-        if (nr == 3) AH(k + 2, k - 1) = 0.0;
-      }
-      // columns k..k+nr-1 over rows 0..r1 of the matrix and all rows of the Schur vectors
-      const int r1 = (k + 3 < hi) ? k + 3 : hi;
-      for (int t = tid; t <= r1 + n; t += NH_T) {
-        double *row;
-        int ldm;
-        if (t <= r1) { row = A + t; ldm = lda; }
-        else { row = Q + (t - r1 - 1); ldm = ldq; }
-        const double a0 = row[(size_t)k * ldm], a1 = row[(size_t)(k + 1) * ldm];
-        if (nr == 3) {
-          const double a2 = row[(size_t)(k + 2) * ldm];
-          const double d = fma(a2, v2, fma(a1, v1, a0));
-          row[(size_t)k * ldm] = fma(-d, w0, a0);
-          row[(size_t)(k + 1) * ldm] = fma(-d, w1, a1);
-          row[(size_t)(k + 2) * ldm] = fma(-d, w2, a2);
-        } else {
-          const double d = fma(a1, v1, a0);
-          row[(size_t)k * ldm] = fma(-d, w0, a0);
-          row[(size_t)(k + 1) * ldm] = fma(-d, w1, a1);
+      if (warp == 0 && k + 1 <= hi - 1) {
+        // the next step's reflector from column k, which becomes (beta, 0, 0): no other warp touches those
+        // entries in this step or the next
+        const int nr1 = (3 < hi - k) ? 3 : hi - k;
+        const double y0 = AH(k + 1, k), y1 = AH(k + 2, k), y2 = nr1 == 3 ? AH(k + 3, k) : 0.0;
+        double t1, u1, u2, b1;
+        nh_house3(y0, y1, y2, t1, u1, u2, b1);
+        __syncwarp();  // every lane has read column k
+        if (lane == 0) {
+          sh.rf[(k + 1) & 1][0] = t1;
+          sh.rf[(k + 1) & 1][1] = u1;
+          sh.rf[(k + 1) & 1][2] = u2;
+          if (t1 != 0.0) {
+            AH(k + 1, k) = b1;
+            AH(k + 2, k) = 0.0;
+            if (nr1 == 3) AH(k + 3, k) = 0.0;
+          }
         }
       }
       nh_sync();
