@@ -81,6 +81,7 @@ def load():
         "EPSGB300ServerCancel": ([P], I),
         "EPSGB300SetTimeLimit": ([P, D], I),
         "EPSGB300SetGraphCapture": ([P, I], I),
+        "EPSSetDeflationSpace": ([P, I, P], I),
         "EPSGB300SetRestartMethod": ([P, I], I),
         "EPSGB300SetGSMethod": ([P, I], I),
         "EPSGB300BatchGetTuning": ([ctypes.POINTER(I), I], I),
@@ -454,6 +455,13 @@ class EPS:
         """Wall-time budget of EPSSolve (checked after each restart; 0 = none)."""
         _check(load().EPSGB300SetTimeLimit(self.handle, float(seconds)), "EPSGB300SetTimeLimit")
 
+    def setDeflationSpace(self, vectors):
+        """EPSSetDeflationSpace: the eigenvectors sought are orthogonal to the span of these (length-n arrays); the
+        vectors are copied."""
+        vs = [Vec(np.ascontiguousarray(v, dtype=np.float64)) for v in vectors]
+        arr = (ctypes.c_void_p * max(1, len(vs)))(*[v.handle.value for v in vs])
+        _check(load().EPSSetDeflationSpace(self.handle, len(vs), arr), "EPSSetDeflationSpace")
+
     def setGraphCapture(self, mode):
         """Factorisation segments as CUDA graphs: -1 auto (n <= 262144), 0 off, 1 on (EPSGB300SetGraphCapture)."""
         _check(load().EPSGB300SetGraphCapture(self.handle, int(mode)), "EPSGB300SetGraphCapture")
@@ -680,7 +688,7 @@ def batch_set_tuning(tiles):
 
 def solve(csr, *, hermitian=True, which="LM", nev=1, ncv=None, mpd=None, tol=None, max_it=None, v0=None,
           arith="pair", vectors=True, ds=None, lock=None, restart=None, harmonic=False, target=None, B=None,
-          conv=None, purify=None, gs=None):
+          conv=None, purify=None, gs=None, keep=None, deflation=None):
     """One-call convenience: returns dict(eigr, eigi, X, nconv, its, reason, errors, stats).  B (CSR arrays of a
     diagonal matrix) makes the problem generalised: EPS_GHEP when hermitian, else EPS_GNHEP."""
     A = Mat(*csr)
@@ -711,6 +719,10 @@ def solve(csr, *, hermitian=True, which="LM", nev=1, ncv=None, mpd=None, tol=Non
         eps.setGSMethod(gs)
     if lock is not None:
         eps.setKrylovSchurLocking(lock)
+    if keep is not None:
+        eps.setKrylovSchurRestart(keep)
+    if deflation is not None:
+        eps.setDeflationSpace(list(np.asarray(deflation, dtype=np.float64).reshape(A.m, -1).T))
     if v0 is not None:
         eps.setInitialSpace(v0)
     eps.solve()

@@ -93,6 +93,7 @@ PetscErrorCode ksg_engine_check(EPS e, int max_ncv, bool allow_f32) {
             "batched engine: Ritz extraction with the largest/smallest criteria only (use EPSSolve for targets)");
   KSG_CHECK(!e->B && e->conv == EPS_CONV_REL, PETSC_ERR_SUP,
             "batched engine: standard problems with the relative convergence test only (use EPSSolve)");
+  KSG_CHECK(e->ndefl == 0, PETSC_ERR_SUP, "batched engine: no deflation spaces (use EPSSolve)");
   return 0;
 }
 

@@ -1300,6 +1300,15 @@ extern "C" PetscErrorCode EPSSetUp(EPS eps) {
   }
   KSG_CHECK(eps->lock || mpd >= ncv, PETSC_ERR_SUP, "Should not use mpd parameter in non-locking variant");
   KSG_CHECK(eps->v0.empty() || (int)eps->v0.size() == n, PETSC_ERR_ARG_SIZ, "Initial vector has the wrong length");
+  // deflation spaces: the constraint columns join every projection; the harmonic, generalised and precision forms
+  // keep their own bases and do not take them
+  KSG_CHECK(eps->ndefl == 0 || (int)eps->defl.size() == eps->ndefl * n, PETSC_ERR_ARG_SIZ,
+            "The deflation vectors have the wrong length");
+  KSG_CHECK(eps->ndefl == 0 || (!eps->B && eps->extraction != EPS_HARMONIC && eps->arith != ARITH_F32),
+            PETSC_ERR_SUP, "Deflation spaces are provided for standard problems with Ritz extraction in the pair or "
+                           "FP64 arithmetic");
+  KSG_CHECK(ncv + 1 + eps->ndefl <= gs_wide_max_columns(), PETSC_ERR_SUP,
+            "ncv (%d) plus the deflation space (%d) exceeds %d columns", ncv, eps->ndefl, gs_wide_max_columns() - 1);
   KSG_CHECK(eps->nini <= ncv, PETSC_ERR_USER_INPUT, "The number of initial vectors is larger than ncv");
   eps->nev_e = nev;
   eps->ncv_e = ncv;
@@ -1316,7 +1325,8 @@ extern "C" PetscErrorCode EPSSetUp(EPS eps) {
   if (!eps->stream) KSG_CUDA(cudaStreamCreateWithFlags(&eps->stream, cudaStreamNonBlocking));
   eps_clear_graphs(eps);  // captured segments hold the old buffers' addresses
   const int ld = eps->ld;
-  KSG_CUDA(eps->V.alloc((size_t)eps->ldv * (ld + 1)));
+  eps->nc = 0;
+  KSG_CUDA(eps->V.alloc((size_t)eps->ldv * (ld + 1 + eps->ndefl)));  // constraint columns, then the basis
   KSG_CUDA(cudaMemsetAsync(eps->V.p, 0, sizeof(double) * eps->V.count, eps->stream));
   KSG_CUDA(eps->d.alloc(ld + 1));
   KSG_CUDA(eps->e.alloc(ld + 1));
@@ -1326,11 +1336,11 @@ extern "C" PetscErrorCode EPSSetUp(EPS eps) {
   KSG_CUDA(eps->eigr.alloc(ld));
   KSG_CUDA(eps->eigi.alloc(ld));
   KSG_CUDA(eps->errest.alloc(ld));
-  KSG_CUDA(eps->coef.alloc(2 * ld + 8));
+  KSG_CUDA(eps->coef.alloc(2 * (ld + eps->ndefl) + 8));
   KSG_CUDA(eps->work.alloc(4 * ld + 8));
   KSG_CUDA(eps->dsf.alloc(ds_fast_scratch_doubles(ld)));
   KSG_CUDA(eps->rtc.alloc(restart_tc_scratch_bytes(ld)));  // grown on the first tcgen05 restart
-  eps->pstride = (int)ksg_part_stride(ld);
+  eps->pstride = (int)ksg_part_stride(ld + eps->ndefl);
   KSG_CUDA(eps->part.alloc(ksg_part_blocks(n) * eps->pstride));
   KSG_CUDA(eps->st.alloc(1));
   KSG_CUDA(eps->ctl.alloc(1));
@@ -1365,6 +1375,17 @@ extern "C" PetscErrorCode EPSSetUp(EPS eps) {
   eps->opscale = 1.0;
   if (nrm > 0.0 && (nrm > 1048576.0 || nrm < 1.0 / 1048576.0)) eps->opscale = ldexp(1.0, -ilogb(nrm));
   eps->lanes = spmv_lanes_for((double)op->nnz / n);
+  // BVInsertConstraints: each deflation vector orthonormalised against the ones kept before it (the same two-pass
+  // Gram-Schmidt kernels), a linearly dependent one dropped
+  for (int i = 0; i < eps->ndefl; ++i) {
+    KSG_TRY(ksg_put_column(ksg_col(eps->V.p, eps->ldv, eps->nc, eps->storage), eps->defl.data() + (size_t)i * n, n,
+                           eps->storage, eps->stream));
+    double cn = 0.0;
+    int dep = 0;
+    KSG_TRY(ksg_orthonormalize_column(eps->V.p, eps->ldv, n, eps->nc, eps->coef.p, eps->part.p, eps->pstride,
+                                      eps->st.p, eps->arith, eps->stream, &cn, &dep, 2, eps->storage, nullptr));
+    if (!dep && cn != 0.0) eps->nc++;
+  }
   // matrix norms of EPS_CONV_NORM (epssetup.c:343-353): ||B|| only for generalised problems, else 0
   if (eps->conv == EPS_CONV_NORM) {
     eps->nrma = ksg_mat_norm_inf(eps->A);
@@ -1474,6 +1495,8 @@ static PetscErrorCode eps_factorize_launch(EPS eps, int k0, int nv, double *byte
   a.pstride = eps->pstride;
   a.st = eps->st.p;
   a.tc = eps->gs_tc_on ? &eps->gt : nullptr;
+  a.nc = eps->nc;
+  const int nc = eps->nc;
   const double colb = 8.0 * n;
   const Mat op = eps->op;
   LongRows lr;
@@ -1489,14 +1512,14 @@ static PetscErrorCode eps_factorize_launch(EPS eps, int k0, int nv, double *byte
     lr.part = eps->seg_part.p;
   }
   for (int j = k0; j < nv; ++j) {
-    void *u = ksg_col(eps->V.p, eps->ldv, j, eps->storage);
-    void *w = ksg_col(eps->V.p, eps->ldv, j + 1, eps->storage);
+    void *u = ksg_col(eps->V.p, eps->ldv, nc + j, eps->storage);
+    void *w = ksg_col(eps->V.p, eps->ldv, nc + j + 1, eps->storage);
     {
       LaunchScope ls(eps, EPS_GB300_K_SPMV, spmv_bytes(eps));
       KSG_CUDA(launch_spmv_storage(op->d_rp.p, op->d_ci.p, op->d_va.p, op->d_va2.p, u, w, n, eps->lanes, eps->st.p,
                                    eps->opscale, eps->storage, s, &lr, op->d_va32.p));
     }
-    a.J = j;
+    a.J = nc + j;  // the constraint columns, then Krylov columns 0..j-1
     a.j = j;
     a.U = u;
     a.W = w;
@@ -1510,9 +1533,9 @@ static PetscErrorCode eps_factorize_launch(EPS eps, int k0, int nv, double *byte
     }
     *bytes += spmv_bytes(eps) + colb * (j + 2) + colb * (j + 4);
   }
-  a.J = nv;
+  a.J = nc + nv;
   a.j = nv;
-  a.U = ksg_col(eps->V.p, eps->ldv, nv, eps->storage);
+  a.U = ksg_col(eps->V.p, eps->ldv, nc + nv, eps->storage);
   a.W = nullptr;
   {
     LaunchScope ls(eps, EPS_GB300_K_GS_DOT, colb * (nv + 1));
@@ -1576,14 +1599,20 @@ static PetscErrorCode eps_factorize(EPS eps, int k0, int nv, double *bytes) {
   return 0;
 }
 
+// the Krylov basis: column nc of V (the constraint columns of a deflation space come first), as a double pointer
+// whose column stride is ldv 8-byte entries in the pair and FP64 formats
+static inline double *eps_basis(EPS eps) {
+  return static_cast<double *>(ksg_col(eps->V.p, eps->ldv, eps->nc, eps->storage));
+}
+
 // basis column <-> FP64 device vector, for the pair and FP64 storage formats
 static cudaError_t eps_column_to_f64(EPS eps, int col, double *x, cudaStream_t s) {
-  const void *c = ksg_col(eps->V.p, eps->ldv, col, eps->storage);
+  const void *c = ksg_col(eps->V.p, eps->ldv, eps->nc + col, eps->storage);
   if (eps->storage == STORE_PAIR) return launch_pair_to_f64(static_cast<const float2 *>(c), x, eps->n, s);
   return cudaMemcpyAsync(x, c, sizeof(double) * eps->n, cudaMemcpyDeviceToDevice, s);
 }
 static cudaError_t eps_f64_to_column(EPS eps, const double *x, int col, cudaStream_t s) {
-  void *c = ksg_col(eps->V.p, eps->ldv, col, eps->storage);
+  void *c = ksg_col(eps->V.p, eps->ldv, eps->nc + col, eps->storage);
   if (eps->storage == STORE_PAIR) return launch_f64_to_pair(x, static_cast<float2 *>(c), eps->n, s);
   return cudaMemcpyAsync(c, x, sizeof(double) * eps->n, cudaMemcpyDeviceToDevice, s);
 }
@@ -1621,7 +1650,7 @@ PetscErrorCode ksg_eps_put_start(EPS eps, cudaStream_t s) {
     ksg_random_fill(h.data(), eps->n, eps->seed, 0);
     src = h.data();
   }
-  KSG_TRY(ksg_put_column(eps->V.p, src, eps->n, eps->storage, s));
+  KSG_TRY(ksg_put_column(ksg_col(eps->V.p, eps->ldv, eps->nc, eps->storage), src, eps->n, eps->storage, s));
   KSG_CUDA(cudaStreamSynchronize(s));  // h is pageable and goes out of scope
   if (eps->problem == EPS_GHEP && eps->B) KSG_TRY(eps_apply_op_column(eps, 0, s));
   return 0;
@@ -1630,13 +1659,13 @@ PetscErrorCode ksg_eps_put_start(EPS eps, cudaStream_t s) {
 PetscErrorCode ksg_eps_new_start_vector(EPS eps, int col, int *breakdown) {
   std::vector<double> h(eps->n);
   ksg_random_fill(h.data(), eps->n, eps->seed, ++eps->rng_counter);
-  void *dst = ksg_col(eps->V.p, eps->ldv, col, eps->storage);
+  void *dst = ksg_col(eps->V.p, eps->ldv, eps->nc + col, eps->storage);
   KSG_TRY(ksg_put_column(dst, h.data(), eps->n, eps->storage, eps->stream));
   if (eps->problem == EPS_GHEP && eps->B) KSG_TRY(eps_apply_op_column(eps, col, eps->stream));
   double nrm = 0.0;
   int ld = 0;
-  KSG_TRY(ksg_orthonormalize_column(eps->V.p, eps->ldv, eps->n, col, eps->coef.p, eps->part.p, eps->pstride,
-                                    eps->st.p, eps->arith, eps->stream, &nrm, &ld, 2, eps->storage,
+  KSG_TRY(ksg_orthonormalize_column(eps->V.p, eps->ldv, eps->n, eps->nc + col, eps->coef.p, eps->part.p,
+                                    eps->pstride, eps->st.p, eps->arith, eps->stream, &nrm, &ld, 2, eps->storage,
                                     eps->gs_tc_on ? &eps->gt : nullptr));
   *breakdown = ld || nrm == 0.0;
   return 0;
@@ -1708,7 +1737,7 @@ PetscErrorCode ksg_eps_assemble(EPS eps, int nconv, const double *er, const doub
         eps->r_eigi[i] = -eps->r_eigi[i];
         eps->r_eigi[i + 1] = -eps->r_eigi[i + 1];
         // negate a basis column: both halves of a pair, the float, or the double
-        KSG_CUDA(launch_negate(ksg_col(eps->V.p, eps->ldv, i + 1, eps->storage),
+        KSG_CUDA(launch_negate(ksg_col(eps->V.p, eps->ldv, eps->nc + i + 1, eps->storage),
                                eps->storage == STORE_PAIR ? 2 * n : n, eps->storage != STORE_F64, s));
       }
       i++;
@@ -1740,15 +1769,15 @@ static cudaError_t eps_restart(EPS eps, int a0, int K, int s0, int N, const doub
         if (e != cudaSuccess) return e;
       }
       if (eps->storage == STORE_F64)
-        return launch_restart_t5_f64(eps->V.p, eps->ldv, eps->n, a0, K, s0, N, Q, eps->ld, eps->rtc.p, eps->ld, s,
+        return launch_restart_t5_f64(eps_basis(eps), eps->ldv, eps->n, a0, K, s0, N, Q, eps->ld, eps->rtc.p, eps->ld, s,
                                      eps->vexp.p, eps->gt.ldt);
-      return launch_restart_t5(reinterpret_cast<float2 *>(eps->V.p), eps->ldv, eps->n, a0, K, s0, N, Q, eps->ld,
+      return launch_restart_t5(reinterpret_cast<float2 *>(eps_basis(eps)), eps->ldv, eps->n, a0, K, s0, N, Q, eps->ld,
                                eps->rtc.p, eps->ld, s);
     }
-    return launch_restart_tc(reinterpret_cast<float2 *>(eps->V.p), eps->ldv, eps->n, a0, K, s0, N, Q, eps->ld,
+    return launch_restart_tc(reinterpret_cast<float2 *>(eps_basis(eps)), eps->ldv, eps->n, a0, K, s0, N, Q, eps->ld,
                              eps->rtc.p, eps->ld, s);
   }
-  return launch_restart(eps->V.p, eps->ldv, eps->n, a0, K, s0, N, Q, eps->ld, eps->arith, s, eps->storage);
+  return launch_restart(eps_basis(eps), eps->ldv, eps->n, a0, K, s0, N, Q, eps->ld, eps->arith, s, eps->storage);
 }
 
 __global__ void k_residual(const double *y, const double *yi, const double *x, const double *xi, const double *b,
@@ -1797,7 +1826,7 @@ static PetscErrorCode eps_solve_core(EPS eps, double tol, std::chrono::steady_cl
   {
     const int rm = eps->restart_method;
     eps->gs_tc_on = eps->storage == STORE_F64 && eps->arith == ARITH_F64 && eps->gs_method == EPS_GB300_GS_TENSOR &&
-                    herm && eps->vexp.p && ld <= gs_tc_max_columns() && ncv < n &&
+                    herm && eps->vexp.p && ld <= gs_tc_max_columns() && ncv < n && eps->nc == 0 &&
                     (rm == EPS_GB300_RESTART_TCGEN05 || (rm == EPS_GB300_RESTART_TENSOR && kRestartTensorIsTcgen05));
     if (eps->gs_tc_on) KSG_CUDA(cudaMemsetAsync(eps->gterr.p, 0, sizeof(int), s));
   }
@@ -1806,8 +1835,9 @@ static PetscErrorCode eps_solve_core(EPS eps, double tol, std::chrono::steady_cl
     KSG_TRY(ksg_eps_put_start(eps, s));
     double nrm = 0.0;
     int lindep = 0;
-    KSG_TRY(ksg_orthonormalize_column(eps->V.p, eps->ldv, n, 0, eps->coef.p, eps->part.p, eps->pstride, eps->st.p,
-                                      eps->arith, s, &nrm, &lindep, 1, eps->storage,
+    // against the constraint columns (if any) with refinement as needed, else a normalisation
+    KSG_TRY(ksg_orthonormalize_column(eps->V.p, eps->ldv, n, eps->nc, eps->coef.p, eps->part.p, eps->pstride,
+                                      eps->st.p, eps->arith, s, &nrm, &lindep, eps->nc ? 0 : 1, eps->storage,
                                       eps->gs_tc_on ? &eps->gt : nullptr));
     KSG_CHECK(!lindep && nrm != 0.0, PETSC_ERR_PLIB, "Initial vector is zero or belongs to the deflation space");
   }
@@ -1890,13 +1920,13 @@ static PetscErrorCode eps_solve_core(EPS eps, double tol, std::chrono::steady_cl
       // with g~ from the projected solver (work) and gamma in the control block; the BVMultVec form of the
       // Gram-Schmidt update kernel
       StepArgs ha = {};
-      ha.V = eps->V.p;
+      ha.V = eps_basis(eps);  // (no constraint columns with harmonic extraction)
       ha.ldv = eps->ldv;
       ha.n = n;
       ha.J = nv;
       ha.j = nv;
       ha.hermitian = 1;
-      ha.U = ksg_col(eps->V.p, eps->ldv, nv, eps->storage);
+      ha.U = ksg_col(eps_basis(eps), eps->ldv, nv, eps->storage);
       ha.eta = 0.7071;
       ha.coef = eps->work.p;
       ha.part = eps->part.p;
@@ -1922,8 +1952,8 @@ static PetscErrorCode eps_solve_core(EPS eps, double tol, std::chrono::steady_cl
           if (bd) reason = EPS_DIVERGED_BREAKDOWN;
         }
       } else {
-        KSG_CUDA(cudaMemcpyAsync(ksg_col(eps->V.p, eps->ldv, k + l, eps->storage),
-                                 ksg_col(eps->V.p, eps->ldv, nv, eps->storage), ksg_entry_bytes(eps->storage) * n,
+        KSG_CUDA(cudaMemcpyAsync(ksg_col(eps_basis(eps), eps->ldv, k + l, eps->storage),
+                                 ksg_col(eps_basis(eps), eps->ldv, nv, eps->storage), ksg_entry_bytes(eps->storage) * n,
                                  cudaMemcpyDeviceToDevice, s));
       }
     }
@@ -2108,7 +2138,7 @@ extern "C" PetscErrorCode EPSGetEigenvector(EPS eps, PetscInt i, Vec Vr, Vec Vi)
   KSG_CHECK((!Vr || Vr->n == n) && (!Vi || Vi->n == n), PETSC_ERR_ARG_SIZ, "Vector of the wrong size");
   const int k = eps->perm[i];
   const double ei = eps->r_eigi[k];
-  const double *col = eps->V.p + (size_t)k * eps->ldv;
+  const double *col = eps_basis(eps) + (size_t)k * eps->ldv;
   const size_t bytes = sizeof(double) * n;
   const int sto = eps->storage;
   if (ei > 0.0) {
@@ -2193,8 +2223,8 @@ extern "C" PetscErrorCode EPSComputeError(EPS eps, PetscInt i, EPSErrorType type
   const int k = eps->perm[i];
   double kr = eps->r_eigr[k], ki = eps->r_eigi[k];
   const int kx = (ki < 0.0) ? k - 1 : k;  // the stored pair is (x, xi) for the eigenvalue with positive imaginary part
-  const double *x = static_cast<const double *>(ksg_col(eps->V.p, eps->ldv, kx, eps->storage));
-  const double *xi = (ki != 0.0) ? static_cast<const double *>(ksg_col(eps->V.p, eps->ldv, kx + 1, eps->storage))
+  const double *x = static_cast<const double *>(ksg_col(eps_basis(eps), eps->ldv, kx, eps->storage));
+  const double *xi = (ki != 0.0) ? static_cast<const double *>(ksg_col(eps_basis(eps), eps->ldv, kx + 1, eps->storage))
                                   : nullptr;
   if (ki < 0.0) ki = -ki;
   const int gen = eps->B != nullptr;
@@ -2313,7 +2343,7 @@ extern "C" PetscErrorCode EPSGB300GetDeviceEigenvectors(EPS eps, const double **
       KSG_CUDA(cudaMemcpyAsync(eps->d_perm.p, cols.data(), sizeof(int) * m, cudaMemcpyHostToDevice, eps->stream));
       const double *bis = (eps->B && eps->problem == EPS_GHEP) ? eps->d_bisqrt.p : nullptr;
       dim3 grid((unsigned)std::min<long long>((n + 255) / 256, 1024), (unsigned)m);
-      k_gather_eigvecs<<<grid, 256, 0, eps->stream>>>(eps->V.p, eps->ldv, eps->storage, eps->d_perm.p, bis, n, m,
+      k_gather_eigvecs<<<grid, 256, 0, eps->stream>>>(eps_basis(eps), eps->ldv, eps->storage, eps->d_perm.p, bis, n, m,
                                                       eps->xvec.p, ldx);
       KSG_CUDA(cudaGetLastError());
       KSG_CUDA(cudaStreamSynchronize(eps->stream));
@@ -2337,7 +2367,7 @@ extern "C" PetscErrorCode EPSGB300OrthogonalityError(EPS eps, PetscReal *err) {
   const int m = eps->nconv;
   double worst = 0.0;
   StepArgs a = {};
-  a.V = eps->V.p;
+  a.V = eps_basis(eps);
   a.ldv = eps->ldv;
   a.n = eps->n;
   a.coef = eps->coef.p;
@@ -2350,7 +2380,7 @@ extern "C" PetscErrorCode EPSGB300OrthogonalityError(EPS eps, PetscReal *err) {
     KSG_CUDA(launch_segment_begin(eps->st.p, 0, 0, eps->stream));
     a.J = j;
     a.j = j;
-    a.U = eps->V.p + (size_t)j * eps->ldv;
+    a.U = eps_basis(eps) + (size_t)j * eps->ldv;
     KSG_CUDA(launch_gs_dot(a, 1, GS_DOTS, eps->storage == STORE_PAIR ? ARITH_PAIR : ARITH_F64, eps->stream,
                            eps->storage));
     KSG_CUDA(cudaMemcpyAsync(h.data(), eps->coef.p, sizeof(double) * (j + 1), cudaMemcpyDeviceToHost, eps->stream));

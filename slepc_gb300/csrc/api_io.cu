@@ -931,10 +931,22 @@ extern "C" PetscErrorCode EPSGDGetDoubleExpansion(EPS eps, PetscBool *) {
   return ksg_set_error(PETSC_ERR_SUP, "EPSGDGetDoubleExpansion: the EPS type is krylovschur, not gd");
 }
 
-extern "C" PetscErrorCode EPSSetDeflationSpace(EPS eps, PetscInt n, Vec[]) {
+// EPSSetDeflationSpace (epsdefault.c / epssetup.c:523-560): the vectors are copied; EPSSetUp orthonormalises them
+// on the device into constraint columns ahead of the Krylov basis (BVInsertConstraints), dropping dependent ones
+extern "C" PetscErrorCode EPSSetDeflationSpace(EPS eps, PetscInt n, Vec v[]) {
   KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
   KSG_CHECK(n >= 0, PETSC_ERR_ARG_OUTOFRANGE, "Argument n cannot be negative");
-  KSG_CHECK(n == 0, PETSC_ERR_SUP, "A deflation space is not provided");
+  KSG_CHECK(n == 0 || v, PETSC_ERR_ARG_NULL, "Null vector array");
+  int len = 0;
+  for (PetscInt i = 0; i < n; ++i) {
+    KSG_CHECK(v[i] && v[i]->a, PETSC_ERR_ARG_NULL, "Null vector %d", (int)i);
+    KSG_CHECK(i == 0 || v[i]->n == len, PETSC_ERR_ARG_SIZ, "The deflation vectors must have one length");
+    len = v[i]->n;
+  }
+  eps->defl.assign((size_t)n * len, 0.0);
+  for (PetscInt i = 0; i < n; ++i) std::copy(v[i]->a, v[i]->a + len, eps->defl.begin() + (size_t)i * len);
+  eps->ndefl = (int)n;
+  eps->setup = 0;  // the next solve sets up again with the new constraints
   return 0;
 }
 

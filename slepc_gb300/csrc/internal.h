@@ -196,6 +196,10 @@ struct _p_EPS {
   DBuf<int> gterr;         // its error flag
   ksg::GTArgs gt = {};
   int gs_tc_on = 0;        // the current solve runs the tensor-core Gram-Schmidt
+  // EPSSetDeflationSpace: the vectors as given (ndefl x n, host) and, after EPSSetUp, the orthonormal constraint
+  // columns kept from them (columns 0..nc-1 of V, ahead of the Krylov basis)
+  std::vector<double> defl;
+  int ndefl = 0, nc = 0;
   DBuf<double> xvec;      // EPSGB300GetDeviceEigenvectors: FP64 eigenvectors in EPSGetEigenpair order
   DBuf<int> d_perm;       // its column map
   int xvec_valid = 0;     // xvec holds the current solve's vectors

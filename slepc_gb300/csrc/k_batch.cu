@@ -69,7 +69,7 @@ KS_DEVICE void *batch_col(const BatchInst &p, int j) {
 
 template <int STO>
 KS_DEVICE StepArgs batch_step_args(const BatchInst &p, int j, int nx) {
-  StepArgs a;
+  StepArgs a = {};  // no constraint columns (nc = 0) in the batched engine
   a.V = p.V;
   a.ldv = p.ldv;
   a.n = p.n;

@@ -353,6 +353,7 @@ __device__ void gs_epilogue(const StepArgs &a, const double *res, int mode) {
     return;
   }
   const int J = a.J, j = a.j;
+  const int off = a.nc;  // coefficient of Krylov column i: coef[off + i] (constraint columns come first)
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   __shared__ double sh_nu, sh_bp, sh_tau, sh_invnu, sh_hj, sh_sigma;
   __shared__ int sh_lindep, sh_first;
@@ -417,11 +418,11 @@ __device__ void gs_epilogue(const StepArgs &a, const double *res, int mode) {
   if (!first) {
     if (a.hermitian) {
       if (tid == 0) {
-        a.d[j - 1] += bp * a.coef[j - 1];
+        a.d[j - 1] += bp * a.coef[off + j - 1];
         a.e[j - 1] = lindep ? 0.0 : bp * nu;
       }
     } else {
-      for (int i = tid; i < j; i += blockDim.x) a.H[i + (size_t)(j - 1) * a.ldh] += bp * a.coef[i];
+      for (int i = tid; i < j; i += blockDim.x) a.H[i + (size_t)(j - 1) * a.ldh] += bp * a.coef[off + i];
       if (tid == 0) a.H[j + (size_t)(j - 1) * a.ldh] = lindep ? 0.0 : bp * nu;
     }
   }
@@ -434,10 +435,10 @@ __device__ void gs_epilogue(const StepArgs &a, const double *res, int mode) {
       // row j of H[0:j+1, 0:j]: the arrow (first step of a segment) or the subdiagonal entry
       double hs = 0.0;
       if (first) {
-        for (int i = lane; i < j; i += 32) hs = ::fma(a.e[i], a.coef[i], hs);
+        for (int i = lane; i < j; i += 32) hs = ::fma(a.e[i], a.coef[off + i], hs);
         hs = warp_sum_f64(hs);
       } else if (lane == 0) {
-        hs = a.e[j - 1] * a.coef[j - 1];
+        hs = a.e[j - 1] * a.coef[off + j - 1];
       }
       if (lane == 0) a.d[j] = (hj - hs) * invnu;
     }
@@ -446,8 +447,8 @@ __device__ void gs_epilogue(const StepArgs &a, const double *res, int mode) {
     for (int i = tid; i <= j; i += blockDim.x) {
       double hs = 0.0;
       const int c0 = (i >= 2) ? 0 : 0;
-      for (int c = c0; c < j; ++c) hs = ::fma(a.H[i + (size_t)c * a.ldh], a.coef[c], hs);
-      const double y = (i < j) ? res[i * NX + 1] : hj;
+      for (int c = c0; c < j; ++c) hs = ::fma(a.H[i + (size_t)c * a.ldh], a.coef[off + c], hs);
+      const double y = (i < j) ? res[(off + i) * NX + 1] : hj;
       Hc[i] = (y - hs) * invnu;
     }
   }

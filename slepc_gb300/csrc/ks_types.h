@@ -80,6 +80,8 @@ struct StepArgs {
   int pstride;       // stride between blocks in part (float2 units)
   KrylovState *st;
   const GTArgs *tc;  // host side: non-null routes IEEE-double Gram-Schmidt to the tensor-core kernels (k_gs_tc.cu)
+  int nc;            // constraint columns (a deflation space) ahead of the basis in V: columns 0..nc-1 take part in
+                     // the projections, and coefficient nc + i belongs to Krylov column i
 };
 
 }  // namespace ksg

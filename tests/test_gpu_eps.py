@@ -651,3 +651,52 @@ def test_graph_segments_match_direct_launches(lib, arith, herm):
         assert got[1] == want[1] and np.array_equal(got[0], want[0])
         replays.append(e.getStats()["graph_segments"])
     assert replays[2] > 0 and replays[2] >= replays[0]
+
+
+@pytest.mark.parametrize("arith", ["f64", "pair"])
+def test_ex11_deflation_space_golden_on_gpu(lib, orc, arith):
+    """ex11.c: the Fiedler vectors of a 10 x 10 mesh's graph Laplacian with the constant vector (its null space) as
+    deflation space (EPSSetDeflationSpace): the eigenvalues ex11_1.out prints, every eigenvector orthogonal to the
+    deflation space, and the oracle's deflated solve at 1e-10; without the space the zero eigenvalue comes first."""
+    g = G["ex11_1"]
+    csr = matgen.graph_laplacian_2d(*g["grid"])
+    n = len(csr[0]) - 1
+    v0 = matgen.start_vector(n, 1)
+    res = run(csr, hermitian=True, which=g["which"], nev=g["nev"], keep=g["keep"], tol=g["tol"], v0=v0, arith=arith,
+              deflation=np.ones(n))
+    assert res["reason"] == 1 and res["nconv"] >= g["nev"]
+    assert [round(float(v), 5) for v in res["eigr"][:g["nev"]]] == g["eigenvalues"]
+    X = res["X"][:, :res["nconv"]]
+    assert np.abs(X.sum(axis=0)).max() < 1e-10 * np.sqrt(n)
+    check_residuals(csr, res, 1e-8)
+    ref = orc.solve(*csr, hermitian=True, which=g["which"], nev=g["nev"], keep=g["keep"], tol=1e-12,
+                    deflation=np.ones(n), v0=v0)
+    tight = run(csr, hermitian=True, which=g["which"], nev=g["nev"], keep=g["keep"], tol=1e-12, v0=v0, arith=arith,
+                deflation=np.ones(n))
+    assert rel_match(tight["eigr"][:g["nev"]], ref.eigr[:ref.nconv], 1e-10)
+    plain = run(csr, hermitian=True, which=g["which"], nev=g["nev"], keep=g["keep"], tol=g["tol"], v0=v0, arith=arith)
+    assert abs(plain["eigr"][0]) < 1e-8
+
+
+def test_deflation_space_of_eigenvectors(lib):
+    """Deflating the three lowest eigenvectors of a 1-D Laplacian (and a dependent fourth vector, which is dropped)
+    leaves the next eigenvalues as the smallest ones found; the eigenvectors are orthogonal to the space. Harmonic
+    extraction and generalised problems refuse a deflation space (PETSC_ERR_SUP)."""
+    n = 400
+    csr = matgen.laplacian_1d(n)
+    exact = np.sort(matgen.laplacian_eigenvalues([n]))
+    k = np.arange(1, n + 1)
+    W = np.stack([np.sin(j * np.pi * k / (n + 1)) for j in (1, 2, 3)], axis=1)  # the three lowest eigenvectors
+    W = np.concatenate([W, (W[:, :1] + 2.0 * W[:, 1:2])], axis=1)
+    res = run(csr, hermitian=True, which="SR", nev=4, ncv=24, tol=1e-10, v0=matgen.start_vector(n, 2), arith="f64",
+              deflation=W)
+    assert res["reason"] == 1 and res["nconv"] >= 4
+    assert np.max(np.abs(np.sort(res["eigr"][:4]) - exact[3:7]) / exact[3:7]) < 1e-10
+    Q, _ = np.linalg.qr(W[:, :3])
+    assert np.abs(Q.T @ res["X"][:, :res["nconv"]]).max() < 1e-10
+    with pytest.raises(sg.SlepcError) as e:
+        run(csr, hermitian=True, which="TM", target=0.1, harmonic=True, nev=2, ncv=20, deflation=W[:, :1])
+    assert e.value.code == 56
+    with pytest.raises(sg.SlepcError) as e:
+        run(csr, hermitian=True, which="SR", nev=2, ncv=20, deflation=W[:, :1], B=matgen.diagonal(np.ones(n) * 2.0))
+    assert e.value.code == 56
