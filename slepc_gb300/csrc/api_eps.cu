@@ -1186,6 +1186,58 @@ extern "C" PetscErrorCode EPSSetFromOptions(EPS eps) {
 //          those of the reference; eigenvectors come back as x = D^-1/2 y.
 //   GNHEP: C = D^-1 A = B^-1 A itself; vectors are unchanged.
 // Each entry of C is a_rc (s_r s_c) with s = D^-1/2, one rounding per product, so C is exactly symmetric when A is.
+// EPS_GNHEP with a non-diagonal B: the operator C = B^-1 A formed on the device (k_dense.cu: P B = L U, then the
+// n solves), held as a CSR matrix of its nonzero entries; the iteration and the eigenvectors are those of C, as the
+// reference's B^-1 A with a direct solve per step.  EPS_GHEP with a non-diagonal B would need the B-inner product
+// and is refused.
+static PetscErrorCode eps_setup_general_b(EPS eps) {
+  const Mat A = eps->A, B = eps->B;
+  const int n = A->m;
+  KSG_CHECK(eps->problem == EPS_GNHEP, PETSC_ERR_SUP,
+            "EPS_GHEP with a non-diagonal B is not provided (EPS_GNHEP is, through B^-1 A)");
+  KSG_CHECK(!B->dense, PETSC_ERR_SUP, "A non-diagonal B must be an AIJ matrix");
+  KSG_CHECK(n <= general_b_max_n(), PETSC_ERR_SUP,
+            "A non-diagonal B is factorised densely on the device: at most %d rows (here %d)", general_b_max_n(), n);
+  KSG_TRY(ksg_mat_upload(A));
+  KSG_TRY(ksg_mat_upload(B));
+  DBuf<double> Bd, Cd;
+  DBuf<int> piv, err;
+  KSG_CUDA(Bd.alloc((size_t)n * n));
+  KSG_CUDA(Cd.alloc((size_t)n * n));
+  KSG_CUDA(piv.alloc(n));
+  KSG_CUDA(err.alloc(1));
+  cudaStream_t s = eps->stream;
+  KSG_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), s));
+  KSG_CUDA(launch_general_b_operator(A->d_rp.p, A->d_ci.p, A->d_va.p, B->d_rp.p, B->d_ci.p, B->d_va.p, n, Bd.p, Cd.p,
+                                     piv.p, err.p, s));
+  std::vector<double> c((size_t)n * n);
+  int herr = 0;
+  KSG_CUDA(cudaMemcpyAsync(c.data(), Cd.p, sizeof(double) * c.size(), cudaMemcpyDeviceToHost, s));
+  KSG_CUDA(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  KSG_CUDA(cudaStreamSynchronize(s));
+  KSG_CHECK(herr == 0, PETSC_ERR_ARG_WRONG, "B is singular (zero pivot in column %d of its LU factorisation)",
+            herr - 1);
+  Mat C = new _p_Mat();
+  C->m = C->n = n;
+  C->own_i.assign(1, 0);
+  for (int r = 0; r < n; ++r) {
+    for (int col = 0; col < n; ++col) {
+      const double v = c[(size_t)r * n + col];
+      if (v != 0.0) {
+        C->own_j.push_back(col);
+        C->own_a.push_back(v);
+      }
+    }
+    C->own_i.push_back((int)C->own_j.size());
+  }
+  C->ai = C->own_i.data();
+  C->aj = C->own_j.data();
+  C->aa = C->own_a.data();
+  C->nnz = (long long)C->own_j.size();
+  eps->op = C;
+  return 0;
+}
+
 static PetscErrorCode eps_setup_operator(EPS eps) {
   eps_drop_operator(eps);
   eps->bdiag.clear();
@@ -1200,21 +1252,22 @@ static PetscErrorCode eps_setup_operator(EPS eps) {
   const int ghep = eps->problem == EPS_GHEP;
   KSG_CHECK(!A->dense, PETSC_ERR_SUP, "Generalised problems need an AIJ matrix A");
   std::vector<double> d(n, 0.0);
+  bool diagonal = true;
   if (B->dense) {
     for (int c = 0; c < n; ++c)
       for (int r = 0; r < n; ++r) {
         const double v = B->data[r + (size_t)c * B->lda];
         if (r == c) d[r] = v;
-        else KSG_CHECK(v == 0.0, PETSC_ERR_SUP, "B must be diagonal on this path (entry (%d,%d) is %g)", r, c, v);
+        else diagonal = diagonal && v == 0.0;
       }
   } else {
     for (int r = 0; r < n; ++r)
       for (int p = B->ai[r]; p < B->ai[r + 1]; ++p) {
         if (B->aj[p] == r) d[r] += B->aa[p];
-        else KSG_CHECK(B->aa[p] == 0.0, PETSC_ERR_SUP, "B must be diagonal on this path (entry (%d,%d) is %g)", r,
-                       (int)B->aj[p], B->aa[p]);
+        else diagonal = diagonal && B->aa[p] == 0.0;
       }
   }
+  if (!diagonal) return eps_setup_general_b(eps);
   std::vector<double> sc(n);
   for (int r = 0; r < n; ++r) {
     if (ghep) {
@@ -2264,10 +2317,26 @@ extern "C" PetscErrorCode EPSComputeError(EPS eps, PetscInt i, EPSErrorType type
     KSG_CUDA(cudaGetLastError());
   }
   const Mat A = eps->A;
-  KSG_CUDA(launch_spmv(A->d_rp.p, A->d_ci.p, A->d_va.p, x, y.p, n, eps->lanes, nullptr, 1.0, s));
-  if (xi) KSG_CUDA(launch_spmv(A->d_rp.p, A->d_ci.p, A->d_va.p, xi, yi.p, n, eps->lanes, nullptr, 1.0, s));
-  k_residual<<<blocks, 256, 0, s>>>(y.p, xi ? yi.p : nullptr, x, xi, gen ? eps->d_bdiag.p : nullptr, kr, ki, n,
-                                    part.p);
+  const int alanes = spmv_lanes_for((double)A->nnz / n);
+  KSG_CUDA(launch_spmv(A->d_rp.p, A->d_ci.p, A->d_va.p, x, y.p, n, alanes, nullptr, 1.0, s));
+  if (xi) KSG_CUDA(launch_spmv(A->d_rp.p, A->d_ci.p, A->d_va.p, xi, yi.p, n, alanes, nullptr, 1.0, s));
+  DBuf<double> bx, bxi;
+  if (gen && eps->bdiag.empty()) {
+    // a non-diagonal B: the residual takes B x (and B xi) from its own product
+    const Mat B = eps->B;
+    KSG_TRY(ksg_mat_upload(B));
+    const int blanes = spmv_lanes_for((double)B->nnz / n);
+    KSG_CUDA(bx.alloc(n));
+    KSG_CUDA(launch_spmv(B->d_rp.p, B->d_ci.p, B->d_va.p, x, bx.p, n, blanes, nullptr, 1.0, s));
+    if (xi) {
+      KSG_CUDA(bxi.alloc(n));
+      KSG_CUDA(launch_spmv(B->d_rp.p, B->d_ci.p, B->d_va.p, xi, bxi.p, n, blanes, nullptr, 1.0, s));
+    }
+    x = bx.p;
+    xi = xi ? bxi.p : nullptr;
+  }
+  k_residual<<<blocks, 256, 0, s>>>(y.p, xi ? yi.p : nullptr, x, xi,
+                                    (gen && !eps->bdiag.empty()) ? eps->d_bdiag.p : nullptr, kr, ki, n, part.p);
   KSG_CUDA(cudaGetLastError());
   std::vector<double> h(3 * blocks);
   KSG_CUDA(cudaMemcpyAsync(h.data(), part.p, sizeof(double) * 3 * blocks, cudaMemcpyDeviceToHost, s));

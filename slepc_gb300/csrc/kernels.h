@@ -151,5 +151,11 @@ int ds_fast_launches();
 // full DS_DO_ALL contract of launch_ds_hep for the Krylov-Schur loop (a.st and a.ctl required)
 cudaError_t launch_ds_hep_fast(const DSArgs &a, const DSFArgs &f, int n_max, cudaStream_t s);
 cudaError_t launch_nhep_vectors(double *T, int ld, int n, double *X, cudaStream_t s);
+// C = B^-1 A for a non-diagonal B (k_dense.cu): Bd and Cd are n x n device scratch (row-major; Cd returns C), piv n
+// ints, *err zeroed by the caller (set to k + 1 at a zero pivot); n <= general_b_max_n()
+cudaError_t launch_general_b_operator(const int *arp, const int *aci, const double *ava, const int *brp,
+                                      const int *bci, const double *bva, int n, double *Bd, double *Cd, int *piv,
+                                      int *err, cudaStream_t s);
+int general_b_max_n();
 
 }  // namespace ksg

@@ -151,3 +151,48 @@ def test_generalised_errors(lib):
     with pytest.raises(sg.SlepcError) as e:
         sg.solve_batch([eps])
     assert e.value.code == PETSC_ERR_SUP
+
+
+def _npz(name):
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", name))
+    return d["rowptr"], d["colidx"], d["vals"]
+
+
+@pytest.mark.parametrize("arith", ["f64", "pair"])
+def test_ex7_general_b_on_gpu(lib, orc, arith):
+    """ex7.c: the GNHEP pencil bfw62a / bfw62b (B symmetric indefinite, not diagonal): C = B^-1 A formed on the
+    device (LU with partial pivoting, then the 62 solves). The golden eigenvalues within the run's tolerance, the
+    oracle's per-step direct solve and scipy's dense generalised solve at tol 1e-12, EPSComputeError's residual
+    ||A x - k B x|| with the user's B; then the pencil (A, A): every eigenvalue 1 (ex7_3.out prints one restart; here
+    C = A^-1 A is the identity up to rounding, and the Krylov space grows out of that rounding, so the restart
+    count may be one or two). A singular B is an error at set-up."""
+    import scipy.linalg as sl
+    g = G["ex7_1"]
+    A, B = _npz("bfw62a.npz"), _npz("bfw62b.npz")
+    v0 = matgen.start_vector(62, 1)
+    res = sg.solve(A, hermitian=False, which=g["which"], nev=g["nev"], tol=g["tol"], B=B, v0=v0, arith=arith)
+    assert res["reason"] == 1 and res["nconv"] >= g["nev"]
+    got = res["eigr"] + 1j * res["eigi"]
+    for a, b in g["eigenvalues"]:
+        z = complex(a, b)
+        assert np.min(np.abs(got - z)) <= 10 * g["tol"] * abs(z) + 1e-5, z
+    tight = sg.solve(A, hermitian=False, which=g["which"], nev=g["nev"], tol=1e-12, B=B, v0=v0, arith=arith)
+    w = sl.eig(matgen.csr_to_dense(*A), matgen.csr_to_dense(*B), right=False)
+    ref = orc.solve(*A, hermitian=False, which=g["which"], nev=g["nev"], tol=1e-12, B=B, v0=v0)
+    refz = np.asarray(ref.eigr[:ref.nconv]) + 1j * np.asarray(ref.eigi[:ref.nconv])
+    for x, y in zip(tight["eigr"][:4], tight["eigi"][:4]):
+        z = complex(x, y)
+        assert np.min(np.abs(w - z)) <= 1e-10 * abs(z)
+        assert np.min(np.abs(refz - z)) <= 1e-10 * abs(z)
+    assert max(tight["errors"][:4]) <= 1e-10
+    g3 = G["ex7_3"]
+    r3 = sg.solve(A, hermitian=False, which=g3["which"], nev=g3["nev"], tol=g3["tol"], B=A, v0=v0, arith=arith)
+    assert r3["reason"] == 1 and r3["its"] <= g3["iterations"] + 1
+    assert [[round(float(x), 5), round(float(y), 5)] for x, y in zip(r3["eigr"][:4], r3["eigi"][:4])] == \
+        g3["eigenvalues"]
+    rp, ci, va = B
+    sing = (rp, ci, va.copy())
+    sing[2][rp[5]:rp[6]] = 0.0  # a zero row: B singular
+    with pytest.raises(sg.SlepcError) as e:
+        sg.solve(A, hermitian=False, which="LM", nev=2, B=sing, v0=v0)
+    assert e.value.code == PETSC_ERR_ARG_WRONG
