@@ -1186,37 +1186,54 @@ extern "C" PetscErrorCode EPSSetFromOptions(EPS eps) {
 //          those of the reference; eigenvectors come back as x = D^-1/2 y.
 //   GNHEP: C = D^-1 A = B^-1 A itself; vectors are unchanged.
 // Each entry of C is a_rc (s_r s_c) with s = D^-1/2, one rounding per product, so C is exactly symmetric when A is.
-// EPS_GNHEP with a non-diagonal B: the operator C = B^-1 A formed on the device (k_dense.cu: P B = L U, then the
-// n solves), held as a CSR matrix of its nonzero entries; the iteration and the eigenvectors are those of C, as the
-// reference's B^-1 A with a direct solve per step.  EPS_GHEP with a non-diagonal B would need the B-inner product
-// and is refused.
+// A non-diagonal B (k_dense.cu), the operator formed once on the device and held as a CSR matrix of its nonzero
+// entries: for EPS_GNHEP C = B^-1 A (P B = L U, then the n solves), whose iteration and eigenvectors are those of
+// the reference's B^-1 A with a direct solve per step; for EPS_GHEP C = L^-1 A L^-T with B = L L^T (the basis holds
+// y = L^T x, and x = L^-T y wherever an eigenvector leaves the solver).
 static PetscErrorCode eps_setup_general_b(EPS eps) {
   const Mat A = eps->A, B = eps->B;
   const int n = A->m;
-  KSG_CHECK(eps->problem == EPS_GNHEP, PETSC_ERR_SUP,
-            "EPS_GHEP with a non-diagonal B is not provided (EPS_GNHEP is, through B^-1 A)");
   KSG_CHECK(!B->dense, PETSC_ERR_SUP, "A non-diagonal B must be an AIJ matrix");
   KSG_CHECK(n <= general_b_max_n(), PETSC_ERR_SUP,
             "A non-diagonal B is factorised densely on the device: at most %d rows (here %d)", general_b_max_n(), n);
   KSG_TRY(ksg_mat_upload(A));
   KSG_TRY(ksg_mat_upload(B));
-  DBuf<double> Bd, Cd;
+  const int ghep = eps->problem == EPS_GHEP;
+  DBuf<double> Bd, Cd, Td;
   DBuf<int> piv, err;
   KSG_CUDA(Bd.alloc((size_t)n * n));
   KSG_CUDA(Cd.alloc((size_t)n * n));
-  KSG_CUDA(piv.alloc(n));
   KSG_CUDA(err.alloc(1));
   cudaStream_t s = eps->stream;
   KSG_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), s));
-  KSG_CUDA(launch_general_b_operator(A->d_rp.p, A->d_ci.p, A->d_va.p, B->d_rp.p, B->d_ci.p, B->d_va.p, n, Bd.p, Cd.p,
-                                     piv.p, err.p, s));
+  if (ghep) {
+    // B = L L^T and C = L^-1 A L^-T: the iteration runs on y = L^T x with the standard inner product, the
+    // B-inner product of the reference in exact arithmetic (the diagonal case's D^1/2 scaling, generalised)
+    KSG_CUDA(Td.alloc((size_t)n * n));
+    KSG_CUDA(launch_general_b_ghep(A->d_rp.p, A->d_ci.p, A->d_va.p, B->d_rp.p, B->d_ci.p, B->d_va.p, n, Bd.p, Cd.p,
+                                   Td.p, err.p, s));
+  } else {
+    KSG_CUDA(piv.alloc(n));
+    KSG_CUDA(launch_general_b_operator(A->d_rp.p, A->d_ci.p, A->d_va.p, B->d_rp.p, B->d_ci.p, B->d_va.p, n, Bd.p,
+                                       Cd.p, piv.p, err.p, s));
+  }
   std::vector<double> c((size_t)n * n);
   int herr = 0;
-  KSG_CUDA(cudaMemcpyAsync(c.data(), Cd.p, sizeof(double) * c.size(), cudaMemcpyDeviceToHost, s));
+  KSG_CUDA(cudaMemcpyAsync(c.data(), ghep ? Td.p : Cd.p, sizeof(double) * c.size(), cudaMemcpyDeviceToHost, s));
   KSG_CUDA(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
   KSG_CUDA(cudaStreamSynchronize(s));
-  KSG_CHECK(herr == 0, PETSC_ERR_ARG_WRONG, "B is singular (zero pivot in column %d of its LU factorisation)",
-            herr - 1);
+  if (ghep)
+    KSG_CHECK(herr == 0, PETSC_ERR_ARG_WRONG, "EPS_GHEP needs a positive definite B (pivot %d of its Cholesky "
+                                              "factorisation is not positive)", herr - 1);
+  else
+    KSG_CHECK(herr == 0, PETSC_ERR_ARG_WRONG, "B is singular (zero pivot in column %d of its LU factorisation)",
+              herr - 1);
+  if (ghep) {
+    eps->d_chol.p = Bd.p;  // keep L
+    eps->d_chol.count = Bd.count;
+    Bd.p = nullptr;
+    Bd.count = 0;
+  }
   Mat C = new _p_Mat();
   C->m = C->n = n;
   C->own_i.assign(1, 0);
@@ -1243,6 +1260,7 @@ static PetscErrorCode eps_setup_operator(EPS eps) {
   eps->bdiag.clear();
   eps->d_bdiag.release();
   eps->d_bisqrt.release();
+  eps->d_chol.release();
   if (!eps->B) {
     eps->op = eps->A;
     return 0;
@@ -1693,6 +1711,19 @@ PetscErrorCode ksg_eps_put_start(EPS eps, cudaStream_t s) {
   if (!eps->v0_internal.empty()) src = eps->v0_internal.data();  // the precision form's refinement sweep
   else if (!eps->v0.empty()) {
     src = eps->v0.data();
+    if (eps->problem == EPS_GHEP && eps->B && eps->d_chol.p) {
+      // y0 = L^T v0 on the device, then into the range of the operator
+      const int n = eps->n;
+      DBuf<double> x, y;
+      KSG_CUDA(x.alloc(n));
+      KSG_CUDA(y.alloc(n));
+      KSG_CUDA(cudaMemcpyAsync(x.p, eps->v0.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
+      KSG_CUDA(launch_lt_mv(eps->d_chol.p, x.p, y.p, n, s));
+      KSG_CUDA(eps_f64_to_column(eps, y.p, 0, s));
+      KSG_CUDA(cudaStreamSynchronize(s));
+      KSG_TRY(eps_apply_op_column(eps, 0, s));
+      return 0;
+    }
     if (eps->problem == EPS_GHEP && eps->B) {
       h.resize(eps->n);
       for (int r = 0; r < eps->n; ++r) h[r] = eps->v0[r] * sqrt(eps->bdiag[r]);
@@ -2207,8 +2238,18 @@ extern "C" PetscErrorCode EPSGetEigenvector(EPS eps, PetscInt i, Vec Vr, Vec Vi)
     if (Vr) KSG_TRY(ksg_get_column(Vr->a, col, n, sto, eps->stream));
     if (Vi) memset(Vi->a, 0, bytes);
   }
-  if (Vr && eps->B && eps->problem == EPS_GHEP)  // the basis holds y = D^1/2 x
-    for (int r = 0; r < n; ++r) Vr->a[r] *= 1.0 / sqrt(eps->bdiag[r]);
+  if (Vr && eps->B && eps->problem == EPS_GHEP) {
+    if (eps->d_chol.p) {  // the basis holds y = L^T x: x = L^-T y on the device
+      DBuf<double> t;
+      KSG_CUDA(t.alloc(n));
+      KSG_CUDA(cudaMemcpyAsync(t.p, Vr->a, bytes, cudaMemcpyHostToDevice, eps->stream));
+      KSG_CUDA(launch_lt_solve(eps->d_chol.p, t.p, n, 1, n, eps->stream));
+      KSG_CUDA(cudaMemcpyAsync(Vr->a, t.p, bytes, cudaMemcpyDeviceToHost, eps->stream));
+      KSG_CUDA(cudaStreamSynchronize(eps->stream));
+    } else {  // the basis holds y = D^1/2 x
+      for (int r = 0; r < n; ++r) Vr->a[r] *= 1.0 / sqrt(eps->bdiag[r]);
+    }
+  }
   return 0;
 }
 extern "C" PetscErrorCode EPSGetEigenpair(EPS eps, PetscInt i, PetscScalar *eigr, PetscScalar *eigi, Vec Vr, Vec Vi) {
@@ -2313,15 +2354,29 @@ extern "C" PetscErrorCode EPSComputeError(EPS eps, PetscInt i, EPSErrorType type
     x = xd.p;
   }
   if (ghep) {  // eigenvalues of EPS_GHEP are real: no xi
-    k_diag_mul<<<blocks, 256, 0, s>>>(xd.p, eps->d_bisqrt.p, n);
-    KSG_CUDA(cudaGetLastError());
+    if (eps->d_chol.p) {
+      KSG_CUDA(launch_lt_solve(eps->d_chol.p, xd.p, n, 1, n, s));  // x = L^-T y
+    } else {
+      k_diag_mul<<<blocks, 256, 0, s>>>(xd.p, eps->d_bisqrt.p, n);
+      KSG_CUDA(cudaGetLastError());
+    }
   }
   const Mat A = eps->A;
   const int alanes = spmv_lanes_for((double)A->nnz / n);
   KSG_CUDA(launch_spmv(A->d_rp.p, A->d_ci.p, A->d_va.p, x, y.p, n, alanes, nullptr, 1.0, s));
   if (xi) KSG_CUDA(launch_spmv(A->d_rp.p, A->d_ci.p, A->d_va.p, xi, yi.p, n, alanes, nullptr, 1.0, s));
   DBuf<double> bx, bxi;
+  double xnorm2 = -1.0;  // ||x||^2 when the residual kernel receives B x instead of x
   if (gen && eps->bdiag.empty()) {
+    if (ghep) {
+      k_residual<<<blocks, 256, 0, s>>>(x, nullptr, x, nullptr, nullptr, 0.0, 0.0, n, part.p);
+      KSG_CUDA(cudaGetLastError());
+      std::vector<double> hp(3 * blocks);
+      KSG_CUDA(cudaMemcpyAsync(hp.data(), part.p, sizeof(double) * 3 * blocks, cudaMemcpyDeviceToHost, s));
+      KSG_CUDA(cudaStreamSynchronize(s));
+      xnorm2 = 0.0;
+      for (int b = 0; b < blocks; ++b) xnorm2 += hp[3 * b];
+    }
     // a non-diagonal B: the residual takes B x (and B xi) from its own product
     const Mat B = eps->B;
     KSG_TRY(ksg_mat_upload(B));
@@ -2349,7 +2404,7 @@ extern "C" PetscErrorCode EPSComputeError(EPS eps, PetscInt i, EPSErrorType type
   }
   double nrm = xi ? hypot(sqrt(s0), sqrt(s1)) : sqrt(s0);
   const double lam = hypot(kr, ki);
-  const double vecnorm = ghep ? sqrt(s2) : 1.0;  // epssolve.c:767
+  const double vecnorm = ghep ? sqrt(xnorm2 >= 0.0 ? xnorm2 : s2) : 1.0;  // epssolve.c:767
   switch (type) {
     case EPS_ERROR_ABSOLUTE: break;
     case EPS_ERROR_RELATIVE: nrm /= lam * vecnorm; break;
@@ -2415,6 +2470,8 @@ extern "C" PetscErrorCode EPSGB300GetDeviceEigenvectors(EPS eps, const double **
       k_gather_eigvecs<<<grid, 256, 0, eps->stream>>>(eps_basis(eps), eps->ldv, eps->storage, eps->d_perm.p, bis, n, m,
                                                       eps->xvec.p, ldx);
       KSG_CUDA(cudaGetLastError());
+      if (eps->B && eps->problem == EPS_GHEP && eps->d_chol.p)  // x = L^-T y for every column
+        KSG_CUDA(launch_lt_solve(eps->d_chol.p, eps->xvec.p, n, m, ldx, eps->stream));
       KSG_CUDA(cudaStreamSynchronize(eps->stream));
     }
     eps->xvec_valid = 1;

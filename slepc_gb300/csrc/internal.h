@@ -184,6 +184,7 @@ struct _p_EPS {
   Mat op = nullptr;
   std::vector<double> bdiag;       // the diagonal of B (generalised problems)
   DBuf<double> d_bdiag, d_bisqrt;  // device copies of diag(B) and diag(B)^-1/2
+  DBuf<double> d_chol;             // EPS_GHEP with a non-diagonal B = L L^T: L (row-major, lower); the basis holds L^T x
   double nrma = 0.0, nrmb = 0.0;   // infinity norms for EPS_CONV_NORM (nrmb stays 0 for standard problems)
   long long a_state = -1, b_state = -1;  // the matrices' states at EPSSetUp
   int lanes = 8;

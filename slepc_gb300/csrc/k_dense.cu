@@ -109,6 +109,116 @@ __global__ void k_lu_solve_cols(const double *__restrict__ LU, const int *__rest
   }
 }
 
+// B = L L^T in place (row-major, L in the lower triangle); *err = k + 1 when the k-th pivot is not positive (B not
+// positive definite)
+__global__ void __launch_bounds__(DN_THREADS) k_chol_rm(double *__restrict__ B, int n, int *__restrict__ err) {
+  __shared__ double s_d;
+  const int tid = threadIdx.x;
+  for (int k = 0; k < n; ++k) {
+    if (tid == 0) {
+      const double p = B[(size_t)k * n + k];
+      s_d = (p > 0.0) ? sqrt(p) : -1.0;
+      if (s_d < 0.0 && *err == 0) *err = k + 1;
+    }
+    __syncthreads();
+    const double dk = s_d;
+    if (dk < 0.0) return;
+    if (tid == 0) B[(size_t)k * n + k] = dk;
+    const double inv = 1.0 / dk;
+    for (int i = k + 1 + tid; i < n; i += DN_THREADS) B[(size_t)i * n + k] *= inv;
+    __syncthreads();
+    // the trailing lower triangle: B(i, c) -= L(i, k) L(c, k), k < c <= i
+    const int m = n - k - 1;
+    for (long long t = tid; t < (long long)m * m; t += DN_THREADS) {
+      const int i = k + 1 + (int)(t / m), c = k + 1 + (int)(t % m);
+      if (c <= i) B[(size_t)i * n + c] = fma(-B[(size_t)i * n + k], B[(size_t)c * n + k], B[(size_t)i * n + c]);
+    }
+    __syncthreads();
+  }
+}
+
+// X <- L^-1 X (L lower, row-major): thread c solves column c of the row-major n x m X
+__global__ void k_lower_solve_cols(const double *__restrict__ L, double *__restrict__ X, int n, int m,
+                                   const int *__restrict__ err) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m || *err) return;
+  for (int i = 0; i < n; ++i) {
+    double s = X[(size_t)i * m + c];
+    const double *l = L + (size_t)i * n;
+    for (int j = 0; j < i; ++j) s = fma(-l[j], X[(size_t)j * m + c], s);
+    X[(size_t)i * m + c] = s / l[i];
+  }
+}
+
+__global__ void k_transpose_sq(const double *__restrict__ X, double *__restrict__ Y, int n) {
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < (long long)n * n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(t / n), j = (int)(t % n);
+    Y[(size_t)j * n + i] = X[t];
+  }
+}
+
+// C <- (C + C^T) / 2: the operator of a symmetric pencil exactly symmetric
+__global__ void k_symmetrize_sq(double *__restrict__ C, int n) {
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < (long long)n * n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(t / n), j = (int)(t % n);
+    if (j > i) {
+      const double v = 0.5 * (C[t] + C[(size_t)j * n + i]);
+      C[t] = v;
+      C[(size_t)j * n + i] = v;
+    }
+  }
+}
+
+// y = L^T x (L lower, row-major): thread i sums L(j, i) x_j over j >= i
+__global__ void k_lt_mv(const double *__restrict__ L, const double *__restrict__ x, double *__restrict__ y, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int j = i; j < n; ++j) s = fma(L[(size_t)j * n + i], x[j], s);
+    y[i] = s;
+  }
+}
+
+// X <- L^-T X for m column-major right-hand sides (leading dimension ldx): thread c back-substitutes column c
+__global__ void k_lt_solve_cols_cm(const double *__restrict__ L, double *__restrict__ X, int n, int m, long long ldx) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m) return;
+  double *x = X + (size_t)c * ldx;
+  for (int i = n - 1; i >= 0; --i) {
+    double s = x[i];
+    for (int j = i + 1; j < n; ++j) s = fma(-L[(size_t)j * n + i], x[j], s);
+    x[i] = s / L[(size_t)i * n + i];
+  }
+}
+
+cudaError_t launch_general_b_ghep(const int *arp, const int *aci, const double *ava, const int *brp, const int *bci,
+                                  const double *bva, int n, double *Ld, double *Cd, double *Td, int *err,
+                                  cudaStream_t s) {
+  if (n <= 0 || n > general_b_max_n()) return cudaErrorInvalidValue;
+  const int g = n < 1024 ? n : 1024;
+  const int gs = (int)(((long long)n * n + 255) / 256 < 4096 ? ((long long)n * n + 255) / 256 : 4096);
+  k_csr_to_dense_rm<<<g, 256, 0, s>>>(brp, bci, bva, n, Ld);
+  k_csr_to_dense_rm<<<g, 256, 0, s>>>(arp, aci, ava, n, Cd);
+  k_chol_rm<<<1, DN_THREADS, 0, s>>>(Ld, n, err);
+  k_lower_solve_cols<<<(n + 127) / 128, 128, 0, s>>>(Ld, Cd, n, n, err);  // L^-1 A
+  k_transpose_sq<<<gs, 256, 0, s>>>(Cd, Td, n);                           // (L^-1 A)^T = A L^-T
+  k_lower_solve_cols<<<(n + 127) / 128, 128, 0, s>>>(Ld, Td, n, n, err);  // L^-1 A L^-T (A symmetric)
+  k_symmetrize_sq<<<gs, 256, 0, s>>>(Td, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lt_mv(const double *L, const double *x, double *y, int n, cudaStream_t s) {
+  k_lt_mv<<<(n + 127) / 128, 128, 0, s>>>(L, x, y, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lt_solve(const double *L, double *X, int n, int m, long long ldx, cudaStream_t s) {
+  if (m <= 0) return cudaSuccess;
+  k_lt_solve_cols_cm<<<(m + 127) / 128, 128, 0, s>>>(L, X, n, m, ldx);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_general_b_operator(const int *arp, const int *aci, const double *ava, const int *brp,
                                       const int *bci, const double *bva, int n, double *Bd, double *Cd, int *piv,
                                       int *err, cudaStream_t s) {

@@ -157,5 +157,13 @@ cudaError_t launch_general_b_operator(const int *arp, const int *aci, const doub
                                       const int *bci, const double *bva, int n, double *Bd, double *Cd, int *piv,
                                       int *err, cudaStream_t s);
 int general_b_max_n();
+// EPS_GHEP with a non-diagonal B = L L^T: Ld returns L (row-major, lower), Td returns C = L^-1 A L^-T (row-major,
+// symmetric); Cd is scratch; *err = k + 1 when B is not positive definite
+cudaError_t launch_general_b_ghep(const int *arp, const int *aci, const double *ava, const int *brp, const int *bci,
+                                  const double *bva, int n, double *Ld, double *Cd, double *Td, int *err,
+                                  cudaStream_t s);
+cudaError_t launch_lt_mv(const double *L, const double *x, double *y, int n, cudaStream_t s);  // y = L^T x
+// X <- L^-T X for m column-major vectors of leading dimension ldx (x = L^-T y: the eigenvectors of the pencil)
+cudaError_t launch_lt_solve(const double *L, double *X, int n, int m, long long ldx, cudaStream_t s);
 
 }  // namespace ksg

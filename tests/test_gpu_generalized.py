@@ -127,15 +127,24 @@ def test_convergence_tests_match_oracle(lib, orc, conv):
 
 
 def test_generalised_errors(lib):
-    """Non-diagonal B, an indefinite B for EPS_GHEP, and the batched engine with B: errors, not solves."""
+    """A non-diagonal B that is not positive definite for EPS_GHEP, a non-diagonal B above the dense size limit, an
+    indefinite diagonal B for EPS_GHEP, and the batched engine with B: errors, not solves."""
     csr = matgen.laplacian_1d(50)
     eps, A, B = ghep_eps(csr, np.ones(50))
     eps.setDimensions(2)
     eps.destroy()
-    nondiag = sg.Mat(*matgen.laplacian_1d(50))
+    rp, ci, va = matgen.laplacian_1d(50)
+    nondiag = sg.Mat(rp, ci, -va)  # negative definite
     eps = sg.EPS().create()
     eps.setOperators(sg.Mat(*csr), nondiag)
     eps.setProblemType(sg.EPS.ProblemType.GHEP)
+    with pytest.raises(sg.SlepcError) as e:
+        eps.setUp()
+    assert e.value.code == PETSC_ERR_ARG_WRONG
+    big = matgen.laplacian_1d(3000)
+    eps = sg.EPS().create()
+    eps.setOperators(sg.Mat(*big), sg.Mat(*big))
+    eps.setProblemType(sg.EPS.ProblemType.GNHEP)
     with pytest.raises(sg.SlepcError) as e:
         eps.setUp()
     assert e.value.code == PETSC_ERR_SUP
@@ -196,3 +205,37 @@ def test_ex7_general_b_on_gpu(lib, orc, arith):
     with pytest.raises(sg.SlepcError) as e:
         sg.solve(A, hermitian=False, which="LM", nev=2, B=sing, v0=v0)
     assert e.value.code == PETSC_ERR_ARG_WRONG
+
+
+def test_ghep_general_b_on_gpu(lib, orc):
+    """EPS_GHEP with a non-diagonal SPD B (a tridiagonal mass matrix): B = L L^T on the device and C = L^-1 A L^-T,
+    against scipy.linalg.eigh(A, B) and the oracle's B-inner-product Lanczos, B-orthonormal purified eigenvectors
+    (both ends of the spectrum), EPSComputeError with the user's B, and the device eigenvector array."""
+    import scipy.linalg as sl
+    m = 12
+    csr = matgen.laplacian_2d(m, m)
+    n = m * m
+    rp, ci, va = [0], [], []
+    for r in range(n):
+        for c, v in ((r - 1, 1.0), (r, 4.0), (r + 1, 1.0)):
+            if 0 <= c < n:
+                ci.append(c)
+                va.append(v / 6.0)
+        rp.append(len(ci))
+    Bc = (np.array(rp, np.int32), np.array(ci, np.int32), np.array(va))
+    Bd = matgen.csr_to_dense(*Bc)
+    w = sl.eigh(matgen.csr_to_dense(*csr), Bd, eigvals_only=True)
+    v0 = matgen.start_vector(n, 3)
+    for which, arith in (("LR", "f64"), ("SR", "f64"), ("LR", "pair")):
+        res = sg.solve(csr, hermitian=True, which=which, nev=5, tol=1e-12, B=Bc, v0=v0, arith=arith)
+        assert res["reason"] == 1 and res["nconv"] >= 5
+        for lam in res["eigr"][:5]:
+            assert np.min(np.abs(w - lam)) <= 1e-10 * abs(lam)
+        ref = orc.solve(*csr, hermitian=True, which=which, nev=5, tol=1e-12, B=Bc, v0=v0)
+        for lam in ref.eigr[:5]:
+            assert np.min(np.abs(res["eigr"][:res["nconv"]] - lam)) <= 1e-10 * abs(lam)
+        X = res["X"][:, :res["nconv"]]
+        assert np.abs(X.T @ Bd @ X - np.eye(res["nconv"])).max() < 1e-10
+        assert max(res["errors"][:5]) <= 1e-10
+        Xd = res["eps"].copyDeviceEigenvectors()
+        assert np.allclose(Xd[:, :res["nconv"]], X, rtol=0, atol=1e-13)
