@@ -133,7 +133,8 @@ PetscErrorCode EPSGB300GetDeviceBasis(EPS eps, const double **V, PetscInt *ld);
  * reference (whose unit of work is one EPSSolve, krylovschur.c:227-337); each problem runs the same algorithm.
  * The batch advances one Krylov step of every unconverged problem per kernel launch and runs a restart cycle of all
  * of them as one CUDA graph; a problem's arithmetic depends only on the problem, so its results are the same in
- * any batch, including a batch of one.  Requirements: pair arithmetic (the default), ncv <= 79, one device.
+ * any batch, including a batch of one.  Requirements: pair arithmetic (the default), ncv <= 143, one device,
+ * standard problems with Ritz extraction and no deflation space.
  * The symmetric projected problems use the FP64 QR solver (EPS_GB300_DS_QR). */
 PetscErrorCode EPSGB300SolveBatch(PetscInt count, EPS *eps);
 
@@ -146,7 +147,7 @@ PetscErrorCode EPSGB300SolveBatch(PetscInt count, EPS *eps);
  * the usual EPSGet* calls read them and EPSGB300GetStats' solve_seconds is the latency from submission to result.
  * The client must not touch a submitted EPS until Wait reports it done.  Results do not depend on what else is
  * served at the same time.  max_requests bounds the solves admitted at once, max_ncv the ncv of any request
- * (<= 79).  Destroy waits for every submitted request.  No counterpart in the reference. */
+ * (<= 143).  Destroy waits for every submitted request.  No counterpart in the reference. */
 typedef struct _p_EPSGB300Server *EPSGB300Server;
 typedef struct {
   long long submitted, completed, failed, queued, live, max_live, cycles;
