@@ -12,6 +12,7 @@ from slepc_gb300 import matgen
 P = ctypes.c_void_p
 PETSC_ERR_SUP, PETSC_ERR_ARG_WRONG, PETSC_ERR_ARG_OUTOFRANGE = 56, 62, 63
 PETSC_ERR_ARG_WRONGSTATE, PETSC_ERR_ARG_INCOMP, PETSC_ERR_ARG_NULL = 73, 75, 85
+PETSC_ERR_ARG_SIZ = 60
 
 
 @pytest.fixture(scope="module")
@@ -116,3 +117,30 @@ def test_balance_settings(lib):
         eps.destroy()
     finally:
         sg.initialize(["prog"])
+
+
+def test_gb300_setting_checks(lib):
+    """The GB300 settings' argument checks: graph-capture mode, projected-solver method (the adaptive default among
+    them), and EPSSetDeflationSpace (negative count, a null vector, vectors of different lengths); none needs the
+    device."""
+    eps = sg.EPS().create()
+    lib.EPSGB300SetGraphCapture.argtypes = [P, ctypes.c_int]
+    assert lib.EPSGB300SetGraphCapture(eps.handle, 2) == PETSC_ERR_ARG_OUTOFRANGE
+    for mode in (-1, 0, 1):
+        assert lib.EPSGB300SetGraphCapture(eps.handle, mode) == 0
+    lib.EPSGB300SetProjectedSolver.argtypes = [P, ctypes.c_int]
+    lib.EPSGB300GetProjectedSolver.argtypes = [P, P]
+    m = ctypes.c_int(-1)
+    assert lib.EPSGB300GetProjectedSolver(eps.handle, ctypes.byref(m)) == 0 and m.value == 2  # EPS_GB300_DS_AUTO
+    assert lib.EPSGB300SetProjectedSolver(eps.handle, 3) == PETSC_ERR_ARG_OUTOFRANGE
+    for meth in ("qr", "refined", "auto"):
+        eps.setProjectedSolver(meth)
+    lib.EPSSetDeflationSpace.argtypes = [P, ctypes.c_int, P]
+    assert lib.EPSSetDeflationSpace(eps.handle, -1, None) == PETSC_ERR_ARG_OUTOFRANGE
+    assert lib.EPSSetDeflationSpace(eps.handle, 1, None) == PETSC_ERR_ARG_NULL
+    v1, v2 = sg.Vec(np.ones(10)), sg.Vec(np.ones(12))
+    arr = (P * 2)(v1.handle.value, v2.handle.value)
+    assert lib.EPSSetDeflationSpace(eps.handle, 2, arr) == PETSC_ERR_ARG_SIZ
+    eps.setDeflationSpace([np.ones(10), np.arange(10.0)])  # accepted; orthonormalised at set-up
+    assert lib.EPSSetDeflationSpace(eps.handle, 0, None) == 0  # an empty space clears it
+    eps.destroy()
