@@ -580,8 +580,9 @@ def main():
                          "it); f32: the precision form")
     ap.add_argument("--restart", default="tensor", choices=["tensor", "pair", "mma_sync", "tcgen05"],
                     help="kernel of the thick restart (EPSGB300SetRestartMethod)")
-    ap.add_argument("--gs", default="fma", choices=["tensor", "fma"],
-                    help="Gram-Schmidt of the f64 arithmetic: exact slice products on the tensor cores, or FP64 FMA")
+    ap.add_argument("--gs", default="fma", choices=["tensor", "fma", "integer"],
+                    help="Gram-Schmidt of the f64 arithmetic: FP64 FMA, or exact products on the tensor cores or the "
+                         "integer pipes")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-parity", action="store_true", help="skip the host-side parity block")

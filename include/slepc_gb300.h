@@ -52,10 +52,14 @@ typedef enum { EPS_GB300_DS_REFINED = 0, EPS_GB300_DS_QR = 1, EPS_GB300_DS_AUTO 
  *       error-free split of each value's 55/56-bit fixed point, against its column/tile exponent, into byte or
  *       7-bit slices), the slice sums recombined as exact integers, rounded once per chunk of at most 512 rows and
  *       accumulated in double-double: more accurate than FP64 FMA.  On the 128^3 Laplacian it is still slower
- *       than the FMA kernels (the slicing on the CUDA cores bounds it).  Used for the symmetric (Lanczos) variant
- *       with the tcgen05 restart; the other cases use the FMA kernels.
- * Option -eps_gb300_gs tensor|fma. */
-typedef enum { EPS_GB300_GS_TENSOR = 0, EPS_GB300_GS_FMA = 1 } EPSGB300GSMethod;
+ *       than the FMA kernels (the slicing on the CUDA cores bounds it).
+ *   EPS_GB300_GS_INTEGER: every product exact on the integer pipes (each value's 54-bit fixed point against its
+ *       column/tile exponent as two 27-bit halves, four 32 x 32 -> 64-bit multiply-adds per product, exact 64- and
+ *       128-bit integer sums), rounded once per row (update half) or per thread's share of a column (dot half) and
+ *       merged in double-double: as accurate as the tensor form, without the FP64 pipe's bound.
+ * The exact forms are used for the symmetric (Lanczos) variant with the tcgen05 restart and no deflation space; the
+ * other cases use the FMA kernels.  Option -eps_gb300_gs tensor|fma|integer. */
+typedef enum { EPS_GB300_GS_TENSOR = 0, EPS_GB300_GS_FMA = 1, EPS_GB300_GS_INTEGER = 2 } EPSGB300GSMethod;
 PetscErrorCode EPSGB300SetGSMethod(EPS eps, EPSGB300GSMethod method);
 PetscErrorCode EPSGB300GetGSMethod(EPS eps, EPSGB300GSMethod *method);
 PetscErrorCode EPSGB300SetProjectedSolver(EPS eps, EPSGB300DSMethod method);
@@ -105,6 +109,8 @@ typedef struct {
   long long ds_fallbacks;       /* restarts whose mixed-precision projected solve failed its accuracy check and was
                                    redone by the FP64 QR solver */
   long long graph_segments;     /* factorisation segments replayed from captured CUDA graphs */
+  long long gs_exact;           /* 1 when the Gram-Schmidt pair ran with exact products (EPS_GB300_GS_TENSOR or
+                                   EPS_GB300_GS_INTEGER took effect), else 0 */
 } EPSGB300Stats;
 PetscErrorCode EPSGB300GetStats(EPS eps, EPSGB300Stats *stats);
 

@@ -446,10 +446,13 @@ class EPS:
         tensor-core kernel explicitly: 'mma_sync' or 'tcgen05' (bit-identical results)."""
         _check(load().EPSGB300SetRestartMethod(self.handle, self.RESTART_METHODS[method]), "EPSGB300SetRestartMethod")
 
+    GS_METHODS = {"tensor": 0, "fma": 1, "integer": 2}
+
     def setGSMethod(self, method):
-        """'fma' (IEEE FP64 FMA, the default) or 'tensor' (exact slice products on the tensor cores) for the
-        Gram-Schmidt pair of IEEE-double storage (EPSGB300SetGSMethod)."""
-        _check(load().EPSGB300SetGSMethod(self.handle, 1 if method == "fma" else 0), "EPSGB300SetGSMethod")
+        """'fma' (IEEE FP64 FMA, the default), 'tensor' (exact slice products on the tensor cores) or 'integer'
+        (exact products on the integer pipes) for the Gram-Schmidt pair of IEEE-double storage
+        (EPSGB300SetGSMethod)."""
+        _check(load().EPSGB300SetGSMethod(self.handle, self.GS_METHODS[method]), "EPSGB300SetGSMethod")
 
     def setTimeLimit(self, seconds):
         """Wall-time budget of EPSSolve (checked after each restart; 0 = none)."""
@@ -561,17 +564,18 @@ class EPS:
         return self._view("EPSView", (), path, False)
 
     def getStats(self):
-        buf = (ctypes.c_char * 88)()
+        buf = (ctypes.c_char * 96)()
         _check(load().EPSGB300GetStats(self.handle, buf), "EPSGB300GetStats")
         steps, restarts = np.frombuffer(bytes(buf[:16]), dtype=np.int64)
         solve_s, bytes_moved, setup_s = np.frombuffer(bytes(buf[16:40]), dtype=np.float64)
         launches = np.frombuffer(bytes(buf[40:48]), dtype=np.int64)[0]
         dev_ms = np.frombuffer(bytes(buf[48:56]), dtype=np.float64)[0]
-        psteps, prestarts, dsfb, graphs = np.frombuffer(bytes(buf[56:88]), dtype=np.int64)
+        psteps, prestarts, dsfb, graphs, gs_exact = np.frombuffer(bytes(buf[56:96]), dtype=np.int64)
         return {"krylov_steps": int(steps), "restarts": int(restarts), "solve_seconds": float(solve_s),
                 "bytes_moved": float(bytes_moved), "setup_seconds": float(setup_s), "kernel_launches": int(launches),
                 "solve_device_ms": float(dev_ms), "precision_steps": int(psteps),
-                "precision_restarts": int(prestarts), "ds_fallbacks": int(dsfb), "graph_segments": int(graphs)}
+                "precision_restarts": int(prestarts), "ds_fallbacks": int(dsfb), "graph_segments": int(graphs),
+                "gs_exact": int(gs_exact)}
 
     KERNEL_CLASSES = ("spmv", "gs_dot", "gs_update", "restart", "ds")
 

@@ -1001,8 +1001,8 @@ extern "C" PetscErrorCode EPSGB300GetProjectedSolver(EPS eps, EPSGB300DSMethod *
 }
 extern "C" PetscErrorCode EPSGB300SetGSMethod(EPS eps, EPSGB300GSMethod method) {
   KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
-  KSG_CHECK(method == EPS_GB300_GS_TENSOR || method == EPS_GB300_GS_FMA, PETSC_ERR_ARG_OUTOFRANGE,
-            "Unknown Gram-Schmidt method");
+  KSG_CHECK(method == EPS_GB300_GS_TENSOR || method == EPS_GB300_GS_FMA || method == EPS_GB300_GS_INTEGER,
+            PETSC_ERR_ARG_OUTOFRANGE, "Unknown Gram-Schmidt method");
   eps->gs_method = method;
   return 0;
 }
@@ -1170,7 +1170,9 @@ extern "C" PetscErrorCode EPSSetFromOptions(EPS eps) {
                                                : !strcmp(v, "refined") ? EPS_GB300_DS_REFINED
                                                                        : EPS_GB300_DS_AUTO));
     else if (!strcmp(o, "-eps_gb300_gs") && v)
-      KSG_TRY(EPSGB300SetGSMethod(eps, !strcmp(v, "fma") ? EPS_GB300_GS_FMA : EPS_GB300_GS_TENSOR));
+      KSG_TRY(EPSGB300SetGSMethod(eps, !strcmp(v, "fma")       ? EPS_GB300_GS_FMA
+                                       : !strcmp(v, "integer") ? EPS_GB300_GS_INTEGER
+                                                               : EPS_GB300_GS_TENSOR));
     else if (!strcmp(o, "-eps_gb300_graphs") && v)
       KSG_TRY(EPSGB300SetGraphCapture(eps, atoi(v)));
   }
@@ -1905,13 +1907,16 @@ static PetscErrorCode eps_solve_core(EPS eps, double tol, std::chrono::steady_cl
   const int n = eps->n, ld = eps->ld, ncv = eps->ncv_e, mpd = eps->mpd_e, nev = eps->nev_e;
   const int herm = ksg_eps_lanczos(eps);
   const int harmonic = eps->extraction == EPS_HARMONIC;
-  // IEEE-double Gram-Schmidt on the tensor cores: the symmetric (Lanczos) variant with the tcgen05 restart, whose
-  // kernels and this one keep the basis columns' exponent table up to date
+  // IEEE-double Gram-Schmidt with exact products (tensor cores or integer pipes): the symmetric (Lanczos) variant
+  // with the tcgen05 restart, whose kernels and these keep the basis columns' exponent table up to date
   {
     const int rm = eps->restart_method;
-    eps->gs_tc_on = eps->storage == STORE_F64 && eps->arith == ARITH_F64 && eps->gs_method == EPS_GB300_GS_TENSOR &&
-                    herm && eps->vexp.p && ld <= gs_tc_max_columns() && ncv < n && eps->nc == 0 &&
+    const int exact = eps->gs_method == EPS_GB300_GS_TENSOR || eps->gs_method == EPS_GB300_GS_INTEGER;
+    eps->gs_tc_on = eps->storage == STORE_F64 && eps->arith == ARITH_F64 && exact && herm && eps->vexp.p &&
+                    ld <= gs_tc_max_columns() && ncv < n && eps->nc == 0 &&
                     (rm == EPS_GB300_RESTART_TCGEN05 || (rm == EPS_GB300_RESTART_TENSOR && kRestartTensorIsTcgen05));
+    eps->gt.integer = eps->gs_method == EPS_GB300_GS_INTEGER;
+    if (eps->gs_tc_on) eps->stats.gs_exact = 1;
     if (eps->gs_tc_on) KSG_CUDA(cudaMemsetAsync(eps->gterr.p, 0, sizeof(int), s));
   }
   // start vector: the initial space, or a random vector (EPSGetStartVector, epssolve.c:841-873)
@@ -2101,6 +2106,7 @@ extern "C" PetscErrorCode EPSSolve(EPS eps) {
   eps->stats.restarts = 0;
   eps->stats.ds_fallbacks = 0;
   eps->stats.graph_segments = 0;
+  eps->stats.gs_exact = 0;
   eps->stats.bytes_moved = 0.0;
   eps->stats.kernel_launches = 0;
   eps->stats.precision_steps = 0;
@@ -2168,7 +2174,7 @@ extern "C" PetscErrorCode EPSSolve(EPS eps) {
     KSG_CUDA(cudaMemcpy(&flag, eps->gterr.p, sizeof(int), cudaMemcpyDeviceToHost));
     KSG_CHECK(flag != 1, PETSC_ERR_GPU, "tensor-core Gram-Schmidt: a bounded wait ran out; results are not valid");
     KSG_CHECK(flag != 2, PETSC_ERR_PLIB,
-              "tensor-core Gram-Schmidt: a basis value exceeded its recorded exponent; results are not valid");
+              "exact-product Gram-Schmidt: a basis value exceeded its recorded exponent; results are not valid");
   }
   {
     float ms = 0.0f;

@@ -46,6 +46,7 @@
 #include <type_traits>
 
 #include "common.cuh"
+#include "gs_fixed.cuh"
 #include "kernels.h"
 #include "krylov_body.cuh"
 #include "ks_types.h"
@@ -232,23 +233,6 @@ KS_DEVICE void gt_slice8h(const double *v, int e, uint4 *out, int *ovf) {
   }
 }
 
-// scale exponent of a value: |v| < 2^(E - 1022) for its biased exponent E >= 1; recorded in [-127, 127], -128 for zero
-KS_DEVICE int gt_expo(double v) { return (int)(((unsigned long long)__double_as_longlong(v) >> 52) & 0x7FF); }
-KS_DEVICE int gt_escale(int Emax) {
-  if (Emax == 0) return -128;
-  const int e = Emax - 1022;
-  return e < -127 ? -127 : (e > 127 ? 127 : e);
-}
-
-// 2^k as a double over the whole exponent range used here (|k| < 1100)
-KS_DEVICE double gt_pow2(int k) { return t5_pow2(k); }
-
-// 128-bit two's complement (hi, lo) helpers
-KS_DEVICE void gt_add128(long long &hi, unsigned long long &lo, long long bhi, unsigned long long blo) {
-  const unsigned long long s = lo + blo;
-  hi = hi + bhi + (s < lo ? 1 : 0);
-  lo = s;
-}
 // (hi, lo) = Y * 2^sh for a signed Y = H 2^42 + R (|H| < 2^33, |R| < 2^61), 0 <= sh < 64
 KS_DEVICE void gt_make128(long long H, long long R, int sh, long long &hi, unsigned long long &lo) {
   hi = H >> 22;
@@ -259,27 +243,6 @@ KS_DEVICE void gt_make128(long long H, long long R, int sh, long long &hi, unsig
     lo <<= sh;
   }
 }
-// the value of a 128-bit integer as a double (two roundings at most: within 1 ulp)
-KS_DEVICE double gt_to_double(long long hi, unsigned long long lo) {
-  return fma(__ll2double_rn(hi), 18446744073709551616.0, __ull2double_rn(lo));
-}
-
-// double-double accumulation (TwoSum)
-KS_DEVICE void gt_dd_add(double &hi, double &lo, double x) {
-  const double s = hi + x;
-  const double bb = s - hi;
-  lo += (hi - (s - bb)) + (x - bb);
-  hi = s;
-}
-
-// the recorded scale of V column j over tiles [t0, t0 + nt): the largest exponent (-128 when every tile is zero)
-KS_DEVICE int gt_vscale(const GTArgs &g, int j, int t0, int nt) {
-  int e = -128;
-  const signed char *p = g.vexp + (size_t)j * g.ldt + t0;
-  for (int t = 0; t < nt; ++t) e = max(e, (int)p[t]);
-  return e;
-}
-
 KS_DEVICE void gt_init_barriers(const GTShared &S) {
   const int counts[GB_N] = {GT_SW, GT_SW, GT_SW, GT_SW, 1, 1, 1, 1, GT_EW, GT_EW, 1, 1, GT_EW, GT_EW, 1};
   for (int i = 0; i < GB_N; ++i)

@@ -360,14 +360,16 @@ static cudaError_t dot_dispatch(const StepArgs &a, int mode, int blocks, cudaStr
 }
 
 // storage: STORE_F64 (doubles) or STORE_PAIR (FP32 pairs, pair arithmetic only)
-// the tensor-core pair runs IEEE-double Gram-Schmidt when the caller supplies its arguments and the basis has columns
+// the exact-product pair (tensor cores or integer pipes) runs IEEE-double Gram-Schmidt when the caller supplies its
+// arguments and the basis has columns
 static bool gs_use_tc(const StepArgs &a, int arith, int storage) {
   return a.tc && storage == STORE_F64 && arith == ARITH_F64 && a.J >= 1 && a.J <= gs_tc_max_columns();
 }
 
 cudaError_t launch_gs_dot(const StepArgs &a, int nx, int mode, int arith, cudaStream_t s, int storage,
                           int max_blocks) {
-  if (gs_use_tc(a, arith, storage)) return launch_gs_dot_tc(a, nx, mode, *a.tc, s);
+  if (gs_use_tc(a, arith, storage))
+    return a.tc->integer ? launch_gs_dot_ix(a, nx, mode, *a.tc, s) : launch_gs_dot_tc(a, nx, mode, *a.tc, s);
   int blocks = gs_dot_blocks(a.n);
   if (max_blocks > 0 && blocks > max_blocks) blocks = max_blocks;
   if (storage == STORE_F32)
@@ -380,7 +382,8 @@ cudaError_t launch_gs_dot(const StepArgs &a, int nx, int mode, int arith, cudaSt
 }
 
 cudaError_t launch_gs_update(const StepArgs &a, int nx, int mode, int arith, cudaStream_t s, int storage) {
-  if (gs_use_tc(a, arith, storage)) return launch_gs_update_tc(a, nx, mode, *a.tc, s);
+  if (gs_use_tc(a, arith, storage))
+    return a.tc->integer ? launch_gs_update_ix(a, nx, mode, *a.tc, s) : launch_gs_update_tc(a, nx, mode, *a.tc, s);
   if (a.tc && storage == STORE_F64 && arith == ARITH_F64 && mode != GS_COMBINE) {
     // the FP64-FMA kernel writes the column (no basis columns to project out): record its tile exponents for the
     // tensor-core launches that read it later

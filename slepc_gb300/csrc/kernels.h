@@ -85,11 +85,16 @@ struct GTArgs {
   double *part;       // per-block partials (gs_tc_part_doubles() doubles)
   int pstride;        // half A: doubles per block in part (set by the launcher)
   int *err;           // set to 1 when a bounded wait ran out, to 2 when a value reached its recorded scale
+  int integer;        // 1: the integer-pipe kernels (k_gs_ix.cu) instead of the tensor-core ones
 };
 int gs_tc_max_columns();
 size_t gs_tc_part_doubles();
 cudaError_t launch_gs_dot_tc(const StepArgs &a, int nx, int mode, const GTArgs &g, cudaStream_t s);
 cudaError_t launch_gs_update_tc(const StepArgs &a, int nx, int mode, const GTArgs &g, cudaStream_t s);
+// the same pair with exact products on the integer pipes (k_gs_ix.cu): the same exponent table, partials and flag
+int gs_ix_max_columns();
+cudaError_t launch_gs_dot_ix(const StepArgs &a, int nx, int mode, const GTArgs &g, cudaStream_t s);
+cudaError_t launch_gs_update_ix(const StepArgs &a, int nx, int mode, const GTArgs &g, cudaStream_t s);
 // the exponents of the 128-row tiles of one IEEE-double column (vexp_col = the table row of that column)
 cudaError_t launch_record_vexp(const double *col, int n, signed char *vexp_col, cudaStream_t s);
 

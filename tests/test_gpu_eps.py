@@ -106,6 +106,30 @@ def test_lap3d_parity(lib, orc, arith):
     assert host_orth(res) <= 1e-12
 
 
+@pytest.mark.parametrize("case", ["lap3d16", "lap2d_37x41", "lap3d24_ncv143", "lap3d64"])
+def test_integer_gram_schmidt_parity(lib, case):
+    """EPS_GB300_GS_INTEGER (every Gram-Schmidt product exact on the integer pipes) against the closed-form spectrum
+    (1e-10), host-side residuals and orthogonality, and the FP64-FMA kernels: the same eigenvalues (1e-12, both
+    ways) and about the same restart count.  The cases cover an odd row count, the widest basis the kernels take
+    (143 columns) and more 512-row chunks than SMs."""
+    dims, nev, ncv = {"lap3d16": ([16] * 3, 20, 48), "lap2d_37x41": ([37, 41], 12, 40),
+                      "lap3d24_ncv143": ([24] * 3, 70, 143), "lap3d64": ([64] * 3, 20, 48)}[case]
+    csr = matgen.laplacian_3d(dims[0]) if len(dims) == 3 else matgen.laplacian_2d(*dims)
+    n = int(np.prod(dims))
+    kw = dict(hermitian=True, which="LR", nev=nev, ncv=ncv, tol=1e-10, v0=matgen.start_vector(n, 3), arith="f64")
+    a = run(csr, gs="integer", **kw)
+    b = run(csr, gs="fma", **kw)
+    assert a["stats"]["gs_exact"] == 1 and b["stats"]["gs_exact"] == 0
+    assert a["reason"] == 1 and a["nconv"] >= nev
+    exact = matgen.laplacian_eigenvalues(dims)
+    assert rel_match(a["eigr"], exact, 1e-10)
+    check_residuals(csr, a, 1e-10)
+    assert host_orth(a) <= 1e-12
+    assert rel_match(a["eigr"][:nev], b["eigr"][:b["nconv"]], 1e-12)
+    assert rel_match(b["eigr"][:nev], a["eigr"][:a["nconv"]], 1e-12)
+    assert abs(a["its"] - b["its"]) <= max(2, b["its"] // 10)
+
+
 def test_brusselator_golden_on_gpu(lib, orc):
     g = G["ex9_1"]
     csr = matgen.brusselator(g["N"])
