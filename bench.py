@@ -576,13 +576,13 @@ def main():
     ap.add_argument("--batch-plain-sample", type=int, default=256,
                     help="problems of the batched workload timed through the one-problem-per-launch path")
     ap.add_argument("--arith", default="f64", choices=["pair", "f64", "f32"],
-                    help="f64: IEEE FP64 storage and FMA (the headline); pair: FP32-pair arithmetic (reported beside "
+                    help="f64: IEEE FP64 storage (the headline); pair: FP32-pair arithmetic (reported beside "
                          "it); f32: the precision form")
     ap.add_argument("--restart", default="tensor", choices=["tensor", "pair", "mma_sync", "tcgen05"],
                     help="kernel of the thick restart (EPSGB300SetRestartMethod)")
-    ap.add_argument("--gs", default="fma", choices=["tensor", "fma", "integer"],
-                    help="Gram-Schmidt of the f64 arithmetic: FP64 FMA, or exact products on the tensor cores or the "
-                         "integer pipes")
+    ap.add_argument("--gs", default="integer", choices=["tensor", "fma", "integer"],
+                    help="Gram-Schmidt of the f64 arithmetic: exact products on the integer pipes (the library's "
+                         "default), FP64 FMA, or exact products on the tensor cores")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-parity", action="store_true", help="skip the host-side parity block")
@@ -617,7 +617,11 @@ def main():
 # FP64 FMA throughput of this GPU (DFMA microbenchmark: 1.20 TFLOP/s).  A Gram-Schmidt half does two FMAs per 8-byte
 # basis entry (0.5 flop/byte), so IEEE FP64 Gram-Schmidt is bounded at 1.20e12 * 2 = 2.4 TB/s, below the HBM rate.
 DFMA_TFLOPS = 1.20
-ARITH_LABEL = {"f64": "IEEE FP64 storage and FMA",
+GS_LABEL = {"integer": "Gram-Schmidt products exact on the integer pipes (54-bit fixed point, exact integer sums, "
+                       "one rounding per result)",
+            "fma": "Gram-Schmidt in IEEE FP64 FMA",
+            "tensor": "Gram-Schmidt products exact on the tensor cores (Ozaki slices)"}
+ARITH_LABEL = {"f64": "IEEE FP64 storage, FP64 arithmetic elsewhere",
                "pair": "FP32-pair storage and arithmetic (hi+lo floats, 47-bit significand, ~2^-46 per product)",
                "f32": "FP32 storage, pair accumulation, FP64-class refinement sweep"}
 
@@ -761,8 +765,8 @@ def run_plain(args, wl):
         roof["krylov_step_GBps"] = round(krylov_bytes / (krylov_ms / 1000.0) / 1e9, 1) if krylov_ms > 0 else None
         roof["krylov_step_frac"] = round(roof["krylov_step_GBps"] / peak, 4) if krylov_ms > 0 else None
         roof["solve_bytes"] = sum(v[1] for v in prof.values())
-        if arith == "f64":
-            # the FP64 pipe bounds IEEE Gram-Schmidt before HBM does: 2 DFMA per 8-byte entry
+        if arith == "f64" and args.gs == "fma":
+            # the FP64 pipe bounds FMA Gram-Schmidt before HBM does: 2 DFMA per 8-byte entry
             bound = DFMA_TFLOPS * 1e12 * 2.0 / 1e9
             roof["fp64_fma_bound"] = {
                 "dfma_tflops": DFMA_TFLOPS, "gs_flop_per_byte": 0.5, "bound_GBps": bound,
@@ -830,7 +834,9 @@ def run_plain(args, wl):
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.arith == "f64" else args.arith,
                 "data": "synthetic",
                 "config": {"workload": wl["desc"], "n": n, "nnz": nnz, "arith": args.arith,
-                           "arith_detail": ARITH_LABEL[args.arith], "restart": args.restart,
+                           "arith_detail": ARITH_LABEL[args.arith] + ("; " + GS_LABEL[args.gs]
+                                                                      if args.arith == "f64" else ""),
+                           "gs": args.gs if args.arith == "f64" else None, "restart": args.restart,
                            "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (basis 2.2 GB)"
                            if args.workload == "lap3d128" else "small inputs",
                            "krylov_steps_per_solve": main_run["steps"][-1],

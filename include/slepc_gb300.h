@@ -47,16 +47,17 @@ typedef enum { EPS_GB300_DS_REFINED = 0, EPS_GB300_DS_QR = 1, EPS_GB300_DS_AUTO 
 
 /* Gram-Schmidt of IEEE-double storage (EPS_GB300_ARITH_F64) inside EPSSolve.  No counterpart in the reference, whose
  * orthogonalisation (BVOrthogonalizeCGS1, src/sys/classes/bv/interface/bvorthog.c:91-132) calls FP64 BLAS gemv.
- *   EPS_GB300_GS_FMA (default): IEEE FP64 FMA in every product (bound by GB300's FP64 pipe near 2.4 TB/s).
+ *   EPS_GB300_GS_FMA: IEEE FP64 FMA in every product (bound by GB300's FP64 pipe near 2.4 TB/s).
  *   EPS_GB300_GS_TENSOR: every product of the two Gram-Schmidt halves exact on the FP16 tensor cores (an
  *       error-free split of each value's 55/56-bit fixed point, against its column/tile exponent, into byte or
  *       7-bit slices), the slice sums recombined as exact integers, rounded once per chunk of at most 512 rows and
  *       accumulated in double-double: more accurate than FP64 FMA.  On the 128^3 Laplacian it is still slower
  *       than the FMA kernels (the slicing on the CUDA cores bounds it).
- *   EPS_GB300_GS_INTEGER: every product exact on the integer pipes (each value's 54-bit fixed point against its
+ *   EPS_GB300_GS_INTEGER (default): every product exact on the integer pipes (each value's 54-bit fixed point against its
  *       column/tile exponent as two 27-bit halves, four 32 x 32 -> 64-bit multiply-adds per product, exact 64- and
  *       128-bit integer sums), rounded once per row (update half) or per thread's share of a column (dot half) and
- *       merged in double-double: as accurate as the tensor form, without the FP64 pipe's bound.
+ *       merged in double-double: as accurate as the tensor form, without the FP64 pipe's bound (on the 128^3
+ *       Laplacian the two halves run at 2.8 and 3.0 TB/s against 2.3 for the FMA kernels).
  * The exact forms are used for the symmetric (Lanczos) variant with the tcgen05 restart and no deflation space; the
  * other cases use the FMA kernels.  Option -eps_gb300_gs tensor|fma|integer. */
 typedef enum { EPS_GB300_GS_TENSOR = 0, EPS_GB300_GS_FMA = 1, EPS_GB300_GS_INTEGER = 2 } EPSGB300GSMethod;

@@ -449,9 +449,8 @@ class EPS:
     GS_METHODS = {"tensor": 0, "fma": 1, "integer": 2}
 
     def setGSMethod(self, method):
-        """'fma' (IEEE FP64 FMA, the default), 'tensor' (exact slice products on the tensor cores) or 'integer'
-        (exact products on the integer pipes) for the Gram-Schmidt pair of IEEE-double storage
-        (EPSGB300SetGSMethod)."""
+        """'integer' (exact products on the integer pipes, the default), 'fma' (IEEE FP64 FMA) or 'tensor' (exact
+        slice products on the tensor cores) for the Gram-Schmidt pair of IEEE-double storage (EPSGB300SetGSMethod)."""
         _check(load().EPSGB300SetGSMethod(self.handle, self.GS_METHODS[method]), "EPSGB300SetGSMethod")
 
     def setTimeLimit(self, seconds):

@@ -54,28 +54,28 @@ KS_DEVICE int gt_vscale(const GTArgs &g, int j, int t0, int nt) {
 // ---------------------------------------------------------------------------------------------------------------
 
 // X = trunc(v 2^(53 - e)), |X| < 2^53 when |v| < 2^e (the full significand of every value in the top binade
-// [2^(e-1), 2^e), fewer bits below), returned as H 2^26 + L with H = floor(X / 2^26) (|H| <= 2^27) and
-// 0 <= L < 2^26.  Integer operations only.  A value at or above 2^e (or not finite) makes *flag negative.
+// [2^(e-1), 2^e), fewer bits below), returned as X = H 2^26 + L with the sign of v on both halves (|H| < 2^27,
+// |L| < 2^26).  Integer operations only.  A value at or above 2^e (or not finite) makes *flag negative.
 KS_DEVICE void ix_split53(double v, int e, int &H, int &L, int &flag) {
   const unsigned long long u = (unsigned long long)__double_as_longlong(v);
   const unsigned hw = (unsigned)(u >> 32);
   const int E = (int)((hw >> 20) & 0x7FFu);
-  const int s0 = 1022 + e - E;  // X = m >> s0 for m = 2^52 | fraction (zero and subnormals shift out entirely)
+  const int s0 = 1022 + e - E;  // |X| = m >> s0 for m = 2^52 | fraction (zero and subnormals shift out entirely)
   flag |= s0;
   const unsigned long long m =
       ((unsigned long long)((hw & 0xFFFFFu) | 0x100000u) << 32) | (unsigned long long)(unsigned)u;
   const unsigned long long x = m >> min((unsigned)s0, 63u);
-  const long long xs = (hw >> 31) ? -(long long)x : (long long)x;
-  H = (int)(xs >> 26);
-  L = (int)((unsigned)xs & 0x3FFFFFFu);
+  const int sm = (int)hw >> 31;  // 0, or -1 for a negative value
+  H = ((int)(x >> 26) ^ sm) - sm;
+  L = ((int)((unsigned)x & 0x3FFFFFFu) ^ sm) - sm;
 }
 
 // The exact sum P = hh 2^52 + mm 2^26 + ll of a run of split products, as a 128-bit integer.
-KS_DEVICE void ix_combine(long long hh, long long mm, unsigned long long ll, long long &hi, unsigned long long &lo) {
+KS_DEVICE void ix_combine(long long hh, long long mm, long long ll, long long &hi, unsigned long long &lo) {
   hi = hh >> 12;
   lo = (unsigned long long)hh << 52;
   gt_add128(hi, lo, mm >> 38, (unsigned long long)mm << 26);
-  gt_add128(hi, lo, 0, ll);
+  gt_add128(hi, lo, ll >> 63, (unsigned long long)ll);
 }
 
 // arithmetic right shift of a 128-bit integer by 0 <= s <= 127

@@ -6,9 +6,9 @@
 //
 //   a value v with |v| < 2^e becomes the 54-bit two's complement fixed point X = trunc(v 2^(53-e)) -- the whole
 //   significand of every value in the top binade of its scale, fewer bits below it -- split as X = H 2^26 + L
-//   (|H| <= 2^27, 0 <= L < 2^26) with integer operations only (ix_split53);
+//   (|H| < 2^27, |L| < 2^26, both with the sign of v) with integer operations only (ix_split53);
 //   a product X_v X_u = HH 2^52 + (HL + LH) 2^26 + LL is four IMAD.WIDE, and the three partial sums of a run of
-//   products stay exact in 64-bit integers (|HH|, |HL| < 2^54, LL < 2^52: runs of up to 342 products);
+//   products stay exact in 64-bit integers (|HH| < 2^54, |HL|, |LL| < 2^53: runs of up to 256 products);
 //   a run's sum is one exact 128-bit integer, then either rounded once to a double (half B, per row) or added to a
 //   128-bit accumulator with a binary exponent (half A, per column: ix_acc_add drops bits 2^-106 below the scale).
 //
@@ -48,11 +48,13 @@ constexpr int IX_MAXJ = 144;
 constexpr int IU_THREADS = 256;                 // half B
 constexpr int IU_ROWS = 2 * IU_THREADS;         // rows per pass of half B
 
-// one product of split values into the three exact partial sums
-KS_DEVICE void ix_mac(long long &hh, long long &mm, unsigned long long &ll, int Hv, int Lv, int Hx, int Lx) {
-  hh += (long long)Hv * Hx;
-  mm += (long long)Hv * Lx + (long long)Lv * Hx;
-  ll += (unsigned long long)(unsigned)Lv * (unsigned)Lx;
+// one product of split values into the three exact partial sums: four 32 x 32 -> 64-bit multiply-adds
+KS_DEVICE void ix_madw(long long &acc, int a, int b) { asm("mad.wide.s32 %0, %1, %2, %0;" : "+l"(acc) : "r"(a), "r"(b)); }
+KS_DEVICE void ix_mac(long long &hh, long long &mm, long long &ll, int Hv, int Lv, int Hx, int Lx) {
+  ix_madw(hh, Hv, Hx);
+  ix_madw(mm, Hv, Lx);
+  ix_madw(mm, Lv, Hx);
+  ix_madw(ll, Lv, Lx);
 }
 
 // ---------------------------------------------------------------------------------------------------------------
@@ -70,8 +72,8 @@ KS_DEVICE void ix_cp_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"
 // dynamic shared memory of half A: raw u, w of two tiles (copied one tile ahead), the split pairs of one tile, the
 // per-column accumulators
 constexpr size_t IXD_RAW = 0;                                           // double [2][2][IX_TMAX]
-constexpr size_t IXD_SU = IXD_RAW + 2 * 2 * IX_TMAX * sizeof(double);   // int4 [IX_TMAX]
-constexpr size_t IXD_ACC = IXD_SU + IX_TMAX * sizeof(int4);             // IxAcc [IX_MAXJ][2]
+constexpr size_t IXD_SU = IXD_RAW + 2 * 2 * IX_TMAX * sizeof(double);   // int2 [u, w][IX_TMAX]
+constexpr size_t IXD_ACC = IXD_SU + 2 * IX_TMAX * sizeof(int2);         // IxAcc [IX_MAXJ][2]
 constexpr size_t IXD_SMEM = IXD_ACC + IX_MAXJ * 2 * sizeof(IxAcc);
 
 template <int NX>
@@ -80,7 +82,7 @@ __global__ void __launch_bounds__(IX_THREADS, 1) k_gs_dot_ix(StepArgs a, int mod
   if (st->stop) return;
   extern __shared__ __align__(16) unsigned char smx[];
   double *raw = reinterpret_cast<double *>(smx + IXD_RAW);  // [buffer][u, w][row]
-  int4 *su = reinterpret_cast<int4 *>(smx + IXD_SU);        // (H_u, L_u, H_w, L_w) per row of the tile
+  int2 *su = reinterpret_cast<int2 *>(smx + IXD_SU);        // (H, L) of u, then of w, per row of the tile
   IxAcc *cacc = reinterpret_cast<IxAcc *>(smx + IXD_ACC);   // [column][vector]
   __shared__ int emx[IX_THREADS / 32][2];
   __shared__ double sred[IX_THREADS / 32][3];
@@ -116,24 +118,29 @@ __global__ void __launch_bounds__(IX_THREADS, 1) k_gs_dot_ix(StepArgs a, int mod
   auto load_item = [&](int t, int kk, int gq, double (&v)[16]) {
     const double *col = V + (size_t)(warp + IX_WARPS * kk) * a.ldv;
     const long long rb = (long long)t * TR + IX_GROUP * gq + 2 * lane;
+    if (rb + 64 * 7 + 1 < n) {
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      const long long r = rb + 64 * i;
-      if (r + 1 < n) {
-        const double2 x = __ldcs(reinterpret_cast<const double2 *>(col + r));
+      for (int i = 0; i < 8; ++i) {
+        const double2 x = __ldcs(reinterpret_cast<const double2 *>(col + rb + 64 * i));
         v[2 * i] = x.x;
         v[2 * i + 1] = x.y;
-      } else {
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const long long r = rb + 64 * i;
         v[2 * i] = r < n ? col[r] : 0.0;
-        v[2 * i + 1] = 0.0;
+        v[2 * i + 1] = r + 1 < n ? col[r + 1] : 0.0;
       }
     }
   };
 
   int t = blockIdx.x;
   copy_raw(t, 0);
-  double nx[16];
-  if (nk > 0 && t < ntile) load_item(t, 0, 0, nx);
+  // the software pipeline alternates between two load buffers (par: the one holding the current group)
+  double bA[16], bB[16];
+  int par = 0;
+  if (nk > 0 && t < ntile) load_item(t, 0, 0, bA);
   for (int it = 0; t < ntile; ++it, t += gridDim.x) {
     const int b = it & 1;
     // ---- stage the tile's u, w as split pairs against the tile's scales ----
@@ -175,7 +182,8 @@ __global__ void __launch_bounds__(IX_THREADS, 1) k_gs_dot_ix(StepArgs a, int mod
       int Hu, Lu, Hw = 0, Lw = 0;
       ix_split53(ru[r] * sigma, eu, Hu, Lu, flag);
       if (NX == 2) ix_split53(rw[r], ew, Hw, Lw, flag);
-      su[r] = make_int4(Hu, Lu, Hw, Lw);
+      su[r] = make_int2(Hu, Lu);
+      su[IX_TMAX + r] = make_int2(Hw, Lw);
     }
     __syncthreads();  // pairs visible; emx free for the next tile
     // ---- the warp's columns: lanes over rows, one column at a time ----
@@ -186,34 +194,37 @@ __global__ void __launch_bounds__(IX_THREADS, 1) k_gs_dot_ix(StepArgs a, int mod
       int ec = lane < nt128 ? (int)g.vexp[(size_t)c * g.ldt + t128 + lane] : -128;
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) ec = max(ec, __shfl_xor_sync(0xffffffffu, ec, off));
-      long long hh[NX], mm[NX];
-      unsigned long long ll[NX];
+      long long hh[NX], mm[NX], ll[NX];
 #pragma unroll
       for (int x = 0; x < NX; ++x) {
         hh[x] = 0;
         mm[x] = 0;
         ll[x] = 0;
       }
-      for (int gq = 0; gq < G; ++gq) {
-        double cv[16];
-#pragma unroll
-        for (int e = 0; e < 16; ++e) cv[e] = nx[e];
-        // the next group: of this column, the next column, or this warp's first column in the next tile
-        if (gq + 1 < G) load_item(t, kk, gq + 1, nx);
-        else if (kk + 1 < nk) load_item(t, kk + 1, 0, nx);
-        else if (t + (int)gridDim.x < ntile) load_item(t + (int)gridDim.x, 0, 0, nx);
+      // one group: the next one is loaded (of this column, the next column, or this warp's first column in the next
+      // tile) while this one is consumed
+      auto group = [&](int gq, const double (&cv)[16], double (&nv)[16]) {
+        if (gq + 1 < G) load_item(t, kk, gq + 1, nv);
+        else if (kk + 1 < nk) load_item(t, kk + 1, 0, nv);
+        else if (t + (int)gridDim.x < ntile) load_item(t + (int)gridDim.x, 0, 0, nv);
         const int rb = IX_GROUP * gq + 2 * lane;
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
-          const int4 p0 = su[rb + 64 * i], p1 = su[rb + 64 * i + 1];
+          const int4 pu = *reinterpret_cast<const int4 *>(su + rb + 64 * i);
+          const int4 pw = NX == 2 ? *reinterpret_cast<const int4 *>(su + IX_TMAX + rb + 64 * i) : make_int4(0, 0, 0, 0);
           int Hv, Lv;
           ix_split53(cv[2 * i], ec, Hv, Lv, flag);
-          ix_mac(hh[0], mm[0], ll[0], Hv, Lv, p0.x, p0.y);
-          if (NX == 2) ix_mac(hh[NX - 1], mm[NX - 1], ll[NX - 1], Hv, Lv, p0.z, p0.w);
+          ix_mac(hh[0], mm[0], ll[0], Hv, Lv, pu.x, pu.y);
+          if (NX == 2) ix_mac(hh[NX - 1], mm[NX - 1], ll[NX - 1], Hv, Lv, pw.x, pw.y);
           ix_split53(cv[2 * i + 1], ec, Hv, Lv, flag);
-          ix_mac(hh[0], mm[0], ll[0], Hv, Lv, p1.x, p1.y);
-          if (NX == 2) ix_mac(hh[NX - 1], mm[NX - 1], ll[NX - 1], Hv, Lv, p1.z, p1.w);
+          ix_mac(hh[0], mm[0], ll[0], Hv, Lv, pu.z, pu.w);
+          if (NX == 2) ix_mac(hh[NX - 1], mm[NX - 1], ll[NX - 1], Hv, Lv, pw.z, pw.w);
         }
+      };
+      for (int gq = 0; gq < G; ++gq) {
+        if (par == 0) group(gq, bA, bB);
+        else group(gq, bB, bA);
+        par ^= 1;
       }
       // the column's exact sum over the tile: 128-bit butterfly over the lanes, folded by lane 0
 #pragma unroll
@@ -384,8 +395,7 @@ __global__ void __launch_bounds__(IU_THREADS, 2) k_gs_update_ix(StepArgs a, int 
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) et = max(et, __shfl_xor_sync(0xffffffffu, et, off));
     const bool two = r + 1 < n, one = r < n;
-    long long hh[2][NX], mm[2][NX];
-    unsigned long long ll[2][NX];
+    long long hh[2][NX], mm[2][NX], ll[2][NX];
 #pragma unroll
     for (int e = 0; e < 2; ++e)
 #pragma unroll
@@ -396,38 +406,30 @@ __global__ void __launch_bounds__(IU_THREADS, 2) k_gs_update_ix(StepArgs a, int 
       }
     if (one && et > -128) {
       const double *colp = V + r;
-      auto load2 = [&](int c, double &x0, double &x1) {
-        if (two) {
-          const double2 v = __ldcs(reinterpret_cast<const double2 *>(colp + (size_t)c * a.ldv));
-          x0 = v.x;
-          x1 = v.y;
-        } else {
-          x0 = colp[(size_t)c * a.ldv];
-          x1 = 0.0;
-        }
-      };
-      // groups of 8 columns, the next group's loads in flight while the current one is consumed
-      double xa[8], xb[8];
-#pragma unroll
-      for (int q = 0; q < 8; ++q)
-        if (q < J) load2(q, xa[q], xb[q]);
-      for (int c0 = 0; c0 < J; c0 += 8) {
-        double ca[8], cb[8];
+      // groups of 8 columns in two buffers: the next group's loads in flight while the current one is consumed
+      auto loadg = [&](int c0, double (&x0)[8], double (&x1)[8]) {
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
-          ca[q] = xa[q];
-          cb[q] = xb[q];
+          if (c0 + q < J) {
+            if (two) {
+              const double2 v = __ldcs(reinterpret_cast<const double2 *>(colp + (size_t)(c0 + q) * a.ldv));
+              x0[q] = v.x;
+              x1[q] = v.y;
+            } else {
+              x0[q] = colp[(size_t)(c0 + q) * a.ldv];
+              x1[q] = 0.0;
+            }
+          }
         }
-#pragma unroll
-        for (int q = 0; q < 8; ++q)
-          if (c0 + 8 + q < J) load2(c0 + 8 + q, xa[q], xb[q]);
+      };
+      auto consume = [&](int c0, const double (&x0)[8], const double (&x1)[8]) {
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
           if (c0 + q < J) {
             const int4 cq = cp[c0 + q];
             int H0, L0, H1, L1;
-            ix_split53(ca[q], et, H0, L0, flag);
-            ix_split53(cb[q], et, H1, L1, flag);
+            ix_split53(x0[q], et, H0, L0, flag);
+            ix_split53(x1[q], et, H1, L1, flag);
             ix_mac(hh[0][0], mm[0][0], ll[0][0], H0, L0, cq.x, cq.y);
             ix_mac(hh[1][0], mm[1][0], ll[1][0], H1, L1, cq.x, cq.y);
             if (NX == 2) {
@@ -436,6 +438,15 @@ __global__ void __launch_bounds__(IU_THREADS, 2) k_gs_update_ix(StepArgs a, int 
             }
           }
         }
+      };
+      double a0[8], a1[8], b0[8], b1[8];
+      loadg(0, a0, a1);
+      for (int c0 = 0; c0 < J; c0 += 16) {
+        if (c0 + 8 < J) loadg(c0 + 8, b0, b1);
+        consume(c0, a0, a1);
+        if (c0 + 8 >= J) break;
+        if (c0 + 16 < J) loadg(c0 + 16, a0, a1);
+        consume(c0 + 8, b0, b1);
       }
     }
     int Ev = 0;

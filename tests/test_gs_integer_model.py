@@ -42,9 +42,9 @@ def split53(v, e):
     m = (u & ((1 << 52) - 1)) | (1 << 52)
     sh = s0 if 0 <= s0 <= 63 else 63
     x = m >> sh
-    xs = -x if (u >> 63) else x
-    H, L = xs >> 26, xs & ((1 << 26) - 1)
-    assert -(1 << 31) <= H < (1 << 31) and 0 <= L < (1 << 26)
+    sgn = -1 if (u >> 63) else 1
+    H, L = sgn * (x >> 26), sgn * (x & ((1 << 26) - 1))  # the sign of v on both halves
+    assert abs(H) < (1 << 27) and abs(L) < (1 << 26)
     return H, L, s0 >= 0
 
 
@@ -52,8 +52,7 @@ def mac(acc, Hv, Lv, Hx, Lx):
     hh, mm, ll = acc
     hh = i64(hh + Hv * Hx)
     mm = i64(mm + Hv * Lx + Lv * Hx)
-    ll = ll + Lv * Lx
-    assert 0 <= ll < (1 << 64)
+    ll = i64(ll + Lv * Lx)
     return hh, mm, ll
 
 
@@ -132,7 +131,7 @@ def test_split_is_the_truncated_fixed_point():
         X = H * (1 << 26) + L
         exact = Fraction(v) * Fraction(2) ** (53 - e)
         assert X == int(exact)  # truncation toward zero
-        assert abs(X) < (1 << 53) and -(1 << 27) <= H <= (1 << 27)
+        assert abs(X) < (1 << 53) and abs(H) < (1 << 27) and abs(L) < (1 << 26)
         # the top binade keeps the whole significand
         if abs(v) >= 2.0 ** (e - 1):
             assert Fraction(X) == exact
@@ -147,7 +146,7 @@ def test_partial_sums_fit_their_registers_at_the_longest_runs():
     # half B: a row sums J <= 144 columns.  Every term at its extreme magnitude (twice: two products per step).
     runs = max(16 * IX_GMAX, IX_MAXJ)
     assert runs == 144
-    Hmax, Lmax = 1 << 27, (1 << 26) - 1
+    Hmax, Lmax = (1 << 27) - 1, (1 << 26) - 1
     for sh in (1, -1):
         acc = (0, 0, 0)
         for _ in range(runs):
@@ -156,6 +155,7 @@ def test_partial_sums_fit_their_registers_at_the_longest_runs():
         combine(*acc)
     # 128-bit combine of a run, then a few thousand chunk folds at the top scale stay in range
     P = combine(runs * Hmax * Hmax, 2 * runs * Hmax * Lmax, runs * Lmax * Lmax)
+    assert combine(-runs * Hmax * Hmax, -2 * runs * Hmax * Lmax, -runs * Lmax * Lmax) == -P
     assert abs(32 * P) < (1 << 127)  # the lanes' butterfly
     A = None
     for _ in range(5000):

@@ -135,14 +135,14 @@ def test_gb300_setting_checks(lib):
     assert lib.EPSGB300SetProjectedSolver(eps.handle, 3) == PETSC_ERR_ARG_OUTOFRANGE
     for meth in ("qr", "refined", "auto"):
         eps.setProjectedSolver(meth)
-    # Gram-Schmidt methods: tensor 0, fma 1 (default), integer 2
+    # Gram-Schmidt methods: tensor 0, fma 1, integer 2 (default)
     lib.EPSGB300SetGSMethod.argtypes = [P, ctypes.c_int]
     lib.EPSGB300GetGSMethod.argtypes = [P, P]
-    assert lib.EPSGB300GetGSMethod(eps.handle, ctypes.byref(m)) == 0 and m.value == 1
+    assert lib.EPSGB300GetGSMethod(eps.handle, ctypes.byref(m)) == 0 and m.value == 2
     assert lib.EPSGB300SetGSMethod(eps.handle, 3) == PETSC_ERR_ARG_OUTOFRANGE
-    for meth, code in (("tensor", 0), ("integer", 2), ("fma", 1)):
+    for meth, val in (("tensor", 0), ("integer", 2), ("fma", 1)):
         eps.setGSMethod(meth)
-        assert lib.EPSGB300GetGSMethod(eps.handle, ctypes.byref(m)) == 0 and m.value == code
+        assert lib.EPSGB300GetGSMethod(eps.handle, ctypes.byref(m)) == 0 and m.value == val
     lib.EPSSetDeflationSpace.argtypes = [P, ctypes.c_int, P]
     assert lib.EPSSetDeflationSpace(eps.handle, -1, None) == PETSC_ERR_ARG_OUTOFRANGE
     assert lib.EPSSetDeflationSpace(eps.handle, 1, None) == PETSC_ERR_ARG_NULL
