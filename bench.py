@@ -580,9 +580,10 @@ def main():
                          "it); f32: the precision form")
     ap.add_argument("--restart", default="tensor", choices=["tensor", "pair", "mma_sync", "tcgen05"],
                     help="kernel of the thick restart (EPSGB300SetRestartMethod)")
-    ap.add_argument("--gs", default="integer", choices=["tensor", "fma", "integer"],
-                    help="Gram-Schmidt of the f64 arithmetic: exact products on the integer pipes (the library's "
-                         "default), FP64 FMA, or exact products on the tensor cores")
+    ap.add_argument("--gs", default="auto", choices=["auto", "tensor", "fma", "integer"],
+                    help="Gram-Schmidt of the f64 arithmetic: the library's default (exact integer products, FP64 FMA "
+                         "where segments replay from graphs), exact products on the integer pipes, FP64 FMA, or exact "
+                         "products on the tensor cores")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-parity", action="store_true", help="skip the host-side parity block")
@@ -747,6 +748,7 @@ def run_plain(args, wl):
         e.solve()
         prof = e.getProfile()
         e.setProfiling(False)
+        exact_gs = bool(e.getStats()["gs_exact"])
         peak, peak_kind = measured_peaks()
         top = max(("gs_dot", "gs_update", "spmv", "restart"), key=lambda k: prof[k][0])
         ms_k, by_k, nl_k = prof[top]
@@ -765,7 +767,7 @@ def run_plain(args, wl):
         roof["krylov_step_GBps"] = round(krylov_bytes / (krylov_ms / 1000.0) / 1e9, 1) if krylov_ms > 0 else None
         roof["krylov_step_frac"] = round(roof["krylov_step_GBps"] / peak, 4) if krylov_ms > 0 else None
         roof["solve_bytes"] = sum(v[1] for v in prof.values())
-        if arith == "f64" and args.gs == "fma":
+        if arith == "f64" and not exact_gs:
             # the FP64 pipe bounds FMA Gram-Schmidt before HBM does: 2 DFMA per 8-byte entry
             bound = DFMA_TFLOPS * 1e12 * 2.0 / 1e9
             roof["fp64_fma_bound"] = {
@@ -803,6 +805,7 @@ def run_plain(args, wl):
 
     roofline = roofline_of(eps, args.arith)
     stats = eps.getStats()
+    gs_used = args.gs if args.gs != "auto" else ("integer" if stats["gs_exact"] else "fma")
 
     # the pair arithmetic beside the headline, labelled as what it is (narrower than IEEE FP64)
     pair = None
@@ -834,9 +837,9 @@ def run_plain(args, wl):
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.arith == "f64" else args.arith,
                 "data": "synthetic",
                 "config": {"workload": wl["desc"], "n": n, "nnz": nnz, "arith": args.arith,
-                           "arith_detail": ARITH_LABEL[args.arith] + ("; " + GS_LABEL[args.gs]
+                           "arith_detail": ARITH_LABEL[args.arith] + ("; " + GS_LABEL[gs_used]
                                                                       if args.arith == "f64" else ""),
-                           "gs": args.gs if args.arith == "f64" else None, "restart": args.restart,
+                           "gs": gs_used if args.arith == "f64" else None, "restart": args.restart,
                            "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (basis 2.2 GB)"
                            if args.workload == "lap3d128" else "small inputs",
                            "krylov_steps_per_solve": main_run["steps"][-1],

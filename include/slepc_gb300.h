@@ -53,14 +53,18 @@ typedef enum { EPS_GB300_DS_REFINED = 0, EPS_GB300_DS_QR = 1, EPS_GB300_DS_AUTO 
  *       7-bit slices), the slice sums recombined as exact integers, rounded once per chunk of at most 512 rows and
  *       accumulated in double-double: more accurate than FP64 FMA.  On the 128^3 Laplacian it is still slower
  *       than the FMA kernels (the slicing on the CUDA cores bounds it).
- *   EPS_GB300_GS_INTEGER (default): every product exact on the integer pipes (each value's 54-bit fixed point against its
+ *   EPS_GB300_GS_INTEGER: every product exact on the integer pipes (each value's 54-bit fixed point against its
  *       column/tile exponent as two 27-bit halves, four 32 x 32 -> 64-bit multiply-adds per product, exact 64- and
  *       128-bit integer sums), rounded once per row (update half) or per thread's share of a column (dot half) and
  *       merged in double-double: as accurate as the tensor form, without the FP64 pipe's bound (on the 128^3
  *       Laplacian the two halves run at 2.8 and 3.0 TB/s against 2.3 for the FMA kernels).
- * The exact forms are used for the symmetric (Lanczos) variant with the tcgen05 restart and no deflation space; the
- * other cases use the FMA kernels.  Option -eps_gb300_gs tensor|fma|integer. */
-typedef enum { EPS_GB300_GS_TENSOR = 0, EPS_GB300_GS_FMA = 1, EPS_GB300_GS_INTEGER = 2 } EPSGB300GSMethod;
+ *   EPS_GB300_GS_AUTO (default): EPS_GB300_GS_INTEGER for solves whose factorisation segments run as direct
+ *       launches, EPS_GB300_GS_FMA for those replayed from CUDA graphs (EPSGB300SetGraphCapture: by default the
+ *       problems of at most 262144 rows, where launch gaps matter more than the Gram-Schmidt rate).
+ * The exact forms are used for the symmetric (Lanczos) variant with the tcgen05 restart and no deflation space, and
+ * run as direct launches; the other cases use the FMA kernels.  Option -eps_gb300_gs auto|integer|fma|tensor. */
+typedef enum { EPS_GB300_GS_TENSOR = 0, EPS_GB300_GS_FMA = 1, EPS_GB300_GS_INTEGER = 2, EPS_GB300_GS_AUTO = 3 }
+    EPSGB300GSMethod;
 PetscErrorCode EPSGB300SetGSMethod(EPS eps, EPSGB300GSMethod method);
 PetscErrorCode EPSGB300GetGSMethod(EPS eps, EPSGB300GSMethod *method);
 PetscErrorCode EPSGB300SetProjectedSolver(EPS eps, EPSGB300DSMethod method);

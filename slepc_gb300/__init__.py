@@ -446,11 +446,12 @@ class EPS:
         tensor-core kernel explicitly: 'mma_sync' or 'tcgen05' (bit-identical results)."""
         _check(load().EPSGB300SetRestartMethod(self.handle, self.RESTART_METHODS[method]), "EPSGB300SetRestartMethod")
 
-    GS_METHODS = {"tensor": 0, "fma": 1, "integer": 2}
+    GS_METHODS = {"tensor": 0, "fma": 1, "integer": 2, "auto": 3}
 
     def setGSMethod(self, method):
-        """'integer' (exact products on the integer pipes, the default), 'fma' (IEEE FP64 FMA) or 'tensor' (exact
-        slice products on the tensor cores) for the Gram-Schmidt pair of IEEE-double storage (EPSGB300SetGSMethod)."""
+        """'auto' (the default: 'integer' unless the factorisation segments replay from CUDA graphs, then 'fma'),
+        'integer' (exact products on the integer pipes), 'fma' (IEEE FP64 FMA) or 'tensor' (exact slice products on
+        the tensor cores) for the Gram-Schmidt pair of IEEE-double storage (EPSGB300SetGSMethod)."""
         _check(load().EPSGB300SetGSMethod(self.handle, self.GS_METHODS[method]), "EPSGB300SetGSMethod")
 
     def setTimeLimit(self, seconds):

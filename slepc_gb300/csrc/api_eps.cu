@@ -622,6 +622,9 @@ PetscErrorCode ksg_orthonormalize_column(void *V, long long ldv, int n, int j, d
 // ---------------------------------------------------------------------------------------------------------------
 // EPS
 // ---------------------------------------------------------------------------------------------------------------
+// factorisation segments replay from CUDA graphs by default up to this many rows (EPSGB300SetGraphCapture)
+constexpr int kGraphMaxRows = 262144;
+
 static void eps_clear_graphs(EPS eps) {
   for (auto &kv : eps->seg_graphs)
     if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
@@ -1001,7 +1004,8 @@ extern "C" PetscErrorCode EPSGB300GetProjectedSolver(EPS eps, EPSGB300DSMethod *
 }
 extern "C" PetscErrorCode EPSGB300SetGSMethod(EPS eps, EPSGB300GSMethod method) {
   KSG_CHECK(eps, PETSC_ERR_ARG_NULL, "Null EPS");
-  KSG_CHECK(method == EPS_GB300_GS_TENSOR || method == EPS_GB300_GS_FMA || method == EPS_GB300_GS_INTEGER,
+  KSG_CHECK(method == EPS_GB300_GS_TENSOR || method == EPS_GB300_GS_FMA || method == EPS_GB300_GS_INTEGER ||
+                method == EPS_GB300_GS_AUTO,
             PETSC_ERR_ARG_OUTOFRANGE, "Unknown Gram-Schmidt method");
   eps->gs_method = method;
   return 0;
@@ -1172,7 +1176,8 @@ extern "C" PetscErrorCode EPSSetFromOptions(EPS eps) {
     else if (!strcmp(o, "-eps_gb300_gs") && v)
       KSG_TRY(EPSGB300SetGSMethod(eps, !strcmp(v, "fma")       ? EPS_GB300_GS_FMA
                                        : !strcmp(v, "integer") ? EPS_GB300_GS_INTEGER
-                                                               : EPS_GB300_GS_TENSOR));
+                                       : !strcmp(v, "tensor")  ? EPS_GB300_GS_TENSOR
+                                                               : EPS_GB300_GS_AUTO));
     else if (!strcmp(o, "-eps_gb300_graphs") && v)
       KSG_TRY(EPSGB300SetGraphCapture(eps, atoi(v)));
   }
@@ -1628,7 +1633,7 @@ static PetscErrorCode eps_factorize_launch(EPS eps, int k0, int nv, double *byte
 // second time on (the same kernels with the same arguments; the stop flag in the device state ends a segment early
 // in either form).  A capture that fails turns graphs off for this EPS and runs the launches directly.
 static PetscErrorCode eps_factorize(EPS eps, int k0, int nv, double *bytes) {
-  const bool on = eps->graph_mode == 1 || (eps->graph_mode == -1 && eps->n <= 262144);
+  const bool on = eps->graph_mode == 1 || (eps->graph_mode == -1 && eps->n <= kGraphMaxRows);
   if (!on || eps->prof || eps->gs_tc_on) return eps_factorize_launch(eps, k0, nv, bytes);
   const std::array<int, 4> key = {k0, nv, eps->storage, eps->arith};
   auto it = eps->seg_graphs.find(key);
@@ -1911,11 +1916,14 @@ static PetscErrorCode eps_solve_core(EPS eps, double tol, std::chrono::steady_cl
   // with the tcgen05 restart, whose kernels and these keep the basis columns' exponent table up to date
   {
     const int rm = eps->restart_method;
-    const int exact = eps->gs_method == EPS_GB300_GS_TENSOR || eps->gs_method == EPS_GB300_GS_INTEGER;
+    // the automatic choice: exact integer products unless the segments will replay from CUDA graphs
+    const bool graphs = eps->graph_mode == 1 || (eps->graph_mode == -1 && n <= kGraphMaxRows);
+    const int exact = eps->gs_method == EPS_GB300_GS_TENSOR || eps->gs_method == EPS_GB300_GS_INTEGER ||
+                      (eps->gs_method == EPS_GB300_GS_AUTO && !graphs);
     eps->gs_tc_on = eps->storage == STORE_F64 && eps->arith == ARITH_F64 && exact && herm && eps->vexp.p &&
                     ld <= gs_tc_max_columns() && ncv < n && eps->nc == 0 &&
                     (rm == EPS_GB300_RESTART_TCGEN05 || (rm == EPS_GB300_RESTART_TENSOR && kRestartTensorIsTcgen05));
-    eps->gt.integer = eps->gs_method == EPS_GB300_GS_INTEGER;
+    eps->gt.integer = eps->gs_method != EPS_GB300_GS_TENSOR;
     if (eps->gs_tc_on) eps->stats.gs_exact = 1;
     if (eps->gs_tc_on) KSG_CUDA(cudaMemsetAsync(eps->gterr.p, 0, sizeof(int), s));
   }

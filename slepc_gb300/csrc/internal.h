@@ -165,7 +165,7 @@ struct _p_EPS {
   int arith = ksg::ARITH_PAIR;
   int storage = ksg::STORE_PAIR;  // basis format: pairs with pair arithmetic, doubles with FP64 arithmetic
   int ds_method = EPS_GB300_DS_AUTO;  // EPSGB300DSMethod
-  int gs_method = EPS_GB300_GS_INTEGER;  // EPSGB300GSMethod
+  int gs_method = EPS_GB300_GS_AUTO;  // EPSGB300GSMethod
   double time_limit = 0.0;        // EPSGB300SetTimeLimit (0: none)
   int restart_method = 0;         // EPSGB300RestartMethod
   int device = -1;

@@ -135,12 +135,12 @@ def test_gb300_setting_checks(lib):
     assert lib.EPSGB300SetProjectedSolver(eps.handle, 3) == PETSC_ERR_ARG_OUTOFRANGE
     for meth in ("qr", "refined", "auto"):
         eps.setProjectedSolver(meth)
-    # Gram-Schmidt methods: tensor 0, fma 1, integer 2 (default)
+    # Gram-Schmidt methods: tensor 0, fma 1, integer 2, auto 3 (default)
     lib.EPSGB300SetGSMethod.argtypes = [P, ctypes.c_int]
     lib.EPSGB300GetGSMethod.argtypes = [P, P]
-    assert lib.EPSGB300GetGSMethod(eps.handle, ctypes.byref(m)) == 0 and m.value == 2
-    assert lib.EPSGB300SetGSMethod(eps.handle, 3) == PETSC_ERR_ARG_OUTOFRANGE
-    for meth, val in (("tensor", 0), ("integer", 2), ("fma", 1)):
+    assert lib.EPSGB300GetGSMethod(eps.handle, ctypes.byref(m)) == 0 and m.value == 3
+    assert lib.EPSGB300SetGSMethod(eps.handle, 4) == PETSC_ERR_ARG_OUTOFRANGE
+    for meth, val in (("tensor", 0), ("integer", 2), ("fma", 1), ("auto", 3)):
         eps.setGSMethod(meth)
         assert lib.EPSGB300GetGSMethod(eps.handle, ctypes.byref(m)) == 0 and m.value == val
     lib.EPSSetDeflationSpace.argtypes = [P, ctypes.c_int, P]
