@@ -639,7 +639,9 @@ def test_wide_basis_nonsymmetric(lib):
 @pytest.mark.parametrize("arith,herm", [("f64", True), ("pair", True), ("f64", False)])
 def test_graph_segments_match_direct_launches(lib, arith, herm):
     """Factorisation segments replayed from captured CUDA graphs give the same bits as direct launches: three
-    solves with graphs on (the second and third replay the segments seen before) against one with them off."""
+    solves with graphs on (the second and third replay the segments seen before) against one with them off.  The
+    Gram-Schmidt method is fixed (FP64 FMA for IEEE-double storage): the automatic choice differs between the two
+    launch modes."""
     if herm:
         csr, kw = matgen.laplacian_2d(100), dict(hermitian=True, which="LM", nev=10, ncv=32)
     else:
@@ -655,6 +657,7 @@ def test_graph_segments_match_direct_launches(lib, arith, herm):
         e.setTolerances(1e-10)
         e.setWhichEigenpairs(kw["which"])
         e.setArithmetic(arith)
+        e.setGSMethod("fma")
         e.setGraphCapture(mode)
         e.setInitialSpace(matgen.start_vector(n, 4))
         return e
