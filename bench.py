@@ -753,7 +753,8 @@ def run_plain(args, wl):
         top = max(("gs_dot", "gs_update", "spmv", "restart"), key=lambda k: prof[k][0])
         ms_k, by_k, nl_k = prof[top]
         achieved = by_k / (ms_k / 1000.0) / 1e9 if ms_k > 0 else None
-        tr = (committed_traffic(args.workload + ("" if arith == "pair" else "_" + arith)) or {}).get(top)
+        tkey = args.workload + ("" if arith == "pair" else "_" + arith) + ("_integer" if exact_gs else "")
+        tr = (committed_traffic(tkey) or committed_traffic(tkey.replace("_integer", "")) or {}).get(top)
         traffic = tr * by_k / nl_k if (tr and nl_k) else None  # DRAM bytes per launch: ncu ratio x algorithmic
         roof = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak if achieved else None, "peak_source": peak_kind,
