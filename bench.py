@@ -7,7 +7,8 @@ between steps.
 
   value      nev converged eigenpairs per solve / device time of EPSSolve (CUDA events on the solver's stream),
              matrix resident in HBM since EPSSetUp (the start vector's 16.8 MB upload is inside EPSSolve).
-             Arithmetic: IEEE FP64 storage and products (--arith f64, the default)
+             Arithmetic: IEEE FP64 storage (--arith f64, the default); Gram-Schmidt products exact on the integer
+             pipes, each result rounded once (--gs auto: the library's default for this size; --gs fma for FP64 FMA)
   parity     after the timed solves, on the host: every converged eigenvalue against the closed-form spectrum
              (set-based over distinct values), ||Ax - lam x|| / (||A||_inf |lam|) with scipy.sparse on the CSR
              arrays, ||X^T X - I|| in numpy, from the eigenvectors EPSGetEigenpair returns; exit code 3 if a bound fails
