@@ -114,6 +114,13 @@ def main():
     line = [l for l in txt.splitlines() if re.search(r"\d\.\d{5}", l)][-1]
     g["ex11_1"] = {"source": "src/eps/tutorials/output/ex11_1.out", "grid": [10, 10], "nev": 4, "which": "SR",
                    "keep": 0.2, "tol": 1e-8, "eigenvalues": floats(line)}
+    # 1-D Laplacian n=30, HEP, smallest real, nev 4, EPS_CONV_ABS, tol 1e-8, with the exact eigenvectors of the two
+    # lowest eigenvalues, sin(pi j (i+1)/(n+1)) sqrt(2/(n+1)), as deflation space (src/eps/tests/test24.c TEST 1, -ncon
+    # 2; the test's solver is LOBPCG, the printed eigenvalues are those of the deflated problem)
+    txt = read("src/eps/tests/output/test24_1.out")
+    line = [l for l in txt.splitlines() if re.search(r"\d\.\d{5}", l)][-1]
+    g["test24_1"] = {"source": "src/eps/tests/output/test24_1.out", "n": 30, "ncon": 2, "nev": 4, "which": "SR",
+                     "conv": "abs", "tol": 1e-8, "eigenvalues": floats(line)}
     # EPSView of a Krylov-Schur NHEP solve, largest real (src/eps/tests/test23.c TEST 1): the EPS Object block
     lines = read("src/eps/tests/output/test23_1.out").splitlines()
     i0 = next(i for i, l in enumerate(lines) if l.startswith("EPS Object"))

@@ -417,3 +417,21 @@ def test_ex11_deflation_space_golden(orc):
     # without the deflation space the zero eigenvalue comes first
     r0 = orc.solve(*csr, hermitian=True, which=g["which"], nev=g["nev"], keep=g["keep"], tol=g["tol"])
     assert abs(r0.eigr[0]) < 1e-8 and round(r0.eigr[1], 5) == g["eigenvalues"][0]
+
+
+def test_test24_constrained_laplacian_golden(orc):
+    """test24.c: the 1-D Laplacian (n = 30), smallest real, nev 4, EPS_CONV_ABS, with the exact eigenvectors of its
+    two lowest eigenvalues as deflation space: the eigenvalues test24_1.out prints (those of the deflated problem,
+    2 - 2 cos(k pi / 31) for k = 3..6), every eigenvector orthogonal to the constraints."""
+    g = G["test24_1"]
+    n, ncon = g["n"], g["ncon"]
+    csr = matgen.laplacian_1d(n)
+    j = np.arange(1, n + 1)
+    C = np.stack([np.sin(np.pi / (n + 1) * j * (i + 1)) * np.sqrt(2.0 / (n + 1)) for i in range(ncon)], axis=1)
+    r = orc.solve(*csr, hermitian=True, which=g["which"], nev=g["nev"], tol=g["tol"], conv=g["conv"],
+                  v0=matgen.start_vector(n, 1), deflation=C)
+    assert r.reason == 1 and r.nconv >= g["nev"]
+    assert [round(v, 5) for v in r.eigr[:g["nev"]]] == g["eigenvalues"]
+    assert np.abs(C.T @ r.X[:, :g["nev"]]).max() < 1e-10
+    exact = [2 - 2 * np.cos(k * np.pi / (n + 1)) for k in range(ncon + 1, ncon + 1 + g["nev"])]
+    assert np.allclose(r.eigr[:g["nev"]], exact, rtol=1e-9)
